@@ -1,0 +1,210 @@
+/*
+ * splatlight.h -- C ABI of the GB300 splat pipeline (project -> stable depth sort -> per-tile ranges -> composite,
+ * with the per-Gaussian lighting it composites).  Plain C: pointers, sizes and int status codes; no CUDA or torch
+ * types.  Streams are passed as `void*` holding a cudaStream_t (NULL = the legacy default stream).
+ *
+ * Each entry point names the reference interface it replaces.  Paths are within the reference project.
+ *
+ * Memory: the caller owns host memory; the library owns every device buffer it allocates (opaque handles, *_destroy).
+ * Output pointers may be host or device memory: the `*_on_device` flag says which.
+ * Errors: every call returns SL_OK (0) or a negative SL_ERR_* code and never aborts; sl_last_error() gives the text
+ * of the last failure on the calling thread.
+ * Threading: a handle is thread-compatible (one caller at a time); distinct handles may be used concurrently.
+ */
+#ifndef SPLATLIGHT_H
+#define SPLATLIGHT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SL_API __attribute__((visibility("default")))
+#else
+#define SL_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------------------------- */
+#define SL_OK 0
+#define SL_ERR_INVALID_ARG (-1)   /* a null pointer, a bad size or a value out of range */
+#define SL_ERR_LAYOUT (-2)        /* asset layout check failed (format, version, stride, field offset, count) */
+#define SL_ERR_OOM (-3)           /* device allocation failed */
+#define SL_ERR_CUDA (-4)          /* a CUDA runtime call failed */
+#define SL_ERR_TIMEOUT (-5)       /* a bounded device-side wait gave up (the stream stays usable) */
+#define SL_ERR_UNSUPPORTED (-6)   /* the frame enables a feature outside this pipeline (explode, LOD, lens warp ...) */
+#define SL_ERR_ADMISSION (-7)     /* serving: the request does not fit the device-memory budget */
+#define SL_ERR_OVERFLOW (-8)      /* a fixed-capacity buffer (tile entries) was too small; grow and retry */
+#define SL_ERR_NO_DEVICE (-9)     /* no CUDA device, or the device is not an sm_103 part */
+
+/* ---- scene records (gs-runtime layout; shaders/common.wgsl:5-25, runtime/wgsl/common.wgsl:4-65) --------------- */
+
+/* 64 B, uploaded unchanged from gaussians.bin (src/asset.js:9; shaders/common.wgsl:6-14) */
+typedef struct sl_gaussian {
+  float mu[3];           /* centre, part rest frame */
+  float kappa;           /* peak extinction scale, 1/m */
+  float quat[4];         /* x, y, z, w */
+  float scale[3];        /* std devs, ascending: x = short axis */
+  uint32_t part_surface; /* part | surface << 16 */
+  float albedo[3];       /* linear albedo; emitter records: emitted radiance Le */
+  uint32_t flags;        /* low 16 bits: material */
+} sl_gaussian;
+
+/* 128 B (src/asset.js:10; shaders/common.wgsl:17-25).  xf rows are [R row | t] (world_from_rest). */
+typedef struct sl_part {
+  float xf[12];
+  float xf_prev[12];
+  float bound[4];        /* rest-frame centre, radius */
+  uint32_t root, g_lo, g_hi, flags; /* flags bit 1 moved this frame, bit 2 hidden */
+} sl_part;
+
+/* 96 B tree node; leaves are nodes [0, count) (runtime/wgsl/common.wgsl:12-19) */
+typedef struct sl_node {
+  float mean[3];
+  float radius;
+  float cinv_diag[3];
+  float kappa;
+  float cinv_off[3];     /* xy xz yz */
+  float smax;
+  float sn_diag[3];      /* SGGX S-hat (projected-area extinction) */
+  uint32_t part;
+  float sn_off[3];
+  uint32_t child_lo;
+  uint32_t child_hi, depth, pad0, pad1; /* leaves: pad0 = bits of iso_norm after sl_lighting_init_iso */
+} sl_node;
+
+/* 32 B (runtime/wgsl/common.wgsl:59-65; specular mix runtime/wgsl/material_ext.wgsl:10-42) */
+typedef struct sl_material {
+  float flake[3];          /* SGGX diagonal in the Gaussian's frame: (1, r^2, r^2) for roughness r */
+  uint32_t phase_samples;
+  float vfloor;
+  uint32_t flags;          /* bit 0 emissive, bit 2 one-sided, bit 3 specular flakes */
+  uint32_t pad0, pad1;     /* specular: pad0 low half = fp16 k; emissive: fp16 (r, g), (b, 0) */
+} sl_material;
+
+/* 128 B V grid: 8 x 16 bytes of own-part visibility (runtime/wgsl/common.wgsl:21) */
+typedef struct sl_vgrid { uint32_t w[32]; } sl_vgrid;
+
+/* The 1200-byte RenderFrame uniform exactly as the host writes it (shaders/common.wgsl:44-77; src/main.js:526-556;
+ * FRAME_BYTES src/renderer.js:9).  Fields this pipeline reads are marked (*); the others must hold their "off"
+ * values (zero), else sl_render returns SL_ERR_UNSUPPORTED. */
+typedef struct sl_render_frame {
+  float view[16];                /* (*) column-major world -> view (src/math.js:36-46) */
+  float proj[16];                /* carried, unused (the path projects with focal lengths) */
+  float palette[4][4];           /* (*) slots 0-2; palette[3] = (bounce gain*, emitter count*, blur shutter, blur cov) */
+  uint32_t part_material[16];    /* (*) palette slot per part 0-15 */
+  float lamp[4];                 /* lamp.w must be 0 (camera-only flakes are outside the pipeline) */
+  float lamp_color[4];           /* lamp_color.w = reflection flags, must be 0 (no coverage split) */
+  float viewport[2];             /* (*) pixels */
+  float focal[2];                /* (*) pixels */
+  float near_plane;              /* (*) */
+  float far_plane;               /* (*) */
+  uint32_t count;                /* (*) Gaussians in the asset */
+  uint32_t view_mode;            /* (*) 0 flat albedo, 1 depth, 2 overdraw (contributor count), 3 lit */
+  float albedo_scale;            /* (*) */
+  float flake_roughness;
+  float exposure;
+  float lowpass_px2;             /* (*) screen-space dilation of the 2D covariance */
+  float palette_ext[4][4];       /* (*) palette slots 4-7 */
+  float mat_view[16][4];         /* (*) only .w bit 0 (glass) is read: glass flags the splat, nothing else */
+  uint32_t part_material_ext[16];/* (*) palette slot per part 16-31 */
+  uint32_t lod[4];               /* lod.x must be 0 (screen-space LOD off) */
+  float explode[4];
+  float explode_c[4];
+  float explode_k[4];            /* explode_k.z must be <= 0.5 (explode off) */
+  float mat_view_ext[16][4];
+  uint32_t tone[4];
+  float part_fade[32];           /* (*) per part draw-time fade */
+  uint32_t particles[4];         /* particles.y must be 0 */
+} sl_render_frame;
+
+/* ---- errors -------------------------------------------------------------------------------------------------- */
+
+/* Copies the calling thread's last error text (NUL-terminated, truncated to `cap`).  Returns its full length. */
+SL_API size_t sl_last_error(char* buf, size_t cap);
+
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+SL_API int sl_version(void);
+
+/* ---- asset layout (src/asset.js:18-38 checkHeader / checkBuffer) --------------------------------------------- */
+
+/* Checks one buffer description of asset.json against the layout the kernels assume: the buffer name is one of
+ * gaussians, parts, lamps, materials, nodes, kids, vgrid; stride and every listed field offset must match, and
+ * 0 < count <= 2^24.  `field_names`/`field_offsets` hold `n_fields` pairs (offset UINT32_MAX = missing field).
+ * Returns SL_OK or SL_ERR_LAYOUT (text in sl_last_error).  Replaces checkHeader's per-buffer loop, src/asset.js:21-29. */
+SL_API int sl_asset_check_buffer(const char* name, uint32_t stride, uint32_t count, const char* const* field_names,
+                          const uint32_t* field_offsets, uint32_t n_fields);
+
+/* Checks a buffer's byte length against count x stride (src/asset.js:32-38 checkBuffer). */
+SL_API int sl_asset_check_bytes(uint64_t byte_length, uint32_t count, uint32_t stride);
+
+/* ---- renderer (src/renderer.js SplatRenderer) ---------------------------------------------------------------- */
+
+typedef struct sl_renderer sl_renderer;
+typedef struct sl_lighting sl_lighting;
+
+/* Tile shape of the binned compositor: 16x16 (default), 8x32 or 32x8 pixels. */
+typedef struct sl_render_options {
+  uint32_t tile_w, tile_h;       /* 0 = keep */
+  float t_stop;                  /* early-termination transmittance scale (0 = default 1e-4 / max radiance) */
+  uint32_t entry_capacity;       /* tile entries pre-allocated (0 = grow on demand) */
+} sl_render_options;
+
+typedef struct sl_render_stats {
+  uint32_t slots;                /* n = count + 1 + emitters: the slots projected and sorted */
+  uint32_t visible;              /* valid keys (scan.wgsl's instance count) */
+  uint32_t entries;              /* (tile, splat) pairs binned */
+  uint32_t tiles;                /* tiles in the view */
+  float ms_project, ms_sort, ms_bin, ms_composite, ms_total; /* device times when timing is on, else 0 */
+} sl_render_stats;
+
+/* new SplatRenderer(device, canvasFormat, shaders, asset) (src/renderer.js:38-233): uploads the asset's Gaussians
+ * and parts and sizes every per-slot buffer for count + 1 + max_emitters slots (MAX_EMITTERS, src/renderer.js:17). */
+SL_API int sl_renderer_create(const sl_gaussian* gaussians, uint32_t count, const sl_part* parts, uint32_t part_count,
+                       uint32_t max_emitters, sl_renderer** out);
+SL_API int sl_renderer_destroy(sl_renderer* r);
+
+/* writeParts(partBytes) (src/renderer.js:407-409): replaces the part records (xf, xf_prev, flags). */
+SL_API int sl_renderer_set_parts(sl_renderer* r, const sl_part* parts, uint32_t part_count);
+
+/* The emitters buffer project.wgsl draws in slots count+1 .. count+n (shaders/project.wgsl:121, 226-230; the
+ * renderer's emitterBuf): world-space emissive Gaussians whose albedo holds Le.  n <= max_emitters. */
+SL_API int sl_renderer_set_emitters(sl_renderer* r, const sl_gaussian* emitters, uint32_t n);
+
+/* bindColour(colourBuf, bounceBuf, emitterBuf) (src/renderer.js:264-268) with caller-provided radiance: `colour`
+ * holds one float4 per Gaussian (rgb used), `lo_b` three float4 per Gaussian (the eye bounce at [3i]) or NULL.
+ * Device pointers; they must stay valid while bound.  Replaced by sl_renderer_bind_lighting. */
+SL_API int sl_renderer_bind_colour(sl_renderer* r, const float* colour_dev, const float* lo_b_dev);
+
+SL_API int sl_renderer_set_options(sl_renderer* r, const sl_render_options* opt);
+
+/* Turns per-stage CUDA-event timing into the stats on (1) or off (0). */
+SL_API int sl_renderer_set_timing(sl_renderer* r, int on);
+
+/* encode(encoder, target, frameBytes, viewMode, timers) (src/renderer.js:411-524) without the display pass: project
+ * -> stable radix sort of the 16-bit depth keys -> per-tile ranges -> front-to-back composite.  `frame` is the
+ * 1200-byte RenderFrame (view_mode inside it).  Writes viewport W x H RGBA fp32 (row 0 at the top; premultiplied
+ * linear rgb, alpha = coverage) to `out_rgba`.  View mode 2 writes the per-pixel contributor count to .r (and to
+ * the counts debug buffer).  Stream-ordered on `stream`; with a host `out_rgba` the call returns after the copy. */
+SL_API int sl_render(sl_renderer* r, const sl_render_frame* frame, float* out_rgba, int out_on_device,
+              sl_render_stats* stats, void* stream);
+
+/* Debug read-back of the last sl_render on this renderer (host buffers; any may be NULL):
+ *   keys   u32 per slot, INVALID 0xFFFFFFFF (project.wgsl's keys[])
+ *   order  u32 per slot, the stable permutation (radix.wgsl's vals_out after the last pass)
+ *   ranges u32 pairs [start, end) per tile, row-major tiles
+ *   counts u32 per pixel: fragments with alpha >= 1/255 (the overdraw view; filled by view mode 2 only)
+ * Sizes: slots, slots, 2 x tiles, W x H as returned in the stats. */
+SL_API int sl_renderer_read_debug(sl_renderer* r, uint32_t* keys, uint32_t* order, uint32_t* ranges, uint32_t* counts);
+
+/* The per-tile splat lists of the last sl_render: `entries` (slot indices, tile after tile, each tile's splats in
+ * back-to-front order) holds stats.entries values; [ranges[2t], ranges[2t+1]) indexes tile t's list. */
+SL_API int sl_renderer_read_entries(sl_renderer* r, uint32_t* entries, uint64_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPLATLIGHT_H */

@@ -1,0 +1,95 @@
+"""ctypes binding of libsplatlight.so (the C ABI in include/splatlight.h).
+
+The library is built in-tree by splatlight_gb300.build (or __graft_entry__.build()).  There is no fallback: if the
+shared library is missing or fails to load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libsplatlight.so"
+
+SL_OK = 0
+ERRORS = {
+    -1: "SL_ERR_INVALID_ARG", -2: "SL_ERR_LAYOUT", -3: "SL_ERR_OOM", -4: "SL_ERR_CUDA", -5: "SL_ERR_TIMEOUT",
+    -6: "SL_ERR_UNSUPPORTED", -7: "SL_ERR_ADMISSION", -8: "SL_ERR_OVERFLOW", -9: "SL_ERR_NO_DEVICE",
+}
+
+
+class SplatlightError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("slots", C.c_uint32), ("visible", C.c_uint32), ("entries", C.c_uint32), ("tiles", C.c_uint32),
+                ("ms_project", C.c_float), ("ms_sort", C.c_float), ("ms_bin", C.c_float),
+                ("ms_composite", C.c_float), ("ms_total", C.c_float)]
+
+
+class RenderOptions(C.Structure):
+    _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("t_stop", C.c_float),
+                ("entry_capacity", C.c_uint32)]
+
+
+_P = C.c_void_p
+_U32 = C.c_uint32
+_U64 = C.c_uint64
+_I = C.c_int
+
+# name -> (restype, argtypes); every symbol include/splatlight.h declares
+PROTOTYPES: dict[str, tuple] = {
+    "sl_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
+    "sl_version": (_I, []),
+    "sl_asset_check_buffer": (_I, [C.c_char_p, _U32, _U32, C.POINTER(C.c_char_p), C.POINTER(_U32), _U32]),
+    "sl_asset_check_bytes": (_I, [_U64, _U32, _U32]),
+    "sl_renderer_create": (_I, [_P, _U32, _P, _U32, _U32, C.POINTER(_P)]),
+    "sl_renderer_destroy": (_I, [_P]),
+    "sl_renderer_set_parts": (_I, [_P, _P, _U32]),
+    "sl_renderer_set_emitters": (_I, [_P, _P, _U32]),
+    "sl_renderer_bind_colour": (_I, [_P, _P, _P]),
+    "sl_renderer_set_options": (_I, [_P, C.POINTER(RenderOptions)]),
+    "sl_renderer_set_timing": (_I, [_P, _I]),
+    "sl_render": (_I, [_P, _P, _P, _I, C.POINTER(RenderStats), _P]),
+    "sl_renderer_read_debug": (_I, [_P, _P, _P, _P, _P]),
+    "sl_renderer_read_entries": (_I, [_P, _P, _U64]),
+}
+
+_lib: C.CDLL | None = None
+
+
+def lib() -> C.CDLL:
+    """Loads libsplatlight.so once; raises if it is missing (no CPU fallback exists)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH.name} is not built: run splatlight_gb300.build.build() (needs nvcc)")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in PROTOTYPES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(1024)
+    lib().sl_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def check(code: int) -> None:
+    if code != SL_OK:
+        raise SplatlightError(code, last_error())
+
+
+def ptr(a) -> int | None:
+    """Address of a numpy array, a torch tensor (host or device) or None."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data

@@ -1,0 +1,191 @@
+// Tile compositor: one CTA of 256 threads per screen tile, one pixel per thread.  The tile's sorted splat list is
+// walked from its nearest entry to its farthest (front to back), in batches of 256 records; each batch is gathered
+// into shared memory by the TMA unit (cp.async.bulk, one 48-byte bulk copy per record, completion counted on an
+// mbarrier) while the previous batch is composited (double buffering).  Per pixel:
+//   local = (d . g0, d . g1), keep if |local.x|, |local.y| <= r (inside the quad) and q = |local|^2 <= qcut
+//   (alpha >= 1/255), alpha = 1 - exp(-tau0 exp(-q/2)), C += T alpha rgb, T *= 1 - alpha
+// which composites the same ordered splats as the reference's back-to-front premultiplied "over" blend
+// (shaders/splat.wgsl:66-78, src/renderer.js:133-143), in fp32.  A pixel stops once T < t_stop / max radiance (the
+// skipped tail is below 1e-4 in every channel); a warp whose pixels all stopped skips the batch (warp vote) and the CTA
+// leaves when every pixel stopped.  The overdraw view (count_mode) never stops early and counts kept fragments.
+// Every mbarrier wait is bounded; a give-up sets FrameCounters::timeout and the kernel still drains its copies.
+#include "sl_internal.h"
+
+namespace sl {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr uint32_t kRecBytes = sizeof(SplatRec);
+constexpr uint32_t kWaitLimit = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// true when the phase with the given parity completed; bounded
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (uint32_t k = 0; k < kWaitLimit; k++) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+template <int TW>
+__global__ void __launch_bounds__(kThreads) composite_kernel(const CompositeParams P, const uint2* __restrict__ ranges,
+                                                             const uint32_t* __restrict__ tile_vals,
+                                                             const SplatRec* __restrict__ recs,
+                                                             const FrameCounters* ctr, float4* __restrict__ out,
+                                                             uint32_t* __restrict__ counts) {
+  constexpr int TH = kThreads / TW;
+  __shared__ SplatRec buf[2][kThreads];
+  __shared__ __align__(8) uint64_t bars[2];
+
+  const int t = threadIdx.x;
+  const uint32_t tile = blockIdx.x;
+  const uint32_t tx = tile % P.tiles_x, ty = tile / P.tiles_x;
+  const uint32_t px = tx * TW + (uint32_t)(t % TW), py = ty * TH + (uint32_t)(t / TW);
+  const bool inside = px < P.width && py < P.height;
+
+  const uint32_t bar0 = smem_addr(&bars[0]), bar1 = smem_addr(&bars[1]);
+  if (t == 0) {
+    mbar_init(bar0, kThreads);
+    mbar_init(bar1, kThreads);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  const uint2 rg = ranges[tile];
+  const uint32_t s = rg.x, e = rg.y;
+  const uint32_t n_batches = (e - s + kThreads - 1) / kThreads;
+  const float maxrad = fmaxf(__uint_as_float(ctr->max_rad_bits), 1.0f);
+  const float t_stop = P.count_mode ? -1.0f : P.t_stop_scale / maxrad;
+  const float pxc = (float)px + 0.5f, pyc = (float)py + 0.5f;
+  const float kNegHalfLog2e = -0.72134752044448170f;
+  const float kNegLog2e = -1.44269504088896341f;
+
+  float T = 1.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f;
+  uint32_t kept = 0;
+  bool alive = inside;
+  bool timed_out = false;
+
+  // gather batch b (entries [max(s, e-256(b+1)), e-256b), nearest first) into buf[b & 1]
+  auto issue = [&](uint32_t b) {
+    const uint32_t hi = e - kThreads * b;
+    const uint32_t lo = (hi - s) > (uint32_t)kThreads ? hi - kThreads : s;
+    const uint32_t bar = (b & 1u) ? bar1 : bar0;
+    if ((uint32_t)t < hi - lo) {
+      const uint32_t slot = tile_vals[hi - 1u - (uint32_t)t];
+      mbar_arrive_expect(bar, kRecBytes);
+      bulk_copy_g2s(smem_addr(&buf[b & 1u][t]), recs + slot, kRecBytes, bar);
+    } else {
+      mbar_arrive(bar);
+    }
+  };
+
+  if (n_batches > 0) issue(0);
+  for (uint32_t b = 0; b < n_batches; b++) {
+    if (b + 1 < n_batches) issue(b + 1);
+    const uint32_t bar = (b & 1u) ? bar1 : bar0;
+    if (!mbar_wait(bar, (b >> 1) & 1u)) timed_out = true;
+    const uint32_t hi = e - kThreads * b;
+    const uint32_t nb = (hi - s) > (uint32_t)kThreads ? (uint32_t)kThreads : hi - s;
+    const SplatRec* rb = buf[b & 1u];
+    if (__any_sync(0xffffffffu, alive)) {
+      for (uint32_t j = 0; j < nb; j++) {
+        const float4 A = rb[j].a;
+        const float4 B = rb[j].b;
+        const float dx = pxc - A.x, dy = pyc - A.y;
+        const float lx = fmaf(dx, A.z, dy * A.w);
+        const float ly = fmaf(dx, B.x, dy * B.y);
+        const float q = fmaf(lx, lx, ly * ly);
+        const bool keep = alive && fabsf(lx) <= B.z && fabsf(ly) <= B.z && q <= B.w;
+        if (keep) {
+          const float4 C = rb[j].c;
+          const float ev = ex2_approx(q * kNegHalfLog2e);
+          const float alpha = 1.0f - ex2_approx(C.w * kNegLog2e * ev);
+          const float wgt = T * alpha;
+          cr = fmaf(wgt, C.x, cr);
+          cg = fmaf(wgt, C.y, cg);
+          cb = fmaf(wgt, C.z, cb);
+          T = T - wgt;
+          kept++;
+          if (T < t_stop) alive = false;
+        }
+        if ((j & 31u) == 31u && !__any_sync(0xffffffffu, alive)) break;
+      }
+    }
+    if (__syncthreads_count(alive) == 0) {
+      // every pixel is done: drain the batch already in flight before leaving
+      if (b + 1 < n_batches) {
+        if (!mbar_wait((b & 1u) ? bar0 : bar1, ((b + 1) >> 1) & 1u)) timed_out = true;
+      }
+      break;
+    }
+  }
+  if (timed_out) atomicExch(const_cast<uint32_t*>(&ctr->timeout), 1u);
+  if (inside) {
+    const size_t pix = (size_t)py * P.width + px;
+    if (P.count_mode) {
+      out[pix] = make_float4((float)kept, 0.0f, 0.0f, 0.0f);
+      if (counts) counts[pix] = kept;
+    } else {
+      out[pix] = make_float4(cr, cg, cb, 1.0f - T);
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_composite(const CompositeParams& P, const uint2* ranges, const uint32_t* tile_vals,
+                             const SplatRec* recs, const FrameCounters* ctr, float4* out, uint32_t* counts,
+                             cudaStream_t s) {
+  const uint32_t tiles = P.tiles_x * P.tiles_y;
+  if (tiles == 0) return cudaSuccess;
+  if (P.tile_w * P.tile_h != (uint32_t)kThreads) return cudaErrorInvalidValue;
+  switch (P.tile_w) {
+    case 16:
+      composite_kernel<16><<<tiles, kThreads, 0, s>>>(P, ranges, tile_vals, recs, ctr, out, counts);
+      break;
+    case 8:
+      composite_kernel<8><<<tiles, kThreads, 0, s>>>(P, ranges, tile_vals, recs, ctr, out, counts);
+      break;
+    case 32:
+      composite_kernel<32><<<tiles, kThreads, 0, s>>>(P, ranges, tile_vals, recs, ctr, out, counts);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace sl

@@ -1,0 +1,292 @@
+// Projection: one thread per slot turns a 3D Gaussian into a screen-space splat record, a 16-bit back-to-front
+// depth key and a tile rectangle (shaders/project.wgsl:84-370, plain path).  A coalesced streaming kernel: each
+// thread reads its 64-byte record as four 16-byte vector loads and writes a 48-byte splat, a 2-byte key and an
+// 8-byte tile rectangle; the digit histograms the radix sort needs are reduced in shared memory and added once per
+// block.
+//
+// Compiled with --fmad=false: every a*b+c rounds twice, as in the CPU restatement, so keys, tile rectangles and the
+// per-fragment keep bound are bit-identical to it.  Sums evaluate left to right, matrix-vector products as
+// col0*v.x + col1*v.y + col2*v.z, normalize(v) = v / sqrt(dot(v, v)), and ln comes from sl_detmath.h.
+#include "sl_detmath.h"
+#include "sl_internal.h"
+
+namespace sl {
+namespace {
+
+struct V3 {
+  float x, y, z;
+};
+struct M3 {
+  V3 c[3];
+};
+
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ float dot3(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 scale3(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ V3 mulv(const M3& m, V3 v) {
+  return v3(m.c[0].x * v.x + m.c[1].x * v.y + m.c[2].x * v.z, m.c[0].y * v.x + m.c[1].y * v.y + m.c[2].y * v.z,
+            m.c[0].z * v.x + m.c[1].z * v.y + m.c[2].z * v.z);
+}
+__device__ __forceinline__ M3 mulm(const M3& a, const M3& b) {
+  M3 r;
+  r.c[0] = mulv(a, b.c[0]);
+  r.c[1] = mulv(a, b.c[1]);
+  r.c[2] = mulv(a, b.c[2]);
+  return r;
+}
+// quat_to_mat, shaders/common.wgsl:83-89
+__device__ __forceinline__ M3 quat_mat(float x, float y, float z, float w) {
+  M3 m;
+  m.c[0] = v3(1.0f - 2.0f * (y * y + z * z), 2.0f * (x * y + w * z), 2.0f * (x * z - w * y));
+  m.c[1] = v3(2.0f * (x * y - w * z), 1.0f - 2.0f * (x * x + z * z), 2.0f * (y * z + w * x));
+  m.c[2] = v3(2.0f * (x * z + w * y), 2.0f * (y * z - w * x), 1.0f - 2.0f * (x * x + y * y));
+  return m;
+}
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+
+constexpr int kThreads = 256;
+
+__global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant__ ProjectParams P,
+                                                           const float4* __restrict__ gaussians,
+                                                           const float4* __restrict__ emitters,
+                                                           const float4* __restrict__ colour,
+                                                           const float4* __restrict__ lo_b, uint16_t* __restrict__ key16,
+                                                           SplatRec* __restrict__ recs, ushort4* __restrict__ rects,
+                                                           uint32_t* __restrict__ digit_hist, FrameCounters* ctr) {
+  __shared__ uint32_t h_lo[256], h_hi[256];
+  __shared__ uint32_t s_visible;
+  __shared__ uint32_t s_maxrad;
+  const int t = threadIdx.x;
+  h_lo[t] = 0u;
+  h_hi[t] = 0u;
+  if (t == 0) {
+    s_visible = 0u;
+    s_maxrad = 0u;
+  }
+  __syncthreads();
+
+  const uint32_t i = blockIdx.x * kThreads + t;
+  uint32_t key = kInvalidKey16;
+  ushort4 rect = make_ushort4(1, 1, 0, 0);
+  float maxrad = 0.0f;
+  bool live = i < P.n_slots && i != P.count && i <= P.count + P.n_emit;
+
+  float4 g0, g1, g2, g3;
+  uint32_t material = kEmitterMaterial;
+  float keep = 1.0f;
+  V3 mu;
+  M3 rot;
+  if (live) {
+    const float4* src = (i > P.count) ? emitters + 4u * (i - P.count - 1u) : gaussians + 4u * i;
+    g0 = __ldg(src + 0);
+    g1 = __ldg(src + 1);
+    g2 = __ldg(src + 2);
+    g3 = __ldg(src + 3);
+    if (i > P.count) {  // project.wgsl:226-230
+      mu = v3(g0.x, g0.y, g0.z);
+      rot = quat_mat(g1.x, g1.y, g1.z, g1.w);
+    } else {  // :232-251
+      uint32_t part = __float_as_uint(g2.w) & 0xffffu;
+      part = part > kMaxParts - 1u ? kMaxParts - 1u : part;
+      const PartXf& p = P.parts[part];
+      keep = p.keep;
+      if ((p.flags & kPartHidden) != 0u || keep <= 0.0f) {
+        live = false;
+      } else {
+        const float* a = p.xf;
+        mu = v3(a[0] * g0.x + a[1] * g0.y + a[2] * g0.z + a[3] * 1.0f,
+                a[4] * g0.x + a[5] * g0.y + a[6] * g0.z + a[7] * 1.0f,
+                a[8] * g0.x + a[9] * g0.y + a[10] * g0.z + a[11] * 1.0f);
+        M3 R;
+        R.c[0] = v3(a[0], a[4], a[8]);
+        R.c[1] = v3(a[1], a[5], a[9]);
+        R.c[2] = v3(a[2], a[6], a[10]);
+        rot = mulm(R, quat_mat(g1.x, g1.y, g1.z, g1.w));
+        material = p.material;
+      }
+    }
+  }
+
+  if (live) {
+    const float* V = P.view;
+    V3 tv = v3(V[0] * mu.x + V[4] * mu.y + V[8] * mu.z + V[12] * 1.0f,
+               V[1] * mu.x + V[5] * mu.y + V[9] * mu.z + V[13] * 1.0f,
+               V[2] * mu.x + V[6] * mu.y + V[10] * mu.z + V[14] * 1.0f);
+    float depth = -tv.z;
+    live = !(depth < P.near_plane || depth > P.far_plane);
+    if (live) {
+      M3 W;
+      W.c[0] = v3(V[0], V[1], V[2]);
+      W.c[1] = v3(V[4], V[5], V[6]);
+      W.c[2] = v3(V[8], V[9], V[10]);
+      M3 wr = mulm(W, rot);
+      const float sx = g2.x, sy = g2.y, sz = g2.z;
+      V3 s2 = v3(sx * sx, sy * sy, sz * sz);
+      V3 m0 = scale3(wr.c[0], sx), m1 = scale3(wr.c[1], sy), m2 = scale3(wr.c[2], sz);
+      // cov[r][c] = sum_k m_k[r] m_k[c]
+      const float mk0[3] = {m0.x, m0.y, m0.z}, mk1[3] = {m1.x, m1.y, m1.z}, mk2[3] = {m2.x, m2.y, m2.z};
+      float cv[3][3];
+#pragma unroll
+      for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) cv[r][c] = mk0[r] * mk0[c] + mk1[r] * mk1[c] + mk2[r] * mk2[c];
+      M3 cov;
+      cov.c[0] = v3(cv[0][0], cv[1][0], cv[2][0]);
+      cov.c[1] = v3(cv[0][1], cv[1][1], cv[2][1]);
+      cov.c[2] = v3(cv[0][2], cv[1][2], cv[2][2]);
+
+      const float fx = P.focal[0], fy = P.focal[1];
+      float iz = 1.0f / depth;
+      float px = fx * tv.x * iz;
+      float py = fy * tv.y * iz;
+      float limx = 1.3f * P.viewport[0] * 0.5f;
+      float limy = 1.3f * P.viewport[1] * 0.5f;
+      float cxv = clampf(tv.x * iz, -limx / fx, limx / fx) * depth;
+      float cyv = clampf(tv.y * iz, -limy / fy, limy / fy) * depth;
+      V3 j0 = v3(fx * iz, 0.0f, fx * cxv * iz * iz);
+      V3 j1 = v3(0.0f, fy * iz, fy * cyv * iz * iz);
+      V3 cj0 = mulv(cov, j0), cj1 = mulv(cov, j1);
+      float a = dot3(j0, cj0);
+      float b = dot3(j0, cj1);
+      float c = dot3(j1, cj1);
+      float det0 = a * c - b * b;
+      a += P.lowpass_px2;
+      c += P.lowpass_px2;
+      float det = a * c - b * b;
+      live = det > 0.0f;
+      float tau0 = 0.0f, qcut = 0.0f, r = 0.0f;
+      const float kTauMin = -sl_logf(1.0f - 1.0f / 255.0f);
+      if (live) {
+        float dlen = sqrtf(dot3(tv, tv));
+        V3 d = v3(tv.x / dlen, tv.y / dlen, tv.z / dlen);
+        V3 dl = v3(dot3(wr.c[0], d), dot3(wr.c[1], d), dot3(wr.c[2], d));
+        V3 is2 = v3(1.0f / s2.x, 1.0f / s2.y, 1.0f / s2.z);
+        float q = dot3(v3(dl.x * dl.x, dl.y * dl.y, dl.z * dl.z), is2);
+        const float kTwoPi = 6.283185307f;
+        tau0 = __uint_as_float(__float_as_uint(g0.w)) * sqrtf(kTwoPi / q) * sqrtf(fmaxf(det0, 0.0f) / det);
+        tau0 *= keep;
+        live = !(tau0 <= kTauMin);
+      }
+      if (live) {
+        qcut = 2.0f * sl_logf(tau0 / kTauMin);
+        r = sqrtf(qcut);
+        float mid = 0.5f * (a + c);
+        float disc = sqrtf(0.25f * (a - c) * (a - c) + b * b);
+        float l0 = mid + disc;
+        float l1 = fmaxf(det / l0, 1e-6f);
+        float e0x = 1.0f, e0y = 0.0f;
+        if (a >= c) {
+          if (fabsf(b) > 0.0f || l0 > a) {
+            float vx = l0 - c, vy = b, vl = sqrtf(vx * vx + vy * vy);
+            e0x = vx / vl;
+            e0y = vy / vl;
+          }
+        } else {
+          float vx = b, vy = l0 - a, vl = sqrtf(vx * vx + vy * vy);
+          e0x = vx / vl;
+          e0y = vy / vl;
+        }
+        float e1x = -e0y, e1y = e0x;
+        float sl0 = sqrtf(l0), sl1 = sqrtf(l1);
+        float tnx = 2.0f / P.viewport[0], tny = 2.0f / P.viewport[1];
+        float ax0 = e0x * sl0 * r * tnx, ay0 = e0y * sl0 * r * tny;
+        float ax1 = e1x * sl1 * r * tnx, ay1 = e1y * sl1 * r * tny;
+        float ccx = px * tnx, ccy = py * tny;
+        float extx = fabsf(ax0) + fabsf(ax1), exty = fabsf(ay0) + fabsf(ay1);
+        live = !(sl0 * r < 0.1f) && !(fabsf(ccx) - extx > 1.0f || fabsf(ccy) - exty > 1.0f);
+        if (live) {
+          // radiance (project.wgsl:420-453)
+          float cr = g3.x, cg = g3.y, cb = g3.z;
+          if (material == kEmitterMaterial) {
+          } else if (P.view_mode == 3u) {
+            float4 cl = colour ? colour[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 bo = lo_b ? lo_b[3u * i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            cr = cl.x + P.bounce_gain * bo.x;
+            cg = cl.y + P.bounce_gain * bo.y;
+            cb = cl.z + P.bounce_gain * bo.z;
+            if (material < 8u) {
+              cr *= P.palette[material][0];
+              cg *= P.palette[material][1];
+              cb *= P.palette[material][2];
+            }
+          } else if (material < 8u && P.palette[material][3] > 0.5f) {
+            cr = P.palette[material][0];
+            cg = P.palette[material][1];
+            cb = P.palette[material][2];
+          }
+          if (material != kEmitterMaterial) {
+            cr *= P.albedo_scale;
+            cg *= P.albedo_scale;
+            cb *= P.albedo_scale;
+          }
+          // 16-bit log-depth key (:466-471)
+          float lnr = sl_logf(P.far_plane / P.near_plane);
+          float tt = clampf(sl_logf(depth / P.near_plane) / lnr, 0.0f, 1.0f);
+          uint32_t k = 65535u - (uint32_t)(tt * 65535.0f + 0.5f);
+          key = k > 0xfffeu ? 0xfffeu : k;
+          if (P.view_mode == 1u) cr = cg = cb = 1.0f - tt;
+
+          const float Wf = P.viewport[0], Hf = P.viewport[1];
+          float cx = px + 0.5f * Wf;
+          float cy = 0.5f * Hf - py;
+          float a0x = e0x * sl0 * r, a0y = e0y * sl0 * r;
+          float a1x = e1x * sl1 * r, a1y = e1y * sl1 * r;
+          float n0 = fmaxf(a0x * a0x + a0y * a0y, 1e-12f);
+          float n1 = fmaxf(a1x * a1x + a1y * a1y, 1e-12f);
+          SplatRec rec;
+          rec.a = make_float4(cx, cy, a0x * r / n0, -(a0y * r / n0));
+          rec.b = make_float4(a1x * r / n1, -(a1y * r / n1), r, qcut);
+          rec.c = make_float4(cr, cg, cb, tau0);
+          recs[i] = rec;
+          maxrad = fmaxf(fmaxf(cr, cg), fmaxf(cb, 0.0f));
+          // candidate pixels: ellipse bounding box plus one pixel; tiles it overlaps
+          float hx = r * sqrtf(a) + 1.0f, hy = r * sqrtf(c) + 1.0f;
+          float xl = fmaxf(cx - hx - 0.5f, -1.0f), xh = fminf(cx + hx - 0.5f, Wf);
+          float yl = fmaxf(cy - hy - 0.5f, -1.0f), yh = fminf(cy + hy - 0.5f, Hf);
+          int ix0 = (int)ceilf(xl), ix1 = (int)floorf(xh);
+          int iy0 = (int)ceilf(yl), iy1 = (int)floorf(yh);
+          ix0 = ix0 < 0 ? 0 : ix0;
+          iy0 = iy0 < 0 ? 0 : iy0;
+          ix1 = ix1 > (int)Wf - 1 ? (int)Wf - 1 : ix1;
+          iy1 = iy1 > (int)Hf - 1 ? (int)Hf - 1 : iy1;
+          if (ix0 <= ix1 && iy0 <= iy1)
+            rect = make_ushort4((unsigned short)(ix0 / (int)P.tile_w), (unsigned short)(iy0 / (int)P.tile_h),
+                                (unsigned short)(ix1 / (int)P.tile_w), (unsigned short)(iy1 / (int)P.tile_h));
+        }
+      }
+    }
+  }
+
+  if (i < P.n_slots) {
+    key16[i] = (uint16_t)key;
+    rects[i] = rect;
+    atomicAdd(&h_lo[key & 0xffu], 1u);
+    atomicAdd(&h_hi[key >> 8], 1u);
+    if (key != kInvalidKey16) {
+      atomicAdd(&s_visible, 1u);
+      atomicMax(&s_maxrad, __float_as_uint(maxrad));
+    }
+  }
+  __syncthreads();
+  if (h_lo[t]) atomicAdd(&digit_hist[t], h_lo[t]);
+  if (h_hi[t]) atomicAdd(&digit_hist[256 + t], h_hi[t]);
+  if (t == 0) {
+    if (s_visible) atomicAdd(&ctr->visible, s_visible);
+    if (s_maxrad) atomicMax(&ctr->max_rad_bits, s_maxrad);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_project(const ProjectParams& P, const sl_gaussian* gaussians, const sl_gaussian* emitters,
+                           const float4* colour, const float4* lo_b, uint16_t* key16, SplatRec* recs,
+                           ushort4* rects, uint32_t* digit_hist, FrameCounters* ctr, cudaStream_t s) {
+  if (P.n_slots == 0) return cudaSuccess;
+  uint32_t blocks = (P.n_slots + kThreads - 1) / kThreads;
+  project_kernel<<<blocks, kThreads, 0, s>>>(P, reinterpret_cast<const float4*>(gaussians),
+                                             reinterpret_cast<const float4*>(emitters), colour, lo_b, key16, recs,
+                                             rects, digit_hist, ctr);
+  return cudaGetLastError();
+}
+
+}  // namespace sl

@@ -1,0 +1,105 @@
+// Internal declarations shared by the CUDA translation units of libsplatlight.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "splatlight.h"
+
+namespace sl {
+
+constexpr uint32_t kInvalidKey16 = 0xffffu;   // 16-bit depth key of a culled slot (sorts after every valid key)
+constexpr uint32_t kEmitterMaterial = 254u;   // shaders/common.wgsl:41
+constexpr uint32_t kMaxParts = 32u;           // shaders/common.wgsl:39
+constexpr uint32_t kPartHidden = 4u;          // shaders/common.wgsl:40
+
+// One projected splat as the compositor reads it: 48 B, 16-byte aligned, one bulk copy per record.
+//   a = (cx, cy, g0x, g0y)   centre in framebuffer pixels (y down) and the first grad row
+//   b = (g1x, g1y, r, qcut)  second grad row, quad radius, keep bound q <= qcut
+//   c = (r, g, b, tau0)      radiance and peak optical depth
+struct __align__(16) SplatRec {
+  float4 a, b, c;
+};
+
+// Per-part data the projection reads (shaders/common.wgsl:17-25 Part, RenderFrame.part_material/part_fade).
+struct PartXf {
+  float xf[12];
+  uint32_t flags;
+  uint32_t material;
+  float keep;  // 1 - clamp(part_fade)
+  uint32_t pad;
+};
+
+// Everything project() reads from the RenderFrame, packed once per frame by the host (kernel parameter).
+struct ProjectParams {
+  float view[16];
+  float focal[2];
+  float viewport[2];
+  float near_plane, far_plane, lowpass_px2, albedo_scale;
+  float bounce_gain;
+  uint32_t count, n_emit, n_slots, view_mode, part_count;
+  uint32_t tile_w, tile_h, tiles_x, tiles_y;
+  float palette[8][4];  // slots 0-7 (slot 3 = white, w 0)
+  PartXf parts[kMaxParts];
+};
+
+// Frame-wide device counters written by the pipeline (one per view).
+struct FrameCounters {
+  uint32_t visible;        // valid keys
+  uint32_t max_rad_bits;   // max radiance component (float bits, >= 0)
+  uint32_t entries;        // tile entries
+  uint32_t overflow;       // entries beyond capacity
+  uint32_t timeout;        // a bounded device wait gave up
+  uint32_t pad[3];
+};
+
+// ---- launchers (each returns cudaError_t of the launch) ----------------------------------------------------------
+
+// project.cu
+cudaError_t launch_project(const ProjectParams& P, const sl_gaussian* gaussians, const sl_gaussian* emitters,
+                           const float4* colour, const float4* lo_b, uint16_t* key16, SplatRec* recs,
+                           ushort4* rects, uint32_t* digit_hist /*[2][256]*/, FrameCounters* ctr,
+                           cudaStream_t s);
+
+// sort.cu: onesweep LSD radix sort of 16-bit keys with u32 values.
+struct SortScratch {
+  uint16_t* keys_alt;
+  uint32_t* vals_alt;
+  uint32_t* status;      // [passes][max_tiles][256]
+  uint32_t* tile_ctr;    // [passes]
+  uint32_t max_tiles;
+};
+size_t sort_tiles_for(uint32_t n);
+// Sorts keys[0, n) (16-bit, `bits` significant bits) stably; vals: input values (NULL = slot index);
+// writes the permutation/values to vals_out.  digit_hist: [passes][256] counts of the digits of every key
+// (pass p = bits 8p .. 8p+7), filled by the producer kernel.  Keys are ping-ponged through scratch.
+cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals_out, uint32_t n, int bits,
+                         const uint32_t* digit_hist, SortScratch& sc, FrameCounters* ctr, cudaStream_t s);
+// Counts the digit histograms of u16 keys (used when no producer kernel filled them).
+cudaError_t launch_digit_hist16(const uint16_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s);
+
+// scan.cu: exclusive scan of u32 (single pass, decoupled look-back); total written to *total if not null.
+size_t scan_scratch_bytes(uint32_t n);
+cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total, void* scratch,
+                               FrameCounters* ctr, cudaStream_t s);
+
+// tiles.cu
+cudaError_t launch_tile_counts(const uint32_t* order, const ushort4* rects, uint32_t n, const FrameCounters* ctr,
+                               uint32_t* counts, cudaStream_t s);
+cudaError_t launch_tile_emit(const uint32_t* order, const ushort4* rects, const uint32_t* offsets, uint32_t n,
+                             uint32_t tiles_x, uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys,
+                             uint32_t* tile_vals, uint32_t* tile_counts, uint32_t* digit_hist, cudaStream_t s);
+cudaError_t launch_tile_ranges(const uint32_t* tile_starts, const uint32_t* tile_counts, uint32_t tiles,
+                               uint2* ranges, cudaStream_t s);
+
+// composite.cu
+struct CompositeParams {
+  uint32_t width, height, tile_w, tile_h, tiles_x, tiles_y;
+  uint32_t count_mode;  // 1: overdraw view (contributor counts, no early termination)
+  float t_stop_scale;   // early termination when T < t_stop_scale / max radiance
+};
+cudaError_t launch_composite(const CompositeParams& P, const uint2* ranges, const uint32_t* tile_vals,
+                             const SplatRec* recs, const FrameCounters* ctr, float4* out, uint32_t* counts,
+                             cudaStream_t s);
+
+}  // namespace sl

@@ -1,0 +1,236 @@
+// Stable LSD radix sort of 16-bit keys with 32-bit values, onesweep style (one read and one write of the keys and
+// values per 8-bit digit pass, Adinets & Merrill 2022): the digit histograms of every pass are counted up front (by
+// the producer kernel, or launch_digit_hist16), then each pass is a single kernel over tiles of 4096 keys that
+//   1. ranks its keys per warp with __match_any_sync (peers holding the same digit) and a per-warp digit counter, so
+//      ranks follow index order within the tile (stability);
+//   2. publishes its per-digit counts and looks back over earlier tiles (decoupled look-back, one thread per digit)
+//      for the exclusive prefix; every spin is bounded and a give-up sets FrameCounters::timeout;
+//   3. reorders the tile in shared memory by digit and writes it out in digit runs (coalesced).
+// Tiles are taken in launch order from an atomic counter, so a tile only waits on tiles that already started.
+// Replaces the three-dispatch-per-pass radix sort of shaders/radix.wgsl:1-139 (same stable order: by key, ties in
+// index order); INVALID keys (0xFFFF) sort after every valid key, as there.
+#include "sl_internal.h"
+
+namespace sl {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kItems = 16;
+constexpr uint32_t kTile = kThreads * kItems;  // 4096
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagPrefix = 2u << 30;
+constexpr uint32_t kValueMask = (1u << 30) - 1u;
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ uint32_t load_relaxed(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Exclusive scan of one value per thread over a 256-thread block; returns the exclusive prefix, *total = sum.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_tot, uint32_t* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  uint32_t base = 0, sum = 0;
+#pragma unroll
+  for (int k = 0; k < kWarps; k++) {
+    uint32_t t = warp_tot[k];
+    base += (k < w) ? t : 0u;
+    sum += t;
+  }
+  __syncthreads();
+  if (total) *total = sum;
+  return base + x - v;
+}
+
+__global__ void __launch_bounds__(kThreads) onesweep_pass(const uint16_t* __restrict__ keys_in,
+                                                          const uint32_t* __restrict__ vals_in,
+                                                          uint16_t* __restrict__ keys_out,
+                                                          uint32_t* __restrict__ vals_out, uint32_t n, int shift,
+                                                          const uint32_t* __restrict__ digit_hist,
+                                                          uint32_t* status, uint32_t* tile_ctr, FrameCounters* ctr) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t warp_hist[kWarps][256];
+  __shared__ uint32_t digit_base[256];
+  __shared__ uint32_t local_start[256];
+  __shared__ uint32_t warp_tot[kWarps];
+  __shared__ uint16_t s_keys[kTile];
+  __shared__ uint32_t s_vals[kTile];
+
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  if (t == 0) s_tile = atomicAdd(tile_ctr, 1u);
+#pragma unroll
+  for (int k = 0; k < kWarps; k++) warp_hist[k][t] = 0u;
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t tile_base = tile * kTile;
+
+  uint32_t keys[kItems], vals[kItems], ranks[kItems];
+  const uint32_t wbase = tile_base + (uint32_t)w * (32u * kItems) + (uint32_t)lane;
+#pragma unroll
+  for (int it = 0; it < kItems; it++) {
+    uint32_t idx = wbase + (uint32_t)it * 32u;
+    bool valid = idx < n;
+    keys[it] = valid ? (uint32_t)keys_in[idx] : 0xffffu;
+    vals[it] = valid ? (vals_in ? vals_in[idx] : idx) : 0u;
+  }
+  const uint32_t lt = lanemask_lt();
+#pragma unroll
+  for (int it = 0; it < kItems; it++) {
+    uint32_t idx = wbase + (uint32_t)it * 32u;
+    bool valid = idx < n;
+    uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+    uint32_t d = (keys[it] >> shift) & 0xffu;
+    uint32_t rank = 0;
+    if (valid) {
+      uint32_t peers = __match_any_sync(vmask, d);
+      uint32_t before = warp_hist[w][d];
+      rank = before + __popc(peers & lt);
+      __syncwarp(vmask);
+      if ((peers & lt) == 0u) warp_hist[w][d] = before + __popc(peers);
+      __syncwarp(vmask);
+    }
+    ranks[it] = rank;
+  }
+  __syncthreads();
+
+  // per digit: exclusive prefix across warps, and the tile's count
+  uint32_t run = 0;
+#pragma unroll
+  for (int k = 0; k < kWarps; k++) {
+    uint32_t c = warp_hist[k][t];
+    warp_hist[k][t] = run;
+    run += c;
+  }
+  const uint32_t tile_count = run;
+
+  // publish this tile's counts, then look back for the exclusive prefix of digit t
+  uint32_t* st = status + (size_t)tile * 256u;
+  if (tile == 0) {
+    atomicExch(&st[t], kFlagPrefix | tile_count);
+  } else {
+    atomicExch(&st[t], kFlagAgg | tile_count);
+  }
+  uint32_t excl = 0;
+  if (tile > 0) {
+    int32_t j = (int32_t)tile - 1;
+    uint32_t spins = 0;
+    while (j >= 0) {
+      uint32_t s = load_relaxed(status + (size_t)j * 256u + t);
+      uint32_t flag = s & ~kValueMask;
+      if (flag == 0u) {
+        if (++spins > kSpinLimit) {
+          atomicExch(&ctr->timeout, 1u);
+          break;
+        }
+        __nanosleep(32);
+        continue;
+      }
+      excl += s & kValueMask;
+      if (flag == kFlagPrefix) break;
+      j--;
+    }
+    atomicExch(&st[t], kFlagPrefix | ((excl + tile_count) & kValueMask));
+  }
+
+  // global start of digit t: exclusive scan of the pass histogram, plus earlier tiles
+  uint32_t gstart = block_exclusive_scan(digit_hist[t], warp_tot, nullptr);
+  digit_base[t] = gstart + excl;
+  local_start[t] = block_exclusive_scan(tile_count, warp_tot, nullptr);
+  __syncthreads();
+
+#pragma unroll
+  for (int it = 0; it < kItems; it++) {
+    uint32_t idx = wbase + (uint32_t)it * 32u;
+    if (idx < n) {
+      uint32_t d = (keys[it] >> shift) & 0xffu;
+      uint32_t pos = local_start[d] + warp_hist[w][d] + ranks[it];
+      s_keys[pos] = (uint16_t)keys[it];
+      s_vals[pos] = vals[it];
+    }
+  }
+  __syncthreads();
+
+  const uint32_t tile_n = (n - tile_base) < kTile ? (n - tile_base) : kTile;
+  for (uint32_t j = t; j < tile_n; j += kThreads) {
+    uint32_t key = s_keys[j];
+    uint32_t d = (key >> shift) & 0xffu;
+    uint32_t dst = digit_base[d] + (j - local_start[d]);
+    if (keys_out) keys_out[dst] = (uint16_t)key;
+    vals_out[dst] = s_vals[j];
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) digit_hist16_kernel(const uint16_t* __restrict__ keys, uint32_t n,
+                                                                int passes, uint32_t* hist) {
+  __shared__ uint32_t h[2][256];
+  const int t = threadIdx.x;
+  h[0][t] = 0u;
+  h[1][t] = 0u;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * kThreads + t; i < n; i += gridDim.x * kThreads) {
+    uint32_t k = keys[i];
+    atomicAdd(&h[0][k & 0xffu], 1u);
+    if (passes > 1) atomicAdd(&h[1][k >> 8], 1u);
+  }
+  __syncthreads();
+  if (h[0][t]) atomicAdd(&hist[t], h[0][t]);
+  if (passes > 1 && h[1][t]) atomicAdd(&hist[256 + t], h[1][t]);
+}
+
+}  // namespace
+
+size_t sort_tiles_for(uint32_t n) { return (n + kTile - 1) / kTile; }
+
+cudaError_t launch_digit_hist16(const uint16_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  uint32_t blocks = (n + kThreads * 16 - 1) / (kThreads * 16);
+  if (blocks > 1216) blocks = 1216;  // 8 per SM on 152 SMs
+  digit_hist16_kernel<<<blocks, kThreads, 0, s>>>(keys, n, passes, hist);
+  return cudaGetLastError();
+}
+
+cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals_out, uint32_t n, int bits,
+                         const uint32_t* digit_hist, SortScratch& sc, FrameCounters* ctr, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  if (n > kValueMask) return cudaErrorInvalidValue;
+  const uint32_t tiles = (uint32_t)sort_tiles_for(n);
+  if (tiles > sc.max_tiles) return cudaErrorInvalidValue;
+  const int passes = bits <= 8 ? 1 : 2;
+  cudaError_t e = cudaMemsetAsync(sc.status, 0, sizeof(uint32_t) * 256u * tiles * (size_t)passes, s);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(sc.tile_ctr, 0, sizeof(uint32_t) * 2, s);
+  if (e != cudaSuccess) return e;
+  if (passes == 1) {
+    uint32_t* out = (vals_in == vals_out) ? sc.vals_alt : vals_out;
+    onesweep_pass<<<tiles, kThreads, 0, s>>>(keys, vals_in, nullptr, out, n, 0, digit_hist, sc.status, sc.tile_ctr,
+                                             ctr);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && out != vals_out)
+      e = cudaMemcpyAsync(vals_out, out, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
+    return e;
+  }
+  onesweep_pass<<<tiles, kThreads, 0, s>>>(keys, vals_in, sc.keys_alt, sc.vals_alt, n, 0, digit_hist, sc.status,
+                                           sc.tile_ctr, ctr);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  onesweep_pass<<<tiles, kThreads, 0, s>>>(sc.keys_alt, sc.vals_alt, nullptr, vals_out, n, 8, digit_hist + 256,
+                                           sc.status + (size_t)256u * tiles, sc.tile_ctr + 1, ctr);
+  return cudaGetLastError();
+}
+
+}  // namespace sl

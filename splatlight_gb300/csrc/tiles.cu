@@ -1,0 +1,101 @@
+// Per-tile splat lists.  After the depth sort, every visible splat (in back-to-front order) is expanded into one
+// (tile, slot) entry per screen tile its candidate rectangle overlaps; a stable radix sort by tile id then leaves each
+// tile's splats contiguous and still in depth order, and the per-tile entry counts give the ranges.  This replaces the
+// reference's fixed-function path (one instanced quad per sorted splat, shaders/splat.wgsl:51-55, src/renderer.js:
+// 474-485): the ranges are the rasteriser's coverage made explicit per tile.
+#include "sl_internal.h"
+
+namespace sl {
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ uint32_t rect_tiles(ushort4 r) {
+  return (r.x <= r.z && r.y <= r.w) ? (uint32_t)(r.z - r.x + 1) * (uint32_t)(r.w - r.y + 1) : 0u;
+}
+
+__global__ void __launch_bounds__(kThreads) tile_count_kernel(const uint32_t* __restrict__ order,
+                                                              const ushort4* __restrict__ rects, uint32_t n,
+                                                              const FrameCounters* ctr, uint32_t* __restrict__ counts) {
+  uint32_t p = blockIdx.x * kThreads + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t visible = ctr->visible;
+  counts[p] = p < visible ? rect_tiles(rects[order[p]]) : 0u;
+}
+
+__global__ void __launch_bounds__(kThreads) tile_emit_kernel(const uint32_t* __restrict__ order,
+                                                             const ushort4* __restrict__ rects,
+                                                             const uint32_t* __restrict__ offsets, uint32_t n,
+                                                             uint32_t tiles_x, uint32_t capacity, FrameCounters* ctr,
+                                                             uint16_t* __restrict__ tile_keys,
+                                                             uint32_t* __restrict__ tile_vals,
+                                                             uint32_t* __restrict__ tile_counts,
+                                                             uint32_t* __restrict__ digit_hist) {
+  __shared__ uint32_t h_lo[256], h_hi[256];
+  const int t = threadIdx.x;
+  h_lo[t] = 0u;
+  h_hi[t] = 0u;
+  __syncthreads();
+  const uint32_t p = blockIdx.x * kThreads + t;
+  const uint32_t visible = ctr->visible;
+  if (p < n && p < visible) {
+    const uint32_t slot = order[p];
+    const ushort4 r = rects[slot];
+    uint32_t e = offsets[p];
+    if (r.x <= r.z && r.y <= r.w) {
+      const uint32_t cnt = rect_tiles(r);
+      if (e + cnt > capacity) {
+        atomicExch(&ctr->overflow, 1u);
+      } else {
+        for (uint32_t ty = r.y; ty <= r.w; ty++) {
+          for (uint32_t tx = r.x; tx <= r.z; tx++) {
+            const uint32_t tile = ty * tiles_x + tx;
+            tile_keys[e] = (uint16_t)tile;
+            tile_vals[e] = slot;
+            e++;
+            atomicAdd(&h_lo[tile & 0xffu], 1u);
+            atomicAdd(&h_hi[tile >> 8], 1u);
+            atomicAdd(&tile_counts[tile], 1u);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (h_lo[t]) atomicAdd(&digit_hist[t], h_lo[t]);
+  if (h_hi[t]) atomicAdd(&digit_hist[256 + t], h_hi[t]);
+}
+
+__global__ void tile_ranges_kernel(const uint32_t* __restrict__ starts, const uint32_t* __restrict__ counts,
+                                   uint32_t tiles, uint2* __restrict__ ranges) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < tiles) ranges[t] = make_uint2(starts[t], starts[t] + counts[t]);
+}
+
+}  // namespace
+
+cudaError_t launch_tile_counts(const uint32_t* order, const ushort4* rects, uint32_t n, const FrameCounters* ctr,
+                               uint32_t* counts, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  tile_count_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, n, ctr, counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_emit(const uint32_t* order, const ushort4* rects, const uint32_t* offsets, uint32_t n,
+                             uint32_t tiles_x, uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys,
+                             uint32_t* tile_vals, uint32_t* tile_counts, uint32_t* digit_hist, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  tile_emit_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, offsets, n, tiles_x, capacity,
+                                                                       ctr, tile_keys, tile_vals, tile_counts,
+                                                                       digit_hist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_ranges(const uint32_t* tile_starts, const uint32_t* tile_counts, uint32_t tiles,
+                               uint2* ranges, cudaStream_t s) {
+  if (tiles == 0) return cudaSuccess;
+  tile_ranges_kernel<<<(tiles + 255) / 256, 256, 0, s>>>(tile_starts, tile_counts, tiles, ranges);
+  return cudaGetLastError();
+}
+
+}  // namespace sl
