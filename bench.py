@@ -1,0 +1,303 @@
+"""Benchmark of the GB300 splat pipeline (one JSON line on stdout).
+
+Workload (default): the hill-like scene of 1,048,576 Gaussians (seed 1) rendered at 1920x1080, fov 50 deg -- the
+plain single-frame forward configuration.  A step is one frame of the plain per-view path through the C ABI:
+project -> onesweep depth sort -> tile binning (+ tile sort, ranges) -> front-to-back composite, lit view.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config hill|cornell] [--impl ours|reference]
+
+value      views/s over all ranks, device time: CUDA events around each frame on the render stream, the L2 flushed
+           (a 256 MiB write) between frames outside the timed region, inputs resident in HBM.
+e2e        the same metric through the public API with host buffers: each step uploads the frame's RenderFrame and
+           part records and reads the W x H x 4 fp32 image back into pinned host memory, wall clock.
+roofline   the dominant kernel (by device time) against its bound; the sort is reported beside it against HBM.
+cpu_baseline  the CPU restatement (oracle/, a port of the reference algorithm) timed on this host's cores (rank 0).
+--impl reference  the CPU restatement of the reference pipeline alone (the reference's WGSL needs WebGPU, which is
+           not available on this machine), all host threads, each step one full frame of the same workload.
+Replicas only on N > 1: every rank renders its own frames, no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+MEASURED = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM = 6800.0  # GB/s
+KERNELS_PER_FRAME = 11  # project, 2 depth-sort passes, tile counts, scan, emit, 2 tile-sort passes, scan, ranges, composite
+
+
+def peaks():
+    if MEASURED.exists():
+        m = json.loads(MEASURED.read_text())
+        return float(m["hbm_gbs"]), float(m.get("sm_max_mhz", 2070.0)), "measured"
+    return FALLBACK_HBM, 2070.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_scene(name):
+    from splatlight_gb300 import scene
+    return scene.hill() if name == "hill" else scene.cornell()
+
+
+def frame_for(s, view_mode):
+    from splatlight_gb300 import camera
+    return camera.make_frame(s.eye, s.target, s.up, s.fov_deg, s.width, s.height, s.count, far=s.far,
+                             view_mode=view_mode, n_emit=len(s.emitters))
+
+
+def workload_desc(s):
+    return (f"{s.name}: {s.count:,} Gaussians + {len(s.emitters)} emitters, {s.width}x{s.height}, fov {s.fov_deg:g} deg, "
+            f"lit view (radiance per Gaussian resident), plain per-view path")
+
+
+def cpu_frame_seconds(s, colour, threads):
+    """One full frame of the CPU restatement (project, sort, bin, composite) on `threads` host threads."""
+    from oracle import oracle
+    f = frame_for(s, 3)
+    t0 = time.perf_counter()
+    oracle.render(s.gaussians, s.parts, f, emitters=s.emitters, colour=colour, threads=threads, want_entries=False)
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle
+    oracle.build()
+    s = make_scene(args.config)
+    colour = np.random.default_rng(7).uniform(0, 2, (s.count, 4)).astype(np.float32)
+    threads = os.cpu_count() or 1
+    t_warm = cpu_frame_seconds(s, colour, threads)
+    # bounded: at most ~90 s of CPU frames whatever --steps asks (each step is one full frame)
+    n_run = max(1, min(args.steps, int(90.0 / max(t_warm, 1e-3))))
+    times = [cpu_frame_seconds(s, colour, threads) for _ in range(n_run)]
+    ms = 1000.0 * sum(times) / len(times)
+    v = 1000.0 / ms
+    line = {"impl": "reference", "metric": "views/s", "value": round(v, 4), "unit": "views/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload_desc(s), "implementation": "CPU restatement of the reference pipeline "
+                       "(the reference's WGSL needs WebGPU: unavailable on this box)"},
+            "cpu_baseline": {"value": round(v, 4), "unit": "views/s", "cores": threads, "kind": "port",
+                             "sample": f"{n_run} full frames of the workload (bounded to ~90 s)"},
+            "e2e": {"value": round(v, 4), "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--config", default="hill", choices=["hill", "cornell"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    args.warmup = max(args.warmup, 3)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    __import__("__graft_entry__").build()
+    from splatlight_gb300.renderer import SplatRenderer
+
+    s = make_scene(args.config)
+    W, H = s.width, s.height
+    colour_host = np.random.default_rng(7).uniform(0, 2, (s.count, 4)).astype(np.float32)
+    colour = torch.from_numpy(colour_host).cuda()
+    f = frame_for(s, 3)
+    r = SplatRenderer(s.gaussians, s.parts)
+    r.set_emitters(s.emitters)
+    r.bind_colour(colour)
+    stream = torch.cuda.Stream()
+    out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    # warm-up (also sizes the tile-entry buffers)
+    for _ in range(args.warmup):
+        r.render(f, out=out, stream=stream.cuda_stream)
+
+    # device-timed steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier()
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.zero_()
+                starts[k].record(stream)
+                r.render(f, out=out, stream=stream.cuda_stream)
+                ends[k].record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    ms = sum(step_ms) / len(step_ms)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    views_per_s = world * 1000.0 / ms
+    stats = r.last_stats
+
+    # per-stage device times (events inside the pipeline), for the rooflines
+    r.set_timing(True)
+    stage = {"project": [], "sort": [], "bin": [], "composite": []}
+    frags = []
+    for _ in range(max(5, min(args.steps, 20))):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        r.render(f, out=out, stream=stream.cuda_stream)
+        st = r.last_stats
+        stage["project"].append(st.ms_project)
+        stage["sort"].append(st.ms_sort)
+        stage["bin"].append(st.ms_bin)
+        stage["composite"].append(st.ms_composite)
+        frags.append(st.fragments)
+    r.set_timing(False)
+    stage_ms = {k: statistics.median(v) for k, v in stage.items()}
+
+    # end to end through the public API with host buffers: frame + parts up, image down (pinned), wall clock
+    host_out = torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True)
+    host_out_np = host_out.numpy()
+    parts = s.parts.copy()
+    for _ in range(2):
+        r.write_parts(parts)
+        r.render(f, out=host_out_np)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r.write_parts(parts)
+        r.render(f, out=host_out_np)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = f.nbytes + parts.nbytes
+    d2h = W * H * 16
+
+    hbm, sm_max_cfg, peak_kind = peaks()
+    clocks = clk.summary()
+    sm_mhz = clocks["sm_max_mhz"] or sm_max_cfg
+    # sort: 2 onesweep passes over u16 keys + u32 values: (2 + 6) + (6 + 4) bytes per slot
+    sort_bytes = 18.0 * stats.slots
+    sort_gbs = sort_bytes / (stage_ms["sort"] * 1e-3) / 1e9
+    # composite: 20 FP32 flops per blended fragment (local coordinates 4, q 2, tests 3, alpha 4, blend 7), nominal
+    # FP32 issue peak = 152 SMs x 128 lanes x 2 flops x clock
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    frag = statistics.median(frags)
+    comp_tflops = 20.0 * frag / (stage_ms["composite"] * 1e-3) / 1e12
+    roof_sort = {"bound": "hbm", "achieved": round(sort_gbs, 1), "peak": hbm, "unit": "GB/s",
+                 "frac": round(sort_gbs / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+                 "algorithmic_bytes_per_launch": sort_bytes, "kernel": "onesweep_pass x2 (depth keys)"}
+    roof_comp = {"bound": "fp32", "achieved": round(comp_tflops, 3), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
+                 "frac": round(comp_tflops / fp32_peak, 4), "traffic": None,
+                 "peak_kind": "nominal FP32 issue rate at the sampled max SM clock (no measured FP32 peak exists)",
+                 "algorithmic_flops_per_launch": 20.0 * frag, "kernel": "composite_kernel<16>"}
+    dominant = max(stage_ms, key=stage_ms.get)
+    roofline = roof_comp if dominant == "composite" else roof_sort
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sec = cpu_frame_seconds(s, colour_host, threads)
+        cpu = {"value": round(1.0 / sec, 4), "unit": "views/s", "cores": threads, "kind": "port",
+               "sample": "1 full frame of the same workload (project, sort, bin, composite)"}
+
+    if rank == 0:
+        line = {"metric": "views/s", "value": round(views_per_s, 2), "unit": "views/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": workload_desc(s), "parallelism": f"replicas x{world}",
+                           "l2": "flushed (256 MiB write) between timed frames", "tile": "16x16",
+                           "slots": int(stats.slots), "visible": int(stats.visible), "entries": int(stats.entries)},
+                "e2e": {"value": round(world / e2e_s, 2), "unit": "views/s", "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(d2h)},
+                "gpu_launches": KERNELS_PER_FRAME * args.steps,
+                "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
+                "roofline": roofline, "sort_roofline": roof_sort, "composite_roofline": roof_comp,
+                "cpu_baseline": cpu, "clocks": clocks}
+        print(json.dumps(line))
+    r.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

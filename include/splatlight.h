@@ -157,6 +157,7 @@ typedef struct sl_render_stats {
   uint32_t visible;              /* valid keys (scan.wgsl's instance count) */
   uint32_t entries;              /* (tile, splat) pairs binned */
   uint32_t tiles;                /* tiles in the view */
+  uint32_t fragments;            /* fragments the compositor blended (after early termination) */
   float ms_project, ms_sort, ms_bin, ms_composite, ms_total; /* device times when timing is on, else 0 */
 } sl_render_stats;
 

@@ -25,6 +25,7 @@ class SplatlightError(RuntimeError):
 
 class RenderStats(C.Structure):
     _fields_ = [("slots", C.c_uint32), ("visible", C.c_uint32), ("entries", C.c_uint32), ("tiles", C.c_uint32),
+                ("fragments", C.c_uint32),
                 ("ms_project", C.c_float), ("ms_sort", C.c_float), ("ms_bin", C.c_float),
                 ("ms_composite", C.c_float), ("ms_total", C.c_float)]
 

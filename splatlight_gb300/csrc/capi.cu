@@ -2,8 +2,8 @@
 // The per-frame chain (sl_render) is stream-ordered and launches, in order:
 //   project  -> onesweep pass x2 (depth keys) -> tile counts -> scan -> tile emit -> onesweep pass x1-2 (tile ids)
 //   -> scan (tile starts) -> ranges -> composite
-// with one synchronisation at the end (frame counters: visible, entries, overflow, timeout).  If the tile-entry
-// capacity was too small the frame is re-run once after growing it.
+// with one synchronisation at the end (frame counters: visible, entries, overflow, timeout); the tile sort reads the
+// entry count on the device.  If the tile-entry capacity was too small the frame is re-run after growing it.
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -362,7 +362,8 @@ static int render_once(sl_renderer* r, const sl_render_frame* f, float4* out_dev
                                vb.key16.as<uint16_t>(), vb.recs.as<SplatRec>(), vb.rects.as<ushort4>(), hist, ctr, s),
                 "project");
   if (ev) SL_CHECK_CUDA(cudaEventRecord(ev[1], s), "event");
-  SL_CHECK_CUDA(sort16_pairs(vb.key16.as<uint16_t>(), nullptr, vb.order.as<uint32_t>(), n, 16, hist, sc, ctr, s),
+  SL_CHECK_CUDA(sort16_pairs(vb.key16.as<uint16_t>(), nullptr, vb.order.as<uint32_t>(), n, nullptr, 16, hist, sc,
+                             ctr, s),
                 "depth sort");
   if (ev) SL_CHECK_CUDA(cudaEventRecord(ev[2], s), "event");
   SL_CHECK_CUDA(launch_tile_counts(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), n, ctr, vb.slot_counts.as<uint32_t>(), s),
@@ -375,17 +376,10 @@ static int render_once(sl_renderer* r, const sl_render_frame* f, float4* out_dev
                                  vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), vb.tile_counts.as<uint32_t>(),
                                  hist + 512, s),
                 "tile emit");
-  // the entry count is only known on the device: sort up to the capacity bound read by the kernels themselves
-  // would need a device-side launch; instead synchronise once here (cheap: the scan result is a single word)
-  SL_CHECK_CUDA(cudaMemcpyAsync(r->host_ctr, ctr, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s), "counters");
-  SL_CHECK_CUDA(cudaStreamSynchronize(s), "sync");
-  const uint32_t entries = r->host_ctr->entries;
-  if (r->host_ctr->overflow || entries > cap) {
-    r->entry_capacity = (uint64_t)entries + entries / 4 + 4096;
-    return SL_ERR_OVERFLOW;
-  }
+  // the entry count is only known on the device: the tile sort reads it there (grid sized for the capacity)
   SL_CHECK_CUDA(sort16_pairs(vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), vb.tile_vals.as<uint32_t>(),
-                             entries, bits_for(tiles - 1), hist + 512, sc, ctr, s),
+                             (uint32_t)(cap > 0xffffffffull ? 0xffffffffu : cap), &ctr->entries, bits_for(tiles - 1),
+                             hist + 512, sc, ctr, s),
                 "tile sort");
   SL_CHECK_CUDA(exclusive_scan_u32(vb.tile_counts.as<uint32_t>(), vb.tile_starts.as<uint32_t>(), tiles, nullptr,
                                    vb.scan_scratch.ptr, ctr, s),
@@ -412,11 +406,9 @@ static int render_once(sl_renderer* r, const sl_render_frame* f, float4* out_dev
   r->last_w = W;
   r->last_h = H;
   r->last_tiles = tiles;
-  r->last_entries = entries;
   r->last_mode = f->view_mode;
   if (stats) {
     stats->slots = n;
-    stats->entries = entries;
     stats->tiles = tiles;
   }
   return SL_OK;
@@ -446,16 +438,22 @@ int sl_render(sl_renderer* r, const sl_render_frame* f, float* out_rgba, int out
     uint32_t* counts_dev = count_mode ? r->vb.counts.as<uint32_t>() : nullptr;
     sl_render_stats local{};
     rc = render_once(r, f, out_dev, counts_dev, s, stats ? &local : nullptr);
-    if (rc == SL_ERR_OVERFLOW) continue;
     if (rc) return rc;
     if (!out_on_device)
       SL_CHECK_CUDA(cudaMemcpyAsync(out_rgba, out_dev, 16ull * W * H, cudaMemcpyDeviceToHost, s), "output copy");
     SL_CHECK_CUDA(cudaStreamSynchronize(s), "sync");
-    r->have_frame = true;
     const FrameCounters& hc = *r->host_ctr;
+    if (hc.overflow || hc.entries > r->entry_capacity) {  // too many tile entries: grow and render again
+      r->entry_capacity = (uint64_t)hc.entries + hc.entries / 4 + 4096;
+      continue;
+    }
+    r->last_entries = hc.entries;
+    local.entries = hc.entries;
+    r->have_frame = true;
     if (stats) {
       *stats = local;
       stats->visible = hc.visible;
+      stats->fragments = hc.fragments;
       if (r->timing) {
         float ms[4] = {0, 0, 0, 0};
         cudaEventElapsedTime(&ms[0], r->tm.ev[0], r->tm.ev[1]);

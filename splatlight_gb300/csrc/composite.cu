@@ -153,6 +153,8 @@ __global__ void __launch_bounds__(kThreads) composite_kernel(const CompositePara
     }
   }
   if (timed_out) atomicExch(const_cast<uint32_t*>(&ctr->timeout), 1u);
+  uint32_t wk = __reduce_add_sync(0xffffffffu, kept);
+  if ((t & 31) == 0 && wk) atomicAdd(const_cast<uint32_t*>(&ctr->fragments), wk);
   if (inside) {
     const size_t pix = (size_t)py * P.width + px;
     if (P.count_mode) {

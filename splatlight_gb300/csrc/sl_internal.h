@@ -50,7 +50,8 @@ struct FrameCounters {
   uint32_t entries;        // tile entries
   uint32_t overflow;       // entries beyond capacity
   uint32_t timeout;        // a bounded device wait gave up
-  uint32_t pad[3];
+  uint32_t fragments;      // fragments composited (kept and blended) by the compositor
+  uint32_t pad[2];
 };
 
 // ---- launchers (each returns cudaError_t of the launch) ----------------------------------------------------------
@@ -73,8 +74,10 @@ size_t sort_tiles_for(uint32_t n);
 // Sorts keys[0, n) (16-bit, `bits` significant bits) stably; vals: input values (NULL = slot index);
 // writes the permutation/values to vals_out.  digit_hist: [passes][256] counts of the digits of every key
 // (pass p = bits 8p .. 8p+7), filled by the producer kernel.  Keys are ping-ponged through scratch.
-cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals_out, uint32_t n, int bits,
-                         const uint32_t* digit_hist, SortScratch& sc, FrameCounters* ctr, cudaStream_t s);
+// n is the element count, or with n_dev non-null an upper bound and *n_dev (read on the device) the count.
+cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals_out, uint32_t n,
+                         const uint32_t* n_dev, int bits, const uint32_t* digit_hist, SortScratch& sc,
+                         FrameCounters* ctr, cudaStream_t s);
 // Counts the digit histograms of u16 keys (used when no producer kernel filled them).
 cudaError_t launch_digit_hist16(const uint16_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s);
 

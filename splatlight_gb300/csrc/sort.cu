@@ -61,7 +61,8 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
 __global__ void __launch_bounds__(kThreads) onesweep_pass(const uint16_t* __restrict__ keys_in,
                                                           const uint32_t* __restrict__ vals_in,
                                                           uint16_t* __restrict__ keys_out,
-                                                          uint32_t* __restrict__ vals_out, uint32_t n, int shift,
+                                                          uint32_t* __restrict__ vals_out, uint32_t n_max,
+                                                          const uint32_t* __restrict__ n_dev, int shift,
                                                           const uint32_t* __restrict__ digit_hist,
                                                           uint32_t* status, uint32_t* tile_ctr, FrameCounters* ctr) {
   __shared__ uint32_t s_tile;
@@ -73,12 +74,20 @@ __global__ void __launch_bounds__(kThreads) onesweep_pass(const uint16_t* __rest
   __shared__ uint32_t s_vals[kTile];
 
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  // element count: a host bound, or the smaller device-side count (tile entries, known only on the device)
+  // (a device count above the bound means the producer overflowed its buffer: sort nothing, the host re-runs)
+  uint32_t n = n_max;
+  if (n_dev) {
+    uint32_t nd = *n_dev;
+    n = nd <= n_max ? nd : 0u;
+  }
   if (t == 0) s_tile = atomicAdd(tile_ctr, 1u);
 #pragma unroll
   for (int k = 0; k < kWarps; k++) warp_hist[k][t] = 0u;
   __syncthreads();
   const uint32_t tile = s_tile;
   const uint32_t tile_base = tile * kTile;
+  if (tile_base >= n) return;  // the grid covers n_max; tiles past n have nothing to do (no later tile waits on them)
 
   uint32_t keys[kItems], vals[kItems], ranks[kItems];
   const uint32_t wbase = tile_base + (uint32_t)w * (32u * kItems) + (uint32_t)lane;
@@ -171,6 +180,7 @@ __global__ void __launch_bounds__(kThreads) onesweep_pass(const uint16_t* __rest
     uint32_t key = s_keys[j];
     uint32_t d = (key >> shift) & 0xffu;
     uint32_t dst = digit_base[d] + (j - local_start[d]);
+    if (dst >= n) continue;  // only after a look-back timeout (reported); never write out of range
     if (keys_out) keys_out[dst] = (uint16_t)key;
     vals_out[dst] = s_vals[j];
   }
@@ -205,8 +215,9 @@ cudaError_t launch_digit_hist16(const uint16_t* keys, uint32_t n, int passes, ui
   return cudaGetLastError();
 }
 
-cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals_out, uint32_t n, int bits,
-                         const uint32_t* digit_hist, SortScratch& sc, FrameCounters* ctr, cudaStream_t s) {
+cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals_out, uint32_t n,
+                         const uint32_t* n_dev, int bits, const uint32_t* digit_hist, SortScratch& sc,
+                         FrameCounters* ctr, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   if (n > kValueMask) return cudaErrorInvalidValue;
   const uint32_t tiles = (uint32_t)sort_tiles_for(n);
@@ -218,18 +229,18 @@ cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals
   if (e != cudaSuccess) return e;
   if (passes == 1) {
     uint32_t* out = (vals_in == vals_out) ? sc.vals_alt : vals_out;
-    onesweep_pass<<<tiles, kThreads, 0, s>>>(keys, vals_in, nullptr, out, n, 0, digit_hist, sc.status, sc.tile_ctr,
-                                             ctr);
+    onesweep_pass<<<tiles, kThreads, 0, s>>>(keys, vals_in, nullptr, out, n, n_dev, 0, digit_hist, sc.status,
+                                             sc.tile_ctr, ctr);
     e = cudaGetLastError();
     if (e == cudaSuccess && out != vals_out)
       e = cudaMemcpyAsync(vals_out, out, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
     return e;
   }
-  onesweep_pass<<<tiles, kThreads, 0, s>>>(keys, vals_in, sc.keys_alt, sc.vals_alt, n, 0, digit_hist, sc.status,
-                                           sc.tile_ctr, ctr);
+  onesweep_pass<<<tiles, kThreads, 0, s>>>(keys, vals_in, sc.keys_alt, sc.vals_alt, n, n_dev, 0, digit_hist,
+                                           sc.status, sc.tile_ctr, ctr);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  onesweep_pass<<<tiles, kThreads, 0, s>>>(sc.keys_alt, sc.vals_alt, nullptr, vals_out, n, 8, digit_hist + 256,
-                                           sc.status + (size_t)256u * tiles, sc.tile_ctr + 1, ctr);
+  onesweep_pass<<<tiles, kThreads, 0, s>>>(sc.keys_alt, sc.vals_alt, nullptr, vals_out, n, n_dev, 8,
+                                           digit_hist + 256, sc.status + (size_t)256u * tiles, sc.tile_ctr + 1, ctr);
   return cudaGetLastError();
 }
 
