@@ -204,6 +204,15 @@ SL_API int sl_renderer_read_debug(sl_renderer* r, uint32_t* keys, uint32_t* orde
  * back-to-front order) holds stats.entries values; [ranges[2t], ranges[2t+1]) indexes tile t's list. */
 SL_API int sl_renderer_read_entries(sl_renderer* r, uint32_t* entries, uint64_t cap);
 
+/* ---- sort (shaders/radix.wgsl) --------------------------------------------------------------------------------- */
+
+/* The stable sort of 16-bit depth keys on its own (shaders/radix.wgsl:1-139; encoded by src/renderer.js:425-434):
+ * writes to order_dev the permutation that sorts keys_dev[0, n) ascending, ties in index order (radix.wgsl's vals_out
+ * after its last pass, values = index).  Device pointers; n < 2^30.  Scratch is allocated stream-ordered on `stream`
+ * and released before return; the call returns after the sort completed (SL_ERR_TIMEOUT if a bounded device-side
+ * wait gave up). */
+SL_API int sl_sort_keys16(const uint16_t* keys_dev, uint32_t n, uint32_t* order_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
