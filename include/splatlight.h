@@ -213,6 +213,15 @@ SL_API int sl_renderer_read_entries(sl_renderer* r, uint32_t* entries, uint64_t 
  * wait gave up). */
 SL_API int sl_sort_keys16(const uint16_t* keys_dev, uint32_t n, uint32_t* order_dev, void* stream);
 
+/* sl_sort_keys16 without any device allocation, for callers that may not allocate (a host engine that owns all
+ * device memory through its own pool under a hard cap, or a frame loop whose latency budget rules out allocator
+ * calls).  No counterpart in the reference.  Same inputs, output and status codes as sl_sort_keys16, for
+ * n <= 1,048,576 keys (larger n: SL_ERR_INVALID_ARG).  Scratch is one fixed 6.5 MiB device array inside the library,
+ * held by every GPU that loads it until the process exits; the caller still passes keys and order.  The first call
+ * on a device looks up the array's device address (make it before any stream capture).  All calls share the array:
+ * calls that overlap on the GPU (other streams, other threads) race, so serialise them. */
+SL_API int sl_sort_keys16_noalloc(const uint16_t* keys_dev, uint32_t n, uint32_t* order_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

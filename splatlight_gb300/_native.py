@@ -57,6 +57,7 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_renderer_read_debug": (_I, [_P, _P, _P, _P, _P]),
     "sl_renderer_read_entries": (_I, [_P, _P, _U64]),
     "sl_sort_keys16": (_I, [_P, _U32, _P, _P]),
+    "sl_sort_keys16_noalloc": (_I, [_P, _U32, _P, _P]),
 }
 
 _lib: C.CDLL | None = None
