@@ -10,6 +10,8 @@
  *   - the fragment keep test alpha >= 1/255 is evaluated in its closed form q <= qcut = 2 ln(tau0 / tau_min), the
  *     bound shaders/project.wgsl:290-295 derives for the quad radius (r = sqrt(qcut)); in real arithmetic the two
  *     are the same test, in fp32 they can differ only for fragments whose alpha rounds to within an ulp of 1/255.
+ *     The quad (|local| <= r per axis) circumscribes that ellipse, so it removes nothing the keep test keeps, up to
+ *     the same rounding; it is therefore not tested separately.
  * Pixel geometry: framebuffer pixel (ix, iy), iy down from the top, centre (ix + 0.5, iy + 0.5); a splat's Mahalanobis
  * offset at a pixel is local = (d . g0, d . g1) with g = a r / |a|^2 per quad axis a in pixels -- the grad varying of
  * shaders/splat.wgsl:44-46 -- which equals the quad's interpolated `local` (shaders/splat.wgsl:43) in real arithmetic.
@@ -370,7 +372,6 @@ void orc_composite(const orc_splat* splats, const uint32_t* order, uint32_t visi
           float dx = ((float)ix + 0.5f) - s->cx;
           float lx = fmaf(dx, s->g0x, dy * s->g0y);
           float ly = fmaf(dx, s->g1x, dy * s->g1y);
-          if (fabsf(lx) > s->r || fabsf(ly) > s->r) continue; /* outside the quad */
           float q = fmaf(lx, lx, ly * ly);
           if (q > s->qcut) continue; /* alpha < 1/255: discarded (splat.wgsl:73) */
           size_t pix = (size_t)iy * width + (size_t)ix;

@@ -28,7 +28,8 @@ int cuda_fail(cudaError_t e, const char* what) {
 void ViewBuffers::release_all() {
   DevBuf* all[] = {&key16,     &recs,      &rects,       &order,       &slot_counts, &slot_offsets, &keys_alt,
                    &vals_alt,  &status,    &tile_ctr,    &tile_keys,   &tile_vals,   &tile_counts,  &tile_starts,
-                   &ranges,    &digit_hist, &scan_scratch, &counters, &out,         &counts};
+                   &ranges,    &digit_hist, &scan_scratch, &counters, &out,         &counts,       &run_start,
+                   &run_end};
   for (DevBuf* b : all) b->release();
 }
 
@@ -322,6 +323,8 @@ static cudaError_t ensure_view_buffers(ViewBuffers& vb, uint32_t n, uint32_t til
   ENS(vb.tile_counts, 4ull * tiles + 16);
   ENS(vb.tile_starts, 4ull * tiles + 16);
   ENS(vb.ranges, 8ull * tiles + 16);
+  ENS(vb.run_start, 4ull * tiles + 16);
+  ENS(vb.run_end, 4ull * tiles + 16);
   ENS(vb.digit_hist, 4ull * 4 * 256);
   size_t sc = scan_scratch_bytes(n);
   size_t sc2 = scan_scratch_bytes(tiles);
@@ -357,7 +360,8 @@ static int render_once(sl_renderer* r, const sl_render_frame* f, float4* out_dev
   if (ev) SL_CHECK_CUDA(cudaEventRecord(ev[0], s), "event");
   SL_CHECK_CUDA(cudaMemsetAsync(ctr, 0, sizeof(FrameCounters), s), "memset counters");
   SL_CHECK_CUDA(cudaMemsetAsync(hist, 0, 4 * 4 * 256, s), "memset hist");
-  SL_CHECK_CUDA(cudaMemsetAsync(vb.tile_counts.ptr, 0, 4ull * tiles, s), "memset tile counts");
+  SL_CHECK_CUDA(cudaMemsetAsync(vb.run_start.ptr, 0, 4ull * tiles, s), "memset runs");
+  SL_CHECK_CUDA(cudaMemsetAsync(vb.run_end.ptr, 0, 4ull * tiles, s), "memset runs");
   SL_CHECK_CUDA(launch_project(P, r->gaussians.as<sl_gaussian>(), r->emitters.as<sl_gaussian>(), colour, lo_b,
                                vb.key16.as<uint16_t>(), vb.recs.as<SplatRec>(), vb.rects.as<ushort4>(), hist, ctr, s),
                 "project");
@@ -373,14 +377,20 @@ static int render_once(sl_renderer* r, const sl_render_frame* f, float4* out_dev
                 "entry scan");
   SL_CHECK_CUDA(launch_tile_emit(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.slot_offsets.as<uint32_t>(), n,
                                  P.tiles_x, (uint32_t)(cap > 0xffffffffull ? 0xffffffffu : cap), ctr,
-                                 vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), vb.tile_counts.as<uint32_t>(),
-                                 hist + 512, s),
+                                 vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), hist + 512, s),
                 "tile emit");
   // the entry count is only known on the device: the tile sort reads it there (grid sized for the capacity)
+  const uint32_t cap32 = (uint32_t)(cap > 0xffffffffull ? 0xffffffffu : cap);
   SL_CHECK_CUDA(sort16_pairs(vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), vb.tile_vals.as<uint32_t>(),
-                             (uint32_t)(cap > 0xffffffffull ? 0xffffffffu : cap), &ctr->entries, bits_for(tiles - 1),
-                             hist + 512, sc, ctr, s),
+                             cap32, &ctr->entries, bits_for(tiles - 1), hist + 512, sc, ctr, s,
+                             vb.tile_keys.as<uint16_t>()),
                 "tile sort");
+  SL_CHECK_CUDA(launch_tile_runs(vb.tile_keys.as<uint16_t>(), &ctr->entries, cap32, vb.run_start.as<uint32_t>(),
+                                 vb.run_end.as<uint32_t>(), s),
+                "tile runs");
+  SL_CHECK_CUDA(launch_tile_run_counts(vb.run_start.as<uint32_t>(), vb.run_end.as<uint32_t>(), tiles,
+                                       vb.tile_counts.as<uint32_t>(), s),
+                "tile counts");
   SL_CHECK_CUDA(exclusive_scan_u32(vb.tile_counts.as<uint32_t>(), vb.tile_starts.as<uint32_t>(), tiles, nullptr,
                                    vb.scan_scratch.ptr, ctr, s),
                 "tile scan");

@@ -1,14 +1,18 @@
-// Tile compositor: one CTA of 256 threads per screen tile, one pixel per thread.  The tile's sorted splat list is
-// walked from its nearest entry to its farthest (front to back), in batches of 256 records; each batch is gathered
-// into shared memory by the TMA unit (cp.async.bulk, one 48-byte bulk copy per record, completion counted on an
-// mbarrier) while the previous batch is composited (double buffering).  Per pixel:
-//   local = (d . g0, d . g1), keep if |local.x|, |local.y| <= r (inside the quad) and q = |local|^2 <= qcut
-//   (alpha >= 1/255), alpha = 1 - exp(-tau0 exp(-q/2)), C += T alpha rgb, T *= 1 - alpha
+// Tile compositor: one CTA of 256 threads per screen tile, one pixel per thread, each warp an 8x4-pixel block.  The
+// tile's sorted splat list is walked from its nearest entry to its farthest (front to back), in batches of 256
+// records; each batch is gathered into shared memory by the TMA unit (cp.async.bulk, one 48-byte bulk copy per
+// record, completion counted on an mbarrier) while the previous batch is composited (double buffering).  Once a batch
+// lands, every thread tests its own record's candidate box against the 8 warp blocks and the warps ballot those
+// bits into per-block masks, so each warp visits only the records that can reach its pixels.  Per pixel:
+//   local = (d . g0, d . g1), q = |local|^2, keep if q <= qcut (alpha >= 1/255),
+//   alpha = 1 - exp(-tau0 exp(-q/2)), C += T alpha rgb, T *= 1 - alpha
 // which composites the same ordered splats as the reference's back-to-front premultiplied "over" blend
 // (shaders/splat.wgsl:66-78, src/renderer.js:133-143), in fp32.  A pixel stops once T < t_stop / max radiance (the
 // skipped tail is below 1e-4 in every channel); a warp whose pixels all stopped skips the batch (warp vote) and the CTA
 // leaves when every pixel stopped.  The overdraw view (count_mode) never stops early and counts kept fragments.
 // Every mbarrier wait is bounded; a give-up sets FrameCounters::timeout and the kernel still drains its copies.
+#include <cuda_fp16.h>
+
 #include "sl_internal.h"
 
 namespace sl {
@@ -64,16 +68,22 @@ template <int TW>
 __global__ void __launch_bounds__(kThreads) composite_kernel(const CompositeParams P, const uint2* __restrict__ ranges,
                                                              const uint32_t* __restrict__ tile_vals,
                                                              const SplatRec* __restrict__ recs,
-                                                             const FrameCounters* ctr, float4* __restrict__ out,
+                                                             FrameCounters* ctr, float4* __restrict__ out,
                                                              uint32_t* __restrict__ counts) {
   constexpr int TH = kThreads / TW;
+  constexpr int BX = TW / 8;  // warp blocks of 8 x 4 pixels per tile row
+  constexpr int BY = TH / 4;
+  static_assert(BX * BY == kThreads / 32, "one 8x4 block per warp");
   __shared__ SplatRec buf[2][kThreads];
+  __shared__ uint32_t masks[kThreads / 32][kThreads / 32];  // [warp block][loader warp]: records touching the block
   __shared__ __align__(8) uint64_t bars[2];
 
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const uint32_t tile = blockIdx.x;
   const uint32_t tx = tile % P.tiles_x, ty = tile / P.tiles_x;
-  const uint32_t px = tx * TW + (uint32_t)(t % TW), py = ty * TH + (uint32_t)(t / TW);
+  const uint32_t x0 = tx * TW, y0 = ty * TH;  // tile origin, pixels
+  const uint32_t px = x0 + (uint32_t)((w % BX) * 8 + (lane & 7));
+  const uint32_t py = y0 + (uint32_t)((w / BX) * 4 + (lane >> 3));
   const bool inside = px < P.width && py < P.height;
 
   const uint32_t bar0 = smem_addr(&bars[0]), bar1 = smem_addr(&bars[1]);
@@ -90,6 +100,7 @@ __global__ void __launch_bounds__(kThreads) composite_kernel(const CompositePara
   const float maxrad = fmaxf(__uint_as_float(ctr->max_rad_bits), 1.0f);
   const float t_stop = P.count_mode ? -1.0f : P.t_stop_scale / maxrad;
   const float pxc = (float)px + 0.5f, pyc = (float)py + 0.5f;
+  const float fx0 = (float)x0, fy0 = (float)y0;
   const float kNegHalfLog2e = -0.72134752044448170f;
   const float kNegLog2e = -1.44269504088896341f;
 
@@ -120,28 +131,60 @@ __global__ void __launch_bounds__(kThreads) composite_kernel(const CompositePara
     const uint32_t hi = e - kThreads * b;
     const uint32_t nb = (hi - s) > (uint32_t)kThreads ? (uint32_t)kThreads : hi - s;
     const SplatRec* rb = buf[b & 1u];
+
+    // culling, SIMD across records: which warp blocks can record t reach?  Its candidate box is centre +- (hx, hy)
+    // (one pixel of margin included, rounded up); block (bx, by) holds pixel centres x0 + 8bx + [0.5, 7.5],
+    // y0 + 4by + [0.5, 3.5].
+    uint32_t bits = 0;
+    if ((uint32_t)t < nb) {
+      const float4 A = rb[t].a;
+      const float hb = rb[t].b.z;
+      const __half2 hxy = *reinterpret_cast<const __half2*>(&hb);
+      const float hx = __low2float(hxy), hy = __high2float(hxy);
+      int bx0 = (int)ceilf((A.x - hx - 7.5f - fx0) * 0.125f), bx1 = (int)floorf((A.x + hx - 0.5f - fx0) * 0.125f);
+      int by0 = (int)ceilf((A.y - hy - 3.5f - fy0) * 0.25f), by1 = (int)floorf((A.y + hy - 0.5f - fy0) * 0.25f);
+      bx0 = max(bx0, 0);
+      by0 = max(by0, 0);
+      bx1 = min(bx1, BX - 1);
+      by1 = min(by1, BY - 1);
+      if (bx0 <= bx1) {
+        const uint32_t row = ((2u << bx1) - 1u) & ~((1u << bx0) - 1u);
+        for (int by = by0; by <= by1; by++) bits |= row << (by * BX);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kThreads / 32; k++) {
+      const uint32_t m = __ballot_sync(0xffffffffu, (bits >> k) & 1u);
+      if (lane == 0) masks[k][w] = m;
+    }
+    __syncthreads();
+
     if (__any_sync(0xffffffffu, alive)) {
-      for (uint32_t j = 0; j < nb; j++) {
-        const float4 A = rb[j].a;
-        const float4 B = rb[j].b;
-        const float dx = pxc - A.x, dy = pyc - A.y;
-        const float lx = fmaf(dx, A.z, dy * A.w);
-        const float ly = fmaf(dx, B.x, dy * B.y);
-        const float q = fmaf(lx, lx, ly * ly);
-        const bool keep = alive && fabsf(lx) <= B.z && fabsf(ly) <= B.z && q <= B.w;
-        if (keep) {
-          const float4 C = rb[j].c;
-          const float ev = ex2_approx(q * kNegHalfLog2e);
-          const float alpha = 1.0f - ex2_approx(C.w * kNegLog2e * ev);
-          const float wgt = T * alpha;
-          cr = fmaf(wgt, C.x, cr);
-          cg = fmaf(wgt, C.y, cg);
-          cb = fmaf(wgt, C.z, cb);
-          T = T - wgt;
-          kept++;
-          if (T < t_stop) alive = false;
+      for (int lw = 0; lw < kThreads / 32; lw++) {
+        uint32_t m = masks[w][lw];
+        while (m) {
+          const uint32_t j = (uint32_t)(lw * 32 + __ffs(m) - 1);
+          m &= m - 1u;
+          const float4 A = rb[j].a;
+          const float4 B = rb[j].b;
+          const float dx = pxc - A.x, dy = pyc - A.y;
+          const float lx = fmaf(dx, A.z, dy * A.w);
+          const float ly = fmaf(dx, B.x, dy * B.y);
+          const float q = fmaf(lx, lx, ly * ly);
+          if (alive && q <= B.w) {
+            const float4 C = rb[j].c;
+            const float ev = ex2_approx(q * kNegHalfLog2e);
+            const float alpha = 1.0f - ex2_approx(C.w * kNegLog2e * ev);
+            const float wgt = T * alpha;
+            cr = fmaf(wgt, C.x, cr);
+            cg = fmaf(wgt, C.y, cg);
+            cb = fmaf(wgt, C.z, cb);
+            T = T - wgt;
+            kept++;
+            if (T < t_stop) alive = false;
+          }
         }
-        if ((j & 31u) == 31u && !__any_sync(0xffffffffu, alive)) break;
+        if (!__any_sync(0xffffffffu, alive)) break;
       }
     }
     if (__syncthreads_count(alive) == 0) {
@@ -152,9 +195,9 @@ __global__ void __launch_bounds__(kThreads) composite_kernel(const CompositePara
       break;
     }
   }
-  if (timed_out) atomicExch(const_cast<uint32_t*>(&ctr->timeout), 1u);
-  uint32_t wk = __reduce_add_sync(0xffffffffu, kept);
-  if ((t & 31) == 0 && wk) atomicAdd(const_cast<uint32_t*>(&ctr->fragments), wk);
+  if (timed_out) atomicExch(&ctr->timeout, 1u);
+  const uint32_t wk = __reduce_add_sync(0xffffffffu, kept);
+  if (lane == 0 && wk) atomicAdd(&ctr->fragments, wk);
   if (inside) {
     const size_t pix = (size_t)py * P.width + px;
     if (P.count_mode) {
@@ -169,7 +212,7 @@ __global__ void __launch_bounds__(kThreads) composite_kernel(const CompositePara
 }  // namespace
 
 cudaError_t launch_composite(const CompositeParams& P, const uint2* ranges, const uint32_t* tile_vals,
-                             const SplatRec* recs, const FrameCounters* ctr, float4* out, uint32_t* counts,
+                             const SplatRec* recs, FrameCounters* ctr, float4* out, uint32_t* counts,
                              cudaStream_t s) {
   const uint32_t tiles = P.tiles_x * P.tiles_y;
   if (tiles == 0) return cudaSuccess;

@@ -7,6 +7,8 @@
 // Compiled with --fmad=false: every a*b+c rounds twice, as in the CPU restatement, so keys, tile rectangles and the
 // per-fragment keep bound are bit-identical to it.  Sums evaluate left to right, matrix-vector products as
 // col0*v.x + col1*v.y + col2*v.z, normalize(v) = v / sqrt(dot(v, v)), and ln comes from sl_detmath.h.
+#include <cuda_fp16.h>
+
 #include "sl_detmath.h"
 #include "sl_internal.h"
 
@@ -233,14 +235,16 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
           float a1x = e1x * sl1 * r, a1y = e1y * sl1 * r;
           float n0 = fmaxf(a0x * a0x + a0y * a0y, 1e-12f);
           float n1 = fmaxf(a1x * a1x + a1y * a1y, 1e-12f);
+          // candidate pixels: ellipse bounding box plus one pixel; tiles it overlaps
+          float hx = r * sqrtf(a) + 1.0f, hy = r * sqrtf(c) + 1.0f;
           SplatRec rec;
           rec.a = make_float4(cx, cy, a0x * r / n0, -(a0y * r / n0));
-          rec.b = make_float4(a1x * r / n1, -(a1y * r / n1), r, qcut);
+          // half extents of that box, rounded up to half precision: the compositor's conservative block culling
+          __half2 hxy = __halves2half2(__float2half_ru(hx), __float2half_ru(hy));
+          rec.b = make_float4(a1x * r / n1, -(a1y * r / n1), *reinterpret_cast<float*>(&hxy), qcut);
           rec.c = make_float4(cr, cg, cb, tau0);
           recs[i] = rec;
           maxrad = fmaxf(fmaxf(cr, cg), fmaxf(cb, 0.0f));
-          // candidate pixels: ellipse bounding box plus one pixel; tiles it overlaps
-          float hx = r * sqrtf(a) + 1.0f, hy = r * sqrtf(c) + 1.0f;
           float xl = fmaxf(cx - hx - 0.5f, -1.0f), xh = fminf(cx + hx - 0.5f, Wf);
           float yl = fmaxf(cy - hy - 0.5f, -1.0f), yh = fminf(cy + hy - 0.5f, Hf);
           int ix0 = (int)ceilf(xl), ix1 = (int)floorf(xh);

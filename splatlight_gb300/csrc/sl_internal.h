@@ -15,7 +15,7 @@ constexpr uint32_t kPartHidden = 4u;          // shaders/common.wgsl:40
 
 // One projected splat as the compositor reads it: 48 B, 16-byte aligned, one bulk copy per record.
 //   a = (cx, cy, g0x, g0y)   centre in framebuffer pixels (y down) and the first grad row
-//   b = (g1x, g1y, r, qcut)  second grad row, quad radius, keep bound q <= qcut
+//   b = (g1x, g1y, hxy, qcut) second grad row, half2 half extents of the candidate box (bits), keep bound q <= qcut
 //   c = (r, g, b, tau0)      radiance and peak optical depth
 struct __align__(16) SplatRec {
   float4 a, b, c;
@@ -75,9 +75,10 @@ size_t sort_tiles_for(uint32_t n);
 // writes the permutation/values to vals_out.  digit_hist: [passes][256] counts of the digits of every key
 // (pass p = bits 8p .. 8p+7), filled by the producer kernel.  Keys are ping-ponged through scratch.
 // n is the element count, or with n_dev non-null an upper bound and *n_dev (read on the device) the count.
+// keys_out: where the last pass writes the sorted keys (NULL: not written).
 cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals_out, uint32_t n,
                          const uint32_t* n_dev, int bits, const uint32_t* digit_hist, SortScratch& sc,
-                         FrameCounters* ctr, cudaStream_t s);
+                         FrameCounters* ctr, cudaStream_t s, uint16_t* keys_out = nullptr);
 // Counts the digit histograms of u16 keys (used when no producer kernel filled them).
 cudaError_t launch_digit_hist16(const uint16_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s);
 
@@ -91,7 +92,13 @@ cudaError_t launch_tile_counts(const uint32_t* order, const ushort4* rects, uint
                                uint32_t* counts, cudaStream_t s);
 cudaError_t launch_tile_emit(const uint32_t* order, const ushort4* rects, const uint32_t* offsets, uint32_t n,
                              uint32_t tiles_x, uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys,
-                             uint32_t* tile_vals, uint32_t* tile_counts, uint32_t* digit_hist, cudaStream_t s);
+                             uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s);
+// After the tile sort: per tile the run [start, end) of its id in the sorted keys (both zero for an empty tile;
+// the arrays are cleared by the caller), then counts = end - start.
+cudaError_t launch_tile_runs(const uint16_t* sorted_keys, const uint32_t* n_dev, uint32_t n_max, uint32_t* run_start,
+                             uint32_t* run_end, cudaStream_t s);
+cudaError_t launch_tile_run_counts(const uint32_t* run_start, const uint32_t* run_end, uint32_t tiles,
+                                   uint32_t* counts, cudaStream_t s);
 cudaError_t launch_tile_ranges(const uint32_t* tile_starts, const uint32_t* tile_counts, uint32_t tiles,
                                uint2* ranges, cudaStream_t s);
 
@@ -102,7 +109,7 @@ struct CompositeParams {
   float t_stop_scale;   // early termination when T < t_stop_scale / max radiance
 };
 cudaError_t launch_composite(const CompositeParams& P, const uint2* ranges, const uint32_t* tile_vals,
-                             const SplatRec* recs, const FrameCounters* ctr, float4* out, uint32_t* counts,
+                             const SplatRec* recs, FrameCounters* ctr, float4* out, uint32_t* counts,
                              cudaStream_t s);
 
 }  // namespace sl

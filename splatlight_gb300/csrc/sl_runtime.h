@@ -45,7 +45,7 @@ struct ViewBuffers {
   DevBuf key16, recs, rects, order, slot_counts, slot_offsets;  // per slot
   DevBuf keys_alt, vals_alt, status, tile_ctr;                 // sort scratch (max of slots, entries)
   DevBuf tile_keys, tile_vals;                                 // per entry
-  DevBuf tile_counts, tile_starts, ranges;                     // per tile
+  DevBuf tile_counts, tile_starts, ranges, run_start, run_end; // per tile
   DevBuf digit_hist;                                           // [4][256]: depth-key passes, tile-key passes
   DevBuf scan_scratch;
   DevBuf counters;                                             // FrameCounters

@@ -217,7 +217,7 @@ cudaError_t launch_digit_hist16(const uint16_t* keys, uint32_t n, int passes, ui
 
 cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals_out, uint32_t n,
                          const uint32_t* n_dev, int bits, const uint32_t* digit_hist, SortScratch& sc,
-                         FrameCounters* ctr, cudaStream_t s) {
+                         FrameCounters* ctr, cudaStream_t s, uint16_t* keys_out) {
   if (n == 0) return cudaSuccess;
   if (n > kValueMask) return cudaErrorInvalidValue;
   const uint32_t tiles = (uint32_t)sort_tiles_for(n);
@@ -229,17 +229,20 @@ cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals
   if (e != cudaSuccess) return e;
   if (passes == 1) {
     uint32_t* out = (vals_in == vals_out) ? sc.vals_alt : vals_out;
-    onesweep_pass<<<tiles, kThreads, 0, s>>>(keys, vals_in, nullptr, out, n, n_dev, 0, digit_hist, sc.status,
+    uint16_t* kout = (keys_out == keys) ? sc.keys_alt : keys_out;
+    onesweep_pass<<<tiles, kThreads, 0, s>>>(keys, vals_in, kout, out, n, n_dev, 0, digit_hist, sc.status,
                                              sc.tile_ctr, ctr);
     e = cudaGetLastError();
     if (e == cudaSuccess && out != vals_out)
       e = cudaMemcpyAsync(vals_out, out, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && kout && kout != keys_out)
+      e = cudaMemcpyAsync(keys_out, kout, sizeof(uint16_t) * n, cudaMemcpyDeviceToDevice, s);
     return e;
   }
   onesweep_pass<<<tiles, kThreads, 0, s>>>(keys, vals_in, sc.keys_alt, sc.vals_alt, n, n_dev, 0, digit_hist,
                                            sc.status, sc.tile_ctr, ctr);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  onesweep_pass<<<tiles, kThreads, 0, s>>>(sc.keys_alt, sc.vals_alt, nullptr, vals_out, n, n_dev, 8,
+  onesweep_pass<<<tiles, kThreads, 0, s>>>(sc.keys_alt, sc.vals_alt, keys_out, vals_out, n, n_dev, 8,
                                            digit_hist + 256, sc.status + (size_t)256u * tiles, sc.tile_ctr + 1, ctr);
   return cudaGetLastError();
 }

@@ -1,6 +1,7 @@
 // Per-tile splat lists.  After the depth sort, every visible splat (in back-to-front order) is expanded into one
 // (tile, slot) entry per screen tile its candidate rectangle overlaps; a stable radix sort by tile id then leaves each
-// tile's splats contiguous and still in depth order, and the per-tile entry counts give the ranges.  This replaces the
+// tile's splats contiguous and still in depth order, and the runs of equal ids in the sorted keys give the ranges
+// (no per-entry global atomics: only the sort's digit histograms are counted, in shared memory).  This replaces the
 // reference's fixed-function path (one instanced quad per sorted splat, shaders/splat.wgsl:51-55, src/renderer.js:
 // 474-485): the ranges are the rasteriser's coverage made explicit per tile.
 #include "sl_internal.h"
@@ -29,7 +30,6 @@ __global__ void __launch_bounds__(kThreads) tile_emit_kernel(const uint32_t* __r
                                                              uint32_t tiles_x, uint32_t capacity, FrameCounters* ctr,
                                                              uint16_t* __restrict__ tile_keys,
                                                              uint32_t* __restrict__ tile_vals,
-                                                             uint32_t* __restrict__ tile_counts,
                                                              uint32_t* __restrict__ digit_hist) {
   __shared__ uint32_t h_lo[256], h_hi[256];
   const int t = threadIdx.x;
@@ -48,14 +48,20 @@ __global__ void __launch_bounds__(kThreads) tile_emit_kernel(const uint32_t* __r
         atomicExch(&ctr->overflow, 1u);
       } else {
         for (uint32_t ty = r.y; ty <= r.w; ty++) {
+          // one row of tiles: ids are consecutive, so the high digit is shared by most of the row
+          const uint32_t row = ty * tiles_x;
           for (uint32_t tx = r.x; tx <= r.z; tx++) {
-            const uint32_t tile = ty * tiles_x + tx;
+            const uint32_t tile = row + tx;
             tile_keys[e] = (uint16_t)tile;
             tile_vals[e] = slot;
             e++;
             atomicAdd(&h_lo[tile & 0xffu], 1u);
-            atomicAdd(&h_hi[tile >> 8], 1u);
-            atomicAdd(&tile_counts[tile], 1u);
+          }
+          const uint32_t first = row + r.x, last = row + r.z;
+          if ((first >> 8) == (last >> 8)) {
+            atomicAdd(&h_hi[first >> 8], (uint32_t)(r.z - r.x + 1));
+          } else {
+            for (uint32_t tx = r.x; tx <= r.z; tx++) atomicAdd(&h_hi[(row + tx) >> 8], 1u);
           }
         }
       }
@@ -64,6 +70,26 @@ __global__ void __launch_bounds__(kThreads) tile_emit_kernel(const uint32_t* __r
   __syncthreads();
   if (h_lo[t]) atomicAdd(&digit_hist[t], h_lo[t]);
   if (h_hi[t]) atomicAdd(&digit_hist[256 + t], h_hi[t]);
+}
+
+// runs of equal ids in the sorted tile keys: start and end of each tile's run
+__global__ void __launch_bounds__(kThreads) tile_runs_kernel(const uint16_t* __restrict__ keys,
+                                                             const uint32_t* __restrict__ n_dev, uint32_t n_max,
+                                                             uint32_t* __restrict__ run_start,
+                                                             uint32_t* __restrict__ run_end) {
+  const uint32_t nd = *n_dev;
+  const uint32_t n = nd <= n_max ? nd : 0u;  // overflowed frames are re-run by the host
+  for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const uint32_t k = keys[i];
+    if (i == 0 || keys[i - 1] != k) run_start[k] = i;
+    if (i + 1 == n || keys[i + 1] != k) run_end[k] = i + 1;
+  }
+}
+
+__global__ void tile_run_counts_kernel(const uint32_t* __restrict__ run_start, const uint32_t* __restrict__ run_end,
+                                       uint32_t tiles, uint32_t* __restrict__ counts) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < tiles) counts[t] = run_end[t] - run_start[t];
 }
 
 __global__ void tile_ranges_kernel(const uint32_t* __restrict__ starts, const uint32_t* __restrict__ counts,
@@ -83,11 +109,26 @@ cudaError_t launch_tile_counts(const uint32_t* order, const ushort4* rects, uint
 
 cudaError_t launch_tile_emit(const uint32_t* order, const ushort4* rects, const uint32_t* offsets, uint32_t n,
                              uint32_t tiles_x, uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys,
-                             uint32_t* tile_vals, uint32_t* tile_counts, uint32_t* digit_hist, cudaStream_t s) {
+                             uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   tile_emit_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, offsets, n, tiles_x, capacity,
-                                                                       ctr, tile_keys, tile_vals, tile_counts,
-                                                                       digit_hist);
+                                                                       ctr, tile_keys, tile_vals, digit_hist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_runs(const uint16_t* sorted_keys, const uint32_t* n_dev, uint32_t n_max, uint32_t* run_start,
+                             uint32_t* run_end, cudaStream_t s) {
+  if (n_max == 0) return cudaSuccess;
+  uint32_t blocks = (n_max + kThreads * 8 - 1) / (kThreads * 8);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  tile_runs_kernel<<<blocks, kThreads, 0, s>>>(sorted_keys, n_dev, n_max, run_start, run_end);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_run_counts(const uint32_t* run_start, const uint32_t* run_end, uint32_t tiles,
+                                   uint32_t* counts, cudaStream_t s) {
+  if (tiles == 0) return cudaSuccess;
+  tile_run_counts_kernel<<<(tiles + 255) / 256, 256, 0, s>>>(run_start, run_end, tiles, counts);
   return cudaGetLastError();
 }
 

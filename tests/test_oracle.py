@@ -46,7 +46,7 @@ def _dense(spl, order, visible, W, H):
         lx = dx * float(s["g0x"]) + dy * float(s["g0y"])
         ly = dx * float(s["g1x"]) + dy * float(s["g1y"])
         q = lx * lx + ly * ly
-        keep = (np.abs(lx) <= s["r"]) & (np.abs(ly) <= s["r"]) & (q <= s["qcut"])
+        keep = q <= s["qcut"]
         near = np.abs(q - float(s["qcut"])) <= 1e-4 * max(float(s["qcut"]), 1.0)
         q_margin |= near
         cnt += keep
@@ -84,7 +84,7 @@ def test_binning_and_composite_against_dense(orc, which):
             dx, dy = x + 0.5 - s_["cx"], y + 0.5 - s_["cy"]
             lx = dx * s_["g0x"] + dy * s_["g0y"]
             ly = dx * s_["g1x"] + dy * s_["g1y"]
-            if lx * lx + ly * ly < 0.999 * s_["qcut"] and max(abs(lx), abs(ly)) < 0.999 * s_["r"]:
+            if lx * lx + ly * ly < 0.999 * s_["qcut"]:
                 assert int(order[p]) in lst
 
 
