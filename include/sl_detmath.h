@@ -26,8 +26,9 @@
  *        gradual underflow is rounded once, by the final multiply).
  *   log: x = m 2^e with m in [sqrt(1/2), sqrt(2)); ln m = 2 atanh(s), s = (m - 1) / (m + 1), by the odd series
  *        2 (s + s^3/3 + ... + s^15/15); ln x = e ln2_hi + (e ln2_lo + ln m).
- * Accuracy: within 2 ulp of the correctly rounded result over the ranges the pipeline uses (tested against double
- * precision in the unit tests).  sl_expf is used where only a tolerance applies (blending weights in the CPU
+ *   atan/atan2/asin/acos: argument inversion and two angle halvings, then the odd Taylor series (see sl_atanf).
+ * Accuracy: exp/log within 2 ulp of the correctly rounded result over the ranges the pipeline uses, atan family within
+ * a few ulp (tested against double precision in the unit tests).  sl_expf is used where only a tolerance applies (blending weights in the CPU
  * restatement), so that restatement also gives the same bits on x86-64 and aarch64 hosts.
  */
 #ifndef SL_DETMATH_H
@@ -131,5 +132,51 @@ SL_DM_FN float sl_logf(float x) {
   float fe = (float)e;
   return fe * kLn2Hi + (fe * kLn2Lo + lnm);
 }
+
+/* log2(x) = ln(x) / ln 2 (the lighting's mip-level selection). */
+SL_DM_FN float sl_log2f(float x) { return sl_logf(x) * 1.44269504088896341f; }
+
+/* atan(x), fp32, deterministic.  Method: for |x| > 1, atan(x) = sign(x) pi/2 - atan(1/x); then two angle halvings,
+ * atan(t) = 2 atan(t / (1 + sqrt(1 + t^2))), bring |t| below tan(pi/16) = 0.199, where the odd Taylor series of atan
+ * to t^15 is accurate to 1e-13; the result is 4 atan(t') (+ the pi/2 offset). */
+SL_DM_FN float sl_atanf(float x) {
+  if (x != x) return x;
+  const float kHalfPi = 1.57079632679489662f;
+  float ax = x < 0.0f ? -x : x;
+  int inv = ax > 1.0f;
+  float t = inv ? 1.0f / ax : ax;
+  t = t / (1.0f + sqrtf(1.0f + t * t));
+  t = t / (1.0f + sqrtf(1.0f + t * t));
+  float z = t * t;
+  float p = -6.66666666666666667e-02f;           /* -1/15 */
+  p = p * z + 7.69230769230769231e-02f;          /* 1/13 */
+  p = p * z - 9.09090909090909091e-02f;          /* -1/11 */
+  p = p * z + 1.11111111111111111e-01f;          /* 1/9 */
+  p = p * z - 1.42857142857142857e-01f;          /* -1/7 */
+  p = p * z + 2.0e-01f;                          /* 1/5 */
+  p = p * z - 3.33333333333333333e-01f;          /* -1/3 */
+  float a = 4.0f * (t + t * (z * p));
+  if (inv) a = kHalfPi - a;
+  return x < 0.0f ? -a : a;
+}
+
+/* atan2(y, x) with the usual quadrant conventions (atan2(0, 0) = 0). */
+SL_DM_FN float sl_atan2f(float y, float x) {
+  const float kPi = 3.14159265358979324f;
+  const float kHalfPi = 1.57079632679489662f;
+  if (x != x || y != y) return x + y;
+  if (x == 0.0f) {
+    if (y > 0.0f) return kHalfPi;
+    if (y < 0.0f) return -kHalfPi;
+    return 0.0f;
+  }
+  float a = sl_atanf(y / x);
+  if (x > 0.0f) return a;
+  return y >= 0.0f ? a + kPi : a - kPi;
+}
+
+/* asin(x) = atan2(x, sqrt((1 - x)(1 + x))), acos(x) = atan2(sqrt((1 - x)(1 + x)), x), for x in [-1, 1]. */
+SL_DM_FN float sl_asinf(float x) { return sl_atan2f(x, sqrtf((1.0f - x) * (1.0f + x))); }
+SL_DM_FN float sl_acosf(float x) { return sl_atan2f(sqrtf((1.0f - x) * (1.0f + x)), x); }
 
 #endif /* SL_DETMATH_H */

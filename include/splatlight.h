@@ -204,6 +204,55 @@ SL_API int sl_renderer_read_debug(sl_renderer* r, uint32_t* keys, uint32_t* orde
  * back-to-front order) holds stats.entries values; [ranges[2t], ranges[2t+1]) indexes tile t's list. */
 SL_API int sl_renderer_read_entries(sl_renderer* r, uint32_t* entries, uint64_t cap);
 
+/* ---- lighting (src/lighting.js Lighting, src/environment.js Environment) -------------------------------------- */
+
+/* A distant light (the sun) as environment.wgsl's EnvLight (:20-23, written by src/environment.js:111-153). */
+typedef struct sl_env_light {
+  float dir[3];          /* unit direction toward the light, world */
+  float std;             /* angular standard deviation, radians */
+  float irradiance[3];   /* on a plane facing the light */
+  int32_t casts_shadows;
+} sl_env_light;
+
+/* new Lighting(device, sources, asset, gaussBuf, partBuf) (src/lighting.js:318-525): the lighting of a renderer's
+ * scene.  nodes: the asset's leaf nodes (count records, runtime/wgsl/common.wgsl:12-19; pad0 is overwritten by
+ * iso_init); vgrid: one V grid per Gaussian; materials: material_count records (<= 256). */
+SL_API int sl_lighting_create(sl_renderer* r, const sl_node* nodes, const sl_vgrid* vgrid, const sl_material* materials,
+                              uint32_t material_count, sl_lighting** out);
+SL_API int sl_lighting_destroy(sl_lighting* l);
+
+/* setEmitters / setAssetEmitters + writeEmitParams (src/lighting.js:612-721, :657-673): the emissive Gaussians
+ * (world space, albedo = Le) become the light set; the emitter tree is built on the host (buildEmitterTree,
+ * src/lighting.js:99-169), EmitParams.scale = scale, one_sided / normal / skip_part as EmitParams.  The renderer
+ * draws the same records in its emitter slots (its max_emitters permitting).  The light's shadow maps re-splat at
+ * the next update. */
+SL_API int sl_lighting_set_emitters(sl_lighting* l, const sl_gaussian* emitters, uint32_t n, float scale,
+                                    int one_sided, const float* normal, uint32_t skip_part);
+
+/* Environment.set / write (src/environment.js:106-153): up to 4 distant lights; sky_ambient adds albedo * sky_ambient
+ * to every non-emissive Gaussian (a constant stand-in for the probe-bounce sky, which is outside this pipeline). */
+SL_API int sl_lighting_set_environment(sl_lighting* l, const sl_env_light* lights, uint32_t n, float sky_ambient);
+
+/* Resolution of the emitter light's per-part opacity map (src/light_shadow.js:18, default 512) and of the sun's maps
+ * (src/sun_map.js:54, default 512), 0 = no such shadows; light-cut mode (1 cut, 0 every emitter; emissive.wgsl:23),
+ * cut angle theta (EMIT_THETA = 4) and ASG highlights (EmitParams.n5 bit 3, on by default). */
+SL_API int sl_lighting_set_options(sl_lighting* l, uint32_t shadow_res, uint32_t sun_res, uint32_t mode, float theta,
+                                   int asg);
+
+/* encode(encoder, eye, timers, changed, still) (src/lighting.js:1258-1274) + Environment.encodeDirect
+ * (src/environment.js:181-189): iso_init on first use, the opacity maps of moved parts (moved_mask bit p) or of
+ * every part after a light change, then shade_emit + env_direct into the radiance buffer the renderer reads.
+ * forward (may be NULL) centres the sun cascades ahead of the camera.  Stream-ordered. */
+SL_API int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, uint32_t moved_mask,
+                              void* stream);
+
+/* Debug read-back (host buffers, any may be NULL): radiance float4 per Gaussian, the emitter shadow T per Gaussian
+ * (lamp_state slot 0), the distant-light T float4 per Gaussian (env_T), the leaf nodes with iso_norm. */
+SL_API int sl_lighting_read(sl_lighting* l, float* colour, float* lamp_T, float* env_T, sl_node* nodes);
+
+/* bindColour with a Lighting object's radiance buffer (src/renderer.js:264-268). */
+SL_API int sl_renderer_bind_lighting(sl_renderer* r, sl_lighting* l);
+
 /* ---- sort (shaders/radix.wgsl) --------------------------------------------------------------------------------- */
 
 /* The stable sort of 16-bit depth keys on its own (shaders/radix.wgsl:1-139; encoded by src/renderer.js:425-434):

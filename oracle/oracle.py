@@ -26,7 +26,7 @@ def build(force: bool = False) -> Path:
         return LIB
     BUILD.mkdir(exist_ok=True)
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
+    cmd = ["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
            "-I", str(ROOT / "include"), "-I", str(HERE), *map(str, SOURCES), "-o", str(tmp), "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -65,6 +65,9 @@ _EXTRA: dict = {
                                  C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int]),
     "orc_logf_n": (None, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "orc_expf_n": (None, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "orc_atan2f_n": (None, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]),
+    "orc_asinf_n": (None, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "orc_acosf_n": (None, [C.c_void_p, C.c_void_p, C.c_uint64]),
 }
 
 
@@ -146,3 +149,103 @@ def project(gaussians, parts, frame, emitters=None, colour=None, threads: int = 
     vis = lib().orc_project(_p(g), len(g), _p(p), len(p), _p(e), _p(col), None, f.ctypes.data, n, keys.ctypes.data,
                             spl.ctypes.data, threads)
     return keys, spl, int(vis)
+
+
+def atan2f(y: np.ndarray, x: np.ndarray) -> np.ndarray:
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    o = np.empty_like(x)
+    lib().orc_atan2f_n(y.ctypes.data, x.ctypes.data, o.ctypes.data, x.size)
+    return o
+
+
+def asinf(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.empty_like(x)
+    lib().orc_asinf_n(x.ctypes.data, y.ctypes.data, x.size)
+    return y
+
+
+def acosf(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.empty_like(x)
+    lib().orc_acosf_n(x.ctypes.data, y.ctypes.data, x.size)
+    return y
+
+
+class EnvLight(C.Structure):
+    _fields_ = [("dir", C.c_float * 3), ("std", C.c_float), ("irr", C.c_float * 3), ("shadows", C.c_int32)]
+
+
+class LightSetup(C.Structure):
+    _fields_ = [("emit_rec", C.c_void_p), ("n_emit", C.c_uint32), ("scale", C.c_float), ("theta", C.c_float),
+                ("mode", C.c_uint32), ("asg", C.c_uint32), ("one_sided", C.c_uint32), ("normal", C.c_float * 3),
+                ("edge_soft", C.c_float), ("skip_part", C.c_uint32), ("shadow_res", C.c_uint32),
+                ("lights", C.c_void_p), ("n_lights", C.c_uint32), ("sun_res", C.c_uint32),
+                ("sky_ambient", C.c_float), ("eye", C.c_float * 3), ("fwd", C.c_float * 3)]
+
+
+def lighting(scene, eye=None, target=None, threads: int = 8, shadow_res=None, sun_res=None, mode: int = 1,
+             asg: bool = True):
+    """The restated lighting update on a splatlight_gb300.scene.Scene: returns (colour (G, 4), lamp_T (G,),
+    env_T (G, 4), nodes with iso_norm).  Emitters are the scene's host emitter records."""
+    L = lib()
+    L.orc_lighting.restype = C.c_int
+    L.orc_lighting.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                               C.c_uint32, C.POINTER(LightSetup), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+    eye = np.asarray(scene.eye if eye is None else eye, np.float64)
+    tgt = np.asarray(scene.target if target is None else target, np.float64)
+    fwd = (tgt - eye) / np.linalg.norm(tgt - eye)
+    rec = np.ascontiguousarray(scene.emitters).view(np.float32).reshape(-1, 16).copy()
+    lights = (EnvLight * 4)()
+    n_l = 0
+    if scene.sun is not None:
+        lights[0].dir[:] = list(scene.sun.direction)
+        lights[0].std = scene.sun.angular_std
+        lights[0].irr[:] = list(scene.sun.irradiance)
+        lights[0].shadows = 1 if scene.sun.casts_shadows else 0
+        n_l = 1
+    S = LightSetup()
+    S.emit_rec = rec.ctypes.data if len(rec) else None
+    S.n_emit = len(rec)
+    S.scale = 1.0
+    S.theta = 4.0
+    S.mode = mode
+    S.asg = 1 if asg else 0
+    S.one_sided = 0
+    S.normal[:] = [0.0, 0.0, 1.0]
+    S.edge_soft = 0.2
+    S.skip_part = 0xFFFFFFFF
+    S.shadow_res = scene.shadow_res if shadow_res is None else shadow_res
+    S.lights = C.addressof(lights)
+    S.n_lights = n_l
+    S.sun_res = scene.sun_res if sun_res is None else sun_res
+    S.sky_ambient = scene.sky_ambient
+    S.eye[:] = eye.tolist()
+    S.fwd[:] = fwd.tolist()
+    g = np.ascontiguousarray(scene.gaussians)
+    p = np.ascontiguousarray(scene.parts)
+    nodes = np.ascontiguousarray(scene.nodes).copy()
+    vg = np.ascontiguousarray(scene.vgrid)
+    m = np.ascontiguousarray(scene.materials)
+    n = len(g)
+    colour = np.zeros((n, 4), np.float32)
+    lamp_t = np.ones(n, np.float32)
+    env_t = np.ones((n, 4), np.float32)
+    rc = L.orc_lighting(g.ctypes.data, n, p.ctypes.data, len(p), nodes.ctypes.data, vg.ctypes.data, m.ctypes.data,
+                        len(m), C.byref(S), colour.ctypes.data, lamp_t.ctypes.data, env_t.ctypes.data, threads)
+    if rc != 0:
+        raise RuntimeError(f"oracle lighting failed ({rc})")
+    return colour, lamp_t, env_t, nodes
+
+
+def emitter_tree(rec: np.ndarray):
+    """buildEmitterTree restated: (nodes (2n-1, 24) float32, root, root widened covariance)."""
+    L = lib()
+    L.orc_emitter_tree.restype = C.c_uint32
+    L.orc_emitter_tree.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+    r = np.ascontiguousarray(rec, np.float32).reshape(-1, 16)
+    out = np.zeros((2 * len(r) - 1, 24), np.float32)
+    cov = np.zeros(6, np.float32)
+    root = L.orc_emitter_tree(r.ctypes.data, len(r), out.ctypes.data, cov.ctypes.data)
+    return out, int(root), cov

@@ -422,3 +422,12 @@ void orc_logf_n(const float* x, float* y, uint64_t n) {
 void orc_expf_n(const float* x, float* y, uint64_t n) {
   for (uint64_t i = 0; i < n; i++) y[i] = sl_expf(x[i]);
 }
+void orc_atan2f_n(const float* y, const float* x, float* out, uint64_t n) {
+  for (uint64_t i = 0; i < n; i++) out[i] = sl_atan2f(y[i], x[i]);
+}
+void orc_asinf_n(const float* x, float* y, uint64_t n) {
+  for (uint64_t i = 0; i < n; i++) y[i] = sl_asinf(x[i]);
+}
+void orc_acosf_n(const float* x, float* y, uint64_t n) {
+  for (uint64_t i = 0; i < n; i++) y[i] = sl_acosf(x[i]);
+}

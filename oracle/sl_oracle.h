@@ -62,6 +62,9 @@ int64_t orc_render(const sl_gaussian* gaussians, uint32_t count, const sl_part* 
 /* element-wise sl_logf / sl_expf of include/sl_detmath.h (accuracy tests) */
 void orc_logf_n(const float* x, float* y, uint64_t n);
 void orc_expf_n(const float* x, float* y, uint64_t n);
+void orc_atan2f_n(const float* y, const float* x, float* out, uint64_t n);
+void orc_asinf_n(const float* x, float* y, uint64_t n);
+void orc_acosf_n(const float* x, float* y, uint64_t n);
 
 #ifdef __cplusplus
 }

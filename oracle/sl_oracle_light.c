@@ -1,0 +1,1224 @@
+/*
+ * sl_oracle_light.c -- CPU restatement of the per-Gaussian lighting that the splat pipeline composites.  TEST
+ * INFRASTRUCTURE (see sl_oracle.c).  fp32 with -ffp-contract=off; transcendental functions from sl_detmath.h so the
+ * GPU kernels (compiled with --fmad=false and the same functions) can agree to the last bit wherever the operation
+ * order is the same.  Host-side set-up (the emitter tree, the shadow-map frames) is float64, as the reference's JS.
+ *
+ * Follows, per stage:
+ *   iso_init        runtime/wgsl/iso_init.wgsl:29-56 (per-leaf iso_norm into Node.pad0)
+ *   emitter tree    src/lighting.js:99-169 buildEmitterTree (+ EIN3 :55-56, ASG_WIDEN :66), EmitParams :657-673
+ *   light map A     runtime/wgsl/light_shadow.wgsl:69-143, 191-392 (lsm_splat, lsm_resolve, lsm_down, lsm_lookup);
+ *                   host src/light_shadow.js:89-140 (resolution, mip levels, light point and spread)
+ *   sun maps        runtime/wgsl/sun_map.wgsl:91-324; host src/sun_map.js:23-159 (layer plan, cascades, margin)
+ *   shade_emit      runtime/wgsl/emissive.wgsl:123-150, 853-980 (M39 iso transfer, ASG specular on)
+ *   env_direct      runtime/wgsl/environment.wgsl:207-308 (env_add)
+ *   materials       runtime/wgsl/material_ext.wgsl:27-181; common.wgsl:113-254 (erfc, sym_mul, dirm, vgrid, ein,
+ *                   footprint, quat_matrix)
+ * Build-defined (no reference counterpart): a constant sky ambient, colour += albedo * sky_ambient for non-emissive
+ * Gaussians (the reference's sky reaches Gaussians only through the probe bounce, which is outside this pipeline).
+ */
+#define _GNU_SOURCE
+#include "sl_oracle_light.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "sl_detmath.h"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define PI_F 3.14159265358979f
+#define NONE_U32 0xFFFFFFFFu
+
+typedef struct { float x, y, z; } f3;
+typedef struct { float x, y; } f2;
+typedef struct { f3 c[3]; } m3f;   /* columns */
+typedef struct { f2 c[2]; } m2f;   /* columns */
+typedef struct { float x, y, z, w; } f4;
+
+static f3 F3(float x, float y, float z) { f3 r = {x, y, z}; return r; }
+static f2 F2(float x, float y) { f2 r = {x, y}; return r; }
+static f3 add3(f3 a, f3 b) { return F3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static f3 sub3(f3 a, f3 b) { return F3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static f3 mul3(f3 a, float s) { return F3(a.x * s, a.y * s, a.z * s); }
+static f3 mul3v(f3 a, f3 b) { return F3(a.x * b.x, a.y * b.y, a.z * b.z); }
+static f3 div3(f3 a, float s) { return F3(a.x / s, a.y / s, a.z / s); }
+static float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static float len3(f3 a) { return sqrtf(dot3(a, a)); }
+static f3 norm3(f3 a) { return div3(a, len3(a)); }
+static f3 cross3(f3 a, f3 b) { return F3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+static float dot2(f2 a, f2 b) { return a.x * b.x + a.y * b.y; }
+static f2 sub2(f2 a, f2 b) { return F2(a.x - b.x, a.y - b.y); }
+static f2 mul2(f2 a, float s) { return F2(a.x * s, a.y * s); }
+static f2 div2(f2 a, float s) { return F2(a.x / s, a.y / s); }
+static float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+static float mixf(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+static f4 mix4(f4 a, f4 b, float t) {
+  f4 r = {mixf(a.x, b.x, t), mixf(a.y, b.y, t), mixf(a.z, b.z, t), mixf(a.w, b.w, t)};
+  return r;
+}
+static float smoothstepf(float e0, float e1, float x) {
+  float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
+  return t * t * (3.0f - 2.0f * t);
+}
+static f3 m3_mulv(const m3f* m, f3 v) {
+  return F3(m->c[0].x * v.x + m->c[1].x * v.y + m->c[2].x * v.z, m->c[0].y * v.x + m->c[1].y * v.y + m->c[2].y * v.z,
+            m->c[0].z * v.x + m->c[1].z * v.y + m->c[2].z * v.z);
+}
+static m3f m3_mul(const m3f* a, const m3f* b) {
+  m3f r;
+  for (int j = 0; j < 3; j++) r.c[j] = m3_mulv(a, b->c[j]);
+  return r;
+}
+static m3f m3_t(const m3f* a) {
+  m3f r;
+  r.c[0] = F3(a->c[0].x, a->c[1].x, a->c[2].x);
+  r.c[1] = F3(a->c[0].y, a->c[1].y, a->c[2].y);
+  r.c[2] = F3(a->c[0].z, a->c[1].z, a->c[2].z);
+  return r;
+}
+static m3f m3_diag(f3 d) {
+  m3f r;
+  r.c[0] = F3(d.x, 0.0f, 0.0f);
+  r.c[1] = F3(0.0f, d.y, 0.0f);
+  r.c[2] = F3(0.0f, 0.0f, d.z);
+  return r;
+}
+static f2 m2_mulv(const m2f* m, f2 v) { return F2(m->c[0].x * v.x + m->c[1].x * v.y, m->c[0].y * v.x + m->c[1].y * v.y); }
+static m2f m2_mul(const m2f* a, const m2f* b) {
+  m2f r;
+  r.c[0] = m2_mulv(a, b->c[0]);
+  r.c[1] = m2_mulv(a, b->c[1]);
+  return r;
+}
+static m2f m2_t(const m2f* a) {
+  m2f r;
+  r.c[0] = F2(a->c[0].x, a->c[1].x);
+  r.c[1] = F2(a->c[0].y, a->c[1].y);
+  return r;
+}
+static m2f m2_scale(const m2f* a, float s) {
+  m2f r;
+  r.c[0] = mul2(a->c[0], s);
+  r.c[1] = mul2(a->c[1], s);
+  return r;
+}
+static float m2_det(const m2f* m) { return m->c[0].x * m->c[1].y - m->c[1].x * m->c[0].y; }
+/* inv2 (light_shadow.wgsl:98-101) */
+static m2f m2_inv(const m2f* m) {
+  float d = m2_det(m);
+  m2f r;
+  r.c[0] = F2(m->c[1].y, -m->c[0].y);
+  r.c[1] = F2(-m->c[1].x, m->c[0].x);
+  return m2_scale(&r, 1.0f / d);
+}
+static float f16_to_f32(uint32_t h) {
+  uint32_t e = (h >> 10) & 31u, m = h & 1023u;
+  float s = (h & 0x8000u) ? -1.0f : 1.0f;
+  if (e == 0) return s * (float)m * 5.9604644775390625e-08f;
+  if (e == 31) return m ? NAN : s * INFINITY;
+  return s * (1.0f + (float)m / 1024.0f) * sl_bits_to_float((uint32_t)(e - 15 + 127) << 23);
+}
+
+/* ---- runtime/wgsl/common.wgsl helpers ---------------------------------------------------------------------- */
+
+static f3 xf_point(const float* m, f3 p) {
+  return F3(m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3], m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
+            m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11]);
+}
+static f3 xf_dir_inv(const float* m, f3 d) {
+  return add3(add3(mul3(F3(m[0], m[1], m[2]), d.x), mul3(F3(m[4], m[5], m[6]), d.y)), mul3(F3(m[8], m[9], m[10]), d.z));
+}
+/* erfc_pos, Numerical Recipes erfcc (common.wgsl:113-118) */
+static float erfc_pos(float z) {
+  float t = 1.0f / (1.0f + 0.5f * z);
+  float p = -z * z - 1.26551223f +
+            t * (1.00002368f +
+                 t * (0.37409196f +
+                      t * (0.09678418f +
+                           t * (-0.18628806f +
+                                t * (0.27886807f + t * (-1.13520398f + t * (1.48851587f + t * (-0.82215223f + t * 0.17087277f))))))));
+  return t * sl_expf(p);
+}
+static f3 sym_mul(f3 d, f3 o, f3 v) {
+  return F3(d.x * v.x + o.x * v.y + o.y * v.z, o.x * v.x + d.y * v.y + o.z * v.z, o.y * v.x + o.z * v.y + d.z * v.z);
+}
+static f3 nd_cinv_d(const sl_node* n) { return F3(n->cinv_diag[0], n->cinv_diag[1], n->cinv_diag[2]); }
+static f3 nd_cinv_o(const sl_node* n) { return F3(n->cinv_off[0], n->cinv_off[1], n->cinv_off[2]); }
+static f3 nd_sn_d(const sl_node* n) { return F3(n->sn_diag[0], n->sn_diag[1], n->sn_diag[2]); }
+static f3 nd_sn_o(const sl_node* n) { return F3(n->sn_off[0], n->sn_off[1], n->sn_off[2]); }
+static float dirm(const sl_node* n, f3 w) { return sqrtf(fmaxf(dot3(w, sym_mul(nd_sn_d(n), nd_sn_o(n), w)), 0.0f)); }
+static float vgrid_cell(const sl_vgrid* v, uint32_t i, uint32_t j) {
+  uint32_t k = i * 16u + j;
+  return (float)((v->w[k >> 2u] >> ((k & 3u) * 8u)) & 0xFFu) * (1.0f / 255.0f);
+}
+/* vgrid_lookup (common.wgsl:162-177) */
+static float vgrid_lookup(const sl_vgrid* v, f3 w) {
+  float el = sl_asinf(clampf(w.z, -1.0f, 1.0f));
+  float fi = clampf((0.5f * PI_F - el) / (PI_F / 8.0f) - 0.5f, 0.0f, 7.0f);
+  uint32_t i0 = (uint32_t)fi;
+  if (i0 > 6u) i0 = 6u;
+  float ti = fi - (float)i0;
+  float az = (fabsf(w.x) + fabsf(w.y) < 1e-30f) ? 0.0f : sl_atan2f(w.y, w.x);
+  float fj = (az + PI_F) / (2.0f * PI_F) * 16.0f - 0.5f;
+  float j0f = floorf(fj);
+  float tj = fj - j0f;
+  uint32_t j0 = (uint32_t)((int32_t)j0f + 16) % 16u;
+  uint32_t j1 = (j0 + 1u) % 16u;
+  float a = mixf(vgrid_cell(v, i0, j0), vgrid_cell(v, i0, j1), tj);
+  float b = mixf(vgrid_cell(v, i0 + 1u, j0), vgrid_cell(v, i0 + 1u, j1), tj);
+  return mixf(a, b, ti);
+}
+static f3 basis_k(f3 w) {
+  f3 a = F3(0.0f, 0.0f, 1.0f);
+  if (fabsf(w.z) >= 0.999f) a = F3(1.0f, 0.0f, 0.0f);
+  return norm3(cross3(a, w));
+}
+/* quat_matrix (common.wgsl:218-223) */
+static m3f quat_matrix(const float* q) {
+  float x = q[0], y = q[1], z = q[2], w = q[3];
+  m3f m;
+  m.c[0] = F3(1.0f - 2.0f * (y * y + z * z), 2.0f * (x * y + z * w), 2.0f * (x * z - y * w));
+  m.c[1] = F3(2.0f * (x * y - z * w), 1.0f - 2.0f * (x * x + z * z), 2.0f * (y * z + x * w));
+  m.c[2] = F3(2.0f * (x * z + y * w), 2.0f * (y * z - x * w), 1.0f - 2.0f * (x * x + y * y));
+  return m;
+}
+/* ein (common.wgsl:226-239) */
+static float ein(float x) {
+  if (x < 1.0f) {
+    float term = x, s = x;
+    for (int k = 2; k <= 12; k++) {
+      term *= -x / (float)k;
+      s += term / (float)k;
+    }
+    return s;
+  }
+  float p = x * x * x * x + 8.5733287401f * x * x * x + 18.0590169730f * x * x + 8.6347608925f * x + 0.2677737343f;
+  float q = x * x * x * x + 9.5733223454f * x * x * x + 25.6329561486f * x * x + 21.0996530827f * x + 3.9584969228f;
+  return sl_logf(x) + 0.5772156649f + p / q / (x * sl_expf(x));
+}
+/* footprint (common.wgsl:242-246) */
+static float footprint(const sl_node* n, float detC, f3 w) {
+  float a = dot3(w, sym_mul(nd_cinv_d(n), nd_cinv_o(n), w));
+  float K = n->kappa * dirm(n, w) * sqrtf(2.0f * PI_F / a);
+  return 2.0f * PI_F * sqrtf(detC * a) * ein(K);
+}
+static float iso_norm(const sl_node* n) { return sl_bits_to_float(n->pad0); }
+
+/* ---- material_ext.wgsl ------------------------------------------------------------------------------------- */
+
+static float sym_det(f3 d, f3 o) {
+  return d.x * (d.y * d.z - o.z * o.z) - o.x * (o.x * d.z - o.z * o.y) + o.y * (o.x * o.z - d.y * o.y);
+}
+static float sym_adj_quad(f3 d, f3 o, f3 w) {
+  float a00 = d.y * d.z - o.z * o.z, a11 = d.x * d.z - o.y * o.y, a22 = d.x * d.y - o.x * o.x;
+  float a01 = o.y * o.z - o.x * d.z, a02 = o.x * o.z - o.y * d.y, a12 = o.x * o.y - d.x * o.z;
+  return a00 * w.x * w.x + a11 * w.y * w.y + a22 * w.z * w.z + 2.0f * (a01 * w.x * w.y + a02 * w.x * w.z + a12 * w.y * w.z);
+}
+static float phase_specular(f3 Sd, f3 So, f3 wi, f3 wo) {
+  f3 h = add3(wi, wo);
+  float hl = len3(h);
+  if (hl < 1e-6f) return 0.0f;
+  f3 wh = div3(h, hl);
+  float det = fmaxf(sym_det(Sd, So), 1e-20f);
+  float q = sym_adj_quad(Sd, So, wh) / det;
+  float D = 1.0f / (PI_F * sqrtf(det) * q * q);
+  float sigma = sqrtf(fmaxf(dot3(wi, sym_mul(Sd, So, wi)), 1e-12f));
+  return D / (4.0f * sigma);
+}
+static float spec_weight(const sl_material* m) {
+  if ((m->flags & 8u) == 0u || (m->flags & 1u) != 0u) return 0.0f;
+  return clampf(f16_to_f32(m->pad0 & 0xFFFFu), 0.0f, 1.0f);
+}
+static float iso_lobe_from(float k, float p, float damp) { return (1.0f - k) + k * 4.0f * PI_F * p * damp; }
+static float iso_damp(float inorm, float avr) { return fminf(1.0f, 1.0f / fmaxf(4.0f * PI_F * inorm * avr, 1e-30f)); }
+static f3 mirror3(f3 wi, f3 n) { return sub3(mul3(n, 2.0f * dot3(wi, n)), wi); }
+static void onb(f3 n, f3* b0, f3* b1) {
+  float s = n.z >= 0.0f ? 1.0f : -1.0f;
+  float a = -1.0f / (s + n.z);
+  float b = n.x * n.y * a;
+  *b0 = F3(1.0f + s * n.x * n.x * a, s * b, -s * n.x);
+  *b1 = F3(b, s + n.y * n.y * a, -n.y);
+}
+typedef struct { float x, y, z; } s2m; /* symmetric 2x2 (xx, xy, yy) */
+static float s2_det(s2m s) { return s.x * s.z - s.y * s.y; }
+static float s2_quad(s2m s, f2 v) { return s.x * v.x * v.x + 2.0f * s.y * v.x * v.y + s.z * v.y * v.y; }
+static float s2_quad_inv(s2m s, f2 v) {
+  return (s.z * v.x * v.x - 2.0f * s.y * v.x * v.y + s.x * v.y * v.y) / fmaxf(s2_det(s), 1e-30f);
+}
+static s2m s2_xf(s2m s, f2 t0, f2 t1) {
+  f2 a = F2(s.x * t0.x + s.y * t0.y, s.y * t0.x + s.z * t0.y);
+  f2 b = F2(s.x * t1.x + s.y * t1.y, s.y * t1.x + s.z * t1.y);
+  s2m r = {dot2(t0, a), dot2(t0, b), dot2(t1, b)};
+  return r;
+}
+static s2m s2_add(s2m a, s2m b) { s2m r = {a.x + b.x, a.y + b.y, a.z + b.z}; return r; }
+static s2m s2_div(s2m a, float d) { s2m r = {a.x / d, a.y / d, a.z / d}; return r; }
+static f3 s2_major(s2m s) {
+  float h = 0.5f * (s.x - s.z);
+  float lam = 0.5f * (s.x + s.z) + sqrtf(h * h + s.y * s.y);
+  f2 v = s.x >= s.z ? F2(lam - s.z, s.y) : F2(s.y, lam - s.x);
+  float l = sqrtf(dot2(v, v));
+  f2 u = l > 1e-20f ? div2(v, l) : F2(1.0f, 0.0f);
+  return F3(u.x, u.y, lam);
+}
+static float s2_minor(s2m s) {
+  float h = 0.5f * (s.x - s.z);
+  return 0.5f * (s.x + s.z) - sqrtf(h * h + s.y * s.y);
+}
+static f2 log_map(f3 c, f3 cb0, f3 cb1, f3 a) {
+  float ca = clampf(dot3(c, a), -1.0f, 1.0f);
+  f3 v = sub3(a, mul3(c, ca));
+  float nv = len3(v);
+  if (nv < 1e-9f) return F2(0.0f, 0.0f);
+  float k = sl_acosf(ca) / nv;
+  return F2(k * dot3(cb0, v), k * dot3(cb1, v));
+}
+/* asg_phase (material_ext.wgsl:127-181) */
+static float asg_phase(f3 wi, f3 lb0, f3 lb1, s2m sl, f3 n0, f3 t1, f3 t2, f3 flake, f3 Sd, f3 So, f3 wo) {
+  static const float ASG_W[3] = {0.61163f, 0.35083f, 0.0267f};
+  static const float ASG_A[3] = {2.54696f, 0.6893f, 0.10727f};
+  float pc = phase_specular(Sd, So, wi, wo);
+  if (flake.x <= fmaxf(flake.y, flake.z) * 1.0001f) return pc;
+  float co = dot3(n0, wo);
+  f3 n = co >= 0.0f ? n0 : mul3(n0, -1.0f);
+  float cos_o = fabsf(co);
+  f3 wr = sub3(mul3(n, 2.0f * cos_o), wo);
+  f3 rb0, rb1;
+  onb(wr, &rb0, &rb1);
+  f3 dw1 = add3(mul3(n, 2.0f * dot3(wo, t1)), mul3(t1, 2.0f * cos_o));
+  f3 dw2 = add3(mul3(n, 2.0f * dot3(wo, t2)), mul3(t2, 2.0f * cos_o));
+  f2 j0 = F2(dot3(rb0, dw1), dot3(rb0, dw2));
+  f2 j1 = F2(dot3(rb1, dw1), dot3(rb1, dw2));
+  f2 ia = F2(flake.y / (flake.x - flake.y), flake.z / (flake.x - flake.z));
+  s2m s0 = {dot2(F2(j0.x * j0.x, j0.y * j0.y), ia), dot2(F2(j0.x * j1.x, j0.y * j1.y), ia),
+            dot2(F2(j1.x * j1.x, j1.y * j1.y), ia)};
+  float pk = flake.x * flake.x / (PI_F * sqrtf(flake.x * flake.y * flake.z)) /
+             (4.0f * sqrtf(fmaxf(dot3(wr, sym_mul(Sd, So, wr)), 1e-12f)));
+  f3 cs = add3(wi, wr);
+  float cl = len3(cs);
+  if (cl < 1e-4f) return pc;
+  f3 c = div3(cs, cl);
+  f3 cb0, cb1;
+  onb(c, &cb0, &cb1);
+  f2 dm = sub2(log_map(c, cb0, cb1, wr), log_map(c, cb0, cb1, wi));
+  s2m sL = s2_xf(sl, F2(dot3(cb0, lb0), dot3(cb0, lb1)), F2(dot3(cb1, lb0), dot3(cb1, lb1)));
+  s2m sR = s2_xf(s0, F2(dot3(cb0, rb0), dot3(cb0, rb1)), F2(dot3(cb1, rb0), dot3(cb1, rb1)));
+  float ndm = fmaxf(sqrtf(dot2(dm, dm)), 1e-9f);
+  float d = sqrtf(s2_quad_inv(s2_add(sL, s2_div(sR, 2.0f * ASG_A[2])), dm));
+  float along = sqrtf(fmaxf(s2_quad(sL, dm), 0.0f)) / ndm;
+  float far_ = smoothstepf(1.0f, 2.5f, d) * (1.0f - smoothstepf(0.15f, 0.3f, along / ndm));
+  f3 maj = s2_major(sl);
+  float ratio = sqrtf(maj.z / fmaxf(s2_minor(s0) / (2.0f * ASG_A[0]), 1e-30f));
+  float t = fmaxf(far_, 1.0f - smoothstepf(0.12f, 0.3f, ratio));
+  float p_asg = 0.0f;
+  if (t < 1.0f) {
+    for (int k = 0; k < 3; k++) {
+      s2m sk = s2_div(sR, 2.0f * ASG_A[k]);
+      s2m st = s2_add(sL, sk);
+      p_asg += ASG_W[k] * sqrtf(fmaxf(s2_det(sk), 0.0f) / fmaxf(s2_det(st), 1e-30f)) * sl_expf(-0.5f * s2_quad_inv(st, dm));
+    }
+    p_asg *= pk;
+  }
+  float p_pt = pc;
+  if (t > 0.0f) {
+    f3 ax = mul3(add3(mul3(lb0, maj.x), mul3(lb1, maj.y)), sqrtf(3.0f * maj.z));
+    p_pt = (2.0f / 3.0f) * pc + (1.0f / 6.0f) * (phase_specular(Sd, So, norm3(add3(wi, ax)), wo) +
+                                                  phase_specular(Sd, So, norm3(sub3(wi, ax)), wo));
+  }
+  return mixf(p_asg, p_pt, t);
+}
+
+/* ---- iso_init.wgsl ----------------------------------------------------------------------------------------- */
+
+void orc_iso_dirs(float* dirs /* 128 x 4: w.xyz, solid angle */) {
+  for (int c = 0; c < 128; c++) {
+    int i = c / 16, j = c % 16;
+    double el = 0.5 * M_PI - (i + 0.5) * M_PI / 8.0;
+    double az = -M_PI + (j + 0.5) * 2.0 * M_PI / 16.0;
+    double top = 0.5 * M_PI - i * M_PI / 8.0;
+    dirs[4 * c + 0] = (float)(cos(el) * cos(az));
+    dirs[4 * c + 1] = (float)(cos(el) * sin(az));
+    dirs[4 * c + 2] = (float)sin(el);
+    dirs[4 * c + 3] = (float)((2.0 * M_PI / 16.0) * (sin(top) - sin(top - M_PI / 8.0)));
+  }
+}
+
+static void iso_one(uint32_t g, const sl_gaussian* gs, sl_node* nodes, const sl_vgrid* vgrid, const float* dirs) {
+  const sl_gaussian* G = &gs[g];
+  const sl_node* nd = &nodes[g];
+  float s3 = G->scale[0] * G->scale[1] * G->scale[2];
+  float S = 0.0f, S0 = 0.0f;
+  for (uint32_t c = 0; c < 128u; c++) {
+    f3 w = F3(dirs[4 * c], dirs[4 * c + 1], dirs[4 * c + 2]);
+    float om = dirs[4 * c + 3];
+    uint32_t k = c; /* i * 16 + j */
+    float v = (float)((vgrid[g].w[k >> 2u] >> ((k & 3u) * 8u)) & 0xFFu) * (1.0f / 255.0f);
+    float a = footprint(nd, s3 * s3, w) * om;
+    S += a * v;
+    S0 += a;
+  }
+  float n = 1.0f / fmaxf(fmaxf(S, 0.02f * S0), 1e-30f);
+  nodes[g].pad0 = sl_float_to_bits(n);
+  nodes[g].pad1 = 0u;
+}
+
+/* ---- emitter tree (src/lighting.js:99-169) ---------------------------------------------------------------- */
+
+typedef struct {
+  double mu[3], C[6], M[6], Cs[6], mass, Le[3], radius;
+  uint32_t lo, hi;
+} tnode;
+
+static double ein3(void) {
+  double acc = 0.0;
+  for (int i = 0; i < 3000; i++) {
+    double x = (i + 0.5) * 0.001;
+    acc += (1.0 - exp(-x)) / x * 0.001;
+  }
+  return acc;
+}
+static double sdet(const double* m) {
+  double a = m[0], d = m[1], f = m[2], b = m[3], c = m[4], e = m[5];
+  return a * (d * f - e * e) - b * (b * f - e * c) + c * (b * e - d * c);
+}
+static void sinv(const double* m, double* o) {
+  double a = m[0], d = m[1], f = m[2], b = m[3], c = m[4], e = m[5], det = sdet(m);
+  o[0] = (d * f - e * e) / det;
+  o[1] = (a * f - c * c) / det;
+  o[2] = (a * d - b * b) / det;
+  o[3] = (c * e - b * f) / det;
+  o[4] = (b * e - c * d) / det;
+  o[5] = (b * c - a * e) / det;
+}
+static double squad(const double* m, const double* w) {
+  return m[0] * w[0] * w[0] + m[1] * w[1] * w[1] + m[2] * w[2] * w[2] +
+         2 * (m[3] * w[0] * w[1] + m[4] * w[0] * w[2] + m[5] * w[1] * w[2]);
+}
+/* symAxes: Jacobi rotations, 12 sweeps (lighting.js:75-89); axes[k] = eigenvector k */
+static void sym_axes(const double* m, double axes[3][3]) {
+  double A[3][3] = {{m[0], m[3], m[4]}, {m[3], m[1], m[5]}, {m[4], m[5], m[2]}};
+  double V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  static const int PQ[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+  for (int sweep = 0; sweep < 12; sweep++) {
+    for (int r = 0; r < 3; r++) {
+      int p = PQ[r][0], q = PQ[r][1];
+      if (fabs(A[p][q]) < 1e-30) continue;
+      double th = 0.5 * atan2(2 * A[p][q], A[q][q] - A[p][p]);
+      double c = cos(th), s = sin(th);
+      for (int k = 0; k < 3; k++) { double x = A[k][p], y = A[k][q]; A[k][p] = c * x - s * y; A[k][q] = s * x + c * y; }
+      for (int k = 0; k < 3; k++) { double x = A[p][k], y = A[q][k]; A[p][k] = c * x - s * y; A[q][k] = s * x + c * y; }
+      for (int k = 0; k < 3; k++) { double x = V[k][p], y = V[k][q]; V[k][p] = c * x - s * y; V[k][q] = s * x + c * y; }
+    }
+  }
+  for (int k = 0; k < 3; k++)
+    for (int i = 0; i < 3; i++) axes[k][i] = V[i][k];
+}
+static double lum(const double* c) { return 0.2126 * c[0] + 0.7152 * c[1] + 0.0722 * c[2]; }
+
+typedef struct {
+  const float* rec;
+  tnode* info;
+  float* out;   /* 24 floats per node */
+  uint32_t next;
+  double ein3, widen;
+  uint32_t* idx_buf;
+} tbuild;
+
+static uint32_t t_write(tbuild* B, const tnode* nd) {
+  uint32_t id = B->next++;
+  float* f = B->out + 24u * id;
+  uint32_t* u = (uint32_t*)f;
+  f[0] = (float)nd->mu[0]; f[1] = (float)nd->mu[1]; f[2] = (float)nd->mu[2]; f[3] = (float)nd->radius;
+  f[4] = (float)nd->M[0]; f[5] = (float)nd->M[1]; f[6] = (float)nd->M[2]; f[7] = 0.0f;
+  f[8] = (float)nd->M[3]; f[9] = (float)nd->M[4]; f[10] = (float)nd->M[5]; u[11] = nd->lo;
+  f[12] = (float)nd->Le[0]; f[13] = (float)nd->Le[1]; f[14] = (float)nd->Le[2]; u[15] = nd->hi;
+  f[16] = (float)nd->Cs[0]; f[17] = (float)nd->Cs[1]; f[18] = (float)nd->Cs[2]; f[19] = 0.0f;
+  f[20] = (float)nd->Cs[3]; f[21] = (float)nd->Cs[4]; f[22] = (float)nd->Cs[5]; f[23] = 0.0f;
+  B->info[id] = *nd;
+  return id;
+}
+
+static tnode t_leaf(tbuild* B, uint32_t i) {
+  const float* o = B->rec + 16u * i;
+  tnode nd;
+  memset(&nd, 0, sizeof nd);
+  double x = o[4], y = o[5], z = o[6], w = o[7];
+  double R[3][3] = {{1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)},
+                    {2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)},
+                    {2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)}};
+  double s2[3] = {(double)o[8] * o[8], (double)o[9] * o[9], (double)o[10] * o[10]};
+  static const int IJ[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  for (int j = 0; j < 6; j++) {
+    int r = IJ[j][0], k = IJ[j][1];
+    nd.C[j] = R[r][0] * R[k][0] * s2[0] + R[r][1] * R[k][1] * s2[1] + R[r][2] * R[k][2] * s2[2];
+  }
+  double g = pow(2 * M_PI * B->ein3, 2) * sdet(nd.C);
+  double Ci[6];
+  sinv(nd.C, Ci);
+  for (int j = 0; j < 6; j++) nd.M[j] = Ci[j] * g;
+  nd.mass = o[3] * pow(2 * M_PI, 1.5) * sqrt(sdet(nd.C));
+  for (int j = 0; j < 6; j++) nd.Cs[j] = nd.C[j] * B->widen;
+  nd.mu[0] = o[0]; nd.mu[1] = o[1]; nd.mu[2] = o[2];
+  nd.Le[0] = o[12]; nd.Le[1] = o[13]; nd.Le[2] = o[14];
+  double smax = fmax(fmax(o[8], o[9]), o[10]);
+  nd.radius = 3 * smax;
+  nd.lo = NONE_U32;
+  nd.hi = i;
+  return nd;
+}
+
+static const float* g_sort_rec;
+static int g_sort_ax;
+static int cmp_pos(const void* a, const void* b) {
+  uint32_t p = *(const uint32_t*)a, q = *(const uint32_t*)b;
+  double d = (double)g_sort_rec[16u * p + g_sort_ax] - (double)g_sort_rec[16u * q + g_sort_ax];
+  if (d < 0) return -1;
+  if (d > 0) return 1;
+  return p < q ? -1 : (p > q ? 1 : 0);  /* stable: ties keep index order (JS sort is stable) */
+}
+
+static uint32_t t_build(tbuild* B, uint32_t* idx, uint32_t n) {
+  if (n == 1) {
+    tnode l = t_leaf(B, idx[0]);
+    return t_write(B, &l);
+  }
+  double lo[3], hi[3];
+  for (int k = 0; k < 3; k++) { lo[k] = INFINITY; hi[k] = -INFINITY; }
+  for (uint32_t a = 0; a < n; a++)
+    for (int k = 0; k < 3; k++) {
+      double v = B->rec[16u * idx[a] + k];
+      lo[k] = fmin(lo[k], v);
+      hi[k] = fmax(hi[k], v);
+    }
+  int ax = 0;
+  for (int k = 0; k < 3; k++)
+    if (hi[k] - lo[k] > hi[ax] - lo[ax]) ax = k;
+  /* the JS sort compares positions; ties are stable in the order of idx, which is ascending index order here */
+  g_sort_rec = B->rec;
+  g_sort_ax = ax;
+  /* idx arrives in index order at every level only at the root; keep the incoming order for ties instead */
+  uint32_t* tmp = (uint32_t*)malloc(sizeof(uint32_t) * n * 2);
+  for (uint32_t a = 0; a < n; a++) { tmp[2 * a] = idx[a]; tmp[2 * a + 1] = a; }
+  /* insertion sort by (position, incoming rank): stable and deterministic (n <= a few thousand emitters) */
+  for (uint32_t a = 1; a < n; a++) {
+    uint32_t k0 = tmp[2 * a], r0 = tmp[2 * a + 1];
+    double v0 = B->rec[16u * k0 + ax];
+    int64_t b = (int64_t)a - 1;
+    while (b >= 0) {
+      double vb = B->rec[16u * tmp[2 * b] + ax];
+      if (vb > v0) {
+        tmp[2 * (b + 1)] = tmp[2 * b];
+        tmp[2 * (b + 1) + 1] = tmp[2 * b + 1];
+        b--;
+      } else {
+        break;
+      }
+    }
+    tmp[2 * (b + 1)] = k0;
+    tmp[2 * (b + 1) + 1] = r0;
+  }
+  for (uint32_t a = 0; a < n; a++) idx[a] = tmp[2 * a];
+  free(tmp);
+  uint32_t half = n >> 1;
+  uint32_t ia = t_build(B, idx, half);
+  uint32_t ib = t_build(B, idx + half, n - half);
+  const tnode* kids[2] = {&B->info[ia], &B->info[ib]};
+  tnode nd;
+  memset(&nd, 0, sizeof nd);
+  double m = kids[0]->mass + kids[1]->mass;
+  for (int k = 0; k < 3; k++) nd.mu[k] = (kids[0]->mass * kids[0]->mu[k] + kids[1]->mass * kids[1]->mu[k]) / m;
+  static const int IJ[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  for (int j = 0; j < 6; j++) {
+    int r = IJ[j][0], k = IJ[j][1];
+    double acc = 0.0, accs = 0.0;
+    for (int c = 0; c < 2; c++) {
+      acc += kids[c]->mass * (kids[c]->C[j] + (kids[c]->mu[r] - nd.mu[r]) * (kids[c]->mu[k] - nd.mu[k]));
+      accs += kids[c]->mass * (kids[c]->Cs[j] + (kids[c]->mu[r] - nd.mu[r]) * (kids[c]->mu[k] - nd.mu[k]));
+    }
+    nd.C[j] = acc / m;
+    nd.Cs[j] = accs / m;
+  }
+  double axes[3][3];
+  sym_axes(nd.C, axes);
+  double tot[3], num[3] = {0, 0, 0}, den = 0.0;
+  for (int k = 0; k < 3; k++) {
+    tot[k] = 0.0;
+    for (int c = 0; c < 2; c++) tot[k] += lum(kids[c]->Le) * sqrt(fmax(squad(kids[c]->M, axes[k]), 0.0));
+  }
+  for (int c = 0; c < 2; c++) {
+    double sw = 0.0;
+    for (int k = 0; k < 3; k++) sw += sqrt(fmax(squad(kids[c]->M, axes[k]), 0.0));
+    for (int ch = 0; ch < 3; ch++) num[ch] += kids[c]->Le[ch] * sw;
+    den += sw;
+  }
+  for (int ch = 0; ch < 3; ch++) nd.Le[ch] = num[ch] / den;
+  double L = fmax(lum(nd.Le), 1e-12);
+  for (int j = 0; j < 6; j++) nd.M[j] = 0.0;
+  for (int k = 0; k < 3; k++) {
+    double lam = pow(tot[k] / L, 2);
+    for (int j = 0; j < 6; j++) nd.M[j] += lam * axes[k][IJ[j][0]] * axes[k][IJ[j][1]];
+  }
+  double rad = -INFINITY;
+  for (int c = 0; c < 2; c++) {
+    double dx = kids[c]->mu[0] - nd.mu[0], dy = kids[c]->mu[1] - nd.mu[1], dz = kids[c]->mu[2] - nd.mu[2];
+    rad = fmax(rad, sqrt(dx * dx + dy * dy + dz * dz) + kids[c]->radius);
+  }
+  nd.radius = rad;
+  nd.mass = m;
+  nd.lo = ia;
+  nd.hi = ib;
+  return t_write(B, &nd);
+}
+
+uint32_t orc_emitter_tree(const float* rec, uint32_t n, float* nodes_out, float* root_cov) {
+  tbuild B;
+  B.rec = rec;
+  B.info = (tnode*)calloc(2u * n, sizeof(tnode));
+  B.out = nodes_out;
+  B.next = 0;
+  B.ein3 = ein3();
+  B.widen = B.ein3 / (1.0 - exp(-3.0));
+  uint32_t* idx = (uint32_t*)malloc(sizeof(uint32_t) * n);
+  for (uint32_t i = 0; i < n; i++) idx[i] = i;
+  uint32_t root = t_build(&B, idx, n);
+  if (root_cov)
+    for (int j = 0; j < 6; j++) root_cov[j] = (float)B.info[root].Cs[j];
+  free(idx);
+  free(B.info);
+  return root;
+}
+
+/* eig3 closed form (src/light_shadow.js:169-180), ascending */
+static void eig3(const double* m, double* ev) {
+  double a = m[0], d = m[1], f = m[2], b = m[3], c = m[4], e = m[5];
+  double p1 = b * b + c * c + e * e;
+  double q = (a + d + f) / 3;
+  double p2 = (a - q) * (a - q) + (d - q) * (d - q) + (f - q) * (f - q) + 2 * p1;
+  double p = sqrt(p2 / 6);
+  if (p < 1e-30) { ev[0] = ev[1] = ev[2] = q; return; }
+  double B[6] = {(a - q) / p, (d - q) / p, (f - q) / p, b / p, c / p, e / p};
+  double r = (B[0] * (B[1] * B[2] - B[5] * B[5]) - B[3] * (B[3] * B[2] - B[5] * B[4]) + B[4] * (B[3] * B[5] - B[1] * B[4])) / 2;
+  double phi = acos(fmin(1, fmax(-1, r))) / 3;
+  double e1 = q + 2 * p * cos(phi), e3 = q + 2 * p * cos(phi + 2 * M_PI / 3);
+  ev[0] = e3;
+  ev[1] = 3 * q - e1 - e3;
+  ev[2] = e1;
+}
+
+/* ---- opacity maps: shared splat / resolve / mips (light_shadow.wgsl:191-341, sun_map.wgsl:155-277) ------------ */
+
+typedef struct {
+  /* light map A: light frame */
+  f3 center, normal, t1, t2;
+  uint32_t hemi;
+} lframe;
+
+static f2 oct_uv(const lframe* L, f3 w) {
+  f3 l = F3(dot3(w, L->t1), dot3(w, L->t2), dot3(w, L->normal));
+  if (L->hemi) {
+    float z = fmaxf(l.z, 0.0f);
+    f2 p = div2(F2(l.x, l.y), fmaxf(fabsf(l.x) + fabsf(l.y) + z, 1e-12f));
+    return F2(p.x + p.y, p.x - p.y);
+  }
+  f2 p = div2(F2(l.x, l.y), fmaxf(fabsf(l.x) + fabsf(l.y) + fabsf(l.z), 1e-12f));
+  if (l.z < 0.0f) {
+    float sx = p.x >= 0.0f ? 1.0f : -1.0f, sy = p.y >= 0.0f ? 1.0f : -1.0f;
+    p = F2((1.0f - fabsf(p.y)) * sx, (1.0f - fabsf(p.x)) * sy);
+  }
+  return p;
+}
+static m2f oct_jac(const lframe* L, f3 w, f3 b0, f3 b1) {
+  float e = 1e-3f;
+  f2 u0 = oct_uv(L, w);
+  f2 ua = oct_uv(L, norm3(add3(w, mul3(b0, e))));
+  f2 ub = oct_uv(L, norm3(add3(w, mul3(b1, e))));
+  m2f J;
+  J.c[0] = div2(sub2(ua, u0), e);
+  J.c[1] = div2(sub2(ub, u0), e);
+  return J;
+}
+static f3 part_rot_col(const float* xf, int c) { return F3(xf[c], xf[4 + c], xf[8 + c]); }
+/* world covariance R C R^T of a leaf (light_shadow.wgsl:125-137) */
+static m3f leaf_cov_world(const sl_gaussian* G, const float* xf) {
+  m3f R;
+  for (int c = 0; c < 3; c++) R.c[c] = part_rot_col(xf, c);
+  m3f Rq = quat_matrix(G->quat);
+  f3 s2 = F3(G->scale[0] * G->scale[0], G->scale[1] * G->scale[1], G->scale[2] * G->scale[2]);
+  m3f D = m3_diag(s2);
+  m3f t0 = m3_mul(&Rq, &D);
+  m3f RqT = m3_t(&Rq);
+  m3f C = m3_mul(&t0, &RqT);
+  m3f t1 = m3_mul(&R, &C);
+  m3f RT = m3_t(&R);
+  return m3_mul(&t1, &RT);
+}
+
+static void atomic_add_u32(uint32_t* p, uint32_t v) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+  *p += v;
+}
+static uint32_t to_u32(float x) {
+  if (!(x > 0.0f)) return 0u;
+  if (x >= 4294967040.0f) return 0xFFFFFF00u;
+  return (uint32_t)x;
+}
+
+/* splat one leaf into light map A layer p (light_shadow.wgsl:212-286) */
+static void lsm_splat_one(const lframe* L, uint32_t res, uint32_t g, uint32_t p, const sl_gaussian* gs,
+                          const sl_node* nodes, const sl_part* parts, uint32_t* acc) {
+  const float FIX = 65536.0f, LOWPASS = 0.3f;
+  const float* xf = parts[p].xf;
+  const sl_node* nd = &nodes[g];
+  f3 mu = F3(gs[g].mu[0], gs[g].mu[1], gs[g].mu[2]);
+  f3 m = xf_point(xf, mu);
+  f3 dv = sub3(m, L->center);
+  float r = len3(dv);
+  if (r < 1e-4f) return;
+  f3 w = div3(dv, r);
+  m3f C = leaf_cov_world(&gs[g], xf);
+  if (L->hemi && dot3(dv, L->normal) < -3.0f * sqrtf(dot3(L->normal, m3_mulv(&C, L->normal)))) return;
+  f3 b0 = basis_k(w), b1 = cross3(w, b0);
+  f3 c0 = m3_mulv(&C, b0), c1 = m3_mulv(&C, b1);
+  float cbbx = dot3(b0, c0), cbby = dot3(b0, c1), cbbz = dot3(b1, c1);
+  f3 cw = m3_mulv(&C, w);
+  f2 cbz = F2(dot3(b0, cw), dot3(b1, cw));
+  float czz = dot3(w, cw);
+  m2f Cbb;
+  Cbb.c[0] = F2(cbbx, cbby);
+  Cbb.c[1] = F2(cbby, cbbz);
+  m2f Cbb_i = m2_inv(&Cbb);
+  float sz2 = fmaxf(czz - dot2(cbz, m2_mulv(&Cbb_i, cbz)), 1e-12f);
+  float tau0 = nd->kappa * dirm(nd, xf_dir_inv(xf, w)) * sqrtf(2.0f * PI_F * sz2);
+  float half_res = 0.5f * (float)res;
+  m2f J0 = oct_jac(L, w, b0, b1);
+  m2f J = m2_scale(&J0, half_res);
+  m2f Sang = m2_scale(&Cbb, 1.0f / (r * r));
+  m2f t = m2_mul(&J, &Sang);
+  m2f JT = m2_t(&J);
+  m2f S = m2_mul(&t, &JT);
+  float det0 = m2_det(&S);
+  S.c[0].x += LOWPASS;
+  S.c[1].y += LOWPASS;
+  float det1 = m2_det(&S);
+  tau0 *= sqrtf(fmaxf(det0, 0.0f) / det1);
+  m2f Si = m2_inv(&S);
+  m2f Ji = m2_inv(&J);
+  m2f JiT = m2_t(&Ji);
+  f2 gz = m2_mulv(&JiT, mul2(m2_mulv(&Cbb_i, cbz), r));
+  f2 uv = oct_uv(L, w);
+  f2 ct = F2((uv.x * 0.5f + 0.5f) * (float)res, (uv.y * 0.5f + 0.5f) * (float)res);
+  int hx = (int)ceilf(3.0f * sqrtf(S.c[0].x)), hy = (int)ceilf(3.0f * sqrtf(S.c[1].y));
+  if (hx > 48) hx = 48;
+  if (hy > 48) hy = 48;
+  int cx = (int)floorf(ct.x), cy = (int)floorf(ct.y);
+  uint32_t base = p * res * res;
+  int ires = (int)res;
+  for (int y = cy - hy > 0 ? cy - hy : 0; y <= (cy + hy < ires - 1 ? cy + hy : ires - 1); y++) {
+    for (int x = cx - hx > 0 ? cx - hx : 0; x <= (cx + hx < ires - 1 ? cx + hx : ires - 1); x++) {
+      f2 dt = sub2(F2((float)x + 0.5f, (float)y + 0.5f), ct);
+      float q = dot2(dt, m2_mulv(&Si, dt));
+      if (q > 9.0f) continue;
+      float tt = fminf(tau0 * sl_expf(-0.5f * q), 64.0f);
+      float t_fix = tt * FIX;
+      if (t_fix < 0.5f) continue;
+      float z = fmaxf(r + dot2(gz, dt), 0.0f);
+      uint32_t k = (base + (uint32_t)y * res + (uint32_t)x) * 3u;
+      atomic_add_u32(&acc[k], to_u32(t_fix + 0.5f));
+      atomic_add_u32(&acc[k + 1], to_u32(t_fix * z + 0.5f));
+      atomic_add_u32(&acc[k + 2], to_u32(t_fix * (z * z + sz2) + 0.5f));
+    }
+  }
+}
+
+static void resolve_layer(const uint32_t* acc, float fix, uint32_t texels, f4* mip0) {
+  for (uint32_t i = 0; i < texels; i++) {
+    float s0 = (float)acc[3 * i] / fix;
+    f4 o = {0, 0, 0, 0};
+    if (s0 > 1e-5f) {
+      float a = 1.0f - sl_expf(-s0);
+      o.x = a;
+      o.y = a * (float)acc[3 * i + 1] / (fix * s0);
+      o.z = a * (float)acc[3 * i + 2] / (fix * s0);
+    }
+    mip0[i] = o;
+  }
+}
+static void mips_layer(f4* layer, const uint32_t* level_off, uint32_t levels, uint32_t res) {
+  for (uint32_t k = 1; k < levels; k++) {
+    uint32_t rk = res >> k, pr = rk * 2;
+    for (uint32_t y = 0; y < rk; y++)
+      for (uint32_t x = 0; x < rk; x++) {
+        const f4* s = layer + level_off[k - 1] + (2 * y) * pr + 2 * x;
+        f4 a = s[0], b = s[1], c = s[pr], d = s[pr + 1];
+        f4 o = {0.25f * (a.x + b.x + c.x + d.x), 0.25f * (a.y + b.y + c.y + d.y), 0.25f * (a.z + b.z + c.z + d.z),
+                0.25f * (a.w + b.w + c.w + d.w)};
+        layer[level_off[k] + y * rk + x] = o;
+      }
+  }
+}
+static f4 mip_at(const f4* layer, const uint32_t* level_off, uint32_t res, uint32_t k, f2 tc) {
+  uint32_t rk = res >> k;
+  if (rk < 1u) rk = 1u;
+  float sc = (float)(1u << k);
+  float cxf = clampf(tc.x / sc - 0.5f, 0.0f, (float)(rk - 1u)), cyf = clampf(tc.y / sc - 0.5f, 0.0f, (float)(rk - 1u));
+  uint32_t i0x = (uint32_t)floorf(cxf), i0y = (uint32_t)floorf(cyf);
+  uint32_t i1x = i0x + 1u < rk - 1u ? i0x + 1u : rk - 1u, i1y = i0y + 1u < rk - 1u ? i0y + 1u : rk - 1u;
+  float fx = cxf - (float)i0x, fy = cyf - (float)i0y;
+  const f4* b = layer + level_off[k];
+  f4 a = mix4(b[i0y * rk + i0x], b[i0y * rk + i1x], fx);
+  f4 c = mix4(b[i1y * rk + i0x], b[i1y * rk + i1x], fx);
+  return mix4(a, c, fy);
+}
+static f4 mip_tri(const f4* layer, const uint32_t* level_off, uint32_t res, uint32_t levels, float l, f2 tc) {
+  float lc = clampf(l, 0.0f, (float)(levels - 1u));
+  uint32_t k0 = (uint32_t)floorf(lc);
+  uint32_t k1 = k0 + 1u < levels - 1u ? k0 + 1u : levels - 1u;
+  return mix4(mip_at(layer, level_off, res, k0, tc), mip_at(layer, level_off, res, k1, tc), lc - (float)k0);
+}
+static float phi_cdf(float x) {
+  float a = fabsf(x) * 0.70710678f;
+  float h = 0.5f * erfc_pos(a);
+  return x >= 0.0f ? 1.0f - h : h;
+}
+
+/* ---- the whole lighting update ------------------------------------------------------------------------------- */
+
+static uint32_t mat_index(const sl_gaussian* G, uint32_t mat_count) {
+  uint32_t m = G->flags & 0xFFFFu, top = (mat_count > 1u ? mat_count : 1u) - 1u;
+  return m < top ? m : top;
+}
+
+int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, uint32_t part_count, sl_node* nodes,
+                 const sl_vgrid* vgrid, const sl_material* mats, uint32_t mat_count, const orc_light_setup* S,
+                 float* colour, float* lamp_T, float* env_T, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  /* iso_init (once per asset) */
+  float dirs[512];
+  orc_iso_dirs(dirs);
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static, 1024)
+#endif
+  for (int64_t g = 0; g < (int64_t)count; g++) iso_one((uint32_t)g, gs, nodes, vgrid, dirs);
+
+  /* emitter tree + params (lighting.js:657-673) */
+  uint32_t n_emit = S->n_emit;
+  float* tree = NULL;
+  uint32_t root = 0;
+  float root_cov[6] = {0, 0, 0, 0, 0, 0};
+  if (n_emit) {
+    tree = (float*)calloc((size_t)(2u * n_emit - 1u) * 24u, sizeof(float));
+    root = orc_emitter_tree(S->emit_rec, n_emit, tree, root_cov);
+  }
+
+  /* light map A (light_shadow.js:89-165): all layers dirty, then the lookup */
+  for (uint32_t g = 0; g < count; g++) lamp_T[g] = 1.0f;
+  if (n_emit && S->shadow_res) {
+    uint32_t res = S->shadow_res, levels = 0, off = 0, level_off[16];
+    for (uint32_t k = res; k >= 1u; k >>= 1) { level_off[levels++] = off; off += k * k; }
+    uint32_t layer_texels = off;
+    lframe L;
+    L.center = F3(tree[24u * root], tree[24u * root + 1], tree[24u * root + 2]);
+    double n[3] = {S->normal[0], S->normal[1], S->normal[2]};
+    double nl = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int k = 0; k < 3; k++) n[k] /= nl;
+    double a[3] = {fabs(n[0]) < 0.9 ? 1.0 : 0.0, fabs(n[0]) < 0.9 ? 0.0 : 1.0, 0.0};
+    double t1[3] = {n[1] * a[2] - n[2] * a[1], n[2] * a[0] - n[0] * a[2], n[0] * a[1] - n[1] * a[0]};
+    double tl = sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+    for (int k = 0; k < 3; k++) t1[k] /= tl;
+    double t2[3] = {n[1] * t1[2] - n[2] * t1[1], n[2] * t1[0] - n[0] * t1[2], n[0] * t1[1] - n[1] * t1[0]};
+    L.normal = F3((float)n[0], (float)n[1], (float)n[2]);
+    L.t1 = F3((float)t1[0], (float)t1[1], (float)t1[2]);
+    L.t2 = F3((float)t2[0], (float)t2[1], (float)t2[2]);
+    L.hemi = S->one_sided ? 1u : 0u;
+    double cd[6] = {root_cov[0], root_cov[1], root_cov[2], root_cov[3], root_cov[4], root_cov[5]};
+    double ev[3];
+    eig3(cd, ev);
+    float sigma_l = (float)sqrt(0.5 * (ev[1] + ev[2]));
+    uint32_t* acc = (uint32_t*)calloc((size_t)part_count * res * res * 3u, sizeof(uint32_t));
+    f4* mip = (f4*)calloc((size_t)part_count * layer_texels, sizeof(f4));
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 256)
+#endif
+    for (int64_t g = 0; g < (int64_t)count; g++) {
+      uint32_t p = gs[g].part_surface & 0xFFFFu;
+      if (p >= part_count || p == S->skip_part) continue;
+      lsm_splat_one(&L, res, (uint32_t)g, p, gs, nodes, parts, acc);
+    }
+    for (uint32_t p = 0; p < part_count; p++) {
+      resolve_layer(acc + (size_t)p * res * res * 3u, 65536.0f, res * res, mip + (size_t)p * layer_texels);
+      mips_layer(mip + (size_t)p * layer_texels, level_off, levels, res);
+    }
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static, 1024)
+#endif
+    for (int64_t gi = 0; gi < (int64_t)count; gi++) {
+      uint32_t g = (uint32_t)gi;
+      const sl_gaussian* G = &gs[g];
+      uint32_t own = G->part_surface & 0xFFFFu;
+      f3 P = xf_point(parts[own].xf, F3(G->mu[0], G->mu[1], G->mu[2]));
+      f3 dv = sub3(P, L.center);
+      float z = len3(dv);
+      if (z < 1e-4f) { lamp_T[g] = 1.0f; continue; }
+      f3 w = div3(dv, z);
+      f3 b0 = basis_k(w), b1 = cross3(w, b0);
+      m2f J = oct_jac(&L, w, b0, b1);
+      float tex_ang = (2.0f / (float)res) / sqrtf(fmaxf(fabsf(m2_det(&J)), 1e-12f));
+      f2 uv = oct_uv(&L, w);
+      f2 tc = F2((uv.x * 0.5f + 0.5f) * (float)res, (uv.y * 0.5f + 0.5f) * (float)res);
+      float T = 1.0f;
+      for (uint32_t p = 0; p < part_count; p++) {
+        if (p == own || p == S->skip_part) continue;
+        const float* bs = parts[p].bound;
+        f3 bc = sub3(xf_point(parts[p].xf, F3(bs[0], bs[1], bs[2])), L.center);
+        float dc = len3(bc);
+        float zn = fmaxf(dc - bs[3], 0.02f);
+        if (z <= zn) continue;
+        float search = 2.0f * sigma_l * (z - zn) / (zn * z);
+        if (dc > bs[3]) {
+          float ang = sl_acosf(clampf(dot3(div3(bc, dc), w), -1.0f, 1.0f));
+          if (ang > sl_asinf(bs[3] / dc) + search + 2.0f * tex_ang) continue;
+        }
+        const f4* layer = mip + (size_t)p * layer_texels;
+        float ls = sl_log2f(fmaxf(2.0f * search / tex_ang, 1.0f));
+        f4 a0 = mip_tri(layer, level_off, res, levels, ceilf(ls), tc);
+        if (a0.x < 1e-4f) continue;
+        float zb = fmaxf(a0.y / a0.x, 0.02f);
+        float pen = sigma_l * fmaxf(z - zb, 0.0f) / (zb * z);
+        f4 s = mip_tri(layer, level_off, res, levels, sl_log2f(fmaxf(2.0f * pen / tex_ang, 1.0f)), tc);
+        if (s.x < 1e-5f) continue;
+        float mu_ = s.y / s.x;
+        float sd = sqrtf(fmaxf(s.z / s.x - mu_ * mu_, 1e-8f));
+        T *= 1.0f - s.x * phi_cdf((z - mu_) / sd);
+      }
+      lamp_T[g] = T;
+    }
+    free(acc);
+    free(mip);
+  }
+
+  /* sun maps (sun_map.js:23-159, sun_map.wgsl) */
+  for (uint32_t g = 0; g < count; g++) env_T[4u * g] = env_T[4u * g + 1] = env_T[4u * g + 2] = env_T[4u * g + 3] = 1.0f;
+  uint32_t K = S->n_lights < 4u ? S->n_lights : 4u;
+  uint32_t Pn = part_count < 32u ? part_count : 32u;
+  if (K && S->sun_res) {
+    /* layer plan: per part with Gaussians, per light: cascades (8 m, 32 m) below 1.5 x the bound for large static
+     * parts, then the fitted map */
+    typedef struct { uint32_t p, k, kind; float c[2], half; } ldesc;
+    ldesc* desc = (ldesc*)calloc((size_t)Pn * K * 3u, sizeof(ldesc));
+    uint32_t nl = 0;
+    double ext = 0.0, sig_max = 0.0;
+    for (uint32_t p = 0; p < Pn; p++) {
+      const float* b = parts[p].bound;
+      ext = fmax(ext, sqrt((double)b[0] * b[0] + (double)b[1] * b[1] + (double)b[2] * b[2]) + b[3]);
+    }
+    for (uint32_t k = 0; k < K; k++) sig_max = fmax(sig_max, S->lights[k].std);
+    float margin = (float)(3.0 * sig_max * 2.0 * ext);
+    static const double CASC[2] = {8.0, 32.0};
+    for (uint32_t p = 0; p < Pn; p++) {
+      if (!(parts[p].g_hi > parts[p].g_lo)) continue;
+      int big = parts[p].bound[3] > CASC[0] && (parts[p].flags & 1u);
+      for (uint32_t k = 0; k < K; k++) {
+        if (big)
+          for (int c = 0; c < 2; c++) {
+            if (!(CASC[c] < parts[p].bound[3] * 1.5)) continue;
+            double L[3] = {S->lights[k].dir[0], S->lights[k].dir[1], S->lights[k].dir[2]};
+            double aa[3] = {0, 0, 1};
+            if (fabs(L[2]) >= 0.999) { aa[0] = 1; aa[2] = 0; }
+            double t1[3] = {aa[1] * L[2] - aa[2] * L[1], aa[2] * L[0] - aa[0] * L[2], aa[0] * L[1] - aa[1] * L[0]};
+            double tn = sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+            for (int q = 0; q < 3; q++) t1[q] /= tn;
+            double t2[3] = {L[1] * t1[2] - L[2] * t1[1], L[2] * t1[0] - L[0] * t1[2], L[0] * t1[1] - L[1] * t1[0]};
+            double h = CASC[c];
+            double at[3] = {S->eye[0] + S->fwd[0] * h * 0.75, S->eye[1] + S->fwd[1] * h * 0.75,
+                            S->eye[2] + S->fwd[2] * h * 0.75};
+            ldesc* d = &desc[nl++];
+            d->p = p;
+            d->k = k;
+            d->kind = 1;
+            d->half = (float)h;
+            d->c[0] = (float)(at[0] * t1[0] + at[1] * t1[1] + at[2] * t1[2]);
+            d->c[1] = (float)(at[0] * t2[0] + at[1] * t2[1] + at[2] * t2[2]);
+          }
+        ldesc* d = &desc[nl++];
+        d->p = p;
+        d->k = k;
+        d->kind = 0;
+      }
+    }
+    uint32_t res = S->sun_res, levels = 0, off = 0, level_off[16];
+    for (uint32_t k = res; k >= 1u; k >>= 1) { level_off[levels++] = off; off += k * k; }
+    uint32_t layer_texels = off;
+    /* sm_frame (sun_map.wgsl:91-107) */
+    typedef struct { f2 c; float half, zref; f3 t1, t2; uint32_t part, light; } slayer;
+    slayer* ly = (slayer*)calloc(nl ? nl : 1, sizeof(slayer));
+    for (uint32_t l = 0; l < nl; l++) {
+      f3 Ld = F3(S->lights[desc[l].k].dir[0], S->lights[desc[l].k].dir[1], S->lights[desc[l].k].dir[2]);
+      f3 t1 = basis_k(Ld), t2 = cross3(Ld, t1);
+      const float* b = parts[desc[l].p].bound;
+      f3 c = xf_point(parts[desc[l].p].xf, F3(b[0], b[1], b[2]));
+      f2 cc = F2(dot3(c, t1), dot3(c, t2));
+      float half = b[3] + margin;
+      if (desc[l].kind == 1u) { cc = F2(desc[l].c[0], desc[l].c[1]); half = desc[l].half; }
+      ly[l].c = cc;
+      ly[l].half = half;
+      ly[l].zref = dot3(c, Ld) + b[3];
+      ly[l].t1 = t1;
+      ly[l].t2 = t2;
+      ly[l].part = desc[l].p;
+      ly[l].light = desc[l].k;
+    }
+    uint32_t* acc = (uint32_t*)calloc((size_t)(nl ? nl : 1) * res * res * 3u, sizeof(uint32_t));
+    f4* mip = (f4*)calloc((size_t)(nl ? nl : 1) * layer_texels, sizeof(f4));
+    const float SM_FIX = 4096.0f, SM_LOWPASS = 0.3f;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 256)
+#endif
+    for (int64_t gi = 0; gi < (int64_t)count; gi++) {
+      uint32_t g = (uint32_t)gi;
+      uint32_t p = gs[g].part_surface & 0xFFFFu;
+      if (p >= Pn) continue;
+      for (uint32_t l = 0; l < nl; l++) {
+        if (ly[l].part != p || !(S->lights[ly[l].light].shadows)) continue;
+        /* sm_splat_one (sun_map.wgsl:155-219) */
+        const float* xf = parts[p].xf;
+        const sl_node* nd = &nodes[g];
+        f3 x = xf_point(xf, F3(gs[g].mu[0], gs[g].mu[1], gs[g].mu[2]));
+        f3 w = F3(S->lights[ly[l].light].dir[0], S->lights[ly[l].light].dir[1], S->lights[ly[l].light].dir[2]);
+        f3 b0 = ly[l].t1, b1 = ly[l].t2;
+        m3f C = leaf_cov_world(&gs[g], xf);
+        f3 c0 = m3_mulv(&C, b0), c1 = m3_mulv(&C, b1), cw = m3_mulv(&C, w);
+        m2f Cbb;
+        Cbb.c[0] = F2(dot3(b0, c0), dot3(b1, c0));
+        Cbb.c[1] = F2(dot3(b0, c1), dot3(b1, c1));
+        f2 cbz = F2(dot3(b0, cw), dot3(b1, cw));
+        m2f Cbb_i = m2_inv(&Cbb);
+        float sz2 = fmaxf(dot3(w, cw) - dot2(cbz, m2_mulv(&Cbb_i, cbz)), 1e-12f);
+        float tex = (float)res / (2.0f * ly[l].half);
+        m2f Sm = m2_scale(&Cbb, tex * tex);
+        float det0 = m2_det(&Sm);
+        Sm.c[0].x += SM_LOWPASS;
+        Sm.c[1].y += SM_LOWPASS;
+        float det1 = m2_det(&Sm);
+        float tau0 = nd->kappa * dirm(nd, xf_dir_inv(xf, w)) * sqrtf(2.0f * PI_F * sz2) * sqrtf(fmaxf(det0, 0.0f) / det1);
+        m2f Si = m2_inv(&Sm);
+        float z0 = ly[l].zref - dot3(x, w);
+        f2 gz = div2(m2_mulv(&Cbb_i, cbz), tex);
+        f2 ct = F2((dot3(x, b0) - ly[l].c.x + ly[l].half) * tex, (dot3(x, b1) - ly[l].c.y + ly[l].half) * tex);
+        int hx = (int)ceilf(3.0f * sqrtf(Sm.c[0].x)), hy = (int)ceilf(3.0f * sqrtf(Sm.c[1].y));
+        if (hx > 32) hx = 32;
+        if (hy > 32) hy = 32;
+        int cx = (int)floorf(ct.x), cy = (int)floorf(ct.y);
+        uint32_t base = l * res * res;
+        int ires = (int)res;
+        for (int y = cy - hy > 0 ? cy - hy : 0; y <= (cy + hy < ires - 1 ? cy + hy : ires - 1); y++) {
+          for (int xx = cx - hx > 0 ? cx - hx : 0; xx <= (cx + hx < ires - 1 ? cx + hx : ires - 1); xx++) {
+            f2 dt = sub2(F2((float)xx + 0.5f, (float)y + 0.5f), ct);
+            float q = dot2(dt, m2_mulv(&Si, dt));
+            if (q > 9.0f) continue;
+            float tt = fminf(tau0 * sl_expf(-0.5f * q), 64.0f);
+            float t_fix = tt * SM_FIX;
+            if (t_fix < 0.5f) continue;
+            float z = fmaxf(z0 - dot2(gz, dt), 0.0f);
+            uint32_t i = (base + (uint32_t)y * res + (uint32_t)xx) * 3u;
+            atomic_add_u32(&acc[i], to_u32(t_fix + 0.5f));
+            atomic_add_u32(&acc[i + 1], to_u32(t_fix * z + 0.5f));
+            atomic_add_u32(&acc[i + 2], to_u32(t_fix * (z * z + sz2) + 0.5f));
+          }
+        }
+      }
+    }
+    for (uint32_t l = 0; l < nl; l++) {
+      resolve_layer(acc + (size_t)l * res * res * 3u, SM_FIX, res * res, mip + (size_t)l * layer_texels);
+      mips_layer(mip + (size_t)l * layer_texels, level_off, levels, res);
+    }
+    /* sm_lookup (sun_map.wgsl:287-324) */
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static, 1024)
+#endif
+    for (int64_t gi = 0; gi < (int64_t)count; gi++) {
+      uint32_t g = (uint32_t)gi;
+      const sl_gaussian* G = &gs[g];
+      uint32_t own = G->part_surface & 0xFFFFu;
+      f3 P = xf_point(parts[own].xf, F3(G->mu[0], G->mu[1], G->mu[2]));
+      float T[4] = {1, 1, 1, 1};
+      uint32_t used = NONE_U32;
+      for (uint32_t l = 0; l < nl; l++) {
+        uint32_t key = ly[l].part * 8u + ly[l].light;
+        if (ly[l].part == own || key == used || !(S->lights[ly[l].light].shadows)) continue;
+        f3 w = F3(S->lights[ly[l].light].dir[0], S->lights[ly[l].light].dir[1], S->lights[ly[l].light].dir[2]);
+        f2 uv = sub2(F2(dot3(P, ly[l].t1), dot3(P, ly[l].t2)), ly[l].c);
+        float inner = (desc[l].kind == 1u ? 0.9f : 1.0f) * ly[l].half;
+        if (fabsf(uv.x) >= inner || fabsf(uv.y) >= inner) continue;
+        used = key;
+        float z = ly[l].zref - dot3(P, w);
+        if (z <= 0.0f) continue;
+        float texel = 2.0f * ly[l].half / (float)res;
+        f2 tc = F2((uv.x + ly[l].half) / texel, (uv.y + ly[l].half) / texel);
+        float sig = S->lights[ly[l].light].std;
+        float search = 2.0f * sig * z;
+        const f4* layer = mip + (size_t)l * layer_texels;
+        f4 a0 = mip_tri(layer, level_off, res, levels, sl_log2f(fmaxf(2.0f * search / texel, 1.0f)), tc);
+        if (a0.x < 1e-4f) continue;
+        float zb = a0.y / a0.x;
+        float pen = sig * fmaxf(z - zb, 0.0f);
+        f4 s = mip_tri(layer, level_off, res, levels, sl_log2f(fmaxf(2.0f * pen / texel, 1.0f)), tc);
+        if (s.x < 1e-5f) continue;
+        float mu_ = s.y / s.x;
+        float sd = sqrtf(fmaxf(s.z / s.x - mu_ * mu_, 1e-8f));
+        T[ly[l].light] *= 1.0f - s.x * phi_cdf((z - mu_) / sd);
+      }
+      for (int k = 0; k < 4; k++) env_T[4u * g + (uint32_t)k] = T[k];
+    }
+    free(acc);
+    free(mip);
+    free(ly);
+    free(desc);
+  }
+
+  /* shade: shade_emit (emissive.wgsl:944-980) + env_direct (environment.wgsl:225-308) + sky ambient */
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static, 512)
+#endif
+  for (int64_t gi = 0; gi < (int64_t)count; gi++) {
+    uint32_t g = (uint32_t)gi;
+    const sl_gaussian* G = &gs[g];
+    const sl_node* nd = &nodes[g];
+    const sl_material* mat = &mats[mat_index(G, mat_count)];
+    const float* xf = parts[G->part_surface & 0xFFFFu].xf;
+    m3f Rq = quat_matrix(G->quat);
+    m3f Dm = m3_diag(F3(mat->flake[0], mat->flake[1], mat->flake[2]));
+    m3f t0 = m3_mul(&Rq, &Dm);
+    m3f RqT = m3_t(&Rq);
+    m3f Sloc = m3_mul(&t0, &RqT);
+    float s3 = G->scale[0] * G->scale[1] * G->scale[2];
+    float detC = s3 * s3;
+    f3 P = xf_point(xf, F3(G->mu[0], G->mu[1], G->mu[2]));
+    f3 n = Rq.c[0], t1 = Rq.c[1], t2 = Rq.c[2];
+    f3 Sd = F3(Sloc.c[0].x, Sloc.c[1].y, Sloc.c[2].z), So = F3(Sloc.c[1].x, Sloc.c[2].x, Sloc.c[2].y);
+    f3 flake = F3(mat->flake[0], mat->flake[1], mat->flake[2]);
+    f3 alb = F3(G->albedo[0], G->albedo[1], G->albedo[2]);
+    float ks = spec_weight(mat);
+    int emissive = (mat->flags & 1u) != 0u;
+    f3 eye = F3(S->eye[0], S->eye[1], S->eye[2]);
+    f3 c = F3(0.0f, 0.0f, 0.0f);
+    if (n_emit || emissive) {
+      f3 wo0 = xf_dir_inv(xf, norm3(sub3(eye, P)));
+      f3 acc = F3(0.0f, 0.0f, 0.0f);
+      if (n_emit) {
+        uint32_t stack[48];
+        uint32_t sp = 1;
+        stack[0] = root;
+        int shape = S->asg && ks > 0.0f;
+        while (sp > 0u) {
+          sp--;
+          const float* e = tree + 24u * stack[sp];
+          uint32_t child_lo = sl_float_to_bits(e[11]), child_hi = sl_float_to_bits(e[15]);
+          f3 emean = F3(e[0], e[1], e[2]);
+          int use;
+          if (child_lo == NONE_U32 || S->mode == 0u) {
+            use = child_lo == NONE_U32;
+          } else {
+            f3 d = sub3(P, emean);
+            use = dot3(d, d) > S->theta * S->theta * e[3] * e[3];
+          }
+          if (!use) {
+            if (sp + 2u <= 48u) { stack[sp] = child_lo; stack[sp + 1u] = child_hi; sp += 2u; }
+            continue;
+          }
+          f3 d = sub3(emean, P);
+          float d2 = dot3(d, d);
+          if (d2 < 1e-8f) continue;
+          f3 ww = div3(d, sqrtf(d2));
+          f3 wi = xf_dir_inv(xf, ww);
+          float vi = vgrid_lookup(&vgrid[g], wi);
+          if (vi <= 1e-7f) continue;
+          float fp = footprint(nd, detC, wi);
+          /* intensity(e, -ww) (emissive.wgsl:123-130): one-sided emitters fade over |cos| < edge_soft */
+          f3 mw = mul3(ww, -1.0f);
+          float s = 1.0f;
+          if (S->one_sided) {
+            f3 nn = F3(S->normal[0], S->normal[1], S->normal[2]);
+            float cs = dot3(mw, nn);
+            s = S->edge_soft > 0.0f ? smoothstepf(-S->edge_soft, S->edge_soft, cs) : (cs > 0.0f ? 1.0f : 0.0f);
+          }
+          float mq = sqrtf(fmaxf(dot3(mw, sym_mul(F3(e[4], e[5], e[6]), F3(e[8], e[9], e[10]), mw)), 0.0f));
+          f3 I = mul3(F3(e[12], e[13], e[14]), s * S->scale * mq);
+          f3 light = mul3(mul3(I, vi), fp / d2 * 1.0f);
+          if (ks <= 0.0f) {
+            acc = add3(acc, light);
+            continue;
+          }
+          f3 wr = mirror3(wi, n);
+          float damp = iso_damp(iso_norm(nd), footprint(nd, detC, wr) * vgrid_lookup(&vgrid[g], wr));
+          if (shape) {
+            f3 bw0, bw1;
+            onb(ww, &bw0, &bw1);
+            f3 cd = F3(e[16], e[17], e[18]), co = F3(e[20], e[21], e[22]);
+            f3 cc0 = sym_mul(cd, co, bw0), cc1 = sym_mul(cd, co, bw1);
+            s2m slm = {dot3(bw0, cc0) / d2, dot3(bw0, cc1) / d2, dot3(bw1, cc1) / d2};
+            f3 lb0 = xf_dir_inv(xf, bw0), lb1 = xf_dir_inv(xf, bw1);
+            float p = asg_phase(wi, lb0, lb1, slm, n, t1, t2, flake, Sd, So, wo0);
+            acc = add3(acc, mul3(light, iso_lobe_from(ks, p, damp)));
+            continue;
+          }
+          float k = ks;
+          float lobe = k <= 0.0f ? 1.0f : iso_lobe_from(k, phase_specular(Sd, So, wi, wo0), damp);
+          acc = add3(acc, mul3(light, lobe));
+        }
+      }
+      float T = lamp_T[g];
+      c = mul3(mul3v(alb, acc), T * iso_norm(nd));
+      if (emissive && ((mat->flags & 4u) == 0u || dot3(wo0, n) > 0.0f)) {
+        c = add3(c, F3(f16_to_f32(mat->pad0 & 0xFFFFu), f16_to_f32(mat->pad0 >> 16), f16_to_f32(mat->pad1 & 0xFFFFu)));
+      }
+    }
+    /* env_direct (environment.wgsl:266-308) */
+    if (K && !emissive) {
+      float inorm = iso_norm(nd);
+      if (ks <= 0.0f) {
+        f3 dc = F3(0.0f, 0.0f, 0.0f);
+        for (uint32_t k = 0; k < K; k++) {
+          f3 wi = xf_dir_inv(xf, F3(S->lights[k].dir[0], S->lights[k].dir[1], S->lights[k].dir[2]));
+          float v = vgrid_lookup(&vgrid[g], wi);
+          if (v <= 1e-7f) continue;
+          dc = add3(dc, mul3(F3(S->lights[k].irr[0], S->lights[k].irr[1], S->lights[k].irr[2]),
+                             env_T[4u * g + k] * v * footprint(nd, detC, wi)));
+        }
+        c = add3(c, mul3(mul3v(alb, dc), inorm));
+      } else {
+        f3 wo = xf_dir_inv(xf, norm3(sub3(eye, P)));
+        f3 diff = F3(0.0f, 0.0f, 0.0f), spec = F3(0.0f, 0.0f, 0.0f);
+        for (uint32_t k = 0; k < K; k++) {
+          f3 wi = xf_dir_inv(xf, F3(S->lights[k].dir[0], S->lights[k].dir[1], S->lights[k].dir[2]));
+          float v = vgrid_lookup(&vgrid[g], wi);
+          if (v <= 1e-7f) continue;
+          f3 light = mul3(F3(S->lights[k].irr[0], S->lights[k].irr[1], S->lights[k].irr[2]),
+                          env_T[4u * g + k] * v * footprint(nd, detC, wi));
+          f3 wr = mirror3(wi, n);
+          float damp = iso_damp(inorm, footprint(nd, detC, wr) * vgrid_lookup(&vgrid[g], wr));
+          float s2 = S->lights[k].std * S->lights[k].std;
+          f3 ob0, ob1;
+          onb(wi, &ob0, &ob1);
+          s2m slm = {s2, 0.0f, s2};
+          float p = asg_phase(wi, ob0, ob1, slm, n, t1, t2, flake, Sd, So, wo);
+          diff = add3(diff, mul3(light, 1.0f - ks));
+          spec = add3(spec, mul3(light, iso_lobe_from(ks, p, damp) - (1.0f - ks)));
+        }
+        c = add3(c, mul3v(mul3(alb, inorm), add3(diff, spec)));
+      }
+    }
+    if (!emissive && S->sky_ambient > 0.0f) c = add3(c, mul3(alb, S->sky_ambient));
+    colour[4u * g] = c.x;
+    colour[4u * g + 1] = c.y;
+    colour[4u * g + 2] = c.z;
+    colour[4u * g + 3] = 1.0f;
+  }
+  free(tree);
+  return 0;
+}

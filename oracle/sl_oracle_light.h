@@ -1,0 +1,61 @@
+/*
+ * sl_oracle_light.h -- CPU restatement of the per-Gaussian lighting (TEST INFRASTRUCTURE; see sl_oracle_light.c).
+ */
+#ifndef SL_ORACLE_LIGHT_H
+#define SL_ORACLE_LIGHT_H
+
+#include <stdint.h>
+
+#include "splatlight.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_env_light {
+  float dir[3];   /* unit direction toward the light (world) */
+  float std;      /* angular standard deviation, radians */
+  float irr[3];   /* irradiance on a plane facing the light */
+  int32_t shadows;
+} orc_env_light;
+
+typedef struct orc_light_setup {
+  /* emissive Gaussian lights: 16 floats per record (a Gaussian in world space, albedo = Le) */
+  const float* emit_rec;
+  uint32_t n_emit;
+  float scale;        /* EmitParams.scale (overlap correction) */
+  float theta;        /* cut rule, EMIT_THETA = 4 */
+  uint32_t mode;      /* 1: light cut, 0: every emitter */
+  uint32_t asg;       /* EmitParams.n5 bit 3: lights as shapes in shiny highlights */
+  uint32_t one_sided; /* emitters emit toward +normal only */
+  float normal[3];
+  float edge_soft;
+  uint32_t skip_part; /* the emitters' own part (0xFFFFFFFF: none) */
+  uint32_t shadow_res;/* light map A resolution per part layer (0: no emitter shadows) */
+  /* distant lights */
+  const orc_env_light* lights;
+  uint32_t n_lights;
+  uint32_t sun_res;   /* sun map resolution (0: no sun shadows) */
+  float sky_ambient;  /* constant ambient (no reference counterpart) */
+  float eye[3];
+  float fwd[3];       /* camera forward, for the sun cascades */
+} orc_light_setup;
+
+/* The 128 iso_init cell directions and solid angles (iso_init.wgsl:39-45), 4 floats each, computed in float64. */
+void orc_iso_dirs(float* dirs);
+
+/* buildEmitterTree (src/lighting.js:99-169): 2n-1 nodes of 24 floats (EmitNode + its ASG covariance, the packing
+ * of packEmitNodes); returns the root index; root_cov: the root's widened covariance (xx yy zz xy xz yz). */
+uint32_t orc_emitter_tree(const float* rec, uint32_t n, float* nodes_out, float* root_cov);
+
+/* The whole lighting update: iso_init into nodes[].pad0, emitter tree, light map A -> lamp_T, sun maps -> env_T,
+ * then shade_emit + env_direct + sky ambient -> colour (float4 per Gaussian). */
+int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, uint32_t part_count, sl_node* nodes,
+                 const sl_vgrid* vgrid, const sl_material* mats, uint32_t mat_count, const orc_light_setup* S,
+                 float* colour, float* lamp_T, float* env_T, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -56,6 +56,14 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_render": (_I, [_P, _P, _P, _I, C.POINTER(RenderStats), _P]),
     "sl_renderer_read_debug": (_I, [_P, _P, _P, _P, _P]),
     "sl_renderer_read_entries": (_I, [_P, _P, _U64]),
+    "sl_lighting_create": (_I, [_P, _P, _P, _P, _U32, C.POINTER(_P)]),
+    "sl_lighting_destroy": (_I, [_P]),
+    "sl_lighting_set_emitters": (_I, [_P, _P, _U32, C.c_float, _I, _P, _U32]),
+    "sl_lighting_set_environment": (_I, [_P, _P, _U32, C.c_float]),
+    "sl_lighting_set_options": (_I, [_P, _U32, _U32, _U32, C.c_float, _I]),
+    "sl_lighting_update": (_I, [_P, _P, _P, _U32, _P]),
+    "sl_lighting_read": (_I, [_P, _P, _P, _P, _P]),
+    "sl_renderer_bind_lighting": (_I, [_P, _P]),
     "sl_sort_keys16": (_I, [_P, _U32, _P, _P]),
     "sl_sort_keys16_noalloc": (_I, [_P, _U32, _P, _P]),
 }

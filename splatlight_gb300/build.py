@@ -20,7 +20,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libsplatlight.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # translation units whose arithmetic is part of the bit-parity contract
-NO_FMAD = {"project.cu"}
+NO_FMAD = {"project.cu", "lighting.cu"}
 
 
 def nvcc() -> str:
@@ -37,6 +37,7 @@ def sources() -> list[Path]:
 def _compile(src: Path) -> Path:
     obj = BUILD / (src.stem + ".o")
     cmd = [nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+           "-Xcompiler", "-ffp-contract=off",
            "-I", str(ROOT / "include"), "-I", str(CSRC), "--expt-relaxed-constexpr", "-c", str(src), "-o", str(obj)]
     if src.name in NO_FMAD:
         cmd.insert(1, "--fmad=false")

@@ -1,0 +1,710 @@
+// C ABI of the lighting (src/lighting.js Lighting, src/light_shadow.js LightShadow, src/sun_map.js SunMap,
+// src/environment.js Environment): the host-side emitter tree, the opacity-map plans, and the per-frame update that
+// launches the lighting kernels of lighting.cu.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "sl_lighting.h"
+#include "sl_runtime.h"
+
+struct sl_lighting {
+  sl_renderer* r = nullptr;
+  int device = 0;
+  uint32_t count = 0, material_count = 0;
+  sl::DevBuf nodes, vgrid, materials, parts, tree, lamp_T, env_T, colour;
+  bool iso_done = false;
+  // emitters (src/lighting.js:612-721, EmitParams :657-673)
+  std::vector<float> rec;
+  uint32_t n_emit = 0, root = 0, one_sided = 0, skip_part = 0xFFFFFFFFu;
+  float scale = 1.0f, normal[3] = {0.0f, 0.0f, 1.0f}, edge_soft = 0.2f;
+  double root_cov[6] = {0, 0, 0, 0, 0, 0};
+  // options
+  uint32_t shadow_res = 512, sun_res = 512, mode = 1;
+  float theta = 4.0f;
+  uint32_t asg = 1;
+  // environment (src/environment.js:111-153)
+  std::vector<sl_env_light> lights;
+  float sky_ambient = 0.0f;
+  // light map A
+  sl::DevBuf lm_acc, lm_mip;
+  sl::LightMapParams LP{};
+  bool lm_dirty = true;
+  // sun maps
+  sl::DevBuf sm_acc, sm_mip, sm_layers, sm_dirty;
+  sl::SunParams SP{};
+  std::vector<sl::SunLayer> layers;
+  std::vector<int> have_center;
+  bool sm_dirty_all = true;
+  bool lamp_filled = false, env_filled = false;
+};
+
+namespace sl {
+namespace {
+
+// ---- emitter tree: src/lighting.js:99-169 buildEmitterTree (float64, as the JS) ---------------------------------
+
+struct TNode {
+  double mu[3], C[6], M[6], Cs[6], mass, Le[3], radius;
+  uint32_t lo, hi;
+};
+
+double ein3() {
+  double acc = 0.0;
+  for (int i = 0; i < 3000; i++) {
+    double x = (i + 0.5) * 0.001;
+    acc += (1.0 - std::exp(-x)) / x * 0.001;
+  }
+  return acc;
+}
+double sym_det(const double* m) {
+  double a = m[0], d = m[1], f = m[2], b = m[3], c = m[4], e = m[5];
+  return a * (d * f - e * e) - b * (b * f - e * c) + c * (b * e - d * c);
+}
+void sym_inv(const double* m, double* o) {
+  double a = m[0], d = m[1], f = m[2], b = m[3], c = m[4], e = m[5], det = sym_det(m);
+  o[0] = (d * f - e * e) / det;
+  o[1] = (a * f - c * c) / det;
+  o[2] = (a * d - b * b) / det;
+  o[3] = (c * e - b * f) / det;
+  o[4] = (b * e - c * d) / det;
+  o[5] = (b * c - a * e) / det;
+}
+double sym_quad(const double* m, const double* w) {
+  return m[0] * w[0] * w[0] + m[1] * w[1] * w[1] + m[2] * w[2] * w[2] +
+         2 * (m[3] * w[0] * w[1] + m[4] * w[0] * w[2] + m[5] * w[1] * w[2]);
+}
+// principal axes by Jacobi rotations, 12 sweeps (lighting.js:75-89)
+void sym_axes(const double* m, double axes[3][3]) {
+  double A[3][3] = {{m[0], m[3], m[4]}, {m[3], m[1], m[5]}, {m[4], m[5], m[2]}};
+  double V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  const int PQ[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+  for (int sweep = 0; sweep < 12; sweep++) {
+    for (auto& pq : PQ) {
+      int p = pq[0], q = pq[1];
+      if (std::fabs(A[p][q]) < 1e-30) continue;
+      double th = 0.5 * std::atan2(2 * A[p][q], A[q][q] - A[p][p]);
+      double c = std::cos(th), s = std::sin(th);
+      for (int k = 0; k < 3; k++) {
+        double x = A[k][p], y = A[k][q];
+        A[k][p] = c * x - s * y;
+        A[k][q] = s * x + c * y;
+      }
+      for (int k = 0; k < 3; k++) {
+        double x = A[p][k], y = A[q][k];
+        A[p][k] = c * x - s * y;
+        A[q][k] = s * x + c * y;
+      }
+      for (int k = 0; k < 3; k++) {
+        double x = V[k][p], y = V[k][q];
+        V[k][p] = c * x - s * y;
+        V[k][q] = s * x + c * y;
+      }
+    }
+  }
+  for (int k = 0; k < 3; k++)
+    for (int i = 0; i < 3; i++) axes[k][i] = V[i][k];
+}
+double lum(const double* c) { return 0.2126 * c[0] + 0.7152 * c[1] + 0.0722 * c[2]; }
+const int kIJ[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+
+struct TreeBuilder {
+  const float* rec;
+  std::vector<TNode> info;
+  std::vector<float> out;  // 24 floats per node (EmitNode + its ASG covariance, lighting.js packEmitNodes)
+  uint32_t next = 0;
+  double e3, widen;
+
+  uint32_t write(const TNode& nd) {
+    uint32_t id = next++;
+    float* f = &out[24u * id];
+    f[0] = (float)nd.mu[0];
+    f[1] = (float)nd.mu[1];
+    f[2] = (float)nd.mu[2];
+    f[3] = (float)nd.radius;
+    f[4] = (float)nd.M[0];
+    f[5] = (float)nd.M[1];
+    f[6] = (float)nd.M[2];
+    f[7] = 0.0f;
+    f[8] = (float)nd.M[3];
+    f[9] = (float)nd.M[4];
+    f[10] = (float)nd.M[5];
+    memcpy(&f[11], &nd.lo, 4);
+    f[12] = (float)nd.Le[0];
+    f[13] = (float)nd.Le[1];
+    f[14] = (float)nd.Le[2];
+    memcpy(&f[15], &nd.hi, 4);
+    f[16] = (float)nd.Cs[0];
+    f[17] = (float)nd.Cs[1];
+    f[18] = (float)nd.Cs[2];
+    f[19] = 0.0f;
+    f[20] = (float)nd.Cs[3];
+    f[21] = (float)nd.Cs[4];
+    f[22] = (float)nd.Cs[5];
+    f[23] = 0.0f;
+    info[id] = nd;
+    return id;
+  }
+
+  TNode leaf(uint32_t i) {
+    const float* o = rec + 16u * i;
+    TNode nd{};
+    double x = o[4], y = o[5], z = o[6], w = o[7];
+    double R[3][3] = {{1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)},
+                      {2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)},
+                      {2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)}};
+    double s2[3] = {(double)o[8] * o[8], (double)o[9] * o[9], (double)o[10] * o[10]};
+    for (int j = 0; j < 6; j++) {
+      int r = kIJ[j][0], k = kIJ[j][1];
+      nd.C[j] = R[r][0] * R[k][0] * s2[0] + R[r][1] * R[k][1] * s2[1] + R[r][2] * R[k][2] * s2[2];
+    }
+    double g = std::pow(2 * M_PI * e3, 2) * sym_det(nd.C);
+    double Ci[6];
+    sym_inv(nd.C, Ci);
+    for (int j = 0; j < 6; j++) nd.M[j] = Ci[j] * g;
+    nd.mass = o[3] * std::pow(2 * M_PI, 1.5) * std::sqrt(sym_det(nd.C));
+    for (int j = 0; j < 6; j++) nd.Cs[j] = nd.C[j] * widen;
+    for (int k = 0; k < 3; k++) {
+      nd.mu[k] = o[k];
+      nd.Le[k] = o[12 + k];
+    }
+    nd.radius = 3 * std::max(std::max((double)o[8], (double)o[9]), (double)o[10]);
+    nd.lo = 0xFFFFFFFFu;
+    nd.hi = i;
+    return nd;
+  }
+
+  uint32_t build(std::vector<uint32_t> idx) {
+    const uint32_t n = (uint32_t)idx.size();
+    if (n == 1) return write(leaf(idx[0]));
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i : idx)
+      for (int k = 0; k < 3; k++) {
+        lo[k] = std::min(lo[k], (double)rec[16u * i + k]);
+        hi[k] = std::max(hi[k], (double)rec[16u * i + k]);
+      }
+    int ax = 0;
+    for (int k = 0; k < 3; k++)
+      if (hi[k] - lo[k] > hi[ax] - lo[ax]) ax = k;
+    // median split on the longest axis; std::stable_sort keeps ties in their incoming order, as JS's stable sort
+    std::stable_sort(idx.begin(), idx.end(), [&](uint32_t p, uint32_t q) {
+      return (double)rec[16u * p + ax] < (double)rec[16u * q + ax];
+    });
+    const uint32_t half = n >> 1;
+    uint32_t ia = build(std::vector<uint32_t>(idx.begin(), idx.begin() + half));
+    uint32_t ib = build(std::vector<uint32_t>(idx.begin() + half, idx.end()));
+    const TNode* kids[2] = {&info[ia], &info[ib]};
+    TNode nd{};
+    double m = kids[0]->mass + kids[1]->mass;
+    for (int k = 0; k < 3; k++) nd.mu[k] = (kids[0]->mass * kids[0]->mu[k] + kids[1]->mass * kids[1]->mu[k]) / m;
+    for (int j = 0; j < 6; j++) {
+      int r = kIJ[j][0], k = kIJ[j][1];
+      double acc = 0.0, accs = 0.0;
+      for (const TNode* ch : kids) {
+        acc += ch->mass * (ch->C[j] + (ch->mu[r] - nd.mu[r]) * (ch->mu[k] - nd.mu[k]));
+        accs += ch->mass * (ch->Cs[j] + (ch->mu[r] - nd.mu[r]) * (ch->mu[k] - nd.mu[k]));
+      }
+      nd.C[j] = acc / m;
+      nd.Cs[j] = accs / m;
+    }
+    double axes[3][3];
+    sym_axes(nd.C, axes);
+    double tot[3], num[3] = {0, 0, 0}, den = 0.0;
+    for (int k = 0; k < 3; k++) {
+      tot[k] = 0.0;
+      for (const TNode* ch : kids) tot[k] += lum(ch->Le) * std::sqrt(std::max(sym_quad(ch->M, axes[k]), 0.0));
+    }
+    for (const TNode* ch : kids) {
+      double sw = 0.0;
+      for (int k = 0; k < 3; k++) sw += std::sqrt(std::max(sym_quad(ch->M, axes[k]), 0.0));
+      for (int c = 0; c < 3; c++) num[c] += ch->Le[c] * sw;
+      den += sw;
+    }
+    for (int c = 0; c < 3; c++) nd.Le[c] = num[c] / den;
+    double L = std::max(lum(nd.Le), 1e-12);
+    for (int k = 0; k < 3; k++) {
+      double lam = std::pow(tot[k] / L, 2);
+      for (int j = 0; j < 6; j++) nd.M[j] += lam * axes[k][kIJ[j][0]] * axes[k][kIJ[j][1]];
+    }
+    double rad = -INFINITY;
+    for (const TNode* ch : kids) {
+      double dx = ch->mu[0] - nd.mu[0], dy = ch->mu[1] - nd.mu[1], dz = ch->mu[2] - nd.mu[2];
+      rad = std::max(rad, std::sqrt(dx * dx + dy * dy + dz * dz) + ch->radius);
+    }
+    nd.radius = rad;
+    nd.mass = m;
+    nd.lo = ia;
+    nd.hi = ib;
+    return write(nd);
+  }
+};
+
+// eigenvalues of a symmetric 3x3, ascending (src/light_shadow.js:169-180)
+void eig3(const double* m, double* ev) {
+  double a = m[0], d = m[1], f = m[2], b = m[3], c = m[4], e = m[5];
+  double p1 = b * b + c * c + e * e;
+  double q = (a + d + f) / 3;
+  double p2 = (a - q) * (a - q) + (d - q) * (d - q) + (f - q) * (f - q) + 2 * p1;
+  double p = std::sqrt(p2 / 6);
+  if (p < 1e-30) {
+    ev[0] = ev[1] = ev[2] = q;
+    return;
+  }
+  double B[6] = {(a - q) / p, (d - q) / p, (f - q) / p, b / p, c / p, e / p};
+  double r = (B[0] * (B[1] * B[2] - B[5] * B[5]) - B[3] * (B[3] * B[2] - B[5] * B[4]) + B[4] * (B[3] * B[5] - B[1] * B[4])) / 2;
+  double phi = std::acos(std::min(1.0, std::max(-1.0, r))) / 3;
+  double e1 = q + 2 * p * std::cos(phi), e3 = q + 2 * p * std::cos(phi + 2 * M_PI / 3);
+  ev[0] = e3;
+  ev[1] = 3 * q - e1 - e3;
+  ev[2] = e1;
+}
+
+// iso_init cell directions and solid angles (iso_init.wgsl:39-45), float64 then rounded
+void iso_dirs(float* d) {
+  for (int c = 0; c < 128; c++) {
+    int i = c / 16, j = c % 16;
+    double el = 0.5 * M_PI - (i + 0.5) * M_PI / 8.0;
+    double az = -M_PI + (j + 0.5) * 2.0 * M_PI / 16.0;
+    double top = 0.5 * M_PI - i * M_PI / 8.0;
+    d[4 * c + 0] = (float)(std::cos(el) * std::cos(az));
+    d[4 * c + 1] = (float)(std::cos(el) * std::sin(az));
+    d[4 * c + 2] = (float)std::sin(el);
+    d[4 * c + 3] = (float)((2.0 * M_PI / 16.0) * (std::sin(top) - std::sin(top - M_PI / 8.0)));
+  }
+}
+
+void levels_for(uint32_t res, uint32_t& levels, uint32_t* level_off, uint32_t& layer_texels) {
+  uint32_t off = 0;
+  levels = 0;
+  for (uint32_t k = res; k >= 1u; k >>= 1) {
+    level_off[levels++] = off;
+    off += k * k;
+  }
+  layer_texels = off;
+}
+
+// basisK of src/sun_map.js:165-169 (float64)
+void basis_k64(const double* w, double* t1) {
+  double a[3] = {0, 0, 1};
+  if (std::fabs(w[2]) >= 0.999) {
+    a[0] = 1;
+    a[2] = 0;
+  }
+  double c[3] = {a[1] * w[2] - a[2] * w[1], a[2] * w[0] - a[0] * w[2], a[0] * w[1] - a[1] * w[0]};
+  double l = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+  for (int k = 0; k < 3; k++) t1[k] = c[k] / l;
+}
+// float32 basis_k / cross of sun_map.wgsl sm_frame (common.wgsl:181-185), with the kernels' rounding order
+void basis_k32(const float* w, float* t1, float* t2) {
+  float a[3] = {0.0f, 0.0f, 1.0f};
+  if (std::fabs(w[2]) >= 0.999f) {
+    a[0] = 1.0f;
+    a[2] = 0.0f;
+  }
+  volatile float c0 = a[1] * w[2] - a[2] * w[1], c1 = a[2] * w[0] - a[0] * w[2], c2 = a[0] * w[1] - a[1] * w[0];
+  volatile float l = std::sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+  t1[0] = c0 / l;
+  t1[1] = c1 / l;
+  t1[2] = c2 / l;
+  t2[0] = w[1] * t1[2] - w[2] * t1[1];
+  t2[1] = w[2] * t1[0] - w[0] * t1[2];
+  t2[2] = w[0] * t1[1] - w[1] * t1[0];
+}
+
+}  // namespace
+}  // namespace sl
+
+using namespace sl;
+
+#define SL_CHECK_CUDA(expr, what)                          \
+  do {                                                     \
+    cudaError_t _e = (expr);                               \
+    if (_e != cudaSuccess) return cuda_fail(_e, what);     \
+  } while (0)
+
+extern "C" {
+
+int sl_lighting_create(sl_renderer* r, const sl_node* nodes, const sl_vgrid* vgrid, const sl_material* materials,
+                       uint32_t material_count, sl_lighting** out) {
+  if (!out) return fail(SL_ERR_INVALID_ARG, "out is null");
+  *out = nullptr;
+  if (!r || !nodes || !vgrid || !materials || material_count == 0 || material_count > 256)
+    return fail(SL_ERR_INVALID_ARG, "bad lighting arguments");
+  cudaSetDevice(r->device);
+  sl_lighting* l = new sl_lighting();
+  l->r = r;
+  l->device = r->device;
+  l->count = r->count;
+  l->material_count = material_count;
+  cudaError_t e = l->nodes.ensure(sizeof(sl_node) * (size_t)r->count);
+  if (e == cudaSuccess) e = cudaMemcpy(l->nodes.ptr, nodes, sizeof(sl_node) * (size_t)r->count, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = l->vgrid.ensure(sizeof(sl_vgrid) * (size_t)r->count);
+  if (e == cudaSuccess) e = cudaMemcpy(l->vgrid.ptr, vgrid, sizeof(sl_vgrid) * (size_t)r->count, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = l->materials.ensure(sizeof(sl_material) * material_count);
+  if (e == cudaSuccess) e = cudaMemcpy(l->materials.ptr, materials, sizeof(sl_material) * material_count, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = l->parts.ensure(sizeof(sl_part) * kMaxParts);
+  if (e == cudaSuccess) e = l->lamp_T.ensure(4ull * r->count);
+  if (e == cudaSuccess) e = l->env_T.ensure(16ull * r->count);
+  if (e == cudaSuccess) e = l->colour.ensure(16ull * r->count);
+  if (e == cudaSuccess) e = l->tree.ensure(4 * 24);
+  if (e != cudaSuccess) {
+    delete l;
+    return cuda_fail(e, "sl_lighting_create");
+  }
+  *out = l;
+  return SL_OK;
+}
+
+int sl_lighting_destroy(sl_lighting* l) {
+  if (!l) return SL_OK;
+  cudaSetDevice(l->device);
+  cudaDeviceSynchronize();
+  if (l->r && l->r->lighting == l) {
+    l->r->lighting = nullptr;
+    l->r->colour = nullptr;
+  }
+  sl::DevBuf* all[] = {&l->nodes, &l->vgrid, &l->materials, &l->parts, &l->tree, &l->lamp_T, &l->env_T, &l->colour,
+                       &l->lm_acc, &l->lm_mip, &l->sm_acc, &l->sm_mip, &l->sm_layers, &l->sm_dirty};
+  for (sl::DevBuf* b : all) b->release();
+  delete l;
+  return SL_OK;
+}
+
+int sl_lighting_set_emitters(sl_lighting* l, const sl_gaussian* emitters, uint32_t n, float scale, int one_sided,
+                             const float* normal, uint32_t skip_part) {
+  if (!l || (n && !emitters)) return fail(SL_ERR_INVALID_ARG, "null argument");
+  if (n > 16384) return fail(SL_ERR_INVALID_ARG, "more than MAX_EMITTERS (16384) emitters");
+  cudaSetDevice(l->device);
+  l->n_emit = n;
+  l->scale = scale;
+  l->one_sided = one_sided ? 1u : 0u;
+  if (normal) {
+    l->normal[0] = normal[0];
+    l->normal[1] = normal[1];
+    l->normal[2] = normal[2];
+  }
+  l->skip_part = skip_part;
+  l->rec.assign(reinterpret_cast<const float*>(emitters), reinterpret_cast<const float*>(emitters) + 16ull * n);
+  if (n) {
+    TreeBuilder B;
+    B.rec = l->rec.data();
+    B.info.resize(2ull * n);
+    B.out.assign(24ull * (2 * n - 1), 0.0f);
+    B.e3 = ein3();
+    B.widen = B.e3 / (1.0 - std::exp(-3.0));
+    std::vector<uint32_t> idx(n);
+    std::iota(idx.begin(), idx.end(), 0u);
+    l->root = B.build(idx);
+    for (int j = 0; j < 6; j++) l->root_cov[j] = (double)(float)B.info[l->root].Cs[j];
+    SL_CHECK_CUDA(l->tree.ensure(B.out.size() * 4), "emitter tree");
+    SL_CHECK_CUDA(cudaMemcpy(l->tree.ptr, B.out.data(), B.out.size() * 4, cudaMemcpyHostToDevice), "emitter tree");
+  }
+  // the renderer draws the same emitters in slots count+1 .. count+n (bindColour's emitterBuf, renderer.js:264-268)
+  if (n <= l->r->max_emitters) {
+    int rc = sl_renderer_set_emitters(l->r, emitters, n);
+    if (rc) return rc;
+  }
+  l->lm_dirty = true;
+  return SL_OK;
+}
+
+int sl_lighting_set_environment(sl_lighting* l, const sl_env_light* lights, uint32_t n, float sky_ambient) {
+  if (!l || (n && !lights)) return fail(SL_ERR_INVALID_ARG, "null argument");
+  if (n > 4) return fail(SL_ERR_INVALID_ARG, "at most 4 distant lights (environment.wgsl Env.lights)");
+  l->lights.assign(lights, lights + n);
+  l->sky_ambient = sky_ambient;
+  l->sm_dirty_all = true;
+  l->have_center.clear();
+  return SL_OK;
+}
+
+int sl_lighting_set_options(sl_lighting* l, uint32_t shadow_res, uint32_t sun_res, uint32_t mode, float theta,
+                            int asg) {
+  if (!l) return fail(SL_ERR_INVALID_ARG, "null lighting");
+  auto pow2 = [](uint32_t x) { return x == 0 || ((x & (x - 1)) == 0 && x >= 64 && x <= 8192); };
+  if (!pow2(shadow_res) || !pow2(sun_res)) return fail(SL_ERR_INVALID_ARG, "map resolutions: 0 or a power of two in [64, 8192]");
+  if (mode > 1) return fail(SL_ERR_INVALID_ARG, "mode must be 0 (every emitter) or 1 (light cut)");
+  l->shadow_res = shadow_res;
+  l->sun_res = sun_res;
+  l->mode = mode;
+  l->theta = theta;
+  l->asg = asg ? 1u : 0u;
+  l->lm_dirty = true;
+  l->sm_dirty_all = true;
+  l->have_center.clear();
+  return SL_OK;
+}
+
+int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, uint32_t moved_mask, void* stream) {
+  if (!l || !eye) return fail(SL_ERR_INVALID_ARG, "null argument");
+  cudaSetDevice(l->device);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  sl_renderer* r = l->r;
+  const uint32_t G = l->count, P = r->part_count;
+  const sl_gaussian* gs = r->gaussians.as<sl_gaussian>();
+  sl_part* parts = l->parts.as<sl_part>();
+  SL_CHECK_CUDA(cudaMemcpyAsync(parts, r->parts.data(), sizeof(sl_part) * P, cudaMemcpyHostToDevice, s), "parts");
+
+  if (!l->iso_done) {  // iso_init: once per asset (lighting.js:529-555)
+    float dirs[512];
+    iso_dirs(dirs);
+    SL_CHECK_CUDA(upload_iso_dirs(dirs, s), "iso directions");
+    SL_CHECK_CUDA(launch_iso(gs, l->nodes.as<sl_node>(), l->vgrid.as<sl_vgrid>(), G, s), "iso_init");
+    l->iso_done = true;
+  }
+
+  // light map A (light_shadow.js:113-165): re-splat every layer when the light changed, else the moved parts'
+  const bool lmap = l->n_emit && l->shadow_res;
+  if (lmap && (l->lm_dirty || moved_mask)) {
+    LightMapParams& L = l->LP;
+    memset(&L, 0, sizeof(L));
+    const float* t = reinterpret_cast<const float*>(l->tree.ptr);
+    std::vector<float> root(24);
+    SL_CHECK_CUDA(cudaMemcpy(root.data(), t + 24u * l->root, 96, cudaMemcpyDeviceToHost), "tree root");
+    L.center[0] = root[0];
+    L.center[1] = root[1];
+    L.center[2] = root[2];
+    double n[3] = {l->normal[0], l->normal[1], l->normal[2]};
+    double nl = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (double& v : n) v /= nl;
+    double a[3] = {std::fabs(n[0]) < 0.9 ? 1.0 : 0.0, std::fabs(n[0]) < 0.9 ? 0.0 : 1.0, 0.0};
+    double t1[3] = {n[1] * a[2] - n[2] * a[1], n[2] * a[0] - n[0] * a[2], n[0] * a[1] - n[1] * a[0]};
+    double tl = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+    for (double& v : t1) v /= tl;
+    double t2[3] = {n[1] * t1[2] - n[2] * t1[1], n[2] * t1[0] - n[0] * t1[2], n[0] * t1[1] - n[1] * t1[0]};
+    for (int k = 0; k < 3; k++) {
+      L.normal[k] = (float)n[k];
+      L.t1[k] = (float)t1[k];
+      L.t2[k] = (float)t2[k];
+    }
+    double ev[3];
+    eig3(l->root_cov, ev);
+    L.sigma_l = (float)std::sqrt(0.5 * (ev[1] + ev[2]));
+    L.hemi = l->one_sided;
+    L.res = l->shadow_res;
+    levels_for(L.res, L.levels, L.level_off, L.layer_texels);
+    L.part_count = P;
+    L.skip_part = l->skip_part;
+    L.dirty = l->lm_dirty ? (P >= 32 ? 0xFFFFFFFFu : ((1u << P) - 1u)) : moved_mask;
+    const size_t acc_layer = 12ull * L.res * L.res;
+    SL_CHECK_CUDA(l->lm_acc.ensure(acc_layer * P), "light map");
+    SL_CHECK_CUDA(l->lm_mip.ensure(16ull * L.layer_texels * P), "light map mips");
+    for (uint32_t p = 0; p < P; p++)
+      if ((L.dirty >> p) & 1u)
+        SL_CHECK_CUDA(cudaMemsetAsync(l->lm_acc.as<char>() + acc_layer * p, 0, acc_layer, s), "clear light map");
+    SL_CHECK_CUDA(launch_lsm_splat(L, gs, l->nodes.as<sl_node>(), parts, G, l->lm_acc.as<uint32_t>(), s), "lsm_splat");
+    SL_CHECK_CUDA(launch_resolve(l->lm_acc.as<uint32_t>(), 65536.0f, L.res * L.res, P, L.layer_texels, nullptr,
+                                 l->lm_mip.as<float4>(), s),
+                  "lsm_resolve");
+    SL_CHECK_CUDA(launch_mips(l->lm_mip.as<float4>(), L.res, L.levels, L.level_off, P, L.layer_texels, nullptr, s),
+                  "lsm_down");
+    SL_CHECK_CUDA(launch_lsm_lookup(L, gs, parts, G, l->lm_mip.as<float4>(), l->lamp_T.as<float>(), s), "lsm_lookup");
+    l->lm_dirty = false;
+    l->lamp_filled = true;
+  } else if (!lmap && !l->lamp_filled) {
+    std::vector<float> ones(G, 1.0f);
+    SL_CHECK_CUDA(cudaMemcpy(l->lamp_T.ptr, ones.data(), 4ull * G, cudaMemcpyHostToDevice), "lamp T");
+    l->lamp_filled = true;
+  }
+
+  // sun maps (sun_map.js:23-159)
+  const uint32_t K = (uint32_t)std::min<size_t>(l->lights.size(), 4);
+  const uint32_t Pn = std::min<uint32_t>(P, 32u);
+  if (K && l->sun_res) {
+    SunParams& SP = l->SP;
+    memset(&SP, 0, sizeof(SP));
+    SP.res = l->sun_res;
+    levels_for(SP.res, SP.levels, SP.level_off, SP.layer_texels);
+    SP.n_parts = Pn;
+    for (uint32_t k = 0; k < K; k++) {
+      for (int c = 0; c < 3; c++) {
+        SP.lights[k].dir[c] = l->lights[k].dir[c];
+        SP.lights[k].irr[c] = l->lights[k].irradiance[c];
+      }
+      SP.lights[k].std = l->lights[k].std;
+      SP.lights[k].shadows = l->lights[k].casts_shadows ? 1u : 0u;
+    }
+    // the layer plan: per part with Gaussians and per light, cascades then the fitted map (sun_map.js:40-52)
+    double ext = 0.0, sig_max = 0.0;
+    for (uint32_t p = 0; p < Pn; p++) {
+      const float* b = r->parts[p].bound;
+      ext = std::max(ext, std::sqrt((double)b[0] * b[0] + (double)b[1] * b[1] + (double)b[2] * b[2]) + b[3]);
+    }
+    for (uint32_t k = 0; k < K; k++) sig_max = std::max(sig_max, (double)l->lights[k].std);
+    const float margin = (float)(3.0 * sig_max * 2.0 * ext);
+    const double kCasc[2] = {8.0, 32.0};
+    std::vector<SunLayer> plan;
+    for (uint32_t p = 0; p < Pn; p++) {
+      SP.part_first[p] = (uint32_t)plan.size();
+      const sl_part& part = r->parts[p];
+      if (part.g_hi > part.g_lo) {
+        const bool big = part.bound[3] > kCasc[0] && (part.flags & 1u);
+        for (uint32_t k = 0; k < K; k++) {
+          float Ld[3] = {l->lights[k].dir[0], l->lights[k].dir[1], l->lights[k].dir[2]};
+          float t1[3], t2[3];
+          basis_k32(Ld, t1, t2);
+          if (big)
+            for (int c = 0; c < 2; c++) {
+              if (!(kCasc[c] < part.bound[3] * 1.5)) continue;
+              double L64[3] = {Ld[0], Ld[1], Ld[2]}, c1[3];
+              basis_k64(L64, c1);
+              double c2[3] = {L64[1] * c1[2] - L64[2] * c1[1], L64[2] * c1[0] - L64[0] * c1[2], L64[0] * c1[1] - L64[1] * c1[0]};
+              double h = kCasc[c];
+              double at[3];
+              for (int q = 0; q < 3; q++) at[q] = (double)eye[q] + (forward ? (double)forward[q] : 0.0) * h * 0.75;
+              SunLayer ly{};
+              ly.c[0] = (float)(at[0] * c1[0] + at[1] * c1[1] + at[2] * c1[2]);
+              ly.c[1] = (float)(at[0] * c2[0] + at[1] * c2[1] + at[2] * c2[2]);
+              ly.half = (float)h;
+              ly.kind = 1;
+              ly.part = p;
+              ly.light = k;
+              plan.push_back(ly);
+            }
+          SunLayer ly{};
+          ly.kind = 0;
+          ly.part = p;
+          ly.light = k;
+          plan.push_back(ly);
+        }
+      }
+      SP.part_layers[p] = (uint32_t)plan.size() - SP.part_first[p];
+    }
+    // sm_frame (sun_map.wgsl:91-107) on the host, in float32 with the kernels' rounding order; dirty flags
+    const size_t nl = plan.size();
+    if (l->layers.size() != nl) {
+      l->layers.assign(nl, SunLayer{});
+      l->have_center.assign(nl, 0);
+      l->sm_dirty_all = true;
+    }
+    bool any = false;
+    for (size_t li = 0; li < nl; li++) {
+      SunLayer& ly = plan[li];
+      const sl_part& part = r->parts[ly.part];
+      float Ld[3] = {l->lights[ly.light].dir[0], l->lights[ly.light].dir[1], l->lights[ly.light].dir[2]};
+      basis_k32(Ld, ly.t1, ly.t2);
+      const float* b = part.bound;
+      const float* xf = part.xf;
+      volatile float cx = xf[0] * b[0] + xf[1] * b[1] + xf[2] * b[2] + xf[3];
+      volatile float cy = xf[4] * b[0] + xf[5] * b[1] + xf[6] * b[2] + xf[7];
+      volatile float cz = xf[8] * b[0] + xf[9] * b[1] + xf[10] * b[2] + xf[11];
+      bool dirty = l->sm_dirty_all || ((moved_mask >> ly.part) & 1u);
+      if (ly.kind == 1u) {
+        const SunLayer& old = l->layers[li];
+        const float h = ly.half;
+        if (l->have_center[li] && !l->sm_dirty_all &&
+            std::hypot((double)ly.c[0] - old.c[0], (double)ly.c[1] - old.c[1]) <= h / 4) {
+          ly.c[0] = old.c[0];
+          ly.c[1] = old.c[1];
+        } else {
+          dirty = true;
+        }
+        l->have_center[li] = 1;
+      } else {
+        volatile float d0 = cx * ly.t1[0] + cy * ly.t1[1] + cz * ly.t1[2];
+        volatile float d1 = cx * ly.t2[0] + cy * ly.t2[1] + cz * ly.t2[2];
+        ly.c[0] = d0;
+        ly.c[1] = d1;
+        ly.half = b[3] + margin;
+      }
+      volatile float zr = cx * Ld[0] + cy * Ld[1] + cz * Ld[2];
+      ly.zref = zr + b[3];
+      ly.dirty = dirty ? 1u : 0u;
+      any = any || dirty;
+    }
+    SP.n_layers = (uint32_t)nl;
+    if (any) {
+      const size_t acc_layer = 12ull * SP.res * SP.res;
+      SL_CHECK_CUDA(l->sm_acc.ensure(acc_layer * std::max<size_t>(nl, 1)), "sun map");
+      SL_CHECK_CUDA(l->sm_mip.ensure(16ull * SP.layer_texels * std::max<size_t>(nl, 1)), "sun map mips");
+      SL_CHECK_CUDA(l->sm_layers.ensure(sizeof(SunLayer) * std::max<size_t>(nl, 1)), "sun layers");
+      SL_CHECK_CUDA(l->sm_dirty.ensure(4 * std::max<size_t>(nl, 1)), "sun dirty");
+      std::vector<uint32_t> dl(nl);
+      for (size_t li = 0; li < nl; li++) {
+        dl[li] = plan[li].dirty;
+        if (plan[li].dirty)
+          SL_CHECK_CUDA(cudaMemsetAsync(l->sm_acc.as<char>() + acc_layer * li, 0, acc_layer, s), "clear sun map");
+      }
+      SL_CHECK_CUDA(cudaMemcpyAsync(l->sm_layers.ptr, plan.data(), sizeof(SunLayer) * nl, cudaMemcpyHostToDevice, s),
+                    "sun layers");
+      SL_CHECK_CUDA(cudaMemcpyAsync(l->sm_dirty.ptr, dl.data(), 4 * nl, cudaMemcpyHostToDevice, s), "sun dirty");
+      SL_CHECK_CUDA(launch_sm_splat(SP, l->sm_layers.as<SunLayer>(), gs, l->nodes.as<sl_node>(), parts, G,
+                                    l->sm_acc.as<uint32_t>(), s),
+                    "sm_splat");
+      SL_CHECK_CUDA(launch_resolve(l->sm_acc.as<uint32_t>(), 4096.0f, SP.res * SP.res, (uint32_t)nl, SP.layer_texels,
+                                   l->sm_dirty.as<uint32_t>(), l->sm_mip.as<float4>(), s),
+                    "sm_resolve");
+      SL_CHECK_CUDA(launch_mips(l->sm_mip.as<float4>(), SP.res, SP.levels, SP.level_off, (uint32_t)nl, SP.layer_texels,
+                                l->sm_dirty.as<uint32_t>(), s),
+                    "sm_down");
+      SL_CHECK_CUDA(launch_sm_lookup(SP, l->sm_layers.as<SunLayer>(), gs, parts, G, l->sm_mip.as<float4>(),
+                                     l->env_T.as<float4>(), s),
+                    "sm_lookup");
+      SL_CHECK_CUDA(cudaStreamSynchronize(s), "sun maps");  // plan/dl host vectors go out of scope
+      l->layers = plan;
+      l->sm_dirty_all = false;
+      l->env_filled = true;
+    }
+  } else if (!l->env_filled) {
+    std::vector<float> ones(4ull * G, 1.0f);
+    SL_CHECK_CUDA(cudaMemcpy(l->env_T.ptr, ones.data(), 16ull * G, cudaMemcpyHostToDevice), "env T");
+    l->env_filled = true;
+  }
+
+  // shade (emissive.wgsl shade_emit + environment.wgsl env_direct + the constant sky ambient)
+  ShadeParams SH;
+  memset(&SH, 0, sizeof(SH));
+  for (int k = 0; k < 3; k++) {
+    SH.eye[k] = eye[k];
+    SH.normal[k] = l->normal[k];
+  }
+  SH.n_emit = l->n_emit;
+  SH.root = l->root;
+  SH.mode = l->mode;
+  SH.asg = l->asg;
+  SH.one_sided = l->one_sided;
+  SH.material_count = l->material_count;
+  SH.scale = l->scale;
+  SH.theta = l->theta;
+  SH.edge_soft = l->edge_soft;
+  SH.sky_ambient = l->sky_ambient;
+  SH.n_lights = K;
+  for (uint32_t k = 0; k < K; k++) {
+    for (int c = 0; c < 3; c++) {
+      SH.lights[k].dir[c] = l->lights[k].dir[c];
+      SH.lights[k].irr[c] = l->lights[k].irradiance[c];
+    }
+    SH.lights[k].std = l->lights[k].std;
+    SH.lights[k].shadows = l->lights[k].casts_shadows ? 1u : 0u;
+  }
+  SL_CHECK_CUDA(launch_shade(SH, gs, l->nodes.as<sl_node>(), l->vgrid.as<sl_vgrid>(), parts, l->materials.as<sl_material>(),
+                             l->tree.as<float>(), l->lamp_T.as<float>(), l->env_T.as<float4>(), l->colour.as<float4>(), G, s),
+                "shade");
+  return SL_OK;
+}
+
+int sl_lighting_read(sl_lighting* l, float* colour, float* lamp_T, float* env_T, sl_node* nodes) {
+  if (!l) return fail(SL_ERR_INVALID_ARG, "null lighting");
+  cudaSetDevice(l->device);
+  SL_CHECK_CUDA(cudaDeviceSynchronize(), "sync");
+  const size_t G = l->count;
+  if (colour) SL_CHECK_CUDA(cudaMemcpy(colour, l->colour.ptr, 16 * G, cudaMemcpyDeviceToHost), "colour");
+  if (lamp_T) SL_CHECK_CUDA(cudaMemcpy(lamp_T, l->lamp_T.ptr, 4 * G, cudaMemcpyDeviceToHost), "lamp T");
+  if (env_T) SL_CHECK_CUDA(cudaMemcpy(env_T, l->env_T.ptr, 16 * G, cudaMemcpyDeviceToHost), "env T");
+  if (nodes) SL_CHECK_CUDA(cudaMemcpy(nodes, l->nodes.ptr, sizeof(sl_node) * G, cudaMemcpyDeviceToHost), "nodes");
+  return SL_OK;
+}
+
+int sl_renderer_bind_lighting(sl_renderer* r, sl_lighting* l) {
+  if (!r || !l) return fail(SL_ERR_INVALID_ARG, "null argument");
+  if (l->r != r) return fail(SL_ERR_INVALID_ARG, "the lighting object belongs to another renderer");
+  r->lighting = l;
+  r->colour = l->colour.as<float4>();
+  r->lo_b = nullptr;
+  return SL_OK;
+}
+
+}  // extern "C"

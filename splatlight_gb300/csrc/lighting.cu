@@ -1,0 +1,591 @@
+// Per-Gaussian lighting kernels: iso_init, the emitter light's per-part opacity map (map A), the sun's orthographic
+// opacity maps, and one fused shade kernel (shade_emit + env_direct + the constant sky ambient) writing the radiance
+// the projection reads.  One thread per Gaussian (or per texel for resolve / mip passes); opacity maps accumulate
+// u32 fixed-point atomics, so their sums do not depend on the order the Gaussians run in.
+//
+//   iso_kernel        runtime/wgsl/iso_init.wgsl:29-56
+//   lsm_splat_kernel  runtime/wgsl/light_shadow.wgsl:191-286     lsm_lookup_kernel  :347-392
+//   sm_splat_kernel   runtime/wgsl/sun_map.wgsl:127-219          sm_lookup_kernel   :287-324
+//   resolve / down    light_shadow.wgsl:290-321, sun_map.wgsl:228-258
+//   shade_kernel      runtime/wgsl/emissive.wgsl:853-980 + environment.wgsl:207-308
+// Compiled with --fmad=false (see light_math.cuh).
+#include "light_math.cuh"
+#include "sl_lighting.h"
+
+namespace sl {
+
+__constant__ float4 c_iso_dirs[128];  // iso_init cell directions (xyz) and solid angles (w)
+
+namespace {
+
+using namespace lm;
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ f3 ld3(const float* p) { return F3(p[0], p[1], p[2]); }
+
+__global__ void __launch_bounds__(kThreads) iso_kernel(const sl_gaussian* __restrict__ gs, sl_node* nodes,
+                                                       const sl_vgrid* __restrict__ vgrid, uint32_t count) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= count) return;
+  const sl_gaussian& G = gs[g];
+  Leaf nd = load_leaf(&nodes[g]);
+  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
+  float S = 0.0f, S0 = 0.0f;
+  const sl_vgrid& vg = vgrid[g];
+  for (uint32_t c = 0; c < 128u; c++) {
+    const float4 d = c_iso_dirs[c];
+    const float v = (float)((vg.w[c >> 2u] >> ((c & 3u) * 8u)) & 0xFFu) * (1.0f / 255.0f);
+    const float a = footprint(nd, s3 * s3, F3(d.x, d.y, d.z)) * d.w;
+    S += a * v;
+    S0 += a;
+  }
+  const float n = 1.0f / fmaxf(fmaxf(S, 0.02f * S0), 1e-30f);
+  nodes[g].pad0 = __float_as_uint(n);
+  nodes[g].pad1 = 0u;
+}
+
+// ---- light map A -----------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ f2 oct_uv(const LightMapParams& L, f3 w) {
+  f3 l = F3(dot3(w, ld3(L.t1)), dot3(w, ld3(L.t2)), dot3(w, ld3(L.normal)));
+  if (L.hemi) {
+    float z = fmaxf(l.z, 0.0f);
+    f2 p = div2(F2(l.x, l.y), fmaxf(fabsf(l.x) + fabsf(l.y) + z, 1e-12f));
+    return F2(p.x + p.y, p.x - p.y);
+  }
+  f2 p = div2(F2(l.x, l.y), fmaxf(fabsf(l.x) + fabsf(l.y) + fabsf(l.z), 1e-12f));
+  if (l.z < 0.0f) {
+    float sx = p.x >= 0.0f ? 1.0f : -1.0f, sy = p.y >= 0.0f ? 1.0f : -1.0f;
+    p = F2((1.0f - fabsf(p.y)) * sx, (1.0f - fabsf(p.x)) * sy);
+  }
+  return p;
+}
+__device__ __forceinline__ m2 oct_jac(const LightMapParams& L, f3 w, f3 b0, f3 b1) {
+  const float e = 1e-3f;
+  f2 u0 = oct_uv(L, w);
+  f2 ua = oct_uv(L, norm3(add3(w, mul3(b0, e))));
+  f2 ub = oct_uv(L, norm3(add3(w, mul3(b1, e))));
+  m2 J;
+  J.c[0] = div2(sub2(ua, u0), e);
+  J.c[1] = div2(sub2(ub, u0), e);
+  return J;
+}
+// world covariance R (Rq S^2 Rq^T) R^T of a leaf (light_shadow.wgsl:125-137)
+__device__ __forceinline__ m3 leaf_cov_world(const sl_gaussian& G, const float* xf) {
+  m3 R;
+  R.c[0] = F3(xf[0], xf[4], xf[8]);
+  R.c[1] = F3(xf[1], xf[5], xf[9]);
+  R.c[2] = F3(xf[2], xf[6], xf[10]);
+  m3 Rq = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]);
+  m3 D = m3diag(F3(G.scale[0] * G.scale[0], G.scale[1] * G.scale[1], G.scale[2] * G.scale[2]));
+  m3 t0 = m3m(Rq, D);
+  m3 C = m3m(t0, m3t(Rq));
+  m3 t1 = m3m(R, C);
+  return m3m(t1, m3t(R));
+}
+
+__global__ void __launch_bounds__(kThreads) lsm_splat_kernel(const __grid_constant__ LightMapParams L,
+                                                             const sl_gaussian* __restrict__ gs,
+                                                             const sl_node* __restrict__ nodes,
+                                                             const sl_part* __restrict__ parts, uint32_t count,
+                                                             uint32_t* acc) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= count) return;
+  const sl_gaussian& G = gs[g];
+  const uint32_t p = G.part_surface & 0xFFFFu;
+  if (p >= L.part_count || p == L.skip_part || ((L.dirty >> p) & 1u) == 0u) return;
+  const float FIX = 65536.0f, LOWPASS = 0.3f;
+  const float* xf = parts[p].xf;
+  const Leaf nd = load_leaf(&nodes[g]);
+  f3 m = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  f3 dv = sub3(m, ld3(L.center));
+  float r = len3(dv);
+  if (r < 1e-4f) return;
+  f3 w = div3(dv, r);
+  m3 C = leaf_cov_world(G, xf);
+  if (L.hemi && dot3(dv, ld3(L.normal)) < -3.0f * sqrtf(dot3(ld3(L.normal), m3v(C, ld3(L.normal))))) return;
+  f3 b0 = basis_k(w), b1 = cross3(w, b0);
+  f3 c0 = m3v(C, b0), c1 = m3v(C, b1);
+  float cbbx = dot3(b0, c0), cbby = dot3(b0, c1), cbbz = dot3(b1, c1);
+  f3 cw = m3v(C, w);
+  f2 cbz = F2(dot3(b0, cw), dot3(b1, cw));
+  float czz = dot3(w, cw);
+  m2 Cbb;
+  Cbb.c[0] = F2(cbbx, cbby);
+  Cbb.c[1] = F2(cbby, cbbz);
+  m2 Cbb_i = m2inv(Cbb);
+  float sz2 = fmaxf(czz - dot2(cbz, m2v(Cbb_i, cbz)), 1e-12f);
+  float tau0 = nd.kappa * dirm(nd, xf_dir_inv(xf, w)) * sqrtf(2.0f * kPi * sz2);
+  float half_res = 0.5f * (float)L.res;
+  m2 J = m2s(oct_jac(L, w, b0, b1), half_res);
+  m2 Sang = m2s(Cbb, 1.0f / (r * r));
+  m2 S = m2m(m2m(J, Sang), m2t(J));
+  float det0 = m2det(S);
+  S.c[0].x += LOWPASS;
+  S.c[1].y += LOWPASS;
+  float det1 = m2det(S);
+  tau0 *= sqrtf(fmaxf(det0, 0.0f) / det1);
+  m2 Si = m2inv(S);
+  f2 gz = m2v(m2t(m2inv(J)), mul2(m2v(Cbb_i, cbz), r));
+  f2 uv = oct_uv(L, w);
+  f2 ct = F2((uv.x * 0.5f + 0.5f) * (float)L.res, (uv.y * 0.5f + 0.5f) * (float)L.res);
+  int hx = (int)ceilf(3.0f * sqrtf(S.c[0].x)), hy = (int)ceilf(3.0f * sqrtf(S.c[1].y));
+  hx = hx > 48 ? 48 : hx;
+  hy = hy > 48 ? 48 : hy;
+  int cx = (int)floorf(ct.x), cy = (int)floorf(ct.y);
+  const uint32_t base = p * L.res * L.res;
+  const int ires = (int)L.res;
+  const int y0 = cy - hy > 0 ? cy - hy : 0, y1 = cy + hy < ires - 1 ? cy + hy : ires - 1;
+  const int x0 = cx - hx > 0 ? cx - hx : 0, x1 = cx + hx < ires - 1 ? cx + hx : ires - 1;
+  for (int y = y0; y <= y1; y++) {
+    for (int x = x0; x <= x1; x++) {
+      f2 dt = sub2(F2((float)x + 0.5f, (float)y + 0.5f), ct);
+      float q = dot2(dt, m2v(Si, dt));
+      if (q > 9.0f) continue;
+      float tt = fminf(tau0 * sl_expf(-0.5f * q), 64.0f);
+      float t_fix = tt * FIX;
+      if (t_fix < 0.5f) continue;
+      float z = fmaxf(r + dot2(gz, dt), 0.0f);
+      uint32_t k = (base + (uint32_t)y * L.res + (uint32_t)x) * 3u;
+      atomicAdd(&acc[k], to_u32(t_fix + 0.5f));
+      atomicAdd(&acc[k + 1], to_u32(t_fix * z + 0.5f));
+      atomicAdd(&acc[k + 2], to_u32(t_fix * (z * z + sz2) + 0.5f));
+    }
+  }
+}
+
+// resolve: (alpha, alpha mu, alpha m2) per texel of every dirty layer (light_shadow.wgsl:290-304)
+__global__ void __launch_bounds__(kThreads) resolve_kernel(const uint32_t* __restrict__ acc, float fix,
+                                                           uint32_t texels, uint32_t layers, uint32_t layer_texels,
+                                                           const uint32_t* __restrict__ dirty_layers,
+                                                           float4* __restrict__ mip) {
+  const uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (i >= (uint64_t)texels * layers) return;
+  const uint32_t l = (uint32_t)(i / texels);
+  if (dirty_layers && !dirty_layers[l]) return;
+  const uint32_t j = (uint32_t)(i - (uint64_t)l * texels);
+  float s0 = (float)acc[3 * i] / fix;
+  float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (s0 > 1e-5f) {
+    float a = 1.0f - sl_expf(-s0);
+    o.x = a;
+    o.y = a * (float)acc[3 * i + 1] / (fix * s0);
+    o.z = a * (float)acc[3 * i + 2] / (fix * s0);
+  }
+  mip[(uint64_t)l * layer_texels + j] = o;
+}
+
+// one mip level from the level above, mean of 4 children (light_shadow.wgsl:307-321)
+__global__ void __launch_bounds__(kThreads) down_kernel(float4* mip, uint32_t rk, uint32_t off_src, uint32_t off_dst,
+                                                        uint32_t layers, uint32_t layer_texels,
+                                                        const uint32_t* __restrict__ dirty_layers) {
+  const uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+  const uint32_t n = rk * rk;
+  if (i >= (uint64_t)n * layers) return;
+  const uint32_t l = (uint32_t)(i / n);
+  if (dirty_layers && !dirty_layers[l]) return;
+  const uint32_t j = (uint32_t)(i - (uint64_t)l * n);
+  const uint32_t y = j / rk, x = j - y * rk, pr = rk * 2u;
+  const float4* s = mip + (uint64_t)l * layer_texels + off_src + (2u * y) * pr + 2u * x;
+  const float4 a = s[0], b = s[1], c = s[pr], d = s[pr + 1];
+  mip[(uint64_t)l * layer_texels + off_dst + j] =
+      make_float4(0.25f * (a.x + b.x + c.x + d.x), 0.25f * (a.y + b.y + c.y + d.y), 0.25f * (a.z + b.z + c.z + d.z),
+                  0.25f * (a.w + b.w + c.w + d.w));
+}
+
+__device__ __forceinline__ float4 mip_at(const float4* layer, const uint32_t* level_off, uint32_t res, uint32_t k,
+                                         f2 tc) {
+  uint32_t rk = res >> k;
+  rk = rk < 1u ? 1u : rk;
+  float sc = (float)(1u << k);
+  float cxf = clampf(tc.x / sc - 0.5f, 0.0f, (float)(rk - 1u)), cyf = clampf(tc.y / sc - 0.5f, 0.0f, (float)(rk - 1u));
+  uint32_t i0x = (uint32_t)floorf(cxf), i0y = (uint32_t)floorf(cyf);
+  uint32_t i1x = i0x + 1u < rk - 1u ? i0x + 1u : rk - 1u, i1y = i0y + 1u < rk - 1u ? i0y + 1u : rk - 1u;
+  float fx = cxf - (float)i0x, fy = cyf - (float)i0y;
+  const float4* b = layer + level_off[k];
+  float4 a = mix4(b[i0y * rk + i0x], b[i0y * rk + i1x], fx);
+  float4 c = mix4(b[i1y * rk + i0x], b[i1y * rk + i1x], fx);
+  return mix4(a, c, fy);
+}
+__device__ __forceinline__ float4 mip_tri(const float4* layer, const uint32_t* level_off, uint32_t res,
+                                          uint32_t levels, float l, f2 tc) {
+  float lc = clampf(l, 0.0f, (float)(levels - 1u));
+  uint32_t k0 = (uint32_t)floorf(lc);
+  uint32_t k1 = k0 + 1u < levels - 1u ? k0 + 1u : levels - 1u;
+  return mix4(mip_at(layer, level_off, res, k0, tc), mip_at(layer, level_off, res, k1, tc), lc - (float)k0);
+}
+
+__global__ void __launch_bounds__(kThreads) lsm_lookup_kernel(const __grid_constant__ LightMapParams L,
+                                                              const sl_gaussian* __restrict__ gs,
+                                                              const sl_part* __restrict__ parts, uint32_t count,
+                                                              const float4* __restrict__ mip, float* __restrict__ lamp_T) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= count) return;
+  const sl_gaussian& G = gs[g];
+  const uint32_t own = G.part_surface & 0xFFFFu;
+  f3 P = xf_point(parts[own].xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  f3 dv = sub3(P, ld3(L.center));
+  float z = len3(dv);
+  if (z < 1e-4f) {
+    lamp_T[g] = 1.0f;
+    return;
+  }
+  f3 w = div3(dv, z);
+  f3 b0 = basis_k(w), b1 = cross3(w, b0);
+  m2 J = oct_jac(L, w, b0, b1);
+  float tex_ang = (2.0f / (float)L.res) / sqrtf(fmaxf(fabsf(m2det(J)), 1e-12f));
+  f2 uv = oct_uv(L, w);
+  f2 tc = F2((uv.x * 0.5f + 0.5f) * (float)L.res, (uv.y * 0.5f + 0.5f) * (float)L.res);
+  float T = 1.0f;
+  for (uint32_t p = 0; p < L.part_count; p++) {
+    if (p == own || p == L.skip_part) continue;
+    const float* bs = parts[p].bound;
+    f3 bc = sub3(xf_point(parts[p].xf, F3(bs[0], bs[1], bs[2])), ld3(L.center));
+    float dc = len3(bc);
+    float zn = fmaxf(dc - bs[3], 0.02f);
+    if (z <= zn) continue;
+    float search = 2.0f * L.sigma_l * (z - zn) / (zn * z);
+    if (dc > bs[3]) {
+      float ang = sl_acosf(clampf(dot3(div3(bc, dc), w), -1.0f, 1.0f));
+      if (ang > sl_asinf(bs[3] / dc) + search + 2.0f * tex_ang) continue;
+    }
+    const float4* layer = mip + (uint64_t)p * L.layer_texels;
+    float ls = sl_log2f(fmaxf(2.0f * search / tex_ang, 1.0f));
+    float4 a0 = mip_tri(layer, L.level_off, L.res, L.levels, ceilf(ls), tc);
+    if (a0.x < 1e-4f) continue;
+    float zb = fmaxf(a0.y / a0.x, 0.02f);
+    float pen = L.sigma_l * fmaxf(z - zb, 0.0f) / (zb * z);
+    float4 s = mip_tri(layer, L.level_off, L.res, L.levels, sl_log2f(fmaxf(2.0f * pen / tex_ang, 1.0f)), tc);
+    if (s.x < 1e-5f) continue;
+    float mu_ = s.y / s.x;
+    float sd = sqrtf(fmaxf(s.z / s.x - mu_ * mu_, 1e-8f));
+    T *= 1.0f - s.x * phi_cdf((z - mu_) / sd);
+  }
+  lamp_T[g] = T;
+}
+
+// ---- sun maps ----------------------------------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kThreads) sm_splat_kernel(const __grid_constant__ SunParams SP,
+                                                            const SunLayer* __restrict__ layers,
+                                                            const sl_gaussian* __restrict__ gs,
+                                                            const sl_node* __restrict__ nodes,
+                                                            const sl_part* __restrict__ parts, uint32_t count,
+                                                            uint32_t* acc) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= count) return;
+  const sl_gaussian& G = gs[g];
+  const uint32_t p = G.part_surface & 0xFFFFu;
+  if (p >= SP.n_parts) return;
+  const float SM_FIX = 4096.0f, SM_LOWPASS = 0.3f;
+  const uint32_t l_first = SP.part_first[p], l_end = l_first + SP.part_layers[p];
+  for (uint32_t l = l_first; l < l_end; l++) {
+    const SunLayer ly = layers[l];
+    if (!ly.dirty || !SP.lights[ly.light].shadows) continue;
+    const float* xf = parts[p].xf;
+    const Leaf nd = load_leaf(&nodes[g]);
+    f3 x = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+    f3 w = ld3(SP.lights[ly.light].dir);
+    f3 b0 = ld3(ly.t1), b1 = ld3(ly.t2);
+    m3 C = leaf_cov_world(G, xf);
+    f3 c0 = m3v(C, b0), c1 = m3v(C, b1), cw = m3v(C, w);
+    m2 Cbb;
+    Cbb.c[0] = F2(dot3(b0, c0), dot3(b1, c0));
+    Cbb.c[1] = F2(dot3(b0, c1), dot3(b1, c1));
+    f2 cbz = F2(dot3(b0, cw), dot3(b1, cw));
+    m2 Cbb_i = m2inv(Cbb);
+    float sz2 = fmaxf(dot3(w, cw) - dot2(cbz, m2v(Cbb_i, cbz)), 1e-12f);
+    float tex = (float)SP.res / (2.0f * ly.half);
+    m2 Sm = m2s(Cbb, tex * tex);
+    float det0 = m2det(Sm);
+    Sm.c[0].x += SM_LOWPASS;
+    Sm.c[1].y += SM_LOWPASS;
+    float det1 = m2det(Sm);
+    float tau0 = nd.kappa * dirm(nd, xf_dir_inv(xf, w)) * sqrtf(2.0f * kPi * sz2) * sqrtf(fmaxf(det0, 0.0f) / det1);
+    m2 Si = m2inv(Sm);
+    float z0 = ly.zref - dot3(x, w);
+    f2 gz = div2(m2v(Cbb_i, cbz), tex);
+    f2 ct = F2((dot3(x, b0) - ly.c[0] + ly.half) * tex, (dot3(x, b1) - ly.c[1] + ly.half) * tex);
+    int hx = (int)ceilf(3.0f * sqrtf(Sm.c[0].x)), hy = (int)ceilf(3.0f * sqrtf(Sm.c[1].y));
+    hx = hx > 32 ? 32 : hx;
+    hy = hy > 32 ? 32 : hy;
+    int cx = (int)floorf(ct.x), cy = (int)floorf(ct.y);
+    const uint32_t base = l * SP.res * SP.res;
+    const int ires = (int)SP.res;
+    const int y0 = cy - hy > 0 ? cy - hy : 0, y1 = cy + hy < ires - 1 ? cy + hy : ires - 1;
+    const int x0 = cx - hx > 0 ? cx - hx : 0, x1 = cx + hx < ires - 1 ? cx + hx : ires - 1;
+    for (int y = y0; y <= y1; y++) {
+      for (int xx = x0; xx <= x1; xx++) {
+        f2 dt = sub2(F2((float)xx + 0.5f, (float)y + 0.5f), ct);
+        float q = dot2(dt, m2v(Si, dt));
+        if (q > 9.0f) continue;
+        float tt = fminf(tau0 * sl_expf(-0.5f * q), 64.0f);
+        float t_fix = tt * SM_FIX;
+        if (t_fix < 0.5f) continue;
+        float z = fmaxf(z0 - dot2(gz, dt), 0.0f);
+        uint32_t i = (base + (uint32_t)y * SP.res + (uint32_t)xx) * 3u;
+        atomicAdd(&acc[i], to_u32(t_fix + 0.5f));
+        atomicAdd(&acc[i + 1], to_u32(t_fix * z + 0.5f));
+        atomicAdd(&acc[i + 2], to_u32(t_fix * (z * z + sz2) + 0.5f));
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) sm_lookup_kernel(const __grid_constant__ SunParams SP,
+                                                             const SunLayer* __restrict__ layers,
+                                                             const sl_gaussian* __restrict__ gs,
+                                                             const sl_part* __restrict__ parts, uint32_t count,
+                                                             const float4* __restrict__ mip, float4* __restrict__ env_T) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= count) return;
+  const sl_gaussian& G = gs[g];
+  const uint32_t own = G.part_surface & 0xFFFFu;
+  f3 P = xf_point(parts[own].xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  float T[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+  uint32_t used = kNone;
+  for (uint32_t l = 0; l < SP.n_layers; l++) {
+    const SunLayer ly = layers[l];
+    const uint32_t key = ly.part * 8u + ly.light;
+    if (ly.part == own || key == used || !SP.lights[ly.light].shadows) continue;
+    f3 w = ld3(SP.lights[ly.light].dir);
+    f2 uv = sub2(F2(dot3(P, ld3(ly.t1)), dot3(P, ld3(ly.t2))), F2(ly.c[0], ly.c[1]));
+    float inner = (ly.kind == 1u ? 0.9f : 1.0f) * ly.half;
+    if (fabsf(uv.x) >= inner || fabsf(uv.y) >= inner) continue;
+    used = key;
+    float z = ly.zref - dot3(P, w);
+    if (z <= 0.0f) continue;
+    float texel = 2.0f * ly.half / (float)SP.res;
+    f2 tc = F2((uv.x + ly.half) / texel, (uv.y + ly.half) / texel);
+    float sig = SP.lights[ly.light].std;
+    float search = 2.0f * sig * z;
+    const float4* layer = mip + (uint64_t)l * SP.layer_texels;
+    float4 a0 = mip_tri(layer, SP.level_off, SP.res, SP.levels, sl_log2f(fmaxf(2.0f * search / texel, 1.0f)), tc);
+    if (a0.x < 1e-4f) continue;
+    float zb = a0.y / a0.x;
+    float pen = sig * fmaxf(z - zb, 0.0f);
+    float4 s = mip_tri(layer, SP.level_off, SP.res, SP.levels, sl_log2f(fmaxf(2.0f * pen / texel, 1.0f)), tc);
+    if (s.x < 1e-5f) continue;
+    float mu_ = s.y / s.x;
+    float sd = sqrtf(fmaxf(s.z / s.x - mu_ * mu_, 1e-8f));
+    T[ly.light] *= 1.0f - s.x * phi_cdf((z - mu_) / sd);
+  }
+  env_T[g] = make_float4(T[0], T[1], T[2], T[3]);
+}
+
+// ---- shade ------------------------------------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kThreads) shade_kernel(const __grid_constant__ ShadeParams SH,
+                                                         const sl_gaussian* __restrict__ gs,
+                                                         const sl_node* __restrict__ nodes,
+                                                         const sl_vgrid* __restrict__ vgrid,
+                                                         const sl_part* __restrict__ parts,
+                                                         const sl_material* __restrict__ mats,
+                                                         const float* __restrict__ tree,
+                                                         const float* __restrict__ lamp_T,
+                                                         const float4* __restrict__ env_T,
+                                                         float4* __restrict__ colour, uint32_t count) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= count) return;
+  const sl_gaussian& G = gs[g];
+  const Leaf nd = load_leaf(&nodes[g]);
+  uint32_t mi = G.flags & 0xFFFFu;
+  const uint32_t mtop = (SH.material_count > 1u ? SH.material_count : 1u) - 1u;
+  mi = mi < mtop ? mi : mtop;
+  const sl_material mat = mats[mi];
+  const float* xf = parts[G.part_surface & 0xFFFFu].xf;
+  m3 Rq = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]);
+  m3 Sloc = m3m(m3m(Rq, m3diag(F3(mat.flake[0], mat.flake[1], mat.flake[2]))), m3t(Rq));
+  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
+  const float detC = s3 * s3;
+  const f3 P = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  const f3 n = Rq.c[0], t1 = Rq.c[1], t2 = Rq.c[2];
+  const f3 Sd = F3(Sloc.c[0].x, Sloc.c[1].y, Sloc.c[2].z), So = F3(Sloc.c[1].x, Sloc.c[2].x, Sloc.c[2].y);
+  const f3 flake = F3(mat.flake[0], mat.flake[1], mat.flake[2]);
+  const f3 alb = F3(G.albedo[0], G.albedo[1], G.albedo[2]);
+  const float ks = spec_weight(mat);
+  const bool emissive = (mat.flags & 1u) != 0u;
+  const f3 eye = ld3(SH.eye);
+  const sl_vgrid& vg = vgrid[g];
+  f3 c = F3(0.0f, 0.0f, 0.0f);
+  if (SH.n_emit || emissive) {
+    const f3 wo0 = xf_dir_inv(xf, norm3(sub3(eye, P)));
+    f3 acc = F3(0.0f, 0.0f, 0.0f);
+    if (SH.n_emit) {
+      uint32_t stack[48];
+      uint32_t sp = 1;
+      stack[0] = SH.root;
+      const bool shape = SH.asg && ks > 0.0f;
+      while (sp > 0u) {
+        sp--;
+        const float* e = tree + 24u * stack[sp];
+        const uint32_t child_lo = __float_as_uint(e[11]), child_hi = __float_as_uint(e[15]);
+        const f3 emean = F3(e[0], e[1], e[2]);
+        bool use;
+        if (child_lo == kNone || SH.mode == 0u) {
+          use = child_lo == kNone;
+        } else {
+          f3 d = sub3(P, emean);
+          use = dot3(d, d) > SH.theta * SH.theta * e[3] * e[3];
+        }
+        if (!use) {
+          if (sp + 2u <= 48u) {
+            stack[sp] = child_lo;
+            stack[sp + 1u] = child_hi;
+            sp += 2u;
+          }
+          continue;
+        }
+        f3 d = sub3(emean, P);
+        float d2 = dot3(d, d);
+        if (d2 < 1e-8f) continue;
+        f3 ww = div3(d, sqrtf(d2));
+        f3 wi = xf_dir_inv(xf, ww);
+        float vi = vgrid_lookup(vg, wi);
+        if (vi <= 1e-7f) continue;
+        float fp = footprint(nd, detC, wi);
+        f3 mw = mul3(ww, -1.0f);
+        float s = 1.0f;
+        if (SH.one_sided) {
+          float cs = dot3(mw, ld3(SH.normal));
+          s = SH.edge_soft > 0.0f ? smoothstepf(-SH.edge_soft, SH.edge_soft, cs) : (cs > 0.0f ? 1.0f : 0.0f);
+        }
+        float mq = sqrtf(fmaxf(dot3(mw, sym_mul(F3(e[4], e[5], e[6]), F3(e[8], e[9], e[10]), mw)), 0.0f));
+        f3 I = mul3(F3(e[12], e[13], e[14]), s * SH.scale * mq);
+        f3 light = mul3(mul3(I, vi), fp / d2 * 1.0f);
+        if (ks <= 0.0f) {
+          acc = add3(acc, light);
+          continue;
+        }
+        f3 wr = mirror3(wi, n);
+        float damp = iso_damp(nd.iso_norm, footprint(nd, detC, wr) * vgrid_lookup(vg, wr));
+        if (shape) {
+          f3 bw0, bw1;
+          onb(ww, bw0, bw1);
+          f3 cd = F3(e[16], e[17], e[18]), co = F3(e[20], e[21], e[22]);
+          f3 cc0 = sym_mul(cd, co, bw0), cc1 = sym_mul(cd, co, bw1);
+          s2m slm{dot3(bw0, cc0) / d2, dot3(bw0, cc1) / d2, dot3(bw1, cc1) / d2};
+          f3 lb0 = xf_dir_inv(xf, bw0), lb1 = xf_dir_inv(xf, bw1);
+          float pp = asg_phase(wi, lb0, lb1, slm, n, t1, t2, flake, Sd, So, wo0);
+          acc = add3(acc, mul3(light, iso_lobe_from(ks, pp, damp)));
+          continue;
+        }
+        float lobe = iso_lobe_from(ks, phase_specular(Sd, So, wi, wo0), damp);
+        acc = add3(acc, mul3(light, lobe));
+      }
+    }
+    const float T = lamp_T[g];
+    c = mul3(mul3v(alb, acc), T * nd.iso_norm);
+    if (emissive && ((mat.flags & 4u) == 0u || dot3(wo0, n) > 0.0f))
+      c = add3(c, F3(half_lo(mat.pad0), half_hi(mat.pad0), half_lo(mat.pad1)));
+  }
+  if (SH.n_lights && !emissive) {
+    const float inorm = nd.iso_norm;
+    const float4 et = env_T[g];
+    const float Tk[4] = {et.x, et.y, et.z, et.w};
+    if (ks <= 0.0f) {
+      f3 dc = F3(0.0f, 0.0f, 0.0f);
+      for (uint32_t k = 0; k < SH.n_lights; k++) {
+        f3 wi = xf_dir_inv(xf, ld3(SH.lights[k].dir));
+        float v = vgrid_lookup(vg, wi);
+        if (v <= 1e-7f) continue;
+        dc = add3(dc, mul3(ld3(SH.lights[k].irr), Tk[k] * v * footprint(nd, detC, wi)));
+      }
+      c = add3(c, mul3(mul3v(alb, dc), inorm));
+    } else {
+      f3 wo = xf_dir_inv(xf, norm3(sub3(eye, P)));
+      f3 diff = F3(0.0f, 0.0f, 0.0f), spec = F3(0.0f, 0.0f, 0.0f);
+      for (uint32_t k = 0; k < SH.n_lights; k++) {
+        f3 wi = xf_dir_inv(xf, ld3(SH.lights[k].dir));
+        float v = vgrid_lookup(vg, wi);
+        if (v <= 1e-7f) continue;
+        f3 light = mul3(ld3(SH.lights[k].irr), Tk[k] * v * footprint(nd, detC, wi));
+        f3 wr = mirror3(wi, n);
+        float damp = iso_damp(inorm, footprint(nd, detC, wr) * vgrid_lookup(vg, wr));
+        float s2 = SH.lights[k].std * SH.lights[k].std;
+        f3 ob0, ob1;
+        onb(wi, ob0, ob1);
+        float pp = asg_phase(wi, ob0, ob1, s2m{s2, 0.0f, s2}, n, t1, t2, flake, Sd, So, wo);
+        diff = add3(diff, mul3(light, 1.0f - ks));
+        spec = add3(spec, mul3(light, iso_lobe_from(ks, pp, damp) - (1.0f - ks)));
+      }
+      c = add3(c, mul3v(mul3(alb, inorm), add3(diff, spec)));
+    }
+  }
+  if (!emissive && SH.sky_ambient > 0.0f) c = add3(c, mul3(alb, SH.sky_ambient));
+  colour[g] = make_float4(c.x, c.y, c.z, 1.0f);
+}
+
+}  // namespace
+
+cudaError_t upload_iso_dirs(const float* dirs128x4, cudaStream_t s) {
+  return cudaMemcpyToSymbolAsync(c_iso_dirs, dirs128x4, sizeof(float) * 512, 0, cudaMemcpyHostToDevice, s);
+}
+
+static uint32_t blocks_for(uint64_t n) { return (uint32_t)((n + kThreads - 1) / kThreads); }
+
+cudaError_t launch_iso(const sl_gaussian* gs, sl_node* nodes, const sl_vgrid* vgrid, uint32_t count, cudaStream_t s) {
+  if (!count) return cudaSuccess;
+  iso_kernel<<<blocks_for(count), kThreads, 0, s>>>(gs, nodes, vgrid, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lsm_splat(const LightMapParams& L, const sl_gaussian* gs, const sl_node* nodes,
+                             const sl_part* parts, uint32_t count, uint32_t* acc, cudaStream_t s) {
+  if (!count) return cudaSuccess;
+  lsm_splat_kernel<<<blocks_for(count), kThreads, 0, s>>>(L, gs, nodes, parts, count, acc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_resolve(const uint32_t* acc, float fix, uint32_t texels, uint32_t layers, uint32_t layer_texels,
+                           const uint32_t* dirty_layers, float4* mip, cudaStream_t s) {
+  uint64_t n = (uint64_t)texels * layers;
+  if (!n) return cudaSuccess;
+  resolve_kernel<<<blocks_for(n), kThreads, 0, s>>>(acc, fix, texels, layers, layer_texels, dirty_layers, mip);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mips(float4* mip, uint32_t res, uint32_t levels, const uint32_t* level_off, uint32_t layers,
+                        uint32_t layer_texels, const uint32_t* dirty_layers, cudaStream_t s) {
+  for (uint32_t k = 1; k < levels; k++) {
+    uint32_t rk = res >> k;
+    uint64_t n = (uint64_t)rk * rk * layers;
+    down_kernel<<<blocks_for(n), kThreads, 0, s>>>(mip, rk, level_off[k - 1], level_off[k], layers, layer_texels,
+                                                   dirty_layers);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_lsm_lookup(const LightMapParams& L, const sl_gaussian* gs, const sl_part* parts, uint32_t count,
+                              const float4* mip, float* lamp_T, cudaStream_t s) {
+  if (!count) return cudaSuccess;
+  lsm_lookup_kernel<<<blocks_for(count), kThreads, 0, s>>>(L, gs, parts, count, mip, lamp_T);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sm_splat(const SunParams& SP, const SunLayer* layers, const sl_gaussian* gs, const sl_node* nodes,
+                            const sl_part* parts, uint32_t count, uint32_t* acc, cudaStream_t s) {
+  if (!count) return cudaSuccess;
+  sm_splat_kernel<<<blocks_for(count), kThreads, 0, s>>>(SP, layers, gs, nodes, parts, count, acc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sm_lookup(const SunParams& SP, const SunLayer* layers, const sl_gaussian* gs, const sl_part* parts,
+                             uint32_t count, const float4* mip, float4* env_T, cudaStream_t s) {
+  if (!count) return cudaSuccess;
+  sm_lookup_kernel<<<blocks_for(count), kThreads, 0, s>>>(SP, layers, gs, parts, count, mip, env_T);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const ShadeParams& SH, const sl_gaussian* gs, const sl_node* nodes, const sl_vgrid* vgrid,
+                         const sl_part* parts, const sl_material* mats, const float* tree, const float* lamp_T,
+                         const float4* env_T, float4* colour, uint32_t count, cudaStream_t s) {
+  if (!count) return cudaSuccess;
+  shade_kernel<<<blocks_for(count), kThreads, 0, s>>>(SH, gs, nodes, vgrid, parts, mats, tree, lamp_T, env_T, colour,
+                                                      count);
+  return cudaGetLastError();
+}
+
+}  // namespace sl

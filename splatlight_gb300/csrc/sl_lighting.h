@@ -1,0 +1,65 @@
+// Internal declarations of the lighting kernels and their parameter blocks.
+#pragma once
+
+#include "sl_internal.h"
+
+namespace sl {
+
+// light map A frame and layout (light_shadow.wgsl:26-38 LSParams, the fields map A reads)
+struct LightMapParams {
+  float center[3], normal[3], t1[3], t2[3];
+  float sigma_l;
+  uint32_t hemi, res, levels, layer_texels, part_count, skip_part, dirty;
+  uint32_t level_off[16];
+};
+
+struct EnvLightDev {
+  float dir[3];
+  float std;
+  float irr[3];
+  uint32_t shadows;
+};
+
+// sun_map.wgsl:24-35 SunParams (what the kernels read) + the layer ranges per part
+struct SunParams {
+  uint32_t n_layers, res, levels, layer_texels, n_parts;
+  uint32_t level_off[16];
+  uint32_t part_first[32], part_layers[32];
+  EnvLightDev lights[4];
+};
+
+// one sun-map layer (sun_map.wgsl:32 SunLayer + the plan's kind and dirty flag)
+struct SunLayer {
+  float c[2];
+  float half, zref;
+  float t1[3], t2[3];
+  uint32_t part, light, kind, dirty;
+};
+
+struct ShadeParams {
+  float eye[3];
+  uint32_t n_emit, root, mode, asg, one_sided, material_count, n_lights;
+  float scale, theta, edge_soft, sky_ambient;
+  float normal[3];
+  EnvLightDev lights[4];
+};
+
+cudaError_t upload_iso_dirs(const float* dirs128x4, cudaStream_t s);
+cudaError_t launch_iso(const sl_gaussian* gs, sl_node* nodes, const sl_vgrid* vgrid, uint32_t count, cudaStream_t s);
+cudaError_t launch_lsm_splat(const LightMapParams& L, const sl_gaussian* gs, const sl_node* nodes,
+                             const sl_part* parts, uint32_t count, uint32_t* acc, cudaStream_t s);
+cudaError_t launch_resolve(const uint32_t* acc, float fix, uint32_t texels, uint32_t layers, uint32_t layer_texels,
+                           const uint32_t* dirty_layers, float4* mip, cudaStream_t s);
+cudaError_t launch_mips(float4* mip, uint32_t res, uint32_t levels, const uint32_t* level_off, uint32_t layers,
+                        uint32_t layer_texels, const uint32_t* dirty_layers, cudaStream_t s);
+cudaError_t launch_lsm_lookup(const LightMapParams& L, const sl_gaussian* gs, const sl_part* parts, uint32_t count,
+                              const float4* mip, float* lamp_T, cudaStream_t s);
+cudaError_t launch_sm_splat(const SunParams& SP, const SunLayer* layers, const sl_gaussian* gs, const sl_node* nodes,
+                            const sl_part* parts, uint32_t count, uint32_t* acc, cudaStream_t s);
+cudaError_t launch_sm_lookup(const SunParams& SP, const SunLayer* layers, const sl_gaussian* gs, const sl_part* parts,
+                             uint32_t count, const float4* mip, float4* env_T, cudaStream_t s);
+cudaError_t launch_shade(const ShadeParams& SH, const sl_gaussian* gs, const sl_node* nodes, const sl_vgrid* vgrid,
+                         const sl_part* parts, const sl_material* mats, const float* tree, const float* lamp_T,
+                         const float4* env_T, float4* colour, uint32_t count, cudaStream_t s);
+
+}  // namespace sl

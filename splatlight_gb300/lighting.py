@@ -1,0 +1,110 @@
+"""Lighting: the per-Gaussian lighting the splat path composites, mirroring src/lighting.js (Lighting: setEmitters
+:612, encode :1258), src/environment.js (Environment.set :106) and their shadow maps, over the C ABI."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .renderer import SplatRenderer
+from .structs import GAUSSIAN, MATERIAL, NODE, VGRID
+
+
+class EnvLight(C.Structure):
+    _fields_ = [("dir", C.c_float * 3), ("std", C.c_float), ("irradiance", C.c_float * 3),
+                ("casts_shadows", C.c_int32)]
+
+
+class Lighting:
+    """Radiance per Gaussian from emissive-Gaussian lights (light cut over a host emitter tree, per-part opacity map
+    shadows) and distant lights (sun maps), bound to a SplatRenderer's scene."""
+
+    def __init__(self, renderer: SplatRenderer, nodes: np.ndarray, vgrid: np.ndarray, materials: np.ndarray):
+        self._lib = N.lib()
+        self.renderer = renderer
+        nd = np.ascontiguousarray(nodes, dtype=NODE)
+        vg = np.ascontiguousarray(vgrid, dtype=VGRID)
+        mt = np.ascontiguousarray(materials, dtype=MATERIAL)
+        h = C.c_void_p()
+        N.check(self._lib.sl_lighting_create(renderer.handle, nd.ctypes.data, vg.ctypes.data, mt.ctypes.data, len(mt),
+                                             C.byref(h)))
+        self._h = h
+        self.count = renderer.count
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.sl_lighting_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_emitters(self, emitters: np.ndarray, scale: float = 1.0, one_sided: bool = False, normal=(0.0, 0.0, 1.0),
+                     skip_part: int = 0xFFFFFFFF) -> None:
+        e = np.ascontiguousarray(emitters, dtype=GAUSSIAN)
+        nrm = (C.c_float * 3)(*normal)
+        N.check(self._lib.sl_lighting_set_emitters(self._h, e.ctypes.data if len(e) else None, len(e), scale,
+                                                   1 if one_sided else 0, nrm, skip_part))
+
+    def set_environment(self, lights=(), sky_ambient: float = 0.0) -> None:
+        """lights: iterable of (direction, angular std in radians, irradiance rgb, casts shadows)."""
+        arr = (EnvLight * 4)()
+        n = 0
+        for d, std, irr, sh in lights:
+            arr[n].dir[:] = list(d)
+            arr[n].std = std
+            arr[n].irradiance[:] = list(irr)
+            arr[n].casts_shadows = 1 if sh else 0
+            n += 1
+        N.check(self._lib.sl_lighting_set_environment(self._h, C.addressof(arr) if n else None, n, sky_ambient))
+
+    def set_options(self, shadow_res: int = 512, sun_res: int = 512, mode: int = 1, theta: float = 4.0,
+                    asg: bool = True) -> None:
+        N.check(self._lib.sl_lighting_set_options(self._h, shadow_res, sun_res, mode, theta, 1 if asg else 0))
+
+    def update(self, eye, forward=None, moved_mask: int = 0, stream=None) -> None:
+        e = (C.c_float * 3)(*[float(v) for v in eye])
+        f = (C.c_float * 3)(*[float(v) for v in forward]) if forward is not None else None
+        N.check(self._lib.sl_lighting_update(self._h, e, f, moved_mask, stream))
+
+    def bind(self) -> None:
+        N.check(self._lib.sl_renderer_bind_lighting(self.renderer.handle, self._h))
+
+    def read(self):
+        """(colour (G, 4), lamp_T (G,), env_T (G, 4), nodes) from the device."""
+        n = self.count
+        col = np.empty((n, 4), np.float32)
+        lt = np.empty(n, np.float32)
+        et = np.empty((n, 4), np.float32)
+        nd = np.empty(n, dtype=NODE)
+        N.check(self._lib.sl_lighting_read(self._h, col.ctypes.data, lt.ctypes.data, et.ctypes.data, nd.ctypes.data))
+        return col, lt, et, nd
+
+
+def for_scene(renderer: SplatRenderer, scene) -> Lighting:
+    """A Lighting set up from a splatlight_gb300.scene.Scene: its host emitters, its sun and sky, its map sizes."""
+    L = Lighting(renderer, scene.nodes, scene.vgrid, scene.materials)
+    L.set_options(shadow_res=scene.shadow_res, sun_res=scene.sun_res)
+    L.set_emitters(scene.emitters)
+    if scene.sun is not None:
+        L.set_environment([(scene.sun.direction, scene.sun.angular_std, scene.sun.irradiance,
+                            scene.sun.casts_shadows)], scene.sky_ambient)
+    else:
+        L.set_environment([], scene.sky_ambient)
+    L.bind()
+    return L
+
+
+def camera_forward(scene, eye=None, target=None) -> np.ndarray:
+    """Unit view direction as float32 (the value both the GPU path and the restatement receive)."""
+    eye = np.asarray(scene.eye if eye is None else eye, np.float64)
+    tgt = np.asarray(scene.target if target is None else target, np.float64)
+    return ((tgt - eye) / np.linalg.norm(tgt - eye)).astype(np.float32)
