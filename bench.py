@@ -34,7 +34,9 @@ sys.path.insert(0, str(ROOT))
 
 MEASURED = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM = 6800.0  # GB/s
-KERNELS_PER_FRAME = 11  # project, 2 depth-sort passes, tile counts, scan, emit, 2 tile-sort passes, scan, ranges, composite
+# shade; project, 2 depth-sort passes, tile counts, scan, emit, 2 tile-sort passes, tile runs, run counts, scan,
+# ranges, composite
+KERNELS_PER_FRAME = 14
 
 
 def peaks():
@@ -106,17 +108,28 @@ def frame_for(s, view_mode):
 
 
 def workload_desc(s):
-    return (f"{s.name}: {s.count:,} Gaussians + {len(s.emitters)} emitters, {s.width}x{s.height}, fov {s.fov_deg:g} deg, "
-            f"lit view (radiance per Gaussian resident), plain per-view path")
+    sun = f", sun with {s.sun_res}^2 maps, sky ambient {s.sky_ambient:g}" if s.sun is not None else ""
+    return (f"{s.name}: {s.count:,} Gaussians + {len(s.emitters)} emitters ({s.shadow_res}^2 light map){sun}, "
+            f"{s.width}x{s.height}, fov {s.fov_deg:g} deg, lit view; plain per-view path, per frame the lighting pass "
+            f"(opacity maps cached: static scene) + project/sort/bin/composite")
 
 
-def cpu_frame_seconds(s, colour, threads):
-    """One full frame of the CPU restatement (project, sort, bin, composite) on `threads` host threads."""
+def cpu_frame_seconds(s, cache, threads):
+    """One full frame of the CPU restatement on `threads` host threads: the lighting pass (shade_emit + env_direct;
+    the opacity maps of the static scene come from `cache`, as on the GPU) then project, sort, bin, composite."""
     from oracle import oracle
     f = frame_for(s, 3)
     t0 = time.perf_counter()
+    colour, _, _, _ = oracle.lighting(s, threads=threads, cached=cache)
     oracle.render(s.gaussians, s.parts, f, emitters=s.emitters, colour=colour, threads=threads, want_entries=False)
     return time.perf_counter() - t0
+
+
+def cpu_cache(s, threads):
+    """iso_init and the opacity maps of the static scene, computed once (untimed)."""
+    from oracle import oracle
+    _, lamp_t, env_t, nodes = oracle.lighting(s, threads=threads)
+    return lamp_t, env_t, nodes
 
 
 def run_reference(args):
@@ -126,12 +139,12 @@ def run_reference(args):
     from oracle import oracle
     oracle.build()
     s = make_scene(args.config)
-    colour = np.random.default_rng(7).uniform(0, 2, (s.count, 4)).astype(np.float32)
     threads = os.cpu_count() or 1
-    t_warm = cpu_frame_seconds(s, colour, threads)
+    cache = cpu_cache(s, threads)
+    t_warm = cpu_frame_seconds(s, cache, threads)
     # bounded: at most ~90 s of CPU frames whatever --steps asks (each step is one full frame)
     n_run = max(1, min(args.steps, int(90.0 / max(t_warm, 1e-3))))
-    times = [cpu_frame_seconds(s, colour, threads) for _ in range(n_run)]
+    times = [cpu_frame_seconds(s, cache, threads) for _ in range(n_run)]
     ms = 1000.0 * sum(times) / len(times)
     v = 1000.0 / ms
     line = {"impl": "reference", "metric": "views/s", "value": round(v, 4), "unit": "views/s", "n_gpus": args.gpus,
@@ -177,21 +190,29 @@ def main():
     __import__("__graft_entry__").build()
     from splatlight_gb300.renderer import SplatRenderer
 
+    from splatlight_gb300.lighting import camera_forward, for_scene
+
     s = make_scene(args.config)
     W, H = s.width, s.height
-    colour_host = np.random.default_rng(7).uniform(0, 2, (s.count, 4)).astype(np.float32)
-    colour = torch.from_numpy(colour_host).cuda()
     f = frame_for(s, 3)
     r = SplatRenderer(s.gaussians, s.parts)
-    r.set_emitters(s.emitters)
-    r.bind_colour(colour)
+    L = for_scene(r, s)           # emitters, sun, sky; binds the radiance buffer the projection reads
+    fwd = camera_forward(s)
     stream = torch.cuda.Stream()
+    L.update(s.eye, fwd, stream=stream.cuda_stream)   # first update: iso_init + opacity maps (static scene)
+    torch.cuda.synchronize()
+
+    def step(out_buf):
+        # one frame: the lighting pass (shade_emit + env_direct; the maps hold while nothing moves) and the render
+        L.update(s.eye, fwd, stream=stream.cuda_stream)
+        return r.render(f, out=out_buf, stream=stream.cuda_stream)
+
     out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     # warm-up (also sizes the tile-entry buffers)
     for _ in range(args.warmup):
-        r.render(f, out=out, stream=stream.cuda_stream)
+        step(out)
 
     # device-timed steps
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -202,7 +223,7 @@ def main():
             for k in range(args.steps):
                 flush.zero_()
                 starts[k].record(stream)
-                r.render(f, out=out, stream=stream.cuda_stream)
+                step(out)
                 ends[k].record(stream)
         torch.cuda.synchronize()
     barrier()
@@ -214,15 +235,23 @@ def main():
         ms = float(t.item())
     views_per_s = world * 1000.0 / ms
     stats = r.last_stats
+    if not np.isfinite(out.sum().item()):
+        raise RuntimeError("non-finite image")
 
     # per-stage device times (events inside the pipeline), for the rooflines
     r.set_timing(True)
-    stage = {"project": [], "sort": [], "bin": [], "composite": []}
+    stage = {"lighting": [], "project": [], "sort": [], "bin": [], "composite": []}
     frags = []
     for _ in range(max(5, min(args.steps, 20))):
         with torch.cuda.stream(stream):
             flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.update(s.eye, fwd, stream=stream.cuda_stream)
+        e1.record(stream)
         r.render(f, out=out, stream=stream.cuda_stream)
+        stage["lighting"].append(e0.elapsed_time(e1))
         st = r.last_stats
         stage["project"].append(st.ms_project)
         stage["sort"].append(st.ms_sort)
@@ -238,11 +267,13 @@ def main():
     parts = s.parts.copy()
     for _ in range(2):
         r.write_parts(parts)
+        L.update(s.eye, fwd)
         r.render(f, out=host_out_np)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         r.write_parts(parts)
+        L.update(s.eye, fwd)
         r.render(f, out=host_out_np)
     e2e_s = (time.perf_counter() - t0) / args.steps
     if dist is not None:
@@ -276,9 +307,9 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        sec = cpu_frame_seconds(s, colour_host, threads)
+        sec = cpu_frame_seconds(s, cpu_cache(s, threads), threads)
         cpu = {"value": round(1.0 / sec, 4), "unit": "views/s", "cores": threads, "kind": "port",
-               "sample": "1 full frame of the same workload (project, sort, bin, composite)"}
+               "sample": "1 full frame of the same workload (lighting pass, project, sort, bin, composite)"}
 
     if rank == 0:
         line = {"metric": "views/s", "value": round(views_per_s, 2), "unit": "views/s", "n_gpus": world,
@@ -294,6 +325,7 @@ def main():
                 "roofline": roofline, "sort_roofline": roof_sort, "composite_roofline": roof_comp,
                 "cpu_baseline": cpu, "clocks": clocks}
         print(json.dumps(line))
+    L.close()
     r.close()
     if dist is not None:
         dist.destroy_process_group()

@@ -182,13 +182,15 @@ class LightSetup(C.Structure):
                 ("mode", C.c_uint32), ("asg", C.c_uint32), ("one_sided", C.c_uint32), ("normal", C.c_float * 3),
                 ("edge_soft", C.c_float), ("skip_part", C.c_uint32), ("shadow_res", C.c_uint32),
                 ("lights", C.c_void_p), ("n_lights", C.c_uint32), ("sun_res", C.c_uint32),
-                ("sky_ambient", C.c_float), ("eye", C.c_float * 3), ("fwd", C.c_float * 3)]
+                ("sky_ambient", C.c_float), ("eye", C.c_float * 3), ("fwd", C.c_float * 3),
+                ("shade_only", C.c_uint32)]
 
 
 def lighting(scene, eye=None, target=None, threads: int = 8, shadow_res=None, sun_res=None, mode: int = 1,
-             asg: bool = True):
+             asg: bool = True, cached=None):
     """The restated lighting update on a splatlight_gb300.scene.Scene: returns (colour (G, 4), lamp_T (G,),
-    env_T (G, 4), nodes with iso_norm).  Emitters are the scene's host emitter records."""
+    env_T (G, 4), nodes with iso_norm).  Emitters are the scene's host emitter records.  cached: the (lamp_T,
+    env_T, nodes) of an earlier call -- then only the shading pass runs (the maps of a static scene hold)."""
     L = lib()
     L.orc_lighting.restype = C.c_int
     L.orc_lighting.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -232,6 +234,9 @@ def lighting(scene, eye=None, target=None, threads: int = 8, shadow_res=None, su
     colour = np.zeros((n, 4), np.float32)
     lamp_t = np.ones(n, np.float32)
     env_t = np.ones((n, 4), np.float32)
+    if cached is not None:
+        lamp_t, env_t, nodes = (np.ascontiguousarray(c).copy() for c in cached)
+        S.shade_only = 1
     rc = L.orc_lighting(g.ctypes.data, n, p.ctypes.data, len(p), nodes.ctypes.data, vg.ctypes.data, m.ctypes.data,
                         len(m), C.byref(S), colour.ctypes.data, lamp_t.ctypes.data, env_t.ctypes.data, threads)
     if rc != 0:

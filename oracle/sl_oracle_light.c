@@ -801,10 +801,12 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
   /* iso_init (once per asset) */
   float dirs[512];
   orc_iso_dirs(dirs);
+  if (!S->shade_only) {
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nthreads) schedule(static, 1024)
 #endif
-  for (int64_t g = 0; g < (int64_t)count; g++) iso_one((uint32_t)g, gs, nodes, vgrid, dirs);
+    for (int64_t g = 0; g < (int64_t)count; g++) iso_one((uint32_t)g, gs, nodes, vgrid, dirs);
+  }
 
   /* emitter tree + params (lighting.js:657-673) */
   uint32_t n_emit = S->n_emit;
@@ -817,8 +819,9 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
   }
 
   /* light map A (light_shadow.js:89-165): all layers dirty, then the lookup */
-  for (uint32_t g = 0; g < count; g++) lamp_T[g] = 1.0f;
-  if (n_emit && S->shadow_res) {
+  if (!S->shade_only)
+    for (uint32_t g = 0; g < count; g++) lamp_T[g] = 1.0f;
+  if (n_emit && S->shadow_res && !S->shade_only) {
     uint32_t res = S->shadow_res, levels = 0, off = 0, level_off[16];
     for (uint32_t k = res; k >= 1u; k >>= 1) { level_off[levels++] = off; off += k * k; }
     uint32_t layer_texels = off;
@@ -903,10 +906,11 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
   }
 
   /* sun maps (sun_map.js:23-159, sun_map.wgsl) */
-  for (uint32_t g = 0; g < count; g++) env_T[4u * g] = env_T[4u * g + 1] = env_T[4u * g + 2] = env_T[4u * g + 3] = 1.0f;
+  if (!S->shade_only)
+    for (uint32_t g = 0; g < count; g++) env_T[4u * g] = env_T[4u * g + 1] = env_T[4u * g + 2] = env_T[4u * g + 3] = 1.0f;
   uint32_t K = S->n_lights < 4u ? S->n_lights : 4u;
   uint32_t Pn = part_count < 32u ? part_count : 32u;
-  if (K && S->sun_res) {
+  if (K && S->sun_res && !S->shade_only) {
     /* layer plan: per part with Gaussians, per light: cascades (8 m, 32 m) below 1.5 x the bound for large static
      * parts, then the fitted map */
     typedef struct { uint32_t p, k, kind; float c[2], half; } ldesc;

@@ -39,6 +39,7 @@ typedef struct orc_light_setup {
   float sky_ambient;  /* constant ambient (no reference counterpart) */
   float eye[3];
   float fwd[3];       /* camera forward, for the sun cascades */
+  uint32_t shade_only;/* 1: nodes (iso_norm), lamp_T and env_T are inputs from an earlier call; only shade */
 } orc_light_setup;
 
 /* The 128 iso_init cell directions and solid angles (iso_init.wgsl:39-45), 4 floats each, computed in float64. */
