@@ -21,6 +21,8 @@ LIB = PKG / "libsplatlight.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # translation units whose arithmetic is part of the bit-parity contract
 NO_FMAD = {"project.cu", "lighting.cu"}
+# translation units compiled for speed: fused multiply-add, approximate division and square root
+FAST = {"shade.cu"}
 
 
 def nvcc() -> str:
@@ -41,6 +43,8 @@ def _compile(src: Path) -> Path:
            "-I", str(ROOT / "include"), "-I", str(CSRC), "--expt-relaxed-constexpr", "-c", str(src), "-o", str(obj)]
     if src.name in NO_FMAD:
         cmd.insert(1, "--fmad=false")
+    if src.name in FAST:
+        cmd[1:1] = ["-prec-div=false", "-prec-sqrt=false"]
     if os.environ.get("SL_PTXAS_VERBOSE"):
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,14 +1,14 @@
-// Per-Gaussian lighting kernels: iso_init, the emitter light's per-part opacity map (map A), the sun's orthographic
-// opacity maps, and one fused shade kernel (shade_emit + env_direct + the constant sky ambient) writing the radiance
-// the projection reads.  One thread per Gaussian (or per texel for resolve / mip passes); opacity maps accumulate
-// u32 fixed-point atomics, so their sums do not depend on the order the Gaussians run in.
+// Per-Gaussian lighting kernels: iso_init, the emitter light's per-part opacity map (map A) and the sun's
+// orthographic opacity maps, which give the shading pass (shade.cu) its shadow transmittances.  One thread per
+// Gaussian (or per texel for resolve / mip passes); opacity maps accumulate u32 fixed-point atomics, so their sums do
+// not depend on the order the Gaussians run in.
 //
 //   iso_kernel        runtime/wgsl/iso_init.wgsl:29-56
 //   lsm_splat_kernel  runtime/wgsl/light_shadow.wgsl:191-286     lsm_lookup_kernel  :347-392
 //   sm_splat_kernel   runtime/wgsl/sun_map.wgsl:127-219          sm_lookup_kernel   :287-324
 //   resolve / down    light_shadow.wgsl:290-321, sun_map.wgsl:228-258
-//   shade_kernel      runtime/wgsl/emissive.wgsl:853-980 + environment.wgsl:207-308
-// Compiled with --fmad=false (see light_math.cuh).
+// The shading pass lives in shade.cu.  Compiled with --fmad=false (see light_math.cuh): the opacity maps' mip-level
+// selection (ceil of a log2) is discontinuous, so these kernels reproduce the CPU restatement's arithmetic exactly.
 #include "light_math.cuh"
 #include "sl_lighting.h"
 
@@ -373,149 +373,6 @@ __global__ void __launch_bounds__(kThreads) sm_lookup_kernel(const __grid_consta
   env_T[g] = make_float4(T[0], T[1], T[2], T[3]);
 }
 
-// ---- shade ------------------------------------------------------------------------------------------------------
-
-__global__ void __launch_bounds__(kThreads) shade_kernel(const __grid_constant__ ShadeParams SH,
-                                                         const sl_gaussian* __restrict__ gs,
-                                                         const sl_node* __restrict__ nodes,
-                                                         const sl_vgrid* __restrict__ vgrid,
-                                                         const sl_part* __restrict__ parts,
-                                                         const sl_material* __restrict__ mats,
-                                                         const float* __restrict__ tree,
-                                                         const float* __restrict__ lamp_T,
-                                                         const float4* __restrict__ env_T,
-                                                         float4* __restrict__ colour, uint32_t count) {
-  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
-  if (g >= count) return;
-  const sl_gaussian& G = gs[g];
-  const Leaf nd = load_leaf(&nodes[g]);
-  uint32_t mi = G.flags & 0xFFFFu;
-  const uint32_t mtop = (SH.material_count > 1u ? SH.material_count : 1u) - 1u;
-  mi = mi < mtop ? mi : mtop;
-  const sl_material mat = mats[mi];
-  const float* xf = parts[G.part_surface & 0xFFFFu].xf;
-  m3 Rq = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]);
-  m3 Sloc = m3m(m3m(Rq, m3diag(F3(mat.flake[0], mat.flake[1], mat.flake[2]))), m3t(Rq));
-  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
-  const float detC = s3 * s3;
-  const f3 P = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
-  const f3 n = Rq.c[0], t1 = Rq.c[1], t2 = Rq.c[2];
-  const f3 Sd = F3(Sloc.c[0].x, Sloc.c[1].y, Sloc.c[2].z), So = F3(Sloc.c[1].x, Sloc.c[2].x, Sloc.c[2].y);
-  const f3 flake = F3(mat.flake[0], mat.flake[1], mat.flake[2]);
-  const f3 alb = F3(G.albedo[0], G.albedo[1], G.albedo[2]);
-  const float ks = spec_weight(mat);
-  const bool emissive = (mat.flags & 1u) != 0u;
-  const f3 eye = ld3(SH.eye);
-  const sl_vgrid& vg = vgrid[g];
-  f3 c = F3(0.0f, 0.0f, 0.0f);
-  if (SH.n_emit || emissive) {
-    const f3 wo0 = xf_dir_inv(xf, norm3(sub3(eye, P)));
-    f3 acc = F3(0.0f, 0.0f, 0.0f);
-    if (SH.n_emit) {
-      uint32_t stack[48];
-      uint32_t sp = 1;
-      stack[0] = SH.root;
-      const bool shape = SH.asg && ks > 0.0f;
-      while (sp > 0u) {
-        sp--;
-        const float* e = tree + 24u * stack[sp];
-        const uint32_t child_lo = __float_as_uint(e[11]), child_hi = __float_as_uint(e[15]);
-        const f3 emean = F3(e[0], e[1], e[2]);
-        bool use;
-        if (child_lo == kNone || SH.mode == 0u) {
-          use = child_lo == kNone;
-        } else {
-          f3 d = sub3(P, emean);
-          use = dot3(d, d) > SH.theta * SH.theta * e[3] * e[3];
-        }
-        if (!use) {
-          if (sp + 2u <= 48u) {
-            stack[sp] = child_lo;
-            stack[sp + 1u] = child_hi;
-            sp += 2u;
-          }
-          continue;
-        }
-        f3 d = sub3(emean, P);
-        float d2 = dot3(d, d);
-        if (d2 < 1e-8f) continue;
-        f3 ww = div3(d, sqrtf(d2));
-        f3 wi = xf_dir_inv(xf, ww);
-        float vi = vgrid_lookup(vg, wi);
-        if (vi <= 1e-7f) continue;
-        float fp = footprint(nd, detC, wi);
-        f3 mw = mul3(ww, -1.0f);
-        float s = 1.0f;
-        if (SH.one_sided) {
-          float cs = dot3(mw, ld3(SH.normal));
-          s = SH.edge_soft > 0.0f ? smoothstepf(-SH.edge_soft, SH.edge_soft, cs) : (cs > 0.0f ? 1.0f : 0.0f);
-        }
-        float mq = sqrtf(fmaxf(dot3(mw, sym_mul(F3(e[4], e[5], e[6]), F3(e[8], e[9], e[10]), mw)), 0.0f));
-        f3 I = mul3(F3(e[12], e[13], e[14]), s * SH.scale * mq);
-        f3 light = mul3(mul3(I, vi), fp / d2 * 1.0f);
-        if (ks <= 0.0f) {
-          acc = add3(acc, light);
-          continue;
-        }
-        f3 wr = mirror3(wi, n);
-        float damp = iso_damp(nd.iso_norm, footprint(nd, detC, wr) * vgrid_lookup(vg, wr));
-        if (shape) {
-          f3 bw0, bw1;
-          onb(ww, bw0, bw1);
-          f3 cd = F3(e[16], e[17], e[18]), co = F3(e[20], e[21], e[22]);
-          f3 cc0 = sym_mul(cd, co, bw0), cc1 = sym_mul(cd, co, bw1);
-          s2m slm{dot3(bw0, cc0) / d2, dot3(bw0, cc1) / d2, dot3(bw1, cc1) / d2};
-          f3 lb0 = xf_dir_inv(xf, bw0), lb1 = xf_dir_inv(xf, bw1);
-          float pp = asg_phase(wi, lb0, lb1, slm, n, t1, t2, flake, Sd, So, wo0);
-          acc = add3(acc, mul3(light, iso_lobe_from(ks, pp, damp)));
-          continue;
-        }
-        float lobe = iso_lobe_from(ks, phase_specular(Sd, So, wi, wo0), damp);
-        acc = add3(acc, mul3(light, lobe));
-      }
-    }
-    const float T = lamp_T[g];
-    c = mul3(mul3v(alb, acc), T * nd.iso_norm);
-    if (emissive && ((mat.flags & 4u) == 0u || dot3(wo0, n) > 0.0f))
-      c = add3(c, F3(half_lo(mat.pad0), half_hi(mat.pad0), half_lo(mat.pad1)));
-  }
-  if (SH.n_lights && !emissive) {
-    const float inorm = nd.iso_norm;
-    const float4 et = env_T[g];
-    const float Tk[4] = {et.x, et.y, et.z, et.w};
-    if (ks <= 0.0f) {
-      f3 dc = F3(0.0f, 0.0f, 0.0f);
-      for (uint32_t k = 0; k < SH.n_lights; k++) {
-        f3 wi = xf_dir_inv(xf, ld3(SH.lights[k].dir));
-        float v = vgrid_lookup(vg, wi);
-        if (v <= 1e-7f) continue;
-        dc = add3(dc, mul3(ld3(SH.lights[k].irr), Tk[k] * v * footprint(nd, detC, wi)));
-      }
-      c = add3(c, mul3(mul3v(alb, dc), inorm));
-    } else {
-      f3 wo = xf_dir_inv(xf, norm3(sub3(eye, P)));
-      f3 diff = F3(0.0f, 0.0f, 0.0f), spec = F3(0.0f, 0.0f, 0.0f);
-      for (uint32_t k = 0; k < SH.n_lights; k++) {
-        f3 wi = xf_dir_inv(xf, ld3(SH.lights[k].dir));
-        float v = vgrid_lookup(vg, wi);
-        if (v <= 1e-7f) continue;
-        f3 light = mul3(ld3(SH.lights[k].irr), Tk[k] * v * footprint(nd, detC, wi));
-        f3 wr = mirror3(wi, n);
-        float damp = iso_damp(inorm, footprint(nd, detC, wr) * vgrid_lookup(vg, wr));
-        float s2 = SH.lights[k].std * SH.lights[k].std;
-        f3 ob0, ob1;
-        onb(wi, ob0, ob1);
-        float pp = asg_phase(wi, ob0, ob1, s2m{s2, 0.0f, s2}, n, t1, t2, flake, Sd, So, wo);
-        diff = add3(diff, mul3(light, 1.0f - ks));
-        spec = add3(spec, mul3(light, iso_lobe_from(ks, pp, damp) - (1.0f - ks)));
-      }
-      c = add3(c, mul3v(mul3(alb, inorm), add3(diff, spec)));
-    }
-  }
-  if (!emissive && SH.sky_ambient > 0.0f) c = add3(c, mul3(alb, SH.sky_ambient));
-  colour[g] = make_float4(c.x, c.y, c.z, 1.0f);
-}
-
 }  // namespace
 
 cudaError_t upload_iso_dirs(const float* dirs128x4, cudaStream_t s) {
@@ -579,13 +436,5 @@ cudaError_t launch_sm_lookup(const SunParams& SP, const SunLayer* layers, const 
   return cudaGetLastError();
 }
 
-cudaError_t launch_shade(const ShadeParams& SH, const sl_gaussian* gs, const sl_node* nodes, const sl_vgrid* vgrid,
-                         const sl_part* parts, const sl_material* mats, const float* tree, const float* lamp_T,
-                         const float4* env_T, float4* colour, uint32_t count, cudaStream_t s) {
-  if (!count) return cudaSuccess;
-  shade_kernel<<<blocks_for(count), kThreads, 0, s>>>(SH, gs, nodes, vgrid, parts, mats, tree, lamp_T, env_T, colour,
-                                                      count);
-  return cudaGetLastError();
-}
 
 }  // namespace sl

@@ -1,0 +1,182 @@
+// The shading pass: one thread per Gaussian sums the emissive-Gaussian lights over its light cut (shade_emit,
+// runtime/wgsl/emissive.wgsl:853-980) and the distant lights (env_direct / env_add, environment.wgsl:207-308), plus
+// the constant sky ambient, into the radiance the projection reads.  Unlike the opacity maps this output is
+// continuous in its inputs, so the translation unit is compiled for speed (fused multiply-add, approximate division
+// and square root): it agrees with the CPU restatement to ~1e-6 relative, not to the bit.
+// A V grid of all 255 (no own-part occlusion) is recognised once per Gaussian: its lookup is exactly 1 for every
+// direction (each cell is 255/255 = 1 and a mix of ones is one), so the three lookups per light are skipped.
+#include "light_math.cuh"
+#include "sl_lighting.h"
+
+namespace sl {
+namespace {
+
+using namespace lm;
+constexpr int kThreads = 128;
+
+__device__ __forceinline__ f3 ld3(const float* p) { return F3(p[0], p[1], p[2]); }
+
+__device__ __forceinline__ float vlook(const sl_vgrid& v, bool open, f3 w) { return open ? 1.0f : vgrid_lookup(v, w); }
+
+__global__ void __launch_bounds__(kThreads) shade_kernel(const __grid_constant__ ShadeParams SH,
+                                                         const sl_gaussian* __restrict__ gs,
+                                                         const sl_node* __restrict__ nodes,
+                                                         const sl_vgrid* __restrict__ vgrid,
+                                                         const sl_part* __restrict__ parts,
+                                                         const sl_material* __restrict__ mats,
+                                                         const float* __restrict__ tree,
+                                                         const float* __restrict__ lamp_T,
+                                                         const float4* __restrict__ env_T,
+                                                         float4* __restrict__ colour, uint32_t count) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= count) return;
+  const sl_gaussian& G = gs[g];
+  const Leaf nd = load_leaf(&nodes[g]);
+  uint32_t mi = G.flags & 0xFFFFu;
+  const uint32_t mtop = (SH.material_count > 1u ? SH.material_count : 1u) - 1u;
+  mi = mi < mtop ? mi : mtop;
+  const sl_material mat = mats[mi];
+  const float* xf = parts[G.part_surface & 0xFFFFu].xf;
+  m3 Rq = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]);
+  m3 Sloc = m3m(m3m(Rq, m3diag(F3(mat.flake[0], mat.flake[1], mat.flake[2]))), m3t(Rq));
+  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
+  const float detC = s3 * s3;
+  const f3 P = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  const f3 n = Rq.c[0], t1 = Rq.c[1], t2 = Rq.c[2];
+  const f3 Sd = F3(Sloc.c[0].x, Sloc.c[1].y, Sloc.c[2].z), So = F3(Sloc.c[1].x, Sloc.c[2].x, Sloc.c[2].y);
+  const f3 flake = F3(mat.flake[0], mat.flake[1], mat.flake[2]);
+  const f3 alb = F3(G.albedo[0], G.albedo[1], G.albedo[2]);
+  const float ks = spec_weight(mat);
+  const bool emissive = (mat.flags & 1u) != 0u;
+  const f3 eye = ld3(SH.eye);
+  const sl_vgrid& vg = vgrid[g];
+  bool open = true;
+  {
+    const uint4* w4 = reinterpret_cast<const uint4*>(vg.w);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const uint4 q = w4[k];
+      open = open && (q.x & q.y & q.z & q.w) == 0xFFFFFFFFu;
+    }
+  }
+  f3 c = F3(0.0f, 0.0f, 0.0f);
+  if (SH.n_emit || emissive) {
+    const f3 wo0 = xf_dir_inv(xf, norm3(sub3(eye, P)));
+    f3 acc = F3(0.0f, 0.0f, 0.0f);
+    if (SH.n_emit) {
+      uint32_t stack[48];
+      uint32_t sp = 1;
+      stack[0] = SH.root;
+      const bool shape = SH.asg && ks > 0.0f;
+      while (sp > 0u) {
+        sp--;
+        const float* e = tree + 24u * stack[sp];
+        const uint32_t child_lo = __float_as_uint(e[11]), child_hi = __float_as_uint(e[15]);
+        const f3 emean = F3(e[0], e[1], e[2]);
+        bool use;
+        if (child_lo == kNone || SH.mode == 0u) {
+          use = child_lo == kNone;
+        } else {
+          f3 d = sub3(P, emean);
+          use = dot3(d, d) > SH.theta * SH.theta * e[3] * e[3];
+        }
+        if (!use) {
+          if (sp + 2u <= 48u) {
+            stack[sp] = child_lo;
+            stack[sp + 1u] = child_hi;
+            sp += 2u;
+          }
+          continue;
+        }
+        f3 d = sub3(emean, P);
+        float d2 = dot3(d, d);
+        if (d2 < 1e-8f) continue;
+        f3 ww = div3(d, sqrtf(d2));
+        f3 wi = xf_dir_inv(xf, ww);
+        float vi = vlook(vg, open, wi);
+        if (vi <= 1e-7f) continue;
+        float fp = footprint(nd, detC, wi);
+        f3 mw = mul3(ww, -1.0f);
+        float s = 1.0f;
+        if (SH.one_sided) {
+          float cs = dot3(mw, ld3(SH.normal));
+          s = SH.edge_soft > 0.0f ? smoothstepf(-SH.edge_soft, SH.edge_soft, cs) : (cs > 0.0f ? 1.0f : 0.0f);
+        }
+        float mq = sqrtf(fmaxf(dot3(mw, sym_mul(F3(e[4], e[5], e[6]), F3(e[8], e[9], e[10]), mw)), 0.0f));
+        f3 I = mul3(F3(e[12], e[13], e[14]), s * SH.scale * mq);
+        f3 light = mul3(mul3(I, vi), fp / d2 * 1.0f);
+        if (ks <= 0.0f) {
+          acc = add3(acc, light);
+          continue;
+        }
+        f3 wr = mirror3(wi, n);
+        float damp = iso_damp(nd.iso_norm, footprint(nd, detC, wr) * vlook(vg, open, wr));
+        if (shape) {
+          f3 bw0, bw1;
+          onb(ww, bw0, bw1);
+          f3 cd = F3(e[16], e[17], e[18]), co = F3(e[20], e[21], e[22]);
+          f3 cc0 = sym_mul(cd, co, bw0), cc1 = sym_mul(cd, co, bw1);
+          s2m slm{dot3(bw0, cc0) / d2, dot3(bw0, cc1) / d2, dot3(bw1, cc1) / d2};
+          f3 lb0 = xf_dir_inv(xf, bw0), lb1 = xf_dir_inv(xf, bw1);
+          float pp = asg_phase(wi, lb0, lb1, slm, n, t1, t2, flake, Sd, So, wo0);
+          acc = add3(acc, mul3(light, iso_lobe_from(ks, pp, damp)));
+          continue;
+        }
+        float lobe = iso_lobe_from(ks, phase_specular(Sd, So, wi, wo0), damp);
+        acc = add3(acc, mul3(light, lobe));
+      }
+    }
+    const float T = lamp_T[g];
+    c = mul3(mul3v(alb, acc), T * nd.iso_norm);
+    if (emissive && ((mat.flags & 4u) == 0u || dot3(wo0, n) > 0.0f))
+      c = add3(c, F3(half_lo(mat.pad0), half_hi(mat.pad0), half_lo(mat.pad1)));
+  }
+  if (SH.n_lights && !emissive) {
+    const float inorm = nd.iso_norm;
+    const float4 et = env_T[g];
+    const float Tk[4] = {et.x, et.y, et.z, et.w};
+    if (ks <= 0.0f) {
+      f3 dc = F3(0.0f, 0.0f, 0.0f);
+      for (uint32_t k = 0; k < SH.n_lights; k++) {
+        f3 wi = xf_dir_inv(xf, ld3(SH.lights[k].dir));
+        float v = vlook(vg, open, wi);
+        if (v <= 1e-7f) continue;
+        dc = add3(dc, mul3(ld3(SH.lights[k].irr), Tk[k] * v * footprint(nd, detC, wi)));
+      }
+      c = add3(c, mul3(mul3v(alb, dc), inorm));
+    } else {
+      f3 wo = xf_dir_inv(xf, norm3(sub3(eye, P)));
+      f3 diff = F3(0.0f, 0.0f, 0.0f), spec = F3(0.0f, 0.0f, 0.0f);
+      for (uint32_t k = 0; k < SH.n_lights; k++) {
+        f3 wi = xf_dir_inv(xf, ld3(SH.lights[k].dir));
+        float v = vlook(vg, open, wi);
+        if (v <= 1e-7f) continue;
+        f3 light = mul3(ld3(SH.lights[k].irr), Tk[k] * v * footprint(nd, detC, wi));
+        f3 wr = mirror3(wi, n);
+        float damp = iso_damp(inorm, footprint(nd, detC, wr) * vlook(vg, open, wr));
+        float s2 = SH.lights[k].std * SH.lights[k].std;
+        f3 ob0, ob1;
+        onb(wi, ob0, ob1);
+        float pp = asg_phase(wi, ob0, ob1, s2m{s2, 0.0f, s2}, n, t1, t2, flake, Sd, So, wo);
+        diff = add3(diff, mul3(light, 1.0f - ks));
+        spec = add3(spec, mul3(light, iso_lobe_from(ks, pp, damp) - (1.0f - ks)));
+      }
+      c = add3(c, mul3v(mul3(alb, inorm), add3(diff, spec)));
+    }
+  }
+  if (!emissive && SH.sky_ambient > 0.0f) c = add3(c, mul3(alb, SH.sky_ambient));
+  colour[g] = make_float4(c.x, c.y, c.z, 1.0f);
+}
+
+}  // namespace
+
+cudaError_t launch_shade(const ShadeParams& SH, const sl_gaussian* gs, const sl_node* nodes, const sl_vgrid* vgrid,
+                         const sl_part* parts, const sl_material* mats, const float* tree, const float* lamp_T,
+                         const float4* env_T, float4* colour, uint32_t count, cudaStream_t s) {
+  if (!count) return cudaSuccess;
+  shade_kernel<<<(count + kThreads - 1) / kThreads, kThreads, 0, s>>>(SH, gs, nodes, vgrid, parts, mats, tree, lamp_T,
+                                                                      env_T, colour, count);
+  return cudaGetLastError();
+}
+
+}  // namespace sl
