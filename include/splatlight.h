@@ -271,6 +271,61 @@ SL_API int sl_sort_keys16(const uint16_t* keys_dev, uint32_t n, uint32_t* order_
  * calls that overlap on the GPU (other streams, other threads) race, so serialise them. */
 SL_API int sl_sort_keys16_noalloc(const uint16_t* keys_dev, uint32_t n, uint32_t* order_dev, void* stream);
 
+/* ---- batched frames (no counterpart in the reference, which draws one RenderFrame per call) ------------------- */
+
+/* A ragged batch of views over several resident scenes (renderers), each view its own RenderFrame (camera,
+ * resolution, view mode), rendered by one chain of kernels: one projection launch over every view's slots, one
+ * shading launch (lit views, with their scene's lighting maps and the view's eye), one segmented depth sort (view id
+ * above the 16 depth bits), one tile binning, one tile sort, one compositor launch.  Every view's image, permutation,
+ * per-tile ranges and contributor counts equal what sl_render gives for that frame alone, with the same tile shape
+ * (the lit radiance: with the lighting's maps as of its last sl_lighting_update).  The chain runs as one CUDA graph,
+ * captured for the batch's capacity and replayed while batches fit. */
+typedef struct sl_batch sl_batch;
+
+typedef struct sl_batch_options {
+  uint32_t max_views;            /* views per batch (0 = 64; at most 256) */
+  uint32_t max_tiles;            /* tiles of all views (0 = grow on demand) */
+  uint64_t max_slots;            /* slots of all views, each view padded to 256 (0 = grow on demand) */
+  uint64_t max_entries;          /* tile entries of all views (0 = 2 per slot, grown on overflow) */
+  uint32_t tile_w, tile_h;       /* 16x16 (default), 8x32 or 32x8 */
+  uint32_t no_graph;             /* 1: launch the chain directly instead of replaying a graph */
+  uint32_t pad;
+} sl_batch_options;
+
+typedef struct sl_batch_stats {
+  uint32_t views, slots, tiles, entries; /* slots: padded total; entries: (tile, splat) pairs of all views */
+  uint64_t visible, fragments;
+  float ms_total;                /* device time of the chain when timing is on, else 0 */
+  uint32_t graph_replayed;       /* 1 when the chain ran as a replay of the captured graph */
+} sl_batch_stats;
+
+/* Creates a batch over n_scenes renderers (lightings[k]: the lighting bound to renderers[k], or NULL / a NULL array
+ * for unlit scenes; lit views of an unlit scene get radiance 0).  Capacities grow on demand (buffers reallocated,
+ * the graph re-captured). */
+SL_API int sl_batch_create(sl_renderer* const* renderers, sl_lighting* const* lightings, uint32_t n_scenes,
+                           const sl_batch_options* opt, sl_batch** out);
+SL_API int sl_batch_destroy(sl_batch* b);
+/* Tile shape for the following batches: 16x16, 8x32 or 32x8 (SL_ERR_INVALID_ARG otherwise). */
+SL_API int sl_batch_set_tile(sl_batch* b, uint32_t tile_w, uint32_t tile_h);
+SL_API int sl_batch_set_timing(sl_batch* b, int enabled);
+/* Renders n_views views: view v draws frames[v] of scene scene_of_view[v], eyes[3v..3v+2] its camera position (the
+ * lit radiance's view direction).  Images are packed in view order into out_dev (device, float RGBA, out_floats
+ * floats at least 4 x the sum of W x H); view_offsets[v] (optional, host) receives the first float of view v.  The
+ * call returns after the batch completed; stats (optional) describe it. */
+SL_API int sl_batch_render(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames,
+                           const float* eyes, uint32_t n_views, float* out_dev, uint64_t out_floats,
+                           uint64_t* view_offsets, sl_batch_stats* stats, void* stream);
+/* Debug read-back of view `view` of the last batch, in that view's own indices (as sl_renderer_read_debug):
+ * order (n slots), ranges (2 per tile), entries (the tile lists' slots, entries_cap at least *n_entries).  Any
+ * pointer may be NULL. */
+SL_API int sl_batch_read_view(sl_batch* b, uint32_t view, uint32_t* order, uint32_t* ranges, uint32_t* entries,
+                              uint64_t entries_cap, uint64_t* n_entries);
+/* Picks the fastest tile shape for this batch of views (renders it with each of 16x16, 8x32, 32x8, timed on the
+ * device, `reps` times each) and keeps it; writes the per-shape times (ms) to ms_out[3] if not NULL. */
+SL_API int sl_batch_autotune(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames,
+                             const float* eyes, uint32_t n_views, float* out_dev, uint64_t out_floats, uint32_t reps,
+                             uint32_t* tile_w, uint32_t* tile_h, float* ms_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

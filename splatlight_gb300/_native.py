@@ -35,6 +35,18 @@ class RenderOptions(C.Structure):
                 ("entry_capacity", C.c_uint32)]
 
 
+class BatchOptions(C.Structure):
+    _fields_ = [("max_views", C.c_uint32), ("max_tiles", C.c_uint32), ("max_slots", C.c_uint64),
+                ("max_entries", C.c_uint64), ("tile_w", C.c_uint32), ("tile_h", C.c_uint32),
+                ("no_graph", C.c_uint32), ("pad", C.c_uint32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("views", C.c_uint32), ("slots", C.c_uint32), ("tiles", C.c_uint32), ("entries", C.c_uint32),
+                ("visible", C.c_uint64), ("fragments", C.c_uint64), ("ms_total", C.c_float),
+                ("graph_replayed", C.c_uint32)]
+
+
 _P = C.c_void_p
 _U32 = C.c_uint32
 _U64 = C.c_uint64
@@ -66,6 +78,14 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_renderer_bind_lighting": (_I, [_P, _P]),
     "sl_sort_keys16": (_I, [_P, _U32, _P, _P]),
     "sl_sort_keys16_noalloc": (_I, [_P, _U32, _P, _P]),
+    "sl_batch_create": (_I, [_P, _P, _U32, C.POINTER(BatchOptions), C.POINTER(_P)]),
+    "sl_batch_destroy": (_I, [_P]),
+    "sl_batch_set_tile": (_I, [_P, _U32, _U32]),
+    "sl_batch_set_timing": (_I, [_P, _I]),
+    "sl_batch_render": (_I, [_P, _P, _P, _P, _U32, _P, _U64, _P, C.POINTER(BatchStats), _P]),
+    "sl_batch_read_view": (_I, [_P, _U32, _P, _P, _P, _U64, C.POINTER(_U64)]),
+    "sl_batch_autotune": (_I, [_P, _P, _P, _P, _U32, _P, _U64, _U32, C.POINTER(_U32), C.POINTER(_U32),
+                               _P, _P]),
 }
 
 _lib: C.CDLL | None = None

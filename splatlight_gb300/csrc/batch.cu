@@ -1,0 +1,116 @@
+// Batched tile binning: the per-view binning of tiles.cu over all views of a batch at once.  The depth-sorted
+// permutation covers every view's slots in view order (keys carry the view above the depth bits), so each visible
+// splat emits (global tile id, slot) entries with global tile id = the view's first tile + its local tile id; one
+// stable sort by that id leaves every tile's list contiguous and in back-to-front order.  Element counts are read
+// on the device (grids are sized for the batch's capacity, so a CUDA graph of the chain can be replayed for any
+// batch that fits).
+#include "sl_internal.h"
+
+namespace sl {
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ uint32_t rect_tiles(ushort4 r) {
+  return (r.x <= r.z && r.y <= r.w) ? (uint32_t)(r.z - r.x + 1) * (uint32_t)(r.w - r.y + 1) : 0u;
+}
+
+__global__ void __launch_bounds__(kThreads) btile_count_kernel(const uint32_t* __restrict__ order,
+                                                               const ushort4* __restrict__ rects,
+                                                               const uint32_t* __restrict__ totals, uint32_t n_max,
+                                                               uint32_t* __restrict__ counts) {
+  const uint32_t p = blockIdx.x * kThreads + threadIdx.x;
+  if (p >= n_max) return;
+  counts[p] = p < totals[0] ? rect_tiles(rects[order[p]]) : 0u;
+}
+
+__global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __restrict__ order,
+                                                              const ushort4* __restrict__ rects,
+                                                              const uint32_t* __restrict__ offsets,
+                                                              const BatchView* __restrict__ views,
+                                                              const uint32_t* __restrict__ block_view,
+                                                              const uint32_t* __restrict__ totals, uint32_t n_max,
+                                                              uint32_t capacity, FrameCounters* ctr,
+                                                              uint32_t* __restrict__ tile_keys,
+                                                              uint32_t* __restrict__ tile_vals,
+                                                              uint32_t* __restrict__ digit_hist) {
+  __shared__ uint32_t h[3][256];
+  const int t = threadIdx.x;
+  h[0][t] = 0u;
+  h[1][t] = 0u;
+  h[2][t] = 0u;
+  __syncthreads();
+  const uint32_t p = blockIdx.x * kThreads + t;
+  if (p < n_max && p < totals[0]) {
+    const uint32_t slot = order[p];
+    const ushort4 r = rects[slot];
+    if (r.x <= r.z && r.y <= r.w) {
+      uint32_t e = offsets[p];
+      const uint32_t cnt = rect_tiles(r);
+      if (e + cnt > capacity) {
+        atomicExch(&ctr->overflow, 1u);
+      } else {
+        const uint32_t v = block_view[slot >> 8];
+        const uint32_t base = views[v].tile_base, tiles_x = views[v].tiles_x;
+        for (uint32_t ty = r.y; ty <= r.w; ty++) {
+          const uint32_t row = base + ty * tiles_x;
+          for (uint32_t tx = r.x; tx <= r.z; tx++) {
+            const uint32_t tile = row + tx;
+            tile_keys[e] = tile;
+            tile_vals[e] = slot;
+            e++;
+            atomicAdd(&h[0][tile & 0xffu], 1u);
+            atomicAdd(&h[1][(tile >> 8) & 0xffu], 1u);
+            atomicAdd(&h[2][(tile >> 16) & 0xffu], 1u);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int q = 0; q < 3; q++)
+    if (h[q][t]) atomicAdd(&digit_hist[256 * q + t], h[q][t]);
+}
+
+__global__ void __launch_bounds__(kThreads) btile_runs_kernel(const uint32_t* __restrict__ keys,
+                                                              const uint32_t* __restrict__ n_dev, uint32_t n_max,
+                                                              uint32_t* __restrict__ run_start,
+                                                              uint32_t* __restrict__ run_end) {
+  const uint32_t nd = *n_dev;
+  const uint32_t n = nd <= n_max ? nd : 0u;
+  for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const uint32_t k = keys[i];
+    if (i == 0 || keys[i - 1] != k) run_start[k] = i;
+    if (i + 1 == n || keys[i + 1] != k) run_end[k] = i + 1;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_btile_count(const uint32_t* order, const ushort4* rects, const uint32_t* totals, uint32_t n_max,
+                               uint32_t* counts, cudaStream_t s) {
+  if (!n_max) return cudaSuccess;
+  btile_count_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, totals, n_max, counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const uint32_t* offsets,
+                              const BatchView* views, const uint32_t* block_view, const uint32_t* totals,
+                              uint32_t n_max, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
+                              uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s) {
+  if (!n_max) return cudaSuccess;
+  btile_emit_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(
+      order, rects, offsets, views, block_view, totals, n_max, capacity, ctr, tile_keys, tile_vals, digit_hist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_btile_runs(const uint32_t* keys, const uint32_t* n_dev, uint32_t n_max, uint32_t* run_start,
+                              uint32_t* run_end, cudaStream_t s) {
+  if (!n_max) return cudaSuccess;
+  uint32_t blocks = (n_max + kThreads * 8 - 1) / (kThreads * 8);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  btile_runs_kernel<<<blocks, kThreads, 0, s>>>(keys, n_dev, n_max, run_start, run_end);
+  return cudaGetLastError();
+}
+
+}  // namespace sl

@@ -11,36 +11,6 @@
 #include "sl_lighting.h"
 #include "sl_runtime.h"
 
-struct sl_lighting {
-  sl_renderer* r = nullptr;
-  int device = 0;
-  uint32_t count = 0, material_count = 0;
-  sl::DevBuf nodes, vgrid, materials, parts, tree, lamp_T, env_T, colour;
-  bool iso_done = false;
-  // emitters (src/lighting.js:612-721, EmitParams :657-673)
-  std::vector<float> rec;
-  uint32_t n_emit = 0, root = 0, one_sided = 0, skip_part = 0xFFFFFFFFu;
-  float scale = 1.0f, normal[3] = {0.0f, 0.0f, 1.0f}, edge_soft = 0.2f;
-  double root_cov[6] = {0, 0, 0, 0, 0, 0};
-  // options
-  uint32_t shadow_res = 512, sun_res = 512, mode = 1;
-  float theta = 4.0f;
-  uint32_t asg = 1;
-  // environment (src/environment.js:111-153)
-  std::vector<sl_env_light> lights;
-  float sky_ambient = 0.0f;
-  // light map A
-  sl::DevBuf lm_acc, lm_mip;
-  sl::LightMapParams LP{};
-  bool lm_dirty = true;
-  // sun maps
-  sl::DevBuf sm_acc, sm_mip, sm_layers, sm_dirty;
-  sl::SunParams SP{};
-  std::vector<sl::SunLayer> layers;
-  std::vector<int> have_center;
-  bool sm_dirty_all = true;
-  bool lamp_filled = false, env_filled = false;
-};
 
 namespace sl {
 namespace {
@@ -315,6 +285,38 @@ void basis_k32(const float* w, float* t1, float* t2) {
 }
 
 }  // namespace
+}  // namespace sl
+
+namespace sl {
+
+void shade_params(const sl_lighting* l, const float* eye, ShadeParams& SH) {
+  memset(&SH, 0, sizeof(SH));
+  for (int k = 0; k < 3; k++) {
+    SH.eye[k] = eye ? eye[k] : 0.0f;
+    SH.normal[k] = l->normal[k];
+  }
+  SH.n_emit = l->n_emit;
+  SH.root = l->root;
+  SH.mode = l->mode;
+  SH.asg = l->asg;
+  SH.one_sided = l->one_sided;
+  SH.material_count = l->material_count;
+  SH.scale = l->scale;
+  SH.theta = l->theta;
+  SH.edge_soft = l->edge_soft;
+  SH.sky_ambient = l->sky_ambient;
+  const uint32_t K = (uint32_t)std::min<size_t>(l->lights.size(), 4);
+  SH.n_lights = K;
+  for (uint32_t k = 0; k < K; k++) {
+    for (int c = 0; c < 3; c++) {
+      SH.lights[k].dir[c] = l->lights[k].dir[c];
+      SH.lights[k].irr[c] = l->lights[k].irradiance[c];
+    }
+    SH.lights[k].std = l->lights[k].std;
+    SH.lights[k].shadows = l->lights[k].casts_shadows ? 1u : 0u;
+  }
+}
+
 }  // namespace sl
 
 using namespace sl;
@@ -656,30 +658,7 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
 
   // shade (emissive.wgsl shade_emit + environment.wgsl env_direct + the constant sky ambient)
   ShadeParams SH;
-  memset(&SH, 0, sizeof(SH));
-  for (int k = 0; k < 3; k++) {
-    SH.eye[k] = eye[k];
-    SH.normal[k] = l->normal[k];
-  }
-  SH.n_emit = l->n_emit;
-  SH.root = l->root;
-  SH.mode = l->mode;
-  SH.asg = l->asg;
-  SH.one_sided = l->one_sided;
-  SH.material_count = l->material_count;
-  SH.scale = l->scale;
-  SH.theta = l->theta;
-  SH.edge_soft = l->edge_soft;
-  SH.sky_ambient = l->sky_ambient;
-  SH.n_lights = K;
-  for (uint32_t k = 0; k < K; k++) {
-    for (int c = 0; c < 3; c++) {
-      SH.lights[k].dir[c] = l->lights[k].dir[c];
-      SH.lights[k].irr[c] = l->lights[k].irradiance[c];
-    }
-    SH.lights[k].std = l->lights[k].std;
-    SH.lights[k].shadows = l->lights[k].casts_shadows ? 1u : 0u;
-  }
+  shade_params(l, eye, SH);
   SL_CHECK_CUDA(launch_shade(SH, gs, l->nodes.as<sl_node>(), l->vgrid.as<sl_vgrid>(), parts, l->materials.as<sl_material>(),
                              l->tree.as<float>(), l->lamp_T.as<float>(), l->env_T.as<float4>(), l->colour.as<float4>(), G, s),
                 "shade");

@@ -64,12 +64,13 @@ __device__ __forceinline__ float ex2_approx(float x) {
   return y;
 }
 
+// One tile: (x0, y0) its origin in a width x height image, [s, e) its range in tile_vals, out/counts the image.
 template <int TW>
-__global__ void __launch_bounds__(kThreads) composite_kernel(const CompositeParams P, const uint2* __restrict__ ranges,
-                                                             const uint32_t* __restrict__ tile_vals,
-                                                             const SplatRec* __restrict__ recs,
-                                                             FrameCounters* ctr, float4* __restrict__ out,
-                                                             uint32_t* __restrict__ counts) {
+__device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_t width, uint32_t height, uint32_t s,
+                                               uint32_t e, const uint32_t* __restrict__ tile_vals,
+                                               const SplatRec* __restrict__ recs, uint32_t count_mode, float t_stop,
+                                               FrameCounters* ctr, float4* __restrict__ out,
+                                               uint32_t* __restrict__ counts) {
   constexpr int TH = kThreads / TW;
   constexpr int BX = TW / 8;  // warp blocks of 8 x 4 pixels per tile row
   constexpr int BY = TH / 4;
@@ -79,12 +80,9 @@ __global__ void __launch_bounds__(kThreads) composite_kernel(const CompositePara
   __shared__ __align__(8) uint64_t bars[2];
 
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  const uint32_t tile = blockIdx.x;
-  const uint32_t tx = tile % P.tiles_x, ty = tile / P.tiles_x;
-  const uint32_t x0 = tx * TW, y0 = ty * TH;  // tile origin, pixels
   const uint32_t px = x0 + (uint32_t)((w % BX) * 8 + (lane & 7));
   const uint32_t py = y0 + (uint32_t)((w / BX) * 4 + (lane >> 3));
-  const bool inside = px < P.width && py < P.height;
+  const bool inside = px < width && py < height;
 
   const uint32_t bar0 = smem_addr(&bars[0]), bar1 = smem_addr(&bars[1]);
   if (t == 0) {
@@ -94,11 +92,7 @@ __global__ void __launch_bounds__(kThreads) composite_kernel(const CompositePara
   }
   __syncthreads();
 
-  const uint2 rg = ranges[tile];
-  const uint32_t s = rg.x, e = rg.y;
   const uint32_t n_batches = (e - s + kThreads - 1) / kThreads;
-  const float maxrad = fmaxf(__uint_as_float(ctr->max_rad_bits), 1.0f);
-  const float t_stop = P.count_mode ? -1.0f : P.t_stop_scale / maxrad;
   const float pxc = (float)px + 0.5f, pyc = (float)py + 0.5f;
   const float fx0 = (float)x0, fy0 = (float)y0;
   const float kNegHalfLog2e = -0.72134752044448170f;
@@ -199,14 +193,58 @@ __global__ void __launch_bounds__(kThreads) composite_kernel(const CompositePara
   const uint32_t wk = __reduce_add_sync(0xffffffffu, kept);
   if (lane == 0 && wk) atomicAdd(&ctr->fragments, wk);
   if (inside) {
-    const size_t pix = (size_t)py * P.width + px;
-    if (P.count_mode) {
+    const size_t pix = (size_t)py * width + px;
+    if (count_mode) {
       out[pix] = make_float4((float)kept, 0.0f, 0.0f, 0.0f);
       if (counts) counts[pix] = kept;
     } else {
       out[pix] = make_float4(cr, cg, cb, 1.0f - T);
     }
   }
+}
+
+
+template <int TW>
+__global__ void __launch_bounds__(kThreads) composite_kernel(const CompositeParams P, const uint2* __restrict__ ranges,
+                                                             const uint32_t* __restrict__ tile_vals,
+                                                             const SplatRec* __restrict__ recs,
+                                                             FrameCounters* ctr, float4* __restrict__ out,
+                                                             uint32_t* __restrict__ counts) {
+  constexpr int TH = kThreads / TW;
+  const uint32_t tile = blockIdx.x;
+  const uint32_t tx = tile % P.tiles_x, ty = tile / P.tiles_x;
+  const uint2 rg = ranges[tile];
+  const float maxrad = fmaxf(__uint_as_float(ctr->max_rad_bits), 1.0f);
+  const float t_stop = P.count_mode ? -1.0f : P.t_stop_scale / maxrad;
+  composite_tile<TW>(tx * TW, ty * TH, P.width, P.height, rg.x, rg.y, tile_vals, recs, P.count_mode, t_stop, ctr, out,
+                     counts);
+}
+
+// Batched: one CTA per tile of any view; the view comes from a binary search of the tiles' prefix over views.
+template <int TW>
+__global__ void __launch_bounds__(kThreads) bcomposite_kernel(const BatchComposite B, const uint2* __restrict__ ranges,
+                                                              const uint32_t* __restrict__ tile_vals,
+                                                              const SplatRec* __restrict__ recs,
+                                                              const BatchViewOut* __restrict__ views,
+                                                              const uint32_t* __restrict__ view_maxrad,
+                                                              const BatchDyn* __restrict__ dyn, FrameCounters* ctr) {
+  constexpr int TH = kThreads / TW;
+  const uint32_t tile = blockIdx.x;
+  if (tile >= dyn->total_tiles) return;  // grid sized for the capacity
+  float4* out = dyn->out;
+  uint32_t lo = 0, hi = dyn->n_views;  // the last view whose tile_base <= tile
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (views[mid].tile_base <= tile) lo = mid; else hi = mid;
+  }
+  const BatchViewOut v = views[lo];
+  const uint32_t lt = tile - v.tile_base;
+  const uint32_t tx = lt % v.tiles_x, ty = lt / v.tiles_x;
+  const uint2 rg = ranges[tile];
+  const float maxrad = fmaxf(__uint_as_float(view_maxrad[lo]), 1.0f);
+  const float t_stop = v.count_mode ? -1.0f : B.t_stop_scale / maxrad;
+  composite_tile<TW>(tx * TW, ty * TH, v.width, v.height, rg.x, rg.y, tile_vals, recs, v.count_mode, t_stop, ctr,
+                     out + v.out_offset, nullptr);
 }
 
 }  // namespace
@@ -233,4 +271,26 @@ cudaError_t launch_composite(const CompositeParams& P, const uint2* ranges, cons
   return cudaGetLastError();
 }
 
+}  // namespace sl
+
+namespace sl {
+cudaError_t launch_bcomposite(const BatchComposite& B, const uint2* ranges, const uint32_t* tile_vals,
+                              const SplatRec* recs, const BatchViewOut* views, const uint32_t* view_maxrad,
+                              const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s) {
+  if (max_tiles == 0) return cudaSuccess;
+  switch (B.tile_w) {
+    case 16:
+      bcomposite_kernel<16><<<max_tiles, kThreads, 0, s>>>(B, ranges, tile_vals, recs, views, view_maxrad, dyn, ctr);
+      break;
+    case 8:
+      bcomposite_kernel<8><<<max_tiles, kThreads, 0, s>>>(B, ranges, tile_vals, recs, views, view_maxrad, dyn, ctr);
+      break;
+    case 32:
+      bcomposite_kernel<32><<<max_tiles, kThreads, 0, s>>>(B, ranges, tile_vals, recs, views, view_maxrad, dyn, ctr);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
 }  // namespace sl

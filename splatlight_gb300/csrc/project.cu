@@ -48,26 +48,13 @@ __device__ __forceinline__ float clampf(float x, float lo, float hi) { return fm
 
 constexpr int kThreads = 256;
 
-__global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant__ ProjectParams P,
-                                                           const float4* __restrict__ gaussians,
-                                                           const float4* __restrict__ emitters,
-                                                           const float4* __restrict__ colour,
-                                                           const float4* __restrict__ lo_b, uint16_t* __restrict__ key16,
-                                                           SplatRec* __restrict__ recs, ushort4* __restrict__ rects,
-                                                           uint32_t* __restrict__ digit_hist, FrameCounters* ctr) {
-  __shared__ uint32_t h_lo[256], h_hi[256];
-  __shared__ uint32_t s_visible;
-  __shared__ uint32_t s_maxrad;
-  const int t = threadIdx.x;
-  h_lo[t] = 0u;
-  h_hi[t] = 0u;
-  if (t == 0) {
-    s_visible = 0u;
-    s_maxrad = 0u;
-  }
-  __syncthreads();
-
-  const uint32_t i = blockIdx.x * kThreads + t;
+// One slot i of project.wgsl main (:84-370, plain path): key (kInvalidKey16 when culled), tile rectangle and the
+// largest radiance component; the splat record goes to *rec_out.  colour / lo_b may be null (radiance 0, filled in
+// later by the batched shading pass).
+__device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i, const float4* __restrict__ gaussians,
+                                             const float4* __restrict__ emitters, const float4* __restrict__ colour,
+                                             const float4* __restrict__ lo_b, SplatRec* rec_out, uint32_t& key_out,
+                                             ushort4& rect_out, float& maxrad_out) {
   uint32_t key = kInvalidKey16;
   ushort4 rect = make_ushort4(1, 1, 0, 0);
   float maxrad = 0.0f;
@@ -243,7 +230,7 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
           __half2 hxy = __halves2half2(__float2half_ru(hx), __float2half_ru(hy));
           rec.b = make_float4(a1x * r / n1, -(a1y * r / n1), *reinterpret_cast<float*>(&hxy), qcut);
           rec.c = make_float4(cr, cg, cb, tau0);
-          recs[i] = rec;
+          *rec_out = rec;
           maxrad = fmaxf(fmaxf(cr, cg), fmaxf(cb, 0.0f));
           float xl = fmaxf(cx - hx - 0.5f, -1.0f), xh = fminf(cx + hx - 0.5f, Wf);
           float yl = fmaxf(cy - hy - 0.5f, -1.0f), yh = fminf(cy + hy - 0.5f, Hf);
@@ -261,6 +248,35 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
     }
   }
 
+  key_out = key;
+  rect_out = rect;
+  maxrad_out = maxrad;
+}
+
+__global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant__ ProjectParams P,
+                                                           const float4* __restrict__ gaussians,
+                                                           const float4* __restrict__ emitters,
+                                                           const float4* __restrict__ colour,
+                                                           const float4* __restrict__ lo_b, uint16_t* __restrict__ key16,
+                                                           SplatRec* __restrict__ recs, ushort4* __restrict__ rects,
+                                                           uint32_t* __restrict__ digit_hist, FrameCounters* ctr) {
+  __shared__ uint32_t h_lo[256], h_hi[256];
+  __shared__ uint32_t s_visible;
+  __shared__ uint32_t s_maxrad;
+  const int t = threadIdx.x;
+  h_lo[t] = 0u;
+  h_hi[t] = 0u;
+  if (t == 0) {
+    s_visible = 0u;
+    s_maxrad = 0u;
+  }
+  __syncthreads();
+
+  const uint32_t i = blockIdx.x * kThreads + t;
+  uint32_t key;
+  ushort4 rect;
+  float maxrad;
+  project_slot(P, i, gaussians, emitters, colour, lo_b, recs + i, key, rect, maxrad);
   if (i < P.n_slots) {
     key16[i] = (uint16_t)key;
     rects[i] = rect;
@@ -280,7 +296,70 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
   }
 }
 
+// Batched: one block of 256 slots of one view; the view comes from block_view (kNoView: padding past the batch).
+// Keys carry the view above the 16 depth bits, so one stable sort orders every view's slots exactly as the per-view
+// sort does; lit radiance is filled in by the batched shading pass.
+__global__ void __launch_bounds__(kThreads) bproject_kernel(const BatchView* __restrict__ views,
+                                                            const uint32_t* __restrict__ block_view,
+                                                            uint32_t* __restrict__ keys32, SplatRec* __restrict__ recs,
+                                                            ushort4* __restrict__ rects, uint32_t* __restrict__ digit_hist,
+                                                            uint32_t* __restrict__ view_maxrad,
+                                                            uint32_t* __restrict__ view_visible) {
+  __shared__ ProjectParams sP;
+  __shared__ uint32_t h[3][256];
+  __shared__ uint32_t s_visible, s_maxrad;
+  const uint32_t v = block_view[blockIdx.x];
+  if (v == kNoView) return;
+  const int t = threadIdx.x;
+  const BatchView& V = views[v];
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&V.P);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&sP);
+    for (uint32_t k = t; k < sizeof(ProjectParams) / 4; k += kThreads) dst[k] = src[k];
+  }
+  h[0][t] = 0u;
+  h[1][t] = 0u;
+  h[2][t] = 0u;
+  if (t == 0) {
+    s_visible = 0u;
+    s_maxrad = 0u;
+  }
+  __syncthreads();
+  const uint32_t i = (blockIdx.x - V.block_first) * kThreads + t;
+  const uint32_t gslot = V.slot_base + i;
+  uint32_t key;
+  ushort4 rect;
+  float maxrad;
+  project_slot(sP, i, V.gaussians, V.emitters, V.colour, V.lo_b, recs + gslot, key, rect, maxrad);
+  const uint32_t key32 = (v << 16) | key;
+  keys32[gslot] = key32;
+  rects[gslot] = rect;
+  atomicAdd(&h[0][key32 & 0xffu], 1u);
+  atomicAdd(&h[1][(key32 >> 8) & 0xffu], 1u);
+  atomicAdd(&h[2][(key32 >> 16) & 0xffu], 1u);
+  if (key != kInvalidKey16) {
+    atomicAdd(&s_visible, 1u);
+    atomicMax(&s_maxrad, __float_as_uint(maxrad));
+  }
+  __syncthreads();
+  for (int p = 0; p < 3; p++)
+    if (h[p][t]) atomicAdd(&digit_hist[256 * p + t], h[p][t]);
+  if (t == 0) {
+    if (s_visible) atomicAdd(&view_visible[v], s_visible);
+    if (s_maxrad) atomicMax(&view_maxrad[v], s_maxrad);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_bproject(const BatchView* views, const uint32_t* block_view, uint32_t max_blocks, uint32_t* keys32,
+                            SplatRec* recs, ushort4* rects, uint32_t* digit_hist, uint32_t* view_maxrad,
+                            uint32_t* view_visible, cudaStream_t s) {
+  if (max_blocks == 0) return cudaSuccess;
+  bproject_kernel<<<max_blocks, kThreads, 0, s>>>(views, block_view, keys32, recs, rects, digit_hist, view_maxrad,
+                                                  view_visible);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_project(const ProjectParams& P, const sl_gaussian* gaussians, const sl_gaussian* emitters,
                            const float4* colour, const float4* lo_b, uint16_t* key16, SplatRec* recs,

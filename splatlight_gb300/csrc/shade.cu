@@ -18,18 +18,12 @@ __device__ __forceinline__ f3 ld3(const float* p) { return F3(p[0], p[1], p[2]);
 
 __device__ __forceinline__ float vlook(const sl_vgrid& v, bool open, f3 w) { return open ? 1.0f : vgrid_lookup(v, w); }
 
-__global__ void __launch_bounds__(kThreads) shade_kernel(const __grid_constant__ ShadeParams SH,
-                                                         const sl_gaussian* __restrict__ gs,
-                                                         const sl_node* __restrict__ nodes,
-                                                         const sl_vgrid* __restrict__ vgrid,
-                                                         const sl_part* __restrict__ parts,
-                                                         const sl_material* __restrict__ mats,
-                                                         const float* __restrict__ tree,
-                                                         const float* __restrict__ lamp_T,
-                                                         const float4* __restrict__ env_T,
-                                                         float4* __restrict__ colour, uint32_t count) {
-  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
-  if (g >= count) return;
+// Radiance of Gaussian g seen from SH.eye (shade_leaf + env_add), rgb.
+__device__ __forceinline__ f3 shade_one(const ShadeParams& SH, const sl_gaussian* __restrict__ gs,
+                                        const sl_node* __restrict__ nodes, const sl_vgrid* __restrict__ vgrid,
+                                        const sl_part* __restrict__ parts, const sl_material* __restrict__ mats,
+                                        const float* __restrict__ tree, const float* __restrict__ lamp_T,
+                                        const float4* __restrict__ env_T, uint32_t g) {
   const sl_gaussian& G = gs[g];
   const Leaf nd = load_leaf(&nodes[g]);
   uint32_t mi = G.flags & 0xFFFFu;
@@ -165,10 +159,93 @@ __global__ void __launch_bounds__(kThreads) shade_kernel(const __grid_constant__
     }
   }
   if (!emissive && SH.sky_ambient > 0.0f) c = add3(c, mul3(alb, SH.sky_ambient));
+  return c;
+}
+
+__global__ void __launch_bounds__(kThreads) shade_kernel(const __grid_constant__ ShadeParams SH,
+                                                         const sl_gaussian* __restrict__ gs,
+                                                         const sl_node* __restrict__ nodes,
+                                                         const sl_vgrid* __restrict__ vgrid,
+                                                         const sl_part* __restrict__ parts,
+                                                         const sl_material* __restrict__ mats,
+                                                         const float* __restrict__ tree,
+                                                         const float* __restrict__ lamp_T,
+                                                         const float4* __restrict__ env_T,
+                                                         float4* __restrict__ colour, uint32_t count) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= count) return;
+  const f3 c = shade_one(SH, gs, nodes, vgrid, parts, mats, tree, lamp_T, env_T, g);
   colour[g] = make_float4(c.x, c.y, c.z, 1.0f);
 }
 
+// Batched: the visible scene Gaussians of every lit view, shaded from the view's eye, with the palette and albedo
+// scale the projection applies to bound radiance (project.wgsl:424-453), written into the splat records.
+__global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __restrict__ views,
+                                                          const BatchScene* __restrict__ scenes,
+                                                          const uint32_t* __restrict__ block_view,
+                                                          const uint32_t* __restrict__ keys32,
+                                                          SplatRec* __restrict__ recs,
+                                                          uint32_t* __restrict__ view_maxrad) {
+  __shared__ ShadeParams sSH;
+  __shared__ uint32_t s_max;
+  const uint32_t v = block_view[blockIdx.x / 2];
+  if (v == kNoView) return;
+  const BatchView& V = views[v];
+  const BatchScene& S = scenes[V.scene];
+  if (V.P.view_mode != 3u || !S.lit) return;
+  const int t = threadIdx.x;
+  if (t == 0) {
+    sSH = S.SH;
+    sSH.eye[0] = V.eye[0];
+    sSH.eye[1] = V.eye[1];
+    sSH.eye[2] = V.eye[2];
+    s_max = 0u;
+  }
+  __syncthreads();
+  const uint32_t i = (blockIdx.x / 2 - V.block_first) * 256u + (blockIdx.x & 1u) * kThreads + t;
+  const uint32_t gslot = V.slot_base + i;
+  float mx = 0.0f;
+  uint32_t material = kEmitterMaterial;
+  if (i < V.P.count && (keys32[gslot] & 0xFFFFu) != 0xFFFFu) {
+    const sl_gaussian& G = reinterpret_cast<const sl_gaussian*>(V.gaussians)[i];
+    uint32_t part = G.part_surface & 0xffffu;
+    part = part > kMaxParts - 1u ? kMaxParts - 1u : part;
+    material = V.P.parts[part].material;
+  }
+  if (material != kEmitterMaterial) {  // emissive materials keep their albedo as radiance (the projection's rule)
+    const f3 c = shade_one(sSH, reinterpret_cast<const sl_gaussian*>(V.gaussians), S.nodes, S.vgrid, S.parts, S.mats,
+                           S.tree, S.lamp_T, S.env_T, i);
+    // no bounce buffer on the batched path: radiance = shaded colour x palette x albedo scale
+    float cr = c.x, cg = c.y, cb = c.z;
+    if (material < 8u) {
+      cr *= V.P.palette[material][0];
+      cg *= V.P.palette[material][1];
+      cb *= V.P.palette[material][2];
+    }
+    cr *= V.P.albedo_scale;
+    cg *= V.P.albedo_scale;
+    cb *= V.P.albedo_scale;
+    float4 cc = recs[gslot].c;
+    cc.x = cr;
+    cc.y = cg;
+    cc.z = cb;
+    recs[gslot].c = cc;
+    mx = fmaxf(fmaxf(cr, cg), fmaxf(cb, 0.0f));
+  }
+  if (mx > 0.0f) atomicMax(&s_max, __float_as_uint(mx));
+  __syncthreads();
+  if (t == 0 && s_max) atomicMax(&view_maxrad[v], s_max);
+}
+
 }  // namespace
+
+cudaError_t launch_bshade(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
+                          uint32_t max_blocks, const uint32_t* keys32, SplatRec* recs, uint32_t* view_maxrad,
+                          cudaStream_t s) {
+  if (max_blocks == 0) return cudaSuccess;
+  bshade_kernel<<<2 * max_blocks, kThreads, 0, s>>>(views, scenes, block_view, keys32, recs, view_maxrad);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_shade(const ShadeParams& SH, const sl_gaussian* gs, const sl_node* nodes, const sl_vgrid* vgrid,
                          const sl_part* parts, const sl_material* mats, const float* tree, const float* lamp_T,

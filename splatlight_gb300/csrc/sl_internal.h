@@ -79,6 +79,11 @@ size_t sort_tiles_for(uint32_t n);
 cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals_out, uint32_t n,
                          const uint32_t* n_dev, int bits, const uint32_t* digit_hist, SortScratch& sc,
                          FrameCounters* ctr, cudaStream_t s, uint16_t* keys_out = nullptr);
+// The same for 32-bit keys (up to 4 passes); status holds 256 words per tile and pass, tile_ctr 4 counters.
+cudaError_t sort32_pairs(uint32_t* keys, uint32_t* keys_alt, const uint32_t* vals_in, uint32_t* vals_out,
+                         uint32_t* vals_alt, uint32_t n, const uint32_t* n_dev, int bits, const uint32_t* digit_hist,
+                         uint32_t* status, uint32_t* tile_ctr, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s,
+                         uint32_t* keys_out = nullptr);
 // Counts the digit histograms of u16 keys (used when no producer kernel filled them).
 cudaError_t launch_digit_hist16(const uint16_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s);
 
@@ -111,5 +116,57 @@ struct CompositeParams {
 cudaError_t launch_composite(const CompositeParams& P, const uint2* ranges, const uint32_t* tile_vals,
                              const SplatRec* recs, FrameCounters* ctr, float4* out, uint32_t* counts,
                              cudaStream_t s);
+
+// ---- batched path ---------------------------------------------------------------------------------------------
+
+// One view of a batch as the projection and shading read it (device array).
+struct BatchView {
+  ProjectParams P;                       // the view's RenderFrame, packed as for the per-view path
+  const float4* gaussians;               // its scene's records
+  const float4* emitters;
+  const float4* colour;                  // bound radiance of a scene without lighting (else null: the shading pass)
+  const float4* lo_b;
+  uint32_t scene;                        // index into the batch's scenes
+  uint32_t slot_base;                    // first global slot (a multiple of 256)
+  uint32_t block_first;                  // slot_base / 256
+  uint32_t tile_base, tiles_x;           // first global tile, tiles per row
+  float eye[3];                          // shading eye
+};
+constexpr uint32_t kNoView = 0xFFFFFFFFu;
+cudaError_t launch_bproject(const BatchView* views, const uint32_t* block_view, uint32_t max_blocks, uint32_t* keys32,
+                            SplatRec* recs, ushort4* rects, uint32_t* digit_hist /*[3][256]*/,
+                            uint32_t* view_maxrad, uint32_t* view_visible, cudaStream_t s);
+
+// What the batched compositor needs of each view (device array, ascending tile_base).
+struct BatchViewOut {
+  uint32_t tile_base, tiles_x, width, height;
+  uint32_t count_mode, pad0;
+  uint64_t out_offset;  // first float4 of the view's image in the packed output
+};
+struct BatchComposite {
+  uint32_t tile_w, tile_h;
+  float t_stop_scale;
+  uint32_t pad;
+};
+// Per-batch values the captured chain reads from device memory (uploaded before every launch).
+struct BatchDyn {
+  uint32_t total_slots;   // padded slots of all views
+  uint32_t total_tiles;
+  uint32_t n_views;
+  uint32_t total_blocks;
+  float4* out;            // packed images
+};
+cudaError_t launch_bcomposite(const BatchComposite& B, const uint2* ranges, const uint32_t* tile_vals,
+                              const SplatRec* recs, const BatchViewOut* views, const uint32_t* view_maxrad,
+                              const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s);
+// batch.cu (totals: the BatchDyn, read as u32 words: [0] total slots, [1] total tiles)
+cudaError_t launch_btile_count(const uint32_t* order, const ushort4* rects, const uint32_t* totals, uint32_t n_max,
+                               uint32_t* counts, cudaStream_t s);
+cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const uint32_t* offsets,
+                              const BatchView* views, const uint32_t* block_view, const uint32_t* totals,
+                              uint32_t n_max, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
+                              uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s);
+cudaError_t launch_btile_runs(const uint32_t* keys, const uint32_t* n_dev, uint32_t n_max, uint32_t* run_start,
+                              uint32_t* run_end, cudaStream_t s);
 
 }  // namespace sl

@@ -44,6 +44,22 @@ struct ShadeParams {
   EnvLightDev lights[4];
 };
 
+// One scene's lighting as the batched shading pass reads it.
+struct BatchScene {
+  const sl_node* nodes;
+  const sl_vgrid* vgrid;
+  const sl_part* parts;
+  const sl_material* mats;
+  const float* tree;
+  const float* lamp_T;
+  const float4* env_T;
+  ShadeParams SH;   // eye replaced per view
+  uint32_t lit;     // 0: no lighting bound (radiance 0, as an unbound colour buffer)
+};
+cudaError_t launch_bshade(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
+                          uint32_t max_blocks, const uint32_t* keys32, SplatRec* recs, uint32_t* view_maxrad,
+                          cudaStream_t s);
+
 cudaError_t upload_iso_dirs(const float* dirs128x4, cudaStream_t s);
 cudaError_t launch_iso(const sl_gaussian* gs, sl_node* nodes, const sl_vgrid* vgrid, uint32_t count, cudaStream_t s);
 cudaError_t launch_lsm_splat(const LightMapParams& L, const sl_gaussian* gs, const sl_node* nodes,

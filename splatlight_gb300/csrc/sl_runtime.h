@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "sl_internal.h"
+#include "sl_lighting.h"
 
 namespace sl {
 
@@ -78,3 +79,40 @@ struct sl_renderer {
   uint32_t last_slots = 0, last_w = 0, last_h = 0, last_tiles = 0, last_entries = 0, last_mode = 0;
   bool have_frame = false;
 };
+
+// Host state of a Lighting object (capi_lighting.cu).
+struct sl_lighting {
+  sl_renderer* r = nullptr;
+  int device = 0;
+  uint32_t count = 0, material_count = 0;
+  sl::DevBuf nodes, vgrid, materials, parts, tree, lamp_T, env_T, colour;
+  bool iso_done = false;
+  // emitters (src/lighting.js:612-721, EmitParams :657-673)
+  std::vector<float> rec;
+  uint32_t n_emit = 0, root = 0, one_sided = 0, skip_part = 0xFFFFFFFFu;
+  float scale = 1.0f, normal[3] = {0.0f, 0.0f, 1.0f}, edge_soft = 0.2f;
+  double root_cov[6] = {0, 0, 0, 0, 0, 0};
+  // options
+  uint32_t shadow_res = 512, sun_res = 512, mode = 1;
+  float theta = 4.0f;
+  uint32_t asg = 1;
+  // environment (src/environment.js:111-153)
+  std::vector<sl_env_light> lights;
+  float sky_ambient = 0.0f;
+  // light map A
+  sl::DevBuf lm_acc, lm_mip;
+  sl::LightMapParams LP{};
+  bool lm_dirty = true;
+  // sun maps
+  sl::DevBuf sm_acc, sm_mip, sm_layers, sm_dirty;
+  sl::SunParams SP{};
+  std::vector<sl::SunLayer> layers;
+  std::vector<int> have_center;
+  bool sm_dirty_all = true;
+  bool lamp_filled = false, env_filled = false;
+};
+
+namespace sl {
+// ShadeParams of a lighting object seen from `eye` (capi_lighting.cu)
+void shade_params(const sl_lighting* l, const float* eye, ShadeParams& SH);
+}  // namespace sl

@@ -1,4 +1,4 @@
-// Stable LSD radix sort of 16-bit keys with 32-bit values, onesweep style (one read and one write of the keys and
+// Stable LSD radix sort of 16- or 32-bit keys with 32-bit values, onesweep style (one read and one write of the keys and
 // values per 8-bit digit pass, Adinets & Merrill 2022): the digit histograms of every pass are counted up front (by
 // the producer kernel, or launch_digit_hist16), then each pass is a single kernel over tiles of 4096 keys that
 //   1. ranks its keys per warp with __match_any_sync (peers holding the same digit) and a per-warp digit counter, so
@@ -58,9 +58,10 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
   return base + x - v;
 }
 
-__global__ void __launch_bounds__(kThreads) onesweep_pass(const uint16_t* __restrict__ keys_in,
+template <typename KeyT>
+__global__ void __launch_bounds__(kThreads) onesweep_pass(const KeyT* __restrict__ keys_in,
                                                           const uint32_t* __restrict__ vals_in,
-                                                          uint16_t* __restrict__ keys_out,
+                                                          KeyT* __restrict__ keys_out,
                                                           uint32_t* __restrict__ vals_out, uint32_t n_max,
                                                           const uint32_t* __restrict__ n_dev, int shift,
                                                           const uint32_t* __restrict__ digit_hist,
@@ -70,7 +71,7 @@ __global__ void __launch_bounds__(kThreads) onesweep_pass(const uint16_t* __rest
   __shared__ uint32_t digit_base[256];
   __shared__ uint32_t local_start[256];
   __shared__ uint32_t warp_tot[kWarps];
-  __shared__ uint16_t s_keys[kTile];
+  __shared__ KeyT s_keys[kTile];
   __shared__ uint32_t s_vals[kTile];
 
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(kThreads) onesweep_pass(const uint16_t* __rest
   for (int it = 0; it < kItems; it++) {
     uint32_t idx = wbase + (uint32_t)it * 32u;
     bool valid = idx < n;
-    keys[it] = valid ? (uint32_t)keys_in[idx] : 0xffffu;
+    keys[it] = valid ? (uint32_t)keys_in[idx] : 0xffffffffu;
     vals[it] = valid ? (vals_in ? vals_in[idx] : idx) : 0u;
   }
   const uint32_t lt = lanemask_lt();
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(kThreads) onesweep_pass(const uint16_t* __rest
     if (idx < n) {
       uint32_t d = (keys[it] >> shift) & 0xffu;
       uint32_t pos = local_start[d] + warp_hist[w][d] + ranks[it];
-      s_keys[pos] = (uint16_t)keys[it];
+      s_keys[pos] = (KeyT)keys[it];
       s_vals[pos] = vals[it];
     }
   }
@@ -181,7 +182,7 @@ __global__ void __launch_bounds__(kThreads) onesweep_pass(const uint16_t* __rest
     uint32_t d = (key >> shift) & 0xffu;
     uint32_t dst = digit_base[d] + (j - local_start[d]);
     if (dst >= n) continue;  // only after a look-back timeout (reported); never write out of range
-    if (keys_out) keys_out[dst] = (uint16_t)key;
+    if (keys_out) keys_out[dst] = (KeyT)key;
     vals_out[dst] = s_vals[j];
   }
 }
@@ -215,36 +216,66 @@ cudaError_t launch_digit_hist16(const uint16_t* keys, uint32_t n, int passes, ui
   return cudaGetLastError();
 }
 
-cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals_out, uint32_t n,
-                         const uint32_t* n_dev, int bits, const uint32_t* digit_hist, SortScratch& sc,
-                         FrameCounters* ctr, cudaStream_t s, uint16_t* keys_out) {
+namespace {
+
+// LSD passes over the low `bits` key bits, 8 per pass.  Keys ping-pong between `keys` (clobbered) and keys_alt;
+// values land in vals_out after the last pass (through vals_alt when that is needed to avoid reading and writing one
+// buffer in the same pass); keys_out, if given, receives the sorted keys.
+template <typename KeyT>
+cudaError_t sort_pairs(KeyT* keys, KeyT* keys_alt, const uint32_t* vals_in, uint32_t* vals_out, uint32_t* vals_alt,
+                       uint32_t n, const uint32_t* n_dev, int bits, const uint32_t* digit_hist, uint32_t* status,
+                       uint32_t* tile_ctr, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s, KeyT* keys_out) {
   if (n == 0) return cudaSuccess;
   if (n > kValueMask) return cudaErrorInvalidValue;
   const uint32_t tiles = (uint32_t)sort_tiles_for(n);
-  if (tiles > sc.max_tiles) return cudaErrorInvalidValue;
-  const int passes = bits <= 8 ? 1 : 2;
-  cudaError_t e = cudaMemsetAsync(sc.status, 0, sizeof(uint32_t) * 256u * tiles * (size_t)passes, s);
+  if (tiles > max_tiles) return cudaErrorInvalidValue;
+  const int passes = bits <= 8 ? 1 : (bits + 7) / 8;
+  if (passes > 4) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(status, 0, sizeof(uint32_t) * 256u * tiles * (size_t)passes, s);
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(sc.tile_ctr, 0, sizeof(uint32_t) * 2, s);
+  e = cudaMemsetAsync(tile_ctr, 0, sizeof(uint32_t) * 4, s);
   if (e != cudaSuccess) return e;
-  if (passes == 1) {
-    uint32_t* out = (vals_in == vals_out) ? sc.vals_alt : vals_out;
-    uint16_t* kout = (keys_out == keys) ? sc.keys_alt : keys_out;
-    onesweep_pass<<<tiles, kThreads, 0, s>>>(keys, vals_in, kout, out, n, n_dev, 0, digit_hist, sc.status,
-                                             sc.tile_ctr, ctr);
-    e = cudaGetLastError();
-    if (e == cudaSuccess && out != vals_out)
-      e = cudaMemcpyAsync(vals_out, out, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
-    if (e == cudaSuccess && kout && kout != keys_out)
-      e = cudaMemcpyAsync(keys_out, kout, sizeof(uint16_t) * n, cudaMemcpyDeviceToDevice, s);
-    return e;
+  // value buffers per pass: the last pass writes vals_out; earlier ones alternate so no pass reads what it writes
+  uint32_t* vdst[4];
+  for (int p = 0; p < passes; p++) vdst[p] = ((passes - 1 - p) % 2 == 0) ? vals_out : vals_alt;
+  bool copy_back = false;
+  if (vals_in && vals_in == vdst[0]) {  // the first pass would overwrite its own input: shift by one buffer
+    for (int p = 0; p < passes; p++) vdst[p] = (vdst[p] == vals_out) ? vals_alt : vals_out;
+    copy_back = true;  // the result then sits in vals_alt
   }
-  onesweep_pass<<<tiles, kThreads, 0, s>>>(keys, vals_in, sc.keys_alt, sc.vals_alt, n, n_dev, 0, digit_hist,
-                                           sc.status, sc.tile_ctr, ctr);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  onesweep_pass<<<tiles, kThreads, 0, s>>>(sc.keys_alt, sc.vals_alt, keys_out, vals_out, n, n_dev, 8,
-                                           digit_hist + 256, sc.status + (size_t)256u * tiles, sc.tile_ctr + 1, ctr);
-  return cudaGetLastError();
+  const KeyT* kin = keys;
+  const uint32_t* vin = vals_in;
+  for (int p = 0; p < passes; p++) {
+    const bool last = p == passes - 1;
+    KeyT* kdst = last ? keys_out : ((p % 2 == 0) ? keys_alt : keys);
+    if (last && keys_out && keys_out == kin) kdst = (kin == keys) ? keys_alt : keys;  // never write what is read
+    onesweep_pass<KeyT><<<tiles, kThreads, 0, s>>>(kin, vin, kdst, vdst[p], n, n_dev, 8 * p, digit_hist + 256 * p,
+                                                   status + (size_t)256u * tiles * p, tile_ctr + p, ctr);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (last && keys_out && kdst != keys_out)
+      if ((e = cudaMemcpyAsync(keys_out, kdst, sizeof(KeyT) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess) return e;
+    kin = kdst ? kdst : kin;
+    vin = vdst[p];
+  }
+  if (copy_back) e = cudaMemcpyAsync(vals_out, vals_alt, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
+  return e;
+}
+
+}  // namespace
+
+cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals_out, uint32_t n,
+                         const uint32_t* n_dev, int bits, const uint32_t* digit_hist, SortScratch& sc,
+                         FrameCounters* ctr, cudaStream_t s, uint16_t* keys_out) {
+  return sort_pairs<uint16_t>(keys, sc.keys_alt, vals_in, vals_out, sc.vals_alt, n, n_dev, bits, digit_hist,
+                              sc.status, sc.tile_ctr, sc.max_tiles, ctr, s, keys_out);
+}
+
+cudaError_t sort32_pairs(uint32_t* keys, uint32_t* keys_alt, const uint32_t* vals_in, uint32_t* vals_out,
+                         uint32_t* vals_alt, uint32_t n, const uint32_t* n_dev, int bits, const uint32_t* digit_hist,
+                         uint32_t* status, uint32_t* tile_ctr, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s,
+                         uint32_t* keys_out) {
+  return sort_pairs<uint32_t>(keys, keys_alt, vals_in, vals_out, vals_alt, n, n_dev, bits, digit_hist, status,
+                              tile_ctr, max_tiles, ctr, s, keys_out);
 }
 
 }  // namespace sl

@@ -1,0 +1,187 @@
+"""The batched path (sl_batch_*): a ragged batch of views over several resident scenes equals, view by view, the
+per-view path (itself pinned to the CPU restatement by test_gpu_parity_plain / test_gpu_lighting): the stable
+permutation, the per-tile ranges and lists bit-exact, the images identical; a view alone and in a mix of others give
+the same result; the captured graph replays for later batches that fit; capacities grow on demand."""
+import numpy as np
+import pytest
+
+from splatlight_gb300 import camera, scene
+from splatlight_gb300.batch import BatchRenderer, View
+from splatlight_gb300.lighting import camera_forward, for_scene
+from splatlight_gb300.renderer import SplatRenderer
+from splatlight_gb300.structs import VIEW_DEPTH, VIEW_FLAT, VIEW_LIT, VIEW_OVERDRAW
+
+pytestmark = pytest.mark.gpu
+
+RGB_TOL = 1e-3
+
+
+def _frame(s, W, H, mode, eye=None, target=None):
+    return camera.make_frame(s.eye if eye is None else eye, s.target if target is None else target, s.up, s.fov_deg,
+                             W, H, s.count, far=s.far, view_mode=mode, n_emit=len(s.emitters))
+
+
+def _plain(r, f, tile):
+    r.set_options(tile_w=tile[0], tile_h=tile[1])
+    img = r.render(f)
+    return img, r.read_debug()
+
+
+def _assert_view(B, k, view, r, tile, exact=True):
+    f = np.asarray(view.frame).reshape(())
+    img_b = view._img
+    img_p, dbg = _plain(r, f, tile)
+    order, ranges, entries = B.read_view(k, r.last_stats.slots, r.last_stats.tiles)
+    assert np.array_equal(order, dbg["order"]), k
+    assert np.array_equal(ranges, dbg["ranges"]), k
+    assert np.array_equal(entries, dbg["entries"]), k
+    if exact:
+        assert np.array_equal(img_b, img_p), (k, float(np.abs(img_b - img_p).max()))
+    else:
+        assert float(np.abs(img_b - img_p).max()) <= RGB_TOL
+
+
+def _scenes():
+    a = scene.subset(scene.cornell(), 20000)
+    b = scene.subset(scene.hill(), 60000)
+    return a, b
+
+
+def _views(a, b):
+    """A ragged mix: two scenes, five resolutions, three view modes, several cameras."""
+    hill_eye = lambda yaw, pitch, rad: camera.orbit_eye((0.0, 0.0, 1.0), rad, yaw, pitch)
+    vs = [
+        View(0, _frame(a, 160, 120, VIEW_FLAT), a.eye),
+        View(1, _frame(b, 320, 180, VIEW_FLAT, eye=hill_eye(0.3, 0.4, 12.0), target=(0, 0, 1)), hill_eye(0.3, 0.4, 12.0)),
+        View(0, _frame(a, 97, 61, VIEW_OVERDRAW, eye=(0.4, 0.2, 3.2)), (0.4, 0.2, 3.2)),
+        View(1, _frame(b, 255, 257, VIEW_DEPTH, eye=hill_eye(2.0, 0.15, 6.0), target=(0, 0, 1)), hill_eye(2.0, 0.15, 6.0)),
+        View(1, _frame(b, 480, 270, VIEW_OVERDRAW, eye=hill_eye(4.0, 0.9, 20.0), target=(0, 0, 1)), hill_eye(4.0, 0.9, 20.0)),
+        View(0, _frame(a, 33, 200, VIEW_FLAT, eye=(-0.5, 0.3, 2.5)), (-0.5, 0.3, 2.5)),
+    ]
+    return vs
+
+
+def _render(B, views):
+    imgs = B.render(views)
+    for v, im in zip(views, imgs):
+        v._img = im
+    return imgs
+
+
+@pytest.mark.parametrize("tile", [(16, 16), (8, 32), (32, 8)])
+def test_ragged_mix_equals_per_view(cuda, tile):
+    a, b = _scenes()
+    with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
+        ra.set_emitters(a.emitters)
+        rb.set_emitters(b.emitters)
+        with BatchRenderer([ra, rb], max_views=16, tile=tile) as B:
+            views = _views(a, b)
+            _render(B, views)
+            assert B.last_stats.views == len(views)
+            for k, v in enumerate(views):
+                _assert_view(B, k, v, [ra, rb][v.scene], tile)
+
+
+def test_alone_and_in_mix(cuda):
+    a, b = _scenes()
+    with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
+        ra.set_emitters(a.emitters)
+        rb.set_emitters(b.emitters)
+        with BatchRenderer([ra, rb], max_views=16) as B:
+            views = _views(a, b)
+            mix = [im.copy() for im in _render(B, views)]
+            for k, v in enumerate(views):
+                alone = B.render([v])[0]
+                assert np.array_equal(alone, mix[k]), k
+            # reversed order: every view still the same
+            rev = B.render(views[::-1])
+            for k, im in enumerate(rev[::-1]):
+                assert np.array_equal(im, mix[k]), k
+
+
+def test_graph_replay_and_growth(cuda):
+    a, b = _scenes()
+    with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
+        ra.set_emitters(a.emitters)
+        rb.set_emitters(b.emitters)
+        # tiny capacities: the first batch grows slots, tiles and (through the overflow retry) tile entries
+        with BatchRenderer([ra, rb], max_views=8, max_slots=256, max_tiles=8, max_entries=64) as B:
+            views = _views(a, b)[:4]
+            first = [im.copy() for im in _render(B, views)]
+            for k, v in enumerate(views):
+                _assert_view(B, k, v, [ra, rb][v.scene], (16, 16))
+            again = B.render(views)
+            assert B.last_stats.graph_replayed == 1
+            for x, y in zip(first, again):
+                assert np.array_equal(x, y)
+            fewer = views[1:3]
+            _render(B, fewer)
+            assert B.last_stats.graph_replayed == 1
+            for k, v in enumerate(fewer):
+                _assert_view(B, k, v, [ra, rb][v.scene], (16, 16))
+
+
+def test_no_graph_matches_graph(cuda):
+    a, b = _scenes()
+    with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
+        ra.set_emitters(a.emitters)
+        rb.set_emitters(b.emitters)
+        views = _views(a, b)
+        with BatchRenderer([ra, rb], graph=True) as B1, BatchRenderer([ra, rb], graph=False) as B2:
+            x = [im.copy() for im in B1.render(views)]
+            y = B2.render(views)
+            for p, q in zip(x, y):
+                assert np.array_equal(p, q)
+
+
+def test_lit_views_two_scenes(cuda):
+    """Lit views: each scene's lighting updated at that view's camera; the batched shading pass gives the same
+    radiance as the lighting's own pass (RGB within 1e-3; ordering and lists exact)."""
+    a, b = _scenes()
+    b = scene.dataclasses.replace(b, shadow_res=256, sun_res=512)
+    with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
+        La = for_scene(ra, a)
+        Lb = for_scene(rb, b)
+        La.update(a.eye, camera_forward(a))
+        Lb.update(b.eye, camera_forward(b))
+        views = [View(0, _frame(a, 200, 150, VIEW_LIT), a.eye),
+                 View(1, _frame(b, 320, 180, VIEW_LIT), b.eye),
+                 View(0, _frame(a, 64, 64, VIEW_FLAT, eye=(0.2, 0.1, 3.0)), (0.2, 0.1, 3.0)),
+                 View(1, _frame(b, 160, 90, VIEW_LIT), b.eye)]
+        with BatchRenderer([ra, rb], [La, Lb]) as B:
+            _render(B, views)
+            for k, v in enumerate(views):
+                _assert_view(B, k, v, [ra, rb][v.scene], (16, 16), exact=False)
+        La.close()
+        Lb.close()
+
+
+def test_autotune_keeps_results(cuda):
+    a, b = _scenes()
+    with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
+        ra.set_emitters(a.emitters)
+        rb.set_emitters(b.emitters)
+        views = _views(a, b)
+        with BatchRenderer([ra, rb]) as B:
+            tile, ms = B.autotune(views, reps=2)
+            assert tile in ((16, 16), (8, 32), (32, 8))
+            assert all(t > 0 for t in ms.values())
+            _render(B, views)
+            for k, v in enumerate(views):
+                _assert_view(B, k, v, [ra, rb][v.scene], tile)
+
+
+def test_bad_arguments(cuda):
+    a, _ = _scenes()
+    from splatlight_gb300._native import SplatlightError
+    with SplatRenderer(a.gaussians, a.parts) as ra:
+        ra.set_emitters(a.emitters)
+        with BatchRenderer([ra], max_views=2) as B:
+            v = View(0, _frame(a, 64, 64, VIEW_FLAT), a.eye)
+            with pytest.raises(SplatlightError):
+                B.render([v, v, v])                    # more than max_views
+            with pytest.raises(SplatlightError):
+                B.render([View(3, v.frame, a.eye)])    # no such scene
+            with pytest.raises(SplatlightError):
+                B.set_tile(16, 8)
+            assert np.isfinite(B.render([v])[0]).all()
