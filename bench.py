@@ -132,6 +132,122 @@ def cpu_cache(s, threads):
     return lamp_t, env_t, nodes
 
 
+MIX_RES = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
+
+
+def batch_mix(n_views=64, seed=7):
+    """The ragged batch workload: 4 scenes (cornell-like 100k and 400k Gaussians, seed 0; hill-like 1M and 2M, seed
+    1), n_views views round-robin over them, each with a resolution drawn from MIX_RES and a camera on a sphere of
+    radius U[3, 6] around the scene centre looking at it, lit view."""
+    from splatlight_gb300 import camera, scene
+    scenes = [scene.cornell(100_000, seed=0), scene.cornell(400_000, seed=0), scene.hill(1_048_576, seed=1),
+              scene.hill(2_097_152, seed=1)]
+    rng = np.random.default_rng(seed)
+    views = []
+    for v in range(n_views):
+        k = v % len(scenes)
+        s = scenes[k]
+        W, H = MIX_RES[int(rng.integers(len(MIX_RES)))]
+        up = np.asarray(s.up, np.float64)
+        while True:
+            d = rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            if abs(float(d @ up)) < 0.95:
+                break
+        c = np.asarray(s.target, np.float64)
+        eye = c + rng.uniform(3.0, 6.0) * d
+        f = camera.make_frame(tuple(eye), tuple(c), s.up, s.fov_deg, W, H, s.count, far=s.far, view_mode=3,
+                              n_emit=len(s.emitters))
+        views.append((k, f, tuple(np.float32(eye))))
+    return scenes, views
+
+
+def run_batch(args, stream, flush):
+    """Batched path vs the plain per-view path on the ragged 64-view mix (device time, L2 flushed between steps)."""
+    import torch
+    from splatlight_gb300.batch import BatchRenderer, View
+    from splatlight_gb300.lighting import camera_forward, for_scene
+    from splatlight_gb300.renderer import SplatRenderer
+    scenes, mix = batch_mix()
+    rs, ls = [], []
+    for s in scenes:
+        r = SplatRenderer(s.gaussians, s.parts)
+        L = for_scene(r, s)
+        L.update(s.eye, camera_forward(s))   # the resident light state: maps at the scene's reference camera
+        rs.append(r)
+        ls.append(L)
+    torch.cuda.synchronize()
+    views = [View(k, f, e) for k, f, e in mix]
+    sizes = [(int(f["viewport"][1]), int(f["viewport"][0])) for _, f, _ in mix]
+    pix = sum(h * w for h, w in sizes)
+    B = BatchRenderer(rs, ls, max_views=len(views))
+    out = torch.empty(4 * pix, dtype=torch.float32, device="cuda")
+    tile, tune_ms = B.autotune(views, reps=2)
+    sc = stream.cuda_stream
+
+    def batched():
+        return B.render_device(views, out=out, stream=sc)
+
+    plain_out = [torch.empty((h, w, 4), dtype=torch.float32, device="cuda") for h, w in sizes]
+
+    def plain():
+        for (k, f, e), o in zip(mix, plain_out):
+            ls[k].shade(e, stream=sc)
+            rs[k].render(f, out=o, stream=sc)
+
+    def timed(fn, steps):
+        ts = []
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.median(ts)
+
+    for _ in range(max(args.warmup, 3)):
+        batched()
+        plain()
+    torch.cuda.synchronize()
+    steps = max(3, min(args.steps, 10))
+    ms_b = timed(batched, steps)
+    st = B.last_stats
+    ms_p = timed(plain, steps)
+    # image error of every batched view against the plain per-view path (same light state)
+    _, offs = batched()
+    torch.cuda.synchronize()
+    err = 0.0
+    for (h, w), o, po in zip(sizes, offs, plain_out):
+        img = out[int(o):int(o) + 4 * h * w].view(h, w, 4)
+        err = max(err, float((img - po).abs().max().item()))
+    n = len(views)
+    res = {"workload": f"{n} lit views over 4 resident scenes (cornell-like 100k, 400k; hill-like 1M, 2M "
+                       "Gaussians), resolutions from 256^2, 512^2, 1280x720, 1920x1080, cameras on radius U[3,6] "
+                       "spheres; light maps resident per scene",
+           "views": n, "pixels": pix, "batched_views_per_s": round(n * 1000.0 / ms_b, 2),
+           "batched_ms_per_batch": round(ms_b, 3),
+           "plain_views_per_s": round(n * 1000.0 / ms_p, 2), "plain_ms_per_batch": round(ms_p, 3),
+           "speedup_vs_plain": round(ms_p / ms_b, 3), "max_abs_err_vs_plain": err,
+           "tile": f"{tile[0]}x{tile[1]}", "autotune_ms": {k: round(v, 3) for k, v in tune_ms.items()},
+           "slots": int(st.slots), "visible": int(st.visible), "entries": int(st.entries),
+           "graph_replayed": int(st.graph_replayed), "kernels_per_batch": BATCH_KERNELS}
+    B.close()
+    for L in ls:
+        L.close()
+    for r in rs:
+        r.close()
+    return res
+
+
+# bproject, bshade, 3 depth-sort passes, tile counts, scan, emit, 3 tile-sort passes, runs, run counts, scan, ranges,
+# bcomposite
+BATCH_KERNELS = 17
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -166,6 +282,7 @@ def main():
     ap.add_argument("--config", default="hill", choices=["hill", "cornell"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the ragged-batch leg")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -304,6 +421,10 @@ def main():
     dominant = max(stage_ms, key=stage_ms.get)
     roofline = roof_comp if dominant == "composite" else roof_sort
 
+    batch = None
+    if not args.no_batch:
+        batch = run_batch(args, stream, flush)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -323,7 +444,7 @@ def main():
                 "gpu_launches": KERNELS_PER_FRAME * args.steps,
                 "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
                 "roofline": roofline, "sort_roofline": roof_sort, "composite_roofline": roof_comp,
-                "cpu_baseline": cpu, "clocks": clocks}
+                "cpu_baseline": cpu, "clocks": clocks, "batched": batch}
         print(json.dumps(line))
     L.close()
     r.close()

@@ -246,6 +246,10 @@ SL_API int sl_lighting_set_options(sl_lighting* l, uint32_t shadow_res, uint32_t
 SL_API int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, uint32_t moved_mask,
                               void* stream);
 
+/* The shading pass alone at a new eye, with the opacity maps and cut as the last sl_lighting_update left them (the
+ * per-frame shade_emit + env_direct dispatches of src/lighting.js when no layer is dirty).  Needs a prior update. */
+SL_API int sl_lighting_shade(sl_lighting* l, const float* eye, void* stream);
+
 /* Debug read-back (host buffers, any may be NULL): radiance float4 per Gaussian, the emitter shadow T per Gaussian
  * (lamp_state slot 0), the distant-light T float4 per Gaussian (env_T), the leaf nodes with iso_norm. */
 SL_API int sl_lighting_read(sl_lighting* l, float* colour, float* lamp_T, float* env_T, sl_node* nodes);

@@ -74,6 +74,7 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_lighting_set_environment": (_I, [_P, _P, _U32, C.c_float]),
     "sl_lighting_set_options": (_I, [_P, _U32, _U32, _U32, C.c_float, _I]),
     "sl_lighting_update": (_I, [_P, _P, _P, _U32, _P]),
+    "sl_lighting_shade": (_I, [_P, _P, _P]),
     "sl_lighting_read": (_I, [_P, _P, _P, _P, _P]),
     "sl_renderer_bind_lighting": (_I, [_P, _P]),
     "sl_sort_keys16": (_I, [_P, _U32, _P, _P]),

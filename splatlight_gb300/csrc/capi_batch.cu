@@ -281,6 +281,7 @@ void stage(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* fr
       S.tree = l->tree.as<float>();
       S.lamp_T = l->lamp_T.as<float>();
       S.env_T = l->env_T.as<float4>();
+      S.order = l->order.as<uint32_t>();
       shade_params(l, nullptr, S.SH);
       S.lit = l->iso_done ? 1u : 0u;  // maps exist after the lighting's first update
     }

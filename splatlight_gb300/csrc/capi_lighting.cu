@@ -289,6 +289,68 @@ void basis_k32(const float* w, float* t1, float* t2) {
 
 namespace sl {
 
+// Skip links for a stackless walk of the light cut (the GPU shading pass).  The cut is the walk of a 48-entry stack
+// that pushes (lo, hi) and so pops hi first: node order = preorder with the hi subtree before the lo one.  Per node,
+// word 7 = the node that walk reaches once this node's subtree is done (its skip); word 19 = 1 when the stack would
+// be full there (depth of pending lo siblings + 2 > 48), where the stack walk neither uses nor refines the node.
+constexpr uint32_t kNoChild = 0xFFFFFFFFu;
+
+void link_tree(std::vector<float>& out, uint32_t node, uint32_t skip, uint32_t pending) {
+  for (;;) {
+    float* f = &out[24u * node];
+    memcpy(&f[7], &skip, 4);
+    const uint32_t full = pending + 2u > 48u ? 1u : 0u;
+    memcpy(&f[19], &full, 4);
+    uint32_t lo, hi;
+    memcpy(&lo, &f[11], 4);
+    memcpy(&hi, &f[15], 4);
+    if (lo == kNoChild) return;
+    link_tree(out, hi, lo, pending + 1u);  // hi first; lo is pending meanwhile
+    node = lo;                              // then lo, which ends where this node ends
+  }
+}
+
+// Shading order: the Gaussians sorted by a 30-bit Morton code of their model-space means over the scene's bounds,
+// so a warp's threads shade nearby points whose light cuts agree (less divergence in the cut walk).
+cudaError_t build_shade_order(sl_lighting* l) {
+  const uint32_t G = l->count;
+  std::vector<sl_gaussian> g(G);
+  cudaError_t e = cudaMemcpy(g.data(), l->r->gaussians.ptr, sizeof(sl_gaussian) * (size_t)G, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return e;
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (const sl_gaussian& x : g)
+    for (int k = 0; k < 3; k++)
+      if (std::isfinite(x.mu[k])) {
+        lo[k] = std::min(lo[k], x.mu[k]);
+        hi[k] = std::max(hi[k], x.mu[k]);
+      }
+  auto spread = [](uint32_t v) {  // 10 bits -> every third bit
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+  };
+  std::vector<uint64_t> key(G);
+  for (uint32_t i = 0; i < G; i++) {
+    uint32_t q[3];
+    for (int k = 0; k < 3; k++) {
+      const float span = hi[k] > lo[k] ? hi[k] - lo[k] : 1.0f;
+      float t = std::isfinite(g[i].mu[k]) ? (g[i].mu[k] - lo[k]) / span : 0.0f;
+      t = std::min(std::max(t, 0.0f), 1.0f);
+      q[k] = (uint32_t)(t * 1023.0f);
+    }
+    const uint32_t m = spread(q[0]) | (spread(q[1]) << 1) | (spread(q[2]) << 2);
+    key[i] = ((uint64_t)m << 32) | i;
+  }
+  std::sort(key.begin(), key.end());
+  std::vector<uint32_t> order(G);
+  for (uint32_t i = 0; i < G; i++) order[i] = (uint32_t)key[i];
+  if ((e = l->order.ensure(4ull * G + 16)) != cudaSuccess) return e;
+  return cudaMemcpy(l->order.ptr, order.data(), 4ull * G, cudaMemcpyHostToDevice);
+}
+
 void shade_params(const sl_lighting* l, const float* eye, ShadeParams& SH) {
   memset(&SH, 0, sizeof(SH));
   for (int k = 0; k < 3; k++) {
@@ -352,6 +414,7 @@ int sl_lighting_create(sl_renderer* r, const sl_node* nodes, const sl_vgrid* vgr
   if (e == cudaSuccess) e = l->env_T.ensure(16ull * r->count);
   if (e == cudaSuccess) e = l->colour.ensure(16ull * r->count);
   if (e == cudaSuccess) e = l->tree.ensure(4 * 24);
+  if (e == cudaSuccess) e = build_shade_order(l);
   if (e != cudaSuccess) {
     delete l;
     return cuda_fail(e, "sl_lighting_create");
@@ -369,7 +432,7 @@ int sl_lighting_destroy(sl_lighting* l) {
     l->r->colour = nullptr;
   }
   sl::DevBuf* all[] = {&l->nodes, &l->vgrid, &l->materials, &l->parts, &l->tree, &l->lamp_T, &l->env_T, &l->colour,
-                       &l->lm_acc, &l->lm_mip, &l->sm_acc, &l->sm_mip, &l->sm_layers, &l->sm_dirty};
+                       &l->lm_acc, &l->lm_mip, &l->sm_acc, &l->sm_mip, &l->sm_layers, &l->sm_dirty, &l->order};
   for (sl::DevBuf* b : all) b->release();
   delete l;
   return SL_OK;
@@ -401,6 +464,7 @@ int sl_lighting_set_emitters(sl_lighting* l, const sl_gaussian* emitters, uint32
     std::iota(idx.begin(), idx.end(), 0u);
     l->root = B.build(idx);
     for (int j = 0; j < 6; j++) l->root_cov[j] = (double)(float)B.info[l->root].Cs[j];
+    link_tree(B.out, l->root, kNoChild, 0);
     SL_CHECK_CUDA(l->tree.ensure(B.out.size() * 4), "emitter tree");
     SL_CHECK_CUDA(cudaMemcpy(l->tree.ptr, B.out.data(), B.out.size() * 4, cudaMemcpyHostToDevice), "emitter tree");
   }
@@ -660,7 +724,23 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
   ShadeParams SH;
   shade_params(l, eye, SH);
   SL_CHECK_CUDA(launch_shade(SH, gs, l->nodes.as<sl_node>(), l->vgrid.as<sl_vgrid>(), parts, l->materials.as<sl_material>(),
-                             l->tree.as<float>(), l->lamp_T.as<float>(), l->env_T.as<float4>(), l->colour.as<float4>(), G, s),
+                             l->tree.as<float>(), l->lamp_T.as<float>(), l->env_T.as<float4>(), l->order.as<uint32_t>(),
+                             l->colour.as<float4>(), G, s),
+                "shade");
+  return SL_OK;
+}
+
+int sl_lighting_shade(sl_lighting* l, const float* eye, void* stream) {
+  if (!l || !eye) return fail(SL_ERR_INVALID_ARG, "null argument");
+  if (!l->iso_done) return fail(SL_ERR_INVALID_ARG, "shade needs a prior sl_lighting_update (maps, iso_norm)");
+  cudaSetDevice(l->device);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  ShadeParams SH;
+  shade_params(l, eye, SH);
+  SL_CHECK_CUDA(launch_shade(SH, l->r->gaussians.as<sl_gaussian>(), l->nodes.as<sl_node>(), l->vgrid.as<sl_vgrid>(),
+                             l->parts.as<sl_part>(), l->materials.as<sl_material>(), l->tree.as<float>(),
+                             l->lamp_T.as<float>(), l->env_T.as<float4>(), l->order.as<uint32_t>(),
+                             l->colour.as<float4>(), l->count, s),
                 "shade");
   return SL_OK;
 }

@@ -12,6 +12,23 @@
 namespace sl {
 namespace lm {
 
+// Transcendentals: the deterministic shared definitions by default (the opacity-map kernels must match the CPU
+// restatement bit for bit); a translation unit that defines SL_FAST_SHADE (the shading pass, whose output is
+// continuous in its inputs and checked to a tolerance) uses the hardware approximations instead.
+#ifdef SL_FAST_SHADE
+__device__ __forceinline__ float lm_exp(float x) { return __expf(x); }
+__device__ __forceinline__ float lm_log(float x) { return __logf(x); }
+__device__ __forceinline__ float lm_acos(float x) { return acosf(x); }
+__device__ __forceinline__ float lm_asin(float x) { return asinf(x); }
+__device__ __forceinline__ float lm_atan2(float y, float x) { return atan2f(y, x); }
+#else
+__device__ __forceinline__ float lm_exp(float x) { return sl_expf(x); }
+__device__ __forceinline__ float lm_log(float x) { return sl_logf(x); }
+__device__ __forceinline__ float lm_acos(float x) { return sl_acosf(x); }
+__device__ __forceinline__ float lm_asin(float x) { return sl_asinf(x); }
+__device__ __forceinline__ float lm_atan2(float y, float x) { return sl_atan2f(y, x); }
+#endif
+
 constexpr float kPi = 3.14159265358979f;
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 
@@ -127,7 +144,7 @@ __device__ __forceinline__ float erfc_pos(float z) {
                       t * (0.09678418f +
                            t * (-0.18628806f +
                                 t * (0.27886807f + t * (-1.13520398f + t * (1.48851587f + t * (-0.82215223f + t * 0.17087277f))))))));
-  return t * sl_expf(p);
+  return t * lm_exp(p);
 }
 __device__ __forceinline__ f3 sym_mul(f3 d, f3 o, f3 v) {
   return F3(d.x * v.x + o.x * v.y + o.y * v.z, o.x * v.x + d.y * v.y + o.z * v.z, o.y * v.x + o.z * v.y + d.z * v.z);
@@ -157,12 +174,12 @@ __device__ __forceinline__ float vgrid_cell(const sl_vgrid& v, uint32_t i, uint3
 }
 // vgrid_lookup (common.wgsl:162-177)
 __device__ __forceinline__ float vgrid_lookup(const sl_vgrid& v, f3 w) {
-  float el = sl_asinf(clampf(w.z, -1.0f, 1.0f));
+  float el = lm_asin(clampf(w.z, -1.0f, 1.0f));
   float fi = clampf((0.5f * kPi - el) / (kPi / 8.0f) - 0.5f, 0.0f, 7.0f);
   uint32_t i0 = (uint32_t)fi;
   i0 = i0 > 6u ? 6u : i0;
   float ti = fi - (float)i0;
-  float az = (fabsf(w.x) + fabsf(w.y) < 1e-30f) ? 0.0f : sl_atan2f(w.y, w.x);
+  float az = (fabsf(w.x) + fabsf(w.y) < 1e-30f) ? 0.0f : lm_atan2(w.y, w.x);
   float fj = (az + kPi) / (2.0f * kPi) * 16.0f - 0.5f;
   float j0f = floorf(fj);
   float tj = fj - j0f;
@@ -186,6 +203,24 @@ __device__ __forceinline__ m3 quat_matrix(float x, float y, float z, float w) {
   return m;
 }
 // ein (common.wgsl:226-239): series below 1, else Abramowitz-Stegun 5.1.56
+#ifdef SL_FAST_SHADE
+// the same 12-term series Ein(x) = sum_k (-1)^(k+1) x^k / (k k!) evaluated by Horner's rule from its coefficients
+__device__ __forceinline__ float ein(float x) {
+  if (x < 1.0f) {
+    constexpr float c[12] = {(float)(1.0), (float)(-1.0 / 4.0), (float)(1.0 / 18.0), (float)(-1.0 / 96.0),
+                             (float)(1.0 / 600.0), (float)(-1.0 / 4320.0), (float)(1.0 / 35280.0),
+                             (float)(-1.0 / 322560.0), (float)(1.0 / 3265920.0), (float)(-1.0 / 36288000.0),
+                             (float)(1.0 / 439084800.0), (float)(-1.0 / 5748019200.0)};
+    float s = c[11];
+#pragma unroll
+    for (int k = 10; k >= 0; k--) s = s * x + c[k];
+    return s * x;
+  }
+  float p = (((x + 8.5733287401f) * x + 18.0590169730f) * x + 8.6347608925f) * x + 0.2677737343f;
+  float q = (((x + 9.5733223454f) * x + 25.6329561486f) * x + 21.0996530827f) * x + 3.9584969228f;
+  return lm_log(x) + 0.5772156649f + p / (q * x * lm_exp(x));
+}
+#else
 __device__ __forceinline__ float ein(float x) {
   if (x < 1.0f) {
     float term = x, s = x;
@@ -199,6 +234,7 @@ __device__ __forceinline__ float ein(float x) {
   float q = x * x * x * x + 9.5733223454f * x * x * x + 25.6329561486f * x * x + 21.0996530827f * x + 3.9584969228f;
   return sl_logf(x) + 0.5772156649f + p / q / (x * sl_expf(x));
 }
+#endif
 // footprint (common.wgsl:242-246)
 __device__ __forceinline__ float footprint(const Leaf& n, float detC, f3 w) {
   float a = dot3(w, sym_mul(n.cinv_d, n.cinv_o, w));
@@ -276,7 +312,7 @@ __device__ __forceinline__ f2 log_map(f3 c, f3 cb0, f3 cb1, f3 a) {
   f3 v = sub3(a, mul3(c, ca));
   float nv = len3(v);
   if (nv < 1e-9f) return F2(0.0f, 0.0f);
-  float k = sl_acosf(ca) / nv;
+  float k = lm_acos(ca) / nv;
   return F2(k * dot3(cb0, v), k * dot3(cb1, v));
 }
 // asg_phase (material_ext.wgsl:127-181)
@@ -322,7 +358,7 @@ __device__ inline float asg_phase(f3 wi, f3 lb0, f3 lb1, s2m sl, f3 n0, f3 t1, f
     for (int k = 0; k < 3; k++) {
       s2m sk = s2_div(sR, 2.0f * ASG_A[k]);
       s2m st = s2_add(sL, sk);
-      p_asg += ASG_W[k] * sqrtf(fmaxf(s2_det(sk), 0.0f) / fmaxf(s2_det(st), 1e-30f)) * sl_expf(-0.5f * s2_quad_inv(st, dm));
+      p_asg += ASG_W[k] * sqrtf(fmaxf(s2_det(sk), 0.0f) / fmaxf(s2_det(st), 1e-30f)) * lm_exp(-0.5f * s2_quad_inv(st, dm));
     }
     p_asg *= pk;
   }

@@ -5,6 +5,7 @@
 // and square root): it agrees with the CPU restatement to ~1e-6 relative, not to the bit.
 // A V grid of all 255 (no own-part occlusion) is recognised once per Gaussian: its lookup is exactly 1 for every
 // direction (each cell is 255/255 = 1 and a mix of ones is one), so the three lookups per light are skipped.
+#define SL_FAST_SHADE 1  // hardware exp/log/acos, Horner-form Ein: tolerance-checked output
 #include "light_math.cuh"
 #include "sl_lighting.h"
 
@@ -58,14 +59,14 @@ __device__ __forceinline__ f3 shade_one(const ShadeParams& SH, const sl_gaussian
     const f3 wo0 = xf_dir_inv(xf, norm3(sub3(eye, P)));
     f3 acc = F3(0.0f, 0.0f, 0.0f);
     if (SH.n_emit) {
-      uint32_t stack[48];
-      uint32_t sp = 1;
-      stack[0] = SH.root;
+      // the cut walk of a 48-entry stack (hi child popped first), stackless: word 7 of a node is where the walk
+      // goes once the node's subtree is done, word 19 marks nodes the full stack could not refine
+      uint32_t node = SH.root;
       const bool shape = SH.asg && ks > 0.0f;
-      while (sp > 0u) {
-        sp--;
-        const float* e = tree + 24u * stack[sp];
+      for (uint32_t guard = 0; node != kNone && guard < (1u << 16); guard++) {
+        const float* e = tree + 24u * node;
         const uint32_t child_lo = __float_as_uint(e[11]), child_hi = __float_as_uint(e[15]);
+        const uint32_t skip = __float_as_uint(e[7]);
         const f3 emean = F3(e[0], e[1], e[2]);
         bool use;
         if (child_lo == kNone || SH.mode == 0u) {
@@ -75,13 +76,10 @@ __device__ __forceinline__ f3 shade_one(const ShadeParams& SH, const sl_gaussian
           use = dot3(d, d) > SH.theta * SH.theta * e[3] * e[3];
         }
         if (!use) {
-          if (sp + 2u <= 48u) {
-            stack[sp] = child_lo;
-            stack[sp + 1u] = child_hi;
-            sp += 2u;
-          }
+          node = (child_lo != kNone && __float_as_uint(e[19]) == 0u) ? child_hi : skip;
           continue;
         }
+        node = skip;
         f3 d = sub3(emean, P);
         float d2 = dot3(d, d);
         if (d2 < 1e-8f) continue;
@@ -171,9 +169,11 @@ __global__ void __launch_bounds__(kThreads) shade_kernel(const __grid_constant__
                                                          const float* __restrict__ tree,
                                                          const float* __restrict__ lamp_T,
                                                          const float4* __restrict__ env_T,
+                                                         const uint32_t* __restrict__ order,
                                                          float4* __restrict__ colour, uint32_t count) {
-  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
-  if (g >= count) return;
+  const uint32_t j = blockIdx.x * kThreads + threadIdx.x;
+  if (j >= count) return;
+  const uint32_t g = order[j];
   const f3 c = shade_one(SH, gs, nodes, vgrid, parts, mats, tree, lamp_T, env_T, g);
   colour[g] = make_float4(c.x, c.y, c.z, 1.0f);
 }
@@ -202,11 +202,12 @@ __global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __res
     s_max = 0u;
   }
   __syncthreads();
-  const uint32_t i = (blockIdx.x / 2 - V.block_first) * 256u + (blockIdx.x & 1u) * kThreads + t;
+  const uint32_t j = (blockIdx.x / 2 - V.block_first) * 256u + (blockIdx.x & 1u) * kThreads + t;
+  const uint32_t i = j < V.P.count ? S.order[j] : j;  // the scene's shading order
   const uint32_t gslot = V.slot_base + i;
   float mx = 0.0f;
   uint32_t material = kEmitterMaterial;
-  if (i < V.P.count && (keys32[gslot] & 0xFFFFu) != 0xFFFFu) {
+  if (j < V.P.count && (keys32[gslot] & 0xFFFFu) != 0xFFFFu) {
     const sl_gaussian& G = reinterpret_cast<const sl_gaussian*>(V.gaussians)[i];
     uint32_t part = G.part_surface & 0xffffu;
     part = part > kMaxParts - 1u ? kMaxParts - 1u : part;
@@ -249,10 +250,10 @@ cudaError_t launch_bshade(const BatchView* views, const BatchScene* scenes, cons
 
 cudaError_t launch_shade(const ShadeParams& SH, const sl_gaussian* gs, const sl_node* nodes, const sl_vgrid* vgrid,
                          const sl_part* parts, const sl_material* mats, const float* tree, const float* lamp_T,
-                         const float4* env_T, float4* colour, uint32_t count, cudaStream_t s) {
+                         const float4* env_T, const uint32_t* order, float4* colour, uint32_t count, cudaStream_t s) {
   if (!count) return cudaSuccess;
   shade_kernel<<<(count + kThreads - 1) / kThreads, kThreads, 0, s>>>(SH, gs, nodes, vgrid, parts, mats, tree, lamp_T,
-                                                                      env_T, colour, count);
+                                                                      env_T, order, colour, count);
   return cudaGetLastError();
 }
 

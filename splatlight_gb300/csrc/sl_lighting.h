@@ -53,6 +53,7 @@ struct BatchScene {
   const float* tree;
   const float* lamp_T;
   const float4* env_T;
+  const uint32_t* order;  // shading order of the scene's Gaussians
   ShadeParams SH;   // eye replaced per view
   uint32_t lit;     // 0: no lighting bound (radiance 0, as an unbound colour buffer)
 };
@@ -76,6 +77,6 @@ cudaError_t launch_sm_lookup(const SunParams& SP, const SunLayer* layers, const 
                              uint32_t count, const float4* mip, float4* env_T, cudaStream_t s);
 cudaError_t launch_shade(const ShadeParams& SH, const sl_gaussian* gs, const sl_node* nodes, const sl_vgrid* vgrid,
                          const sl_part* parts, const sl_material* mats, const float* tree, const float* lamp_T,
-                         const float4* env_T, float4* colour, uint32_t count, cudaStream_t s);
+                         const float4* env_T, const uint32_t* order, float4* colour, uint32_t count, cudaStream_t s);
 
 }  // namespace sl

@@ -86,6 +86,7 @@ struct sl_lighting {
   int device = 0;
   uint32_t count = 0, material_count = 0;
   sl::DevBuf nodes, vgrid, materials, parts, tree, lamp_T, env_T, colour;
+  sl::DevBuf order;  // shading order (Morton order of the means)
   bool iso_done = false;
   // emitters (src/lighting.js:612-721, EmitParams :657-673)
   std::vector<float> rec;

@@ -75,6 +75,11 @@ class Lighting:
         f = (C.c_float * 3)(*[float(v) for v in forward]) if forward is not None else None
         N.check(self._lib.sl_lighting_update(self._h, e, f, moved_mask, stream))
 
+    def shade(self, eye, stream=None) -> None:
+        """The shading pass alone at a new eye; the maps stay as the last update left them."""
+        e = (C.c_float * 3)(*[float(v) for v in eye])
+        N.check(self._lib.sl_lighting_shade(self._h, e, stream))
+
     def bind(self) -> None:
         N.check(self._lib.sl_renderer_bind_lighting(self.renderer.handle, self._h))
 

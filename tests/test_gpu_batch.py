@@ -156,6 +156,23 @@ def test_lit_views_two_scenes(cuda):
         Lb.close()
 
 
+def test_lit_views_many_eyes(cuda):
+    """Several lit views of one scene from different cameras: the batch shades each view at its own eye with the
+    scene's maps; the per-view path gives the same with the maps kept and the shading pass re-run at that eye."""
+    a, _ = _scenes()
+    with SplatRenderer(a.gaussians, a.parts) as ra:
+        La = for_scene(ra, a)
+        La.update(a.eye, camera_forward(a))
+        eyes = [(0.0, 0.0, 3.5), (0.6, 0.3, 3.0), (-0.8, -0.2, 2.6), (0.1, 0.7, 3.9)]
+        views = [View(0, _frame(a, 128 + 32 * k, 96 + 16 * k, VIEW_LIT, eye=e), e) for k, e in enumerate(eyes)]
+        with BatchRenderer([ra], [La]) as B:
+            _render(B, views)
+            for k, v in enumerate(views):
+                La.shade(v.eye)
+                _assert_view(B, k, v, ra, (16, 16), exact=False)
+        La.close()
+
+
 def test_autotune_keeps_results(cuda):
     a, b = _scenes()
     with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
