@@ -283,6 +283,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the ragged-batch leg")
+    ap.add_argument("--only-batch", action="store_true", help="the ragged-batch leg alone (its own JSON line)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -306,6 +307,15 @@ def main():
 
     __import__("__graft_entry__").build()
     from splatlight_gb300.renderer import SplatRenderer
+
+    if args.only_batch:
+        stream = torch.cuda.Stream()
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        res = run_batch(args, stream, flush)
+        if rank == 0:
+            print(json.dumps({"metric": "views/s", "value": res["batched_views_per_s"], "unit": "views/s",
+                              "n_gpus": world, "batched": res}))
+        return
 
     from splatlight_gb300.lighting import camera_forward, for_scene
 

@@ -68,6 +68,8 @@ _EXTRA: dict = {
     "orc_atan2f_n": (None, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]),
     "orc_asinf_n": (None, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "orc_acosf_n": (None, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "orc_row_tiles": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32),
+                                C.POINTER(C.c_uint32)]),
 }
 
 
@@ -254,3 +256,11 @@ def emitter_tree(rec: np.ndarray):
     cov = np.zeros(6, np.float32)
     root = L.orc_emitter_tree(r.ctypes.data, len(r), out.ctypes.data, cov.ctypes.data)
     return out, int(root), cov
+
+
+def row_tiles(splat, ty: int, tile=(16, 16)):
+    """sl_row_tiles of one SPLAT record: (t0, t1) tile columns of tile row ty, or None when the row holds none."""
+    rec = np.ascontiguousarray(np.asarray(splat, dtype=SPLAT).reshape(1))
+    a, b = C.c_uint32(), C.c_uint32()
+    ok = lib().orc_row_tiles(rec.ctypes.data, ty, tile[0], tile[1], C.byref(a), C.byref(b))
+    return (a.value, b.value) if ok else None

@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include "sl_detmath.h"
+#include "sl_tilespan.h"
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -310,6 +311,8 @@ void orc_sort16(const uint32_t* keys, uint32_t n, uint32_t* order) {
   free(hist);
 }
 
+/* Per-tile lists: every visible splat, in back-to-front order, joins the list of each tile its ellipse can reach
+ * (sl_tilespan.h: per row of tiles inside its candidate rectangle, the columns the ellipse spans over that row). */
 int64_t orc_bin(const orc_splat* splats, const uint32_t* order, uint32_t visible, uint32_t width, uint32_t height,
                 uint32_t tile_w, uint32_t tile_h, uint32_t* ranges, uint32_t* entries, uint64_t cap) {
   uint32_t ntx = (width + tile_w - 1u) / tile_w, nty = (height + tile_h - 1u) / tile_h;
@@ -318,8 +321,13 @@ int64_t orc_bin(const orc_splat* splats, const uint32_t* order, uint32_t visible
   for (uint32_t p = 0; p < visible; p++) {
     const orc_splat* s = &splats[order[p]];
     if (s->ix0 > s->ix1 || s->iy0 > s->iy1) continue;
-    for (uint32_t ty = (uint32_t)s->iy0 / tile_h; ty <= (uint32_t)s->iy1 / tile_h; ty++)
-      for (uint32_t tx = (uint32_t)s->ix0 / tile_w; tx <= (uint32_t)s->ix1 / tile_w; tx++) cnt[ty * ntx + tx + 1u]++;
+    for (uint32_t ty = (uint32_t)s->iy0 / tile_h; ty <= (uint32_t)s->iy1 / tile_h; ty++) {
+      uint32_t t0, t1;
+      if (!sl_row_tiles(s->cx, s->cy, s->g0x, s->g0y, s->g1x, s->g1y, s->qcut, (uint32_t)s->ix0 / tile_w,
+                        (uint32_t)s->ix1 / tile_w, ty, tile_w, tile_h, &t0, &t1))
+        continue;
+      for (uint32_t tx = t0; tx <= t1; tx++) cnt[ty * ntx + tx + 1u]++;
+    }
   }
   for (uint32_t t = 0; t < ntiles; t++) cnt[t + 1u] += cnt[t];
   uint64_t total = cnt[ntiles];
@@ -336,13 +344,22 @@ int64_t orc_bin(const orc_splat* splats, const uint32_t* order, uint32_t visible
     for (uint32_t p = 0; p < visible; p++) {
       const orc_splat* s = &splats[order[p]];
       if (s->ix0 > s->ix1 || s->iy0 > s->iy1) continue;
-      for (uint32_t ty = (uint32_t)s->iy0 / tile_h; ty <= (uint32_t)s->iy1 / tile_h; ty++)
-        for (uint32_t tx = (uint32_t)s->ix0 / tile_w; tx <= (uint32_t)s->ix1 / tile_w; tx++)
-          entries[cnt[ty * ntx + tx]++] = order[p];
+      for (uint32_t ty = (uint32_t)s->iy0 / tile_h; ty <= (uint32_t)s->iy1 / tile_h; ty++) {
+        uint32_t t0, t1;
+        if (!sl_row_tiles(s->cx, s->cy, s->g0x, s->g0y, s->g1x, s->g1y, s->qcut, (uint32_t)s->ix0 / tile_w,
+                          (uint32_t)s->ix1 / tile_w, ty, tile_w, tile_h, &t0, &t1))
+          continue;
+        for (uint32_t tx = t0; tx <= t1; tx++) entries[cnt[ty * ntx + tx]++] = order[p];
+      }
     }
   }
   free(cnt);
   return (int64_t)total;
+}
+
+int orc_row_tiles(const orc_splat* s, uint32_t ty, uint32_t tile_w, uint32_t tile_h, uint32_t* t0, uint32_t* t1) {
+  return sl_row_tiles(s->cx, s->cy, s->g0x, s->g0y, s->g1x, s->g1y, s->qcut, (uint32_t)s->ix0 / tile_w,
+                      (uint32_t)s->ix1 / tile_w, ty, tile_w, tile_h, t0, t1);
 }
 
 void orc_composite(const orc_splat* splats, const uint32_t* order, uint32_t visible, uint32_t width,

@@ -46,6 +46,8 @@ void orc_sort16(const uint32_t* keys, uint32_t n, uint32_t* order);
  * is too small. */
 int64_t orc_bin(const orc_splat* splats, const uint32_t* order, uint32_t visible, uint32_t width, uint32_t height,
                 uint32_t tile_w, uint32_t tile_h, uint32_t* ranges, uint32_t* entries, uint64_t cap);
+/* sl_row_tiles of one splat (tile row ty), for tests. */
+int orc_row_tiles(const orc_splat* s, uint32_t ty, uint32_t tile_w, uint32_t tile_h, uint32_t* t0, uint32_t* t1);
 
 /* splat.wgsl vs/fs + premultiplied "over" blend (shaders/splat.wgsl:22-78; src/renderer.js:133-143), back to front
  * in sort order, fp32.  rgba: W x H x 4 (row 0 at the top); counts: fragments kept (alpha >= 1/255). */

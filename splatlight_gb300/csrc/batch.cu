@@ -5,33 +5,50 @@
 // on the device (grids are sized for the batch's capacity, so a CUDA graph of the chain can be replayed for any
 // batch that fits).
 #include "sl_internal.h"
+#include "sl_tilespan.h"
 
 namespace sl {
 namespace {
 
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ uint32_t rect_tiles(ushort4 r) {
-  return (r.x <= r.z && r.y <= r.w) ? (uint32_t)(r.z - r.x + 1) * (uint32_t)(r.w - r.y + 1) : 0u;
+// Tiles a splat reaches: per tile row of its candidate rectangle, the columns its ellipse spans over that row.
+__device__ __forceinline__ uint32_t splat_tiles(const SplatRec& rec, ushort4 r, uint32_t tw, uint32_t th) {
+  if (!(r.x <= r.z && r.y <= r.w)) return 0u;
+  uint32_t n = 0;
+  for (uint32_t ty = r.y; ty <= r.w; ty++) {
+    uint32_t t0, t1;
+    if (sl_row_tiles(rec.a.x, rec.a.y, rec.a.z, rec.a.w, rec.b.x, rec.b.y, rec.b.w, r.x, r.z, ty, tw, th, &t0, &t1))
+      n += t1 - t0 + 1u;
+  }
+  return n;
 }
 
 __global__ void __launch_bounds__(kThreads) btile_count_kernel(const uint32_t* __restrict__ order,
                                                                const ushort4* __restrict__ rects,
+                                                               const SplatRec* __restrict__ recs,
                                                                const uint32_t* __restrict__ totals, uint32_t n_max,
+                                                               uint32_t tw, uint32_t th,
                                                                uint32_t* __restrict__ counts) {
   const uint32_t p = blockIdx.x * kThreads + threadIdx.x;
   if (p >= n_max) return;
-  counts[p] = p < totals[0] ? rect_tiles(rects[order[p]]) : 0u;
+  uint32_t c = 0;
+  if (p < totals[0]) {
+    const uint32_t slot = order[p];
+    c = splat_tiles(recs[slot], rects[slot], tw, th);
+  }
+  counts[p] = c;
 }
 
 __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __restrict__ order,
                                                               const ushort4* __restrict__ rects,
+                                                              const SplatRec* __restrict__ recs,
                                                               const uint32_t* __restrict__ offsets,
                                                               const BatchView* __restrict__ views,
                                                               const uint32_t* __restrict__ block_view,
                                                               const uint32_t* __restrict__ totals, uint32_t n_max,
-                                                              uint32_t capacity, FrameCounters* ctr,
-                                                              uint32_t* __restrict__ tile_keys,
+                                                              uint32_t tw, uint32_t th, uint32_t capacity,
+                                                              FrameCounters* ctr, uint32_t* __restrict__ tile_keys,
                                                               uint32_t* __restrict__ tile_vals,
                                                               uint32_t* __restrict__ digit_hist) {
   __shared__ uint32_t h[3][256];
@@ -46,15 +63,20 @@ __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __
     const ushort4 r = rects[slot];
     if (r.x <= r.z && r.y <= r.w) {
       uint32_t e = offsets[p];
-      const uint32_t cnt = rect_tiles(r);
+      const SplatRec rec = recs[slot];
+      const uint32_t cnt = splat_tiles(rec, r, tw, th);
       if (e + cnt > capacity) {
         atomicExch(&ctr->overflow, 1u);
       } else {
         const uint32_t v = block_view[slot >> 8];
         const uint32_t base = views[v].tile_base, tiles_x = views[v].tiles_x;
         for (uint32_t ty = r.y; ty <= r.w; ty++) {
+          uint32_t t0, t1;
+          if (!sl_row_tiles(rec.a.x, rec.a.y, rec.a.z, rec.a.w, rec.b.x, rec.b.y, rec.b.w, r.x, r.z, ty, tw, th, &t0,
+                            &t1))
+            continue;
           const uint32_t row = base + ty * tiles_x;
-          for (uint32_t tx = r.x; tx <= r.z; tx++) {
+          for (uint32_t tx = t0; tx <= t1; tx++) {
             const uint32_t tile = row + tx;
             tile_keys[e] = tile;
             tile_vals[e] = slot;
@@ -87,20 +109,24 @@ __global__ void __launch_bounds__(kThreads) btile_runs_kernel(const uint32_t* __
 
 }  // namespace
 
-cudaError_t launch_btile_count(const uint32_t* order, const ushort4* rects, const uint32_t* totals, uint32_t n_max,
-                               uint32_t* counts, cudaStream_t s) {
+cudaError_t launch_btile_count(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
+                               const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t* counts,
+                               cudaStream_t s) {
   if (!n_max) return cudaSuccess;
-  btile_count_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, totals, n_max, counts);
+  btile_count_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, recs, totals, n_max, tw, th,
+                                                                            counts);
   return cudaGetLastError();
 }
 
-cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const uint32_t* offsets,
-                              const BatchView* views, const uint32_t* block_view, const uint32_t* totals,
-                              uint32_t n_max, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
-                              uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s) {
+cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
+                              const uint32_t* offsets, const BatchView* views, const uint32_t* block_view,
+                              const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t capacity,
+                              FrameCounters* ctr, uint32_t* tile_keys, uint32_t* tile_vals, uint32_t* digit_hist,
+                              cudaStream_t s) {
   if (!n_max) return cudaSuccess;
   btile_emit_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(
-      order, rects, offsets, views, block_view, totals, n_max, capacity, ctr, tile_keys, tile_vals, digit_hist);
+      order, rects, recs, offsets, views, block_view, totals, n_max, tw, th, capacity, ctr, tile_keys, tile_vals,
+      digit_hist);
   return cudaGetLastError();
 }
 

@@ -370,13 +370,15 @@ static int render_once(sl_renderer* r, const sl_render_frame* f, float4* out_dev
                              ctr, s),
                 "depth sort");
   if (ev) SL_CHECK_CUDA(cudaEventRecord(ev[2], s), "event");
-  SL_CHECK_CUDA(launch_tile_counts(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), n, ctr, vb.slot_counts.as<uint32_t>(), s),
+  SL_CHECK_CUDA(launch_tile_counts(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.recs.as<SplatRec>(), n, P.tile_w,
+                                   P.tile_h, ctr, vb.slot_counts.as<uint32_t>(), s),
                 "tile counts");
   SL_CHECK_CUDA(exclusive_scan_u32(vb.slot_counts.as<uint32_t>(), vb.slot_offsets.as<uint32_t>(), n, &ctr->entries,
                                    vb.scan_scratch.ptr, ctr, s),
                 "entry scan");
-  SL_CHECK_CUDA(launch_tile_emit(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.slot_offsets.as<uint32_t>(), n,
-                                 P.tiles_x, (uint32_t)(cap > 0xffffffffull ? 0xffffffffu : cap), ctr,
+  SL_CHECK_CUDA(launch_tile_emit(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.recs.as<SplatRec>(),
+                                 vb.slot_offsets.as<uint32_t>(), n, P.tiles_x, P.tile_w, P.tile_h,
+                                 (uint32_t)(cap > 0xffffffffull ? 0xffffffffu : cap), ctr,
                                  vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), hist + 512, s),
                 "tile emit");
   // the entry count is only known on the device: the tile sort reads it there (grid sized for the capacity)

@@ -173,11 +173,13 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   CK(sort32_pairs(b->keys32.as<uint32_t>(), b->keys_alt.as<uint32_t>(), nullptr, b->order.as<uint32_t>(),
                   b->vals_alt.as<uint32_t>(), S, totals, 16 + bits_for(V - 1), hist, b->status.as<uint32_t>(),
                   b->tile_ctr.as<uint32_t>(), max_tiles_sort, ctr, s));
-  CK(launch_btile_count(b->order.as<uint32_t>(), b->rects.as<ushort4>(), totals, S, b->slot_counts.as<uint32_t>(), s));
+  CK(launch_btile_count(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->recs.as<SplatRec>(), totals, S, b->tile_w,
+                        b->tile_h, b->slot_counts.as<uint32_t>(), s));
   CK(exclusive_scan_u32(b->slot_counts.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), S, &ctr->entries,
                         b->scan_scratch.ptr, ctr, s));
-  CK(launch_btile_emit(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->slot_offsets.as<uint32_t>(),
-                       b->views.as<BatchView>(), b->block_view.as<uint32_t>(), totals, S, E, ctr,
+  CK(launch_btile_emit(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->recs.as<SplatRec>(),
+                       b->slot_offsets.as<uint32_t>(), b->views.as<BatchView>(), b->block_view.as<uint32_t>(), totals,
+                       S, b->tile_w, b->tile_h, E, ctr,
                        b->tile_keys.as<uint32_t>(), b->tile_vals.as<uint32_t>(), hist + 768, s));
   CK(sort32_pairs(b->tile_keys.as<uint32_t>(), b->tile_keys_alt.as<uint32_t>(), b->tile_vals.as<uint32_t>(),
                   b->tile_vals.as<uint32_t>(), b->tile_vals_alt.as<uint32_t>(), E, &ctr->entries, bits_for(T - 1),

@@ -93,11 +93,12 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, ui
                                FrameCounters* ctr, cudaStream_t s);
 
 // tiles.cu
-cudaError_t launch_tile_counts(const uint32_t* order, const ushort4* rects, uint32_t n, const FrameCounters* ctr,
-                               uint32_t* counts, cudaStream_t s);
-cudaError_t launch_tile_emit(const uint32_t* order, const ushort4* rects, const uint32_t* offsets, uint32_t n,
-                             uint32_t tiles_x, uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys,
-                             uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s);
+cudaError_t launch_tile_counts(const uint32_t* order, const ushort4* rects, const SplatRec* recs, uint32_t n,
+                               uint32_t tw, uint32_t th, const FrameCounters* ctr, uint32_t* counts, cudaStream_t s);
+cudaError_t launch_tile_emit(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
+                             const uint32_t* offsets, uint32_t n, uint32_t tiles_x, uint32_t tw, uint32_t th,
+                             uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys, uint32_t* tile_vals,
+                             uint32_t* digit_hist, cudaStream_t s);
 // After the tile sort: per tile the run [start, end) of its id in the sorted keys (both zero for an empty tile;
 // the arrays are cleared by the caller), then counts = end - start.
 cudaError_t launch_tile_runs(const uint16_t* sorted_keys, const uint32_t* n_dev, uint32_t n_max, uint32_t* run_start,
@@ -160,12 +161,14 @@ cudaError_t launch_bcomposite(const BatchComposite& B, const uint2* ranges, cons
                               const SplatRec* recs, const BatchViewOut* views, const uint32_t* view_maxrad,
                               const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s);
 // batch.cu (totals: the BatchDyn, read as u32 words: [0] total slots, [1] total tiles)
-cudaError_t launch_btile_count(const uint32_t* order, const ushort4* rects, const uint32_t* totals, uint32_t n_max,
-                               uint32_t* counts, cudaStream_t s);
-cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const uint32_t* offsets,
-                              const BatchView* views, const uint32_t* block_view, const uint32_t* totals,
-                              uint32_t n_max, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
-                              uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s);
+cudaError_t launch_btile_count(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
+                               const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t* counts,
+                               cudaStream_t s);
+cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
+                              const uint32_t* offsets, const BatchView* views, const uint32_t* block_view,
+                              const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t capacity,
+                              FrameCounters* ctr, uint32_t* tile_keys, uint32_t* tile_vals, uint32_t* digit_hist,
+                              cudaStream_t s);
 cudaError_t launch_btile_runs(const uint32_t* keys, const uint32_t* n_dev, uint32_t n_max, uint32_t* run_start,
                               uint32_t* run_end, cudaStream_t s);
 

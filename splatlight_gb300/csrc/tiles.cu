@@ -5,29 +5,47 @@
 // reference's fixed-function path (one instanced quad per sorted splat, shaders/splat.wgsl:51-55, src/renderer.js:
 // 474-485): the ranges are the rasteriser's coverage made explicit per tile.
 #include "sl_internal.h"
+#include "sl_tilespan.h"
 
 namespace sl {
 namespace {
 
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ uint32_t rect_tiles(ushort4 r) {
-  return (r.x <= r.z && r.y <= r.w) ? (uint32_t)(r.z - r.x + 1) * (uint32_t)(r.w - r.y + 1) : 0u;
+// Tiles a splat reaches: per tile row of its candidate rectangle, the columns its ellipse spans over that row.
+__device__ __forceinline__ uint32_t splat_tiles(const SplatRec& rec, ushort4 r, uint32_t tw, uint32_t th) {
+  if (!(r.x <= r.z && r.y <= r.w)) return 0u;
+  uint32_t n = 0;
+  for (uint32_t ty = r.y; ty <= r.w; ty++) {
+    uint32_t t0, t1;
+    if (sl_row_tiles(rec.a.x, rec.a.y, rec.a.z, rec.a.w, rec.b.x, rec.b.y, rec.b.w, r.x, r.z, ty, tw, th, &t0, &t1))
+      n += t1 - t0 + 1u;
+  }
+  return n;
 }
 
 __global__ void __launch_bounds__(kThreads) tile_count_kernel(const uint32_t* __restrict__ order,
-                                                              const ushort4* __restrict__ rects, uint32_t n,
-                                                              const FrameCounters* ctr, uint32_t* __restrict__ counts) {
+                                                              const ushort4* __restrict__ rects,
+                                                              const SplatRec* __restrict__ recs, uint32_t n,
+                                                              uint32_t tw, uint32_t th, const FrameCounters* ctr,
+                                                              uint32_t* __restrict__ counts) {
   uint32_t p = blockIdx.x * kThreads + threadIdx.x;
   if (p >= n) return;
   const uint32_t visible = ctr->visible;
-  counts[p] = p < visible ? rect_tiles(rects[order[p]]) : 0u;
+  uint32_t c = 0;
+  if (p < visible) {
+    const uint32_t slot = order[p];
+    c = splat_tiles(recs[slot], rects[slot], tw, th);
+  }
+  counts[p] = c;
 }
 
 __global__ void __launch_bounds__(kThreads) tile_emit_kernel(const uint32_t* __restrict__ order,
                                                              const ushort4* __restrict__ rects,
+                                                             const SplatRec* __restrict__ recs,
                                                              const uint32_t* __restrict__ offsets, uint32_t n,
-                                                             uint32_t tiles_x, uint32_t capacity, FrameCounters* ctr,
+                                                             uint32_t tiles_x, uint32_t tw, uint32_t th,
+                                                             uint32_t capacity, FrameCounters* ctr,
                                                              uint16_t* __restrict__ tile_keys,
                                                              uint32_t* __restrict__ tile_vals,
                                                              uint32_t* __restrict__ digit_hist) {
@@ -43,25 +61,30 @@ __global__ void __launch_bounds__(kThreads) tile_emit_kernel(const uint32_t* __r
     const ushort4 r = rects[slot];
     uint32_t e = offsets[p];
     if (r.x <= r.z && r.y <= r.w) {
-      const uint32_t cnt = rect_tiles(r);
+      const SplatRec rec = recs[slot];
+      const uint32_t cnt = splat_tiles(rec, r, tw, th);
       if (e + cnt > capacity) {
         atomicExch(&ctr->overflow, 1u);
       } else {
         for (uint32_t ty = r.y; ty <= r.w; ty++) {
+          uint32_t t0, t1;
+          if (!sl_row_tiles(rec.a.x, rec.a.y, rec.a.z, rec.a.w, rec.b.x, rec.b.y, rec.b.w, r.x, r.z, ty, tw, th, &t0,
+                            &t1))
+            continue;
           // one row of tiles: ids are consecutive, so the high digit is shared by most of the row
           const uint32_t row = ty * tiles_x;
-          for (uint32_t tx = r.x; tx <= r.z; tx++) {
+          for (uint32_t tx = t0; tx <= t1; tx++) {
             const uint32_t tile = row + tx;
             tile_keys[e] = (uint16_t)tile;
             tile_vals[e] = slot;
             e++;
             atomicAdd(&h_lo[tile & 0xffu], 1u);
           }
-          const uint32_t first = row + r.x, last = row + r.z;
+          const uint32_t first = row + t0, last = row + t1;
           if ((first >> 8) == (last >> 8)) {
-            atomicAdd(&h_hi[first >> 8], (uint32_t)(r.z - r.x + 1));
+            atomicAdd(&h_hi[first >> 8], t1 - t0 + 1u);
           } else {
-            for (uint32_t tx = r.x; tx <= r.z; tx++) atomicAdd(&h_hi[(row + tx) >> 8], 1u);
+            for (uint32_t tx = t0; tx <= t1; tx++) atomicAdd(&h_hi[(row + tx) >> 8], 1u);
           }
         }
       }
@@ -100,19 +123,21 @@ __global__ void tile_ranges_kernel(const uint32_t* __restrict__ starts, const ui
 
 }  // namespace
 
-cudaError_t launch_tile_counts(const uint32_t* order, const ushort4* rects, uint32_t n, const FrameCounters* ctr,
-                               uint32_t* counts, cudaStream_t s) {
+cudaError_t launch_tile_counts(const uint32_t* order, const ushort4* rects, const SplatRec* recs, uint32_t n,
+                               uint32_t tw, uint32_t th, const FrameCounters* ctr, uint32_t* counts, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  tile_count_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, n, ctr, counts);
+  tile_count_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, recs, n, tw, th, ctr, counts);
   return cudaGetLastError();
 }
 
-cudaError_t launch_tile_emit(const uint32_t* order, const ushort4* rects, const uint32_t* offsets, uint32_t n,
-                             uint32_t tiles_x, uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys,
-                             uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s) {
+cudaError_t launch_tile_emit(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
+                             const uint32_t* offsets, uint32_t n, uint32_t tiles_x, uint32_t tw, uint32_t th,
+                             uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys, uint32_t* tile_vals,
+                             uint32_t* digit_hist, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  tile_emit_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, offsets, n, tiles_x, capacity,
-                                                                       ctr, tile_keys, tile_vals, digit_hist);
+  tile_emit_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, recs, offsets, n, tiles_x, tw, th,
+                                                                       capacity, ctr, tile_keys, tile_vals,
+                                                                       digit_hist);
   return cudaGetLastError();
 }
 
