@@ -243,9 +243,9 @@ def run_batch(args, stream, flush):
     return res
 
 
-# bproject, bshade, 3 depth-sort passes, tile counts, scan, emit, 3 tile-sort passes, runs, run counts, scan, ranges,
-# bcomposite
-BATCH_KERNELS = 17
+# bproject, shading flags, scan, compact, bshade, 3 depth-sort passes, tile counts, scan, emit, 3 tile-sort passes,
+# runs, run counts, scan, ranges, bcomposite
+BATCH_KERNELS = 20
 
 
 def run_reference(args):

@@ -313,12 +313,14 @@ SL_API int sl_batch_destroy(sl_batch* b);
 SL_API int sl_batch_set_tile(sl_batch* b, uint32_t tile_w, uint32_t tile_h);
 SL_API int sl_batch_set_timing(sl_batch* b, int enabled);
 /* Renders n_views views: view v draws frames[v] of scene scene_of_view[v], eyes[3v..3v+2] its camera position (the
- * lit radiance's view direction).  Images are packed in view order into out_dev (device, float RGBA, out_floats
+ * lit radiance's view direction), light_scales[v] (NULL = all 1) the intensity scale of every light of its scene
+ * (emitters and distant lights; the sky ambient is unscaled) -- the same radiance as sl_lighting_set_emitters with
+ * scale x light_scale and sl_lighting_set_environment with each irradiance x light_scale.  Images are packed in view order into out_dev (device, float RGBA, out_floats
  * floats at least 4 x the sum of W x H); view_offsets[v] (optional, host) receives the first float of view v.  The
  * call returns after the batch completed; stats (optional) describe it. */
 SL_API int sl_batch_render(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames,
-                           const float* eyes, uint32_t n_views, float* out_dev, uint64_t out_floats,
-                           uint64_t* view_offsets, sl_batch_stats* stats, void* stream);
+                           const float* eyes, const float* light_scales, uint32_t n_views, float* out_dev,
+                           uint64_t out_floats, uint64_t* view_offsets, sl_batch_stats* stats, void* stream);
 /* Debug read-back of view `view` of the last batch, in that view's own indices (as sl_renderer_read_debug):
  * order (n slots), ranges (2 per tile), entries (the tile lists' slots, entries_cap at least *n_entries).  Any
  * pointer may be NULL. */
@@ -327,8 +329,9 @@ SL_API int sl_batch_read_view(sl_batch* b, uint32_t view, uint32_t* order, uint3
 /* Picks the fastest tile shape for this batch of views (renders it with each of 16x16, 8x32, 32x8, timed on the
  * device, `reps` times each) and keeps it; writes the per-shape times (ms) to ms_out[3] if not NULL. */
 SL_API int sl_batch_autotune(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames,
-                             const float* eyes, uint32_t n_views, float* out_dev, uint64_t out_floats, uint32_t reps,
-                             uint32_t* tile_w, uint32_t* tile_h, float* ms_out, void* stream);
+                             const float* eyes, const float* light_scales, uint32_t n_views, float* out_dev,
+                             uint64_t out_floats, uint32_t reps, uint32_t* tile_w, uint32_t* tile_h, float* ms_out,
+                             void* stream);
 
 #ifdef __cplusplus
 }

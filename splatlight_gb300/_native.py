@@ -83,9 +83,9 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_batch_destroy": (_I, [_P]),
     "sl_batch_set_tile": (_I, [_P, _U32, _U32]),
     "sl_batch_set_timing": (_I, [_P, _I]),
-    "sl_batch_render": (_I, [_P, _P, _P, _P, _U32, _P, _U64, _P, C.POINTER(BatchStats), _P]),
+    "sl_batch_render": (_I, [_P, _P, _P, _P, _P, _U32, _P, _U64, _P, C.POINTER(BatchStats), _P]),
     "sl_batch_read_view": (_I, [_P, _U32, _P, _P, _P, _U64, C.POINTER(_U64)]),
-    "sl_batch_autotune": (_I, [_P, _P, _P, _P, _U32, _P, _U64, _U32, C.POINTER(_U32), C.POINTER(_U32),
+    "sl_batch_autotune": (_I, [_P, _P, _P, _P, _P, _U32, _P, _U64, _U32, C.POINTER(_U32), C.POINTER(_U32),
                                _P, _P]),
 }
 

@@ -17,6 +17,7 @@ class View:
     scene: int            # index into the batch's renderers
     frame: np.ndarray     # RenderFrame record (structs.FRAME)
     eye: tuple            # camera position (the lit radiance's view direction)
+    light_scale: float = 1.0  # intensity scale of every light of the scene (the request's light state)
 
 
 class BatchRenderer:
@@ -67,13 +68,15 @@ class BatchRenderer:
         frames = np.zeros(n, dtype=FRAME)
         scenes = np.zeros(n, dtype=np.uint32)
         eyes = np.zeros((n, 3), dtype=np.float32)
+        scales = np.ones(n, dtype=np.float32)
         pix = 0
         for k, v in enumerate(views):
             frames[k] = np.asarray(v.frame, dtype=FRAME).reshape(())
             scenes[k] = v.scene
             eyes[k] = np.asarray(v.eye, dtype=np.float32)
+            scales[k] = v.light_scale
             pix += int(frames[k]["viewport"][0]) * int(frames[k]["viewport"][1])
-        return frames, scenes, eyes, pix
+        return frames, scenes, eyes, scales, pix
 
     def _device_out(self, floats: int, out):
         import torch
@@ -85,13 +88,13 @@ class BatchRenderer:
 
     def render_device(self, views, out=None, stream=None):
         """Renders the batch into a device float tensor (packed images); returns (tensor, offsets in floats)."""
-        frames, scenes, eyes, pix = self._pack(views)
+        frames, scenes, eyes, scales, pix = self._pack(views)
         dev = self._device_out(4 * pix, out)
         offs = np.zeros(len(views), dtype=np.uint64)
         N.check(self._lib.sl_batch_render(self._h, scenes.ctypes.data, frames.ctypes.data, eyes.ctypes.data,
-                                          len(views), dev.data_ptr(), dev.numel(), offs.ctypes.data,
+                                          scales.ctypes.data, len(views), dev.data_ptr(), dev.numel(), offs.ctypes.data,
                                           C.byref(self.last_stats), stream))
-        self._keep = (frames, scenes, eyes)
+        self._keep = (frames, scenes, eyes, scales)
         return dev, offs
 
     def render(self, views, stream=None) -> list[np.ndarray]:
@@ -106,12 +109,12 @@ class BatchRenderer:
 
     def autotune(self, views, reps: int = 3):
         """Times the batch with each tile shape, keeps the fastest; returns ((tile_w, tile_h), ms per shape)."""
-        frames, scenes, eyes, pix = self._pack(views)
+        frames, scenes, eyes, scales, pix = self._pack(views)
         dev = self._device_out(4 * pix, None)
         tw, th = C.c_uint32(), C.c_uint32()
         ms = np.zeros(3, dtype=np.float32)
         N.check(self._lib.sl_batch_autotune(self._h, scenes.ctypes.data, frames.ctypes.data, eyes.ctypes.data,
-                                            len(views), dev.data_ptr(), dev.numel(), reps, C.byref(tw),
+                                            scales.ctypes.data, len(views), dev.data_ptr(), dev.numel(), reps, C.byref(tw),
                                             C.byref(th), ms.ctypes.data, None))
         return (tw.value, th.value), {"16x16": float(ms[0]), "8x32": float(ms[1]), "32x8": float(ms[2])}
 

@@ -6,6 +6,7 @@
 // batch that fits).
 #include "sl_internal.h"
 #include "sl_tilespan.h"
+#include "sl_lighting.h"
 
 namespace sl {
 namespace {
@@ -82,8 +83,14 @@ __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __
             tile_vals[e] = slot;
             e++;
             atomicAdd(&h[0][tile & 0xffu], 1u);
-            atomicAdd(&h[1][(tile >> 8) & 0xffu], 1u);
-            atomicAdd(&h[2][(tile >> 16) & 0xffu], 1u);
+          }
+          // the upper digits are shared by a run of ids within one 256-block: one add per run
+          for (uint32_t a = row + t0; a <= row + t1;) {
+            const uint32_t run_end = min(row + t1, a | 0xffu);
+            const uint32_t n_run = run_end - a + 1u;
+            atomicAdd(&h[1][(a >> 8) & 0xffu], n_run);
+            atomicAdd(&h[2][(a >> 16) & 0xffu], n_run);
+            a = run_end + 1u;
           }
         }
       }
@@ -92,6 +99,48 @@ __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __
   __syncthreads();
   for (int q = 0; q < 3; q++)
     if (h[q][t]) atomicAdd(&digit_hist[256 * q + t], h[q][t]);
+}
+
+// shading-list flags: position g of the padded slots <-> the view's Gaussian order[g - slot_base] (shading order)
+__device__ __forceinline__ bool shade_candidate(const BatchView* views, const BatchScene* scenes,
+                                                const uint32_t* block_view, const uint32_t* keys32, uint32_t g,
+                                                uint32_t& view, uint32_t& gslot) {
+  const uint32_t v = block_view[g >> 8];
+  if (v == kNoView) return false;
+  const BatchView& V = views[v];
+  const BatchScene& S = scenes[V.scene];
+  const uint32_t j = g - V.slot_base;
+  if (V.P.view_mode != 3u || !S.lit || j >= V.P.count) return false;
+  view = v;
+  gslot = V.slot_base + S.order[j];
+  return (keys32[gslot] & 0xFFFFu) != 0xFFFFu;
+}
+
+__global__ void __launch_bounds__(kThreads) bshade_flags_kernel(const BatchView* __restrict__ views,
+                                                                const BatchScene* __restrict__ scenes,
+                                                                const uint32_t* __restrict__ block_view,
+                                                                const uint32_t* __restrict__ keys32,
+                                                                const uint32_t* __restrict__ totals, uint32_t n_max,
+                                                                uint32_t* __restrict__ flags) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= n_max) return;
+  uint32_t v, gslot;
+  flags[g] = (g < totals[0] && shade_candidate(views, scenes, block_view, keys32, g, v, gslot)) ? 1u : 0u;
+}
+
+__global__ void __launch_bounds__(kThreads) bshade_compact_kernel(const BatchView* __restrict__ views,
+                                                                  const BatchScene* __restrict__ scenes,
+                                                                  const uint32_t* __restrict__ block_view,
+                                                                  const uint32_t* __restrict__ flags,
+                                                                  const uint32_t* __restrict__ offsets,
+                                                                  const uint32_t* __restrict__ totals, uint32_t n_max,
+                                                                  uint32_t* __restrict__ list) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= n_max || g >= totals[0] || !flags[g]) return;
+  const uint32_t v = block_view[g >> 8];
+  const BatchView& V = views[v];
+  const uint32_t j = g - V.slot_base;
+  list[V.slot_base + (offsets[g] - offsets[V.slot_base])] = V.slot_base + scenes[V.scene].order[j];
 }
 
 __global__ void __launch_bounds__(kThreads) btile_runs_kernel(const uint32_t* __restrict__ keys,
@@ -127,6 +176,24 @@ cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const
   btile_emit_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(
       order, rects, recs, offsets, views, block_view, totals, n_max, tw, th, capacity, ctr, tile_keys, tile_vals,
       digit_hist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bshade_flags(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
+                                const uint32_t* keys32, const uint32_t* totals, uint32_t n_max, uint32_t* flags,
+                                cudaStream_t s) {
+  if (!n_max) return cudaSuccess;
+  bshade_flags_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(views, scenes, block_view, keys32, totals,
+                                                                             n_max, flags);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bshade_compact(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
+                                  const uint32_t* flags, const uint32_t* offsets, const uint32_t* totals,
+                                  uint32_t n_max, uint32_t* list, cudaStream_t s) {
+  if (!n_max) return cudaSuccess;
+  bshade_compact_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(views, scenes, block_view, flags,
+                                                                               offsets, totals, n_max, list);
   return cudaGetLastError();
 }
 

@@ -10,46 +10,8 @@
 #include <string>
 #include <vector>
 
-#include "sl_runtime.h"
+#include "sl_batch.h"
 
-namespace sl {
-int check_frame(const sl_render_frame* f, uint32_t count, uint32_t n_emitters, const std::vector<sl_part>& parts);
-void pack_project_params(const sl_render_frame* f, const std::vector<sl_part>& parts, uint32_t count,
-                         uint32_t n_emit, uint32_t tile_w, uint32_t tile_h, ProjectParams& P);
-}  // namespace sl
-
-struct sl_batch {
-  int device = 0;
-  std::vector<sl_renderer*> scenes;
-  std::vector<sl_lighting*> lights;
-  // capacity
-  uint32_t max_views = 0, max_blocks = 0, max_tiles = 0;
-  uint64_t max_slots = 0, entry_cap = 0;
-  uint32_t tile_w = 16, tile_h = 16;
-  float t_stop_scale = 1e-4f;
-  bool use_graph = true;
-  // device buffers
-  sl::DevBuf views, views_out, block_view, scenes_dev, dyn, keys32, keys_alt, vals_alt, order, recs, rects,
-      slot_counts, slot_offsets, tile_keys, tile_keys_alt, tile_vals, tile_vals_alt, status, tile_ctr, hist,
-      scan_scratch, run_start, run_end, tile_counts, tile_starts, ranges, counters, view_maxrad, view_visible;
-  // pinned staging
-  sl::BatchView* h_views = nullptr;
-  sl::BatchViewOut* h_out = nullptr;
-  uint32_t* h_block_view = nullptr;
-  sl::BatchScene* h_scenes = nullptr;
-  sl::BatchDyn* h_dyn = nullptr;
-  sl::FrameCounters* h_ctr = nullptr;
-  uint32_t* h_visible = nullptr;
-  // graph
-  cudaStream_t cap_stream = nullptr;
-  cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};  // per tile shape (16x16, 8x32, 32x8)
-  bool timing = false;
-  cudaEvent_t ev[2] = {nullptr, nullptr};
-  // last batch
-  uint32_t last_views = 0, last_slots = 0, last_tiles = 0, last_entries = 0;
-  std::vector<uint64_t> offsets;
-  std::vector<uint32_t> slot_base, tile_base, n_slots, tiles;
-};
 
 namespace sl {
 namespace {
@@ -167,8 +129,17 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   CK(launch_bproject(b->views.as<BatchView>(), b->block_view.as<uint32_t>(), B, b->keys32.as<uint32_t>(),
                      b->recs.as<SplatRec>(), b->rects.as<ushort4>(), hist, b->view_maxrad.as<uint32_t>(),
                      b->view_visible.as<uint32_t>(), s));
+  // the shading list (visible Gaussians of lit views in shading order, per view), then the shading pass
+  CK(launch_bshade_flags(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(),
+                         b->keys32.as<uint32_t>(), totals, S, b->slot_counts.as<uint32_t>(), s));
+  CK(exclusive_scan_u32(b->slot_counts.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), S, &ctr->shade_n,
+                        b->scan_scratch.ptr, ctr, s));
+  CK(launch_bshade_compact(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(),
+                           b->slot_counts.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), totals, S,
+                           b->vals_alt.as<uint32_t>(), s));
   CK(launch_bshade(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(), B,
-                   b->keys32.as<uint32_t>(), b->recs.as<SplatRec>(), b->view_maxrad.as<uint32_t>(), s));
+                   b->vals_alt.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), &ctr->shade_n, b->dyn.as<BatchDyn>(),
+                   b->recs.as<SplatRec>(), b->view_maxrad.as<uint32_t>(), s));
   const uint32_t max_tiles_sort = (uint32_t)(b->status.bytes / (4ull * 256 * 4));
   CK(sort32_pairs(b->keys32.as<uint32_t>(), b->keys_alt.as<uint32_t>(), nullptr, b->order.as<uint32_t>(),
                   b->vals_alt.as<uint32_t>(), S, totals, 16 + bits_for(V - 1), hist, b->status.as<uint32_t>(),
@@ -233,7 +204,7 @@ int fit_capacity(sl_batch* b, uint64_t slots, uint64_t tiles) {
 
 // Fills the pinned staging for this batch (views, outputs, block map, scenes, totals).
 void stage(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames, const float* eyes,
-           uint32_t n_views, float* out_dev, uint64_t slot, uint64_t tile) {
+           const float* light_scales, uint32_t n_views, float* out_dev, uint64_t slot, uint64_t tile) {
   for (uint32_t v = 0; v < n_views; v++) {
     sl_renderer* r = b->scenes[scene_of_view[v]];
     BatchView& V = b->h_views[v];
@@ -251,6 +222,7 @@ void stage(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* fr
     V.tile_base = b->tile_base[v];
     V.tiles_x = V.P.tiles_x;
     for (int c = 0; c < 3; c++) V.eye[c] = eyes[3 * v + c];
+    V.light_scale = light_scales ? light_scales[v] : 1.0f;
     BatchViewOut& O = b->h_out[v];
     O.tile_base = b->tile_base[v];
     O.tiles_x = V.P.tiles_x;
@@ -327,6 +299,93 @@ int launch_chain(sl_batch* b, cudaStream_t s, bool* replayed) {
 }
 
 }  // namespace
+
+namespace sl {
+
+int batch_layout(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames, uint32_t n_views,
+                 uint64_t* slots, uint64_t* tiles, uint64_t* pixels) {
+  b->slot_base.assign(n_views, 0);
+  b->tile_base.assign(n_views, 0);
+  b->n_slots.assign(n_views, 0);
+  b->tiles.assign(n_views, 0);
+  b->offsets.assign(n_views, 0);
+  uint64_t slot = 0, tile = 0, pix = 0;
+  for (uint32_t v = 0; v < n_views; v++) {
+    const uint32_t k = scene_of_view[v];
+    if (k >= b->scenes.size()) return fail(SL_ERR_INVALID_ARG, "view " + std::to_string(v) + ": bad scene index");
+    sl_renderer* r = b->scenes[k];
+    int rc = check_frame(&frames[v], r->count, r->n_emitters, r->parts);
+    if (rc) return view_fail(v, rc);
+    const uint32_t W = (uint32_t)frames[v].viewport[0], H = (uint32_t)frames[v].viewport[1];
+    const uint32_t n = r->count + 1u + (uint32_t)frames[v].palette[3][1];
+    const uint32_t tx = (W + b->tile_w - 1) / b->tile_w, ty = (H + b->tile_h - 1) / b->tile_h;
+    b->slot_base[v] = (uint32_t)slot;
+    b->n_slots[v] = n;
+    b->tile_base[v] = (uint32_t)tile;
+    b->tiles[v] = tx * ty;
+    b->offsets[v] = 4 * pix;
+    slot += ((uint64_t)n + 255) & ~255ull;
+    tile += (uint64_t)tx * ty;
+    pix += (uint64_t)W * H;
+    if (slot > kMaxCap) return fail(SL_ERR_INVALID_ARG, "batch too large (2^30 slots)");
+  }
+  *slots = slot;
+  *tiles = tile;
+  *pixels = pix;
+  return SL_OK;
+}
+
+int batch_fit(sl_batch* b, uint64_t slots, uint64_t tiles) { return fit_capacity(b, slots, tiles); }
+
+int batch_launch(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames, const float* eyes,
+                 const float* light_scales, uint32_t n_views, float* out_dev, uint64_t slots, uint64_t tiles,
+                 cudaStream_t s, bool* replayed) {
+  stage(b, scene_of_view, frames, eyes, light_scales, n_views, out_dev, slots, tiles);
+  cudaError_t e;
+  if (b->timing && (e = cudaEventRecord(b->ev[0], s)) != cudaSuccess) return cuda_fail(e, "timing");
+  int rc = launch_chain(b, s, replayed);
+  if (rc) return rc;
+  if (b->timing && (e = cudaEventRecord(b->ev[1], s)) != cudaSuccess) return cuda_fail(e, "timing");
+  return SL_OK;
+}
+
+int batch_finish(sl_batch* b, uint32_t n_views, uint64_t slots, uint64_t tiles, bool replayed, uint64_t* view_offsets,
+                 sl_batch_stats* stats, bool* retry) {
+  *retry = false;
+  const FrameCounters& hc = *b->h_ctr;
+  if (hc.overflow || hc.entries > b->entry_cap) {  // grow the tile-entry capacity: the caller launches again
+    const uint64_t want = (uint64_t)hc.entries + hc.entries / 4 + 4096;
+    if (b->entry_cap >= kMaxCap || hc.entries >= kMaxCap) return fail(SL_ERR_OVERFLOW, "tile entries beyond 2^30");
+    b->entry_cap = std::min<uint64_t>(std::max<uint64_t>(want, 2 * b->entry_cap), kMaxCap);
+    cudaError_t e = allocate(b);
+    if (e != cudaSuccess) return cuda_fail(e, "growing the tile entries");
+    *retry = true;
+    return SL_OK;
+  }
+  b->last_views = n_views;
+  b->last_slots = (uint32_t)slots;
+  b->last_tiles = (uint32_t)tiles;
+  b->last_entries = hc.entries;
+  if (view_offsets)
+    for (uint32_t v = 0; v < n_views; v++) view_offsets[v] = b->offsets[v];
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    stats->views = n_views;
+    stats->slots = (uint32_t)slots;
+    stats->tiles = (uint32_t)tiles;
+    stats->entries = hc.entries;
+    stats->fragments = hc.fragments;
+    uint64_t vis = 0;
+    for (uint32_t v = 0; v < n_views; v++) vis += b->h_visible[v];
+    stats->visible = vis;
+    stats->graph_replayed = replayed ? 1u : 0u;
+    if (b->timing) cudaEventElapsedTime(&stats->ms_total, b->ev[0], b->ev[1]);
+  }
+  if (hc.timeout) return fail(SL_ERR_TIMEOUT, "a bounded device-side wait gave up");
+  return SL_OK;
+}
+
+}  // namespace sl
 
 extern "C" {
 
@@ -415,89 +474,34 @@ int sl_batch_set_timing(sl_batch* b, int enabled) {
 }
 
 int sl_batch_render(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames, const float* eyes,
-                    uint32_t n_views, float* out_dev, uint64_t out_floats, uint64_t* view_offsets,
-                    sl_batch_stats* stats, void* stream) {
+                    const float* light_scales, uint32_t n_views, float* out_dev, uint64_t out_floats,
+                    uint64_t* view_offsets, sl_batch_stats* stats, void* stream) {
   if (!b || !scene_of_view || !frames || !eyes || !out_dev || n_views == 0) return fail(SL_ERR_INVALID_ARG, "null argument");
   if (n_views > b->max_views) return fail(SL_ERR_INVALID_ARG, "more views than the batch's max_views");
   if (reinterpret_cast<uintptr_t>(out_dev) % 16) return fail(SL_ERR_INVALID_ARG, "out_dev must be 16-byte aligned");
   cudaSetDevice(b->device);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  // per-view layout: slot ranges padded to 256, tile ranges, image offsets
-  b->slot_base.assign(n_views, 0);
-  b->tile_base.assign(n_views, 0);
-  b->n_slots.assign(n_views, 0);
-  b->tiles.assign(n_views, 0);
-  b->offsets.assign(n_views, 0);
   uint64_t slot = 0, tile = 0, pix = 0;
-  for (uint32_t v = 0; v < n_views; v++) {
-    const uint32_t k = scene_of_view[v];
-    if (k >= b->scenes.size()) return fail(SL_ERR_INVALID_ARG, "view " + std::to_string(v) + ": bad scene index");
-    sl_renderer* r = b->scenes[k];
-    int rc = check_frame(&frames[v], r->count, r->n_emitters, r->parts);
-    if (rc) return view_fail(v, rc);
-    const uint32_t W = (uint32_t)frames[v].viewport[0], H = (uint32_t)frames[v].viewport[1];
-    const uint32_t n = r->count + 1u + (uint32_t)frames[v].palette[3][1];
-    const uint32_t tx = (W + b->tile_w - 1) / b->tile_w, ty = (H + b->tile_h - 1) / b->tile_h;
-    b->slot_base[v] = (uint32_t)slot;
-    b->n_slots[v] = n;
-    b->tile_base[v] = (uint32_t)tile;
-    b->tiles[v] = tx * ty;
-    b->offsets[v] = 4 * pix;
-    slot += ((uint64_t)n + 255) & ~255ull;
-    tile += (uint64_t)tx * ty;
-    pix += (uint64_t)W * H;
-    if (slot > kMaxCap) return fail(SL_ERR_INVALID_ARG, "batch too large (2^30 slots)");
-  }
+  int rc = batch_layout(b, scene_of_view, frames, n_views, &slot, &tile, &pix);
+  if (rc) return rc;
   if (4 * pix > out_floats) return fail(SL_ERR_INVALID_ARG, "output buffer too small for the batch's images");
-  int rc = fit_capacity(b, slot, tile);
+  rc = batch_fit(b, slot, tile);
   if (rc) return rc;
   for (int attempt = 0; attempt < 3; attempt++) {
-    stage(b, scene_of_view, frames, eyes, n_views, out_dev, slot, tile);
-    cudaError_t e;
-    if (b->timing && (e = cudaEventRecord(b->ev[0], s)) != cudaSuccess) return cuda_fail(e, "timing");
-    bool replayed = false;
-    rc = launch_chain(b, s, &replayed);
+    bool replayed = false, retry = false;
+    rc = batch_launch(b, scene_of_view, frames, eyes, light_scales, n_views, out_dev, slot, tile, s, &replayed);
     if (rc) return rc;
-    if (b->timing && (e = cudaEventRecord(b->ev[1], s)) != cudaSuccess) return cuda_fail(e, "timing");
-    e = cudaStreamSynchronize(s);
+    cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "batch");
-    const FrameCounters& hc = *b->h_ctr;
-    if (hc.overflow || hc.entries > b->entry_cap) {  // grow the tile-entry capacity and render again
-      const uint64_t want = (uint64_t)hc.entries + hc.entries / 4 + 4096;
-      if (b->entry_cap >= kMaxCap || hc.entries >= kMaxCap) return fail(SL_ERR_OVERFLOW, "tile entries beyond 2^30");
-      b->entry_cap = std::min<uint64_t>(std::max<uint64_t>(want, 2 * b->entry_cap), kMaxCap);
-      e = allocate(b);
-      if (e != cudaSuccess) return cuda_fail(e, "growing the tile entries");
-      continue;
-    }
-    b->last_views = n_views;
-    b->last_slots = (uint32_t)slot;
-    b->last_tiles = (uint32_t)tile;
-    b->last_entries = hc.entries;
-    if (view_offsets)
-      for (uint32_t v = 0; v < n_views; v++) view_offsets[v] = b->offsets[v];
-    if (stats) {
-      memset(stats, 0, sizeof(*stats));
-      stats->views = n_views;
-      stats->slots = (uint32_t)slot;
-      stats->tiles = (uint32_t)tile;
-      stats->entries = hc.entries;
-      stats->fragments = hc.fragments;
-      uint64_t vis = 0;
-      for (uint32_t v = 0; v < n_views; v++) vis += b->h_visible[v];
-      stats->visible = vis;
-      stats->graph_replayed = replayed ? 1u : 0u;
-      if (b->timing) cudaEventElapsedTime(&stats->ms_total, b->ev[0], b->ev[1]);
-    }
-    if (hc.timeout) return fail(SL_ERR_TIMEOUT, "a bounded device-side wait gave up");
-    return SL_OK;
+    rc = batch_finish(b, n_views, slot, tile, replayed, view_offsets, stats, &retry);
+    if (rc || !retry) return rc;
   }
   return fail(SL_ERR_OVERFLOW, "tile entry capacity kept overflowing");
 }
 
 int sl_batch_autotune(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames, const float* eyes,
-                      uint32_t n_views, float* out_dev, uint64_t out_floats, uint32_t reps, uint32_t* tile_w,
-                      uint32_t* tile_h, float* ms_out, void* stream) {
+                      const float* light_scales, uint32_t n_views, float* out_dev, uint64_t out_floats,
+                      uint32_t reps, uint32_t* tile_w, uint32_t* tile_h, float* ms_out, void* stream) {
   if (!b) return fail(SL_ERR_INVALID_ARG, "null batch");
   static const uint32_t kShapes[3][2] = {{16, 16}, {8, 32}, {32, 8}};
   if (reps == 0) reps = 3;
@@ -510,10 +514,12 @@ int sl_batch_autotune(sl_batch* b, const uint32_t* scene_of_view, const sl_rende
     b->tile_w = kShapes[k][0];
     b->tile_h = kShapes[k][1];
     sl_batch_stats st;
-    int rc = sl_batch_render(b, scene_of_view, frames, eyes, n_views, out_dev, out_floats, nullptr, &st, stream);
+    int rc = sl_batch_render(b, scene_of_view, frames, eyes, light_scales, n_views, out_dev, out_floats, nullptr, &st,
+                             stream);
     float sum = 0.0f;
     for (uint32_t r = 0; rc == SL_OK && r < reps; r++) {
-      rc = sl_batch_render(b, scene_of_view, frames, eyes, n_views, out_dev, out_floats, nullptr, &st, stream);
+      rc = sl_batch_render(b, scene_of_view, frames, eyes, light_scales, n_views, out_dev, out_floats, nullptr, &st,
+                           stream);
       sum += st.ms_total;
     }
     if (rc) {

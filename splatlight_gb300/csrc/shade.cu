@@ -183,7 +183,10 @@ __global__ void __launch_bounds__(kThreads) shade_kernel(const __grid_constant__
 __global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __restrict__ views,
                                                           const BatchScene* __restrict__ scenes,
                                                           const uint32_t* __restrict__ block_view,
-                                                          const uint32_t* __restrict__ keys32,
+                                                          const uint32_t* __restrict__ list,
+                                                          const uint32_t* __restrict__ offsets,
+                                                          const uint32_t* __restrict__ shade_n,
+                                                          const BatchDyn* __restrict__ dyn,
                                                           SplatRec* __restrict__ recs,
                                                           uint32_t* __restrict__ view_maxrad) {
   __shared__ ShadeParams sSH;
@@ -193,21 +196,28 @@ __global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __res
   const BatchView& V = views[v];
   const BatchScene& S = scenes[V.scene];
   if (V.P.view_mode != 3u || !S.lit) return;
+  // this view's visible Gaussians: list[slot_base, slot_base + n_vis) (the exclusive scan of its flags)
+  const uint32_t first = offsets[V.slot_base];
+  const uint32_t last = v + 1u < dyn->n_views ? offsets[views[v + 1u].slot_base] : *shade_n;
+  const uint32_t j = (blockIdx.x / 2 - V.block_first) * 256u + (blockIdx.x & 1u) * kThreads + threadIdx.x;
+  if ((blockIdx.x / 2 - V.block_first) * 256u + (blockIdx.x & 1u) * kThreads >= last - first) return;
   const int t = threadIdx.x;
   if (t == 0) {
     sSH = S.SH;
     sSH.eye[0] = V.eye[0];
     sSH.eye[1] = V.eye[1];
     sSH.eye[2] = V.eye[2];
+    sSH.scale *= V.light_scale;  // the request's light state: every light's intensity scaled
+    for (uint32_t k = 0; k < 4; k++)
+      for (int c = 0; c < 3; c++) sSH.lights[k].irr[c] *= V.light_scale;
     s_max = 0u;
   }
   __syncthreads();
-  const uint32_t j = (blockIdx.x / 2 - V.block_first) * 256u + (blockIdx.x & 1u) * kThreads + t;
-  const uint32_t i = j < V.P.count ? S.order[j] : j;  // the scene's shading order
-  const uint32_t gslot = V.slot_base + i;
   float mx = 0.0f;
-  uint32_t material = kEmitterMaterial;
-  if (j < V.P.count && (keys32[gslot] & 0xFFFFu) != 0xFFFFu) {
+  uint32_t material = kEmitterMaterial, gslot = 0, i = 0;
+  if (j < last - first) {
+    gslot = list[V.slot_base + j];
+    i = gslot - V.slot_base;
     const sl_gaussian& G = reinterpret_cast<const sl_gaussian*>(V.gaussians)[i];
     uint32_t part = G.part_surface & 0xffffu;
     part = part > kMaxParts - 1u ? kMaxParts - 1u : part;
@@ -241,10 +251,11 @@ __global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __res
 }  // namespace
 
 cudaError_t launch_bshade(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
-                          uint32_t max_blocks, const uint32_t* keys32, SplatRec* recs, uint32_t* view_maxrad,
-                          cudaStream_t s) {
+                          uint32_t max_blocks, const uint32_t* list, const uint32_t* offsets, const uint32_t* shade_n,
+                          const BatchDyn* dyn, SplatRec* recs, uint32_t* view_maxrad, cudaStream_t s) {
   if (max_blocks == 0) return cudaSuccess;
-  bshade_kernel<<<2 * max_blocks, kThreads, 0, s>>>(views, scenes, block_view, keys32, recs, view_maxrad);
+  bshade_kernel<<<2 * max_blocks, kThreads, 0, s>>>(views, scenes, block_view, list, offsets, shade_n, dyn, recs,
+                                                    view_maxrad);
   return cudaGetLastError();
 }
 

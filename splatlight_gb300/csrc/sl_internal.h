@@ -51,7 +51,8 @@ struct FrameCounters {
   uint32_t overflow;       // entries beyond capacity
   uint32_t timeout;        // a bounded device wait gave up
   uint32_t fragments;      // fragments composited (kept and blended) by the compositor
-  uint32_t pad[2];
+  uint32_t shade_n;        // batched path: visible Gaussians of lit views (the shading list's length)
+  uint32_t pad;
 };
 
 // ---- launchers (each returns cudaError_t of the launch) ----------------------------------------------------------
@@ -132,6 +133,7 @@ struct BatchView {
   uint32_t block_first;                  // slot_base / 256
   uint32_t tile_base, tiles_x;           // first global tile, tiles per row
   float eye[3];                          // shading eye
+  float light_scale;                     // the request's light-intensity scale (emitters and distant lights)
 };
 constexpr uint32_t kNoView = 0xFFFFFFFFu;
 cudaError_t launch_bproject(const BatchView* views, const uint32_t* block_view, uint32_t max_blocks, uint32_t* keys32,
@@ -169,6 +171,16 @@ cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const
                               const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t capacity,
                               FrameCounters* ctr, uint32_t* tile_keys, uint32_t* tile_vals, uint32_t* digit_hist,
                               cudaStream_t s);
+// The batched shading list: per view, its visible Gaussians of lit views in its scene's shading order.  flags[g]
+// (g over every view's padded slots, shading-order position g - slot_base) is 1 when that Gaussian is visible;
+// after the exclusive scan of the flags into offsets, list[slot_base + k] is the k-th one's global slot.
+struct BatchScene;
+cudaError_t launch_bshade_flags(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
+                                const uint32_t* keys32, const uint32_t* totals, uint32_t n_max, uint32_t* flags,
+                                cudaStream_t s);
+cudaError_t launch_bshade_compact(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
+                                  const uint32_t* flags, const uint32_t* offsets, const uint32_t* totals,
+                                  uint32_t n_max, uint32_t* list, cudaStream_t s);
 cudaError_t launch_btile_runs(const uint32_t* keys, const uint32_t* n_dev, uint32_t n_max, uint32_t* run_start,
                               uint32_t* run_end, cudaStream_t s);
 

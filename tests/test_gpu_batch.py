@@ -173,6 +173,32 @@ def test_lit_views_many_eyes(cuda):
         La.close()
 
 
+def test_light_scale_matches_plain(cuda):
+    """A request's light-intensity scale: the batched view equals the per-view path with every light's intensity
+    (emitters and sun) scaled through the lighting setters (RGB within 1e-3)."""
+    _, b = _scenes()
+    b = scene.dataclasses.replace(b, shadow_res=256, sun_res=512)
+    k = 1.7
+    with SplatRenderer(b.gaussians, b.parts) as rb:
+        Lb = for_scene(rb, b)
+        Lb.update(b.eye, camera_forward(b))
+        views = [View(0, _frame(b, 320, 180, VIEW_LIT), b.eye, light_scale=k),
+                 View(0, _frame(b, 160, 90, VIEW_LIT), b.eye, light_scale=1.0)]
+        with BatchRenderer([rb], [Lb]) as B:
+            imgs = [im.copy() for im in B.render(views)]
+            base = rb.render(views[1].frame)
+            assert float(np.abs(imgs[1] - base).max()) <= RGB_TOL
+            Lb.set_emitters(b.emitters, scale=k)
+            sun = b.sun
+            Lb.set_environment([(sun.direction, sun.angular_std, tuple(np.float32(sun.irradiance) * np.float32(k)),
+                                 sun.casts_shadows)], b.sky_ambient)
+            Lb.update(b.eye, camera_forward(b))
+            scaled = rb.render(views[0].frame)
+            assert float(np.abs(imgs[0] - scaled).max()) <= RGB_TOL
+            assert float(imgs[0][..., :3].max()) > 0.0   # the lit image is not empty
+        Lb.close()
+
+
 def test_autotune_keeps_results(cuda):
     a, b = _scenes()
     with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
