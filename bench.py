@@ -243,6 +243,123 @@ def run_batch(args, stream, flush):
     return res
 
 
+SERVE_RES = [(512, 512), (1280, 720), (1920, 1080)]
+
+
+def serve_scenes():
+    """The 6 resident scenes of the serving workload: hill-like, 50k .. 3M Gaussians, seeds 10-15."""
+    from splatlight_gb300 import scene
+    counts = [50_000, 200_000, 500_000, 1_048_576, 2_097_152, 3_145_728]
+    return [scene.hill(n, seed=10 + k) for k, n in enumerate(counts)]
+
+
+def run_serving(args, rates=(100, 500, 2000)):
+    """Poisson arrivals at each rate for --serve-seconds: each request names one of 6 resident scenes, a camera on a
+    radius-U[3,8] sphere around the scene centre, a resolution from SERVE_RES and a light scale in U[0.5, 2]; the
+    server batches continuously (2 pipelines); latency = result on the host - arrival, wall clock."""
+    import threading
+
+    import torch
+    from splatlight_gb300 import camera
+    from splatlight_gb300.lighting import camera_forward, for_scene
+    from splatlight_gb300.renderer import SplatRenderer
+    from splatlight_gb300.server import RenderServer
+    scenes = serve_scenes()
+    rs, ls = [], []
+    for s in scenes:
+        r = SplatRenderer(s.gaussians, s.parts)
+        L = for_scene(r, s)
+        L.update(s.eye, camera_forward(s))
+        rs.append(r)
+        ls.append(L)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(42)
+
+    def request():
+        k = int(rng.integers(len(scenes)))
+        s = scenes[k]
+        W, H = SERVE_RES[int(rng.integers(len(SERVE_RES)))]
+        up = np.asarray(s.up, np.float64)
+        while True:
+            d = rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            if abs(float(d @ up)) < 0.95:
+                break
+        c = np.asarray(s.target, np.float64)
+        eye = tuple(np.float32(c + rng.uniform(3.0, 8.0) * d))
+        f = camera.make_frame(eye, tuple(c), s.up, s.fov_deg, W, H, s.count, far=s.far, view_mode=3,
+                              n_emit=len(s.emitters))
+        return k, f, eye, float(rng.uniform(0.5, 2.0))
+
+    out = {"workload": "Poisson arrivals over 6 resident hill-like scenes (50k, 200k, 500k, 1M, 2M, 3M Gaussians, "
+                       "seeds 10-15), cameras on radius U[3,8] spheres, 512^2 / 1280x720 / 1920x1080, light scale "
+                       "U[0.5,2], lit; images delivered to pinned host memory",
+           "seconds_per_rate": args.serve_seconds, "rates": []}
+    srv = RenderServer(rs, ls, max_views=64, pipelines=2, max_slots=48 << 20, max_pixels=24 << 20,
+                       max_tiles=1 << 19, result_slots=96)
+    # warm-up: capture the graphs, size the entry buffers
+    for k in range(16):
+        q = request()
+        srv.submit(*q, tag=k)
+    got = 0
+    while got < 16:
+        got += len(srv.poll(wait_us=50000, copy=False))
+    for lam in rates:
+        n = max(1, int(lam * args.serve_seconds))
+        gaps = rng.exponential(1.0 / lam, size=n)
+        reqs = [request() for _ in range(n)]
+        arrivals = {}
+        done = []
+        stop = threading.Event()
+
+        deadline = [None]
+
+        def poller():
+            while not stop.is_set() or len(done) < n:
+                for r in srv.poll(wait_us=2000, copy=False):
+                    done.append((r.tag, time.perf_counter(), r.status, r.batch_views))
+                if stop.is_set() and len(done) >= n:
+                    break
+                if deadline[0] is not None and time.perf_counter() > deadline[0]:
+                    break
+
+        th = threading.Thread(target=poller)
+        th.start()
+        t0 = time.perf_counter()
+        t_next = t0
+        for i, q in enumerate(reqs):
+            t_next += gaps[i]
+            while True:
+                dt = t_next - time.perf_counter()
+                if dt <= 0:
+                    break
+                time.sleep(min(dt, 0.0005))
+            arrivals[i] = time.perf_counter()
+            srv.submit(*q, tag=i)
+        t_sub = time.perf_counter()
+        deadline[0] = t_sub + 120.0
+        stop.set()
+        th.join()
+        t_end = max(t for _, t, _, _ in done)
+        lat = np.array([(t - arrivals[tag]) * 1000.0 for tag, t, st, _ in done if st == 0])
+        fails = sum(1 for _, _, st, _ in done if st != 0)
+        out["rates"].append({"lambda": lam, "requests": n, "failed": fails, "unfinished": n - len(done),
+                             "offered_per_s": round(n / (t_sub - t0), 1),
+                             "views_per_s": round(n / (t_end - t0), 1),
+                             "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                             "p99_ms": round(float(np.percentile(lat, 99)), 2),
+                             "mean_batch": round(float(np.mean([b for *_, b in done])), 1)})
+    st = srv.stats()
+    out["device_bytes"] = st["device_bytes"]
+    out["batches"] = st["batches"]
+    srv.close()
+    for L in ls:
+        L.close()
+    for r in rs:
+        r.close()
+    return out
+
+
 # bproject, shading flags, scan, compact, bshade, 3 depth-sort passes, tile counts, scan, emit, 3 tile-sort passes,
 # runs, run counts, scan, ranges, bcomposite
 BATCH_KERNELS = 20
@@ -284,6 +401,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the ragged-batch leg")
     ap.add_argument("--only-batch", action="store_true", help="the ragged-batch leg alone (its own JSON line)")
+    ap.add_argument("--only-serve", action="store_true", help="the serving leg alone (its own JSON line)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--serve-seconds", type=float, default=4.0, help="arrival window per rate (the config: 60)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -308,6 +428,13 @@ def main():
     __import__("__graft_entry__").build()
     from splatlight_gb300.renderer import SplatRenderer
 
+    if args.only_serve:
+        res = run_serving(args)
+        if rank == 0:
+            best = max(res["rates"], key=lambda x: x["views_per_s"])
+            print(json.dumps({"metric": "views/s", "value": best["views_per_s"], "unit": "views/s",
+                              "n_gpus": world, "serving": res}))
+        return
     if args.only_batch:
         stream = torch.cuda.Stream()
         flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -434,6 +561,9 @@ def main():
     batch = None
     if not args.no_batch:
         batch = run_batch(args, stream, flush)
+    serving = None
+    if not args.no_serve:
+        serving = run_serving(args)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -454,7 +584,7 @@ def main():
                 "gpu_launches": KERNELS_PER_FRAME * args.steps,
                 "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
                 "roofline": roofline, "sort_roofline": roof_sort, "composite_roofline": roof_comp,
-                "cpu_baseline": cpu, "clocks": clocks, "batched": batch}
+                "cpu_baseline": cpu, "clocks": clocks, "batched": batch, "serving": serving}
         print(json.dumps(line))
     L.close()
     r.close()

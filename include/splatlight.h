@@ -38,6 +38,7 @@ extern "C" {
 #define SL_ERR_ADMISSION (-7)     /* serving: the request does not fit the device-memory budget */
 #define SL_ERR_OVERFLOW (-8)      /* a fixed-capacity buffer (tile entries) was too small; grow and retry */
 #define SL_ERR_NO_DEVICE (-9)     /* no CUDA device, or the device is not an sm_103 part */
+#define SL_ERR_CANCELLED (-10)    /* serving: the server shut down before the request was admitted */
 
 /* ---- scene records (gs-runtime layout; shaders/common.wgsl:5-25, runtime/wgsl/common.wgsl:4-65) --------------- */
 
@@ -332,6 +333,68 @@ SL_API int sl_batch_autotune(sl_batch* b, const uint32_t* scene_of_view, const s
                              const float* eyes, const float* light_scales, uint32_t n_views, float* out_dev,
                              uint64_t out_floats, uint32_t reps, uint32_t* tile_w, uint32_t* tile_h, float* ms_out,
                              void* stream);
+
+/* ---- serving (no counterpart in the reference) ----------------------------------------------------------------- */
+
+/* A request server over resident scenes: requests (scene, RenderFrame, eye, light-intensity scale) arrive from any
+ * thread and are rendered by continuous batching -- a worker thread admits pending requests, first come first
+ * served, into the next batch of a free pipeline while the batch's slots, tiles and pixels fit its limits, launches
+ * it (the batched chain of sl_batch_render, as a replayed graph) and copies each image into a pinned result slot.
+ * With two or more pipelines a batch forms and launches while earlier ones run, so their work overlaps on the
+ * device.  Each result equals sl_batch_render of that request alone (same tile shape), whatever else shares its
+ * batch.  Device memory is fixed at creation (scenes + pipelines); a request whose footprint exceeds an empty batch
+ * is refused at submit (SL_ERR_ADMISSION).  The renderers and lightings must stay unchanged while the server runs. */
+typedef struct sl_server sl_server;
+
+typedef struct sl_server_options {
+  uint32_t max_views;            /* requests per batch (0 = 64, at most 256) */
+  uint32_t pipelines;            /* batches in flight (0 = 2, at most 8) */
+  uint64_t max_slots;            /* padded slots per batch (0 = 32 Mi) */
+  uint64_t max_pixels;           /* image pixels per batch (0 = 32 Mi) */
+  uint64_t max_view_pixels;      /* pixels of one request (0 = 1920 x 1080): the size of a result slot */
+  uint64_t hbm_budget_bytes;     /* device memory the pipelines may take (0 = unchecked) */
+  uint32_t max_tiles;            /* tiles per batch (0 = 512 Ki) */
+  uint32_t result_slots;         /* pinned result slots (0 = 2 x max_views) */
+  uint32_t tile_w, tile_h;       /* 16x16 (default), 8x32 or 32x8 */
+} sl_server_options;
+
+typedef struct sl_server_request {
+  uint32_t scene;                /* index into the server's scenes */
+  float eye[3];                  /* camera position (lit radiance) */
+  float light_scale;             /* intensity scale of the scene's lights (1 = as set) */
+  uint32_t pad;
+  sl_render_frame frame;
+} sl_server_request;
+
+typedef struct sl_server_result {
+  uint64_t tag;                  /* the submit's tag */
+  int32_t status;                /* SL_OK, or why the request failed (SL_ERR_CANCELLED: never admitted) */
+  uint32_t batch_views;          /* requests in the batch it ran in */
+  uint32_t width, height;
+  uint32_t result_slot;          /* release with sl_server_release after reading the image */
+  uint32_t pad;
+  double t_submit, t_start, t_done; /* seconds since the server started: submitted, launched, results ready */
+  const float* image;            /* height x width x 4 linear RGBA in pinned host memory (NULL on failure) */
+} sl_server_result;
+
+typedef struct sl_server_stats {
+  uint64_t submitted, completed, rejected, failed, batches, batch_views, graph_replays, pending;
+  uint64_t device_bytes;         /* scenes + pipeline buffers */
+  uint64_t free_result_slots;
+} sl_server_stats;
+
+SL_API int sl_server_create(sl_renderer* const* renderers, sl_lighting* const* lightings, uint32_t n_scenes,
+                            const sl_server_options* opt, sl_server** out);
+/* Queues one request (validated here: SL_ERR_INVALID_ARG, or SL_ERR_ADMISSION when it can never fit a batch). */
+SL_API int sl_server_submit(sl_server* s, const sl_server_request* req, uint64_t tag);
+/* Up to cap finished results (waits up to wait_us microseconds for the first); *n_out = how many. */
+SL_API int sl_server_poll(sl_server* s, sl_server_result* out, uint32_t cap, uint32_t* n_out, uint32_t wait_us);
+/* Returns a result slot to the pool (its image pointer is invalid afterwards). */
+SL_API int sl_server_release(sl_server* s, uint32_t result_slot);
+SL_API int sl_server_get_stats(sl_server* s, sl_server_stats* stats);
+/* Stops accepting requests, finishes the admitted and pending ones while result slots last (the rest are cancelled),
+ * and frees everything. */
+SL_API int sl_server_destroy(sl_server* s);
 
 #ifdef __cplusplus
 }

@@ -14,6 +14,7 @@ SL_OK = 0
 ERRORS = {
     -1: "SL_ERR_INVALID_ARG", -2: "SL_ERR_LAYOUT", -3: "SL_ERR_OOM", -4: "SL_ERR_CUDA", -5: "SL_ERR_TIMEOUT",
     -6: "SL_ERR_UNSUPPORTED", -7: "SL_ERR_ADMISSION", -8: "SL_ERR_OVERFLOW", -9: "SL_ERR_NO_DEVICE",
+    -10: "SL_ERR_CANCELLED",
 }
 
 
@@ -45,6 +46,24 @@ class BatchStats(C.Structure):
     _fields_ = [("views", C.c_uint32), ("slots", C.c_uint32), ("tiles", C.c_uint32), ("entries", C.c_uint32),
                 ("visible", C.c_uint64), ("fragments", C.c_uint64), ("ms_total", C.c_float),
                 ("graph_replayed", C.c_uint32)]
+
+
+class ServerOptions(C.Structure):
+    _fields_ = [("max_views", C.c_uint32), ("pipelines", C.c_uint32), ("max_slots", C.c_uint64),
+                ("max_pixels", C.c_uint64), ("max_view_pixels", C.c_uint64), ("hbm_budget_bytes", C.c_uint64),
+                ("max_tiles", C.c_uint32), ("result_slots", C.c_uint32), ("tile_w", C.c_uint32),
+                ("tile_h", C.c_uint32)]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("tag", C.c_uint64), ("status", C.c_int32), ("batch_views", C.c_uint32), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("result_slot", C.c_uint32), ("pad", C.c_uint32), ("t_submit", C.c_double),
+                ("t_start", C.c_double), ("t_done", C.c_double), ("image", C.POINTER(C.c_float))]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("submitted", "completed", "rejected", "failed", "batches", "batch_views",
+                                         "graph_replays", "pending", "device_bytes", "free_result_slots")]
 
 
 _P = C.c_void_p
@@ -85,6 +104,12 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_batch_set_timing": (_I, [_P, _I]),
     "sl_batch_render": (_I, [_P, _P, _P, _P, _P, _U32, _P, _U64, _P, C.POINTER(BatchStats), _P]),
     "sl_batch_read_view": (_I, [_P, _U32, _P, _P, _P, _U64, C.POINTER(_U64)]),
+    "sl_server_create": (_I, [_P, _P, _U32, C.POINTER(ServerOptions), C.POINTER(_P)]),
+    "sl_server_submit": (_I, [_P, _P, _U64]),
+    "sl_server_poll": (_I, [_P, C.POINTER(ServerResult), _U32, C.POINTER(_U32), _U32]),
+    "sl_server_release": (_I, [_P, _U32]),
+    "sl_server_get_stats": (_I, [_P, C.POINTER(ServerStats)]),
+    "sl_server_destroy": (_I, [_P]),
     "sl_batch_autotune": (_I, [_P, _P, _P, _P, _P, _U32, _P, _U64, _U32, C.POINTER(_U32), C.POINTER(_U32),
                                _P, _P]),
 }
