@@ -360,6 +360,44 @@ def run_serving(args, rates=(100, 500, 2000)):
     return out
 
 
+def run_diff(args, stream, flush):
+    """Inverse-rendering steps (forward + L2 loss + hand-written backward) on 500k hill-like Gaussians at 800x800
+    against a target rendered from perturbed parameters; device time per step, L2 flushed between steps."""
+    import torch
+    from splatlight_gb300 import camera, scene
+    from splatlight_gb300.diff import DiffRenderer, params_from_scene, perturb
+    s = scene.hill(500_000, seed=1)
+    params, lights = params_from_scene(s, n_lights=8)
+    f = camera.make_frame(s.eye, s.target, s.up, s.fov_deg, 800, 800, s.count, far=s.far, view_mode=3, n_emit=0)
+    D = DiffRenderer(s.count)
+    Pt, Lt = D.to_device(perturb(params, np.random.default_rng(2)), lights)
+    target = D.forward(Pt, Lt, f, s.eye)
+    P, Lt = D.to_device(params, lights)
+    sc = stream.cuda_stream
+    for _ in range(max(args.warmup, 3)):
+        with torch.cuda.stream(stream):
+            D.step(P, Lt, f, s.eye, target, stream=sc)
+    ts = []
+    loss = 0.0
+    for _ in range(max(3, min(args.steps, 10))):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        loss, G, _ = D.step(P, Lt, f, s.eye, target, stream=sc)
+        b.record(stream)
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    ms = statistics.median(ts)
+    gnorm = {k: float(v.norm().item()) for k, v in G.items()}
+    D.close()
+    return {"workload": "500,000 hill-like Gaussians (seed 1), 800x800, 8 point lights; target from parameters "
+                        "perturbed N(0,0.02) means / log-scales, N(0,0.1) opacity logits, N(0,0.05) albedo",
+            "ms_per_step": round(ms, 3), "steps_per_s": round(1000.0 / ms, 2), "loss": loss,
+            "grad_norms": {k: round(v, 6) for k, v in gnorm.items()}}
+
+
 # bproject, shading flags, scan, compact, bshade, 3 depth-sort passes, tile counts, scan, emit, 3 tile-sort passes,
 # runs, run counts, scan, ranges, bcomposite
 BATCH_KERNELS = 20
@@ -403,6 +441,8 @@ def main():
     ap.add_argument("--only-batch", action="store_true", help="the ragged-batch leg alone (its own JSON line)")
     ap.add_argument("--only-serve", action="store_true", help="the serving leg alone (its own JSON line)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--only-diff", action="store_true", help="the differentiation leg alone (its own JSON line)")
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiation leg")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="arrival window per rate (the config: 60)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -428,6 +468,14 @@ def main():
     __import__("__graft_entry__").build()
     from splatlight_gb300.renderer import SplatRenderer
 
+    if args.only_diff:
+        stream = torch.cuda.Stream()
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        res = run_diff(args, stream, flush)
+        if rank == 0:
+            print(json.dumps({"metric": "inverse-rendering steps/s", "value": res["steps_per_s"], "unit": "steps/s",
+                              "n_gpus": world, "differentiation": res}))
+        return
     if args.only_serve:
         res = run_serving(args)
         if rank == 0:
@@ -564,6 +612,9 @@ def main():
     serving = None
     if not args.no_serve:
         serving = run_serving(args)
+    differentiation = None
+    if not args.no_diff:
+        differentiation = run_diff(args, stream, flush)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -584,7 +635,8 @@ def main():
                 "gpu_launches": KERNELS_PER_FRAME * args.steps,
                 "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
                 "roofline": roofline, "sort_roofline": roof_sort, "composite_roofline": roof_comp,
-                "cpu_baseline": cpu, "clocks": clocks, "batched": batch, "serving": serving}
+                "cpu_baseline": cpu, "clocks": clocks, "batched": batch, "serving": serving,
+                "differentiation": differentiation}
         print(json.dumps(line))
     L.close()
     r.close()

@@ -334,6 +334,51 @@ SL_API int sl_batch_autotune(sl_batch* b, const uint32_t* scene_of_view, const s
                              uint64_t out_floats, uint32_t reps, uint32_t* tile_w, uint32_t* tile_h, float* ms_out,
                              void* stream);
 
+/* ---- differentiable rendering (no counterpart in the reference) ------------------------------------------------- */
+
+/* An inverse-rendering step over free per-Gaussian parameters: the forward projects them as the splat path does
+ * (view-space covariance, 2D conic with the low-pass dilation, peak optical depth tau0 = softplus(opacity logit)
+ * sqrt(det0/det) / (s0 sqrt(q_d)); shaders/project.wgsl:237-261 with kappa = softplus(logit) / (sqrt(2 pi) s0)),
+ * shades each Gaussian by point emitters -- albedo (ambient + sum_l s_l Le_l max(n.w,0) / (pi d^2)) + ks sum_l s_l Le_l
+ * max(n.w,0) exp((n.h - 1) / r^2) / (pi r^2 d^2), n the short axis facing the eye, r the roughness -- and composites
+ * front to back with alpha = min(1 - exp(-tau0 e^{-q/2}), 0.99), fragments of optical depth below 1e-6 skipped and a
+ * pixel stopping before its transmittance would fall below 1e-4 (16x16 tiles, the same depth keys and stable sort).
+ * The backward of L = sum over pixels and rgb of (image - target)^2 walks each tile list back to front, recomputing
+ * transmittance from the final value (no per-pixel fragment lists).  All arrays are device pointers. */
+typedef struct sl_diff sl_diff;
+
+typedef struct sl_diff_scene {
+  const float* means;            /* n x 3, world */
+  const float* log_scales;       /* n x 3 */
+  const float* quats;            /* n x 4 (x, y, z, w), normalised in the forward */
+  const float* opacity_logits;   /* n */
+  const float* albedo;           /* n x 3 */
+  const float* roughness;        /* n, > 0 */
+  uint32_t n, n_lights;          /* n_lights <= 32 */
+  const float* light_pos;        /* n_lights x 3 */
+  const float* light_le;         /* n_lights x 3: emitted radiance at scale 1 */
+  const float* light_scale;      /* n_lights: the intensities being optimised */
+  float ambient, ks;
+} sl_diff_scene;
+
+typedef struct sl_diff_grads {   /* same shapes as the parameters; every array is overwritten */
+  float *means, *log_scales, *quats, *opacity_logits, *albedo, *roughness, *light_scale;
+} sl_diff_grads;
+
+SL_API int sl_diff_create(uint32_t n, sl_diff** out);
+SL_API int sl_diff_destroy(sl_diff* d);
+/* The forward alone: W x H x 4 RGBA (alpha = 1 - T) into image_dev.  Camera, viewport, near/far and low-pass from
+ * frame; eye = the camera position for the shading. */
+SL_API int sl_diff_forward(sl_diff* d, const sl_diff_scene* scene, const sl_render_frame* frame, const float* eye,
+                           float* image_dev, void* stream);
+/* Forward + backward against target_dev (W x H x 4; rgb used): gradients into grads, the loss to *loss, the image to
+ * image_dev if not NULL.  Returns after the step completed. */
+SL_API int sl_diff_step(sl_diff* d, const sl_diff_scene* scene, const sl_render_frame* frame, const float* eye,
+                        const float* target_dev, float* image_dev, const sl_diff_grads* grads, double* loss,
+                        void* stream);
+/* The depth order of the last forward (host; n_visible entries, far to near). */
+SL_API int sl_diff_read_order(sl_diff* d, uint32_t* order, uint32_t* n_visible);
+
 /* ---- serving (no counterpart in the reference) ----------------------------------------------------------------- */
 
 /* A request server over resident scenes: requests (scene, RenderFrame, eye, light-intensity scale) arrive from any

@@ -66,6 +66,18 @@ class ServerStats(C.Structure):
                                          "graph_replays", "pending", "device_bytes", "free_result_slots")]
 
 
+class DiffScene(C.Structure):
+    _fields_ = [("means", C.c_void_p), ("log_scales", C.c_void_p), ("quats", C.c_void_p),
+                ("opacity_logits", C.c_void_p), ("albedo", C.c_void_p), ("roughness", C.c_void_p),
+                ("n", C.c_uint32), ("n_lights", C.c_uint32), ("light_pos", C.c_void_p), ("light_le", C.c_void_p),
+                ("light_scale", C.c_void_p), ("ambient", C.c_float), ("ks", C.c_float)]
+
+
+class DiffGrads(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("means", "log_scales", "quats", "opacity_logits", "albedo", "roughness",
+                                         "light_scale")]
+
+
 _P = C.c_void_p
 _U32 = C.c_uint32
 _U64 = C.c_uint64
@@ -104,6 +116,11 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_batch_set_timing": (_I, [_P, _I]),
     "sl_batch_render": (_I, [_P, _P, _P, _P, _P, _U32, _P, _U64, _P, C.POINTER(BatchStats), _P]),
     "sl_batch_read_view": (_I, [_P, _U32, _P, _P, _P, _U64, C.POINTER(_U64)]),
+    "sl_diff_create": (_I, [_U32, C.POINTER(_P)]),
+    "sl_diff_destroy": (_I, [_P]),
+    "sl_diff_forward": (_I, [_P, C.POINTER(DiffScene), _P, _P, _P, _P]),
+    "sl_diff_step": (_I, [_P, C.POINTER(DiffScene), _P, _P, _P, _P, C.POINTER(DiffGrads), C.POINTER(C.c_double), _P]),
+    "sl_diff_read_order": (_I, [_P, _P, C.POINTER(_U32)]),
     "sl_server_create": (_I, [_P, _P, _U32, C.POINTER(ServerOptions), C.POINTER(_P)]),
     "sl_server_submit": (_I, [_P, _P, _U64]),
     "sl_server_poll": (_I, [_P, C.POINTER(ServerResult), _U32, C.POINTER(_U32), _U32]),
