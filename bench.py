@@ -37,6 +37,8 @@ FALLBACK_HBM = 6800.0  # GB/s
 # shade; project, 2 depth-sort passes, tile counts, scan, emit, 2 tile-sort passes, tile runs, run counts, scan,
 # ranges, composite
 KERNELS_PER_FRAME = 14
+# DRAM bytes per Gaussian of one shade_kernel launch (read + write), from ncu on the 1,048,576-Gaussian frame
+SHADE_DRAM_BYTES_PER_G = (464.748544e6 + 22.484992e6) / 1048576
 
 
 def peaks():
@@ -360,6 +362,65 @@ def run_serving(args, rates=(100, 500, 2000)):
     return out
 
 
+def run_sort(args, stream, flush, n=1 << 26):
+    """The stable radix sort alone on n random keys: 16-bit (2 passes, sl_sort_keys16) and 24-bit segmented-style
+    32-bit keys (3 passes, sl_sort_keys32), device time per call (digit histograms + passes + scratch clears), against
+    the library sort (torch.sort, stable: CUB's radix sort) on the same keys.  Bandwidth uses the algorithmic bytes
+    per element 4 + 16 P (P passes; a key+value read and write per pass plus one key read for the histograms)."""
+    import ctypes as C
+
+    import torch
+    from splatlight_gb300 import _native as N
+    lib = N.lib()
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    k16 = torch.randint(0, 65536, (n,), device="cuda", dtype=torch.int32, generator=g)
+    k16h = k16.to(torch.int16)    # the same values as u16 bits
+    k24 = torch.randint(0, 1 << 24, (n,), device="cuda", dtype=torch.int32, generator=g)
+    order = torch.empty(n, dtype=torch.int32, device="cuda")
+    sc = stream.cuda_stream
+    hbm, _, peak_kind = peaks()
+
+    def timed(fn, reps):
+        ts = []
+        for _ in range(reps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.median(ts)
+
+    def ours16():
+        N.check(lib.sl_sort_keys16(k16h.data_ptr(), n, order.data_ptr(), C.c_void_p(sc)))
+
+    def ours24():
+        N.check(lib.sl_sort_keys32(k24.data_ptr(), n, 24, order.data_ptr(), C.c_void_p(sc)))
+
+    def lib16():
+        with torch.cuda.stream(stream):
+            torch.sort(k16, stable=True)
+
+    def lib24():
+        with torch.cuda.stream(stream):
+            torch.sort(k24, stable=True)
+
+    res = {"n": n, "peak_gbs": hbm, "peak_kind": peak_kind}
+    for name, fn, passes in (("ours_16bit", ours16, 2), ("ours_24bit", ours24, 3), ("library_16bit", lib16, 2),
+                             ("library_24bit", lib24, 3)):
+        for _ in range(3):
+            fn()
+        ms = timed(fn, 5)
+        b = (4 + 16 * passes) * n
+        res[name] = {"ms": round(ms, 4), "gbs": round(b / (ms * 1e-3) / 1e9, 1),
+                     "frac": round(b / (ms * 1e-3) / 1e9 / hbm, 4), "bytes_per_elem": 4 + 16 * passes}
+    return res
+
+
 def run_diff(args, stream, flush):
     """Inverse-rendering steps (forward + L2 loss + hand-written backward) on 500k hill-like Gaussians at 800x800
     against a target rendered from perturbed parameters; device time per step, L2 flushed between steps."""
@@ -442,6 +503,8 @@ def main():
     ap.add_argument("--only-serve", action="store_true", help="the serving leg alone (its own JSON line)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--only-diff", action="store_true", help="the differentiation leg alone (its own JSON line)")
+    ap.add_argument("--only-sort", action="store_true", help="the sort leg alone (its own JSON line)")
+    ap.add_argument("--sort-n", type=int, default=1 << 26, help="keys for the sort leg")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiation leg")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="arrival window per rate (the config: 60)")
     args = ap.parse_args()
@@ -468,6 +531,14 @@ def main():
     __import__("__graft_entry__").build()
     from splatlight_gb300.renderer import SplatRenderer
 
+    if args.only_sort:
+        stream = torch.cuda.Stream()
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        res = run_sort(args, stream, flush, args.sort_n)
+        if rank == 0:
+            print(json.dumps({"metric": "sort GB/s", "value": res["ours_24bit"]["gbs"], "unit": "GB/s",
+                              "n_gpus": world, "sort": res}))
+        return
     if args.only_diff:
         stream = torch.cuda.Stream()
         flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -603,8 +674,17 @@ def main():
                  "frac": round(comp_tflops / fp32_peak, 4), "traffic": None,
                  "peak_kind": "nominal FP32 issue rate at the sampled max SM clock (no measured FP32 peak exists)",
                  "algorithmic_flops_per_launch": 20.0 * frag, "kernel": "composite_kernel<16>"}
+    # shading pass (the lighting stage in steady state): survey 8(d) counts 336 B per Gaussian (record, leaf node,
+    # V grid, lamp T, env T in; radiance out); its DRAM traffic per Gaussian from the ncu capture in
+    # profiles/shade_kernel_hill1m.md (487 MB for 1,048,576 Gaussians); it is issue-bound (the same profile)
+    shade_bytes = 336.0 * s.count
+    shade_gbs = shade_bytes / (stage_ms["lighting"] * 1e-3) / 1e9
+    roof_shade = {"bound": "hbm", "achieved": round(shade_gbs, 1), "peak": hbm, "unit": "GB/s",
+                  "frac": round(shade_gbs / hbm, 4), "traffic": round(SHADE_DRAM_BYTES_PER_G * s.count),
+                  "peak_kind": peak_kind, "algorithmic_bytes_per_launch": shade_bytes,
+                  "kernel": "shade_kernel (issue-bound: see profiles/shade_kernel_hill1m.md)"}
     dominant = max(stage_ms, key=stage_ms.get)
-    roofline = roof_comp if dominant == "composite" else roof_sort
+    roofline = {"composite": roof_comp, "lighting": roof_shade}.get(dominant, roof_sort)
 
     batch = None
     if not args.no_batch:
@@ -615,6 +695,7 @@ def main():
     differentiation = None
     if not args.no_diff:
         differentiation = run_diff(args, stream, flush)
+    sort_leg = run_sort(args, stream, flush)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -635,8 +716,9 @@ def main():
                 "gpu_launches": KERNELS_PER_FRAME * args.steps,
                 "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
                 "roofline": roofline, "sort_roofline": roof_sort, "composite_roofline": roof_comp,
+                "shade_roofline": roof_shade,
                 "cpu_baseline": cpu, "clocks": clocks, "batched": batch, "serving": serving,
-                "differentiation": differentiation}
+                "differentiation": differentiation, "sort": sort_leg}
         print(json.dumps(line))
     L.close()
     r.close()

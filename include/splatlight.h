@@ -263,9 +263,14 @@ SL_API int sl_renderer_bind_lighting(sl_renderer* r, sl_lighting* l);
 /* The stable sort of 16-bit depth keys on its own (shaders/radix.wgsl:1-139; encoded by src/renderer.js:425-434):
  * writes to order_dev the permutation that sorts keys_dev[0, n) ascending, ties in index order (radix.wgsl's vals_out
  * after its last pass, values = index).  Device pointers; n < 2^30.  Scratch is allocated stream-ordered on `stream`
- * and released before return; the call returns after the sort completed (SL_ERR_TIMEOUT if a bounded device-side
+ * from a memory pool private to the library (its memory kept between calls) and returned to it before return; the call returns after the sort completed (SL_ERR_TIMEOUT if a bounded device-side
  * wait gave up). */
 SL_API int sl_sort_keys16(const uint16_t* keys_dev, uint32_t n, uint32_t* order_dev, void* stream);
+
+/* The same stable sort for 32-bit keys of which the low `bits` are significant (1..32; one onesweep pass per 8 bits):
+ * the segmented form the batched path sorts with (view id above the 16 depth bits; tile ids of many views).  keys_dev
+ * is left intact.  No reference counterpart beyond radix.wgsl's 16-bit case. */
+SL_API int sl_sort_keys32(const uint32_t* keys_dev, uint32_t n, uint32_t bits, uint32_t* order_dev, void* stream);
 
 /* sl_sort_keys16 without any device allocation, for callers that may not allocate (a host engine that owns all
  * device memory through its own pool under a hard cap, or a frame loop whose latency budget rules out allocator

@@ -110,6 +110,7 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_renderer_bind_lighting": (_I, [_P, _P]),
     "sl_sort_keys16": (_I, [_P, _U32, _P, _P]),
     "sl_sort_keys16_noalloc": (_I, [_P, _U32, _P, _P]),
+    "sl_sort_keys32": (_I, [_P, _U32, _U32, _P, _P]),
     "sl_batch_create": (_I, [_P, _P, _U32, C.POINTER(BatchOptions), C.POINTER(_P)]),
     "sl_batch_destroy": (_I, [_P]),
     "sl_batch_set_tile": (_I, [_P, _U32, _U32]),

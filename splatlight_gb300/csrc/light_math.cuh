@@ -371,6 +371,107 @@ __device__ inline float asg_phase(f3 wi, f3 lb0, f3 lb1, s2m sl, f3 n0, f3 t1, f
   return mixf(p_asg, p_pt, t);
 }
 
+// ---- the same specular and ASG phases with their per-Gaussian parts computed once (the shading pass evaluates them
+// for every light of a Gaussian's cut; only the light's direction and lobe change between calls) ----------------
+struct SpecPre {
+  f3 Sd, So;
+  float det, c0;                       // max(det S, 1e-20), pi sqrt(det)
+  float a00, a11, a22, a01, a02, a12;  // adjugate of S
+};
+__device__ __forceinline__ SpecPre spec_prepare(f3 Sd, f3 So) {
+  SpecPre p;
+  p.Sd = Sd;
+  p.So = So;
+  p.det = fmaxf(sym_det(Sd, So), 1e-20f);
+  p.c0 = kPi * sqrtf(p.det);
+  p.a00 = Sd.y * Sd.z - So.z * So.z;
+  p.a11 = Sd.x * Sd.z - So.y * So.y;
+  p.a22 = Sd.x * Sd.y - So.x * So.x;
+  p.a01 = So.y * So.z - So.x * Sd.z;
+  p.a02 = So.x * So.z - So.y * Sd.y;
+  p.a12 = So.x * So.y - Sd.x * So.z;
+  return p;
+}
+__device__ __forceinline__ float phase_specular_p(const SpecPre& p, f3 wi, f3 wo) {
+  f3 h = add3(wi, wo);
+  float hl = len3(h);
+  if (hl < 1e-6f) return 0.0f;
+  f3 w = div3(h, hl);
+  float adj = p.a00 * w.x * w.x + p.a11 * w.y * w.y + p.a22 * w.z * w.z +
+              2.0f * (p.a01 * w.x * w.y + p.a02 * w.x * w.z + p.a12 * w.y * w.z);
+  float q = adj / p.det;
+  float D = 1.0f / (p.c0 * q * q);
+  float sigma = sqrtf(fmaxf(dot3(wi, sym_mul(p.Sd, p.So, wi)), 1e-12f));
+  return D / (4.0f * sigma);
+}
+struct AsgPre {
+  bool aniso;
+  f3 wr, rb0, rb1;
+  s2m s0;
+  float pk, minor0;
+};
+// the parts of asg_phase (material_ext.wgsl:127-181) that depend on the Gaussian and the view only
+__device__ __forceinline__ AsgPre asg_prepare(f3 n0, f3 t1, f3 t2, f3 flake, f3 Sd, f3 So, f3 wo) {
+  const float ASG_A0 = 2.54696f;
+  AsgPre a;
+  a.aniso = !(flake.x <= fmaxf(flake.y, flake.z) * 1.0001f);
+  float co = dot3(n0, wo);
+  f3 n = co >= 0.0f ? n0 : mul3(n0, -1.0f);
+  float cos_o = fabsf(co);
+  a.wr = sub3(mul3(n, 2.0f * cos_o), wo);
+  onb(a.wr, a.rb0, a.rb1);
+  f3 dw1 = add3(mul3(n, 2.0f * dot3(wo, t1)), mul3(t1, 2.0f * cos_o));
+  f3 dw2 = add3(mul3(n, 2.0f * dot3(wo, t2)), mul3(t2, 2.0f * cos_o));
+  f2 j0 = F2(dot3(a.rb0, dw1), dot3(a.rb0, dw2));
+  f2 j1 = F2(dot3(a.rb1, dw1), dot3(a.rb1, dw2));
+  f2 ia = F2(flake.y / (flake.x - flake.y), flake.z / (flake.x - flake.z));
+  a.s0 = s2m{dot2(F2(j0.x * j0.x, j0.y * j0.y), ia), dot2(F2(j0.x * j1.x, j0.y * j1.y), ia),
+             dot2(F2(j1.x * j1.x, j1.y * j1.y), ia)};
+  a.pk = flake.x * flake.x / (kPi * sqrtf(flake.x * flake.y * flake.z)) /
+         (4.0f * sqrtf(fmaxf(dot3(a.wr, sym_mul(Sd, So, a.wr)), 1e-12f)));
+  a.minor0 = fmaxf(s2_minor(a.s0) / (2.0f * ASG_A0), 1e-30f);
+  return a;
+}
+__device__ __forceinline__ float asg_phase_p(const AsgPre& a, const SpecPre& sp, f3 wi, f3 lb0, f3 lb1, s2m sl,
+                                             f3 wo) {
+  const float ASG_W[3] = {0.61163f, 0.35083f, 0.0267f};
+  const float ASG_A[3] = {2.54696f, 0.6893f, 0.10727f};
+  float pc = phase_specular_p(sp, wi, wo);
+  if (!a.aniso) return pc;
+  f3 cs = add3(wi, a.wr);
+  float cl = len3(cs);
+  if (cl < 1e-4f) return pc;
+  f3 c = div3(cs, cl);
+  f3 cb0, cb1;
+  onb(c, cb0, cb1);
+  f2 dm = sub2(log_map(c, cb0, cb1, a.wr), log_map(c, cb0, cb1, wi));
+  s2m sL = s2_xf(sl, F2(dot3(cb0, lb0), dot3(cb0, lb1)), F2(dot3(cb1, lb0), dot3(cb1, lb1)));
+  s2m sR = s2_xf(a.s0, F2(dot3(cb0, a.rb0), dot3(cb0, a.rb1)), F2(dot3(cb1, a.rb0), dot3(cb1, a.rb1)));
+  float ndm = fmaxf(sqrtf(dot2(dm, dm)), 1e-9f);
+  float d = sqrtf(s2_quad_inv(s2_add(sL, s2_div(sR, 2.0f * ASG_A[2])), dm));
+  float along = sqrtf(fmaxf(s2_quad(sL, dm), 0.0f)) / ndm;
+  float far_ = smoothstepf(1.0f, 2.5f, d) * (1.0f - smoothstepf(0.15f, 0.3f, along / ndm));
+  f3 maj = s2_major(sl);
+  float ratio = sqrtf(maj.z / a.minor0);
+  float t = fmaxf(far_, 1.0f - smoothstepf(0.12f, 0.3f, ratio));
+  float p_asg = 0.0f;
+  if (t < 1.0f) {
+    for (int k = 0; k < 3; k++) {
+      s2m sk = s2_div(sR, 2.0f * ASG_A[k]);
+      s2m st = s2_add(sL, sk);
+      p_asg += ASG_W[k] * sqrtf(fmaxf(s2_det(sk), 0.0f) / fmaxf(s2_det(st), 1e-30f)) * lm_exp(-0.5f * s2_quad_inv(st, dm));
+    }
+    p_asg *= a.pk;
+  }
+  float p_pt = pc;
+  if (t > 0.0f) {
+    f3 ax = mul3(add3(mul3(lb0, maj.x), mul3(lb1, maj.y)), sqrtf(3.0f * maj.z));
+    p_pt = (2.0f / 3.0f) * pc + (1.0f / 6.0f) * (phase_specular_p(sp, norm3(add3(wi, ax)), wo) +
+                                                  phase_specular_p(sp, norm3(sub3(wi, ax)), wo));
+  }
+  return mixf(p_asg, p_pt, t);
+}
+
 __device__ __forceinline__ float phi_cdf(float x) {
   float a = fabsf(x) * 0.70710678f;
   float h = 0.5f * erfc_pos(a);

@@ -55,8 +55,15 @@ __device__ __forceinline__ f3 shade_one(const ShadeParams& SH, const sl_gaussian
     }
   }
   f3 c = F3(0.0f, 0.0f, 0.0f);
+  const f3 wo0 = xf_dir_inv(xf, norm3(sub3(eye, P)));
+  // per-Gaussian parts of the specular and ASG phases, shared by every light below
+  SpecPre sp;
+  AsgPre ap;
+  if (ks > 0.0f) {
+    sp = spec_prepare(Sd, So);
+    ap = asg_prepare(n, t1, t2, flake, Sd, So, wo0);
+  }
   if (SH.n_emit || emissive) {
-    const f3 wo0 = xf_dir_inv(xf, norm3(sub3(eye, P)));
     f3 acc = F3(0.0f, 0.0f, 0.0f);
     if (SH.n_emit) {
       // the cut walk of a 48-entry stack (hi child popped first), stackless: word 7 of a node is where the walk
@@ -110,11 +117,11 @@ __device__ __forceinline__ f3 shade_one(const ShadeParams& SH, const sl_gaussian
           f3 cc0 = sym_mul(cd, co, bw0), cc1 = sym_mul(cd, co, bw1);
           s2m slm{dot3(bw0, cc0) / d2, dot3(bw0, cc1) / d2, dot3(bw1, cc1) / d2};
           f3 lb0 = xf_dir_inv(xf, bw0), lb1 = xf_dir_inv(xf, bw1);
-          float pp = asg_phase(wi, lb0, lb1, slm, n, t1, t2, flake, Sd, So, wo0);
+          float pp = asg_phase_p(ap, sp, wi, lb0, lb1, slm, wo0);
           acc = add3(acc, mul3(light, iso_lobe_from(ks, pp, damp)));
           continue;
         }
-        float lobe = iso_lobe_from(ks, phase_specular(Sd, So, wi, wo0), damp);
+        float lobe = iso_lobe_from(ks, phase_specular_p(sp, wi, wo0), damp);
         acc = add3(acc, mul3(light, lobe));
       }
     }
@@ -137,7 +144,7 @@ __device__ __forceinline__ f3 shade_one(const ShadeParams& SH, const sl_gaussian
       }
       c = add3(c, mul3(mul3v(alb, dc), inorm));
     } else {
-      f3 wo = xf_dir_inv(xf, norm3(sub3(eye, P)));
+      const f3 wo = wo0;
       f3 diff = F3(0.0f, 0.0f, 0.0f), spec = F3(0.0f, 0.0f, 0.0f);
       for (uint32_t k = 0; k < SH.n_lights; k++) {
         f3 wi = xf_dir_inv(xf, ld3(SH.lights[k].dir));
@@ -149,7 +156,7 @@ __device__ __forceinline__ f3 shade_one(const ShadeParams& SH, const sl_gaussian
         float s2 = SH.lights[k].std * SH.lights[k].std;
         f3 ob0, ob1;
         onb(wi, ob0, ob1);
-        float pp = asg_phase(wi, ob0, ob1, s2m{s2, 0.0f, s2}, n, t1, t2, flake, Sd, So, wo);
+        float pp = asg_phase_p(ap, sp, wi, ob0, ob1, s2m{s2, 0.0f, s2}, wo);
         diff = add3(diff, mul3(light, 1.0f - ks));
         spec = add3(spec, mul3(light, iso_lobe_from(ks, pp, damp) - (1.0f - ks)));
       }

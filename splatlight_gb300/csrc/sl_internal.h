@@ -84,7 +84,10 @@ cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals
 cudaError_t sort32_pairs(uint32_t* keys, uint32_t* keys_alt, const uint32_t* vals_in, uint32_t* vals_out,
                          uint32_t* vals_alt, uint32_t n, const uint32_t* n_dev, int bits, const uint32_t* digit_hist,
                          uint32_t* status, uint32_t* tile_ctr, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s,
-                         uint32_t* keys_out = nullptr);
+                         uint32_t* keys_out = nullptr, const uint32_t* keys_first = nullptr);
+// keys_first (optional): the first pass reads the keys from there and leaves them intact (keys is then scratch).
+// Counts the digit histograms of u32 keys ([passes][256]).
+cudaError_t launch_digit_hist32(const uint32_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s);
 // Counts the digit histograms of u16 keys (used when no producer kernel filled them).
 cudaError_t launch_digit_hist16(const uint16_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s);
 

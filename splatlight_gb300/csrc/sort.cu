@@ -1,8 +1,8 @@
 // Stable LSD radix sort of 16- or 32-bit keys with 32-bit values, onesweep style (one read and one write of the keys and
 // values per 8-bit digit pass, Adinets & Merrill 2022): the digit histograms of every pass are counted up front (by
 // the producer kernel, or launch_digit_hist16), then each pass is a single kernel over tiles of 4096 keys that
-//   1. ranks its keys per warp with __match_any_sync (peers holding the same digit) and a per-warp digit counter, so
-//      ranks follow index order within the tile (stability);
+//   1. ranks its keys per warp -- the peers holding the same digit found by one ballot per digit bit, a per-warp
+//      digit counter in shared memory -- so ranks follow index order within the tile (stability);
 //   2. publishes its per-digit counts and looks back over earlier tiles (decoupled look-back, one thread per digit)
 //      for the exclusive prefix; every spin is bounded and a give-up sets FrameCounters::timeout;
 //   3. reorders the tile in shared memory by digit and writes it out in digit runs (coalesced).
@@ -58,8 +58,21 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
   return base + x - v;
 }
 
+// Lanes of `mask` whose 8-bit digit equals this lane's: the intersection over the digit's bits of the ballot of
+// lanes sharing that bit (eight ballots; measured faster than the match instruction in this kernel).
+__device__ __forceinline__ uint32_t digit_peers(uint32_t mask, uint32_t d) {
+  uint32_t peers = mask;
+#pragma unroll
+  for (int b = 0; b < 8; b++) {
+    const uint32_t m = __ballot_sync(mask, (d >> b) & 1u);
+    peers &= ((d >> b) & 1u) ? m : ~m;
+  }
+  return peers;
+}
+
+// Four blocks per SM (64 registers): the occupancy that hides the look-back and scatter latencies.
 template <typename KeyT>
-__global__ void __launch_bounds__(kThreads) onesweep_pass(const KeyT* __restrict__ keys_in,
+__global__ void __launch_bounds__(kThreads, 4) onesweep_pass(const KeyT* __restrict__ keys_in,
                                                           const uint32_t* __restrict__ vals_in,
                                                           KeyT* __restrict__ keys_out,
                                                           uint32_t* __restrict__ vals_out, uint32_t n_max,
@@ -108,7 +121,7 @@ __global__ void __launch_bounds__(kThreads) onesweep_pass(const KeyT* __restrict
     uint32_t d = (keys[it] >> shift) & 0xffu;
     uint32_t rank = 0;
     if (valid) {
-      uint32_t peers = __match_any_sync(vmask, d);
+      uint32_t peers = digit_peers(vmask, d);
       uint32_t before = warp_hist[w][d];
       rank = before + __popc(peers & lt);
       __syncwarp(vmask);
@@ -204,9 +217,32 @@ __global__ void __launch_bounds__(kThreads) digit_hist16_kernel(const uint16_t* 
   if (passes > 1 && h[1][t]) atomicAdd(&hist[256 + t], h[1][t]);
 }
 
+__global__ void __launch_bounds__(kThreads) digit_hist32_kernel(const uint32_t* __restrict__ keys, uint32_t n,
+                                                                int passes, uint32_t* hist) {
+  __shared__ uint32_t h[4][256];
+  const int t = threadIdx.x;
+  for (int p = 0; p < 4; p++) h[p][t] = 0u;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * kThreads + t; i < n; i += gridDim.x * kThreads) {
+    const uint32_t k = keys[i];
+    for (int p = 0; p < passes; p++) atomicAdd(&h[p][(k >> (8 * p)) & 0xffu], 1u);
+  }
+  __syncthreads();
+  for (int p = 0; p < passes; p++)
+    if (h[p][t]) atomicAdd(&hist[256 * p + t], h[p][t]);
+}
+
 }  // namespace
 
 size_t sort_tiles_for(uint32_t n) { return (n + kTile - 1) / kTile; }
+
+cudaError_t launch_digit_hist32(const uint32_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  uint32_t blocks = (n + kThreads * 16 - 1) / (kThreads * 16);
+  if (blocks > 1216) blocks = 1216;
+  digit_hist32_kernel<<<blocks, kThreads, 0, s>>>(keys, n, passes, hist);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_digit_hist16(const uint16_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
@@ -224,7 +260,8 @@ namespace {
 template <typename KeyT>
 cudaError_t sort_pairs(KeyT* keys, KeyT* keys_alt, const uint32_t* vals_in, uint32_t* vals_out, uint32_t* vals_alt,
                        uint32_t n, const uint32_t* n_dev, int bits, const uint32_t* digit_hist, uint32_t* status,
-                       uint32_t* tile_ctr, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s, KeyT* keys_out) {
+                       uint32_t* tile_ctr, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s, KeyT* keys_out,
+                       const KeyT* keys_first = nullptr) {
   if (n == 0) return cudaSuccess;
   if (n > kValueMask) return cudaErrorInvalidValue;
   const uint32_t tiles = (uint32_t)sort_tiles_for(n);
@@ -243,7 +280,7 @@ cudaError_t sort_pairs(KeyT* keys, KeyT* keys_alt, const uint32_t* vals_in, uint
     for (int p = 0; p < passes; p++) vdst[p] = (vdst[p] == vals_out) ? vals_alt : vals_out;
     copy_back = true;  // the result then sits in vals_alt
   }
-  const KeyT* kin = keys;
+  const KeyT* kin = keys_first ? keys_first : keys;  // keys_first: read by the first pass only (left intact)
   const uint32_t* vin = vals_in;
   for (int p = 0; p < passes; p++) {
     const bool last = p == passes - 1;
@@ -273,9 +310,9 @@ cudaError_t sort16_pairs(uint16_t* keys, const uint32_t* vals_in, uint32_t* vals
 cudaError_t sort32_pairs(uint32_t* keys, uint32_t* keys_alt, const uint32_t* vals_in, uint32_t* vals_out,
                          uint32_t* vals_alt, uint32_t n, const uint32_t* n_dev, int bits, const uint32_t* digit_hist,
                          uint32_t* status, uint32_t* tile_ctr, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s,
-                         uint32_t* keys_out) {
+                         uint32_t* keys_out, const uint32_t* keys_first) {
   return sort_pairs<uint32_t>(keys, keys_alt, vals_in, vals_out, vals_alt, n, n_dev, bits, digit_hist, status,
-                              tile_ctr, max_tiles, ctr, s, keys_out);
+                              tile_ctr, max_tiles, ctr, s, keys_out, keys_first);
 }
 
 }  // namespace sl

@@ -40,3 +40,24 @@ def test_large(cuda, orc):
     k = rng.integers(0, 65536, n).astype(np.uint32)
     got = _sort(cuda, k)
     assert np.array_equal(got, orc.sort16(k))
+
+
+def _sort32(torch, keys: np.ndarray, bits: int) -> np.ndarray:
+    from splatlight_gb300 import _native as N
+    k = torch.from_numpy(keys.astype(np.uint32).view(np.int32)).cuda()
+    before = k.clone()
+    o = torch.empty(max(len(keys), 1), dtype=torch.int32, device="cuda")
+    N.check(N.lib().sl_sort_keys32(k.data_ptr(), len(keys), bits, o.data_ptr(), None))
+    assert torch.equal(k, before)   # the input keys are left intact
+    return o[: len(keys)].cpu().numpy().view(np.uint32)
+
+
+@pytest.mark.parametrize("n,bits", [(1, 8), (4097, 17), (300001, 24), (1 << 20, 32), (2_000_003, 22)])
+def test_sort32_segmented_keys(cuda, n, bits):
+    """32-bit keys (view id above 16 depth bits, tile ids of many views): stable order by the low `bits` bits,
+    against numpy's stable argsort."""
+    rng = np.random.default_rng(bits)
+    k = rng.integers(0, 1 << bits, n, dtype=np.uint64).astype(np.uint32)
+    k[rng.random(n) < 0.2] = k[0]          # heavy ties
+    ref = np.argsort(k, kind="stable").astype(np.uint32)
+    assert np.array_equal(_sort32(cuda, k, bits), ref)
