@@ -25,20 +25,14 @@ __device__ __forceinline__ uint32_t splat_tiles(const SplatRec& rec, ushort4 r, 
   return n;
 }
 
+// per sorted position: the tile count the projection stored for that slot
 __global__ void __launch_bounds__(kThreads) btile_count_kernel(const uint32_t* __restrict__ order,
-                                                               const ushort4* __restrict__ rects,
-                                                               const SplatRec* __restrict__ recs,
+                                                               const uint32_t* __restrict__ tile_n,
                                                                const uint32_t* __restrict__ totals, uint32_t n_max,
-                                                               uint32_t tw, uint32_t th,
                                                                uint32_t* __restrict__ counts) {
   const uint32_t p = blockIdx.x * kThreads + threadIdx.x;
   if (p >= n_max) return;
-  uint32_t c = 0;
-  if (p < totals[0]) {
-    const uint32_t slot = order[p];
-    c = splat_tiles(recs[slot], rects[slot], tw, th);
-  }
-  counts[p] = c;
+  counts[p] = p < totals[0] ? tile_n[order[p]] : 0u;
 }
 
 __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __restrict__ order,
@@ -158,12 +152,10 @@ __global__ void __launch_bounds__(kThreads) btile_runs_kernel(const uint32_t* __
 
 }  // namespace
 
-cudaError_t launch_btile_count(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
-                               const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t* counts,
-                               cudaStream_t s) {
+cudaError_t launch_btile_count(const uint32_t* order, const uint32_t* tile_n, const uint32_t* totals, uint32_t n_max,
+                               uint32_t* counts, cudaStream_t s) {
   if (!n_max) return cudaSuccess;
-  btile_count_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, recs, totals, n_max, tw, th,
-                                                                            counts);
+  btile_count_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, tile_n, totals, n_max, counts);
   return cudaGetLastError();
 }
 

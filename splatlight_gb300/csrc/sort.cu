@@ -1,6 +1,6 @@
 // Stable LSD radix sort of 16- or 32-bit keys with 32-bit values, onesweep style (one read and one write of the keys and
 // values per 8-bit digit pass, Adinets & Merrill 2022): the digit histograms of every pass are counted up front (by
-// the producer kernel, or launch_digit_hist16), then each pass is a single kernel over tiles of 4096 keys that
+// the producer kernel, or launch_digit_hist16), then each pass is a single kernel over tiles of 6144 keys that
 //   1. ranks its keys per warp -- the peers holding the same digit found by one ballot per digit bit, a per-warp
 //      digit counter in shared memory -- so ranks follow index order within the tile (stability);
 //   2. publishes its per-digit counts and looks back over earlier tiles (decoupled look-back, one thread per digit)
@@ -16,8 +16,8 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kItems = 16;
-constexpr uint32_t kTile = kThreads * kItems;  // 4096
+constexpr int kItems = 24;
+constexpr uint32_t kTile = kThreads * kItems;  // 6144
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
@@ -70,9 +70,9 @@ __device__ __forceinline__ uint32_t digit_peers(uint32_t mask, uint32_t d) {
   return peers;
 }
 
-// Four blocks per SM (64 registers): the occupancy that hides the look-back and scatter latencies.
+// Tiles of 6144 keys at three blocks per SM (the best of the tile sizes and register budgets measured).
 template <typename KeyT>
-__global__ void __launch_bounds__(kThreads, 4) onesweep_pass(const KeyT* __restrict__ keys_in,
+__global__ void __launch_bounds__(kThreads, 3) onesweep_pass(const KeyT* __restrict__ keys_in,
                                                           const uint32_t* __restrict__ vals_in,
                                                           KeyT* __restrict__ keys_out,
                                                           uint32_t* __restrict__ vals_out, uint32_t n_max,

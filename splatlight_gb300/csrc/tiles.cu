@@ -40,6 +40,16 @@ __global__ void __launch_bounds__(kThreads) tile_count_kernel(const uint32_t* __
   counts[p] = c;
 }
 
+// the same counts from the per-slot tile counts the projection stored (gathered into depth order)
+__global__ void __launch_bounds__(kThreads) tile_count_gather_kernel(const uint32_t* __restrict__ order,
+                                                                     const uint32_t* __restrict__ tile_n, uint32_t n,
+                                                                     const FrameCounters* ctr,
+                                                                     uint32_t* __restrict__ counts) {
+  uint32_t p = blockIdx.x * kThreads + threadIdx.x;
+  if (p >= n) return;
+  counts[p] = p < ctr->visible ? tile_n[order[p]] : 0u;
+}
+
 __global__ void __launch_bounds__(kThreads) tile_emit_kernel(const uint32_t* __restrict__ order,
                                                              const ushort4* __restrict__ rects,
                                                              const SplatRec* __restrict__ recs,
@@ -127,6 +137,13 @@ cudaError_t launch_tile_counts(const uint32_t* order, const ushort4* rects, cons
                                uint32_t tw, uint32_t th, const FrameCounters* ctr, uint32_t* counts, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   tile_count_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, recs, n, tw, th, ctr, counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_counts_gather(const uint32_t* order, const uint32_t* tile_n, uint32_t n,
+                                      const FrameCounters* ctr, uint32_t* counts, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  tile_count_gather_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, tile_n, n, ctr, counts);
   return cudaGetLastError();
 }
 
