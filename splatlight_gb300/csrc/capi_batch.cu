@@ -5,7 +5,6 @@
 // the kernels read comes from device memory uploaded (from pinned staging) at the head of the chain, so the chain is
 // captured once in a CUDA graph and replayed for every batch that fits.  An autotuner picks the tile shape.
 #include <algorithm>
-#include <chrono>
 #include <cstring>
 #include <string>
 #include <vector>

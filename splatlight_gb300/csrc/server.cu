@@ -6,7 +6,6 @@
 // pixels per batch; a request larger than an empty batch is refused at submit), and the pinned host result slots
 // are a fixed pool (a batch waits for free slots; the caller releases a slot after reading its image).
 #include <algorithm>
-#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
