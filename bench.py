@@ -41,6 +41,21 @@ KERNELS_PER_FRAME = 14
 SHADE_DRAM_BYTES_PER_G = (464.748544e6 + 22.484992e6) / 1048576
 
 
+def max_over_ranks(value: float, dist, device: str) -> float:
+    """The slowest rank's time (replicas: every rank renders its own frames; the job takes as long as the slowest)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_throughput(world: int, ms_per_step: float) -> float:
+    """Whole-job views/s: each of the world ranks finishes one view per step of the slowest rank."""
+    return world * 1000.0 / ms_per_step
+
+
 def peaks():
     if MEASURED.exists():
         m = json.loads(MEASURED.read_text())
@@ -623,11 +638,8 @@ def main():
     barrier()
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     ms = sum(step_ms) / len(step_ms)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    views_per_s = world * 1000.0 / ms
+    ms = max_over_ranks(ms, dist, "cuda")
+    views_per_s = replicas_throughput(world, ms)
     stats = r.last_stats
     if not np.isfinite(out.sum().item()):
         raise RuntimeError("non-finite image")
@@ -670,10 +682,7 @@ def main():
         L.update(s.eye, fwd)
         r.render(f, out=host_out_np)
     e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, dist, "cuda")
     h2d = f.nbytes + parts.nbytes
     d2h = W * H * 16
 

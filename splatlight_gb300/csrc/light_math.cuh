@@ -444,11 +444,25 @@ __device__ __forceinline__ float asg_phase_p(const AsgPre& a, const SpecPre& sp,
   f3 c = div3(cs, cl);
   f3 cb0, cb1;
   onb(c, cb0, cb1);
-  f2 dm = sub2(log_map(c, cb0, cb1, a.wr), log_map(c, cb0, cb1, wi));
+  // log_map(c, wr) - log_map(c, wi): c bisects wi and wr, so both make the same angle with c (one acos) and the
+  // components along c cancel; the tangent-plane difference is (wr - wi) projected on (cb0, cb1), scaled by
+  // angle / sin(angle)
+  f2 dm = F2(0.0f, 0.0f);
+  {
+    const float ca = clampf(dot3(c, wi), -1.0f, 1.0f);
+    const f3 v = sub3(wi, mul3(c, ca));
+    const float nv = len3(v);
+    if (!(nv < 1e-9f)) {
+      const float k = lm_acos(ca) / nv;
+      const f3 dw = sub3(a.wr, wi);
+      dm = F2(k * dot3(cb0, dw), k * dot3(cb1, dw));
+    }
+  }
   s2m sL = s2_xf(sl, F2(dot3(cb0, lb0), dot3(cb0, lb1)), F2(dot3(cb1, lb0), dot3(cb1, lb1)));
   s2m sR = s2_xf(a.s0, F2(dot3(cb0, a.rb0), dot3(cb0, a.rb1)), F2(dot3(cb1, a.rb0), dot3(cb1, a.rb1)));
   float ndm = fmaxf(sqrtf(dot2(dm, dm)), 1e-9f);
-  float d = sqrtf(s2_quad_inv(s2_add(sL, s2_div(sR, 2.0f * ASG_A[2])), dm));
+  const float kInv2A[3] = {1.0f / (2.0f * ASG_A[0]), 1.0f / (2.0f * ASG_A[1]), 1.0f / (2.0f * ASG_A[2])};
+  float d = sqrtf(s2_quad_inv(s2_add(sL, s2m{sR.x * kInv2A[2], sR.y * kInv2A[2], sR.z * kInv2A[2]}), dm));
   float along = sqrtf(fmaxf(s2_quad(sL, dm), 0.0f)) / ndm;
   float far_ = smoothstepf(1.0f, 2.5f, d) * (1.0f - smoothstepf(0.15f, 0.3f, along / ndm));
   f3 maj = s2_major(sl);
@@ -456,10 +470,12 @@ __device__ __forceinline__ float asg_phase_p(const AsgPre& a, const SpecPre& sp,
   float t = fmaxf(far_, 1.0f - smoothstepf(0.12f, 0.3f, ratio));
   float p_asg = 0.0f;
   if (t < 1.0f) {
+    const float detR = fmaxf(s2_det(sR), 0.0f);
     for (int k = 0; k < 3; k++) {
-      s2m sk = s2_div(sR, 2.0f * ASG_A[k]);
+      s2m sk = s2m{sR.x * kInv2A[k], sR.y * kInv2A[k], sR.z * kInv2A[k]};
       s2m st = s2_add(sL, sk);
-      p_asg += ASG_W[k] * sqrtf(fmaxf(s2_det(sk), 0.0f) / fmaxf(s2_det(st), 1e-30f)) * lm_exp(-0.5f * s2_quad_inv(st, dm));
+      p_asg += ASG_W[k] * sqrtf(detR * (kInv2A[k] * kInv2A[k]) / fmaxf(s2_det(st), 1e-30f)) *
+               lm_exp(-0.5f * s2_quad_inv(st, dm));
     }
     p_asg *= a.pk;
   }
