@@ -258,6 +258,16 @@ SL_API int sl_lighting_read(sl_lighting* l, float* colour, float* lamp_T, float*
 /* bindColour with a Lighting object's radiance buffer (src/renderer.js:264-268). */
 SL_API int sl_renderer_bind_lighting(sl_renderer* r, sl_lighting* l);
 
+/* ---- display resolve (shaders/display.wgsl:120-189) -------------------------------------------------------------- */
+
+/* The frame's linear RGBA image (device, W x H x 4 floats, as sl_render writes it) to 8-bit sRGB RGBA (device,
+ * W x H x 4 bytes): exposure (frame->exposure), the tone curve frame->tone[0] (0 clamp, 1 AgX, 2 ACES filmic,
+ * 3 Reinhard on luminance, 4 Khronos PBR Neutral, 5 Hable filmic), the sRGB transfer function; view mode 2 maps the
+ * contributor count through the reference's heat ramp.  The sky background the reference blends where splats leave
+ * it showing belongs to its environment sky model (not on this path): those pixels stay black.  Stream-ordered. */
+SL_API int sl_display(const float* image_dev, uint32_t width, uint32_t height, const sl_render_frame* frame,
+                      uint8_t* out_dev, void* stream);
+
 /* ---- sort (shaders/radix.wgsl) --------------------------------------------------------------------------------- */
 
 /* The stable sort of 16-bit depth keys on its own (shaders/radix.wgsl:1-139; encoded by src/renderer.js:425-434):

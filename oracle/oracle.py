@@ -294,3 +294,15 @@ def diff_render(params: dict, lights: dict, frame, eye, order, target=None, thre
               float(lights["ks"]), _p(view), _p(focal), _p(vp), float(f["near"]), float(f["far"]),
               float(f["lowpass_px2"]), _p(e), _p(o), len(o), _p(t), _p(img), threads)
     return img, loss
+
+
+def display(img, exposure: float = 1.0, tone: int = 0, view_mode: int = 3):
+    """Display resolve (sl_oracle_display.c): H x W x 4 float -> H x W x 4 uint8."""
+    L = lib()
+    fn = L.orc_display
+    fn.restype = None
+    fn.argtypes = [C.c_void_p, C.c_uint32, C.c_float, C.c_uint32, C.c_uint32, C.c_void_p]
+    a = np.ascontiguousarray(img, dtype=np.float32)
+    out = np.empty(a.shape[:-1] + (4,), np.uint8)
+    fn(a.ctypes.data, a.size // 4, exposure, tone, view_mode, out.ctypes.data)
+    return out

@@ -108,6 +108,7 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_lighting_shade": (_I, [_P, _P, _P]),
     "sl_lighting_read": (_I, [_P, _P, _P, _P, _P]),
     "sl_renderer_bind_lighting": (_I, [_P, _P]),
+    "sl_display": (_I, [_P, _U32, _U32, _P, _P, _P]),
     "sl_sort_keys16": (_I, [_P, _U32, _P, _P]),
     "sl_sort_keys16_noalloc": (_I, [_P, _U32, _P, _P]),
     "sl_sort_keys32": (_I, [_P, _U32, _U32, _P, _P]),
