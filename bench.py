@@ -280,6 +280,7 @@ def run_serving(args, rates=(100, 500, 2000)):
     from splatlight_gb300 import camera
     from splatlight_gb300.lighting import camera_forward, for_scene
     from splatlight_gb300.renderer import SplatRenderer
+    from splatlight_gb300._native import SplatlightError
     from splatlight_gb300.server import RenderServer
     scenes = serve_scenes()
     rs, ls = [], []
@@ -312,8 +313,10 @@ def run_serving(args, rates=(100, 500, 2000)):
                        "seeds 10-15), cameras on radius U[3,8] spheres, 512^2 / 1280x720 / 1920x1080, light scale "
                        "U[0.5,2], lit; images delivered to pinned host memory",
            "seconds_per_rate": args.serve_seconds, "rates": []}
+    # the pending queue is bounded (512 requests, a few batches' worth): beyond it a request is refused at submit,
+    # which keeps the latency of admitted requests bounded when arrivals outrun the device
     srv = RenderServer(rs, ls, max_views=64, pipelines=2, max_slots=48 << 20, max_pixels=24 << 20,
-                       max_tiles=1 << 19, result_slots=96)
+                       max_tiles=1 << 19, result_slots=96, max_pending=512)
     # warm-up: capture the graphs, size the entry buffers
     for k in range(16):
         q = request()
@@ -327,15 +330,16 @@ def run_serving(args, rates=(100, 500, 2000)):
         reqs = [request() for _ in range(n)]
         arrivals = {}
         done = []
+        refused = 0
         stop = threading.Event()
 
         deadline = [None]
 
         def poller():
-            while not stop.is_set() or len(done) < n:
+            while not stop.is_set() or len(done) < n - refused:
                 for r in srv.poll(wait_us=2000, copy=False):
                     done.append((r.tag, time.perf_counter(), r.status, r.batch_views))
-                if stop.is_set() and len(done) >= n:
+                if stop.is_set() and len(done) >= n - refused:
                     break
                 if deadline[0] is not None and time.perf_counter() > deadline[0]:
                     break
@@ -352,7 +356,12 @@ def run_serving(args, rates=(100, 500, 2000)):
                     break
                 time.sleep(min(dt, 0.0005))
             arrivals[i] = time.perf_counter()
-            srv.submit(*q, tag=i)
+            try:
+                srv.submit(*q, tag=i)
+            except SplatlightError as e:
+                if e.code != -7:
+                    raise
+                refused += 1
         t_sub = time.perf_counter()
         deadline[0] = t_sub + 300.0
         stop.set()
@@ -360,9 +369,11 @@ def run_serving(args, rates=(100, 500, 2000)):
         t_end = max(t for _, t, _, _ in done)
         lat = np.array([(t - arrivals[tag]) * 1000.0 for tag, t, st, _ in done if st == 0])
         fails = sum(1 for _, _, st, _ in done if st != 0)
-        out["rates"].append({"lambda": lam, "requests": n, "failed": fails, "unfinished": n - len(done),
+        n_adm = n - refused
+        out["rates"].append({"lambda": lam, "requests": n, "refused_at_admission": refused, "failed": fails,
+                             "unfinished": n_adm - len(done),
                              "offered_per_s": round(n / (t_sub - t0), 1),
-                             "views_per_s": round(n / (t_end - t0), 1),
+                             "views_per_s": round(len(done) / (t_end - t0), 1),
                              "p50_ms": round(float(np.percentile(lat, 50)), 2),
                              "p99_ms": round(float(np.percentile(lat, 99)), 2),
                              "mean_batch": round(float(np.mean([b for *_, b in done])), 1)})

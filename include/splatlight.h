@@ -416,6 +416,9 @@ typedef struct sl_server_options {
   uint32_t max_tiles;            /* tiles per batch (0 = 512 Ki) */
   uint32_t result_slots;         /* pinned result slots (0 = 2 x max_views) */
   uint32_t tile_w, tile_h;       /* 16x16 (default), 8x32 or 32x8 */
+  uint32_t max_pending;          /* requests waiting for admission (0 = unbounded); beyond it submit refuses
+                                    (SL_ERR_ADMISSION), which bounds the latency of what is admitted under overload */
+  uint32_t pad;
 } sl_server_options;
 
 typedef struct sl_server_request {
@@ -445,7 +448,8 @@ typedef struct sl_server_stats {
 
 SL_API int sl_server_create(sl_renderer* const* renderers, sl_lighting* const* lightings, uint32_t n_scenes,
                             const sl_server_options* opt, sl_server** out);
-/* Queues one request (validated here: SL_ERR_INVALID_ARG, or SL_ERR_ADMISSION when it can never fit a batch). */
+/* Queues one request (validated here: SL_ERR_INVALID_ARG, or SL_ERR_ADMISSION when it can never fit a batch or the
+ * pending queue is full). */
 SL_API int sl_server_submit(sl_server* s, const sl_server_request* req, uint64_t tag);
 /* Up to cap finished results (waits up to wait_us microseconds for the first); *n_out = how many. */
 SL_API int sl_server_poll(sl_server* s, sl_server_result* out, uint32_t cap, uint32_t* n_out, uint32_t wait_us);

@@ -52,7 +52,7 @@ class ServerOptions(C.Structure):
     _fields_ = [("max_views", C.c_uint32), ("pipelines", C.c_uint32), ("max_slots", C.c_uint64),
                 ("max_pixels", C.c_uint64), ("max_view_pixels", C.c_uint64), ("hbm_budget_bytes", C.c_uint64),
                 ("max_tiles", C.c_uint32), ("result_slots", C.c_uint32), ("tile_w", C.c_uint32),
-                ("tile_h", C.c_uint32)]
+                ("tile_h", C.c_uint32), ("max_pending", C.c_uint32), ("pad", C.c_uint32)]
 
 
 class ServerResult(C.Structure):

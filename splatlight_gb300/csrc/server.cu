@@ -367,6 +367,10 @@ int sl_server_submit(sl_server* S, const sl_server_request* req, uint64_t tag) {
   {
     std::lock_guard<std::mutex> lk(S->mu);
     if (S->stop) return fail(SL_ERR_CANCELLED, "the server is shutting down");
+    if (S->opt.max_pending && S->pending.size() >= S->opt.max_pending) {
+      S->rejected++;
+      return fail(SL_ERR_ADMISSION, "the pending queue is full (" + std::to_string(S->opt.max_pending) + ")");
+    }
     q.t_submit = S->now();
     S->pending.push_back(q);
     S->submitted++;

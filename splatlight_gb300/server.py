@@ -35,7 +35,7 @@ class Result:
 class RenderServer:
     def __init__(self, renderers, lightings=None, max_views: int = 64, pipelines: int = 2, max_slots: int = 0,
                  max_pixels: int = 0, max_view_pixels: int = 0, max_tiles: int = 0, result_slots: int = 0,
-                 hbm_budget_bytes: int = 0, tile=(16, 16)):
+                 hbm_budget_bytes: int = 0, tile=(16, 16), max_pending: int = 0):
         self._lib = N.lib()
         self._renderers = list(renderers)
         self._lightings = list(lightings) if lightings is not None else None
@@ -45,7 +45,7 @@ class RenderServer:
             ls = (C.c_void_p * len(self._lightings))(*[(l.handle if l is not None else None)
                                                         for l in self._lightings])
         o = N.ServerOptions(max_views, pipelines, max_slots, max_pixels, max_view_pixels, hbm_budget_bytes,
-                            max_tiles, result_slots, tile[0], tile[1])
+                            max_tiles, result_slots, tile[0], tile[1], max_pending, 0)
         h = C.c_void_p()
         N.check(self._lib.sl_server_create(rs, ls, len(self._renderers), C.byref(o), C.byref(h)))
         self._h = h

@@ -143,3 +143,23 @@ def test_shutdown_with_unreleased_slots(world):
     t0 = time.time()
     srv.close()
     assert time.time() - t0 < 10.0
+
+
+def test_bounded_pending_queue(world):
+    """With max_pending set, a request beyond the queue bound is refused at submit (SL_ERR_ADMISSION); what was
+    admitted still completes."""
+    scenes, rs, ls = world
+    a = scenes[0]
+    f = _frame(a, 64, 64, VIEW_FLAT, a.eye)
+    with RenderServer(rs, ls, max_views=1, pipelines=1, max_view_pixels=64 * 64, result_slots=1,
+                      max_pending=2) as srv:
+        srv.submit(0, f, a.eye, tag=0)
+        time.sleep(0.3)                       # request 0 holds the only result slot until it is polled
+        srv.submit(0, f, a.eye, tag=1)
+        srv.submit(0, f, a.eye, tag=2)
+        with pytest.raises(SplatlightError) as e:
+            srv.submit(0, f, a.eye, tag=3)
+        assert e.value.code == -7
+        got = _drain(srv, 3)
+        assert all(r.status == 0 for r in got.values())
+        assert srv.stats()["rejected"] == 1
