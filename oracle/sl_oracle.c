@@ -81,6 +81,16 @@ static v3 part_apply(const sl_part* p, const float x[3]) {
   return v3_make(o[0], o[1], o[2]);
 }
 
+/* the same with the pose at the start of the exposure (xf_prev), for motion blur (shaders/project.wgsl:140-145) */
+static v3 part_apply_prev(const sl_part* p, const float x[3]) {
+  float o[3];
+  for (int r = 0; r < 3; r++) {
+    const float* a = p->xf_prev + 4 * r;
+    o[r] = a[0] * x[0] + a[1] * x[1] + a[2] * x[2] + a[3] * 1.0f;
+  }
+  return v3_make(o[0], o[1], o[2]);
+}
+
 /* palette_slot, shaders/project.wgsl:27-31 */
 static const float* palette_slot(const sl_render_frame* f, uint32_t m) {
   static const float white0[4] = {1.0f, 1.0f, 1.0f, 0.0f};
@@ -106,6 +116,7 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   m3 rot;
   uint32_t material = ORC_EMITTER_MATERIAL;
   float keep = 1.0f;
+  v3 vel = v3_make(0.0f, 0.0f, 0.0f);
   if (i > count) { /* :226-230 */
     g = &emitters[i - count - 1u];
     mu = v3_make(g->mu[0], g->mu[1], g->mu[2]);
@@ -121,6 +132,13 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
     mu = part_apply(p, g->mu);
     rot = m3_mul(part_rotation(p), quat_to_mat(g->quat));
     material = part < 16u ? f->part_material[part] : f->part_material_ext[part - 16u];
+    /* motion blur (:138-146): a box-shutter average of the move over the exposure, centred mid-exposure */
+    float shutter = f->palette[3][2];
+    if (shutter > 0.0f && (p->flags & 2u) != 0u) {
+      v3 prev = part_apply_prev(p, g->mu);
+      vel = v3_make(shutter * (mu.x - prev.x), shutter * (mu.y - prev.y), shutter * (mu.z - prev.z));
+      mu = v3_make(mu.x - 0.5f * vel.x, mu.y - 0.5f * vel.y, mu.z - 0.5f * vel.z);
+    }
   }
 
   /* tv = view * vec4(mu, 1) (:263) */
@@ -147,6 +165,16 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
     const float* mk[3] = {&m.c[0].x, &m.c[1].x, &m.c[2].x};
     for (int r = 0; r < 3; r++)
       for (int c = 0; c < 3; c++) cv[r][c] = mk[0][r] * mk[0][c] + mk[1][r] * mk[1][c] + mk[2][r] * mk[2][c];
+  }
+  /* the sharp covariance (coverage cap); blurred: + (W vel)(W vel)^T / 12 (:207-209) */
+  int blurred = vel.x != 0.0f || vel.y != 0.0f || vel.z != 0.0f;
+  m3 cov_s;
+  for (int c = 0; c < 3; c++) cov_s.c[c] = v3_make(cv[0][c], cv[1][c], cv[2][c]);
+  if (blurred) {
+    v3 wv = m3_mul_v(W, vel);
+    float w3[3] = {wv.x, wv.y, wv.z};
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) cv[r][c] = cv[r][c] + (w3[r] * w3[c]) * (1.0f / 12.0f);
   }
   m3 cov;
   for (int c = 0; c < 3; c++) cov.c[c] = v3_make(cv[0][c], cv[1][c], cv[2][c]);
@@ -179,8 +207,28 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   v3 dl = m3_tmul_v(wr, d);
   v3 is2 = v3_make(1.0f / s2.x, 1.0f / s2.y, 1.0f / s2.z);
   float q = v3_dot(v3_make(dl.x * dl.x, dl.y * dl.y, dl.z * dl.z), is2);
+  float q_s = q, kappa = g->kappa;
+  if (blurred) { /* Sherman-Morrison for q, the determinant lemma for kappa (:241-250) */
+    v3 vl = m3_tmul_v(rot, vel);
+    float mv2 = v3_dot(v3_make(vl.x * vl.x, vl.y * vl.y, vl.z * vl.z), is2);
+    float dv = v3_dot(v3_make(dl.x * vl.x, dl.y * vl.y, dl.z * vl.z), is2);
+    q -= dv * dv / (12.0f + mv2);
+    kappa /= sqrtf(1.0f + mv2 / 12.0f);
+  }
   const float kTwoPi = 6.283185307f;
-  float tau0 = g->kappa * sqrtf(kTwoPi / q) * sqrtf(fmaxf(det0, 0.0f) / det);
+  float tau0 = kappa * sqrtf(kTwoPi / q) * sqrtf(fmaxf(det0, 0.0f) / det);
+  if (blurred && f->palette[3][3] > 0.5f) { /* coverage cap (:252-272) */
+    v3 cs0 = m3_mul_v(cov_s, j0), cs1 = m3_mul_v(cov_s, j1);
+    float a_s = v3_dot(j0, cs0) + f->lowpass_px2;
+    float b_s = v3_dot(j0, cs1);
+    float c_s = v3_dot(j1, cs1) + f->lowpass_px2;
+    float det0_s = (a_s - f->lowpass_px2) * (c_s - f->lowpass_px2) - b_s * b_s;
+    float det_s = a_s * c_s - b_s * b_s;
+    float tau_s = g->kappa * sqrtf(kTwoPi / q_s) * sqrtf(fmaxf(det0_s, 0.0f) / det_s);
+    float ap = (1.0f - sl_expf(-tau_s)) * sqrtf(det_s / det);
+    float tc = -sl_logf(fmaxf(1.0f - ap, 1e-6f));
+    tau0 = fminf(tau0, tc);
+  }
   tau0 *= keep; /* :384 */
 
   /* cutoff radius (:393-398) */

@@ -246,9 +246,12 @@ int check_frame(const sl_render_frame* f, uint32_t count, uint32_t n_emitters, c
   if (f->lod[0] != 0u) return fail(SL_ERR_UNSUPPORTED, "screen-space LOD (frame.lod) is outside this pipeline");
   if (f->explode_k[2] > 0.5f) return fail(SL_ERR_UNSUPPORTED, "explode is outside this pipeline");
   if (f->particles[1] != 0u) return fail(SL_ERR_UNSUPPORTED, "Gaussian particles are outside this pipeline");
-  if (f->palette[3][2] > 0.0f)
+  if (f->palette[3][2] > 0.0f && f->view_mode == 3u)
     for (const sl_part& p : parts)
-      if (p.flags & 2u) return fail(SL_ERR_UNSUPPORTED, "motion blur of a moving part is outside this pipeline");
+      if (p.flags & 2u)
+        return fail(SL_ERR_UNSUPPORTED,
+                    "the lit view of a blurred moving part needs the lighting's stretched records "
+                    "(runtime/wgsl/motion_blur.wgsl), outside this pipeline");
   return SL_OK;
 }
 
@@ -265,6 +268,8 @@ void pack_project_params(const sl_render_frame* f, const std::vector<sl_part>& p
   P.lowpass_px2 = f->lowpass_px2;
   P.albedo_scale = f->albedo_scale;
   P.bounce_gain = f->palette[3][0];
+  P.shutter = f->palette[3][2];
+  P.blur_cov = f->palette[3][3] > 0.5f ? 1u : 0u;
   P.count = count;
   P.n_emit = n_emit;
   P.n_slots = count + 1u + n_emit;
@@ -284,6 +289,7 @@ void pack_project_params(const sl_render_frame* f, const std::vector<sl_part>& p
     PartXf& x = P.parts[p];
     if (p < parts.size()) {
       memcpy(x.xf, parts[p].xf, sizeof(x.xf));
+      memcpy(x.xf_prev, parts[p].xf_prev, sizeof(x.xf_prev));
       x.flags = parts[p].flags;
     } else {
       x.flags = kPartHidden;

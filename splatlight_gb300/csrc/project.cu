@@ -67,6 +67,7 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
   float keep = 1.0f;
   V3 mu;
   M3 rot;
+  V3 vel = v3(0.0f, 0.0f, 0.0f);  // motion blur: world-space displacement over the exposure (project.wgsl:138-146)
   if (live) {
     const float4* src = (i > P.count) ? emitters + 4u * (i - P.count - 1u) : gaussians + 4u * i;
     g0 = __ldg(src + 0);
@@ -94,6 +95,14 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
         R.c[2] = v3(a[2], a[6], a[10]);
         rot = mulm(R, quat_mat(g1.x, g1.y, g1.z, g1.w));
         material = p.material;
+        if (P.shutter > 0.0f && (p.flags & 2u) != 0u) {
+          const float* b = p.xf_prev;
+          const V3 prev = v3(b[0] * g0.x + b[1] * g0.y + b[2] * g0.z + b[3] * 1.0f,
+                             b[4] * g0.x + b[5] * g0.y + b[6] * g0.z + b[7] * 1.0f,
+                             b[8] * g0.x + b[9] * g0.y + b[10] * g0.z + b[11] * 1.0f);
+          vel = v3(P.shutter * (mu.x - prev.x), P.shutter * (mu.y - prev.y), P.shutter * (mu.z - prev.z));
+          mu = v3(mu.x - 0.5f * vel.x, mu.y - 0.5f * vel.y, mu.z - 0.5f * vel.z);
+        }
       }
     }
   }
@@ -121,6 +130,20 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
       for (int r = 0; r < 3; r++)
 #pragma unroll
         for (int c = 0; c < 3; c++) cv[r][c] = mk0[r] * mk0[c] + mk1[r] * mk1[c] + mk2[r] * mk2[c];
+      // the sharp covariance, kept for the coverage cap; blurred: + (W vel)(W vel)^T / 12 (project.wgsl:207-209)
+      const bool blurred = vel.x != 0.0f || vel.y != 0.0f || vel.z != 0.0f;
+      M3 cov_s;
+      cov_s.c[0] = v3(cv[0][0], cv[1][0], cv[2][0]);
+      cov_s.c[1] = v3(cv[0][1], cv[1][1], cv[2][1]);
+      cov_s.c[2] = v3(cv[0][2], cv[1][2], cv[2][2]);
+      if (blurred) {
+        const V3 wv = mulv(W, vel);
+        const float w3[3] = {wv.x, wv.y, wv.z};
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+          for (int c = 0; c < 3; c++) cv[r][c] = cv[r][c] + (w3[r] * w3[c]) * (1.0f / 12.0f);
+      }
       M3 cov;
       cov.c[0] = v3(cv[0][0], cv[1][0], cv[2][0]);
       cov.c[1] = v3(cv[0][1], cv[1][1], cv[2][1]);
@@ -153,8 +176,33 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
         V3 dl = v3(dot3(wr.c[0], d), dot3(wr.c[1], d), dot3(wr.c[2], d));
         V3 is2 = v3(1.0f / s2.x, 1.0f / s2.y, 1.0f / s2.z);
         float q = dot3(v3(dl.x * dl.x, dl.y * dl.y, dl.z * dl.z), is2);
+        const float q_s = q;
+        float kappa = __uint_as_float(__float_as_uint(g0.w));
+        if (blurred) {
+          // Sigma' = Sigma + v v^T / 12 in the Gaussian's frame: Sherman-Morrison for the view ray's q, the
+          // determinant lemma for the density that keeps the mass (project.wgsl:241-250)
+          const V3 vl = v3(dot3(rot.c[0], vel), dot3(rot.c[1], vel), dot3(rot.c[2], vel));
+          const float mv2 = dot3(v3(vl.x * vl.x, vl.y * vl.y, vl.z * vl.z), is2);
+          const float dv = dot3(v3(dl.x * vl.x, dl.y * vl.y, dl.z * vl.z), is2);
+          q -= dv * dv / (12.0f + mv2);
+          kappa /= sqrtf(1.0f + mv2 / 12.0f);
+        }
         const float kTwoPi = 6.283185307f;
-        tau0 = __uint_as_float(__float_as_uint(g0.w)) * sqrtf(kTwoPi / q) * sqrtf(fmaxf(det0, 0.0f) / det);
+        tau0 = kappa * sqrtf(kTwoPi / q) * sqrtf(fmaxf(det0, 0.0f) / det);
+        if (blurred && P.blur_cov) {
+          // coverage cap: a box shutter averages coverage, so the smear's peak alpha is capped at the sharp splat's
+          // (same Jacobian) x sqrt(det_s / det) (project.wgsl:252-272)
+          const V3 cs0 = mulv(cov_s, j0), cs1 = mulv(cov_s, j1);
+          const float a_s = dot3(j0, cs0) + P.lowpass_px2;
+          const float b_s = dot3(j0, cs1);
+          const float c_s = dot3(j1, cs1) + P.lowpass_px2;
+          const float det0_s = (a_s - P.lowpass_px2) * (c_s - P.lowpass_px2) - b_s * b_s;
+          const float det_s = a_s * c_s - b_s * b_s;
+          const float tau_s = __uint_as_float(__float_as_uint(g0.w)) * sqrtf(kTwoPi / q_s) *
+                              sqrtf(fmaxf(det0_s, 0.0f) / det_s);
+          const float ap = (1.0f - sl_expf(-tau_s)) * sqrtf(det_s / det);
+          tau0 = fminf(tau0, -sl_logf(fmaxf(1.0f - ap, 1e-6f)));
+        }
         tau0 *= keep;
         live = !(tau0 <= kTauMin);
       }

@@ -24,6 +24,7 @@ struct __align__(16) SplatRec {
 // Per-part data the projection reads (shaders/common.wgsl:17-25 Part, RenderFrame.part_material/part_fade).
 struct PartXf {
   float xf[12];
+  float xf_prev[12];  // the pose at the start of the exposure (motion blur of a moving part, flags bit 1)
   uint32_t flags;
   uint32_t material;
   float keep;  // 1 - clamp(part_fade)
@@ -37,6 +38,8 @@ struct ProjectParams {
   float viewport[2];
   float near_plane, far_plane, lowpass_px2, albedo_scale;
   float bounce_gain;
+  float shutter;         // palette[3].z: motion-blur shutter fraction (0 = off)
+  uint32_t blur_cov;     // palette[3].w > 0.5: cap a smeared splat's peak coverage at the sharp one's
   uint32_t count, n_emit, n_slots, view_mode, part_count;
   uint32_t tile_w, tile_h, tiles_x, tiles_y;
   float palette[8][4];  // slots 0-7 (slot 3 = white, w 0)

@@ -101,3 +101,30 @@ def test_overdraw_counts_equal_kept_fragments(orc):
     for t0, t1 in r1["ranges"]:
         seg = pos[r1["entries"][t0:t1]]
         assert np.all(np.diff(seg) > 0)
+
+
+def test_blur_centres_the_smear_mid_exposure(orc):
+    """A translated part with shutter 1: every splat of it sits half way between its previous and current
+    projections, and its footprint grows along the motion."""
+    import numpy as np
+    from splatlight_gb300 import camera, scene
+    s = scene.subset(scene.cornell(), 3000)
+    parts = s.parts.copy()
+    parts["xf_prev"][5] = parts["xf"][5]
+    parts["xf"][5][3] += 0.2
+    parts["flags"][5] |= 2
+    f = camera.make_frame(s.eye, s.target, s.up, s.fov_deg, 128, 128, s.count, far=s.far, view_mode=0, n_emit=0)
+    keys_now, now, _ = orc.project(s.gaussians, parts, f)
+    p_prev = s.parts.copy()
+    keys_prev, prev, _ = orc.project(s.gaussians, p_prev, f)
+    f["palette"][3][2] = 1.0
+    keys_b, blur, _ = orc.project(s.gaussians, parts, f)
+    sel = np.nonzero((s.gaussians["part_surface"] & 0xFFFF) == 5)[0]
+    sel = sel[(keys_now[sel] != 0xFFFFFFFF) & (keys_prev[sel] != 0xFFFFFFFF) & (keys_b[sel] != 0xFFFFFFFF)]
+    assert len(sel) > 20
+    mid = 0.5 * (now["cx"][sel] + prev["cx"][sel])
+    assert np.abs(blur["cx"][sel] - mid).max() < 0.2          # pixels (perspective makes it inexact)
+    # the smear lengthens the splat: its candidate rectangle spans more pixels than the sharp one's
+    w_now = (now["ix1"] - now["ix0"])[sel]
+    w_blur = (blur["ix1"] - blur["ix0"])[sel]
+    assert np.median(w_blur - w_now) > 0
