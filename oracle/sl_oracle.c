@@ -3,6 +3,10 @@
  * back-to-front composite).  TEST INFRASTRUCTURE: only tests/, the smoke check and the benchmark's CPU-baseline
  * leg load this library; the product path never does.
  *
+ * Parity unpinned: the reference is WGSL on WebGPU (no graphics stack here to run it) and ships no tests or golden
+ * vectors, so this restatement is pinned by reading the cited lines, by float64 brute-force and known-answer checks
+ * (tests/test_oracle*.py) and by the committed fixtures tests/golden/*.npz that tests/golden/make_golden.py made.
+ *
  * Arithmetic contract (shared with the CUDA kernels; both follow it independently):
  *   - fp32 throughout, compiled with -ffp-contract=off: every a*b+c below rounds twice unless written as fmaf();
  *   - sums and dot products evaluate left to right; matrix-vector products as col0*v.x + col1*v.y + col2*v.z;
