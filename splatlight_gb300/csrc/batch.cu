@@ -6,6 +6,7 @@
 // batch that fits).
 #include "sl_internal.h"
 #include "sl_tilespan.h"
+#include "sl_emit.cuh"
 #include "sl_lighting.h"
 
 namespace sl {
@@ -25,20 +26,41 @@ __device__ __forceinline__ uint32_t splat_tiles(const SplatRec& rec, ushort4 r, 
   return n;
 }
 
-// per sorted position: the tile count the projection stored for that slot
 __global__ void __launch_bounds__(kThreads) btile_count_kernel(const uint32_t* __restrict__ order,
-                                                               const uint32_t* __restrict__ tile_n,
+                                                               const ushort4* __restrict__ rects,
+                                                               const SplatRec* __restrict__ recs,
                                                                const uint32_t* __restrict__ totals, uint32_t n_max,
+                                                               uint32_t tw, uint32_t th,
                                                                uint32_t* __restrict__ counts) {
   const uint32_t p = blockIdx.x * kThreads + threadIdx.x;
   if (p >= n_max) return;
-  counts[p] = p < totals[0] ? tile_n[order[p]] : 0u;
+  uint32_t c = 0;
+  if (p < totals[0]) {
+    const uint32_t slot = order[p];
+    c = splat_tiles(recs[slot], rects[slot], tw, th);
+  }
+  counts[p] = c;
 }
+
+// digit histograms of 32-bit tile ids: low byte per id, the two upper bytes per run of ids within one 256-block
+struct Hist24 {
+  uint32_t (*h)[256];
+  __device__ __forceinline__ void add(uint32_t first, uint32_t n) {
+    for (uint32_t k = 0; k < n; k++) atomicAdd(&h[0][(first + k) & 0xffu], 1u);
+    for (uint32_t a = first, end = first + n; a < end;) {
+      const uint32_t stop = min(end, (a | 0xffu) + 1u);
+      atomicAdd(&h[1][(a >> 8) & 0xffu], stop - a);
+      atomicAdd(&h[2][(a >> 16) & 0xffu], stop - a);
+      a = stop;
+    }
+  }
+};
 
 __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __restrict__ order,
                                                               const ushort4* __restrict__ rects,
                                                               const SplatRec* __restrict__ recs,
                                                               const uint32_t* __restrict__ offsets,
+                                                              const uint32_t* __restrict__ counts,
                                                               const BatchView* __restrict__ views,
                                                               const uint32_t* __restrict__ block_view,
                                                               const uint32_t* __restrict__ totals, uint32_t n_max,
@@ -53,43 +75,26 @@ __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __
   h[2][t] = 0u;
   __syncthreads();
   const uint32_t p = blockIdx.x * kThreads + t;
+  bool mine = false;
+  uint32_t slot = 0, e0 = 0, cnt = 0, base = 0, stride = 0;
+  ushort4 r = make_ushort4(1, 1, 0, 0);
+  SplatRec rec{};
   if (p < n_max && p < totals[0]) {
-    const uint32_t slot = order[p];
-    const ushort4 r = rects[slot];
-    if (r.x <= r.z && r.y <= r.w) {
-      uint32_t e = offsets[p];
-      const SplatRec rec = recs[slot];
-      const uint32_t cnt = splat_tiles(rec, r, tw, th);
-      if (e + cnt > capacity) {
-        atomicExch(&ctr->overflow, 1u);
-      } else {
-        const uint32_t v = block_view[slot >> 8];
-        const uint32_t base = views[v].tile_base, tiles_x = views[v].tiles_x;
-        for (uint32_t ty = r.y; ty <= r.w; ty++) {
-          uint32_t t0, t1;
-          if (!sl_row_tiles(rec.a.x, rec.a.y, rec.a.z, rec.a.w, rec.b.x, rec.b.y, rec.b.w, r.x, r.z, ty, tw, th, &t0,
-                            &t1))
-            continue;
-          const uint32_t row = base + ty * tiles_x;
-          for (uint32_t tx = t0; tx <= t1; tx++) {
-            const uint32_t tile = row + tx;
-            tile_keys[e] = tile;
-            tile_vals[e] = slot;
-            e++;
-            atomicAdd(&h[0][tile & 0xffu], 1u);
-          }
-          // the upper digits are shared by a run of ids within one 256-block: one add per run
-          for (uint32_t a = row + t0; a <= row + t1;) {
-            const uint32_t run_end = min(row + t1, a | 0xffu);
-            const uint32_t n_run = run_end - a + 1u;
-            atomicAdd(&h[1][(a >> 8) & 0xffu], n_run);
-            atomicAdd(&h[2][(a >> 16) & 0xffu], n_run);
-            a = run_end + 1u;
-          }
-        }
-      }
+    cnt = counts[p];
+    if (cnt) {
+      slot = order[p];
+      r = rects[slot];
+      rec = recs[slot];
+      e0 = offsets[p];
+      const uint32_t v = block_view[slot >> 8];
+      base = views[v].tile_base;
+      stride = views[v].tiles_x;
+      if (e0 + cnt > capacity) atomicExch(&ctr->overflow, 1u);
+      else mine = true;
     }
   }
+  Hist24 hh{h};
+  emit_warp<uint32_t>(mine, slot, r, rec, e0, cnt, tw, th, base, stride, tile_keys, tile_vals, hh);
   __syncthreads();
   for (int q = 0; q < 3; q++)
     if (h[q][t]) atomicAdd(&digit_hist[256 * q + t], h[q][t]);
@@ -152,22 +157,24 @@ __global__ void __launch_bounds__(kThreads) btile_runs_kernel(const uint32_t* __
 
 }  // namespace
 
-cudaError_t launch_btile_count(const uint32_t* order, const uint32_t* tile_n, const uint32_t* totals, uint32_t n_max,
-                               uint32_t* counts, cudaStream_t s) {
+cudaError_t launch_btile_count(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
+                               const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t* counts,
+                               cudaStream_t s) {
   if (!n_max) return cudaSuccess;
-  btile_count_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, tile_n, totals, n_max, counts);
+  btile_count_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, recs, totals, n_max, tw, th,
+                                                                            counts);
   return cudaGetLastError();
 }
 
 cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
-                              const uint32_t* offsets, const BatchView* views, const uint32_t* block_view,
-                              const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t capacity,
-                              FrameCounters* ctr, uint32_t* tile_keys, uint32_t* tile_vals, uint32_t* digit_hist,
-                              cudaStream_t s) {
+                              const uint32_t* offsets, const uint32_t* counts, const BatchView* views,
+                              const uint32_t* block_view, const uint32_t* totals, uint32_t n_max, uint32_t tw,
+                              uint32_t th, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
+                              uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s) {
   if (!n_max) return cudaSuccess;
   btile_emit_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(
-      order, rects, recs, offsets, views, block_view, totals, n_max, tw, th, capacity, ctr, tile_keys, tile_vals,
-      digit_hist);
+      order, rects, recs, offsets, counts, views, block_view, totals, n_max, tw, th, capacity, ctr, tile_keys,
+      tile_vals, digit_hist);
   return cudaGetLastError();
 }
 

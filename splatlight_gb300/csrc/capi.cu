@@ -29,7 +29,7 @@ void ViewBuffers::release_all() {
   DevBuf* all[] = {&key16,     &recs,      &rects,       &order,       &slot_counts, &slot_offsets, &keys_alt,
                    &vals_alt,  &status,    &tile_ctr,    &tile_keys,   &tile_vals,   &tile_counts,  &tile_starts,
                    &ranges,    &digit_hist, &scan_scratch, &counters, &out,         &counts,       &run_start,
-                   &run_end,   &tile_n};
+                   &run_end};
   for (DevBuf* b : all) b->release();
 }
 
@@ -319,7 +319,6 @@ static cudaError_t ensure_view_buffers(ViewBuffers& vb, uint32_t n, uint32_t til
   ENS(vb.order, 4ull * n + 16);
   ENS(vb.slot_counts, 4ull * n + 16);
   ENS(vb.slot_offsets, 4ull * n + 16);
-  ENS(vb.tile_n, 4ull * n + 16);
   uint64_t big = cap > n ? cap : n;
   ENS(vb.keys_alt, 2 * big + 16);
   ENS(vb.vals_alt, 4 * big + 16);
@@ -370,22 +369,22 @@ static int render_once(sl_renderer* r, const sl_render_frame* f, float4* out_dev
   SL_CHECK_CUDA(cudaMemsetAsync(vb.run_start.ptr, 0, 4ull * tiles, s), "memset runs");
   SL_CHECK_CUDA(cudaMemsetAsync(vb.run_end.ptr, 0, 4ull * tiles, s), "memset runs");
   SL_CHECK_CUDA(launch_project(P, r->gaussians.as<sl_gaussian>(), r->emitters.as<sl_gaussian>(), colour, lo_b,
-                               vb.key16.as<uint16_t>(), vb.recs.as<SplatRec>(), vb.rects.as<ushort4>(),
-                               vb.tile_n.as<uint32_t>(), hist, ctr, s),
+                               vb.key16.as<uint16_t>(), vb.recs.as<SplatRec>(), vb.rects.as<ushort4>(), hist, ctr, s),
                 "project");
   if (ev) SL_CHECK_CUDA(cudaEventRecord(ev[1], s), "event");
   SL_CHECK_CUDA(sort16_pairs(vb.key16.as<uint16_t>(), nullptr, vb.order.as<uint32_t>(), n, nullptr, 16, hist, sc,
                              ctr, s),
                 "depth sort");
   if (ev) SL_CHECK_CUDA(cudaEventRecord(ev[2], s), "event");
-  SL_CHECK_CUDA(launch_tile_counts_gather(vb.order.as<uint32_t>(), vb.tile_n.as<uint32_t>(), n, ctr,
-                                          vb.slot_counts.as<uint32_t>(), s),
+  SL_CHECK_CUDA(launch_tile_counts(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.recs.as<SplatRec>(), n, P.tile_w,
+                                   P.tile_h, ctr, vb.slot_counts.as<uint32_t>(), s),
                 "tile counts");
   SL_CHECK_CUDA(exclusive_scan_u32(vb.slot_counts.as<uint32_t>(), vb.slot_offsets.as<uint32_t>(), n, &ctr->entries,
                                    vb.scan_scratch.ptr, ctr, s),
                 "entry scan");
   SL_CHECK_CUDA(launch_tile_emit(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.recs.as<SplatRec>(),
-                                 vb.slot_offsets.as<uint32_t>(), n, P.tiles_x, P.tile_w, P.tile_h,
+                                 vb.slot_offsets.as<uint32_t>(), vb.slot_counts.as<uint32_t>(), n, P.tiles_x, P.tile_w,
+                                 P.tile_h,
                                  (uint32_t)(cap > 0xffffffffull ? 0xffffffffu : cap), ctr,
                                  vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), hist + 512, s),
                 "tile emit");

@@ -75,7 +75,6 @@ cudaError_t allocate(sl_batch* b) {
   ENS(b->order, 4 * S + 16);
   ENS(b->recs, sizeof(SplatRec) * S);
   ENS(b->rects, 8 * S);
-  ENS(b->tile_n, 4 * S + 16);
   ENS(b->slot_counts, 4 * S + 16);
   ENS(b->slot_offsets, 4 * S + 16);
   ENS(b->tile_keys, 4 * E + 16);
@@ -127,7 +126,7 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   const uint32_t* totals = b->dyn.as<uint32_t>();  // BatchDyn words: total slots, total tiles, ...
   uint32_t* hist = b->hist.as<uint32_t>();
   CK(launch_bproject(b->views.as<BatchView>(), b->block_view.as<uint32_t>(), B, b->keys32.as<uint32_t>(),
-                     b->recs.as<SplatRec>(), b->rects.as<ushort4>(), b->tile_n.as<uint32_t>(), hist, b->view_maxrad.as<uint32_t>(),
+                     b->recs.as<SplatRec>(), b->rects.as<ushort4>(), hist, b->view_maxrad.as<uint32_t>(),
                      b->view_visible.as<uint32_t>(), s));
   // the shading list (visible Gaussians of lit views in shading order, per view), then the shading pass
   CK(launch_bshade_flags(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(),
@@ -144,11 +143,13 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   CK(sort32_pairs(b->keys32.as<uint32_t>(), b->keys_alt.as<uint32_t>(), nullptr, b->order.as<uint32_t>(),
                   b->vals_alt.as<uint32_t>(), S, totals, 16 + bits_for(V - 1), hist, b->status.as<uint32_t>(),
                   b->tile_ctr.as<uint32_t>(), max_tiles_sort, ctr, s));
-  CK(launch_btile_count(b->order.as<uint32_t>(), b->tile_n.as<uint32_t>(), totals, S, b->slot_counts.as<uint32_t>(), s));
+  CK(launch_btile_count(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->recs.as<SplatRec>(), totals, S, b->tile_w,
+                        b->tile_h, b->slot_counts.as<uint32_t>(), s));
   CK(exclusive_scan_u32(b->slot_counts.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), S, &ctr->entries,
                         b->scan_scratch.ptr, ctr, s));
   CK(launch_btile_emit(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->recs.as<SplatRec>(),
-                       b->slot_offsets.as<uint32_t>(), b->views.as<BatchView>(), b->block_view.as<uint32_t>(), totals,
+                       b->slot_offsets.as<uint32_t>(), b->slot_counts.as<uint32_t>(), b->views.as<BatchView>(),
+                       b->block_view.as<uint32_t>(), totals,
                        S, b->tile_w, b->tile_h, E, ctr,
                        b->tile_keys.as<uint32_t>(), b->tile_vals.as<uint32_t>(), hist + 768, s));
   CK(sort32_pairs(b->tile_keys.as<uint32_t>(), b->tile_keys_alt.as<uint32_t>(), b->tile_vals.as<uint32_t>(),
@@ -446,7 +447,7 @@ int sl_batch_destroy(sl_batch* b) {
   drop_graph(b);
   free_pinned(b);
   sl::DevBuf* all[] = {&b->views, &b->views_out, &b->block_view, &b->scenes_dev, &b->dyn, &b->keys32, &b->keys_alt,
-                       &b->vals_alt, &b->order, &b->recs, &b->rects, &b->tile_n, &b->slot_counts, &b->slot_offsets,
+                       &b->vals_alt, &b->order, &b->recs, &b->rects, &b->slot_counts, &b->slot_offsets,
                        &b->tile_keys, &b->tile_keys_alt, &b->tile_vals, &b->tile_vals_alt, &b->status, &b->tile_ctr,
                        &b->hist, &b->scan_scratch, &b->run_start, &b->run_end, &b->tile_counts, &b->tile_starts,
                        &b->ranges, &b->counters, &b->view_maxrad, &b->view_visible};

@@ -128,7 +128,8 @@ int run(sl_diff* d, const sl_diff_scene* sc, const sl_render_frame* f, const flo
                         vb.scan_scratch.ptr, ctr, s),
      "entry scan");
   CK(launch_tile_emit(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.recs.as<SplatRec>(),
-                      vb.slot_offsets.as<uint32_t>(), n, tx, 16, 16, cap32, ctr, vb.tile_keys.as<uint16_t>(),
+                      vb.slot_offsets.as<uint32_t>(), vb.slot_counts.as<uint32_t>(), n, tx, 16, 16, cap32, ctr,
+                      vb.tile_keys.as<uint16_t>(),
                       vb.tile_vals.as<uint32_t>(), hist + 512, s),
      "tile emit");
   CK(sort16_pairs(vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), vb.tile_vals.as<uint32_t>(), cap32,

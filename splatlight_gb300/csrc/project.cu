@@ -11,7 +11,6 @@
 
 #include "sl_detmath.h"
 #include "sl_internal.h"
-#include "sl_tilespan.h"
 
 namespace sl {
 namespace {
@@ -55,11 +54,10 @@ constexpr int kThreads = 256;
 __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i, const float4* __restrict__ gaussians,
                                              const float4* __restrict__ emitters, const float4* __restrict__ colour,
                                              const float4* __restrict__ lo_b, SplatRec* rec_out, uint32_t& key_out,
-                                             ushort4& rect_out, float& maxrad_out, uint32_t& ntiles_out) {
+                                             ushort4& rect_out, float& maxrad_out) {
   uint32_t key = kInvalidKey16;
   ushort4 rect = make_ushort4(1, 1, 0, 0);
   float maxrad = 0.0f;
-  uint32_t ntiles = 0;
   bool live = i < P.n_slots && i != P.count && i <= P.count + P.n_emit;
 
   float4 g0, g1, g2, g3;
@@ -290,17 +288,9 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
           iy0 = iy0 < 0 ? 0 : iy0;
           ix1 = ix1 > (int)Wf - 1 ? (int)Wf - 1 : ix1;
           iy1 = iy1 > (int)Hf - 1 ? (int)Hf - 1 : iy1;
-          if (ix0 <= ix1 && iy0 <= iy1) {
+          if (ix0 <= ix1 && iy0 <= iy1)
             rect = make_ushort4((unsigned short)(ix0 / (int)P.tile_w), (unsigned short)(iy0 / (int)P.tile_h),
                                 (unsigned short)(ix1 / (int)P.tile_w), (unsigned short)(iy1 / (int)P.tile_h));
-            // tiles the binning will emit for this splat (the same row spans, from the same record values)
-            for (uint32_t ty = rect.y; ty <= rect.w; ty++) {
-              uint32_t t0, t1;
-              if (sl_row_tiles(rec.a.x, rec.a.y, rec.a.z, rec.a.w, rec.b.x, rec.b.y, rec.b.w, rect.x, rect.z, ty,
-                               P.tile_w, P.tile_h, &t0, &t1))
-                ntiles += t1 - t0 + 1u;
-            }
-          }
         }
       }
     }
@@ -309,7 +299,6 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
   key_out = key;
   rect_out = rect;
   maxrad_out = maxrad;
-  ntiles_out = ntiles;
 }
 
 __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant__ ProjectParams P,
@@ -318,7 +307,6 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
                                                            const float4* __restrict__ colour,
                                                            const float4* __restrict__ lo_b, uint16_t* __restrict__ key16,
                                                            SplatRec* __restrict__ recs, ushort4* __restrict__ rects,
-                                                           uint32_t* __restrict__ tile_n,
                                                            uint32_t* __restrict__ digit_hist, FrameCounters* ctr) {
   __shared__ uint32_t h_lo[256], h_hi[256];
   __shared__ uint32_t s_visible;
@@ -336,12 +324,10 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
   uint32_t key;
   ushort4 rect;
   float maxrad;
-  uint32_t ntiles;
-  project_slot(P, i, gaussians, emitters, colour, lo_b, recs + i, key, rect, maxrad, ntiles);
+  project_slot(P, i, gaussians, emitters, colour, lo_b, recs + i, key, rect, maxrad);
   if (i < P.n_slots) {
     key16[i] = (uint16_t)key;
     rects[i] = rect;
-    tile_n[i] = ntiles;
     atomicAdd(&h_lo[key & 0xffu], 1u);
     atomicAdd(&h_hi[key >> 8], 1u);
     if (key != kInvalidKey16) {
@@ -364,8 +350,7 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
 __global__ void __launch_bounds__(kThreads) bproject_kernel(const BatchView* __restrict__ views,
                                                             const uint32_t* __restrict__ block_view,
                                                             uint32_t* __restrict__ keys32, SplatRec* __restrict__ recs,
-                                                            ushort4* __restrict__ rects, uint32_t* __restrict__ tile_n,
-                                                            uint32_t* __restrict__ digit_hist,
+                                                            ushort4* __restrict__ rects, uint32_t* __restrict__ digit_hist,
                                                             uint32_t* __restrict__ view_maxrad,
                                                             uint32_t* __restrict__ view_visible) {
   __shared__ ProjectParams sP;
@@ -393,12 +378,10 @@ __global__ void __launch_bounds__(kThreads) bproject_kernel(const BatchView* __r
   uint32_t key;
   ushort4 rect;
   float maxrad;
-  uint32_t ntiles;
-  project_slot(sP, i, V.gaussians, V.emitters, V.colour, V.lo_b, recs + gslot, key, rect, maxrad, ntiles);
+  project_slot(sP, i, V.gaussians, V.emitters, V.colour, V.lo_b, recs + gslot, key, rect, maxrad);
   const uint32_t key32 = (v << 16) | key;
   keys32[gslot] = key32;
   rects[gslot] = rect;
-  tile_n[gslot] = ntiles;
   atomicAdd(&h[0][key32 & 0xffu], 1u);
   atomicAdd(&h[1][(key32 >> 8) & 0xffu], 1u);
   atomicAdd(&h[2][(key32 >> 16) & 0xffu], 1u);
@@ -418,23 +401,22 @@ __global__ void __launch_bounds__(kThreads) bproject_kernel(const BatchView* __r
 }  // namespace
 
 cudaError_t launch_bproject(const BatchView* views, const uint32_t* block_view, uint32_t max_blocks, uint32_t* keys32,
-                            SplatRec* recs, ushort4* rects, uint32_t* tile_n, uint32_t* digit_hist,
-                            uint32_t* view_maxrad, uint32_t* view_visible, cudaStream_t s) {
+                            SplatRec* recs, ushort4* rects, uint32_t* digit_hist, uint32_t* view_maxrad,
+                            uint32_t* view_visible, cudaStream_t s) {
   if (max_blocks == 0) return cudaSuccess;
-  bproject_kernel<<<max_blocks, kThreads, 0, s>>>(views, block_view, keys32, recs, rects, tile_n, digit_hist,
-                                                  view_maxrad, view_visible);
+  bproject_kernel<<<max_blocks, kThreads, 0, s>>>(views, block_view, keys32, recs, rects, digit_hist, view_maxrad,
+                                                  view_visible);
   return cudaGetLastError();
 }
 
 cudaError_t launch_project(const ProjectParams& P, const sl_gaussian* gaussians, const sl_gaussian* emitters,
                            const float4* colour, const float4* lo_b, uint16_t* key16, SplatRec* recs,
-                           ushort4* rects, uint32_t* tile_n, uint32_t* digit_hist, FrameCounters* ctr,
-                           cudaStream_t s) {
+                           ushort4* rects, uint32_t* digit_hist, FrameCounters* ctr, cudaStream_t s) {
   if (P.n_slots == 0) return cudaSuccess;
   uint32_t blocks = (P.n_slots + kThreads - 1) / kThreads;
   project_kernel<<<blocks, kThreads, 0, s>>>(P, reinterpret_cast<const float4*>(gaussians),
                                              reinterpret_cast<const float4*>(emitters), colour, lo_b, key16, recs,
-                                             rects, tile_n, digit_hist, ctr);
+                                             rects, digit_hist, ctr);
   return cudaGetLastError();
 }
 

@@ -61,11 +61,9 @@ struct FrameCounters {
 // ---- launchers (each returns cudaError_t of the launch) ----------------------------------------------------------
 
 // project.cu
-// tile_n[slot]: the tiles the binning will emit for the slot (its row spans), 0 when culled
 cudaError_t launch_project(const ProjectParams& P, const sl_gaussian* gaussians, const sl_gaussian* emitters,
                            const float4* colour, const float4* lo_b, uint16_t* key16, SplatRec* recs,
-                           ushort4* rects, uint32_t* tile_n, uint32_t* digit_hist /*[2][256]*/, FrameCounters* ctr,
-                           cudaStream_t s);
+                           ushort4* rects, uint32_t* digit_hist /*[2][256]*/, FrameCounters* ctr, cudaStream_t s);
 
 // sort.cu: onesweep LSD radix sort of 16-bit keys with u32 values.
 struct SortScratch {
@@ -103,13 +101,11 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, ui
 // tiles.cu
 cudaError_t launch_tile_counts(const uint32_t* order, const ushort4* rects, const SplatRec* recs, uint32_t n,
                                uint32_t tw, uint32_t th, const FrameCounters* ctr, uint32_t* counts, cudaStream_t s);
-// The same from the per-slot counts the projection stored (tile_n, indexed by slot).
-cudaError_t launch_tile_counts_gather(const uint32_t* order, const uint32_t* tile_n, uint32_t n,
-                                      const FrameCounters* ctr, uint32_t* counts, cudaStream_t s);
+// counts: the per-position tile counts the scan of offsets was made from
 cudaError_t launch_tile_emit(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
-                             const uint32_t* offsets, uint32_t n, uint32_t tiles_x, uint32_t tw, uint32_t th,
-                             uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys, uint32_t* tile_vals,
-                             uint32_t* digit_hist, cudaStream_t s);
+                             const uint32_t* offsets, const uint32_t* counts, uint32_t n, uint32_t tiles_x,
+                             uint32_t tw, uint32_t th, uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys,
+                             uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s);
 // After the tile sort: per tile the run [start, end) of its id in the sorted keys (both zero for an empty tile;
 // the arrays are cleared by the caller), then counts = end - start.
 cudaError_t launch_tile_runs(const uint16_t* sorted_keys, const uint32_t* n_dev, uint32_t n_max, uint32_t* run_start,
@@ -147,7 +143,7 @@ struct BatchView {
 };
 constexpr uint32_t kNoView = 0xFFFFFFFFu;
 cudaError_t launch_bproject(const BatchView* views, const uint32_t* block_view, uint32_t max_blocks, uint32_t* keys32,
-                            SplatRec* recs, ushort4* rects, uint32_t* tile_n, uint32_t* digit_hist /*[3][256]*/,
+                            SplatRec* recs, ushort4* rects, uint32_t* digit_hist /*[3][256]*/,
                             uint32_t* view_maxrad, uint32_t* view_visible, cudaStream_t s);
 
 // What the batched compositor needs of each view (device array, ascending tile_base).
@@ -173,13 +169,14 @@ cudaError_t launch_bcomposite(const BatchComposite& B, const uint2* ranges, cons
                               const SplatRec* recs, const BatchViewOut* views, const uint32_t* view_maxrad,
                               const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s);
 // batch.cu (totals: the BatchDyn, read as u32 words: [0] total slots, [1] total tiles)
-cudaError_t launch_btile_count(const uint32_t* order, const uint32_t* tile_n, const uint32_t* totals, uint32_t n_max,
-                               uint32_t* counts, cudaStream_t s);
+cudaError_t launch_btile_count(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
+                               const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t* counts,
+                               cudaStream_t s);
 cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
-                              const uint32_t* offsets, const BatchView* views, const uint32_t* block_view,
-                              const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t capacity,
-                              FrameCounters* ctr, uint32_t* tile_keys, uint32_t* tile_vals, uint32_t* digit_hist,
-                              cudaStream_t s);
+                              const uint32_t* offsets, const uint32_t* counts, const BatchView* views,
+                              const uint32_t* block_view, const uint32_t* totals, uint32_t n_max, uint32_t tw,
+                              uint32_t th, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
+                              uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s);
 // The batched shading list: per view, its visible Gaussians of lit views in its scene's shading order.  flags[g]
 // (g over every view's padded slots, shading-order position g - slot_base) is 1 when that Gaussian is visible;
 // after the exclusive scan of the flags into offsets, list[slot_base + k] is the k-th one's global slot.

@@ -43,7 +43,7 @@ struct DevBuf {
 
 // Per-view working buffers of the project -> sort -> bin -> composite chain.
 struct ViewBuffers {
-  DevBuf key16, recs, rects, order, slot_counts, slot_offsets, tile_n;  // per slot
+  DevBuf key16, recs, rects, order, slot_counts, slot_offsets;  // per slot
   DevBuf keys_alt, vals_alt, status, tile_ctr;                 // sort scratch (max of slots, entries)
   DevBuf tile_keys, tile_vals;                                 // per entry
   DevBuf tile_counts, tile_starts, ranges, run_start, run_end; // per tile

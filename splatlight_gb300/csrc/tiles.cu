@@ -6,6 +6,7 @@
 // 474-485): the ranges are the rasteriser's coverage made explicit per tile.
 #include "sl_internal.h"
 #include "sl_tilespan.h"
+#include "sl_emit.cuh"
 
 namespace sl {
 namespace {
@@ -40,20 +41,25 @@ __global__ void __launch_bounds__(kThreads) tile_count_kernel(const uint32_t* __
   counts[p] = c;
 }
 
-// the same counts from the per-slot tile counts the projection stored (gathered into depth order)
-__global__ void __launch_bounds__(kThreads) tile_count_gather_kernel(const uint32_t* __restrict__ order,
-                                                                     const uint32_t* __restrict__ tile_n, uint32_t n,
-                                                                     const FrameCounters* ctr,
-                                                                     uint32_t* __restrict__ counts) {
-  uint32_t p = blockIdx.x * kThreads + threadIdx.x;
-  if (p >= n) return;
-  counts[p] = p < ctr->visible ? tile_n[order[p]] : 0u;
-}
+// digit histograms of 16-bit tile ids (low byte per id, high byte per run of ids within one 256-block)
+struct Hist16 {
+  uint32_t* lo;
+  uint32_t* hi;
+  __device__ __forceinline__ void add(uint32_t first, uint32_t n) {
+    for (uint32_t k = 0; k < n; k++) atomicAdd(&lo[(first + k) & 0xffu], 1u);
+    for (uint32_t a = first, end = first + n; a < end;) {
+      const uint32_t stop = min(end, (a | 0xffu) + 1u);
+      atomicAdd(&hi[(a >> 8) & 0xffu], stop - a);
+      a = stop;
+    }
+  }
+};
 
 __global__ void __launch_bounds__(kThreads) tile_emit_kernel(const uint32_t* __restrict__ order,
                                                              const ushort4* __restrict__ rects,
                                                              const SplatRec* __restrict__ recs,
-                                                             const uint32_t* __restrict__ offsets, uint32_t n,
+                                                             const uint32_t* __restrict__ offsets,
+                                                             const uint32_t* __restrict__ counts, uint32_t n,
                                                              uint32_t tiles_x, uint32_t tw, uint32_t th,
                                                              uint32_t capacity, FrameCounters* ctr,
                                                              uint16_t* __restrict__ tile_keys,
@@ -66,40 +72,23 @@ __global__ void __launch_bounds__(kThreads) tile_emit_kernel(const uint32_t* __r
   __syncthreads();
   const uint32_t p = blockIdx.x * kThreads + t;
   const uint32_t visible = ctr->visible;
+  bool mine = false;
+  uint32_t slot = 0, e0 = 0, cnt = 0;
+  ushort4 r = make_ushort4(1, 1, 0, 0);
+  SplatRec rec{};
   if (p < n && p < visible) {
-    const uint32_t slot = order[p];
-    const ushort4 r = rects[slot];
-    uint32_t e = offsets[p];
-    if (r.x <= r.z && r.y <= r.w) {
-      const SplatRec rec = recs[slot];
-      const uint32_t cnt = splat_tiles(rec, r, tw, th);
-      if (e + cnt > capacity) {
-        atomicExch(&ctr->overflow, 1u);
-      } else {
-        for (uint32_t ty = r.y; ty <= r.w; ty++) {
-          uint32_t t0, t1;
-          if (!sl_row_tiles(rec.a.x, rec.a.y, rec.a.z, rec.a.w, rec.b.x, rec.b.y, rec.b.w, r.x, r.z, ty, tw, th, &t0,
-                            &t1))
-            continue;
-          // one row of tiles: ids are consecutive, so the high digit is shared by most of the row
-          const uint32_t row = ty * tiles_x;
-          for (uint32_t tx = t0; tx <= t1; tx++) {
-            const uint32_t tile = row + tx;
-            tile_keys[e] = (uint16_t)tile;
-            tile_vals[e] = slot;
-            e++;
-            atomicAdd(&h_lo[tile & 0xffu], 1u);
-          }
-          const uint32_t first = row + t0, last = row + t1;
-          if ((first >> 8) == (last >> 8)) {
-            atomicAdd(&h_hi[first >> 8], t1 - t0 + 1u);
-          } else {
-            for (uint32_t tx = t0; tx <= t1; tx++) atomicAdd(&h_hi[(row + tx) >> 8], 1u);
-          }
-        }
-      }
+    cnt = counts[p];
+    if (cnt) {
+      slot = order[p];
+      r = rects[slot];
+      rec = recs[slot];
+      e0 = offsets[p];
+      if (e0 + cnt > capacity) atomicExch(&ctr->overflow, 1u);
+      else mine = true;
     }
   }
+  Hist16 h{h_lo, h_hi};
+  emit_warp<uint16_t>(mine, slot, r, rec, e0, cnt, tw, th, 0u, tiles_x, tile_keys, tile_vals, h);
   __syncthreads();
   if (h_lo[t]) atomicAdd(&digit_hist[t], h_lo[t]);
   if (h_hi[t]) atomicAdd(&digit_hist[256 + t], h_hi[t]);
@@ -140,20 +129,13 @@ cudaError_t launch_tile_counts(const uint32_t* order, const ushort4* rects, cons
   return cudaGetLastError();
 }
 
-cudaError_t launch_tile_counts_gather(const uint32_t* order, const uint32_t* tile_n, uint32_t n,
-                                      const FrameCounters* ctr, uint32_t* counts, cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
-  tile_count_gather_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, tile_n, n, ctr, counts);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_tile_emit(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
-                             const uint32_t* offsets, uint32_t n, uint32_t tiles_x, uint32_t tw, uint32_t th,
-                             uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys, uint32_t* tile_vals,
-                             uint32_t* digit_hist, cudaStream_t s) {
+                             const uint32_t* offsets, const uint32_t* counts, uint32_t n, uint32_t tiles_x,
+                             uint32_t tw, uint32_t th, uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys,
+                             uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  tile_emit_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, recs, offsets, n, tiles_x, tw, th,
-                                                                       capacity, ctr, tile_keys, tile_vals,
+  tile_emit_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, recs, offsets, counts, n, tiles_x,
+                                                                       tw, th, capacity, ctr, tile_keys, tile_vals,
                                                                        digit_hist);
   return cudaGetLastError();
 }
