@@ -73,4 +73,40 @@ __device__ __forceinline__ void emit_warp(bool mine, uint32_t slot, ushort4 r, c
   }
 }
 
+// The tile count of this lane's splat (0 when !mine), the same per-row spans summed; splats whose candidate rectangle
+// has more than kSmallTiles tiles are counted by the whole warp, a row per lane.
+__device__ __forceinline__ uint32_t count_warp(bool mine, ushort4 r, const SplatRec& rec, uint32_t tw, uint32_t th) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const bool valid = mine && r.x <= r.z && r.y <= r.w;
+  const bool small = valid && (uint32_t)(r.z - r.x + 1) * (uint32_t)(r.w - r.y + 1) <= kSmallTiles;
+  uint32_t n = 0;
+  if (small)
+    for (uint32_t ty = r.y; ty <= r.w; ty++) {
+      uint32_t t0, t1;
+      if (sl_row_tiles(rec.a.x, rec.a.y, rec.a.z, rec.a.w, rec.b.x, rec.b.y, rec.b.w, r.x, r.z, ty, tw, th, &t0, &t1))
+        n += t1 - t0 + 1u;
+    }
+  uint32_t big = __ballot_sync(0xffffffffu, valid && !small);
+  while (big) {
+    const int src = __ffs(big) - 1;
+    big &= big - 1u;
+    const uint32_t s_xy = __shfl_sync(0xffffffffu, (uint32_t)r.x | ((uint32_t)r.y << 16), src);
+    const uint32_t s_zw = __shfl_sync(0xffffffffu, (uint32_t)r.z | ((uint32_t)r.w << 16), src);
+    const float ax = __shfl_sync(0xffffffffu, rec.a.x, src), ay = __shfl_sync(0xffffffffu, rec.a.y, src);
+    const float az = __shfl_sync(0xffffffffu, rec.a.z, src), aw = __shfl_sync(0xffffffffu, rec.a.w, src);
+    const float bx = __shfl_sync(0xffffffffu, rec.b.x, src), by = __shfl_sync(0xffffffffu, rec.b.y, src);
+    const float bw = __shfl_sync(0xffffffffu, rec.b.w, src);
+    const uint32_t rx = s_xy & 0xffffu, ry = s_xy >> 16, rz = s_zw & 0xffffu, rw = s_zw >> 16;
+    uint32_t sum = 0;
+    for (uint32_t ty = ry + lane; ty <= rw; ty += 32u) {
+      uint32_t t0, t1;
+      if (sl_row_tiles(ax, ay, az, aw, bx, by, bw, rx, rz, ty, tw, th, &t0, &t1)) sum += t1 - t0 + 1u;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == (uint32_t)src) n = sum;
+  }
+  return n;
+}
+
 }  // namespace sl

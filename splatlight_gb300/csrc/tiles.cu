@@ -13,32 +13,23 @@ namespace {
 
 constexpr int kThreads = 256;
 
-// Tiles a splat reaches: per tile row of its candidate rectangle, the columns its ellipse spans over that row.
-__device__ __forceinline__ uint32_t splat_tiles(const SplatRec& rec, ushort4 r, uint32_t tw, uint32_t th) {
-  if (!(r.x <= r.z && r.y <= r.w)) return 0u;
-  uint32_t n = 0;
-  for (uint32_t ty = r.y; ty <= r.w; ty++) {
-    uint32_t t0, t1;
-    if (sl_row_tiles(rec.a.x, rec.a.y, rec.a.z, rec.a.w, rec.b.x, rec.b.y, rec.b.w, r.x, r.z, ty, tw, th, &t0, &t1))
-      n += t1 - t0 + 1u;
-  }
-  return n;
-}
-
 __global__ void __launch_bounds__(kThreads) tile_count_kernel(const uint32_t* __restrict__ order,
                                                               const ushort4* __restrict__ rects,
                                                               const SplatRec* __restrict__ recs, uint32_t n,
                                                               uint32_t tw, uint32_t th, const FrameCounters* ctr,
                                                               uint32_t* __restrict__ counts) {
-  uint32_t p = blockIdx.x * kThreads + threadIdx.x;
-  if (p >= n) return;
+  const uint32_t p = blockIdx.x * kThreads + threadIdx.x;
   const uint32_t visible = ctr->visible;
-  uint32_t c = 0;
-  if (p < visible) {
+  const bool mine = p < n && p < visible;
+  ushort4 r = make_ushort4(1, 1, 0, 0);
+  SplatRec rec{};
+  if (mine) {
     const uint32_t slot = order[p];
-    c = splat_tiles(recs[slot], rects[slot], tw, th);
+    r = rects[slot];
+    rec = recs[slot];
   }
-  counts[p] = c;
+  const uint32_t c = count_warp(mine, r, rec, tw, th);
+  if (p < n) counts[p] = c;
 }
 
 // digit histograms of 16-bit tile ids (low byte per id, high byte per run of ids within one 256-block)
