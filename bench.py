@@ -506,9 +506,9 @@ def run_diff(args, stream, flush):
             "grad_norms": {k: round(v, 6) for k, v in gnorm.items()}}
 
 
-# bproject, shading flags, scan, compact, bshade, 3 depth-sort passes, tile counts, scan, emit, 3 tile-sort passes,
-# runs, run counts, scan, ranges, bcomposite
-BATCH_KERNELS = 20
+# bproject, 3 depth-sort passes, tile counts, scan, emit, 3 tile-sort passes, runs, run counts, scan, ranges,
+# coverage pass, shading flags, scan, compact, bshade, bcomposite
+BATCH_KERNELS = 21
 
 
 def run_reference(args):

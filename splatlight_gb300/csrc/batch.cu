@@ -91,9 +91,10 @@ __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __
     if (h[q][t]) atomicAdd(&digit_hist[256 * q + t], h[q][t]);
 }
 
-// shading-list flags: position g of the padded slots <-> the view's Gaussian order[g - slot_base] (shading order)
+// shading-list flags: position g of the padded slots <-> the view's Gaussian order[g - slot_base] (shading order);
+// a Gaussian is shaded when the coverage pass marked it (it blends a fragment before its pixels terminate)
 __device__ __forceinline__ bool shade_candidate(const BatchView* views, const BatchScene* scenes,
-                                                const uint32_t* block_view, const uint32_t* keys32, uint32_t g,
+                                                const uint32_t* block_view, const uint8_t* marks, uint32_t g,
                                                 uint32_t& view, uint32_t& gslot) {
   const uint32_t v = block_view[g >> 8];
   if (v == kNoView) return false;
@@ -103,19 +104,19 @@ __device__ __forceinline__ bool shade_candidate(const BatchView* views, const Ba
   if (V.P.view_mode != 3u || !S.lit || j >= V.P.count) return false;
   view = v;
   gslot = V.slot_base + S.order[j];
-  return (keys32[gslot] & 0xFFFFu) != 0xFFFFu;
+  return marks[gslot] != 0u;
 }
 
 __global__ void __launch_bounds__(kThreads) bshade_flags_kernel(const BatchView* __restrict__ views,
                                                                 const BatchScene* __restrict__ scenes,
                                                                 const uint32_t* __restrict__ block_view,
-                                                                const uint32_t* __restrict__ keys32,
+                                                                const uint8_t* __restrict__ marks,
                                                                 const uint32_t* __restrict__ totals, uint32_t n_max,
                                                                 uint32_t* __restrict__ flags) {
   const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
   if (g >= n_max) return;
   uint32_t v, gslot;
-  flags[g] = (g < totals[0] && shade_candidate(views, scenes, block_view, keys32, g, v, gslot)) ? 1u : 0u;
+  flags[g] = (g < totals[0] && shade_candidate(views, scenes, block_view, marks, g, v, gslot)) ? 1u : 0u;
 }
 
 __global__ void __launch_bounds__(kThreads) bshade_compact_kernel(const BatchView* __restrict__ views,
@@ -170,10 +171,10 @@ cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const
 }
 
 cudaError_t launch_bshade_flags(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
-                                const uint32_t* keys32, const uint32_t* totals, uint32_t n_max, uint32_t* flags,
+                                const uint8_t* marks, const uint32_t* totals, uint32_t n_max, uint32_t* flags,
                                 cudaStream_t s) {
   if (!n_max) return cudaSuccess;
-  bshade_flags_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(views, scenes, block_view, keys32, totals,
+  bshade_flags_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(views, scenes, block_view, marks, totals,
                                                                              n_max, flags);
   return cudaGetLastError();
 }

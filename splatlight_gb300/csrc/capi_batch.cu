@@ -29,6 +29,8 @@ void free_pinned(sl_batch* b) {
   cudaFreeHost(b->h_dyn);
   cudaFreeHost(b->h_ctr);
   cudaFreeHost(b->h_visible);
+  cudaFreeHost(b->h_maxrad);
+  cudaFreeHost(b->h_tmark);
   b->h_views = nullptr;
   b->h_out = nullptr;
   b->h_block_view = nullptr;
@@ -36,6 +38,8 @@ void free_pinned(sl_batch* b) {
   b->h_dyn = nullptr;
   b->h_ctr = nullptr;
   b->h_visible = nullptr;
+  b->h_maxrad = nullptr;
+  b->h_tmark = nullptr;
 }
 
 void drop_graph(sl_batch* b) {
@@ -93,6 +97,8 @@ cudaError_t allocate(sl_batch* b) {
   ENS(b->counters, sizeof(FrameCounters));
   ENS(b->view_maxrad, 4ull * V + 16);
   ENS(b->view_visible, 4ull * V + 16);
+  ENS(b->marks, S + 16);
+  ENS(b->view_tmark, 4ull * V + 16);
 #undef ENS
   if ((e = cudaMallocHost((void**)&b->h_views, sizeof(BatchView) * V)) != cudaSuccess) return e;
   if ((e = cudaMallocHost((void**)&b->h_out, sizeof(BatchViewOut) * V)) != cudaSuccess) return e;
@@ -101,6 +107,8 @@ cudaError_t allocate(sl_batch* b) {
   if ((e = cudaMallocHost((void**)&b->h_dyn, sizeof(BatchDyn))) != cudaSuccess) return e;
   if ((e = cudaMallocHost((void**)&b->h_ctr, sizeof(FrameCounters))) != cudaSuccess) return e;
   if ((e = cudaMallocHost((void**)&b->h_visible, 4ull * V + 16)) != cudaSuccess) return e;
+  if ((e = cudaMallocHost((void**)&b->h_maxrad, 4ull * V + 16)) != cudaSuccess) return e;
+  if ((e = cudaMallocHost((void**)&b->h_tmark, 4ull * V + 16)) != cudaSuccess) return e;
   return cudaSuccess;
 }
 
@@ -122,23 +130,13 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   CK(cudaMemsetAsync(b->view_visible.ptr, 0, 4ull * V, s));
   CK(cudaMemsetAsync(b->run_start.ptr, 0, 4ull * T, s));
   CK(cudaMemsetAsync(b->run_end.ptr, 0, 4ull * T, s));
+  CK(cudaMemsetAsync(b->marks.ptr, 0, S, s));
   FrameCounters* ctr = b->counters.as<FrameCounters>();
   const uint32_t* totals = b->dyn.as<uint32_t>();  // BatchDyn words: total slots, total tiles, ...
   uint32_t* hist = b->hist.as<uint32_t>();
   CK(launch_bproject(b->views.as<BatchView>(), b->block_view.as<uint32_t>(), B, b->keys32.as<uint32_t>(),
                      b->recs.as<SplatRec>(), b->rects.as<ushort4>(), hist, b->view_maxrad.as<uint32_t>(),
                      b->view_visible.as<uint32_t>(), s));
-  // the shading list (visible Gaussians of lit views in shading order, per view), then the shading pass
-  CK(launch_bshade_flags(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(),
-                         b->keys32.as<uint32_t>(), totals, S, b->slot_counts.as<uint32_t>(), s));
-  CK(exclusive_scan_u32(b->slot_counts.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), S, &ctr->shade_n,
-                        b->scan_scratch.ptr, ctr, s));
-  CK(launch_bshade_compact(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(),
-                           b->slot_counts.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), totals, S,
-                           b->vals_alt.as<uint32_t>(), s));
-  CK(launch_bshade(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(), B,
-                   b->vals_alt.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), &ctr->shade_n, b->dyn.as<BatchDyn>(),
-                   b->recs.as<SplatRec>(), b->view_maxrad.as<uint32_t>(), s));
   const uint32_t max_tiles_sort = (uint32_t)(b->status.bytes / (4ull * 256 * 4));
   CK(sort32_pairs(b->keys32.as<uint32_t>(), b->keys_alt.as<uint32_t>(), nullptr, b->order.as<uint32_t>(),
                   b->vals_alt.as<uint32_t>(), S, totals, 16 + bits_for(V - 1), hist, b->status.as<uint32_t>(),
@@ -162,12 +160,29 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   CK(exclusive_scan_u32(b->tile_counts.as<uint32_t>(), b->tile_starts.as<uint32_t>(), T, nullptr, b->scan_scratch.ptr,
                         ctr, s));
   CK(launch_tile_ranges(b->tile_starts.as<uint32_t>(), b->tile_counts.as<uint32_t>(), T, b->ranges.as<uint2>(), s));
-  BatchComposite C{b->tile_w, b->tile_h, b->t_stop_scale, 0};
+  // deferred shading: the coverage pass marks the splats of lit views that blend a fragment, the shading list is
+  // their Gaussians in shading order, and only those are shaded before the composite
+  const BatchComposite C{b->tile_w, b->tile_h, b->t_stop_scale, 0};
+  CK(launch_bmark(C, b->ranges.as<uint2>(), b->tile_vals.as<uint32_t>(), b->recs.as<SplatRec>(),
+                  b->views_out.as<BatchViewOut>(), b->view_maxrad.as<uint32_t>(), b->dyn.as<BatchDyn>(), T, ctr,
+                  b->marks.as<uint8_t>(), b->view_tmark.as<float>(), s));
+  CK(launch_bshade_flags(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(),
+                         b->marks.as<uint8_t>(), totals, S, b->slot_counts.as<uint32_t>(), s));
+  CK(exclusive_scan_u32(b->slot_counts.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), S, &ctr->shade_n,
+                        b->scan_scratch.ptr, ctr, s));
+  CK(launch_bshade_compact(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(),
+                           b->slot_counts.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), totals, S,
+                           b->vals_alt.as<uint32_t>(), s));
+  CK(launch_bshade(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(), B,
+                   b->vals_alt.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), &ctr->shade_n, b->dyn.as<BatchDyn>(),
+                   b->recs.as<SplatRec>(), b->view_maxrad.as<uint32_t>(), s));
   CK(launch_bcomposite(C, b->ranges.as<uint2>(), b->tile_vals.as<uint32_t>(), b->recs.as<SplatRec>(),
                        b->views_out.as<BatchViewOut>(), b->view_maxrad.as<uint32_t>(), b->dyn.as<BatchDyn>(), T, ctr,
                        s));
   CK(cudaMemcpyAsync(b->h_ctr, ctr, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(b->h_visible, b->view_visible.ptr, 4ull * V, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(b->h_maxrad, b->view_maxrad.ptr, 4ull * V, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(b->h_tmark, b->view_tmark.ptr, 4ull * V, cudaMemcpyDeviceToHost, s));
 #undef CK
   return cudaSuccess;
 }
@@ -229,7 +244,8 @@ void stage(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* fr
     O.width = (uint32_t)frames[v].viewport[0];
     O.height = (uint32_t)frames[v].viewport[1];
     O.count_mode = frames[v].view_mode == 2u ? 1u : 0u;
-    O.pad0 = 0;
+    const sl_lighting* l = b->lights[scene_of_view[v]];
+    O.lit = (frames[v].view_mode == 3u && l && l->iso_done) ? (b->shade_blended[v] ? 2u : 1u) : 0u;
     O.out_offset = b->offsets[v] / 4;
   }
   for (uint32_t v = n_views; v < b->max_views; v++) {  // unused view rows: past every tile
@@ -309,6 +325,7 @@ int batch_layout(sl_batch* b, const uint32_t* scene_of_view, const sl_render_fra
   b->n_slots.assign(n_views, 0);
   b->tiles.assign(n_views, 0);
   b->offsets.assign(n_views, 0);
+  b->shade_blended.assign(n_views, 0);
   uint64_t slot = 0, tile = 0, pix = 0;
   for (uint32_t v = 0; v < n_views; v++) {
     const uint32_t k = scene_of_view[v];
@@ -359,6 +376,22 @@ int batch_finish(sl_batch* b, uint32_t n_views, uint64_t slots, uint64_t tiles, 
     b->entry_cap = std::min<uint64_t>(std::max<uint64_t>(want, 2 * b->entry_cap), kMaxCap);
     cudaError_t e = allocate(b);
     if (e != cudaSuccess) return cuda_fail(e, "growing the tile entries");
+    *retry = true;
+    return SL_OK;
+  }
+  // A lit view whose composite threshold (t_stop / its radiance bound after shading) fell below twice its coverage
+  // threshold may have composited past the marked splats: it runs again with every blended splat shaded (mode 2).
+  // The decision and its result depend on the view alone, not on the rest of the batch.
+  bool again = false;
+  for (uint32_t v = 0; v < n_views; v++) {
+    if (b->h_out[v].lit != 1u) continue;
+    const float t_stop = b->t_stop_scale / std::max(__builtin_bit_cast(float, b->h_maxrad[v]), 1.0f);
+    if (t_stop < 2.0f * b->h_tmark[v]) {
+      b->shade_blended[v] = 1;
+      again = true;
+    }
+  }
+  if (again) {
     *retry = true;
     return SL_OK;
   }
@@ -450,7 +483,8 @@ int sl_batch_destroy(sl_batch* b) {
                        &b->vals_alt, &b->order, &b->recs, &b->rects, &b->slot_counts, &b->slot_offsets,
                        &b->tile_keys, &b->tile_keys_alt, &b->tile_vals, &b->tile_vals_alt, &b->status, &b->tile_ctr,
                        &b->hist, &b->scan_scratch, &b->run_start, &b->run_end, &b->tile_counts, &b->tile_starts,
-                       &b->ranges, &b->counters, &b->view_maxrad, &b->view_visible};
+                       &b->ranges, &b->counters, &b->view_maxrad, &b->view_visible, &b->marks,
+                       &b->view_tmark};
   for (sl::DevBuf* x : all) x->release();
   for (auto& ev : b->ev)
     if (ev) cudaEventDestroy(ev);

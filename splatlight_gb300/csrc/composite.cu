@@ -65,17 +65,20 @@ __device__ __forceinline__ float ex2_approx(float x) {
 }
 
 // One tile: (x0, y0) its origin in a width x height image, [s, e) its range in tile_vals, out/counts the image.
-template <int TW>
+// kMark: the coverage pass of the batched path -- the same walk and alphas, no colour: marks[slot] = 1 for every splat
+// that blends a fragment before the pixel's transmittance falls below t_stop, and no image is written.
+template <int TW, bool kMark = false>
 __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_t width, uint32_t height, uint32_t s,
                                                uint32_t e, const uint32_t* __restrict__ tile_vals,
                                                const SplatRec* __restrict__ recs, uint32_t count_mode, float t_stop,
                                                FrameCounters* ctr, float4* __restrict__ out,
-                                               uint32_t* __restrict__ counts) {
+                                               uint32_t* __restrict__ counts, uint8_t* __restrict__ marks = nullptr) {
   constexpr int TH = kThreads / TW;
   constexpr int BX = TW / 8;  // warp blocks of 8 x 4 pixels per tile row
   constexpr int BY = TH / 4;
   static_assert(BX * BY == kThreads / 32, "one 8x4 block per warp");
   __shared__ SplatRec buf[2][kThreads];
+  __shared__ uint32_t sslot[kMark ? 2 : 1][kMark ? kThreads : 1];  // coverage pass: the slots of the batch
   __shared__ uint32_t masks[kThreads / 32][kThreads / 32];  // [warp block][loader warp]: records touching the block
   __shared__ __align__(8) uint64_t bars[2];
 
@@ -110,6 +113,7 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
     const uint32_t bar = (b & 1u) ? bar1 : bar0;
     if ((uint32_t)t < hi - lo) {
       const uint32_t slot = tile_vals[hi - 1u - (uint32_t)t];
+      if constexpr (kMark) sslot[b & 1u][t] = slot;
       mbar_arrive_expect(bar, kRecBytes);
       bulk_copy_g2s(smem_addr(&buf[b & 1u][t]), recs + slot, kRecBytes, bar);
     } else {
@@ -165,7 +169,16 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
           const float lx = fmaf(dx, A.z, dy * A.w);
           const float ly = fmaf(dx, B.x, dy * B.y);
           const float q = fmaf(lx, lx, ly * ly);
-          if (alive && q <= B.w) {
+          if constexpr (kMark) {
+            const bool hit = alive && q <= B.w;
+            if (hit) {
+              const float ev = ex2_approx(q * kNegHalfLog2e);
+              const float alpha = 1.0f - ex2_approx(rb[j].c.w * kNegLog2e * ev);
+              T = T - T * alpha;
+              if (T < t_stop) alive = false;
+            }
+            if (__any_sync(0xffffffffu, hit) && lane == 0) marks[sslot[b & 1u][j]] = 1u;  // one store per warp
+          } else if (alive && q <= B.w) {
             const float4 C = rb[j].c;
             const float ev = ex2_approx(q * kNegHalfLog2e);
             const float alpha = 1.0f - ex2_approx(C.w * kNegLog2e * ev);
@@ -190,6 +203,7 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
     }
   }
   if (timed_out) atomicExch(&ctr->timeout, 1u);
+  if constexpr (kMark) return;
   const uint32_t wk = __reduce_add_sync(0xffffffffu, kept);
   if (lane == 0 && wk) atomicAdd(&ctr->fragments, wk);
   if (inside) {
@@ -247,7 +261,59 @@ __global__ void __launch_bounds__(kThreads) bcomposite_kernel(const BatchComposi
                      out + v.out_offset, nullptr);
 }
 
+// The batched coverage pass over the tiles of lit views (see composite_tile): mode 1 stops each pixel at the view's
+// t_mark, mode 2 never stops (every splat that blends any pixel is marked).
+template <int TW>
+__global__ void __launch_bounds__(kThreads) bmark_kernel(const BatchComposite B, const uint2* __restrict__ ranges,
+                                                         const uint32_t* __restrict__ tile_vals,
+                                                         const SplatRec* __restrict__ recs,
+                                                         const BatchViewOut* __restrict__ views,
+                                                         const uint32_t* __restrict__ view_maxrad,
+                                                         const BatchDyn* __restrict__ dyn, FrameCounters* ctr,
+                                                         uint8_t* __restrict__ marks, float* __restrict__ view_tmark) {
+  constexpr int TH = kThreads / TW;
+  const uint32_t tile = blockIdx.x;
+  if (tile >= dyn->total_tiles) return;
+  uint32_t lo = 0, hi = dyn->n_views;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (views[mid].tile_base <= tile) lo = mid; else hi = mid;
+  }
+  const BatchViewOut v = views[lo];
+  if (v.lit == 0u) return;  // only lit views are shaded
+  const float t_mark = B.t_stop_scale / fmaxf(2.0f * __uint_as_float(view_maxrad[lo]), kRadianceCap);
+  const uint32_t lt = tile - v.tile_base;
+  if (lt == 0 && threadIdx.x == 0) view_tmark[lo] = t_mark;
+  const uint32_t tx = lt % v.tiles_x, ty = lt / v.tiles_x;
+  const uint2 rg = ranges[tile];
+  composite_tile<TW, true>(tx * TW, ty * TH, v.width, v.height, rg.x, rg.y, tile_vals, recs, 0u,
+                           v.lit == 1u ? t_mark : -1.0f, ctr, nullptr, nullptr, marks);
+}
+
 }  // namespace
+
+cudaError_t launch_bmark(const BatchComposite& B, const uint2* ranges, const uint32_t* tile_vals, const SplatRec* recs,
+                         const BatchViewOut* views, const uint32_t* view_maxrad, const BatchDyn* dyn,
+                         uint32_t max_tiles, FrameCounters* ctr, uint8_t* marks, float* view_tmark, cudaStream_t s) {
+  if (max_tiles == 0) return cudaSuccess;
+  switch (B.tile_w) {
+    case 16:
+      bmark_kernel<16><<<max_tiles, kThreads, 0, s>>>(B, ranges, tile_vals, recs, views, view_maxrad, dyn, ctr, marks,
+                                                      view_tmark);
+      break;
+    case 8:
+      bmark_kernel<8><<<max_tiles, kThreads, 0, s>>>(B, ranges, tile_vals, recs, views, view_maxrad, dyn, ctr, marks,
+                                                     view_tmark);
+      break;
+    case 32:
+      bmark_kernel<32><<<max_tiles, kThreads, 0, s>>>(B, ranges, tile_vals, recs, views, view_maxrad, dyn, ctr, marks,
+                                                      view_tmark);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
 
 cudaError_t launch_composite(const CompositeParams& P, const uint2* ranges, const uint32_t* tile_vals,
                              const SplatRec* recs, FrameCounters* ctr, float4* out, uint32_t* counts,

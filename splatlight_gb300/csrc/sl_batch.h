@@ -18,7 +18,8 @@ struct sl_batch {
   // device buffers
   sl::DevBuf views, views_out, block_view, scenes_dev, dyn, keys32, keys_alt, vals_alt, order, recs, rects,
       slot_counts, slot_offsets, tile_keys, tile_keys_alt, tile_vals, tile_vals_alt, status, tile_ctr, hist,
-      scan_scratch, run_start, run_end, tile_counts, tile_starts, ranges, counters, view_maxrad, view_visible;
+      scan_scratch, run_start, run_end, tile_counts, tile_starts, ranges, counters, view_maxrad, view_visible, marks,
+      view_tmark;
   // pinned staging
   sl::BatchView* h_views = nullptr;
   sl::BatchViewOut* h_out = nullptr;
@@ -27,6 +28,8 @@ struct sl_batch {
   sl::BatchDyn* h_dyn = nullptr;
   sl::FrameCounters* h_ctr = nullptr;
   uint32_t* h_visible = nullptr;
+  uint32_t* h_maxrad = nullptr;  // per view: its radiance bound (float bits) after shading
+  float* h_tmark = nullptr;      // per view: its coverage pass's threshold
   // graph
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};  // per tile shape (16x16, 8x32, 32x8)
@@ -36,6 +39,7 @@ struct sl_batch {
   uint32_t last_views = 0, last_slots = 0, last_tiles = 0, last_entries = 0;
   std::vector<uint64_t> offsets;
   std::vector<uint32_t> slot_base, tile_base, n_slots, tiles;
+  std::vector<uint8_t> shade_blended;  // per view of this batch: shade every blended splat (coverage mode 2)
 };
 
 namespace sl {

@@ -149,7 +149,9 @@ cudaError_t launch_bproject(const BatchView* views, const uint32_t* block_view, 
 // What the batched compositor needs of each view (device array, ascending tile_base).
 struct BatchViewOut {
   uint32_t tile_base, tiles_x, width, height;
-  uint32_t count_mode, pad0;
+  uint32_t count_mode;
+  uint32_t lit;         // 0: not shaded; shaded (view mode 3 of a lit scene) where the coverage pass marks a splat,
+                        // 1: blended before T < t_mark (launch_bmark), 2: blended anywhere (never stops)
   uint64_t out_offset;  // first float4 of the view's image in the packed output
 };
 struct BatchComposite {
@@ -163,7 +165,7 @@ struct BatchDyn {
   uint32_t total_tiles;
   uint32_t n_views;
   uint32_t total_blocks;
-  float4* out;            // packed images
+  float4* out;            // the packed images
 };
 cudaError_t launch_bcomposite(const BatchComposite& B, const uint2* ranges, const uint32_t* tile_vals,
                               const SplatRec* recs, const BatchViewOut* views, const uint32_t* view_maxrad,
@@ -177,12 +179,21 @@ cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const
                               const uint32_t* block_view, const uint32_t* totals, uint32_t n_max, uint32_t tw,
                               uint32_t th, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
                               uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s);
-// The batched shading list: per view, its visible Gaussians of lit views in its scene's shading order.  flags[g]
-// (g over every view's padded slots, shading-order position g - slot_base) is 1 when that Gaussian is visible;
+// The batched coverage pass over the tiles of lit views, run between binning and shading: marks[slot] = 1 for each
+// splat that blends a fragment before the pixel's transmittance falls below t_mark (BatchViewOut::lit 1) or at all
+// (lit 2).  t_mark = t_stop_scale / max(2 r, kRadianceCap), r the view's radiance bound so far (its unshaded splats,
+// view_maxrad), is written to view_tmark[view].  The composite, whose threshold is t_stop_scale / (the bound after
+// shading), blends only marked splats as long as that threshold stays >= 2 t_mark.
+constexpr float kRadianceCap = 64.0f;
+cudaError_t launch_bmark(const BatchComposite& B, const uint2* ranges, const uint32_t* tile_vals, const SplatRec* recs,
+                         const BatchViewOut* views, const uint32_t* view_maxrad, const BatchDyn* dyn,
+                         uint32_t max_tiles, FrameCounters* ctr, uint8_t* marks, float* view_tmark, cudaStream_t s);
+// The batched shading list: per view, its marked Gaussians of lit views in its scene's shading order.  flags[g]
+// (g over every view's padded slots, shading-order position g - slot_base) is 1 when the coverage pass marked it;
 // after the exclusive scan of the flags into offsets, list[slot_base + k] is the k-th one's global slot.
 struct BatchScene;
 cudaError_t launch_bshade_flags(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
-                                const uint32_t* keys32, const uint32_t* totals, uint32_t n_max, uint32_t* flags,
+                                const uint8_t* marks, const uint32_t* totals, uint32_t n_max, uint32_t* flags,
                                 cudaStream_t s);
 cudaError_t launch_bshade_compact(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
                                   const uint32_t* flags, const uint32_t* offsets, const uint32_t* totals,
