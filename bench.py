@@ -251,6 +251,8 @@ def run_batch(args, stream, flush):
            "speedup_vs_plain": round(ms_p / ms_b, 3), "max_abs_err_vs_plain": err,
            "tile": f"{tile[0]}x{tile[1]}", "autotune_ms": {k: round(v, 3) for k, v in tune_ms.items()},
            "slots": int(st.slots), "visible": int(st.visible), "entries": int(st.entries),
+           "shaded": int(st.shaded), "reshaded_views": int(st.reshaded_views),
+           "max_radiance": round(float(st.max_radiance), 4),
            "graph_replayed": int(st.graph_replayed), "kernels_per_batch": BATCH_KERNELS}
     B.close()
     for L in ls:
@@ -506,9 +508,9 @@ def run_diff(args, stream, flush):
             "grad_norms": {k: round(v, 6) for k, v in gnorm.items()}}
 
 
-# bproject, 3 depth-sort passes, tile counts, scan, emit, 3 tile-sort passes, runs, run counts, scan, ranges,
-# coverage pass, shading flags, scan, compact, bshade, bcomposite
-BATCH_KERNELS = 21
+# bproject, 3 depth-sort passes, tile counts, scan, emit, 2 tile-sort passes, runs (to ranges), coverage pass, shading
+# flags, scan, compact, bshade, bcomposite
+BATCH_KERNELS = 17
 
 
 def run_reference(args):

@@ -317,6 +317,9 @@ typedef struct sl_batch_stats {
   uint64_t visible, fragments;
   float ms_total;                /* device time of the chain when timing is on, else 0 */
   uint32_t graph_replayed;       /* 1 when the chain ran as a replay of the captured graph */
+  uint32_t shaded;               /* Gaussians shaded, over the lit views (those the coverage pass marked) */
+  uint32_t reshaded_views;       /* lit views run a second time with every blended splat shaded (radiance bound) */
+  float max_radiance;            /* largest radiance bound of a view (the compositor's stop is t_stop / it) */
 } sl_batch_stats;
 
 /* Creates a batch over n_scenes renderers (lightings[k]: the lighting bound to renderers[k], or NULL / a NULL array

@@ -45,7 +45,8 @@ class BatchOptions(C.Structure):
 class BatchStats(C.Structure):
     _fields_ = [("views", C.c_uint32), ("slots", C.c_uint32), ("tiles", C.c_uint32), ("entries", C.c_uint32),
                 ("visible", C.c_uint64), ("fragments", C.c_uint64), ("ms_total", C.c_float),
-                ("graph_replayed", C.c_uint32)]
+                ("graph_replayed", C.c_uint32), ("shaded", C.c_uint32), ("reshaded_views", C.c_uint32),
+                ("max_radiance", C.c_float)]
 
 
 class ServerOptions(C.Structure):

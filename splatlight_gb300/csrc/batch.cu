@@ -34,14 +34,14 @@ __global__ void __launch_bounds__(kThreads) btile_count_kernel(const uint32_t* _
 }
 
 // digit histograms of 32-bit tile ids: low byte per id, the two upper bytes per run of ids within one 256-block
-struct Hist24 {
+// Digit counts of the low 16 bits (the view-local tile id) for the two passes of the tile sort.
+struct HistLocal16 {
   uint32_t (*h)[256];
   __device__ __forceinline__ void add(uint32_t first, uint32_t n) {
     for (uint32_t k = 0; k < n; k++) atomicAdd(&h[0][(first + k) & 0xffu], 1u);
     for (uint32_t a = first, end = first + n; a < end;) {
       const uint32_t stop = min(end, (a | 0xffu) + 1u);
       atomicAdd(&h[1][(a >> 8) & 0xffu], stop - a);
-      atomicAdd(&h[2][(a >> 16) & 0xffu], stop - a);
       a = stop;
     }
   }
@@ -59,11 +59,10 @@ __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __
                                                               FrameCounters* ctr, uint32_t* __restrict__ tile_keys,
                                                               uint32_t* __restrict__ tile_vals,
                                                               uint32_t* __restrict__ digit_hist) {
-  __shared__ uint32_t h[3][256];
+  __shared__ uint32_t h[2][256];
   const int t = threadIdx.x;
   h[0][t] = 0u;
   h[1][t] = 0u;
-  h[2][t] = 0u;
   __syncthreads();
   const uint32_t p = blockIdx.x * kThreads + t;
   bool mine = false;
@@ -78,16 +77,16 @@ __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __
       rec = recs[slot];
       e0 = offsets[p];
       const uint32_t v = block_view[slot >> 8];
-      base = views[v].tile_base;
+      base = v << 16;  // key: view above its local tile id
       stride = views[v].tiles_x;
       if (e0 + cnt > capacity) atomicExch(&ctr->overflow, 1u);
       else mine = true;
     }
   }
-  Hist24 hh{h};
+  HistLocal16 hh{h};
   emit_warp<uint32_t>(mine, slot, r, rec, e0, cnt, tw, th, base, stride, tile_keys, tile_vals, hh);
   __syncthreads();
-  for (int q = 0; q < 3; q++)
+  for (int q = 0; q < 2; q++)
     if (h[q][t]) atomicAdd(&digit_hist[256 * q + t], h[q][t]);
 }
 
@@ -134,16 +133,22 @@ __global__ void __launch_bounds__(kThreads) bshade_compact_kernel(const BatchVie
   list[V.slot_base + (offsets[g] - offsets[V.slot_base])] = V.slot_base + scenes[V.scene].order[j];
 }
 
+// After the stable sort on the local tile id the entries run in (local tile, view, depth) order: every (view, tile)
+// pair is one contiguous run of its depth-ordered entries.  Its bounds go straight to ranges[tile_base[view] + local]
+// (ranges zeroed beforehand: empty tiles keep [0, 0)).
 __global__ void __launch_bounds__(kThreads) btile_runs_kernel(const uint32_t* __restrict__ keys,
                                                               const uint32_t* __restrict__ n_dev, uint32_t n_max,
-                                                              uint32_t* __restrict__ run_start,
-                                                              uint32_t* __restrict__ run_end) {
+                                                              const BatchViewOut* __restrict__ views,
+                                                              uint2* __restrict__ ranges) {
   const uint32_t nd = *n_dev;
   const uint32_t n = nd <= n_max ? nd : 0u;
   for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     const uint32_t k = keys[i];
-    if (i == 0 || keys[i - 1] != k) run_start[k] = i;
-    if (i + 1 == n || keys[i + 1] != k) run_end[k] = i + 1;
+    const bool first = i == 0 || keys[i - 1] != k, last = i + 1 == n || keys[i + 1] != k;
+    if (!first && !last) continue;
+    const uint32_t g = views[k >> 16].tile_base + (k & 0xffffu);
+    if (first) ranges[g].x = i;
+    if (last) ranges[g].y = i + 1;
   }
 }
 
@@ -188,12 +193,12 @@ cudaError_t launch_bshade_compact(const BatchView* views, const BatchScene* scen
   return cudaGetLastError();
 }
 
-cudaError_t launch_btile_runs(const uint32_t* keys, const uint32_t* n_dev, uint32_t n_max, uint32_t* run_start,
-                              uint32_t* run_end, cudaStream_t s) {
+cudaError_t launch_btile_runs(const uint32_t* keys, const uint32_t* n_dev, uint32_t n_max, const BatchViewOut* views,
+                              uint2* ranges, cudaStream_t s) {
   if (!n_max) return cudaSuccess;
   uint32_t blocks = (n_max + kThreads * 8 - 1) / (kThreads * 8);
   if (blocks > 152 * 8) blocks = 152 * 8;
-  btile_runs_kernel<<<blocks, kThreads, 0, s>>>(keys, n_dev, n_max, run_start, run_end);
+  btile_runs_kernel<<<blocks, kThreads, 0, s>>>(keys, n_dev, n_max, views, ranges);
   return cudaGetLastError();
 }
 

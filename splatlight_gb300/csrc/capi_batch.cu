@@ -1,10 +1,12 @@
 // Batched rendering over several resident scenes (C ABI): a ragged batch of views, each with its own scene, camera,
-// resolution and view mode, goes through one chain of kernels -- batched projection, batched shading of the visible
-// Gaussians, one segmented depth sort (view id above the 16 depth bits), batched tile binning, one tile sort, one
-// compositor launch over every tile of every view.  Grids are sized for the batch's capacity and every per-batch value
+// resolution and view mode, goes through one chain of kernels -- batched projection, one segmented depth sort (view id
+// above the 16 depth bits), batched tile binning, one two-pass tile sort on the view-local tile id, a coverage pass
+// over the lit views' tiles, batched shading of the Gaussians it marked (deferred shading: each view at its own eye),
+// one compositor launch over every tile of every view.  Grids are sized for the batch's capacity and every per-batch value
 // the kernels read comes from device memory uploaded (from pinned staging) at the head of the chain, so the chain is
 // captured once in a CUDA graph and replayed for every batch that fits.  An autotuner picks the tile shape.
 #include <algorithm>
+#include <cstdint>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -89,10 +91,6 @@ cudaError_t allocate(sl_batch* b) {
   ENS(b->tile_ctr, 16);
   ENS(b->hist, 4ull * 6 * 256);
   ENS(b->scan_scratch, std::max(scan_scratch_bytes((uint32_t)S), scan_scratch_bytes(T)));
-  ENS(b->run_start, 4ull * T + 16);
-  ENS(b->run_end, 4ull * T + 16);
-  ENS(b->tile_counts, 4ull * T + 16);
-  ENS(b->tile_starts, 4ull * T + 16);
   ENS(b->ranges, 8ull * T + 16);
   ENS(b->counters, sizeof(FrameCounters));
   ENS(b->view_maxrad, 4ull * V + 16);
@@ -128,8 +126,7 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   CK(cudaMemsetAsync(b->hist.ptr, 0, 4ull * 6 * 256, s));
   CK(cudaMemsetAsync(b->view_maxrad.ptr, 0, 4ull * V, s));
   CK(cudaMemsetAsync(b->view_visible.ptr, 0, 4ull * V, s));
-  CK(cudaMemsetAsync(b->run_start.ptr, 0, 4ull * T, s));
-  CK(cudaMemsetAsync(b->run_end.ptr, 0, 4ull * T, s));
+  CK(cudaMemsetAsync(b->ranges.ptr, 0, 8ull * T, s));
   CK(cudaMemsetAsync(b->marks.ptr, 0, S, s));
   FrameCounters* ctr = b->counters.as<FrameCounters>();
   const uint32_t* totals = b->dyn.as<uint32_t>();  // BatchDyn words: total slots, total tiles, ...
@@ -150,16 +147,14 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
                        b->block_view.as<uint32_t>(), totals,
                        S, b->tile_w, b->tile_h, E, ctr,
                        b->tile_keys.as<uint32_t>(), b->tile_vals.as<uint32_t>(), hist + 768, s));
+  // the tile sort: stable on the 16-bit view-local tile id (two passes); entries arrive in (view, depth) order, so
+  // each (view, tile) run comes out contiguous and depth-ordered
   CK(sort32_pairs(b->tile_keys.as<uint32_t>(), b->tile_keys_alt.as<uint32_t>(), b->tile_vals.as<uint32_t>(),
-                  b->tile_vals.as<uint32_t>(), b->tile_vals_alt.as<uint32_t>(), E, &ctr->entries, bits_for(T - 1),
-                  hist + 768, b->status.as<uint32_t>(), b->tile_ctr.as<uint32_t>(), max_tiles_sort, ctr, s,
+                  b->tile_vals.as<uint32_t>(), b->tile_vals_alt.as<uint32_t>(), E, &ctr->entries, 16, hist + 768,
+                  b->status.as<uint32_t>(), b->tile_ctr.as<uint32_t>(), max_tiles_sort, ctr, s,
                   b->tile_keys.as<uint32_t>()));
-  CK(launch_btile_runs(b->tile_keys.as<uint32_t>(), &ctr->entries, E, b->run_start.as<uint32_t>(),
-                       b->run_end.as<uint32_t>(), s));
-  CK(launch_tile_run_counts(b->run_start.as<uint32_t>(), b->run_end.as<uint32_t>(), T, b->tile_counts.as<uint32_t>(), s));
-  CK(exclusive_scan_u32(b->tile_counts.as<uint32_t>(), b->tile_starts.as<uint32_t>(), T, nullptr, b->scan_scratch.ptr,
-                        ctr, s));
-  CK(launch_tile_ranges(b->tile_starts.as<uint32_t>(), b->tile_counts.as<uint32_t>(), T, b->ranges.as<uint2>(), s));
+  CK(launch_btile_runs(b->tile_keys.as<uint32_t>(), &ctr->entries, E, b->views_out.as<BatchViewOut>(),
+                       b->ranges.as<uint2>(), s));
   // deferred shading: the coverage pass marks the splats of lit views that blend a fragment, the shading list is
   // their Gaussians in shading order, and only those are shaded before the composite
   const BatchComposite C{b->tile_w, b->tile_h, b->t_stop_scale, 0};
@@ -336,6 +331,8 @@ int batch_layout(sl_batch* b, const uint32_t* scene_of_view, const sl_render_fra
     const uint32_t W = (uint32_t)frames[v].viewport[0], H = (uint32_t)frames[v].viewport[1];
     const uint32_t n = r->count + 1u + (uint32_t)frames[v].palette[3][1];
     const uint32_t tx = (W + b->tile_w - 1) / b->tile_w, ty = (H + b->tile_h - 1) / b->tile_h;
+    if ((uint64_t)tx * ty > 65536u)  // tile keys hold the view-local tile id in 16 bits
+      return fail(SL_ERR_INVALID_ARG, "view " + std::to_string(v) + ": more than 65536 tiles");
     b->slot_base[v] = (uint32_t)slot;
     b->n_slots[v] = n;
     b->tile_base[v] = (uint32_t)tile;
@@ -412,6 +409,11 @@ int batch_finish(sl_batch* b, uint32_t n_views, uint64_t slots, uint64_t tiles, 
     for (uint32_t v = 0; v < n_views; v++) vis += b->h_visible[v];
     stats->visible = vis;
     stats->graph_replayed = replayed ? 1u : 0u;
+    stats->shaded = hc.shade_n;
+    for (uint32_t v = 0; v < n_views; v++) {
+      stats->reshaded_views += b->shade_blended[v];
+      stats->max_radiance = std::max(stats->max_radiance, __builtin_bit_cast(float, b->h_maxrad[v]));
+    }
     if (b->timing) cudaEventElapsedTime(&stats->ms_total, b->ev[0], b->ev[1]);
   }
   if (hc.timeout) return fail(SL_ERR_TIMEOUT, "a bounded device-side wait gave up");
@@ -482,7 +484,7 @@ int sl_batch_destroy(sl_batch* b) {
   sl::DevBuf* all[] = {&b->views, &b->views_out, &b->block_view, &b->scenes_dev, &b->dyn, &b->keys32, &b->keys_alt,
                        &b->vals_alt, &b->order, &b->recs, &b->rects, &b->slot_counts, &b->slot_offsets,
                        &b->tile_keys, &b->tile_keys_alt, &b->tile_vals, &b->tile_vals_alt, &b->status, &b->tile_ctr,
-                       &b->hist, &b->scan_scratch, &b->run_start, &b->run_end, &b->tile_counts, &b->tile_starts,
+                       &b->hist, &b->scan_scratch,
                        &b->ranges, &b->counters, &b->view_maxrad, &b->view_visible, &b->marks,
                        &b->view_tmark};
   for (sl::DevBuf* x : all) x->release();
@@ -586,24 +588,39 @@ int sl_batch_read_view(sl_batch* b, uint32_t view, uint32_t* order, uint32_t* ra
   std::vector<uint2> rg(nt);
   cudaError_t e = cudaMemcpy(rg.data(), b->ranges.as<uint2>() + tb, 8ull * nt, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "ranges");
-  // the view's entries are contiguous: tile starts are one exclusive scan over every view's tiles
-  const uint32_t e0 = nt ? rg[0].x : 0u, e1 = nt ? rg[nt - 1].y : 0u;
+  // each tile's run is contiguous, the view's runs are spread over the batch's entries ((local tile, view) order):
+  // gathered here in tile order, the ranges rebased to that list
+  uint64_t total = 0;
+  uint32_t lo = UINT32_MAX, hi = 0;
+  for (uint32_t t = 0; t < nt; t++) {
+    total += rg[t].y - rg[t].x;
+    if (rg[t].y > rg[t].x) {
+      lo = std::min(lo, rg[t].x);
+      hi = std::max(hi, rg[t].y);
+    }
+  }
   if (order) {
     e = cudaMemcpy(order, b->order.as<uint32_t>() + sb, 4ull * n, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "order");
     for (uint32_t i = 0; i < n; i++) order[i] -= sb;
   }
-  if (ranges)
+  if (ranges) {
+    uint32_t at = 0;
     for (uint32_t t = 0; t < nt; t++) {
-      ranges[2 * t] = rg[t].x - e0;
-      ranges[2 * t + 1] = rg[t].y - e0;
+      ranges[2 * t] = at;
+      at += rg[t].y - rg[t].x;
+      ranges[2 * t + 1] = at;
     }
-  if (n_entries) *n_entries = e1 - e0;
-  if (entries) {
-    if (entries_cap < e1 - e0) return fail(SL_ERR_INVALID_ARG, "entries buffer too small");
-    e = cudaMemcpy(entries, b->tile_vals.as<uint32_t>() + e0, 4ull * (e1 - e0), cudaMemcpyDeviceToHost);
+  }
+  if (n_entries) *n_entries = total;
+  if (entries && total) {
+    if (entries_cap < total) return fail(SL_ERR_INVALID_ARG, "entries buffer too small");
+    std::vector<uint32_t> span(hi - lo);
+    e = cudaMemcpy(span.data(), b->tile_vals.as<uint32_t>() + lo, 4ull * (hi - lo), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "entries");
-    for (uint64_t i = 0; i < e1 - e0; i++) entries[i] -= sb;
+    uint64_t at = 0;
+    for (uint32_t t = 0; t < nt; t++)
+      for (uint32_t i = rg[t].x; i < rg[t].y; i++) entries[at++] = span[i - lo] - sb;
   }
   return SL_OK;
 }

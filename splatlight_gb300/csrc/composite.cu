@@ -65,8 +65,10 @@ __device__ __forceinline__ float ex2_approx(float x) {
 }
 
 // One tile: (x0, y0) its origin in a width x height image, [s, e) its range in tile_vals, out/counts the image.
-// kMark: the coverage pass of the batched path -- the same walk and alphas, no colour: marks[slot] = 1 for every splat
-// that blends a fragment before the pixel's transmittance falls below t_stop, and no image is written.
+// kMark: the coverage pass of the batched path -- the same walk, no colour, the transmittance kept as log2 T (one ex2
+// per fragment; it follows the composite's T to within rounding, and the composite's own threshold is at least twice
+// this one): marks[slot] = 1 for every splat that blends a fragment before the pixel's transmittance falls below
+// t_stop (never, for t_stop <= 0), and no image is written.
 template <int TW, bool kMark = false>
 __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_t width, uint32_t height, uint32_t s,
                                                uint32_t e, const uint32_t* __restrict__ tile_vals,
@@ -79,6 +81,7 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
   static_assert(BX * BY == kThreads / 32, "one 8x4 block per warp");
   __shared__ SplatRec buf[2][kThreads];
   __shared__ uint32_t sslot[kMark ? 2 : 1][kMark ? kThreads : 1];  // coverage pass: the slots of the batch
+  __shared__ uint8_t smark[kMark ? 2 : 1][kMark ? kThreads : 1];    // coverage pass: the batch's blended records
   __shared__ uint32_t masks[kThreads / 32][kThreads / 32];  // [warp block][loader warp]: records touching the block
   __shared__ __align__(8) uint64_t bars[2];
 
@@ -88,6 +91,7 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
   const bool inside = px < width && py < height;
 
   const uint32_t bar0 = smem_addr(&bars[0]), bar1 = smem_addr(&bars[1]);
+  if constexpr (kMark) smark[0][t] = smark[1][t] = 0;
   if (t == 0) {
     mbar_init(bar0, kThreads);
     mbar_init(bar1, kThreads);
@@ -103,6 +107,10 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
 
   float T = 1.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f;
   uint32_t kept = 0;
+  // coverage pass: log2 T, which falls by tau0 exp(-q/2) log2(e) per blended fragment (the composite's factor
+  // 1 - alpha = exp(-tau0 exp(-q/2))), against log2 of the threshold (never reached for t_stop <= 0)
+  float l2T = 0.0f;
+  const float l2stop = kMark && t_stop > 0.0f ? __log2f(t_stop) : -INFINITY;
   bool alive = inside;
   bool timed_out = false;
 
@@ -170,14 +178,11 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
           const float ly = fmaf(dx, B.x, dy * B.y);
           const float q = fmaf(lx, lx, ly * ly);
           if constexpr (kMark) {
-            const bool hit = alive && q <= B.w;
-            if (hit) {
-              const float ev = ex2_approx(q * kNegHalfLog2e);
-              const float alpha = 1.0f - ex2_approx(rb[j].c.w * kNegLog2e * ev);
-              T = T - T * alpha;
-              if (T < t_stop) alive = false;
+            if (alive && q <= B.w) {
+              l2T = fmaf(rb[j].c.w * kNegLog2e, ex2_approx(q * kNegHalfLog2e), l2T);
+              smark[b & 1u][j] = 1u;
+              if (l2T < l2stop) alive = false;
             }
-            if (__any_sync(0xffffffffu, hit) && lane == 0) marks[sslot[b & 1u][j]] = 1u;  // one store per warp
           } else if (alive && q <= B.w) {
             const float4 C = rb[j].c;
             const float ev = ex2_approx(q * kNegHalfLog2e);
@@ -194,7 +199,14 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
         if (!__any_sync(0xffffffffu, alive)) break;
       }
     }
-    if (__syncthreads_count(alive) == 0) {
+    const bool any_alive = __syncthreads_count(alive) != 0;
+    if constexpr (kMark) {  // one store per blended record of the batch
+      if (smark[b & 1u][t]) {
+        marks[sslot[b & 1u][t]] = 1u;
+        smark[b & 1u][t] = 0;
+      }
+    }
+    if (!any_alive) {
       // every pixel is done: drain the batch already in flight before leaving
       if (b + 1 < n_batches) {
         if (!mbar_wait((b & 1u) ? bar0 : bar1, ((b + 1) >> 1) & 1u)) timed_out = true;

@@ -54,7 +54,7 @@ struct FrameCounters {
   uint32_t overflow;       // entries beyond capacity
   uint32_t timeout;        // a bounded device wait gave up
   uint32_t fragments;      // fragments composited (kept and blended) by the compositor
-  uint32_t shade_n;        // batched path: visible Gaussians of lit views (the shading list's length)
+  uint32_t shade_n;        // batched path: marked Gaussians of lit views (the shading list's length)
   uint32_t pad;
 };
 
@@ -198,7 +198,9 @@ cudaError_t launch_bshade_flags(const BatchView* views, const BatchScene* scenes
 cudaError_t launch_bshade_compact(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
                                   const uint32_t* flags, const uint32_t* offsets, const uint32_t* totals,
                                   uint32_t n_max, uint32_t* list, cudaStream_t s);
-cudaError_t launch_btile_runs(const uint32_t* keys, const uint32_t* n_dev, uint32_t n_max, uint32_t* run_start,
-                              uint32_t* run_end, cudaStream_t s);
+// Tile keys are (view << 16) | view-local tile id; after the stable sort on the local id each (view, tile) run's
+// bounds are written to ranges[tile_base[view] + local] (ranges zeroed first).
+cudaError_t launch_btile_runs(const uint32_t* keys, const uint32_t* n_dev, uint32_t n_max, const BatchViewOut* views,
+                              uint2* ranges, cudaStream_t s);
 
 }  // namespace sl

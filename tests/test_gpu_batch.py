@@ -199,6 +199,30 @@ def test_light_scale_matches_plain(cuda):
         Lb.close()
 
 
+def test_coverage_pass_and_bright_views(cuda):
+    """Deferred shading: the batch shades only the Gaussians its coverage pass marks (fewer than the visible ones); a
+    view whose shaded radiance passes the coverage pass's bound runs again with every blended splat shaded, and each
+    view's image is the same alone as in the mix (bit for bit) -- the decision depends on the view alone."""
+    _, b = _scenes()
+    b = scene.dataclasses.replace(b, shadow_res=256, sun_res=512)
+    with SplatRenderer(b.gaussians, b.parts) as rb:
+        Lb = for_scene(rb, b)
+        Lb.update(b.eye, camera_forward(b))
+        normal = View(0, _frame(b, 320, 180, VIEW_LIT), b.eye, light_scale=1.0)
+        bright = View(0, _frame(b, 256, 144, VIEW_LIT), b.eye, light_scale=500.0)
+        with BatchRenderer([rb], [Lb]) as B:
+            alone_n = B.render([normal])[0].copy()
+            st = B.last_stats
+            assert 0 < st.shaded < st.visible and st.reshaded_views == 0
+            alone_b = B.render([bright])[0].copy()
+            assert B.last_stats.reshaded_views == 1
+            mix = [im.copy() for im in B.render([bright, normal])]
+            assert B.last_stats.reshaded_views == 1
+            assert np.array_equal(mix[0], alone_b) and np.array_equal(mix[1], alone_n)
+            assert float(alone_b[..., :3].max()) > 32.0
+        Lb.close()
+
+
 def test_autotune_keeps_results(cuda):
     a, b = _scenes()
     with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
