@@ -26,36 +26,59 @@
 #define SL_SPAN_FN static inline
 #endif
 
-/* Tile columns [*tx0, *tx1] of tile row ty (tiles tw x th pixels) that the splat (centre cx, cy; gradients g0, g1;
- * cutoff qcut) can reach, within the candidate rectangle's columns [rx0, rx1].  Returns 0 when the row holds none. */
-SL_SPAN_FN int sl_row_tiles(float cx, float cy, float g0x, float g0y, float g1x, float g1y, float qcut, uint32_t rx0,
-                            uint32_t rx1, uint32_t ty, uint32_t tw, uint32_t th, uint32_t* tx0, uint32_t* tx1) {
+/* The per-splat part of the row spans (the same for every tile row of the splat). */
+typedef struct sl_span_prep {
+  float cx, cy, a, b, D, Q, half_w, ylim, ys, m;
+  int full; /* nearly degenerate conic: every row keeps the candidate rectangle's columns */
+} sl_span_prep;
+
+SL_SPAN_FN void sl_span_init(float cx, float cy, float g0x, float g0y, float g1x, float g1y, float qcut,
+                             sl_span_prep* p) {
   const float a = g0x * g0x + g1x * g1x;
   const float b = g0x * g0y + g1x * g1y;
   const float c = g0y * g0y + g1y * g1y;
   const float ac = a * c;
   const float D = ac - b * b;
-  *tx0 = rx0;
-  *tx1 = rx1;
-  if (!(a > 0.0f) || !(c > 0.0f) || !(D > 1e-4f * ac)) return 1;
+  p->cx = cx;
+  p->cy = cy;
+  p->a = a;
+  p->b = b;
+  p->D = D;
+  p->full = (!(a > 0.0f) || !(c > 0.0f) || !(D > 1e-4f * ac)) ? 1 : 0;
+  if (p->full) {
+    p->Q = p->half_w = p->ylim = p->ys = p->m = 0.0f;
+    return;
+  }
   const float Q = qcut * 1.0001f;
   const float half_w = sqrtf(Q * c / D);   /* the ellipse's half width (x) */
   const float half_h = sqrtf(Q * a / D);   /* and half height (y) */
-  const float d0 = ((float)(ty * th) + 0.5f) - cy;
-  const float d1 = ((float)(ty * th + th) - 0.5f) - cy;
-  const float ylim = half_h * 1.001f + 1.0f;
-  if (d0 > ylim || d1 < -ylim) return 0;   /* the band lies beyond the ellipse's top or bottom */
-  const float ys = b * sqrtf(Q / (c * D)); /* the rightmost point sits at dy = -ys, the leftmost at +ys */
-  float yr = -ys, yl = ys;
+  p->Q = Q;
+  p->half_w = half_w;
+  p->ylim = half_h * 1.001f + 1.0f;
+  p->ys = b * sqrtf(Q / (c * D));          /* the rightmost point sits at dy = -ys, the leftmost at +ys */
+  p->m = 1.0f + 1e-3f * half_w;
+}
+
+/* Tile columns [*tx0, *tx1] of tile row ty (tiles tw x th pixels, tw a power of two: tile_shift = log2 tw) that the
+ * prepared splat can reach, within the candidate rectangle's columns [rx0, rx1].  Returns 0 when the row holds
+ * none. */
+SL_SPAN_FN int sl_span_row(const sl_span_prep* p, uint32_t rx0, uint32_t rx1, uint32_t ty, uint32_t tw,
+                           uint32_t tile_shift, uint32_t th, uint32_t* tx0, uint32_t* tx1) {
+  *tx0 = rx0;
+  *tx1 = rx1;
+  if (p->full) return 1;
+  const float d0 = ((float)(ty * th) + 0.5f) - p->cy;
+  const float d1 = ((float)(ty * th + th) - 0.5f) - p->cy;
+  if (d0 > p->ylim || d1 < -p->ylim) return 0;   /* the band lies beyond the ellipse's top or bottom */
+  float yr = -p->ys, yl = p->ys;
   yr = yr < d0 ? d0 : (yr > d1 ? d1 : yr);
   yl = yl < d0 ? d0 : (yl > d1 ? d1 : yl);
-  float ar = a * Q - D * (yr * yr);
-  float al = a * Q - D * (yl * yl);
+  float ar = p->a * p->Q - p->D * (yr * yr);
+  float al = p->a * p->Q - p->D * (yl * yl);
   ar = ar > 0.0f ? ar : 0.0f;
   al = al > 0.0f ? al : 0.0f;
-  const float m = 1.0f + 1e-3f * half_w;
-  const float xh = cx + (sqrtf(ar) - b * yr) / a + m;
-  const float xl = cx + (-sqrtf(al) - b * yl) / a - m;
+  const float xh = p->cx + (sqrtf(ar) - p->b * yr) / p->a + p->m;
+  const float xl = p->cx + (-sqrtf(al) - p->b * yl) / p->a - p->m;
   /* pixel columns whose centre ix + 0.5 lies in [xl, xh], then their tiles */
   const float fl = ceilf(xl - 0.5f), fh = floorf(xh - 0.5f);
   if (fh < fl) return 0;
@@ -63,9 +86,25 @@ SL_SPAN_FN int sl_row_tiles(float cx, float cy, float g0x, float g0y, float g1x,
   if (fh < lo_t || fl > hi_t) return 0;
   const uint32_t il = fl > lo_t ? (uint32_t)fl : rx0 * tw;
   const uint32_t ih = fh < hi_t ? (uint32_t)fh : (rx1 + 1u) * tw - 1u;
-  *tx0 = il / tw;
-  *tx1 = ih / tw;
+  *tx0 = il >> tile_shift;
+  *tx1 = ih >> tile_shift;
   return 1;
+}
+
+SL_SPAN_FN uint32_t sl_tile_shift(uint32_t tw) {
+  uint32_t s = 0;
+  while ((1u << s) < tw) s++;
+  return s;
+}
+
+/* Tile columns [*tx0, *tx1] of tile row ty (tiles tw x th pixels, tw a power of two) that the splat (centre cx, cy;
+ * gradients g0, g1; cutoff qcut) can reach, within the candidate rectangle's columns [rx0, rx1].  Returns 0 when the
+ * row holds none. */
+SL_SPAN_FN int sl_row_tiles(float cx, float cy, float g0x, float g0y, float g1x, float g1y, float qcut, uint32_t rx0,
+                            uint32_t rx1, uint32_t ty, uint32_t tw, uint32_t th, uint32_t* tx0, uint32_t* tx1) {
+  sl_span_prep p;
+  sl_span_init(cx, cy, g0x, g0y, g1x, g1y, qcut, &p);
+  return sl_span_row(&p, rx0, rx1, ty, tw, sl_tile_shift(tw), th, tx0, tx1);
 }
 
 #endif /* SL_TILESPAN_H */

@@ -27,26 +27,13 @@ __global__ void __launch_bounds__(kThreads) btile_count_kernel(const uint32_t* _
   if (mine) {
     const uint32_t slot = order[p];
     r = rects[slot];
-    rec = recs[slot];
+    if (r.x <= r.z && r.y <= r.w) rec = recs[slot];  // culled slots (empty rectangle) need no record
   }
   const uint32_t c = count_warp(mine, r, rec, tw, th);
   if (p < n_max) counts[p] = c;
 }
 
-// digit histograms of 32-bit tile ids: low byte per id, the two upper bytes per run of ids within one 256-block
-// Digit counts of the low 16 bits (the view-local tile id) for the two passes of the tile sort.
-struct HistLocal16 {
-  uint32_t (*h)[256];
-  __device__ __forceinline__ void add(uint32_t first, uint32_t n) {
-    for (uint32_t k = 0; k < n; k++) atomicAdd(&h[0][(first + k) & 0xffu], 1u);
-    for (uint32_t a = first, end = first + n; a < end;) {
-      const uint32_t stop = min(end, (a | 0xffu) + 1u);
-      atomicAdd(&h[1][(a >> 8) & 0xffu], stop - a);
-      a = stop;
-    }
-  }
-};
-
+// Entries of the batch: key (view << 16) | view-local tile id, value the slot; digit counts of the local id.
 __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __restrict__ order,
                                                               const ushort4* __restrict__ rects,
                                                               const SplatRec* __restrict__ recs,
@@ -59,10 +46,10 @@ __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __
                                                               FrameCounters* ctr, uint32_t* __restrict__ tile_keys,
                                                               uint32_t* __restrict__ tile_vals,
                                                               uint32_t* __restrict__ digit_hist) {
-  __shared__ uint32_t h[2][256];
+  __shared__ uint32_t h_lo[256], h_hi[256], warp_tot[kThreads / 32];
   const int t = threadIdx.x;
-  h[0][t] = 0u;
-  h[1][t] = 0u;
+  RunHist16 hh{h_lo, h_hi};  // the digits of the 16-bit view-local tile id
+  hh.clear();
   __syncthreads();
   const uint32_t p = blockIdx.x * kThreads + t;
   bool mine = false;
@@ -83,11 +70,9 @@ __global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __
       else mine = true;
     }
   }
-  HistLocal16 hh{h};
   emit_warp<uint32_t>(mine, slot, r, rec, e0, cnt, tw, th, base, stride, tile_keys, tile_vals, hh);
   __syncthreads();
-  for (int q = 0; q < 2; q++)
-    if (h[q][t]) atomicAdd(&digit_hist[256 * q + t], h[q][t]);
+  hh.flush(digit_hist, warp_tot);
 }
 
 // shading-list flags: position g of the padded slots <-> the view's Gaussian order[g - slot_base] (shading order);

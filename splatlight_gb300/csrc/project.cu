@@ -48,6 +48,25 @@ __device__ __forceinline__ float clampf(float x, float lo, float hi) { return fm
 
 constexpr int kThreads = 256;
 
+// A block's tallies of its slots' keys (in: the thread holds a slot): valid keys into the two depth-digit histograms
+// (spread: shared atomics rarely collide), invalid keys (all digits 0xFF) and the visible count and radiance maximum
+// one warp-aggregated add each, instead of 256 threads' atomics on one word.
+__device__ __forceinline__ void block_tally(bool in, uint32_t key, float maxrad, uint32_t* h_lo, uint32_t* h_hi,
+                                            uint32_t* s_visible, uint32_t* s_invalid, uint32_t* s_maxrad) {
+  const bool vis = in && key != kInvalidKey16;
+  if (vis) {
+    atomicAdd(&h_lo[key & 0xffu], 1u);
+    atomicAdd(&h_hi[key >> 8], 1u);
+  }
+  const uint32_t vmask = __ballot_sync(0xffffffffu, vis), imask = __ballot_sync(0xffffffffu, in && !vis);
+  const uint32_t wmax = __reduce_max_sync(0xffffffffu, vis ? __float_as_uint(maxrad) : 0u);
+  if ((threadIdx.x & 31u) == 0u) {
+    if (vmask) atomicAdd(s_visible, (uint32_t)__popc(vmask));
+    if (imask) atomicAdd(s_invalid, (uint32_t)__popc(imask));
+    if (wmax) atomicMax(s_maxrad, wmax);
+  }
+}
+
 // One slot i of project.wgsl main (:84-370, plain path): key (kInvalidKey16 when culled), tile rectangle and the
 // largest radiance component; the splat record goes to *rec_out.  colour / lo_b may be null (radiance 0, filled in
 // later by the batched shading pass).
@@ -309,13 +328,13 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
                                                            SplatRec* __restrict__ recs, ushort4* __restrict__ rects,
                                                            uint32_t* __restrict__ digit_hist, FrameCounters* ctr) {
   __shared__ uint32_t h_lo[256], h_hi[256];
-  __shared__ uint32_t s_visible;
-  __shared__ uint32_t s_maxrad;
+  __shared__ uint32_t s_visible, s_invalid, s_maxrad;
   const int t = threadIdx.x;
   h_lo[t] = 0u;
   h_hi[t] = 0u;
   if (t == 0) {
     s_visible = 0u;
+    s_invalid = 0u;
     s_maxrad = 0u;
   }
   __syncthreads();
@@ -325,19 +344,16 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
   ushort4 rect;
   float maxrad;
   project_slot(P, i, gaussians, emitters, colour, lo_b, recs + i, key, rect, maxrad);
-  if (i < P.n_slots) {
+  const bool in = i < P.n_slots;
+  if (in) {
     key16[i] = (uint16_t)key;
     rects[i] = rect;
-    atomicAdd(&h_lo[key & 0xffu], 1u);
-    atomicAdd(&h_hi[key >> 8], 1u);
-    if (key != kInvalidKey16) {
-      atomicAdd(&s_visible, 1u);
-      atomicMax(&s_maxrad, __float_as_uint(maxrad));
-    }
   }
+  block_tally(in, key, maxrad, h_lo, h_hi, &s_visible, &s_invalid, &s_maxrad);
   __syncthreads();
-  if (h_lo[t]) atomicAdd(&digit_hist[t], h_lo[t]);
-  if (h_hi[t]) atomicAdd(&digit_hist[256 + t], h_hi[t]);
+  const uint32_t lo = h_lo[t] + (t == 255 ? s_invalid : 0u), hi = h_hi[t] + (t == 255 ? s_invalid : 0u);
+  if (lo) atomicAdd(&digit_hist[t], lo);
+  if (hi) atomicAdd(&digit_hist[256 + t], hi);
   if (t == 0) {
     if (s_visible) atomicAdd(&ctr->visible, s_visible);
     if (s_maxrad) atomicMax(&ctr->max_rad_bits, s_maxrad);
@@ -354,8 +370,8 @@ __global__ void __launch_bounds__(kThreads) bproject_kernel(const BatchView* __r
                                                             uint32_t* __restrict__ view_maxrad,
                                                             uint32_t* __restrict__ view_visible) {
   __shared__ ProjectParams sP;
-  __shared__ uint32_t h[3][256];
-  __shared__ uint32_t s_visible, s_maxrad;
+  __shared__ uint32_t h[2][256];
+  __shared__ uint32_t s_visible, s_invalid, s_maxrad;
   const uint32_t v = block_view[blockIdx.x];
   if (v == kNoView) return;
   const int t = threadIdx.x;
@@ -367,9 +383,9 @@ __global__ void __launch_bounds__(kThreads) bproject_kernel(const BatchView* __r
   }
   h[0][t] = 0u;
   h[1][t] = 0u;
-  h[2][t] = 0u;
   if (t == 0) {
     s_visible = 0u;
+    s_invalid = 0u;
     s_maxrad = 0u;
   }
   __syncthreads();
@@ -382,16 +398,12 @@ __global__ void __launch_bounds__(kThreads) bproject_kernel(const BatchView* __r
   const uint32_t key32 = (v << 16) | key;
   keys32[gslot] = key32;
   rects[gslot] = rect;
-  atomicAdd(&h[0][key32 & 0xffu], 1u);
-  atomicAdd(&h[1][(key32 >> 8) & 0xffu], 1u);
-  atomicAdd(&h[2][(key32 >> 16) & 0xffu], 1u);
-  if (key != kInvalidKey16) {
-    atomicAdd(&s_visible, 1u);
-    atomicMax(&s_maxrad, __float_as_uint(maxrad));
-  }
+  block_tally(true, key, maxrad, h[0], h[1], &s_visible, &s_invalid, &s_maxrad);
   __syncthreads();
-  for (int p = 0; p < 3; p++)
-    if (h[p][t]) atomicAdd(&digit_hist[256 * p + t], h[p][t]);
+  const uint32_t lo = h[0][t] + (t == 255 ? s_invalid : 0u), hi = h[1][t] + (t == 255 ? s_invalid : 0u);
+  if (lo) atomicAdd(&digit_hist[t], lo);
+  if (hi) atomicAdd(&digit_hist[256 + t], hi);
+  if (t == 0) atomicAdd(&digit_hist[512 + v], (uint32_t)kThreads);  // the view byte: every slot of the block
   if (t == 0) {
     if (s_visible) atomicAdd(&view_visible[v], s_visible);
     if (s_maxrad) atomicMax(&view_maxrad[v], s_maxrad);

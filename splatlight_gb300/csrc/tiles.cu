@@ -32,20 +32,6 @@ __global__ void __launch_bounds__(kThreads) tile_count_kernel(const uint32_t* __
   if (p < n) counts[p] = c;
 }
 
-// digit histograms of 16-bit tile ids (low byte per id, high byte per run of ids within one 256-block)
-struct Hist16 {
-  uint32_t* lo;
-  uint32_t* hi;
-  __device__ __forceinline__ void add(uint32_t first, uint32_t n) {
-    for (uint32_t k = 0; k < n; k++) atomicAdd(&lo[(first + k) & 0xffu], 1u);
-    for (uint32_t a = first, end = first + n; a < end;) {
-      const uint32_t stop = min(end, (a | 0xffu) + 1u);
-      atomicAdd(&hi[(a >> 8) & 0xffu], stop - a);
-      a = stop;
-    }
-  }
-};
-
 __global__ void __launch_bounds__(kThreads) tile_emit_kernel(const uint32_t* __restrict__ order,
                                                              const ushort4* __restrict__ rects,
                                                              const SplatRec* __restrict__ recs,
@@ -56,13 +42,13 @@ __global__ void __launch_bounds__(kThreads) tile_emit_kernel(const uint32_t* __r
                                                              uint16_t* __restrict__ tile_keys,
                                                              uint32_t* __restrict__ tile_vals,
                                                              uint32_t* __restrict__ digit_hist) {
-  __shared__ uint32_t h_lo[256], h_hi[256];
+  __shared__ uint32_t h_lo[256], h_hi[256], warp_tot[kThreads / 32];
   const int t = threadIdx.x;
-  h_lo[t] = 0u;
-  h_hi[t] = 0u;
-  __syncthreads();
+  RunHist16 h{h_lo, h_hi};
+  h.clear();
   const uint32_t p = blockIdx.x * kThreads + t;
   const uint32_t visible = ctr->visible;
+  __syncthreads();
   bool mine = false;
   uint32_t slot = 0, e0 = 0, cnt = 0;
   ushort4 r = make_ushort4(1, 1, 0, 0);
@@ -78,11 +64,9 @@ __global__ void __launch_bounds__(kThreads) tile_emit_kernel(const uint32_t* __r
       else mine = true;
     }
   }
-  Hist16 h{h_lo, h_hi};
   emit_warp<uint16_t>(mine, slot, r, rec, e0, cnt, tw, th, 0u, tiles_x, tile_keys, tile_vals, h);
   __syncthreads();
-  if (h_lo[t]) atomicAdd(&digit_hist[t], h_lo[t]);
-  if (h_hi[t]) atomicAdd(&digit_hist[256 + t], h_hi[t]);
+  h.flush(digit_hist, warp_tot);
 }
 
 // runs of equal ids in the sorted tile keys: start and end of each tile's run
