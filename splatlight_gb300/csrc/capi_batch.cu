@@ -320,7 +320,7 @@ int batch_layout(sl_batch* b, const uint32_t* scene_of_view, const sl_render_fra
   b->n_slots.assign(n_views, 0);
   b->tiles.assign(n_views, 0);
   b->offsets.assign(n_views, 0);
-  b->shade_blended.assign(n_views, 0);
+  if (b->shade_blended.size() != n_views) b->shade_blended.assign(n_views, 0);
   uint64_t slot = 0, tile = 0, pix = 0;
   for (uint32_t v = 0; v < n_views; v++) {
     const uint32_t k = scene_of_view[v];
@@ -350,6 +350,8 @@ int batch_layout(sl_batch* b, const uint32_t* scene_of_view, const sl_render_fra
 }
 
 int batch_fit(sl_batch* b, uint64_t slots, uint64_t tiles) { return fit_capacity(b, slots, tiles); }
+
+void batch_begin(sl_batch* b, uint32_t n_views) { b->shade_blended.assign(n_views, 0); }
 
 int batch_launch(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames, const float* eyes,
                  const float* light_scales, uint32_t n_views, float* out_dev, uint64_t slots, uint64_t tiles,
@@ -523,6 +525,7 @@ int sl_batch_render(sl_batch* b, const uint32_t* scene_of_view, const sl_render_
   if (4 * pix > out_floats) return fail(SL_ERR_INVALID_ARG, "output buffer too small for the batch's images");
   rc = batch_fit(b, slot, tile);
   if (rc) return rc;
+  batch_begin(b, n_views);
   for (int attempt = 0; attempt < 3; attempt++) {
     bool replayed = false, retry = false;
     rc = batch_launch(b, scene_of_view, frames, eyes, light_scales, n_views, out_dev, slot, tile, s, &replayed);

@@ -225,6 +225,7 @@ void worker_loop(sl_server* S) {
       }
       if (p.reqs.empty()) continue;
       p.attempts = 0;
+      batch_begin(p.b, (uint32_t)p.reqs.size());
       int rc = launch(S, p);
       if (rc) fail_batch(S, p, rc);
       progressed = true;

@@ -53,6 +53,8 @@ int batch_layout(sl_batch* b, const uint32_t* scene_of_view, const sl_render_fra
                  uint64_t* slots, uint64_t* tiles, uint64_t* pixels);
 // Grows the capacities to hold the layout (buffers reallocated, graphs dropped).
 int batch_fit(sl_batch* b, uint64_t slots, uint64_t tiles);
+// Starts a new batch of n_views (per-view state that its re-launches keep: the coverage mode of each view).
+void batch_begin(sl_batch* b, uint32_t n_views);
 // Stages the batch and launches its chain on s (asynchronous).  light_scales may be null (1 for every view).
 int batch_launch(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames, const float* eyes,
                  const float* light_scales, uint32_t n_views, float* out_dev, uint64_t slots, uint64_t tiles,

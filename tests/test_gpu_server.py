@@ -100,6 +100,25 @@ def test_served_equals_per_view_path(world):
         assert err <= RGB_TOL, (k, err)
 
 
+def test_bright_request_reruns_and_completes(world):
+    """A request bright enough to pass the coverage pass's radiance bound is re-run with every blended splat shaded
+    (inside the same batch's retry): it completes, and every request equals its image rendered alone."""
+    scenes, rs, ls = world
+    b = scenes[1]
+    a = scenes[0]
+    reqs = [(1, _frame(b, 160, 120, VIEW_LIT, b.eye), b.eye, 500.0), (1, _frame(b, 96, 64, VIEW_LIT, b.eye), b.eye, 1.0),
+            (0, _frame(a, 64, 64, VIEW_LIT, a.eye), a.eye, 1.0)]
+    with RenderServer(rs, ls, max_views=8, pipelines=1, max_view_pixels=160 * 120) as srv:
+        for k, (si, f, eye, lsc) in enumerate(reqs):
+            srv.submit(si, f, eye, lsc, tag=k)
+        got = _drain(srv, len(reqs))
+        assert srv.stats()["failed"] == 0
+    with BatchRenderer(rs, ls, max_views=4) as B:
+        for k, (si, f, eye, lsc) in enumerate(reqs):
+            assert got[k].status == 0
+            assert np.array_equal(got[k].image, B.render([View(si, f, eye, lsc)])[0]), k
+
+
 def test_admission_and_bad_requests(world):
     scenes, rs, ls = world
     a = scenes[0]
