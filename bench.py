@@ -382,6 +382,7 @@ def run_serving(args, rates=(100, 500, 2000)):
     st = srv.stats()
     out["device_bytes"] = st["device_bytes"]
     out["batches"] = st["batches"]
+    out["reshaded_views"] = st["reshaded_views"]
     srv.close()
     # the plain per-view path on a sample of the same requests, one at a time (the shading pass at the request's eye
     # and the frame; the light scale, a change of light state for the per-view path, is left at 1 there)

@@ -64,7 +64,8 @@ class ServerResult(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("submitted", "completed", "rejected", "failed", "batches", "batch_views",
-                                         "graph_replays", "pending", "device_bytes", "free_result_slots")]
+                                         "graph_replays", "pending", "device_bytes", "free_result_slots",
+                                         "reshaded_views")]
 
 
 class DiffScene(C.Structure):

@@ -241,6 +241,8 @@ void stage(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* fr
     O.count_mode = frames[v].view_mode == 2u ? 1u : 0u;
     const sl_lighting* l = b->lights[scene_of_view[v]];
     O.lit = (frames[v].view_mode == 3u && l && l->iso_done) ? (b->shade_blended[v] ? 2u : 1u) : 0u;
+    O.rad_cap = kRadianceCap * std::max(1.0f, V.light_scale);
+    O.pad = 0;
     O.out_offset = b->offsets[v] / 4;
   }
   for (uint32_t v = n_views; v < b->max_views; v++) {  // unused view rows: past every tile

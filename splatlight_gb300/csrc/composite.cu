@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(kThreads) bmark_kernel(const BatchComposite B,
   }
   const BatchViewOut v = views[lo];
   if (v.lit == 0u) return;  // only lit views are shaded
-  const float t_mark = B.t_stop_scale / fmaxf(2.0f * __uint_as_float(view_maxrad[lo]), kRadianceCap);
+  const float t_mark = B.t_stop_scale / fmaxf(2.0f * __uint_as_float(view_maxrad[lo]), v.rad_cap);
   const uint32_t lt = tile - v.tile_base;
   if (lt == 0 && threadIdx.x == 0) view_tmark[lo] = t_mark;
   const uint32_t tx = lt % v.tiles_x, ty = lt / v.tiles_x;

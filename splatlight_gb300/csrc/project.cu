@@ -83,7 +83,7 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
   uint32_t material = kEmitterMaterial;
   float keep = 1.0f;
   V3 mu;
-  M3 rot;
+  uint32_t part = 0xFFFFFFFFu;  // the Gaussian's part (its rotation is composed only for slots past the depth test)
   V3 vel = v3(0.0f, 0.0f, 0.0f);  // motion blur: world-space displacement over the exposure (project.wgsl:138-146)
   if (live) {
     const float4* src = (i > P.count) ? emitters + 4u * (i - P.count - 1u) : gaussians + 4u * i;
@@ -93,9 +93,8 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
     g3 = __ldg(src + 3);
     if (i > P.count) {  // project.wgsl:226-230
       mu = v3(g0.x, g0.y, g0.z);
-      rot = quat_mat(g1.x, g1.y, g1.z, g1.w);
     } else {  // :232-251
-      uint32_t part = __float_as_uint(g2.w) & 0xffffu;
+      part = __float_as_uint(g2.w) & 0xffffu;
       part = part > kMaxParts - 1u ? kMaxParts - 1u : part;
       const PartXf& p = P.parts[part];
       keep = p.keep;
@@ -106,11 +105,6 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
         mu = v3(a[0] * g0.x + a[1] * g0.y + a[2] * g0.z + a[3] * 1.0f,
                 a[4] * g0.x + a[5] * g0.y + a[6] * g0.z + a[7] * 1.0f,
                 a[8] * g0.x + a[9] * g0.y + a[10] * g0.z + a[11] * 1.0f);
-        M3 R;
-        R.c[0] = v3(a[0], a[4], a[8]);
-        R.c[1] = v3(a[1], a[5], a[9]);
-        R.c[2] = v3(a[2], a[6], a[10]);
-        rot = mulm(R, quat_mat(g1.x, g1.y, g1.z, g1.w));
         material = p.material;
         if (P.shutter > 0.0f && (p.flags & 2u) != 0u) {
           const float* b = p.xf_prev;
@@ -132,6 +126,17 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
     float depth = -tv.z;
     live = !(depth < P.near_plane || depth > P.far_plane);
     if (live) {
+      M3 rot;
+      if (part == 0xFFFFFFFFu) {
+        rot = quat_mat(g1.x, g1.y, g1.z, g1.w);
+      } else {
+        const float* a = P.parts[part].xf;
+        M3 R;
+        R.c[0] = v3(a[0], a[4], a[8]);
+        R.c[1] = v3(a[1], a[5], a[9]);
+        R.c[2] = v3(a[2], a[6], a[10]);
+        rot = mulm(R, quat_mat(g1.x, g1.y, g1.z, g1.w));
+      }
       M3 W;
       W.c[0] = v3(V[0], V[1], V[2]);
       W.c[1] = v3(V[4], V[5], V[6]);

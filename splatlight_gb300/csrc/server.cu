@@ -69,6 +69,7 @@ struct sl_server {
   Clock::time_point epoch;
   // statistics
   uint64_t submitted = 0, completed = 0, rejected = 0, failed = 0, batches = 0, batch_views = 0, replays = 0;
+  uint64_t reshaded = 0;  // views re-run with every blended splat shaded (radiance above the coverage allowance)
   uint64_t device_bytes = 0;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - epoch).count(); }
@@ -196,6 +197,7 @@ void complete(sl_server* S, Pipe& p) {
   S->batches++;
   S->batch_views += p.reqs.size();
   if (p.replayed) S->replays++;
+  for (uint8_t f : p.b->shade_blended) S->reshaded += f;
   p.reqs.clear();
   p.busy = false;
   S->cv.notify_all();
@@ -419,6 +421,7 @@ int sl_server_get_stats(sl_server* S, sl_server_stats* st) {
   st->pending = S->pending.size();
   st->device_bytes = S->device_bytes;
   st->free_result_slots = S->free_slots.size();
+  st->reshaded_views = S->reshaded;
   return SL_OK;
 }
 

@@ -153,6 +153,8 @@ struct BatchViewOut {
   uint32_t lit;         // 0: not shaded; shaded (view mode 3 of a lit scene) where the coverage pass marks a splat,
                         // 1: blended before T < t_mark (launch_bmark), 2: blended anywhere (never stops)
   uint64_t out_offset;  // first float4 of the view's image in the packed output
+  float rad_cap;        // the coverage pass's radiance allowance: kRadianceCap x max(1, the view's light scale)
+  uint32_t pad;
 };
 struct BatchComposite {
   uint32_t tile_w, tile_h;
@@ -181,8 +183,9 @@ cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const
                               uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s);
 // The batched coverage pass over the tiles of lit views, run between binning and shading: marks[slot] = 1 for each
 // splat that blends a fragment before the pixel's transmittance falls below t_mark (BatchViewOut::lit 1) or at all
-// (lit 2).  t_mark = t_stop_scale / max(2 r, kRadianceCap), r the view's radiance bound so far (its unshaded splats,
-// view_maxrad), is written to view_tmark[view].  The composite, whose threshold is t_stop_scale / (the bound after
+// (lit 2).  t_mark = t_stop_scale / max(2 r, rad_cap), r the view's radiance bound so far (its unshaded splats,
+// view_maxrad), rad_cap = kRadianceCap x max(1, light scale) (shaded radiance scales with the light intensities), is
+// written to view_tmark[view].  The composite, whose threshold is t_stop_scale / (the bound after
 // shading), blends only marked splats as long as that threshold stays >= 2 t_mark.
 constexpr float kRadianceCap = 64.0f;
 cudaError_t launch_bmark(const BatchComposite& B, const uint2* ranges, const uint32_t* tile_vals, const SplatRec* recs,

@@ -201,16 +201,25 @@ def test_light_scale_matches_plain(cuda):
 
 def test_coverage_pass_and_bright_views(cuda):
     """Deferred shading: the batch shades only the Gaussians its coverage pass marks (fewer than the visible ones); a
-    view whose shaded radiance passes the coverage pass's bound runs again with every blended splat shaded, and each
-    view's image is the same alone as in the mix (bit for bit) -- the decision depends on the view alone."""
-    _, b = _scenes()
+    view whose shaded radiance passes the coverage pass's allowance (here: a scene whose lights are 500x brighter, at
+    request light scale 1; the allowance already grows with the request's own scale) runs again with every blended
+    splat shaded, and each view's image is the same alone as in the mix (bit for bit) -- the decision depends on the
+    view alone."""
+    a, b = _scenes()
     b = scene.dataclasses.replace(b, shadow_res=256, sun_res=512)
-    with SplatRenderer(b.gaussians, b.parts) as rb:
+    with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
+        La = for_scene(ra, a)
+        La.update(a.eye, camera_forward(a))
         Lb = for_scene(rb, b)
+        k = 500.0
+        Lb.set_emitters(b.emitters, scale=k)
+        sun = b.sun
+        Lb.set_environment([(sun.direction, sun.angular_std, tuple(np.float32(sun.irradiance) * np.float32(k)),
+                             sun.casts_shadows)], b.sky_ambient)
         Lb.update(b.eye, camera_forward(b))
-        normal = View(0, _frame(b, 320, 180, VIEW_LIT), b.eye, light_scale=1.0)
-        bright = View(0, _frame(b, 256, 144, VIEW_LIT), b.eye, light_scale=500.0)
-        with BatchRenderer([rb], [Lb]) as B:
+        normal = View(0, _frame(a, 200, 150, VIEW_LIT), a.eye)
+        bright = View(1, _frame(b, 256, 144, VIEW_LIT), b.eye)
+        with BatchRenderer([ra, rb], [La, Lb]) as B:
             alone_n = B.render([normal])[0].copy()
             st = B.last_stats
             assert 0 < st.shaded < st.visible and st.reshaded_views == 0
@@ -220,6 +229,7 @@ def test_coverage_pass_and_bright_views(cuda):
             assert B.last_stats.reshaded_views == 1
             assert np.array_equal(mix[0], alone_b) and np.array_equal(mix[1], alone_n)
             assert float(alone_b[..., :3].max()) > 32.0
+        La.close()
         Lb.close()
 
 

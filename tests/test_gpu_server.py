@@ -101,22 +101,34 @@ def test_served_equals_per_view_path(world):
 
 
 def test_bright_request_reruns_and_completes(world):
-    """A request bright enough to pass the coverage pass's radiance bound is re-run with every blended splat shaded
-    (inside the same batch's retry): it completes, and every request equals its image rendered alone."""
+    """A request of a scene bright enough to pass the coverage pass's radiance allowance is re-run with every blended
+    splat shaded (inside the same batch's retry): it completes, and every request equals its image rendered alone."""
     scenes, rs, ls = world
     b = scenes[1]
     a = scenes[0]
-    reqs = [(1, _frame(b, 160, 120, VIEW_LIT, b.eye), b.eye, 500.0), (1, _frame(b, 96, 64, VIEW_LIT, b.eye), b.eye, 1.0),
-            (0, _frame(a, 64, 64, VIEW_LIT, a.eye), a.eye, 1.0)]
-    with RenderServer(rs, ls, max_views=8, pipelines=1, max_view_pixels=160 * 120) as srv:
-        for k, (si, f, eye, lsc) in enumerate(reqs):
-            srv.submit(si, f, eye, lsc, tag=k)
-        got = _drain(srv, len(reqs))
-        assert srv.stats()["failed"] == 0
-    with BatchRenderer(rs, ls, max_views=4) as B:
-        for k, (si, f, eye, lsc) in enumerate(reqs):
-            assert got[k].status == 0
-            assert np.array_equal(got[k].image, B.render([View(si, f, eye, lsc)])[0]), k
+    with SplatRenderer(b.gaussians, b.parts) as rb:
+        Lb = for_scene(rb, b)
+        k = 500.0
+        Lb.set_emitters(b.emitters, scale=k)
+        sun = b.sun
+        Lb.set_environment([(sun.direction, sun.angular_std, tuple(np.float32(sun.irradiance) * np.float32(k)),
+                             sun.casts_shadows)], b.sky_ambient)
+        Lb.update(b.eye, camera_forward(b))
+        R, L = [rs[0], rb], [ls[0], Lb]
+        reqs = [(1, _frame(b, 160, 120, VIEW_LIT, b.eye), b.eye, 1.0),
+                (0, _frame(a, 96, 64, VIEW_LIT, a.eye), a.eye, 1.0),
+                (0, _frame(a, 64, 64, VIEW_FLAT, a.eye), a.eye, 1.0)]
+        with RenderServer(R, L, max_views=8, pipelines=1, max_view_pixels=160 * 120) as srv:
+            for t, (si, f, eye, lsc) in enumerate(reqs):
+                srv.submit(si, f, eye, lsc, tag=t)
+            got = _drain(srv, len(reqs))
+            st = srv.stats()
+            assert st["failed"] == 0 and st["reshaded_views"] >= 1
+        with BatchRenderer(R, L, max_views=4) as B:
+            for t, (si, f, eye, lsc) in enumerate(reqs):
+                assert got[t].status == 0
+                assert np.array_equal(got[t].image, B.render([View(si, f, eye, lsc)])[0]), t
+        Lb.close()
 
 
 def test_admission_and_bad_requests(world):
