@@ -45,10 +45,25 @@ void free_pinned(sl_batch* b) {
 }
 
 void drop_graph(sl_batch* b) {
-  for (auto& x : b->exec) {
-    if (x) cudaGraphExecDestroy(x);
-    x = nullptr;
-  }
+  for (auto& row : b->exec)
+    for (auto& x : row) {
+      if (x) cudaGraphExecDestroy(x);
+      x = nullptr;
+    }
+}
+
+// The sizes a launch of capacity class c works with: slots, blocks of 256 slots, tiles, tile entries.
+struct ClassCaps {
+  uint32_t S, B, T, E;
+};
+ClassCaps class_caps(const sl_batch* b, int c) {
+  static const uint32_t kDiv[sl_batch::kClasses] = {16, 4, 1};
+  ClassCaps k;
+  k.S = (uint32_t)std::max<uint64_t>(256, ((b->max_slots / kDiv[c]) + 255) & ~255ull);
+  k.B = k.S / 256;
+  k.T = std::max<uint32_t>(64, b->max_tiles / kDiv[c]);
+  k.E = (uint32_t)std::max<uint64_t>(6144, b->entry_cap / kDiv[c]);
+  return k;
 }
 
 int shape_index(uint32_t tile_w, uint32_t tile_h) {
@@ -110,13 +125,13 @@ cudaError_t allocate(sl_batch* b) {
   return cudaSuccess;
 }
 
-// The whole chain on stream s, reading every per-batch value from device memory.
+// The whole chain on stream s for capacity class b->cls, reading every per-batch value from device memory.
 cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   cudaError_t e;
 #define CK(x) \
   if ((e = (x)) != cudaSuccess) return e
-  const uint32_t V = b->max_views, B = b->max_blocks, T = b->max_tiles;
-  const uint32_t S = (uint32_t)b->max_slots, E = (uint32_t)b->entry_cap;
+  const ClassCaps k = class_caps(b, b->cls);
+  const uint32_t V = b->max_views, B = k.B, T = k.T, S = k.S, E = k.E;
   CK(cudaMemcpyAsync(b->views.ptr, b->h_views, sizeof(BatchView) * V, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(b->views_out.ptr, b->h_out, sizeof(BatchViewOut) * V, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(b->block_view.ptr, b->h_block_view, 4ull * B, cudaMemcpyHostToDevice, s));
@@ -255,7 +270,8 @@ void stage(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* fr
     const uint32_t first = b->slot_base[v] / 256, nb = (b->n_slots[v] + 255) / 256;
     for (uint32_t k = 0; k < nb; k++) b->h_block_view[first + k] = v;
   }
-  for (uint32_t blk = used; blk < b->max_blocks; blk++) b->h_block_view[blk] = kNoView;
+  const uint32_t nb = class_caps(b, b->cls).B;
+  for (uint32_t blk = used; blk < nb; blk++) b->h_block_view[blk] = kNoView;
   for (size_t k = 0; k < b->scenes.size(); k++) {
     BatchScene& S = b->h_scenes[k];
     memset(&S, 0, sizeof(S));
@@ -285,8 +301,8 @@ int launch_chain(sl_batch* b, cudaStream_t s, bool* replayed) {
   cudaError_t e;
   *replayed = false;
   if (b->use_graph) {
-    const int k = shape_index(b->tile_w, b->tile_h);
-    if (!b->exec[k]) {
+    cudaGraphExec_t& exec = b->exec[shape_index(b->tile_w, b->tile_h)][b->cls];
+    if (!exec) {
       cudaGraph_t g = nullptr;
       e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
       if (e == cudaSuccess) {
@@ -294,16 +310,16 @@ int launch_chain(sl_batch* b, cudaStream_t s, bool* replayed) {
         e = cudaStreamEndCapture(b->cap_stream, &g);
         if (e1 != cudaSuccess) e = e1;
       }
-      if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec[k], g, 0);
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
       if (g) cudaGraphDestroy(g);
       if (e != cudaSuccess) {
-        b->exec[k] = nullptr;
+        exec = nullptr;
         return cuda_fail(e, "capturing the batch graph");
       }
     } else {
       *replayed = true;
     }
-    e = cudaGraphLaunch(b->exec[k], s);
+    e = cudaGraphLaunch(exec, s);
   } else {
     e = enqueue(b, s);
   }
@@ -353,11 +369,23 @@ int batch_layout(sl_batch* b, const uint32_t* scene_of_view, const sl_render_fra
 
 int batch_fit(sl_batch* b, uint64_t slots, uint64_t tiles) { return fit_capacity(b, slots, tiles); }
 
-void batch_begin(sl_batch* b, uint32_t n_views) { b->shade_blended.assign(n_views, 0); }
+void batch_begin(sl_batch* b, uint32_t n_views) {
+  b->shade_blended.assign(n_views, 0);
+  b->cls_min = 0;
+}
 
 int batch_launch(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames, const float* eyes,
                  const float* light_scales, uint32_t n_views, float* out_dev, uint64_t slots, uint64_t tiles,
                  cudaStream_t s, bool* replayed) {
+  // the smallest capacity class that holds the batch's slots and tiles (and, after an overflow, its entries)
+  b->cls = sl_batch::kClasses - 1;
+  for (int c = b->cls_min; c < sl_batch::kClasses; c++) {
+    const ClassCaps k = class_caps(b, c);
+    if (slots <= k.S && tiles <= k.T) {
+      b->cls = c;
+      break;
+    }
+  }
   stage(b, scene_of_view, frames, eyes, light_scales, n_views, out_dev, slots, tiles);
   cudaError_t e;
   if (b->timing && (e = cudaEventRecord(b->ev[0], s)) != cudaSuccess) return cuda_fail(e, "timing");
@@ -371,12 +399,20 @@ int batch_finish(sl_batch* b, uint32_t n_views, uint64_t slots, uint64_t tiles, 
                  sl_batch_stats* stats, bool* retry) {
   *retry = false;
   const FrameCounters& hc = *b->h_ctr;
-  if (hc.overflow || hc.entries > b->entry_cap) {  // grow the tile-entry capacity: the caller launches again
+  if (hc.overflow || hc.entries > class_caps(b, b->cls).E) {  // the caller launches again
+    // a larger class whose entries hold them, else grow the tile-entry capacity
+    for (int c = b->cls + 1; c < sl_batch::kClasses; c++)
+      if (hc.entries <= class_caps(b, c).E) {
+        b->cls_min = c;
+        *retry = true;
+        return SL_OK;
+      }
     const uint64_t want = (uint64_t)hc.entries + hc.entries / 4 + 4096;
     if (b->entry_cap >= kMaxCap || hc.entries >= kMaxCap) return fail(SL_ERR_OVERFLOW, "tile entries beyond 2^30");
     b->entry_cap = std::min<uint64_t>(std::max<uint64_t>(want, 2 * b->entry_cap), kMaxCap);
     cudaError_t e = allocate(b);
     if (e != cudaSuccess) return cuda_fail(e, "growing the tile entries");
+    b->cls_min = sl_batch::kClasses - 1;  // the grown capacity holds them
     *retry = true;
     return SL_OK;
   }

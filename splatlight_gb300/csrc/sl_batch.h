@@ -32,7 +32,12 @@ struct sl_batch {
   float* h_tmark = nullptr;      // per view: its coverage pass's threshold
   // graph
   cudaStream_t cap_stream = nullptr;
-  cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};  // per tile shape (16x16, 8x32, 32x8)
+  // per tile shape (16x16, 8x32, 32x8) and capacity class (grids and clears sized for 1/16, 1/4 or all of the
+  // capacity: a small batch does not pay for the largest one)
+  static constexpr int kClasses = 3;
+  cudaGraphExec_t exec[3][kClasses] = {};
+  int cls = 0;      // the class of the current launch
+  int cls_min = 0;  // raised when a launch's tile entries outgrew its class (this batch only)
   bool timing = false;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   // last batch
