@@ -34,7 +34,7 @@ extern "C" {
 #define SL_ERR_OOM (-3)           /* device allocation failed */
 #define SL_ERR_CUDA (-4)          /* a CUDA runtime call failed */
 #define SL_ERR_TIMEOUT (-5)       /* a bounded device-side wait gave up (the stream stays usable) */
-#define SL_ERR_UNSUPPORTED (-6)   /* the frame enables a feature outside this pipeline (explode, LOD, lens warp ...) */
+#define SL_ERR_UNSUPPORTED (-6)   /* the frame enables a feature outside this pipeline (explode, lens warp ...) */
 #define SL_ERR_ADMISSION (-7)     /* serving: the request does not fit the device-memory budget */
 #define SL_ERR_OVERFLOW (-8)      /* a fixed-capacity buffer (tile entries) was too small; grow and retry */
 #define SL_ERR_NO_DEVICE (-9)     /* no CUDA device, or the device is not an sm_103 part */
@@ -111,7 +111,8 @@ typedef struct sl_render_frame {
   float palette_ext[4][4];       /* (*) palette slots 4-7 */
   float mat_view[16][4];         /* (*) only .w bit 0 (glass) is read: glass flags the splat, nothing else */
   uint32_t part_material_ext[16];/* (*) palette slot per part 16-31 */
-  uint32_t lod[4];               /* lod.x must be 0 (screen-space LOD off) */
+  uint32_t lod[4];               /* screen-space LOD: threshold px (float bits, 0 = off), node slot base, internal
+                                    nodes (sl_lod_create on the renderer first; not in batches) */
   float explode[4];
   float explode_c[4];
   float explode_k[4];            /* explode_k.z must be <= 0.5 (explode off) */
@@ -257,6 +258,39 @@ SL_API int sl_lighting_read(sl_lighting* l, float* colour, float* lamp_T, float*
 
 /* bindColour with a Lighting object's radiance buffer (src/renderer.js:264-268). */
 SL_API int sl_renderer_bind_lighting(sl_renderer* r, sl_lighting* l);
+
+/* ---- screen-space LOD (src/lod.js nodeGaussians + Lod, runtime/wgsl/lod.wgsl) -------------------------------- */
+
+/* The asset's tree drawn as a level of detail: every internal node is a moment-matched Gaussian of its subtree, drawn in
+ * place of its leaves when it is small on screen.  A frame with LOD on has frame.lod = (threshold px as float bits,
+ * node slot base, internal node count, 0): slots [count, base) hold the lamp marker and the emitters (the rest of
+ * them unused), slots [base, base + N - count) the internal nodes; only the leaves and nodes of the cut are drawn. */
+typedef struct sl_lod sl_lod;
+
+/* nodeGaussians(asset) + new Lod(...) (src/lod.js:44-128): n_nodes records, leaves [0, count) of the renderer's scene
+ * first, then the internal nodes; kids: the children lists ([child_lo, child_hi) of each internal node index it).  The
+ * internal nodes' Gaussian records (mean, kappa, eigen-frame quaternion and scales of the covariance, the part, the
+ * leaves' mass-weighted albedo, the first leaf's material) are made on the host in float64 and kept on the device
+ * with the per-depth node lists.  Part roots come from the renderer's parts (sl_part.root).  One LOD per renderer:
+ * sl_render reads it for frames with LOD on.  Needs at most 32 parts. */
+SL_API int sl_lod_create(sl_renderer* r, const sl_node* nodes, uint32_t n_nodes, const uint32_t* kids,
+                         uint32_t n_kids, sl_lod** out);
+SL_API int sl_lod_destroy(sl_lod* l);
+/* Lod.encodeSelect (src/lod.js:139-167), lod.wgsl lod_select: the cut for this frame, top-down, one launch per tree
+ * depth (threshold = frame.lod[0] as float; the view, focal and near plane of the frame; the renderer's part poses).
+ * emit_part: the emitters' part, always opened to its leaves (0xFFFFFFFF: none); size_rule: 1 projected area (the
+ * reference's default), 0 bounding radius; blur_lod > 0 with the frame's shutter open: a moving part opens only nodes
+ * larger than blur_lod x its smear (motion blur variant D). */
+SL_API int sl_lod_select(sl_lod* l, const sl_render_frame* frame, uint32_t emit_part, uint32_t size_rule,
+                         float blur_lod, void* stream);
+/* Lod.encodeColour (src/lod.js:170-172), lod.wgsl lod_colour: the lit colour of the drawn nodes (colour_all: of every
+ * node), bottom-up, one launch per depth: the mass-weighted mean of the children's shown colours (a leaf's: its
+ * bound radiance + bounce gain x its bounce toward the eye, frame.palette[3].x).  Run after the lighting and
+ * sl_lod_select, before sl_render of a lit view. */
+SL_API int sl_lod_colour(sl_lod* l, const sl_render_frame* frame, uint32_t colour_all, void* stream);
+/* Debug read-back (host; any may be NULL): flags (n_nodes u32: 0 none, 1 open, 2 drawn, 3 candidate, 4 under a drawn
+ * node), node colours (4 floats per internal node), the internal nodes' Gaussian records. */
+SL_API int sl_lod_read(sl_lod* l, uint32_t* flags, float* node_colour, sl_gaussian* records);
 
 /* ---- display resolve (shaders/display.wgsl:120-189) -------------------------------------------------------------- */
 

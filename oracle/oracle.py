@@ -47,6 +47,9 @@ def lib():
         P, U32, U64, I = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
         L.orc_render.restype = C.c_int64
         L.orc_render.argtypes = [P, U32, P, U32, P, P, P, P, U32, U32, P, P, P, P, U64, C.POINTER(U64), P, P, I]
+        L.orc_render_lod.restype = C.c_int64
+        L.orc_render_lod.argtypes = [P, U32, P, U32, P, P, P, P, U32, U32, P, P, P, P, U64, C.POINTER(U64), P, P, I,
+                                     P]
         L.orc_sort16.restype = None
         L.orc_sort16.argtypes = [P, U32, P]
         _lib = L
@@ -71,6 +74,11 @@ _EXTRA: dict = {
     "orc_acosf_n": (None, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "orc_row_tiles": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32),
                                 C.POINTER(C.c_uint32)]),
+    "orc_lod_records": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "orc_lod_select": (None, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                              C.c_uint32, C.c_uint32, C.c_float, C.c_void_p]),
+    "orc_lod_colour": (None, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                              C.c_float, C.c_uint32, C.c_void_p]),
 }
 
 
@@ -78,13 +86,26 @@ def _p(a):
     return None if a is None else a.ctypes.data
 
 
+class LodCut(C.Structure):
+    """orc_lod: a screen-space LOD cut as the restated projection reads it."""
+    _fields_ = [("flags", C.c_void_p), ("nodes", C.c_void_p), ("colour", C.c_void_p), ("node_base", C.c_uint32),
+                ("n_int", C.c_uint32)]
+
+
 def render(gaussians, parts, frame, emitters=None, colour=None, lo_b=None, tile=(16, 16), threads: int = 1,
-           want_entries: bool = True):
-    """Runs the restated pipeline; returns dict(keys, order, ranges, entries, rgba, counts, visible)."""
+           want_entries: bool = True, lod=None):
+    """Runs the restated pipeline; returns dict(keys, order, ranges, entries, rgba, counts, visible).  lod: None or
+    (flags, node records, node colours) for a frame whose ``lod`` field is set (slots from frame.lod[1])."""
     L = lib()
     f = np.ascontiguousarray(frame).reshape(())
     n_emit = int(f["palette"][3][1])
     n = len(gaussians) + 1 + n_emit
+    cut = None
+    if lod is not None:
+        flags, recs, ncol = (np.ascontiguousarray(x) for x in lod)
+        ncol = np.ascontiguousarray(ncol, dtype=np.float32)
+        cut = LodCut(flags.ctypes.data, recs.ctypes.data, ncol.ctypes.data, int(f["lod"][1]), int(f["lod"][2]))
+        n = int(f["lod"][1]) + int(f["lod"][2])
     W, H = int(f["viewport"][0]), int(f["viewport"][1])
     tw, th = tile
     tiles = ((W + tw - 1) // tw) * ((H + th - 1) // th)
@@ -102,15 +123,16 @@ def render(gaussians, parts, frame, emitters=None, colour=None, lo_b=None, tile=
     cap = 0
     entries = None
     # first pass sizes the entries (the binning count is cheap)
-    vis = L.orc_render(_p(g), len(g), _p(p), len(p), _p(e), _p(col), _p(lob), f.ctypes.data, tw, th,
-                       _p(keys), _p(order), _p(ranges), None, 0, C.byref(ne), _p(rgba), _p(counts), threads)
+    cref = C.byref(cut) if cut is not None else None
+    vis = L.orc_render_lod(_p(g), len(g), _p(p), len(p), _p(e), _p(col), _p(lob), f.ctypes.data, tw, th,
+                           _p(keys), _p(order), _p(ranges), None, 0, C.byref(ne), _p(rgba), _p(counts), threads, cref)
     if vis < 0:
         raise RuntimeError(f"oracle render failed ({vis})")
     if want_entries:
         cap = int(ne.value)
         entries = np.empty(max(cap, 1), dtype=np.uint32)
-        vis2 = L.orc_render(_p(g), len(g), _p(p), len(p), _p(e), _p(col), _p(lob), f.ctypes.data, tw, th,
-                            None, None, None, entries.ctypes.data, cap, C.byref(ne), None, None, threads)
+        vis2 = L.orc_render_lod(_p(g), len(g), _p(p), len(p), _p(e), _p(col), _p(lob), f.ctypes.data, tw, th,
+                                None, None, None, entries.ctypes.data, cap, C.byref(ne), None, None, threads, cref)
         if vis2 < 0:
             raise RuntimeError(f"oracle binning failed ({vis2})")
         entries = entries[:cap]
@@ -307,3 +329,41 @@ def display(img, exposure: float = 1.0, tone: int = 0, view_mode: int = 3):
     out = np.empty(a.shape[:-1] + (4,), np.uint8)
     fn(a.ctypes.data, a.size // 4, exposure, tone, view_mode, out.ctypes.data)
     return out
+
+
+def lod_records(gaussians, nodes, kids):
+    """src/lod.js nodeGaussians restated (sl_oracle_lod.c): the internal nodes' Gaussian records."""
+    from splatlight_gb300.structs import GAUSSIAN
+    g = np.ascontiguousarray(gaussians)
+    nd = np.ascontiguousarray(nodes)
+    k = np.ascontiguousarray(kids, dtype=np.uint32)
+    out = np.zeros(max(len(nd) - len(g), 1), dtype=GAUSSIAN)
+    rc = lib().orc_lod_records(g.ctypes.data, len(g), nd.ctypes.data, len(nd), k.ctypes.data, out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("orc_lod_records failed")
+    return out[:len(nd) - len(g)]
+
+
+def lod_select(nodes, G, kids, parts, frame, flags, emit_part=0xFFFFFFFF, size_rule=1, blur_lod=0.0):
+    """lod.wgsl lod_select restated: updates ``flags`` (N u32, the previous frame's cut) in place."""
+    nd = np.ascontiguousarray(nodes)
+    k = np.ascontiguousarray(kids, dtype=np.uint32)
+    p = np.ascontiguousarray(parts)
+    f = np.ascontiguousarray(frame).reshape(())
+    assert flags.dtype == np.uint32 and flags.flags.c_contiguous
+    lib().orc_lod_select(nd.ctypes.data, len(nd), G, k.ctypes.data, p.ctypes.data, len(p), f.ctypes.data, emit_part,
+                         size_rule, blur_lod, flags.ctypes.data)
+    return flags
+
+
+def lod_colour(nodes, G, kids, flags, colour, lo_b=None, gain=0.0, colour_all=False):
+    """lod.wgsl lod_colour restated: (N - G, 4) node colours from the leaves' colours (G, 4)."""
+    nd = np.ascontiguousarray(nodes)
+    k = np.ascontiguousarray(kids, dtype=np.uint32)
+    fl = np.ascontiguousarray(flags, dtype=np.uint32)
+    col = np.ascontiguousarray(colour, dtype=np.float32) if colour is not None else None
+    lob = np.ascontiguousarray(lo_b, dtype=np.float32) if lo_b is not None else None
+    out = np.zeros((max(len(nd) - G, 1), 4), np.float32)
+    lib().orc_lod_colour(nd.ctypes.data, len(nd), G, k.ctypes.data, fl.ctypes.data, _p(col), _p(lob), gain,
+                         1 if colour_all else 0, out.ctypes.data)
+    return out[:len(nd) - G]

@@ -108,12 +108,21 @@ static float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi
 /* one slot of shaders/project.wgsl main (:84-370), plain path; returns the key */
 static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t count, const sl_part* parts,
                             const sl_gaussian* emitters, const float* colour, const float* lo_b,
-                            const sl_render_frame* f, orc_splat* out) {
+                            const sl_render_frame* f, orc_splat* out, const orc_lod* lod) {
   memset(out, 0, sizeof(*out));
   out->ix0 = 1;
   out->ix1 = 0;
   uint32_t n_emit = (uint32_t)f->palette[3][1];
-  if (i == count || i > count + n_emit) return ORC_INVALID;
+  /* screen-space LOD (:90-109): slots from the node base are the tree's internal nodes, drawn when in the cut; leaves
+   * are drawn when in the cut */
+  uint32_t node = 0xFFFFFFFFu;
+  if (lod && i >= lod->node_base) {
+    node = i - lod->node_base;
+    if (node >= lod->n_int || lod->flags[count + node] != 2u) return ORC_INVALID;
+  } else {
+    if (i == count || i > count + n_emit) return ORC_INVALID;
+    if (lod && i < count && lod->flags[i] != 2u) return ORC_INVALID;
+  }
 
   const sl_gaussian* g;
   v3 mu;
@@ -121,12 +130,12 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   uint32_t material = ORC_EMITTER_MATERIAL;
   float keep = 1.0f;
   v3 vel = v3_make(0.0f, 0.0f, 0.0f);
-  if (i > count) { /* :226-230 */
+  if (i > count && node == 0xFFFFFFFFu) { /* :226-230 */
     g = &emitters[i - count - 1u];
     mu = v3_make(g->mu[0], g->mu[1], g->mu[2]);
     rot = quat_to_mat(g->quat);
   } else { /* :232-251 */
-    g = &gaussians[i];
+    g = node != 0xFFFFFFFFu ? &lod->nodes[node] : &gaussians[i];
     uint32_t part = g->part_surface & 0xffffu;
     if (part > ORC_MAX_PARTS - 1u) part = ORC_MAX_PARTS - 1u;
     const sl_part* p = &parts[part];
@@ -277,6 +286,10 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   } else if (f->view_mode == 3u) {
     float gain = f->palette[3][0];
     for (int k = 0; k < 3; k++) {
+      if (node != 0xFFFFFFFFu) { /* a drawn node's lit colour, bounce included (lod_colour) */
+        rgb[k] = lod->colour[4u * node + (uint32_t)k];
+        continue;
+      }
       float cl = colour ? colour[4u * i + (uint32_t)k] : 0.0f;
       float bo = lo_b ? lo_b[12u * i + (uint32_t)k] : 0.0f;
       rgb[k] = cl + gain * bo;
@@ -336,9 +349,10 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   return key;
 }
 
-uint32_t orc_project(const sl_gaussian* gaussians, uint32_t count, const sl_part* parts, uint32_t part_count,
-                     const sl_gaussian* emitters, const float* colour, const float* lo_b,
-                     const sl_render_frame* frame, uint32_t n_slots, uint32_t* keys, orc_splat* splats, int nthreads) {
+uint32_t orc_project_lod(const sl_gaussian* gaussians, uint32_t count, const sl_part* parts, uint32_t part_count,
+                         const sl_gaussian* emitters, const float* colour, const float* lo_b,
+                         const sl_render_frame* frame, uint32_t n_slots, uint32_t* keys, orc_splat* splats,
+                         int nthreads, const orc_lod* lod) {
   (void)part_count;
   uint32_t visible = 0;
 #ifdef _OPENMP
@@ -346,11 +360,18 @@ uint32_t orc_project(const sl_gaussian* gaussians, uint32_t count, const sl_part
 #pragma omp parallel for num_threads(nthreads) schedule(static, 4096) reduction(+ : visible)
 #endif
   for (int64_t i = 0; i < (int64_t)n_slots; i++) {
-    uint32_t k = project_one((uint32_t)i, gaussians, count, parts, emitters, colour, lo_b, frame, &splats[i]);
+    uint32_t k = project_one((uint32_t)i, gaussians, count, parts, emitters, colour, lo_b, frame, &splats[i], lod);
     keys[i] = k;
     if (k != ORC_INVALID) visible++;
   }
   return visible;
+}
+
+uint32_t orc_project(const sl_gaussian* gaussians, uint32_t count, const sl_part* parts, uint32_t part_count,
+                     const sl_gaussian* emitters, const float* colour, const float* lo_b,
+                     const sl_render_frame* frame, uint32_t n_slots, uint32_t* keys, orc_splat* splats, int nthreads) {
+  return orc_project_lod(gaussians, count, parts, part_count, emitters, colour, lo_b, frame, n_slots, keys, splats,
+                         nthreads, NULL);
 }
 
 /* radix.wgsl: two stable 8-bit LSD passes over the low 16 key bits (shift 0 then 8, :44-59); the composition of
@@ -462,18 +483,19 @@ void orc_composite(const orc_splat* splats, const uint32_t* order, uint32_t visi
   }
 }
 
-int64_t orc_render(const sl_gaussian* gaussians, uint32_t count, const sl_part* parts, uint32_t part_count,
-                   const sl_gaussian* emitters, const float* colour, const float* lo_b,
-                   const sl_render_frame* frame, uint32_t tile_w, uint32_t tile_h,
-                   uint32_t* keys, uint32_t* order, uint32_t* ranges, uint32_t* entries, uint64_t entries_cap,
-                   uint64_t* n_entries, float* rgba, uint32_t* counts, int nthreads) {
+int64_t orc_render_lod(const sl_gaussian* gaussians, uint32_t count, const sl_part* parts, uint32_t part_count,
+                       const sl_gaussian* emitters, const float* colour, const float* lo_b,
+                       const sl_render_frame* frame, uint32_t tile_w, uint32_t tile_h,
+                       uint32_t* keys, uint32_t* order, uint32_t* ranges, uint32_t* entries, uint64_t entries_cap,
+                       uint64_t* n_entries, float* rgba, uint32_t* counts, int nthreads, const orc_lod* lod) {
   uint32_t n_emit = (uint32_t)frame->palette[3][1];
-  uint32_t n = count + 1u + n_emit;
+  uint32_t n = lod ? lod->node_base + lod->n_int : count + 1u + n_emit;
   uint32_t W = (uint32_t)frame->viewport[0], H = (uint32_t)frame->viewport[1];
   uint32_t* k = keys ? keys : (uint32_t*)malloc(sizeof(uint32_t) * n);
   uint32_t* o = order ? order : (uint32_t*)malloc(sizeof(uint32_t) * n);
   orc_splat* s = (orc_splat*)malloc(sizeof(orc_splat) * n);
-  uint32_t visible = orc_project(gaussians, count, parts, part_count, emitters, colour, lo_b, frame, n, k, s, nthreads);
+  uint32_t visible =
+      orc_project_lod(gaussians, count, parts, part_count, emitters, colour, lo_b, frame, n, k, s, nthreads, lod);
   orc_sort16(k, n, o);
   int64_t ne = orc_bin(s, o, visible, W, H, tile_w, tile_h, ranges, entries, entries_cap);
   if (n_entries) *n_entries = ne < 0 ? 0 : (uint64_t)ne;
@@ -482,6 +504,15 @@ int64_t orc_render(const sl_gaussian* gaussians, uint32_t count, const sl_part* 
   if (!keys) free(k);
   if (!order) free(o);
   return ne < 0 ? -8 : (int64_t)visible;
+}
+
+int64_t orc_render(const sl_gaussian* gaussians, uint32_t count, const sl_part* parts, uint32_t part_count,
+                   const sl_gaussian* emitters, const float* colour, const float* lo_b,
+                   const sl_render_frame* frame, uint32_t tile_w, uint32_t tile_h,
+                   uint32_t* keys, uint32_t* order, uint32_t* ranges, uint32_t* entries, uint64_t entries_cap,
+                   uint64_t* n_entries, float* rgba, uint32_t* counts, int nthreads) {
+  return orc_render_lod(gaussians, count, parts, part_count, emitters, colour, lo_b, frame, tile_w, tile_h, keys, order,
+                        ranges, entries, entries_cap, n_entries, rgba, counts, nthreads, NULL);
 }
 
 /* element-wise sl_logf / sl_expf, for the accuracy tests of the shared deterministic functions */

@@ -31,12 +31,28 @@ typedef struct orc_splat {
   uint32_t valid;
 } orc_splat;
 
+/* A screen-space LOD cut as the projection reads it (shaders/project.wgsl:90-109): node flags (2 = drawn; leaves
+ * [0, count), internal nodes from count), the internal nodes' Gaussian records and lit colours (4 floats each), and
+ * their slots [node_base, node_base + n_int). */
+typedef struct orc_lod {
+  const uint32_t* flags;
+  const sl_gaussian* nodes;
+  const float* colour;
+  uint32_t node_base, n_int;
+} orc_lod;
+
 /* project.wgsl main (shaders/project.wgsl:84-370), plain path: writes per slot the key (INVALID 0xFFFFFFFF) and
  * the splat.  n = count + 1 + n_emit slots.  colour: float4 per Gaussian (lit view) or NULL; lo_b: 3 float4 per
  * Gaussian or NULL.  Returns the number of valid keys. */
 uint32_t orc_project(const sl_gaussian* gaussians, uint32_t count, const sl_part* parts, uint32_t part_count,
                      const sl_gaussian* emitters, const float* colour, const float* lo_b,
                      const sl_render_frame* frame, uint32_t n_slots, uint32_t* keys, orc_splat* splats, int nthreads);
+
+/* orc_project with a screen-space LOD cut (lod may be NULL); n_slots = node_base + n_int with LOD on. */
+uint32_t orc_project_lod(const sl_gaussian* gaussians, uint32_t count, const sl_part* parts, uint32_t part_count,
+                         const sl_gaussian* emitters, const float* colour, const float* lo_b,
+                         const sl_render_frame* frame, uint32_t n_slots, uint32_t* keys, orc_splat* splats,
+                         int nthreads, const orc_lod* lod);
 
 /* radix.wgsl (shaders/radix.wgsl:1-139): stable LSD sort of the low 16 key bits, values = slot index. */
 void orc_sort16(const uint32_t* keys, uint32_t n, uint32_t* order);
@@ -60,6 +76,24 @@ int64_t orc_render(const sl_gaussian* gaussians, uint32_t count, const sl_part* 
                    const sl_render_frame* frame, uint32_t tile_w, uint32_t tile_h,
                    uint32_t* keys, uint32_t* order, uint32_t* ranges, uint32_t* entries, uint64_t entries_cap,
                    uint64_t* n_entries, float* rgba, uint32_t* counts, int nthreads);
+
+/* orc_render with a screen-space LOD cut (lod may be NULL). */
+int64_t orc_render_lod(const sl_gaussian* gaussians, uint32_t count, const sl_part* parts, uint32_t part_count,
+                       const sl_gaussian* emitters, const float* colour, const float* lo_b,
+                       const sl_render_frame* frame, uint32_t tile_w, uint32_t tile_h,
+                       uint32_t* keys, uint32_t* order, uint32_t* ranges, uint32_t* entries, uint64_t entries_cap,
+                       uint64_t* n_entries, float* rgba, uint32_t* counts, int nthreads, const orc_lod* lod);
+
+/* Screen-space LOD (sl_oracle_lod.c): src/lod.js nodeGaussians (internal nodes G..N-1 as Gaussian records, float64;
+ * returns 0), lod.wgsl lod_select (flags updated in place, depth by depth) and lod_colour (ncolour: 4 floats per
+ * internal node, deepest first; colour: 4 floats per leaf or NULL; lo_b: 12 floats per leaf or NULL). */
+int orc_lod_records(const sl_gaussian* gauss, uint32_t G, const sl_node* nodes, uint32_t N, const uint32_t* kids,
+                    sl_gaussian* out);
+void orc_lod_select(const sl_node* nodes, uint32_t N, uint32_t G, const uint32_t* kids, const sl_part* parts,
+                    uint32_t part_count, const sl_render_frame* f, uint32_t emit_part, uint32_t size_rule,
+                    float blur_lod, uint32_t* flags);
+void orc_lod_colour(const sl_node* nodes, uint32_t N, uint32_t G, const uint32_t* kids, const uint32_t* flags,
+                    const float* colour, const float* lo_b, float gain, uint32_t colour_all, float* ncolour);
 
 /* element-wise sl_logf / sl_expf of include/sl_detmath.h (accuracy tests) */
 void orc_logf_n(const float* x, float* y, uint64_t n);

@@ -111,6 +111,11 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_lighting_read": (_I, [_P, _P, _P, _P, _P]),
     "sl_renderer_bind_lighting": (_I, [_P, _P]),
     "sl_display": (_I, [_P, _U32, _U32, _P, _P, _P]),
+    "sl_lod_create": (_I, [_P, _P, _U32, _P, _U32, C.POINTER(_P)]),
+    "sl_lod_destroy": (_I, [_P]),
+    "sl_lod_select": (_I, [_P, _P, _U32, _U32, C.c_float, _P]),
+    "sl_lod_colour": (_I, [_P, _P, _U32, _P]),
+    "sl_lod_read": (_I, [_P, _P, _P, _P]),
     "sl_sort_keys16": (_I, [_P, _U32, _P, _P]),
     "sl_sort_keys16_noalloc": (_I, [_P, _U32, _P, _P]),
     "sl_sort_keys32": (_I, [_P, _U32, _U32, _P, _P]),

@@ -1,9 +1,9 @@
 """Builds libsplatlight.so (every CUDA kernel and the C ABI) in-tree for sm_103a with nvcc.
 
 Each translation unit compiles in parallel to an object under splatlight_gb300/_build/, then one shared library is
-linked next to this file.  project.cu, lighting.cu, tiles.cu and batch.cu are compiled with --fmad=false: their
-arithmetic must match the CPU restatement bit for bit (sort keys, tile rectangles and row spans, the fragment keep
-bound, the opacity maps).  shade.cu is compiled for speed (its output is checked to a tolerance).
+linked next to this file.  project.cu, lighting.cu, tiles.cu, batch.cu and lod.cu are compiled with --fmad=false:
+their arithmetic must match the CPU restatement bit for bit (sort keys, tile rectangles and row spans, the fragment
+keep bound, the opacity maps, the LOD cut).  shade.cu is compiled for speed (its output is checked to a tolerance).
 """
 from __future__ import annotations
 
@@ -21,7 +21,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libsplatlight.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # translation units whose arithmetic is part of the bit-parity contract
-NO_FMAD = {"project.cu", "lighting.cu", "tiles.cu", "batch.cu"}
+NO_FMAD = {"project.cu", "lighting.cu", "tiles.cu", "batch.cu", "lod.cu"}
 # translation units compiled for speed: fused multiply-add, approximate division and square root
 FAST = {"shade.cu"}
 

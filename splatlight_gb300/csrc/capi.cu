@@ -166,6 +166,7 @@ int sl_renderer_destroy(sl_renderer* r) {
   if (!r) return SL_OK;
   cudaSetDevice(r->device);
   cudaDeviceSynchronize();
+  if (r->lod) r->lod->r = nullptr;  // the LOD outlives its renderer only as an empty handle
   r->vb.release_all();
   r->gaussians.release();
   r->emitters.release();
@@ -228,7 +229,8 @@ int sl_renderer_set_timing(sl_renderer* r, int on) {
 
 namespace sl {
 
-int check_frame(const sl_render_frame* f, uint32_t count, uint32_t n_emitters, const std::vector<sl_part>& parts) {
+int check_frame(const sl_render_frame* f, uint32_t count, uint32_t n_emitters, const std::vector<sl_part>& parts,
+                const sl_lod* lod) {
   if (f->count != count) return fail(SL_ERR_INVALID_ARG, "frame.count differs from the renderer's Gaussian count");
   if (!(f->viewport[0] >= 1.0f && f->viewport[1] >= 1.0f && f->viewport[0] <= 16384.0f && f->viewport[1] <= 16384.0f) ||
       f->viewport[0] != (float)(uint32_t)f->viewport[0] || f->viewport[1] != (float)(uint32_t)f->viewport[1])
@@ -243,7 +245,15 @@ int check_frame(const sl_render_frame* f, uint32_t count, uint32_t n_emitters, c
   if (f->lamp[3] > 0.5f) return fail(SL_ERR_UNSUPPORTED, "camera-only flakes (lamp.w = 1) are outside this pipeline");
   if ((uint32_t)(f->lamp_color[3] + 0.5f) != 0u)
     return fail(SL_ERR_UNSUPPORTED, "reflection coverage / Fresnel (lamp_color.w) are outside this pipeline");
-  if (f->lod[0] != 0u) return fail(SL_ERR_UNSUPPORTED, "screen-space LOD (frame.lod) is outside this pipeline");
+  if (f->lod[0] != 0u) {
+    if (!lod)
+      return fail(SL_ERR_UNSUPPORTED, "screen-space LOD (frame.lod) needs sl_lod_create on this renderer (and is not "
+                                      "batched)");
+    if ((uint64_t)f->lod[1] < (uint64_t)count + 1u + (uint32_t)ne || f->lod[2] != lod->n_int ||
+        (uint64_t)f->lod[1] + f->lod[2] > 0x7FFFFFFFull)
+      return fail(SL_ERR_INVALID_ARG, "frame.lod: the node slot base must follow the frame's emitters and the node "
+                                      "count must be the tree's internal node count");
+  }
   if (f->explode_k[2] > 0.5f) return fail(SL_ERR_UNSUPPORTED, "explode is outside this pipeline");
   if (f->particles[1] != 0u) return fail(SL_ERR_UNSUPPORTED, "Gaussian particles are outside this pipeline");
   if (f->palette[3][2] > 0.0f && f->view_mode == 3u)
@@ -348,6 +358,14 @@ static int render_once(sl_renderer* r, const sl_render_frame* f, float4* out_dev
   const uint32_t n_emit = (uint32_t)f->palette[3][1];
   ProjectParams P;
   pack_project_params(f, r->parts, r->count, n_emit, r->tile_w, r->tile_h, P);
+  LodDraw lod{nullptr, nullptr, nullptr};
+  if (f->lod[0] != 0u) {  // screen-space LOD: the tree's internal nodes take the slots from frame.lod[1]
+    P.lod_on = 1u;
+    P.node_base = f->lod[1];
+    P.n_int = f->lod[2];
+    P.n_slots = P.node_base + P.n_int;
+    lod = LodDraw{r->lod->flags.as<uint32_t>(), r->lod->records.as<sl_gaussian>(), r->lod->colour.as<float4>()};
+  }
   const uint32_t n = P.n_slots;
   const uint32_t tiles = P.tiles_x * P.tiles_y;
   const uint32_t W = (uint32_t)f->viewport[0], H = (uint32_t)f->viewport[1];
@@ -369,7 +387,8 @@ static int render_once(sl_renderer* r, const sl_render_frame* f, float4* out_dev
   SL_CHECK_CUDA(cudaMemsetAsync(vb.run_start.ptr, 0, 4ull * tiles, s), "memset runs");
   SL_CHECK_CUDA(cudaMemsetAsync(vb.run_end.ptr, 0, 4ull * tiles, s), "memset runs");
   SL_CHECK_CUDA(launch_project(P, r->gaussians.as<sl_gaussian>(), r->emitters.as<sl_gaussian>(), colour, lo_b,
-                               vb.key16.as<uint16_t>(), vb.recs.as<SplatRec>(), vb.rects.as<ushort4>(), hist, ctr, s),
+                               vb.key16.as<uint16_t>(), vb.recs.as<SplatRec>(), vb.rects.as<ushort4>(), hist, ctr, s,
+                               lod),
                 "project");
   if (ev) SL_CHECK_CUDA(cudaEventRecord(ev[1], s), "event");
   SL_CHECK_CUDA(sort16_pairs(vb.key16.as<uint16_t>(), nullptr, vb.order.as<uint32_t>(), n, nullptr, 16, hist, sc,
@@ -440,12 +459,13 @@ extern "C" {
 int sl_render(sl_renderer* r, const sl_render_frame* f, float* out_rgba, int out_on_device, sl_render_stats* stats,
               void* stream) {
   if (!r || !f || !out_rgba) return fail(SL_ERR_INVALID_ARG, "null argument");
-  int rc = check_frame(f, r->count, r->n_emitters, r->parts);
+  int rc = check_frame(f, r->count, r->n_emitters, r->parts, r->lod);
   if (rc) return rc;
   cudaSetDevice(r->device);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const uint32_t n_emit = (uint32_t)f->palette[3][1];
-  const uint32_t n = r->count + 1u + n_emit;
+  // slots: the scene, the lamp marker, the frame's emitters; with LOD on, up to the end of the tree's node slots
+  const uint32_t n = f->lod[0] != 0u ? f->lod[1] + f->lod[2] : r->count + 1u + n_emit;
   const uint32_t W = (uint32_t)f->viewport[0], H = (uint32_t)f->viewport[1];
   const uint32_t tiles = ((W + r->tile_w - 1) / r->tile_w) * ((H + r->tile_h - 1) / r->tile_h);
   const bool count_mode = f->view_mode == 2u;

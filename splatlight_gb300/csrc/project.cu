@@ -73,11 +73,23 @@ __device__ __forceinline__ void block_tally(bool in, uint32_t key, float maxrad,
 __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i, const float4* __restrict__ gaussians,
                                              const float4* __restrict__ emitters, const float4* __restrict__ colour,
                                              const float4* __restrict__ lo_b, SplatRec* rec_out, uint32_t& key_out,
-                                             ushort4& rect_out, float& maxrad_out) {
+                                             ushort4& rect_out, float& maxrad_out,
+                                             const LodDraw* lod = nullptr) {
   uint32_t key = kInvalidKey16;
   ushort4 rect = make_ushort4(1, 1, 0, 0);
   float maxrad = 0.0f;
   bool live = i < P.n_slots && i != P.count && i <= P.count + P.n_emit;
+  // screen-space LOD (project.wgsl:90-109): slots from node_base are the tree's internal nodes; only the leaves and
+  // nodes of the cut (flag 2) are drawn, and the emitter slots past the frame's emitters stay empty
+  uint32_t node = 0xFFFFFFFFu;
+  if (lod != nullptr && P.lod_on) {
+    if (i >= P.node_base && i < P.n_slots) {
+      node = i - P.node_base;
+      live = node < P.n_int && lod->flags[P.count + node] == 2u;
+    } else if (live && i < P.count && lod->flags[i] != 2u) {
+      live = false;
+    }
+  }
 
   float4 g0, g1, g2, g3;
   uint32_t material = kEmitterMaterial;
@@ -86,12 +98,13 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
   uint32_t part = 0xFFFFFFFFu;  // the Gaussian's part (its rotation is composed only for slots past the depth test)
   V3 vel = v3(0.0f, 0.0f, 0.0f);  // motion blur: world-space displacement over the exposure (project.wgsl:138-146)
   if (live) {
-    const float4* src = (i > P.count) ? emitters + 4u * (i - P.count - 1u) : gaussians + 4u * i;
+    const float4* src = node != 0xFFFFFFFFu ? reinterpret_cast<const float4*>(lod->nodes) + 4u * node
+                        : (i > P.count) ? emitters + 4u * (i - P.count - 1u) : gaussians + 4u * i;
     g0 = __ldg(src + 0);
     g1 = __ldg(src + 1);
     g2 = __ldg(src + 2);
     g3 = __ldg(src + 3);
-    if (i > P.count) {  // project.wgsl:226-230
+    if (i > P.count && node == 0xFFFFFFFFu) {  // project.wgsl:226-230
       mu = v3(g0.x, g0.y, g0.z);
     } else {  // :232-251
       part = __float_as_uint(g2.w) & 0xffffu;
@@ -260,11 +273,18 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
           float cr = g3.x, cg = g3.y, cb = g3.z;
           if (material == kEmitterMaterial) {
           } else if (P.view_mode == 3u) {
-            float4 cl = colour ? colour[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-            float4 bo = lo_b ? lo_b[3u * i] : make_float4(0.f, 0.f, 0.f, 0.f);
-            cr = cl.x + P.bounce_gain * bo.x;
-            cg = cl.y + P.bounce_gain * bo.y;
-            cb = cl.z + P.bounce_gain * bo.z;
+            if (node != 0xFFFFFFFFu) {  // a drawn node's lit colour, bounce included (lod_colour)
+              const float4 nc = lod->colour[node];
+              cr = nc.x;
+              cg = nc.y;
+              cb = nc.z;
+            } else {
+              float4 cl = colour ? colour[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+              float4 bo = lo_b ? lo_b[3u * i] : make_float4(0.f, 0.f, 0.f, 0.f);
+              cr = cl.x + P.bounce_gain * bo.x;
+              cg = cl.y + P.bounce_gain * bo.y;
+              cb = cl.z + P.bounce_gain * bo.z;
+            }
             if (material < 8u) {
               cr *= P.palette[material][0];
               cg *= P.palette[material][1];
@@ -331,7 +351,8 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
                                                            const float4* __restrict__ colour,
                                                            const float4* __restrict__ lo_b, uint16_t* __restrict__ key16,
                                                            SplatRec* __restrict__ recs, ushort4* __restrict__ rects,
-                                                           uint32_t* __restrict__ digit_hist, FrameCounters* ctr) {
+                                                           uint32_t* __restrict__ digit_hist, FrameCounters* ctr,
+                                                           const LodDraw lod) {
   __shared__ uint32_t h_lo[256], h_hi[256];
   __shared__ uint32_t s_visible, s_invalid, s_maxrad;
   const int t = threadIdx.x;
@@ -348,7 +369,7 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
   uint32_t key;
   ushort4 rect;
   float maxrad;
-  project_slot(P, i, gaussians, emitters, colour, lo_b, recs + i, key, rect, maxrad);
+  project_slot(P, i, gaussians, emitters, colour, lo_b, recs + i, key, rect, maxrad, &lod);
   const bool in = i < P.n_slots;
   if (in) {
     key16[i] = (uint16_t)key;
@@ -428,12 +449,14 @@ cudaError_t launch_bproject(const BatchView* views, const uint32_t* block_view, 
 
 cudaError_t launch_project(const ProjectParams& P, const sl_gaussian* gaussians, const sl_gaussian* emitters,
                            const float4* colour, const float4* lo_b, uint16_t* key16, SplatRec* recs,
-                           ushort4* rects, uint32_t* digit_hist, FrameCounters* ctr, cudaStream_t s) {
+                           ushort4* rects, uint32_t* digit_hist, FrameCounters* ctr, cudaStream_t s,
+                           LodDraw lod) {
   if (P.n_slots == 0) return cudaSuccess;
+  if (P.lod_on && (lod.flags == nullptr || lod.nodes == nullptr || lod.colour == nullptr)) return cudaErrorInvalidValue;
   uint32_t blocks = (P.n_slots + kThreads - 1) / kThreads;
   project_kernel<<<blocks, kThreads, 0, s>>>(P, reinterpret_cast<const float4*>(gaussians),
                                              reinterpret_cast<const float4*>(emitters), colour, lo_b, key16, recs,
-                                             rects, digit_hist, ctr);
+                                             rects, digit_hist, ctr, lod);
   return cudaGetLastError();
 }
 

@@ -43,7 +43,16 @@ struct ProjectParams {
   uint32_t count, n_emit, n_slots, view_mode, part_count;
   uint32_t tile_w, tile_h, tiles_x, tiles_y;
   float palette[8][4];  // slots 0-7 (slot 3 = white, w 0)
+  uint32_t lod_on, node_base, n_int, lod_pad;  // screen-space LOD (frame.lod): slots from node_base are tree nodes
   PartXf parts[kMaxParts];
+};
+
+// What the projection reads of a screen-space LOD cut (csrc/lod.cu): the flag of every tree node (2 = drawn), the
+// internal nodes' Gaussian records and their lit colours.
+struct LodDraw {
+  const uint32_t* flags;
+  const sl_gaussian* nodes;
+  const float4* colour;
 };
 
 // Frame-wide device counters written by the pipeline (one per view).
@@ -63,7 +72,25 @@ struct FrameCounters {
 // project.cu
 cudaError_t launch_project(const ProjectParams& P, const sl_gaussian* gaussians, const sl_gaussian* emitters,
                            const float4* colour, const float4* lo_b, uint16_t* key16, SplatRec* recs,
-                           ushort4* rects, uint32_t* digit_hist /*[2][256]*/, FrameCounters* ctr, cudaStream_t s);
+                           ushort4* rects, uint32_t* digit_hist /*[2][256]*/, FrameCounters* ctr, cudaStream_t s,
+                           LodDraw lod = LodDraw{nullptr, nullptr, nullptr});
+
+// lod.cu: one tree depth of lod_select (nodes level[off, off + n_all)) / lod_colour (the depth's internal nodes)
+struct LodPart {
+  float xf[12], xf_prev[12];
+  uint32_t root, flags;
+};
+struct LodSelectParams {
+  float view[16];
+  float focal, near_plane, threshold, shutter, blur_lod;
+  uint32_t G, emit_part, size_rule, part_count;
+  LodPart parts[kMaxParts];
+};
+cudaError_t launch_lod_select(const LodSelectParams& P, const sl_node* nodes, const uint32_t* kids,
+                              const uint32_t* level, uint32_t off, uint32_t n_all, uint32_t* flags, cudaStream_t s);
+cudaError_t launch_lod_colour(uint32_t G, float gain, uint32_t colour_all, const sl_node* nodes, const uint32_t* kids,
+                              const uint32_t* level, uint32_t off, uint32_t n_int, const uint32_t* flags,
+                              const float4* colour, const float4* lo_b, float4* ncolour, cudaStream_t s);
 
 // sort.cu: onesweep LSD radix sort of 16-bit keys with u32 values.
 struct SortScratch {

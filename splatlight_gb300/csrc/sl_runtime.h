@@ -68,6 +68,7 @@ struct sl_renderer {
   const float4* colour = nullptr;  // bound radiance (float4 per Gaussian)
   const float4* lo_b = nullptr;
   sl_lighting* lighting = nullptr;
+  sl_lod* lod = nullptr;  // screen-space LOD of this renderer's scene (capi_lod.cu)
   uint32_t tile_w = 16, tile_h = 16;
   float t_stop_scale = 1e-4f;
   uint64_t entry_capacity = 0;
@@ -78,6 +79,16 @@ struct sl_renderer {
   // last frame (debug read-back)
   uint32_t last_slots = 0, last_w = 0, last_h = 0, last_tiles = 0, last_entries = 0, last_mode = 0;
   bool have_frame = false;
+};
+
+// Host state of a screen-space LOD (capi_lod.cu): the tree, its internal nodes as Gaussians, the flags of the cut,
+// the nodes' lit colours, and the nodes by depth (each depth: its internal nodes, then its leaves).
+struct sl_lod {
+  sl_renderer* r = nullptr;
+  int device = 0;
+  uint32_t N = 0, G = 0, n_int = 0;
+  sl::DevBuf nodes, kids, flags, records, colour, level;
+  std::vector<uint32_t> lvl_off, lvl_int, lvl_all;  // per depth: offset into level, internal count, all count
 };
 
 // Host state of a Lighting object (capi_lighting.cu).

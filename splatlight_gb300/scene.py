@@ -130,6 +130,98 @@ def leaf_nodes(g: np.ndarray) -> np.ndarray:
     return nd
 
 
+def _morton30(u: np.ndarray) -> np.ndarray:
+    """30-bit Morton codes of points in [0, 1)^3 (n, 3)."""
+    q = np.clip((u * 1024.0).astype(np.int64), 0, 1023)
+
+    def spread(v):
+        v = (v | (v << 16)) & 0x030000FF
+        v = (v | (v << 8)) & 0x0300F00F
+        v = (v | (v << 4)) & 0x030C30C3
+        v = (v | (v << 2)) & 0x09249249
+        return v
+    return (spread(q[:, 0]) << 2) | (spread(q[:, 1]) << 1) | spread(q[:, 2])
+
+
+def lod_tree(g: np.ndarray, parts: np.ndarray):
+    """The scene's tree for screen-space LOD: one binary tree per part over its Gaussians, moment-matched (the tool that
+    bakes the reference's asset trees is not part of the reference; this builds the same kind of tree for synthetic
+    scenes).  Leaves are leaf_nodes(g), taken in Morton order of their means within the part; each level pairs
+    neighbours (an odd one out moves up a level unchanged).  An internal node's mass (kappa sqrt(det C)) is its
+    children's sum, its mean and covariance their mass-weighted moments, its radius bounds their spheres
+    (|mu_child - mu| + R_child), float64.  Returns (nodes: G leaves then the internal nodes, kids, parts with
+    ``root`` set; empty parts get root 0xFFFFFFFF)."""
+    G = len(g)
+    leaves = leaf_nodes(g)
+    R = quat_rot(g["quat"].astype(np.float64))
+    sc = g["scale"].astype(np.float64)
+    cov = [np.einsum("nij,nj,nkj->nik", R, sc * sc, R)]
+    mean = [g["mu"].astype(np.float64)]
+    mass = [g["kappa"].astype(np.float64) * np.sqrt(np.linalg.det(cov[0]))]
+    rad = [leaves["radius"].astype(np.float64)]
+    part_of = [(g["part_surface"] & 0xFFFF).astype(np.int64)]
+    kids_a, kids_b = [], []
+    next_id = G
+    parts = parts.copy()
+    for p in range(len(parts)):
+        idx = np.nonzero(part_of[0] == p)[0]
+        if len(idx) == 0:
+            parts[p]["root"] = 0xFFFFFFFF
+            continue
+        mu = mean[0][idx]
+        lo, hi = mu.min(axis=0), mu.max(axis=0)
+        cur = idx[np.argsort(_morton30((mu - lo) / np.maximum(hi - lo, 1e-12) * 0.999999), kind="stable")]
+        while len(cur) > 1:
+            a, b = cur[0:len(cur) - 1:2], cur[1::2]
+            m_all, mu_all, c_all, r_all = (np.concatenate(x) for x in (mass, mean, cov, rad))
+            ma, mb = m_all[a], m_all[b]
+            m = ma + mb
+            mu_n = (ma[:, None] * mu_all[a] + mb[:, None] * mu_all[b]) / m[:, None]
+            da, db = mu_all[a] - mu_n, mu_all[b] - mu_n
+            c_n = (ma[:, None, None] * (c_all[a] + da[:, :, None] * da[:, None, :]) +
+                   mb[:, None, None] * (c_all[b] + db[:, :, None] * db[:, None, :])) / m[:, None, None]
+            r_n = np.maximum(np.linalg.norm(da, axis=1) + r_all[a], np.linalg.norm(db, axis=1) + r_all[b])
+            ids = np.arange(next_id, next_id + len(a))
+            next_id += len(a)
+            mass.append(m)
+            mean.append(mu_n)
+            cov.append(c_n)
+            rad.append(r_n)
+            part_of.append(np.full(len(a), p))
+            kids_a.append(a)
+            kids_b.append(b)
+            cur = np.concatenate([ids, cur[-1:]]) if len(cur) % 2 else ids
+        parts[p]["root"] = int(cur[0])
+    n_int = next_id - G
+    N = G + n_int
+    nodes = np.zeros(N, dtype=NODE)
+    nodes[:G] = leaves
+    if n_int:
+        m_i, mu_i, c_i, r_i, p_i = (np.concatenate(x[1:]) for x in (mass, mean, cov, rad, part_of))
+        ci = np.linalg.inv(c_i)
+        nodes["mean"][G:] = mu_i
+        nodes["radius"][G:] = r_i
+        nodes["cinv_diag"][G:] = np.stack([ci[:, 0, 0], ci[:, 1, 1], ci[:, 2, 2]], axis=1)
+        nodes["cinv_off"][G:] = np.stack([ci[:, 0, 1], ci[:, 0, 2], ci[:, 1, 2]], axis=1)
+        nodes["kappa"][G:] = m_i / np.sqrt(np.linalg.det(c_i))
+        nodes["smax"][G:] = np.sqrt(np.linalg.eigvalsh(c_i)[:, 2])
+        nodes["part"][G:] = p_i
+        k = np.arange(n_int, dtype=np.uint32)
+        nodes["child_lo"][G:] = 2 * k
+        nodes["child_hi"][G:] = 2 * k + 2
+    kids = np.empty(2 * n_int, np.uint32)
+    if n_int:
+        kids[0::2] = np.concatenate(kids_a)
+        kids[1::2] = np.concatenate(kids_b)
+    # depths, top-down: parents are made after their children
+    depth = np.zeros(N, np.int64)
+    for n in range(N - 1, G - 1, -1):
+        depth[kids[2 * (n - G)]] = depth[n] + 1
+        depth[kids[2 * (n - G) + 1]] = depth[n] + 1
+    nodes["depth"] = depth
+    return nodes, kids, parts
+
+
 def _parts(g: np.ndarray, n_parts: int) -> np.ndarray:
     p = np.zeros(n_parts, dtype=PART)
     ident = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], dtype=np.float32)
