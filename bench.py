@@ -471,6 +471,89 @@ def run_sort(args, stream, flush, n=1 << 26):
     return res
 
 
+def run_lod(args, stream, flush, threshold_px: float = 2.0):
+    """The headline workload (hill-like 1,048,576 Gaussians, 1920x1080, lit) with the reference's default screen-space
+    LOD (2 px, projected-area rule) over a moment-matched tree of the scene (scene.lod_tree, built once, untimed):
+    per frame the shading pass, the cut (sl_lod_select), the drawn nodes' colours (sl_lod_colour) and the frame,
+    against the same frames without LOD (device time, L2 flushed between frames)."""
+    import torch
+    from splatlight_gb300 import scene as scn
+    from splatlight_gb300.lighting import camera_forward, for_scene
+    from splatlight_gb300.lod import DRAW, Lod, frame_lod
+    from splatlight_gb300.renderer import SplatRenderer
+    s = make_scene("hill")
+    t0 = time.perf_counter()
+    nodes, kids, parts = scn.lod_tree(s.gaussians, s.parts)
+    t_tree = time.perf_counter() - t0
+    s = scn.dataclasses.replace(s, parts=parts)
+    r = SplatRenderer(s.gaussians, s.parts)
+    L = for_scene(r, s)
+    fwd = camera_forward(s)
+    sc = stream.cuda_stream
+    L.update(s.eye, fwd, stream=sc)
+    t0 = time.perf_counter()
+    lod = Lod(r, nodes, kids)
+    t_create = time.perf_counter() - t0
+    G, N = len(s.gaussians), len(nodes)
+    f0 = frame_for(s, 3)
+    f = frame_lod(f0.copy(), threshold_px, N - G)
+    out = torch.empty((s.height, s.width, 4), dtype=torch.float32, device="cuda")
+    ref = torch.empty_like(out)
+
+    def with_lod():
+        L.shade(s.eye, stream=sc)
+        lod.select(f, stream=sc)
+        lod.colour(f, stream=sc)
+        r.render(f, out=out, stream=sc)
+
+    def without():
+        L.shade(s.eye, stream=sc)
+        r.render(f0, out=ref, stream=sc)
+
+    def timed(fn, steps):
+        ts = []
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.median(ts)
+
+    for _ in range(max(args.warmup, 3)):
+        with_lod()
+        without()
+    torch.cuda.synchronize()
+    steps = max(3, min(args.steps, 20))
+    ms_l = timed(with_lod, steps)
+    st = r.last_stats
+    ms_p = timed(without, steps)
+
+    def cut_only():
+        lod.select(f, stream=sc)
+        lod.colour(f, stream=sc)
+
+    ms_cut = timed(cut_only, steps)
+    flags = lod.read()[0]
+    res = {"workload": "hill-like 1,048,576 Gaussians, 1920x1080, lit; screen-space LOD at "
+                       f"{threshold_px:g} px (projected-area rule) over a {N - G:,}-node moment-matched tree",
+           "lod_views_per_s": round(1000.0 / ms_l, 2), "lod_ms_per_frame": round(ms_l, 4),
+           "plain_views_per_s": round(1000.0 / ms_p, 2), "plain_ms_per_frame": round(ms_p, 4),
+           "speedup_vs_plain": round(ms_p / ms_l, 3), "select_colour_ms": round(ms_cut, 4),
+           "drawn_leaves": int((flags[:G] == DRAW).sum()), "drawn_nodes": int((flags[G:] == DRAW).sum()),
+           "visible": int(st.visible), "entries": int(st.entries),
+           "mean_abs_diff_vs_plain": round(float((out - ref).abs().mean().item()), 6),
+           "tree_build_s": round(t_tree, 2), "lod_create_s": round(t_create, 2)}
+    lod.close()
+    L.close()
+    r.close()
+    return res
+
+
 def run_diff(args, stream, flush):
     """Inverse-rendering steps (forward + L2 loss + hand-written backward) on 500k hill-like Gaussians at 800x800
     against a target rendered from perturbed parameters; device time per step, L2 flushed between steps."""
@@ -554,6 +637,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--only-diff", action="store_true", help="the differentiation leg alone (its own JSON line)")
     ap.add_argument("--only-sort", action="store_true", help="the sort leg alone (its own JSON line)")
+    ap.add_argument("--only-lod", action="store_true", help="the screen-space LOD leg alone (its own JSON line)")
+    ap.add_argument("--no-lod", action="store_true", help="skip the screen-space LOD leg")
     ap.add_argument("--sort-n", type=int, default=1 << 26, help="keys for the sort leg")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiation leg")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="arrival window per rate (the config: 60)")
@@ -588,6 +673,14 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": "sort GB/s", "value": res["ours_24bit"]["gbs"], "unit": "GB/s",
                               "n_gpus": world, "sort": res}))
+        return
+    if args.only_lod:
+        stream = torch.cuda.Stream()
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        res = run_lod(args, stream, flush)
+        if rank == 0:
+            print(json.dumps({"metric": "views/s", "value": res["lod_views_per_s"], "unit": "views/s",
+                              "n_gpus": world, "lod": res}))
         return
     if args.only_diff:
         stream = torch.cuda.Stream()
@@ -740,6 +833,9 @@ def main():
     if not args.no_diff:
         differentiation = run_diff(args, stream, flush)
     sort_leg = run_sort(args, stream, flush)
+    lod_leg = None
+    if not args.no_lod:
+        lod_leg = run_lod(args, stream, flush)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -762,7 +858,7 @@ def main():
                 "roofline": roofline, "sort_roofline": roof_sort, "composite_roofline": roof_comp,
                 "shade_roofline": roof_shade,
                 "cpu_baseline": cpu, "clocks": clocks, "batched": batch, "serving": serving,
-                "differentiation": differentiation, "sort": sort_leg}
+                "differentiation": differentiation, "sort": sort_leg, "lod": lod_leg}
         print(json.dumps(line))
     L.close()
     r.close()

@@ -1,6 +1,6 @@
 // Screen-space LOD (C ABI): src/lod.js's nodeGaussians (the internal nodes of the scene's tree as Gaussian records,
-// float64 on the host) and Lod (the per-depth node lists; encodeSelect / encodeColour as one kernel launch per depth,
-// csrc/lod.cu).  The renderer's projection draws the cut for frames with frame.lod on (csrc/project.cu).
+// float64 on the host) and Lod (the per-depth node lists; encodeSelect / encodeColour as one kernel launch per large
+// depth and one for the small top depths together, csrc/lod.cu).  The renderer's projection draws the cut for frames with frame.lod on (csrc/project.cu).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -214,6 +214,10 @@ int sl_lod_create(sl_renderer* r, const sl_node* nodes, uint32_t n_nodes, const 
     level.insert(level.end(), inner[d].begin(), inner[d].end());
     level.insert(level.end(), leaves[d].begin(), leaves[d].end());
   }
+  while (l->top < l->lvl_all.size() && l->lvl_all[l->top] <= kLodTopNodes) l->top++;
+  std::vector<uint32_t> tables(l->lvl_off);
+  tables.insert(tables.end(), l->lvl_all.begin(), l->lvl_all.end());
+  tables.insert(tables.end(), l->lvl_int.begin(), l->lvl_int.end());
   auto up = [&](DevBuf& b, const void* src, size_t bytes) -> cudaError_t {
     cudaError_t e1 = b.ensure(std::max<size_t>(bytes, 16));
     if (e1 == cudaSuccess && bytes) e1 = cudaMemcpy(b.ptr, src, bytes, cudaMemcpyHostToDevice);
@@ -223,6 +227,7 @@ int sl_lod_create(sl_renderer* r, const sl_node* nodes, uint32_t n_nodes, const 
       (e = up(l->kids, kids, 4ull * n_kids)) != cudaSuccess ||
       (e = up(l->records, recs.data(), sizeof(sl_gaussian) * recs.size())) != cudaSuccess ||
       (e = up(l->level, level.data(), 4ull * level.size())) != cudaSuccess ||
+      (e = up(l->tables, tables.data(), 4ull * tables.size())) != cudaSuccess ||
       (e = l->flags.ensure(4ull * N + 16)) != cudaSuccess || (e = l->colour.ensure(16ull * l->n_int + 16)) != cudaSuccess ||
       (e = cudaMemset(l->flags.ptr, 0, 4ull * N)) != cudaSuccess ||
       (e = cudaMemset(l->colour.ptr, 0, 16ull * l->n_int)) != cudaSuccess) {
@@ -239,7 +244,7 @@ int sl_lod_destroy(sl_lod* l) {
   cudaSetDevice(l->device);
   cudaDeviceSynchronize();
   if (l->r && l->r->lod == l) l->r->lod = nullptr;
-  DevBuf* all[] = {&l->nodes, &l->kids, &l->flags, &l->records, &l->colour, &l->level};
+  DevBuf* all[] = {&l->nodes, &l->kids, &l->flags, &l->records, &l->colour, &l->level, &l->tables};
   for (DevBuf* b : all) b->release();
   delete l;
   return SL_OK;
@@ -273,9 +278,14 @@ int sl_lod_select(sl_lod* l, const sl_render_frame* f, uint32_t emit_part, uint3
     P.parts[p].root = r->parts[p].root;
     P.parts[p].flags = r->parts[p].flags;
   }
-  for (size_t d = 0; d < l->lvl_off.size(); d++) {
-    cudaError_t e = launch_lod_select(P, l->nodes.as<sl_node>(), l->kids.as<uint32_t>(), l->level.as<uint32_t>(),
-                                      l->lvl_off[d], l->lvl_all[d], l->flags.as<uint32_t>(), s);
+  const uint32_t D = (uint32_t)l->lvl_off.size();
+  const uint32_t* tab = l->tables.as<uint32_t>();
+  cudaError_t e = launch_lod_select_top(P, l->nodes.as<sl_node>(), l->kids.as<uint32_t>(), l->level.as<uint32_t>(), tab,
+                                        tab + D, l->top, l->flags.as<uint32_t>(), s);
+  if (e != cudaSuccess) return cuda_fail(e, "lod_select");
+  for (uint32_t d = l->top; d < D; d++) {
+    e = launch_lod_select(P, l->nodes.as<sl_node>(), l->kids.as<uint32_t>(), l->level.as<uint32_t>(), l->lvl_off[d],
+                          l->lvl_all[d], l->flags.as<uint32_t>(), s);
     if (e != cudaSuccess) return cuda_fail(e, "lod_select");
   }
   return SL_OK;
@@ -287,12 +297,19 @@ int sl_lod_colour(sl_lod* l, const sl_render_frame* f, uint32_t colour_all, void
   cudaSetDevice(l->device);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const float gain = f->palette[3][0];
-  for (size_t d = l->lvl_off.size(); d-- > 0;) {
+  const uint32_t D = (uint32_t)l->lvl_off.size();
+  for (uint32_t d = D; d-- > l->top;) {
+    if (l->lvl_int[d] == 0) continue;
     cudaError_t e = launch_lod_colour(l->G, gain, colour_all, l->nodes.as<sl_node>(), l->kids.as<uint32_t>(),
                                       l->level.as<uint32_t>(), l->lvl_off[d], l->lvl_int[d], l->flags.as<uint32_t>(),
                                       l->r->colour, l->r->lo_b, l->colour.as<float4>(), s);
     if (e != cudaSuccess) return cuda_fail(e, "lod_colour");
   }
+  const uint32_t* tab = l->tables.as<uint32_t>();
+  cudaError_t e = launch_lod_colour_top(l->G, gain, colour_all, l->nodes.as<sl_node>(), l->kids.as<uint32_t>(),
+                                        l->level.as<uint32_t>(), tab, tab + 2 * D, l->top, l->flags.as<uint32_t>(),
+                                        l->r->colour, l->r->lo_b, l->colour.as<float4>(), s);
+  if (e != cudaSuccess) return cuda_fail(e, "lod_colour");
   return SL_OK;
 }
 

@@ -6,7 +6,8 @@
 //   lod_colour  bottom-up, one launch per depth (deepest first) over its internal nodes that are drawn or under a
 //               drawn node: the mass-weighted mean (mass = kappa / sqrt(det cinv)) of the children's shown colours.
 // Each node writes only its own flag and its children's, and a depth's nodes share no children, so one launch per
-// depth needs no atomics.  Compiled with --fmad=false: the open/draw decisions and the colour sums match the CPU
+// depth needs no atomics; the small top depths (a tree's first dozen) run in one CTA with a barrier between depths,
+// so a frame costs a launch per large depth only.  Compiled with --fmad=false: the open/draw decisions and the colour sums match the CPU
 // restatement bit for bit.
 #include "sl_internal.h"
 #include "sl_lodsize.h"
@@ -15,16 +16,12 @@ namespace sl {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kBlock = 1024;  // the single CTA of the small top depths
 constexpr uint32_t kNone = 0u, kOpen = 1u, kDraw = 2u, kCand = 3u, kUnder = 4u;
 
-__global__ void __launch_bounds__(kThreads) lod_select_kernel(const __grid_constant__ LodSelectParams P,
-                                                              const sl_node* __restrict__ nodes,
-                                                              const uint32_t* __restrict__ kids,
-                                                              const uint32_t* __restrict__ level, uint32_t off,
-                                                              uint32_t n_all, uint32_t* __restrict__ flags) {
-  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
-  if (g >= n_all) return;
-  const uint32_t n = level[off + g];
+__device__ __forceinline__ void select_node(const LodSelectParams& P, const sl_node* __restrict__ nodes,
+                                            const uint32_t* __restrict__ kids, uint32_t n,
+                                            uint32_t* __restrict__ flags) {
   const sl_node& nd = nodes[n];
   const uint32_t f = flags[n];
   const uint32_t part = nd.part;
@@ -65,6 +62,30 @@ __global__ void __launch_bounds__(kThreads) lod_select_kernel(const __grid_const
   for (uint32_t k = nd.child_lo; k < nd.child_hi; k++) flags[kids[k]] = open ? kCand : kUnder;
 }
 
+__global__ void __launch_bounds__(kThreads) lod_select_kernel(const __grid_constant__ LodSelectParams P,
+                                                              const sl_node* __restrict__ nodes,
+                                                              const uint32_t* __restrict__ kids,
+                                                              const uint32_t* __restrict__ level, uint32_t off,
+                                                              uint32_t n_all, uint32_t* __restrict__ flags) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g < n_all) select_node(P, nodes, kids, level[off + g], flags);
+}
+
+// The small top depths in one CTA, a barrier between depths (their flags are written and read by this CTA alone).
+__global__ void __launch_bounds__(kBlock) lod_select_top_kernel(const __grid_constant__ LodSelectParams P,
+                                                                const sl_node* __restrict__ nodes,
+                                                                const uint32_t* __restrict__ kids,
+                                                                const uint32_t* __restrict__ level,
+                                                                const uint32_t* __restrict__ lvl_off,
+                                                                const uint32_t* __restrict__ lvl_all, uint32_t depths,
+                                                                uint32_t* __restrict__ flags) {
+  for (uint32_t d = 0; d < depths; d++) {
+    const uint32_t off = lvl_off[d], n_all = lvl_all[d];
+    for (uint32_t g = threadIdx.x; g < n_all; g += kBlock) select_node(P, nodes, kids, level[off + g], flags);
+    __syncthreads();
+  }
+}
+
 __device__ __forceinline__ float node_mass(const sl_node& nd) {
   const float* a = nd.cinv_diag;
   const float* o = nd.cinv_off;
@@ -73,17 +94,11 @@ __device__ __forceinline__ float node_mass(const sl_node& nd) {
   return nd.kappa / sqrtf(det_inv > 1e-30f ? det_inv : 1e-30f);
 }
 
-__global__ void __launch_bounds__(kThreads) lod_colour_kernel(uint32_t G, float gain, uint32_t colour_all,
-                                                              const sl_node* __restrict__ nodes,
-                                                              const uint32_t* __restrict__ kids,
-                                                              const uint32_t* __restrict__ level, uint32_t off,
-                                                              uint32_t n_int, const uint32_t* __restrict__ flags,
-                                                              const float4* __restrict__ colour,
-                                                              const float4* __restrict__ lo_b,
-                                                              float4* __restrict__ ncolour) {
-  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
-  if (g >= n_int) return;
-  const uint32_t n = level[off + g];
+__device__ __forceinline__ void colour_node(uint32_t G, float gain, uint32_t colour_all,
+                                            const sl_node* __restrict__ nodes, const uint32_t* __restrict__ kids,
+                                            uint32_t n, const uint32_t* __restrict__ flags,
+                                            const float4* __restrict__ colour, const float4* __restrict__ lo_b,
+                                            float4* __restrict__ ncolour) {
   const uint32_t f = flags[n];
   if (f != kDraw && f != kUnder && !colour_all) return;
   const sl_node& nd = nodes[n];
@@ -113,12 +128,61 @@ __global__ void __launch_bounds__(kThreads) lod_colour_kernel(uint32_t G, float 
   ncolour[n - G] = make_float4(cr / d, cg / d, cb / d, 1.0f);
 }
 
+__global__ void __launch_bounds__(kThreads) lod_colour_kernel(uint32_t G, float gain, uint32_t colour_all,
+                                                              const sl_node* __restrict__ nodes,
+                                                              const uint32_t* __restrict__ kids,
+                                                              const uint32_t* __restrict__ level, uint32_t off,
+                                                              uint32_t n_int, const uint32_t* __restrict__ flags,
+                                                              const float4* __restrict__ colour,
+                                                              const float4* __restrict__ lo_b,
+                                                              float4* __restrict__ ncolour) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g < n_int) colour_node(G, gain, colour_all, nodes, kids, level[off + g], flags, colour, lo_b, ncolour);
+}
+
+// The small top depths bottom-up in one CTA (after the larger depths below them).
+__global__ void __launch_bounds__(kBlock) lod_colour_top_kernel(uint32_t G, float gain, uint32_t colour_all,
+                                                                const sl_node* __restrict__ nodes,
+                                                                const uint32_t* __restrict__ kids,
+                                                                const uint32_t* __restrict__ level,
+                                                                const uint32_t* __restrict__ lvl_off,
+                                                                const uint32_t* __restrict__ lvl_int, uint32_t depths,
+                                                                const uint32_t* __restrict__ flags,
+                                                                const float4* __restrict__ colour,
+                                                                const float4* __restrict__ lo_b,
+                                                                float4* __restrict__ ncolour) {
+  for (uint32_t d = depths; d-- > 0;) {
+    const uint32_t off = lvl_off[d], n_int = lvl_int[d];
+    for (uint32_t g = threadIdx.x; g < n_int; g += kBlock)
+      colour_node(G, gain, colour_all, nodes, kids, level[off + g], flags, colour, lo_b, ncolour);
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_lod_select(const LodSelectParams& P, const sl_node* nodes, const uint32_t* kids,
                               const uint32_t* level, uint32_t off, uint32_t n_all, uint32_t* flags, cudaStream_t s) {
   if (n_all == 0) return cudaSuccess;
   lod_select_kernel<<<(n_all + kThreads - 1) / kThreads, kThreads, 0, s>>>(P, nodes, kids, level, off, n_all, flags);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lod_select_top(const LodSelectParams& P, const sl_node* nodes, const uint32_t* kids,
+                                  const uint32_t* level, const uint32_t* lvl_off, const uint32_t* lvl_all,
+                                  uint32_t depths, uint32_t* flags, cudaStream_t s) {
+  if (depths == 0) return cudaSuccess;
+  lod_select_top_kernel<<<1, kBlock, 0, s>>>(P, nodes, kids, level, lvl_off, lvl_all, depths, flags);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lod_colour_top(uint32_t G, float gain, uint32_t colour_all, const sl_node* nodes,
+                                  const uint32_t* kids, const uint32_t* level, const uint32_t* lvl_off,
+                                  const uint32_t* lvl_int, uint32_t depths, const uint32_t* flags,
+                                  const float4* colour, const float4* lo_b, float4* ncolour, cudaStream_t s) {
+  if (depths == 0) return cudaSuccess;
+  lod_colour_top_kernel<<<1, kBlock, 0, s>>>(G, gain, colour_all, nodes, kids, level, lvl_off, lvl_int, depths, flags,
+                                             colour, lo_b, ncolour);
   return cudaGetLastError();
 }
 

@@ -91,6 +91,15 @@ cudaError_t launch_lod_select(const LodSelectParams& P, const sl_node* nodes, co
 cudaError_t launch_lod_colour(uint32_t G, float gain, uint32_t colour_all, const sl_node* nodes, const uint32_t* kids,
                               const uint32_t* level, uint32_t off, uint32_t n_int, const uint32_t* flags,
                               const float4* colour, const float4* lo_b, float4* ncolour, cudaStream_t s);
+// The depths [0, depths) in one CTA (lvl_off / lvl_all / lvl_int: device copies of the per-depth tables).
+constexpr uint32_t kLodTopNodes = 1024;  // a depth with at most this many nodes joins the one-CTA top
+cudaError_t launch_lod_select_top(const LodSelectParams& P, const sl_node* nodes, const uint32_t* kids,
+                                  const uint32_t* level, const uint32_t* lvl_off, const uint32_t* lvl_all,
+                                  uint32_t depths, uint32_t* flags, cudaStream_t s);
+cudaError_t launch_lod_colour_top(uint32_t G, float gain, uint32_t colour_all, const sl_node* nodes,
+                                  const uint32_t* kids, const uint32_t* level, const uint32_t* lvl_off,
+                                  const uint32_t* lvl_int, uint32_t depths, const uint32_t* flags,
+                                  const float4* colour, const float4* lo_b, float4* ncolour, cudaStream_t s);
 
 // sort.cu: onesweep LSD radix sort of 16-bit keys with u32 values.
 struct SortScratch {

@@ -88,7 +88,9 @@ struct sl_lod {
   int device = 0;
   uint32_t N = 0, G = 0, n_int = 0;
   sl::DevBuf nodes, kids, flags, records, colour, level;
+  sl::DevBuf tables;                                 // device copy of lvl_off, lvl_all, lvl_int (depth-major rows)
   std::vector<uint32_t> lvl_off, lvl_int, lvl_all;  // per depth: offset into level, internal count, all count
+  uint32_t top = 0;                                  // depths [0, top) run in one CTA (kLodTopNodes nodes at most)
 };
 
 // Host state of a Lighting object (capi_lighting.cu).

@@ -155,39 +155,42 @@ def lod_tree(g: np.ndarray, parts: np.ndarray):
     leaves = leaf_nodes(g)
     R = quat_rot(g["quat"].astype(np.float64))
     sc = g["scale"].astype(np.float64)
-    cov = [np.einsum("nij,nj,nkj->nik", R, sc * sc, R)]
-    mean = [g["mu"].astype(np.float64)]
-    mass = [g["kappa"].astype(np.float64) * np.sqrt(np.linalg.det(cov[0]))]
-    rad = [leaves["radius"].astype(np.float64)]
-    part_of = [(g["part_surface"] & 0xFFFF).astype(np.int64)]
+    cap = max(2 * G, 1)
+    cov = np.zeros((cap, 3, 3))
+    mean = np.zeros((cap, 3))
+    mass = np.zeros(cap)
+    rad = np.zeros(cap)
+    part_of = np.zeros(cap, np.int64)
+    cov[:G] = np.einsum("nij,nj,nkj->nik", R, sc * sc, R)
+    mean[:G] = g["mu"]
+    mass[:G] = g["kappa"].astype(np.float64) * np.sqrt(np.linalg.det(cov[:G]))
+    rad[:G] = leaves["radius"]
+    part_of[:G] = g["part_surface"] & 0xFFFF
     kids_a, kids_b = [], []
     next_id = G
     parts = parts.copy()
     for p in range(len(parts)):
-        idx = np.nonzero(part_of[0] == p)[0]
+        idx = np.nonzero(part_of[:G] == p)[0]
         if len(idx) == 0:
             parts[p]["root"] = 0xFFFFFFFF
             continue
-        mu = mean[0][idx]
+        mu = mean[idx]
         lo, hi = mu.min(axis=0), mu.max(axis=0)
         cur = idx[np.argsort(_morton30((mu - lo) / np.maximum(hi - lo, 1e-12) * 0.999999), kind="stable")]
         while len(cur) > 1:
             a, b = cur[0:len(cur) - 1:2], cur[1::2]
-            m_all, mu_all, c_all, r_all = (np.concatenate(x) for x in (mass, mean, cov, rad))
-            ma, mb = m_all[a], m_all[b]
+            ma, mb = mass[a], mass[b]
             m = ma + mb
-            mu_n = (ma[:, None] * mu_all[a] + mb[:, None] * mu_all[b]) / m[:, None]
-            da, db = mu_all[a] - mu_n, mu_all[b] - mu_n
-            c_n = (ma[:, None, None] * (c_all[a] + da[:, :, None] * da[:, None, :]) +
-                   mb[:, None, None] * (c_all[b] + db[:, :, None] * db[:, None, :])) / m[:, None, None]
-            r_n = np.maximum(np.linalg.norm(da, axis=1) + r_all[a], np.linalg.norm(db, axis=1) + r_all[b])
+            mu_n = (ma[:, None] * mean[a] + mb[:, None] * mean[b]) / m[:, None]
+            da, db = mean[a] - mu_n, mean[b] - mu_n
             ids = np.arange(next_id, next_id + len(a))
             next_id += len(a)
-            mass.append(m)
-            mean.append(mu_n)
-            cov.append(c_n)
-            rad.append(r_n)
-            part_of.append(np.full(len(a), p))
+            cov[ids] = (ma[:, None, None] * (cov[a] + da[:, :, None] * da[:, None, :]) +
+                        mb[:, None, None] * (cov[b] + db[:, :, None] * db[:, None, :])) / m[:, None, None]
+            rad[ids] = np.maximum(np.linalg.norm(da, axis=1) + rad[a], np.linalg.norm(db, axis=1) + rad[b])
+            mass[ids] = m
+            mean[ids] = mu_n
+            part_of[ids] = p
             kids_a.append(a)
             kids_b.append(b)
             cur = np.concatenate([ids, cur[-1:]]) if len(cur) % 2 else ids
@@ -197,15 +200,15 @@ def lod_tree(g: np.ndarray, parts: np.ndarray):
     nodes = np.zeros(N, dtype=NODE)
     nodes[:G] = leaves
     if n_int:
-        m_i, mu_i, c_i, r_i, p_i = (np.concatenate(x[1:]) for x in (mass, mean, cov, rad, part_of))
+        c_i = cov[G:N]
         ci = np.linalg.inv(c_i)
-        nodes["mean"][G:] = mu_i
-        nodes["radius"][G:] = r_i
+        nodes["mean"][G:] = mean[G:N]
+        nodes["radius"][G:] = rad[G:N]
         nodes["cinv_diag"][G:] = np.stack([ci[:, 0, 0], ci[:, 1, 1], ci[:, 2, 2]], axis=1)
         nodes["cinv_off"][G:] = np.stack([ci[:, 0, 1], ci[:, 0, 2], ci[:, 1, 2]], axis=1)
-        nodes["kappa"][G:] = m_i / np.sqrt(np.linalg.det(c_i))
+        nodes["kappa"][G:] = mass[G:N] / np.sqrt(np.linalg.det(c_i))
         nodes["smax"][G:] = np.sqrt(np.linalg.eigvalsh(c_i)[:, 2])
-        nodes["part"][G:] = p_i
+        nodes["part"][G:] = part_of[G:N]
         k = np.arange(n_int, dtype=np.uint32)
         nodes["child_lo"][G:] = 2 * k
         nodes["child_hi"][G:] = 2 * k + 2
@@ -215,9 +218,17 @@ def lod_tree(g: np.ndarray, parts: np.ndarray):
         kids[1::2] = np.concatenate(kids_b)
     # depths, top-down: parents are made after their children
     depth = np.zeros(N, np.int64)
-    for n in range(N - 1, G - 1, -1):
-        depth[kids[2 * (n - G)]] = depth[n] + 1
-        depth[kids[2 * (n - G) + 1]] = depth[n] + 1
+    parent = np.full(N, -1, np.int64)
+    if n_int:
+        parent[kids[0::2]] = np.arange(G, N)
+        parent[kids[1::2]] = np.arange(G, N)
+    # a node's depth = its parent's + 1; parents have larger ids, so sweep ids downward level by level
+    pending = np.nonzero(parent >= 0)[0]
+    while len(pending):
+        depth[pending] = depth[parent[pending]] + 1
+        # re-sweep until stable (each pass fixes at least one more level)
+        changed = depth[pending] != depth[parent[pending]] + 1
+        pending = pending[changed] if changed.any() else pending[:0]
     nodes["depth"] = depth
     return nodes, kids, parts
 
