@@ -152,6 +152,9 @@ typedef struct sl_render_options {
   uint32_t tile_w, tile_h;       /* 0 = keep */
   float t_stop;                  /* early-termination transmittance scale (0 = default 1e-4 / max radiance) */
   uint32_t entry_capacity;       /* tile entries pre-allocated (0 = grow on demand) */
+  uint32_t sort_mode;            /* 0 keep; 1 the stable radix sort (default, radix.wgsl); 2 the counting sort
+                                    (scan.wgsl + scatter.wgsl: 65536-bucket key histogram, exclusive offsets, atomic
+                                    placement -- splats sharing a key land in arbitrary order) (src/renderer.js:122) */
 } sl_render_options;
 
 typedef struct sl_render_stats {

@@ -74,6 +74,10 @@ _EXTRA: dict = {
     "orc_acosf_n": (None, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "orc_row_tiles": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32),
                                 C.POINTER(C.c_uint32)]),
+    "orc_bin": (C.c_int64, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                            C.c_void_p, C.c_void_p, C.c_uint64]),
+    "orc_composite": (None, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                             C.c_int]),
     "orc_lod_records": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "orc_lod_select": (None, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                               C.c_uint32, C.c_uint32, C.c_float, C.c_void_p]),
@@ -367,3 +371,33 @@ def lod_colour(nodes, G, kids, flags, colour, lo_b=None, gain=0.0, colour_all=Fa
     lib().orc_lod_colour(nd.ctypes.data, len(nd), G, k.ctypes.data, fl.ctypes.data, _p(col), _p(lob), gain,
                          1 if colour_all else 0, out.ctypes.data)
     return out[:len(nd) - G]
+
+
+def render_given_order(gaussians, parts, frame, order, emitters=None, colour=None, lo_b=None, tile=(16, 16),
+                       threads: int = 1):
+    """The restated projection, then binning and compositing in a given order of the visible slots (the counting
+    sort's order on the GPU, whose ties land in arbitrary order): dict(keys, ranges, entries, rgba, counts, visible)."""
+    L = lib()
+    f = np.ascontiguousarray(frame).reshape(())
+    n = len(gaussians) + 1 + int(f["palette"][3][1])
+    W, H = int(f["viewport"][0]), int(f["viewport"][1])
+    tw, th = tile
+    tiles = ((W + tw - 1) // tw) * ((H + th - 1) // th)
+    g, p = np.ascontiguousarray(gaussians), np.ascontiguousarray(parts)
+    e = np.ascontiguousarray(emitters) if emitters is not None and len(emitters) else None
+    col = np.ascontiguousarray(colour, dtype=np.float32) if colour is not None else None
+    lob = np.ascontiguousarray(lo_b, dtype=np.float32) if lo_b is not None else None
+    keys = np.empty(n, np.uint32)
+    splats = np.zeros(n, SPLAT)
+    vis = int(L.orc_project(_p(g), len(g), _p(p), len(p), _p(e), _p(col), _p(lob), f.ctypes.data, n, keys.ctypes.data,
+                            splats.ctypes.data, threads))
+    o = np.ascontiguousarray(order[:vis], dtype=np.uint32)
+    ranges = np.empty((tiles, 2), np.uint32)
+    total = int(L.orc_bin(splats.ctypes.data, o.ctypes.data, vis, W, H, tw, th, ranges.ctypes.data, None, 0))
+    entries = np.empty(max(total, 1), np.uint32)
+    L.orc_bin(splats.ctypes.data, o.ctypes.data, vis, W, H, tw, th, None, entries.ctypes.data, total)
+    rgba = np.empty((H, W, 4), np.float32)
+    counts = np.empty((H, W), np.uint32)
+    L.orc_composite(splats.ctypes.data, o.ctypes.data, vis, W, H, rgba.ctypes.data, counts.ctypes.data, threads)
+    return {"keys": keys, "ranges": ranges, "entries": entries[:total], "rgba": rgba, "counts": counts,
+            "visible": vis}

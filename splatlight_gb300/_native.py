@@ -33,7 +33,7 @@ class RenderStats(C.Structure):
 
 class RenderOptions(C.Structure):
     _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("t_stop", C.c_float),
-                ("entry_capacity", C.c_uint32)]
+                ("entry_capacity", C.c_uint32), ("sort_mode", C.c_uint32)]
 
 
 class BatchOptions(C.Structure):

@@ -29,7 +29,7 @@ void ViewBuffers::release_all() {
   DevBuf* all[] = {&key16,     &recs,      &rects,       &order,       &slot_counts, &slot_offsets, &keys_alt,
                    &vals_alt,  &status,    &tile_ctr,    &tile_keys,   &tile_vals,   &tile_counts,  &tile_starts,
                    &ranges,    &digit_hist, &scan_scratch, &counters, &out,         &counts,       &run_start,
-                   &run_end};
+                   &run_end,   &key_hist};
   for (DevBuf* b : all) b->release();
 }
 
@@ -211,6 +211,8 @@ int sl_renderer_set_options(sl_renderer* r, const sl_render_options* opt) {
   }
   if (opt->t_stop > 0.0f) r->t_stop_scale = opt->t_stop;
   if (opt->entry_capacity) r->entry_capacity = opt->entry_capacity;
+  if (opt->sort_mode > 2u) return fail(SL_ERR_INVALID_ARG, "sort_mode must be 0 (keep), 1 (stable) or 2 (counting)");
+  if (opt->sort_mode) r->sort_mode = opt->sort_mode;
   return SL_OK;
 }
 
@@ -342,7 +344,8 @@ static cudaError_t ensure_view_buffers(ViewBuffers& vb, uint32_t n, uint32_t til
   ENS(vb.run_start, 4ull * tiles + 16);
   ENS(vb.run_end, 4ull * tiles + 16);
   ENS(vb.digit_hist, 4ull * 4 * 256);
-  size_t sc = scan_scratch_bytes(n);
+  ENS(vb.key_hist, 2 * 4ull * 65536);
+  size_t sc = scan_scratch_bytes(n > 65536u ? n : 65536u);  // also the counting sort's 65536 key offsets
   size_t sc2 = scan_scratch_bytes(tiles);
   ENS(vb.scan_scratch, sc > sc2 ? sc : sc2);
   ENS(vb.counters, sizeof(FrameCounters));
@@ -391,9 +394,18 @@ static int render_once(sl_renderer* r, const sl_render_frame* f, float4* out_dev
                                lod),
                 "project");
   if (ev) SL_CHECK_CUDA(cudaEventRecord(ev[1], s), "event");
-  SL_CHECK_CUDA(sort16_pairs(vb.key16.as<uint16_t>(), nullptr, vb.order.as<uint32_t>(), n, nullptr, 16, hist, sc,
-                             ctr, s),
-                "depth sort");
+  if (r->sort_mode == 2u) {  // counting sort (scan.wgsl, scatter.wgsl): ties land in arbitrary order
+    SL_CHECK_CUDA(cudaMemsetAsync(vb.key_hist.ptr, 0, 4ull * 65536, s), "memset key histogram");
+    SL_CHECK_CUDA(launch_key_hist(vb.key16.as<uint16_t>(), n, vb.key_hist.as<uint32_t>(), s), "key histogram");
+    uint32_t* offsets = vb.key_hist.as<uint32_t>() + 65536;
+    SL_CHECK_CUDA(exclusive_scan_u32(vb.key_hist.as<uint32_t>(), offsets, 65536, nullptr, vb.scan_scratch.ptr, ctr, s),
+                  "key offsets");
+    SL_CHECK_CUDA(launch_key_scatter(vb.key16.as<uint16_t>(), n, offsets, vb.order.as<uint32_t>(), s), "key scatter");
+  } else {
+    SL_CHECK_CUDA(sort16_pairs(vb.key16.as<uint16_t>(), nullptr, vb.order.as<uint32_t>(), n, nullptr, 16, hist, sc,
+                               ctr, s),
+                  "depth sort");
+  }
   if (ev) SL_CHECK_CUDA(cudaEventRecord(ev[2], s), "event");
   SL_CHECK_CUDA(launch_tile_counts(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.recs.as<SplatRec>(), n, P.tile_w,
                                    P.tile_h, ctr, vb.slot_counts.as<uint32_t>(), s),

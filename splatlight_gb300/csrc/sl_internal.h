@@ -75,6 +75,11 @@ cudaError_t launch_project(const ProjectParams& P, const sl_gaussian* gaussians,
                            ushort4* rects, uint32_t* digit_hist /*[2][256]*/, FrameCounters* ctr, cudaStream_t s,
                            LodDraw lod = LodDraw{nullptr, nullptr, nullptr});
 
+// sort_api.cu: the counting sort of 16-bit depth keys (shaders/scan.wgsl + scatter.wgsl): key counts (valid keys),
+// then, after an exclusive scan of the 65536 counts into offsets, order[atomicAdd(&offsets[key], 1)] = i.
+cudaError_t launch_key_hist(const uint16_t* key16, uint32_t n, uint32_t* hist, cudaStream_t s);
+cudaError_t launch_key_scatter(const uint16_t* key16, uint32_t n, uint32_t* offsets, uint32_t* order, cudaStream_t s);
+
 // lod.cu: one tree depth of lod_select (nodes level[off, off + n_all)) / lod_colour (the depth's internal nodes)
 struct LodPart {
   float xf[12], xf_prev[12];

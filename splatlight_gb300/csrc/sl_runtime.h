@@ -48,6 +48,7 @@ struct ViewBuffers {
   DevBuf tile_keys, tile_vals;                                 // per entry
   DevBuf tile_counts, tile_starts, ranges, run_start, run_end; // per tile
   DevBuf digit_hist;                                           // [4][256]: depth-key passes, tile-key passes
+  DevBuf key_hist;                                             // counting sort: 65536 key counts, then offsets
   DevBuf scan_scratch;
   DevBuf counters;                                             // FrameCounters
   DevBuf out, counts;                                          // composite targets when the caller's are on the host
@@ -70,6 +71,7 @@ struct sl_renderer {
   sl_lighting* lighting = nullptr;
   sl_lod* lod = nullptr;  // screen-space LOD of this renderer's scene (capi_lod.cu)
   uint32_t tile_w = 16, tile_h = 16;
+  uint32_t sort_mode = 1;  // 1 stable radix sort, 2 counting sort
   float t_stop_scale = 1e-4f;
   uint64_t entry_capacity = 0;
   bool timing = false;

@@ -80,6 +80,40 @@ cudaError_t sort16_in_scratch(const uint16_t* keys, uint32_t n, uint32_t* order,
   return sort16_pairs(const_cast<uint16_t*>(keys), nullptr, order, n, nullptr, 16, hist, sc, ctr, s);
 }
 
+namespace {
+
+// scatter.wgsl's histogram side (shaders/project.wgsl:369 atomicAdd(histogram[key])): one count per valid key
+__global__ void __launch_bounds__(256) key_hist_kernel(const uint16_t* __restrict__ key16, uint32_t n,
+                                                       uint32_t* __restrict__ hist) {
+  const uint32_t i = blockIdx.x * 256u + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t k = key16[i];
+  if (k != kInvalidKey16) atomicAdd(&hist[k], 1u);
+}
+
+// shaders/scatter.wgsl:9-18: each valid slot takes the next position of its key's range
+__global__ void __launch_bounds__(256) key_scatter_kernel(const uint16_t* __restrict__ key16, uint32_t n,
+                                                          uint32_t* __restrict__ offsets, uint32_t* __restrict__ order) {
+  const uint32_t i = blockIdx.x * 256u + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t k = key16[i];
+  if (k != kInvalidKey16) order[atomicAdd(&offsets[k], 1u)] = i;
+}
+
+}  // namespace
+
+cudaError_t launch_key_hist(const uint16_t* key16, uint32_t n, uint32_t* hist, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  key_hist_kernel<<<(n + 255u) / 256u, 256, 0, s>>>(key16, n, hist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_key_scatter(const uint16_t* key16, uint32_t n, uint32_t* offsets, uint32_t* order, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  key_scatter_kernel<<<(n + 255u) / 256u, 256, 0, s>>>(key16, n, offsets, order);
+  return cudaGetLastError();
+}
+
 }  // namespace sl
 
 using namespace sl;

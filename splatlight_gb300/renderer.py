@@ -64,8 +64,10 @@ class SplatRenderer:
         self._bound = (colour, lo_b)
         N.check(self._lib.sl_renderer_bind_colour(self._h, N.ptr(colour), N.ptr(lo_b)))
 
-    def set_options(self, tile_w: int = 0, tile_h: int = 0, t_stop: float = 0.0, entry_capacity: int = 0) -> None:
-        o = N.RenderOptions(tile_w, tile_h, t_stop, entry_capacity)
+    def set_options(self, tile_w: int = 0, tile_h: int = 0, t_stop: float = 0.0, entry_capacity: int = 0,
+                    sort_mode: int = 0) -> None:
+        """sort_mode: 0 keep, 1 stable radix sort (default), 2 counting sort (ties in arbitrary order)."""
+        o = N.RenderOptions(tile_w, tile_h, t_stop, entry_capacity, sort_mode)
         N.check(self._lib.sl_renderer_set_options(self._h, C.byref(o)))
 
     def set_timing(self, on: bool) -> None:

@@ -133,3 +133,13 @@ def test_leaf_cut_renders_as_plain(tree):
     b = oracle.render(s.gaussians, s.parts, f0, emitters=s.emitters)
     assert np.array_equal(a["rgba"], b["rgba"]) and np.array_equal(a["ranges"], b["ranges"])
     assert np.array_equal(a["entries"], b["entries"])
+
+
+def test_render_given_the_stable_order_is_render():
+    """render_given_order (the counting sort's check) with the stable order reproduces the whole restated frame."""
+    s = scene.subset(scene.cornell(), 5000)
+    f = _frame(s, (0.3, 0.2, 3.2), W=160, H=120)
+    a = oracle.render(s.gaussians, s.parts, f, emitters=s.emitters)
+    b = oracle.render_given_order(s.gaussians, s.parts, f, a["order"], emitters=s.emitters)
+    assert np.array_equal(a["rgba"], b["rgba"]) and np.array_equal(a["entries"], b["entries"])
+    assert np.array_equal(a["ranges"], b["ranges"]) and np.array_equal(a["counts"], b["counts"])
