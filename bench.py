@@ -185,7 +185,7 @@ def run_batch(args, stream, flush):
     from splatlight_gb300.batch import BatchRenderer, View
     from splatlight_gb300.lighting import camera_forward, for_scene
     from splatlight_gb300.renderer import SplatRenderer
-    scenes, mix = batch_mix()
+    scenes, mix = batch_mix(n_views=args.batch_views)
     rs, ls = [], []
     for s in scenes:
         r = SplatRenderer(s.gaussians, s.parts)
@@ -638,6 +638,7 @@ def main():
     ap.add_argument("--only-diff", action="store_true", help="the differentiation leg alone (its own JSON line)")
     ap.add_argument("--only-sort", action="store_true", help="the sort leg alone (its own JSON line)")
     ap.add_argument("--only-lod", action="store_true", help="the screen-space LOD leg alone (its own JSON line)")
+    ap.add_argument("--batch-views", type=int, default=64, help="views of the ragged batch (the config: 64)")
     ap.add_argument("--no-lod", action="store_true", help="skip the screen-space LOD leg")
     ap.add_argument("--sort-n", type=int, default=1 << 26, help="keys for the sort leg")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiation leg")
