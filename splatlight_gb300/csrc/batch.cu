@@ -137,7 +137,39 @@ __global__ void __launch_bounds__(kThreads) btile_runs_kernel(const uint32_t* __
   }
 }
 
+// One block of 256 slots: its valid keys (depth bits not 0xFFFF) and their slots, in slot order, from block_off[blk]
+// (a ballot per warp, the warps' counts in shared memory).
+__global__ void __launch_bounds__(kThreads) bcompact_kernel(const uint32_t* __restrict__ block_view,
+                                                            const uint32_t* __restrict__ keys32,
+                                                            const uint32_t* __restrict__ block_off,
+                                                            uint32_t* __restrict__ keys_c,
+                                                            uint32_t* __restrict__ slots_c) {
+  __shared__ uint32_t warp_n[kThreads / 32];
+  const uint32_t blk = blockIdx.x;
+  if (block_view[blk] == kNoView) return;
+  const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
+  const uint32_t gslot = blk * kThreads + t;
+  const uint32_t key = keys32[gslot];
+  const bool valid = (key & 0xFFFFu) != 0xFFFFu;
+  const uint32_t m = __ballot_sync(0xffffffffu, valid);
+  if (lane == 0) warp_n[w] = __popc(m);
+  __syncthreads();
+  uint32_t pos = block_off[blk] + __popc(m & ((1u << lane) - 1u));
+  for (uint32_t k = 0; k < w; k++) pos += warp_n[k];
+  if (valid) {
+    keys_c[pos] = key;
+    slots_c[pos] = gslot;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_bcompact(const uint32_t* block_view, const uint32_t* keys32, const uint32_t* block_off,
+                            uint32_t max_blocks, uint32_t* keys_c, uint32_t* slots_c, cudaStream_t s) {
+  if (!max_blocks) return cudaSuccess;
+  bcompact_kernel<<<max_blocks, kThreads, 0, s>>>(block_view, keys32, block_off, keys_c, slots_c);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_btile_count(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
                                const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t* counts,

@@ -110,6 +110,8 @@ cudaError_t allocate(sl_batch* b) {
   ENS(b->counters, sizeof(FrameCounters));
   ENS(b->view_maxrad, 4ull * V + 16);
   ENS(b->view_visible, 4ull * V + 16);
+  ENS(b->block_valid, 4ull * B + 16);
+  ENS(b->block_off, 4ull * B + 16);
   ENS(b->marks, S + 16);
   ENS(b->view_tmark, 4ull * V + 16);
 #undef ENS
@@ -148,18 +150,25 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   uint32_t* hist = b->hist.as<uint32_t>();
   CK(launch_bproject(b->views.as<BatchView>(), b->block_view.as<uint32_t>(), B, b->keys32.as<uint32_t>(),
                      b->recs.as<SplatRec>(), b->rects.as<ushort4>(), hist, b->view_maxrad.as<uint32_t>(),
-                     b->view_visible.as<uint32_t>(), s));
+                     b->view_visible.as<uint32_t>(), b->block_valid.as<uint32_t>(), s));
+  // the depth sort runs over the visible slots only: their keys compacted in slot order (stability kept), the count
+  // in ctr->visible (read on the device by the sort and the binning)
+  CK(exclusive_scan_u32(b->block_valid.as<uint32_t>(), b->block_off.as<uint32_t>(), B, &ctr->visible,
+                        b->scan_scratch.ptr, ctr, s));
+  CK(launch_bcompact(b->block_view.as<uint32_t>(), b->keys32.as<uint32_t>(), b->block_off.as<uint32_t>(), B,
+                     b->tile_keys.as<uint32_t>(), b->tile_vals.as<uint32_t>(), s));
+  const uint32_t* n_visible = &ctr->visible;
   const uint32_t max_tiles_sort = (uint32_t)(b->status.bytes / (4ull * 256 * 4));
-  CK(sort32_pairs(b->keys32.as<uint32_t>(), b->keys_alt.as<uint32_t>(), nullptr, b->order.as<uint32_t>(),
-                  b->vals_alt.as<uint32_t>(), S, totals, 16 + bits_for(V - 1), hist, b->status.as<uint32_t>(),
-                  b->tile_ctr.as<uint32_t>(), max_tiles_sort, ctr, s));
-  CK(launch_btile_count(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->recs.as<SplatRec>(), totals, S, b->tile_w,
-                        b->tile_h, b->slot_counts.as<uint32_t>(), s));
+  CK(sort32_pairs(b->tile_keys.as<uint32_t>(), b->keys_alt.as<uint32_t>(), b->tile_vals.as<uint32_t>(),
+                  b->order.as<uint32_t>(), b->vals_alt.as<uint32_t>(), S, n_visible, 16 + bits_for(V - 1), hist,
+                  b->status.as<uint32_t>(), b->tile_ctr.as<uint32_t>(), max_tiles_sort, ctr, s));
+  CK(launch_btile_count(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->recs.as<SplatRec>(), n_visible, S,
+                        b->tile_w, b->tile_h, b->slot_counts.as<uint32_t>(), s));
   CK(exclusive_scan_u32(b->slot_counts.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), S, &ctr->entries,
                         b->scan_scratch.ptr, ctr, s));
   CK(launch_btile_emit(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->recs.as<SplatRec>(),
                        b->slot_offsets.as<uint32_t>(), b->slot_counts.as<uint32_t>(), b->views.as<BatchView>(),
-                       b->block_view.as<uint32_t>(), totals,
+                       b->block_view.as<uint32_t>(), n_visible,
                        S, b->tile_w, b->tile_h, E, ctr,
                        b->tile_keys.as<uint32_t>(), b->tile_vals.as<uint32_t>(), hist + 768, s));
   // the tile sort: stable on the 16-bit view-local tile id (two passes); entries arrive in (view, depth) order, so
@@ -524,7 +533,7 @@ int sl_batch_destroy(sl_batch* b) {
   sl::DevBuf* all[] = {&b->views, &b->views_out, &b->block_view, &b->scenes_dev, &b->dyn, &b->keys32, &b->keys_alt,
                        &b->vals_alt, &b->order, &b->recs, &b->rects, &b->slot_counts, &b->slot_offsets,
                        &b->tile_keys, &b->tile_keys_alt, &b->tile_vals, &b->tile_vals_alt, &b->status, &b->tile_ctr,
-                       &b->hist, &b->scan_scratch,
+                       &b->hist, &b->scan_scratch, &b->block_valid, &b->block_off,
                        &b->ranges, &b->counters, &b->view_maxrad, &b->view_visible, &b->marks,
                        &b->view_tmark};
   for (sl::DevBuf* x : all) x->release();
@@ -641,9 +650,21 @@ int sl_batch_read_view(sl_batch* b, uint32_t view, uint32_t* order, uint32_t* ra
     }
   }
   if (order) {
-    e = cudaMemcpy(order, b->order.as<uint32_t>() + sb, 4ull * n, cudaMemcpyDeviceToHost);
+    // the depth sort ran over the visible slots only (views in order): this view's are at the sum of the earlier
+    // views' visible counts; its culled slots follow in index order, as the per-view stable sort places them
+    uint64_t pos = 0;
+    for (uint32_t v = 0; v < view; v++) pos += b->h_visible[v];
+    const uint32_t vis = b->h_visible[view];
+    if (vis > n) return fail(SL_ERR_INVALID_ARG, "inconsistent visible count");
+    e = cudaMemcpy(order, b->order.as<uint32_t>() + pos, 4ull * vis, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "order");
-    for (uint32_t i = 0; i < n; i++) order[i] -= sb;
+    for (uint32_t i = 0; i < vis; i++) order[i] -= sb;
+    std::vector<uint32_t> keys(n);
+    e = cudaMemcpy(keys.data(), b->keys32.as<uint32_t>() + sb, 4ull * n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "keys");
+    uint32_t at = vis;
+    for (uint32_t i = 0; i < n && at < n; i++)
+      if ((keys[i] & 0xFFFFu) == 0xFFFFu) order[at++] = i;
   }
   if (ranges) {
     uint32_t at = 0;

@@ -394,12 +394,16 @@ __global__ void __launch_bounds__(kThreads) bproject_kernel(const BatchView* __r
                                                             uint32_t* __restrict__ keys32, SplatRec* __restrict__ recs,
                                                             ushort4* __restrict__ rects, uint32_t* __restrict__ digit_hist,
                                                             uint32_t* __restrict__ view_maxrad,
-                                                            uint32_t* __restrict__ view_visible) {
+                                                            uint32_t* __restrict__ view_visible,
+                                                            uint32_t* __restrict__ block_valid) {
   __shared__ ProjectParams sP;
   __shared__ uint32_t h[2][256];
   __shared__ uint32_t s_visible, s_invalid, s_maxrad;
   const uint32_t v = block_view[blockIdx.x];
-  if (v == kNoView) return;
+  if (v == kNoView) {
+    if (threadIdx.x == 0) block_valid[blockIdx.x] = 0u;
+    return;
+  }
   const int t = threadIdx.x;
   const BatchView& V = views[v];
   {
@@ -426,11 +430,12 @@ __global__ void __launch_bounds__(kThreads) bproject_kernel(const BatchView* __r
   rects[gslot] = rect;
   block_tally(true, key, maxrad, h[0], h[1], &s_visible, &s_invalid, &s_maxrad);
   __syncthreads();
-  const uint32_t lo = h[0][t] + (t == 255 ? s_invalid : 0u), hi = h[1][t] + (t == 255 ? s_invalid : 0u);
-  if (lo) atomicAdd(&digit_hist[t], lo);
-  if (hi) atomicAdd(&digit_hist[256 + t], hi);
-  if (t == 0) atomicAdd(&digit_hist[512 + v], (uint32_t)kThreads);  // the view byte: every slot of the block
+  // the digits of the valid keys only: the depth sort runs over the compacted valid keys (bcompact)
+  if (h[0][t]) atomicAdd(&digit_hist[t], h[0][t]);
+  if (h[1][t]) atomicAdd(&digit_hist[256 + t], h[1][t]);
   if (t == 0) {
+    block_valid[blockIdx.x] = s_visible;
+    if (s_visible) atomicAdd(&digit_hist[512 + v], s_visible);  // the view byte
     if (s_visible) atomicAdd(&view_visible[v], s_visible);
     if (s_maxrad) atomicMax(&view_maxrad[v], s_maxrad);
   }
@@ -440,10 +445,10 @@ __global__ void __launch_bounds__(kThreads) bproject_kernel(const BatchView* __r
 
 cudaError_t launch_bproject(const BatchView* views, const uint32_t* block_view, uint32_t max_blocks, uint32_t* keys32,
                             SplatRec* recs, ushort4* rects, uint32_t* digit_hist, uint32_t* view_maxrad,
-                            uint32_t* view_visible, cudaStream_t s) {
+                            uint32_t* view_visible, uint32_t* block_valid, cudaStream_t s) {
   if (max_blocks == 0) return cudaSuccess;
   bproject_kernel<<<max_blocks, kThreads, 0, s>>>(views, block_view, keys32, recs, rects, digit_hist, view_maxrad,
-                                                  view_visible);
+                                                  view_visible, block_valid);
   return cudaGetLastError();
 }
 

@@ -183,9 +183,14 @@ struct BatchView {
   float light_scale;                     // the request's light-intensity scale (emitters and distant lights)
 };
 constexpr uint32_t kNoView = 0xFFFFFFFFu;
+// block_valid[block]: the block's valid keys (0 for blocks past the batch); digit_hist counts valid keys only.
 cudaError_t launch_bproject(const BatchView* views, const uint32_t* block_view, uint32_t max_blocks, uint32_t* keys32,
                             SplatRec* recs, ushort4* rects, uint32_t* digit_hist /*[3][256]*/,
-                            uint32_t* view_maxrad, uint32_t* view_visible, cudaStream_t s);
+                            uint32_t* view_maxrad, uint32_t* view_visible, uint32_t* block_valid, cudaStream_t s);
+// batch.cu: the valid keys of every block, in slot order, at block_off[block] (the exclusive scan of block_valid):
+// keys_c / slots_c, for the depth sort over the visible slots only.
+cudaError_t launch_bcompact(const uint32_t* block_view, const uint32_t* keys32, const uint32_t* block_off,
+                            uint32_t max_blocks, uint32_t* keys_c, uint32_t* slots_c, cudaStream_t s);
 
 // What the batched compositor needs of each view (device array, ascending tile_base).
 struct BatchViewOut {
