@@ -121,6 +121,33 @@ def test_graph_replay_and_growth(cuda):
                 _assert_view(B, k, v, [ra, rb][v.scene], (16, 16))
 
 
+def test_capacity_classes(cuda):
+    """A small batch runs the graph of a small capacity class (1/16 or 1/4 of the capacity); when its tile entries
+    outgrow the class it runs again in the class that holds them.  Every class gives the same images, bit for bit,
+    as a batch sized exactly for the views."""
+    a, b = _scenes()
+    with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
+        ra.set_emitters(a.emitters)
+        rb.set_emitters(b.emitters)
+        views = _views(a, b)[:2]
+        with BatchRenderer([ra, rb], max_views=8) as exact:
+            ref = [im.copy() for im in _render(exact, views)]
+            entries = exact.last_stats.entries
+        # slots for 64 such batches; entries for 8x these views: class 0 holds 1/16 of that, fewer than the views need
+        with BatchRenderer([ra, rb], max_views=8, max_slots=64 * exact.last_stats.slots,
+                           max_entries=8 * entries) as big:
+            assert 8 * entries // 16 < entries
+            got = [im.copy() for im in _render(big, views)]
+            for x, y in zip(ref, got):
+                assert np.array_equal(x, y)
+            for k, v in enumerate(views):
+                _assert_view(big, k, v, [ra, rb][v.scene], (16, 16))
+            again = big.render(views)          # the class that held them, replayed
+            assert big.last_stats.graph_replayed == 1
+            for x, y in zip(ref, again):
+                assert np.array_equal(x, y)
+
+
 def test_no_graph_matches_graph(cuda):
     a, b = _scenes()
     with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
