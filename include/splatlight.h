@@ -193,7 +193,9 @@ SL_API int sl_renderer_set_timing(sl_renderer* r, int on);
  * -> stable radix sort of the 16-bit depth keys -> per-tile ranges -> front-to-back composite.  `frame` is the
  * 1200-byte RenderFrame (view_mode inside it).  Writes viewport W x H RGBA fp32 (row 0 at the top; premultiplied
  * linear rgb, alpha = coverage) to `out_rgba`.  View mode 2 writes the per-pixel contributor count to .r (and to
- * the counts debug buffer).  Stream-ordered on `stream`; with a host `out_rgba` the call returns after the copy. */
+ * the counts debug buffer).  Stream-ordered on `stream`; with a host `out_rgba` the call returns once the image is
+ * there (page-locked host memory is written in place by the compositor over the host link; pageable memory through
+ * a device copy). */
 SL_API int sl_render(sl_renderer* r, const sl_render_frame* frame, float* out_rgba, int out_on_device,
               sl_render_stats* stats, void* stream);
 

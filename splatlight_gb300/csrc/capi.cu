@@ -486,11 +486,24 @@ int sl_render(sl_renderer* r, const sl_render_frame* f, float* out_rgba, int out
     cudaError_t e = ensure_view_buffers(r->vb, n, tiles, r->entry_capacity, W * H, !out_on_device, count_mode);
     if (e != cudaSuccess) return cuda_fail(e, "allocating view buffers");
     float4* out_dev = out_on_device ? reinterpret_cast<float4*>(out_rgba) : r->vb.out.as<float4>();
+    // a pinned (page-locked, device-mapped) host image: the compositor writes it in place over the host link, the
+    // device-to-host read fused into the kernel that produces the image (no staging copy)
+    bool direct = false;
+    if (!out_on_device) {
+      cudaPointerAttributes pa{};
+      if (cudaPointerGetAttributes(&pa, out_rgba) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+          pa.devicePointer != nullptr && reinterpret_cast<uintptr_t>(pa.devicePointer) % 16 == 0) {
+        out_dev = reinterpret_cast<float4*>(pa.devicePointer);
+        direct = true;
+      } else {
+        cudaGetLastError();  // a pageable pointer is not an error here
+      }
+    }
     uint32_t* counts_dev = count_mode ? r->vb.counts.as<uint32_t>() : nullptr;
     sl_render_stats local{};
     rc = render_once(r, f, out_dev, counts_dev, s, stats ? &local : nullptr);
     if (rc) return rc;
-    if (!out_on_device)
+    if (!out_on_device && !direct)
       SL_CHECK_CUDA(cudaMemcpyAsync(out_rgba, out_dev, 16ull * W * H, cudaMemcpyDeviceToHost, s), "output copy");
     SL_CHECK_CUDA(cudaStreamSynchronize(s), "sync");
     const FrameCounters& hc = *r->host_ctr;

@@ -191,3 +191,20 @@ def test_counting_sort(cuda, orc, mode):
         else:
             assert float(np.abs(img - ref["rgba"]).max()) <= RGB_TOL
         r.set_options(sort_mode=1)
+
+
+def test_pinned_host_image_written_in_place(cuda):
+    """A page-locked host image is written by the compositor in place (no staging copy): the same pixels as a
+    pageable host image and as a device image."""
+    torch = cuda
+    s = scene.subset(scene.cornell(), 20000)
+    with SplatRenderer(s.gaussians, s.parts) as r:
+        r.set_emitters(s.emitters)
+        for mode in (VIEW_FLAT, VIEW_OVERDRAW):
+            f = _frame(s, 200, 150, mode)
+            pageable = r.render(f)
+            pinned = torch.empty((150, 200, 4), dtype=torch.float32, pin_memory=True).numpy()
+            r.render(f, out=pinned)
+            dev = torch.empty((150, 200, 4), dtype=torch.float32, device="cuda")
+            r.render(f, out=dev)
+            assert np.array_equal(pinned, pageable) and np.array_equal(dev.cpu().numpy(), pageable)
