@@ -185,8 +185,9 @@ __global__ void __launch_bounds__(kThreads) shade_kernel(const __grid_constant__
   colour[g] = make_float4(c.x, c.y, c.z, 1.0f);
 }
 
-// Batched: the visible scene Gaussians of every lit view, shaded from the view's eye, with the palette and albedo
-// scale the projection applies to bound radiance (project.wgsl:424-453), written into the splat records.
+// Batched: the marked scene Gaussians of every lit view (the coverage pass), shaded from the view's eye, with the
+// palette and albedo scale the projection applies to bound radiance (project.wgsl:424-453), written into the splat
+// records.
 __global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __restrict__ views,
                                                           const BatchScene* __restrict__ scenes,
                                                           const uint32_t* __restrict__ block_view,
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __res
   const BatchView& V = views[v];
   const BatchScene& S = scenes[V.scene];
   if (V.P.view_mode != 3u || !S.lit) return;
-  // this view's visible Gaussians: list[slot_base, slot_base + n_vis) (the exclusive scan of its flags)
+  // this view's marked Gaussians: list[slot_base, slot_base + n) (the exclusive scan of its flags)
   const uint32_t first = offsets[V.slot_base];
   const uint32_t last = v + 1u < dyn->n_views ? offsets[views[v + 1u].slot_base] : *shade_n;
   const uint32_t j = (blockIdx.x / 2 - V.block_first) * 256u + (blockIdx.x & 1u) * kThreads + threadIdx.x;

@@ -57,7 +57,7 @@ struct BatchScene {
   ShadeParams SH;   // eye replaced per view
   uint32_t lit;     // 0: no lighting bound (radiance 0, as an unbound colour buffer)
 };
-// Shades each lit view's visible Gaussians (the shading list; see launch_bshade_flags) at the view's eye and light
+// Shades each lit view's marked Gaussians (the shading list; see launch_bshade_flags) at the view's eye and light
 // scale into their splat records' radiance, and raises the view's maximum radiance.
 cudaError_t launch_bshade(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
                           uint32_t max_blocks, const uint32_t* list, const uint32_t* offsets, const uint32_t* shade_n,
