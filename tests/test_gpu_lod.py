@@ -56,6 +56,28 @@ def test_flags_match_over_frames(world, rule):
         assert (got == DRAW).sum() > 0
 
 
+def test_flags_with_blur_and_emitter_part(world):
+    """The emitters' part always opens to its leaves; with the shutter open a moving part opens only nodes larger than
+    blur_lod x its smear (motion blur variant D): both bit-exact against the restatement."""
+    s, nodes, kids, r, lod = world
+    G, N = len(s.gaussians), len(nodes)
+    parts = s.parts.copy()
+    parts[1]["flags"] |= 2                                   # part 1 moves this frame
+    parts[1]["xf_prev"] = parts[1]["xf"]
+    parts[1]["xf_prev"][3] -= 0.4                            # from 0.4 m to the left
+    r.write_parts(parts)
+    try:
+        ref = lod.read()[0].copy()
+        for emit_part, blur in ((0, 0.0), (0xFFFFFFFF, 3.0), (2, 8.0)):
+            f = frame_lod(_frame(s, (1.0, -8.0, 4.0)), 2.0, N - G)
+            f["palette"][3][2] = 0.5                         # shutter
+            lod.select(f, emit_part=emit_part, blur_lod=blur)
+            oracle.lod_select(nodes, G, kids, parts, f, ref, emit_part=emit_part, blur_lod=blur)
+            assert np.array_equal(lod.read()[0], ref), (emit_part, blur)
+    finally:
+        r.write_parts(s.parts)
+
+
 @pytest.mark.parametrize("mode", [VIEW_FLAT, VIEW_OVERDRAW])
 def test_frame_with_cut_matches(world, mode):
     s, nodes, kids, r, lod = world
