@@ -775,6 +775,25 @@ def main():
     r.set_timing(False)
     stage_ms = {k: statistics.median(v) for k, v in stage.items()}
 
+    # the opacity maps rebuilt as when every part moved (light map A re-splatted, every sun layer re-splatted, then
+    # the shading pass): the per-frame lighting cost of a scene whose parts all move
+    all_parts = (1 << len(s.parts)) - 1
+    maps = []
+    for _ in range(5):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.update(s.eye, fwd, moved_mask=all_parts, stream=stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        maps.append(e0.elapsed_time(e1))
+    L.update(s.eye, fwd, stream=stream.cuda_stream)
+    lighting_maps = {"update_every_part_moved_ms": round(statistics.median(maps), 4),
+                     "shading_pass_only_ms": round(stage_ms["lighting"], 4),
+                     "maps": f"light map A {s.shadow_res}^2 per part ({len(s.parts)} parts), sun layers {s.sun_res}^2"}
+
     # end to end through the public API with host buffers: frame + parts up, image down (pinned), wall clock
     host_out = torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True)
     host_out_np = host_out.numpy()
@@ -859,7 +878,7 @@ def main():
                 "roofline": roofline, "sort_roofline": roof_sort, "composite_roofline": roof_comp,
                 "shade_roofline": roof_shade,
                 "cpu_baseline": cpu, "clocks": clocks, "batched": batch, "serving": serving,
-                "differentiation": differentiation, "sort": sort_leg, "lod": lod_leg}
+                "differentiation": differentiation, "sort": sort_leg, "lod": lod_leg, "lighting_maps": lighting_maps}
         print(json.dumps(line))
     L.close()
     r.close()

@@ -84,26 +84,87 @@ __device__ __forceinline__ m3 leaf_cov_world(const sl_gaussian& G, const float* 
   return m3m(t1, m3t(R));
 }
 
-__global__ void __launch_bounds__(kThreads) lsm_splat_kernel(const __grid_constant__ LightMapParams L,
-                                                             const sl_gaussian* __restrict__ gs,
-                                                             const sl_node* __restrict__ nodes,
-                                                             const sl_part* __restrict__ parts, uint32_t count,
-                                                             uint32_t* acc) {
-  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
-  if (g >= count) return;
+// One Gaussian's footprint in a map layer: the texels [x0, x1] x [y0, y1] around its centre ct (texels), the inverse of
+// its low-passed texel covariance Si, its peak optical depth, the depth at the centre and its gradient, the depth
+// variance along the light, the fixed-point scale and the layer's first texel.
+struct Foot {
+  m2 Si;
+  f2 ct, gz;
+  float tau0, zc, sz2, fix;
+  uint32_t base, res;
+  int x0, x1, y0, y1;
+};
+
+// One texel of a footprint: tau, tau z and tau (z^2 + sigma_z^2) in u32 fixed point, added atomically (the sums do
+// not depend on the order).  kSun: the depth falls along the gradient (sun layers), else it rises (map A).
+template <bool kSun>
+__device__ __forceinline__ void splat_texel(const Foot& F, int x, int y, uint32_t* acc) {
+  f2 dt = sub2(F2((float)x + 0.5f, (float)y + 0.5f), F.ct);
+  float q = dot2(dt, m2v(F.Si, dt));
+  if (q > 9.0f) return;
+  float tt = fminf(F.tau0 * sl_expf(-0.5f * q), 64.0f);
+  float t_fix = tt * F.fix;
+  if (t_fix < 0.5f) return;
+  float z = kSun ? fmaxf(F.zc - dot2(F.gz, dt), 0.0f) : fmaxf(F.zc + dot2(F.gz, dt), 0.0f);
+  uint32_t i = (F.base + (uint32_t)y * F.res + (uint32_t)x) * 3u;
+  atomicAdd(&acc[i], to_u32(t_fix + 0.5f));
+  atomicAdd(&acc[i + 1], to_u32(t_fix * z + 0.5f));
+  atomicAdd(&acc[i + 2], to_u32(t_fix * (z * z + F.sz2) + 0.5f));
+}
+
+__device__ __forceinline__ float shf(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ int shi(int v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+// A warp's 32 footprints (`mine` false for lanes without one): small ones (at most 16 texels) by their own lane, the
+// larger ones by the whole warp, one footprint at a time, a texel per lane -- footprints range from one texel to
+// 97 x 97, and a lane looping over a large one alone would hold its warp's other lanes idle.
+template <bool kSun>
+__device__ __forceinline__ void splat_warp(bool mine, const Foot& F, uint32_t* acc) {
+  const int w = F.x1 - F.x0 + 1, h = F.y1 - F.y0 + 1;
+  const int n = (mine && w > 0 && h > 0) ? w * h : 0;
+  if (n > 0 && n <= 16)
+    for (int y = F.y0; y <= F.y1; y++)
+      for (int x = F.x0; x <= F.x1; x++) splat_texel<kSun>(F, x, y, acc);
+  uint32_t big = __ballot_sync(0xffffffffu, n > 16);
+  const int lane = (int)(threadIdx.x & 31u);
+  while (big) {
+    const int src = __ffs(big) - 1;
+    big &= big - 1u;
+    Foot G;
+    G.Si.c[0] = F2(shf(F.Si.c[0].x, src), shf(F.Si.c[0].y, src));
+    G.Si.c[1] = F2(shf(F.Si.c[1].x, src), shf(F.Si.c[1].y, src));
+    G.ct = F2(shf(F.ct.x, src), shf(F.ct.y, src));
+    G.gz = F2(shf(F.gz.x, src), shf(F.gz.y, src));
+    G.tau0 = shf(F.tau0, src);
+    G.zc = shf(F.zc, src);
+    G.sz2 = shf(F.sz2, src);
+    G.fix = shf(F.fix, src);
+    G.base = (uint32_t)shi((int)F.base, src);
+    G.res = (uint32_t)shi((int)F.res, src);
+    G.x0 = shi(F.x0, src);
+    G.y0 = shi(F.y0, src);
+    const int gw = shi(w, src), gn = shi(n, src);
+    for (int k = lane; k < gn; k += 32) splat_texel<kSun>(G, G.x0 + k % gw, G.y0 + k / gw, acc);
+  }
+}
+
+// map A (light_shadow.wgsl:191-286): Gaussian g's footprint in its part's octahedral layer; false when it has none
+__device__ __forceinline__ bool lsm_foot(const LightMapParams& L, const sl_gaussian* __restrict__ gs,
+                                         const sl_node* __restrict__ nodes, const sl_part* __restrict__ parts,
+                                         uint32_t g, Foot& F) {
   const sl_gaussian& G = gs[g];
   const uint32_t p = G.part_surface & 0xFFFFu;
-  if (p >= L.part_count || p == L.skip_part || ((L.dirty >> p) & 1u) == 0u) return;
+  if (p >= L.part_count || p == L.skip_part || ((L.dirty >> p) & 1u) == 0u) return false;
   const float FIX = 65536.0f, LOWPASS = 0.3f;
   const float* xf = parts[p].xf;
   const Leaf nd = load_leaf(&nodes[g]);
   f3 m = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
   f3 dv = sub3(m, ld3(L.center));
   float r = len3(dv);
-  if (r < 1e-4f) return;
+  if (r < 1e-4f) return false;
   f3 w = div3(dv, r);
   m3 C = leaf_cov_world(G, xf);
-  if (L.hemi && dot3(dv, ld3(L.normal)) < -3.0f * sqrtf(dot3(ld3(L.normal), m3v(C, ld3(L.normal))))) return;
+  if (L.hemi && dot3(dv, ld3(L.normal)) < -3.0f * sqrtf(dot3(ld3(L.normal), m3v(C, ld3(L.normal))))) return false;
   f3 b0 = basis_k(w), b1 = cross3(w, b0);
   f3 c0 = m3v(C, b0), c1 = m3v(C, b1);
   float cbbx = dot3(b0, c0), cbby = dot3(b0, c1), cbbz = dot3(b1, c1);
@@ -137,21 +198,31 @@ __global__ void __launch_bounds__(kThreads) lsm_splat_kernel(const __grid_consta
   const int ires = (int)L.res;
   const int y0 = cy - hy > 0 ? cy - hy : 0, y1 = cy + hy < ires - 1 ? cy + hy : ires - 1;
   const int x0 = cx - hx > 0 ? cx - hx : 0, x1 = cx + hx < ires - 1 ? cx + hx : ires - 1;
-  for (int y = y0; y <= y1; y++) {
-    for (int x = x0; x <= x1; x++) {
-      f2 dt = sub2(F2((float)x + 0.5f, (float)y + 0.5f), ct);
-      float q = dot2(dt, m2v(Si, dt));
-      if (q > 9.0f) continue;
-      float tt = fminf(tau0 * sl_expf(-0.5f * q), 64.0f);
-      float t_fix = tt * FIX;
-      if (t_fix < 0.5f) continue;
-      float z = fmaxf(r + dot2(gz, dt), 0.0f);
-      uint32_t k = (base + (uint32_t)y * L.res + (uint32_t)x) * 3u;
-      atomicAdd(&acc[k], to_u32(t_fix + 0.5f));
-      atomicAdd(&acc[k + 1], to_u32(t_fix * z + 0.5f));
-      atomicAdd(&acc[k + 2], to_u32(t_fix * (z * z + sz2) + 0.5f));
-    }
-  }
+  F.Si = Si;
+  F.ct = ct;
+  F.gz = gz;
+  F.tau0 = tau0;
+  F.zc = r;
+  F.sz2 = sz2;
+  F.fix = FIX;
+  F.base = base;
+  F.res = L.res;
+  F.x0 = x0;
+  F.x1 = x1;
+  F.y0 = y0;
+  F.y1 = y1;
+  return true;
+}
+
+__global__ void __launch_bounds__(kThreads) lsm_splat_kernel(const __grid_constant__ LightMapParams L,
+                                                             const sl_gaussian* __restrict__ gs,
+                                                             const sl_node* __restrict__ nodes,
+                                                             const sl_part* __restrict__ parts, uint32_t count,
+                                                             uint32_t* acc) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  Foot F{};
+  const bool mine = g < count && lsm_foot(L, gs, nodes, parts, g, F);
+  splat_warp<false>(mine, F, acc);
 }
 
 // resolve: (alpha, alpha mu, alpha m2) per texel of every dirty layer (light_shadow.wgsl:290-304)
@@ -266,6 +337,61 @@ __global__ void __launch_bounds__(kThreads) lsm_lookup_kernel(const __grid_const
 
 // ---- sun maps ----------------------------------------------------------------------------------------------------
 
+// Gaussian g's footprint in sun layer l (sun_map.wgsl:127-219); false when it has none there
+__device__ __forceinline__ bool sm_foot(const SunParams& SP, const SunLayer* __restrict__ layers,
+                                        const sl_gaussian* __restrict__ gs, const sl_node* __restrict__ nodes,
+                                        const sl_part* __restrict__ parts, uint32_t g, uint32_t p, uint32_t l,
+                                        Foot& F) {
+  const sl_gaussian& G = gs[g];
+  const float SM_FIX = 4096.0f, SM_LOWPASS = 0.3f;
+  const SunLayer ly = layers[l];
+  if (!ly.dirty || !SP.lights[ly.light].shadows) return false;
+  const float* xf = parts[p].xf;
+  const Leaf nd = load_leaf(&nodes[g]);
+  f3 x = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  f3 w = ld3(SP.lights[ly.light].dir);
+  f3 b0 = ld3(ly.t1), b1 = ld3(ly.t2);
+  m3 C = leaf_cov_world(G, xf);
+  f3 c0 = m3v(C, b0), c1 = m3v(C, b1), cw = m3v(C, w);
+  m2 Cbb;
+  Cbb.c[0] = F2(dot3(b0, c0), dot3(b1, c0));
+  Cbb.c[1] = F2(dot3(b0, c1), dot3(b1, c1));
+  f2 cbz = F2(dot3(b0, cw), dot3(b1, cw));
+  m2 Cbb_i = m2inv(Cbb);
+  float sz2 = fmaxf(dot3(w, cw) - dot2(cbz, m2v(Cbb_i, cbz)), 1e-12f);
+  float tex = (float)SP.res / (2.0f * ly.half);
+  m2 Sm = m2s(Cbb, tex * tex);
+  float det0 = m2det(Sm);
+  Sm.c[0].x += SM_LOWPASS;
+  Sm.c[1].y += SM_LOWPASS;
+  float det1 = m2det(Sm);
+  float tau0 = nd.kappa * dirm(nd, xf_dir_inv(xf, w)) * sqrtf(2.0f * kPi * sz2) * sqrtf(fmaxf(det0, 0.0f) / det1);
+  m2 Si = m2inv(Sm);
+  float z0 = ly.zref - dot3(x, w);
+  f2 gz = div2(m2v(Cbb_i, cbz), tex);
+  f2 ct = F2((dot3(x, b0) - ly.c[0] + ly.half) * tex, (dot3(x, b1) - ly.c[1] + ly.half) * tex);
+  int hx = (int)ceilf(3.0f * sqrtf(Sm.c[0].x)), hy = (int)ceilf(3.0f * sqrtf(Sm.c[1].y));
+  hx = hx > 32 ? 32 : hx;
+  hy = hy > 32 ? 32 : hy;
+  int cx = (int)floorf(ct.x), cy = (int)floorf(ct.y);
+  const int ires = (int)SP.res;
+  F.Si = Si;
+  F.ct = ct;
+  F.gz = gz;
+  F.tau0 = tau0;
+  F.zc = z0;
+  F.sz2 = sz2;
+  F.fix = SM_FIX;
+  F.base = l * SP.res * SP.res;
+  F.res = SP.res;
+  F.y0 = cy - hy > 0 ? cy - hy : 0;
+  F.y1 = cy + hy < ires - 1 ? cy + hy : ires - 1;
+  F.x0 = cx - hx > 0 ? cx - hx : 0;
+  F.x1 = cx + hx < ires - 1 ? cx + hx : ires - 1;
+  return true;
+}
+
+// Every layer of the Gaussian's part, warp-uniformly: the j-th layer of each lane's part at step j.
 __global__ void __launch_bounds__(kThreads) sm_splat_kernel(const __grid_constant__ SunParams SP,
                                                             const SunLayer* __restrict__ layers,
                                                             const sl_gaussian* __restrict__ gs,
@@ -273,62 +399,19 @@ __global__ void __launch_bounds__(kThreads) sm_splat_kernel(const __grid_constan
                                                             const sl_part* __restrict__ parts, uint32_t count,
                                                             uint32_t* acc) {
   const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
-  if (g >= count) return;
-  const sl_gaussian& G = gs[g];
-  const uint32_t p = G.part_surface & 0xFFFFu;
-  if (p >= SP.n_parts) return;
-  const float SM_FIX = 4096.0f, SM_LOWPASS = 0.3f;
-  const uint32_t l_first = SP.part_first[p], l_end = l_first + SP.part_layers[p];
-  for (uint32_t l = l_first; l < l_end; l++) {
-    const SunLayer ly = layers[l];
-    if (!ly.dirty || !SP.lights[ly.light].shadows) continue;
-    const float* xf = parts[p].xf;
-    const Leaf nd = load_leaf(&nodes[g]);
-    f3 x = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
-    f3 w = ld3(SP.lights[ly.light].dir);
-    f3 b0 = ld3(ly.t1), b1 = ld3(ly.t2);
-    m3 C = leaf_cov_world(G, xf);
-    f3 c0 = m3v(C, b0), c1 = m3v(C, b1), cw = m3v(C, w);
-    m2 Cbb;
-    Cbb.c[0] = F2(dot3(b0, c0), dot3(b1, c0));
-    Cbb.c[1] = F2(dot3(b0, c1), dot3(b1, c1));
-    f2 cbz = F2(dot3(b0, cw), dot3(b1, cw));
-    m2 Cbb_i = m2inv(Cbb);
-    float sz2 = fmaxf(dot3(w, cw) - dot2(cbz, m2v(Cbb_i, cbz)), 1e-12f);
-    float tex = (float)SP.res / (2.0f * ly.half);
-    m2 Sm = m2s(Cbb, tex * tex);
-    float det0 = m2det(Sm);
-    Sm.c[0].x += SM_LOWPASS;
-    Sm.c[1].y += SM_LOWPASS;
-    float det1 = m2det(Sm);
-    float tau0 = nd.kappa * dirm(nd, xf_dir_inv(xf, w)) * sqrtf(2.0f * kPi * sz2) * sqrtf(fmaxf(det0, 0.0f) / det1);
-    m2 Si = m2inv(Sm);
-    float z0 = ly.zref - dot3(x, w);
-    f2 gz = div2(m2v(Cbb_i, cbz), tex);
-    f2 ct = F2((dot3(x, b0) - ly.c[0] + ly.half) * tex, (dot3(x, b1) - ly.c[1] + ly.half) * tex);
-    int hx = (int)ceilf(3.0f * sqrtf(Sm.c[0].x)), hy = (int)ceilf(3.0f * sqrtf(Sm.c[1].y));
-    hx = hx > 32 ? 32 : hx;
-    hy = hy > 32 ? 32 : hy;
-    int cx = (int)floorf(ct.x), cy = (int)floorf(ct.y);
-    const uint32_t base = l * SP.res * SP.res;
-    const int ires = (int)SP.res;
-    const int y0 = cy - hy > 0 ? cy - hy : 0, y1 = cy + hy < ires - 1 ? cy + hy : ires - 1;
-    const int x0 = cx - hx > 0 ? cx - hx : 0, x1 = cx + hx < ires - 1 ? cx + hx : ires - 1;
-    for (int y = y0; y <= y1; y++) {
-      for (int xx = x0; xx <= x1; xx++) {
-        f2 dt = sub2(F2((float)xx + 0.5f, (float)y + 0.5f), ct);
-        float q = dot2(dt, m2v(Si, dt));
-        if (q > 9.0f) continue;
-        float tt = fminf(tau0 * sl_expf(-0.5f * q), 64.0f);
-        float t_fix = tt * SM_FIX;
-        if (t_fix < 0.5f) continue;
-        float z = fmaxf(z0 - dot2(gz, dt), 0.0f);
-        uint32_t i = (base + (uint32_t)y * SP.res + (uint32_t)xx) * 3u;
-        atomicAdd(&acc[i], to_u32(t_fix + 0.5f));
-        atomicAdd(&acc[i + 1], to_u32(t_fix * z + 0.5f));
-        atomicAdd(&acc[i + 2], to_u32(t_fix * (z * z + sz2) + 0.5f));
-      }
+  uint32_t p = 0, l_first = 0, n_layers = 0;
+  if (g < count) {
+    p = gs[g].part_surface & 0xFFFFu;
+    if (p < SP.n_parts) {
+      l_first = SP.part_first[p];
+      n_layers = SP.part_layers[p];
     }
+  }
+  const uint32_t steps = __reduce_max_sync(0xffffffffu, n_layers);
+  for (uint32_t j = 0; j < steps; j++) {
+    Foot F{};
+    const bool mine = j < n_layers && sm_foot(SP, layers, gs, nodes, parts, g, p, l_first + j, F);
+    splat_warp<true>(mine, F, acc);
   }
 }
 
