@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
 // Batched: one block of 256 slots of one view; the view comes from block_view (kNoView: padding past the batch).
 // Keys carry the view above the 16 depth bits, so one stable sort orders every view's slots exactly as the per-view
 // sort does; lit radiance is filled in by the batched shading pass.
-__global__ void __launch_bounds__(kThreads) bproject_kernel(const BatchView* __restrict__ views,
+__global__ void __launch_bounds__(kThreads, 4) bproject_kernel(const BatchView* __restrict__ views,
                                                             const uint32_t* __restrict__ block_view,
                                                             uint32_t* __restrict__ keys32, SplatRec* __restrict__ recs,
                                                             ushort4* __restrict__ rects, uint32_t* __restrict__ digit_hist,
@@ -406,10 +406,12 @@ __global__ void __launch_bounds__(kThreads) bproject_kernel(const BatchView* __r
   }
   const int t = threadIdx.x;
   const BatchView& V = views[v];
-  {
+  {  // the frame's fields and the scene's parts only (every Gaussian's part is below part_count: checked at creation)
     const uint32_t* src = reinterpret_cast<const uint32_t*>(&V.P);
     uint32_t* dst = reinterpret_cast<uint32_t*>(&sP);
-    for (uint32_t k = t; k < sizeof(ProjectParams) / 4; k += kThreads) dst[k] = src[k];
+    const uint32_t np = V.P.part_count < kMaxParts ? V.P.part_count : kMaxParts;
+    const uint32_t words = (uint32_t)((offsetof(ProjectParams, parts) + np * sizeof(PartXf)) / 4);
+    for (uint32_t k = t; k < words; k += kThreads) dst[k] = src[k];
   }
   h[0][t] = 0u;
   h[1][t] = 0u;
