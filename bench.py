@@ -592,9 +592,9 @@ def run_diff(args, stream, flush):
             "grad_norms": {k: round(v, 6) for k, v in gnorm.items()}}
 
 
-# bproject, scan and compaction of the visible keys, 3 depth-sort passes, tile counts, scan, emit, 2 tile-sort passes,
-# runs (to ranges), coverage pass, shading flags, scan, compact, bshade, bcomposite
-BATCH_KERNELS = 19
+# bproject, scan and compaction of the visible keys, 3 depth-sort passes, binning (counts, offsets and entries in one
+# pass), 2 tile-sort passes, runs (to ranges), coverage pass, shading flags, scan, compact, bshade, bcomposite
+BATCH_KERNELS = 17
 
 
 def run_reference(args):

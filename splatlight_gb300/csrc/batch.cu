@@ -14,61 +14,117 @@ namespace {
 
 constexpr int kThreads = 256;
 
-__global__ void __launch_bounds__(kThreads) btile_count_kernel(const uint32_t* __restrict__ order,
-                                                               const ushort4* __restrict__ rects,
-                                                               const SplatRec* __restrict__ recs,
-                                                               const uint32_t* __restrict__ totals, uint32_t n_max,
-                                                               uint32_t tw, uint32_t th,
-                                                               uint32_t* __restrict__ counts) {
-  const uint32_t p = blockIdx.x * kThreads + threadIdx.x;
-  const bool mine = p < n_max && p < totals[0];
-  ushort4 r = make_ushort4(1, 1, 0, 0);
-  SplatRec rec{};
-  if (mine) {
-    const uint32_t slot = order[p];
-    r = rects[slot];
-    if (r.x <= r.z && r.y <= r.w) rec = recs[slot];  // culled slots (empty rectangle) need no record
-  }
-  const uint32_t c = count_warp(mine, r, rec, tw, th);
-  if (p < n_max) counts[p] = c;
+constexpr uint64_t kBinAgg = 1ull << 32;     // status word: the block's own entry count is published
+constexpr uint64_t kBinPrefix = 2ull << 32;  // status word: the entries of every block up to this one
+constexpr uint32_t kBinSpinLimit = 1u << 22;
+
+__device__ __forceinline__ uint64_t load_relaxed64(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
 }
 
-// Entries of the batch: key (view << 16) | view-local tile id, value the slot; digit counts of the local id.
-__global__ void __launch_bounds__(kThreads) btile_emit_kernel(const uint32_t* __restrict__ order,
-                                                              const ushort4* __restrict__ rects,
-                                                              const SplatRec* __restrict__ recs,
-                                                              const uint32_t* __restrict__ offsets,
-                                                              const uint32_t* __restrict__ counts,
-                                                              const BatchView* __restrict__ views,
-                                                              const uint32_t* __restrict__ block_view,
-                                                              const uint32_t* __restrict__ totals, uint32_t n_max,
-                                                              uint32_t tw, uint32_t th, uint32_t capacity,
-                                                              FrameCounters* ctr, uint32_t* __restrict__ tile_keys,
-                                                              uint32_t* __restrict__ tile_vals,
-                                                              uint32_t* __restrict__ digit_hist) {
+// The binning of the batch in one pass over the depth-sorted visible splats: each block of 256 sorted positions
+// counts its splats' tile entries (the per-row spans), learns the entries of every earlier block by a decoupled
+// look-back over per-block status words (blocks take their positions from a ticket counter, so every earlier block is
+// already running and the wait ends), and writes its entries: key (view << 16) | view-local tile id, value the slot,
+// at the running offset, so entries stay in sorted (view, depth) order.  The digit counts of the local id go to
+// digit_hist for the tile sort; the last block writes the batch's entry total (which may exceed capacity: the entries
+// past it are not written and the overflow flag is set).
+__global__ void __launch_bounds__(kThreads) btile_bin_kernel(const uint32_t* __restrict__ order,
+                                                             const ushort4* __restrict__ rects,
+                                                             const SplatRec* __restrict__ recs,
+                                                             const BatchView* __restrict__ views,
+                                                             const uint32_t* __restrict__ block_view,
+                                                             const uint32_t* __restrict__ n_dev, uint32_t n_max,
+                                                             uint32_t tw, uint32_t th, uint32_t capacity,
+                                                             FrameCounters* ctr, uint32_t* __restrict__ tile_keys,
+                                                             uint32_t* __restrict__ tile_vals,
+                                                             uint32_t* __restrict__ digit_hist, uint32_t* ticket,
+                                                             uint64_t* status) {
   __shared__ uint32_t h_lo[256], h_hi[256], warp_tot[kThreads / 32];
-  const int t = threadIdx.x;
+  __shared__ uint32_t s_blk, s_excl;
+  const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
+  const uint32_t nd = *n_dev;
+  const uint32_t n = nd < n_max ? nd : n_max;
+  if (t == 0) s_blk = atomicAdd(ticket, 1u);
   RunHist16 hh{h_lo, h_hi};  // the digits of the 16-bit view-local tile id
   hh.clear();
   __syncthreads();
-  const uint32_t p = blockIdx.x * kThreads + t;
-  bool mine = false;
-  uint32_t slot = 0, e0 = 0, cnt = 0, base = 0, stride = 0;
+  const uint32_t blk = s_blk;
+  if (blk * kThreads >= n) return;  // past the visible positions (the whole block)
+  const uint32_t p = blk * kThreads + t;
+  const bool in = p < n;
+  uint32_t slot = 0;
   ushort4 r = make_ushort4(1, 1, 0, 0);
   SplatRec rec{};
-  if (p < n_max && p < totals[0]) {
-    cnt = counts[p];
-    if (cnt) {
-      slot = order[p];
-      r = rects[slot];
-      rec = recs[slot];
-      e0 = offsets[p];
-      const uint32_t v = block_view[slot >> 8];
-      base = v << 16;  // key: view above its local tile id
-      stride = views[v].tiles_x;
-      if (e0 + cnt > capacity) atomicExch(&ctr->overflow, 1u);
-      else mine = true;
+  if (in) {
+    slot = order[p];
+    r = rects[slot];
+    if (r.x <= r.z && r.y <= r.w) rec = recs[slot];  // culled slots (empty rectangle) need no record
+  }
+  const uint32_t cnt = count_warp(in, r, rec, tw, th);
+  uint32_t base = 0, stride = 0;
+  if (cnt) {  // the view's tile-id base and row stride, fetched while the block waits for its offset
+    const uint32_t v = block_view[slot >> 8];
+    base = v << 16;
+    stride = views[v].tiles_x;
+  }
+
+  // block-wide exclusive scan of the counts, then the offset of the block from the look-back
+  uint32_t x = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31u) warp_tot[w] = x;
+  __syncthreads();
+  uint32_t wbase = 0, agg = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kThreads / 32; k++) {
+    const uint32_t tt = warp_tot[k];
+    wbase += k < w ? tt : 0u;
+    agg += tt;
+  }
+  if (w == 0) {  // warp 0: the look-back, 32 predecessors' status words per step (nearest in lane 0)
+    if (lane == 0)
+      atomicExch(reinterpret_cast<unsigned long long*>(status + blk),
+                 (unsigned long long)((blk == 0 ? kBinPrefix : kBinAgg) | agg));
+    uint32_t excl = 0;
+    int32_t top = (int32_t)blk - 1;
+    uint32_t spins = 0;
+    while (top >= 0) {
+      const int32_t j = top - (int32_t)lane;
+      const uint64_t st = j >= 0 ? load_relaxed64(status + j) : kBinPrefix;  // before block 0: a prefix of 0
+      const uint32_t flag = (uint32_t)(st >> 32);
+      const uint32_t pm = __ballot_sync(0xffffffffu, flag == 2u), zm = __ballot_sync(0xffffffffu, flag == 0u);
+      const uint32_t pfirst = pm ? (uint32_t)__ffs(pm) - 1u : 32u, zfirst = zm ? (uint32_t)__ffs(zm) - 1u : 32u;
+      if (zfirst < pfirst) {  // a nearer block has not published yet: read the window again
+        if (++spins > kBinSpinLimit) {
+          if (lane == 0) atomicExch(&ctr->timeout, 1u);
+          break;
+        }
+        __nanosleep(32);
+        continue;
+      }
+      excl += __reduce_add_sync(0xffffffffu, lane <= pfirst ? (uint32_t)st : 0u);
+      if (pm) break;
+      top -= 32;
     }
+    if (lane == 0) {
+      if (blk != 0)
+        atomicExch(reinterpret_cast<unsigned long long*>(status + blk), (unsigned long long)(kBinPrefix | (excl + agg)));
+      s_excl = excl;
+      if ((blk + 1u) * kThreads >= n) ctr->entries = excl + agg;  // the last block
+    }
+  }
+  __syncthreads();
+  const uint32_t e0 = s_excl + wbase + x - cnt;
+  bool mine = false;
+  if (cnt) {
+    if (e0 + cnt > capacity) atomicExch(&ctr->overflow, 1u);
+    else mine = true;
   }
   emit_warp<uint32_t>(mine, slot, r, rec, e0, cnt, tw, th, base, stride, tile_keys, tile_vals, hh);
   __syncthreads();
@@ -171,24 +227,20 @@ cudaError_t launch_bcompact(const uint32_t* block_view, const uint32_t* keys32, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_btile_count(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
-                               const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t* counts,
-                               cudaStream_t s) {
-  if (!n_max) return cudaSuccess;
-  btile_count_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(order, rects, recs, totals, n_max, tw, th,
-                                                                            counts);
-  return cudaGetLastError();
-}
+size_t btile_bin_scratch_bytes(uint32_t n_max) { return 16 + 8ull * ((n_max + kThreads - 1) / kThreads + 1); }
 
-cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
-                              const uint32_t* offsets, const uint32_t* counts, const BatchView* views,
-                              const uint32_t* block_view, const uint32_t* totals, uint32_t n_max, uint32_t tw,
-                              uint32_t th, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
-                              uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s) {
+cudaError_t launch_btile_bin(const uint32_t* order, const ushort4* rects, const SplatRec* recs, const BatchView* views,
+                             const uint32_t* block_view, const uint32_t* n_dev, uint32_t n_max, uint32_t tw,
+                             uint32_t th, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
+                             uint32_t* tile_vals, uint32_t* digit_hist, void* scratch, cudaStream_t s) {
   if (!n_max) return cudaSuccess;
-  btile_emit_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(
-      order, rects, recs, offsets, counts, views, block_view, totals, n_max, tw, th, capacity, ctr, tile_keys,
-      tile_vals, digit_hist);
+  const uint32_t blocks = (n_max + kThreads - 1) / kThreads;
+  cudaError_t e = cudaMemsetAsync(scratch, 0, btile_bin_scratch_bytes(n_max), s);
+  if (e != cudaSuccess) return e;
+  uint32_t* ticket = reinterpret_cast<uint32_t*>(scratch);
+  uint64_t* status = reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(scratch) + 16);
+  btile_bin_kernel<<<blocks, kThreads, 0, s>>>(order, rects, recs, views, block_view, n_dev, n_max, tw, th, capacity,
+                                               ctr, tile_keys, tile_vals, digit_hist, ticket, status);
   return cudaGetLastError();
 }
 

@@ -98,6 +98,7 @@ cudaError_t allocate(sl_batch* b) {
   ENS(b->rects, 8 * S);
   ENS(b->slot_counts, 4 * S + 16);
   ENS(b->slot_offsets, 4 * S + 16);
+  ENS(b->bin_scratch, btile_bin_scratch_bytes((uint32_t)S));
   ENS(b->tile_keys, 4 * E + 16);
   ENS(b->tile_keys_alt, 4 * E + 16);
   ENS(b->tile_vals, 4 * E + 16);
@@ -162,15 +163,9 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   CK(sort32_pairs(b->tile_keys.as<uint32_t>(), b->keys_alt.as<uint32_t>(), b->tile_vals.as<uint32_t>(),
                   b->order.as<uint32_t>(), b->vals_alt.as<uint32_t>(), S, n_visible, 16 + bits_for(V - 1), hist,
                   b->status.as<uint32_t>(), b->tile_ctr.as<uint32_t>(), max_tiles_sort, ctr, s));
-  CK(launch_btile_count(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->recs.as<SplatRec>(), n_visible, S,
-                        b->tile_w, b->tile_h, b->slot_counts.as<uint32_t>(), s));
-  CK(exclusive_scan_u32(b->slot_counts.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), S, &ctr->entries,
-                        b->scan_scratch.ptr, ctr, s));
-  CK(launch_btile_emit(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->recs.as<SplatRec>(),
-                       b->slot_offsets.as<uint32_t>(), b->slot_counts.as<uint32_t>(), b->views.as<BatchView>(),
-                       b->block_view.as<uint32_t>(), n_visible,
-                       S, b->tile_w, b->tile_h, E, ctr,
-                       b->tile_keys.as<uint32_t>(), b->tile_vals.as<uint32_t>(), hist + 768, s));
+  CK(launch_btile_bin(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->recs.as<SplatRec>(), b->views.as<BatchView>(),
+                      b->block_view.as<uint32_t>(), n_visible, S, b->tile_w, b->tile_h, E, ctr,
+                      b->tile_keys.as<uint32_t>(), b->tile_vals.as<uint32_t>(), hist + 768, b->bin_scratch.ptr, s));
   // the tile sort: stable on the 16-bit view-local tile id (two passes); entries arrive in (view, depth) order, so
   // each (view, tile) run comes out contiguous and depth-ordered
   CK(sort32_pairs(b->tile_keys.as<uint32_t>(), b->tile_keys_alt.as<uint32_t>(), b->tile_vals.as<uint32_t>(),
@@ -533,7 +528,7 @@ int sl_batch_destroy(sl_batch* b) {
   sl::DevBuf* all[] = {&b->views, &b->views_out, &b->block_view, &b->scenes_dev, &b->dyn, &b->keys32, &b->keys_alt,
                        &b->vals_alt, &b->order, &b->recs, &b->rects, &b->slot_counts, &b->slot_offsets,
                        &b->tile_keys, &b->tile_keys_alt, &b->tile_vals, &b->tile_vals_alt, &b->status, &b->tile_ctr,
-                       &b->hist, &b->scan_scratch, &b->block_valid, &b->block_off,
+                       &b->hist, &b->scan_scratch, &b->bin_scratch, &b->block_valid, &b->block_off,
                        &b->ranges, &b->counters, &b->view_maxrad, &b->view_visible, &b->marks,
                        &b->view_tmark};
   for (sl::DevBuf* x : all) x->release();

@@ -219,14 +219,13 @@ cudaError_t launch_bcomposite(const BatchComposite& B, const uint2* ranges, cons
                               const SplatRec* recs, const BatchViewOut* views, const uint32_t* view_maxrad,
                               const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s);
 // batch.cu (totals: the BatchDyn, read as u32 words: [0] total slots, [1] total tiles)
-cudaError_t launch_btile_count(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
-                               const uint32_t* totals, uint32_t n_max, uint32_t tw, uint32_t th, uint32_t* counts,
-                               cudaStream_t s);
-cudaError_t launch_btile_emit(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
-                              const uint32_t* offsets, const uint32_t* counts, const BatchView* views,
-                              const uint32_t* block_view, const uint32_t* totals, uint32_t n_max, uint32_t tw,
-                              uint32_t th, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
-                              uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s);
+// batch.cu: the batch's tile entries in one pass (counts, their ordered offsets by a decoupled look-back, emission);
+// the entry total goes to ctr->entries.  scratch: btile_bin_scratch_bytes(n_max) bytes, cleared by the launcher.
+size_t btile_bin_scratch_bytes(uint32_t n_max);
+cudaError_t launch_btile_bin(const uint32_t* order, const ushort4* rects, const SplatRec* recs, const BatchView* views,
+                             const uint32_t* block_view, const uint32_t* n_dev, uint32_t n_max, uint32_t tw,
+                             uint32_t th, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
+                             uint32_t* tile_vals, uint32_t* digit_hist, void* scratch, cudaStream_t s);
 // The batched coverage pass over the tiles of lit views, run between binning and shading: marks[slot] = 1 for each
 // splat that blends a fragment before the pixel's transmittance falls below t_mark (BatchViewOut::lit 1) or at all
 // (lit 2).  t_mark = t_stop_scale / max(2 r, rad_cap), r the view's radiance bound so far (its unshaded splats,
