@@ -594,7 +594,7 @@ def run_diff(args, stream, flush):
 
 # bproject, scan and compaction of the visible keys, 3 depth-sort passes, binning (counts, offsets and entries in one
 # pass), 2 tile-sort passes, runs (to ranges), coverage pass, shading flags, scan, compact, bshade, bcomposite
-BATCH_KERNELS = 17
+BATCH_KERNELS = 16
 
 
 def run_reference(args):

@@ -82,6 +82,29 @@ def test_ragged_mix_equals_per_view(cuda, tile):
                 _assert_view(B, k, v, [ra, rb][v.scene], tile)
 
 
+def test_view_with_nothing_visible(cuda):
+    """A camera turned away from its scene: no visible splat, so the binning emits no entry (every block of the
+    one-pass binning is past the visible count and the entry total stays 0); alone and between other views it gives
+    the per-view path's empty image, lists and ranges."""
+    a, b = _scenes()
+    away = tuple(2.0 * np.asarray(a.eye, np.float64) - np.asarray(a.target, np.float64))
+    with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
+        ra.set_emitters(a.emitters)
+        rb.set_emitters(b.emitters)
+        with BatchRenderer([ra, rb], max_views=16) as B:
+            empty = View(0, _frame(a, 200, 150, VIEW_FLAT, target=away), a.eye)
+            img = _render(B, [empty])[0]
+            assert B.last_stats.entries == 0
+            assert not img.any()
+            _assert_view(B, 0, empty, ra, (16, 16))
+            views = _views(a, b)
+            mix = views[:3] + [empty] + views[3:]
+            _render(B, mix)
+            assert B.last_stats.entries > 0
+            for k, v in enumerate(mix):
+                _assert_view(B, k, v, [ra, rb][v.scene], (16, 16))
+
+
 def test_alone_and_in_mix(cuda):
     a, b = _scenes()
     with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
