@@ -82,6 +82,10 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
   __shared__ SplatRec buf[2][kThreads];
   __shared__ uint32_t sslot[kMark ? 2 : 1][kMark ? kThreads : 1];  // coverage pass: the slots of the batch
   __shared__ uint8_t smark[kMark ? 2 : 1][kMark ? kThreads : 1];    // coverage pass: the batch's blended records
+  // coverage pass: per record of the batch, (g0, o0, tau0 log2 e) and (g1, o1, qcut'), with o = -g . (centre - tile
+  // origin), so a fragment's lx = g0 . (pixel - tile origin) + o0 is two FMAs (written by the record's thread in the
+  // culling step, read after its barrier; the next batch rewrites it only after the batch's closing barrier)
+  __shared__ float4 mrec[kMark ? 2 * kThreads : 1];
   __shared__ uint32_t masks[kThreads / 32][kThreads / 32];  // [warp block][loader warp]: records touching the block
   __shared__ __align__(8) uint64_t bars[2];
 
@@ -101,9 +105,14 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
 
   const uint32_t n_batches = (e - s + kThreads - 1) / kThreads;
   const float pxc = (float)px + 0.5f, pyc = (float)py + 0.5f;
+  const float pxr = (float)(px - x0) + 0.5f, pyr = (float)(py - y0) + 0.5f;  // relative to the tile's origin
   const float fx0 = (float)x0, fy0 = (float)y0;
   const float kNegHalfLog2e = -0.72134752044448170f;
   const float kNegLog2e = -1.44269504088896341f;
+  // coverage pass: its keep test evaluates q in tile-relative coordinates (a few ulps away from the composite's q, whose
+  // rounding it need not match), so it keeps fragments up to a cutoff 1e-4 (relative) above the composite's: every
+  // fragment the composite blends is marked
+  const float kMarkCutScale = 1.0001f;
 
   float T = 1.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f;
   uint32_t kept = 0;
@@ -157,6 +166,12 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
         const uint32_t row = ((2u << bx1) - 1u) & ~((1u << bx0) - 1u);
         for (int by = by0; by <= by1; by++) bits |= row << (by * BX);
       }
+      if constexpr (kMark) {
+        const float4 B = rb[t].b;
+        const float cxr = A.x - fx0, cyr = A.y - fy0;
+        mrec[2 * t] = make_float4(A.z, A.w, -(A.z * cxr + A.w * cyr), rb[t].c.w * kNegLog2e);
+        mrec[2 * t + 1] = make_float4(B.x, B.y, -(B.x * cxr + B.y * cyr), B.w * kMarkCutScale);
+      }
     }
 #pragma unroll
     for (int k = 0; k < kThreads / 32; k++) {
@@ -171,19 +186,25 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
         while (m) {
           const uint32_t j = (uint32_t)(lw * 32 + __ffs(m) - 1);
           m &= m - 1u;
+          if constexpr (kMark) {
+            const float4 P0 = mrec[2 * j], P1 = mrec[2 * j + 1];
+            const float lx = fmaf(pxr, P0.x, fmaf(pyr, P0.y, P0.z));
+            const float ly = fmaf(pxr, P1.x, fmaf(pyr, P1.y, P1.z));
+            const float q = fmaf(lx, lx, ly * ly);
+            if (alive && q <= P1.w) {
+              l2T = fmaf(P0.w, ex2_approx(q * kNegHalfLog2e), l2T);
+              smark[b & 1u][j] = 1u;
+              if (l2T < l2stop) alive = false;
+            }
+            continue;
+          }
           const float4 A = rb[j].a;
           const float4 B = rb[j].b;
           const float dx = pxc - A.x, dy = pyc - A.y;
           const float lx = fmaf(dx, A.z, dy * A.w);
           const float ly = fmaf(dx, B.x, dy * B.y);
           const float q = fmaf(lx, lx, ly * ly);
-          if constexpr (kMark) {
-            if (alive && q <= B.w) {
-              l2T = fmaf(rb[j].c.w * kNegLog2e, ex2_approx(q * kNegHalfLog2e), l2T);
-              smark[b & 1u][j] = 1u;
-              if (l2T < l2stop) alive = false;
-            }
-          } else if (alive && q <= B.w) {
+          if (alive && q <= B.w) {
             const float4 C = rb[j].c;
             const float ev = ex2_approx(q * kNegHalfLog2e);
             const float alpha = 1.0f - ex2_approx(C.w * kNegLog2e * ev);
