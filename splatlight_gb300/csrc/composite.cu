@@ -82,8 +82,9 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
   __shared__ SplatRec buf[2][kThreads];
   __shared__ uint32_t sslot[kMark ? 2 : 1][kMark ? kThreads : 1];  // coverage pass: the slots of the batch
   __shared__ uint8_t smark[kMark ? 2 : 1][kMark ? kThreads : 1];    // coverage pass: the batch's blended records
-  // coverage pass: per record of the batch, (g0, o0, tau0 log2 e) and (g1, o1, qcut'), with o = -g . (centre - tile
-  // origin), so a fragment's lx = g0 . (pixel - tile origin) + o0 is two FMAs (written by the record's thread in the
+  // coverage pass: per record of the batch, (g0, o0, -tau0 log2 e) and (g1, o1, qcut'), with o = -g . (centre - tile
+  // origin), so a fragment's lx = g0 . (pixel - tile origin) + o0 is two FMAs (g, o and the cutoff scaled to give q in
+  // units of the exponent of 2) (written by the record's thread in the
   // culling step, read after its barrier; the next batch rewrites it only after the batch's closing barrier)
   __shared__ float4 mrec[kMark ? 2 * kThreads : 1];
   __shared__ uint32_t masks[kThreads / 32][kThreads / 32];  // [warp block][loader warp]: records touching the block
@@ -169,8 +170,12 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
       if constexpr (kMark) {
         const float4 B = rb[t].b;
         const float cxr = A.x - fx0, cyr = A.y - fy0;
-        mrec[2 * t] = make_float4(A.z, A.w, -(A.z * cxr + A.w * cyr), rb[t].c.w * kNegLog2e);
-        mrec[2 * t + 1] = make_float4(B.x, B.y, -(B.x * cxr + B.y * cyr), B.w * kMarkCutScale);
+        // gradients and offsets scaled by sqrt(log2(e) / 2): q comes out as (q / 2) log2 e, the exponent of 2 the
+        // fragment's exp(-q / 2) needs, and the cutoff is scaled alike
+        const float ks = 0.84932180f;
+        mrec[2 * t] = make_float4(A.z * ks, A.w * ks, -(A.z * cxr + A.w * cyr) * ks, rb[t].c.w * kNegLog2e);
+        mrec[2 * t + 1] = make_float4(B.x * ks, B.y * ks, -(B.x * cxr + B.y * cyr) * ks,
+                                      B.w * kMarkCutScale * -kNegHalfLog2e);
       }
     }
 #pragma unroll
@@ -192,7 +197,7 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
             const float ly = fmaf(pxr, P1.x, fmaf(pyr, P1.y, P1.z));
             const float q = fmaf(lx, lx, ly * ly);
             if (alive && q <= P1.w) {
-              l2T = fmaf(P0.w, ex2_approx(q * kNegHalfLog2e), l2T);
+              l2T = fmaf(P0.w, ex2_approx(-q), l2T);
               smark[b & 1u][j] = 1u;
               if (l2T < l2stop) alive = false;
             }
