@@ -593,8 +593,8 @@ def run_diff(args, stream, flush):
 
 
 # bproject, scan and compaction of the visible keys, 3 depth-sort passes, binning (counts, offsets and entries in one
-# pass), 2 tile-sort passes, runs (to ranges), coverage pass, shading flags, scan, compact, bshade, bcomposite
-BATCH_KERNELS = 16
+# pass), 2 tile-sort passes, runs (to ranges), coverage pass, shading list (one pass), bshade, bcomposite
+BATCH_KERNELS = 14
 
 
 def run_reference(args):

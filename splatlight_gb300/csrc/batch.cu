@@ -147,31 +147,44 @@ __device__ __forceinline__ bool shade_candidate(const BatchView* views, const Ba
   return marks[gslot] != 0u;
 }
 
-__global__ void __launch_bounds__(kThreads) bshade_flags_kernel(const BatchView* __restrict__ views,
-                                                                const BatchScene* __restrict__ scenes,
-                                                                const uint32_t* __restrict__ block_view,
-                                                                const uint8_t* __restrict__ marks,
-                                                                const uint32_t* __restrict__ totals, uint32_t n_max,
-                                                                uint32_t* __restrict__ flags) {
-  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
-  if (g >= n_max) return;
-  uint32_t v, gslot;
-  flags[g] = (g < totals[0] && shade_candidate(views, scenes, block_view, marks, g, v, gslot)) ? 1u : 0u;
-}
-
-__global__ void __launch_bounds__(kThreads) bshade_compact_kernel(const BatchView* __restrict__ views,
-                                                                  const BatchScene* __restrict__ scenes,
-                                                                  const uint32_t* __restrict__ block_view,
-                                                                  const uint32_t* __restrict__ flags,
-                                                                  const uint32_t* __restrict__ offsets,
-                                                                  const uint32_t* __restrict__ totals, uint32_t n_max,
-                                                                  uint32_t* __restrict__ list) {
-  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
-  if (g >= n_max || g >= totals[0] || !flags[g]) return;
-  const uint32_t v = block_view[g >> 8];
-  const BatchView& V = views[v];
-  const uint32_t j = g - V.slot_base;
-  list[V.slot_base + (offsets[g] - offsets[V.slot_base])] = V.slot_base + scenes[V.scene].order[j];
+// The shading list of the batch in one pass over the padded slots: each block of 256 slots (one view's) flags the
+// Gaussians of its positions in shading order that the coverage pass marked, takes a range of the view's list for
+// them with one atomic add on view_shade[view] (zeroed beforehand; it ends as the view's count) and writes their
+// global slots there in shading order, adding its count to ctr->shade_n.  Blocks claim their ranges in any order:
+// each Gaussian is shaded on its own and the view's radiance bound is a maximum, so the order of the list changes no
+// result; within a block the entries keep the shading order, which keeps a warp's Gaussians close together.
+__global__ void __launch_bounds__(kThreads) bshade_list_kernel(const BatchView* __restrict__ views,
+                                                               const BatchScene* __restrict__ scenes,
+                                                               const uint32_t* __restrict__ block_view,
+                                                               const uint8_t* __restrict__ marks,
+                                                               const uint32_t* __restrict__ totals,
+                                                               FrameCounters* ctr, uint32_t* __restrict__ list,
+                                                               uint32_t* __restrict__ view_shade) {
+  __shared__ uint32_t warp_n[kThreads / 32];
+  __shared__ uint32_t s_base;
+  const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
+  const uint32_t v = block_view[blockIdx.x];
+  if (v == kNoView) return;  // padding past the batch (the whole block)
+  const uint32_t g = blockIdx.x * kThreads + t;
+  uint32_t vv = 0, gslot = 0;
+  const bool f = g < totals[0] && shade_candidate(views, scenes, block_view, marks, g, vv, gslot);
+  const uint32_t m = __ballot_sync(0xffffffffu, f);
+  if (lane == 0) warp_n[w] = __popc(m);
+  __syncthreads();
+  uint32_t wbase = 0, agg = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kThreads / 32; k++) {
+    const uint32_t c = warp_n[k];
+    wbase += k < w ? c : 0u;
+    agg += c;
+  }
+  if (agg == 0) return;  // the whole block
+  if (t == 0) {
+    s_base = atomicAdd(&view_shade[v], agg);
+    atomicAdd(&ctr->shade_n, agg);
+  }
+  __syncthreads();
+  if (f) list[views[v].slot_base + s_base + wbase + __popc(m & ((1u << lane) - 1u))] = gslot;
 }
 
 // After the stable sort on the local tile id the entries run in (local tile, view, depth) order: every (view, tile)
@@ -244,21 +257,13 @@ cudaError_t launch_btile_bin(const uint32_t* order, const ushort4* rects, const 
   return cudaGetLastError();
 }
 
-cudaError_t launch_bshade_flags(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
-                                const uint8_t* marks, const uint32_t* totals, uint32_t n_max, uint32_t* flags,
-                                cudaStream_t s) {
-  if (!n_max) return cudaSuccess;
-  bshade_flags_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(views, scenes, block_view, marks, totals,
-                                                                             n_max, flags);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_bshade_compact(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
-                                  const uint32_t* flags, const uint32_t* offsets, const uint32_t* totals,
-                                  uint32_t n_max, uint32_t* list, cudaStream_t s) {
-  if (!n_max) return cudaSuccess;
-  bshade_compact_kernel<<<(n_max + kThreads - 1) / kThreads, kThreads, 0, s>>>(views, scenes, block_view, flags,
-                                                                               offsets, totals, n_max, list);
+cudaError_t launch_bshade_list(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
+                               const uint8_t* marks, const uint32_t* totals, uint32_t max_blocks, uint32_t n_views,
+                               FrameCounters* ctr, uint32_t* list, uint32_t* view_shade, cudaStream_t s) {
+  if (!max_blocks) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(view_shade, 0, 4ull * n_views, s);
+  if (e != cudaSuccess) return e;
+  bshade_list_kernel<<<max_blocks, kThreads, 0, s>>>(views, scenes, block_view, marks, totals, ctr, list, view_shade);
   return cudaGetLastError();
 }
 

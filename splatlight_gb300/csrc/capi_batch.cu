@@ -115,6 +115,7 @@ cudaError_t allocate(sl_batch* b) {
   ENS(b->block_off, 4ull * B + 16);
   ENS(b->marks, S + 16);
   ENS(b->view_tmark, 4ull * V + 16);
+  ENS(b->view_shade, 4ull * V + 16);
 #undef ENS
   if ((e = cudaMallocHost((void**)&b->h_views, sizeof(BatchView) * V)) != cudaSuccess) return e;
   if ((e = cudaMallocHost((void**)&b->h_out, sizeof(BatchViewOut) * V)) != cudaSuccess) return e;
@@ -180,16 +181,12 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   CK(launch_bmark(C, b->ranges.as<uint2>(), b->tile_vals.as<uint32_t>(), b->recs.as<SplatRec>(),
                   b->views_out.as<BatchViewOut>(), b->view_maxrad.as<uint32_t>(), b->dyn.as<BatchDyn>(), T, ctr,
                   b->marks.as<uint8_t>(), b->view_tmark.as<float>(), s));
-  CK(launch_bshade_flags(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(),
-                         b->marks.as<uint8_t>(), totals, S, b->slot_counts.as<uint32_t>(), s));
-  CK(exclusive_scan_u32(b->slot_counts.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), S, &ctr->shade_n,
-                        b->scan_scratch.ptr, ctr, s));
-  CK(launch_bshade_compact(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(),
-                           b->slot_counts.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), totals, S,
-                           b->vals_alt.as<uint32_t>(), s));
+  CK(launch_bshade_list(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(),
+                        b->marks.as<uint8_t>(), totals, B, V, ctr, b->vals_alt.as<uint32_t>(),
+                        b->view_shade.as<uint32_t>(), s));
   CK(launch_bshade(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(), B,
-                   b->vals_alt.as<uint32_t>(), b->slot_offsets.as<uint32_t>(), &ctr->shade_n, b->dyn.as<BatchDyn>(),
-                   b->recs.as<SplatRec>(), b->view_maxrad.as<uint32_t>(), s));
+                   b->vals_alt.as<uint32_t>(), b->view_shade.as<uint32_t>(), b->recs.as<SplatRec>(),
+                   b->view_maxrad.as<uint32_t>(), s));
   CK(launch_bcomposite(C, b->ranges.as<uint2>(), b->tile_vals.as<uint32_t>(), b->recs.as<SplatRec>(),
                        b->views_out.as<BatchViewOut>(), b->view_maxrad.as<uint32_t>(), b->dyn.as<BatchDyn>(), T, ctr,
                        s));
@@ -530,7 +527,7 @@ int sl_batch_destroy(sl_batch* b) {
                        &b->tile_keys, &b->tile_keys_alt, &b->tile_vals, &b->tile_vals_alt, &b->status, &b->tile_ctr,
                        &b->hist, &b->scan_scratch, &b->bin_scratch, &b->block_valid, &b->block_off,
                        &b->ranges, &b->counters, &b->view_maxrad, &b->view_visible, &b->marks,
-                       &b->view_tmark};
+                       &b->view_tmark, &b->view_shade};
   for (sl::DevBuf* x : all) x->release();
   for (auto& ev : b->ev)
     if (ev) cudaEventDestroy(ev);

@@ -192,9 +192,7 @@ __global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __res
                                                           const BatchScene* __restrict__ scenes,
                                                           const uint32_t* __restrict__ block_view,
                                                           const uint32_t* __restrict__ list,
-                                                          const uint32_t* __restrict__ offsets,
-                                                          const uint32_t* __restrict__ shade_n,
-                                                          const BatchDyn* __restrict__ dyn,
+                                                          const uint32_t* __restrict__ view_shade,
                                                           SplatRec* __restrict__ recs,
                                                           uint32_t* __restrict__ view_maxrad) {
   __shared__ ShadeParams sSH;
@@ -204,11 +202,10 @@ __global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __res
   const BatchView& V = views[v];
   const BatchScene& S = scenes[V.scene];
   if (V.P.view_mode != 3u || !S.lit) return;
-  // this view's marked Gaussians: list[slot_base, slot_base + n) (the exclusive scan of its flags)
-  const uint32_t first = offsets[V.slot_base];
-  const uint32_t last = v + 1u < dyn->n_views ? offsets[views[v + 1u].slot_base] : *shade_n;
+  // this view's marked Gaussians: list[slot_base, slot_base + n)
+  const uint32_t n = view_shade[v];
   const uint32_t j = (blockIdx.x / 2 - V.block_first) * 256u + (blockIdx.x & 1u) * kThreads + threadIdx.x;
-  if ((blockIdx.x / 2 - V.block_first) * 256u + (blockIdx.x & 1u) * kThreads >= last - first) return;
+  if ((blockIdx.x / 2 - V.block_first) * 256u + (blockIdx.x & 1u) * kThreads >= n) return;
   const int t = threadIdx.x;
   if (t == 0) {
     sSH = S.SH;
@@ -223,7 +220,7 @@ __global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __res
   __syncthreads();
   float mx = 0.0f;
   uint32_t material = kEmitterMaterial, gslot = 0, i = 0;
-  if (j < last - first) {
+  if (j < n) {
     gslot = list[V.slot_base + j];
     i = gslot - V.slot_base;
     const sl_gaussian& G = reinterpret_cast<const sl_gaussian*>(V.gaussians)[i];
@@ -259,11 +256,10 @@ __global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __res
 }  // namespace
 
 cudaError_t launch_bshade(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
-                          uint32_t max_blocks, const uint32_t* list, const uint32_t* offsets, const uint32_t* shade_n,
-                          const BatchDyn* dyn, SplatRec* recs, uint32_t* view_maxrad, cudaStream_t s) {
+                          uint32_t max_blocks, const uint32_t* list, const uint32_t* view_shade, SplatRec* recs,
+                          uint32_t* view_maxrad, cudaStream_t s) {
   if (max_blocks == 0) return cudaSuccess;
-  bshade_kernel<<<2 * max_blocks, kThreads, 0, s>>>(views, scenes, block_view, list, offsets, shade_n, dyn, recs,
-                                                    view_maxrad);
+  bshade_kernel<<<2 * max_blocks, kThreads, 0, s>>>(views, scenes, block_view, list, view_shade, recs, view_maxrad);
   return cudaGetLastError();
 }
 

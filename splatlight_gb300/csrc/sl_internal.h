@@ -236,16 +236,13 @@ constexpr float kRadianceCap = 64.0f;
 cudaError_t launch_bmark(const BatchComposite& B, const uint2* ranges, const uint32_t* tile_vals, const SplatRec* recs,
                          const BatchViewOut* views, const uint32_t* view_maxrad, const BatchDyn* dyn,
                          uint32_t max_tiles, FrameCounters* ctr, uint8_t* marks, float* view_tmark, cudaStream_t s);
-// The batched shading list: per view, its marked Gaussians of lit views in its scene's shading order.  flags[g]
-// (g over every view's padded slots, shading-order position g - slot_base) is 1 when the coverage pass marked it;
-// after the exclusive scan of the flags into offsets, list[slot_base + k] is the k-th one's global slot.
+// The batched shading list: per view, the Gaussians of lit views the coverage pass marked, at list[slot_base, +n)
+// (their global slots; each block's in shading order, the blocks in any order), n in view_shade[view] (n_views words,
+// cleared by the launcher) and the batch's total added to ctr->shade_n.
 struct BatchScene;
-cudaError_t launch_bshade_flags(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
-                                const uint8_t* marks, const uint32_t* totals, uint32_t n_max, uint32_t* flags,
-                                cudaStream_t s);
-cudaError_t launch_bshade_compact(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
-                                  const uint32_t* flags, const uint32_t* offsets, const uint32_t* totals,
-                                  uint32_t n_max, uint32_t* list, cudaStream_t s);
+cudaError_t launch_bshade_list(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
+                               const uint8_t* marks, const uint32_t* totals, uint32_t max_blocks, uint32_t n_views,
+                               FrameCounters* ctr, uint32_t* list, uint32_t* view_shade, cudaStream_t s);
 // Tile keys are (view << 16) | view-local tile id; after the stable sort on the local id each (view, tile) run's
 // bounds are written to ranges[tile_base[view] + local] (ranges zeroed first).
 cudaError_t launch_btile_runs(const uint32_t* keys, const uint32_t* n_dev, uint32_t n_max, const BatchViewOut* views,

@@ -57,11 +57,11 @@ struct BatchScene {
   ShadeParams SH;   // eye replaced per view
   uint32_t lit;     // 0: no lighting bound (radiance 0, as an unbound colour buffer)
 };
-// Shades each lit view's marked Gaussians (the shading list; see launch_bshade_flags) at the view's eye and light
+// Shades each lit view's marked Gaussians (the shading list; see launch_bshade_list) at the view's eye and light
 // scale into their splat records' radiance, and raises the view's maximum radiance.
 cudaError_t launch_bshade(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
-                          uint32_t max_blocks, const uint32_t* list, const uint32_t* offsets, const uint32_t* shade_n,
-                          const BatchDyn* dyn, SplatRec* recs, uint32_t* view_maxrad, cudaStream_t s);
+                          uint32_t max_blocks, const uint32_t* list, const uint32_t* view_shade, SplatRec* recs,
+                          uint32_t* view_maxrad, cudaStream_t s);
 
 cudaError_t upload_iso_dirs(const float* dirs128x4, cudaStream_t s);
 cudaError_t launch_iso(const sl_gaussian* gs, sl_node* nodes, const sl_vgrid* vgrid, uint32_t count, cudaStream_t s);
