@@ -346,6 +346,7 @@ def run_serving(args, rates=(100, 500, 2000)):
                 if deadline[0] is not None and time.perf_counter() > deadline[0]:
                     break
 
+        st0 = srv.stats()
         th = threading.Thread(target=poller)
         th.start()
         t0 = time.perf_counter()
@@ -372,7 +373,12 @@ def run_serving(args, rates=(100, 500, 2000)):
         lat = np.array([(t - arrivals[tag]) * 1000.0 for tag, t, st, _ in done if st == 0])
         fails = sum(1 for _, _, st, _ in done if st != 0)
         n_adm = n - refused
+        st1 = srv.stats()
+        d_batches = st1["batches"] - st0["batches"]
         out["rates"].append({"lambda": lam, "requests": n, "refused_at_admission": refused, "failed": fails,
+                             "batches": d_batches,
+                             "graph_captures": d_batches - (st1["graph_replays"] - st0["graph_replays"]),
+                             "relaunches": st1["relaunches"] - st0["relaunches"],
                              "unfinished": n_adm - len(done),
                              "offered_per_s": round(n / (t_sub - t0), 1),
                              "views_per_s": round(len(done) / (t_end - t0), 1),
@@ -383,6 +389,7 @@ def run_serving(args, rates=(100, 500, 2000)):
     out["device_bytes"] = st["device_bytes"]
     out["batches"] = st["batches"]
     out["reshaded_views"] = st["reshaded_views"]
+    out["relaunches"] = st["relaunches"]
     srv.close()
     # the plain per-view path on a sample of the same requests, one at a time (the shading pass at the request's eye
     # and the frame; the light scale, a change of light state for the per-view path, is left at 1 there)

@@ -487,6 +487,7 @@ typedef struct sl_server_stats {
   uint64_t device_bytes;         /* scenes + pipeline buffers */
   uint64_t free_result_slots;
   uint64_t reshaded_views;       /* views re-run with every blended splat shaded (sl_batch_stats.reshaded_views) */
+  uint64_t relaunches;           /* batches launched again (tile entries beyond the capacity class, or a re-shade) */
 } sl_server_stats;
 
 SL_API int sl_server_create(sl_renderer* const* renderers, sl_lighting* const* lightings, uint32_t n_scenes,

@@ -65,7 +65,7 @@ class ServerResult(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("submitted", "completed", "rejected", "failed", "batches", "batch_views",
                                          "graph_replays", "pending", "device_bytes", "free_result_slots",
-                                         "reshaded_views")]
+                                         "reshaded_views", "relaunches")]
 
 
 class DiffScene(C.Structure):

@@ -378,11 +378,13 @@ void batch_begin(sl_batch* b, uint32_t n_views) {
 int batch_launch(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames, const float* eyes,
                  const float* light_scales, uint32_t n_views, float* out_dev, uint64_t slots, uint64_t tiles,
                  cudaStream_t s, bool* replayed) {
-  // the smallest capacity class that holds the batch's slots and tiles (and, after an overflow, its entries)
+  // the smallest capacity class that holds the batch's slots and tiles and the entries it is expected to have (and,
+  // after an overflow, its entries)
   b->cls = sl_batch::kClasses - 1;
+  const double est_entries = (double)slots * (double)b->entry_ratio;
   for (int c = b->cls_min; c < sl_batch::kClasses; c++) {
     const ClassCaps k = class_caps(b, c);
-    if (slots <= k.S && tiles <= k.T) {
+    if (slots <= k.S && tiles <= k.T && est_entries <= (double)k.E) {
       b->cls = c;
       break;
     }
@@ -400,6 +402,7 @@ int batch_finish(sl_batch* b, uint32_t n_views, uint64_t slots, uint64_t tiles, 
                  sl_batch_stats* stats, bool* retry) {
   *retry = false;
   const FrameCounters& hc = *b->h_ctr;
+  if (slots) b->entry_ratio = std::max(b->entry_ratio, (float)((double)hc.entries / (double)slots));
   if (hc.overflow || hc.entries > class_caps(b, b->cls).E) {  // the caller launches again
     // a larger class whose entries hold them, else grow the tile-entry capacity
     for (int c = b->cls + 1; c < sl_batch::kClasses; c++)

@@ -70,6 +70,7 @@ struct sl_server {
   // statistics
   uint64_t submitted = 0, completed = 0, rejected = 0, failed = 0, batches = 0, batch_views = 0, replays = 0;
   uint64_t reshaded = 0;  // views re-run with every blended splat shaded (radiance above the coverage allowance)
+  uint64_t relaunches = 0;  // batches launched again (entries beyond the capacity class, or a re-shade)
   uint64_t device_bytes = 0;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - epoch).count(); }
@@ -169,6 +170,10 @@ void complete(sl_server* S, Pipe& p) {
   bool retry = false;
   int rc = batch_finish(p.b, (uint32_t)p.reqs.size(), p.slots, p.tiles, p.replayed, nullptr, nullptr, &retry);
   if (rc == SL_OK && retry && ++p.attempts < 3) {
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->relaunches++;
+    }
     p.busy = false;
     rc = launch(S, p);
     if (rc == SL_OK) return;
@@ -422,6 +427,7 @@ int sl_server_get_stats(sl_server* S, sl_server_stats* st) {
   st->device_bytes = S->device_bytes;
   st->free_result_slots = S->free_slots.size();
   st->reshaded_views = S->reshaded;
+  st->relaunches = S->relaunches;
   return SL_OK;
 }
 

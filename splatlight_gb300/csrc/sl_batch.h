@@ -14,6 +14,8 @@ struct sl_batch {
   uint64_t max_slots = 0, entry_cap = 0;
   uint32_t tile_w = 16, tile_h = 16;
   float t_stop_scale = 1e-4f;
+  float entry_ratio = 0.0f;  // the most tile entries per slot a batch has had: the capacity class must hold the
+                             // batch's slots times this (a class too small for the entries costs a second launch)
   bool use_graph = true;
   // device buffers
   sl::DevBuf views, views_out, block_view, scenes_dev, dyn, keys32, keys_alt, vals_alt, order, recs, rects,
