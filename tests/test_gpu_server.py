@@ -124,6 +124,7 @@ def test_bright_request_reruns_and_completes(world):
             got = _drain(srv, len(reqs))
             st = srv.stats()
             assert st["failed"] == 0 and st["reshaded_views"] >= 1
+            assert st["relaunches"] >= 1  # the re-shade runs the batch again
         with BatchRenderer(R, L, max_views=4) as B:
             for t, (si, f, eye, lsc) in enumerate(reqs):
                 assert got[t].status == 0
