@@ -604,6 +604,42 @@ def run_diff(args, stream, flush):
 BATCH_KERNELS = 14
 
 
+def deferred_one_view(args, s, r, L, f, fwd, plain_out, flush, stream):
+    """The same lit frame through the batch API as a batch of one view: projection, sort and binning first, then only
+    the Gaussians the coverage pass marks are shaded (deferred shading) before the composite.  Device time per view,
+    L2 flushed between views, and the largest image difference from the plain path's frame (same light state)."""
+    import torch
+    from splatlight_gb300.batch import BatchRenderer, View
+    H, W = int(f["viewport"][1]), int(f["viewport"][0])
+    B = BatchRenderer([r], [L], max_views=1)
+    views = [View(0, f, s.eye)]
+    out = torch.empty(4 * W * H, dtype=torch.float32, device="cuda")
+    sc = stream.cuda_stream
+    for _ in range(max(args.warmup, 3)):
+        B.render_device(views, out=out, stream=sc)
+    ts = []
+    for _ in range(max(5, min(args.steps, 20))):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        B.render_device(views, out=out, stream=sc)
+        b.record(stream)
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    st = B.last_stats
+    ms = statistics.median(ts)
+    L.update(s.eye, fwd, stream=sc)
+    r.render(f, out=plain_out, stream=sc)
+    torch.cuda.synchronize()
+    err = float((out.view(H, W, 4) - plain_out).abs().max().item())
+    B.close()
+    return {"workload": "the same frame as a batch of one view (sl_batch_render)", "views_per_s": round(1000.0 / ms, 2),
+            "ms_per_view": round(ms, 4), "max_abs_err_vs_plain": err, "visible": int(st.visible),
+            "shaded": int(st.shaded), "reshaded_views": int(st.reshaded_views)}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -797,6 +833,7 @@ def main():
         e1.synchronize()
         maps.append(e0.elapsed_time(e1))
     L.update(s.eye, fwd, stream=stream.cuda_stream)
+    deferred = deferred_one_view(args, s, r, L, f, fwd, out, flush, stream)
     lighting_maps = {"update_every_part_moved_ms": round(statistics.median(maps), 4),
                      "shading_pass_only_ms": round(stage_ms["lighting"], 4),
                      "maps": f"light map A {s.shadow_res}^2 per part ({len(s.parts)} parts), sun layers {s.sun_res}^2"}
@@ -885,7 +922,8 @@ def main():
                 "roofline": roofline, "sort_roofline": roof_sort, "composite_roofline": roof_comp,
                 "shade_roofline": roof_shade,
                 "cpu_baseline": cpu, "clocks": clocks, "batched": batch, "serving": serving,
-                "differentiation": differentiation, "sort": sort_leg, "lod": lod_leg, "lighting_maps": lighting_maps}
+                "differentiation": differentiation, "sort": sort_leg, "lod": lod_leg, "lighting_maps": lighting_maps,
+                "deferred_one_view": deferred}
         print(json.dumps(line))
     L.close()
     r.close()
