@@ -275,7 +275,8 @@ def serve_scenes():
 def run_serving(args, rates=(100, 500, 2000)):
     """Poisson arrivals at each rate for --serve-seconds: each request names one of 6 resident scenes, a camera on a
     radius-U[3,8] sphere around the scene centre, a resolution from SERVE_RES and a light scale in U[0.5, 2]; the
-    server batches continuously (2 pipelines); latency = result on the host - arrival, wall clock."""
+    server batches continuously (2 pipelines); latency = result on the host - arrival, wall clock, as the caller's
+    polling thread sees it, and beside it the server's own (its completion - its submit, on its clock)."""
     import threading
 
     import torch
@@ -340,7 +341,8 @@ def run_serving(args, rates=(100, 500, 2000)):
         def poller():
             while not stop.is_set() or len(done) < n - refused:
                 for r in srv.poll(wait_us=2000, copy=False):
-                    done.append((r.tag, time.perf_counter(), r.status, r.batch_views))
+                    done.append((r.tag, time.perf_counter(), r.status, r.batch_views,
+                                 (r.t_done - r.t_submit) * 1000.0))
                 if stop.is_set() and len(done) >= n - refused:
                     break
                 if deadline[0] is not None and time.perf_counter() > deadline[0]:
@@ -369,9 +371,10 @@ def run_serving(args, rates=(100, 500, 2000)):
         deadline[0] = t_sub + 300.0
         stop.set()
         th.join()
-        t_end = max(t for _, t, _, _ in done)
-        lat = np.array([(t - arrivals[tag]) * 1000.0 for tag, t, st, _ in done if st == 0])
-        fails = sum(1 for _, _, st, _ in done if st != 0)
+        t_end = max(t for _, t, _, _, _ in done)
+        lat = np.array([(t - arrivals[tag]) * 1000.0 for tag, t, st, _, _ in done if st == 0])
+        lat_srv = np.array([ms for _, _, st, _, ms in done if st == 0])
+        fails = sum(1 for _, _, st, _, _ in done if st != 0)
         n_adm = n - refused
         st1 = srv.stats()
         d_batches = st1["batches"] - st0["batches"]
@@ -384,7 +387,9 @@ def run_serving(args, rates=(100, 500, 2000)):
                              "views_per_s": round(len(done) / (t_end - t0), 1),
                              "p50_ms": round(float(np.percentile(lat, 50)), 2),
                              "p99_ms": round(float(np.percentile(lat, 99)), 2),
-                             "mean_batch": round(float(np.mean([b for *_, b in done])), 1)})
+                             "server_p50_ms": round(float(np.percentile(lat_srv, 50)), 2),
+                             "server_p99_ms": round(float(np.percentile(lat_srv, 99)), 2),
+                             "mean_batch": round(float(np.mean([b for _, _, _, b, _ in done])), 1)})
     st = srv.stats()
     out["device_bytes"] = st["device_bytes"]
     out["batches"] = st["batches"]
