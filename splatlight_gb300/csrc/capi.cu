@@ -231,8 +231,7 @@ int sl_renderer_set_timing(sl_renderer* r, int on) {
 
 namespace sl {
 
-int check_frame(const sl_render_frame* f, uint32_t count, uint32_t n_emitters, const std::vector<sl_part>& parts,
-                const sl_lod* lod) {
+int check_frame(const sl_render_frame* f, uint32_t count, uint32_t n_emitters, const sl_lod* lod) {
   if (f->count != count) return fail(SL_ERR_INVALID_ARG, "frame.count differs from the renderer's Gaussian count");
   if (!(f->viewport[0] >= 1.0f && f->viewport[1] >= 1.0f && f->viewport[0] <= 16384.0f && f->viewport[1] <= 16384.0f) ||
       f->viewport[0] != (float)(uint32_t)f->viewport[0] || f->viewport[1] != (float)(uint32_t)f->viewport[1])
@@ -258,12 +257,6 @@ int check_frame(const sl_render_frame* f, uint32_t count, uint32_t n_emitters, c
   }
   if (f->explode_k[2] > 0.5f) return fail(SL_ERR_UNSUPPORTED, "explode is outside this pipeline");
   if (f->particles[1] != 0u) return fail(SL_ERR_UNSUPPORTED, "Gaussian particles are outside this pipeline");
-  if (f->palette[3][2] > 0.0f && f->view_mode == 3u)
-    for (const sl_part& p : parts)
-      if (p.flags & 2u)
-        return fail(SL_ERR_UNSUPPORTED,
-                    "the lit view of a blurred moving part needs the lighting's stretched records "
-                    "(runtime/wgsl/motion_blur.wgsl), outside this pipeline");
   return SL_OK;
 }
 
@@ -471,7 +464,7 @@ extern "C" {
 int sl_render(sl_renderer* r, const sl_render_frame* f, float* out_rgba, int out_on_device, sl_render_stats* stats,
               void* stream) {
   if (!r || !f || !out_rgba) return fail(SL_ERR_INVALID_ARG, "null argument");
-  int rc = check_frame(f, r->count, r->n_emitters, r->parts, r->lod);
+  int rc = check_frame(f, r->count, r->n_emitters, r->lod);
   if (rc) return rc;
   cudaSetDevice(r->device);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);

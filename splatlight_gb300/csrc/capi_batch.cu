@@ -345,7 +345,7 @@ int batch_layout(sl_batch* b, const uint32_t* scene_of_view, const sl_render_fra
     const uint32_t k = scene_of_view[v];
     if (k >= b->scenes.size()) return fail(SL_ERR_INVALID_ARG, "view " + std::to_string(v) + ": bad scene index");
     sl_renderer* r = b->scenes[k];
-    int rc = check_frame(&frames[v], r->count, r->n_emitters, r->parts);
+    int rc = check_frame(&frames[v], r->count, r->n_emitters);
     if (rc) return view_fail(v, rc);
     const uint32_t W = (uint32_t)frames[v].viewport[0], H = (uint32_t)frames[v].viewport[1];
     const uint32_t n = r->count + 1u + (uint32_t)frames[v].palette[3][1];

@@ -352,7 +352,7 @@ int sl_server_submit(sl_server* S, const sl_server_request* req, uint64_t tag) {
   if (!S || !req) return fail(SL_ERR_INVALID_ARG, "null argument");
   if (req->scene >= S->scenes.size()) return fail(SL_ERR_INVALID_ARG, "no such scene");
   sl_renderer* r = S->scenes[req->scene];
-  int rc = check_frame(&req->frame, r->count, r->n_emitters, r->parts);
+  int rc = check_frame(&req->frame, r->count, r->n_emitters);
   if (rc) return rc;
   if (!(req->light_scale >= 0.0f) || !(req->light_scale < 1e30f)) return fail(SL_ERR_INVALID_ARG, "bad light scale");
   Req q;

@@ -51,8 +51,7 @@ struct sl_batch {
 
 namespace sl {
 // Validates a frame for a renderer; lod: the renderer's screen-space LOD (null: frames with LOD on are refused).
-int check_frame(const sl_render_frame* f, uint32_t count, uint32_t n_emitters, const std::vector<sl_part>& parts,
-                const sl_lod* lod = nullptr);
+int check_frame(const sl_render_frame* f, uint32_t count, uint32_t n_emitters, const sl_lod* lod = nullptr);
 void pack_project_params(const sl_render_frame* f, const std::vector<sl_part>& parts, uint32_t count,
                          uint32_t n_emit, uint32_t tile_w, uint32_t tile_h, ProjectParams& P);
 

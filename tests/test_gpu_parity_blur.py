@@ -1,12 +1,11 @@
 """Motion blur in the projection (shaders/project.wgsl:138-146, 207-272): a part moving over the exposure, its
 Gaussians stretched by the box-shutter average (covariance + v v^T / 12, Sherman-Morrison q, mass-keeping kappa,
 coverage cap), bit-exact keys, permutation, tile lists and contributor counts and RGB within 1e-3 against the CPU
-restatement; the lit view of a blurred moving part (whose lighting needs stretched records) is refused."""
+restatement, in the flat, overdraw and lit views."""
 import numpy as np
 import pytest
 
 from splatlight_gb300 import camera, scene
-from splatlight_gb300._native import SplatlightError
 from splatlight_gb300.renderer import SplatRenderer
 from splatlight_gb300.structs import VIEW_FLAT, VIEW_LIT, VIEW_OVERDRAW
 
@@ -53,13 +52,32 @@ def test_blur_parity(cuda, orc, mode, cov_cap):
         assert not np.array_equal(r.render(f0), img)
 
 
-def test_lit_view_of_a_blurred_moving_part_is_refused(cuda):
-    s = scene.subset(scene.cornell(), 4000)
-    f = camera.make_frame(s.eye, s.target, s.up, s.fov_deg, 64, 64, s.count, far=s.far, view_mode=VIEW_LIT,
+def test_lit_view_of_a_blurred_moving_part(cuda, orc):
+    """The lit view of a moving part with the blur in the projection only (the reference's ?blurlight=0: the lighting
+    shades and shadows every Gaussian at its pose, the projection smears the display): the lighting, then the
+    frame's keys, permutation, tile lists bit-exact and RGB within 1e-3 against the CPU restatement."""
+    from splatlight_gb300.lighting import camera_forward, for_scene
+    s = scene.subset(scene.cornell(), 20000)
+    s = scene.dataclasses.replace(s, parts=_moving(s))
+    f = camera.make_frame(s.eye, s.target, s.up, s.fov_deg, 192, 160, s.count, far=s.far, view_mode=VIEW_LIT,
                           n_emit=len(s.emitters))
     f["palette"][3][2] = 0.5
-    with SplatRenderer(s.gaussians, _moving(s)) as r:
-        r.set_emitters(s.emitters)
-        with pytest.raises(SplatlightError) as e:
-            r.render(f)
-        assert e.value.code == -6
+    f["palette"][3][3] = 1.0
+    with SplatRenderer(s.gaussians, s.parts) as r:
+        L = for_scene(r, s)
+        L.update(s.eye, camera_forward(s))
+        col, _, _, _ = L.read()
+        ocol, _, _, _ = orc.lighting(s, threads=8)
+        assert np.allclose(col, ocol, rtol=1e-3, atol=1e-5), np.abs(col - ocol).max()
+        img = r.render(f)
+        dbg = r.read_debug()
+        ref = orc.render(s.gaussians, s.parts, f, emitters=s.emitters, colour=ocol, threads=8)
+        assert np.array_equal(dbg["keys"], ref["keys"])
+        assert np.array_equal(dbg["order"], ref["order"])
+        assert np.array_equal(dbg["ranges"], ref["ranges"])
+        assert np.array_equal(dbg["entries"], ref["entries"])
+        assert float(np.abs(img - ref["rgba"]).max()) <= 1e-3
+        f0 = f.copy()
+        f0["palette"][3][2] = 0.0
+        assert not np.array_equal(r.render(f0), img)
+        L.close()
