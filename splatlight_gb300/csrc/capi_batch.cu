@@ -96,8 +96,6 @@ cudaError_t allocate(sl_batch* b) {
   ENS(b->order, 4 * S + 16);
   ENS(b->recs, sizeof(SplatRec) * S);
   ENS(b->rects, 8 * S);
-  ENS(b->slot_counts, 4 * S + 16);
-  ENS(b->slot_offsets, 4 * S + 16);
   ENS(b->bin_scratch, btile_bin_scratch_bytes((uint32_t)S));
   ENS(b->tile_keys, 4 * E + 16);
   ENS(b->tile_keys_alt, 4 * E + 16);
@@ -526,7 +524,7 @@ int sl_batch_destroy(sl_batch* b) {
   drop_graph(b);
   free_pinned(b);
   sl::DevBuf* all[] = {&b->views, &b->views_out, &b->block_view, &b->scenes_dev, &b->dyn, &b->keys32, &b->keys_alt,
-                       &b->vals_alt, &b->order, &b->recs, &b->rects, &b->slot_counts, &b->slot_offsets,
+                       &b->vals_alt, &b->order, &b->recs, &b->rects,
                        &b->tile_keys, &b->tile_keys_alt, &b->tile_vals, &b->tile_vals_alt, &b->status, &b->tile_ctr,
                        &b->hist, &b->scan_scratch, &b->bin_scratch, &b->block_valid, &b->block_off,
                        &b->ranges, &b->counters, &b->view_maxrad, &b->view_visible, &b->marks,

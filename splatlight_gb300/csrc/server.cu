@@ -293,9 +293,9 @@ int sl_server_create(sl_renderer* const* renderers, sl_lighting* const* lighting
   }
   if (o.pipelines > 8 || o.max_views > 256 || o.max_view_pixels > o.max_pixels)
     return fail(SL_ERR_INVALID_ARG, "server options out of range");
-  // device footprint of the pipelines: per slot (keys x2, values x2, order, record, rect, counts, offsets) 80 B,
+  // device footprint of the pipelines: per slot (keys x2, values x2, order, record, rect, coverage mark) 73 B,
   // per tile entry (keys x2, values x2) 16 B at 2 entries per slot to start, per tile 28 B, per pixel 16 B
-  const uint64_t per_pipe = 80ull * o.max_slots + 32ull * o.max_slots + 28ull * o.max_tiles + 16ull * o.max_pixels;
+  const uint64_t per_pipe = 73ull * o.max_slots + 32ull * o.max_slots + 28ull * o.max_tiles + 16ull * o.max_pixels;
   uint64_t scene_bytes = 0;
   for (uint32_t k = 0; k < n_scenes; k++) {
     if (!renderers[k]) return fail(SL_ERR_INVALID_ARG, "null renderer");

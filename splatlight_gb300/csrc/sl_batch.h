@@ -19,7 +19,7 @@ struct sl_batch {
   bool use_graph = true;
   // device buffers
   sl::DevBuf views, views_out, block_view, scenes_dev, dyn, keys32, keys_alt, vals_alt, order, recs, rects,
-      slot_counts, slot_offsets, tile_keys, tile_keys_alt, tile_vals, tile_vals_alt, status, tile_ctr, hist,
+      tile_keys, tile_keys_alt, tile_vals, tile_vals_alt, status, tile_ctr, hist,
       scan_scratch, bin_scratch, ranges, block_valid, block_off, counters, view_maxrad, view_visible, marks,
       view_tmark, view_shade;
   // pinned staging
