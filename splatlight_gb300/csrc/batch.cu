@@ -131,8 +131,8 @@ __global__ void __launch_bounds__(kThreads) btile_bin_kernel(const uint32_t* __r
   hh.flush(digit_hist, warp_tot);
 }
 
-// shading-list candidates: position g of the padded slots <-> the view's Gaussian order[g - slot_base] (shading order);
-// a Gaussian is shaded when the coverage pass marked it (it blends a fragment before its pixels terminate)
+// shading-list candidates: position g of the padded slots <-> the view's Gaussian order[g - slot_base] (shading
+// order); a Gaussian is shaded when the coverage pass marked it (it blends a fragment before its pixels terminate)
 __device__ __forceinline__ bool shade_candidate(const BatchView* views, const BatchScene* scenes,
                                                 const uint32_t* block_view, const uint8_t* marks, uint32_t g,
                                                 uint32_t& view, uint32_t& gslot) {
