@@ -34,9 +34,9 @@ sys.path.insert(0, str(ROOT))
 
 MEASURED = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM = 6800.0  # GB/s
-# shade; project, 2 depth-sort passes, tile counts, scan, emit, 2 tile-sort passes, tile runs, run counts, scan,
-# ranges, composite
-KERNELS_PER_FRAME = 14
+# shade; project, 2 depth-sort passes, binning (counts, offsets and entries in one pass), 2 tile-sort passes, ranges,
+# composite
+KERNELS_PER_FRAME = 9
 # DRAM bytes per Gaussian of one shade_kernel launch (read + write), from ncu on the 1,048,576-Gaussian frame
 SHADE_DRAM_BYTES_PER_G = (464.748544e6 + 22.484992e6) / 1048576
 

@@ -14,16 +14,6 @@ namespace {
 
 constexpr int kThreads = 256;
 
-constexpr uint64_t kBinAgg = 1ull << 32;     // status word: the block's own entry count is published
-constexpr uint64_t kBinPrefix = 2ull << 32;  // status word: the entries of every block up to this one
-constexpr uint32_t kBinSpinLimit = 1u << 22;
-
-__device__ __forceinline__ uint64_t load_relaxed64(const uint64_t* p) {
-  uint64_t v;
-  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-
 // The binning of the batch in one pass over the depth-sorted visible splats: each block of 256 sorted positions
 // counts its splats' tile entries (the per-row spans), learns the entries of every earlier block by a decoupled
 // look-back over per-block status words (blocks take their positions from a ticket counter, so every earlier block is
@@ -87,34 +77,9 @@ __global__ void __launch_bounds__(kThreads) btile_bin_kernel(const uint32_t* __r
     wbase += k < w ? tt : 0u;
     agg += tt;
   }
-  if (w == 0) {  // warp 0: the look-back, 32 predecessors' status words per step (nearest in lane 0)
-    if (lane == 0)
-      atomicExch(reinterpret_cast<unsigned long long*>(status + blk),
-                 (unsigned long long)((blk == 0 ? kBinPrefix : kBinAgg) | agg));
-    uint32_t excl = 0;
-    int32_t top = (int32_t)blk - 1;
-    uint32_t spins = 0;
-    while (top >= 0) {
-      const int32_t j = top - (int32_t)lane;
-      const uint64_t st = j >= 0 ? load_relaxed64(status + j) : kBinPrefix;  // before block 0: a prefix of 0
-      const uint32_t flag = (uint32_t)(st >> 32);
-      const uint32_t pm = __ballot_sync(0xffffffffu, flag == 2u), zm = __ballot_sync(0xffffffffu, flag == 0u);
-      const uint32_t pfirst = pm ? (uint32_t)__ffs(pm) - 1u : 32u, zfirst = zm ? (uint32_t)__ffs(zm) - 1u : 32u;
-      if (zfirst < pfirst) {  // a nearer block has not published yet: read the window again
-        if (++spins > kBinSpinLimit) {
-          if (lane == 0) atomicExch(&ctr->timeout, 1u);
-          break;
-        }
-        __nanosleep(32);
-        continue;
-      }
-      excl += __reduce_add_sync(0xffffffffu, lane <= pfirst ? (uint32_t)st : 0u);
-      if (pm) break;
-      top -= 32;
-    }
+  if (w == 0) {  // warp 0: the block's offset from the look-back
+    const uint32_t excl = lookback_warp(status, blk, 0u, agg, &ctr->timeout);
     if (lane == 0) {
-      if (blk != 0)
-        atomicExch(reinterpret_cast<unsigned long long*>(status + blk), (unsigned long long)(kBinPrefix | (excl + agg)));
       s_excl = excl;
       if ((blk + 1u) * kThreads >= n) ctr->entries = excl + agg;  // the last block
     }

@@ -26,10 +26,9 @@ int cuda_fail(cudaError_t e, const char* what) {
 }
 
 void ViewBuffers::release_all() {
-  DevBuf* all[] = {&key16,     &recs,      &rects,       &order,       &slot_counts, &slot_offsets, &keys_alt,
-                   &vals_alt,  &status,    &tile_ctr,    &tile_keys,   &tile_vals,   &tile_counts,  &tile_starts,
-                   &ranges,    &digit_hist, &scan_scratch, &counters, &out,         &counts,       &run_start,
-                   &run_end,   &key_hist};
+  DevBuf* all[] = {&key16,    &recs,       &rects,        &order,    &bin_scratch, &keys_alt, &vals_alt,
+                   &status,   &tile_ctr,   &tile_keys,    &tile_vals, &ranges,      &digit_hist, &scan_scratch,
+                   &counters, &out,        &counts,       &key_hist};
   for (DevBuf* b : all) b->release();
 }
 
@@ -322,8 +321,7 @@ static cudaError_t ensure_view_buffers(ViewBuffers& vb, uint32_t n, uint32_t til
   ENS(vb.recs, sizeof(SplatRec) * (size_t)n);
   ENS(vb.rects, 8ull * n);
   ENS(vb.order, 4ull * n + 16);
-  ENS(vb.slot_counts, 4ull * n + 16);
-  ENS(vb.slot_offsets, 4ull * n + 16);
+  ENS(vb.bin_scratch, tile_bin_scratch_bytes(n));
   uint64_t big = cap > n ? cap : n;
   ENS(vb.keys_alt, 2 * big + 16);
   ENS(vb.vals_alt, 4 * big + 16);
@@ -331,16 +329,10 @@ static cudaError_t ensure_view_buffers(ViewBuffers& vb, uint32_t n, uint32_t til
   ENS(vb.tile_ctr, 16);
   ENS(vb.tile_keys, 2 * cap + 16);
   ENS(vb.tile_vals, 4 * cap + 16);
-  ENS(vb.tile_counts, 4ull * tiles + 16);
-  ENS(vb.tile_starts, 4ull * tiles + 16);
   ENS(vb.ranges, 8ull * tiles + 16);
-  ENS(vb.run_start, 4ull * tiles + 16);
-  ENS(vb.run_end, 4ull * tiles + 16);
   ENS(vb.digit_hist, 4ull * 4 * 256);
   ENS(vb.key_hist, 2 * 4ull * 65536);
-  size_t sc = scan_scratch_bytes(n > 65536u ? n : 65536u);  // also the counting sort's 65536 key offsets
-  size_t sc2 = scan_scratch_bytes(tiles);
-  ENS(vb.scan_scratch, sc > sc2 ? sc : sc2);
+  ENS(vb.scan_scratch, scan_scratch_bytes(65536u));  // the counting sort's 65536 key offsets
   ENS(vb.counters, sizeof(FrameCounters));
   if (need_out) ENS(vb.out, 16ull * pixels);
   if (need_counts) ENS(vb.counts, 4ull * pixels);
@@ -380,8 +372,7 @@ static int render_once(sl_renderer* r, const sl_render_frame* f, float4* out_dev
   if (ev) SL_CHECK_CUDA(cudaEventRecord(ev[0], s), "event");
   SL_CHECK_CUDA(cudaMemsetAsync(ctr, 0, sizeof(FrameCounters), s), "memset counters");
   SL_CHECK_CUDA(cudaMemsetAsync(hist, 0, 4 * 4 * 256, s), "memset hist");
-  SL_CHECK_CUDA(cudaMemsetAsync(vb.run_start.ptr, 0, 4ull * tiles, s), "memset runs");
-  SL_CHECK_CUDA(cudaMemsetAsync(vb.run_end.ptr, 0, 4ull * tiles, s), "memset runs");
+  SL_CHECK_CUDA(cudaMemsetAsync(vb.ranges.ptr, 0, 8ull * tiles, s), "memset ranges");
   SL_CHECK_CUDA(launch_project(P, r->gaussians.as<sl_gaussian>(), r->emitters.as<sl_gaussian>(), colour, lo_b,
                                vb.key16.as<uint16_t>(), vb.recs.as<SplatRec>(), vb.rects.as<ushort4>(), hist, ctr, s,
                                lod),
@@ -400,35 +391,18 @@ static int render_once(sl_renderer* r, const sl_render_frame* f, float4* out_dev
                   "depth sort");
   }
   if (ev) SL_CHECK_CUDA(cudaEventRecord(ev[2], s), "event");
-  SL_CHECK_CUDA(launch_tile_counts(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.recs.as<SplatRec>(), n, P.tile_w,
-                                   P.tile_h, ctr, vb.slot_counts.as<uint32_t>(), s),
-                "tile counts");
-  SL_CHECK_CUDA(exclusive_scan_u32(vb.slot_counts.as<uint32_t>(), vb.slot_offsets.as<uint32_t>(), n, &ctr->entries,
-                                   vb.scan_scratch.ptr, ctr, s),
-                "entry scan");
-  SL_CHECK_CUDA(launch_tile_emit(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.recs.as<SplatRec>(),
-                                 vb.slot_offsets.as<uint32_t>(), vb.slot_counts.as<uint32_t>(), n, P.tiles_x, P.tile_w,
-                                 P.tile_h,
-                                 (uint32_t)(cap > 0xffffffffull ? 0xffffffffu : cap), ctr,
-                                 vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), hist + 512, s),
-                "tile emit");
+  SL_CHECK_CUDA(launch_tile_bin(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.recs.as<SplatRec>(), n,
+                                P.tiles_x, P.tile_w, P.tile_h, (uint32_t)(cap > 0xffffffffull ? 0xffffffffu : cap), ctr,
+                                vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), hist + 512,
+                                vb.bin_scratch.ptr, s),
+                "tile binning");
   // the entry count is only known on the device: the tile sort reads it there (grid sized for the capacity)
   const uint32_t cap32 = (uint32_t)(cap > 0xffffffffull ? 0xffffffffu : cap);
   SL_CHECK_CUDA(sort16_pairs(vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), vb.tile_vals.as<uint32_t>(),
                              cap32, &ctr->entries, bits_for(tiles - 1), hist + 512, sc, ctr, s,
                              vb.tile_keys.as<uint16_t>()),
                 "tile sort");
-  SL_CHECK_CUDA(launch_tile_runs(vb.tile_keys.as<uint16_t>(), &ctr->entries, cap32, vb.run_start.as<uint32_t>(),
-                                 vb.run_end.as<uint32_t>(), s),
-                "tile runs");
-  SL_CHECK_CUDA(launch_tile_run_counts(vb.run_start.as<uint32_t>(), vb.run_end.as<uint32_t>(), tiles,
-                                       vb.tile_counts.as<uint32_t>(), s),
-                "tile counts");
-  SL_CHECK_CUDA(exclusive_scan_u32(vb.tile_counts.as<uint32_t>(), vb.tile_starts.as<uint32_t>(), tiles, nullptr,
-                                   vb.scan_scratch.ptr, ctr, s),
-                "tile scan");
-  SL_CHECK_CUDA(launch_tile_ranges(vb.tile_starts.as<uint32_t>(), vb.tile_counts.as<uint32_t>(), tiles,
-                                   vb.ranges.as<uint2>(), s),
+  SL_CHECK_CUDA(launch_tile_ranges(vb.tile_keys.as<uint16_t>(), &ctr->entries, cap32, vb.ranges.as<uint2>(), s),
                 "tile ranges");
   if (ev) SL_CHECK_CUDA(cudaEventRecord(ev[3], s), "event");
   CompositeParams C;
@@ -541,7 +515,16 @@ int sl_renderer_read_debug(sl_renderer* r, uint32_t* keys, uint32_t* order, uint
     for (uint32_t i = 0; i < n; i++) keys[i] = k16[i] == kInvalidKey16 ? 0xffffffffu : k16[i];
   }
   if (order) SL_CHECK_CUDA(cudaMemcpy(order, r->vb.order.ptr, 4ull * n, cudaMemcpyDeviceToHost), "order");
-  if (ranges) SL_CHECK_CUDA(cudaMemcpy(ranges, r->vb.ranges.ptr, 8ull * r->last_tiles, cudaMemcpyDeviceToHost), "ranges");
+  if (ranges) {
+    SL_CHECK_CUDA(cudaMemcpy(ranges, r->vb.ranges.ptr, 8ull * r->last_tiles, cudaMemcpyDeviceToHost), "ranges");
+    // the device keeps [0, 0) for empty tiles; read back as the cumulative bounds of the tiles' lists in tile order
+    // (an empty tile at the end of the lists before it)
+    uint32_t at = 0;
+    for (uint32_t t = 0; t < r->last_tiles; t++) {
+      if (ranges[2 * t + 1] > ranges[2 * t]) at = ranges[2 * t + 1];
+      else ranges[2 * t] = ranges[2 * t + 1] = at;
+    }
+  }
   if (counts) {
     if (r->last_mode != 2u) return fail(SL_ERR_INVALID_ARG, "contributor counts come from view mode 2");
     SL_CHECK_CUDA(cudaMemcpy(counts, r->vb.counts.ptr, 4ull * r->last_w * r->last_h, cudaMemcpyDeviceToHost), "counts");

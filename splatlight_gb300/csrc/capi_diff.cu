@@ -63,21 +63,15 @@ cudaError_t ensure(sl_diff* d, uint32_t tiles, uint32_t pixels) {
   ENS(vb.recs, sizeof(SplatRec) * (size_t)n + 16);
   ENS(vb.rects, 8ull * n + 16);
   ENS(vb.order, 4ull * n + 16);
-  ENS(vb.slot_counts, 4ull * n + 16);
-  ENS(vb.slot_offsets, 4ull * n + 16);
   ENS(vb.keys_alt, 2 * big + 16);
   ENS(vb.vals_alt, 4 * big + 16);
   ENS(vb.status, 4ull * 256 * 2 * (sort_tiles_for((uint32_t)big) + 1));
   ENS(vb.tile_ctr, 16);
   ENS(vb.tile_keys, 2 * cap + 16);
   ENS(vb.tile_vals, 4 * cap + 16);
-  ENS(vb.tile_counts, 4ull * tiles + 16);
-  ENS(vb.tile_starts, 4ull * tiles + 16);
   ENS(vb.ranges, 8ull * tiles + 16);
-  ENS(vb.run_start, 4ull * tiles + 16);
-  ENS(vb.run_end, 4ull * tiles + 16);
   ENS(vb.digit_hist, 4ull * 4 * 256);
-  ENS(vb.scan_scratch, std::max(scan_scratch_bytes(n), scan_scratch_bytes(tiles)));
+  ENS(vb.bin_scratch, tile_bin_scratch_bytes(n));
   ENS(vb.counters, sizeof(FrameCounters));
   ENS(d->drec, sizeof(DiffRec) * (size_t)n + 16);
   ENS(d->g2, sizeof(DiffGrad2D) * (size_t)n + 16);
@@ -114,38 +108,19 @@ int run(sl_diff* d, const sl_diff_scene* sc, const sl_render_frame* f, const flo
   if ((e = (x)) != cudaSuccess) return cuda_fail(e, what)
   CK(cudaMemsetAsync(ctr, 0, sizeof(FrameCounters), s), "memset");
   CK(cudaMemsetAsync(hist, 0, 4 * 4 * 256, s), "memset");
-  CK(cudaMemsetAsync(vb.run_start.ptr, 0, 4ull * tiles, s), "memset");
-  CK(cudaMemsetAsync(vb.run_end.ptr, 0, 4ull * tiles, s), "memset");
+  CK(cudaMemsetAsync(vb.ranges.ptr, 0, 8ull * tiles, s), "memset");
   CK(launch_dproject(K, P, L, n, vb.key16.as<uint16_t>(), d->drec.as<DiffRec>(), vb.recs.as<SplatRec>(),
                      vb.rects.as<ushort4>(), hist, ctr, s),
      "diff project");
   CK(sort16_pairs(vb.key16.as<uint16_t>(), nullptr, vb.order.as<uint32_t>(), n, nullptr, 16, hist, scr, ctr, s),
      "depth sort");
-  CK(launch_tile_counts(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.recs.as<SplatRec>(), n, 16, 16, ctr,
-                        vb.slot_counts.as<uint32_t>(), s),
-     "tile counts");
-  CK(exclusive_scan_u32(vb.slot_counts.as<uint32_t>(), vb.slot_offsets.as<uint32_t>(), n, &ctr->entries,
-                        vb.scan_scratch.ptr, ctr, s),
-     "entry scan");
-  CK(launch_tile_emit(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.recs.as<SplatRec>(),
-                      vb.slot_offsets.as<uint32_t>(), vb.slot_counts.as<uint32_t>(), n, tx, 16, 16, cap32, ctr,
-                      vb.tile_keys.as<uint16_t>(),
-                      vb.tile_vals.as<uint32_t>(), hist + 512, s),
-     "tile emit");
+  CK(launch_tile_bin(vb.order.as<uint32_t>(), vb.rects.as<ushort4>(), vb.recs.as<SplatRec>(), n, tx, 16, 16, cap32,
+                     ctr, vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), hist + 512, vb.bin_scratch.ptr, s),
+     "tile binning");
   CK(sort16_pairs(vb.tile_keys.as<uint16_t>(), vb.tile_vals.as<uint32_t>(), vb.tile_vals.as<uint32_t>(), cap32,
                   &ctr->entries, bits16(tiles - 1), hist + 512, scr, ctr, s, vb.tile_keys.as<uint16_t>()),
      "tile sort");
-  CK(launch_tile_runs(vb.tile_keys.as<uint16_t>(), &ctr->entries, cap32, vb.run_start.as<uint32_t>(),
-                      vb.run_end.as<uint32_t>(), s),
-     "tile runs");
-  CK(launch_tile_run_counts(vb.run_start.as<uint32_t>(), vb.run_end.as<uint32_t>(), tiles, vb.tile_counts.as<uint32_t>(),
-                            s),
-     "run counts");
-  CK(exclusive_scan_u32(vb.tile_counts.as<uint32_t>(), vb.tile_starts.as<uint32_t>(), tiles, nullptr,
-                        vb.scan_scratch.ptr, ctr, s),
-     "tile scan");
-  CK(launch_tile_ranges(vb.tile_starts.as<uint32_t>(), vb.tile_counts.as<uint32_t>(), tiles, vb.ranges.as<uint2>(), s),
-     "tile ranges");
+  CK(launch_tile_ranges(vb.tile_keys.as<uint16_t>(), &ctr->entries, cap32, vb.ranges.as<uint2>(), s), "tile ranges");
   CK(launch_dcomposite_fwd(vb.ranges.as<uint2>(), vb.tile_vals.as<uint32_t>(), d->drec.as<DiffRec>(), W, H, tx, tiles,
                            d->img.as<float4>(), d->tfinal.as<float>(), d->ncontrib.as<uint32_t>(), s),
      "diff composite");

@@ -12,6 +12,56 @@ namespace sl {
 
 constexpr uint32_t kSmallTiles = 48;
 
+// Decoupled look-back over per-block status words (u64: flag << 32 | count; flag 1 the block's own count, 2 the
+// count of every block up to it), for blocks that take their positions from a ticket counter, so every earlier block
+// is already running and each wait ends (bounded all the same: past the limit the frame's timeout flag is set).
+constexpr uint64_t kLookAgg = 1ull << 32;
+constexpr uint64_t kLookPrefix = 2ull << 32;
+constexpr uint32_t kLookSpinLimit = 1u << 22;
+
+__device__ __forceinline__ uint64_t load_relaxed64(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Called by one whole warp for block blk with its count agg (blocks before `first` count as a prefix of 0): publishes
+// agg, reads 32 earlier blocks' words per step (the nearest in lane 0) until a prefix, publishes this block's prefix
+// and returns the count of the blocks in [first, blk) in every lane.
+__device__ __forceinline__ uint32_t lookback_warp(uint64_t* status, uint32_t blk, uint32_t first, uint32_t agg,
+                                                  uint32_t* timeout_flag) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const bool head = blk == first;
+  if (lane == 0)
+    atomicExch(reinterpret_cast<unsigned long long*>(status + blk),
+               (unsigned long long)((head ? kLookPrefix : kLookAgg) | agg));
+  uint32_t excl = 0;
+  const int32_t lo = (int32_t)first;
+  int32_t top = (int32_t)blk - 1;
+  uint32_t spins = 0;
+  while (top >= lo) {
+    const int32_t j = top - (int32_t)lane;
+    const uint64_t st = j >= lo ? load_relaxed64(status + j) : kLookPrefix;  // before the first block: a prefix of 0
+    const uint32_t flag = (uint32_t)(st >> 32);
+    const uint32_t pm = __ballot_sync(0xffffffffu, flag == 2u), zm = __ballot_sync(0xffffffffu, flag == 0u);
+    const uint32_t pfirst = pm ? (uint32_t)__ffs(pm) - 1u : 32u, zfirst = zm ? (uint32_t)__ffs(zm) - 1u : 32u;
+    if (zfirst < pfirst) {  // a nearer block has not published yet: read the window again
+      if (++spins > kLookSpinLimit) {
+        if (lane == 0) atomicExch(timeout_flag, 1u);
+        break;
+      }
+      __nanosleep(32);
+      continue;
+    }
+    excl += __reduce_add_sync(0xffffffffu, lane <= pfirst ? (uint32_t)st : 0u);
+    if (pm) break;
+    top -= 32;
+  }
+  if (lane == 0 && !head)
+    atomicExch(reinterpret_cast<unsigned long long*>(status + blk), (unsigned long long)(kLookPrefix | (excl + agg)));
+  return excl;
+}
+
 // Digit counts of the low 16 bits of the emitted tile keys, for the two passes of the tile sort that follows, in a
 // block's shared memory.  A row of the emission is n consecutive ids: its high-byte digits are one or two runs (an
 // add per run), its low-byte digits n consecutive bins mod 256, kept as a difference array (a step up at the first

@@ -140,21 +140,16 @@ cudaError_t exclusive_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, ui
                                FrameCounters* ctr, cudaStream_t s);
 
 // tiles.cu
-cudaError_t launch_tile_counts(const uint32_t* order, const ushort4* rects, const SplatRec* recs, uint32_t n,
-                               uint32_t tw, uint32_t th, const FrameCounters* ctr, uint32_t* counts, cudaStream_t s);
-// counts: the per-position tile counts the scan of offsets was made from
-cudaError_t launch_tile_emit(const uint32_t* order, const ushort4* rects, const SplatRec* recs,
-                             const uint32_t* offsets, const uint32_t* counts, uint32_t n, uint32_t tiles_x,
-                             uint32_t tw, uint32_t th, uint32_t capacity, FrameCounters* ctr, uint16_t* tile_keys,
-                             uint32_t* tile_vals, uint32_t* digit_hist, cudaStream_t s);
-// After the tile sort: per tile the run [start, end) of its id in the sorted keys (both zero for an empty tile;
-// the arrays are cleared by the caller), then counts = end - start.
-cudaError_t launch_tile_runs(const uint16_t* sorted_keys, const uint32_t* n_dev, uint32_t n_max, uint32_t* run_start,
-                             uint32_t* run_end, cudaStream_t s);
-cudaError_t launch_tile_run_counts(const uint32_t* run_start, const uint32_t* run_end, uint32_t tiles,
-                                   uint32_t* counts, cudaStream_t s);
-cudaError_t launch_tile_ranges(const uint32_t* tile_starts, const uint32_t* tile_counts, uint32_t tiles,
-                               uint2* ranges, cudaStream_t s);
+// One pass: tile counts, their offsets (decoupled look-back) and the entries of the visible sorted splats; the
+// entry total to ctr->entries.  scratch: tile_bin_scratch_bytes(n) bytes, cleared by the launcher.
+size_t tile_bin_scratch_bytes(uint32_t n);
+cudaError_t launch_tile_bin(const uint32_t* order, const ushort4* rects, const SplatRec* recs, uint32_t n,
+                            uint32_t tiles_x, uint32_t tw, uint32_t th, uint32_t capacity, FrameCounters* ctr,
+                            uint16_t* tile_keys, uint32_t* tile_vals, uint32_t* digit_hist /*[2][256]*/,
+                            void* scratch, cudaStream_t s);
+// ranges[tile] = the run of the tile's entries in the sorted keys (ranges zeroed beforehand: empty tiles [0, 0)).
+cudaError_t launch_tile_ranges(const uint16_t* sorted_keys, const uint32_t* n_dev, uint32_t n_max, uint2* ranges,
+                               cudaStream_t s);
 
 // composite.cu
 struct CompositeParams {

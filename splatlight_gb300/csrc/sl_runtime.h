@@ -43,10 +43,11 @@ struct DevBuf {
 
 // Per-view working buffers of the project -> sort -> bin -> composite chain.
 struct ViewBuffers {
-  DevBuf key16, recs, rects, order, slot_counts, slot_offsets;  // per slot
+  DevBuf key16, recs, rects, order;                            // per slot
+  DevBuf bin_scratch;                                          // the one-pass binning's ticket and look-back words
   DevBuf keys_alt, vals_alt, status, tile_ctr;                 // sort scratch (max of slots, entries)
   DevBuf tile_keys, tile_vals;                                 // per entry
-  DevBuf tile_counts, tile_starts, ranges, run_start, run_end; // per tile
+  DevBuf ranges;                                               // per tile
   DevBuf digit_hist;                                           // [4][256]: depth-key passes, tile-key passes
   DevBuf key_hist;                                             // counting sort: 65536 key counts, then offsets
   DevBuf scan_scratch;
