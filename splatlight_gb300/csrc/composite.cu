@@ -110,9 +110,9 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
   const float fx0 = (float)x0, fy0 = (float)y0;
   const float kNegHalfLog2e = -0.72134752044448170f;
   const float kNegLog2e = -1.44269504088896341f;
-  // coverage pass: its keep test evaluates q in tile-relative coordinates (a few ulps away from the composite's q, whose
-  // rounding it need not match), so it keeps fragments up to a cutoff 1e-4 (relative) above the composite's: every
-  // fragment the composite blends is marked
+  // coverage pass: its keep test evaluates q in tile-relative coordinates (a few ulps away from the composite's q,
+  // whose rounding it need not match), so it keeps fragments up to a cutoff 1e-4 (relative) above the composite's:
+  // every fragment the composite blends is marked
   const float kMarkCutScale = 1.0001f;
 
   float T = 1.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f;

@@ -16,7 +16,8 @@ constexpr int kThreads = 256;
 // Tile counts, their offsets and the entries in one pass over the depth-sorted visible splats (positions below
 // ctr->visible): each block of 256 positions counts its splats' tile entries (the per-row spans), learns the entries
 // of every earlier block by a decoupled look-back (blocks take their positions from a ticket counter), and writes its
-// entries -- key the tile id ty * tiles_x + tx, value the slot -- at the running offset, so entries stay in depth order.
+// entries -- key the tile id ty * tiles_x + tx, value the slot -- at the running offset, so entries stay in depth
+// order.
 // The digit counts of the tile id go to digit_hist for the tile sort; the last block writes the entry total to
 // ctr->entries (which may exceed capacity: the entries past it are not written and the overflow flag is set).
 __global__ void __launch_bounds__(kThreads) tile_bin_kernel(const uint32_t* __restrict__ order,
