@@ -327,6 +327,13 @@ def run_serving(args, rates=(100, 500, 2000)):
     got = 0
     while got < 16:
         got += len(srv.poll(wait_us=50000, copy=False))
+    # and a paced run (gaps of 0.2-5 ms), so both pipelines capture the graphs of the small capacity classes that
+    # single requests and small bursts use before any latency is measured
+    for k in range(96):
+        srv.submit(*request(), tag=16 + k)
+        time.sleep(float(rng.uniform(0.0002, 0.005)))
+    while got < 16 + 96:
+        got += len(srv.poll(wait_us=50000, copy=False))
     for lam in rates:
         n = max(1, int(lam * args.serve_seconds))
         gaps = rng.exponential(1.0 / lam, size=n)
