@@ -86,6 +86,23 @@ def test_hill_full_config(cuda, orc):
         assert r.last_stats.entries == ref["n_entries"]
 
 
+def test_tile_entry_overflow_grows_and_renders_again(cuda, orc):
+    """A tile-entry capacity far below the frame's entries: the one-pass binning writes none past it, flags the
+    overflow and reports the exact total; the renderer grows to it and renders again, with lists and image equal to
+    the restatement's and to a render that never overflowed."""
+    s = scene.subset(scene.cornell(), 20000)
+    f = _frame(s, 256, 192, VIEW_FLAT)
+    with SplatRenderer(s.gaussians, s.parts) as r0:
+        r0.set_emitters(s.emitters)
+        want = r0.render(f)
+    with SplatRenderer(s.gaussians, s.parts) as r:
+        r.set_emitters(s.emitters)
+        r.set_options(entry_capacity=64)
+        img, ref = _check(r, s, f, orc, (16, 16))
+        assert ref["n_entries"] > 64
+        assert np.array_equal(img, want)
+
+
 def test_empty_view(cuda, orc):
     """Camera looking away from everything: no valid key, no entry, a transparent image."""
     s = scene.subset(scene.cornell(), 2000)
