@@ -83,9 +83,9 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
   __shared__ uint32_t sslot[kMark ? 2 : 1][kMark ? kThreads : 1];  // coverage pass: the slots of the batch
   __shared__ uint8_t smark[kMark ? 2 : 1][kMark ? kThreads : 1];    // coverage pass: the batch's blended records
   // coverage pass: per record of the batch, (g0, o0, -tau0 log2 e) and (g1, o1, qcut'), with o = -g . (centre - tile
-  // origin), so a fragment's lx = g0 . (pixel - tile origin) + o0 is two FMAs (g, o and the cutoff scaled to give q in
-  // units of the exponent of 2) (written by the record's thread in the
-  // culling step, read after its barrier; the next batch rewrites it only after the batch's closing barrier)
+  // origin), so a fragment's lx = g0 . (pixel - tile origin) + o0 is two FMAs (g, o and the cutoff scaled to give q
+  // in units of the exponent of 2); written by the record's thread in the culling step, read after its barrier, and
+  // rewritten by the next batch only after this batch's closing barrier
   __shared__ float4 mrec[kMark ? 2 * kThreads : 1];
   __shared__ uint32_t masks[kThreads / 32][kThreads / 32];  // [warp block][loader warp]: records touching the block
   __shared__ __align__(8) uint64_t bars[2];
