@@ -324,10 +324,13 @@ SL_API int sl_sort_keys32(const uint32_t* keys_dev, uint32_t n, uint32_t bits, u
 /* sl_sort_keys16 without any device allocation, for callers that may not allocate (a host engine that owns all
  * device memory through its own pool under a hard cap, or a frame loop whose latency budget rules out allocator
  * calls).  No counterpart in the reference.  Same inputs, output and status codes as sl_sort_keys16, for
- * n <= 1,048,576 keys (larger n: SL_ERR_INVALID_ARG).  Scratch is one fixed 6.5 MiB device array inside the library,
- * held by every GPU that loads it until the process exits; the caller still passes keys and order.  The first call
- * on a device looks up the array's device address (make it before any stream capture).  All calls share the array:
- * calls that overlap on the GPU (other streams, other threads) race, so serialise them. */
+ * n <= 1,048,576 keys (larger n: SL_ERR_INVALID_ARG).  Scratch is one fixed device array inside the library
+ * (6,644,224 B: exactly one sort of 1,048,576 keys), held by every GPU that loads it until the process exits; the
+ * caller still passes keys and order.  Every call looks up the array's device address in the current context (no
+ * address is kept between calls, so a cudaDeviceReset or another context on the device is safe); the first call in
+ * a context loads the library's module, so make it before any stream capture.  All calls share the array and it
+ * keeps the last call's contents (each call clears what must start at zero): calls that overlap on the GPU (other
+ * streams, other threads) race, so serialise them. */
 SL_API int sl_sort_keys16_noalloc(const uint16_t* keys_dev, uint32_t n, uint32_t* order_dev, void* stream);
 
 /* ---- batched frames (no counterpart in the reference, which draws one RenderFrame per call) ------------------- */

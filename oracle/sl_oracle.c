@@ -130,11 +130,11 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   uint32_t material = ORC_EMITTER_MATERIAL;
   float keep = 1.0f;
   v3 vel = v3_make(0.0f, 0.0f, 0.0f);
-  if (i > count && node == 0xFFFFFFFFu) { /* :226-230 */
+  if (i > count && node == 0xFFFFFFFFu) { /* :123-127 */
     g = &emitters[i - count - 1u];
     mu = v3_make(g->mu[0], g->mu[1], g->mu[2]);
     rot = quat_to_mat(g->quat);
-  } else { /* :232-251 */
+  } else { /* :128-149 */
     g = node != 0xFFFFFFFFu ? &lod->nodes[node] : &gaussians[i];
     uint32_t part = g->part_surface & 0xffffu;
     if (part > ORC_MAX_PARTS - 1u) part = ORC_MAX_PARTS - 1u;
@@ -160,9 +160,9 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
                   V[1] * mu.x + V[5] * mu.y + V[9] * mu.z + V[13] * 1.0f,
                   V[2] * mu.x + V[6] * mu.y + V[10] * mu.z + V[14] * 1.0f);
   float depth = -tv.z;
-  if (depth < f->near_plane || depth > f->far_plane) return ORC_INVALID; /* :302-303 */
+  if (depth < f->near_plane || depth > f->far_plane) return ORC_INVALID; /* :199-200 */
 
-  /* view-space covariance W R S^2 R^T W^T (:305-309) */
+  /* view-space covariance W R S^2 R^T W^T (:202-206) */
   m3 W;
   W.c[0] = v3_make(V[0], V[1], V[2]);
   W.c[1] = v3_make(V[4], V[5], V[6]);
@@ -179,7 +179,7 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
     for (int r = 0; r < 3; r++)
       for (int c = 0; c < 3; c++) cv[r][c] = mk[0][r] * mk[0][c] + mk[1][r] * mk[1][c] + mk[2][r] * mk[2][c];
   }
-  /* the sharp covariance (coverage cap); blurred: + (W vel)(W vel)^T / 12 (:207-209) */
+  /* the sharp covariance (coverage cap); blurred: + (W vel)(W vel)^T / 12 (:208-210) */
   int blurred = vel.x != 0.0f || vel.y != 0.0f || vel.z != 0.0f;
   m3 cov_s;
   for (int c = 0; c < 3; c++) cov_s.c[c] = v3_make(cv[0][c], cv[1][c], cv[2][c]);
@@ -192,7 +192,7 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   m3 cov;
   for (int c = 0; c < 3; c++) cov.c[c] = v3_make(cv[0][c], cv[1][c], cv[2][c]);
 
-  /* EWA Jacobian, pixel units, y up (:315-334) */
+  /* EWA Jacobian, pixel units, y up (:212-232) */
   float fx = f->focal[0], fy = f->focal[1];
   float iz = 1.0f / depth;
   float px = fx * tv.x * iz;
@@ -214,14 +214,14 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   float det = a * c - b * b;
   if (det <= 0.0f) return ORC_INVALID;
 
-  /* volumetric peak optical depth (:337-364) */
+  /* volumetric peak optical depth (:234-261) */
   float dlen = sqrtf(v3_dot(tv, tv));
   v3 d = v3_make(tv.x / dlen, tv.y / dlen, tv.z / dlen);
   v3 dl = m3_tmul_v(wr, d);
   v3 is2 = v3_make(1.0f / s2.x, 1.0f / s2.y, 1.0f / s2.z);
   float q = v3_dot(v3_make(dl.x * dl.x, dl.y * dl.y, dl.z * dl.z), is2);
   float q_s = q, kappa = g->kappa;
-  if (blurred) { /* Sherman-Morrison for q, the determinant lemma for kappa (:241-250) */
+  if (blurred) { /* Sherman-Morrison for q, the determinant lemma for kappa (:242-250) */
     v3 vl = m3_tmul_v(rot, vel);
     float mv2 = v3_dot(v3_make(vl.x * vl.x, vl.y * vl.y, vl.z * vl.z), is2);
     float dv = v3_dot(v3_make(dl.x * vl.x, dl.y * vl.y, dl.z * vl.z), is2);
@@ -230,7 +230,7 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   }
   const float kTwoPi = 6.283185307f;
   float tau0 = kappa * sqrtf(kTwoPi / q) * sqrtf(fmaxf(det0, 0.0f) / det);
-  if (blurred && f->palette[3][3] > 0.5f) { /* coverage cap (:252-272) */
+  if (blurred && f->palette[3][3] > 0.5f) { /* coverage cap (:251-268) */
     v3 cs0 = m3_mul_v(cov_s, j0), cs1 = m3_mul_v(cov_s, j1);
     float a_s = v3_dot(j0, cs0) + f->lowpass_px2;
     float b_s = v3_dot(j0, cs1);
@@ -244,7 +244,7 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   }
   tau0 *= keep; /* :384 */
 
-  /* cutoff radius (:393-398) */
+  /* cutoff radius (:290-295) */
   const float kAlphaMin = 1.0f / 255.0f;
   float tau_min = -sl_logf(1.0f - kAlphaMin);
   float tau_cut = tau0;
@@ -252,7 +252,7 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   float qcut = 2.0f * sl_logf(tau_cut / tau_min);
   float r = sqrtf(qcut);
 
-  /* eigen-axes of the 2x2 covariance (:400-412) */
+  /* eigen-axes of the 2x2 covariance (:297-309) */
   float mid = 0.5f * (a + c);
   float disc = sqrtf(0.25f * (a - c) * (a - c) + b * b);
   float l0 = mid + disc;
@@ -274,12 +274,12 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   float tnx = 2.0f / f->viewport[0], tny = 2.0f / f->viewport[1];
   float ax0 = e0x * sl0 * r * tnx, ay0 = e0y * sl0 * r * tny;
   float ax1 = e1x * sl1 * r * tnx, ay1 = e1y * sl1 * r * tny;
-  if (sl0 * r < 0.1f) return ORC_INVALID; /* :413-414 */
-  float ccx = px * tnx, ccy = py * tny;   /* :416-418 */
+  if (sl0 * r < 0.1f) return ORC_INVALID; /* :310-311 */
+  float ccx = px * tnx, ccy = py * tny;   /* :313-315 */
   float extx = fabsf(ax0) + fabsf(ax1), exty = fabsf(ay0) + fabsf(ay1);
   if (fabsf(ccx) - extx > 1.0f || fabsf(ccy) - exty > 1.0f) return ORC_INVALID;
 
-  /* colour (:420-453) */
+  /* colour (:317-350) */
   float rgb[3] = {g->albedo[0], g->albedo[1], g->albedo[2]};
   if (material == ORC_EMITTER_MATERIAL) {
     /* emitted radiance, shown as itself */
@@ -305,7 +305,7 @@ static uint32_t project_one(uint32_t i, const sl_gaussian* gaussians, uint32_t c
   if (material != ORC_EMITTER_MATERIAL)
     for (int k = 0; k < 3; k++) rgb[k] *= f->albedo_scale;
 
-  /* 16-bit log-depth key (:466-471) */
+  /* 16-bit log-depth key (:363-369) */
   float lnr = sl_logf(f->far_plane / f->near_plane);
   float t = clampf(sl_logf(depth / f->near_plane) / lnr, 0.0f, 1.0f);
   uint32_t key = 65535u - (uint32_t)(t * 65535.0f + 0.5f);

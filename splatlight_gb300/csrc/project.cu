@@ -104,7 +104,7 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
     g1 = __ldg(src + 1);
     g2 = __ldg(src + 2);
     g3 = __ldg(src + 3);
-    if (i > P.count && node == 0xFFFFFFFFu) {  // project.wgsl:226-230
+    if (i > P.count && node == 0xFFFFFFFFu) {  // project.wgsl:123-127
       mu = v3(g0.x, g0.y, g0.z);
     } else {  // :232-251
       part = __float_as_uint(g2.w) & 0xffffu;
@@ -165,7 +165,7 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
       for (int r = 0; r < 3; r++)
 #pragma unroll
         for (int c = 0; c < 3; c++) cv[r][c] = mk0[r] * mk0[c] + mk1[r] * mk1[c] + mk2[r] * mk2[c];
-      // the sharp covariance, kept for the coverage cap; blurred: + (W vel)(W vel)^T / 12 (project.wgsl:207-209)
+      // the sharp covariance, kept for the coverage cap; blurred: + (W vel)(W vel)^T / 12 (project.wgsl:208-210)
       const bool blurred = vel.x != 0.0f || vel.y != 0.0f || vel.z != 0.0f;
       M3 cov_s;
       cov_s.c[0] = v3(cv[0][0], cv[1][0], cv[2][0]);
@@ -215,7 +215,7 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
         float kappa = __uint_as_float(__float_as_uint(g0.w));
         if (blurred) {
           // Sigma' = Sigma + v v^T / 12 in the Gaussian's frame: Sherman-Morrison for the view ray's q, the
-          // determinant lemma for the density that keeps the mass (project.wgsl:241-250)
+          // determinant lemma for the density that keeps the mass (project.wgsl:242-250)
           const V3 vl = v3(dot3(rot.c[0], vel), dot3(rot.c[1], vel), dot3(rot.c[2], vel));
           const float mv2 = dot3(v3(vl.x * vl.x, vl.y * vl.y, vl.z * vl.z), is2);
           const float dv = dot3(v3(dl.x * vl.x, dl.y * vl.y, dl.z * vl.z), is2);
@@ -226,7 +226,7 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
         tau0 = kappa * sqrtf(kTwoPi / q) * sqrtf(fmaxf(det0, 0.0f) / det);
         if (blurred && P.blur_cov) {
           // coverage cap: a box shutter averages coverage, so the smear's peak alpha is capped at the sharp splat's
-          // (same Jacobian) x sqrt(det_s / det) (project.wgsl:252-272)
+          // (same Jacobian) x sqrt(det_s / det) (project.wgsl:251-268)
           const V3 cs0 = mulv(cov_s, j0), cs1 = mulv(cov_s, j1);
           const float a_s = dot3(j0, cs0) + P.lowpass_px2;
           const float b_s = dot3(j0, cs1);
@@ -269,7 +269,7 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
         float extx = fabsf(ax0) + fabsf(ax1), exty = fabsf(ay0) + fabsf(ay1);
         live = !(sl0 * r < 0.1f) && !(fabsf(ccx) - extx > 1.0f || fabsf(ccy) - exty > 1.0f);
         if (live) {
-          // radiance (project.wgsl:420-453)
+          // radiance (project.wgsl:317-350)
           float cr = g3.x, cg = g3.y, cb = g3.z;
           if (material == kEmitterMaterial) {
           } else if (P.view_mode == 3u) {
@@ -300,7 +300,7 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
             cg *= P.albedo_scale;
             cb *= P.albedo_scale;
           }
-          // 16-bit log-depth key (:466-471)
+          // 16-bit log-depth key (project.wgsl:363-369)
           float lnr = sl_logf(P.far_plane / P.near_plane);
           float tt = clampf(sl_logf(depth / P.near_plane) / lnr, 0.0f, 1.0f);
           uint32_t k = 65535u - (uint32_t)(tt * 65535.0f + 0.5f);

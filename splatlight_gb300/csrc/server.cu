@@ -59,6 +59,9 @@ struct sl_server {
   float* arena = nullptr;
   uint64_t slot_floats = 0;
   std::vector<uint32_t> free_slots;
+  // per result slot: kSlotFree, kSlotBusy (a batch writes it), kSlotReady (its result waits in the queue),
+  // kSlotDelivered (handed out by poll; only this state may be released)
+  std::vector<uint8_t> slot_state;
   // queues
   std::mutex mu;
   std::condition_variable cv;
@@ -78,6 +81,8 @@ struct sl_server {
 
 namespace sl {
 namespace {
+
+enum : uint8_t { kSlotFree = 0, kSlotBusy = 1, kSlotReady = 2, kSlotDelivered = 3 };
 
 uint64_t footprint_slots(const sl_renderer* r, const sl_render_frame& f) {
   return ((uint64_t)r->count + 1u + (uint32_t)f.palette[3][1] + 255) & ~255ull;
@@ -100,6 +105,7 @@ void form_batch(sl_server* S, Pipe& p) {
     S->pending.pop_front();
     r.result_slot = S->free_slots.back();
     S->free_slots.pop_back();
+    S->slot_state[r.result_slot] = kSlotBusy;
     p.reqs.push_back(r);
   }
 }
@@ -156,6 +162,7 @@ void fail_batch(sl_server* S, Pipe& p, int code) {
     res.t_start = r.t_start;
     res.t_done = t;
     res.image = nullptr;
+    S->slot_state[r.result_slot] = kSlotFree;
     S->free_slots.push_back(r.result_slot);
     S->results.push_back(res);
     S->failed++;
@@ -196,6 +203,7 @@ void complete(sl_server* S, Pipe& p) {
     res.t_start = r.t_start;
     res.t_done = t;
     res.image = S->arena + (uint64_t)r.result_slot * S->slot_floats;
+    S->slot_state[r.result_slot] = kSlotReady;
     S->results.push_back(res);
     S->completed++;
   }
@@ -320,6 +328,7 @@ int sl_server_create(sl_renderer* const* renderers, sl_lighting* const* lighting
     return cuda_fail(e, "pinned result slots");
   }
   for (uint32_t k = o.result_slots; k > 0; k--) S->free_slots.push_back(k - 1);
+  S->slot_state.assign(o.result_slots, kSlotFree);
   S->pipes.resize(o.pipelines);
   int rc = SL_OK;
   for (Pipe& p : S->pipes) {
@@ -394,7 +403,9 @@ int sl_server_poll(sl_server* S, sl_server_result* out, uint32_t cap, uint32_t* 
     S->cv.wait_for(lk, std::chrono::microseconds(wait_us), [S] { return !S->results.empty(); });
   uint32_t n = 0;
   while (n < cap && !S->results.empty()) {
-    out[n++] = S->results.front();
+    const sl_server_result& res = S->results.front();
+    if (res.status == SL_OK) S->slot_state[res.result_slot] = kSlotDelivered;
+    out[n++] = res;
     S->results.pop_front();
   }
   *n_out = n;
@@ -405,8 +416,11 @@ int sl_server_release(sl_server* S, uint32_t result_slot) {
   if (!S) return fail(SL_ERR_INVALID_ARG, "null server");
   std::lock_guard<std::mutex> lk(S->mu);
   if (result_slot >= S->opt.result_slots) return fail(SL_ERR_INVALID_ARG, "no such result slot");
-  for (uint32_t f : S->free_slots)
-    if (f == result_slot) return fail(SL_ERR_INVALID_ARG, "result slot released twice");
+  const uint8_t st = S->slot_state[result_slot];
+  if (st != kSlotDelivered)
+    return fail(SL_ERR_INVALID_ARG, st == kSlotFree ? "result slot released twice (or never handed out)"
+                                                    : "result slot not yet handed out by sl_server_poll");
+  S->slot_state[result_slot] = kSlotFree;
   S->free_slots.push_back(result_slot);
   S->cv.notify_all();
   return SL_OK;

@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(kThreads) shade_kernel(const __grid_constant__
 }
 
 // Batched: the marked scene Gaussians of every lit view (the coverage pass), shaded from the view's eye, with the
-// palette and albedo scale the projection applies to bound radiance (project.wgsl:424-453), written into the splat
+// palette and albedo scale the projection applies to bound radiance (project.wgsl:321-350), written into the splat
 // records.
 __global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __restrict__ views,
                                                           const BatchScene* __restrict__ scenes,

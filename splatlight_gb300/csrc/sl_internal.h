@@ -106,7 +106,29 @@ cudaError_t launch_lod_colour_top(uint32_t G, float gain, uint32_t colour_all, c
                                   const uint32_t* lvl_int, uint32_t depths, const uint32_t* flags,
                                   const float4* colour, const float4* lo_b, float4* ncolour, cudaStream_t s);
 
-// sort.cu: onesweep LSD radix sort of 16-bit keys with u32 values.
+// sort.cu: onesweep LSD radix sort of 16-bit keys with u32 values, over tiles of kSortTileKeys keys.
+constexpr uint32_t kSortTileKeys = 6144;
+constexpr size_t sort_tiles_const(uint32_t n) { return (n + kSortTileKeys - 1) / kSortTileKeys; }
+
+// Scratch layout of one standalone 16-bit sort of n keys (sort_api.cu): every offset 256-byte aligned.
+struct Sort16Layout {
+  size_t hist, counters, tile_ctr, status, keys_alt, vals_alt, total;
+  uint32_t tiles;
+};
+constexpr size_t align256c(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr Sort16Layout sort16_layout(uint32_t n) {
+  Sort16Layout L{};
+  L.tiles = (uint32_t)sort_tiles_const(n ? n : 1);
+  L.hist = 0;                                                  // [2][256] digit counts
+  L.counters = align256c(L.hist + 2 * 256 * 4);                // FrameCounters
+  L.tile_ctr = align256c(L.counters + sizeof(FrameCounters));  // one tile ticket per pass
+  L.status = align256c(L.tile_ctr + 16);                       // look-back words, [2][tiles][256]
+  L.keys_alt = align256c(L.status + 2ull * 256 * 4 * L.tiles);
+  L.vals_alt = align256c(L.keys_alt + 2ull * n);
+  L.total = align256c(L.vals_alt + 4ull * n);
+  return L;
+}
+
 struct SortScratch {
   uint16_t* keys_alt;
   uint32_t* vals_alt;

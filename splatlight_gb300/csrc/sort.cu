@@ -18,6 +18,7 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kItems = 24;
 constexpr uint32_t kTile = kThreads * kItems;  // 6144
+static_assert(kTile == kSortTileKeys, "sort tile size and the scratch layouts disagree");
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
@@ -234,7 +235,7 @@ __global__ void __launch_bounds__(kThreads) digit_hist32_kernel(const uint32_t* 
 
 }  // namespace
 
-size_t sort_tiles_for(uint32_t n) { return (n + kTile - 1) / kTile; }
+size_t sort_tiles_for(uint32_t n) { return sort_tiles_const(n); }
 
 cudaError_t launch_digit_hist32(const uint32_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s) {
   if (n == 0) return cudaSuccess;

@@ -38,33 +38,7 @@ static cudaError_t scratch_alloc(char** base, size_t bytes, cudaStream_t s) {
   return cudaMallocFromPoolAsync(reinterpret_cast<void**>(base), bytes, pool, s);
 }
 
-// Scratch layout of one 16-bit sort of up to n keys (all offsets 256-byte aligned).
-struct Sort16Layout {
-  size_t hist, counters, tile_ctr, status, keys_alt, vals_alt, total;
-  uint32_t tiles;
-};
-
-static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
-Sort16Layout sort16_layout(uint32_t n) {
-  Sort16Layout L;
-  L.tiles = (uint32_t)sort_tiles_for(n ? n : 1);
-  size_t off = 0;
-  L.hist = off;
-  off = align256(off + 2 * 256 * 4);
-  L.counters = off;
-  off = align256(off + sizeof(FrameCounters));
-  L.tile_ctr = off;
-  off = align256(off + 16);
-  L.status = off;
-  off = align256(off + 2ull * 256 * 4 * L.tiles);
-  L.keys_alt = off;
-  off = align256(off + 2ull * n);
-  L.vals_alt = off;
-  off = align256(off + 4ull * n);
-  L.total = off;
-  return L;
-}
+static size_t align256(size_t x) { return align256c(x); }
 
 // Runs the sort in `base` (a scratch block laid out by sort16_layout(n)); clears what must start at zero.
 cudaError_t sort16_in_scratch(const uint16_t* keys, uint32_t n, uint32_t* order, char* base, cudaStream_t s) {

@@ -6,10 +6,10 @@
 // loads this library keeps for the life of the process.
 //
 // Host code cannot pass the array's name to a kernel: on the host that name is only a stand-in for the device
-// symbol, not a device address.  The first call on each device therefore looks the address up with
-// cudaGetSymbolAddress while that device is current and caches it; later calls on that device reuse it.  Make the
-// first call on a device before any stream capture is in progress.
-#include <mutex>
+// symbol, not a device address.  Every call therefore looks the address up with cudaGetSymbolAddress while the
+// caller's device is current.  No address is cached: after cudaDeviceReset, or in another context on the same
+// device, the library's module is loaded again (possibly at another address), and a cached pointer would be stale.
+// The first call in a context loads the module; make it before any stream capture is in progress.
 #include <string>
 
 #include "sl_runtime.h"
@@ -17,44 +17,19 @@
 namespace sl {
 
 // defined in sort_api.cu
-struct Sort16Layout {
-  size_t hist, counters, tile_ctr, status, keys_alt, vals_alt, total;
-  uint32_t tiles;
-};
-Sort16Layout sort16_layout(uint32_t n);
 cudaError_t sort16_in_scratch(const uint16_t* keys, uint32_t n, uint32_t* order, char* base, cudaStream_t s);
 
 namespace {
 
 constexpr uint32_t kNoAllocMaxKeys = 1u << 20;  // 1,048,576 keys
-// sort16_layout(kNoAllocMaxKeys): histograms 2 KiB, counters and tile counters 256 B each (256-byte aligned),
-// look-back status 2 passes x 256 tiles x 256 digits x 4 B, keys 2 B and values 4 B per key
-constexpr size_t kScratchBytes = 2048 + 256 + 256 + 2ull * 256 * 256 * 4 + 2ull * kNoAllocMaxKeys +
-                                 4ull * kNoAllocMaxKeys;  // 6,818,304 B (6.5 MiB)
-
-std::mutex g_mu;
-char* g_scratch_addr[128] = {};  // device address of the array, per device ordinal
+// exactly the layout one sort of kNoAllocMaxKeys keys needs: digit histograms, counters and tile tickets, the
+// look-back words of both passes over its tiles, the ping-pong keys (2 B) and values (4 B)
+constexpr size_t kScratchBytes = sort16_layout(kNoAllocMaxKeys).total;
+static_assert(kScratchBytes < (8u << 20), "the no-allocation scratch array should stay modest");
 
 }  // namespace
 
 static __device__ __align__(256) unsigned char g_sort16_scratch[kScratchBytes];
-
-// Device address of g_sort16_scratch on the current device (looked up once per device).
-static cudaError_t scratch_address(char** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 128) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_sort16_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_addr[dev] = static_cast<char*>(p);
-  }
-  *out = g_scratch_addr[dev];
-  return cudaSuccess;
-}
 
 }  // namespace sl
 
@@ -68,9 +43,10 @@ extern "C" int sl_sort_keys16_noalloc(const uint16_t* keys_dev, uint32_t n, uint
                                         " keys (its fixed scratch size); got " + std::to_string(n) +
                                         ": use sl_sort_keys16");
   if (sort16_layout(n).total > kScratchBytes) return fail(SL_ERR_INVALID_ARG, "scratch layout exceeds the array");
-  char* base = nullptr;
-  cudaError_t e = scratch_address(&base);
+  void* sym = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&sym, g_sort16_scratch);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(sort scratch)");
+  char* base = static_cast<char*>(sym);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   // every call shares the array and it keeps the previous call's contents: sort16_in_scratch clears the histograms,
   // counters and look-back status before use; keys/values scratch is fully rewritten by the passes

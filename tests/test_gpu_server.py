@@ -195,3 +195,34 @@ def test_bounded_pending_queue(world):
         got = _drain(srv, 3)
         assert all(r.status == 0 for r in got.values())
         assert srv.stats()["rejected"] == 1
+
+
+def test_release_only_delivered_slots(world):
+    """sl_server_release accepts only a slot that sl_server_poll handed out: a slot a batch may still be writing, one
+    never handed out, and one already released are refused, so two views can never share a result slot."""
+    scenes, rs, ls = world
+    a = scenes[0]
+    from splatlight_gb300 import _native as N
+    lib = N.lib()
+    with RenderServer(rs, ls, max_views=1, pipelines=1, max_view_pixels=64 * 64, result_slots=2) as srv:
+        assert lib.sl_server_release(srv._h, 0) == -1          # never handed out
+        srv.submit(0, _frame(a, 64, 64, VIEW_FLAT, a.eye), a.eye, tag=0)
+        got = []
+        for _ in range(200):
+            got = srv.poll(wait_us=50_000, copy=False)       # poll(copy=False) releases what it delivers
+            if got:
+                break
+        assert got and got[0].status == 0
+        assert lib.sl_server_release(srv._h, 1) == -1          # the other slot was never used
+        assert "released twice" in N.last_error()
+        # a delivered slot, released by hand exactly once
+        srv.submit(0, _frame(a, 64, 64, VIEW_FLAT, a.eye), a.eye, tag=1)
+        n = N.C.c_uint32()
+        for _ in range(200):
+            N.check(lib.sl_server_poll(srv._h, srv._res, len(srv._res), N.C.byref(n), 50_000))
+            if n.value:
+                break
+        assert n.value == 1 and srv._res[0].status == 0
+        slot = int(srv._res[0].result_slot)
+        assert lib.sl_server_release(srv._h, slot) == 0
+        assert lib.sl_server_release(srv._h, slot) == -1
