@@ -1,20 +1,31 @@
-"""Benchmark of the GB300 splat pipeline (one JSON line on stdout).
+"""Benchmark of the GB300 splat pipeline: one JSON line on stdout (per-leg details as one JSON line on stderr).
 
-Workload (default): the hill-like scene of 1,048,576 Gaussians (seed 1) rendered at 1920x1080, fov 50 deg -- the
-plain single-frame forward configuration.  A step is one frame of the plain per-view path through the C ABI:
-project -> onesweep depth sort -> tile binning (+ tile sort, ranges) -> front-to-back composite, lit view.
+Headline workload -- the ragged batch: 64 lit views over 4 resident scenes (cornell-like 100k and 400k Gaussians,
+seed 0; hill-like 1M and 2M, seed 1), each view's resolution drawn from 256^2, 512^2, 1280x720 and 1920x1080, its
+camera on a sphere of radius U[3, 6] around the scene centre.  A step is one batch of those 64 views through the
+batched path (sl_batch_render: one CUDA graph of the fused chain over every view).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--config hill|cornell] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-value      views/s over all ranks, device time: CUDA events around each frame on the render stream, the L2 flushed
-           (a 256 MiB write) between frames outside the timed region, inputs resident in HBM.
-e2e        the same metric through the public API with host buffers: each step uploads the frame's RenderFrame and
-           part records and reads the W x H x 4 fp32 image back into pinned host memory, wall clock.
-roofline   the dominant kernel (by device time) against its bound; the sort is reported beside it against HBM.
-cpu_baseline  the CPU restatement (oracle/, a port of the reference algorithm) timed on this host's cores (rank 0).
---impl reference  the CPU restatement of the reference pipeline alone (the reference's WGSL needs WebGPU, which is
-           not available on this machine), all host threads, each step one full frame of the same workload.
-Replicas only on N > 1: every rank renders its own frames, no collective on the data path.
+value      views/s of the batched path over all ranks (replicas), device time: CUDA events around each batch on the
+           render stream, the L2 flushed (a 256 MiB write) before every batch outside the timed region, the scenes,
+           their lighting maps and the views' frames resident in HBM.
+e2e        the same through the public C ABI with host buffers: the views' frames, eyes and light scales staged from
+           the host and every image written into page-locked host memory, wall clock per batch.
+batched    on the same 64 views: the plain per-view path (per view the shading pass over every Gaussian of its scene,
+           then project/sort/bin/composite: the reference's order) and the per-view deferred path (each view as a
+           one-view batch: deferred shading without batching), views/s from the summed per-view device times, the
+           ratios, and the largest image difference between the batched and the plain images.
+served     Poisson arrivals over 6 resident scenes (50k..3M Gaussians) at 100, 500 and 2000 requests/s: views/s and
+           p50/p99 latency (lambda 500 over the configured 60 s window, the others over --serve-seconds-other).
+plain      the single-frame forward of the hill-like 1,048,576-Gaussian scene at 1920x1080 (lit) on the plain path.
+sort       the stable 16-bit key sort alone on 2^26 keys, GB/s against the measured HBM peak.
+roofline   the batched chain's dominant stage against its bound (per-stage device times measured live).
+cpu_baseline  the CPU restatement of the reference pipeline (oracle/, kind "port") on this host's cores, on one view
+           of each scene of the same mix.
+--impl reference  that CPU restatement alone on the same workload, each step one view of the mix, all host threads
+           (the reference's own WGSL needs WebGPU: unavailable on this machine).
+Replicas only on N > 1: every rank renders its own batches, no collective on the data path.
 """
 from __future__ import annotations
 
@@ -34,8 +45,8 @@ sys.path.insert(0, str(ROOT))
 
 MEASURED = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM = 6800.0  # GB/s
-# shade; project, 2 depth-sort passes, binning (counts, offsets and entries in one pass), 2 tile-sort passes, ranges,
-# composite
+# the plain per-view frame: shade; project, 2 depth-sort passes, binning (counts, offsets and entries in one pass),
+# 2 tile-sort passes, ranges, composite
 KERNELS_PER_FRAME = 9
 # DRAM bytes per Gaussian of one shade_kernel launch (read + write), from ncu on the 1,048,576-Gaussian frame
 SHADE_DRAM_BYTES_PER_G = (464.748544e6 + 22.484992e6) / 1048576
@@ -179,89 +190,6 @@ def batch_mix(n_views=64, seed=7):
     return scenes, views
 
 
-def run_batch(args, stream, flush):
-    """Batched path vs the plain per-view path on the ragged 64-view mix (device time, L2 flushed between steps)."""
-    import torch
-    from splatlight_gb300.batch import BatchRenderer, View
-    from splatlight_gb300.lighting import camera_forward, for_scene
-    from splatlight_gb300.renderer import SplatRenderer
-    scenes, mix = batch_mix(n_views=args.batch_views)
-    rs, ls = [], []
-    for s in scenes:
-        r = SplatRenderer(s.gaussians, s.parts)
-        L = for_scene(r, s)
-        L.update(s.eye, camera_forward(s))   # the resident light state: maps at the scene's reference camera
-        rs.append(r)
-        ls.append(L)
-    torch.cuda.synchronize()
-    views = [View(k, f, e) for k, f, e in mix]
-    sizes = [(int(f["viewport"][1]), int(f["viewport"][0])) for _, f, _ in mix]
-    pix = sum(h * w for h, w in sizes)
-    B = BatchRenderer(rs, ls, max_views=len(views))
-    out = torch.empty(4 * pix, dtype=torch.float32, device="cuda")
-    tile, tune_ms = B.autotune(views, reps=2)
-    sc = stream.cuda_stream
-
-    def batched():
-        return B.render_device(views, out=out, stream=sc)
-
-    plain_out = [torch.empty((h, w, 4), dtype=torch.float32, device="cuda") for h, w in sizes]
-
-    def plain():
-        for (k, f, e), o in zip(mix, plain_out):
-            ls[k].shade(e, stream=sc)
-            rs[k].render(f, out=o, stream=sc)
-
-    def timed(fn, steps):
-        ts = []
-        for _ in range(steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            fn()
-            b.record(stream)
-            b.synchronize()
-            ts.append(a.elapsed_time(b))
-        return statistics.median(ts)
-
-    for _ in range(max(args.warmup, 3)):
-        batched()
-        plain()
-    torch.cuda.synchronize()
-    steps = max(3, min(args.steps, 10))
-    ms_b = timed(batched, steps)
-    st = B.last_stats
-    ms_p = timed(plain, steps)
-    # image error of every batched view against the plain per-view path (same light state)
-    _, offs = batched()
-    torch.cuda.synchronize()
-    err = 0.0
-    for (h, w), o, po in zip(sizes, offs, plain_out):
-        img = out[int(o):int(o) + 4 * h * w].view(h, w, 4)
-        err = max(err, float((img - po).abs().max().item()))
-    n = len(views)
-    res = {"workload": f"{n} lit views over 4 resident scenes (cornell-like 100k, 400k; hill-like 1M, 2M "
-                       "Gaussians), resolutions from 256^2, 512^2, 1280x720, 1920x1080, cameras on radius U[3,6] "
-                       "spheres; light maps resident per scene",
-           "views": n, "pixels": pix, "batched_views_per_s": round(n * 1000.0 / ms_b, 2),
-           "batched_ms_per_batch": round(ms_b, 3),
-           "plain_views_per_s": round(n * 1000.0 / ms_p, 2), "plain_ms_per_batch": round(ms_p, 3),
-           "speedup_vs_plain": round(ms_p / ms_b, 3), "max_abs_err_vs_plain": err,
-           "tile": f"{tile[0]}x{tile[1]}", "autotune_ms": {k: round(v, 3) for k, v in tune_ms.items()},
-           "slots": int(st.slots), "visible": int(st.visible), "entries": int(st.entries),
-           "shaded": int(st.shaded), "reshaded_views": int(st.reshaded_views),
-           "max_radiance": round(float(st.max_radiance), 4),
-           "graph_replayed": int(st.graph_replayed), "kernels_per_batch": BATCH_KERNELS}
-    B.close()
-    for L in ls:
-        L.close()
-    for r in rs:
-        r.close()
-    return res
-
-
 SERVE_RES = [(512, 512), (1280, 720), (1920, 1080)]
 
 
@@ -315,7 +243,7 @@ def run_serving(args, rates=(100, 500, 2000)):
     out = {"workload": "Poisson arrivals over 6 resident hill-like scenes (50k, 200k, 500k, 1M, 2M, 3M Gaussians, "
                        "seeds 10-15), cameras on radius U[3,8] spheres, 512^2 / 1280x720 / 1920x1080, light scale "
                        "U[0.5,2], lit; images delivered to pinned host memory",
-           "seconds_per_rate": args.serve_seconds, "rates": []}
+           "seconds": {"500": args.serve_seconds, "100 and 2000": args.serve_seconds_other}, "rates": []}
     # the pending queue is bounded (512 requests, a few batches' worth): beyond it a request is refused at submit,
     # which keeps the latency of admitted requests bounded when arrivals outrun the device
     srv = RenderServer(rs, ls, max_views=64, pipelines=2, max_slots=48 << 20, max_pixels=24 << 20,
@@ -335,7 +263,8 @@ def run_serving(args, rates=(100, 500, 2000)):
     while got < 16 + 96:
         got += len(srv.poll(wait_us=50000, copy=False))
     for lam in rates:
-        n = max(1, int(lam * args.serve_seconds))
+        window = args.serve_seconds if lam == 500 else args.serve_seconds_other
+        n = max(1, int(lam * window))
         gaps = rng.exponential(1.0 / lam, size=n)
         reqs = [request() for _ in range(n)]
         arrivals = {}
@@ -385,7 +314,8 @@ def run_serving(args, rates=(100, 500, 2000)):
         n_adm = n - refused
         st1 = srv.stats()
         d_batches = st1["batches"] - st0["batches"]
-        out["rates"].append({"lambda": lam, "requests": n, "refused_at_admission": refused, "failed": fails,
+        out["rates"].append({"lambda": lam, "seconds": window, "requests": n, "refused_at_admission": refused,
+                             "failed": fails,
                              "batches": d_batches,
                              "graph_captures": d_batches - (st1["graph_replays"] - st0["graph_replays"]),
                              "relaunches": st1["relaunches"] - st0["relaunches"],
@@ -611,45 +541,307 @@ def run_diff(args, stream, flush):
             "grad_norms": {k: round(v, 6) for k, v in gnorm.items()}}
 
 
-# bproject, scan and compaction of the visible keys, 3 depth-sort passes, binning (counts, offsets and entries in one
-# pass), 2 tile-sort passes, runs (to ranges), coverage pass, shading list (one pass), bshade, bcomposite
+# bproject, scan of the blocks' visible counts, compaction of the visible keys, 3 depth-sort passes, binning (counts,
+# offsets and entries in one pass), 2 tile-sort passes, runs (to ranges), coverage pass, shading list (one pass),
+# bshade, bcomposite
 BATCH_KERNELS = 14
+STAGES = ("project", "depth_sort", "bin", "coverage", "shade", "composite")
 
 
-def deferred_one_view(args, s, r, L, f, fwd, plain_out, flush, stream):
-    """The same lit frame through the batch API as a batch of one view: projection, sort and binning first, then only
-    the Gaussians the coverage pass marks are shaded (deferred shading) before the composite.  Device time per view,
-    L2 flushed between views, and the largest image difference from the plain path's frame (same light state)."""
+def timed_device(stream, flush, fn, steps):
+    """Median device time (ms) of fn() over `steps` calls, events on `stream`, the L2 flushed before each call."""
     import torch
-    from splatlight_gb300.batch import BatchRenderer, View
-    H, W = int(f["viewport"][1]), int(f["viewport"][0])
-    B = BatchRenderer([r], [L], max_views=1)
-    views = [View(0, f, s.eye)]
-    out = torch.empty(4 * W * H, dtype=torch.float32, device="cuda")
-    sc = stream.cuda_stream
-    for _ in range(max(args.warmup, 3)):
-        B.render_device(views, out=out, stream=sc)
     ts = []
-    for _ in range(max(5, min(args.steps, 20))):
+    for _ in range(steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        B.render_device(views, out=out, stream=sc)
+        fn()
         b.record(stream)
         b.synchronize()
         ts.append(a.elapsed_time(b))
-    st = B.last_stats
-    ms = statistics.median(ts)
-    L.update(s.eye, fwd, stream=sc)
-    r.render(f, out=plain_out, stream=sc)
+    return statistics.median(ts)
+
+
+def batch_world(n_views):
+    """The headline workload's scenes (renderers + lightings, maps at each scene's reference camera) and views."""
+    import torch
+    from splatlight_gb300.batch import View
+    from splatlight_gb300.lighting import camera_forward, for_scene
+    from splatlight_gb300.renderer import SplatRenderer
+    scenes, mix = batch_mix(n_views=n_views)
+    rs, ls = [], []
+    for s in scenes:
+        r = SplatRenderer(s.gaussians, s.parts)
+        L = for_scene(r, s)
+        L.update(s.eye, camera_forward(s))   # the resident light state: maps at the scene's reference camera
+        rs.append(r)
+        ls.append(L)
     torch.cuda.synchronize()
-    err = float((out.view(H, W, 4) - plain_out).abs().max().item())
+    return scenes, mix, rs, ls, [View(k, f, e) for k, f, e in mix]
+
+
+def stage_rooflines(st, ms, peak_hbm, fp32_peak, peak_kind):
+    """Per stage of the batched chain: algorithmic work / its device time against the stage's bound.  Bytes per unit
+    (reads + writes of the algorithm, no re-reads): projection 64 B record in, 48 B splat + 4 B key + 8 B rectangle out
+    per slot; depth sort 4 + 3 x 16 B per visible slot (3 onesweep passes over key + value); binning per visible slot
+    56 B read, per tile entry 8 B written + 2 x 16 B sorted + 8 B read for the runs; shading 336 B per shaded
+    Gaussian; compositing 20 FP32 flops per blended fragment; the coverage pass 12 FP32 flops per blended fragment
+    (its walk without colour)."""
+    vis, ent, slots = float(st.visible), float(st.entries), float(st.slots)
+    work = {"project": (124.0 * slots, "GB/s", peak_hbm, "hbm"),
+            "depth_sort": (52.0 * vis, "GB/s", peak_hbm, "hbm"),
+            "bin": (56.0 * vis + 48.0 * ent, "GB/s", peak_hbm, "hbm"),
+            "coverage": (12.0 * float(st.fragments), "TFLOP/s", fp32_peak, "fp32 issue"),
+            "shade": (336.0 * float(st.shaded), "GB/s", peak_hbm, "hbm"),
+            "composite": (20.0 * float(st.fragments), "TFLOP/s", fp32_peak, "fp32 issue")}
+    out = {}
+    for k, (w, unit, peak, bound) in work.items():
+        t = ms[k] * 1e-3
+        ach = w / t / (1e9 if unit == "GB/s" else 1e12) if t > 0 else 0.0
+        out[k] = {"ms": round(ms[k], 4), "bound": bound, "achieved": round(ach, 3), "unit": unit,
+                  "peak": round(peak, 1), "frac": round(ach / peak, 4) if peak else None,
+                  "peak_kind": peak_kind if unit == "GB/s" else "nominal FP32 issue rate at the sampled max SM clock",
+                  "algorithmic_per_launch": w}
+    return out
+
+
+def run_headline(args, stream, flush, dist, world, local):
+    """The batched path on the 64-view mix (the bench's value), with its plain and per-view deferred arms."""
+    import torch
+    from splatlight_gb300.batch import BatchRenderer
+    scenes, mix, rs, ls, views = batch_world(args.batch_views)
+    n = len(views)
+    sizes = [(int(f["viewport"][1]), int(f["viewport"][0])) for _, f, _ in mix]
+    pix = sum(h * w for h, w in sizes)
+    B = BatchRenderer(rs, ls, max_views=n)
+    out = torch.empty(4 * pix, dtype=torch.float32, device="cuda")
+    tile, tune_ms = B.autotune(views, reps=2)
+    sc = stream.cuda_stream
+
+    def batched():
+        return B.render_device(views, out=out, stream=sc)
+
+    for _ in range(args.warmup):
+        batched()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            starts[k].record(stream)
+            batched()
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    batch_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    ms = max_over_ranks(sum(batch_ms) / len(batch_ms), dist, "cuda")
+    st = B.last_stats
+    stats = {k: getattr(st, k) for k in ("slots", "visible", "entries", "fragments", "shaded", "reshaded_views",
+                                         "graph_replayed")}
+
+    # per-stage device times (the same chain launched kernel by kernel with events between the stages)
+    B.set_timing(2)
+    per = {k: [] for k in STAGES}
+    for _ in range(3):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        batched()
+        for k, v in zip(STAGES, B.last_stats.ms_stage):
+            per[k].append(v)
+    B.set_timing(0)
+    stage_ms = {k: statistics.median(v) for k, v in per.items()}
+
+    # the plain per-view path on the same views: the shading pass over every Gaussian of the view's scene at its eye,
+    # then the frame; per-view device times summed (host gaps between views excluded), the L2 flushed per round
+    plain_out = [torch.empty((h, w, 4), dtype=torch.float32, device="cuda") for h, w in sizes]
+
+    def plain_round():
+        evs = []
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        for (k, f, e), o in zip(mix, plain_out):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ls[k].shade(e, stream=sc)
+            rs[k].render(f, out=o, stream=sc)
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in evs)
+
+    plain_round()
+    plain_ms = statistics.median([plain_round() for _ in range(3)])
+    # image difference, batched vs plain (the same light state)
+    _, offs = batched()
+    torch.cuda.synchronize()
+    err = 0.0
+    for (h, w), o, po in zip(sizes, offs, plain_out):
+        err = max(err, float((out[int(o):int(o) + 4 * h * w].view(h, w, 4) - po).abs().max().item()))
+
+    # the per-view deferred path: each view as a one-view batch
+    B1 = BatchRenderer(rs, ls, max_views=1)
+    B1.set_tile(*tile)
+    one = [torch.empty(4 * h * w, dtype=torch.float32, device="cuda") for h, w in sizes]
+
+    def deferred_round():
+        evs = []
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        for v, o in zip(views, one):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            B1.render_device([v], out=o, stream=sc)
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in evs)
+
+    deferred_round()
+    deferred_ms = statistics.median([deferred_round() for _ in range(3)])
+    B1.close()
+
+    # end to end through the C ABI with host buffers: images written into page-locked host memory by the compositor
+    host = torch.empty(4 * pix, dtype=torch.float32, pin_memory=True)
+    for _ in range(2):
+        B.render_device(views, out=host, stream=sc)
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(e2e_steps):
+        B.render_device(views, out=host, stream=sc)
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, dist, "cuda")
+    e2e_err = float((host.to("cuda") - out).abs().max().item())
+    h2d = n * (1200 + 4 + 12 + 4)         # per view: RenderFrame, scene index, eye, light scale
+    d2h = 16 * pix
+    del host
     B.close()
-    return {"workload": "the same frame as a batch of one view (sl_batch_render)", "views_per_s": round(1000.0 / ms, 2),
-            "ms_per_view": round(ms, 4), "max_abs_err_vs_plain": err, "visible": int(st.visible),
-            "shaded": int(st.shaded), "reshaded_views": int(st.reshaded_views)}
+    for L in ls:
+        L.close()
+    for r in rs:
+        r.close()
+    return {"ms": ms, "views": n, "pixels": pix, "value": world * n * 1000.0 / ms, "clocks": clk.summary(),
+            "stage_ms": stage_ms, "stats": stats, "tile": tile, "autotune_ms": tune_ms,
+            "plain_ms": plain_ms, "deferred_ms": deferred_ms, "max_abs_err_vs_plain": err,
+            "e2e": {"value": round(world * n / e2e_s, 2), "unit": "views/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)}, "e2e_image_matches_device": e2e_err == 0.0,
+            "scenes": scenes, "mix": mix}
+
+
+def run_plain(args, stream, flush, dist, world):
+    """The single-frame forward of the hill-like 1,048,576-Gaussian scene at 1920x1080, lit, on the plain per-view
+    path: views/s (device time), e2e through the public API with a pinned host image, per-stage times, and the shading,
+    sort and composite rooflines."""
+    import torch
+    from splatlight_gb300.lighting import camera_forward, for_scene
+    from splatlight_gb300.renderer import SplatRenderer
+    s = make_scene("hill")
+    W, H = s.width, s.height
+    f = frame_for(s, 3)
+    r = SplatRenderer(s.gaussians, s.parts)
+    L = for_scene(r, s)
+    fwd = camera_forward(s)
+    sc = stream.cuda_stream
+    L.update(s.eye, fwd, stream=sc)
+    out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+
+    def step():
+        L.update(s.eye, fwd, stream=sc)    # the shading pass (the maps hold while nothing moves)
+        r.render(f, out=out, stream=sc)
+
+    for _ in range(args.warmup):
+        step()
+    ms = timed_device(stream, flush, step, max(5, min(args.steps, 20)))
+    ms = max_over_ranks(ms, dist, "cuda")
+    stats = r.last_stats
+    r.set_timing(True)
+    stage = {"lighting": [], "project": [], "sort": [], "bin": [], "composite": []}
+    frags = []
+    for _ in range(max(5, min(args.steps, 20))):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.update(s.eye, fwd, stream=sc)
+        e1.record(stream)
+        r.render(f, out=out, stream=sc)
+        stage["lighting"].append(e0.elapsed_time(e1))
+        st = r.last_stats
+        for k, v in (("project", st.ms_project), ("sort", st.ms_sort), ("bin", st.ms_bin),
+                     ("composite", st.ms_composite)):
+            stage[k].append(v)
+        frags.append(st.fragments)
+    r.set_timing(False)
+    stage_ms = {k: statistics.median(v) for k, v in stage.items()}
+    host_out = torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True).numpy()
+    parts = s.parts.copy()
+    for _ in range(2):
+        r.write_parts(parts)
+        L.update(s.eye, fwd)
+        r.render(f, out=host_out)
+    t0 = time.perf_counter()
+    n_e2e = max(5, min(args.steps, 20))
+    for _ in range(n_e2e):
+        r.write_parts(parts)
+        L.update(s.eye, fwd)
+        r.render(f, out=host_out)
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / n_e2e, dist, "cuda")
+    all_parts = (1 << len(s.parts)) - 1
+    maps = []
+    for _ in range(5):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.update(s.eye, fwd, moved_mask=all_parts, stream=sc)
+        e1.record(stream)
+        e1.synchronize()
+        maps.append(e0.elapsed_time(e1))
+    L.close()
+    r.close()
+    return {"s": s, "ms": ms, "views_per_s": world * 1000.0 / ms, "stage_ms": stage_ms,
+            "fragments": statistics.median(frags), "slots": int(stats.slots), "visible": int(stats.visible),
+            "entries": int(stats.entries), "e2e_views_per_s": world / e2e_s,
+            "update_every_part_moved_ms": statistics.median(maps)}
+
+
+def cpu_view_seconds(scenes, mix, caches, view, threads):
+    """One view of the mix on the CPU restatement: the shading pass over every Gaussian of its scene at the view's eye
+    (the scene's opacity maps from `caches`, as on the GPU) and the frame (project, sort, bin, composite)."""
+    from oracle import oracle
+    k, f, eye = mix[view]
+    s = scenes[k]
+    t0 = time.perf_counter()
+    tgt = np.asarray(s.target, np.float64)
+    colour, _, _, _ = oracle.lighting(s, eye=np.asarray(eye, np.float64), target=tgt, threads=threads,
+                                      cached=caches[k])
+    oracle.render(s.gaussians, s.parts, f, emitters=s.emitters, colour=colour, threads=threads, want_entries=False)
+    return time.perf_counter() - t0
+
+
+def cpu_caches(scenes, threads):
+    """iso_init and every scene's opacity maps at its reference camera, computed once (untimed)."""
+    return [cpu_cache(s, threads) for s in scenes]
+
+
+def headline_desc(n_views):
+    return (f"ragged batch: {n_views} lit views over 4 resident scenes (cornell-like 100k and 400k Gaussians, seed 0; "
+            "hill-like 1,048,576 and 2,097,152, seed 1), resolutions from 256^2, 512^2, 1280x720, 1920x1080, cameras "
+            "on radius U[3,6] spheres; one step = one batch through the batched path (one CUDA graph)")
 
 
 def run_reference(args):
@@ -658,22 +850,23 @@ def run_reference(args):
         return
     from oracle import oracle
     oracle.build()
-    s = make_scene(args.config)
     threads = os.cpu_count() or 1
-    cache = cpu_cache(s, threads)
-    t_warm = cpu_frame_seconds(s, cache, threads)
-    # bounded: at most ~90 s of CPU frames whatever --steps asks (each step is one full frame)
-    n_run = max(1, min(args.steps, int(90.0 / max(t_warm, 1e-3))))
-    times = [cpu_frame_seconds(s, cache, threads) for _ in range(n_run)]
+    scenes, mix = batch_mix(n_views=args.batch_views)
+    caches = cpu_caches(scenes, threads)
+    for k in range(args.warmup):
+        cpu_view_seconds(scenes, mix, caches, k % len(mix), threads)
+    times = [cpu_view_seconds(scenes, mix, caches, (args.warmup + k) % len(mix), threads) for k in range(args.steps)]
     ms = 1000.0 * sum(times) / len(times)
     v = 1000.0 / ms
     line = {"impl": "reference", "metric": "views/s", "value": round(v, 4), "unit": "views/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_desc(s), "implementation": "CPU restatement of the reference pipeline "
-                       "(the reference's WGSL needs WebGPU: unavailable on this box)"},
+            "config": {"workload": headline_desc(args.batch_views),
+                       "implementation": "CPU restatement of the reference pipeline in the reference's order (per "
+                                         "view: the shading pass over the scene, then project, sort, bin, composite);"
+                                         " the reference's WGSL needs WebGPU: unavailable on this box"},
             "cpu_baseline": {"value": round(v, 4), "unit": "views/s", "cores": threads, "kind": "port",
-                             "sample": f"{n_run} full frames of the workload (bounded to ~90 s)"},
+                             "sample": f"each step one view of the 64-view mix, in mix order ({args.steps} views)"},
             "e2e": {"value": round(v, 4), "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -681,28 +874,29 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--config", default="hill", choices=["hill", "cornell"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch-views", type=int, default=64, help="views of the ragged batch (the config: 64)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-batch", action="store_true", help="skip the ragged-batch leg")
-    ap.add_argument("--only-batch", action="store_true", help="the ragged-batch leg alone (its own JSON line)")
-    ap.add_argument("--only-serve", action="store_true", help="the serving leg alone (its own JSON line)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-plain", action="store_true", help="skip the single-frame plain leg")
+    ap.add_argument("--no-lod", action="store_true", help="skip the screen-space LOD leg")
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiation leg")
+    ap.add_argument("--no-sort", action="store_true", help="skip the sort leg")
+    ap.add_argument("--only-serve", action="store_true", help="the serving leg alone (its own JSON line)")
     ap.add_argument("--only-diff", action="store_true", help="the differentiation leg alone (its own JSON line)")
     ap.add_argument("--only-sort", action="store_true", help="the sort leg alone (its own JSON line)")
     ap.add_argument("--only-lod", action="store_true", help="the screen-space LOD leg alone (its own JSON line)")
-    ap.add_argument("--batch-views", type=int, default=64, help="views of the ragged batch (the config: 64)")
-    ap.add_argument("--no-lod", action="store_true", help="skip the screen-space LOD leg")
+    ap.add_argument("--only-plain", action="store_true", help="the single-frame plain leg alone (its own JSON line)")
     ap.add_argument("--sort-n", type=int, default=1 << 26, help="keys for the sort leg")
-    ap.add_argument("--no-diff", action="store_true", help="skip the differentiation leg")
-    ap.add_argument("--serve-seconds", type=float, default=4.0, help="arrival window per rate (the config: 60)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="arrival window at lambda 500 (the config: 60)")
+    ap.add_argument("--serve-seconds-other", type=float, default=10.0, help="arrival window at lambda 100 and 2000")
     args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
         return
-    args.warmup = max(args.warmup, 3)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -713,232 +907,122 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
-
     __import__("__graft_entry__").build()
-    from splatlight_gb300.renderer import SplatRenderer
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    hbm, sm_max_cfg, peak_kind = peaks()
+
+    def emit(line):
+        if rank == 0:
+            print(json.dumps(line), flush=True)
 
     if args.only_sort:
-        stream = torch.cuda.Stream()
-        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
         res = run_sort(args, stream, flush, args.sort_n)
-        if rank == 0:
-            print(json.dumps({"metric": "sort GB/s", "value": res["ours_24bit"]["gbs"], "unit": "GB/s",
-                              "n_gpus": world, "sort": res}))
+        emit({"metric": "sort GB/s", "value": res["ours_16bit"]["gbs"], "unit": "GB/s", "n_gpus": world, "sort": res})
         return
     if args.only_lod:
-        stream = torch.cuda.Stream()
-        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
         res = run_lod(args, stream, flush)
-        if rank == 0:
-            print(json.dumps({"metric": "views/s", "value": res["lod_views_per_s"], "unit": "views/s",
-                              "n_gpus": world, "lod": res}))
+        emit({"metric": "views/s", "value": res["lod_views_per_s"], "unit": "views/s", "n_gpus": world, "lod": res})
         return
     if args.only_diff:
-        stream = torch.cuda.Stream()
-        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
         res = run_diff(args, stream, flush)
-        if rank == 0:
-            print(json.dumps({"metric": "inverse-rendering steps/s", "value": res["steps_per_s"], "unit": "steps/s",
-                              "n_gpus": world, "differentiation": res}))
+        emit({"metric": "inverse-rendering steps/s", "value": res["steps_per_s"], "unit": "steps/s",
+              "n_gpus": world, "differentiation": res})
         return
     if args.only_serve:
         res = run_serving(args)
-        if rank == 0:
-            best = max(res["rates"], key=lambda x: x["views_per_s"])
-            print(json.dumps({"metric": "views/s", "value": best["views_per_s"], "unit": "views/s",
-                              "n_gpus": world, "serving": res}))
+        emit({"metric": "views/s", "value": max(x["views_per_s"] for x in res["rates"]), "unit": "views/s",
+              "n_gpus": world, "serving": res})
         return
-    if args.only_batch:
-        stream = torch.cuda.Stream()
-        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-        res = run_batch(args, stream, flush)
-        if rank == 0:
-            print(json.dumps({"metric": "views/s", "value": res["batched_views_per_s"], "unit": "views/s",
-                              "n_gpus": world, "batched": res}))
+    if args.only_plain:
+        res = run_plain(args, stream, flush, dist, world)
+        res.pop("s")
+        emit({"metric": "views/s", "value": round(res["views_per_s"], 2), "unit": "views/s", "n_gpus": world,
+              "plain": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in res.items()}})
         return
 
-    from splatlight_gb300.lighting import camera_forward, for_scene
-
-    s = make_scene(args.config)
-    W, H = s.width, s.height
-    f = frame_for(s, 3)
-    r = SplatRenderer(s.gaussians, s.parts)
-    L = for_scene(r, s)           # emitters, sun, sky; binds the radiance buffer the projection reads
-    fwd = camera_forward(s)
-    stream = torch.cuda.Stream()
-    L.update(s.eye, fwd, stream=stream.cuda_stream)   # first update: iso_init + opacity maps (static scene)
-    torch.cuda.synchronize()
-
-    def step(out_buf):
-        # one frame: the lighting pass (shade_emit + env_direct; the maps hold while nothing moves) and the render
-        L.update(s.eye, fwd, stream=stream.cuda_stream)
-        return r.render(f, out=out_buf, stream=stream.cuda_stream)
-
-    out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    # warm-up (also sizes the tile-entry buffers)
-    for _ in range(args.warmup):
-        step(out)
-
-    # device-timed steps
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    barrier()
-    with ClockSampler(local) as clk:
-        with torch.cuda.stream(stream):
-            for k in range(args.steps):
-                flush.zero_()
-                starts[k].record(stream)
-                step(out)
-                ends[k].record(stream)
-        torch.cuda.synchronize()
-    barrier()
-    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-    ms = sum(step_ms) / len(step_ms)
-    ms = max_over_ranks(ms, dist, "cuda")
-    views_per_s = replicas_throughput(world, ms)
-    stats = r.last_stats
-    if not np.isfinite(out.sum().item()):
-        raise RuntimeError("non-finite image")
-
-    # per-stage device times (events inside the pipeline), for the rooflines
-    r.set_timing(True)
-    stage = {"lighting": [], "project": [], "sort": [], "bin": [], "composite": []}
-    frags = []
-    for _ in range(max(5, min(args.steps, 20))):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        L.update(s.eye, fwd, stream=stream.cuda_stream)
-        e1.record(stream)
-        r.render(f, out=out, stream=stream.cuda_stream)
-        stage["lighting"].append(e0.elapsed_time(e1))
-        st = r.last_stats
-        stage["project"].append(st.ms_project)
-        stage["sort"].append(st.ms_sort)
-        stage["bin"].append(st.ms_bin)
-        stage["composite"].append(st.ms_composite)
-        frags.append(st.fragments)
-    r.set_timing(False)
-    stage_ms = {k: statistics.median(v) for k, v in stage.items()}
-
-    # the opacity maps rebuilt as when every part moved (light map A re-splatted, every sun layer re-splatted, then
-    # the shading pass): the per-frame lighting cost of a scene whose parts all move
-    all_parts = (1 << len(s.parts)) - 1
-    maps = []
-    for _ in range(5):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        L.update(s.eye, fwd, moved_mask=all_parts, stream=stream.cuda_stream)
-        e1.record(stream)
-        e1.synchronize()
-        maps.append(e0.elapsed_time(e1))
-    L.update(s.eye, fwd, stream=stream.cuda_stream)
-    deferred = deferred_one_view(args, s, r, L, f, fwd, out, flush, stream)
-    lighting_maps = {"update_every_part_moved_ms": round(statistics.median(maps), 4),
-                     "shading_pass_only_ms": round(stage_ms["lighting"], 4),
-                     "maps": f"light map A {s.shadow_res}^2 per part ({len(s.parts)} parts), sun layers {s.sun_res}^2"}
-
-    # end to end through the public API with host buffers: frame + parts up, image down (pinned), wall clock
-    host_out = torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True)
-    host_out_np = host_out.numpy()
-    parts = s.parts.copy()
-    for _ in range(2):
-        r.write_parts(parts)
-        L.update(s.eye, fwd)
-        r.render(f, out=host_out_np)
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        r.write_parts(parts)
-        L.update(s.eye, fwd)
-        r.render(f, out=host_out_np)
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_s = max_over_ranks(e2e_s, dist, "cuda")
-    h2d = f.nbytes + parts.nbytes
-    d2h = W * H * 16
-
-    hbm, sm_max_cfg, peak_kind = peaks()
-    clocks = clk.summary()
+    hd = run_headline(args, stream, flush, dist, world, local)
+    clocks = hd["clocks"]
     sm_mhz = clocks["sm_max_mhz"] or sm_max_cfg
-    # sort: 2 onesweep passes over u16 keys + u32 values: (2 + 6) + (6 + 4) bytes per slot
-    sort_bytes = 18.0 * stats.slots
-    sort_gbs = sort_bytes / (stage_ms["sort"] * 1e-3) / 1e9
-    # composite: 20 FP32 flops per blended fragment (local coordinates 4, q 2, tests 3, alpha 4, blend 7), nominal
-    # FP32 issue peak = 152 SMs x 128 lanes x 2 flops x clock
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    frag = statistics.median(frags)
-    comp_tflops = 20.0 * frag / (stage_ms["composite"] * 1e-3) / 1e12
-    roof_sort = {"bound": "hbm", "achieved": round(sort_gbs, 1), "peak": hbm, "unit": "GB/s",
-                 "frac": round(sort_gbs / hbm, 4), "traffic": None, "peak_kind": peak_kind,
-                 "algorithmic_bytes_per_launch": sort_bytes, "kernel": "onesweep_pass x2 (depth keys)"}
-    roof_comp = {"bound": "fp32", "achieved": round(comp_tflops, 3), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
-                 "frac": round(comp_tflops / fp32_peak, 4), "traffic": None,
-                 "peak_kind": "nominal FP32 issue rate at the sampled max SM clock (no measured FP32 peak exists)",
-                 "algorithmic_flops_per_launch": 20.0 * frag, "kernel": "composite_kernel<16>"}
-    # shading pass (the lighting stage in steady state): 336 algorithmic bytes per Gaussian (record 64, leaf node 96,
-    # V grid 128, lamp T 16, env T 16 in; radiance 16 out); its DRAM traffic per Gaussian from one ncu capture of the
-    # kernel on this frame (487 MB for 1,048,576 Gaussians); it is issue-bound (same capture)
-    shade_bytes = 336.0 * s.count
-    shade_gbs = shade_bytes / (stage_ms["lighting"] * 1e-3) / 1e9
-    roof_shade = {"bound": "hbm", "achieved": round(shade_gbs, 1), "peak": hbm, "unit": "GB/s",
-                  "frac": round(shade_gbs / hbm, 4), "traffic": round(SHADE_DRAM_BYTES_PER_G * s.count),
-                  "peak_kind": peak_kind, "algorithmic_bytes_per_launch": shade_bytes,
-                  "kernel": "shade_kernel (issue-bound: 73% issue active, FMA pipe 51% in ncu; HBM 5%)"}
-    dominant = max(stage_ms, key=stage_ms.get)
-    roofline = {"composite": roof_comp, "lighting": roof_shade}.get(dominant, roof_sort)
+    roofs = stage_rooflines(type("S", (), hd["stats"])(), hd["stage_ms"], hbm, fp32_peak, peak_kind)
+    dom = max(hd["stage_ms"], key=hd["stage_ms"].get)
+    kernel = {"project": "bproject_kernel", "depth_sort": "onesweep_pass x3 (depth keys)",
+              "bin": "btile_bin_kernel + onesweep_pass x2 (tile ids) + btile_runs_kernel",
+              "coverage": "bmark_kernel", "shade": "bshade_kernel", "composite": "bcomposite_kernel"}[dom]
+    r = roofs[dom]
+    roofline = {"bound": r["bound"], "achieved": r["achieved"], "peak": r["peak"], "unit": r["unit"],
+                "frac": r["frac"], "traffic": None, "peak_kind": r["peak_kind"], "kernel": kernel,
+                "algorithmic_per_launch": r["algorithmic_per_launch"]}
+    n = hd["views"]
+    plain_vps = world * n * 1000.0 / hd["plain_ms"]
+    deferred_vps = world * n * 1000.0 / hd["deferred_ms"]
+    batched = {"views_per_s": round(hd["value"], 2), "plain_views_per_s": round(plain_vps, 2),
+               "x_vs_plain": round(hd["value"] / plain_vps, 3),
+               "per_view_deferred_views_per_s": round(deferred_vps, 2),
+               "x_vs_per_view_deferred": round(hd["value"] / deferred_vps, 3),
+               "max_abs_err_vs_plain": round(hd["max_abs_err_vs_plain"], 6)}
 
-    batch = None
-    if not args.no_batch:
-        batch = run_batch(args, stream, flush)
-    serving = None
+    detail = {"headline": {"stage_ms": {k: round(v, 4) for k, v in hd["stage_ms"].items()}, "stage_rooflines": roofs,
+                           "stats": hd["stats"], "tile": f"{hd['tile'][0]}x{hd['tile'][1]}",
+                           "autotune_ms": {k: round(v, 3) for k, v in hd["autotune_ms"].items()},
+                           "e2e_image_matches_device": hd["e2e_image_matches_device"]}}
+    plain = None
+    if not args.no_plain:
+        p = run_plain(args, stream, flush, dist, world)
+        sm = p["stage_ms"]
+        comp_tf = 20.0 * p["fragments"] / (sm["composite"] * 1e-3) / 1e12
+        sort_gbs = 18.0 * p["slots"] / (sm["sort"] * 1e-3) / 1e9
+        plain = {"views_per_s": round(p["views_per_s"], 2), "e2e_views_per_s": round(p["e2e_views_per_s"], 2),
+                 "lighting_ms": round(sm["lighting"], 4)}
+        detail["plain"] = {"workload": workload_desc(p["s"]), "stage_ms": {k: round(v, 4) for k, v in sm.items()},
+                           "slots": p["slots"], "visible": p["visible"], "entries": p["entries"],
+                           "composite_tflops": round(comp_tf, 3), "composite_frac_fp32": round(comp_tf / fp32_peak, 4),
+                           "depth_sort_gbs": round(sort_gbs, 1),
+                           "update_every_part_moved_ms": round(p["update_every_part_moved_ms"], 4)}
+    served = None
     if not args.no_serve:
-        serving = run_serving(args)
-    differentiation = None
-    if not args.no_diff:
-        differentiation = run_diff(args, stream, flush)
-    sort_leg = run_sort(args, stream, flush)
-    lod_leg = None
+        sv = run_serving(args)
+        detail["serving"] = sv
+        served = {str(x["lambda"]): {"views_per_s": x["views_per_s"], "p50_ms": x["p50_ms"], "p99_ms": x["p99_ms"],
+                                     "s": x["seconds"]} for x in sv["rates"]}
+        served["plain_views_per_s"] = sv["plain_per_view_views_per_s"]
+        served["x_vs_plain"] = sv["served_vs_plain"]
+    sort_c = None
+    if not args.no_sort:
+        so = run_sort(args, stream, flush, args.sort_n)
+        detail["sort"] = so
+        sort_c = {"gbs": so["ours_16bit"]["gbs"], "frac": so["ours_16bit"]["frac"], "n": so["n"]}
     if not args.no_lod:
-        lod_leg = run_lod(args, stream, flush)
+        detail["lod"] = run_lod(args, stream, flush)
+    if not args.no_diff:
+        detail["differentiation"] = run_diff(args, stream, flush)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        sec = cpu_frame_seconds(s, cpu_cache(s, threads), threads)
-        cpu = {"value": round(1.0 / sec, 4), "unit": "views/s", "cores": threads, "kind": "port",
-               "sample": "1 full frame of the same workload (lighting pass, project, sort, bin, composite)"}
+        scenes, mix = hd["scenes"], hd["mix"]
+        caches = cpu_caches(scenes, threads)
+        pick = [next(v for v, (k, _, _) in enumerate(mix) if k == s) for s in range(len(scenes))]
+        sec = sum(cpu_view_seconds(scenes, mix, caches, v, threads) for v in pick)
+        cpu = {"value": round(len(pick) / sec, 4), "unit": "views/s", "cores": threads, "kind": "port",
+               "sample": "the first view of each of the 4 scenes in the mix (per view: the shading pass over the "
+                         "scene, then project, sort, bin, composite)"}
 
     if rank == 0:
-        line = {"metric": "views/s", "value": round(views_per_s, 2), "unit": "views/s", "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": workload_desc(s), "parallelism": f"replicas x{world}",
-                           "l2": "flushed (256 MiB write) between timed frames", "tile": "16x16",
-                           "slots": int(stats.slots), "visible": int(stats.visible), "entries": int(stats.entries)},
-                "e2e": {"value": round(world / e2e_s, 2), "unit": "views/s", "h2d_bytes_per_step": int(h2d),
-                        "d2h_bytes_per_step": int(d2h)},
-                "gpu_launches": KERNELS_PER_FRAME * args.steps,
-                "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
-                "roofline": roofline, "sort_roofline": roof_sort, "composite_roofline": roof_comp,
-                "shade_roofline": roof_shade,
-                "cpu_baseline": cpu, "clocks": clocks, "batched": batch, "serving": serving,
-                "differentiation": differentiation, "sort": sort_leg, "lod": lod_leg, "lighting_maps": lighting_maps,
-                "deferred_one_view": deferred}
-        print(json.dumps(line))
-    L.close()
-    r.close()
+        sys.stderr.write(json.dumps(detail, default=float) + "\n")
+        line = {"metric": "views/s", "value": round(hd["value"], 2), "unit": "views/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(hd["ms"], 4),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded scene generators)",
+                "config": {"workload": headline_desc(n), "parallelism": f"replicas x{world}",
+                           "l2": "flushed (256 MiB write) before every timed batch",
+                           "pixels_per_step": hd["pixels"], "tile": f"{hd['tile'][0]}x{hd['tile'][1]}"},
+                "gpu_launches": BATCH_KERNELS * args.steps, "e2e": hd["e2e"], "roofline": roofline,
+                "cpu_baseline": cpu, "clocks": clocks,
+                "stage_ms": {k: round(v, 3) for k, v in hd["stage_ms"].items()},
+                "plain_1m_1080p": plain, "sort": sort_c, "served": served, "batched": batched}
+        print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
 

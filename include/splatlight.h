@@ -132,6 +132,12 @@ SL_API int sl_version(void);
 
 /* ---- asset layout (src/asset.js:18-38 checkHeader / checkBuffer) --------------------------------------------- */
 
+/* checkHeader's format and version test (src/asset.js:19-20): `format` must be "gs-runtime" and the major part of
+ * `version` (the text before the first '.') must be "0", the major version of the layout this library reads.
+ * Returns SL_OK or SL_ERR_LAYOUT with the reference's message ("Unknown asset format X", "Unsupported asset version
+ * V") in sl_last_error; a null argument is SL_ERR_LAYOUT as an absent field is there. */
+SL_API int sl_asset_check_header(const char* format, const char* version);
+
 /* Checks one buffer description of asset.json against the layout the kernels assume: the buffer name is one of
  * gaussians, parts, lamps, materials, nodes, kids, vgrid; stride and every listed field offset must match, and
  * 0 < count <= 2^24.  `field_names`/`field_offsets` hold `n_fields` pairs (offset UINT32_MAX = missing field).
@@ -362,6 +368,9 @@ typedef struct sl_batch_stats {
   uint32_t shaded;               /* Gaussians shaded, over the lit views (those the coverage pass marked) */
   uint32_t reshaded_views;       /* lit views run a second time with every blended splat shaded (radiance bound) */
   float max_radiance;            /* largest radiance bound of a view (the compositor's stop is t_stop / it) */
+  float ms_stage[6];             /* with per-stage timing (sl_batch_set_timing 2), device ms of: projection (+ scan
+                                    and compaction of the visible keys), depth sort, binning (+ tile sort, ranges),
+                                    coverage pass, shading (list + shading pass), composite; else 0 */
 } sl_batch_stats;
 
 /* Creates a batch over n_scenes renderers (lightings[k]: the lighting bound to renderers[k], or NULL / a NULL array
@@ -372,12 +381,15 @@ SL_API int sl_batch_create(sl_renderer* const* renderers, sl_lighting* const* li
 SL_API int sl_batch_destroy(sl_batch* b);
 /* Tile shape for the following batches: 16x16, 8x32 or 32x8 (SL_ERR_INVALID_ARG otherwise). */
 SL_API int sl_batch_set_tile(sl_batch* b, uint32_t tile_w, uint32_t tile_h);
+/* Device timing of the following batches: 0 off, 1 the whole chain (stats.ms_total), 2 also each stage
+ * (stats.ms_stage; the chain is then launched kernel by kernel instead of from its graph, with the same results). */
 SL_API int sl_batch_set_timing(sl_batch* b, int enabled);
 /* Renders n_views views: view v draws frames[v] of scene scene_of_view[v], eyes[3v..3v+2] its camera position (the
  * lit radiance's view direction), light_scales[v] (NULL = all 1) the intensity scale of every light of its scene
  * (emitters and distant lights; the sky ambient is unscaled) -- the same radiance as sl_lighting_set_emitters with
- * scale x light_scale and sl_lighting_set_environment with each irradiance x light_scale.  Images are packed in view order into out_dev (device, float RGBA, out_floats
- * floats at least 4 x the sum of W x H); view_offsets[v] (optional, host) receives the first float of view v.  The
+ * scale x light_scale and sl_lighting_set_environment with each irradiance x light_scale.  Images are packed in view order into out_dev (device memory, or page-locked host
+ * memory that the compositor writes in place over the host link; float RGBA, out_floats floats at least 4 x the sum
+ * of W x H); view_offsets[v] (optional, host) receives the first float of view v.  The
  * call returns after the batch completed; stats (optional) describe it. */
 SL_API int sl_batch_render(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames,
                            const float* eyes, const float* light_scales, uint32_t n_views, float* out_dev,

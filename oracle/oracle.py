@@ -230,23 +230,23 @@ def lighting(scene, eye=None, target=None, threads: int = 8, shadow_res=None, su
     rec = np.ascontiguousarray(scene.emitters).view(np.float32).reshape(-1, 16).copy()
     lights = (EnvLight * 4)()
     n_l = 0
-    if scene.sun is not None:
-        lights[0].dir[:] = list(scene.sun.direction)
-        lights[0].std = scene.sun.angular_std
-        lights[0].irr[:] = list(scene.sun.irradiance)
-        lights[0].shadows = 1 if scene.sun.casts_shadows else 0
-        n_l = 1
+    for d, std, irr, sh in scene.distant_lights()[:4]:
+        lights[n_l].dir[:] = list(d)
+        lights[n_l].std = std
+        lights[n_l].irr[:] = list(irr)
+        lights[n_l].shadows = 1 if sh else 0
+        n_l += 1
     S = LightSetup()
     S.emit_rec = rec.ctypes.data if len(rec) else None
     S.n_emit = len(rec)
-    S.scale = 1.0
+    S.scale = getattr(scene, "emit_scale", 1.0)
     S.theta = 4.0
     S.mode = mode
     S.asg = 1 if asg else 0
-    S.one_sided = 0
-    S.normal[:] = [0.0, 0.0, 1.0]
+    S.one_sided = 1 if getattr(scene, "emit_one_sided", False) else 0
+    S.normal[:] = list(getattr(scene, "emit_normal", (0.0, 0.0, 1.0)))
     S.edge_soft = 0.2
-    S.skip_part = 0xFFFFFFFF
+    S.skip_part = getattr(scene, "emit_skip_part", 0xFFFFFFFF)
     S.shadow_res = scene.shadow_res if shadow_res is None else shadow_res
     S.lights = C.addressof(lights)
     S.n_lights = n_l

@@ -46,7 +46,7 @@ class BatchStats(C.Structure):
     _fields_ = [("views", C.c_uint32), ("slots", C.c_uint32), ("tiles", C.c_uint32), ("entries", C.c_uint32),
                 ("visible", C.c_uint64), ("fragments", C.c_uint64), ("ms_total", C.c_float),
                 ("graph_replayed", C.c_uint32), ("shaded", C.c_uint32), ("reshaded_views", C.c_uint32),
-                ("max_radiance", C.c_float)]
+                ("max_radiance", C.c_float), ("ms_stage", C.c_float * 6)]
 
 
 class ServerOptions(C.Structure):
@@ -117,6 +117,7 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_lod_colour": (_I, [_P, _P, _U32, _P]),
     "sl_lod_read": (_I, [_P, _P, _P, _P]),
     "sl_sort_keys16": (_I, [_P, _U32, _P, _P]),
+    "sl_asset_check_header": (_I, [C.c_char_p, C.c_char_p]),
     "sl_sort_keys16_noalloc": (_I, [_P, _U32, _P, _P]),
     "sl_sort_keys32": (_I, [_P, _U32, _U32, _P, _P]),
     "sl_batch_create": (_I, [_P, _P, _U32, C.POINTER(BatchOptions), C.POINTER(_P)]),

@@ -59,8 +59,9 @@ class BatchRenderer:
     def set_tile(self, tile_w: int, tile_h: int) -> None:
         N.check(self._lib.sl_batch_set_tile(self._h, tile_w, tile_h))
 
-    def set_timing(self, on: bool) -> None:
-        N.check(self._lib.sl_batch_set_timing(self._h, 1 if on else 0))
+    def set_timing(self, on) -> None:
+        """False/0 off, True/1 the whole chain (last_stats.ms_total), 2 also per stage (last_stats.ms_stage)."""
+        N.check(self._lib.sl_batch_set_timing(self._h, int(on)))
 
     @staticmethod
     def _pack(views):

@@ -78,6 +78,16 @@ static const BufferSpec kLayout[] = {
     {"vgrid", 128, {}, 0},
 };
 
+int sl_asset_check_header(const char* format, const char* version) {
+  // src/asset.js:19: header.format !== 'gs-runtime'
+  if (!format || strcmp(format, "gs-runtime") != 0)
+    return fail(SL_ERR_LAYOUT, std::string("Unknown asset format ") + (format ? format : "undefined"));
+  // src/asset.js:20: String(header.version).split('.')[0] !== MAJOR ('0')
+  std::string v = version ? version : "undefined";
+  if (v.substr(0, v.find('.')) != "0") return fail(SL_ERR_LAYOUT, "Unsupported asset version " + v);
+  return SL_OK;
+}
+
 int sl_asset_check_buffer(const char* name, uint32_t stride, uint32_t count, const char* const* field_names,
                           const uint32_t* field_offsets, uint32_t n_fields) {
   if (!name) return fail(SL_ERR_INVALID_ARG, "buffer name is null");

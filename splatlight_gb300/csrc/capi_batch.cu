@@ -148,6 +148,9 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   FrameCounters* ctr = b->counters.as<FrameCounters>();
   const uint32_t* totals = b->dyn.as<uint32_t>();  // BatchDyn words: total slots, total tiles, ...
   uint32_t* hist = b->hist.as<uint32_t>();
+  // stage boundaries for the per-stage timing (never while the chain is being captured)
+  auto stage = [&](int k) { return b->stage_events ? cudaEventRecord(b->sev[k], s) : cudaSuccess; };
+  CK(stage(0));
   CK(launch_bproject(b->views.as<BatchView>(), b->block_view.as<uint32_t>(), B, b->keys32.as<uint32_t>(),
                      b->recs.as<SplatRec>(), b->rects.as<ushort4>(), hist, b->view_maxrad.as<uint32_t>(),
                      b->view_visible.as<uint32_t>(), b->block_valid.as<uint32_t>(), s));
@@ -157,11 +160,13 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
                         b->scan_scratch.ptr, ctr, s));
   CK(launch_bcompact(b->block_view.as<uint32_t>(), b->keys32.as<uint32_t>(), b->block_off.as<uint32_t>(), B,
                      b->tile_keys.as<uint32_t>(), b->tile_vals.as<uint32_t>(), s));
+  CK(stage(1));
   const uint32_t* n_visible = &ctr->visible;
   const uint32_t max_tiles_sort = (uint32_t)(b->status.bytes / (4ull * 256 * 4));
   CK(sort32_pairs(b->tile_keys.as<uint32_t>(), b->keys_alt.as<uint32_t>(), b->tile_vals.as<uint32_t>(),
                   b->order.as<uint32_t>(), b->vals_alt.as<uint32_t>(), S, n_visible, 16 + bits_for(V - 1), hist,
                   b->status.as<uint32_t>(), b->tile_ctr.as<uint32_t>(), max_tiles_sort, ctr, s));
+  CK(stage(2));
   CK(launch_btile_bin(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->recs.as<SplatRec>(), b->views.as<BatchView>(),
                       b->block_view.as<uint32_t>(), n_visible, S, b->tile_w, b->tile_h, E, ctr,
                       b->tile_keys.as<uint32_t>(), b->tile_vals.as<uint32_t>(), hist + 768, b->bin_scratch.ptr, s));
@@ -173,21 +178,25 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
                   b->tile_keys.as<uint32_t>()));
   CK(launch_btile_runs(b->tile_keys.as<uint32_t>(), &ctr->entries, E, b->views_out.as<BatchViewOut>(),
                        b->ranges.as<uint2>(), s));
+  CK(stage(3));
   // deferred shading: the coverage pass marks the splats of lit views that blend a fragment, the shading list is
   // their Gaussians in shading order, and only those are shaded before the composite
   const BatchComposite C{b->tile_w, b->tile_h, b->t_stop_scale, 0};
   CK(launch_bmark(C, b->ranges.as<uint2>(), b->tile_vals.as<uint32_t>(), b->recs.as<SplatRec>(),
                   b->views_out.as<BatchViewOut>(), b->view_maxrad.as<uint32_t>(), b->dyn.as<BatchDyn>(), T, ctr,
                   b->marks.as<uint8_t>(), b->view_tmark.as<float>(), s));
+  CK(stage(4));
   CK(launch_bshade_list(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(),
                         b->marks.as<uint8_t>(), totals, B, V, ctr, b->vals_alt.as<uint32_t>(),
                         b->view_shade.as<uint32_t>(), s));
   CK(launch_bshade(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(), B,
                    b->vals_alt.as<uint32_t>(), b->view_shade.as<uint32_t>(), b->recs.as<SplatRec>(),
                    b->view_maxrad.as<uint32_t>(), s));
+  CK(stage(5));
   CK(launch_bcomposite(C, b->ranges.as<uint2>(), b->tile_vals.as<uint32_t>(), b->recs.as<SplatRec>(),
                        b->views_out.as<BatchViewOut>(), b->view_maxrad.as<uint32_t>(), b->dyn.as<BatchDyn>(), T, ctr,
                        s));
+  CK(stage(6));
   CK(cudaMemcpyAsync(b->h_ctr, ctr, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(b->h_visible, b->view_visible.ptr, 4ull * V, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(b->h_maxrad, b->view_maxrad.ptr, 4ull * V, cudaMemcpyDeviceToHost, s));
@@ -390,7 +399,16 @@ int batch_launch(sl_batch* b, const uint32_t* scene_of_view, const sl_render_fra
   stage(b, scene_of_view, frames, eyes, light_scales, n_views, out_dev, slots, tiles);
   cudaError_t e;
   if (b->timing && (e = cudaEventRecord(b->ev[0], s)) != cudaSuccess) return cuda_fail(e, "timing");
-  int rc = launch_chain(b, s, replayed);
+  int rc = SL_OK;
+  if (b->stage_timing) {  // per-stage events between the kernels: the same chain, launched directly
+    b->stage_events = true;
+    cudaError_t e2 = enqueue(b, s);
+    b->stage_events = false;
+    *replayed = false;
+    if (e2 != cudaSuccess) return cuda_fail(e2, "batch launch");
+  } else {
+    rc = launch_chain(b, s, replayed);
+  }
   if (rc) return rc;
   if (b->timing && (e = cudaEventRecord(b->ev[1], s)) != cudaSuccess) return cuda_fail(e, "timing");
   return SL_OK;
@@ -457,6 +475,8 @@ int batch_finish(sl_batch* b, uint32_t n_views, uint64_t slots, uint64_t tiles, 
       stats->max_radiance = std::max(stats->max_radiance, __builtin_bit_cast(float, b->h_maxrad[v]));
     }
     if (b->timing) cudaEventElapsedTime(&stats->ms_total, b->ev[0], b->ev[1]);
+    if (b->stage_timing)
+      for (int k = 0; k < 6; k++) cudaEventElapsedTime(&stats->ms_stage[k], b->sev[k], b->sev[k + 1]);
   }
   if (hc.timeout) return fail(SL_ERR_TIMEOUT, "a bounded device-side wait gave up");
   return SL_OK;
@@ -508,6 +528,8 @@ int sl_batch_create(sl_renderer* const* renderers, sl_lighting* const* lightings
   cudaError_t e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&b->ev[0]);
   if (e == cudaSuccess) e = cudaEventCreate(&b->ev[1]);
+  for (auto& ev : b->sev)
+    if (e == cudaSuccess) e = cudaEventCreate(&ev);
   if (e == cudaSuccess) e = allocate(b);
   if (e != cudaSuccess) {
     sl_batch_destroy(b);
@@ -532,6 +554,8 @@ int sl_batch_destroy(sl_batch* b) {
   for (sl::DevBuf* x : all) x->release();
   for (auto& ev : b->ev)
     if (ev) cudaEventDestroy(ev);
+  for (auto& ev : b->sev)
+    if (ev) cudaEventDestroy(ev);
   if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
   delete b;
   return SL_OK;
@@ -547,7 +571,9 @@ int sl_batch_set_tile(sl_batch* b, uint32_t tile_w, uint32_t tile_h) {
 
 int sl_batch_set_timing(sl_batch* b, int enabled) {
   if (!b) return fail(SL_ERR_INVALID_ARG, "null batch");
+  if (enabled < 0 || enabled > 2) return fail(SL_ERR_INVALID_ARG, "timing: 0 off, 1 total, 2 per stage");
   b->timing = enabled != 0;
+  b->stage_timing = enabled == 2;
   return SL_OK;
 }
 
@@ -558,6 +584,19 @@ int sl_batch_render(sl_batch* b, const uint32_t* scene_of_view, const sl_render_
   if (n_views > b->max_views) return fail(SL_ERR_INVALID_ARG, "more views than the batch's max_views");
   if (reinterpret_cast<uintptr_t>(out_dev) % 16) return fail(SL_ERR_INVALID_ARG, "out_dev must be 16-byte aligned");
   cudaSetDevice(b->device);
+  {
+    // page-locked host memory: the compositor writes the images in place over the host link (no staging copy)
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, out_dev) == cudaSuccess && pa.type == cudaMemoryTypeHost) {
+      if (!pa.devicePointer || reinterpret_cast<uintptr_t>(pa.devicePointer) % 16)
+        return fail(SL_ERR_INVALID_ARG, "out_dev: host memory the device cannot write");
+      out_dev = static_cast<float*>(pa.devicePointer);
+    } else if (pa.type == cudaMemoryTypeUnregistered) {
+      cudaGetLastError();
+      return fail(SL_ERR_INVALID_ARG, "out_dev: pageable host memory (pass device or page-locked host memory)");
+    }
+    cudaGetLastError();
+  }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   uint64_t slot = 0, tile = 0, pix = 0;
   int rc = batch_layout(b, scene_of_view, frames, n_views, &slot, &tile, &pix);

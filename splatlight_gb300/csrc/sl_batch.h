@@ -41,7 +41,10 @@ struct sl_batch {
   int cls = 0;      // the class of the current launch
   int cls_min = 0;  // raised when a launch's tile entries outgrew its class (this batch only)
   bool timing = false;
+  bool stage_timing = false;   // per-stage events: the chain runs directly (not from its graph)
+  bool stage_events = false;   // set while enqueue() records them
   cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaEvent_t sev[7] = {};     // stage boundaries: start, projected, depth-sorted, binned, marked, shaded, composited
   // last batch
   uint32_t last_views = 0, last_slots = 0, last_tiles = 0, last_entries = 0;
   std::vector<uint64_t> offsets;

@@ -98,12 +98,9 @@ def for_scene(renderer: SplatRenderer, scene) -> Lighting:
     """A Lighting set up from a splatlight_gb300.scene.Scene: its host emitters, its sun and sky, its map sizes."""
     L = Lighting(renderer, scene.nodes, scene.vgrid, scene.materials)
     L.set_options(shadow_res=scene.shadow_res, sun_res=scene.sun_res)
-    L.set_emitters(scene.emitters)
-    if scene.sun is not None:
-        L.set_environment([(scene.sun.direction, scene.sun.angular_std, scene.sun.irradiance,
-                            scene.sun.casts_shadows)], scene.sky_ambient)
-    else:
-        L.set_environment([], scene.sky_ambient)
+    L.set_emitters(scene.emitters, scale=scene.emit_scale, one_sided=scene.emit_one_sided, normal=scene.emit_normal,
+                   skip_part=scene.emit_skip_part)
+    L.set_environment(scene.distant_lights(), scene.sky_ambient)
     L.bind()
     return L
 

@@ -52,10 +52,33 @@ class Scene:
     sky_ambient: float = 0.0
     shadow_res: int = 1024     # emitter-light shadow map resolution
     sun_res: int = 2048        # sun map resolution
+    extra_lights: tuple = ()   # distant lights after the sun: (direction, angular std, irradiance, casts shadows)
+    # the emitter set's EmitParams (src/lighting.js:657-673): overlap scale, one-sided emission about `normal`, the
+    # part whose Gaussians are the emitters (shadow lookups skip it), and whether the emitter records are drawn in
+    # slots after the scene (host emitters) or are the scene's own Gaussians (an asset's emissive part)
+    emit_scale: float = 1.0
+    emit_one_sided: bool = False
+    emit_normal: tuple = (0.0, 0.0, 1.0)
+    emit_skip_part: int = 0xFFFFFFFF
+    emit_drawn: bool = True
+    tree_nodes: np.ndarray | None = None   # an asset's whole tree (leaves first) and its children lists, for LOD
+    kids: np.ndarray | None = None
 
     @property
     def count(self) -> int:
         return len(self.gaussians)
+
+    @property
+    def n_drawn_emitters(self) -> int:
+        """The emitter count a RenderFrame carries (palette[3].y): the host emitters drawn after the scene."""
+        return len(self.emitters) if self.emit_drawn else 0
+
+    def distant_lights(self) -> list:
+        """[(direction, angular std, irradiance, casts shadows)]: the sun, then any further distant lights."""
+        out = []
+        if self.sun is not None:
+            out.append((self.sun.direction, self.sun.angular_std, self.sun.irradiance, self.sun.casts_shadows))
+        return out + list(self.extra_lights)
 
 
 def _quats(rng, n):
