@@ -1,6 +1,7 @@
 """ctypes wrapper and build recipe of the CPU restatement (oracle/*.c).  TEST INFRASTRUCTURE: imported only by tests/,
-__graft_entry__.smoke() and bench.py's CPU-baseline leg, as the checker -- never by the product.  Parity unpinned:
-the reference (WGSL on WebGPU) cannot run here and ships no golden vectors; see sl_oracle.c for how it is pinned.
+__graft_entry__.smoke() and bench.py's CPU-baseline leg, as the checker -- never by the product.  The reference (WGSL
+on WebGPU) cannot run here and ships no golden vectors; the restatement is pinned on the reference's two shipped
+assets (see sl_oracle.c).
 
 The C sources compile with gcc -O2 -ffp-contract=off (fp32 arithmetic in written order, no fused multiply-add except
 where the source calls fmaf), -fopenmp for the multi-threaded baseline, into oracle/_build/liborc.so.

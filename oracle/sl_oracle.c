@@ -3,9 +3,11 @@
  * back-to-front composite).  TEST INFRASTRUCTURE: only tests/, the smoke check and the benchmark's CPU-baseline
  * leg load this library; the product path never does.
  *
- * Parity unpinned: the reference is WGSL on WebGPU (no graphics stack here to run it) and ships no tests or golden
- * vectors, so this restatement is pinned by reading the cited lines, by float64 brute-force and known-answer checks
- * (tests/test_oracle*.py) and by the committed fixtures tests/golden/*.npz that tests/golden/make_golden.py made.
+ * How it is pinned: the reference is WGSL on WebGPU (no graphics stack here to run it) and ships no tests or golden
+ * vectors; it does ship two gs-runtime scenes (runtime/assets/cornell_sdf_room_plain_bin, hill_lite_bin).  This
+ * restatement renders both as the reference's page shows them, and the GPU path is checked against it on both
+ * (tests/test_gpu_assets.py); beside that, reading the cited lines, float64 brute-force and known-answer checks
+ * (tests/test_oracle*.py) and the regression fixtures tests/golden/*.npz (tests/golden/make_golden.py).
  *
  * Arithmetic contract (shared with the CUDA kernels; both follow it independently):
  *   - fp32 throughout, compiled with -ffp-contract=off: every a*b+c below rounds twice unless written as fmaf();

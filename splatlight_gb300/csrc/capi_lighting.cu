@@ -83,6 +83,7 @@ const int kIJ[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
 
 struct TreeBuilder {
   const float* rec;
+  const double* le_scale = nullptr;  // per emitter: multiplies its Le (the differentiable path's intensities)
   std::vector<TNode> info;
   std::vector<float> out;  // 24 floats per node (EmitNode + its ASG covariance, lighting.js packEmitNodes)
   uint32_t next = 0;
@@ -139,7 +140,7 @@ struct TreeBuilder {
     for (int j = 0; j < 6; j++) nd.Cs[j] = nd.C[j] * widen;
     for (int k = 0; k < 3; k++) {
       nd.mu[k] = o[k];
-      nd.Le[k] = o[12 + k];
+      nd.Le[k] = le_scale ? o[12 + k] * le_scale[i] : o[12 + k];
     }
     nd.radius = 3 * std::max(std::max((double)o[8], (double)o[9]), (double)o[10]);
     nd.lo = 0xFFFFFFFFu;
@@ -308,6 +309,57 @@ void link_tree(std::vector<float>& out, uint32_t node, uint32_t skip, uint32_t p
     link_tree(out, hi, lo, pending + 1u);  // hi first; lo is pending meanwhile
     node = lo;                              // then lo, which ends where this node ends
   }
+}
+
+// The emitter tree of n records (16 floats each, albedo = Le) with each emitter's Le scaled by le_scale[k] (NULL: 1),
+// laid out as the shading pass walks it (24 floats per node, skip links set); returns the root.  With dtab non-null
+// it also receives, per node e and emitter k, the derivatives of the node's Le (3) and M (6: xx yy zz xy xz yz) with
+// respect to le_scale[k], [e][k][9]: central differences of the float64 build (relative step 1e-6; the split
+// structure and the moment-matched shapes do not depend on the intensities, only Le and M do).
+uint32_t build_emitter_tree(const float* rec, uint32_t n, const double* le_scale, std::vector<float>& out,
+                            std::vector<float>* dtab) {
+  const double e3 = ein3();
+  auto run = [&](const double* sc, std::vector<TNode>* info_out, std::vector<float>* packed) {
+    TreeBuilder B;
+    B.rec = rec;
+    B.le_scale = sc;
+    B.info.resize(2ull * n);
+    B.out.assign(24ull * (2 * n - 1), 0.0f);
+    B.e3 = e3;
+    B.widen = e3 / (1.0 - std::exp(-3.0));
+    std::vector<uint32_t> idx(n);
+    std::iota(idx.begin(), idx.end(), 0u);
+    const uint32_t root = B.build(idx);
+    if (packed) {
+      link_tree(B.out, root, kNoChild, 0);
+      *packed = std::move(B.out);
+    }
+    if (info_out) *info_out = std::move(B.info);
+    return root;
+  };
+  std::vector<double> sc(n, 1.0);
+  if (le_scale)
+    for (uint32_t k = 0; k < n; k++) sc[k] = le_scale[k];
+  const uint32_t root = run(sc.data(), nullptr, &out);
+  if (dtab) {
+    const uint32_t nodes = 2 * n - 1;
+    dtab->assign((size_t)nodes * n * 9, 0.0f);
+    std::vector<TNode> ip, im;
+    for (uint32_t k = 0; k < n; k++) {
+      const double h = 1e-6 * std::max(std::fabs(sc[k]), 1e-3);
+      std::vector<double> sp = sc, sm = sc;
+      sp[k] += h;
+      sm[k] -= h;
+      run(sp.data(), &ip, nullptr);
+      run(sm.data(), &im, nullptr);
+      for (uint32_t e = 0; e < nodes; e++) {
+        float* o = &(*dtab)[((size_t)e * n + k) * 9];
+        for (int c = 0; c < 3; c++) o[c] = (float)((ip[e].Le[c] - im[e].Le[c]) / (2 * h));
+        for (int j = 0; j < 6; j++) o[3 + j] = (float)((ip[e].M[j] - im[e].M[j]) / (2 * h));
+      }
+    }
+  }
+  return root;
 }
 
 // Shading order: the Gaussians sorted by a 30-bit Morton code of their model-space means over the scene's bounds,

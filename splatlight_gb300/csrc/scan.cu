@@ -19,6 +19,11 @@ __device__ __forceinline__ uint64_t load_relaxed64(const uint64_t* p) {
   return v;
 }
 
+// publishes a status word (flag and value in one aligned word) without waiting for a round trip
+__device__ __forceinline__ void store_relaxed64(uint64_t* p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 __global__ void __launch_bounds__(kThreads) scan_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
                                                         uint32_t n, uint32_t* total, uint32_t* tile_ctr,
                                                         uint64_t* status, FrameCounters* ctr) {
@@ -68,9 +73,9 @@ __global__ void __launch_bounds__(kThreads) scan_kernel(const uint32_t* __restri
     uint64_t* st = status + tile;
     uint32_t excl = 0;
     if (tile == 0) {
-      atomicExch(reinterpret_cast<unsigned long long*>(st), (unsigned long long)(kPrefix | agg));
+      store_relaxed64(st, kPrefix | agg);
     } else {
-      atomicExch(reinterpret_cast<unsigned long long*>(st), (unsigned long long)(kAgg | agg));
+      store_relaxed64(st, kAgg | agg);
       int32_t j = (int32_t)tile - 1;
       uint32_t spins = 0;
       while (j >= 0) {
@@ -88,7 +93,7 @@ __global__ void __launch_bounds__(kThreads) scan_kernel(const uint32_t* __restri
         if (flag == kPrefix) break;
         j--;
       }
-      atomicExch(reinterpret_cast<unsigned long long*>(st), (unsigned long long)(kPrefix | (uint32_t)(excl + agg)));
+      store_relaxed64(st, kPrefix | (uint32_t)(excl + agg));
     }
     s_excl = excl;
     if (total && tile * kTile + kTile >= n) *total = excl + agg;

@@ -25,6 +25,12 @@ __device__ __forceinline__ uint64_t load_relaxed64(const uint64_t* p) {
   return v;
 }
 
+// Publishes a status word (flag and count in one aligned 64-bit word: a relaxed store suffices, and unlike an atomic
+// exchange it does not hold the thread for a round trip).
+__device__ __forceinline__ void store_relaxed64(uint64_t* p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 // Called by one whole warp for block blk with its count agg (blocks before `first` count as a prefix of 0): publishes
 // agg, reads 32 earlier blocks' words per step (the nearest in lane 0) until a prefix, publishes this block's prefix
 // and returns the count of the blocks in [first, blk) in every lane.
@@ -32,9 +38,7 @@ __device__ __forceinline__ uint32_t lookback_warp(uint64_t* status, uint32_t blk
                                                   uint32_t* timeout_flag) {
   const uint32_t lane = threadIdx.x & 31u;
   const bool head = blk == first;
-  if (lane == 0)
-    atomicExch(reinterpret_cast<unsigned long long*>(status + blk),
-               (unsigned long long)((head ? kLookPrefix : kLookAgg) | agg));
+  if (lane == 0) store_relaxed64(status + blk, (head ? kLookPrefix : kLookAgg) | agg);
   uint32_t excl = 0;
   const int32_t lo = (int32_t)first;
   int32_t top = (int32_t)blk - 1;
@@ -57,8 +61,7 @@ __device__ __forceinline__ uint32_t lookback_warp(uint64_t* status, uint32_t blk
     if (pm) break;
     top -= 32;
   }
-  if (lane == 0 && !head)
-    atomicExch(reinterpret_cast<unsigned long long*>(status + blk), (unsigned long long)(kLookPrefix | (excl + agg)));
+  if (lane == 0 && !head) store_relaxed64(status + blk, kLookPrefix | (excl + agg));
   return excl;
 }
 

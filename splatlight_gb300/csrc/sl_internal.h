@@ -107,7 +107,7 @@ cudaError_t launch_lod_colour_top(uint32_t G, float gain, uint32_t colour_all, c
                                   const float4* colour, const float4* lo_b, float4* ncolour, cudaStream_t s);
 
 // sort.cu: onesweep LSD radix sort of 16-bit keys with u32 values, over tiles of kSortTileKeys keys.
-constexpr uint32_t kSortTileKeys = 6144;
+constexpr uint32_t kSortTileKeys = 4096;
 constexpr size_t sort_tiles_const(uint32_t n) { return (n + kSortTileKeys - 1) / kSortTileKeys; }
 
 // Scratch layout of one standalone 16-bit sort of n keys (sort_api.cu): every offset 256-byte aligned.

@@ -1,14 +1,22 @@
 // Stable LSD radix sort of 16- or 32-bit keys with 32-bit values, onesweep style (one read and one write of the keys and
 // values per 8-bit digit pass, Adinets & Merrill 2022): the digit histograms of every pass are counted up front (by
-// the producer kernel, or launch_digit_hist16), then each pass is a single kernel over tiles of 6144 keys that
-//   1. ranks its keys per warp -- the peers holding the same digit found by one ballot per digit bit, a per-warp
-//      digit counter in shared memory -- so ranks follow index order within the tile (stability);
-//   2. publishes its per-digit counts and looks back over earlier tiles (decoupled look-back, one thread per digit)
-//      for the exclusive prefix; every spin is bounded and a give-up sets FrameCounters::timeout;
-//   3. reorders the tile in shared memory by digit and writes it out in digit runs (coalesced).
-// Tiles are taken in launch order from an atomic counter, so a tile only waits on tiles that already started.
-// Replaces the three-dispatch-per-pass radix sort of shaders/radix.wgsl:1-139 (same stable order: by key, ties in
-// index order); INVALID keys (0xFFFF) sort after every valid key, as there.
+// the producer kernel, or launch_digit_hist16), then each pass is a single kernel over tiles of kTile keys that
+//   1. ranks its keys per warp in index order (stability): the lanes holding the same digit find each other through
+//      a per-warp mask word per digit that each lane ORs its bit into (a shared-memory atomic), and a per-warp digit
+//      counter carries the count from one item to the next -- a handful of instructions per key instead of one ballot
+//      per digit bit;
+//   2. publishes its per-digit counts and looks back over earlier tiles for the exclusive prefix (decoupled
+//      look-back, one thread per digit): kLookWindow predecessors' words per round trip, because with hundreds of
+//      tiles in flight a tile's walk back to the nearest published prefix is long; every spin is bounded and a give-up
+//      sets FrameCounters::timeout;
+//   3. reorders the tile in shared memory by digit (values read straight into place) and writes it out in digit runs
+//      (coalesced), each key's destination one shared load (the digit's global start less its start within the
+//      tile) plus its position.
+// Tiles are taken in launch order from an atomic counter, so a tile only waits on tiles that already started.  (A
+// wait-free variant -- a counting kernel, a scan of the per-tile counts, then this rank-and-scatter -- was measured:
+// its scatter ran 25% faster than this whole pass, but the extra counting pass over the keys cost more than that.)
+// Replaces the three-dispatch-per-pass radix sort of shaders/radix.wgsl:1-139 (the same order: by key, ties in index
+// order); INVALID keys (0xFFFF) sort after every valid key, as there.
 #include "sl_internal.h"
 
 namespace sl {
@@ -16,9 +24,20 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kItems = 24;
-constexpr uint32_t kTile = kThreads * kItems;  // 6144
-static_assert(kTile == kSortTileKeys, "sort tile size and the scratch layouts disagree");
+// Keys per thread: 16 (tiles of 4096, four blocks per SM) for 16-bit keys, 24 (tiles of 6144, three blocks per SM) for
+// 32-bit keys -- the faster of the sizes measured for each (12, 16 and 24 keys per thread).  Scratch is sized for the
+// smaller tile (the most tiles).
+template <typename KeyT> struct SortCfg;
+template <> struct SortCfg<uint16_t> {
+  static constexpr int kItems = 16, kMinBlocks = 4;
+};
+template <> struct SortCfg<uint32_t> {
+  static constexpr int kItems = 24, kMinBlocks = 3;
+};
+static_assert(kThreads * SortCfg<uint16_t>::kItems == kSortTileKeys, "sort tile size and the scratch layouts disagree");
+static_assert(SortCfg<uint32_t>::kItems >= SortCfg<uint16_t>::kItems, "scratch is sized for the smaller tile");
+// Predecessors' words read per look-back round trip (4 measured faster than 16: the walks are short enough).
+constexpr int kLookWindow = 4;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
@@ -36,8 +55,14 @@ __device__ __forceinline__ uint32_t load_relaxed(const uint32_t* p) {
   return v;
 }
 
-// Exclusive scan of one value per thread over a 256-thread block; returns the exclusive prefix, *total = sum.
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_tot, uint32_t* total) {
+// Publishes a look-back word (value and flag in one aligned 32-bit word, so a plain relaxed store is enough and
+// the thread does not wait for a round trip as it would for an atomic exchange).
+__device__ __forceinline__ void store_relaxed(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Exclusive scan of one value per thread over a 256-thread block; returns the exclusive prefix.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_tot) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t x = v;
 #pragma unroll
@@ -47,157 +72,172 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
   }
   if (lane == 31) warp_tot[w] = x;
   __syncthreads();
-  uint32_t base = 0, sum = 0;
+  uint32_t base = 0;
 #pragma unroll
-  for (int k = 0; k < kWarps; k++) {
-    uint32_t t = warp_tot[k];
-    base += (k < w) ? t : 0u;
-    sum += t;
-  }
+  for (int k = 0; k < kWarps; k++) base += (k < w) ? warp_tot[k] : 0u;
   __syncthreads();
-  if (total) *total = sum;
   return base + x - v;
 }
 
-// Lanes of `mask` whose 8-bit digit equals this lane's: the intersection over the digit's bits of the ballot of
-// lanes sharing that bit (eight ballots; measured faster than the match instruction in this kernel).
-__device__ __forceinline__ uint32_t digit_peers(uint32_t mask, uint32_t d) {
-  uint32_t peers = mask;
-#pragma unroll
-  for (int b = 0; b < 8; b++) {
-    const uint32_t m = __ballot_sync(mask, (d >> b) & 1u);
-    peers &= ((d >> b) & 1u) ? m : ~m;
-  }
-  return peers;
-}
+template <typename KeyT, uint32_t kTile>
+struct PassSmem {
+  uint32_t tile;
+  uint32_t warp_tot[kWarps];
+  uint32_t cnt[kWarps][256];      // per warp and digit: running count while ranking, then the warp's start
+  uint32_t match[2][kWarps][256]; // per warp and digit: the lanes holding it in the current item (two, alternating)
+  uint32_t local_start[256];      // the digit's first position in the reordered tile
+  uint32_t gofs[256];             // the digit's global start less local_start
+  KeyT keys[kTile];
+  uint32_t vals[kTile];
+};
 
-// Tiles of 6144 keys at three blocks per SM (the best of the tile sizes and register budgets measured).
 template <typename KeyT>
-__global__ void __launch_bounds__(kThreads, 3) onesweep_pass(const KeyT* __restrict__ keys_in,
+__global__ void __launch_bounds__(kThreads, SortCfg<KeyT>::kMinBlocks) onesweep_pass(const KeyT* __restrict__ keys_in,
                                                           const uint32_t* __restrict__ vals_in,
                                                           KeyT* __restrict__ keys_out,
                                                           uint32_t* __restrict__ vals_out, uint32_t n_max,
                                                           const uint32_t* __restrict__ n_dev, int shift,
                                                           const uint32_t* __restrict__ digit_hist,
                                                           uint32_t* status, uint32_t* tile_ctr, FrameCounters* ctr) {
-  __shared__ uint32_t s_tile;
-  __shared__ uint32_t warp_hist[kWarps][256];
-  __shared__ uint32_t digit_base[256];
-  __shared__ uint32_t local_start[256];
-  __shared__ uint32_t warp_tot[kWarps];
-  __shared__ KeyT s_keys[kTile];
-  __shared__ uint32_t s_vals[kTile];
-
+  constexpr int kItems = SortCfg<KeyT>::kItems;
+  constexpr uint32_t kTile = kThreads * kItems;
+  __shared__ PassSmem<KeyT, kTile> sm;
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   // element count: a host bound, or the smaller device-side count (tile entries, known only on the device)
   // (a device count above the bound means the producer overflowed its buffer: sort nothing, the host re-runs)
   uint32_t n = n_max;
   if (n_dev) {
-    uint32_t nd = *n_dev;
+    const uint32_t nd = *n_dev;
     n = nd <= n_max ? nd : 0u;
   }
-  if (t == 0) s_tile = atomicAdd(tile_ctr, 1u);
+  if (t == 0) sm.tile = atomicAdd(tile_ctr, 1u);
+  const uint32_t hist_t = digit_hist[t];  // this digit's pass count, read early (its latency overlaps the ranking)
 #pragma unroll
-  for (int k = 0; k < kWarps; k++) warp_hist[k][t] = 0u;
+  for (int k = 0; k < kWarps; k++) {
+    sm.cnt[k][t] = 0u;
+    sm.match[0][k][t] = 0u;
+    sm.match[1][k][t] = 0u;
+  }
   __syncthreads();
-  const uint32_t tile = s_tile;
+  const uint32_t tile = sm.tile;
   const uint32_t tile_base = tile * kTile;
   if (tile_base >= n) return;  // the grid covers n_max; tiles past n have nothing to do (no later tile waits on them)
 
-  uint32_t keys[kItems], vals[kItems], ranks[kItems];
+  // warp w holds [tile_base + w 32 kItems, + 32 kItems), item it of lane l at + 32 it + l (coalesced loads)
   const uint32_t wbase = tile_base + (uint32_t)w * (32u * kItems) + (uint32_t)lane;
+  const bool full = tile_base + kTile <= n;
+  uint32_t keys[kItems];
 #pragma unroll
   for (int it = 0; it < kItems; it++) {
-    uint32_t idx = wbase + (uint32_t)it * 32u;
-    bool valid = idx < n;
-    keys[it] = valid ? (uint32_t)keys_in[idx] : 0xffffffffu;
-    vals[it] = valid ? (vals_in ? vals_in[idx] : idx) : 0u;
+    const uint32_t idx = wbase + (uint32_t)it * 32u;
+    keys[it] = (full || idx < n) ? (uint32_t)keys_in[idx] : 0u;
   }
+
+  // ranks in index order: item by item, the lanes sharing a digit OR their bits into match[it & 1][w][d]; each lane's
+  // rank is the warp's count of that digit so far plus its peers below it.  After every peer has read the mask and
+  // the count (a warp barrier), the lowest peer advances the count and clears the mask word, which is ORed into
+  // again only two items later, after two more warp barriers.
   const uint32_t lt = lanemask_lt();
+  uint32_t ranks[kItems];
 #pragma unroll
   for (int it = 0; it < kItems; it++) {
-    uint32_t idx = wbase + (uint32_t)it * 32u;
-    bool valid = idx < n;
-    uint32_t vmask = __ballot_sync(0xffffffffu, valid);
-    uint32_t d = (keys[it] >> shift) & 0xffu;
-    uint32_t rank = 0;
-    if (valid) {
-      uint32_t peers = digit_peers(vmask, d);
-      uint32_t before = warp_hist[w][d];
-      rank = before + __popc(peers & lt);
-      __syncwarp(vmask);
-      if ((peers & lt) == 0u) warp_hist[w][d] = before + __popc(peers);
-      __syncwarp(vmask);
+    const uint32_t idx = wbase + (uint32_t)it * 32u;
+    const bool valid = full || idx < n;
+    const uint32_t d = (keys[it] >> shift) & 0xffu;
+    uint32_t* mw = &sm.match[it & 1][w][d];
+    if (valid) atomicOr(mw, 1u << lane);
+    __syncwarp();
+    const uint32_t peers = valid ? *mw : 0u;
+    const uint32_t before = valid ? sm.cnt[w][d] : 0u;
+    __syncwarp();
+    const uint32_t below = peers & lt;
+    if (valid && below == 0u) {
+      sm.cnt[w][d] = before + __popc(peers);
+      *mw = 0u;
     }
-    ranks[it] = rank;
+    ranks[it] = before + __popc(below);
   }
   __syncthreads();
 
-  // per digit: exclusive prefix across warps, and the tile's count
+  // per digit t: the warps' exclusive starts within the tile, and the tile's count
   uint32_t run = 0;
 #pragma unroll
   for (int k = 0; k < kWarps; k++) {
-    uint32_t c = warp_hist[k][t];
-    warp_hist[k][t] = run;
+    const uint32_t c = sm.cnt[k][t];
+    sm.cnt[k][t] = run;
     run += c;
   }
   const uint32_t tile_count = run;
 
-  // publish this tile's counts, then look back for the exclusive prefix of digit t
+  // publish this tile's counts, then look back for the exclusive prefix of digit t: kLookWindow predecessors' words
+  // per round trip, taken in order -- an aggregate adds and the walk goes on, a prefix adds and ends it, a word not
+  // yet published is read again (after a short sleep; bounded)
   uint32_t* st = status + (size_t)tile * 256u;
-  if (tile == 0) {
-    atomicExch(&st[t], kFlagPrefix | tile_count);
-  } else {
-    atomicExch(&st[t], kFlagAgg | tile_count);
-  }
+  store_relaxed(&st[t], (tile == 0 ? kFlagPrefix : kFlagAgg) | tile_count);
   uint32_t excl = 0;
   if (tile > 0) {
     int32_t j = (int32_t)tile - 1;
     uint32_t spins = 0;
-    while (j >= 0) {
-      uint32_t s = load_relaxed(status + (size_t)j * 256u + t);
-      uint32_t flag = s & ~kValueMask;
-      if (flag == 0u) {
+    bool done = false;
+    while (!done) {
+      uint32_t sv[kLookWindow];
+#pragma unroll
+      for (int k = 0; k < kLookWindow; k++)
+        sv[k] = j - k >= 0 ? load_relaxed(status + (size_t)(j - k) * 256u + t) : 0u;
+      bool stalled = false;
+#pragma unroll
+      for (int k = 0; k < kLookWindow; k++) {
+        if (done || stalled) continue;
+        const uint32_t flag = sv[k] & ~kValueMask;
+        if (flag == 0u) {
+          stalled = true;  // not yet published: read again from here
+          continue;
+        }
+        excl += sv[k] & kValueMask;
+        j--;
+        if (flag == kFlagPrefix) done = true;
+      }
+      if (done) break;
+      if (stalled) {
         if (++spins > kSpinLimit) {
           atomicExch(&ctr->timeout, 1u);
           break;
         }
         __nanosleep(32);
-        continue;
       }
-      excl += s & kValueMask;
-      if (flag == kFlagPrefix) break;
-      j--;
+      // j < 0 cannot happen: tile 0 publishes a prefix at once, so the walk ends there at the latest
     }
-    atomicExch(&st[t], kFlagPrefix | ((excl + tile_count) & kValueMask));
+    store_relaxed(&st[t], kFlagPrefix | ((excl + tile_count) & kValueMask));
   }
 
-  // global start of digit t: exclusive scan of the pass histogram, plus earlier tiles
-  uint32_t gstart = block_exclusive_scan(digit_hist[t], warp_tot, nullptr);
-  digit_base[t] = gstart + excl;
-  local_start[t] = block_exclusive_scan(tile_count, warp_tot, nullptr);
+  // global start of digit t: exclusive scan of the pass histogram, plus earlier tiles; its start within the tile
+  const uint32_t gstart = block_exclusive_scan(hist_t, sm.warp_tot);
+  const uint32_t lstart = block_exclusive_scan(tile_count, sm.warp_tot);
+  sm.local_start[t] = lstart;
+  sm.gofs[t] = gstart + excl - lstart;
   __syncthreads();
 
+  // reorder the tile by digit in shared memory; values are read here, straight from global memory
 #pragma unroll
   for (int it = 0; it < kItems; it++) {
-    uint32_t idx = wbase + (uint32_t)it * 32u;
-    if (idx < n) {
-      uint32_t d = (keys[it] >> shift) & 0xffu;
-      uint32_t pos = local_start[d] + warp_hist[w][d] + ranks[it];
-      s_keys[pos] = (KeyT)keys[it];
-      s_vals[pos] = vals[it];
+    const uint32_t idx = wbase + (uint32_t)it * 32u;
+    if (full || idx < n) {
+      const uint32_t d = (keys[it] >> shift) & 0xffu;
+      const uint32_t pos = sm.local_start[d] + sm.cnt[w][d] + ranks[it];
+      sm.keys[pos] = (KeyT)keys[it];
+      sm.vals[pos] = vals_in ? vals_in[idx] : idx;
     }
   }
   __syncthreads();
 
   const uint32_t tile_n = (n - tile_base) < kTile ? (n - tile_base) : kTile;
+#pragma unroll 4
   for (uint32_t j = t; j < tile_n; j += kThreads) {
-    uint32_t key = s_keys[j];
-    uint32_t d = (key >> shift) & 0xffu;
-    uint32_t dst = digit_base[d] + (j - local_start[d]);
+    const uint32_t key = sm.keys[j];
+    const uint32_t dst = sm.gofs[(key >> shift) & 0xffu] + j;
     if (dst >= n) continue;  // only after a look-back timeout (reported); never write out of range
     if (keys_out) keys_out[dst] = (KeyT)key;
-    vals_out[dst] = s_vals[j];
+    vals_out[dst] = sm.vals[j];
   }
 }
 
@@ -265,7 +305,8 @@ cudaError_t sort_pairs(KeyT* keys, KeyT* keys_alt, const uint32_t* vals_in, uint
                        const KeyT* keys_first = nullptr) {
   if (n == 0) return cudaSuccess;
   if (n > kValueMask) return cudaErrorInvalidValue;
-  const uint32_t tiles = (uint32_t)sort_tiles_for(n);
+  constexpr uint32_t kTile = kThreads * SortCfg<KeyT>::kItems;
+  const uint32_t tiles = (n + kTile - 1) / kTile;
   if (tiles > max_tiles) return cudaErrorInvalidValue;
   const int passes = bits <= 8 ? 1 : (bits + 7) / 8;
   if (passes > 4) return cudaErrorInvalidValue;
