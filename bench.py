@@ -513,9 +513,11 @@ def run_diff(args, stream, flush):
     params, lights = params_from_scene(s, n_lights=8)
     f = camera.make_frame(s.eye, s.target, s.up, s.fov_deg, 800, 800, s.count, far=s.far, view_mode=3, n_emit=0)
     D = DiffRenderer(s.count)
-    Pt, Lt = D.to_device(perturb(params, np.random.default_rng(2)), lights)
+    # per-Gaussian state held constant: the scene's V grids, transmittance and iso_norm read as arrays
+    state = {"vgrid": s.vgrid, "lamp_T": np.ones(s.count, np.float32), "iso_norm": np.ones(s.count, np.float32)}
+    Pt, Lt = D.to_device(perturb(params, np.random.default_rng(2)), lights, state)
     target = D.forward(Pt, Lt, f, s.eye)
-    P, Lt = D.to_device(params, lights)
+    P, Lt = D.to_device(params, lights, state)
     sc = stream.cuda_stream
     for _ in range(max(args.warmup, 3)):
         with torch.cuda.stream(stream):
@@ -535,7 +537,8 @@ def run_diff(args, stream, flush):
     ms = statistics.median(ts)
     gnorm = {k: float(v.norm().item()) for k, v in G.items()}
     D.close()
-    return {"workload": "500,000 hill-like Gaussians (seed 1), 800x800, 8 point lights; target from parameters "
+    return {"workload": "500,000 hill-like Gaussians (seed 1), 800x800, lit by 8 emissive Gaussian lights over the "
+                        "emitter tree's light cut (V grids, transmittance and iso_norm held constant); target from parameters "
                         "perturbed N(0,0.02) means / log-scales, N(0,0.1) opacity logits, N(0,0.05) albedo",
             "ms_per_step": round(ms, 3), "steps_per_s": round(1000.0 / ms, 2), "loss": loss,
             "grad_norms": {k: round(v, 6) for k, v in gnorm.items()}}

@@ -410,13 +410,19 @@ SL_API int sl_batch_autotune(sl_batch* b, const uint32_t* scene_of_view, const s
 
 /* An inverse-rendering step over free per-Gaussian parameters: the forward projects them as the splat path does
  * (view-space covariance, 2D conic with the low-pass dilation, peak optical depth tau0 = softplus(opacity logit)
- * sqrt(det0/det) / (s0 sqrt(q_d)); shaders/project.wgsl:237-261 with kappa = softplus(logit) / (sqrt(2 pi) s0)),
- * shades each Gaussian by point emitters -- albedo (ambient + sum_l s_l Le_l max(n.w,0) / (pi d^2)) + ks sum_l s_l Le_l
- * max(n.w,0) exp((n.h - 1) / r^2) / (pi r^2 d^2), n the short axis facing the eye, r the roughness -- and composites
+ * sqrt(det0/det) / (s0 sqrt(q_d)); shaders/project.wgsl:234-261 with kappa = softplus(logit) / (sqrt(2 pi) s0)),
+ * lights each Gaussian as the product's shading pass does with emissive Gaussian lights (shade_leaf,
+ * runtime/wgsl/emissive.wgsl:853-980: the light cut over the emitter tree built from the lights, intensity
+ * Le scale sqrt(w^T M w), V grid, footprint transfer, SGGX specular lobe with its iso damping; the receiver's leaf
+ * quantities follow from its parameters, the flake from its roughness), times the receiver's opacity-map
+ * transmittance and iso_norm (per-scene lighting state: inputs, held constant), plus albedo x ambient, and composites
  * front to back with alpha = min(1 - exp(-tau0 e^{-q/2}), 0.99), fragments of optical depth below 1e-6 skipped and a
  * pixel stopping before its transmittance would fall below 1e-4 (16x16 tiles, the same depth keys and stable sort).
- * The backward of L = sum over pixels and rgb of (image - target)^2 walks each tile list back to front, recomputing
- * transmittance from the final value (no per-pixel fragment lists).  All arrays are device pointers. */
+ * The backward of L = sum over pixels and rgb of (image - target)^2 walks each tile list back to front, recovering
+ * transmittance from the final value (no per-pixel fragment lists), then the projection's chain rule (hand-written)
+ * and the lighting's Jacobian (forward-mode dual numbers through the same lighting code, one parameter direction at
+ * a time; the light intensities through the emitter tree's derivative tables).  The ASG light-shape highlight is
+ * not part of this model.  Parameter and gradient arrays are device pointers. */
 typedef struct sl_diff sl_diff;
 
 typedef struct sl_diff_scene {
@@ -427,10 +433,12 @@ typedef struct sl_diff_scene {
   const float* albedo;           /* n x 3 */
   const float* roughness;        /* n, > 0 */
   uint32_t n, n_lights;          /* n_lights <= 32 */
-  const float* light_pos;        /* n_lights x 3 */
-  const float* light_le;         /* n_lights x 3: emitted radiance at scale 1 */
-  const float* light_scale;      /* n_lights: the intensities being optimised */
-  float ambient, ks;
+  const sl_gaussian* lights;     /* HOST, n_lights emissive Gaussians (world space; albedo = Le at intensity 1) */
+  const float* light_scale;      /* n_lights: the intensities being optimised (each multiplies its light's Le) */
+  float ambient, ks;             /* albedo x ambient added to every Gaussian; the specular weight of every material */
+  const sl_vgrid* vgrid;         /* n V grids, or NULL (every direction visible) */
+  const float* lamp_T;           /* n: the opacity-map transmittance toward the lights, or NULL (1) */
+  const float* iso_norm;         /* n: iso_init's normalisation, or NULL (1) */
 } sl_diff_scene;
 
 typedef struct sl_diff_grads {   /* same shapes as the parameters; every array is overwritten */

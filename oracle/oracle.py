@@ -294,22 +294,28 @@ def row_tiles(splat, ty: int, tile=(16, 16)):
     return (a.value, b.value) if ok else None
 
 
-def diff_render(params: dict, lights: dict, frame, eye, order, target=None, threads: int = 1):
+def diff_render(params: dict, lights: dict, frame, eye, order, target=None, threads: int = 1, state=None):
     """The differentiable path's forward in FP64, dense compositor (sl_oracle_diff.c).  params: means (n,3),
-    log_scales (n,3), quats (n,4), opacity_logits (n,), albedo (n,3), roughness (n,) as float64; lights: pos (L,3),
-    le (L,3), scale (L,), ambient, ks.  order: the depth order (far to near).  Returns (image H x W x 4, loss)."""
+    log_scales (n,3), quats (n,4), opacity_logits (n,), albedo (n,3), roughness (n,) as float64; lights: rec (L
+    emissive GAUSSIAN records), scale (L,), ambient, ks; state (optional): vgrid (n x 32 u32), lamp_T (n,),
+    iso_norm (n,), held constant.  order: the depth order (far to near).  Returns (image H x W x 4, loss)."""
     L = lib()
     fn = L.orc_diff_render
     fn.restype = C.c_double
-    fn.argtypes = [C.c_void_p] * 6 + [C.c_uint32] + [C.c_void_p] * 3 + [C.c_uint32, C.c_double, C.c_double] + \
-        [C.c_void_p] * 3 + [C.c_float] * 3 + [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int]
+    fn.argtypes = [C.c_void_p] * 6 + [C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_double, C.c_double] + \
+        [C.c_void_p] * 3 + [C.c_void_p] * 3 + [C.c_float] * 3 + \
+        [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int]
     f = np.asarray(frame).reshape(())
     W, H = int(f["viewport"][0]), int(f["viewport"][1])
     P = {k: np.ascontiguousarray(params[k], dtype=np.float64) for k in
          ("means", "log_scales", "quats", "opacity_logits", "albedo", "roughness")}
-    lp = np.ascontiguousarray(lights["pos"], dtype=np.float64)
-    le = np.ascontiguousarray(lights["le"], dtype=np.float64)
+    rec = np.ascontiguousarray(lights["rec"])
     ls = np.ascontiguousarray(lights["scale"], dtype=np.float64)
+    assert len(rec) == len(ls)
+    st = state or {}
+    vg = None if st.get("vgrid") is None else np.ascontiguousarray(st["vgrid"]).view(np.uint32)
+    lt = None if st.get("lamp_T") is None else np.ascontiguousarray(st["lamp_T"], dtype=np.float64)
+    iso = None if st.get("iso_norm") is None else np.ascontiguousarray(st["iso_norm"], dtype=np.float64)
     view = np.ascontiguousarray(f["view"], dtype=np.float32)
     focal = np.ascontiguousarray(f["focal"], dtype=np.float32)
     vp = np.ascontiguousarray(f["viewport"], dtype=np.float32)
@@ -318,9 +324,10 @@ def diff_render(params: dict, lights: dict, frame, eye, order, target=None, thre
     t = None if target is None else np.ascontiguousarray(target, dtype=np.float32)
     img = np.zeros((H, W, 4), np.float64)
     loss = fn(_p(P["means"]), _p(P["log_scales"]), _p(P["quats"]), _p(P["opacity_logits"]), _p(P["albedo"]),
-              _p(P["roughness"]), len(P["roughness"]), _p(lp), _p(le), _p(ls), len(ls), float(lights["ambient"]),
-              float(lights["ks"]), _p(view), _p(focal), _p(vp), float(f["near"]), float(f["far"]),
-              float(f["lowpass_px2"]), _p(e), _p(o), len(o), _p(t), _p(img), threads)
+              _p(P["roughness"]), len(P["roughness"]), rec.ctypes.data if len(rec) else None, _p(ls), len(ls),
+              float(lights["ambient"]), float(lights["ks"]), _p(vg), _p(lt), _p(iso), _p(view), _p(focal), _p(vp),
+              float(f["near"]), float(f["far"]), float(f["lowpass_px2"]), _p(e), _p(o), len(o), _p(t), _p(img),
+              threads)
     return img, loss
 
 

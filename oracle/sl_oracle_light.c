@@ -426,6 +426,7 @@ typedef struct {
   uint32_t next;
   double ein3, widen;
   uint32_t* idx_buf;
+  const double* le_scale;  /* per emitter: multiplies its Le (NULL: 1) */
 } tbuild;
 
 static uint32_t t_write(tbuild* B, const tnode* nd) {
@@ -463,7 +464,8 @@ static tnode t_leaf(tbuild* B, uint32_t i) {
   nd.mass = o[3] * pow(2 * M_PI, 1.5) * sqrt(sdet(nd.C));
   for (int j = 0; j < 6; j++) nd.Cs[j] = nd.C[j] * B->widen;
   nd.mu[0] = o[0]; nd.mu[1] = o[1]; nd.mu[2] = o[2];
-  nd.Le[0] = o[12]; nd.Le[1] = o[13]; nd.Le[2] = o[14];
+  double ls = B->le_scale ? B->le_scale[i] : 1.0;
+  nd.Le[0] = o[12] * ls; nd.Le[1] = o[13] * ls; nd.Le[2] = o[14] * ls;
   double smax = fmax(fmax(o[8], o[9]), o[10]);
   nd.radius = 3 * smax;
   nd.lo = NONE_U32;
@@ -574,8 +576,42 @@ static uint32_t t_build(tbuild* B, uint32_t* idx, uint32_t n) {
   return t_write(B, &nd);
 }
 
+/* The same tree in double precision with each emitter's Le scaled by le_scale (the differentiable path's
+ * intensities): per node 16 doubles (mu xyz, radius, M xx yy zz xy xz yz, Le rgb, child_lo, child_hi, 0; children as
+ * numbers, -1 for none).  Returns the root. */
+uint32_t orc_emitter_tree_d(const float* rec, uint32_t n, const double* le_scale, double* nodes_out) {
+  tbuild B;
+  memset(&B, 0, sizeof B);
+  B.rec = rec;
+  B.info = (tnode*)calloc(2u * n, sizeof(tnode));
+  float* tmp = (float*)calloc(24u * (2u * n), sizeof(float));
+  B.out = tmp;
+  B.ein3 = ein3();
+  B.widen = B.ein3 / (1.0 - exp(-3.0));
+  B.le_scale = le_scale;
+  uint32_t* idx = (uint32_t*)malloc(sizeof(uint32_t) * n);
+  for (uint32_t i = 0; i < n; i++) idx[i] = i;
+  uint32_t root = t_build(&B, idx, n);
+  for (uint32_t e = 0; e < 2 * n - 1; e++) {
+    const tnode* t = &B.info[e];
+    double* o = nodes_out + 16u * e;
+    for (int k = 0; k < 3; k++) o[k] = t->mu[k];
+    o[3] = t->radius;
+    for (int j = 0; j < 6; j++) o[4 + j] = t->M[j];
+    for (int k = 0; k < 3; k++) o[10 + k] = t->Le[k];
+    o[13] = t->lo == NONE_U32 ? -1.0 : (double)t->lo;
+    o[14] = t->lo == NONE_U32 ? -1.0 : (double)t->hi;
+    o[15] = 0.0;
+  }
+  free(idx);
+  free(tmp);
+  free(B.info);
+  return root;
+}
+
 uint32_t orc_emitter_tree(const float* rec, uint32_t n, float* nodes_out, float* root_cov) {
   tbuild B;
+  memset(&B, 0, sizeof B);
   B.rec = rec;
   B.info = (tnode*)calloc(2u * n, sizeof(tnode));
   B.out = nodes_out;

@@ -71,8 +71,9 @@ class ServerStats(C.Structure):
 class DiffScene(C.Structure):
     _fields_ = [("means", C.c_void_p), ("log_scales", C.c_void_p), ("quats", C.c_void_p),
                 ("opacity_logits", C.c_void_p), ("albedo", C.c_void_p), ("roughness", C.c_void_p),
-                ("n", C.c_uint32), ("n_lights", C.c_uint32), ("light_pos", C.c_void_p), ("light_le", C.c_void_p),
-                ("light_scale", C.c_void_p), ("ambient", C.c_float), ("ks", C.c_float)]
+                ("n", C.c_uint32), ("n_lights", C.c_uint32), ("lights", C.c_void_p), ("light_scale", C.c_void_p),
+                ("ambient", C.c_float), ("ks", C.c_float), ("vgrid", C.c_void_p), ("lamp_T", C.c_void_p),
+                ("iso_norm", C.c_void_p)]
 
 
 class DiffGrads(C.Structure):

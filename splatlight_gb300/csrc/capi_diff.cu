@@ -4,8 +4,10 @@
 #include <algorithm>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "sl_diff.h"
+#include "sl_lighting.h"
 #include "sl_runtime.h"
 
 struct sl_diff {
@@ -13,7 +15,9 @@ struct sl_diff {
   uint32_t n = 0;
   uint64_t entry_cap = 0;
   sl::ViewBuffers vb;
-  sl::DevBuf drec, img, tfinal, ncontrib, dimg, g2, loss, target;
+  sl::DevBuf drec, img, tfinal, ncontrib, dimg, g2, loss, target, tree, dtab;
+  std::vector<float> h_tree, h_dtab;
+  std::vector<double> h_scale;
   sl::FrameCounters* host_ctr = nullptr;
   double* host_loss = nullptr;
   uint32_t last_visible = 0, last_entries = 0, last_w = 0, last_h = 0;
@@ -32,8 +36,36 @@ int check_scene(const sl_diff_scene* sc, uint32_t n) {
   if (!sc || !sc->means || !sc->log_scales || !sc->quats || !sc->opacity_logits || !sc->albedo || !sc->roughness)
     return fail(SL_ERR_INVALID_ARG, "null parameter array");
   if (sc->n != n) return fail(SL_ERR_INVALID_ARG, "scene size differs from the diff object's");
-  if (sc->n_lights > kMaxDiffLights || (sc->n_lights && (!sc->light_pos || !sc->light_le || !sc->light_scale)))
+  if (sc->n_lights > kMaxDiffLights || (sc->n_lights && (!sc->lights || !sc->light_scale)))
     return fail(SL_ERR_INVALID_ARG, "bad lights (at most 32)");
+  return SL_OK;
+}
+
+// The emitter tree of the lights at their current intensities (read back from the device), with its derivative
+// table, uploaded for this step.
+int build_lights(sl_diff* d, const sl_diff_scene* sc, DiffLights& L, cudaStream_t s) {
+  const uint32_t n = sc->n_lights;
+  L.tree = dsh::EmitTree{nullptr, 0xFFFFFFFFu, 0u, 1u, 4.0f, 1.0f};
+  L.dtab = nullptr;
+  L.n = n;
+  if (!n) return SL_OK;
+  std::vector<float> scale(n);
+  cudaError_t e = cudaMemcpyAsync(scale.data(), sc->light_scale, 4ull * n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "light intensities");
+  d->h_scale.assign(scale.begin(), scale.end());
+  const uint32_t root = build_emitter_tree(reinterpret_cast<const float*>(sc->lights), n, d->h_scale.data(), d->h_tree,
+                                           &d->h_dtab);
+  if ((e = d->tree.ensure(4 * d->h_tree.size())) != cudaSuccess ||
+      (e = d->dtab.ensure(4 * d->h_dtab.size())) != cudaSuccess ||
+      (e = cudaMemcpyAsync(d->tree.ptr, d->h_tree.data(), 4 * d->h_tree.size(), cudaMemcpyHostToDevice, s)) !=
+          cudaSuccess ||
+      (e = cudaMemcpyAsync(d->dtab.ptr, d->h_dtab.data(), 4 * d->h_dtab.size(), cudaMemcpyHostToDevice, s)) !=
+          cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)  // the host vectors are rewritten by the next step
+    return cuda_fail(e, "emitter tree");
+  L.tree = dsh::EmitTree{d->tree.as<float>(), root, n, 1u, 4.0f, 1.0f};
+  L.dtab = d->dtab.as<float>();
   return SL_OK;
 }
 
@@ -49,7 +81,11 @@ void pack(const sl_diff_scene* sc, const sl_render_frame* f, const float* eye, D
   K.lowpass = f->lowpass_px2;
   for (int k = 0; k < 3; k++) K.eye[k] = eye[k];
   P = DiffParams{sc->means, sc->log_scales, sc->quats, sc->opacity_logits, sc->albedo, sc->roughness, sc->light_scale};
-  L = DiffLights{sc->light_pos, sc->light_le, sc->n_lights, sc->ambient, sc->ks};
+  L.ambient = sc->ambient;
+  L.ks = sc->ks;
+  L.vgrid = sc->vgrid;
+  L.lamp_T = sc->lamp_T;
+  L.iso_norm = sc->iso_norm;
 }
 
 cudaError_t ensure(sl_diff* d, uint32_t tiles, uint32_t pixels) {
@@ -89,8 +125,10 @@ int run(sl_diff* d, const sl_diff_scene* sc, const sl_render_frame* f, const flo
         float* image_out, const sl_diff_grads* G, cudaStream_t s) {
   DiffCamera K;
   DiffParams P;
-  DiffLights L;
+  DiffLights L{};
   pack(sc, f, eye, K, P, L);
+  int lrc = build_lights(d, sc, L, s);
+  if (lrc) return lrc;
   const uint32_t W = (uint32_t)f->viewport[0], H = (uint32_t)f->viewport[1];
   const uint32_t tx = (W + 15) / 16, ty = (H + 15) / 16, tiles = tx * ty, npix = W * H;
   if (tiles > 65535u) return fail(SL_ERR_INVALID_ARG, "too many tiles for 16-bit tile keys");
@@ -204,7 +242,8 @@ int sl_diff_destroy(sl_diff* d) {
   cudaSetDevice(d->device);
   cudaDeviceSynchronize();
   d->vb.release_all();
-  sl::DevBuf* all[] = {&d->drec, &d->img, &d->tfinal, &d->ncontrib, &d->dimg, &d->g2, &d->loss, &d->target};
+  sl::DevBuf* all[] = {&d->drec, &d->img, &d->tfinal, &d->ncontrib, &d->dimg, &d->g2, &d->loss, &d->target,
+                       &d->tree, &d->dtab};
   for (sl::DevBuf* b : all) b->release();
   if (d->host_ctr) cudaFreeHost(d->host_ctr);
   if (d->host_loss) cudaFreeHost(d->host_loss);

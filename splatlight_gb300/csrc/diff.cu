@@ -1,15 +1,18 @@
 // The differentiable splat path (inverse rendering): a forward pass over free parameters -- means, log-scales,
 // quaternions, opacity logits, albedo, roughness and the emissive lights' intensities -- through the same projection
 // (view-space covariance, 2D conic with the low-pass dilation, peak optical depth tau0 = softplus(logit) sqrt(det0 /
-// det) / (s0 sqrt(q_d)), the model of shaders/project.wgsl:237-261), per-Gaussian shading by point emitters (a
-// Lambert term and a normalised spherical-Gaussian specular lobe of width roughness^2), the same 16-bit depth keys,
-// stable sort and tile lists, and front-to-back compositing; then hand-written gradients of an L2 image loss.
+// det) / (s0 sqrt(q_d)), the model of shaders/project.wgsl:234-261), the product's per-Gaussian lighting by emissive
+// Gaussian lights over the emitter tree's light cut (sl_dshade.cuh; emissive.wgsl shade_leaf), the same 16-bit depth
+// keys, stable sort and tile lists, and front-to-back compositing; then hand-written gradients of an L2 image loss.
 //
 // Compositing for the differentiable path: alpha = min(1 - exp(-tau0 e^{-q/2}), 0.99), fragments with optical depth
 // below 1e-6 skipped, a pixel stops before the fragment that would take its transmittance below 1e-4.  The forward
 // stores per pixel only the final transmittance and the number of list entries it visited; the backward walks each
 // tile list back to front, recovering T_f = T_{f+1} / (1 - alpha_f) and the colour behind each fragment, so no
 // per-pixel fragment list is ever stored.  Per-splat gradients are reduced across the warp before one atomic add.
+// The lighting's part of the chain rule is the Jacobian of the radiance with respect to the Gaussian's parameters,
+// evaluated in forward mode (dual numbers through the lighting code itself, one parameter direction per pass), and
+// with respect to the light intensities through the emitter tree's derivative table.
 #include <cuda_fp16.h>
 
 #include "sl_detmath.h"
@@ -122,32 +125,21 @@ __device__ __forceinline__ void geometry(const DiffCamera& K, const float* mu, c
   g.tau0 = g.sp * sqrtf(g.det0 / g.det) / (g.s[0] * sqrtf(g.qd));
 }
 
-// Radiance of one Gaussian: albedo (ambient + sum_l E_l / pi) + ks sum_l E_l D_l, E_l = s_l Le_l max(n.w, 0) / d^2,
-// D_l = exp((n.h - 1) / r^2) / (pi r^2), n the short axis facing the eye.
-__device__ __forceinline__ F3 shade_fwd(const DiffLights& Lt, const float* lscale, F3 mu, F3 n0, F3 eye, F3 alb,
-                                        float rough) {
-  F3 ve = eye - mu;
-  const F3 v = ve * (1.0f / sqrtf(dot(ve, ve)));
-  const F3 n = dot(n0, v) < 0.0f ? n0 * -1.0f : n0;
-  const float r2 = rough * rough;
-  F3 dif = f3(0.0f, 0.0f, 0.0f), spc = f3(0.0f, 0.0f, 0.0f);
-  for (uint32_t l = 0; l < Lt.n; l++) {
-    const F3 D = ld3(Lt.pos + 3 * l) - mu;
-    const float d2 = dot(D, D);
-    const float dl = sqrtf(d2);
-    const F3 w = D * (1.0f / dl);
-    const float cs = dot(n, w);
-    if (!(cs > 0.0f)) continue;
-    const F3 hh = w + v;
-    const F3 h = hh * (1.0f / sqrtf(dot(hh, hh)));
-    const float nh = dot(n, h);
-    const float Dl = expf((nh - 1.0f) / r2) / (kPi * r2);
-    const F3 E = ld3(Lt.le + 3 * l) * (lscale[l] * cs / d2);
-    dif = dif + E * (1.0f / kPi);
-    spc = spc + E * Dl;
-  }
-  return f3(alb.x * (Lt.ambient + dif.x) + Lt.ks * spc.x, alb.y * (Lt.ambient + dif.y) + Lt.ks * spc.y,
-            alb.z * (Lt.ambient + dif.z) + Lt.ks * spc.z);
+// Radiance of Gaussian i as the product's shading pass lights it: albedo (acc T iso_norm + ambient), acc the emitter
+// light over its cut (sl_dshade.cuh).
+__device__ __forceinline__ F3 lit_radiance(const DiffLights& L, const DiffParams& P, const DiffCamera& K, uint32_t i) {
+  const float* m = P.means + 3 * i;
+  const float* l = P.log_scales + 3 * i;
+  const float* q = P.quats + 4 * i;
+  const float mu[3] = {m[0], m[1], m[2]}, ls[3] = {l[0], l[1], l[2]}, q4[4] = {q[0], q[1], q[2], q[3]};
+  const dsh::Recv<float> rv = dsh::receiver<float>(mu, ls, q4, P.opacity_logits[i], P.roughness[i]);
+  const float iso = L.iso_norm ? L.iso_norm[i] : 1.0f, T = L.lamp_T ? L.lamp_T[i] : 1.0f;
+  const dsh::V3<float> eye = dsh::v3(K.eye[0], K.eye[1], K.eye[2]);
+  const dsh::V3<float> acc = dsh::emitter_light<float>(L.tree, rv, L.vgrid ? L.vgrid + i : nullptr, L.ks, iso, eye,
+                                                       [](uint32_t, float, dsh::V3<float>, float) {});
+  const float k = T * iso;
+  const F3 alb = ld3(P.albedo + 3 * i);
+  return f3(alb.x * (acc.x * k + L.ambient), alb.y * (acc.y * k + L.ambient), alb.z * (acc.z * k + L.ambient));
 }
 
 __global__ void __launch_bounds__(kThreads) dproject_kernel(const DiffCamera K, const DiffParams P, const DiffLights Lt,
@@ -180,8 +172,7 @@ __global__ void __launch_bounds__(kThreads) dproject_kernel(const DiffCamera K, 
       d.B = g.b / g.det;
       d.C = g.ap / g.det;
       d.tau0 = g.tau0;
-      const F3 c = shade_fwd(Lt, P.light_scale, ld3(P.means + 3 * i), R[0], ld3(K.eye), ld3(P.albedo + 3 * i),
-                             P.roughness[i]);
+      const F3 c = lit_radiance(Lt, P, K, i);
       d.r = c.x;
       d.g = c.y;
       d.bl = c.z;
@@ -498,56 +489,61 @@ __global__ void __launch_bounds__(kThreads) dproject_bwd_kernel(const DiffCamera
     for (int k = 0; k < 3; k++)
       dR[k] = f3(V[0] * dwr[k].x + V[1] * dwr[k].y + V[2] * dwr[k].z, V[4] * dwr[k].x + V[5] * dwr[k].y + V[6] * dwr[k].z,
                  V[8] * dwr[k].x + V[9] * dwr[k].y + V[10] * dwr[k].z);
-    // ---- shading
-    const F3 mu = ld3(P.means + 3 * i), eye = ld3(K.eye), alb = ld3(P.albedo + 3 * i);
-    const float rough = P.roughness[i], r2 = rough * rough;
+    // ---- lighting: dL/dacc = dL/dc x albedo x T x iso_norm; the radiance's Jacobian by forward mode, one of the
+    // 12 directions (means 3, log-scales 3, quaternion 4, opacity logit, roughness) per pass
     const F3 gc = f3(gd.r, gd.g, gd.b);
-    F3 ve = eye - mu;
-    const float vlen = sqrtf(dot(ve, ve));
-    const F3 v = ve * (1.0f / vlen);
-    const float sgn = dot(R[0], v) < 0.0f ? -1.0f : 1.0f;
-    const F3 nn = R[0] * sgn;
-    F3 dif = f3(0.0f, 0.0f, 0.0f);
-    F3 dn = f3(0.0f, 0.0f, 0.0f), dv = f3(0.0f, 0.0f, 0.0f);
-    float drough = 0.0f;
-    for (uint32_t l = 0; l < Lt.n; l++) {
-      const F3 D = ld3(Lt.pos + 3 * l) - mu;
-      const float d2 = dot(D, D), dl = sqrtf(d2);
-      const F3 w = D * (1.0f / dl);
-      const float cs = dot(nn, w);
-      if (!(cs > 0.0f)) continue;
-      const F3 hh = w + v;
-      const float hl = sqrtf(dot(hh, hh));
-      const F3 h = hh * (1.0f / hl);
-      const float nh = dot(nn, h);
-      const float Dl = expf((nh - 1.0f) / r2) / (kPi * r2);
-      const F3 Le = ld3(Lt.le + 3 * l);
-      const float sl = P.light_scale[l];
-      dif = dif + Le * (sl * cs / d2 / kPi);
-      const float wd = (gc.x * alb.x * Le.x + gc.y * alb.y * Le.y + gc.z * alb.z * Le.z) / kPi;
-      const float ws = Lt.ks * (gc.x * Le.x + gc.y * Le.y + gc.z * Le.z);
-      const float base = cs / d2 * (wd + ws * Dl);
-      atomicAdd(&s_lg[l], base);  // reduced per block, then one global add per light
-      const float dF_dcs = sl / d2 * (wd + ws * Dl);
-      const float dF_dd2 = -sl * cs / (d2 * d2) * (wd + ws * Dl);
-      const float dF_dD = sl * cs / d2 * ws;
-      const float dD_dnh = Dl / r2;
-      drough += dF_dD * Dl * (-2.0f * (nh - 1.0f) / (r2 * rough) - 2.0f / rough);
-      // cs = n.w, nh = n.h
-      dn = dn + w * dF_dcs + h * (dF_dD * dD_dnh);
-      F3 dw = nn * dF_dcs;
-      const F3 dh = nn * (dF_dD * dD_dnh);
-      const F3 dhh = (dh - h * dot(h, dh)) * (1.0f / hl);
-      dw = dw + dhh;
-      dv = dv + dhh;
-      // w = D / |D|, d2 = D.D, D = p - mu
-      const F3 dD = (dw - w * dot(w, dw)) * (1.0f / dl) + D * (2.0f * dF_dd2);
-      dmu = dmu - dD;
+    const F3 alb = ld3(P.albedo + 3 * i);
+    const float Tl = Lt.lamp_T ? Lt.lamp_T[i] : 1.0f, iso = Lt.iso_norm ? Lt.iso_norm[i] : 1.0f;
+    const sl_vgrid* vg = Lt.vgrid ? Lt.vgrid + i : nullptr;
+    const float kk = Tl * iso;
+    const F3 ga = f3(gc.x * alb.x * kk, gc.y * alb.y * kk, gc.z * alb.z * kk);
+    const float* pm = P.means + 3 * i;
+    const float* pl = P.log_scales + 3 * i;
+    const float* pq = P.quats + 4 * i;
+    float dlit[12];
+#pragma unroll 1
+    for (int p = 0; p < 12; p++) {
+      dsh::Dual mu[3], ls[3], q4[4];
+      for (int k = 0; k < 3; k++) {
+        mu[k] = dsh::Dual{pm[k], p == k ? 1.0f : 0.0f};
+        ls[k] = dsh::Dual{pl[k], p == 3 + k ? 1.0f : 0.0f};
+      }
+      for (int k = 0; k < 4; k++) q4[k] = dsh::Dual{pq[k], p == 6 + k ? 1.0f : 0.0f};
+      const dsh::Dual lg{logit, p == 10 ? 1.0f : 0.0f}, rg{P.roughness[i], p == 11 ? 1.0f : 0.0f};
+      const dsh::Recv<dsh::Dual> rv = dsh::receiver<dsh::Dual>(mu, ls, q4, lg, rg);
+      const dsh::V3<dsh::Dual> eye = dsh::v3(dsh::cst<dsh::Dual>(K.eye[0]), dsh::cst<dsh::Dual>(K.eye[1]),
+                                             dsh::cst<dsh::Dual>(K.eye[2]));
+      const dsh::V3<dsh::Dual> acc = dsh::emitter_light<dsh::Dual>(
+          Lt.tree, rv, vg, Lt.ks, iso, eye, [](uint32_t, dsh::Dual, dsh::V3<dsh::Dual>, dsh::Dual) {});
+      dlit[p] = ga.x * acc.x.d + ga.y * acc.y.d + ga.z * acc.z.d;
     }
-    // v = (eye - mu) / |eye - mu|
-    dmu = dmu - (dv - v * dot(v, dv)) * (1.0f / vlen);
-    dR[0] = dR[0] + dn * sgn;
-    const F3 dalb = f3(gc.x * (Lt.ambient + dif.x), gc.y * (Lt.ambient + dif.y), gc.z * (Lt.ambient + dif.z));
+    // the value pass: albedo's gradient, and the light intensities' through the tree's derivative table (per cut node
+    // e and light k: dI_e/ds_k = dLe_e/ds_k scale |w|_M + Le_e scale (w^T dM_e/ds_k w) / (2 |w|_M))
+    dsh::V3<float> acc0;
+    {
+      const float mu[3] = {pm[0], pm[1], pm[2]}, ls[3] = {pl[0], pl[1], pl[2]}, q4[4] = {pq[0], pq[1], pq[2], pq[3]};
+      const dsh::Recv<float> rv = dsh::receiver<float>(mu, ls, q4, logit, P.roughness[i]);
+      const dsh::V3<float> eye = dsh::v3(K.eye[0], K.eye[1], K.eye[2]);
+      const uint32_t nl = Lt.n;
+      const float scale = Lt.tree.scale;
+      acc0 = dsh::emitter_light<float>(
+          Lt.tree, rv, vg, Lt.ks, iso, eye, [&](uint32_t node, float fe, dsh::V3<float> mw, float mq) {
+            if (!Lt.dtab || !(mq > 0.0f)) return;
+            const float* e = Lt.tree.nodes + 24u * node;
+            for (uint32_t k = 0; k < nl; k++) {
+              const float* t = Lt.dtab + ((size_t)node * nl + k) * 9u;
+              const float dq = t[3] * mw.x * mw.x + t[4] * mw.y * mw.y + t[5] * mw.z * mw.z +
+                               2.0f * (t[6] * mw.x * mw.y + t[7] * mw.x * mw.z + t[8] * mw.y * mw.z);
+              const float dm = 0.5f * dq / mq;
+              const float gI = ga.x * (t[0] * mq + e[12] * dm) + ga.y * (t[1] * mq + e[13] * dm) +
+                               ga.z * (t[2] * mq + e[14] * dm);
+              const float v = gI * scale * fe;
+              if (v != 0.0f) atomicAdd(&s_lg[k], v);
+            }
+          });
+    }
+    const F3 dalb = f3(gc.x * (acc0.x * kk + Lt.ambient), gc.y * (acc0.y * kk + Lt.ambient),
+                       gc.z * (acc0.z * kk + Lt.ambient));
     // ---- rotation matrix -> quaternion (normalised)
     const float x = qh[0], y = qh[1], z = qh[2], w = qh[3];
     // G[r][c] = dL/dR[r][c]; column k of R is R[k]
@@ -563,16 +559,16 @@ __global__ void __launch_bounds__(kThreads) dproject_bwd_kernel(const DiffCamera
             2.0f * x * G02 + 2.0f * y * G12;
     dq[3] = 2.0f * z * G10 - 2.0f * y * G20 - 2.0f * z * G01 + 2.0f * x * G21 + 2.0f * y * G02 - 2.0f * x * G12;
     const float proj = x * dq[0] + y * dq[1] + z * dq[2] + w * dq[3];
-    for (int k = 0; k < 4; k++) G.quats[4 * i + k] = (dq[k] - qh[k] * proj) / qn;
-    G.means[3 * i + 0] = dmu.x;
-    G.means[3 * i + 1] = dmu.y;
-    G.means[3 * i + 2] = dmu.z;
-    for (int k = 0; k < 3; k++) G.log_scales[3 * i + k] = ds[k] * g.s[k];
-    G.opacity_logits[i] = dlogit;
+    for (int k = 0; k < 4; k++) G.quats[4 * i + k] = (dq[k] - qh[k] * proj) / qn + dlit[6 + k];
+    G.means[3 * i + 0] = dmu.x + dlit[0];
+    G.means[3 * i + 1] = dmu.y + dlit[1];
+    G.means[3 * i + 2] = dmu.z + dlit[2];
+    for (int k = 0; k < 3; k++) G.log_scales[3 * i + k] = ds[k] * g.s[k] + dlit[3 + k];
+    G.opacity_logits[i] = dlogit + dlit[10];
     G.albedo[3 * i + 0] = dalb.x;
     G.albedo[3 * i + 1] = dalb.y;
     G.albedo[3 * i + 2] = dalb.z;
-    G.roughness[i] = drough;
+    G.roughness[i] = dlit[11];
   } else if (i < n) {
     for (int k = 0; k < 3; k++) {
       G.means[3 * i + k] = 0.0f;

@@ -1,6 +1,7 @@
 // Internal declarations of the differentiable splat path (diff.cu, capi_diff.cu).
 #pragma once
 
+#include "sl_dshade.cuh"
 #include "sl_internal.h"
 
 namespace sl {
@@ -27,11 +28,17 @@ struct DiffParams {
   const float* light_scale;     // lights
 };
 
+// The lighting of the differentiable path (sl_dshade.cuh): the emitter tree built on the host from the lights at
+// their current intensities, its derivative table ([node][light][9]: d(Le rgb, M xx yy zz xy xz yz) / d intensity),
+// and the per-Gaussian lighting state held constant (V grids, opacity-map T, iso_norm; null = visible / 1 / 1).
 struct DiffLights {
-  const float* pos;             // n x 3
-  const float* le;              // n x 3 (radiance of the emitter at scale 1)
+  dsh::EmitTree tree;
+  const float* dtab;
   uint32_t n;
   float ambient, ks;
+  const sl_vgrid* vgrid;
+  const float* lamp_T;
+  const float* iso_norm;
 };
 
 struct DiffGrads {

@@ -1,6 +1,8 @@
 // Internal declarations of the lighting kernels and their parameter blocks.
 #pragma once
 
+#include <vector>
+
 #include "sl_internal.h"
 
 namespace sl {
@@ -80,5 +82,11 @@ cudaError_t launch_sm_lookup(const SunParams& SP, const SunLayer* layers, const 
 cudaError_t launch_shade(const ShadeParams& SH, const sl_gaussian* gs, const sl_node* nodes, const sl_vgrid* vgrid,
                          const sl_part* parts, const sl_material* mats, const float* tree, const float* lamp_T,
                          const float4* env_T, const uint32_t* order, float4* colour, uint32_t count, cudaStream_t s);
+
+// The emitter tree of n records (16 floats each, albedo = Le), each emitter's Le scaled by le_scale[k] (NULL: 1), as
+// the shading pass walks it (24 floats per node); returns the root.  dtab (optional): per node and emitter the
+// derivatives of the node's Le (3) and M (6) with respect to that emitter's scale, [node][emitter][9].
+uint32_t build_emitter_tree(const float* rec, uint32_t n, const double* le_scale, std::vector<float>& out,
+                            std::vector<float>* dtab);
 
 }  // namespace sl

@@ -3,7 +3,8 @@
 
 ``params_from_scene`` turns a generated scene (splatlight_gb300.scene) into those parameters: means, log-scales,
 quaternions, opacity logits (kappa = softplus(logit) / (sqrt(2 pi) s0), the scene's own opacity), albedo, roughness
-(the material's flake roughness), and its first emitters as point lights."""
+(the material's flake roughness), and its first emitters as the emissive Gaussian lights, each with an intensity
+scale (the emitter tree over them is rebuilt at those intensities every step)."""
 from __future__ import annotations
 
 import ctypes as C
@@ -37,9 +38,8 @@ def params_from_scene(s, n_lights: int = 8, ambient: float = 0.2, ks: float = 0.
         "albedo": g["albedo"].astype(np.float32),
         "roughness": rough.astype(np.float32),
     }
-    e = s.emitters[:n_lights]
-    lights = {"pos": e["mu"].astype(np.float32), "le": e["albedo"].astype(np.float32),
-              "scale": np.ones(len(e), np.float32), "ambient": ambient, "ks": ks}
+    e = np.ascontiguousarray(s.emitters[:n_lights])
+    lights = {"rec": e, "scale": np.ones(len(e), np.float32), "ambient": ambient, "ks": ks}
     return params, lights
 
 
@@ -80,20 +80,32 @@ class DiffRenderer:
         self.close()
 
     @staticmethod
-    def to_device(params, lights):
+    def to_device(params, lights, state=None):
+        """Parameters and light intensities as device tensors; the light records stay on the host.  state
+        (optional): per-Gaussian vgrid (n VGRID records), lamp_T (n,) and iso_norm (n,), uploaded as constants."""
         import torch
         P = {k: torch.from_numpy(np.ascontiguousarray(params[k], np.float32)).cuda() for k in PARAMS}
-        Lt = {"pos": torch.from_numpy(np.ascontiguousarray(lights["pos"], np.float32)).cuda(),
-              "le": torch.from_numpy(np.ascontiguousarray(lights["le"], np.float32)).cuda(),
+        Lt = {"rec": np.ascontiguousarray(lights["rec"]),
               "scale": torch.from_numpy(np.ascontiguousarray(lights["scale"], np.float32)).cuda(),
               "ambient": float(lights["ambient"]), "ks": float(lights["ks"])}
+        st = state or {}
+        if st.get("vgrid") is not None:
+            v = np.ascontiguousarray(st["vgrid"]).view(np.int32)
+            Lt["vgrid"] = torch.from_numpy(v.copy()).cuda()
+        for k in ("lamp_T", "iso_norm"):
+            if st.get(k) is not None:
+                Lt[k] = torch.from_numpy(np.ascontiguousarray(st[k], np.float32)).cuda()
         return P, Lt
 
     def _scene(self, P, Lt):
+        def ptr(k):
+            return Lt[k].data_ptr() if Lt.get(k) is not None else None
+        rec = Lt["rec"]
         return N.DiffScene(P["means"].data_ptr(), P["log_scales"].data_ptr(), P["quats"].data_ptr(),
                            P["opacity_logits"].data_ptr(), P["albedo"].data_ptr(), P["roughness"].data_ptr(),
-                           self.n, int(Lt["scale"].numel()), Lt["pos"].data_ptr(), Lt["le"].data_ptr(),
-                           Lt["scale"].data_ptr(), Lt["ambient"], Lt["ks"])
+                           self.n, int(Lt["scale"].numel()), rec.ctypes.data if len(rec) else None,
+                           Lt["scale"].data_ptr(), Lt["ambient"], Lt["ks"], ptr("vgrid"), ptr("lamp_T"),
+                           ptr("iso_norm"))
 
     def forward(self, P, Lt, frame, eye, stream=None):
         import torch

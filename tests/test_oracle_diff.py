@@ -1,9 +1,21 @@
 """The dense FP64 forward of the differentiable path (oracle/sl_oracle_diff.c) on cases with known answers: a Gaussian
 seen along its short axis without the low-pass dilation peaks at alpha = sigmoid(opacity logit) (the splat path's
-kappa convention), and the radiance is linear in the light intensities."""
+kappa convention), and the radiance is linear in the light intensities (two emissive Gaussian lights over their
+emitter tree)."""
 import numpy as np
 
 from splatlight_gb300 import camera
+from splatlight_gb300.structs import GAUSSIAN
+
+
+def _lights():
+    rec = np.zeros(2, GAUSSIAN)
+    rec["mu"] = [[1.0, 1.0, 3.0], [-1.0, 0.5, 2.0]]
+    rec["quat"] = [0.0, 0.0, 0.0, 1.0]
+    rec["scale"] = [0.05, 0.06, 0.07]
+    rec["kappa"] = 3.0 / (np.sqrt(2 * np.pi) * 0.05)
+    rec["albedo"] = [[2.0, 2.0, 2.0], [1.0, 3.0, 1.0]]
+    return rec
 
 
 def _one(logit=0.3, lowpass=0.0, scale=(0.05, 0.2, 0.3)):
@@ -11,8 +23,7 @@ def _one(logit=0.3, lowpass=0.0, scale=(0.05, 0.2, 0.3)):
               "quats": np.array([[0.0, -np.sqrt(0.5), 0.0, np.sqrt(0.5)]]),   # axis 0 along z, towards the camera
               "opacity_logits": np.array([logit]), "albedo": np.array([[0.5, 0.25, 1.0]]),
               "roughness": np.array([0.4])}
-    lights = {"pos": np.array([[1.0, 1.0, 3.0], [-1.0, 0.5, 2.0]]), "le": np.array([[2.0, 2.0, 2.0], [1.0, 3.0, 1.0]]),
-              "scale": np.array([1.0, 1.0]), "ambient": 0.0, "ks": 0.25}
+    lights = {"rec": _lights(), "scale": np.array([1.0, 1.0]), "ambient": 0.0, "ks": 0.25}
     f = camera.make_frame((0.0, 0.0, 5.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 50.0, 65, 65, 1, far=100.0,
                           view_mode=3, n_emit=0, lowpass_px2=lowpass)
     return params, lights, f
