@@ -242,6 +242,15 @@ SL_API int sl_lighting_destroy(sl_lighting* l);
 SL_API int sl_lighting_set_emitters(sl_lighting* l, const sl_gaussian* emitters, uint32_t n, float scale,
                                     int one_sided, const float* normal, uint32_t skip_part);
 
+/* buildEmitterTree + packEmitNodes (src/lighting.js:99-169) on the host alone (no device is touched): the tree of n
+ * emitter records, each emitter's Le scaled by le_scale[k] (NULL: 1), as the shading pass walks it -- 24 floats per
+ * node into nodes_out (2n - 1 nodes: mean, radius, M diagonal, skip link, M off-diagonal, child_lo, Le, child_hi,
+ * the ASG covariance; word 19 set where the walk's 48-entry stack would be full) -- and the root into *root.
+ * dtab_out (optional, (2n - 1) x n x 9 floats): per node and emitter, d(Le rgb, M xx yy zz xy xz yz) / d le_scale[k]
+ * (central differences of the float64 build). */
+SL_API int sl_emitter_tree(const sl_gaussian* emitters, uint32_t n, const double* le_scale, float* nodes_out,
+                           float* dtab_out, uint32_t* root);
+
 /* Environment.set / write (src/environment.js:106-153): up to 4 distant lights; sky_ambient adds albedo * sky_ambient
  * to every non-emissive Gaussian (a constant stand-in for the probe-bounce sky, which is outside this pipeline). */
 SL_API int sl_lighting_set_environment(sl_lighting* l, const sl_env_light* lights, uint32_t n, float sky_ambient);

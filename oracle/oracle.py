@@ -286,6 +286,19 @@ def emitter_tree(rec: np.ndarray):
     return out, int(root), cov
 
 
+def emitter_tree_d(rec: np.ndarray, le_scale=None):
+    """The same tree in float64 with each emitter's Le scaled by le_scale: (nodes (2n-1, 16): mu, radius, M xx yy zz
+    xy xz yz, Le rgb, child_lo, child_hi (-1 for none), 0; root)."""
+    L = lib()
+    L.orc_emitter_tree_d.restype = C.c_uint32
+    L.orc_emitter_tree_d.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+    r = np.ascontiguousarray(rec, np.float32).reshape(-1, 16)
+    sc = None if le_scale is None else np.ascontiguousarray(le_scale, np.float64)
+    out = np.zeros((2 * len(r) - 1, 16), np.float64)
+    root = L.orc_emitter_tree_d(r.ctypes.data, len(r), _p(sc), out.ctypes.data)
+    return out, int(root)
+
+
 def row_tiles(splat, ty: int, tile=(16, 16)):
     """sl_row_tiles of one SPLAT record: (t0, t1) tile columns of tile row ty, or None when the row holds none."""
     rec = np.ascontiguousarray(np.asarray(splat, dtype=SPLAT).reshape(1))

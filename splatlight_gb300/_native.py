@@ -105,6 +105,7 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_lighting_create": (_I, [_P, _P, _P, _P, _U32, C.POINTER(_P)]),
     "sl_lighting_destroy": (_I, [_P]),
     "sl_lighting_set_emitters": (_I, [_P, _P, _U32, C.c_float, _I, _P, _U32]),
+    "sl_emitter_tree": (_I, [_P, _U32, _P, _P, _P, C.POINTER(_U32)]),
     "sl_lighting_set_environment": (_I, [_P, _P, _U32, C.c_float]),
     "sl_lighting_set_options": (_I, [_P, _U32, _U32, _U32, C.c_float, _I]),
     "sl_lighting_update": (_I, [_P, _P, _P, _U32, _P]),

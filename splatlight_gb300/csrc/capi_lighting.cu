@@ -490,6 +490,17 @@ int sl_lighting_destroy(sl_lighting* l) {
   return SL_OK;
 }
 
+int sl_emitter_tree(const sl_gaussian* emitters, uint32_t n, const double* le_scale, float* nodes_out,
+                    float* dtab_out, uint32_t* root) {
+  if (!emitters || !nodes_out || !root || n == 0) return fail(SL_ERR_INVALID_ARG, "null argument or no emitters");
+  if (n > 16384) return fail(SL_ERR_INVALID_ARG, "more than MAX_EMITTERS (16384) emitters");
+  std::vector<float> out, dtab;
+  *root = build_emitter_tree(reinterpret_cast<const float*>(emitters), n, le_scale, out, dtab_out ? &dtab : nullptr);
+  memcpy(nodes_out, out.data(), out.size() * 4);
+  if (dtab_out) memcpy(dtab_out, dtab.data(), dtab.size() * 4);
+  return SL_OK;
+}
+
 int sl_lighting_set_emitters(sl_lighting* l, const sl_gaussian* emitters, uint32_t n, float scale, int one_sided,
                              const float* normal, uint32_t skip_part) {
   if (!l || (n && !emitters)) return fail(SL_ERR_INVALID_ARG, "null argument");

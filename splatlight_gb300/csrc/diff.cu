@@ -528,7 +528,7 @@ __global__ void __launch_bounds__(kThreads) dproject_bwd_kernel(const DiffCamera
       const float scale = Lt.tree.scale;
       acc0 = dsh::emitter_light<float>(
           Lt.tree, rv, vg, Lt.ks, iso, eye, [&](uint32_t node, float fe, dsh::V3<float> mw, float mq) {
-            if (!Lt.dtab || !(mq > 0.0f)) return;
+            if (!Lt.dtab || !(mq > 0.0f) || node >= 2u * nl - 1u) return;  // (2 nl - 1 nodes in the table)
             const float* e = Lt.tree.nodes + 24u * node;
             for (uint32_t k = 0; k < nl; k++) {
               const float* t = Lt.dtab + ((size_t)node * nl + k) * 9u;

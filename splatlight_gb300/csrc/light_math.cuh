@@ -251,17 +251,6 @@ __device__ __forceinline__ float sym_adj_quad(f3 d, f3 o, f3 w) {
   float a01 = o.y * o.z - o.x * d.z, a02 = o.x * o.z - o.y * d.y, a12 = o.x * o.y - d.x * o.z;
   return a00 * w.x * w.x + a11 * w.y * w.y + a22 * w.z * w.z + 2.0f * (a01 * w.x * w.y + a02 * w.x * w.z + a12 * w.y * w.z);
 }
-__device__ __forceinline__ float phase_specular(f3 Sd, f3 So, f3 wi, f3 wo) {
-  f3 h = add3(wi, wo);
-  float hl = len3(h);
-  if (hl < 1e-6f) return 0.0f;
-  f3 wh = div3(h, hl);
-  float det = fmaxf(sym_det(Sd, So), 1e-20f);
-  float q = sym_adj_quad(Sd, So, wh) / det;
-  float D = 1.0f / (kPi * sqrtf(det) * q * q);
-  float sigma = sqrtf(fmaxf(dot3(wi, sym_mul(Sd, So, wi)), 1e-12f));
-  return D / (4.0f * sigma);
-}
 __device__ __forceinline__ float spec_weight(const sl_material& m) {
   if ((m.flags & 8u) == 0u || (m.flags & 1u) != 0u) return 0.0f;
   return clampf(half_lo(m.pad0), 0.0f, 1.0f);
@@ -307,72 +296,9 @@ __device__ __forceinline__ float s2_minor(s2m s) {
   float h = 0.5f * (s.x - s.z);
   return 0.5f * (s.x + s.z) - sqrtf(h * h + s.y * s.y);
 }
-__device__ __forceinline__ f2 log_map(f3 c, f3 cb0, f3 cb1, f3 a) {
-  float ca = clampf(dot3(c, a), -1.0f, 1.0f);
-  f3 v = sub3(a, mul3(c, ca));
-  float nv = len3(v);
-  if (nv < 1e-9f) return F2(0.0f, 0.0f);
-  float k = lm_acos(ca) / nv;
-  return F2(k * dot3(cb0, v), k * dot3(cb1, v));
-}
-// asg_phase (material_ext.wgsl:127-181)
-__device__ inline float asg_phase(f3 wi, f3 lb0, f3 lb1, s2m sl, f3 n0, f3 t1, f3 t2, f3 flake, f3 Sd, f3 So,
-                                  f3 wo) {
-  const float ASG_W[3] = {0.61163f, 0.35083f, 0.0267f};
-  const float ASG_A[3] = {2.54696f, 0.6893f, 0.10727f};
-  float pc = phase_specular(Sd, So, wi, wo);
-  if (flake.x <= fmaxf(flake.y, flake.z) * 1.0001f) return pc;
-  float co = dot3(n0, wo);
-  f3 n = co >= 0.0f ? n0 : mul3(n0, -1.0f);
-  float cos_o = fabsf(co);
-  f3 wr = sub3(mul3(n, 2.0f * cos_o), wo);
-  f3 rb0, rb1;
-  onb(wr, rb0, rb1);
-  f3 dw1 = add3(mul3(n, 2.0f * dot3(wo, t1)), mul3(t1, 2.0f * cos_o));
-  f3 dw2 = add3(mul3(n, 2.0f * dot3(wo, t2)), mul3(t2, 2.0f * cos_o));
-  f2 j0 = F2(dot3(rb0, dw1), dot3(rb0, dw2));
-  f2 j1 = F2(dot3(rb1, dw1), dot3(rb1, dw2));
-  f2 ia = F2(flake.y / (flake.x - flake.y), flake.z / (flake.x - flake.z));
-  s2m s0{dot2(F2(j0.x * j0.x, j0.y * j0.y), ia), dot2(F2(j0.x * j1.x, j0.y * j1.y), ia),
-         dot2(F2(j1.x * j1.x, j1.y * j1.y), ia)};
-  float pk = flake.x * flake.x / (kPi * sqrtf(flake.x * flake.y * flake.z)) /
-             (4.0f * sqrtf(fmaxf(dot3(wr, sym_mul(Sd, So, wr)), 1e-12f)));
-  f3 cs = add3(wi, wr);
-  float cl = len3(cs);
-  if (cl < 1e-4f) return pc;
-  f3 c = div3(cs, cl);
-  f3 cb0, cb1;
-  onb(c, cb0, cb1);
-  f2 dm = sub2(log_map(c, cb0, cb1, wr), log_map(c, cb0, cb1, wi));
-  s2m sL = s2_xf(sl, F2(dot3(cb0, lb0), dot3(cb0, lb1)), F2(dot3(cb1, lb0), dot3(cb1, lb1)));
-  s2m sR = s2_xf(s0, F2(dot3(cb0, rb0), dot3(cb0, rb1)), F2(dot3(cb1, rb0), dot3(cb1, rb1)));
-  float ndm = fmaxf(sqrtf(dot2(dm, dm)), 1e-9f);
-  float d = sqrtf(s2_quad_inv(s2_add(sL, s2_div(sR, 2.0f * ASG_A[2])), dm));
-  float along = sqrtf(fmaxf(s2_quad(sL, dm), 0.0f)) / ndm;
-  float far_ = smoothstepf(1.0f, 2.5f, d) * (1.0f - smoothstepf(0.15f, 0.3f, along / ndm));
-  f3 maj = s2_major(sl);
-  float ratio = sqrtf(maj.z / fmaxf(s2_minor(s0) / (2.0f * ASG_A[0]), 1e-30f));
-  float t = fmaxf(far_, 1.0f - smoothstepf(0.12f, 0.3f, ratio));
-  float p_asg = 0.0f;
-  if (t < 1.0f) {
-    for (int k = 0; k < 3; k++) {
-      s2m sk = s2_div(sR, 2.0f * ASG_A[k]);
-      s2m st = s2_add(sL, sk);
-      p_asg += ASG_W[k] * sqrtf(fmaxf(s2_det(sk), 0.0f) / fmaxf(s2_det(st), 1e-30f)) * lm_exp(-0.5f * s2_quad_inv(st, dm));
-    }
-    p_asg *= pk;
-  }
-  float p_pt = pc;
-  if (t > 0.0f) {
-    f3 ax = mul3(add3(mul3(lb0, maj.x), mul3(lb1, maj.y)), sqrtf(3.0f * maj.z));
-    p_pt = (2.0f / 3.0f) * pc + (1.0f / 6.0f) * (phase_specular(Sd, So, norm3(add3(wi, ax)), wo) +
-                                                  phase_specular(Sd, So, norm3(sub3(wi, ax)), wo));
-  }
-  return mixf(p_asg, p_pt, t);
-}
-
-// ---- the same specular and ASG phases with their per-Gaussian parts computed once (the shading pass evaluates them
-// for every light of a Gaussian's cut; only the light's direction and lobe change between calls) ----------------
+// ---- the specular and ASG phases (material_ext.wgsl:27-63, 127-181) with their per-Gaussian parts computed once
+// (the shading pass evaluates them for every light of a Gaussian's cut; only the light's direction and lobe change
+// between calls) ---------------------------------------------------------------------------------------------------
 struct SpecPre {
   f3 Sd, So;
   float det, c0;                       // max(det S, 1e-20), pi sqrt(det)
@@ -441,33 +367,40 @@ __device__ __forceinline__ float asg_phase_p(const AsgPre& a, const SpecPre& sp,
   f3 cs = add3(wi, a.wr);
   float cl = len3(cs);
   if (cl < 1e-4f) return pc;
-  f3 c = div3(cs, cl);
-  f3 cb0, cb1;
-  onb(c, cb0, cb1);
-  // log_map(c, wr) - log_map(c, wi): c bisects wi and wr, so both make the same angle with c (one acos) and the
-  // components along c cancel; the tangent-plane difference is (wr - wi) projected on (cb0, cb1), scaled by
-  // angle / sin(angle)
-  f2 dm = F2(0.0f, 0.0f);
-  {
-    const float ca = clampf(dot3(c, wi), -1.0f, 1.0f);
-    const f3 v = sub3(wi, mul3(c, ca));
-    const float nv = len3(v);
-    if (!(nv < 1e-9f)) {
-      const float k = lm_acos(ca) / nv;
-      const f3 dw = sub3(a.wr, wi);
-      dm = F2(k * dot3(cb0, dw), k * dot3(cb1, dw));
-    }
-  }
-  s2m sL = s2_xf(sl, F2(dot3(cb0, lb0), dot3(cb0, lb1)), F2(dot3(cb1, lb0), dot3(cb1, lb1)));
-  s2m sR = s2_xf(a.s0, F2(dot3(cb0, a.rb0), dot3(cb0, a.rb1)), F2(dot3(cb1, a.rb0), dot3(cb1, a.rb1)));
-  float ndm = fmaxf(sqrtf(dot2(dm, dm)), 1e-9f);
-  const float kInv2A[3] = {1.0f / (2.0f * ASG_A[0]), 1.0f / (2.0f * ASG_A[1]), 1.0f / (2.0f * ASG_A[2])};
-  float d = sqrtf(s2_quad_inv(s2_add(sL, s2m{sR.x * kInv2A[2], sR.y * kInv2A[2], sR.z * kInv2A[2]}), dm));
-  float along = sqrtf(fmaxf(s2_quad(sL, dm), 0.0f)) / ndm;
-  float far_ = smoothstepf(1.0f, 2.5f, d) * (1.0f - smoothstepf(0.15f, 0.3f, along / ndm));
+  // t = max(far, 1 - smoothstep(0.12, 0.3, ratio)) is 1 whenever ratio <= 0.12 (the light's angular extent small
+  // against the reflection lobe: about half of the evaluations on the hill scene), and then neither the ASG sum nor
+  // the `far` test is needed; the terms below are evaluated only when t can still be below 1
   f3 maj = s2_major(sl);
   float ratio = sqrtf(maj.z / a.minor0);
-  float t = fmaxf(far_, 1.0f - smoothstepf(0.12f, 0.3f, ratio));
+  float t = 1.0f - smoothstepf(0.12f, 0.3f, ratio);
+  const float kInv2A[3] = {1.0f / (2.0f * ASG_A[0]), 1.0f / (2.0f * ASG_A[1]), 1.0f / (2.0f * ASG_A[2])};
+  f2 dm = F2(0.0f, 0.0f);
+  s2m sL{0.0f, 0.0f, 0.0f}, sR{0.0f, 0.0f, 0.0f};
+  if (t < 1.0f) {
+    f3 c = div3(cs, cl);
+    f3 cb0, cb1;
+    onb(c, cb0, cb1);
+    // log_map(c, wr) - log_map(c, wi): c bisects wi and wr, so both make the same angle with c (one acos) and the
+    // components along c cancel; the tangent-plane difference is (wr - wi) projected on (cb0, cb1), scaled by
+    // angle / sin(angle)
+    {
+      const float ca = clampf(dot3(c, wi), -1.0f, 1.0f);
+      const f3 v = sub3(wi, mul3(c, ca));
+      const float nv = len3(v);
+      if (!(nv < 1e-9f)) {
+        const float k = lm_acos(ca) / nv;
+        const f3 dw = sub3(a.wr, wi);
+        dm = F2(k * dot3(cb0, dw), k * dot3(cb1, dw));
+      }
+    }
+    sL = s2_xf(sl, F2(dot3(cb0, lb0), dot3(cb0, lb1)), F2(dot3(cb1, lb0), dot3(cb1, lb1)));
+    sR = s2_xf(a.s0, F2(dot3(cb0, a.rb0), dot3(cb0, a.rb1)), F2(dot3(cb1, a.rb0), dot3(cb1, a.rb1)));
+    float ndm = fmaxf(sqrtf(dot2(dm, dm)), 1e-9f);
+    float d = sqrtf(s2_quad_inv(s2_add(sL, s2m{sR.x * kInv2A[2], sR.y * kInv2A[2], sR.z * kInv2A[2]}), dm));
+    float along = sqrtf(fmaxf(s2_quad(sL, dm), 0.0f)) / ndm;
+    float far_ = smoothstepf(1.0f, 2.5f, d) * (1.0f - smoothstepf(0.15f, 0.3f, along / ndm));
+    t = fmaxf(far_, t);
+  }
   float p_asg = 0.0f;
   if (t < 1.0f) {
     const float detR = fmaxf(s2_det(sR), 0.0f);

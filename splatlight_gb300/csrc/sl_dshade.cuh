@@ -219,9 +219,9 @@ __device__ __forceinline__ T phase_specular(const Recv<T>& r, V3<T> wi, V3<T> wo
   return D / (4.0f * sigma);
 }
 
-// The emitter light gathered by one Gaussian (shade_emitters' acc, emissive.wgsl:873-929), rgb; with lg non-null,
-// also the per-cut-node factor f_e (everything but the node's intensity) so the caller can differentiate the
-// intensities: acc = sum_e I_e(-w_e) f_e.  `visit(node, I_rgb_factor_scalar, mw)` is called per used node.
+// The emitter light gathered by one Gaussian (shade_emitters' acc, emissive.wgsl:873-929), rgb:
+// acc = sum_e Le_e scale |w_e|_M f_e over the cut nodes e.  `visit(e, f_e, w_e, |w_e|_M)` is called once per cut node
+// (f_e: everything but the node's intensity), so a caller can differentiate the intensities.
 template <typename T, typename Visit>
 __device__ __forceinline__ V3<T> emitter_light(const EmitTree& E, const Recv<T>& r, const sl_vgrid* vg, float ks,
                                                float iso_norm, V3<T> eye, Visit visit) {
@@ -245,6 +245,7 @@ __device__ __forceinline__ V3<T> emitter_light(const EmitTree& E, const Recv<T>&
       node = (child_lo != 0xFFFFFFFFu && __float_as_uint(e[19]) == 0u) ? child_hi : skip;
       continue;
     }
+    const uint32_t used = node;  // the cut node lit by (and reported to visit); the walk goes on at its skip link
     node = skip;
     const V3<T> d = sub(emean, r.P);
     const T d2 = dot(d, d);
@@ -264,7 +265,7 @@ __device__ __forceinline__ V3<T> emitter_light(const EmitTree& E, const Recv<T>&
       const T lobe = (1.0f - ks) + ks * 4.0f * 3.14159265358979f * phase_specular(r, wi, wo0) * damp;
       f = f * lobe;
     }
-    visit(node, f, mw, mq);
+    visit(used, f, mw, mq);
     const T I = mq * E.scale;
     acc = add(acc, v3(e[12] * I * f, e[13] * I * f, e[14] * I * f));
   }
