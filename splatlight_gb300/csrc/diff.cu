@@ -23,7 +23,6 @@ namespace sl {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr float kPi = 3.14159265358979f;
 
 struct F3 {
   float x, y, z;
@@ -132,11 +131,11 @@ __device__ __forceinline__ F3 lit_radiance(const DiffLights& L, const DiffParams
   const float* l = P.log_scales + 3 * i;
   const float* q = P.quats + 4 * i;
   const float mu[3] = {m[0], m[1], m[2]}, ls[3] = {l[0], l[1], l[2]}, q4[4] = {q[0], q[1], q[2], q[3]};
-  const dsh::Recv<float> rv = dsh::receiver<float>(mu, ls, q4, P.opacity_logits[i], P.roughness[i]);
+  const dsh::Recv<float, float> rv = dsh::receiver<float, float>(mu, ls, q4, P.opacity_logits[i], P.roughness[i]);
   const float iso = L.iso_norm ? L.iso_norm[i] : 1.0f, T = L.lamp_T ? L.lamp_T[i] : 1.0f;
   const dsh::V3<float> eye = dsh::v3(K.eye[0], K.eye[1], K.eye[2]);
-  const dsh::V3<float> acc = dsh::emitter_light<float>(L.tree, rv, L.vgrid ? L.vgrid + i : nullptr, L.ks, iso, eye,
-                                                       [](uint32_t, float, dsh::V3<float>, float) {});
+  const dsh::V3<float> acc = dsh::emitter_light(L.tree, rv, L.vgrid ? L.vgrid + i : nullptr, L.ks, iso, eye,
+                                                [](uint32_t, float, dsh::V3<float>, float) {});
   const float k = T * iso;
   const F3 alb = ld3(P.albedo + 3 * i);
   return f3(alb.x * (acc.x * k + L.ambient), alb.y * (acc.y * k + L.ambient), alb.z * (acc.z * k + L.ambient));
@@ -392,7 +391,9 @@ __global__ void __launch_bounds__(kThreads) dcomposite_bwd_kernel(const uint2* _
 }
 
 // Per-Gaussian chain rule from the 2D gradients to the parameters (and the lights' intensities).
-__global__ void __launch_bounds__(kThreads) dproject_bwd_kernel(const DiffCamera K, const DiffParams P,
+// Two blocks per SM (at most 128 registers): the lighting Jacobian's dual passes are latency-bound, and twice the
+// resident warps (with some spilling) measured 13.6 ms per step against 15.6 ms at one block of 247 registers.
+__global__ void __launch_bounds__(kThreads, 2) dproject_bwd_kernel(const DiffCamera K, const DiffParams P,
                                                                 const DiffLights Lt, uint32_t n,
                                                                 const DiffGrad2D* __restrict__ g2,
                                                                 const DiffRec* __restrict__ drec, DiffGrads G) {
@@ -500,34 +501,42 @@ __global__ void __launch_bounds__(kThreads) dproject_bwd_kernel(const DiffCamera
     const float* pm = P.means + 3 * i;
     const float* pl = P.log_scales + 3 * i;
     const float* pq = P.quats + 4 * i;
+    const float mu0[3] = {pm[0], pm[1], pm[2]}, ls0[3] = {pl[0], pl[1], pl[2]};
+    const float q40[4] = {pq[0], pq[1], pq[2], pq[3]}, rough0 = P.roughness[i];
+    const dsh::V3<float> eyef = dsh::v3(K.eye[0], K.eye[1], K.eye[2]);
     float dlit[12];
+    // position directions: the shape and material stay plain floats
 #pragma unroll 1
-    for (int p = 0; p < 12; p++) {
-      dsh::Dual mu[3], ls[3], q4[4];
-      for (int k = 0; k < 3; k++) {
-        mu[k] = dsh::Dual{pm[k], p == k ? 1.0f : 0.0f};
-        ls[k] = dsh::Dual{pl[k], p == 3 + k ? 1.0f : 0.0f};
-      }
-      for (int k = 0; k < 4; k++) q4[k] = dsh::Dual{pq[k], p == 6 + k ? 1.0f : 0.0f};
-      const dsh::Dual lg{logit, p == 10 ? 1.0f : 0.0f}, rg{P.roughness[i], p == 11 ? 1.0f : 0.0f};
-      const dsh::Recv<dsh::Dual> rv = dsh::receiver<dsh::Dual>(mu, ls, q4, lg, rg);
-      const dsh::V3<dsh::Dual> eye = dsh::v3(dsh::cst<dsh::Dual>(K.eye[0]), dsh::cst<dsh::Dual>(K.eye[1]),
-                                             dsh::cst<dsh::Dual>(K.eye[2]));
-      const dsh::V3<dsh::Dual> acc = dsh::emitter_light<dsh::Dual>(
-          Lt.tree, rv, vg, Lt.ks, iso, eye, [](uint32_t, dsh::Dual, dsh::V3<dsh::Dual>, dsh::Dual) {});
+    for (int p = 0; p < 3; p++) {
+      dsh::Dual mu[3];
+      for (int k = 0; k < 3; k++) mu[k] = dsh::Dual{mu0[k], p == k ? 1.0f : 0.0f};
+      const dsh::Recv<dsh::Dual, float> rv = dsh::receiver<dsh::Dual, float>(mu, ls0, q40, logit, rough0);
+      const dsh::V3<dsh::Dual> acc =
+          dsh::emitter_light(Lt.tree, rv, vg, Lt.ks, iso, eyef, [](uint32_t, auto, auto, auto) {});
+      dlit[p] = ga.x * acc.x.d + ga.y * acc.y.d + ga.z * acc.z.d;
+    }
+    // shape and material directions (log-scales 3, quaternion 4, opacity logit, roughness): the position, and with it
+    // every light direction, distance, V-grid lookup and light intensity, stays a plain float
+#pragma unroll 1
+    for (int p = 3; p < 12; p++) {
+      dsh::Dual ls[3], q4[4];
+      for (int k = 0; k < 3; k++) ls[k] = dsh::Dual{ls0[k], p == 3 + k ? 1.0f : 0.0f};
+      for (int k = 0; k < 4; k++) q4[k] = dsh::Dual{q40[k], p == 6 + k ? 1.0f : 0.0f};
+      const dsh::Dual lg{logit, p == 10 ? 1.0f : 0.0f}, rg{rough0, p == 11 ? 1.0f : 0.0f};
+      const dsh::Recv<float, dsh::Dual> rv = dsh::receiver<float, dsh::Dual>(mu0, ls, q4, lg, rg);
+      const dsh::V3<dsh::Dual> acc =
+          dsh::emitter_light(Lt.tree, rv, vg, Lt.ks, iso, eyef, [](uint32_t, auto, auto, auto) {});
       dlit[p] = ga.x * acc.x.d + ga.y * acc.y.d + ga.z * acc.z.d;
     }
     // the value pass: albedo's gradient, and the light intensities' through the tree's derivative table (per cut node
     // e and light k: dI_e/ds_k = dLe_e/ds_k scale |w|_M + Le_e scale (w^T dM_e/ds_k w) / (2 |w|_M))
     dsh::V3<float> acc0;
     {
-      const float mu[3] = {pm[0], pm[1], pm[2]}, ls[3] = {pl[0], pl[1], pl[2]}, q4[4] = {pq[0], pq[1], pq[2], pq[3]};
-      const dsh::Recv<float> rv = dsh::receiver<float>(mu, ls, q4, logit, P.roughness[i]);
-      const dsh::V3<float> eye = dsh::v3(K.eye[0], K.eye[1], K.eye[2]);
+      const dsh::Recv<float, float> rv = dsh::receiver<float, float>(mu0, ls0, q40, logit, rough0);
       const uint32_t nl = Lt.n;
       const float scale = Lt.tree.scale;
-      acc0 = dsh::emitter_light<float>(
-          Lt.tree, rv, vg, Lt.ks, iso, eye, [&](uint32_t node, float fe, dsh::V3<float> mw, float mq) {
+      acc0 = dsh::emitter_light(
+          Lt.tree, rv, vg, Lt.ks, iso, eyef, [&](uint32_t node, float fe, dsh::V3<float> mw, float mq) {
             if (!Lt.dtab || !(mq > 0.0f) || node >= 2u * nl - 1u) return;  // (2 nl - 1 nodes in the table)
             const float* e = Lt.tree.nodes + 24u * node;
             for (uint32_t k = 0; k < nl; k++) {
