@@ -622,6 +622,7 @@ def run_headline(args, stream, flush, dist, world, local):
     B = BatchRenderer(rs, ls, max_views=n)
     out = torch.empty(4 * pix, dtype=torch.float32, device="cuda")
     tile, tune_ms = B.autotune(views, reps=2)
+    blocks_per_sm = B.tuning()[1]
     sc = stream.cuda_stream
 
     def batched():
@@ -736,7 +737,7 @@ def run_headline(args, stream, flush, dist, world, local):
     for r in rs:
         r.close()
     return {"ms": ms, "views": n, "pixels": pix, "value": world * n * 1000.0 / ms, "clocks": clk.summary(),
-            "stage_ms": stage_ms, "stats": stats, "tile": tile, "autotune_ms": tune_ms,
+            "stage_ms": stage_ms, "stats": stats, "tile": tile, "autotune_ms": tune_ms, "blocks_per_sm": blocks_per_sm,
             "plain_ms": plain_ms, "deferred_ms": deferred_ms, "max_abs_err_vs_plain": err,
             "e2e": {"value": round(world * n / e2e_s, 2), "unit": "views/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)}, "e2e_image_matches_device": e2e_err == 0.0,
@@ -969,6 +970,7 @@ def main():
     detail = {"headline": {"stage_ms": {k: round(v, 4) for k, v in hd["stage_ms"].items()}, "stage_rooflines": roofs,
                            "stats": hd["stats"], "tile": f"{hd['tile'][0]}x{hd['tile'][1]}",
                            "autotune_ms": {k: round(v, 3) for k, v in hd["autotune_ms"].items()},
+                           "tuned_blocks_per_sm": hd["blocks_per_sm"],
                            "e2e_image_matches_device": hd["e2e_image_matches_device"]}}
     plain = None
     if not args.no_plain:

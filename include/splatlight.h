@@ -409,11 +409,21 @@ SL_API int sl_batch_render(sl_batch* b, const uint32_t* scene_of_view, const sl_
 SL_API int sl_batch_read_view(sl_batch* b, uint32_t view, uint32_t* order, uint32_t* ranges, uint32_t* entries,
                               uint64_t entries_cap, uint64_t* n_entries);
 /* Picks the fastest tile shape for this batch of views (renders it with each of 16x16, 8x32, 32x8, timed on the
- * device, `reps` times each) and keeps it; writes the per-shape times (ms) to ms_out[3] if not NULL. */
+ * device, `reps` times each) and keeps it; writes the per-shape times (ms) to ms_out[3] if not NULL.  Then, with that
+ * shape, picks each of bproject's, btile_bin's, bshade's and bcomposite's block-size variant (the blocks per SM its
+ * register budget is compiled for) by the device time of its stage, one kernel after the other. */
 SL_API int sl_batch_autotune(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* frames,
                              const float* eyes, const float* light_scales, uint32_t n_views, float* out_dev,
                              uint64_t out_floats, uint32_t reps, uint32_t* tile_w, uint32_t* tile_h, float* ms_out,
                              void* stream);
+
+/* The batch's tuning: tile shape and, per kernel (bproject, btile_bin, bshade, bcomposite), the blocks per SM of
+ * the variant in use (min_blocks[4]).  Any pointer may be NULL. */
+SL_API int sl_batch_get_tuning(sl_batch* b, uint32_t* tile_w, uint32_t* tile_h, uint32_t* min_blocks);
+/* Sets the block-size variants by their blocks per SM (min_blocks[4], as sl_batch_get_tuning reports them; bproject
+ * 4 or 3, btile_bin 4 or 5, bshade 4, 3 or 5, bcomposite 6 or 5; SL_ERR_INVALID_ARG for any other).  Every variant
+ * computes the same results. */
+SL_API int sl_batch_set_tuning(sl_batch* b, const uint32_t* min_blocks);
 
 /* ---- differentiable rendering (no counterpart in the reference) ------------------------------------------------- */
 

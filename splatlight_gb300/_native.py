@@ -141,6 +141,8 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_server_destroy": (_I, [_P]),
     "sl_batch_autotune": (_I, [_P, _P, _P, _P, _P, _U32, _P, _U64, _U32, C.POINTER(_U32), C.POINTER(_U32),
                                _P, _P]),
+    "sl_batch_get_tuning": (_I, [_P, C.POINTER(_U32), C.POINTER(_U32), _P]),
+    "sl_batch_set_tuning": (_I, [_P, _P]),
 }
 
 _lib: C.CDLL | None = None

@@ -108,8 +108,24 @@ class BatchRenderer:
         host = dev[: 4 * sum(h * w for h, w in sizes)].cpu().numpy()
         return [host[int(o):int(o) + 4 * h * w].reshape(h, w, 4) for o, (h, w) in zip(offs, sizes)]
 
+    def tuning(self):
+        """((tile_w, tile_h), {kernel: blocks per SM of its variant in use}) for bproject, btile_bin, bshade,
+        bcomposite."""
+        tw, th = C.c_uint32(), C.c_uint32()
+        mb = np.zeros(4, dtype=np.uint32)
+        N.check(self._lib.sl_batch_get_tuning(self._h, C.byref(tw), C.byref(th), mb.ctypes.data))
+        names = ("bproject", "btile_bin", "bshade", "bcomposite")
+        return (tw.value, th.value), {k: int(v) for k, v in zip(names, mb)}
+
+    def set_tuning(self, blocks_per_sm: dict):
+        """Sets each tunable kernel's block-size variant by its blocks per SM (keys as tuning() reports them)."""
+        names = ("bproject", "btile_bin", "bshade", "bcomposite")
+        mb = np.array([blocks_per_sm[k] for k in names], dtype=np.uint32)
+        N.check(self._lib.sl_batch_set_tuning(self._h, mb.ctypes.data))
+
     def autotune(self, views, reps: int = 3):
-        """Times the batch with each tile shape, keeps the fastest; returns ((tile_w, tile_h), ms per shape)."""
+        """Times the batch with each tile shape and keeps the fastest, then each tunable kernel's block-size variant
+        by its stage's time; returns ((tile_w, tile_h), ms per shape)."""
         frames, scenes, eyes, scales, pix = self._pack(views)
         dev = self._device_out(4 * pix, None)
         tw, th = C.c_uint32(), C.c_uint32()

@@ -21,7 +21,8 @@ constexpr int kThreads = 256;
 // at the running offset, so entries stay in sorted (view, depth) order.  The digit counts of the local id go to
 // digit_hist for the tile sort; the last block writes the batch's entry total (which may exceed capacity: the entries
 // past it are not written and the overflow flag is set).
-__global__ void __launch_bounds__(kThreads) btile_bin_kernel(const uint32_t* __restrict__ order,
+template <int MinB>
+__global__ void __launch_bounds__(kThreads, MinB) btile_bin_kernel(const uint32_t* __restrict__ order,
                                                              const ushort4* __restrict__ rects,
                                                              const SplatRec* __restrict__ recs,
                                                              const BatchView* __restrict__ views,
@@ -210,15 +211,25 @@ size_t btile_bin_scratch_bytes(uint32_t n_max) { return 16 + 8ull * ((n_max + kT
 cudaError_t launch_btile_bin(const uint32_t* order, const ushort4* rects, const SplatRec* recs, const BatchView* views,
                              const uint32_t* block_view, const uint32_t* n_dev, uint32_t n_max, uint32_t tw,
                              uint32_t th, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
-                             uint32_t* tile_vals, uint32_t* digit_hist, void* scratch, cudaStream_t s) {
+                             uint32_t* tile_vals, uint32_t* digit_hist, void* scratch, int variant, cudaStream_t s) {
   if (!n_max) return cudaSuccess;
   const uint32_t blocks = (n_max + kThreads - 1) / kThreads;
   cudaError_t e = cudaMemsetAsync(scratch, 0, btile_bin_scratch_bytes(n_max), s);
   if (e != cudaSuccess) return e;
   uint32_t* ticket = reinterpret_cast<uint32_t*>(scratch);
   uint64_t* status = reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(scratch) + 16);
-  btile_bin_kernel<<<blocks, kThreads, 0, s>>>(order, rects, recs, views, block_view, n_dev, n_max, tw, th, capacity,
-                                               ctr, tile_keys, tile_vals, digit_hist, ticket, status);
+  switch (kTuneMinBlocks[1][variant]) {
+    case 4:
+      btile_bin_kernel<4><<<blocks, kThreads, 0, s>>>(order, rects, recs, views, block_view, n_dev, n_max, tw, th,
+                                                      capacity, ctr, tile_keys, tile_vals, digit_hist, ticket, status);
+      break;
+    case 5:
+      btile_bin_kernel<5><<<blocks, kThreads, 0, s>>>(order, rects, recs, views, block_view, n_dev, n_max, tw, th,
+                                                      capacity, ctr, tile_keys, tile_vals, digit_hist, ticket, status);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

@@ -4,7 +4,9 @@
 // over the lit views' tiles, batched shading of the Gaussians it marked (deferred shading: each view at its own eye),
 // one compositor launch over every tile of every view.  Grids are sized for the batch's capacity and every per-batch value
 // the kernels read comes from device memory uploaded (from pinned staging) at the head of the chain, so the chain is
-// captured once in a CUDA graph and replayed for every batch that fits.  An autotuner picks the tile shape.
+// captured once in a CUDA graph and replayed for every batch that fits.  An autotuner picks the tile shape, then the
+// block-size variant (blocks per SM its registers are budgeted for) of each of bproject, btile_bin, bshade and
+// bcomposite.
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
@@ -153,7 +155,7 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   CK(stage(0));
   CK(launch_bproject(b->views.as<BatchView>(), b->block_view.as<uint32_t>(), B, b->keys32.as<uint32_t>(),
                      b->recs.as<SplatRec>(), b->rects.as<ushort4>(), hist, b->view_maxrad.as<uint32_t>(),
-                     b->view_visible.as<uint32_t>(), b->block_valid.as<uint32_t>(), s));
+                     b->view_visible.as<uint32_t>(), b->block_valid.as<uint32_t>(), b->variant[0], s));
   // the depth sort runs over the visible slots only: their keys compacted in slot order (stability kept), the count
   // in ctr->visible (read on the device by the sort and the binning)
   CK(exclusive_scan_u32(b->block_valid.as<uint32_t>(), b->block_off.as<uint32_t>(), B, &ctr->visible,
@@ -169,7 +171,8 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   CK(stage(2));
   CK(launch_btile_bin(b->order.as<uint32_t>(), b->rects.as<ushort4>(), b->recs.as<SplatRec>(), b->views.as<BatchView>(),
                       b->block_view.as<uint32_t>(), n_visible, S, b->tile_w, b->tile_h, E, ctr,
-                      b->tile_keys.as<uint32_t>(), b->tile_vals.as<uint32_t>(), hist + 768, b->bin_scratch.ptr, s));
+                      b->tile_keys.as<uint32_t>(), b->tile_vals.as<uint32_t>(), hist + 768, b->bin_scratch.ptr,
+                      b->variant[1], s));
   // the tile sort: stable on the 16-bit view-local tile id (two passes); entries arrive in (view, depth) order, so
   // each (view, tile) run comes out contiguous and depth-ordered
   CK(sort32_pairs(b->tile_keys.as<uint32_t>(), b->tile_keys_alt.as<uint32_t>(), b->tile_vals.as<uint32_t>(),
@@ -191,11 +194,11 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
                         b->view_shade.as<uint32_t>(), s));
   CK(launch_bshade(b->views.as<BatchView>(), b->scenes_dev.as<BatchScene>(), b->block_view.as<uint32_t>(), B,
                    b->vals_alt.as<uint32_t>(), b->view_shade.as<uint32_t>(), b->recs.as<SplatRec>(),
-                   b->view_maxrad.as<uint32_t>(), s));
+                   b->view_maxrad.as<uint32_t>(), b->variant[2], s));
   CK(stage(5));
   CK(launch_bcomposite(C, b->ranges.as<uint2>(), b->tile_vals.as<uint32_t>(), b->recs.as<SplatRec>(),
                        b->views_out.as<BatchViewOut>(), b->view_maxrad.as<uint32_t>(), b->dyn.as<BatchDyn>(), T, ctr,
-                       s));
+                       b->variant[3], s));
   CK(stage(6));
   CK(cudaMemcpyAsync(b->h_ctr, ctr, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(b->h_visible, b->view_visible.ptr, 4ull * V, cudaMemcpyDeviceToHost, s));
@@ -653,11 +656,64 @@ int sl_batch_autotune(sl_batch* b, const uint32_t* scene_of_view, const sl_rende
       best_k = k;
     }
   }
-  b->timing = timing;
   b->tile_w = kShapes[best_k][0];
   b->tile_h = kShapes[best_k][1];
+  // then each tunable kernel's block-size variant, one kernel at a time, by the device time of its stage
+  static const int kStageOf[kTuneKernels] = {0, 2, 4, 5};  // sl_batch_stats.ms_stage: project, bin, shade, composite
+  const bool stage_timing = b->stage_timing;
+  b->stage_timing = true;
+  int rc = SL_OK;
+  for (int k = 0; k < kTuneKernels && rc == SL_OK; k++) {
+    int best_v = b->variant[k];
+    float best_ms = 0.0f;
+    for (int v = 0; v < kTuneVariants[k] && rc == SL_OK; v++) {
+      b->variant[k] = v;
+      drop_graph(b);
+      sl_batch_stats st;
+      rc = sl_batch_render(b, scene_of_view, frames, eyes, light_scales, n_views, out_dev, out_floats, nullptr, &st,
+                           stream);
+      float sum = 0.0f;
+      for (uint32_t r = 0; rc == SL_OK && r < reps; r++) {
+        rc = sl_batch_render(b, scene_of_view, frames, eyes, light_scales, n_views, out_dev, out_floats, nullptr,
+                             &st, stream);
+        sum += st.ms_stage[kStageOf[k]];
+      }
+      if (rc == SL_OK && (v == 0 || sum < best_ms)) {
+        best_ms = sum;
+        best_v = v;
+      }
+    }
+    b->variant[k] = best_v;
+  }
+  drop_graph(b);
+  b->stage_timing = stage_timing;
+  b->timing = timing;
+  if (rc) return rc;
   if (tile_w) *tile_w = b->tile_w;
   if (tile_h) *tile_h = b->tile_h;
+  return SL_OK;
+}
+
+int sl_batch_set_tuning(sl_batch* b, const uint32_t* min_blocks) {
+  if (!b || !min_blocks) return fail(SL_ERR_INVALID_ARG, "null argument");
+  int v[kTuneKernels];
+  for (int k = 0; k < kTuneKernels; k++) {
+    v[k] = -1;
+    for (int j = 0; j < kTuneVariants[k]; j++)
+      if ((uint32_t)kTuneMinBlocks[k][j] == min_blocks[k]) v[k] = j;
+    if (v[k] < 0) return fail(SL_ERR_INVALID_ARG, "no such block-size variant");
+  }
+  for (int k = 0; k < kTuneKernels; k++) b->variant[k] = v[k];
+  drop_graph(b);
+  return SL_OK;
+}
+
+int sl_batch_get_tuning(sl_batch* b, uint32_t* tile_w, uint32_t* tile_h, uint32_t* min_blocks) {
+  if (!b) return fail(SL_ERR_INVALID_ARG, "null batch");
+  if (tile_w) *tile_w = b->tile_w;
+  if (tile_h) *tile_h = b->tile_h;
+  if (min_blocks)
+    for (int k = 0; k < kTuneKernels; k++) min_blocks[k] = (uint32_t)kTuneMinBlocks[k][b->variant[k]];
   return SL_OK;
 }
 

@@ -163,9 +163,27 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
       by0 = max(by0, 0);
       bx1 = min(bx1, BX - 1);
       by1 = min(by1, BY - 1);
-      if (bx0 <= bx1) {
-        const uint32_t row = ((2u << bx1) - 1u) & ~((1u << bx0) - 1u);
-        for (int by = by0; by <= by1; by++) bits |= row << (by * BX);
+      if (bx0 <= bx1 && by0 <= by1) {
+        // of the blocks in the box, keep those the ellipse q <= qcut can reach: with local = G d, a pixel p of a
+        // block centred at c has |G (p - mu)| >= |G (c - mu)| - R, R the largest |G h| over the block's half-extent
+        // corners h = (+-3.5, +-1.5) (a norm is convex, so its maximum over the rectangle is at a corner); a block
+        // with |G (c - mu)| > sqrt(qcut) + R holds no kept pixel.  The limit carries a relative margin of 1e-3 and
+        // an absolute one of 1e-3, far above the rounding of the per-pixel q, so no kept fragment is ever culled.
+        const float g00 = A.z, g01 = A.w, g10 = rb[t].b.x, g11 = rb[t].b.y;
+        const float r1x = fmaf(3.5f, g00, 1.5f * g01), r1y = fmaf(3.5f, g10, 1.5f * g11);
+        const float r2x = fmaf(3.5f, g00, -1.5f * g01), r2y = fmaf(3.5f, g10, -1.5f * g11);
+        const float R = sqrtf(fmaxf(fmaf(r1x, r1x, r1y * r1y), fmaf(r2x, r2x, r2y * r2y)));
+        const float lim = fmaf(sqrtf(fmaxf(rb[t].b.w, 0.0f)) + R, 1.001f, 1e-3f);
+        const float lim2 = lim * lim;
+        const float ox = fx0 + 4.0f - A.x, oy = fy0 + 2.0f - A.y;  // block (0, 0)'s centre less the splat's
+        for (int by = by0; by <= by1; by++) {
+          const float dy = fmaf(4.0f, (float)by, oy);
+          for (int bx = bx0; bx <= bx1; bx++) {
+            const float dx = fmaf(8.0f, (float)bx, ox);
+            const float lx = fmaf(dx, g00, dy * g01), ly = fmaf(dx, g10, dy * g11);
+            if (fmaf(lx, lx, ly * ly) <= lim2) bits |= 1u << (by * BX + bx);
+          }
+        }
       }
       if constexpr (kMark) {
         const float4 B = rb[t].b;
@@ -273,8 +291,10 @@ __global__ void __launch_bounds__(kThreads) composite_kernel(const CompositePara
 }
 
 // Batched: one CTA per tile of any view; the view comes from a binary search of the tiles' prefix over views.
-template <int TW>
-__global__ void __launch_bounds__(kThreads) bcomposite_kernel(const BatchComposite B, const uint2* __restrict__ ranges,
+// MinB blocks per SM (the autotuner's variants: 6 = at most 40 registers, a few bytes spilled on a cold path; 5 =
+// uncapped at 46 registers, which measured 4% slower on the 64-view mix).
+template <int TW, int MinB>
+__global__ void __launch_bounds__(kThreads, MinB) bcomposite_kernel(const BatchComposite B, const uint2* __restrict__ ranges,
                                                               const uint32_t* __restrict__ tile_vals,
                                                               const SplatRec* __restrict__ recs,
                                                               const BatchViewOut* __restrict__ views,
@@ -380,21 +400,28 @@ cudaError_t launch_composite(const CompositeParams& P, const uint2* ranges, cons
 namespace sl {
 cudaError_t launch_bcomposite(const BatchComposite& B, const uint2* ranges, const uint32_t* tile_vals,
                               const SplatRec* recs, const BatchViewOut* views, const uint32_t* view_maxrad,
-                              const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s) {
+                              const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, int variant,
+                              cudaStream_t s) {
   if (max_tiles == 0) return cudaSuccess;
+  const int mb = kTuneMinBlocks[3][variant];
+  if (mb != 5 && mb != 6) return cudaErrorInvalidValue;
+#define SL_BCOMP(TW, MB)                                                                                        \
+  bcomposite_kernel<TW, MB><<<max_tiles, kThreads, 0, s>>>(B, ranges, tile_vals, recs, views, view_maxrad, dyn, \
+                                                           ctr)
   switch (B.tile_w) {
     case 16:
-      bcomposite_kernel<16><<<max_tiles, kThreads, 0, s>>>(B, ranges, tile_vals, recs, views, view_maxrad, dyn, ctr);
+      if (mb == 6) SL_BCOMP(16, 6); else SL_BCOMP(16, 5);
       break;
     case 8:
-      bcomposite_kernel<8><<<max_tiles, kThreads, 0, s>>>(B, ranges, tile_vals, recs, views, view_maxrad, dyn, ctr);
+      if (mb == 6) SL_BCOMP(8, 6); else SL_BCOMP(8, 5);
       break;
     case 32:
-      bcomposite_kernel<32><<<max_tiles, kThreads, 0, s>>>(B, ranges, tile_vals, recs, views, view_maxrad, dyn, ctr);
+      if (mb == 6) SL_BCOMP(32, 6); else SL_BCOMP(32, 5);
       break;
     default:
       return cudaErrorInvalidValue;
   }
+#undef SL_BCOMP
   return cudaGetLastError();
 }
 }  // namespace sl

@@ -389,7 +389,8 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const __grid_constant
 // Batched: one block of 256 slots of one view; the view comes from block_view (kNoView: padding past the batch).
 // Keys carry the view above the 16 depth bits, so one stable sort orders every view's slots exactly as the per-view
 // sort does; lit radiance is filled in by the batched shading pass.
-__global__ void __launch_bounds__(kThreads, 4) bproject_kernel(const BatchView* __restrict__ views,
+template <int MinB>
+__global__ void __launch_bounds__(kThreads, MinB) bproject_kernel(const BatchView* __restrict__ views,
                                                             const uint32_t* __restrict__ block_view,
                                                             uint32_t* __restrict__ keys32, SplatRec* __restrict__ recs,
                                                             ushort4* __restrict__ rects, uint32_t* __restrict__ digit_hist,
@@ -447,10 +448,20 @@ __global__ void __launch_bounds__(kThreads, 4) bproject_kernel(const BatchView* 
 
 cudaError_t launch_bproject(const BatchView* views, const uint32_t* block_view, uint32_t max_blocks, uint32_t* keys32,
                             SplatRec* recs, ushort4* rects, uint32_t* digit_hist, uint32_t* view_maxrad,
-                            uint32_t* view_visible, uint32_t* block_valid, cudaStream_t s) {
+                            uint32_t* view_visible, uint32_t* block_valid, int variant, cudaStream_t s) {
   if (max_blocks == 0) return cudaSuccess;
-  bproject_kernel<<<max_blocks, kThreads, 0, s>>>(views, block_view, keys32, recs, rects, digit_hist, view_maxrad,
-                                                  view_visible, block_valid);
+  switch (kTuneMinBlocks[0][variant]) {
+    case 4:
+      bproject_kernel<4><<<max_blocks, kThreads, 0, s>>>(views, block_view, keys32, recs, rects, digit_hist,
+                                                         view_maxrad, view_visible, block_valid);
+      break;
+    case 3:
+      bproject_kernel<3><<<max_blocks, kThreads, 0, s>>>(views, block_view, keys32, recs, rects, digit_hist,
+                                                         view_maxrad, view_visible, block_valid);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

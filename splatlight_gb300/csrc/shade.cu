@@ -167,7 +167,7 @@ __device__ __forceinline__ f3 shade_one(const ShadeParams& SH, const sl_gaussian
   return c;
 }
 
-__global__ void __launch_bounds__(kThreads) shade_kernel(const __grid_constant__ ShadeParams SH,
+__global__ void __launch_bounds__(kThreads, 4) shade_kernel(const __grid_constant__ ShadeParams SH,
                                                          const sl_gaussian* __restrict__ gs,
                                                          const sl_node* __restrict__ nodes,
                                                          const sl_vgrid* __restrict__ vgrid,
@@ -188,7 +188,10 @@ __global__ void __launch_bounds__(kThreads) shade_kernel(const __grid_constant__
 // Batched: the marked scene Gaussians of every lit view (the coverage pass), shaded from the view's eye, with the
 // palette and albedo scale the projection applies to bound radiance (project.wgsl:321-350), written into the splat
 // records.
-__global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __restrict__ views,
+// MinB 128-thread blocks per SM (the autotuner's variants: 4 = at most 128 registers, 3 = uncapped at 143, 5 = at
+// most 102; on the 64-view mix 4 measured 6.4 ms against 7.6 ms for 3).
+template <int MinB>
+__global__ void __launch_bounds__(kThreads, MinB) bshade_kernel(const BatchView* __restrict__ views,
                                                           const BatchScene* __restrict__ scenes,
                                                           const uint32_t* __restrict__ block_view,
                                                           const uint32_t* __restrict__ list,
@@ -257,9 +260,24 @@ __global__ void __launch_bounds__(kThreads) bshade_kernel(const BatchView* __res
 
 cudaError_t launch_bshade(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
                           uint32_t max_blocks, const uint32_t* list, const uint32_t* view_shade, SplatRec* recs,
-                          uint32_t* view_maxrad, cudaStream_t s) {
+                          uint32_t* view_maxrad, int variant, cudaStream_t s) {
   if (max_blocks == 0) return cudaSuccess;
-  bshade_kernel<<<2 * max_blocks, kThreads, 0, s>>>(views, scenes, block_view, list, view_shade, recs, view_maxrad);
+  switch (kTuneMinBlocks[2][variant]) {
+    case 4:
+      bshade_kernel<4><<<2 * max_blocks, kThreads, 0, s>>>(views, scenes, block_view, list, view_shade, recs,
+                                                           view_maxrad);
+      break;
+    case 3:
+      bshade_kernel<3><<<2 * max_blocks, kThreads, 0, s>>>(views, scenes, block_view, list, view_shade, recs,
+                                                           view_maxrad);
+      break;
+    case 5:
+      bshade_kernel<5><<<2 * max_blocks, kThreads, 0, s>>>(views, scenes, block_view, list, view_shade, recs,
+                                                           view_maxrad);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

@@ -201,9 +201,15 @@ struct BatchView {
 };
 constexpr uint32_t kNoView = 0xFFFFFFFFu;
 // block_valid[block]: the block's valid keys (0 for blocks past the batch); digit_hist counts valid keys only.
+// The batched chain's block-size variants, picked per kernel by sl_batch_autotune: blocks per SM that each kernel's
+// register budget is compiled for (variant 0 is the default).
+constexpr int kTuneKernels = 4;                  // bproject, btile_bin, bshade, bcomposite
+constexpr int kTuneVariants[kTuneKernels] = {2, 2, 3, 2};
+constexpr int kTuneMinBlocks[kTuneKernels][3] = {{4, 3, 0}, {4, 5, 0}, {4, 3, 5}, {6, 5, 0}};
 cudaError_t launch_bproject(const BatchView* views, const uint32_t* block_view, uint32_t max_blocks, uint32_t* keys32,
                             SplatRec* recs, ushort4* rects, uint32_t* digit_hist /*[3][256]*/,
-                            uint32_t* view_maxrad, uint32_t* view_visible, uint32_t* block_valid, cudaStream_t s);
+                            uint32_t* view_maxrad, uint32_t* view_visible, uint32_t* block_valid, int variant,
+                            cudaStream_t s);
 // batch.cu: the valid keys of every block, in slot order, at block_off[block] (the exclusive scan of block_valid):
 // keys_c / slots_c, for the depth sort over the visible slots only.
 cudaError_t launch_bcompact(const uint32_t* block_view, const uint32_t* keys32, const uint32_t* block_off,
@@ -234,7 +240,8 @@ struct BatchDyn {
 };
 cudaError_t launch_bcomposite(const BatchComposite& B, const uint2* ranges, const uint32_t* tile_vals,
                               const SplatRec* recs, const BatchViewOut* views, const uint32_t* view_maxrad,
-                              const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, cudaStream_t s);
+                              const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, int variant,
+                              cudaStream_t s);
 // batch.cu (totals: the BatchDyn, read as u32 words: [0] total slots, [1] total tiles)
 // batch.cu: the batch's tile entries in one pass (counts, their ordered offsets by a decoupled look-back, emission);
 // the entry total goes to ctr->entries.  scratch: btile_bin_scratch_bytes(n_max) bytes, cleared by the launcher.
@@ -242,7 +249,7 @@ size_t btile_bin_scratch_bytes(uint32_t n_max);
 cudaError_t launch_btile_bin(const uint32_t* order, const ushort4* rects, const SplatRec* recs, const BatchView* views,
                              const uint32_t* block_view, const uint32_t* n_dev, uint32_t n_max, uint32_t tw,
                              uint32_t th, uint32_t capacity, FrameCounters* ctr, uint32_t* tile_keys,
-                             uint32_t* tile_vals, uint32_t* digit_hist, void* scratch, cudaStream_t s);
+                             uint32_t* tile_vals, uint32_t* digit_hist, void* scratch, int variant, cudaStream_t s);
 // The batched coverage pass over the tiles of lit views, run between binning and shading: marks[slot] = 1 for each
 // splat that blends a fragment before the pixel's transmittance falls below t_mark (BatchViewOut::lit 1) or at all
 // (lit 2).  t_mark = t_stop_scale / max(2 r, rad_cap), r the view's radiance bound so far (its unshaded splats,

@@ -63,7 +63,7 @@ struct BatchScene {
 // scale into their splat records' radiance, and raises the view's maximum radiance.
 cudaError_t launch_bshade(const BatchView* views, const BatchScene* scenes, const uint32_t* block_view,
                           uint32_t max_blocks, const uint32_t* list, const uint32_t* view_shade, SplatRec* recs,
-                          uint32_t* view_maxrad, cudaStream_t s);
+                          uint32_t* view_maxrad, int variant, cudaStream_t s);
 
 cudaError_t upload_iso_dirs(const float* dirs128x4, cudaStream_t s);
 cudaError_t launch_iso(const sl_gaussian* gs, sl_node* nodes, const sl_vgrid* vgrid, uint32_t count, cudaStream_t s);

@@ -298,6 +298,41 @@ def test_autotune_keeps_results(cuda):
                 _assert_view(B, k, v, [ra, rb][v.scene], tile)
 
 
+def test_block_size_variants_agree(cuda):
+    """Every block-size variant of bproject, btile_bin, bshade and bcomposite (the autotuner's choices) renders a lit
+    ragged batch identically, bit for bit; the autotuner's pick is one of them and is reported."""
+    a, b = _scenes()
+    b = scene.dataclasses.replace(b, shadow_res=256, sun_res=512)
+    with SplatRenderer(a.gaussians, a.parts) as ra, SplatRenderer(b.gaussians, b.parts) as rb:
+        La = for_scene(ra, a)
+        Lb = for_scene(rb, b)
+        La.update(a.eye, camera_forward(a))
+        Lb.update(b.eye, camera_forward(b))
+        views = [View(0, _frame(a, 200, 150, VIEW_LIT), a.eye),
+                 View(1, _frame(b, 320, 180, VIEW_LIT), b.eye),
+                 View(0, _frame(a, 64, 64, VIEW_OVERDRAW, eye=(0.2, 0.1, 3.0)), (0.2, 0.1, 3.0)),
+                 View(1, _frame(b, 160, 90, VIEW_LIT, eye=(3.0, -6.0, 4.0)), (3.0, -6.0, 4.0))]
+        choices = {"bproject": (4, 3), "btile_bin": (4, 5), "bshade": (4, 3, 5), "bcomposite": (6, 5)}
+        with BatchRenderer([ra, rb], [La, Lb]) as B:
+            base = {k: v[0] for k, v in choices.items()}
+            B.set_tuning(base)
+            ref = [x.copy() for x in B.render(views)]
+            for k, vals in choices.items():
+                for mb in vals[1:]:
+                    B.set_tuning(dict(base, **{k: mb}))
+                    assert B.tuning()[1][k] == mb
+                    for i, img in enumerate(B.render(views)):
+                        assert np.array_equal(img, ref[i]), (k, mb, i)
+            tile, _ = B.autotune(views, reps=1)
+            got = B.tuning()
+            assert got[0] == tile and all(got[1][k] in v for k, v in choices.items())
+            from splatlight_gb300._native import SplatlightError
+            with pytest.raises(SplatlightError):
+                B.set_tuning(dict(base, bshade=7))
+        La.close()
+        Lb.close()
+
+
 def test_bad_arguments(cuda):
     a, _ = _scenes()
     from splatlight_gb300._native import SplatlightError
