@@ -246,8 +246,8 @@ def run_serving(args, rates=(100, 500, 2000)):
            "seconds": {"500": args.serve_seconds, "100 and 2000": args.serve_seconds_other}, "rates": []}
     # the pending queue is bounded (512 requests, a few batches' worth): beyond it a request is refused at submit,
     # which keeps the latency of admitted requests bounded when arrivals outrun the device
-    srv = RenderServer(rs, ls, max_views=64, pipelines=2, max_slots=48 << 20, max_pixels=24 << 20,
-                       max_tiles=1 << 19, result_slots=96, max_pending=512)
+    srv = RenderServer(rs, ls, max_views=64, pipelines=2, max_slots=96 << 20, max_pixels=64 << 20,
+                       max_tiles=1 << 20, result_slots=192, max_pending=512)
     # warm-up: capture the graphs, size the entry buffers
     for k in range(16):
         q = request()
