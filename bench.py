@@ -246,8 +246,8 @@ def run_serving(args, rates=(100, 500, 2000)):
            "seconds": {"500": args.serve_seconds, "100 and 2000": args.serve_seconds_other}, "rates": []}
     # the pending queue is bounded (512 requests, a few batches' worth): beyond it a request is refused at submit,
     # which keeps the latency of admitted requests bounded when arrivals outrun the device
-    srv = RenderServer(rs, ls, max_views=64, pipelines=2, max_slots=96 << 20, max_pixels=64 << 20,
-                       max_tiles=1 << 20, result_slots=192, max_pending=512)
+    srv = RenderServer(rs, ls, max_views=64, pipelines=2, max_slots=48 << 20, max_pixels=24 << 20,
+                       max_tiles=1 << 19, result_slots=96, max_pending=512)
     # warm-up: capture the graphs, size the entry buffers
     for k in range(16):
         q = request()
@@ -651,6 +651,7 @@ def run_headline(args, stream, flush, dist, world, local):
     ms = max_over_ranks(sum(batch_ms) / len(batch_ms), dist, "cuda")
     st = B.last_stats
     stats = {k: getattr(st, k) for k in ("slots", "visible", "entries", "fragments", "shaded", "reshaded_views",
+                                         "max_radiance",
                                          "graph_replayed")}
 
     # per-stage device times (the same chain launched kernel by kernel with events between the stages)

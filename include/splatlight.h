@@ -366,7 +366,10 @@ typedef struct sl_batch_options {
   uint64_t max_entries;          /* tile entries of all views (0 = 2 per slot, grown on overflow) */
   uint32_t tile_w, tile_h;       /* 16x16 (default), 8x32 or 32x8 */
   uint32_t no_graph;             /* 1: launch the chain directly instead of replaying a graph */
-  uint32_t pad;
+  float radiance_allowance;      /* the coverage pass's allowance for shaded radiance (0 = 64): it marks the splats
+                                    blending before T falls below t_stop / max(2 r, allowance x max(1, light
+                                    scale)); a view whose shaded radiance exceeds half of that is re-run with every
+                                    blended splat shaded, so any allowance gives a correct image */
 } sl_batch_options;
 
 typedef struct sl_batch_stats {

@@ -39,7 +39,7 @@ class RenderOptions(C.Structure):
 class BatchOptions(C.Structure):
     _fields_ = [("max_views", C.c_uint32), ("max_tiles", C.c_uint32), ("max_slots", C.c_uint64),
                 ("max_entries", C.c_uint64), ("tile_w", C.c_uint32), ("tile_h", C.c_uint32),
-                ("no_graph", C.c_uint32), ("pad", C.c_uint32)]
+                ("no_graph", C.c_uint32), ("radiance_allowance", C.c_float)]
 
 
 class BatchStats(C.Structure):

@@ -22,7 +22,7 @@ class View:
 
 class BatchRenderer:
     def __init__(self, renderers, lightings=None, max_views: int = 64, tile=(16, 16), graph: bool = True,
-                 max_slots: int = 0, max_tiles: int = 0, max_entries: int = 0):
+                 max_slots: int = 0, max_tiles: int = 0, max_entries: int = 0, radiance_allowance: float = 0.0):
         self._lib = N.lib()
         self._renderers = list(renderers)
         self._lightings = list(lightings) if lightings is not None else None
@@ -31,7 +31,8 @@ class BatchRenderer:
         if self._lightings is not None:
             ls = (C.c_void_p * len(self._lightings))(*[(l.handle if l is not None else None)
                                                         for l in self._lightings])
-        o = N.BatchOptions(max_views, max_tiles, max_slots, max_entries, tile[0], tile[1], 0 if graph else 1, 0)
+        o = N.BatchOptions(max_views, max_tiles, max_slots, max_entries, tile[0], tile[1], 0 if graph else 1,
+                           float(radiance_allowance))
         h = C.c_void_p()
         N.check(self._lib.sl_batch_create(rs, ls, len(self._renderers), C.byref(o), C.byref(h)))
         self._h = h

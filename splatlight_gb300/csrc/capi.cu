@@ -5,7 +5,6 @@
 // with one synchronisation at the end (frame counters: visible, entries, overflow, timeout); the tile sort reads the
 // entry count on the device.  If the tile-entry capacity was too small the frame is re-run after growing it.
 #include <cstdio>
-#include <cmath>
 #include <cstring>
 #include <string>
 
@@ -300,27 +299,12 @@ void pack_project_params(const sl_render_frame* f, const std::vector<sl_part>& p
     float white[4] = {1.0f, 1.0f, 1.0f, 0.0f};
     memcpy(P.palette[m], src ? src : white, sizeof(float) * 4);
   }
-  // a 3x3 (rows r0, r1, r2 at stride `row` within m, columns at stride `col`) is orthonormal to 1e-4
-  auto ortho = [](const float* m, int row, int col) {
-    for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) {
-        double d = 0.0;
-        for (int k = 0; k < 3; k++) d += (double)m[k * row + i * col] * (double)m[k * row + j * col];
-        if (std::fabs(d - (i == j ? 1.0 : 0.0)) > 1e-4) return false;
-      }
-    return true;
-  };
-  // the view's columns (view[0..2], view[4..6], view[8..10]) and the focal lengths
-  P.cull = ortho(f->view, 1, 4) && f->lowpass_px2 >= 0.0f && f->focal[0] > 0.0f && f->focal[1] > 0.0f ? 1u : 0u;
-  P.cull_jx2 = f->focal[0] * f->focal[0] + (0.65f * f->viewport[0]) * (0.65f * f->viewport[0]);
-  P.cull_jy2 = f->focal[1] * f->focal[1] + (0.65f * f->viewport[1]) * (0.65f * f->viewport[1]);
   for (uint32_t p = 0; p < kMaxParts; p++) {
     PartXf& x = P.parts[p];
     if (p < parts.size()) {
       memcpy(x.xf, parts[p].xf, sizeof(x.xf));
       memcpy(x.xf_prev, parts[p].xf_prev, sizeof(x.xf_prev));
       x.flags = parts[p].flags;
-      x.ortho = ortho(parts[p].xf, 4, 1) ? 1u : 0u;  // xf rows [R row | t]
     } else {
       x.flags = kPartHidden;
     }

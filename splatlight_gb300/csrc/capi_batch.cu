@@ -267,7 +267,7 @@ void stage(sl_batch* b, const uint32_t* scene_of_view, const sl_render_frame* fr
     O.count_mode = frames[v].view_mode == 2u ? 1u : 0u;
     const sl_lighting* l = b->lights[scene_of_view[v]];
     O.lit = (frames[v].view_mode == 3u && l && l->iso_done) ? (b->shade_blended[v] ? 2u : 1u) : 0u;
-    O.rad_cap = kRadianceCap * std::max(1.0f, V.light_scale);
+    O.rad_cap = b->rad_allow * std::max(1.0f, V.light_scale);
     O.pad = 0;
     O.out_offset = b->offsets[v] / 4;
   }
@@ -528,6 +528,7 @@ int sl_batch_create(sl_renderer* const* renderers, sl_lighting* const* lightings
   b->tile_w = tw;
   b->tile_h = th;
   b->use_graph = !(opt && opt->no_graph);
+  if (opt && opt->radiance_allowance > 0.0f) b->rad_allow = opt->radiance_allowance;
   cudaError_t e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&b->ev[0]);
   if (e == cudaSuccess) e = cudaEventCreate(&b->ev[1]);

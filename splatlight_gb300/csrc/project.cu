@@ -138,33 +138,6 @@ __device__ __forceinline__ void project_slot(const ProjectParams& P, uint32_t i,
                V[2] * mu.x + V[6] * mu.y + V[10] * mu.z + V[14] * 1.0f);
     float depth = -tv.z;
     live = !(depth < P.near_plane || depth > P.far_plane);
-    // Early lateral cull, before the covariance: a bound on the splat's screen half-extent from its largest scale and
-    // opacity alone.  With the view, part and quaternion rotations orthonormal, tau0 <= kappa sqrt(2 pi) s_max keep
-    // (q >= 1 / s_max^2 and det0 <= det), the 2D covariance's trace a + c <= s_max^2 (jx2 + jy2) / depth^2 + 2
-    // low-pass (the Jacobian's rows, whose clamped x and y terms are at most 0.65 W and 0.65 H), and the extent the
-    // visibility test below uses, (|e0x| sqrt(l0) + |e1x| sqrt(l1)) r, is at most (2 sqrt(a + c) + 1e-3) sqrt(qcut).
-    // A slot whose centre lies farther off screen than that bound (1% and one pixel of margin) fails that test, so
-    // it is dropped here with the same outcome.  Emitter slots, tree nodes, moving parts and scales that are not
-    // positive go the full way.
-    if (live && P.cull && part != 0xFFFFFFFFu && node == 0xFFFFFFFFu && P.parts[part].ortho &&
-        vel.x == 0.0f && vel.y == 0.0f && vel.z == 0.0f && fminf(fminf(g2.x, g2.y), g2.z) > 0.0f) {
-      const float qn2 = g1.x * g1.x + g1.y * g1.y + g1.z * g1.z + g1.w * g1.w;
-      if (qn2 > 0.999f && qn2 < 1.001f) {
-        const float kTauMinC = 0.003929f;  // below -log(1 - 1/255) = 0.00392928
-        const float smax = fmaxf(fmaxf(g2.x, g2.y), g2.z);
-        const float tb = g0.w * 2.50662828f * smax * keep * 1.01f;
-        if (tb <= kTauMinC) {
-          live = false;
-        } else if (tb > kTauMinC) {
-          const float r2 = 2.0f * __logf(tb / kTauMinC) * 1.01f + 0.01f;
-          const float iz = 1.0f / depth;
-          const float A = smax * smax * iz * iz * (P.cull_jx2 + P.cull_jy2) * 1.01f + 2.0f * P.lowpass_px2;
-          const float ext = (2.0f * sqrtf(A) + 1e-3f) * sqrtf(r2) * 1.01f + 1.0f;
-          const float ax = fabsf(P.focal[0] * tv.x * iz), ay = fabsf(P.focal[1] * tv.y * iz);
-          if (ax - ext > 0.5f * P.viewport[0] + 1.0f || ay - ext > 0.5f * P.viewport[1] + 1.0f) live = false;
-        }
-      }
-    }
     if (live) {
       M3 rot;
       if (part == 0xFFFFFFFFu) {

@@ -15,6 +15,7 @@ struct sl_batch {
   uint32_t tile_w = 16, tile_h = 16;
   int variant[sl::kTuneKernels] = {0, 0, 0, 0};  // block-size variant of bproject, btile_bin, bshade, bcomposite
   float t_stop_scale = 1e-4f;
+  float rad_allow = sl::kRadianceCap;  // the coverage pass's radiance allowance (sl_batch_options)
   float entry_ratio = 0.0f;  // the most tile entries per slot a batch has had: the capacity class must hold the
                              // batch's slots times this (a class too small for the entries costs a second launch)
   bool use_graph = true;

@@ -28,7 +28,7 @@ struct PartXf {
   uint32_t flags;
   uint32_t material;
   float keep;  // 1 - clamp(part_fade)
-  uint32_t ortho;  // 1 when the part's rotation (xf's 3x3) is orthonormal to 1e-4: its Gaussians may be culled early
+  uint32_t pad;
 };
 
 // Everything project() reads from the RenderFrame, packed once per frame by the host (kernel parameter).
@@ -44,10 +44,6 @@ struct ProjectParams {
   uint32_t tile_w, tile_h, tiles_x, tiles_y;
   float palette[8][4];  // slots 0-7 (slot 3 = white, w 0)
   uint32_t lod_on, node_base, n_int, lod_pad;  // screen-space LOD (frame.lod): slots from node_base are tree nodes
-  // early lateral cull: 1 when the view's 3x3 is orthonormal (to 1e-4) and the low-pass term is not negative; then
-  // jx2 = fx^2 + (0.65 W)^2 and jy2 = fy^2 + (0.65 H)^2 bound the EWA Jacobian's rows times the depth
-  uint32_t cull;
-  float cull_jx2, cull_jy2, cull_pad;
   PartXf parts[kMaxParts];
 };
 
@@ -257,7 +253,8 @@ cudaError_t launch_btile_bin(const uint32_t* order, const ushort4* rects, const 
 // The batched coverage pass over the tiles of lit views, run between binning and shading: marks[slot] = 1 for each
 // splat that blends a fragment before the pixel's transmittance falls below t_mark (BatchViewOut::lit 1) or at all
 // (lit 2).  t_mark = t_stop_scale / max(2 r, rad_cap), r the view's radiance bound so far (its unshaded splats,
-// view_maxrad), rad_cap = kRadianceCap x max(1, light scale) (shaded radiance scales with the light intensities), is
+// view_maxrad), rad_cap = allowance x max(1, light scale) (shaded radiance scales with the light intensities;
+// the allowance is sl_batch_options.radiance_allowance, kRadianceCap by default), is
 // written to view_tmark[view].  The composite, whose threshold is t_stop_scale / (the bound after
 // shading), blends only marked splats as long as that threshold stays >= 2 t_mark.
 constexpr float kRadianceCap = 64.0f;
