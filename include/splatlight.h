@@ -261,6 +261,15 @@ SL_API int sl_lighting_set_environment(sl_lighting* l, const sl_env_light* light
 SL_API int sl_lighting_set_options(sl_lighting* l, uint32_t shadow_res, uint32_t sun_res, uint32_t mode, float theta,
                                    int asg);
 
+/* Motion blur for the lighting (src/lighting.js:468-507, runtime/wgsl/motion_blur.wgsl): with shutter > 0 (the
+ * reference's default is 0.5), every update rewrites copies of the records of the parts that moved this update or the
+ * last (moved_mask), each leaf of a moving part (sl_part.flags bit 1) stretched along its motion over the exposure,
+ * shutter x (xf - xf_prev): covariance C + d d^T / 12 centred mid-exposure, mass kept; the opacity-map splats (light
+ * map A and the sun maps) draw the copies, so a moving part casts a smeared shadow, while every receiver keeps its
+ * rest record.  This is the reference's ?blurcut=0 form (every record stretched); its default cut of the part's tree
+ * sized to the smear is not built.  0 (the default here) turns it off.  The maps re-splat at the next update. */
+SL_API int sl_lighting_set_blur(sl_lighting* l, float shutter);
+
 /* encode(encoder, eye, timers, changed, still) (src/lighting.js:1258-1274) + Environment.encodeDirect
  * (src/environment.js:181-189): iso_init on first use, the opacity maps of moved parts (moved_mask bit p) or of
  * every part after a light change, then shade_emit + env_direct into the radiance buffer the renderer reads.

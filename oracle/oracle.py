@@ -213,14 +213,15 @@ class LightSetup(C.Structure):
                 ("edge_soft", C.c_float), ("skip_part", C.c_uint32), ("shadow_res", C.c_uint32),
                 ("lights", C.c_void_p), ("n_lights", C.c_uint32), ("sun_res", C.c_uint32),
                 ("sky_ambient", C.c_float), ("eye", C.c_float * 3), ("fwd", C.c_float * 3),
-                ("shade_only", C.c_uint32)]
+                ("shade_only", C.c_uint32), ("blur_shutter", C.c_float)]
 
 
 def lighting(scene, eye=None, target=None, threads: int = 8, shadow_res=None, sun_res=None, mode: int = 1,
-             asg: bool = True, cached=None):
+             asg: bool = True, cached=None, blur_shutter: float = 0.0):
     """The restated lighting update on a splatlight_gb300.scene.Scene: returns (colour (G, 4), lamp_T (G,),
     env_T (G, 4), nodes with iso_norm).  Emitters are the scene's host emitter records.  cached: the (lamp_T,
-    env_T, nodes) of an earlier call -- then only the shading pass runs (the maps of a static scene hold)."""
+    env_T, nodes) of an earlier call -- then only the shading pass runs (the maps of a static scene hold).
+    blur_shutter > 0: the opacity maps draw moving parts (flags bit 1) stretched over the exposure."""
     L = lib()
     L.orc_lighting.restype = C.c_int
     L.orc_lighting.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -253,6 +254,7 @@ def lighting(scene, eye=None, target=None, threads: int = 8, shadow_res=None, su
     S.n_lights = n_l
     S.sun_res = scene.sun_res if sun_res is None else sun_res
     S.sky_ambient = scene.sky_ambient
+    S.blur_shutter = float(blur_shutter)
     S.eye[:] = eye.tolist()
     S.fwd[:] = fwd.tolist()
     g = np.ascontiguousarray(scene.gaussians)
@@ -284,6 +286,18 @@ def emitter_tree(rec: np.ndarray):
     cov = np.zeros(6, np.float32)
     root = L.orc_emitter_tree(r.ctypes.data, len(r), out.ctypes.data, cov.ctypes.data)
     return out, int(root), cov
+
+
+def blur_record(parts, shutter: float, gaussian, node):
+    """motion_blur.wgsl blur_records for one leaf: (Gaussian, node) stretched along its part's motion."""
+    from splatlight_gb300.structs import GAUSSIAN, NODE
+    p = np.ascontiguousarray(parts)
+    g = np.ascontiguousarray(np.asarray(gaussian, dtype=GAUSSIAN).reshape(1))
+    n = np.ascontiguousarray(np.asarray(node, dtype=NODE).reshape(1))
+    go, no = np.zeros(1, GAUSSIAN), np.zeros(1, NODE)
+    lib().orc_blur_record(p.ctypes.data, C.c_uint32(len(p)), C.c_float(shutter), g.ctypes.data, n.ctypes.data,
+                          go.ctypes.data, no.ctypes.data)
+    return go[0], no[0]
 
 
 def emitter_tree_d(rec: np.ndarray, le_scale=None):

@@ -10,6 +10,9 @@
  *   light map A     runtime/wgsl/light_shadow.wgsl:69-143, 191-392 (lsm_splat, lsm_resolve, lsm_down, lsm_lookup);
  *                   host src/light_shadow.js:89-140 (resolution, mip levels, light point and spread)
  *   sun maps        runtime/wgsl/sun_map.wgsl:91-324; host src/sun_map.js:23-159 (layer plan, cascades, margin)
+ *   motion blur     runtime/wgsl/motion_blur.wgsl:22-127 (blur_records: the records the map splats draw for a moving
+ *                   part, stretched over the exposure); lighting.js:468-507 (bound to the opacity-map splats only,
+ *                   the ?blurcut=0 form: every record stretched, its mass kept)
  *   shade_emit      runtime/wgsl/emissive.wgsl:123-150, 853-980 (M39 iso transfer, ASG specular on)
  *   env_direct      runtime/wgsl/environment.wgsl:207-308 (env_add)
  *   materials       runtime/wgsl/material_ext.wgsl:27-181; common.wgsl:113-254 (erfc, sym_mul, dirm, vgrid, ein,
@@ -678,6 +681,154 @@ static m2f oct_jac(const lframe* L, f3 w, f3 b0, f3 b1) {
   return J;
 }
 static f3 part_rot_col(const float* xf, int c) { return F3(xf[c], xf[4 + c], xf[8 + c]); }
+/* ---- motion_blur.wgsl blur_records (:80-127) ------------------------------------------------------------------ */
+
+static float m3_at(const m3f* m, int col, int row) {
+  const f3* c = &m->c[col];
+  return row == 0 ? c->x : (row == 1 ? c->y : c->z);
+}
+static void m3_set(m3f* m, int col, int row, float v) {
+  f3* c = &m->c[col];
+  if (row == 0) c->x = v; else if (row == 1) c->y = v; else c->z = v;
+}
+static m3f m3_identity(void) { return m3_diag(F3(1.0f, 1.0f, 1.0f)); }
+
+/* cyclic Jacobi (8 sweeps over the pairs (0,1) (0,2) (1,2)): the columns of V are eigenvectors, the result the
+ * eigenvalues (motion_blur.wgsl:37-60) */
+static f3 blur_eig3(m3f A, m3f* V) {
+  m3f Q = m3_identity();
+  for (int sweep = 0; sweep < 8; sweep++)
+    for (int k = 0; k < 3; k++) {
+      const int pp = k == 2 ? 1 : 0, q = k == 2 ? 2 : k + 1;
+      const float apq = m3_at(&A, q, pp);
+      if (fabsf(apq) < 1e-30f) continue;
+      const float theta = 0.5f * (m3_at(&A, q, q) - m3_at(&A, pp, pp)) / apq;
+      const float sg = theta + (theta == 0.0f ? 1e-30f : 0.0f);
+      const float sgn = sg > 0.0f ? 1.0f : (sg < 0.0f ? -1.0f : 0.0f);
+      const float t = sgn / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+      const float c = 1.0f / sqrtf(t * t + 1.0f);
+      const float sn = t * c;
+      m3f J = m3_identity();
+      m3_set(&J, pp, pp, c);
+      m3_set(&J, q, q, c);
+      m3_set(&J, q, pp, sn);
+      m3_set(&J, pp, q, -sn);
+      m3f Jt = m3_t(&J);
+      m3f T1 = m3_mul(&Jt, &A);
+      A = m3_mul(&T1, &J);
+      Q = m3_mul(&Q, &J);
+    }
+  *V = Q;
+  return F3(A.c[0].x, A.c[1].y, A.c[2].z);
+}
+
+/* column-major rotation -> quaternion (x, y, z, w), normalised (motion_blur.wgsl:62-78) */
+static void blur_mat_to_quat(const m3f* m, float* q4) {
+  const float m00 = m3_at(m, 0, 0), m11 = m3_at(m, 1, 1), m22 = m3_at(m, 2, 2);
+  const float tr = m00 + m11 + m22;
+  float q[4];
+  if (tr > 0.0f) {
+    const float s = sqrtf(tr + 1.0f) * 2.0f;
+    q[0] = (m3_at(m, 1, 2) - m3_at(m, 2, 1)) / s;
+    q[1] = (m3_at(m, 2, 0) - m3_at(m, 0, 2)) / s;
+    q[2] = (m3_at(m, 0, 1) - m3_at(m, 1, 0)) / s;
+    q[3] = 0.25f * s;
+  } else if (m00 > m11 && m00 > m22) {
+    const float s = sqrtf(1.0f + m00 - m11 - m22) * 2.0f;
+    q[0] = 0.25f * s;
+    q[1] = (m3_at(m, 1, 0) + m3_at(m, 0, 1)) / s;
+    q[2] = (m3_at(m, 2, 0) + m3_at(m, 0, 2)) / s;
+    q[3] = (m3_at(m, 1, 2) - m3_at(m, 2, 1)) / s;
+  } else if (m11 > m22) {
+    const float s = sqrtf(1.0f + m11 - m00 - m22) * 2.0f;
+    q[0] = (m3_at(m, 1, 0) + m3_at(m, 0, 1)) / s;
+    q[1] = 0.25f * s;
+    q[2] = (m3_at(m, 2, 1) + m3_at(m, 1, 2)) / s;
+    q[3] = (m3_at(m, 2, 0) - m3_at(m, 0, 2)) / s;
+  } else {
+    const float s = sqrtf(1.0f + m22 - m00 - m11) * 2.0f;
+    q[0] = (m3_at(m, 2, 0) + m3_at(m, 0, 2)) / s;
+    q[1] = (m3_at(m, 2, 1) + m3_at(m, 1, 2)) / s;
+    q[2] = 0.25f * s;
+    q[3] = (m3_at(m, 0, 1) - m3_at(m, 1, 0)) / s;
+  }
+  const float l = sqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  for (int k = 0; k < 4; k++) q4[k] = q[k] / l;
+}
+
+void orc_blur_record(const sl_part* parts, uint32_t part_count, float shutter, const sl_gaussian* g_in,
+                     const sl_node* n_in, sl_gaussian* g_out, sl_node* n_out) {
+  sl_node nd = *n_in;
+  sl_gaussian G = *g_in;
+  /* blur_disp: the rest-frame displacement of the node's mean over the exposure */
+  f3 d = F3(0.0f, 0.0f, 0.0f);
+  const uint32_t p = nd.part;
+  if (shutter > 0.0f && p < part_count && (parts[p].flags & 2u) != 0u) {
+    const f3 x = F3(nd.mean[0], nd.mean[1], nd.mean[2]);
+    const f3 a = xf_point(parts[p].xf, x), b = xf_point(parts[p].xf_prev, x);
+    d = xf_dir_inv(parts[p].xf, F3(shutter * (a.x - b.x), shutter * (a.y - b.y), shutter * (a.z - b.z)));
+  }
+  const float dd = dot3(d, d);
+  if (dd > 0.0f) {
+    /* Sherman-Morrison: (C + d d^T / 12)^-1 from C^-1 */
+    m3f Ci;
+    Ci.c[0] = F3(nd.cinv_diag[0], nd.cinv_off[0], nd.cinv_off[1]);
+    Ci.c[1] = F3(nd.cinv_off[0], nd.cinv_diag[1], nd.cinv_off[2]);
+    Ci.c[2] = F3(nd.cinv_off[1], nd.cinv_off[2], nd.cinv_diag[2]);
+    const f3 cd = m3_mulv(&Ci, d);
+    const float m = dot3(d, cd);
+    const float inv = 1.0f / (12.0f + m);
+    const float cdv[3] = {cd.x, cd.y, cd.z};
+    m3f Cn;
+    for (int j = 0; j < 3; j++)
+      for (int i = 0; i < 3; i++) m3_set(&Cn, j, i, m3_at(&Ci, j, i) - (cdv[i] * cdv[j]) * inv);
+    nd.mean[0] = nd.mean[0] - 0.5f * d.x;
+    nd.mean[1] = nd.mean[1] - 0.5f * d.y;
+    nd.mean[2] = nd.mean[2] - 0.5f * d.z;
+    nd.cinv_diag[0] = m3_at(&Cn, 0, 0);
+    nd.cinv_diag[1] = m3_at(&Cn, 1, 1);
+    nd.cinv_diag[2] = m3_at(&Cn, 2, 2);
+    nd.cinv_off[0] = m3_at(&Cn, 0, 1);
+    nd.cinv_off[1] = m3_at(&Cn, 0, 2);
+    nd.cinv_off[2] = m3_at(&Cn, 1, 2);
+    nd.kappa = nd.kappa / sqrtf(1.0f + m / 12.0f);
+    nd.smax = sqrtf(nd.smax * nd.smax + dd / 12.0f);
+    nd.radius = sqrtf(nd.radius * nd.radius + 0.75f * dd);
+    /* the Gaussian: the stretched covariance's eigen-frame, ascending, right-handed */
+    m3f Rq = quat_matrix(G.quat);
+    const f3 s2 = F3(G.scale[0] * G.scale[0], G.scale[1] * G.scale[1], G.scale[2] * G.scale[2]);
+    m3f D = m3_diag(s2);
+    m3f T1 = m3_mul(&Rq, &D);
+    m3f RqT = m3_t(&Rq);
+    m3f C = m3_mul(&T1, &RqT);
+    const float dv[3] = {d.x, d.y, d.z};
+    const float k12 = 1.0f / 12.0f;
+    for (int j = 0; j < 3; j++)
+      for (int i = 0; i < 3; i++) m3_set(&C, j, i, m3_at(&C, j, i) + (dv[i] * dv[j]) * k12);
+    m3f V;
+    f3 ev = blur_eig3(C, &V);
+    f3 c0 = V.c[0], c1 = V.c[1], c2 = V.c[2];
+    if (ev.x > ev.y) { ev = F3(ev.y, ev.x, ev.z); f3 t = c0; c0 = c1; c1 = t; }
+    if (ev.y > ev.z) { ev = F3(ev.x, ev.z, ev.y); f3 t = c1; c1 = c2; c2 = t; }
+    if (ev.x > ev.y) { ev = F3(ev.y, ev.x, ev.z); f3 t = c0; c0 = c1; c1 = t; }
+    c2 = cross3(c0, c1);
+    G.mu[0] = G.mu[0] - 0.5f * d.x;
+    G.mu[1] = G.mu[1] - 0.5f * d.y;
+    G.mu[2] = G.mu[2] - 0.5f * d.z;
+    G.kappa = nd.kappa;
+    G.scale[0] = sqrtf(fmaxf(ev.x, 1e-12f));
+    G.scale[1] = sqrtf(fmaxf(ev.y, 1e-12f));
+    G.scale[2] = sqrtf(fmaxf(ev.z, 1e-12f));
+    m3f R;
+    R.c[0] = c0;
+    R.c[1] = c1;
+    R.c[2] = c2;
+    blur_mat_to_quat(&R, G.quat);
+  }
+  *n_out = nd;
+  *g_out = G;
+}
+
 /* world covariance R C R^T of a leaf (light_shadow.wgsl:125-137) */
 static m3f leaf_cov_world(const sl_gaussian* G, const float* xf) {
   m3f R;
@@ -854,6 +1005,21 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
     root = orc_emitter_tree(S->emit_rec, n_emit, tree, root_cov);
   }
 
+  /* motion blur for the lighting (motion_blur.wgsl, lighting.js:468-507): the opacity-map splats draw every record of
+   * a moving part stretched over the exposure; the receivers (lookups, shading) keep their rest records */
+  const sl_gaussian* gsp = gs;
+  const sl_node* ndp = nodes;
+  sl_gaussian* g_blur = NULL;
+  sl_node* n_blur = NULL;
+  if (S->blur_shutter > 0.0f && !S->shade_only) {
+    g_blur = (sl_gaussian*)malloc(sizeof(sl_gaussian) * (count ? count : 1u));
+    n_blur = (sl_node*)malloc(sizeof(sl_node) * (count ? count : 1u));
+    for (uint32_t g = 0; g < count; g++)
+      orc_blur_record(parts, part_count, S->blur_shutter, &gs[g], &nodes[g], &g_blur[g], &n_blur[g]);
+    gsp = g_blur;
+    ndp = n_blur;
+  }
+
   /* light map A (light_shadow.js:89-165): all layers dirty, then the lookup */
   if (!S->shade_only)
     for (uint32_t g = 0; g < count; g++) lamp_T[g] = 1.0f;
@@ -885,9 +1051,9 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 256)
 #endif
     for (int64_t g = 0; g < (int64_t)count; g++) {
-      uint32_t p = gs[g].part_surface & 0xFFFFu;
+      uint32_t p = gsp[g].part_surface & 0xFFFFu;
       if (p >= part_count || p == S->skip_part) continue;
-      lsm_splat_one(&L, res, (uint32_t)g, p, gs, nodes, parts, acc);
+      lsm_splat_one(&L, res, (uint32_t)g, p, gsp, ndp, parts, acc);
     }
     for (uint32_t p = 0; p < part_count; p++) {
       resolve_layer(acc + (size_t)p * res * res * 3u, 65536.0f, res * res, mip + (size_t)p * layer_texels);
@@ -1021,17 +1187,17 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
 #endif
     for (int64_t gi = 0; gi < (int64_t)count; gi++) {
       uint32_t g = (uint32_t)gi;
-      uint32_t p = gs[g].part_surface & 0xFFFFu;
+      uint32_t p = gsp[g].part_surface & 0xFFFFu;
       if (p >= Pn) continue;
       for (uint32_t l = 0; l < nl; l++) {
         if (ly[l].part != p || !(S->lights[ly[l].light].shadows)) continue;
         /* sm_splat_one (sun_map.wgsl:155-219) */
         const float* xf = parts[p].xf;
-        const sl_node* nd = &nodes[g];
-        f3 x = xf_point(xf, F3(gs[g].mu[0], gs[g].mu[1], gs[g].mu[2]));
+        const sl_node* nd = &ndp[g];
+        f3 x = xf_point(xf, F3(gsp[g].mu[0], gsp[g].mu[1], gsp[g].mu[2]));
         f3 w = F3(S->lights[ly[l].light].dir[0], S->lights[ly[l].light].dir[1], S->lights[ly[l].light].dir[2]);
         f3 b0 = ly[l].t1, b1 = ly[l].t2;
-        m3f C = leaf_cov_world(&gs[g], xf);
+        m3f C = leaf_cov_world(&gsp[g], xf);
         f3 c0 = m3_mulv(&C, b0), c1 = m3_mulv(&C, b1), cw = m3_mulv(&C, w);
         m2f Cbb;
         Cbb.c[0] = F2(dot3(b0, c0), dot3(b1, c0));
@@ -1260,5 +1426,7 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
     colour[4u * g + 3] = 1.0f;
   }
   free(tree);
+  free(g_blur);
+  free(n_blur);
   return 0;
 }

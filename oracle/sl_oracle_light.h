@@ -40,7 +40,14 @@ typedef struct orc_light_setup {
   float eye[3];
   float fwd[3];       /* camera forward, for the sun cascades */
   uint32_t shade_only;/* 1: nodes (iso_norm), lamp_T and env_T are inputs from an earlier call; only shade */
+  float blur_shutter; /* > 0: the opacity-map splats draw moving parts' records stretched over the exposure
+                         (motion_blur.wgsl blur_records; every part with flags bit 1 moves) */
 } orc_light_setup;
+
+/* motion_blur.wgsl blur_records (:80-127) for one leaf: its Gaussian and node stretched along its part's motion over
+ * the exposure (shutter x (xf - xf_prev)), mass kept; unchanged for a part that does not move (flags bit 1). */
+void orc_blur_record(const sl_part* parts, uint32_t part_count, float shutter, const sl_gaussian* g_in,
+                     const sl_node* n_in, sl_gaussian* g_out, sl_node* n_out);
 
 /* The 128 iso_init cell directions and solid angles (iso_init.wgsl:39-45), 4 floats each, computed in float64. */
 void orc_iso_dirs(float* dirs);

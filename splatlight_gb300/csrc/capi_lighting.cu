@@ -484,7 +484,8 @@ int sl_lighting_destroy(sl_lighting* l) {
     l->r->colour = nullptr;
   }
   sl::DevBuf* all[] = {&l->nodes, &l->vgrid, &l->materials, &l->parts, &l->tree, &l->lamp_T, &l->env_T, &l->colour,
-                       &l->lm_acc, &l->lm_mip, &l->sm_acc, &l->sm_mip, &l->sm_layers, &l->sm_dirty, &l->order};
+                       &l->lm_acc, &l->lm_mip, &l->sm_acc, &l->sm_mip, &l->sm_layers, &l->sm_dirty, &l->order,
+                       &l->g_blur, &l->n_blur};
   for (sl::DevBuf* b : all) b->release();
   delete l;
   return SL_OK;
@@ -567,6 +568,19 @@ int sl_lighting_set_options(sl_lighting* l, uint32_t shadow_res, uint32_t sun_re
   return SL_OK;
 }
 
+int sl_lighting_set_blur(sl_lighting* l, float shutter) {
+  if (!l) return fail(SL_ERR_INVALID_ARG, "null lighting");
+  if (!(shutter >= 0.0f && shutter <= 1.0f)) return fail(SL_ERR_INVALID_ARG, "shutter outside [0, 1]");
+  if (shutter != l->blur_shutter) {
+    l->blur_shutter = shutter;
+    l->blur_init = false;
+    l->blur_prev = 0;
+    l->lm_dirty = true;
+    l->sm_dirty_all = true;
+  }
+  return SL_OK;
+}
+
 int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, uint32_t moved_mask, void* stream) {
   if (!l || !eye) return fail(SL_ERR_INVALID_ARG, "null argument");
   cudaSetDevice(l->device);
@@ -585,9 +599,38 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
     l->iso_done = true;
   }
 
+  // motion blur: the copies the map splats draw, rewritten for the parts that moved now or in the last update
+  // (lighting.js encodeBlur); every part on the first update after blur was switched on
+  const sl_gaussian* gsp = gs;
+  const sl_node* ndp = l->nodes.as<sl_node>();
+  uint32_t blur_mask = 0;
+  if (l->blur_shutter > 0.0f) {
+    SL_CHECK_CUDA(l->g_blur.ensure(sizeof(sl_gaussian) * (size_t)G), "blur copies");
+    SL_CHECK_CUDA(l->n_blur.ensure(sizeof(sl_node) * (size_t)G), "blur copies");
+    const uint32_t all = P >= 32 ? 0xFFFFFFFFu : ((1u << P) - 1u);
+    if (!l->blur_init) {
+      SL_CHECK_CUDA(cudaMemcpyAsync(l->g_blur.ptr, gs, sizeof(sl_gaussian) * (size_t)G, cudaMemcpyDeviceToDevice, s),
+                    "blur copies");
+      SL_CHECK_CUDA(cudaMemcpyAsync(l->n_blur.ptr, l->nodes.ptr, sizeof(sl_node) * (size_t)G, cudaMemcpyDeviceToDevice,
+                                    s),
+                    "blur copies");
+      blur_mask = all;
+      l->blur_init = true;
+    } else {
+      blur_mask = (moved_mask | l->blur_prev) & all;
+    }
+    l->blur_prev = moved_mask;
+    SL_CHECK_CUDA(launch_blur_records(parts, P, l->blur_shutter, blur_mask, gs, l->nodes.as<sl_node>(),
+                                      l->g_blur.as<sl_gaussian>(), l->n_blur.as<sl_node>(), G, s),
+                  "blur_records");
+    gsp = l->g_blur.as<sl_gaussian>();
+    ndp = l->n_blur.as<sl_node>();
+  }
+  const uint32_t resplat = moved_mask | blur_mask;
+
   // light map A (light_shadow.js:113-165): re-splat every layer when the light changed, else the moved parts'
   const bool lmap = l->n_emit && l->shadow_res;
-  if (lmap && (l->lm_dirty || moved_mask)) {
+  if (lmap && (l->lm_dirty || resplat)) {
     LightMapParams& L = l->LP;
     memset(&L, 0, sizeof(L));
     const float* t = reinterpret_cast<const float*>(l->tree.ptr);
@@ -617,14 +660,14 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
     levels_for(L.res, L.levels, L.level_off, L.layer_texels);
     L.part_count = P;
     L.skip_part = l->skip_part;
-    L.dirty = l->lm_dirty ? (P >= 32 ? 0xFFFFFFFFu : ((1u << P) - 1u)) : moved_mask;
+    L.dirty = l->lm_dirty ? (P >= 32 ? 0xFFFFFFFFu : ((1u << P) - 1u)) : resplat;
     const size_t acc_layer = 12ull * L.res * L.res;
     SL_CHECK_CUDA(l->lm_acc.ensure(acc_layer * P), "light map");
     SL_CHECK_CUDA(l->lm_mip.ensure(16ull * L.layer_texels * P), "light map mips");
     for (uint32_t p = 0; p < P; p++)
       if ((L.dirty >> p) & 1u)
         SL_CHECK_CUDA(cudaMemsetAsync(l->lm_acc.as<char>() + acc_layer * p, 0, acc_layer, s), "clear light map");
-    SL_CHECK_CUDA(launch_lsm_splat(L, gs, l->nodes.as<sl_node>(), parts, G, l->lm_acc.as<uint32_t>(), s), "lsm_splat");
+    SL_CHECK_CUDA(launch_lsm_splat(L, gsp, ndp, parts, G, l->lm_acc.as<uint32_t>(), s), "lsm_splat");
     SL_CHECK_CUDA(launch_resolve(l->lm_acc.as<uint32_t>(), 65536.0f, L.res * L.res, P, L.layer_texels, nullptr,
                                  l->lm_mip.as<float4>(), s),
                   "lsm_resolve");
@@ -720,7 +763,7 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
       volatile float cx = xf[0] * b[0] + xf[1] * b[1] + xf[2] * b[2] + xf[3];
       volatile float cy = xf[4] * b[0] + xf[5] * b[1] + xf[6] * b[2] + xf[7];
       volatile float cz = xf[8] * b[0] + xf[9] * b[1] + xf[10] * b[2] + xf[11];
-      bool dirty = l->sm_dirty_all || ((moved_mask >> ly.part) & 1u);
+      bool dirty = l->sm_dirty_all || ((resplat >> ly.part) & 1u);
       if (ly.kind == 1u) {
         const SunLayer& old = l->layers[li];
         const float h = ly.half;
@@ -760,8 +803,7 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
       SL_CHECK_CUDA(cudaMemcpyAsync(l->sm_layers.ptr, plan.data(), sizeof(SunLayer) * nl, cudaMemcpyHostToDevice, s),
                     "sun layers");
       SL_CHECK_CUDA(cudaMemcpyAsync(l->sm_dirty.ptr, dl.data(), 4 * nl, cudaMemcpyHostToDevice, s), "sun dirty");
-      SL_CHECK_CUDA(launch_sm_splat(SP, l->sm_layers.as<SunLayer>(), gs, l->nodes.as<sl_node>(), parts, G,
-                                    l->sm_acc.as<uint32_t>(), s),
+      SL_CHECK_CUDA(launch_sm_splat(SP, l->sm_layers.as<SunLayer>(), gsp, ndp, parts, G, l->sm_acc.as<uint32_t>(), s),
                     "sm_splat");
       SL_CHECK_CUDA(launch_resolve(l->sm_acc.as<uint32_t>(), 4096.0f, SP.res * SP.res, (uint32_t)nl, SP.layer_texels,
                                    l->sm_dirty.as<uint32_t>(), l->sm_mip.as<float4>(), s),

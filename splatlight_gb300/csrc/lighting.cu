@@ -7,6 +7,7 @@
 //   lsm_splat_kernel  runtime/wgsl/light_shadow.wgsl:191-286     lsm_lookup_kernel  :347-392
 //   sm_splat_kernel   runtime/wgsl/sun_map.wgsl:127-219          sm_lookup_kernel   :287-324
 //   resolve / down    light_shadow.wgsl:290-321, sun_map.wgsl:228-258
+//   blur_records_kernel  runtime/wgsl/motion_blur.wgsl:22-127 (the records the map splats draw for a moving part)
 // The shading pass lives in shade.cu.  Compiled with --fmad=false (see light_math.cuh): the opacity maps' mip-level
 // selection (ceil of a log2) is discontinuous, so these kernels reproduce the CPU restatement's arithmetic exactly.
 #include "light_math.cuh"
@@ -456,6 +457,163 @@ __global__ void __launch_bounds__(kThreads) sm_lookup_kernel(const __grid_consta
   env_T[g] = make_float4(T[0], T[1], T[2], T[3]);
 }
 
+// ---- motion_blur.wgsl blur_records: the records the opacity-map splats draw, stretched along a moving part's motion
+// over the exposure (the box-shutter average: covariance C + d d^T / 12 centred mid-exposure, mass kept) --------------
+
+__device__ __forceinline__ float m3_at(const m3& m, int col, int row) {
+  const f3& c = m.c[col];
+  return row == 0 ? c.x : (row == 1 ? c.y : c.z);
+}
+__device__ __forceinline__ void m3_set(m3& m, int col, int row, float v) {
+  f3& c = m.c[col];
+  if (row == 0) c.x = v; else if (row == 1) c.y = v; else c.z = v;
+}
+
+// cyclic Jacobi, 8 sweeps over the pairs (0,1) (0,2) (1,2) (motion_blur.wgsl:37-60): eigenvectors in V's columns
+__device__ f3 blur_eig3(m3 A, m3& V) {
+  m3 Q = m3diag(F3(1.0f, 1.0f, 1.0f));
+  for (int sweep = 0; sweep < 8; sweep++)
+    for (int k = 0; k < 3; k++) {
+      const int pp = k == 2 ? 1 : 0, q = k == 2 ? 2 : k + 1;
+      const float apq = m3_at(A, q, pp);
+      if (fabsf(apq) < 1e-30f) continue;
+      const float theta = 0.5f * (m3_at(A, q, q) - m3_at(A, pp, pp)) / apq;
+      const float sg = theta + (theta == 0.0f ? 1e-30f : 0.0f);
+      const float sgn = sg > 0.0f ? 1.0f : (sg < 0.0f ? -1.0f : 0.0f);
+      const float t = sgn / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+      const float c = 1.0f / sqrtf(t * t + 1.0f);
+      const float sn = t * c;
+      m3 J = m3diag(F3(1.0f, 1.0f, 1.0f));
+      m3_set(J, pp, pp, c);
+      m3_set(J, q, q, c);
+      m3_set(J, q, pp, sn);
+      m3_set(J, pp, q, -sn);
+      A = m3m(m3m(m3t(J), A), J);
+      Q = m3m(Q, J);
+    }
+  V = Q;
+  return F3(A.c[0].x, A.c[1].y, A.c[2].z);
+}
+
+// column-major rotation -> normalised quaternion (x, y, z, w) (motion_blur.wgsl:62-78)
+__device__ float4 blur_mat_to_quat(const m3& m) {
+  const float m00 = m3_at(m, 0, 0), m11 = m3_at(m, 1, 1), m22 = m3_at(m, 2, 2);
+  const float tr = m00 + m11 + m22;
+  float q0, q1, q2, q3;
+  if (tr > 0.0f) {
+    const float s = sqrtf(tr + 1.0f) * 2.0f;
+    q0 = (m3_at(m, 1, 2) - m3_at(m, 2, 1)) / s;
+    q1 = (m3_at(m, 2, 0) - m3_at(m, 0, 2)) / s;
+    q2 = (m3_at(m, 0, 1) - m3_at(m, 1, 0)) / s;
+    q3 = 0.25f * s;
+  } else if (m00 > m11 && m00 > m22) {
+    const float s = sqrtf(1.0f + m00 - m11 - m22) * 2.0f;
+    q0 = 0.25f * s;
+    q1 = (m3_at(m, 1, 0) + m3_at(m, 0, 1)) / s;
+    q2 = (m3_at(m, 2, 0) + m3_at(m, 0, 2)) / s;
+    q3 = (m3_at(m, 1, 2) - m3_at(m, 2, 1)) / s;
+  } else if (m11 > m22) {
+    const float s = sqrtf(1.0f + m11 - m00 - m22) * 2.0f;
+    q0 = (m3_at(m, 1, 0) + m3_at(m, 0, 1)) / s;
+    q1 = 0.25f * s;
+    q2 = (m3_at(m, 2, 1) + m3_at(m, 1, 2)) / s;
+    q3 = (m3_at(m, 2, 0) - m3_at(m, 0, 2)) / s;
+  } else {
+    const float s = sqrtf(1.0f + m22 - m00 - m11) * 2.0f;
+    q0 = (m3_at(m, 2, 0) + m3_at(m, 0, 2)) / s;
+    q1 = (m3_at(m, 2, 1) + m3_at(m, 1, 2)) / s;
+    q2 = 0.25f * s;
+    q3 = (m3_at(m, 0, 1) - m3_at(m, 1, 0)) / s;
+  }
+  const float l = sqrtf(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
+  return make_float4(q0 / l, q1 / l, q2 / l, q3 / l);
+}
+
+// One thread per leaf of a part in `mask` (the parts that moved this frame or the last): its copy rewritten,
+// stretched when the part moves (flags bit 1) and the shutter is open, else back to its rest record.
+__global__ void __launch_bounds__(kThreads) blur_records_kernel(const sl_part* __restrict__ parts, uint32_t part_count,
+                                                                float shutter, uint32_t mask,
+                                                                const sl_gaussian* __restrict__ g_src,
+                                                                const sl_node* __restrict__ n_src,
+                                                                sl_gaussian* __restrict__ g_dst,
+                                                                sl_node* __restrict__ n_dst, uint32_t count) {
+  const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= count) return;
+  sl_node nd = n_src[i];
+  const uint32_t p = nd.part;
+  if (p >= 32u || ((mask >> p) & 1u) == 0u) return;
+  sl_gaussian G = g_src[i];
+  f3 d = F3(0.0f, 0.0f, 0.0f);
+  if (shutter > 0.0f && p < part_count && (parts[p].flags & 2u) != 0u) {
+    const f3 x = F3(nd.mean[0], nd.mean[1], nd.mean[2]);
+    const f3 a = xf_point(parts[p].xf, x), b = xf_point(parts[p].xf_prev, x);
+    d = xf_dir_inv(parts[p].xf, F3(shutter * (a.x - b.x), shutter * (a.y - b.y), shutter * (a.z - b.z)));
+  }
+  const float dd = dot3(d, d);
+  if (dd > 0.0f) {
+    m3 Ci;  // the node's C^-1; Sherman-Morrison gives (C + d d^T / 12)^-1
+    Ci.c[0] = F3(nd.cinv_diag[0], nd.cinv_off[0], nd.cinv_off[1]);
+    Ci.c[1] = F3(nd.cinv_off[0], nd.cinv_diag[1], nd.cinv_off[2]);
+    Ci.c[2] = F3(nd.cinv_off[1], nd.cinv_off[2], nd.cinv_diag[2]);
+    const f3 cd = m3v(Ci, d);
+    const float m = dot3(d, cd);
+    const float inv = 1.0f / (12.0f + m);
+    const float cdv[3] = {cd.x, cd.y, cd.z};
+    m3 Cn;
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int r = 0; r < 3; r++) m3_set(Cn, j, r, m3_at(Ci, j, r) - (cdv[r] * cdv[j]) * inv);
+    nd.mean[0] = nd.mean[0] - 0.5f * d.x;
+    nd.mean[1] = nd.mean[1] - 0.5f * d.y;
+    nd.mean[2] = nd.mean[2] - 0.5f * d.z;
+    nd.cinv_diag[0] = m3_at(Cn, 0, 0);
+    nd.cinv_diag[1] = m3_at(Cn, 1, 1);
+    nd.cinv_diag[2] = m3_at(Cn, 2, 2);
+    nd.cinv_off[0] = m3_at(Cn, 0, 1);
+    nd.cinv_off[1] = m3_at(Cn, 0, 2);
+    nd.cinv_off[2] = m3_at(Cn, 1, 2);
+    nd.kappa = nd.kappa / sqrtf(1.0f + m / 12.0f);
+    nd.smax = sqrtf(nd.smax * nd.smax + dd / 12.0f);
+    nd.radius = sqrtf(nd.radius * nd.radius + 0.75f * dd);
+    // the Gaussian: the stretched covariance's eigen-frame, scales ascending, right-handed
+    const m3 Rq = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]);
+    const f3 s2 = F3(G.scale[0] * G.scale[0], G.scale[1] * G.scale[1], G.scale[2] * G.scale[2]);
+    m3 C = m3m(m3m(Rq, m3diag(s2)), m3t(Rq));
+    const float dv[3] = {d.x, d.y, d.z};
+    const float k12 = 1.0f / 12.0f;
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int r = 0; r < 3; r++) m3_set(C, j, r, m3_at(C, j, r) + (dv[r] * dv[j]) * k12);
+    m3 V;
+    f3 ev = blur_eig3(C, V);
+    f3 c0 = V.c[0], c1 = V.c[1], c2 = V.c[2];
+    if (ev.x > ev.y) { ev = F3(ev.y, ev.x, ev.z); const f3 t = c0; c0 = c1; c1 = t; }
+    if (ev.y > ev.z) { ev = F3(ev.x, ev.z, ev.y); const f3 t = c1; c1 = c2; c2 = t; }
+    if (ev.x > ev.y) { ev = F3(ev.y, ev.x, ev.z); const f3 t = c0; c0 = c1; c1 = t; }
+    c2 = cross3(c0, c1);
+    G.mu[0] = G.mu[0] - 0.5f * d.x;
+    G.mu[1] = G.mu[1] - 0.5f * d.y;
+    G.mu[2] = G.mu[2] - 0.5f * d.z;
+    G.kappa = nd.kappa;
+    G.scale[0] = sqrtf(fmaxf(ev.x, 1e-12f));
+    G.scale[1] = sqrtf(fmaxf(ev.y, 1e-12f));
+    G.scale[2] = sqrtf(fmaxf(ev.z, 1e-12f));
+    m3 R;
+    R.c[0] = c0;
+    R.c[1] = c1;
+    R.c[2] = c2;
+    const float4 q = blur_mat_to_quat(R);
+    G.quat[0] = q.x;
+    G.quat[1] = q.y;
+    G.quat[2] = q.z;
+    G.quat[3] = q.w;
+  }
+  n_dst[i] = nd;
+  g_dst[i] = G;
+}
+
 }  // namespace
 
 cudaError_t upload_iso_dirs(const float* dirs128x4, cudaStream_t s) {
@@ -467,6 +625,15 @@ static uint32_t blocks_for(uint64_t n) { return (uint32_t)((n + kThreads - 1) / 
 cudaError_t launch_iso(const sl_gaussian* gs, sl_node* nodes, const sl_vgrid* vgrid, uint32_t count, cudaStream_t s) {
   if (!count) return cudaSuccess;
   iso_kernel<<<blocks_for(count), kThreads, 0, s>>>(gs, nodes, vgrid, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_blur_records(const sl_part* parts, uint32_t part_count, float shutter, uint32_t mask,
+                                const sl_gaussian* g_src, const sl_node* n_src, sl_gaussian* g_dst, sl_node* n_dst,
+                                uint32_t count, cudaStream_t s) {
+  if (!count || !mask) return cudaSuccess;
+  blur_records_kernel<<<blocks_for(count), kThreads, 0, s>>>(parts, part_count, shutter, mask, g_src, n_src, g_dst,
+                                                              n_dst, count);
   return cudaGetLastError();
 }
 

@@ -66,6 +66,11 @@ cudaError_t launch_bshade(const BatchView* views, const BatchScene* scenes, cons
                           uint32_t* view_maxrad, int variant, cudaStream_t s);
 
 cudaError_t upload_iso_dirs(const float* dirs128x4, cudaStream_t s);
+// motion_blur.wgsl blur_records over the leaves of the parts in `mask`: g_dst / n_dst receive each leaf stretched
+// along its part's motion (flags bit 1, shutter > 0) or its rest record.
+cudaError_t launch_blur_records(const sl_part* parts, uint32_t part_count, float shutter, uint32_t mask,
+                                const sl_gaussian* g_src, const sl_node* n_src, sl_gaussian* g_dst, sl_node* n_dst,
+                                uint32_t count, cudaStream_t s);
 cudaError_t launch_iso(const sl_gaussian* gs, sl_node* nodes, const sl_vgrid* vgrid, uint32_t count, cudaStream_t s);
 cudaError_t launch_lsm_splat(const LightMapParams& L, const sl_gaussian* gs, const sl_node* nodes,
                              const sl_part* parts, uint32_t count, uint32_t* acc, cudaStream_t s);

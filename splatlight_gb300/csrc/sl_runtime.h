@@ -127,6 +127,11 @@ struct sl_lighting {
   std::vector<int> have_center;
   bool sm_dirty_all = true;
   bool lamp_filled = false, env_filled = false;
+  // motion blur for the lighting (motion_blur.wgsl, lighting.js:468-507): the opacity-map splats draw these copies
+  float blur_shutter = 0.0f;
+  bool blur_init = false;
+  uint32_t blur_prev = 0;  // the parts that moved in the previous update (their copies go back to rest)
+  sl::DevBuf g_blur, n_blur;
 };
 
 namespace sl {

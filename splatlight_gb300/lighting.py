@@ -70,6 +70,10 @@ class Lighting:
                     asg: bool = True) -> None:
         N.check(self._lib.sl_lighting_set_options(self._h, shadow_res, sun_res, mode, theta, 1 if asg else 0))
 
+    def set_blur(self, shutter: float) -> None:
+        """Motion blur for the lighting: moving parts' records drawn stretched into the opacity maps (0 = off)."""
+        N.check(self._lib.sl_lighting_set_blur(self._h, C.c_float(shutter)))
+
     def update(self, eye, forward=None, moved_mask: int = 0, stream=None) -> None:
         e = (C.c_float * 3)(*[float(v) for v in eye])
         f = (C.c_float * 3)(*[float(v) for v in forward]) if forward is not None else None

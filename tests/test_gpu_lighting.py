@@ -83,3 +83,54 @@ def test_update_after_moving_a_part(cuda, orc):
     ocol, olt, oet, _ = orc.lighting(s2, threads=16)
     assert np.allclose(lt, olt, rtol=1e-5, atol=1e-6)
     assert np.allclose(col, ocol, rtol=1e-3, atol=1e-5)
+
+
+@pytest.mark.parametrize("which", ["cornell", "hill"])
+def test_motion_blur_in_the_lighting(cuda, orc, which):
+    """motion_blur.wgsl blur_records: a moving part (flags bit 1, xf_prev behind xf) draws stretched records into the
+    opacity maps (light map A on the Cornell room, the sun maps on the hill) while every receiver keeps its rest
+    record: lamp and env transmittance within 1e-5 of the restatement with the same blur, measurably unlike the
+    unblurred maps, and the lit frame within 1e-3; back to the unblurred maps once the part stops."""
+    if which == "cornell":
+        s = scene.subset(scene.cornell(), 20000)
+        moving, shift = 5, (0.25, 0.0, 0.1)
+    else:
+        s = scene.dataclasses.replace(scene.subset(scene.hill(), 150000), shadow_res=512, sun_res=1024)
+        moving, shift = 2, (0.6, 0.3, 0.0)        # the canopy
+    parts = s.parts.copy()
+    parts["xf_prev"][moving] = parts["xf"][moving]
+    for k, v in zip((3, 7, 11), shift):
+        parts["xf"][moving][k] += v
+    parts["flags"][moving] |= 2
+    s2 = scene.dataclasses.replace(s, parts=parts)
+    fwd = camera_forward(s2)
+    with SplatRenderer(s.gaussians, s.parts) as r:
+        L = for_scene(r, s)
+        L.set_options(shadow_res=s.shadow_res, sun_res=s.sun_res)
+        L.set_blur(0.5)
+        L.update(s.eye, fwd)
+        r.write_parts(parts)
+        L.update(s.eye, fwd, moved_mask=1 << moving)
+        col, lt, et, _ = L.read()
+        ocol, olt, oet, _ = orc.lighting(s2, threads=16, blur_shutter=0.5)
+        assert np.allclose(lt, olt, rtol=1e-5, atol=1e-6), np.abs(lt - olt).max()
+        assert np.allclose(et, oet, rtol=1e-5, atol=1e-6), np.abs(et - oet).max()
+        assert np.allclose(col, ocol, rtol=1e-3, atol=1e-5)
+        _, plt, pet, _ = orc.lighting(s2, threads=16)
+        changed = np.abs(lt - plt).max() if which == "cornell" else np.abs(et - pet).max()
+        assert changed > 1e-3, changed
+        f = camera.make_frame(s.eye, s.target, s.up, s.fov_deg, 320, 240, s.count, far=s.far, view_mode=VIEW_LIT,
+                              n_emit=len(s.emitters))
+        img = r.render(f)
+        ref = orc.render(s.gaussians, parts, f, emitters=s.emitters, colour=ocol, threads=16)
+        assert float(np.abs(img - ref["rgba"]).max()) <= RGB_TOL
+        # the part stops (flags bit 1 cleared, xf_prev = xf): its copies go back to rest in the next update
+        parts2 = parts.copy()
+        parts2["flags"][moving] &= ~np.uint32(2)
+        parts2["xf_prev"][moving] = parts2["xf"][moving]
+        r.write_parts(parts2)
+        L.update(s.eye, fwd, moved_mask=0)
+        _, lt2, et2, _ = L.read()
+        _, olt2, oet2, _ = orc.lighting(scene.dataclasses.replace(s, parts=parts2), threads=16, blur_shutter=0.5)
+        assert np.allclose(lt2, olt2, rtol=1e-5, atol=1e-6) and np.allclose(et2, oet2, rtol=1e-5, atol=1e-6)
+        L.close()
