@@ -444,20 +444,9 @@ def run_lod(args, stream, flush, threshold_px: float = 2.0):
     lod = Lod(r, nodes, kids)
     t_create = time.perf_counter() - t0
     G, N = len(s.gaussians), len(nodes)
-    f0 = frame_for(s, 3)
-    f = frame_lod(f0.copy(), threshold_px, N - G)
+    from splatlight_gb300 import camera
     out = torch.empty((s.height, s.width, 4), dtype=torch.float32, device="cuda")
     ref = torch.empty_like(out)
-
-    def with_lod():
-        L.shade(s.eye, stream=sc)
-        lod.select(f, stream=sc)
-        lod.colour(f, stream=sc)
-        r.render(f, out=out, stream=sc)
-
-    def without():
-        L.shade(s.eye, stream=sc)
-        r.render(f0, out=ref, stream=sc)
 
     def timed(fn, steps):
         ts = []
@@ -473,30 +462,54 @@ def run_lod(args, stream, flush, threshold_px: float = 2.0):
             ts.append(a.elapsed_time(b))
         return statistics.median(ts)
 
-    for _ in range(max(args.warmup, 3)):
-        with_lod()
-        without()
-    torch.cuda.synchronize()
-    steps = max(3, min(args.steps, 20))
-    ms_l = timed(with_lod, steps)
-    st = r.last_stats
-    ms_p = timed(without, steps)
+    def measure(eye, far):
+        """One camera: the lit frame with the LOD cut against the same frame without it."""
+        f0 = camera.make_frame(eye, s.target, s.up, s.fov_deg, s.width, s.height, s.count, far=far, view_mode=3,
+                               n_emit=len(s.emitters))
+        f = frame_lod(f0.copy(), threshold_px, N - G)
 
-    def cut_only():
-        lod.select(f, stream=sc)
-        lod.colour(f, stream=sc)
+        def with_lod():
+            L.shade(eye, stream=sc)
+            lod.select(f, stream=sc)
+            lod.colour(f, stream=sc)
+            r.render(f, out=out, stream=sc)
 
-    ms_cut = timed(cut_only, steps)
-    flags = lod.read()[0]
+        def without():
+            L.shade(eye, stream=sc)
+            r.render(f0, out=ref, stream=sc)
+
+        def cut_only():
+            lod.select(f, stream=sc)
+            lod.colour(f, stream=sc)
+
+        for _ in range(max(args.warmup, 3)):
+            with_lod()
+            without()
+        torch.cuda.synchronize()
+        steps = max(3, min(args.steps, 20))
+        ms_l = timed(with_lod, steps)
+        st = r.last_stats
+        ms_p = timed(without, steps)
+        ms_cut = timed(cut_only, steps)
+        flags = lod.read()[0]
+        return {"lod_views_per_s": round(1000.0 / ms_l, 2), "lod_ms_per_frame": round(ms_l, 4),
+                "plain_views_per_s": round(1000.0 / ms_p, 2), "plain_ms_per_frame": round(ms_p, 4),
+                "speedup_vs_plain": round(ms_p / ms_l, 3), "select_colour_ms": round(ms_cut, 4),
+                "drawn_leaves": int((flags[:G] == DRAW).sum()), "drawn_nodes": int((flags[G:] == DRAW).sum()),
+                "visible": int(st.visible), "entries": int(st.entries),
+                "mean_abs_diff_vs_plain": round(float((out - ref).abs().mean().item()), 6)}
+
     res = {"workload": "hill-like 1,048,576 Gaussians, 1920x1080, lit; screen-space LOD at "
-                       f"{threshold_px:g} px (projected-area rule) over a {N - G:,}-node moment-matched tree",
-           "lod_views_per_s": round(1000.0 / ms_l, 2), "lod_ms_per_frame": round(ms_l, 4),
-           "plain_views_per_s": round(1000.0 / ms_p, 2), "plain_ms_per_frame": round(ms_p, 4),
-           "speedup_vs_plain": round(ms_p / ms_l, 3), "select_colour_ms": round(ms_cut, 4),
-           "drawn_leaves": int((flags[:G] == DRAW).sum()), "drawn_nodes": int((flags[G:] == DRAW).sum()),
-           "visible": int(st.visible), "entries": int(st.entries),
-           "mean_abs_diff_vs_plain": round(float((out - ref).abs().mean().item()), 6),
-           "tree_build_s": round(t_tree, 2), "lod_create_s": round(t_create, 2)}
+                       f"{threshold_px:g} px (projected-area rule) over a {N - G:,}-node moment-matched tree; the "
+                       "reference camera, and the same view from 4x the distance (where the 2 px rule closes subtrees)"}
+    res.update(measure(s.eye, s.far))
+    e = np.asarray(s.eye, np.float64)
+    t = np.asarray(s.target, np.float64)
+    eye_far = tuple(np.float32(t + 4.0 * (e - t)))
+    far = max(float(s.far), 4.0 * float(np.linalg.norm(e - t)) + 40.0)
+    res["distant_view"] = measure(eye_far, far)
+    res["tree_build_s"] = round(t_tree, 2)
+    res["lod_create_s"] = round(t_create, 2)
     lod.close()
     L.close()
     r.close()

@@ -263,12 +263,19 @@ SL_API int sl_lighting_set_options(sl_lighting* l, uint32_t shadow_res, uint32_t
 
 /* Motion blur for the lighting (src/lighting.js:468-507, runtime/wgsl/motion_blur.wgsl): with shutter > 0 (the
  * reference's default is 0.5), every update rewrites copies of the records of the parts that moved this update or the
- * last (moved_mask), each leaf of a moving part (sl_part.flags bit 1) stretched along its motion over the exposure,
+ * last (moved_mask), each record of a moving part (sl_part.flags bit 1) stretched along its motion over the exposure,
  * shutter x (xf - xf_prev): covariance C + d d^T / 12 centred mid-exposure, mass kept; the opacity-map splats (light
  * map A and the sun maps) draw the copies, so a moving part casts a smeared shadow, while every receiver keeps its
- * rest record.  This is the reference's ?blurcut=0 form (every record stretched); its default cut of the part's tree
- * sized to the smear is not built.  0 (the default here) turns it off.  The maps re-splat at the next update. */
-SL_API int sl_lighting_set_blur(sl_lighting* l, float shutter);
+ * rest record.  With a tree (sl_lighting_set_tree) and cut_k > 0 (the reference's ?blurcut, default 1) a moving part
+ * splats the cut of its tree whose nodes are about cut_k x its smear across (light_shadow.wgsl:158-210,
+ * sun_map.wgsl:119-153), each keeping its rest coverage; cut_k 0 (or no tree) stretches every leaf.  shutter 0 (the
+ * default here) turns it off.  The maps re-splat at the next update. */
+SL_API int sl_lighting_set_blur(sl_lighting* l, float shutter, float cut_k);
+/* The scene's tree for the motion-blur cut (src/lighting.js initNodeParents, :557-567): n_nodes records, the leaves
+ * (the renderer's Gaussians, in order) then the internal nodes, whose children are kids[child_lo .. child_hi); the
+ * parts' roots come from the renderer's parts (sl_part.root).  Host arrays, copied. */
+SL_API int sl_lighting_set_tree(sl_lighting* l, const sl_node* nodes, uint32_t n_nodes, const uint32_t* kids,
+                                uint32_t n_kids);
 
 /* encode(encoder, eye, timers, changed, still) (src/lighting.js:1258-1274) + Environment.encodeDirect
  * (src/environment.js:181-189): iso_init on first use, the opacity maps of moved parts (moved_mask bit p) or of

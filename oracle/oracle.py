@@ -213,15 +213,29 @@ class LightSetup(C.Structure):
                 ("edge_soft", C.c_float), ("skip_part", C.c_uint32), ("shadow_res", C.c_uint32),
                 ("lights", C.c_void_p), ("n_lights", C.c_uint32), ("sun_res", C.c_uint32),
                 ("sky_ambient", C.c_float), ("eye", C.c_float * 3), ("fwd", C.c_float * 3),
-                ("shade_only", C.c_uint32), ("blur_shutter", C.c_float)]
+                ("shade_only", C.c_uint32), ("blur_shutter", C.c_float), ("tree_nodes", C.c_void_p),
+                ("tree_parent", C.c_void_p), ("n_tree", C.c_uint32), ("cut_k", C.c_float)]
+
+
+def node_parents(nodes, kids, G: int):
+    """Every node's parent (src/lighting.js initNodeParents): internal nodes with a part own kids[child_lo:child_hi]."""
+    parent = np.full(len(nodes), 0xFFFFFFFF, np.uint32)
+    k = np.asarray(kids, np.uint32)
+    for i in range(G, len(nodes)):
+        if int(nodes["part"][i]) == 0xFFFFFFFF:
+            continue
+        parent[k[int(nodes["child_lo"][i]):int(nodes["child_hi"][i])]] = i
+    return parent
 
 
 def lighting(scene, eye=None, target=None, threads: int = 8, shadow_res=None, sun_res=None, mode: int = 1,
-             asg: bool = True, cached=None, blur_shutter: float = 0.0):
+             asg: bool = True, cached=None, blur_shutter: float = 0.0, tree=None, cut_k: float = 1.0):
     """The restated lighting update on a splatlight_gb300.scene.Scene: returns (colour (G, 4), lamp_T (G,),
     env_T (G, 4), nodes with iso_norm).  Emitters are the scene's host emitter records.  cached: the (lamp_T,
     env_T, nodes) of an earlier call -- then only the shading pass runs (the maps of a static scene hold).
-    blur_shutter > 0: the opacity maps draw moving parts (flags bit 1) stretched over the exposure."""
+    blur_shutter > 0: the opacity maps draw moving parts (flags bit 1) stretched over the exposure; with tree = (nodes,
+    kids) (the leaves, then the internal nodes) and cut_k > 0, a moving part splats the cut of its tree sized to its
+    smear."""
     L = lib()
     L.orc_lighting.restype = C.c_int
     L.orc_lighting.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -255,6 +269,15 @@ def lighting(scene, eye=None, target=None, threads: int = 8, shadow_res=None, su
     S.sun_res = scene.sun_res if sun_res is None else sun_res
     S.sky_ambient = scene.sky_ambient
     S.blur_shutter = float(blur_shutter)
+    keep = []
+    if tree is not None:
+        tn = np.ascontiguousarray(tree[0])
+        tp = node_parents(tn, tree[1], len(scene.gaussians))
+        keep = [tn, tp]
+        S.tree_nodes = tn.ctypes.data
+        S.tree_parent = tp.ctypes.data
+        S.n_tree = len(tn)
+        S.cut_k = float(cut_k)
     S.eye[:] = eye.tolist()
     S.fwd[:] = fwd.tolist()
     g = np.ascontiguousarray(scene.gaussians)

@@ -844,6 +844,58 @@ static m3f leaf_cov_world(const sl_gaussian* G, const float* xf) {
   return m3_mul(&t1, &RT);
 }
 
+/* inv3 (light_shadow.wgsl:119-122) */
+static m3f inv3(const m3f* m) {
+  f3 r0 = cross3(m->c[1], m->c[2]), r1 = cross3(m->c[2], m->c[0]), r2 = cross3(m->c[0], m->c[1]);
+  float id = 1.0f / dot3(m->c[0], r0);
+  m3f r;
+  r.c[0] = F3(r0.x * id, r1.x * id, r2.x * id);
+  r.c[1] = F3(r0.y * id, r1.y * id, r2.y * id);
+  r.c[2] = F3(r0.z * id, r1.z * id, r2.z * id);
+  return r;
+}
+/* world covariance of record g: a leaf from its Gaussian, a tree node from its C^-1 (light_shadow.wgsl:125-137) */
+static m3f rec_cov(const sl_gaussian* gs, const sl_node* nodes, uint32_t count, uint32_t g, const float* xf) {
+  if (g < count) return leaf_cov_world(&gs[g], xf);
+  const sl_node* n = &nodes[g];
+  m3f S;
+  S.c[0] = F3(n->cinv_diag[0], n->cinv_off[0], n->cinv_off[1]);
+  S.c[1] = F3(n->cinv_off[0], n->cinv_diag[1], n->cinv_off[2]);
+  S.c[2] = F3(n->cinv_off[1], n->cinv_off[2], n->cinv_diag[2]);
+  m3f C = inv3(&S);
+  m3f R;
+  for (int c = 0; c < 3; c++) R.c[c] = part_rot_col(xf, c);
+  m3f t = m3_mul(&R, &C);
+  m3f RT = m3_t(&R);
+  return m3_mul(&t, &RT);
+}
+/* the motion-blur cut of the map splats (light_shadow.wgsl:158-210, sun_map.wgsl:119-153) */
+typedef struct {
+  const sl_gaussian* g_rest;
+  const sl_node* n_rest;
+  const uint32_t* parent;
+  uint32_t n_nodes;
+  float k, shutter;
+} bcut;
+/* 0 = not splatted, 1 = as it is, 2 = keeping its rest coverage */
+static int cut_verdict(const bcut* bc, const sl_part* parts, uint32_t count, uint32_t g, uint32_t p) {
+  int leaf = g < count;
+  float L = 0.0f;
+  uint32_t root = parts[p].root;
+  if (bc->k > 0.0f && bc->shutter > 0.0f && (parts[p].flags & 2u) != 0u && root < bc->n_nodes) {
+    const sl_node* rn = &bc->n_rest[root];
+    f3 x = F3(rn->mean[0], rn->mean[1], rn->mean[2]);
+    f3 a = xf_point(parts[p].xf, x), b = xf_point(parts[p].xf_prev, x);
+    L = bc->shutter * len3(sub3(a, b));
+  }
+  if (L <= 0.0f) return leaf ? 1 : 0;
+  float thr = bc->k * L;
+  if (!leaf && bc->n_rest[g].radius > thr) return 0;
+  uint32_t par = bc->parent[g];
+  if (g != root && par != NONE_U32 && bc->n_rest[par].radius <= thr) return 0;
+  return 2;
+}
+
 static void atomic_add_u32(uint32_t* p, uint32_t v) {
 #ifdef _OPENMP
 #pragma omp atomic
@@ -858,17 +910,18 @@ static uint32_t to_u32(float x) {
 
 /* splat one leaf into light map A layer p (light_shadow.wgsl:212-286) */
 static void lsm_splat_one(const lframe* L, uint32_t res, uint32_t g, uint32_t p, const sl_gaussian* gs,
-                          const sl_node* nodes, const sl_part* parts, uint32_t* acc) {
+                          const sl_node* nodes, const sl_part* parts, uint32_t count, const bcut* bc, int verdict,
+                          uint32_t* acc) {
   const float FIX = 65536.0f, LOWPASS = 0.3f;
   const float* xf = parts[p].xf;
   const sl_node* nd = &nodes[g];
-  f3 mu = F3(gs[g].mu[0], gs[g].mu[1], gs[g].mu[2]);
+  f3 mu = g < count ? F3(gs[g].mu[0], gs[g].mu[1], gs[g].mu[2]) : F3(nd->mean[0], nd->mean[1], nd->mean[2]);
   f3 m = xf_point(xf, mu);
   f3 dv = sub3(m, L->center);
   float r = len3(dv);
   if (r < 1e-4f) return;
   f3 w = div3(dv, r);
-  m3f C = leaf_cov_world(&gs[g], xf);
+  m3f C = rec_cov(gs, nodes, count, g, xf);
   if (L->hemi && dot3(dv, L->normal) < -3.0f * sqrtf(dot3(L->normal, m3_mulv(&C, L->normal)))) return;
   f3 b0 = basis_k(w), b1 = cross3(w, b0);
   f3 c0 = m3_mulv(&C, b0), c1 = m3_mulv(&C, b1);
@@ -894,6 +947,29 @@ static void lsm_splat_one(const lframe* L, uint32_t res, uint32_t g, uint32_t p,
   S.c[1].y += LOWPASS;
   float det1 = m2_det(&S);
   tau0 *= sqrtf(fmaxf(det0, 0.0f) / det1);
+  if (verdict == 2) {
+    /* the rest record's peak opacity spread evenly over the stretched footprint: alpha' A' = alpha A */
+    const sl_node* ndr = &bc->n_rest[g];
+    m3f Cr = rec_cov(bc->g_rest, bc->n_rest, count, g, xf);
+    f3 cwr = m3_mulv(&Cr, w);
+    f3 r0 = m3_mulv(&Cr, b0), r1 = m3_mulv(&Cr, b1);
+    m2f Cbr;
+    Cbr.c[0] = F2(dot3(b0, r0), dot3(b0, r1));
+    Cbr.c[1] = F2(dot3(b0, r1), dot3(b1, r1));
+    f2 cbzr = F2(dot3(b0, cwr), dot3(b1, cwr));
+    m2f Cbr_i = m2_inv(&Cbr);
+    float szr = fmaxf(dot3(w, cwr) - dot2(cbzr, m2_mulv(&Cbr_i, cbzr)), 1e-12f);
+    m2f Sa = m2_scale(&Cbr, 1.0f / (r * r));
+    m2f tr = m2_mul(&J, &Sa);
+    m2f Sr = m2_mul(&tr, &JT);
+    float d0r = m2_det(&Sr);
+    Sr.c[0].x += LOWPASS;
+    Sr.c[1].y += LOWPASS;
+    float d1r = m2_det(&Sr);
+    float tau_r = ndr->kappa * dirm(ndr, xf_dir_inv(xf, w)) * sqrtf(2.0f * PI_F * szr) * sqrtf(fmaxf(d0r, 0.0f) / d1r);
+    float a = fminf((1.0f - sl_expf(-tau_r)) * sqrtf(fmaxf(d1r, 1e-30f) / fmaxf(det1, 1e-30f)), 0.999f);
+    tau0 = fminf(-sl_logf(1.0f - a), tau0);
+  }
   m2f Si = m2_inv(&S);
   m2f Ji = m2_inv(&J);
   m2f JiT = m2_t(&Ji);
@@ -1011,13 +1087,30 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
   const sl_node* ndp = nodes;
   sl_gaussian* g_blur = NULL;
   sl_node* n_blur = NULL;
+  const int have_tree = S->tree_nodes && S->n_tree > count;
+  const uint32_t n_nodes = have_tree ? S->n_tree : count;
+  bcut bc = {gs, have_tree ? S->tree_nodes : nodes, have_tree ? S->tree_parent : NULL, n_nodes, 0.0f,
+             S->blur_shutter};
+  uint32_t n_rec = count;
   if (S->blur_shutter > 0.0f && !S->shade_only) {
     g_blur = (sl_gaussian*)malloc(sizeof(sl_gaussian) * (count ? count : 1u));
-    n_blur = (sl_node*)malloc(sizeof(sl_node) * (count ? count : 1u));
+    n_blur = (sl_node*)malloc(sizeof(sl_node) * (n_nodes ? n_nodes : 1u));
     for (uint32_t g = 0; g < count; g++)
-      orc_blur_record(parts, part_count, S->blur_shutter, &gs[g], &nodes[g], &g_blur[g], &n_blur[g]);
+      orc_blur_record(parts, part_count, S->blur_shutter, &gs[g], &bc.n_rest[g], &g_blur[g], &n_blur[g]);
+    for (uint32_t i = count; i < n_nodes; i++) {  /* tree nodes: the node record alone */
+      sl_gaussian dummy;
+      memset(&dummy, 0, sizeof dummy);
+      dummy.quat[3] = 1.0f;
+      dummy.scale[0] = dummy.scale[1] = dummy.scale[2] = 1.0f;
+      sl_gaussian unused;
+      orc_blur_record(parts, part_count, S->blur_shutter, &dummy, &bc.n_rest[i], &unused, &n_blur[i]);
+    }
     gsp = g_blur;
     ndp = n_blur;
+    if (have_tree) {
+      bc.k = S->cut_k;
+      if (bc.k > 0.0f) n_rec = n_nodes;
+    }
   }
 
   /* light map A (light_shadow.js:89-165): all layers dirty, then the lookup */
@@ -1050,10 +1143,12 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 256)
 #endif
-    for (int64_t g = 0; g < (int64_t)count; g++) {
-      uint32_t p = gsp[g].part_surface & 0xFFFFu;
+    for (int64_t gi = 0; gi < (int64_t)n_rec; gi++) {
+      uint32_t g = (uint32_t)gi;
+      uint32_t p = g < count ? (gsp[g].part_surface & 0xFFFFu) : bc.n_rest[g].part;
       if (p >= part_count || p == S->skip_part) continue;
-      lsm_splat_one(&L, res, (uint32_t)g, p, gsp, ndp, parts, acc);
+      int verdict = cut_verdict(&bc, parts, count, g, p);
+      if (verdict) lsm_splat_one(&L, res, g, p, gsp, ndp, parts, count, &bc, verdict, acc);
     }
     for (uint32_t p = 0; p < part_count; p++) {
       resolve_layer(acc + (size_t)p * res * res * 3u, 65536.0f, res * res, mip + (size_t)p * layer_texels);
@@ -1185,19 +1280,22 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 256)
 #endif
-    for (int64_t gi = 0; gi < (int64_t)count; gi++) {
+    for (int64_t gi = 0; gi < (int64_t)n_rec; gi++) {
       uint32_t g = (uint32_t)gi;
-      uint32_t p = gsp[g].part_surface & 0xFFFFu;
+      uint32_t p = g < count ? (gsp[g].part_surface & 0xFFFFu) : bc.n_rest[g].part;
       if (p >= Pn) continue;
+      int verdict = cut_verdict(&bc, parts, count, g, p);
+      if (!verdict) continue;
       for (uint32_t l = 0; l < nl; l++) {
         if (ly[l].part != p || !(S->lights[ly[l].light].shadows)) continue;
         /* sm_splat_one (sun_map.wgsl:155-219) */
         const float* xf = parts[p].xf;
         const sl_node* nd = &ndp[g];
-        f3 x = xf_point(xf, F3(gsp[g].mu[0], gsp[g].mu[1], gsp[g].mu[2]));
+        f3 mu = g < count ? F3(gsp[g].mu[0], gsp[g].mu[1], gsp[g].mu[2]) : F3(nd->mean[0], nd->mean[1], nd->mean[2]);
+        f3 x = xf_point(xf, mu);
         f3 w = F3(S->lights[ly[l].light].dir[0], S->lights[ly[l].light].dir[1], S->lights[ly[l].light].dir[2]);
         f3 b0 = ly[l].t1, b1 = ly[l].t2;
-        m3f C = leaf_cov_world(&gsp[g], xf);
+        m3f C = rec_cov(gsp, ndp, count, g, xf);
         f3 c0 = m3_mulv(&C, b0), c1 = m3_mulv(&C, b1), cw = m3_mulv(&C, w);
         m2f Cbb;
         Cbb.c[0] = F2(dot3(b0, c0), dot3(b1, c0));
@@ -1212,6 +1310,26 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
         Sm.c[1].y += SM_LOWPASS;
         float det1 = m2_det(&Sm);
         float tau0 = nd->kappa * dirm(nd, xf_dir_inv(xf, w)) * sqrtf(2.0f * PI_F * sz2) * sqrtf(fmaxf(det0, 0.0f) / det1);
+        if (verdict == 2) { /* keep the rest record's coverage (sun_map.wgsl:178-193) */
+          const sl_node* ndr = &bc.n_rest[g];
+          m3f Cr = rec_cov(bc.g_rest, bc.n_rest, count, g, xf);
+          f3 r0 = m3_mulv(&Cr, b0), r1 = m3_mulv(&Cr, b1), rw = m3_mulv(&Cr, w);
+          m2f Cbr;
+          Cbr.c[0] = F2(dot3(b0, r0), dot3(b1, r0));
+          Cbr.c[1] = F2(dot3(b0, r1), dot3(b1, r1));
+          f2 cbzr = F2(dot3(b0, rw), dot3(b1, rw));
+          m2f Cbr_i = m2_inv(&Cbr);
+          float szr = fmaxf(dot3(w, rw) - dot2(cbzr, m2_mulv(&Cbr_i, cbzr)), 1e-12f);
+          m2f Sr = m2_scale(&Cbr, tex * tex);
+          float d0r = m2_det(&Sr);
+          Sr.c[0].x += SM_LOWPASS;
+          Sr.c[1].y += SM_LOWPASS;
+          float d1r = m2_det(&Sr);
+          float tau_r = ndr->kappa * dirm(ndr, xf_dir_inv(xf, w)) * sqrtf(2.0f * PI_F * szr) *
+                        sqrtf(fmaxf(d0r, 0.0f) / d1r);
+          float a = fminf((1.0f - sl_expf(-tau_r)) * sqrtf(fmaxf(d1r, 1e-30f) / fmaxf(det1, 1e-30f)), 0.999f);
+          tau0 = fminf(-sl_logf(1.0f - a), tau0);
+        }
         m2f Si = m2_inv(&Sm);
         float z0 = ly[l].zref - dot3(x, w);
         f2 gz = div2(m2_mulv(&Cbb_i, cbz), tex);

@@ -42,6 +42,12 @@ typedef struct orc_light_setup {
   uint32_t shade_only;/* 1: nodes (iso_norm), lamp_T and env_T are inputs from an earlier call; only shade */
   float blur_shutter; /* > 0: the opacity-map splats draw moving parts' records stretched over the exposure
                          (motion_blur.wgsl blur_records; every part with flags bit 1 moves) */
+  /* the motion-blur cut (light_shadow.wgsl:158-210): the scene's tree (the leaves, then the internal nodes), every
+   * node's parent, and the cut factor k (0: every leaf stretched) */
+  const sl_node* tree_nodes;
+  const uint32_t* tree_parent;
+  uint32_t n_tree;
+  float cut_k;
 } orc_light_setup;
 
 /* motion_blur.wgsl blur_records (:80-127) for one leaf: its Gaussian and node stretched along its part's motion over

@@ -108,7 +108,8 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_emitter_tree": (_I, [_P, _U32, _P, _P, _P, C.POINTER(_U32)]),
     "sl_lighting_set_environment": (_I, [_P, _P, _U32, C.c_float]),
     "sl_lighting_set_options": (_I, [_P, _U32, _U32, _U32, C.c_float, _I]),
-    "sl_lighting_set_blur": (_I, [_P, C.c_float]),
+    "sl_lighting_set_blur": (_I, [_P, C.c_float, C.c_float]),
+    "sl_lighting_set_tree": (_I, [_P, _P, _U32, _P, _U32]),
     "sl_lighting_update": (_I, [_P, _P, _P, _U32, _P]),
     "sl_lighting_shade": (_I, [_P, _P, _P]),
     "sl_lighting_read": (_I, [_P, _P, _P, _P, _P]),

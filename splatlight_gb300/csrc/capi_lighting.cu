@@ -485,7 +485,7 @@ int sl_lighting_destroy(sl_lighting* l) {
   }
   sl::DevBuf* all[] = {&l->nodes, &l->vgrid, &l->materials, &l->parts, &l->tree, &l->lamp_T, &l->env_T, &l->colour,
                        &l->lm_acc, &l->lm_mip, &l->sm_acc, &l->sm_mip, &l->sm_layers, &l->sm_dirty, &l->order,
-                       &l->g_blur, &l->n_blur};
+                       &l->g_blur, &l->n_blur, &l->tree_nodes, &l->node_parent};
   for (sl::DevBuf* b : all) b->release();
   delete l;
   return SL_OK;
@@ -568,16 +568,46 @@ int sl_lighting_set_options(sl_lighting* l, uint32_t shadow_res, uint32_t sun_re
   return SL_OK;
 }
 
-int sl_lighting_set_blur(sl_lighting* l, float shutter) {
+int sl_lighting_set_blur(sl_lighting* l, float shutter, float cut_k) {
   if (!l) return fail(SL_ERR_INVALID_ARG, "null lighting");
   if (!(shutter >= 0.0f && shutter <= 1.0f)) return fail(SL_ERR_INVALID_ARG, "shutter outside [0, 1]");
-  if (shutter != l->blur_shutter) {
+  if (!(cut_k >= 0.0f && cut_k <= 1e6f)) return fail(SL_ERR_INVALID_ARG, "bad cut factor");
+  if (shutter != l->blur_shutter || cut_k != l->cut_k) {
     l->blur_shutter = shutter;
+    l->cut_k = cut_k;
     l->blur_init = false;
     l->blur_prev = 0;
     l->lm_dirty = true;
     l->sm_dirty_all = true;
   }
+  return SL_OK;
+}
+
+int sl_lighting_set_tree(sl_lighting* l, const sl_node* nodes, uint32_t n_nodes, const uint32_t* kids,
+                         uint32_t n_kids) {
+  if (!l || !nodes || (n_kids && !kids)) return fail(SL_ERR_INVALID_ARG, "null argument");
+  if (n_nodes < l->count) return fail(SL_ERR_INVALID_ARG, "the tree must start with the scene's leaves");
+  cudaSetDevice(l->device);
+  // every node's parent (lighting.js initNodeParents): for an internal node with a part, its children's
+  std::vector<uint32_t> parent(n_nodes, 0xFFFFFFFFu);
+  for (uint32_t i = l->count; i < n_nodes; i++) {
+    if (nodes[i].part == 0xFFFFFFFFu) continue;
+    if (nodes[i].child_lo > nodes[i].child_hi || nodes[i].child_hi > n_kids)
+      return fail(SL_ERR_INVALID_ARG, "node children outside kids");
+    for (uint32_t j = nodes[i].child_lo; j < nodes[i].child_hi; j++) {
+      if (kids[j] >= n_nodes) return fail(SL_ERR_INVALID_ARG, "kid index outside the tree");
+      parent[kids[j]] = i;
+    }
+  }
+  SL_CHECK_CUDA(l->tree_nodes.ensure(sizeof(sl_node) * (size_t)n_nodes), "tree nodes");
+  SL_CHECK_CUDA(l->node_parent.ensure(4ull * n_nodes), "node parents");
+  SL_CHECK_CUDA(cudaMemcpy(l->tree_nodes.ptr, nodes, sizeof(sl_node) * (size_t)n_nodes, cudaMemcpyHostToDevice),
+                "tree nodes");
+  SL_CHECK_CUDA(cudaMemcpy(l->node_parent.ptr, parent.data(), 4ull * n_nodes, cudaMemcpyHostToDevice), "node parents");
+  l->n_tree = n_nodes;
+  l->blur_init = false;
+  l->lm_dirty = true;
+  l->sm_dirty_all = true;
   return SL_OK;
 }
 
@@ -604,15 +634,18 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
   const sl_gaussian* gsp = gs;
   const sl_node* ndp = l->nodes.as<sl_node>();
   uint32_t blur_mask = 0;
+  const bool tree = l->n_tree > G;
+  const uint32_t N = tree ? l->n_tree : G;  // records: the leaves, then the tree's internal nodes
+  const sl_node* n_rest = tree ? l->tree_nodes.as<sl_node>() : l->nodes.as<sl_node>();
+  BlurCut bc{gs, n_rest, tree ? l->node_parent.as<uint32_t>() : nullptr, N, 0.0f, l->blur_shutter};
   if (l->blur_shutter > 0.0f) {
     SL_CHECK_CUDA(l->g_blur.ensure(sizeof(sl_gaussian) * (size_t)G), "blur copies");
-    SL_CHECK_CUDA(l->n_blur.ensure(sizeof(sl_node) * (size_t)G), "blur copies");
+    SL_CHECK_CUDA(l->n_blur.ensure(sizeof(sl_node) * (size_t)N), "blur copies");
     const uint32_t all = P >= 32 ? 0xFFFFFFFFu : ((1u << P) - 1u);
     if (!l->blur_init) {
       SL_CHECK_CUDA(cudaMemcpyAsync(l->g_blur.ptr, gs, sizeof(sl_gaussian) * (size_t)G, cudaMemcpyDeviceToDevice, s),
                     "blur copies");
-      SL_CHECK_CUDA(cudaMemcpyAsync(l->n_blur.ptr, l->nodes.ptr, sizeof(sl_node) * (size_t)G, cudaMemcpyDeviceToDevice,
-                                    s),
+      SL_CHECK_CUDA(cudaMemcpyAsync(l->n_blur.ptr, n_rest, sizeof(sl_node) * (size_t)N, cudaMemcpyDeviceToDevice, s),
                     "blur copies");
       blur_mask = all;
       l->blur_init = true;
@@ -620,11 +653,12 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
       blur_mask = (moved_mask | l->blur_prev) & all;
     }
     l->blur_prev = moved_mask;
-    SL_CHECK_CUDA(launch_blur_records(parts, P, l->blur_shutter, blur_mask, gs, l->nodes.as<sl_node>(),
-                                      l->g_blur.as<sl_gaussian>(), l->n_blur.as<sl_node>(), G, s),
+    SL_CHECK_CUDA(launch_blur_records(parts, P, l->blur_shutter, blur_mask, gs, n_rest, l->g_blur.as<sl_gaussian>(),
+                                      l->n_blur.as<sl_node>(), G, N, s),
                   "blur_records");
     gsp = l->g_blur.as<sl_gaussian>();
     ndp = l->n_blur.as<sl_node>();
+    if (tree) bc.k = l->cut_k;
   }
   const uint32_t resplat = moved_mask | blur_mask;
 
@@ -667,7 +701,7 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
     for (uint32_t p = 0; p < P; p++)
       if ((L.dirty >> p) & 1u)
         SL_CHECK_CUDA(cudaMemsetAsync(l->lm_acc.as<char>() + acc_layer * p, 0, acc_layer, s), "clear light map");
-    SL_CHECK_CUDA(launch_lsm_splat(L, gsp, ndp, parts, G, l->lm_acc.as<uint32_t>(), s), "lsm_splat");
+    SL_CHECK_CUDA(launch_lsm_splat(L, gsp, ndp, parts, G, bc, l->lm_acc.as<uint32_t>(), s), "lsm_splat");
     SL_CHECK_CUDA(launch_resolve(l->lm_acc.as<uint32_t>(), 65536.0f, L.res * L.res, P, L.layer_texels, nullptr,
                                  l->lm_mip.as<float4>(), s),
                   "lsm_resolve");
@@ -803,7 +837,8 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
       SL_CHECK_CUDA(cudaMemcpyAsync(l->sm_layers.ptr, plan.data(), sizeof(SunLayer) * nl, cudaMemcpyHostToDevice, s),
                     "sun layers");
       SL_CHECK_CUDA(cudaMemcpyAsync(l->sm_dirty.ptr, dl.data(), 4 * nl, cudaMemcpyHostToDevice, s), "sun dirty");
-      SL_CHECK_CUDA(launch_sm_splat(SP, l->sm_layers.as<SunLayer>(), gsp, ndp, parts, G, l->sm_acc.as<uint32_t>(), s),
+      SL_CHECK_CUDA(launch_sm_splat(SP, l->sm_layers.as<SunLayer>(), gsp, ndp, parts, G, bc, l->sm_acc.as<uint32_t>(),
+                                    s),
                     "sm_splat");
       SL_CHECK_CUDA(launch_resolve(l->sm_acc.as<uint32_t>(), 4096.0f, SP.res * SP.res, (uint32_t)nl, SP.layer_texels,
                                    l->sm_dirty.as<uint32_t>(), l->sm_mip.as<float4>(), s),

@@ -85,6 +85,53 @@ __device__ __forceinline__ m3 leaf_cov_world(const sl_gaussian& G, const float* 
   return m3m(t1, m3t(R));
 }
 
+// inv3 (light_shadow.wgsl:119-122): the adjugate's rows as columns, over the determinant
+__device__ __forceinline__ m3 inv3(const m3& m) {
+  const f3 r0 = cross3(m.c[1], m.c[2]), r1 = cross3(m.c[2], m.c[0]), r2 = cross3(m.c[0], m.c[1]);
+  const float id = 1.0f / dot3(m.c[0], r0);
+  m3 r;
+  r.c[0] = F3(r0.x * id, r1.x * id, r2.x * id);
+  r.c[1] = F3(r0.y * id, r1.y * id, r2.y * id);
+  r.c[2] = F3(r0.z * id, r1.z * id, r2.z * id);
+  return r;
+}
+// world covariance of record g: a leaf from its Gaussian, a tree node from its C^-1 (light_shadow.wgsl:125-137)
+__device__ __forceinline__ m3 rec_cov(const sl_gaussian* gs, const sl_node* nodes, uint32_t count, uint32_t g,
+                                      const float* xf) {
+  if (g < count) return leaf_cov_world(gs[g], xf);
+  const sl_node& n = nodes[g];
+  m3 S;
+  S.c[0] = F3(n.cinv_diag[0], n.cinv_off[0], n.cinv_off[1]);
+  S.c[1] = F3(n.cinv_off[0], n.cinv_diag[1], n.cinv_off[2]);
+  S.c[2] = F3(n.cinv_off[1], n.cinv_off[2], n.cinv_diag[2]);
+  const m3 C = inv3(S);
+  m3 R;
+  R.c[0] = F3(xf[0], xf[4], xf[8]);
+  R.c[1] = F3(xf[1], xf[5], xf[9]);
+  R.c[2] = F3(xf[2], xf[6], xf[10]);
+  return m3m(m3m(R, C), m3t(R));
+}
+// The cut's verdict for record g of part p: 0 = not splatted, 1 = splatted as it is, 2 = splatted keeping its rest
+// coverage (light_shadow.wgsl:167-210 smear_len / lsm_splat)
+__device__ __forceinline__ int cut_verdict(const BlurCut& bc, const sl_part* __restrict__ parts, uint32_t count,
+                                           uint32_t g, uint32_t p) {
+  const bool leaf = g < count;
+  float L = 0.0f;
+  const uint32_t root = parts[p].root;
+  if (bc.k > 0.0f && bc.shutter > 0.0f && (parts[p].flags & 2u) != 0u && root < bc.n_nodes) {
+    const sl_node& rn = bc.n_rest[root];
+    const f3 x = F3(rn.mean[0], rn.mean[1], rn.mean[2]);
+    const f3 a = xf_point(parts[p].xf, x), b = xf_point(parts[p].xf_prev, x);
+    L = bc.shutter * len3(sub3(a, b));
+  }
+  if (L <= 0.0f) return leaf ? 1 : 0;
+  const float thr = bc.k * L;
+  if (!leaf && bc.n_rest[g].radius > thr) return 0;
+  const uint32_t par = bc.parent[g];
+  if (g != root && par != kNone && bc.n_rest[par].radius <= thr) return 0;
+  return 2;
+}
+
 // One Gaussian's footprint in a map layer: the texels [x0, x1] x [y0, y1] around its centre ct (texels), the inverse of
 // its low-passed texel covariance Si, its peak optical depth, the depth at the centre and its gradient, the depth
 // variance along the light, the fixed-point scale and the layer's first texel.
@@ -152,19 +199,22 @@ __device__ __forceinline__ void splat_warp(bool mine, const Foot& F, uint32_t* a
 // map A (light_shadow.wgsl:191-286): Gaussian g's footprint in its part's octahedral layer; false when it has none
 __device__ __forceinline__ bool lsm_foot(const LightMapParams& L, const sl_gaussian* __restrict__ gs,
                                          const sl_node* __restrict__ nodes, const sl_part* __restrict__ parts,
-                                         uint32_t g, Foot& F) {
-  const sl_gaussian& G = gs[g];
-  const uint32_t p = G.part_surface & 0xFFFFu;
+                                         uint32_t count, const BlurCut& bc, uint32_t g, Foot& F) {
+  const bool leaf = g < count;
+  const uint32_t p = leaf ? (gs[g].part_surface & 0xFFFFu) : bc.n_rest[g].part;
   if (p >= L.part_count || p == L.skip_part || ((L.dirty >> p) & 1u) == 0u) return false;
+  const int verdict = cut_verdict(bc, parts, count, g, p);
+  if (verdict == 0) return false;
   const float FIX = 65536.0f, LOWPASS = 0.3f;
   const float* xf = parts[p].xf;
   const Leaf nd = load_leaf(&nodes[g]);
-  f3 m = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  const f3 mu = leaf ? F3(gs[g].mu[0], gs[g].mu[1], gs[g].mu[2]) : F3(nodes[g].mean[0], nodes[g].mean[1], nodes[g].mean[2]);
+  f3 m = xf_point(xf, mu);
   f3 dv = sub3(m, ld3(L.center));
   float r = len3(dv);
   if (r < 1e-4f) return false;
   f3 w = div3(dv, r);
-  m3 C = leaf_cov_world(G, xf);
+  m3 C = rec_cov(gs, nodes, count, g, xf);
   if (L.hemi && dot3(dv, ld3(L.normal)) < -3.0f * sqrtf(dot3(ld3(L.normal), m3v(C, ld3(L.normal))))) return false;
   f3 b0 = basis_k(w), b1 = cross3(w, b0);
   f3 c0 = m3v(C, b0), c1 = m3v(C, b1);
@@ -187,6 +237,27 @@ __device__ __forceinline__ bool lsm_foot(const LightMapParams& L, const sl_gauss
   S.c[1].y += LOWPASS;
   float det1 = m2det(S);
   tau0 *= sqrtf(fmaxf(det0, 0.0f) / det1);
+  if (verdict == 2) {
+    // the rest record's peak opacity spread evenly over the stretched footprint: alpha' A' = alpha A
+    const Leaf ndr = load_leaf(&bc.n_rest[g]);
+    const m3 Cr = rec_cov(bc.g_rest, bc.n_rest, count, g, xf);
+    const f3 cwr = m3v(Cr, w);
+    const f3 r0 = m3v(Cr, b0), r1 = m3v(Cr, b1);
+    m2 Cbr;
+    Cbr.c[0] = F2(dot3(b0, r0), dot3(b0, r1));
+    Cbr.c[1] = F2(dot3(b0, r1), dot3(b1, r1));
+    const f2 cbzr = F2(dot3(b0, cwr), dot3(b1, cwr));
+    const float szr = fmaxf(dot3(w, cwr) - dot2(cbzr, m2v(m2inv(Cbr), cbzr)), 1e-12f);
+    m2 Sr = m2m(m2m(J, m2s(Cbr, 1.0f / (r * r))), m2t(J));
+    const float d0r = m2det(Sr);
+    Sr.c[0].x += LOWPASS;
+    Sr.c[1].y += LOWPASS;
+    const float d1r = m2det(Sr);
+    const float tau_r = ndr.kappa * dirm(ndr, xf_dir_inv(xf, w)) * sqrtf(2.0f * kPi * szr) *
+                        sqrtf(fmaxf(d0r, 0.0f) / d1r);
+    const float a = fminf((1.0f - sl_expf(-tau_r)) * sqrtf(fmaxf(d1r, 1e-30f) / fmaxf(det1, 1e-30f)), 0.999f);
+    tau0 = fminf(-sl_logf(1.0f - a), tau0);
+  }
   m2 Si = m2inv(S);
   f2 gz = m2v(m2t(m2inv(J)), mul2(m2v(Cbb_i, cbz), r));
   f2 uv = oct_uv(L, w);
@@ -215,14 +286,15 @@ __device__ __forceinline__ bool lsm_foot(const LightMapParams& L, const sl_gauss
   return true;
 }
 
+// One thread per record: the leaves, and with the motion-blur cut on also the tree's internal nodes.
 __global__ void __launch_bounds__(kThreads) lsm_splat_kernel(const __grid_constant__ LightMapParams L,
                                                              const sl_gaussian* __restrict__ gs,
                                                              const sl_node* __restrict__ nodes,
                                                              const sl_part* __restrict__ parts, uint32_t count,
-                                                             uint32_t* acc) {
+                                                             const BlurCut bc, uint32_t n_rec, uint32_t* acc) {
   const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
   Foot F{};
-  const bool mine = g < count && lsm_foot(L, gs, nodes, parts, g, F);
+  const bool mine = g < n_rec && lsm_foot(L, gs, nodes, parts, count, bc, g, F);
   splat_warp<false>(mine, F, acc);
 }
 
@@ -341,18 +413,19 @@ __global__ void __launch_bounds__(kThreads) lsm_lookup_kernel(const __grid_const
 // Gaussian g's footprint in sun layer l (sun_map.wgsl:127-219); false when it has none there
 __device__ __forceinline__ bool sm_foot(const SunParams& SP, const SunLayer* __restrict__ layers,
                                         const sl_gaussian* __restrict__ gs, const sl_node* __restrict__ nodes,
-                                        const sl_part* __restrict__ parts, uint32_t g, uint32_t p, uint32_t l,
-                                        Foot& F) {
-  const sl_gaussian& G = gs[g];
+                                        const sl_part* __restrict__ parts, uint32_t count, const BlurCut& bc,
+                                        uint32_t g, uint32_t p, int verdict, uint32_t l, Foot& F) {
+  const bool leaf = g < count;
   const float SM_FIX = 4096.0f, SM_LOWPASS = 0.3f;
   const SunLayer ly = layers[l];
   if (!ly.dirty || !SP.lights[ly.light].shadows) return false;
   const float* xf = parts[p].xf;
   const Leaf nd = load_leaf(&nodes[g]);
-  f3 x = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  const f3 mu = leaf ? F3(gs[g].mu[0], gs[g].mu[1], gs[g].mu[2]) : F3(nodes[g].mean[0], nodes[g].mean[1], nodes[g].mean[2]);
+  f3 x = xf_point(xf, mu);
   f3 w = ld3(SP.lights[ly.light].dir);
   f3 b0 = ld3(ly.t1), b1 = ld3(ly.t2);
-  m3 C = leaf_cov_world(G, xf);
+  m3 C = rec_cov(gs, nodes, count, g, xf);
   f3 c0 = m3v(C, b0), c1 = m3v(C, b1), cw = m3v(C, w);
   m2 Cbb;
   Cbb.c[0] = F2(dot3(b0, c0), dot3(b1, c0));
@@ -367,6 +440,25 @@ __device__ __forceinline__ bool sm_foot(const SunParams& SP, const SunLayer* __r
   Sm.c[1].y += SM_LOWPASS;
   float det1 = m2det(Sm);
   float tau0 = nd.kappa * dirm(nd, xf_dir_inv(xf, w)) * sqrtf(2.0f * kPi * sz2) * sqrtf(fmaxf(det0, 0.0f) / det1);
+  if (verdict == 2) {  // keep the rest record's coverage (sun_map.wgsl:178-193)
+    const Leaf ndr = load_leaf(&bc.n_rest[g]);
+    const m3 Cr = rec_cov(bc.g_rest, bc.n_rest, count, g, xf);
+    const f3 r0 = m3v(Cr, b0), r1 = m3v(Cr, b1), rw = m3v(Cr, w);
+    m2 Cbr;
+    Cbr.c[0] = F2(dot3(b0, r0), dot3(b1, r0));
+    Cbr.c[1] = F2(dot3(b0, r1), dot3(b1, r1));
+    const f2 cbzr = F2(dot3(b0, rw), dot3(b1, rw));
+    const float szr = fmaxf(dot3(w, rw) - dot2(cbzr, m2v(m2inv(Cbr), cbzr)), 1e-12f);
+    m2 Sr = m2s(Cbr, tex * tex);
+    const float d0r = m2det(Sr);
+    Sr.c[0].x += SM_LOWPASS;
+    Sr.c[1].y += SM_LOWPASS;
+    const float d1r = m2det(Sr);
+    const float tau_r = ndr.kappa * dirm(ndr, xf_dir_inv(xf, w)) * sqrtf(2.0f * kPi * szr) *
+                        sqrtf(fmaxf(d0r, 0.0f) / d1r);
+    const float a = fminf((1.0f - sl_expf(-tau_r)) * sqrtf(fmaxf(d1r, 1e-30f) / fmaxf(det1, 1e-30f)), 0.999f);
+    tau0 = fminf(-sl_logf(1.0f - a), tau0);
+  }
   m2 Si = m2inv(Sm);
   float z0 = ly.zref - dot3(x, w);
   f2 gz = div2(m2v(Cbb_i, cbz), tex);
@@ -398,20 +490,24 @@ __global__ void __launch_bounds__(kThreads) sm_splat_kernel(const __grid_constan
                                                             const sl_gaussian* __restrict__ gs,
                                                             const sl_node* __restrict__ nodes,
                                                             const sl_part* __restrict__ parts, uint32_t count,
-                                                            uint32_t* acc) {
+                                                            const BlurCut bc, uint32_t n_rec, uint32_t* acc) {
   const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
   uint32_t p = 0, l_first = 0, n_layers = 0;
-  if (g < count) {
-    p = gs[g].part_surface & 0xFFFFu;
+  int verdict = 0;
+  if (g < n_rec) {
+    p = g < count ? (gs[g].part_surface & 0xFFFFu) : bc.n_rest[g].part;
     if (p < SP.n_parts) {
-      l_first = SP.part_first[p];
-      n_layers = SP.part_layers[p];
+      verdict = cut_verdict(bc, parts, count, g, p);
+      if (verdict) {
+        l_first = SP.part_first[p];
+        n_layers = SP.part_layers[p];
+      }
     }
   }
   const uint32_t steps = __reduce_max_sync(0xffffffffu, n_layers);
   for (uint32_t j = 0; j < steps; j++) {
     Foot F{};
-    const bool mine = j < n_layers && sm_foot(SP, layers, gs, nodes, parts, g, p, l_first + j, F);
+    const bool mine = j < n_layers && sm_foot(SP, layers, gs, nodes, parts, count, bc, g, p, verdict, l_first + j, F);
     splat_warp<true>(mine, F, acc);
   }
 }
@@ -529,20 +625,24 @@ __device__ float4 blur_mat_to_quat(const m3& m) {
   return make_float4(q0 / l, q1 / l, q2 / l, q3 / l);
 }
 
-// One thread per leaf of a part in `mask` (the parts that moved this frame or the last): its copy rewritten,
-// stretched when the part moves (flags bit 1) and the shutter is open, else back to its rest record.
+// One thread per record (the leaves, then any tree nodes) of a part in `mask` (the parts that moved this frame or the
+// last): its copy rewritten, stretched when the part moves (flags bit 1) and the shutter is open, else back to its
+// rest record; a leaf's Gaussian is rewritten with its node.
 __global__ void __launch_bounds__(kThreads) blur_records_kernel(const sl_part* __restrict__ parts, uint32_t part_count,
                                                                 float shutter, uint32_t mask,
                                                                 const sl_gaussian* __restrict__ g_src,
                                                                 const sl_node* __restrict__ n_src,
                                                                 sl_gaussian* __restrict__ g_dst,
-                                                                sl_node* __restrict__ n_dst, uint32_t count) {
+                                                                sl_node* __restrict__ n_dst, uint32_t count,
+                                                                uint32_t n_nodes) {
   const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
-  if (i >= count) return;
+  if (i >= n_nodes) return;
   sl_node nd = n_src[i];
   const uint32_t p = nd.part;
   if (p >= 32u || ((mask >> p) & 1u) == 0u) return;
-  sl_gaussian G = g_src[i];
+  const bool leaf = i < count;
+  sl_gaussian G;
+  if (leaf) G = g_src[i];
   f3 d = F3(0.0f, 0.0f, 0.0f);
   if (shutter > 0.0f && p < part_count && (parts[p].flags & 2u) != 0u) {
     const f3 x = F3(nd.mean[0], nd.mean[1], nd.mean[2]);
@@ -576,6 +676,8 @@ __global__ void __launch_bounds__(kThreads) blur_records_kernel(const sl_part* _
     nd.kappa = nd.kappa / sqrtf(1.0f + m / 12.0f);
     nd.smax = sqrtf(nd.smax * nd.smax + dd / 12.0f);
     nd.radius = sqrtf(nd.radius * nd.radius + 0.75f * dd);
+  }
+  if (dd > 0.0f && leaf) {
     // the Gaussian: the stretched covariance's eigen-frame, scales ascending, right-handed
     const m3 Rq = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]);
     const f3 s2 = F3(G.scale[0] * G.scale[0], G.scale[1] * G.scale[1], G.scale[2] * G.scale[2]);
@@ -611,7 +713,7 @@ __global__ void __launch_bounds__(kThreads) blur_records_kernel(const sl_part* _
     G.quat[3] = q.w;
   }
   n_dst[i] = nd;
-  g_dst[i] = G;
+  if (leaf) g_dst[i] = G;
 }
 
 }  // namespace
@@ -630,17 +732,18 @@ cudaError_t launch_iso(const sl_gaussian* gs, sl_node* nodes, const sl_vgrid* vg
 
 cudaError_t launch_blur_records(const sl_part* parts, uint32_t part_count, float shutter, uint32_t mask,
                                 const sl_gaussian* g_src, const sl_node* n_src, sl_gaussian* g_dst, sl_node* n_dst,
-                                uint32_t count, cudaStream_t s) {
-  if (!count || !mask) return cudaSuccess;
-  blur_records_kernel<<<blocks_for(count), kThreads, 0, s>>>(parts, part_count, shutter, mask, g_src, n_src, g_dst,
-                                                              n_dst, count);
+                                uint32_t count, uint32_t n_nodes, cudaStream_t s) {
+  if (!n_nodes || !mask) return cudaSuccess;
+  blur_records_kernel<<<blocks_for(n_nodes), kThreads, 0, s>>>(parts, part_count, shutter, mask, g_src, n_src, g_dst,
+                                                                n_dst, count, n_nodes);
   return cudaGetLastError();
 }
 
 cudaError_t launch_lsm_splat(const LightMapParams& L, const sl_gaussian* gs, const sl_node* nodes,
-                             const sl_part* parts, uint32_t count, uint32_t* acc, cudaStream_t s) {
-  if (!count) return cudaSuccess;
-  lsm_splat_kernel<<<blocks_for(count), kThreads, 0, s>>>(L, gs, nodes, parts, count, acc);
+                             const sl_part* parts, uint32_t count, const BlurCut& bc, uint32_t* acc, cudaStream_t s) {
+  const uint32_t n_rec = bc.k > 0.0f && bc.n_nodes > count ? bc.n_nodes : count;
+  if (!n_rec) return cudaSuccess;
+  lsm_splat_kernel<<<blocks_for(n_rec), kThreads, 0, s>>>(L, gs, nodes, parts, count, bc, n_rec, acc);
   return cudaGetLastError();
 }
 
@@ -673,9 +776,10 @@ cudaError_t launch_lsm_lookup(const LightMapParams& L, const sl_gaussian* gs, co
 }
 
 cudaError_t launch_sm_splat(const SunParams& SP, const SunLayer* layers, const sl_gaussian* gs, const sl_node* nodes,
-                            const sl_part* parts, uint32_t count, uint32_t* acc, cudaStream_t s) {
-  if (!count) return cudaSuccess;
-  sm_splat_kernel<<<blocks_for(count), kThreads, 0, s>>>(SP, layers, gs, nodes, parts, count, acc);
+                            const sl_part* parts, uint32_t count, const BlurCut& bc, uint32_t* acc, cudaStream_t s) {
+  const uint32_t n_rec = bc.k > 0.0f && bc.n_nodes > count ? bc.n_nodes : count;
+  if (!n_rec) return cudaSuccess;
+  sm_splat_kernel<<<blocks_for(n_rec), kThreads, 0, s>>>(SP, layers, gs, nodes, parts, count, bc, n_rec, acc);
   return cudaGetLastError();
 }
 

@@ -15,6 +15,17 @@ struct LightMapParams {
   uint32_t level_off[16];
 };
 
+// The motion-blur cut of the opacity-map splats (light_shadow.wgsl:158-210, sun_map.wgsl:119-153): a moving part
+// splats the nodes of its tree about k x its smear across (radius <= k |d| < the parent's), each keeping its rest
+// coverage; still parts splat their leaves.  k = 0 (or no tree): leaves only, as stretched by blur_records.
+struct BlurCut {
+  const sl_gaussian* g_rest;  // the rest records (receivers' shapes, the cut's coverage reference)
+  const sl_node* n_rest;      // n_nodes rest nodes: the leaves, then the tree's internal nodes
+  const uint32_t* parent;     // n_nodes parents (0xFFFFFFFF for roots)
+  uint32_t n_nodes;
+  float k, shutter;
+};
+
 struct EnvLightDev {
   float dir[3];
   float std;
@@ -66,14 +77,14 @@ cudaError_t launch_bshade(const BatchView* views, const BatchScene* scenes, cons
                           uint32_t* view_maxrad, int variant, cudaStream_t s);
 
 cudaError_t upload_iso_dirs(const float* dirs128x4, cudaStream_t s);
-// motion_blur.wgsl blur_records over the leaves of the parts in `mask`: g_dst / n_dst receive each leaf stretched
-// along its part's motion (flags bit 1, shutter > 0) or its rest record.
+// motion_blur.wgsl blur_records over the records (count leaves, then tree nodes up to n_nodes) of the parts in
+// `mask`: g_dst / n_dst receive each stretched along its part's motion (flags bit 1, shutter > 0) or its rest record.
 cudaError_t launch_blur_records(const sl_part* parts, uint32_t part_count, float shutter, uint32_t mask,
                                 const sl_gaussian* g_src, const sl_node* n_src, sl_gaussian* g_dst, sl_node* n_dst,
-                                uint32_t count, cudaStream_t s);
+                                uint32_t count, uint32_t n_nodes, cudaStream_t s);
 cudaError_t launch_iso(const sl_gaussian* gs, sl_node* nodes, const sl_vgrid* vgrid, uint32_t count, cudaStream_t s);
 cudaError_t launch_lsm_splat(const LightMapParams& L, const sl_gaussian* gs, const sl_node* nodes,
-                             const sl_part* parts, uint32_t count, uint32_t* acc, cudaStream_t s);
+                             const sl_part* parts, uint32_t count, const BlurCut& bc, uint32_t* acc, cudaStream_t s);
 cudaError_t launch_resolve(const uint32_t* acc, float fix, uint32_t texels, uint32_t layers, uint32_t layer_texels,
                            const uint32_t* dirty_layers, float4* mip, cudaStream_t s);
 cudaError_t launch_mips(float4* mip, uint32_t res, uint32_t levels, const uint32_t* level_off, uint32_t layers,
@@ -81,7 +92,7 @@ cudaError_t launch_mips(float4* mip, uint32_t res, uint32_t levels, const uint32
 cudaError_t launch_lsm_lookup(const LightMapParams& L, const sl_gaussian* gs, const sl_part* parts, uint32_t count,
                               const float4* mip, float* lamp_T, cudaStream_t s);
 cudaError_t launch_sm_splat(const SunParams& SP, const SunLayer* layers, const sl_gaussian* gs, const sl_node* nodes,
-                            const sl_part* parts, uint32_t count, uint32_t* acc, cudaStream_t s);
+                            const sl_part* parts, uint32_t count, const BlurCut& bc, uint32_t* acc, cudaStream_t s);
 cudaError_t launch_sm_lookup(const SunParams& SP, const SunLayer* layers, const sl_gaussian* gs, const sl_part* parts,
                              uint32_t count, const float4* mip, float4* env_T, cudaStream_t s);
 cudaError_t launch_shade(const ShadeParams& SH, const sl_gaussian* gs, const sl_node* nodes, const sl_vgrid* vgrid,

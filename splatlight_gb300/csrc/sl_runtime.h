@@ -128,10 +128,13 @@ struct sl_lighting {
   bool sm_dirty_all = true;
   bool lamp_filled = false, env_filled = false;
   // motion blur for the lighting (motion_blur.wgsl, lighting.js:468-507): the opacity-map splats draw these copies
-  float blur_shutter = 0.0f;
+  float blur_shutter = 0.0f, cut_k = 1.0f;
   bool blur_init = false;
   uint32_t blur_prev = 0;  // the parts that moved in the previous update (their copies go back to rest)
   sl::DevBuf g_blur, n_blur;
+  // the scene's tree for the motion-blur cut (leaves then internal nodes) and every node's parent
+  uint32_t n_tree = 0;
+  sl::DevBuf tree_nodes, node_parent;
 };
 
 namespace sl {

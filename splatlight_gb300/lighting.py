@@ -70,9 +70,17 @@ class Lighting:
                     asg: bool = True) -> None:
         N.check(self._lib.sl_lighting_set_options(self._h, shadow_res, sun_res, mode, theta, 1 if asg else 0))
 
-    def set_blur(self, shutter: float) -> None:
-        """Motion blur for the lighting: moving parts' records drawn stretched into the opacity maps (0 = off)."""
-        N.check(self._lib.sl_lighting_set_blur(self._h, C.c_float(shutter)))
+    def set_blur(self, shutter: float, cut_k: float = 1.0) -> None:
+        """Motion blur for the lighting: moving parts' records drawn stretched into the opacity maps (shutter 0 =
+        off); with a tree (set_tree) and cut_k > 0 a moving part splats the cut of its tree sized to its smear."""
+        N.check(self._lib.sl_lighting_set_blur(self._h, C.c_float(shutter), C.c_float(cut_k)))
+
+    def set_tree(self, nodes, kids) -> None:
+        """The scene's tree (leaves then internal nodes, NODE records; kids the children lists) for the blur cut."""
+        nd = np.ascontiguousarray(nodes, dtype=NODE)
+        k = np.ascontiguousarray(kids, dtype=np.uint32)
+        N.check(self._lib.sl_lighting_set_tree(self._h, nd.ctypes.data, len(nd), k.ctypes.data if len(k) else None,
+                                               len(k)))
 
     def update(self, eye, forward=None, moved_mask: int = 0, stream=None) -> None:
         e = (C.c_float * 3)(*[float(v) for v in eye])

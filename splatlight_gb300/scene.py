@@ -189,6 +189,11 @@ def lod_tree(g: np.ndarray, parts: np.ndarray):
     mass[:G] = g["kappa"].astype(np.float64) * np.sqrt(np.linalg.det(cov[:G]))
     rad[:G] = leaves["radius"]
     part_of[:G] = g["part_surface"] & 0xFFFF
+    # the SGGX S-hat of an internal node: its children's, mass-weighted (the shadow splats of the motion-blur cut read
+    # it; the reference's asset trees carry one baked by a tool outside the reference)
+    sn = np.zeros((cap, 6))
+    sn[:G, :3] = leaves["sn_diag"]
+    sn[:G, 3:] = leaves["sn_off"]
     kids_a, kids_b = [], []
     next_id = G
     parts = parts.copy()
@@ -213,6 +218,7 @@ def lod_tree(g: np.ndarray, parts: np.ndarray):
             rad[ids] = np.maximum(np.linalg.norm(da, axis=1) + rad[a], np.linalg.norm(db, axis=1) + rad[b])
             mass[ids] = m
             mean[ids] = mu_n
+            sn[ids] = (ma[:, None] * sn[a] + mb[:, None] * sn[b]) / m[:, None]
             part_of[ids] = p
             kids_a.append(a)
             kids_b.append(b)
@@ -232,6 +238,8 @@ def lod_tree(g: np.ndarray, parts: np.ndarray):
         nodes["kappa"][G:] = mass[G:N] / np.sqrt(np.linalg.det(c_i))
         nodes["smax"][G:] = np.sqrt(np.linalg.eigvalsh(c_i)[:, 2])
         nodes["part"][G:] = part_of[G:N]
+        nodes["sn_diag"][G:] = sn[G:N, :3]
+        nodes["sn_off"][G:] = sn[G:N, 3:]
         k = np.arange(n_int, dtype=np.uint32)
         nodes["child_lo"][G:] = 2 * k
         nodes["child_hi"][G:] = 2 * k + 2

@@ -85,18 +85,25 @@ def test_update_after_moving_a_part(cuda, orc):
     assert np.allclose(col, ocol, rtol=1e-3, atol=1e-5)
 
 
-@pytest.mark.parametrize("which", ["cornell", "hill"])
-def test_motion_blur_in_the_lighting(cuda, orc, which):
+@pytest.mark.parametrize("which,cut", [("cornell", 0.0), ("hill", 0.0), ("cornell", 1.0), ("hill", 1.0)])
+def test_motion_blur_in_the_lighting(cuda, orc, which, cut):
     """motion_blur.wgsl blur_records: a moving part (flags bit 1, xf_prev behind xf) draws stretched records into the
     opacity maps (light map A on the Cornell room, the sun maps on the hill) while every receiver keeps its rest
-    record: lamp and env transmittance within 1e-5 of the restatement with the same blur, measurably unlike the
-    unblurred maps, and the lit frame within 1e-3; back to the unblurred maps once the part stops."""
+    record; with the scene's tree and cut factor 1 (the reference's default ?blurcut) the moving part splats the cut of
+    its tree sized to its smear, each node keeping its rest coverage.  Lamp and env transmittance within 1e-5 of the
+    restatement with the same blur, measurably unlike the unblurred maps, and the lit frame within 1e-3; back to the
+    unblurred maps once the part stops."""
     if which == "cornell":
         s = scene.subset(scene.cornell(), 20000)
         moving, shift = 5, (0.25, 0.0, 0.1)
     else:
         s = scene.dataclasses.replace(scene.subset(scene.hill(), 150000), shadow_res=512, sun_res=1024)
         moving, shift = 2, (0.6, 0.3, 0.0)        # the canopy
+    tree = None
+    if cut > 0.0:
+        nodes, kids, rooted = scene.lod_tree(s.gaussians, s.parts)
+        s = scene.dataclasses.replace(s, parts=rooted)
+        tree = (nodes, kids)
     parts = s.parts.copy()
     parts["xf_prev"][moving] = parts["xf"][moving]
     for k, v in zip((3, 7, 11), shift):
@@ -107,12 +114,14 @@ def test_motion_blur_in_the_lighting(cuda, orc, which):
     with SplatRenderer(s.gaussians, s.parts) as r:
         L = for_scene(r, s)
         L.set_options(shadow_res=s.shadow_res, sun_res=s.sun_res)
-        L.set_blur(0.5)
+        if tree is not None:
+            L.set_tree(*tree)
+        L.set_blur(0.5, cut)
         L.update(s.eye, fwd)
         r.write_parts(parts)
         L.update(s.eye, fwd, moved_mask=1 << moving)
         col, lt, et, _ = L.read()
-        ocol, olt, oet, _ = orc.lighting(s2, threads=16, blur_shutter=0.5)
+        ocol, olt, oet, _ = orc.lighting(s2, threads=16, blur_shutter=0.5, tree=tree, cut_k=cut)
         assert np.allclose(lt, olt, rtol=1e-5, atol=1e-6), np.abs(lt - olt).max()
         assert np.allclose(et, oet, rtol=1e-5, atol=1e-6), np.abs(et - oet).max()
         assert np.allclose(col, ocol, rtol=1e-3, atol=1e-5)
@@ -131,6 +140,7 @@ def test_motion_blur_in_the_lighting(cuda, orc, which):
         r.write_parts(parts2)
         L.update(s.eye, fwd, moved_mask=0)
         _, lt2, et2, _ = L.read()
-        _, olt2, oet2, _ = orc.lighting(scene.dataclasses.replace(s, parts=parts2), threads=16, blur_shutter=0.5)
+        _, olt2, oet2, _ = orc.lighting(scene.dataclasses.replace(s, parts=parts2), threads=16, blur_shutter=0.5,
+                                        tree=tree, cut_k=cut)
         assert np.allclose(lt2, olt2, rtol=1e-5, atol=1e-6) and np.allclose(et2, oet2, rtol=1e-5, atol=1e-6)
         L.close()
