@@ -391,8 +391,8 @@ __global__ void __launch_bounds__(kThreads) dcomposite_bwd_kernel(const uint2* _
 }
 
 // Per-Gaussian chain rule from the 2D gradients to the parameters (and the lights' intensities).
-// Two blocks per SM (at most 128 registers): the lighting Jacobian's dual passes are latency-bound, and twice the
-// resident warps (with some spilling) measured 13.6 ms per step against 15.6 ms at one block of 247 registers.
+// Two blocks per SM (at most 128 registers): the lighting's walk is latency-bound, and twice the resident warps
+// (with some spilling) measured 13.6 ms per step against 15.6 ms at one block of 247 registers.
 __global__ void __launch_bounds__(kThreads, 2) dproject_bwd_kernel(const DiffCamera K, const DiffParams P,
                                                                 const DiffLights Lt, uint32_t n,
                                                                 const DiffGrad2D* __restrict__ g2,
@@ -505,38 +505,18 @@ __global__ void __launch_bounds__(kThreads, 2) dproject_bwd_kernel(const DiffCam
     const float q40[4] = {pq[0], pq[1], pq[2], pq[3]}, rough0 = P.roughness[i];
     const dsh::V3<float> eyef = dsh::v3(K.eye[0], K.eye[1], K.eye[2]);
     float dlit[12];
-    // position directions: the shape and material stay plain floats
-#pragma unroll 1
-    for (int p = 0; p < 3; p++) {
-      dsh::Dual mu[3];
-      for (int k = 0; k < 3; k++) mu[k] = dsh::Dual{mu0[k], p == k ? 1.0f : 0.0f};
-      const dsh::Recv<dsh::Dual, float> rv = dsh::receiver<dsh::Dual, float>(mu, ls0, q40, logit, rough0);
-      const dsh::V3<dsh::Dual> acc =
-          dsh::emitter_light(Lt.tree, rv, vg, Lt.ks, iso, eyef, [](uint32_t, auto, auto, auto) {});
-      dlit[p] = ga.x * acc.x.d + ga.y * acc.y.d + ga.z * acc.z.d;
-    }
-    // shape and material directions (log-scales 3, quaternion 4, opacity logit, roughness): the position, and with it
-    // every light direction, distance, V-grid lookup and light intensity, stays a plain float
-#pragma unroll 1
-    for (int p = 3; p < 12; p++) {
-      dsh::Dual ls[3], q4[4];
-      for (int k = 0; k < 3; k++) ls[k] = dsh::Dual{ls0[k], p == 3 + k ? 1.0f : 0.0f};
-      for (int k = 0; k < 4; k++) q4[k] = dsh::Dual{q40[k], p == 6 + k ? 1.0f : 0.0f};
-      const dsh::Dual lg{logit, p == 10 ? 1.0f : 0.0f}, rg{rough0, p == 11 ? 1.0f : 0.0f};
-      const dsh::Recv<float, dsh::Dual> rv = dsh::receiver<float, dsh::Dual>(mu0, ls, q4, lg, rg);
-      const dsh::V3<dsh::Dual> acc =
-          dsh::emitter_light(Lt.tree, rv, vg, Lt.ks, iso, eyef, [](uint32_t, auto, auto, auto) {});
-      dlit[p] = ga.x * acc.x.d + ga.y * acc.y.d + ga.z * acc.z.d;
-    }
-    // the value pass: albedo's gradient, and the light intensities' through the tree's derivative table (per cut node
-    // e and light k: dI_e/ds_k = dLe_e/ds_k scale |w|_M + Le_e scale (w^T dM_e/ds_k w) / (2 |w|_M))
+    // one walk of the cut in reverse mode: the adjoint of ga . acc with respect to the position and every receiver field,
+    // and (the visitor) the light intensities' gradient through the tree's derivative table (per cut node e and light
+    // k: dI_e/ds_k = dLe_e/ds_k scale |w|_M + Le_e scale (w^T dM_e/ds_k w) / (2 |w|_M)); acc0 gives albedo's gradient
+    dsh::RecvAdj ra;
     dsh::V3<float> acc0;
     {
       const dsh::Recv<float, float> rv = dsh::receiver<float, float>(mu0, ls0, q40, logit, rough0);
       const uint32_t nl = Lt.n;
       const float scale = Lt.tree.scale;
-      acc0 = dsh::emitter_light(
-          Lt.tree, rv, vg, Lt.ks, iso, eyef, [&](uint32_t node, float fe, dsh::V3<float> mw, float mq) {
+      acc0 = dsh::emitter_light_adj(
+          Lt.tree, rv, vg, Lt.ks, iso, eyef, dsh::v3(ga.x, ga.y, ga.z), ra,
+          [&](uint32_t node, float fe, dsh::V3<float> mw, float mq) {
             if (!Lt.dtab || !(mq > 0.0f) || node >= 2u * nl - 1u) return;  // (2 nl - 1 nodes in the table)
             const float* e = Lt.tree.nodes + 24u * node;
             for (uint32_t k = 0; k < nl; k++) {
@@ -550,6 +530,23 @@ __global__ void __launch_bounds__(kThreads, 2) dproject_bwd_kernel(const DiffCam
               if (v != 0.0f) atomicAdd(&s_lg[k], v);
             }
           });
+    }
+    dlit[0] = ra.P.x;
+    dlit[1] = ra.P.y;
+    dlit[2] = ra.P.z;
+    // the receiver's fields against the shape and material parameters (log-scales 3, quaternion 4, opacity logit,
+    // roughness), each in forward mode without a walk, dotted with the fields' adjoints
+#pragma unroll 1
+    for (int p = 3; p < 12; p++) {
+      dsh::Dual ls[3], q4[4];
+      for (int k = 0; k < 3; k++) ls[k] = dsh::Dual{ls0[k], p == 3 + k ? 1.0f : 0.0f};
+      for (int k = 0; k < 4; k++) q4[k] = dsh::Dual{q40[k], p == 6 + k ? 1.0f : 0.0f};
+      const dsh::Dual lg{logit, p == 10 ? 1.0f : 0.0f}, rg{rough0, p == 11 ? 1.0f : 0.0f};
+      const dsh::Recv<float, dsh::Dual> rv = dsh::receiver<float, dsh::Dual>(mu0, ls, q4, lg, rg);
+      auto dd = [](dsh::V3<float> g, dsh::V3<dsh::Dual> f) { return g.x * f.x.d + g.y * f.y.d + g.z * f.z.d; };
+      dlit[p] = dd(ra.n, rv.n) + dd(ra.cinv_d, rv.cinv_d) + dd(ra.cinv_o, rv.cinv_o) + dd(ra.sn_d, rv.sn_d) +
+                dd(ra.sn_o, rv.sn_o) + dd(ra.Sd, rv.Sd) + dd(ra.So, rv.So) + ra.kappa * rv.kappa.d +
+                ra.detC * rv.detC.d;
     }
     const F3 dalb = f3(gc.x * (acc0.x * kk + Lt.ambient), gc.y * (acc0.y * kk + Lt.ambient),
                        gc.z * (acc0.z * kk + Lt.ambient));
