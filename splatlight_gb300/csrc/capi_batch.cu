@@ -198,7 +198,7 @@ cudaError_t enqueue(sl_batch* b, cudaStream_t s) {
   CK(stage(5));
   CK(launch_bcomposite(C, b->ranges.as<uint2>(), b->tile_vals.as<uint32_t>(), b->recs.as<SplatRec>(),
                        b->views_out.as<BatchViewOut>(), b->view_maxrad.as<uint32_t>(), b->dyn.as<BatchDyn>(), T, ctr,
-                       b->variant[3], s));
+                       b->marks.as<uint8_t>(), b->variant[3], s));
   CK(stage(6));
   CK(cudaMemcpyAsync(b->h_ctr, ctr, sizeof(FrameCounters), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(b->h_visible, b->view_visible.ptr, 4ull * V, cudaMemcpyDeviceToHost, s));

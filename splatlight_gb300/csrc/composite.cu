@@ -74,7 +74,8 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
                                                uint32_t e, const uint32_t* __restrict__ tile_vals,
                                                const SplatRec* __restrict__ recs, uint32_t count_mode, float t_stop,
                                                FrameCounters* ctr, float4* __restrict__ out,
-                                               uint32_t* __restrict__ counts, uint8_t* __restrict__ marks = nullptr) {
+                                               uint32_t* __restrict__ counts, uint8_t* __restrict__ marks = nullptr,
+                                               const uint8_t* __restrict__ keep = nullptr) {
   constexpr int TH = kThreads / TW;
   constexpr int BX = TW / 8;  // warp blocks of 8 x 4 pixels per tile row
   constexpr int BY = TH / 4;
@@ -124,16 +125,25 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
   bool alive = inside;
   bool timed_out = false;
 
-  // gather batch b (entries [max(s, e-256(b+1)), e-256b), nearest first) into buf[b & 1]
+  // gather batch b (entries [max(s, e-256(b+1)), e-256b), nearest first) into buf[b & 1]; with keep (a lit view of the
+  // batched path: the coverage pass's marks), a record whose splat blends no fragment anywhere is neither copied nor
+  // culled (bit b & 1 of dropped, for the thread's own record)
+  uint32_t dropped = 0;
   auto issue = [&](uint32_t b) {
     const uint32_t hi = e - kThreads * b;
     const uint32_t lo = (hi - s) > (uint32_t)kThreads ? hi - kThreads : s;
     const uint32_t bar = (b & 1u) ? bar1 : bar0;
+    dropped &= ~(1u << (b & 1u));
     if ((uint32_t)t < hi - lo) {
       const uint32_t slot = tile_vals[hi - 1u - (uint32_t)t];
       if constexpr (kMark) sslot[b & 1u][t] = slot;
-      mbar_arrive_expect(bar, kRecBytes);
-      bulk_copy_g2s(smem_addr(&buf[b & 1u][t]), recs + slot, kRecBytes, bar);
+      if (keep && keep[slot] == 0u) {
+        dropped |= 1u << (b & 1u);
+        mbar_arrive(bar);
+      } else {
+        mbar_arrive_expect(bar, kRecBytes);
+        bulk_copy_g2s(smem_addr(&buf[b & 1u][t]), recs + slot, kRecBytes, bar);
+      }
     } else {
       mbar_arrive(bar);
     }
@@ -152,7 +162,7 @@ __device__ __forceinline__ void composite_tile(uint32_t x0, uint32_t y0, uint32_
     // (one pixel of margin included, rounded up); block (bx, by) holds pixel centres x0 + 8bx + [0.5, 7.5],
     // y0 + 4by + [0.5, 3.5].
     uint32_t bits = 0;
-    if ((uint32_t)t < nb) {
+    if ((uint32_t)t < nb && !((dropped >> (b & 1u)) & 1u)) {
       const float4 A = rb[t].a;
       const float hb = rb[t].b.z;
       const __half2 hxy = *reinterpret_cast<const __half2*>(&hb);
@@ -299,7 +309,8 @@ __global__ void __launch_bounds__(kThreads, MinB) bcomposite_kernel(const BatchC
                                                               const SplatRec* __restrict__ recs,
                                                               const BatchViewOut* __restrict__ views,
                                                               const uint32_t* __restrict__ view_maxrad,
-                                                              const BatchDyn* __restrict__ dyn, FrameCounters* ctr) {
+                                                              const BatchDyn* __restrict__ dyn, FrameCounters* ctr,
+                                                              const uint8_t* __restrict__ marks) {
   constexpr int TH = kThreads / TW;
   const uint32_t tile = blockIdx.x;
   if (tile >= dyn->total_tiles) return;  // grid sized for the capacity
@@ -315,8 +326,10 @@ __global__ void __launch_bounds__(kThreads, MinB) bcomposite_kernel(const BatchC
   const uint2 rg = ranges[tile];
   const float maxrad = fmaxf(__uint_as_float(view_maxrad[lo]), 1.0f);
   const float t_stop = v.count_mode ? -1.0f : B.t_stop_scale / maxrad;
+  // a lit view blends only splats the coverage pass marked (its cut is conservative: an unmarked splat blends no
+  // fragment before T < t_stop), so the rest of its list is skipped
   composite_tile<TW>(tx * TW, ty * TH, v.width, v.height, rg.x, rg.y, tile_vals, recs, v.count_mode, t_stop, ctr,
-                     out + v.out_offset, nullptr);
+                     out + v.out_offset, nullptr, nullptr, v.lit ? marks : nullptr);
 }
 
 // The batched coverage pass over the tiles of lit views (see composite_tile): mode 1 stops each pixel at the view's
@@ -400,14 +413,14 @@ cudaError_t launch_composite(const CompositeParams& P, const uint2* ranges, cons
 namespace sl {
 cudaError_t launch_bcomposite(const BatchComposite& B, const uint2* ranges, const uint32_t* tile_vals,
                               const SplatRec* recs, const BatchViewOut* views, const uint32_t* view_maxrad,
-                              const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, int variant,
-                              cudaStream_t s) {
+                              const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, const uint8_t* marks,
+                              int variant, cudaStream_t s) {
   if (max_tiles == 0) return cudaSuccess;
   const int mb = kTuneMinBlocks[3][variant];
   if (mb != 5 && mb != 6) return cudaErrorInvalidValue;
 #define SL_BCOMP(TW, MB)                                                                                        \
   bcomposite_kernel<TW, MB><<<max_tiles, kThreads, 0, s>>>(B, ranges, tile_vals, recs, views, view_maxrad, dyn, \
-                                                           ctr)
+                                                           ctr, marks)
   switch (B.tile_w) {
     case 16:
       if (mb == 6) SL_BCOMP(16, 6); else SL_BCOMP(16, 5);

@@ -240,8 +240,8 @@ struct BatchDyn {
 };
 cudaError_t launch_bcomposite(const BatchComposite& B, const uint2* ranges, const uint32_t* tile_vals,
                               const SplatRec* recs, const BatchViewOut* views, const uint32_t* view_maxrad,
-                              const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, int variant,
-                              cudaStream_t s);
+                              const BatchDyn* dyn, uint32_t max_tiles, FrameCounters* ctr, const uint8_t* marks,
+                              int variant, cudaStream_t s);
 // batch.cu (totals: the BatchDyn, read as u32 words: [0] total slots, [1] total tiles)
 // batch.cu: the batch's tile entries in one pass (counts, their ordered offsets by a decoupled look-back, emission);
 // the entry total goes to ctr->entries.  scratch: btile_bin_scratch_bytes(n_max) bytes, cleared by the launcher.
