@@ -252,7 +252,7 @@ SL_API int sl_emitter_tree(const sl_gaussian* emitters, uint32_t n, const double
                            float* dtab_out, uint32_t* root);
 
 /* Environment.set / write (src/environment.js:106-153): up to 4 distant lights; sky_ambient adds albedo * sky_ambient
- * to every non-emissive Gaussian (a constant stand-in for the probe-bounce sky, which is outside this pipeline). */
+ * to every non-emissive Gaussian (a constant stand-in for sky light where the probe bounce is not set; 0 with it). */
 SL_API int sl_lighting_set_environment(sl_lighting* l, const sl_env_light* lights, uint32_t n, float sky_ambient);
 
 /* Resolution of the emitter light's per-part opacity map (src/light_shadow.js:18, default 512) and of the sun's maps
@@ -271,11 +271,47 @@ SL_API int sl_lighting_set_options(sl_lighting* l, uint32_t shadow_res, uint32_t
  * sun_map.wgsl:119-153), each keeping its rest coverage; cut_k 0 (or no tree) stretches every leaf.  shutter 0 (the
  * default here) turns it off.  The maps re-splat at the next update. */
 SL_API int sl_lighting_set_blur(sl_lighting* l, float shutter, float cut_k);
-/* The scene's tree for the motion-blur cut (src/lighting.js initNodeParents, :557-567): n_nodes records, the leaves
+/* The scene's tree for the motion-blur cut and the probe gather (src/lighting.js initNodeParents, :557-567): n_nodes
+ * records, the leaves
  * (the renderer's Gaussians, in order) then the internal nodes, whose children are kids[child_lo .. child_hi); the
  * parts' roots come from the renderer's parts (sl_part.root).  Host arrays, copied. */
 SL_API int sl_lighting_set_tree(sl_lighting* l, const sl_node* nodes, uint32_t n_nodes, const uint32_t* kids,
                                 uint32_t n_kids);
+
+/* The probe lattice of the bounce (src/lighting.js probeLayout :220-286; runtime/wgsl/bounce.wgsl ProbeParams :23-56):
+ * dims[0] x dims[1] columns at lo.xy + step.xy (i, j), each with dims[2] probes at ground[i dims[1] + j] + levels[k].
+ * The room layout (terrain 0): ground 0, levels lo.z + k step.z; the terrain layout (terrain 1): ground heights per
+ * column, levels above them, step.z 0. */
+typedef struct sl_probe_layout {
+  uint32_t dims[3];     /* x, y columns (2 .. 1024 columns in all) and levels (2 .. 16) */
+  uint32_t terrain;
+  float lo[3];
+  float step[3];
+  float levels[16];     /* ascending */
+  const float* ground;  /* dims[0] x dims[1] heights, or NULL (0); copied */
+  float tmax;           /* probe ray length: TMAX 6 m, or the scene's diagonal with an environment (lighting.js:226) */
+} sl_probe_layout;
+
+/* Lighting.initBounce (src/lighting.js:723-816) without the sender cut (?sendercut=0): after each update's shading the
+ * probe bounce runs one frame (encodeBounce :1018-1103; runtime/wgsl/bounce.wgsl, M39 stage 2): the Gaussians'
+ * transfer SH2 (iso_xfer, on the first frame and near parts that moved), their light toward the probes for a quarter
+ * of them (direct_dirs_emit + env_dirs), the tree's sums of it and their SH2 (node_leaf, node_up over depths
+ * max_depth - 1 .. 1 (0: the tree's depth), node_sh2), the probes' gather through every part's tree with the sky
+ * beyond (probe_gather), their validity and SH2 (probe_valid, probe_sh2), then each Gaussian's bounce from its 8
+ * probes (bounce_sh, gloss_sh) into lo_b, which the projection adds to the lit colour times the frame's bounce gain
+ * (palette[3].x).  blend: the history weight of each gather after the first (1: taken as is, the reference's default;
+ * 0.5: ?probeblend=ema).  Needs sl_lighting_set_tree.  Every Gaussian reads the lattice: the probes that ride on
+ * movable parts and static probe volumes are not built, nor bounce_dirs (near-mirror materials, flake lobe below
+ * 0.1 rad, take no bounce); near-field visibility is off, as the reference's default. */
+SL_API int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* layout, uint32_t max_depth, float blend);
+/* The environment's sky for the probes (src/environment.js:116-124; bounce.wgsl sky_radiance :148-160): n_coef (<= 16)
+ * real SH coefficients, rgb, bands 0-3, seen by probe rays that leave the scene.  0 coefficients: no sky. */
+SL_API int sl_lighting_set_sky(sl_lighting* l, const float* sh_rgb, uint32_t n_coef);
+/* Debug read-back of the bounce (synchronous; bytes from the start): what = 0 lo_b (3 float4 per Gaussian: toward
+ * the eye, toward the probes, lanes), 1 lo_dir (float4 per Gaussian), 2 the transfer (3 float4 per Gaussian), 3 the
+ * probes' SH2 (9 float4 per probe), 4 probe_data (2 float4 per probe and cell), 5 node_sh (14 words per node),
+ * 6 node_acc (14 float4 per node). */
+SL_API int sl_lighting_read_bounce(sl_lighting* l, uint32_t what, void* dst, size_t bytes);
 
 /* encode(encoder, eye, timers, changed, still) (src/lighting.js:1258-1274) + Environment.encodeDirect
  * (src/environment.js:181-189): iso_init on first use, the opacity maps of moved parts (moved_mask bit p) or of

@@ -459,3 +459,137 @@ def render_given_order(gaussians, parts, frame, order, emitters=None, colour=Non
     L.orc_composite(splats.ctypes.data, o.ctypes.data, vis, W, H, rgba.ctypes.data, counts.ctypes.data, threads)
     return {"keys": keys, "ranges": ranges, "entries": entries[:total], "rgba": rgba, "counts": counts,
             "visible": vis}
+
+
+class ProbeLayoutC(C.Structure):
+    _fields_ = [("dims", C.c_uint32 * 3), ("terrain", C.c_uint32), ("lo", C.c_float * 3), ("step", C.c_float * 3),
+                ("levels", C.c_float * 16), ("ground", C.c_void_p), ("tmax", C.c_float)]
+
+
+class BounceIn(C.Structure):
+    _fields_ = [("gs", C.c_void_p), ("count", C.c_uint32), ("parts", C.c_void_p), ("part_count", C.c_uint32),
+                ("nodes", C.c_void_p), ("n_nodes", C.c_uint32), ("kids", C.c_void_p), ("vgrid", C.c_void_p),
+                ("mats", C.c_void_p), ("mat_count", C.c_uint32), ("tree", C.c_void_p), ("tree_root", C.c_uint32),
+                ("n_emit", C.c_uint32), ("emit_mode", C.c_uint32), ("one_sided", C.c_uint32),
+                ("emit_theta", C.c_float), ("emit_scale", C.c_float), ("edge_soft", C.c_float),
+                ("normal", C.c_float * 3), ("lamp_T", C.c_void_p), ("env_T", C.c_void_p), ("lights", C.c_void_p),
+                ("n_lights", C.c_uint32), ("sky_sh", C.c_void_p), ("lay", ProbeLayoutC), ("max_depth", C.c_uint32),
+                ("eye", C.c_float * 3), ("alpha", C.c_float), ("frame", C.c_uint32), ("force", C.c_uint32),
+                ("moved_mask", C.c_uint32)]
+
+
+class BounceState(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("probe_data", "probe_sh", "xfer", "lo_dir", "lo_b", "node_acc", "node_sh")]
+
+
+def bounce_tables():
+    """(D14 (14, 3), pinv (9, 14)) restated."""
+    L = lib()
+    L.orc_bounce_tables.restype = None
+    L.orc_bounce_tables.argtypes = [C.c_void_p, C.c_void_p]
+    d = np.zeros((14, 3), np.float32)
+    p = np.zeros((9, 14), np.float32)
+    L.orc_bounce_tables(d.ctypes.data, p.ctypes.data)
+    return d, p
+
+
+def f32_to_f16(x: np.ndarray) -> np.ndarray:
+    """The restatement's round-to-nearest-even f32 -> f16 bits, elementwise."""
+    L = lib()
+    L.orc_f32_to_f16.restype = C.c_uint32
+    L.orc_f32_to_f16.argtypes = [C.c_float]
+    return np.array([L.orc_f32_to_f16(float(v)) for v in np.asarray(x, np.float32).ravel()], np.uint32)
+
+
+class Bounce:
+    """The probe bounce restated (sl_oracle_light.c orc_bounce_frame), stateful over frames.  scene: a Scene whose
+    parts carry their tree roots; tree = (nodes, kids) (the leaves, then the internal nodes); lit = the (colour,
+    lamp_T, env_T, nodes) of oracle.lighting on the scene (the leaves' iso_norm and the maps' transmittance);
+    layout: a probes.* layout dict; sky_sh: (16, 3) or None."""
+
+    def __init__(self, scene, tree, lit, layout, sky_sh=None, max_depth: int = 0, blend: float = 1.0):
+        self.scene = scene
+        G = scene.count
+        tn = np.ascontiguousarray(tree[0]).copy()
+        tn["pad0"][:G] = lit[3]["pad0"]
+        tn["pad1"][:G] = lit[3]["pad1"]
+        self.nodes = tn
+        self.kids = np.ascontiguousarray(tree[1], np.uint32)
+        if max_depth == 0:
+            max_depth = int(tn["depth"][G:].max()) + 1 if len(tn) > G else 1
+        self.max_depth = max_depth
+        self.blend = blend
+        self.lamp_T = np.ascontiguousarray(lit[1], np.float32)
+        self.env_T = np.ascontiguousarray(lit[2], np.float32)
+        rec = np.ascontiguousarray(scene.emitters).view(np.float32).reshape(-1, 16).copy()
+        if len(rec):
+            self.tree, self.root, _ = emitter_tree(rec)
+        else:
+            self.tree, self.root = np.zeros((1, 24), np.float32), 0
+        self.n_emit = len(rec)
+        self.lights = (EnvLight * 4)()
+        self.n_lights = 0
+        for d, std, irr, sh in scene.distant_lights()[:4]:
+            self.lights[self.n_lights].dir[:] = list(d)
+            self.lights[self.n_lights].std = std
+            self.lights[self.n_lights].irr[:] = list(irr)
+            self.lights[self.n_lights].shadows = 1 if sh else 0
+            self.n_lights += 1
+        self.sky = None if sky_sh is None else np.ascontiguousarray(sky_sh, np.float32).reshape(16, 3)
+        self.layout = layout
+        self.ground = None if layout.get("ground") is None else np.ascontiguousarray(layout["ground"], np.float32)
+        NP = int(np.prod(layout["dims"]))
+        N = len(tn)
+        self.state = {"probe_data": np.zeros((NP, 128, 8), np.float32), "probe_sh": np.zeros((NP, 9, 4), np.float32),
+                      "xfer": np.zeros((G, 12), np.float32), "lo_dir": np.zeros((G, 4), np.float32),
+                      "lo_b": np.zeros((G, 3, 4), np.float32), "node_acc": np.zeros((N, 14, 4), np.float32),
+                      "node_sh": np.zeros((N, 14), np.uint32)}
+        self.frame = 0
+        self.first = True
+
+    def step(self, eye, moved_mask: int = 0, threads: int = 8):
+        """One frame (the GPU's sl_lighting_update after the shading); returns the state dict."""
+        L = lib()
+        L.orc_bounce_frame.restype = C.c_int
+        L.orc_bounce_frame.argtypes = [C.POINTER(BounceIn), C.POINTER(BounceState), C.c_int]
+        s = self.scene
+        g = np.ascontiguousarray(s.gaussians)
+        p = np.ascontiguousarray(s.parts)
+        vg = np.ascontiguousarray(s.vgrid)
+        m = np.ascontiguousarray(s.materials)
+        B = BounceIn()
+        B.gs, B.count = g.ctypes.data, len(g)
+        B.parts, B.part_count = p.ctypes.data, len(p)
+        B.nodes, B.n_nodes = self.nodes.ctypes.data, len(self.nodes)
+        B.kids = self.kids.ctypes.data if len(self.kids) else None
+        B.vgrid = vg.ctypes.data
+        B.mats, B.mat_count = m.ctypes.data, len(m)
+        B.tree, B.tree_root, B.n_emit = self.tree.ctypes.data, self.root, self.n_emit
+        B.emit_mode, B.emit_theta, B.emit_scale = 1, 4.0, getattr(s, "emit_scale", 1.0)
+        B.one_sided = 1 if getattr(s, "emit_one_sided", False) else 0
+        B.normal[:] = list(getattr(s, "emit_normal", (0.0, 0.0, 1.0)))
+        B.edge_soft = 0.2
+        B.lamp_T, B.env_T = self.lamp_T.ctypes.data, self.env_T.ctypes.data
+        B.lights, B.n_lights = C.addressof(self.lights), self.n_lights
+        B.sky_sh = self.sky.ctypes.data if self.sky is not None else None
+        lay = self.layout
+        B.lay.dims[:] = [int(v) for v in lay["dims"]]
+        B.lay.terrain = 1 if lay["terrain"] else 0
+        B.lay.lo[:] = [float(v) for v in lay["lo"]]
+        B.lay.step[:] = [float(v) for v in lay["step"]]
+        B.lay.levels[:] = [float(v) for v in list(lay["levels"]) + [0.0] * (16 - len(lay["levels"]))]
+        B.lay.ground = self.ground.ctypes.data if self.ground is not None else None
+        B.lay.tmax = float(lay["tmax"])
+        B.max_depth = self.max_depth
+        B.eye[:] = [float(v) for v in eye]
+        B.alpha = 1.0 if self.first else self.blend
+        B.frame = self.frame
+        B.force = 1 if self.first else 0
+        B.moved_mask = moved_mask
+        st = BounceState(**{k: v.ctypes.data for k, v in self.state.items()})
+        rc = L.orc_bounce_frame(C.byref(B), C.byref(st), threads)
+        if rc != 0:
+            raise RuntimeError(f"oracle bounce failed ({rc})")
+        self.first = False
+        self.frame += 1
+        return self.state

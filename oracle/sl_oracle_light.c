@@ -1548,3 +1548,683 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
   free(n_blur);
   return 0;
 }
+
+/* ---- probe bounce (runtime/wgsl/bounce.wgsl; host src/lighting.js:170-286, 723-816, 1018-1103) -------------------
+ * The M39 stage-2 loop of the reference's non-sender-cut path (?sendercut=0) over the probe lattice, one frame per
+ * call: iso_xfer (bounce.wgsl:993-1026), direct_dirs_emit (emissive.wgsl:1012-1016, 1066-1082) and env_dirs
+ * (environment.wgsl:311-359) for a quarter of the Gaussians, node_leaf / node_up / node_sh2 (bounce.wgsl:1166-1236),
+ * probe_gather (:1255-1410, no rectangle lamps), probe_valid (:1417-1447), probe_sh2 (:1029-1041), bounce_sh
+ * (:1044-1095, with gloss_sh :1102-1125).  Every Gaussian reads the lattice (the probes that ride on movable parts and
+ * static probe volumes are not part of this restatement); near-field visibility is off (near_byte = 1, the
+ * reference's default).  The WGSL pow(x, 3) of probe_cheb is taken as x x x. */
+
+#define BN_NCELL 128u
+#define BN_HIT_MAX 16u
+#define BN_STACK 64u
+#define BN_THETA 4.0f
+#define BN_NEAR_R 0.3f
+#define BN_G_VALID 0.95f
+#define BN_GLOSS_SH_MIN 0.1f
+
+static const double bn_d14_raw[14][3] = {{1, 0, 0}, {0, 1, 0}, {1e-4, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {1e-4, 0, -1},
+                                         {1, 1, 1}, {1, 1, -1}, {1, -1, 1}, {1, -1, -1},
+                                         {-1, 1, 1}, {-1, 1, -1}, {-1, -1, 1}, {-1, -1, -1}};
+
+/* D14 (lighting.js:188-189: 6 axes, the verticals leaning 1e-4 off the pole, then the 8 diagonals / sqrt 3) and the
+ * least-squares SH2 fit of values on them, pinv = (A^T A)^-1 A^T (lighting.js pinvD14, Gauss-Jordan), float64 */
+void orc_bounce_tables(float* d14 /* 14 x 3 */, float* pinv /* 9 x 14 */) {
+  double A[14][9], D[14][3];
+  for (int k = 0; k < 14; k++) {
+    double s = k < 6 ? 1.0 : 1.0 / sqrt(3.0);
+    for (int c = 0; c < 3; c++) D[k][c] = bn_d14_raw[k][c] * s;
+    double x = D[k][0], y = D[k][1], z = D[k][2];
+    double b[9] = {0.282095, 0.488603 * y, 0.488603 * z, 0.488603 * x, 1.092548 * x * y, 1.092548 * y * z,
+                   0.315392 * (3 * z * z - 1), 1.092548 * x * z, 0.546274 * (x * x - y * y)};
+    for (int m = 0; m < 9; m++) A[k][m] = b[m];
+    for (int c = 0; c < 3; c++) d14[3 * k + c] = (float)D[k][c];
+  }
+  double M[9][18];
+  for (int i = 0; i < 9; i++)
+    for (int j = 0; j < 9; j++) {
+      double s = 0.0;
+      for (int r = 0; r < 14; r++) s += A[r][i] * A[r][j];
+      M[i][j] = s;
+      M[i][9 + j] = i == j ? 1.0 : 0.0;
+    }
+  for (int c = 0; c < 9; c++) {
+    int piv = c;
+    for (int r = c + 1; r < 9; r++)
+      if (fabs(M[r][c]) > fabs(M[piv][c])) piv = r;
+    for (int j = 0; j < 18; j++) {
+      double t = M[c][j];
+      M[c][j] = M[piv][j];
+      M[piv][j] = t;
+    }
+    double dv = M[c][c];
+    for (int j = 0; j < 18; j++) M[c][j] /= dv;
+    for (int r = 0; r < 9; r++) {
+      if (r == c) continue;
+      double f = M[r][c];
+      for (int j = 0; j < 18; j++) M[r][j] -= f * M[c][j];
+    }
+  }
+  for (int m = 0; m < 9; m++)
+    for (int k = 0; k < 14; k++) {
+      double s = 0.0;
+      for (int j = 0; j < 9; j++) s += M[m][9 + j] * A[k][j];
+      pinv[14 * m + k] = (float)s;
+    }
+}
+
+/* f32 -> f16 bits, round to nearest even (WGSL pack2x16float) */
+uint32_t orc_f32_to_f16(float f) {
+  uint32_t x = sl_float_to_bits(f);
+  uint32_t sign = (x >> 16) & 0x8000u;
+  uint32_t ax = x & 0x7FFFFFFFu;
+  if (ax >= 0x7F800000u) return sign | (ax > 0x7F800000u ? 0x7E00u : 0x7C00u);
+  if (ax >= 0x477FF000u) return sign | 0x7C00u; /* rounds to >= 65520: infinity */
+  if (ax < 0x38800000u) {                        /* below the smallest normal half: subnormal or zero */
+    if (ax < 0x33000000u) return sign;           /* below half the smallest subnormal */
+    /* the value is m 2^(e-150) and a half subnormal step is 2^-24: the step count is m 2^(e-126) */
+    uint32_t e = ax >> 23, m = (ax & 0x7FFFFFu) | 0x800000u;
+    uint32_t shift = 126u - e;
+    uint32_t q = m >> shift, rem = m & ((1u << shift) - 1u), halfway = 1u << (shift - 1u);
+    if (rem > halfway || (rem == halfway && (q & 1u))) q++;
+    return sign | q;
+  }
+  uint32_t e = (ax >> 23) - 112u, m = ax & 0x7FFFFFu;
+  uint32_t h = (e << 10) | (m >> 13), rem = m & 0x1FFFu;
+  if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h++;
+  return sign | h;
+}
+
+static const float BN_PI = 3.14159265358979f;
+
+static f3 bn_cell_dir(const float* cells, uint32_t c) { return F3(cells[4 * c], cells[4 * c + 1], cells[4 * c + 2]); }
+static void bn_sh2(f3 d, float* b) {
+  float x = d.x, y = d.y, z = d.z;
+  b[0] = 0.282095f;
+  b[1] = 0.488603f * y;
+  b[2] = 0.488603f * z;
+  b[3] = 0.488603f * x;
+  b[4] = 1.092548f * x * y;
+  b[5] = 1.092548f * y * z;
+  b[6] = 0.315392f * (3.0f * z * z - 1.0f);
+  b[7] = 1.092548f * x * z;
+  b[8] = 0.546274f * (x * x - y * y);
+}
+static f3 bn_sky(const float* sh, f3 w) {
+  float x = w.x, y = w.y, z = w.z;
+  float b[16] = {0.282095f, 0.488603f * y, 0.488603f * z, 0.488603f * x, 1.092548f * x * y, 1.092548f * y * z,
+                 0.315392f * (3.0f * z * z - 1.0f), 1.092548f * x * z, 0.546274f * (x * x - y * y),
+                 0.590044f * y * (3.0f * x * x - y * y), 2.890611f * x * y * z, 0.457046f * y * (5.0f * z * z - 1.0f),
+                 0.373176f * z * (5.0f * z * z - 3.0f), 0.457046f * x * (5.0f * z * z - 1.0f),
+                 1.445306f * z * (x * x - y * y), 0.590044f * x * (x * x - 3.0f * y * y)};
+  f3 c = F3(0.0f, 0.0f, 0.0f);
+  for (int k = 0; k < 16; k++) c = add3(c, mul3(F3(sh[3 * k], sh[3 * k + 1], sh[3 * k + 2]), b[k]));
+  return F3(fmaxf(c.x, 0.0f), fmaxf(c.y, 0.0f), fmaxf(c.z, 0.0f));
+}
+static float bn_seg_geom(const sl_node* nd, f3 P, f3 w, float t0, float t1) {
+  f3 d = sub3(F3(nd->mean[0], nd->mean[1], nd->mean[2]), P);
+  f3 cw = sym_mul(nd_cinv_d(nd), nd_cinv_o(nd), w);
+  float a = dot3(cw, w);
+  float m = dot3(cw, d) / a;
+  f3 e = sub3(d, mul3(w, m));
+  float q = fmaxf(dot3(e, sym_mul(nd_cinv_d(nd), nd_cinv_o(nd), e)), 0.0f);
+  float s = sqrtf(0.5f * a);
+  float x0 = s * (t0 - m), x1 = s * (t1 - m);
+  float df;
+  if (x0 > 0.0f) df = erfc_pos(x0) - erfc_pos(x1);
+  else if (x1 < 0.0f) df = erfc_pos(-x1) - erfc_pos(-x0);
+  else df = 2.0f - erfc_pos(x1) - erfc_pos(-x0);
+  return sl_expf(-0.5f * q) * sqrtf(BN_PI / (2.0f * a)) * df;
+}
+static uint32_t bn_cell_of(f3 w) {
+  float el = sl_asinf(clampf(w.z, -1.0f, 1.0f));
+  float fi = fmaxf((0.5f * BN_PI - el) / (BN_PI / 8.0f), 0.0f);
+  uint32_t i = (uint32_t)fi;
+  i = i < 7u ? i : 7u;
+  uint32_t j = ((uint32_t)sl_floorf((sl_atan2f(w.y, w.x) + BN_PI) / (2.0f * BN_PI) * 16.0f)) % 16u;
+  return i * 16u + j;
+}
+static float bn_ground(const orc_probe_layout* L, uint32_t i, uint32_t j) {
+  return L->ground ? L->ground[i * L->dims[1] + j] : 0.0f;
+}
+static f3 bn_probe_pos(const orc_probe_layout* L, uint32_t p) {
+  uint32_t i = p / (L->dims[1] * L->dims[2]), j = (p / L->dims[2]) % L->dims[1], k = p % L->dims[2];
+  return F3(L->lo[0] + L->step[0] * (float)i, L->lo[1] + L->step[1] * (float)j, bn_ground(L, i, j) + L->levels[k]);
+}
+static f3 bn_node_radiance(const uint32_t* node_sh, uint32_t ni, const float* b) {
+  float h[28];
+  for (uint32_t j = 0; j < 14u; j++) {
+    uint32_t u = node_sh[ni * 14u + j];
+    h[2 * j] = f16_to_f32(u & 0xFFFFu);
+    h[2 * j + 1] = f16_to_f32(u >> 16);
+  }
+  f3 v = F3(0.0f, 0.0f, 0.0f);
+  for (int m = 0; m < 9; m++) v = add3(v, mul3(F3(h[3 * m], h[3 * m + 1], h[3 * m + 2]), b[m]));
+  return v;
+}
+
+static float bn_cheb(const orc_probe_layout* L, const float* pd, uint32_t p, f3 P) {
+  f3 v = sub3(P, bn_probe_pos(L, p));
+  float dist = len3(v);
+  const float* mm = pd + 8u * (p * BN_NCELL + bn_cell_of(div3(v, fmaxf(dist, 1e-9f)))) + 4u;
+  float var = fmaxf(mm[1] - mm[0] * mm[0], 1e-4f);
+  float dd = fmaxf(dist - 0.03f - mm[0], 0.0f);
+  if (dd <= 0.0f) return 1.0f;
+  float r = var / (var + dd * dd);
+  return r * r * r;
+}
+
+typedef struct { uint32_t pid[8]; float w[8]; } bn_weights;
+
+static bn_weights bn_probe_weights(const orc_probe_layout* L, const float* pd, f3 P) {
+  const uint32_t* dm = L->dims;
+  float fx = clampf((P.x - L->lo[0]) / L->step[0], 0.0f, (float)(dm[0] - 1u));
+  float fy = clampf((P.y - L->lo[1]) / L->step[1], 0.0f, (float)(dm[1] - 1u));
+  uint32_t i = (uint32_t)sl_floorf(fx), j = (uint32_t)sl_floorf(fy);
+  i = i < dm[0] - 2u ? i : dm[0] - 2u;
+  j = j < dm[1] - 2u ? j : dm[1] - 2u;
+  float tx = fx - (float)i, ty = fy - (float)j;
+  float g = mixf(mixf(bn_ground(L, i, j), bn_ground(L, i, j + 1u), ty),
+                 mixf(bn_ground(L, i + 1u, j), bn_ground(L, i + 1u, j + 1u), ty), tx);
+  float h = P.z - g;
+  uint32_t k = 0;
+  while (k + 2u < dm[2] && h > L->levels[k + 1u]) k++;
+  float tz = clampf((h - L->levels[k]) / fmaxf(L->levels[k + 1u] - L->levels[k], 1e-6f), 0.0f, 1.0f);
+  bn_weights out;
+  float wsum = 0.0f;
+  for (uint32_t c = 0; c < 8u; c++) {
+    uint32_t ox = c >> 2u, oy = (c >> 1u) & 1u, oz = c & 1u;
+    uint32_t p = ((i + ox) * dm[1] + (j + oy)) * dm[2] + (k + oz);
+    out.pid[c] = p;
+    float wx = ox ? tx : 1.0f - tx, wy = oy ? ty : 1.0f - ty, wz = oz ? tz : 1.0f - tz;
+    float valid = pd[8u * (p * BN_NCELL) + 6u];
+    float cw = wx * wy * wz * valid;
+    out.w[c] = cw * fmaxf(bn_cheb(L, pd, p, P), 1e-3f);
+    wsum += out.w[c];
+  }
+  if (wsum <= 0.0f) { /* probe_fallback: the 8 best valid probes of the 4x4x4 block */
+    for (int c = 0; c < 8; c++) { out.pid[c] = 0u; out.w[c] = 0.0f; }
+    for (uint32_t q = 0; q < 64u; q++) {
+      int ii = (int)i + (int)(q >> 4u) - 1, jj = (int)j + (int)((q >> 2u) & 3u) - 1, kk = (int)k + (int)(q & 3u) - 1;
+      if (ii < 0 || jj < 0 || kk < 0 || ii >= (int)dm[0] || jj >= (int)dm[1] || kk >= (int)dm[2]) continue;
+      uint32_t p = ((uint32_t)ii * dm[1] + (uint32_t)jj) * dm[2] + (uint32_t)kk;
+      if (pd[8u * (p * BN_NCELL) + 6u] <= 0.0f) continue;
+      float d = fmaxf(len3(sub3(P, bn_probe_pos(L, p))), 0.05f);
+      float w = fmaxf(bn_cheb(L, pd, p, P), 1e-3f) / (d * d);
+      if (w <= out.w[7]) continue;
+      uint32_t at = 7u;
+      while (at > 0u && out.w[at - 1u] < w) {
+        out.w[at] = out.w[at - 1u];
+        out.pid[at] = out.pid[at - 1u];
+        at--;
+      }
+      out.w[at] = w;
+      out.pid[at] = p;
+    }
+    float s = 0.0f;
+    for (int c = 0; c < 8; c++) s += out.w[c];
+    for (int c = 0; c < 8; c++) out.w[c] /= fmaxf(s, 1e-12f);
+    return out;
+  }
+  for (int c = 0; c < 8; c++) out.w[c] /= fmaxf(wsum, 1e-12f);
+  return out;
+}
+
+/* emissive.wgsl DIRS14 (:107-112): the same directions with the diagonals' components written 0.57735 */
+static const float bn_dirs14[14][3] = {{1.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, {1e-4f, 0.0f, 1.0f},
+                                       {-1.0f, 0.0f, 0.0f}, {0.0f, -1.0f, 0.0f}, {1e-4f, 0.0f, -1.0f},
+                                       {0.57735f, 0.57735f, 0.57735f}, {0.57735f, 0.57735f, -0.57735f},
+                                       {0.57735f, -0.57735f, 0.57735f}, {0.57735f, -0.57735f, -0.57735f},
+                                       {-0.57735f, 0.57735f, 0.57735f}, {-0.57735f, 0.57735f, -0.57735f},
+                                       {-0.57735f, -0.57735f, 0.57735f}, {-0.57735f, -0.57735f, -0.57735f}};
+
+/* direct_dirs_one (emissive.wgsl:1066-1082): shade_emitters toward DIRS14 (asg off; M39 transfer), each direction's
+ * colour weighted by footprint x V toward it, then env_dirs_one's distant catch */
+static void bn_direct_one(const orc_bounce_in* in, uint32_t g, float* lo_dir) {
+  const sl_gaussian* G = &in->gs[g];
+  const sl_node* nd = &in->nodes[g];
+  const sl_material* mat = &in->mats[mat_index(G, in->mat_count)];
+  const float* xf = in->parts[G->part_surface & 0xFFFFu].xf;
+  m3f Rq = quat_matrix(G->quat);
+  m3f Dm = m3_diag(F3(mat->flake[0], mat->flake[1], mat->flake[2]));
+  m3f t0 = m3_mul(&Rq, &Dm);
+  m3f RqT = m3_t(&Rq);
+  m3f Sloc = m3_mul(&t0, &RqT);
+  float s3 = G->scale[0] * G->scale[1] * G->scale[2];
+  float detC = s3 * s3;
+  f3 P = xf_point(xf, F3(G->mu[0], G->mu[1], G->mu[2]));
+  f3 n = Rq.c[0];
+  f3 Sd = F3(Sloc.c[0].x, Sloc.c[1].y, Sloc.c[2].z), So = F3(Sloc.c[1].x, Sloc.c[2].x, Sloc.c[2].y);
+  f3 alb = F3(G->albedo[0], G->albedo[1], G->albedo[2]);
+  float ks = spec_weight(mat);
+  int emissive = (mat->flags & 1u) != 0u;
+  f3 wo[14];
+  f3 acc[14];
+  for (int k = 0; k < 14; k++) {
+    wo[k] = xf_dir_inv(xf, F3(bn_dirs14[k][0], bn_dirs14[k][1], bn_dirs14[k][2]));
+    acc[k] = F3(0.0f, 0.0f, 0.0f);
+  }
+  if (in->n_emit) {
+    uint32_t stack[48];
+    uint32_t sp = 1;
+    stack[0] = in->tree_root;
+    while (sp > 0u) {
+      sp--;
+      const float* e = in->tree + 24u * stack[sp];
+      uint32_t child_lo = sl_float_to_bits(e[11]), child_hi = sl_float_to_bits(e[15]);
+      f3 emean = F3(e[0], e[1], e[2]);
+      int use;
+      if (child_lo == NONE_U32 || in->emit_mode == 0u) {
+        use = child_lo == NONE_U32;
+      } else {
+        f3 d = sub3(P, emean);
+        use = dot3(d, d) > in->emit_theta * in->emit_theta * e[3] * e[3];
+      }
+      if (!use) {
+        if (sp + 2u <= 48u) { stack[sp] = child_lo; stack[sp + 1u] = child_hi; sp += 2u; }
+        continue;
+      }
+      f3 d = sub3(emean, P);
+      float d2 = dot3(d, d);
+      if (d2 < 1e-8f) continue;
+      f3 ww = div3(d, sqrtf(d2));
+      f3 wi = xf_dir_inv(xf, ww);
+      float vi = vgrid_lookup(&in->vgrid[g], wi);
+      if (vi <= 1e-7f) continue;
+      float fp = footprint(nd, detC, wi);
+      f3 mw = mul3(ww, -1.0f);
+      float s = 1.0f;
+      if (in->one_sided) {
+        f3 nn = F3(in->normal[0], in->normal[1], in->normal[2]);
+        float cs = dot3(mw, nn);
+        s = in->edge_soft > 0.0f ? smoothstepf(-in->edge_soft, in->edge_soft, cs) : (cs > 0.0f ? 1.0f : 0.0f);
+      }
+      float mq = sqrtf(fmaxf(dot3(mw, sym_mul(F3(e[4], e[5], e[6]), F3(e[8], e[9], e[10]), mw)), 0.0f));
+      f3 I = mul3(F3(e[12], e[13], e[14]), s * in->emit_scale * mq);
+      f3 light = mul3(mul3(I, vi), fp / d2 * 1.0f);
+      if (ks <= 0.0f) {
+        acc[0] = add3(acc[0], light);
+        continue;
+      }
+      f3 wr = mirror3(wi, n);
+      float damp = iso_damp(iso_norm(nd), footprint(nd, detC, wr) * vgrid_lookup(&in->vgrid[g], wr));
+      for (int k = 0; k < 14; k++)
+        acc[k] = add3(acc[k], mul3(light, iso_lobe_from(ks, phase_specular(Sd, So, wi, wo[k]), damp)));
+    }
+  }
+  float T = in->lamp_T[g];
+  float inorm = iso_norm(nd);
+  f3 a0 = acc[0];
+  f3 mean = F3(0.0f, 0.0f, 0.0f);
+  float ws = 0.0f;
+  f3 c0 = F3(0.0f, 0.0f, 0.0f);
+  for (int k = 0; k < 14; k++) {
+    f3 ck = mul3(mul3v(alb, ks <= 0.0f ? a0 : acc[k]), T * inorm);
+    if (k == 0) c0 = ck;
+    float w = footprint(nd, detC, wo[k]) * vgrid_lookup(&in->vgrid[g], wo[k]);
+    mean = add3(mean, mul3(ck, w));
+    ws += w;
+  }
+  f3 c = ws > 0.0f ? div3(mean, fmaxf(ws, 1e-20f)) : c0;
+  /* env_dirs (environment.wgsl:353-359): the distant lights' catch, non-emissive Gaussians */
+  if (in->n_lights && !emissive) {
+    f3 dc = F3(0.0f, 0.0f, 0.0f);
+    for (uint32_t k = 0; k < in->n_lights && k < 4u; k++) {
+      f3 wi = xf_dir_inv(xf, F3(in->lights[k].dir[0], in->lights[k].dir[1], in->lights[k].dir[2]));
+      float v = vgrid_lookup(&in->vgrid[g], wi);
+      if (v <= 1e-7f) continue;
+      dc = add3(dc, mul3(F3(in->lights[k].irr[0], in->lights[k].irr[1], in->lights[k].irr[2]),
+                         in->env_T[4u * g + k] * v * footprint(nd, detC, wi)));
+    }
+    c = add3(c, mul3(mul3v(alb, dc), inorm));
+  }
+  lo_dir[4u * g] = c.x;
+  lo_dir[4u * g + 1] = c.y;
+  lo_dir[4u * g + 2] = c.z;
+  lo_dir[4u * g + 3] = 0.0f;
+}
+
+int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads) {
+  const orc_probe_layout* L = &in->lay;
+  const uint32_t G = in->count, N = in->n_nodes;
+  const uint32_t NP = L->dims[0] * L->dims[1] * L->dims[2];
+  float cells[4 * 128], d14[42], pinv[126];
+  orc_iso_dirs(cells);
+  orc_bounce_tables(d14, pinv);
+  (void)nthreads;
+
+  /* iso_xfer: where something moved relative to the Gaussian, or forced */
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static, 256)
+#endif
+  for (int64_t gi = 0; gi < (int64_t)G; gi++) {
+    uint32_t g = (uint32_t)gi;
+    const sl_gaussian* Gs = &in->gs[g];
+    uint32_t own = Gs->part_surface & 0xFFFFu;
+    const float* xf = in->parts[own].xf;
+    f3 P = xf_point(xf, F3(Gs->mu[0], Gs->mu[1], Gs->mu[2]));
+    int stale = in->force || (own < 32u && ((in->moved_mask >> own) & 1u));
+    for (uint32_t p = 0; p < in->part_count && p < 32u && !stale; p++) {
+      if (p == own || ((in->moved_mask >> p) & 1u) == 0u) continue;
+      const float* b = in->parts[p].bound;
+      float r = b[3] + BN_NEAR_R;
+      stale = len3(sub3(P, xf_point(in->parts[p].xf, F3(b[0], b[1], b[2])))) < r ||
+              len3(sub3(P, xf_point(in->parts[p].xf_prev, F3(b[0], b[1], b[2])))) < r;
+    }
+    if (!stale) continue;
+    const sl_node* nd = &in->nodes[g];
+    float s3 = Gs->scale[0] * Gs->scale[1] * Gs->scale[2];
+    float inorm = iso_norm(nd);
+    float t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t c = 0; c < BN_NCELL; c++) {
+      f3 w = bn_cell_dir(cells, c);
+      f3 u = xf_dir_inv(xf, w);
+      float v = vgrid_lookup(&in->vgrid[g], u) * 1.0f;
+      if (v <= 0.0f) continue;
+      float a = inorm * footprint(nd, s3 * s3, u) * v * cells[4 * c + 3];
+      float y[9];
+      bn_sh2(w, y);
+      for (int m = 0; m < 9; m++) t[m] += a * y[m];
+    }
+    float* xo = st->xfer + 12u * g;
+    for (int m = 0; m < 9; m++) xo[m] = t[m];
+    xo[9] = xo[10] = xo[11] = 0.0f;
+  }
+
+  /* direct_dirs_emit + env_dirs: a quarter of the Gaussians (g % 4 == frame % 4) */
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+#endif
+  for (int64_t gi = in->frame % 4u; gi < (int64_t)G; gi += 4) bn_direct_one(in, (uint32_t)gi, st->lo_dir);
+
+  /* node_leaf */
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static, 256)
+#endif
+  for (int64_t gi = 0; gi < (int64_t)G; gi++) {
+    uint32_t g = (uint32_t)gi;
+    const sl_gaussian* Gs = &in->gs[g];
+    const sl_node* nd = &in->nodes[g];
+    const float* xf = in->parts[Gs->part_surface & 0xFFFFu].xf;
+    float s3 = Gs->scale[0] * Gs->scale[1] * Gs->scale[2];
+    f3 Lr = add3(F3(st->lo_dir[4 * g], st->lo_dir[4 * g + 1], st->lo_dir[4 * g + 2]),
+                 F3(st->lo_b[12 * g + 4], st->lo_b[12 * g + 5], st->lo_b[12 * g + 6]));
+    for (int k = 0; k < 14; k++) {
+      f3 wo = xf_dir_inv(xf, F3(d14[3 * k], d14[3 * k + 1], d14[3 * k + 2]));
+      float w = footprint(nd, s3 * s3, wo) * vgrid_lookup(&in->vgrid[g], wo);
+      float* o = st->node_acc + 4u * (14u * g + (uint32_t)k);
+      o[0] = Lr.x * w;
+      o[1] = Lr.y * w;
+      o[2] = Lr.z * w;
+      o[3] = w;
+    }
+  }
+  /* node_up: depths max_depth - 1 .. 1, children summed in kids order */
+  for (int d = (int)in->max_depth - 1; d >= 1; d--) {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static, 256)
+#endif
+    for (int64_t ii = G; ii < (int64_t)N; ii++) {
+      const sl_node* nd = &in->nodes[ii];
+      if (nd->depth != (uint32_t)d || nd->part == NONE_U32) continue;
+      for (int k = 0; k < 14; k++) {
+        float s[4] = {0, 0, 0, 0};
+        for (uint32_t j = nd->child_lo; j < nd->child_hi; j++) {
+          const float* c = st->node_acc + 4u * (14u * in->kids[j] + (uint32_t)k);
+          for (int q = 0; q < 4; q++) s[q] += c[q];
+        }
+        float* o = st->node_acc + 4u * (14u * (uint32_t)ii + (uint32_t)k);
+        for (int q = 0; q < 4; q++) o[q] = s[q];
+      }
+    }
+  }
+  /* node_sh2: the 14-direction means fitted to SH2, packed as 27 halves */
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static, 256)
+#endif
+  for (int64_t ii = 0; ii < (int64_t)N; ii++) {
+    f3 Lk[14];
+    for (int k = 0; k < 14; k++) {
+      const float* a = st->node_acc + 4u * (14u * (uint32_t)ii + (uint32_t)k);
+      Lk[k] = div3(F3(a[0], a[1], a[2]), fmaxf(a[3], 1e-12f));
+    }
+    float h[28];
+    h[27] = 0.0f;
+    for (int m = 0; m < 9; m++) {
+      f3 c = F3(0.0f, 0.0f, 0.0f);
+      for (int k = 0; k < 14; k++) c = add3(c, mul3(Lk[k], pinv[14 * m + k]));
+      h[3 * m] = c.x;
+      h[3 * m + 1] = c.y;
+      h[3 * m + 2] = c.z;
+    }
+    for (int j = 0; j < 14; j++)
+      st->node_sh[14u * (uint32_t)ii + (uint32_t)j] = orc_f32_to_f16(h[2 * j]) | (orc_f32_to_f16(h[2 * j + 1]) << 16);
+  }
+
+  /* probe_gather: every (probe, cell) ray of the lattice */
+  /* block_rad: half the lattice cell's diagonal (lighting.js:794, float64); 0 for terrain probes (each cuts
+   * around itself) */
+  const float brad = L->terrain ? 0.0f : (float)(0.5 * sqrt((double)L->step[0] * L->step[0] +
+                                                            (double)L->step[1] * L->step[1] +
+                                                            (double)L->step[2] * L->step[2]));
+  const float tmax = L->tmax;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 16)
+#endif
+  for (int64_t id64 = 0; id64 < (int64_t)NP * BN_NCELL; id64++) {
+    uint32_t id = (uint32_t)id64, p = id / BN_NCELL, c = id % BN_NCELL;
+    f3 o = bn_probe_pos(L, p);
+    f3 w = bn_cell_dir(cells, c);
+    uint32_t dz = L->dims[2];
+    f3 cen = o;
+    if (!L->terrain) {
+      float bx = (float)((p / (L->dims[1] * dz)) / 2u), by = (float)(((p / dz) % L->dims[1]) / 2u),
+            bz = (float)((p % dz) / 2u);
+      cen = F3(L->lo[0] + L->step[0] * (2.0f * bx + 0.5f), L->lo[1] + L->step[1] * (2.0f * by + 0.5f),
+               L->lo[2] + L->step[2] * (2.0f * bz + 0.5f));
+    }
+    float t1 = tmax;
+    float ht[BN_HIT_MAX], hv[BN_HIT_MAX];
+    uint32_t hn[BN_HIT_MAX];
+    uint32_t k = 0;
+    for (uint32_t q = 0; q < in->part_count; q++) {
+      const float* xf = in->parts[q].xf;
+      f3 Po = xf_dir_inv(xf, sub3(o, F3(xf[3], xf[7], xf[11])));
+      f3 wr = xf_dir_inv(xf, w);
+      f3 cr = xf_dir_inv(xf, sub3(cen, F3(xf[3], xf[7], xf[11])));
+      if (in->parts[q].root == NONE_U32) continue;
+      uint32_t stack[BN_STACK];
+      stack[0] = in->parts[q].root;
+      uint32_t sp = 1;
+      while (sp > 0u) {
+        sp--;
+        uint32_t ni = stack[sp];
+        const sl_node* nd = &in->nodes[ni];
+        f3 mean = F3(nd->mean[0], nd->mean[1], nd->mean[2]);
+        f3 d = sub3(mean, Po);
+        float tt = clampf(dot3(d, wr), 0.0f, t1);
+        f3 e = sub3(d, mul3(wr, tt));
+        if (dot3(e, e) > nd->radius * nd->radius) continue;
+        int use_node = ni < G;
+        if (!use_node) use_node = len3(sub3(cr, mean)) - brad > BN_THETA * nd->smax;
+        if (use_node) {
+          float tau = nd->kappa * dirm(nd, wr) * bn_seg_geom(nd, Po, wr, 0.0f, t1);
+          if (tau > 1e-6f) {
+            f3 cw = sym_mul(nd_cinv_d(nd), nd_cinv_o(nd), wr);
+            float den = dot3(cw, wr);
+            float tp = fabsf(den) > 1e-30f ? clampf(dot3(cw, d) / den, 0.0f, t1) : t1;
+            uint32_t at = k < BN_HIT_MAX - 1u ? k : BN_HIT_MAX - 1u;
+            uint32_t l = BN_HIT_MAX - 1u;
+            if (k == BN_HIT_MAX && tp >= ht[l]) {
+              ht[l] = fmaxf(ht[l], tp);
+              hv[l] = fminf(hv[l] + tau, 64.0f);
+              continue;
+            }
+            int full = k == BN_HIT_MAX;
+            float sv = full ? hv[l] : 0.0f, stv = full ? ht[l] : 0.0f;
+            while (at > 0u && ht[at - 1u] > tp) {
+              ht[at] = ht[at - 1u];
+              hv[at] = hv[at - 1u];
+              hn[at] = hn[at - 1u];
+              at--;
+            }
+            ht[at] = tp;
+            hv[at] = tau;
+            hn[at] = ni;
+            if (full) {
+              ht[l] = fmaxf(ht[l], stv);
+              hv[l] = fminf(hv[l] + sv, 64.0f);
+            }
+            k = k + 1u < BN_HIT_MAX ? k + 1u : BN_HIT_MAX;
+          }
+        } else {
+          for (uint32_t j = nd->child_lo; j < nd->child_hi; j++)
+            if (sp < BN_STACK) stack[sp++] = in->kids[j];
+        }
+      }
+    }
+    float T = 1.0f, m1 = 0.0f, m2 = 0.0f, first_part = -1.0f, nearv = 0.0f;
+    f3 acc = F3(0.0f, 0.0f, 0.0f);
+    float bw[9];
+    bn_sh2(mul3(w, -1.0f), bw);
+    for (uint32_t i = 0; i < k; i++) {
+      if (T <= 0.0f) break;
+      float al = 1.0f - sl_expf(-hv[i]);
+      f3 rad = bn_node_radiance(st->node_sh, hn[i], bw);
+      rad = F3(fmaxf(rad.x, 0.0f), fmaxf(rad.y, 0.0f), fmaxf(rad.z, 0.0f));
+      acc = add3(acc, mul3(rad, T * al));
+      float dep = clampf(ht[i], 0.0f, t1);
+      m1 += T * al * dep;
+      m2 += T * al * dep * dep;
+      float Tn = T * (1.0f - al);
+      if (T >= 0.5f && Tn < 0.5f) {
+        uint32_t hp = in->nodes[hn[i]].part;
+        first_part = (float)hp;
+        nearv = dep < 0.05f ? 1.0f : 0.0f;
+        if (hn[i] < G && hp < in->part_count &&
+            vgrid_lookup(&in->vgrid[hn[i]], xf_dir_inv(in->parts[hp].xf, mul3(w, -1.0f))) < 0.1f)
+          nearv += 2.0f;
+      }
+      T = Tn;
+    }
+    if (in->sky_sh && t1 >= tmax * 0.999f) acc = add3(acc, mul3(bn_sky(in->sky_sh, w), T));
+    m1 += T * t1;
+    m2 += T * t1 * t1;
+    float a = in->alpha;
+    float* r0 = st->probe_data + 8u * id;
+    float* r1 = r0 + 4;
+    r0[0] = mixf(r0[0], acc.x, a);
+    r0[1] = mixf(r0[1], acc.y, a);
+    r0[2] = mixf(r0[2], acc.z, a);
+    r0[3] = first_part;
+    r1[0] = mixf(r1[0], m1, a);
+    r1[1] = mixf(r1[1], m2, a);
+    r1[3] = nearv;
+  }
+  /* probe_valid */
+  for (uint32_t p = 0; p < NP; p++) {
+    uint32_t cnt[17] = {0};
+    uint32_t nearc = 0, back = 0;
+    for (uint32_t c = 0; c < BN_NCELL; c++) {
+      const float* r0 = st->probe_data + 8u * (p * BN_NCELL + c);
+      uint32_t fl = (uint32_t)(fmaxf(r0[7], 0.0f) + 0.5f);
+      nearc += fl & 1u;
+      back += (fl >> 1u) & 1u;
+      if (r0[3] >= 0.0f) {
+        uint32_t q = (uint32_t)r0[3];
+        cnt[q < 16u ? q : 16u]++;
+      }
+    }
+    int enclosed = 0;
+    for (uint32_t q = 0; q < in->part_count && q < 16u; q++)
+      if ((in->parts[q].flags & 1u) == 0u && (float)cnt[q] > BN_G_VALID * (float)BN_NCELL) enclosed = 1;
+    st->probe_data[8u * (p * BN_NCELL) + 6u] = (enclosed || nearc * 2u > BN_NCELL || back * 2u > BN_NCELL) ? 0.0f : 1.0f;
+  }
+  /* probe_sh2 */
+  for (uint32_t p = 0; p < NP; p++) {
+    f3 c9[9];
+    for (int m = 0; m < 9; m++) c9[m] = F3(0.0f, 0.0f, 0.0f);
+    for (uint32_t c = 0; c < BN_NCELL; c++) {
+      const float* r0 = st->probe_data + 8u * (p * BN_NCELL + c);
+      f3 Lc = mul3(F3(r0[0], r0[1], r0[2]), cells[4 * c + 3]);
+      float y[9];
+      bn_sh2(bn_cell_dir(cells, c), y);
+      for (int m = 0; m < 9; m++) c9[m] = add3(c9[m], mul3(Lc, y[m]));
+    }
+    for (int m = 0; m < 9; m++) {
+      float* o = st->probe_sh + 4u * (9u * p + (uint32_t)m);
+      o[0] = c9[m].x;
+      o[1] = c9[m].y;
+      o[2] = c9[m].z;
+      o[3] = 0.0f;
+    }
+  }
+  /* bounce_sh (+ gloss_sh) */
+  f3 eye = F3(in->eye[0], in->eye[1], in->eye[2]);
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static, 256)
+#endif
+  for (int64_t gi = 0; gi < (int64_t)G; gi++) {
+    uint32_t g = (uint32_t)gi;
+    const sl_gaussian* Gs = &in->gs[g];
+    const sl_material* mat = &in->mats[mat_index(Gs, in->mat_count)];
+    float ks = spec_weight(mat);
+    float lw = sqrtf(fminf(mat->flake[1], mat->flake[2]) / fmaxf(mat->flake[0], 1e-12f));
+    if (ks > 0.0f && !(lw >= BN_GLOSS_SH_MIN)) continue; /* near-mirror: bounce_dirs (not restated) */
+    uint32_t own = Gs->part_surface & 0xFFFFu;
+    const float* xf = in->parts[own].xf;
+    f3 P = xf_point(xf, F3(Gs->mu[0], Gs->mu[1], Gs->mu[2]));
+    bn_weights pw = bn_probe_weights(L, st->probe_data, P);
+    f3 Lsh[9];
+    for (int m = 0; m < 9; m++) Lsh[m] = F3(0.0f, 0.0f, 0.0f);
+    for (int q = 0; q < 8; q++) {
+      float wq = pw.w[q];
+      if (wq <= 0.0f) continue;
+      for (int m = 0; m < 9; m++) {
+        const float* s = st->probe_sh + 4u * (9u * pw.pid[q] + (uint32_t)m);
+        Lsh[m] = add3(Lsh[m], mul3(F3(s[0], s[1], s[2]), wq));
+      }
+    }
+    const float* t = st->xfer + 12u * g;
+    f3 cc = mul3(Lsh[0], t[0]);
+    for (int m = 1; m < 9; m++) cc = add3(cc, mul3(Lsh[m], t[m]));
+    f3 alb = F3(Gs->albedo[0], Gs->albedo[1], Gs->albedo[2]);
+    f3 cb = mul3v(alb, F3(fmaxf(cc.x, 0.0f), fmaxf(cc.y, 0.0f), fmaxf(cc.z, 0.0f)));
+    float* lb = st->lo_b + 12u * g;
+    lb[0] = cb.x; lb[1] = cb.y; lb[2] = cb.z; lb[3] = 0.0f;
+    lb[4] = cb.x; lb[5] = cb.y; lb[6] = cb.z; lb[7] = 0.0f;
+    lb[8] = lb[9] = lb[10] = lb[11] = 0.0f;
+    if (ks > 0.0f) {
+      const sl_node* nd = &in->nodes[g];
+      m3f Rq = quat_matrix(Gs->quat);
+      f3 n = Rq.c[0];
+      f3 wo = xf_dir_inv(xf, norm3(sub3(eye, P)));
+      f3 wm = mirror3(wo, n);
+      float s3 = Gs->scale[0] * Gs->scale[1] * Gs->scale[2];
+      float detC = s3 * s3;
+      float vis = vgrid_lookup(&in->vgrid[g], wm) * footprint(nd, detC, wm);
+      f3 sp = F3(0.0f, 0.0f, 0.0f);
+      if (vis > 0.0f) {
+        float inorm = iso_norm(nd);
+        float damp = iso_damp(inorm, footprint(nd, detC, wo) * vgrid_lookup(&in->vgrid[g], wo));
+        float sg = 2.0f * lw;
+        float a1 = sl_expf(-sg * sg), a2 = sl_expf(-3.0f * sg * sg);
+        f3 wmw = F3(xf[0] * wm.x + xf[1] * wm.y + xf[2] * wm.z, xf[4] * wm.x + xf[5] * wm.y + xf[6] * wm.z,
+                    xf[8] * wm.x + xf[9] * wm.y + xf[10] * wm.z);
+        float y[9];
+        bn_sh2(wmw, y);
+        f3 Lm = mul3(Lsh[0], y[0]);
+        for (int m = 1; m < 4; m++) Lm = add3(Lm, mul3(Lsh[m], a1 * y[m]));
+        for (int m = 4; m < 9; m++) Lm = add3(Lm, mul3(Lsh[m], a2 * y[m]));
+        f3 Lp = F3(fmaxf(Lm.x, 0.0f), fmaxf(Lm.y, 0.0f), fmaxf(Lm.z, 0.0f));
+        sp = mul3(mul3v(mul3(mul3(mul3(mul3(mul3(alb, inorm), ks), 4.0f), BN_PI), damp), Lp), vis);
+      }
+      f3 eyec = add3(mul3(cb, 1.0f - ks), sp);
+      lb[0] = eyec.x; lb[1] = eyec.y; lb[2] = eyec.z;
+    }
+  }
+  return 0;
+}

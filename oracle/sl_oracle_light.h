@@ -68,6 +68,67 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
                  const sl_vgrid* vgrid, const sl_material* mats, uint32_t mat_count, const orc_light_setup* S,
                  float* colour, float* lamp_T, float* env_T, int nthreads);
 
+
+/* ---- probe bounce (bounce.wgsl; lighting.js probeLayout / initBounce / encodeBounce) -------------------------- */
+typedef struct orc_probe_layout {
+  uint32_t dims[3];
+  uint32_t terrain;
+  float lo[3];
+  float step[3];
+  float levels[16];
+  const float* ground; /* dims[0] x dims[1], or NULL (0) */
+  float tmax;
+} orc_probe_layout;
+
+typedef struct orc_bounce_in {
+  const sl_gaussian* gs;
+  uint32_t count;
+  const sl_part* parts;
+  uint32_t part_count;
+  const sl_node* nodes; /* the leaves (iso_norm in pad0) then the internal nodes */
+  uint32_t n_nodes;
+  const uint32_t* kids;
+  const sl_vgrid* vgrid;
+  const sl_material* mats;
+  uint32_t mat_count;
+  const float* tree; /* emitter tree, 24 floats per node (orc_emitter_tree) */
+  uint32_t tree_root, n_emit, emit_mode, one_sided;
+  float emit_theta, emit_scale, edge_soft;
+  float normal[3];
+  const float* lamp_T; /* per Gaussian */
+  const float* env_T;  /* 4 per Gaussian */
+  const orc_env_light* lights;
+  uint32_t n_lights;
+  const float* sky_sh; /* 16 x 3, or NULL */
+  orc_probe_layout lay;
+  uint32_t max_depth;
+  float eye[3];
+  float alpha; /* this gather's history weight */
+  uint32_t frame;
+  uint32_t force;      /* iso_xfer refreshes every Gaussian */
+  uint32_t moved_mask; /* parts that moved this frame (the reference's Part flags bit 1) */
+} orc_bounce_in;
+
+typedef struct orc_bounce_state {
+  float* probe_data; /* NP x 128 x 8 */
+  float* probe_sh;   /* NP x 9 x 4 */
+  float* xfer;       /* G x 12 */
+  float* lo_dir;     /* G x 4 */
+  float* lo_b;       /* G x 12 */
+  float* node_acc;   /* N x 14 x 4 */
+  uint32_t* node_sh; /* N x 14 */
+} orc_bounce_state;
+
+
+/* One frame of the probe bounce (the reference's encodeBounce with ?sendercut=0): iso_xfer, direct_dirs_emit +
+ * env_dirs for the Gaussians g % 4 == frame % 4, node_leaf, node_up, node_sh2, probe_gather, probe_valid, probe_sh2,
+ * bounce_sh.  The state persists between frames (zero it before the first). */
+int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads);
+/* D14 (14 x 3) and the 9 x 14 least-squares SH2 fit on it, float64 then rounded */
+void orc_bounce_tables(float* d14, float* pinv);
+/* f32 -> f16 bits, round to nearest even */
+uint32_t orc_f32_to_f16(float f);
+
 #ifdef __cplusplus
 }
 #endif

@@ -36,6 +36,12 @@ class RenderOptions(C.Structure):
                 ("entry_capacity", C.c_uint32), ("sort_mode", C.c_uint32)]
 
 
+class ProbeLayout(C.Structure):
+    """sl_probe_layout (include/splatlight.h)."""
+    _fields_ = [("dims", C.c_uint32 * 3), ("terrain", C.c_uint32), ("lo", C.c_float * 3), ("step", C.c_float * 3),
+                ("levels", C.c_float * 16), ("ground", C.c_void_p), ("tmax", C.c_float)]
+
+
 class BatchOptions(C.Structure):
     _fields_ = [("max_views", C.c_uint32), ("max_tiles", C.c_uint32), ("max_slots", C.c_uint64),
                 ("max_entries", C.c_uint64), ("tile_w", C.c_uint32), ("tile_h", C.c_uint32),
@@ -110,6 +116,9 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_lighting_set_options": (_I, [_P, _U32, _U32, _U32, C.c_float, _I]),
     "sl_lighting_set_blur": (_I, [_P, C.c_float, C.c_float]),
     "sl_lighting_set_tree": (_I, [_P, _P, _U32, _P, _U32]),
+    "sl_lighting_set_probes": (_I, [_P, _P, _U32, C.c_float]),
+    "sl_lighting_set_sky": (_I, [_P, _P, _U32]),
+    "sl_lighting_read_bounce": (_I, [_P, _U32, _P, C.c_size_t]),
     "sl_lighting_update": (_I, [_P, _P, _P, _U32, _P]),
     "sl_lighting_shade": (_I, [_P, _P, _P]),
     "sl_lighting_read": (_I, [_P, _P, _P, _P, _P]),

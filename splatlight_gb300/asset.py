@@ -297,4 +297,43 @@ def asset_scene(asset: Asset, width: int | None = None, height: int | None = Non
         emit_normal=tuple(emit["normal"]) if emit else (0.0, 0.0, 1.0),
         emit_skip_part=emit["skip_part"] if emit else 0xFFFFFFFF,
         emit_drawn=False,          # the emitters are scene Gaussians: drawn with the scene, not in extra slots
-        tree_nodes=asset.raw["nodes"], kids=asset.raw["kids"])
+        tree_nodes=asset.raw["nodes"], kids=asset.raw["kids"], sky_sh=environment_sky(h.get("environment")),
+        probes=probe_layout(asset))
+
+
+def environment_sky(env: dict | None):
+    """The sky the probes see (parseEnvironment's sh, Environment.write with the sky gain at 1,
+    src/environment.js:25, 116-124): environment.sky.sh_rgb, up to 16 coefficients, (16, 3) float32; None without
+    an environment or a sky."""
+    sh = ((env or {}).get("sky") or {}).get("sh_rgb") or []
+    if not sh:
+        return None
+    out = np.zeros((16, 3), np.float32)
+    out[:min(16, len(sh))] = np.asarray(sh[:16], np.float64)
+    return out
+
+
+def probe_layout(asset: Asset) -> dict:
+    """probeLayout (src/lighting.js:220-286) on the asset's header: the room layout for an asset with `room`, else
+    the terrain layout over `bounds` (probes.layout may force either); probes.dims / heights_m / terrain_parts as
+    given (the static probe volumes of :289-314 are not part of this pipeline)."""
+    from . import probes as PR
+    h = asset.header
+    pr = h.get("probes") or {}
+    terrain = pr.get("layout") == "terrain" or (not h.get("room") and bool(h.get("bounds")) and
+                                                pr.get("layout") != "room")
+    if h.get("room"):
+        box = tuple((float(h["room"][k][0]), float(h["room"][k][1])) for k in "xyz")
+    elif h.get("bounds"):
+        b = h["bounds"]
+        box = tuple((float(b["lo"][k]), float(b["hi"][k])) for k in range(3))
+    else:
+        raise ValueError("asset.json has neither room nor bounds (probe lattice)")
+    env = bool(h.get("environment"))
+    if not terrain:
+        return PR.room_layout(box, environment=env)
+    names = [p.get("name") for p in h["parts"]]
+    tp = [names.index(n) for n in pr.get("terrain_parts", []) if n in names]
+    return PR.terrain_layout(asset.gaussians, asset.parts, box, dims=tuple(pr.get("dims", (16, 16, 5))[:2]),
+                             heights=tuple(pr.get("heights_m", (0.3, 1.0, 3.0, 8.0, 20.0))), terrain_parts=tp,
+                             environment=env)

@@ -21,7 +21,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libsplatlight.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # translation units whose arithmetic is part of the bit-parity contract
-NO_FMAD = {"project.cu", "lighting.cu", "tiles.cu", "batch.cu", "lod.cu"}
+NO_FMAD = {"project.cu", "lighting.cu", "tiles.cu", "batch.cu", "lod.cu", "bounce.cu"}
 # translation units compiled for speed: fused multiply-add, approximate division and square root
 FAST = {"shade.cu"}
 

@@ -1,0 +1,740 @@
+// Probe bounce (runtime/wgsl/bounce.wgsl, the M39 stage-2 loop; host src/lighting.js:723-816, 1018-1103), the
+// reference's path without the sender cut (?sendercut=0): one frame per sl_lighting_update, in its dispatch order
+//   xfer      iso_xfer (bounce.wgsl:993-1026): per Gaussian near something that moved (or on a forced refresh) the
+//             SH2 of its transfer iso_norm A(w) V(w) over the 128 world cells
+//   direct    direct_dirs_emit + env_dirs (emissive.wgsl:1012-1016, 1066-1082; environment.wgsl:311-359): a quarter
+//             of the Gaussians per frame, the light each sends toward the probes (one value: the footprint x V
+//             weighted mean over DIRS14 of the shading toward those directions, plus the distant lights' catch)
+//   leaf / up / sh2  node_leaf, node_up (deepest depth first), node_sh2 (bounce.wgsl:1166-1236): per tree node the
+//             14-direction sums of that light and their SH2 fit, packed as 27 halves
+//   gather    probe_gather (:1255-1410): per (probe, cell) ray the conservative theta-4 cut of every part's tree,
+//             the hits kept depth-sorted (16, the farthest folded into the last), composited front to back with the
+//             nodes' SH2 radiance, the sky SH beyond; depth moments for the Chebyshev test
+//   valid     probe_valid (:1417-1447); psh2: probe_sh2 (:1029-1041)
+//   bounce    bounce_sh (:1044-1095) with gloss_sh (:1102-1125): the 8 surrounding probes (trilinear x valid x
+//             Chebyshev, with the 4x4x4 fallback) dotted with the Gaussian's transfer into lo_b
+// The translation unit is compiled with --fmad=false and the deterministic transcendentals of sl_detmath.h, so the
+// CPU restatement reproduces it.  Every Gaussian reads the lattice (riding part probes and static probe volumes are
+// not built); near-field visibility is off (the reference's default); near-mirror materials (flake lobe below
+// 0.1 rad), which the reference gives to bounce_dirs, keep a zero bounce.
+#include <cuda_fp16.h>
+
+#include "light_math.cuh"
+#include "sl_bounce.h"
+
+namespace sl {
+namespace {
+
+using namespace lm;
+constexpr uint32_t kCells = 128;
+constexpr uint32_t kHitMax = 16;
+constexpr uint32_t kStack = 64;
+constexpr float kProbeTheta = 4.0f;
+constexpr float kNearR = 0.3f;
+constexpr float kGValid = 0.95f;
+constexpr float kGlossShMin = 0.1f;
+
+// emissive.wgsl DIRS14 (:107-112): the diagonals written 0.57735 (the probes' own D14 is exact, in the table)
+__constant__ float c_dirs14[14][3] = {{1.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, {1e-4f, 0.0f, 1.0f},
+                                      {-1.0f, 0.0f, 0.0f}, {0.0f, -1.0f, 0.0f}, {1e-4f, 0.0f, -1.0f},
+                                      {0.57735f, 0.57735f, 0.57735f}, {0.57735f, 0.57735f, -0.57735f},
+                                      {0.57735f, -0.57735f, 0.57735f}, {0.57735f, -0.57735f, -0.57735f},
+                                      {-0.57735f, 0.57735f, 0.57735f}, {-0.57735f, 0.57735f, -0.57735f},
+                                      {-0.57735f, -0.57735f, 0.57735f}, {-0.57735f, -0.57735f, -0.57735f}};
+
+__device__ __forceinline__ f3 ld3(const float* p) { return F3(p[0], p[1], p[2]); }
+__device__ __forceinline__ f3 max0(f3 a) { return F3(fmaxf(a.x, 0.0f), fmaxf(a.y, 0.0f), fmaxf(a.z, 0.0f)); }
+__device__ __forceinline__ f3 cell_dir(const float* tab, uint32_t c) { return ld3(tab + kTabCells + 4u * c); }
+__device__ __forceinline__ float cell_omega(const float* tab, uint32_t c) { return tab[kTabCells + 4u * c + 3u]; }
+
+__device__ __forceinline__ void sh2_basis(f3 d, float* b) {
+  const float x = d.x, y = d.y, z = d.z;
+  b[0] = 0.282095f;
+  b[1] = 0.488603f * y;
+  b[2] = 0.488603f * z;
+  b[3] = 0.488603f * x;
+  b[4] = 1.092548f * x * y;
+  b[5] = 1.092548f * y * z;
+  b[6] = 0.315392f * (3.0f * z * z - 1.0f);
+  b[7] = 1.092548f * x * z;
+  b[8] = 0.546274f * (x * x - y * y);
+}
+
+// sky_radiance (bounce.wgsl:148-160): real SH bands 0-3, clamped at 0
+__device__ __forceinline__ f3 sky_radiance(const float* sh, f3 w) {
+  const float x = w.x, y = w.y, z = w.z;
+  const float b[16] = {0.282095f, 0.488603f * y, 0.488603f * z, 0.488603f * x, 1.092548f * x * y, 1.092548f * y * z,
+                       0.315392f * (3.0f * z * z - 1.0f), 1.092548f * x * z, 0.546274f * (x * x - y * y),
+                       0.590044f * y * (3.0f * x * x - y * y), 2.890611f * x * y * z,
+                       0.457046f * y * (5.0f * z * z - 1.0f), 0.373176f * z * (5.0f * z * z - 3.0f),
+                       0.457046f * x * (5.0f * z * z - 1.0f), 1.445306f * z * (x * x - y * y),
+                       0.590044f * x * (x * x - 3.0f * y * y)};
+  f3 c = F3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+  for (int k = 0; k < 16; k++) c = add3(c, mul3(ld3(sh + 3 * k), b[k]));
+  return max0(c);
+}
+
+// a tree node's fields as the gather reads them
+struct GNode {
+  f3 mean, cinv_d, cinv_o, sn_d, sn_o;
+  float radius, kappa, smax;
+  uint32_t part, child_lo, child_hi;
+};
+__device__ __forceinline__ GNode load_gnode(const sl_node* n) {
+  GNode g;
+  g.mean = F3(n->mean[0], n->mean[1], n->mean[2]);
+  g.radius = n->radius;
+  g.cinv_d = F3(n->cinv_diag[0], n->cinv_diag[1], n->cinv_diag[2]);
+  g.kappa = n->kappa;
+  g.cinv_o = F3(n->cinv_off[0], n->cinv_off[1], n->cinv_off[2]);
+  g.smax = n->smax;
+  g.sn_d = F3(n->sn_diag[0], n->sn_diag[1], n->sn_diag[2]);
+  g.part = n->part;
+  g.sn_o = F3(n->sn_off[0], n->sn_off[1], n->sn_off[2]);
+  g.child_lo = n->child_lo;
+  g.child_hi = n->child_hi;
+  return g;
+}
+
+// seg_geom (common.wgsl:133-151): int_t0^t1 exp(-q(t)/2) dt along P + t w
+__device__ __forceinline__ float seg_geom(const GNode& nd, f3 P, f3 w, float t0, float t1) {
+  const f3 d = sub3(nd.mean, P);
+  const f3 cw = sym_mul(nd.cinv_d, nd.cinv_o, w);
+  const float a = dot3(cw, w);
+  const float m = dot3(cw, d) / a;
+  const f3 e = sub3(d, mul3(w, m));
+  const float q = fmaxf(dot3(e, sym_mul(nd.cinv_d, nd.cinv_o, e)), 0.0f);
+  const float s = sqrtf(0.5f * a);
+  const float x0 = s * (t0 - m), x1 = s * (t1 - m);
+  float df;
+  if (x0 > 0.0f) df = erfc_pos(x0) - erfc_pos(x1);
+  else if (x1 < 0.0f) df = erfc_pos(-x1) - erfc_pos(-x0);
+  else df = 2.0f - erfc_pos(x1) - erfc_pos(-x0);
+  return lm_exp(-0.5f * q) * sqrtf(kPi / (2.0f * a)) * df;
+}
+
+__device__ __forceinline__ uint32_t cell_of(f3 w) {
+  const float el = lm_asin(clampf(w.z, -1.0f, 1.0f));
+  const float fi = fmaxf((0.5f * kPi - el) / (kPi / 8.0f), 0.0f);
+  uint32_t i = (uint32_t)fi;
+  i = i < 7u ? i : 7u;
+  const uint32_t j = ((uint32_t)floorf((lm_atan2(w.y, w.x) + kPi) / (2.0f * kPi) * 16.0f)) % 16u;
+  return i * 16u + j;
+}
+
+__device__ __forceinline__ float ground_at(const BounceParams& B, const float* ground, uint32_t i, uint32_t j) {
+  return ground ? ground[i * B.dims[1] + j] : 0.0f;
+}
+__device__ __forceinline__ f3 probe_pos(const BounceParams& B, const float* ground, uint32_t p) {
+  const uint32_t i = p / (B.dims[1] * B.dims[2]), j = (p / B.dims[2]) % B.dims[1], k = p % B.dims[2];
+  return F3(B.lo[0] + B.step[0] * (float)i, B.lo[1] + B.step[1] * (float)j, ground_at(B, ground, i, j) + B.levels[k]);
+}
+
+// probe_cheb (bounce.wgsl:759-768): DDGI Chebyshev visibility of P from probe p (pow(x, 3) as x x x)
+__device__ __forceinline__ float probe_cheb(const BounceParams& B, const float* ground, const float4* pd, uint32_t p,
+                                            f3 P) {
+  const f3 v = sub3(P, probe_pos(B, ground, p));
+  const float dist = len3(v);
+  const float4 mm = pd[2u * (p * kCells + cell_of(div3(v, fmaxf(dist, 1e-9f)))) + 1u];
+  const float var = fmaxf(mm.y - mm.x * mm.x, 1e-4f);
+  const float dd = fmaxf(dist - 0.03f - mm.x, 0.0f);
+  if (dd <= 0.0f) return 1.0f;
+  const float r = var / (var + dd * dd);
+  return r * r * r;
+}
+
+struct Weights {
+  uint32_t pid[8];
+  float w[8];
+};
+
+// probe_weights, lattice path (bounce.wgsl:798-885, probe_fallback :771-796)
+__device__ __forceinline__ Weights probe_weights(const BounceParams& B, const float* ground, const float4* pd, f3 P) {
+  const uint32_t* dm = B.dims;
+  const float fx = clampf((P.x - B.lo[0]) / B.step[0], 0.0f, (float)(dm[0] - 1u));
+  const float fy = clampf((P.y - B.lo[1]) / B.step[1], 0.0f, (float)(dm[1] - 1u));
+  uint32_t i = (uint32_t)floorf(fx), j = (uint32_t)floorf(fy);
+  i = i < dm[0] - 2u ? i : dm[0] - 2u;
+  j = j < dm[1] - 2u ? j : dm[1] - 2u;
+  const float tx = fx - (float)i, ty = fy - (float)j;
+  const float g = mixf(mixf(ground_at(B, ground, i, j), ground_at(B, ground, i, j + 1u), ty),
+                       mixf(ground_at(B, ground, i + 1u, j), ground_at(B, ground, i + 1u, j + 1u), ty), tx);
+  const float h = P.z - g;
+  uint32_t k = 0;
+  while (k + 2u < dm[2] && h > B.levels[k + 1u]) k++;
+  const float tz = clampf((h - B.levels[k]) / fmaxf(B.levels[k + 1u] - B.levels[k], 1e-6f), 0.0f, 1.0f);
+  Weights out;
+  float wsum = 0.0f;
+#pragma unroll
+  for (uint32_t c = 0; c < 8u; c++) {
+    const uint32_t ox = c >> 2u, oy = (c >> 1u) & 1u, oz = c & 1u;
+    const uint32_t p = ((i + ox) * dm[1] + (j + oy)) * dm[2] + (k + oz);
+    out.pid[c] = p;
+    const float wx = ox ? tx : 1.0f - tx, wy = oy ? ty : 1.0f - ty, wz = oz ? tz : 1.0f - tz;
+    const float valid = pd[2u * (p * kCells) + 1u].z;
+    const float cw = wx * wy * wz * valid;
+    out.w[c] = cw * fmaxf(probe_cheb(B, ground, pd, p, P), 1e-3f);
+    wsum += out.w[c];
+  }
+  if (wsum <= 0.0f) {
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      out.pid[c] = 0u;
+      out.w[c] = 0.0f;
+    }
+    for (uint32_t q = 0; q < 64u; q++) {
+      const int ii = (int)i + (int)(q >> 4u) - 1, jj = (int)j + (int)((q >> 2u) & 3u) - 1,
+                kk = (int)k + (int)(q & 3u) - 1;
+      if (ii < 0 || jj < 0 || kk < 0 || ii >= (int)dm[0] || jj >= (int)dm[1] || kk >= (int)dm[2]) continue;
+      const uint32_t p = ((uint32_t)ii * dm[1] + (uint32_t)jj) * dm[2] + (uint32_t)kk;
+      if (pd[2u * (p * kCells) + 1u].z <= 0.0f) continue;
+      const float d = fmaxf(len3(sub3(P, probe_pos(B, ground, p))), 0.05f);
+      const float w = fmaxf(probe_cheb(B, ground, pd, p, P), 1e-3f) / (d * d);
+      if (w <= out.w[7]) continue;
+      uint32_t at = 7u;
+      while (at > 0u && out.w[at - 1u] < w) {
+        out.w[at] = out.w[at - 1u];
+        out.pid[at] = out.pid[at - 1u];
+        at--;
+      }
+      out.w[at] = w;
+      out.pid[at] = p;
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 8; c++) s += out.w[c];
+#pragma unroll
+    for (int c = 0; c < 8; c++) out.w[c] /= fmaxf(s, 1e-12f);
+    return out;
+  }
+#pragma unroll
+  for (int c = 0; c < 8; c++) out.w[c] /= fmaxf(wsum, 1e-12f);
+  return out;
+}
+
+__device__ __forceinline__ uint32_t mat_index(const sl_gaussian& G, uint32_t mat_count) {
+  const uint32_t mi = G.flags & 0xFFFFu, top = (mat_count > 1u ? mat_count : 1u) - 1u;
+  return mi < top ? mi : top;
+}
+
+// ---- kernels ---------------------------------------------------------------------------------------------------
+
+constexpr int kThreads = 128;
+
+__global__ void __launch_bounds__(kThreads) xfer_kernel(const __grid_constant__ BounceParams B,
+                                                        const sl_gaussian* __restrict__ gs,
+                                                        const sl_node* __restrict__ nodes,
+                                                        const sl_vgrid* __restrict__ vgrid,
+                                                        const sl_part* __restrict__ parts,
+                                                        const float* __restrict__ tab, float4* __restrict__ xfer) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= B.G) return;
+  const sl_gaussian& G = gs[g];
+  const uint32_t own = G.part_surface & 0xFFFFu;
+  const float* xf = parts[own].xf;
+  const f3 P = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  bool stale = B.force || (own < 32u && ((B.moved_mask >> own) & 1u));
+  for (uint32_t p = 0; p < B.part_count && p < 32u && !stale; p++) {
+    if (p == own || ((B.moved_mask >> p) & 1u) == 0u) continue;
+    const float* b = parts[p].bound;
+    const float r = b[3] + kNearR;
+    stale = len3(sub3(P, xf_point(parts[p].xf, F3(b[0], b[1], b[2])))) < r ||
+            len3(sub3(P, xf_point(parts[p].xf_prev, F3(b[0], b[1], b[2])))) < r;
+  }
+  if (!stale) return;
+  const Leaf nd = load_leaf(&nodes[g]);
+  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
+  float t[9];
+#pragma unroll
+  for (int m = 0; m < 9; m++) t[m] = 0.0f;
+  const sl_vgrid& vg = vgrid[g];
+  for (uint32_t c = 0; c < kCells; c++) {
+    const f3 w = cell_dir(tab, c);
+    const f3 u = xf_dir_inv(xf, w);
+    const float v = vgrid_lookup(vg, u) * 1.0f;
+    if (v <= 0.0f) continue;
+    const float a = nd.iso_norm * footprint(nd, s3 * s3, u) * v * cell_omega(tab, c);
+    float y[9];
+    sh2_basis(w, y);
+#pragma unroll
+    for (int m = 0; m < 9; m++) t[m] += a * y[m];
+  }
+  xfer[3u * g] = make_float4(t[0], t[1], t[2], t[3]);
+  xfer[3u * g + 1u] = make_float4(t[4], t[5], t[6], t[7]);
+  xfer[3u * g + 2u] = make_float4(t[8], 0.0f, 0.0f, 0.0f);
+}
+
+// direct_dirs_one + env_dirs_one for g = 4 i + frame % 4
+__global__ void __launch_bounds__(kThreads) direct_kernel(const __grid_constant__ BounceParams B,
+                                                          const __grid_constant__ ShadeParams SH,
+                                                          const sl_gaussian* __restrict__ gs,
+                                                          const sl_node* __restrict__ nodes,
+                                                          const sl_vgrid* __restrict__ vgrid,
+                                                          const sl_part* __restrict__ parts,
+                                                          const sl_material* __restrict__ mats,
+                                                          const float* __restrict__ tree,
+                                                          const float* __restrict__ lamp_T,
+                                                          const float4* __restrict__ env_T,
+                                                          float4* __restrict__ lo_dir) {
+  const uint32_t g = (blockIdx.x * kThreads + threadIdx.x) * 4u + B.frame % 4u;
+  if (g >= B.G) return;
+  const sl_gaussian& G = gs[g];
+  const Leaf nd = load_leaf(&nodes[g]);
+  const sl_material mat = mats[mat_index(G, SH.material_count)];
+  const float* xf = parts[G.part_surface & 0xFFFFu].xf;
+  const m3 Rq = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]);
+  const m3 Sloc = m3m(m3m(Rq, m3diag(F3(mat.flake[0], mat.flake[1], mat.flake[2]))), m3t(Rq));
+  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
+  const float detC = s3 * s3;
+  const f3 P = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  const f3 n = Rq.c[0];
+  const f3 Sd = F3(Sloc.c[0].x, Sloc.c[1].y, Sloc.c[2].z), So = F3(Sloc.c[1].x, Sloc.c[2].x, Sloc.c[2].y);
+  const f3 alb = F3(G.albedo[0], G.albedo[1], G.albedo[2]);
+  const float ks = spec_weight(mat);
+  const bool emissive = (mat.flags & 1u) != 0u;
+  const sl_vgrid& vg = vgrid[g];
+  f3 acc[14];
+#pragma unroll
+  for (int k = 0; k < 14; k++) acc[k] = F3(0.0f, 0.0f, 0.0f);
+  SpecPre sp;
+  if (ks > 0.0f) sp = spec_prepare(Sd, So);
+  if (SH.n_emit) {
+    uint32_t node = SH.root;
+    for (uint32_t guard = 0; node != kNone && guard < (1u << 16); guard++) {
+      const float* e = tree + 24u * node;
+      const uint32_t child_lo = __float_as_uint(e[11]), child_hi = __float_as_uint(e[15]);
+      const uint32_t skip = __float_as_uint(e[7]);
+      const f3 emean = F3(e[0], e[1], e[2]);
+      bool use;
+      if (child_lo == kNone || SH.mode == 0u) {
+        use = child_lo == kNone;
+      } else {
+        const f3 d = sub3(P, emean);
+        use = dot3(d, d) > SH.theta * SH.theta * e[3] * e[3];
+      }
+      if (!use) {
+        node = (child_lo != kNone && __float_as_uint(e[19]) == 0u) ? child_hi : skip;
+        continue;
+      }
+      node = skip;
+      const f3 d = sub3(emean, P);
+      const float d2 = dot3(d, d);
+      if (d2 < 1e-8f) continue;
+      const f3 ww = div3(d, sqrtf(d2));
+      const f3 wi = xf_dir_inv(xf, ww);
+      const float vi = vgrid_lookup(vg, wi);
+      if (vi <= 1e-7f) continue;
+      const float fp = footprint(nd, detC, wi);
+      const f3 mw = mul3(ww, -1.0f);
+      float s = 1.0f;
+      if (SH.one_sided) {
+        const float cs = dot3(mw, ld3(SH.normal));
+        s = SH.edge_soft > 0.0f ? smoothstepf(-SH.edge_soft, SH.edge_soft, cs) : (cs > 0.0f ? 1.0f : 0.0f);
+      }
+      const float mq = sqrtf(fmaxf(dot3(mw, sym_mul(F3(e[4], e[5], e[6]), F3(e[8], e[9], e[10]), mw)), 0.0f));
+      const f3 I = mul3(F3(e[12], e[13], e[14]), s * SH.scale * mq);
+      const f3 light = mul3(mul3(I, vi), fp / d2 * 1.0f);
+      if (ks <= 0.0f) {
+        acc[0] = add3(acc[0], light);
+        continue;
+      }
+      const f3 wr = mirror3(wi, n);
+      const float damp = iso_damp(nd.iso_norm, footprint(nd, detC, wr) * vgrid_lookup(vg, wr));
+#pragma unroll
+      for (int k = 0; k < 14; k++) {
+        const f3 wo = xf_dir_inv(xf, F3(c_dirs14[k][0], c_dirs14[k][1], c_dirs14[k][2]));
+        acc[k] = add3(acc[k], mul3(light, iso_lobe_from(ks, phase_specular_p(sp, wi, wo), damp)));
+      }
+    }
+  }
+  const float T = lamp_T[g];
+  const f3 a0 = acc[0];
+  f3 mean = F3(0.0f, 0.0f, 0.0f), c0 = F3(0.0f, 0.0f, 0.0f);
+  float ws = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 14; k++) {
+    const f3 ck = mul3(mul3v(alb, ks <= 0.0f ? a0 : acc[k]), T * nd.iso_norm);
+    if (k == 0) c0 = ck;
+    const f3 wo = xf_dir_inv(xf, F3(c_dirs14[k][0], c_dirs14[k][1], c_dirs14[k][2]));
+    const float w = footprint(nd, detC, wo) * vgrid_lookup(vg, wo);
+    mean = add3(mean, mul3(ck, w));
+    ws += w;
+  }
+  f3 c = ws > 0.0f ? div3(mean, fmaxf(ws, 1e-20f)) : c0;
+  if (SH.n_lights && !emissive) {
+    const float4 et = env_T[g];
+    const float Tk[4] = {et.x, et.y, et.z, et.w};
+    f3 dc = F3(0.0f, 0.0f, 0.0f);
+    for (uint32_t k = 0; k < SH.n_lights && k < 4u; k++) {
+      const f3 wi = xf_dir_inv(xf, ld3(SH.lights[k].dir));
+      const float v = vgrid_lookup(vg, wi);
+      if (v <= 1e-7f) continue;
+      dc = add3(dc, mul3(ld3(SH.lights[k].irr), Tk[k] * v * footprint(nd, detC, wi)));
+    }
+    c = add3(c, mul3(mul3v(alb, dc), nd.iso_norm));
+  }
+  lo_dir[g] = make_float4(c.x, c.y, c.z, 0.0f);
+}
+
+// node_leaf: per leaf and direction (L w, w), L its light toward the probes plus last frame's bounce
+__global__ void __launch_bounds__(kThreads) leaf_kernel(const __grid_constant__ BounceParams B,
+                                                        const sl_gaussian* __restrict__ gs,
+                                                        const sl_node* __restrict__ nodes,
+                                                        const sl_vgrid* __restrict__ vgrid,
+                                                        const sl_part* __restrict__ parts,
+                                                        const float* __restrict__ tab,
+                                                        const float4* __restrict__ lo_dir,
+                                                        const float4* __restrict__ lo_b, float4* __restrict__ acc) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= B.G) return;
+  const sl_gaussian& G = gs[g];
+  const Leaf nd = load_leaf(&nodes[g]);
+  const float* xf = parts[G.part_surface & 0xFFFFu].xf;
+  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
+  const float4 ld = lo_dir[g], lb = lo_b[3u * g + 1u];
+  const f3 L = add3(F3(ld.x, ld.y, ld.z), F3(lb.x, lb.y, lb.z));
+  const sl_vgrid& vg = vgrid[g];
+  for (int k = 0; k < 14; k++) {
+    const f3 wo = xf_dir_inv(xf, ld3(tab + kTabD14 + 3 * k));
+    const float w = footprint(nd, s3 * s3, wo) * vgrid_lookup(vg, wo);
+    acc[14u * g + (uint32_t)k] = make_float4(L.x * w, L.y * w, L.z * w, w);
+  }
+}
+
+// node_up for one depth: per (internal node, direction) the sum of its children's in kids order
+__global__ void __launch_bounds__(kThreads) up_kernel(const sl_node* __restrict__ nodes,
+                                                      const uint32_t* __restrict__ kids,
+                                                      const uint32_t* __restrict__ list, uint32_t count,
+                                                      float4* __restrict__ acc) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= count * 14u) return;
+  const uint32_t i = list[t / 14u], k = t % 14u;
+  const uint32_t lo = nodes[i].child_lo, hi = nodes[i].child_hi;
+  float4 s = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  for (uint32_t j = lo; j < hi; j++) {
+    const float4 c = acc[14u * kids[j] + k];
+    s.x += c.x;
+    s.y += c.y;
+    s.z += c.z;
+    s.w += c.w;
+  }
+  acc[14u * i + k] = s;
+}
+
+// node_sh2: the 14-direction means fitted to SH2 (pinv), 27 halves in 14 words
+__global__ void __launch_bounds__(kThreads) sh2_kernel(uint32_t N, const float* __restrict__ tab,
+                                                       const float4* __restrict__ acc, uint32_t* __restrict__ node_sh) {
+  const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= N) return;
+  f3 L[14];
+#pragma unroll
+  for (int k = 0; k < 14; k++) {
+    const float4 a = acc[14u * i + (uint32_t)k];
+    L[k] = div3(F3(a.x, a.y, a.z), fmaxf(a.w, 1e-12f));
+  }
+  float h[28];
+  h[27] = 0.0f;
+#pragma unroll
+  for (int m = 0; m < 9; m++) {
+    f3 c = F3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+    for (int k = 0; k < 14; k++) c = add3(c, mul3(L[k], tab[kTabPinv + 14 * m + k]));
+    h[3 * m] = c.x;
+    h[3 * m + 1] = c.y;
+    h[3 * m + 2] = c.z;
+  }
+#pragma unroll
+  for (int j = 0; j < 14; j++) {
+    const uint32_t lo = __half_as_ushort(__float2half_rn(h[2 * j]));
+    const uint32_t hi = __half_as_ushort(__float2half_rn(h[2 * j + 1]));
+    node_sh[14u * i + (uint32_t)j] = lo | (hi << 16);
+  }
+}
+
+__device__ __forceinline__ f3 node_radiance(const uint32_t* __restrict__ node_sh, uint32_t ni, const float* b) {
+  float h[28];
+#pragma unroll
+  for (int j = 0; j < 14; j++) {
+    const uint32_t u = node_sh[14u * ni + (uint32_t)j];
+    h[2 * j] = __half2float(__ushort_as_half((unsigned short)(u & 0xFFFFu)));
+    h[2 * j + 1] = __half2float(__ushort_as_half((unsigned short)(u >> 16)));
+  }
+  f3 v = F3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+  for (int m = 0; m < 9; m++) v = add3(v, mul3(F3(h[3 * m], h[3 * m + 1], h[3 * m + 2]), b[m]));
+  return v;
+}
+
+// probe_gather: one (probe, cell) ray per thread
+__global__ void __launch_bounds__(kThreads) gather_kernel(const __grid_constant__ BounceParams B,
+                                                          const sl_node* __restrict__ tnodes,
+                                                          const uint32_t* __restrict__ kids,
+                                                          const sl_vgrid* __restrict__ vgrid,
+                                                          const sl_part* __restrict__ parts,
+                                                          const float* __restrict__ tab,
+                                                          const float* __restrict__ ground,
+                                                          const uint32_t* __restrict__ node_sh,
+                                                          float4* __restrict__ pd) {
+  const uint32_t id = blockIdx.x * kThreads + threadIdx.x;
+  if (id >= B.NP * kCells) return;
+  const uint32_t p = id / kCells, c = id % kCells;
+  const f3 o = probe_pos(B, ground, p);
+  const f3 w = cell_dir(tab, c);
+  f3 cen = o;
+  if (!B.terrain) {
+    const uint32_t dz = B.dims[2];
+    const float bx = (float)((p / (B.dims[1] * dz)) / 2u), by = (float)(((p / dz) % B.dims[1]) / 2u),
+                bz = (float)((p % dz) / 2u);
+    cen = F3(B.lo[0] + B.step[0] * (2.0f * bx + 0.5f), B.lo[1] + B.step[1] * (2.0f * by + 0.5f),
+             B.lo[2] + B.step[2] * (2.0f * bz + 0.5f));
+  }
+  const float t1 = B.tmax;
+  float ht[kHitMax], hv[kHitMax];
+  uint32_t hn[kHitMax];
+  uint32_t k = 0;
+  uint32_t stack[kStack];
+  for (uint32_t q = 0; q < B.part_count; q++) {
+    const float* xf = parts[q].xf;
+    const uint32_t root = parts[q].root;
+    if (root == kNone) continue;
+    const f3 Po = xf_dir_inv(xf, sub3(o, F3(xf[3], xf[7], xf[11])));
+    const f3 wr = xf_dir_inv(xf, w);
+    const f3 cr = xf_dir_inv(xf, sub3(cen, F3(xf[3], xf[7], xf[11])));
+    stack[0] = root;
+    uint32_t sp = 1;
+    while (sp > 0u) {
+      sp--;
+      const uint32_t ni = stack[sp];
+      const GNode nd = load_gnode(&tnodes[ni]);
+      const f3 d = sub3(nd.mean, Po);
+      const float tt = clampf(dot3(d, wr), 0.0f, t1);
+      const f3 e = sub3(d, mul3(wr, tt));
+      if (dot3(e, e) > nd.radius * nd.radius) continue;
+      bool use_node = ni < B.G;
+      if (!use_node) use_node = len3(sub3(cr, nd.mean)) - B.brad > kProbeTheta * nd.smax;
+      if (use_node) {
+        const float tau = nd.kappa * sqrtf(fmaxf(dot3(wr, sym_mul(nd.sn_d, nd.sn_o, wr)), 0.0f)) *
+                          seg_geom(nd, Po, wr, 0.0f, t1);
+        if (tau > 1e-6f) {
+          const f3 cw = sym_mul(nd.cinv_d, nd.cinv_o, wr);
+          const float den = dot3(cw, wr);
+          const float tp = fabsf(den) > 1e-30f ? clampf(dot3(cw, d) / den, 0.0f, t1) : t1;
+          uint32_t at = k < kHitMax - 1u ? k : kHitMax - 1u;
+          const uint32_t l = kHitMax - 1u;
+          if (k == kHitMax && tp >= ht[l]) {
+            ht[l] = fmaxf(ht[l], tp);
+            hv[l] = fminf(hv[l] + tau, 64.0f);
+            continue;
+          }
+          const bool full = k == kHitMax;
+          const float sv = full ? hv[l] : 0.0f, stv = full ? ht[l] : 0.0f;
+          while (at > 0u && ht[at - 1u] > tp) {
+            ht[at] = ht[at - 1u];
+            hv[at] = hv[at - 1u];
+            hn[at] = hn[at - 1u];
+            at--;
+          }
+          ht[at] = tp;
+          hv[at] = tau;
+          hn[at] = ni;
+          if (full) {
+            ht[l] = fmaxf(ht[l], stv);
+            hv[l] = fminf(hv[l] + sv, 64.0f);
+          }
+          k = k + 1u < kHitMax ? k + 1u : kHitMax;
+        }
+      } else {
+        for (uint32_t j = nd.child_lo; j < nd.child_hi; j++)
+          if (sp < kStack) stack[sp++] = kids[j];
+      }
+    }
+  }
+  float T = 1.0f, m1 = 0.0f, m2 = 0.0f, first_part = -1.0f, nearv = 0.0f;
+  f3 acc = F3(0.0f, 0.0f, 0.0f);
+  float bw[9];
+  sh2_basis(mul3(w, -1.0f), bw);
+  for (uint32_t i = 0; i < k; i++) {
+    if (T <= 0.0f) break;
+    const float al = 1.0f - lm_exp(-hv[i]);
+    const f3 rad = max0(node_radiance(node_sh, hn[i], bw));
+    acc = add3(acc, mul3(rad, T * al));
+    const float dep = clampf(ht[i], 0.0f, t1);
+    m1 += T * al * dep;
+    m2 += T * al * dep * dep;
+    const float Tn = T * (1.0f - al);
+    if (T >= 0.5f && Tn < 0.5f) {
+      const uint32_t hp = tnodes[hn[i]].part;
+      first_part = (float)hp;
+      nearv = dep < 0.05f ? 1.0f : 0.0f;
+      if (hn[i] < B.G && hp < B.part_count &&
+          vgrid_lookup(vgrid[hn[i]], xf_dir_inv(parts[hp].xf, mul3(w, -1.0f))) < 0.1f)
+        nearv += 2.0f;
+    }
+    T = Tn;
+  }
+  if (B.has_sky && t1 >= B.tmax * 0.999f) acc = add3(acc, mul3(sky_radiance(B.sky, w), T));
+  m1 += T * t1;
+  m2 += T * t1 * t1;
+  const float a = B.alpha;
+  const float4 old0 = pd[2u * id], old1 = pd[2u * id + 1u];
+  pd[2u * id] = make_float4(mixf(old0.x, acc.x, a), mixf(old0.y, acc.y, a), mixf(old0.z, acc.z, a), first_part);
+  pd[2u * id + 1u] = make_float4(mixf(old1.x, m1, a), mixf(old1.y, m2, a), old1.z, nearv);
+}
+
+// probe_valid: one probe per thread
+__global__ void __launch_bounds__(kThreads) valid_kernel(const __grid_constant__ BounceParams B,
+                                                         const sl_part* __restrict__ parts, float4* __restrict__ pd) {
+  const uint32_t p = blockIdx.x * kThreads + threadIdx.x;
+  if (p >= B.NP) return;
+  uint32_t cnt[17];
+#pragma unroll
+  for (int i = 0; i < 17; i++) cnt[i] = 0u;
+  uint32_t nearc = 0, back = 0;
+  for (uint32_t c = 0; c < kCells; c++) {
+    const float4 r0 = pd[2u * (p * kCells + c)], r1 = pd[2u * (p * kCells + c) + 1u];
+    const uint32_t fl = (uint32_t)(fmaxf(r1.w, 0.0f) + 0.5f);
+    nearc += fl & 1u;
+    back += (fl >> 1u) & 1u;
+    if (r0.w >= 0.0f) {
+      const uint32_t q = (uint32_t)r0.w;
+      cnt[q < 16u ? q : 16u]++;
+    }
+  }
+  bool enclosed = false;
+  for (uint32_t q = 0; q < B.part_count && q < 16u; q++)
+    if ((parts[q].flags & 1u) == 0u && (float)cnt[q] > kGValid * (float)kCells) enclosed = true;
+  const float valid = (enclosed || nearc * 2u > kCells || back * 2u > kCells) ? 0.0f : 1.0f;
+  pd[2u * (p * kCells) + 1u].z = valid;
+}
+
+// probe_sh2: one probe per thread
+__global__ void __launch_bounds__(kThreads) psh2_kernel(const __grid_constant__ BounceParams B,
+                                                        const float* __restrict__ tab, const float4* __restrict__ pd,
+                                                        float4* __restrict__ probe_sh) {
+  const uint32_t p = blockIdx.x * kThreads + threadIdx.x;
+  if (p >= B.NP) return;
+  f3 c9[9];
+#pragma unroll
+  for (int m = 0; m < 9; m++) c9[m] = F3(0.0f, 0.0f, 0.0f);
+  for (uint32_t c = 0; c < kCells; c++) {
+    const float4 r0 = pd[2u * (p * kCells + c)];
+    const f3 L = mul3(F3(r0.x, r0.y, r0.z), cell_omega(tab, c));
+    float y[9];
+    sh2_basis(cell_dir(tab, c), y);
+#pragma unroll
+    for (int m = 0; m < 9; m++) c9[m] = add3(c9[m], mul3(L, y[m]));
+  }
+#pragma unroll
+  for (int m = 0; m < 9; m++) probe_sh[9u * p + (uint32_t)m] = make_float4(c9[m].x, c9[m].y, c9[m].z, 0.0f);
+}
+
+// bounce_sh + gloss_sh: one Gaussian per thread
+__global__ void __launch_bounds__(kThreads) bounce_kernel(const __grid_constant__ BounceParams B,
+                                                          const sl_gaussian* __restrict__ gs,
+                                                          const sl_node* __restrict__ nodes,
+                                                          const sl_vgrid* __restrict__ vgrid,
+                                                          const sl_part* __restrict__ parts,
+                                                          const sl_material* __restrict__ mats,
+                                                          const float* __restrict__ ground,
+                                                          const float4* __restrict__ pd,
+                                                          const float4* __restrict__ probe_sh,
+                                                          const float4* __restrict__ xfer, float4* __restrict__ lo_b) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= B.G) return;
+  const sl_gaussian& G = gs[g];
+  const sl_material mat = mats[mat_index(G, B.mat_count)];
+  const float ks = spec_weight(mat);
+  const float lw = sqrtf(fminf(mat.flake[1], mat.flake[2]) / fmaxf(mat.flake[0], 1e-12f));
+  if (ks > 0.0f && !(lw >= kGlossShMin)) return;
+  const uint32_t own = G.part_surface & 0xFFFFu;
+  const float* xf = parts[own].xf;
+  const f3 P = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  const Weights pw = probe_weights(B, ground, pd, P);
+  f3 Lsh[9];
+#pragma unroll
+  for (int m = 0; m < 9; m++) Lsh[m] = F3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const float wq = pw.w[q];
+    if (wq <= 0.0f) continue;
+#pragma unroll
+    for (int m = 0; m < 9; m++) {
+      const float4 s = probe_sh[9u * pw.pid[q] + (uint32_t)m];
+      Lsh[m] = add3(Lsh[m], mul3(F3(s.x, s.y, s.z), wq));
+    }
+  }
+  const float4 t0 = xfer[3u * g], t1 = xfer[3u * g + 1u], t2 = xfer[3u * g + 2u];
+  const float t[9] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w, t2.x};
+  f3 cc = mul3(Lsh[0], t[0]);
+#pragma unroll
+  for (int m = 1; m < 9; m++) cc = add3(cc, mul3(Lsh[m], t[m]));
+  const f3 alb = F3(G.albedo[0], G.albedo[1], G.albedo[2]);
+  const f3 cb = mul3v(alb, max0(cc));
+  f3 eyec = cb;
+  if (ks > 0.0f) {
+    const Leaf nd = load_leaf(&nodes[g]);
+    const m3 Rq = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]);
+    const f3 n = Rq.c[0];
+    const f3 wo = xf_dir_inv(xf, norm3(sub3(ld3(B.eye), P)));
+    const f3 wm = mirror3(wo, n);
+    const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
+    const float detC = s3 * s3;
+    const sl_vgrid& vg = vgrid[g];
+    const float vis = vgrid_lookup(vg, wm) * footprint(nd, detC, wm);
+    f3 sp = F3(0.0f, 0.0f, 0.0f);
+    if (vis > 0.0f) {
+      const float damp = iso_damp(nd.iso_norm, footprint(nd, detC, wo) * vgrid_lookup(vg, wo));
+      const float sg = 2.0f * lw;
+      const float a1 = lm_exp(-sg * sg), a2 = lm_exp(-3.0f * sg * sg);
+      const f3 wmw = F3(xf[0] * wm.x + xf[1] * wm.y + xf[2] * wm.z, xf[4] * wm.x + xf[5] * wm.y + xf[6] * wm.z,
+                        xf[8] * wm.x + xf[9] * wm.y + xf[10] * wm.z);
+      float y[9];
+      sh2_basis(wmw, y);
+      f3 Lm = mul3(Lsh[0], y[0]);
+#pragma unroll
+      for (int m = 1; m < 4; m++) Lm = add3(Lm, mul3(Lsh[m], a1 * y[m]));
+#pragma unroll
+      for (int m = 4; m < 9; m++) Lm = add3(Lm, mul3(Lsh[m], a2 * y[m]));
+      sp = mul3(mul3v(mul3(mul3(mul3(mul3(mul3(alb, nd.iso_norm), ks), 4.0f), kPi), damp), max0(Lm)), vis);
+    }
+    eyec = add3(mul3(cb, 1.0f - ks), sp);
+  }
+  lo_b[3u * g] = make_float4(eyec.x, eyec.y, eyec.z, 0.0f);
+  lo_b[3u * g + 1u] = make_float4(cb.x, cb.y, cb.z, 0.0f);
+  lo_b[3u * g + 2u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+inline uint32_t blocks(uint64_t n) { return (uint32_t)((n + kThreads - 1) / kThreads); }
+
+}  // namespace
+
+cudaError_t launch_bounce_frame(const BounceParams& B, const ShadeParams& SH, const BounceBuffers& D,
+                                const std::vector<uint32_t>& level_off, const std::vector<uint32_t>& level_cnt,
+                                cudaStream_t s) {
+  if (B.G == 0) return cudaSuccess;
+  xfer_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.tab, D.xfer);
+  const uint64_t quarter = (B.G + 3u) / 4u;
+  direct_kernel<<<blocks(quarter), kThreads, 0, s>>>(B, SH, D.gs, D.nodes, D.vgrid, D.parts, D.mats, D.tree, D.lamp_T,
+                                                     D.env_T, D.lo_dir);
+  leaf_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.tab, D.lo_dir, D.lo_b,
+                                               D.node_acc);
+  for (int d = (int)level_cnt.size() - 1; d >= 1; d--) {
+    const uint32_t n = level_cnt[(size_t)d];
+    if (n == 0) continue;
+    up_kernel<<<blocks(14ull * n), kThreads, 0, s>>>(D.tnodes, D.kids, D.up_list + level_off[(size_t)d], n,
+                                                     D.node_acc);
+  }
+  sh2_kernel<<<blocks(B.N), kThreads, 0, s>>>(B.N, D.tab, D.node_acc, D.node_sh);
+  if (B.NP) {
+    gather_kernel<<<blocks((uint64_t)B.NP * kCells), kThreads, 0, s>>>(B, D.tnodes, D.kids, D.vgrid, D.parts, D.tab,
+                                                                       D.ground, D.node_sh, D.probe_data);
+    valid_kernel<<<blocks(B.NP), kThreads, 0, s>>>(B, D.parts, D.probe_data);
+    psh2_kernel<<<blocks(B.NP), kThreads, 0, s>>>(B, D.tab, D.probe_data, D.probe_sh);
+  }
+  bounce_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.mats, D.ground, D.probe_data,
+                                                 D.probe_sh, D.xfer, D.lo_b);
+  return cudaGetLastError();
+}
+
+}  // namespace sl

@@ -233,20 +233,6 @@ void eig3(const double* m, double* ev) {
   ev[2] = e1;
 }
 
-// iso_init cell directions and solid angles (iso_init.wgsl:39-45), float64 then rounded
-void iso_dirs(float* d) {
-  for (int c = 0; c < 128; c++) {
-    int i = c / 16, j = c % 16;
-    double el = 0.5 * M_PI - (i + 0.5) * M_PI / 8.0;
-    double az = -M_PI + (j + 0.5) * 2.0 * M_PI / 16.0;
-    double top = 0.5 * M_PI - i * M_PI / 8.0;
-    d[4 * c + 0] = (float)(std::cos(el) * std::cos(az));
-    d[4 * c + 1] = (float)(std::cos(el) * std::sin(az));
-    d[4 * c + 2] = (float)std::sin(el);
-    d[4 * c + 3] = (float)((2.0 * M_PI / 16.0) * (std::sin(top) - std::sin(top - M_PI / 8.0)));
-  }
-}
-
 void levels_for(uint32_t res, uint32_t& levels, uint32_t* level_off, uint32_t& layer_texels) {
   uint32_t off = 0;
   levels = 0;
@@ -289,6 +275,66 @@ void basis_k32(const float* w, float* t1, float* t2) {
 }  // namespace sl
 
 namespace sl {
+
+// iso_init cell directions and solid angles (iso_init.wgsl:39-45), float64 then rounded
+void iso_dirs(float* d) {
+  for (int c = 0; c < 128; c++) {
+    int i = c / 16, j = c % 16;
+    double el = 0.5 * M_PI - (i + 0.5) * M_PI / 8.0;
+    double az = -M_PI + (j + 0.5) * 2.0 * M_PI / 16.0;
+    double top = 0.5 * M_PI - i * M_PI / 8.0;
+    d[4 * c + 0] = (float)(std::cos(el) * std::cos(az));
+    d[4 * c + 1] = (float)(std::cos(el) * std::sin(az));
+    d[4 * c + 2] = (float)std::sin(el);
+    d[4 * c + 3] = (float)((2.0 * M_PI / 16.0) * (std::sin(top) - std::sin(top - M_PI / 8.0)));
+  }
+}
+
+// D14 (lighting.js:188-189: the 6 axes, the verticals leaning 1e-4 off the pole, and the 8 diagonals / sqrt 3) and
+// pinvD14 (:192-207): the least-squares SH2 fit (A^T A)^-1 A^T of values on them, Gauss-Jordan with partial pivoting
+void bounce_tables(float* d14, float* pinv) {
+  static const double raw[14][3] = {{1, 0, 0}, {0, 1, 0}, {1e-4, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {1e-4, 0, -1},
+                                    {1, 1, 1}, {1, 1, -1}, {1, -1, 1}, {1, -1, -1},
+                                    {-1, 1, 1}, {-1, 1, -1}, {-1, -1, 1}, {-1, -1, -1}};
+  double A[14][9];
+  for (int k = 0; k < 14; k++) {
+    const double s = k < 6 ? 1.0 : 1.0 / std::sqrt(3.0);
+    const double x = raw[k][0] * s, y = raw[k][1] * s, z = raw[k][2] * s;
+    const double b[9] = {0.282095, 0.488603 * y, 0.488603 * z, 0.488603 * x, 1.092548 * x * y, 1.092548 * y * z,
+                         0.315392 * (3 * z * z - 1), 1.092548 * x * z, 0.546274 * (x * x - y * y)};
+    for (int m = 0; m < 9; m++) A[k][m] = b[m];
+    d14[3 * k] = (float)x;
+    d14[3 * k + 1] = (float)y;
+    d14[3 * k + 2] = (float)z;
+  }
+  double M[9][18];
+  for (int i = 0; i < 9; i++)
+    for (int j = 0; j < 9; j++) {
+      double acc = 0.0;
+      for (int r = 0; r < 14; r++) acc += A[r][i] * A[r][j];
+      M[i][j] = acc;
+      M[i][9 + j] = i == j ? 1.0 : 0.0;
+    }
+  for (int c = 0; c < 9; c++) {
+    int piv = c;
+    for (int r = c + 1; r < 9; r++)
+      if (std::fabs(M[r][c]) > std::fabs(M[piv][c])) piv = r;
+    for (int j = 0; j < 18; j++) std::swap(M[c][j], M[piv][j]);
+    const double dv = M[c][c];
+    for (int j = 0; j < 18; j++) M[c][j] /= dv;
+    for (int r = 0; r < 9; r++) {
+      if (r == c) continue;
+      const double f = M[r][c];
+      for (int j = 0; j < 18; j++) M[r][j] -= f * M[c][j];
+    }
+  }
+  for (int m = 0; m < 9; m++)
+    for (int k = 0; k < 14; k++) {
+      double acc = 0.0;
+      for (int j = 0; j < 9; j++) acc += M[m][9 + j] * A[k][j];
+      pinv[14 * m + k] = (float)acc;
+    }
+}
 
 // Skip links for a stackless walk of the light cut (the GPU shading pass).  The cut is the walk of a 48-entry stack
 // that pushes (lo, hi) and so pops hi first: node order = preorder with the hi subtree before the lo one.  Per node,
@@ -483,9 +529,12 @@ int sl_lighting_destroy(sl_lighting* l) {
     l->r->lighting = nullptr;
     l->r->colour = nullptr;
   }
+  if (l->r && l->r->lo_b == l->lo_b.as<float4>()) l->r->lo_b = nullptr;
   sl::DevBuf* all[] = {&l->nodes, &l->vgrid, &l->materials, &l->parts, &l->tree, &l->lamp_T, &l->env_T, &l->colour,
                        &l->lm_acc, &l->lm_mip, &l->sm_acc, &l->sm_mip, &l->sm_layers, &l->sm_dirty, &l->order,
-                       &l->g_blur, &l->n_blur, &l->tree_nodes, &l->node_parent};
+                       &l->g_blur, &l->n_blur, &l->tree_nodes, &l->node_parent, &l->kids, &l->bn_tab,
+                       &l->bn_ground, &l->bn_up, &l->probe_data, &l->probe_sh, &l->xfer, &l->lo_dir, &l->lo_b,
+                       &l->node_acc, &l->node_sh};
   for (sl::DevBuf* b : all) b->release();
   delete l;
   return SL_OK;
@@ -601,10 +650,19 @@ int sl_lighting_set_tree(sl_lighting* l, const sl_node* nodes, uint32_t n_nodes,
   }
   SL_CHECK_CUDA(l->tree_nodes.ensure(sizeof(sl_node) * (size_t)n_nodes), "tree nodes");
   SL_CHECK_CUDA(l->node_parent.ensure(4ull * n_nodes), "node parents");
+  SL_CHECK_CUDA(l->kids.ensure(4ull * n_kids + 16), "kids");
   SL_CHECK_CUDA(cudaMemcpy(l->tree_nodes.ptr, nodes, sizeof(sl_node) * (size_t)n_nodes, cudaMemcpyHostToDevice),
                 "tree nodes");
   SL_CHECK_CUDA(cudaMemcpy(l->node_parent.ptr, parent.data(), 4ull * n_nodes, cudaMemcpyHostToDevice), "node parents");
+  if (n_kids) SL_CHECK_CUDA(cudaMemcpy(l->kids.ptr, kids, 4ull * n_kids, cudaMemcpyHostToDevice), "kids");
+  l->tree_depth.resize(n_nodes);
+  l->tree_part.resize(n_nodes);
+  for (uint32_t i = 0; i < n_nodes; i++) {
+    l->tree_depth[i] = nodes[i].depth;
+    l->tree_part[i] = nodes[i].part;
+  }
   l->n_tree = n_nodes;
+  l->bounce_on = false;  // the probes are laid over a tree: set them again
   l->blur_init = false;
   l->lm_dirty = true;
   l->sm_dirty_all = true;
@@ -867,6 +925,46 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
                              l->tree.as<float>(), l->lamp_T.as<float>(), l->env_T.as<float4>(), l->order.as<uint32_t>(),
                              l->colour.as<float4>(), G, s),
                 "shade");
+  if (l->bounce_on) {  // the probe bounce after the shading (lighting.js encodeBounce, ?sendercut=0)
+    for (uint32_t q = 0; q < P; q++)
+      if (r->parts[q].root != 0xFFFFFFFFu && r->parts[q].root >= l->n_tree)
+        return fail(SL_ERR_INVALID_ARG, "a part's tree root lies outside the tree set by sl_lighting_set_tree");
+    BounceParams B = l->BP;
+    B.part_count = P;
+    B.alpha = l->bn_first ? 1.0f : l->bn_blend;
+    B.frame = l->bn_frame;
+    B.force = l->bn_first ? 1u : 0u;
+    B.moved_mask = moved_mask;
+    B.has_sky = l->has_sky ? 1u : 0u;
+    memcpy(B.sky, l->sky, sizeof(B.sky));
+    for (int k = 0; k < 3; k++) B.eye[k] = eye[k];
+    ShadeParams SHd;
+    shade_params(l, eye, SHd);
+    BounceBuffers D{};
+    D.gs = gs;
+    D.nodes = l->nodes.as<sl_node>();
+    D.tnodes = l->tree_nodes.as<sl_node>();
+    D.kids = l->kids.as<uint32_t>();
+    D.vgrid = l->vgrid.as<sl_vgrid>();
+    D.parts = parts;
+    D.mats = l->materials.as<sl_material>();
+    D.tree = l->tree.as<float>();
+    D.lamp_T = l->lamp_T.as<float>();
+    D.env_T = l->env_T.as<float4>();
+    D.tab = l->bn_tab.as<float>();
+    D.ground = l->bn_ground.as<float>();
+    D.up_list = l->bn_up.as<uint32_t>();
+    D.xfer = l->xfer.as<float4>();
+    D.lo_dir = l->lo_dir.as<float4>();
+    D.lo_b = l->lo_b.as<float4>();
+    D.node_acc = l->node_acc.as<float4>();
+    D.probe_data = l->probe_data.as<float4>();
+    D.probe_sh = l->probe_sh.as<float4>();
+    D.node_sh = l->node_sh.as<uint32_t>();
+    SL_CHECK_CUDA(launch_bounce_frame(B, SHd, D, l->bn_level_off, l->bn_level_cnt, s), "probe bounce");
+    l->bn_first = false;
+    l->bn_frame++;
+  }
   return SL_OK;
 }
 
@@ -902,7 +1000,108 @@ int sl_renderer_bind_lighting(sl_renderer* r, sl_lighting* l) {
   if (l->r != r) return fail(SL_ERR_INVALID_ARG, "the lighting object belongs to another renderer");
   r->lighting = l;
   r->colour = l->colour.as<float4>();
-  r->lo_b = nullptr;
+  r->lo_b = l->bounce_on ? l->lo_b.as<float4>() : nullptr;
+  return SL_OK;
+}
+
+int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* lay, uint32_t max_depth, float blend) {
+  if (!l || !lay) return fail(SL_ERR_INVALID_ARG, "null argument");
+  if (l->n_tree < l->count || l->tree_depth.size() != l->n_tree)
+    return fail(SL_ERR_INVALID_ARG, "the probe gather walks the scene's tree: sl_lighting_set_tree first");
+  const uint32_t dx = lay->dims[0], dy = lay->dims[1], dz = lay->dims[2];
+  if (dx < 2 || dy < 2 || dz < 2 || dz > 16 || (uint64_t)dx * dy > 1024)
+    return fail(SL_ERR_INVALID_ARG, "probe layout: 2..16 levels and 2 x 2 .. 1024 columns");
+  if (!(lay->tmax > 0.0f) || !(lay->step[0] > 0.0f) || !(lay->step[1] > 0.0f))
+    return fail(SL_ERR_INVALID_ARG, "probe layout: positive spacing and ray length");
+  for (uint32_t k = 0; k + 1 < dz; k++)
+    if (!(lay->levels[k + 1] > lay->levels[k])) return fail(SL_ERR_INVALID_ARG, "probe levels must ascend");
+  if (!(blend > 0.0f && blend <= 1.0f)) return fail(SL_ERR_INVALID_ARG, "blend must be in (0, 1]");
+  cudaSetDevice(l->device);
+  const uint32_t G = l->count, N = l->n_tree, NP = dx * dy * dz;
+  BounceParams& B = l->BP;
+  B = BounceParams{};
+  B.G = G;
+  B.N = N;
+  B.NP = NP;
+  B.mat_count = l->material_count;
+  B.dims[0] = dx;
+  B.dims[1] = dy;
+  B.dims[2] = dz;
+  B.terrain = lay->terrain ? 1u : 0u;
+  for (int k = 0; k < 3; k++) {
+    B.lo[k] = lay->lo[k];
+    B.step[k] = lay->step[k];
+  }
+  for (uint32_t k = 0; k < 16; k++) B.levels[k] = lay->levels[k];
+  B.tmax = lay->tmax;
+  // block_rad (lighting.js:794): half the cell diagonal, float64; terrain probes each cut around themselves
+  B.brad = B.terrain ? 0.0f
+                     : (float)(0.5 * std::sqrt((double)B.step[0] * B.step[0] + (double)B.step[1] * B.step[1] +
+                                               (double)B.step[2] * B.step[2]));
+  // node_up's lists: internal nodes with a part at depths 1 .. max_depth - 1 (lighting.js:771-789)
+  uint32_t md = max_depth;
+  if (md == 0)
+    for (uint32_t i = G; i < N; i++) md = std::max(md, l->tree_depth[i] + 1u);
+  std::vector<std::vector<uint32_t>> by(md + 1);
+  for (uint32_t i = G; i < N; i++)
+    if (l->tree_part[i] != 0xFFFFFFFFu && l->tree_depth[i] <= md) by[l->tree_depth[i]].push_back(i);
+  std::vector<uint32_t> up;
+  l->bn_level_off.assign(md, 0);
+  l->bn_level_cnt.assign(md, 0);
+  for (uint32_t d = 0; d < md; d++) {
+    l->bn_level_off[d] = (uint32_t)up.size();
+    l->bn_level_cnt[d] = (uint32_t)by[d].size();
+    up.insert(up.end(), by[d].begin(), by[d].end());
+  }
+  float tab[kTabFloats];
+  iso_dirs(tab + kTabCells);
+  bounce_tables(tab + kTabD14, tab + kTabPinv);
+  SL_CHECK_CUDA(l->bn_tab.ensure(sizeof(tab)), "bounce table");
+  SL_CHECK_CUDA(cudaMemcpy(l->bn_tab.ptr, tab, sizeof(tab), cudaMemcpyHostToDevice), "bounce table");
+  SL_CHECK_CUDA(l->bn_up.ensure(4ull * up.size() + 16), "node_up lists");
+  if (!up.empty()) SL_CHECK_CUDA(cudaMemcpy(l->bn_up.ptr, up.data(), 4ull * up.size(), cudaMemcpyHostToDevice), "lists");
+  SL_CHECK_CUDA(l->bn_ground.ensure(4ull * dx * dy), "ground");
+  std::vector<float> ground(dx * dy, 0.0f);
+  if (lay->ground) memcpy(ground.data(), lay->ground, 4ull * dx * dy);
+  SL_CHECK_CUDA(cudaMemcpy(l->bn_ground.ptr, ground.data(), 4ull * dx * dy, cudaMemcpyHostToDevice), "ground");
+  struct Sz {
+    sl::DevBuf* b;
+    size_t bytes;
+  } bufs[] = {{&l->probe_data, 32ull * NP * 128}, {&l->probe_sh, 144ull * NP}, {&l->xfer, 48ull * G},
+              {&l->lo_dir, 16ull * G}, {&l->lo_b, 48ull * G}, {&l->node_acc, 224ull * N}, {&l->node_sh, 56ull * N}};
+  for (const Sz& z : bufs) {
+    SL_CHECK_CUDA(z.b->ensure(z.bytes), "bounce buffers");
+    SL_CHECK_CUDA(cudaMemset(z.b->ptr, 0, z.bytes), "bounce buffers");
+  }
+  l->bn_blend = blend;
+  l->bn_first = true;
+  l->bn_frame = 0;
+  l->bounce_on = true;
+  if (l->r && l->r->lighting == l) l->r->lo_b = l->lo_b.as<float4>();
+  return SL_OK;
+}
+
+int sl_lighting_set_sky(sl_lighting* l, const float* sh_rgb, uint32_t n_coef) {
+  if (!l || (n_coef && !sh_rgb)) return fail(SL_ERR_INVALID_ARG, "null argument");
+  if (n_coef > 16) return fail(SL_ERR_INVALID_ARG, "the probes' sky holds SH bands 0-3 (16 coefficients)");
+  memset(l->sky, 0, sizeof(l->sky));
+  if (n_coef) memcpy(l->sky, sh_rgb, 12ull * n_coef);
+  l->has_sky = n_coef > 0;
+  l->bn_first = true;  // the probes re-gather the new sky (environment.js:151)
+  return SL_OK;
+}
+
+int sl_lighting_read_bounce(sl_lighting* l, uint32_t what, void* dst, size_t bytes) {
+  if (!l || !dst) return fail(SL_ERR_INVALID_ARG, "null argument");
+  if (!l->bounce_on) return fail(SL_ERR_INVALID_ARG, "no probes set");
+  const size_t G = l->count, N = l->n_tree, NP = l->BP.NP;
+  const sl::DevBuf* src[] = {&l->lo_b, &l->lo_dir, &l->xfer, &l->probe_sh, &l->probe_data, &l->node_sh, &l->node_acc};
+  const size_t size[] = {48 * G, 16 * G, 48 * G, 144 * NP, 32 * NP * 128, 56 * N, 224 * N};
+  if (what >= 7) return fail(SL_ERR_INVALID_ARG, "unknown bounce buffer");
+  if (bytes > size[what]) return fail(SL_ERR_INVALID_ARG, "read past the bounce buffer");
+  cudaSetDevice(l->device);
+  SL_CHECK_CUDA(cudaDeviceSynchronize(), "sync");
+  SL_CHECK_CUDA(cudaMemcpy(dst, src[what]->ptr, bytes, cudaMemcpyDeviceToHost), "bounce read");
   return SL_OK;
 }
 

@@ -1,0 +1,59 @@
+// Internal declarations of the probe bounce (bounce.cu): its parameter block and device buffers.
+#pragma once
+
+#include <vector>
+
+#include "sl_lighting.h"
+
+struct sl_lighting;
+
+namespace sl {
+
+// the constant table (one device buffer): 128 cells x (direction, solid angle), D14, the 9 x 14 SH2 fit
+constexpr uint32_t kTabCells = 0;
+constexpr uint32_t kTabD14 = 512;
+constexpr uint32_t kTabPinv = 512 + 42;
+constexpr uint32_t kTabFloats = 512 + 42 + 126;
+
+// bounce.wgsl ProbeParams (the fields this path reads) + the frame's inputs
+struct BounceParams {
+  uint32_t G, N, NP, part_count, mat_count;
+  uint32_t dims[3], terrain;
+  float lo[3], step[3], levels[16];
+  float tmax, brad, alpha;
+  uint32_t frame, force, moved_mask, has_sky;
+  float eye[3];
+  float sky[48];  // 16 SH coefficients (bands 0-3), rgb
+};
+
+struct BounceBuffers {
+  const sl_gaussian* gs;
+  const sl_node* nodes;   // the lighting's leaves (iso_norm)
+  const sl_node* tnodes;  // the tree: the leaves, then the internal nodes
+  const uint32_t* kids;
+  const sl_vgrid* vgrid;
+  const sl_part* parts;
+  const sl_material* mats;
+  const float* tree;      // emitter tree
+  const float* lamp_T;
+  const float4* env_T;
+  const float* tab;
+  const float* ground;    // dims[0] x dims[1] ground heights, or null
+  const uint32_t* up_list;  // internal nodes grouped by depth
+  float4 *xfer, *lo_dir, *lo_b, *node_acc, *probe_data, *probe_sh;
+  uint32_t* node_sh;
+};
+
+// The shading pass's parameters for an eye (capi_lighting.cu); iso_init's 128 cells, float64 then rounded.
+void shade_params(const sl_lighting* l, const float* eye, ShadeParams& SH);
+void iso_dirs(float* d);
+// D14 and the 9 x 14 least-squares SH2 fit on it (lighting.js:188-209), float64 then rounded.
+void bounce_tables(float* d14, float* pinv);
+
+// One frame of the bounce: level_off / level_cnt give each depth's internal nodes in up_list (depths 1 ..
+// max_depth - 1 are summed, deepest first).
+cudaError_t launch_bounce_frame(const BounceParams& B, const ShadeParams& SH, const BounceBuffers& D,
+                                const std::vector<uint32_t>& level_off, const std::vector<uint32_t>& level_cnt,
+                                cudaStream_t s);
+
+}  // namespace sl

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "sl_internal.h"
+#include "sl_bounce.h"
 #include "sl_lighting.h"
 
 namespace sl {
@@ -132,9 +133,21 @@ struct sl_lighting {
   bool blur_init = false;
   uint32_t blur_prev = 0;  // the parts that moved in the previous update (their copies go back to rest)
   sl::DevBuf g_blur, n_blur;
-  // the scene's tree for the motion-blur cut (leaves then internal nodes) and every node's parent
+  // the scene's tree for the motion-blur cut and the probe gather (leaves then internal nodes), every node's parent,
+  // the children lists, and per node its depth and part (host)
   uint32_t n_tree = 0;
-  sl::DevBuf tree_nodes, node_parent;
+  sl::DevBuf tree_nodes, node_parent, kids;
+  std::vector<uint32_t> tree_depth, tree_part;
+  // probe bounce (bounce.cu; lighting.js initBounce / encodeBounce): the layout and frame state in BP, the internal
+  // nodes by depth for node_up, the sky SH
+  bool bounce_on = false, bn_first = true;
+  uint32_t bn_frame = 0;
+  float bn_blend = 1.0f;
+  sl::BounceParams BP{};
+  std::vector<uint32_t> bn_level_off, bn_level_cnt;
+  float sky[48] = {};
+  bool has_sky = false;
+  sl::DevBuf bn_tab, bn_ground, bn_up, probe_data, probe_sh, xfer, lo_dir, lo_b, node_acc, node_sh;
 };
 
 namespace sl {

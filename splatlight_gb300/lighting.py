@@ -81,6 +81,42 @@ class Lighting:
         k = np.ascontiguousarray(kids, dtype=np.uint32)
         N.check(self._lib.sl_lighting_set_tree(self._h, nd.ctypes.data, len(nd), k.ctypes.data if len(k) else None,
                                                len(k)))
+        self.tree_count = len(nd)
+
+    def set_probes(self, layout: dict, max_depth: int = 0, blend: float = 1.0) -> None:
+        """The probe bounce over a lattice (probes.room_layout / probes.terrain_layout); needs set_tree.  From the
+        next update on, each update runs one bounce frame and the renderer adds gain x lo_b to the lit colour."""
+        lay = N.ProbeLayout()
+        lay.dims[:] = [int(v) for v in layout["dims"]]
+        lay.terrain = 1 if layout["terrain"] else 0
+        lay.lo[:] = [float(v) for v in layout["lo"]]
+        lay.step[:] = [float(v) for v in layout["step"]]
+        lv = list(layout["levels"]) + [0.0] * (16 - len(layout["levels"]))
+        lay.levels[:] = [float(v) for v in lv]
+        self._ground = np.ascontiguousarray(layout["ground"], np.float32) if layout.get("ground") is not None else None
+        lay.ground = self._ground.ctypes.data if self._ground is not None else None
+        lay.tmax = float(layout["tmax"])
+        N.check(self._lib.sl_lighting_set_probes(self._h, C.byref(lay), int(max_depth), C.c_float(blend)))
+        self.probe_count = int(np.prod(layout["dims"]))
+
+    def set_sky(self, sh_rgb) -> None:
+        """The probes' sky: up to 16 real SH coefficients (bands 0-3), rgb; None or empty = no sky."""
+        sh = np.ascontiguousarray(np.zeros((0, 3)) if sh_rgb is None else sh_rgb, np.float32).reshape(-1, 3)
+        N.check(self._lib.sl_lighting_set_sky(self._h, sh.ctypes.data if len(sh) else None, len(sh)))
+
+    def read_bounce(self):
+        """The bounce state as a dict of host arrays: lo_b (G, 3, 4), lo_dir (G, 4), xfer (G, 12), probe_sh (NP, 9, 4),
+        probe_data (NP, 128, 8), node_sh (N, 14) and node_acc (N, 14, 4)."""
+        G, NP, Nn = self.count, self.probe_count, self.tree_count
+        shapes = [("lo_b", (G, 3, 4), np.float32), ("lo_dir", (G, 4), np.float32), ("xfer", (G, 12), np.float32),
+                  ("probe_sh", (NP, 9, 4), np.float32), ("probe_data", (NP, 128, 8), np.float32),
+                  ("node_sh", (Nn, 14), np.uint32), ("node_acc", (Nn, 14, 4), np.float32)]
+        out = {}
+        for k, (name, shape, dt) in enumerate(shapes):
+            a = np.empty(shape, dt)
+            N.check(self._lib.sl_lighting_read_bounce(self._h, k, a.ctypes.data, a.nbytes))
+            out[name] = a
+        return out
 
     def update(self, eye, forward=None, moved_mask: int = 0, stream=None) -> None:
         e = (C.c_float * 3)(*[float(v) for v in eye])

@@ -63,6 +63,8 @@ class Scene:
     emit_drawn: bool = True
     tree_nodes: np.ndarray | None = None   # an asset's whole tree (leaves first) and its children lists, for LOD
     kids: np.ndarray | None = None
+    sky_sh: np.ndarray | None = None       # the environment's sky, 16 real SH coefficients (bands 0-3) x rgb
+    probes: dict | None = None             # an asset's probe lattice (probes.room_layout / terrain_layout)
 
     @property
     def count(self) -> int:
@@ -334,6 +336,16 @@ def cornell(n: int = 65536, seed: int = 0, width: int = 512, height: int = 512, 
                    fov_deg=60.0, width=width, height=height, far=50.0, shadow_res=1024)
 
 
+# the hill-like scene's sky for the probe bounce (real SH bands 0-3, rgb): a blue sky brighter toward the zenith and
+# toward the sun's side, dim below the horizon (radiance ~0.35 at the zenith, ~0.1 at the horizon)
+HILL_SKY = np.zeros((16, 3), np.float32)
+HILL_SKY[0] = (0.55, 0.65, 0.85)
+HILL_SKY[2] = (0.30, 0.34, 0.42)     # z
+HILL_SKY[1] = (0.03, 0.03, 0.02)     # y
+HILL_SKY[3] = (0.05, 0.045, 0.03)    # x
+HILL_SKY[6] = (0.06, 0.07, 0.09)     # 3 z^2 - 1
+
+
 def hill(n: int = 1048576, seed: int = 1, width: int = 1920, height: int = 1080, n_emit: int = 32) -> Scene:
     rng = np.random.default_rng(seed)
     n_ground = int(round(0.8 * n))
@@ -359,7 +371,16 @@ def hill(n: int = 1048576, seed: int = 1, width: int = 1920, height: int = 1080,
     return _finish("hill", g, 3, rng, em, eye=(0.0, -14.0, 5.0), target=(0.0, 0.0, 1.5), up=(0.0, 0.0, 1.0),
                    fov_deg=50.0, width=width, height=height, far=100.0,
                    sun=Sun(tuple(sd), (3.0, 2.9, 2.7), 0.5 * math.pi / 180.0), sky_ambient=0.2,
-                   shadow_res=1024, sun_res=2048)
+                   shadow_res=1024, sun_res=2048, sky_sh=HILL_SKY.copy())
+
+
+def with_tree(scene: Scene):
+    """(scene, (nodes, kids)): the scene with its parts' tree roots set and its tree -- an asset's own, else
+    lod_tree's -- for the probe gather and the motion-blur cut."""
+    if scene.tree_nodes is not None and scene.kids is not None:
+        return scene, (scene.tree_nodes, scene.kids)
+    nodes, kids, parts = lod_tree(scene.gaussians, scene.parts)
+    return dataclasses.replace(scene, parts=parts), (nodes, kids)
 
 
 def subset(scene: Scene, n: int, seed: int = 123) -> Scene:

@@ -1,0 +1,129 @@
+"""The probe bounce (runtime/wgsl/bounce.wgsl, the reference's path without the sender cut), GPU against the CPU
+restatement over several frames: the transfer SH2, the light toward the probes, the tree's sums and SH2, the probes'
+gather (colour, depth moments, first-hit part and near flags), validity and SH2, and the Gaussians' bounce lo_b.
+The restatement takes the GPU's own lighting state (iso_norm, lamp and sun transmittance), so the bounce alone is
+compared; those inputs have their own parity tests.  Both sides run the same float32 arithmetic in the same order
+(no fused multiply-add, the shared deterministic transcendentals), so the state agrees to a few float32 ulps.
+
+Scenes: the hill-like scene (terrain lattice, its sky), the Cornell-like room (room lattice, no sky), and the
+reference's Cornell asset with its baked tree (kids.bin), real V grids and room layout when the assets are copied."""
+import dataclasses
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from splatlight_gb300 import camera
+from splatlight_gb300 import probes as PR
+from splatlight_gb300 import scene as S
+from splatlight_gb300.lighting import camera_forward, for_scene
+from splatlight_gb300.renderer import SplatRenderer
+from splatlight_gb300.structs import VIEW_LIT
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parent.parent
+ASSETS = ROOT / "tests" / "golden" / "assets"
+FRAMES = 5
+RTOL, ATOL = 1e-5, 1e-7
+
+
+def _close(name, a, b, rtol=RTOL, atol=ATOL, frac=0.0):
+    """a within rtol/atol of b everywhere, or outside it on at most a fraction `frac` of the entries."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    bad = ~np.isclose(a, b, rtol=rtol, atol=atol)
+    n = int(bad.sum())
+    worst = float(np.max(np.abs(a - b))) if a.size else 0.0
+    assert n <= frac * a.size, f"{name}: {n} of {a.size} differ (max abs {worst:.3e})"
+
+
+def _run(s, tree, layout, frames=FRAMES, gain=1.0):
+    import torch
+    from oracle import oracle as O
+    r = SplatRenderer(s.gaussians, s.parts)
+    L = for_scene(r, s)
+    L.set_tree(*tree)
+    L.set_sky(s.sky_sh)
+    L.set_probes(layout)
+    fwd = camera_forward(s)
+    b = None
+    for f in range(frames):
+        L.update(s.eye, fwd)
+        torch.cuda.synchronize()
+        if b is None:
+            col, lamp_t, env_t, nodes = L.read()
+            b = O.Bounce(s, tree, (col, lamp_t, env_t, nodes), layout, sky_sh=s.sky_sh)
+        ost = b.step(s.eye, threads=16)
+        gst = L.read_bounce()
+        pd, opd = gst["probe_data"], ost["probe_data"]
+        # discrete fields exactly: first-hit part (.w of the colour record), near / backface flags, validity
+        assert np.array_equal(pd[:, :, 3], opd[:, :, 3]), f"frame {f}: first-hit parts differ"
+        assert np.array_equal(pd[:, :, 7], opd[:, :, 7]), f"frame {f}: near flags differ"
+        assert np.array_equal(pd[:, 0, 6], opd[:, 0, 6]), f"frame {f}: probe validity differs"
+        _close(f"frame {f} probe colour", pd[:, :, :3], opd[:, :, :3])
+        _close(f"frame {f} probe moments", pd[:, :, 4:6], opd[:, :, 4:6])
+        _close(f"frame {f} probe SH2", gst["probe_sh"], ost["probe_sh"])
+        _close(f"frame {f} transfer", gst["xfer"], ost["xfer"])
+        _close(f"frame {f} light toward the probes", gst["lo_dir"], ost["lo_dir"])
+        _close(f"frame {f} node sums", gst["node_acc"], ost["node_acc"])
+        # node SH2 as halves: equal, or one f16 step apart where the float sums round differently
+        gh = gst["node_sh"].view(np.uint16).astype(np.int64)
+        oh = ost["node_sh"].view(np.uint16).astype(np.int64)
+        assert np.abs(gh - oh).max() <= 1, f"frame {f}: node SH2 halves differ by more than one step"
+        _close(f"frame {f} bounce", gst["lo_b"], ost["lo_b"])
+    return r, L, gst
+
+
+def _bounce_lit(s):
+    return dataclasses.replace(s, sky_ambient=0.0)
+
+
+def test_bounce_hill_terrain_sky():
+    s = _bounce_lit(S.hill(40000, seed=3, width=320, height=240, n_emit=8))
+    s = dataclasses.replace(s, shadow_res=256, sun_res=256)
+    s, tree = S.with_tree(s)
+    _, _, st = _run(s, tree, PR.for_scene(s))
+    # the sky reaches the ground through the probes: a positive bounce on most Gaussians
+    assert (st["lo_b"][:, 0, :3].sum(axis=1) > 0).mean() > 0.9
+
+
+def test_bounce_cornell_room():
+    s = _bounce_lit(S.cornell(20000, seed=2, width=256, height=256, n_emit=4))
+    s = dataclasses.replace(s, shadow_res=256)
+    s, tree = S.with_tree(s)
+    _run(s, tree, PR.for_scene(s))
+
+
+def test_bounce_cornell_asset():
+    p = ASSETS / "cornell_sdf_room_plain_bin"
+    if not (p / "asset.json").exists():
+        pytest.skip("reference assets not copied (tests/golden/copy_assets.py)")
+    from splatlight_gb300 import asset as A
+    s = A.asset_scene(A.load_asset(p), width=256, height=256)
+    s, tree = S.with_tree(s)
+    _run(s, tree, s.probes, frames=4)
+
+
+def test_bounce_in_the_lit_frame():
+    """The projection adds gain x lo_b (toward the eye) to the lit colour (shaders/project.wgsl:321-326): the frame
+    with the bounce equals the restatement's render of the same colour and bounce."""
+    import torch
+    from oracle import oracle as O
+    s = _bounce_lit(S.hill(30000, seed=5, width=256, height=192, n_emit=8))
+    s = dataclasses.replace(s, shadow_res=256, sun_res=256)
+    s, tree = S.with_tree(s)
+    r, L, st = _run(s, tree, PR.for_scene(s), frames=3)
+    col = L.read()[0]
+    gain = 0.8
+    f = camera.make_frame(s.eye, s.target, s.up, s.fov_deg, s.width, s.height, s.count, far=s.far,
+                          view_mode=VIEW_LIT, n_emit=s.n_drawn_emitters, bounce_gain=gain)
+    img = r.render(f)
+    torch.cuda.synchronize()
+    ref = O.render(s.gaussians, s.parts, f, emitters=s.emitters, colour=col, lo_b=st["lo_b"].reshape(-1, 4),
+                   threads=8)["rgba"]
+    assert np.abs(img - ref).max() <= 1e-3
+    f0 = camera.make_frame(s.eye, s.target, s.up, s.fov_deg, s.width, s.height, s.count, far=s.far,
+                           view_mode=VIEW_LIT, n_emit=s.n_drawn_emitters, bounce_gain=0.0)
+    img0 = r.render(f0)
+    assert img.sum() > img0.sum()   # the bounce brightens the frame

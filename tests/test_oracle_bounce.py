@@ -1,0 +1,102 @@
+"""The probe bounce's CPU side: the restatement's tables and half rounding, the probe layouts (src/lighting.js
+probeLayout), and properties of the restated bounce that hold whatever the scene (no light and no sky: no bounce;
+an open sky: the upward probe rays carry the sky's radiance times their transmittance)."""
+import dataclasses
+import math
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT))
+
+from splatlight_gb300 import probes as PR  # noqa: E402
+from splatlight_gb300 import scene as S  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def orc():
+    from oracle import oracle as O
+    O.build()
+    return O
+
+
+def test_half_rounding_matches_ieee(orc):
+    rng = np.random.default_rng(0)
+    x = np.concatenate([rng.normal(0, 1, 3000), rng.normal(0, 1e4, 1000), 2.0 ** rng.uniform(-30, -10, 1000),
+                        [0.0, -0.0, 65504.0, 65519.0, 65520.0, 1e9, np.inf, -np.inf, 2 ** -25, 2 ** -24, 3 * 2 ** -26]])
+    x = x.astype(np.float32)
+    with np.errstate(over="ignore"):
+        ref = x.astype(np.float16).view(np.uint16).astype(np.uint32)
+    assert np.array_equal(orc.f32_to_f16(x), ref)
+
+
+def test_sh2_fit_is_a_left_inverse(orc):
+    d, p = orc.bounce_tables()
+    assert np.allclose(np.linalg.norm(d.astype(np.float64), axis=1), 1.0, atol=1e-6)
+    x, y, z = (d[:, k].astype(np.float64) for k in range(3))
+    A = np.stack([np.full(14, 0.282095), 0.488603 * y, 0.488603 * z, 0.488603 * x, 1.092548 * x * y,
+                  1.092548 * y * z, 0.315392 * (3 * z * z - 1), 1.092548 * x * z, 0.546274 * (x * x - y * y)], 1)
+    assert np.abs(p.astype(np.float64) @ A - np.eye(9)).max() < 1e-6
+
+
+def test_room_layout():
+    lay = PR.room_layout(((-1.0, 1.0), (0.0, 2.0), (0.0, 2.0)))
+    assert lay["dims"] == [8, 8, 8] and not lay["terrain"] and lay["tmax"] == 6.0
+    assert np.allclose(lay["lo"], [-0.875, 0.125, 0.125])
+    assert np.allclose(lay["step"], [1.75 / 7] * 3)
+    assert np.allclose(lay["levels"], 0.125 + np.arange(8) * 1.75 / 7)
+    env = PR.room_layout(((-1.0, 1.0), (0.0, 2.0), (0.0, 2.0)), environment=True)
+    assert env["tmax"] == 6.0   # the diagonal (3.46 m) is shorter than TMAX
+
+
+def test_terrain_layout_ground_and_fill():
+    g = np.zeros(3, dtype=S.GAUSSIAN)
+    g["mu"] = [[0.1, 0.1, 1.0], [0.2, 0.3, 2.0], [3.5, 3.5, 5.0]]
+    parts = np.zeros(1, dtype=S.PART)
+    parts[0]["g_lo"], parts[0]["g_hi"], parts[0]["flags"] = 0, 3, 1
+    box = ((0.0, 4.0), (0.0, 4.0), (-1.0, 6.0))
+    lay = PR.terrain_layout(g, parts, box, dims=(4, 4), heights=(0.5, 2.0))
+    gr = lay["ground"].reshape(4, 4)
+    assert lay["dims"] == [4, 4, 2] and lay["terrain"]
+    assert gr[0, 0] == 2.0 and gr[3, 3] == 5.0       # the highest centre in each filled cell
+    assert gr[0, 1] == 2.0 and gr[1, 0] == 2.0       # first ring: the filled neighbours' mean
+    assert gr[2, 3] == 5.0 and gr[3, 2] == 5.0
+    assert np.isfinite(gr).all()
+    assert np.isclose(lay["tmax"], max(6.0, math.hypot(4.0, 4.0, 7.0)))
+    assert lay["lo"] == [0.5, 0.5, 0.0] and lay["step"] == [1.0, 1.0, 0.0]
+
+
+def _small_hill(**kw):
+    s = S.hill(6000, seed=4, width=64, height=64, n_emit=4)
+    s = dataclasses.replace(s, sky_ambient=0.0, shadow_res=64, sun_res=64, **kw)
+    return S.with_tree(s)
+
+
+def test_no_light_no_sky_no_bounce(orc):
+    s, tree = _small_hill(emitters=np.zeros(0, dtype=S.GAUSSIAN), sun=None)
+    lit = orc.lighting(s, threads=4)
+    b = orc.Bounce(s, tree, lit, PR.for_scene(s), sky_sh=None)
+    for _ in range(3):
+        st = b.step(s.eye, threads=4)
+    assert not st["lo_b"].any() and not st["probe_sh"].any() and not st["lo_dir"].any()
+
+
+def test_open_sky_reaches_the_probes(orc):
+    """A constant sky of radiance L (band 0 only): the upward rays of the probes above the hill leave the scene, and
+    each carries L times what it crossed (exactly L where it crossed nothing)."""
+    s, tree = _small_hill(emitters=np.zeros(0, dtype=S.GAUSSIAN), sun=None)
+    sky = np.zeros((16, 3), np.float32)
+    L = np.array([0.3, 0.5, 0.7], np.float32)
+    sky[0] = L / np.float32(0.282095)
+    b = orc.Bounce(s, tree, orc.lighting(s, threads=4), PR.for_scene(s), sky_sh=sky)
+    st = b.step(s.eye, threads=4)
+    pd = st["probe_data"]
+    up = pd[:, :16, :]                     # the top elevation row of cells: straight up, above the scene
+    open_rays = up[..., 3] < 0             # no hit took the transmittance below 1/2
+    assert open_rays.mean() > 0.5
+    col = up[..., :3][open_rays]
+    assert np.all(col <= L * (1 + 1e-5))   # the sky times the ray's transmittance (<= 1)
+    assert np.allclose(col.max(axis=0), L, rtol=1e-5)
