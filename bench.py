@@ -516,6 +516,75 @@ def run_lod(args, stream, flush, threshold_px: float = 2.0):
     return res
 
 
+def run_bounce(args, stream, flush):
+    """The probe bounce (the reference's path without the sender cut) on the headline workload (hill-like 1,048,576
+    Gaussians, its moment-matched tree, the 16 x 16 x 5 terrain lattice with its sky): device time of one bounce frame
+    (an update of a still scene is the shading pass plus the bounce; the shading pass alone is timed beside it), and
+    the lit 1920x1080 frame with the bounce added (bounce gain 1) against the frame without it."""
+    import torch
+    from splatlight_gb300 import camera
+    from splatlight_gb300 import probes as PR
+    from splatlight_gb300 import scene as scn
+    from splatlight_gb300.lighting import camera_forward, for_scene
+    from splatlight_gb300.renderer import SplatRenderer
+    s = scn.dataclasses.replace(make_scene("hill"), sky_ambient=0.0)
+    t0 = time.perf_counter()
+    s, tree = scn.with_tree(s)
+    t_tree = time.perf_counter() - t0
+    r = SplatRenderer(s.gaussians, s.parts)
+    L = for_scene(r, s)
+    L.set_tree(*tree)
+    L.set_sky(s.sky_sh)
+    lay = PR.for_scene(s)
+    L.set_probes(lay)
+    fwd = camera_forward(s)
+    sc = stream.cuda_stream
+    out = torch.empty((s.height, s.width, 4), dtype=torch.float32, device="cuda")
+
+    def timed(fn, steps):
+        ts = []
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.median(ts)
+
+    fb = camera.make_frame(s.eye, s.target, s.up, s.fov_deg, s.width, s.height, s.count, far=s.far, view_mode=3,
+                           n_emit=len(s.emitters), bounce_gain=1.0)
+    f0 = camera.make_frame(s.eye, s.target, s.up, s.fov_deg, s.width, s.height, s.count, far=s.far, view_mode=3,
+                           n_emit=len(s.emitters), bounce_gain=0.0)
+    for _ in range(max(args.warmup, 3) + 4):   # the first updates fill the maps and settle the quarter refresh
+        L.update(s.eye, fwd, stream=sc)
+    torch.cuda.synchronize()
+    steps = max(3, min(args.steps, 20))
+    ms_update = timed(lambda: L.update(s.eye, fwd, stream=sc), steps)
+    ms_shade = timed(lambda: L.shade(s.eye, stream=sc), steps)
+    ms_frame_b = timed(lambda: (L.update(s.eye, fwd, stream=sc), r.render(fb, out=out, stream=sc)), steps)
+    ms_frame_0 = timed(lambda: (L.shade(s.eye, stream=sc), r.render(f0, out=out, stream=sc)), steps)
+    st = L.read_bounce()
+    res = {"workload": f"hill-like 1,048,576 Gaussians (seed 1), its {len(tree[0]) - s.count:,}-node moment-matched "
+                       f"tree, terrain lattice {lay['dims'][0]}x{lay['dims'][1]}x{lay['dims'][2]} probes x 128 cells "
+                       "(ray length {:.1f} m), the scene's sky SH; bounce frame = direct light toward the probes for a "
+                       "quarter of the Gaussians, tree sums and SH2, gather, validity, probe SH2, bounce_sh".format(
+                           lay["tmax"]),
+           "bounce_ms": round(ms_update - ms_shade, 4), "update_ms": round(ms_update, 4),
+           "shade_ms": round(ms_shade, 4), "lit_frame_with_bounce_ms": round(ms_frame_b, 4),
+           "lit_frame_without_bounce_ms": round(ms_frame_0, 4),
+           "lit_views_per_s_with_bounce": round(1000.0 / ms_frame_b, 2),
+           "probes": int(np.prod(lay["dims"])), "valid_probes": int((st["probe_data"][:, 0, 6] > 0).sum()),
+           "mean_bounce_rgb": [round(float(v), 5) for v in st["lo_b"][:, 0, :3].mean(axis=0)],
+           "tree_build_s": round(t_tree, 2)}
+    L.close()
+    r.close()
+    return res
+
+
 def run_diff(args, stream, flush):
     """Inverse-rendering steps (forward + L2 loss + hand-written backward) on 500k hill-like Gaussians at 800x800
     against a target rendered from perturbed parameters; device time per step, L2 flushed between steps."""
@@ -907,6 +976,8 @@ def main():
     ap.add_argument("--only-sort", action="store_true", help="the sort leg alone (its own JSON line)")
     ap.add_argument("--only-lod", action="store_true", help="the screen-space LOD leg alone (its own JSON line)")
     ap.add_argument("--only-plain", action="store_true", help="the single-frame plain leg alone (its own JSON line)")
+    ap.add_argument("--only-bounce", action="store_true", help="the probe-bounce leg alone (its own JSON line)")
+    ap.add_argument("--no-bounce", action="store_true", help="skip the probe-bounce leg")
     ap.add_argument("--sort-n", type=int, default=1 << 26, help="keys for the sort leg")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="arrival window at lambda 500 (the config: 60)")
     ap.add_argument("--serve-seconds-other", type=float, default=10.0, help="arrival window at lambda 100 and 2000")
@@ -941,6 +1012,11 @@ def main():
     if args.only_lod:
         res = run_lod(args, stream, flush)
         emit({"metric": "views/s", "value": res["lod_views_per_s"], "unit": "views/s", "n_gpus": world, "lod": res})
+        return
+    if args.only_bounce:
+        res = run_bounce(args, stream, flush)
+        emit({"metric": "bounce frame ms", "value": res["bounce_ms"], "unit": "ms", "higher_is_better": False,
+              "n_gpus": world, "bounce": res})
         return
     if args.only_diff:
         res = run_diff(args, stream, flush)
@@ -1016,6 +1092,8 @@ def main():
         detail["lod"] = run_lod(args, stream, flush)
     if not args.no_diff:
         detail["differentiation"] = run_diff(args, stream, flush)
+    if not args.no_bounce:
+        detail["bounce"] = run_bounce(args, stream, flush)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

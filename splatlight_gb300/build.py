@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # translation units whose arithmetic is part of the bit-parity contract
 NO_FMAD = {"project.cu", "lighting.cu", "tiles.cu", "batch.cu", "lod.cu", "bounce.cu"}
 # translation units compiled for speed: fused multiply-add, approximate division and square root
-FAST = {"shade.cu"}
+FAST = {"shade.cu", "bounce_direct.cu"}
 
 
 def nvcc() -> str:

@@ -2,9 +2,8 @@
 // reference's path without the sender cut (?sendercut=0): one frame per sl_lighting_update, in its dispatch order
 //   xfer      iso_xfer (bounce.wgsl:993-1026): per Gaussian near something that moved (or on a forced refresh) the
 //             SH2 of its transfer iso_norm A(w) V(w) over the 128 world cells
-//   direct    direct_dirs_emit + env_dirs (emissive.wgsl:1012-1016, 1066-1082; environment.wgsl:311-359): a quarter
-//             of the Gaussians per frame, the light each sends toward the probes (one value: the footprint x V
-//             weighted mean over DIRS14 of the shading toward those directions, plus the distant lights' catch)
+//   direct    direct_dirs_emit + env_dirs (bounce_direct.cu): a quarter of the Gaussians per frame, the light each
+//             sends toward the probes
 //   leaf / up / sh2  node_leaf, node_up (deepest depth first), node_sh2 (bounce.wgsl:1166-1236): per tree node the
 //             14-direction sums of that light and their SH2 fit, packed as 27 halves
 //   gather    probe_gather (:1255-1410): per (probe, cell) ray the conservative theta-4 cut of every part's tree,
@@ -14,7 +13,7 @@
 //   bounce    bounce_sh (:1044-1095) with gloss_sh (:1102-1125): the 8 surrounding probes (trilinear x valid x
 //             Chebyshev, with the 4x4x4 fallback) dotted with the Gaussian's transfer into lo_b
 // The translation unit is compiled with --fmad=false and the deterministic transcendentals of sl_detmath.h, so the
-// CPU restatement reproduces it.  Every Gaussian reads the lattice (riding part probes and static probe volumes are
+// CPU restatement reproduces it given the same light toward the probes (whose kernel is compiled for speed).  Every Gaussian reads the lattice (riding part probes and static probe volumes are
 // not built); near-field visibility is off (the reference's default); near-mirror materials (flake lobe below
 // 0.1 rad), which the reference gives to bounce_dirs, keep a zero bounce.
 #include <cuda_fp16.h>
@@ -33,14 +32,6 @@ constexpr float kProbeTheta = 4.0f;
 constexpr float kNearR = 0.3f;
 constexpr float kGValid = 0.95f;
 constexpr float kGlossShMin = 0.1f;
-
-// emissive.wgsl DIRS14 (:107-112): the diagonals written 0.57735 (the probes' own D14 is exact, in the table)
-__constant__ float c_dirs14[14][3] = {{1.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, {1e-4f, 0.0f, 1.0f},
-                                      {-1.0f, 0.0f, 0.0f}, {0.0f, -1.0f, 0.0f}, {1e-4f, 0.0f, -1.0f},
-                                      {0.57735f, 0.57735f, 0.57735f}, {0.57735f, 0.57735f, -0.57735f},
-                                      {0.57735f, -0.57735f, 0.57735f}, {0.57735f, -0.57735f, -0.57735f},
-                                      {-0.57735f, 0.57735f, 0.57735f}, {-0.57735f, 0.57735f, -0.57735f},
-                                      {-0.57735f, -0.57735f, 0.57735f}, {-0.57735f, -0.57735f, -0.57735f}};
 
 __device__ __forceinline__ f3 ld3(const float* p) { return F3(p[0], p[1], p[2]); }
 __device__ __forceinline__ f3 max0(f3 a) { return F3(fmaxf(a.x, 0.0f), fmaxf(a.y, 0.0f), fmaxf(a.z, 0.0f)); }
@@ -265,118 +256,6 @@ __global__ void __launch_bounds__(kThreads) xfer_kernel(const __grid_constant__ 
   xfer[3u * g + 2u] = make_float4(t[8], 0.0f, 0.0f, 0.0f);
 }
 
-// direct_dirs_one + env_dirs_one for g = 4 i + frame % 4
-__global__ void __launch_bounds__(kThreads) direct_kernel(const __grid_constant__ BounceParams B,
-                                                          const __grid_constant__ ShadeParams SH,
-                                                          const sl_gaussian* __restrict__ gs,
-                                                          const sl_node* __restrict__ nodes,
-                                                          const sl_vgrid* __restrict__ vgrid,
-                                                          const sl_part* __restrict__ parts,
-                                                          const sl_material* __restrict__ mats,
-                                                          const float* __restrict__ tree,
-                                                          const float* __restrict__ lamp_T,
-                                                          const float4* __restrict__ env_T,
-                                                          float4* __restrict__ lo_dir) {
-  const uint32_t g = (blockIdx.x * kThreads + threadIdx.x) * 4u + B.frame % 4u;
-  if (g >= B.G) return;
-  const sl_gaussian& G = gs[g];
-  const Leaf nd = load_leaf(&nodes[g]);
-  const sl_material mat = mats[mat_index(G, SH.material_count)];
-  const float* xf = parts[G.part_surface & 0xFFFFu].xf;
-  const m3 Rq = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]);
-  const m3 Sloc = m3m(m3m(Rq, m3diag(F3(mat.flake[0], mat.flake[1], mat.flake[2]))), m3t(Rq));
-  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
-  const float detC = s3 * s3;
-  const f3 P = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
-  const f3 n = Rq.c[0];
-  const f3 Sd = F3(Sloc.c[0].x, Sloc.c[1].y, Sloc.c[2].z), So = F3(Sloc.c[1].x, Sloc.c[2].x, Sloc.c[2].y);
-  const f3 alb = F3(G.albedo[0], G.albedo[1], G.albedo[2]);
-  const float ks = spec_weight(mat);
-  const bool emissive = (mat.flags & 1u) != 0u;
-  const sl_vgrid& vg = vgrid[g];
-  f3 acc[14];
-#pragma unroll
-  for (int k = 0; k < 14; k++) acc[k] = F3(0.0f, 0.0f, 0.0f);
-  SpecPre sp;
-  if (ks > 0.0f) sp = spec_prepare(Sd, So);
-  if (SH.n_emit) {
-    uint32_t node = SH.root;
-    for (uint32_t guard = 0; node != kNone && guard < (1u << 16); guard++) {
-      const float* e = tree + 24u * node;
-      const uint32_t child_lo = __float_as_uint(e[11]), child_hi = __float_as_uint(e[15]);
-      const uint32_t skip = __float_as_uint(e[7]);
-      const f3 emean = F3(e[0], e[1], e[2]);
-      bool use;
-      if (child_lo == kNone || SH.mode == 0u) {
-        use = child_lo == kNone;
-      } else {
-        const f3 d = sub3(P, emean);
-        use = dot3(d, d) > SH.theta * SH.theta * e[3] * e[3];
-      }
-      if (!use) {
-        node = (child_lo != kNone && __float_as_uint(e[19]) == 0u) ? child_hi : skip;
-        continue;
-      }
-      node = skip;
-      const f3 d = sub3(emean, P);
-      const float d2 = dot3(d, d);
-      if (d2 < 1e-8f) continue;
-      const f3 ww = div3(d, sqrtf(d2));
-      const f3 wi = xf_dir_inv(xf, ww);
-      const float vi = vgrid_lookup(vg, wi);
-      if (vi <= 1e-7f) continue;
-      const float fp = footprint(nd, detC, wi);
-      const f3 mw = mul3(ww, -1.0f);
-      float s = 1.0f;
-      if (SH.one_sided) {
-        const float cs = dot3(mw, ld3(SH.normal));
-        s = SH.edge_soft > 0.0f ? smoothstepf(-SH.edge_soft, SH.edge_soft, cs) : (cs > 0.0f ? 1.0f : 0.0f);
-      }
-      const float mq = sqrtf(fmaxf(dot3(mw, sym_mul(F3(e[4], e[5], e[6]), F3(e[8], e[9], e[10]), mw)), 0.0f));
-      const f3 I = mul3(F3(e[12], e[13], e[14]), s * SH.scale * mq);
-      const f3 light = mul3(mul3(I, vi), fp / d2 * 1.0f);
-      if (ks <= 0.0f) {
-        acc[0] = add3(acc[0], light);
-        continue;
-      }
-      const f3 wr = mirror3(wi, n);
-      const float damp = iso_damp(nd.iso_norm, footprint(nd, detC, wr) * vgrid_lookup(vg, wr));
-#pragma unroll
-      for (int k = 0; k < 14; k++) {
-        const f3 wo = xf_dir_inv(xf, F3(c_dirs14[k][0], c_dirs14[k][1], c_dirs14[k][2]));
-        acc[k] = add3(acc[k], mul3(light, iso_lobe_from(ks, phase_specular_p(sp, wi, wo), damp)));
-      }
-    }
-  }
-  const float T = lamp_T[g];
-  const f3 a0 = acc[0];
-  f3 mean = F3(0.0f, 0.0f, 0.0f), c0 = F3(0.0f, 0.0f, 0.0f);
-  float ws = 0.0f;
-#pragma unroll
-  for (int k = 0; k < 14; k++) {
-    const f3 ck = mul3(mul3v(alb, ks <= 0.0f ? a0 : acc[k]), T * nd.iso_norm);
-    if (k == 0) c0 = ck;
-    const f3 wo = xf_dir_inv(xf, F3(c_dirs14[k][0], c_dirs14[k][1], c_dirs14[k][2]));
-    const float w = footprint(nd, detC, wo) * vgrid_lookup(vg, wo);
-    mean = add3(mean, mul3(ck, w));
-    ws += w;
-  }
-  f3 c = ws > 0.0f ? div3(mean, fmaxf(ws, 1e-20f)) : c0;
-  if (SH.n_lights && !emissive) {
-    const float4 et = env_T[g];
-    const float Tk[4] = {et.x, et.y, et.z, et.w};
-    f3 dc = F3(0.0f, 0.0f, 0.0f);
-    for (uint32_t k = 0; k < SH.n_lights && k < 4u; k++) {
-      const f3 wi = xf_dir_inv(xf, ld3(SH.lights[k].dir));
-      const float v = vgrid_lookup(vg, wi);
-      if (v <= 1e-7f) continue;
-      dc = add3(dc, mul3(ld3(SH.lights[k].irr), Tk[k] * v * footprint(nd, detC, wi)));
-    }
-    c = add3(c, mul3(mul3v(alb, dc), nd.iso_norm));
-  }
-  lo_dir[g] = make_float4(c.x, c.y, c.z, 0.0f);
-}
-
 // node_leaf: per leaf and direction (L w, w), L its light toward the probes plus last frame's bounce
 __global__ void __launch_bounds__(kThreads) leaf_kernel(const __grid_constant__ BounceParams B,
                                                         const sl_gaussian* __restrict__ gs,
@@ -506,11 +385,13 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(const __grid_constant_
     while (sp > 0u) {
       sp--;
       const uint32_t ni = stack[sp];
-      const GNode nd = load_gnode(&tnodes[ni]);
-      const f3 d = sub3(nd.mean, Po);
+      // the bound test first, on one 16-byte load (mean, radius); the rest of the node only when the ray meets it
+      const float4 mr = __ldg(reinterpret_cast<const float4*>(&tnodes[ni]));
+      const f3 d = sub3(F3(mr.x, mr.y, mr.z), Po);
       const float tt = clampf(dot3(d, wr), 0.0f, t1);
       const f3 e = sub3(d, mul3(wr, tt));
-      if (dot3(e, e) > nd.radius * nd.radius) continue;
+      if (dot3(e, e) > mr.w * mr.w) continue;
+      const GNode nd = load_gnode(&tnodes[ni]);
       bool use_node = ni < B.G;
       if (!use_node) use_node = len3(sub3(cr, nd.mean)) - B.brad > kProbeTheta * nd.smax;
       if (use_node) {
@@ -713,10 +594,11 @@ cudaError_t launch_bounce_frame(const BounceParams& B, const ShadeParams& SH, co
                                 const std::vector<uint32_t>& level_off, const std::vector<uint32_t>& level_cnt,
                                 cudaStream_t s) {
   if (B.G == 0) return cudaSuccess;
-  xfer_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.tab, D.xfer);
-  const uint64_t quarter = (B.G + 3u) / 4u;
-  direct_kernel<<<blocks(quarter), kThreads, 0, s>>>(B, SH, D.gs, D.nodes, D.vgrid, D.parts, D.mats, D.tree, D.lamp_T,
-                                                     D.env_T, D.lo_dir);
+  // iso_xfer only where something may have changed a transfer: a forced refresh or a part that moved (lighting.js
+  // :1036-1039 skips the dispatch otherwise)
+  if (B.force || B.moved_mask) xfer_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.tab, D.xfer);
+  cudaError_t e = launch_bounce_direct(B, SH, D, s);
+  if (e != cudaSuccess) return e;
   leaf_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.tab, D.lo_dir, D.lo_b,
                                                D.node_acc);
   for (int d = (int)level_cnt.size() - 1; d >= 1; d--) {

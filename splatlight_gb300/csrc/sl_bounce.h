@@ -50,6 +50,9 @@ void iso_dirs(float* d);
 // D14 and the 9 x 14 least-squares SH2 fit on it (lighting.js:188-209), float64 then rounded.
 void bounce_tables(float* d14, float* pinv);
 
+// direct_dirs_emit + env_dirs for the Gaussians g % 4 == frame % 4 (bounce_direct.cu) into lo_dir
+cudaError_t launch_bounce_direct(const BounceParams& B, const ShadeParams& SH, const BounceBuffers& D, cudaStream_t s);
+
 // One frame of the bounce: level_off / level_cnt give each depth's internal nodes in up_list (depths 1 ..
 // max_depth - 1 are summed, deepest first).
 cudaError_t launch_bounce_frame(const BounceParams& B, const ShadeParams& SH, const BounceBuffers& D,

@@ -2,11 +2,15 @@
 restatement over several frames: the transfer SH2, the light toward the probes, the tree's sums and SH2, the probes'
 gather (colour, depth moments, first-hit part and near flags), validity and SH2, and the Gaussians' bounce lo_b.
 The restatement takes the GPU's own lighting state (iso_norm, lamp and sun transmittance), so the bounce alone is
-compared; those inputs have their own parity tests.  Both sides run the same float32 arithmetic in the same order
-(no fused multiply-add, the shared deterministic transcendentals), so the state agrees to a few float32 ulps.
+compared; those inputs have their own parity tests.  The geometry (first-hit parts, near flags, validity, depth
+moments, transfer) is exact or within a few float32 ulps: both sides run the same float32 arithmetic in the same
+order.  The light toward the probes comes from a kernel compiled for speed (as the shading pass), within 1e-4 of the
+restatement; through the half-precision node SH2 (a flip of one half step is 5e-4 of a coefficient) and the frames'
+feedback, the radiance downstream agrees within 2e-3.
 
-Scenes: the hill-like scene (terrain lattice, its sky), the Cornell-like room (room lattice, no sky), and the
-reference's Cornell asset with its baked tree (kids.bin), real V grids and room layout when the assets are copied."""
+Scenes: the hill-like scene (terrain lattice, its sky), the Cornell-like room (room lattice, no sky), and, when the
+assets are copied, the reference's Cornell room (room layout) and hill_lite (terrain layout, its environment's sky),
+each with its baked tree (kids.bin) and real V grids."""
 import dataclasses
 from pathlib import Path
 
@@ -25,13 +29,17 @@ pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parent.parent
 ASSETS = ROOT / "tests" / "golden" / "assets"
 FRAMES = 5
-RTOL, ATOL = 1e-5, 1e-7
+RTOL, ATOL = 1e-5, 1e-7          # geometry: depth moments, transfer
+RAD_RTOL, RAD_ATOL = 2e-3, 1e-6  # radiance downstream of the light toward the probes
 
 
-def _close(name, a, b, rtol=RTOL, atol=ATOL, frac=0.0):
-    """a within rtol/atol of b everywhere, or outside it on at most a fraction `frac` of the entries."""
+def _close(name, a, b, rtol=RTOL, atol=ATOL, frac=0.0, scaled=False):
+    """a within rtol/atol of b everywhere, or outside it on at most a fraction `frac` of the entries; scaled: atol is
+    also at least rtol x the largest |b| (radiance: half steps of the node SH2 move a value near zero by that much)."""
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
+    if scaled and b.size:
+        atol = max(atol, rtol * float(np.abs(b).max()))
     bad = ~np.isclose(a, b, rtol=rtol, atol=atol)
     n = int(bad.sum())
     worst = float(np.max(np.abs(a - b))) if a.size else 0.0
@@ -61,17 +69,17 @@ def _run(s, tree, layout, frames=FRAMES, gain=1.0):
         assert np.array_equal(pd[:, :, 3], opd[:, :, 3]), f"frame {f}: first-hit parts differ"
         assert np.array_equal(pd[:, :, 7], opd[:, :, 7]), f"frame {f}: near flags differ"
         assert np.array_equal(pd[:, 0, 6], opd[:, 0, 6]), f"frame {f}: probe validity differs"
-        _close(f"frame {f} probe colour", pd[:, :, :3], opd[:, :, :3])
         _close(f"frame {f} probe moments", pd[:, :, 4:6], opd[:, :, 4:6])
-        _close(f"frame {f} probe SH2", gst["probe_sh"], ost["probe_sh"])
         _close(f"frame {f} transfer", gst["xfer"], ost["xfer"])
-        _close(f"frame {f} light toward the probes", gst["lo_dir"], ost["lo_dir"])
-        _close(f"frame {f} node sums", gst["node_acc"], ost["node_acc"])
-        # node SH2 as halves: equal, or one f16 step apart where the float sums round differently
-        gh = gst["node_sh"].view(np.uint16).astype(np.int64)
-        oh = ost["node_sh"].view(np.uint16).astype(np.int64)
-        assert np.abs(gh - oh).max() <= 1, f"frame {f}: node SH2 halves differ by more than one step"
-        _close(f"frame {f} bounce", gst["lo_b"], ost["lo_b"])
+        _close(f"frame {f} light toward the probes", gst["lo_dir"], ost["lo_dir"], rtol=1e-4 if f == 0 else RAD_RTOL,
+               atol=RAD_ATOL, scaled=f > 0)
+        _close(f"frame {f} node sums", gst["node_acc"], ost["node_acc"], rtol=RAD_RTOL, atol=RAD_ATOL, scaled=True)
+        gh = gst["node_sh"].view(np.float16).astype(np.float64)
+        oh = ost["node_sh"].view(np.float16).astype(np.float64)
+        _close(f"frame {f} node SH2", gh, oh, rtol=RAD_RTOL, atol=1e-4 * max(1.0, float(np.abs(oh).max())))
+        _close(f"frame {f} probe colour", pd[:, :, :3], opd[:, :, :3], rtol=RAD_RTOL, atol=RAD_ATOL, scaled=True)
+        _close(f"frame {f} probe SH2", gst["probe_sh"], ost["probe_sh"], rtol=RAD_RTOL, atol=RAD_ATOL, scaled=True)
+        _close(f"frame {f} bounce", gst["lo_b"], ost["lo_b"], rtol=RAD_RTOL, atol=RAD_ATOL, scaled=True)
     return r, L, gst
 
 
@@ -103,6 +111,19 @@ def test_bounce_cornell_asset():
     s = A.asset_scene(A.load_asset(p), width=256, height=256)
     s, tree = S.with_tree(s)
     _run(s, tree, s.probes, frames=4)
+
+
+def test_bounce_hill_lite_asset():
+    """The reference's hill_lite: its baked tree, real V grids, the terrain lattice over its bounds and the
+    environment's own sky SH (asset.json environment.sky.sh_rgb), lit by its sun."""
+    p = ASSETS / "hill_lite_bin"
+    if not (p / "asset.json").exists():
+        pytest.skip("reference assets not copied (tests/golden/copy_assets.py)")
+    from splatlight_gb300 import asset as A
+    s = A.asset_scene(A.load_asset(p), width=256, height=256)
+    assert s.sky_sh is not None and s.probes["terrain"]
+    s, tree = S.with_tree(s)
+    _run(s, tree, s.probes, frames=3)
 
 
 def test_bounce_in_the_lit_frame():
