@@ -577,7 +577,8 @@ def run_bounce(args, stream, flush):
            "shade_ms": round(ms_shade, 4), "lit_frame_with_bounce_ms": round(ms_frame_b, 4),
            "lit_frame_without_bounce_ms": round(ms_frame_0, 4),
            "lit_views_per_s_with_bounce": round(1000.0 / ms_frame_b, 2),
-           "probes": int(np.prod(lay["dims"])), "valid_probes": int((st["probe_data"][:, 0, 6] > 0).sum()),
+           "probes": L.probe_count, "lattice_probes": int(np.prod(lay["dims"])),
+           "valid_probes": int((st["probe_data"][:, 0, 6] > 0).sum()),
            "mean_bounce_rgb": [round(float(v), 5) for v in st["lo_b"][:, 0, :3].mean(axis=0)],
            "tree_build_s": round(t_tree, 2)}
     L.close()

@@ -290,6 +290,8 @@ typedef struct sl_probe_layout {
   float levels[16];     /* ascending */
   const float* ground;  /* dims[0] x dims[1] heights, or NULL (0); copied */
   float tmax;           /* probe ray length: TMAX 6 m, or the scene's diagonal with an environment (lighting.js:226) */
+  uint32_t n_vols;      /* static probe volumes (probeVolumes, lighting.js:289-314): up to 32 */
+  uint32_t vols[32][4]; /* (part 0-31, nx, ny, nz): a grid over the part's rest-frame box serving its Gaussians */
 } sl_probe_layout;
 
 /* Lighting.initBounce (src/lighting.js:723-816) without the sender cut (?sendercut=0): after each update's shading the
@@ -299,10 +301,12 @@ typedef struct sl_probe_layout {
  * max_depth - 1 .. 1 (0: the tree's depth), node_sh2), the probes' gather through every part's tree with the sky
  * beyond (probe_gather), their validity and SH2 (probe_valid, probe_sh2), then each Gaussian's bounce from its 8
  * probes (bounce_sh, gloss_sh) into lo_b, which the projection adds to the lit colour times the frame's bounce gain
- * (palette[3].x).  blend: the history weight of each gather after the first (1: taken as is, the reference's default;
- * 0.5: ?probeblend=ema).  Needs sl_lighting_set_tree.  Every Gaussian reads the lattice: the probes that ride on
- * movable parts and static probe volumes are not built, nor bounce_dirs (near-mirror materials, flake lobe below
- * 0.1 rad, take no bounce); near-field visibility is off, as the reference's default. */
+ * (palette[3].x).  After the lattice come 8 probes per part (part_probe_frame's cube, riding with the part; those of
+ * movable parts gather, skipping their own part, and serve that part's Gaussians), then the static volumes' grids
+ * (serving their part's Gaussians).  blend: the history weight of each gather after the first (1: taken as is, the
+ * reference's default; 0.5: ?probeblend=ema).  Needs sl_lighting_set_tree and the renderer's parts (their count is
+ * fixed from here on).  Not built: bounce_dirs (near-mirror materials, flake lobe below 0.1 rad, take no bounce),
+ * near-field visibility and reflection (off by default in the reference). */
 SL_API int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* layout, uint32_t max_depth, float blend);
 /* The environment's sky for the probes (src/environment.js:116-124; bounce.wgsl sky_radiance :148-160): n_coef (<= 16)
  * real SH coefficients, rgb, bands 0-3, seen by probe rays that leave the scene.  0 coefficients: no sky. */

@@ -463,7 +463,16 @@ def render_given_order(gaussians, parts, frame, order, emitters=None, colour=Non
 
 class ProbeLayoutC(C.Structure):
     _fields_ = [("dims", C.c_uint32 * 3), ("terrain", C.c_uint32), ("lo", C.c_float * 3), ("step", C.c_float * 3),
-                ("levels", C.c_float * 16), ("ground", C.c_void_p), ("tmax", C.c_float)]
+                ("levels", C.c_float * 16), ("ground", C.c_void_p), ("tmax", C.c_float), ("part_probes", C.c_uint32),
+                ("n_vols", C.c_uint32), ("vols", (C.c_uint32 * 4) * 32)]
+
+
+def probe_count(layout, part_count: int) -> int:
+    """The lattice, 8 probes per part, then the static volumes' grids."""
+    n = int(np.prod(layout["dims"])) + 8 * part_count
+    for _, nx, ny, nz in layout.get("vols", []):
+        n += nx * ny * nz
+    return n
 
 
 class BounceIn(C.Structure):
@@ -538,7 +547,7 @@ class Bounce:
         self.sky = None if sky_sh is None else np.ascontiguousarray(sky_sh, np.float32).reshape(16, 3)
         self.layout = layout
         self.ground = None if layout.get("ground") is None else np.ascontiguousarray(layout["ground"], np.float32)
-        NP = int(np.prod(layout["dims"]))
+        NP = probe_count(layout, len(scene.parts))
         N = len(tn)
         self.state = {"probe_data": np.zeros((NP, 128, 8), np.float32), "probe_sh": np.zeros((NP, 9, 4), np.float32),
                       "xfer": np.zeros((G, 12), np.float32), "lo_dir": np.zeros((G, 4), np.float32),
@@ -580,6 +589,11 @@ class Bounce:
         B.lay.levels[:] = [float(v) for v in list(lay["levels"]) + [0.0] * (16 - len(lay["levels"]))]
         B.lay.ground = self.ground.ctypes.data if self.ground is not None else None
         B.lay.tmax = float(lay["tmax"])
+        B.lay.part_probes = 1
+        vols = list(lay.get("vols", []))[:32]
+        B.lay.n_vols = len(vols)
+        for i, v in enumerate(vols):
+            B.lay.vols[i][:] = [int(x) for x in v]
         B.max_depth = self.max_depth
         B.eye[:] = [float(v) for v in eye]
         B.alpha = 1.0 if self.first else self.blend

@@ -1690,9 +1690,84 @@ static uint32_t bn_cell_of(f3 w) {
 static float bn_ground(const orc_probe_layout* L, uint32_t i, uint32_t j) {
   return L->ground ? L->ground[i * L->dims[1] + j] : 0.0f;
 }
-static f3 bn_probe_pos(const orc_probe_layout* L, uint32_t p) {
+static f3 bn_lattice_pos(const orc_probe_layout* L, uint32_t p) {
   uint32_t i = p / (L->dims[1] * L->dims[2]), j = (p / L->dims[2]) % L->dims[1], k = p % L->dims[2];
   return F3(L->lo[0] + L->step[0] * (float)i, L->lo[1] + L->step[1] * (float)j, bn_ground(L, i, j) + L->levels[k]);
+}
+
+/* the probes after the lattice (bounce.wgsl:57-75, 217-268): 8 per part (part_probe_frame's 2x2x2 cube in the part's
+ * rest frame), then the static volumes' grids (vol_frame) */
+typedef struct {
+  uint32_t nl, n_probes;                    /* lattice probes; all probes (lattice, 8 per part, volumes) */
+  uint32_t vol_first[32], vol_dims[32][3];  /* per part: its volume's first probe after the lattice, grid (0: none) */
+} bn_probes;
+
+static bn_probes bn_probe_set(const orc_bounce_in* in) {
+  bn_probes B;
+  memset(&B, 0, sizeof(B));
+  B.nl = in->lay.dims[0] * in->lay.dims[1] * in->lay.dims[2];
+  uint32_t off = 8u * in->part_count;   /* the volumes follow every part's 8 (lighting.js:797-799) */
+  for (uint32_t v = 0; v < in->lay.n_vols && v < 32u; v++) {
+    uint32_t q = in->lay.vols[v][0];
+    if (q >= 32u) continue;
+    B.vol_first[q] = off;
+    for (int c = 0; c < 3; c++) B.vol_dims[q][c] = in->lay.vols[v][1 + c];
+    off += in->lay.vols[v][1] * in->lay.vols[v][2] * in->lay.vols[v][3];
+  }
+  B.n_probes = B.nl + off;
+  return B;
+}
+/* is_part_probe_part (bounce.wgsl:264-266): a movable part's Gaussians read its own 8 probes */
+static int bn_is_part_probe_part(const orc_bounce_in* in, uint32_t q) {
+  return q < in->part_count && (in->parts[q].flags & 1u) == 0u && in->parts[q].root != NONE_U32;
+}
+static int bn_has_vol(const bn_probes* B, uint32_t q) { return q < 32u && B->vol_dims[q][0] > 0u; }
+static float bn_sel(uint32_t o, float f) { return o ? f : 1.0f - f; }
+static uint32_t bn_vol_of_probe(const orc_bounce_in* in, const bn_probes* B, uint32_t r) {
+  for (uint32_t q = 0; q < in->part_count && q < 32u; q++) {
+    uint32_t n = B->vol_dims[q][0] * B->vol_dims[q][1] * B->vol_dims[q][2];
+    if (n > 0u && r >= B->vol_first[q] && r < B->vol_first[q] + n) return q;
+  }
+  return NONE_U32;
+}
+static void bn_part_frame(const orc_bounce_in* in, uint32_t q, f3* c, f3* h) {
+  const sl_node* nd = &in->nodes[in->parts[q].root];
+  f3 a = nd_cinv_d(nd), o = nd_cinv_o(nd);
+  float det = a.x * (a.y * a.z - o.z * o.z) - o.x * (o.x * a.z - o.z * o.y) + o.y * (o.x * o.z - a.y * o.y);
+  f3 var = div3(F3(a.y * a.z - o.z * o.z, a.x * a.z - o.y * o.y, a.x * a.y - o.x * o.x), fmaxf(det, 1e-30f));
+  float hb = 0.5f * in->parts[q].bound[3];
+  *c = F3(nd->mean[0], nd->mean[1], nd->mean[2]);
+  *h = F3(fminf(0.95f * sqrtf(fmaxf(var.x, 0.0f)), hb), fminf(0.95f * sqrtf(fmaxf(var.y, 0.0f)), hb),
+          fminf(0.95f * sqrtf(fmaxf(var.z, 0.0f)), hb));
+}
+static void bn_vol_frame(const orc_bounce_in* in, uint32_t q, f3* c, f3* h) {
+  f3 h0;
+  bn_part_frame(in, q, c, &h0);
+  float R = in->parts[q].bound[3];
+  *h = F3(fminf(1.6f * h0.x, R), fminf(1.6f * h0.y, R), fminf(1.6f * h0.z, R));
+}
+static f3 bn_probe_pos(const orc_bounce_in* in, const bn_probes* B, uint32_t p) {
+  const uint32_t nl = B->nl;
+  if (p >= nl + 8u * in->part_count) { /* a static volume's probe */
+    uint32_t r = p - nl, q = bn_vol_of_probe(in, B, r);
+    if (q == NONE_U32) return F3(0.0f, 0.0f, 0.0f);
+    const uint32_t* d = B->vol_dims[q];
+    uint32_t l = r - B->vol_first[q];
+    f3 ijk = F3((float)(l / (d[1] * d[2])), (float)((l / d[2]) % d[1]), (float)(l % d[2]));
+    f3 c, h;
+    bn_vol_frame(in, q, &c, &h);
+    f3 den = F3(fmaxf((float)d[0] - 1.0f, 1.0f), fmaxf((float)d[1] - 1.0f, 1.0f), fmaxf((float)d[2] - 1.0f, 1.0f));
+    f3 t = mul3v(mul3(h, 2.0f), ijk);
+    return xf_point(in->parts[q].xf, add3(sub3(c, h), F3(t.x / den.x, t.y / den.y, t.z / den.z)));
+  }
+  if (p >= nl) { /* a part's probe: the 2x2x2 cube, moving with the part */
+    uint32_t q = (p - nl) / 8u, k = (p - nl) % 8u;
+    f3 sgn = F3((float)(k >> 2u) * 2.0f - 1.0f, (float)((k >> 1u) & 1u) * 2.0f - 1.0f, (float)(k & 1u) * 2.0f - 1.0f);
+    f3 c, h;
+    bn_part_frame(in, q, &c, &h);
+    return xf_point(in->parts[q].xf, add3(c, mul3v(sgn, h)));
+  }
+  return bn_lattice_pos(&in->lay, p);
 }
 static f3 bn_node_radiance(const uint32_t* node_sh, uint32_t ni, const float* b) {
   float h[28];
@@ -1707,7 +1782,7 @@ static f3 bn_node_radiance(const uint32_t* node_sh, uint32_t ni, const float* b)
 }
 
 static float bn_cheb(const orc_probe_layout* L, const float* pd, uint32_t p, f3 P) {
-  f3 v = sub3(P, bn_probe_pos(L, p));
+  f3 v = sub3(P, bn_lattice_pos(L, p));
   float dist = len3(v);
   const float* mm = pd + 8u * (p * BN_NCELL + bn_cell_of(div3(v, fmaxf(dist, 1e-9f)))) + 4u;
   float var = fmaxf(mm[1] - mm[0] * mm[0], 1e-4f);
@@ -1752,7 +1827,7 @@ static bn_weights bn_probe_weights(const orc_probe_layout* L, const float* pd, f
       if (ii < 0 || jj < 0 || kk < 0 || ii >= (int)dm[0] || jj >= (int)dm[1] || kk >= (int)dm[2]) continue;
       uint32_t p = ((uint32_t)ii * dm[1] + (uint32_t)jj) * dm[2] + (uint32_t)kk;
       if (pd[8u * (p * BN_NCELL) + 6u] <= 0.0f) continue;
-      float d = fmaxf(len3(sub3(P, bn_probe_pos(L, p))), 0.05f);
+      float d = fmaxf(len3(sub3(P, bn_lattice_pos(L, p))), 0.05f);
       float w = fmaxf(bn_cheb(L, pd, p, P), 1e-3f) / (d * d);
       if (w <= out.w[7]) continue;
       uint32_t at = 7u;
@@ -1771,6 +1846,47 @@ static bn_weights bn_probe_weights(const orc_probe_layout* L, const float* pd, f
   }
   for (int c = 0; c < 8; c++) out.w[c] /= fmaxf(wsum, 1e-12f);
   return out;
+}
+
+/* probe_weights (bounce.wgsl:813-885): a movable part's Gaussians trilinear over its own 8 probes, a static volume's
+ * over its grid (neither with the Chebyshev test: those probes skip their own object), the rest over the lattice */
+static bn_weights bn_weights_for(const orc_bounce_in* in, const bn_probes* B, const float* pd, f3 P, uint32_t own) {
+  bn_weights out;
+  if (bn_is_part_probe_part(in, own)) {
+    f3 c, h;
+    bn_part_frame(in, own, &c, &h);
+    const float* xf = in->parts[own].xf;
+    f3 lp = xf_dir_inv(xf, sub3(P, F3(xf[3], xf[7], xf[11])));
+    f3 num = add3(sub3(lp, c), h);
+    f3 f = F3(clampf(num.x / fmaxf(2.0f * h.x, 1e-6f), 0.0f, 1.0f), clampf(num.y / fmaxf(2.0f * h.y, 1e-6f), 0.0f, 1.0f),
+              clampf(num.z / fmaxf(2.0f * h.z, 1e-6f), 0.0f, 1.0f));
+    for (uint32_t k = 0; k < 8u; k++) {
+      out.pid[k] = B->nl + own * 8u + k;
+      out.w[k] = bn_sel(k >> 2u, f.x) * bn_sel((k >> 1u) & 1u, f.y) * bn_sel(k & 1u, f.z);
+    }
+    return out;
+  }
+  if (bn_has_vol(B, own)) {
+    f3 c, h;
+    bn_vol_frame(in, own, &c, &h);
+    const float* xf = in->parts[own].xf;
+    f3 lp = xf_dir_inv(xf, sub3(P, F3(xf[3], xf[7], xf[11])));
+    const uint32_t* d = B->vol_dims[own];
+    f3 num = add3(sub3(lp, c), h);
+    f3 fq = F3(clampf(num.x / fmaxf(2.0f * h.x, 1e-6f), 0.0f, 1.0f) * ((float)d[0] - 1.0f),
+               clampf(num.y / fmaxf(2.0f * h.y, 1e-6f), 0.0f, 1.0f) * ((float)d[1] - 1.0f),
+               clampf(num.z / fmaxf(2.0f * h.z, 1e-6f), 0.0f, 1.0f) * ((float)d[2] - 1.0f));
+    uint32_t fi[3] = {(uint32_t)sl_floorf(fq.x), (uint32_t)sl_floorf(fq.y), (uint32_t)sl_floorf(fq.z)};
+    for (int a = 0; a < 3; a++) fi[a] = fi[a] < d[a] - 2u ? fi[a] : d[a] - 2u;
+    f3 fr = F3(fq.x - (float)fi[0], fq.y - (float)fi[1], fq.z - (float)fi[2]);
+    for (uint32_t k = 0; k < 8u; k++) {
+      uint32_t ox = k >> 2u, oy = (k >> 1u) & 1u, oz = k & 1u;
+      out.pid[k] = B->nl + B->vol_first[own] + ((fi[0] + ox) * d[1] + (fi[1] + oy)) * d[2] + (fi[2] + oz);
+      out.w[k] = bn_sel(ox, fr.x) * bn_sel(oy, fr.y) * bn_sel(oz, fr.z);
+    }
+    return out;
+  }
+  return bn_probe_weights(&in->lay, pd, P);
 }
 
 /* emissive.wgsl DIRS14 (:107-112): the same directions with the diagonals' components written 0.57735 */
@@ -1890,7 +2006,8 @@ static void bn_direct_one(const orc_bounce_in* in, uint32_t g, float* lo_dir) {
 int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads) {
   const orc_probe_layout* L = &in->lay;
   const uint32_t G = in->count, N = in->n_nodes;
-  const uint32_t NP = L->dims[0] * L->dims[1] * L->dims[2];
+  const bn_probes PS = bn_probe_set(in);
+  const uint32_t NP = PS.n_probes, NL = PS.nl;
   float cells[4 * 128], d14[42], pinv[126];
   orc_iso_dirs(cells);
   orc_bounce_tables(d14, pinv);
@@ -2016,11 +2133,20 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
 #endif
   for (int64_t id64 = 0; id64 < (int64_t)NP * BN_NCELL; id64++) {
     uint32_t id = (uint32_t)id64, p = id / BN_NCELL, c = id % BN_NCELL;
-    f3 o = bn_probe_pos(L, p);
+    /* a part probe skips its own part (and a static part's stay idle); a volume's probes skip their object */
+    uint32_t skip = NONE_U32;
+    if (p >= NL && p < NL + 8u * in->part_count) {
+      skip = (p - NL) / 8u;
+      if (!bn_is_part_probe_part(in, skip)) continue;
+    } else if (p >= NL) {
+      skip = bn_vol_of_probe(in, &PS, p - NL);
+      if (skip == NONE_U32) continue;
+    }
+    f3 o = bn_probe_pos(in, &PS, p);
     f3 w = bn_cell_dir(cells, c);
     uint32_t dz = L->dims[2];
     f3 cen = o;
-    if (!L->terrain) {
+    if (!L->terrain && p < NL) {
       float bx = (float)((p / (L->dims[1] * dz)) / 2u), by = (float)(((p / dz) % L->dims[1]) / 2u),
             bz = (float)((p % dz) / 2u);
       cen = F3(L->lo[0] + L->step[0] * (2.0f * bx + 0.5f), L->lo[1] + L->step[1] * (2.0f * by + 0.5f),
@@ -2030,7 +2156,9 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
     float ht[BN_HIT_MAX], hv[BN_HIT_MAX];
     uint32_t hn[BN_HIT_MAX];
     uint32_t k = 0;
+    const float pbrad = p < NL ? brad : 0.0f;   /* probes off the lattice cut around themselves */
     for (uint32_t q = 0; q < in->part_count; q++) {
+      if (q == skip) continue;
       const float* xf = in->parts[q].xf;
       f3 Po = xf_dir_inv(xf, sub3(o, F3(xf[3], xf[7], xf[11])));
       f3 wr = xf_dir_inv(xf, w);
@@ -2049,7 +2177,7 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
         f3 e = sub3(d, mul3(wr, tt));
         if (dot3(e, e) > nd->radius * nd->radius) continue;
         int use_node = ni < G;
-        if (!use_node) use_node = len3(sub3(cr, mean)) - brad > BN_THETA * nd->smax;
+        if (!use_node) use_node = len3(sub3(cr, mean)) - pbrad > BN_THETA * nd->smax;
         if (use_node) {
           float tau = nd->kappa * dirm(nd, wr) * bn_seg_geom(nd, Po, wr, 0.0f, t1);
           if (tau > 1e-6f) {
@@ -2126,6 +2254,10 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
   }
   /* probe_valid */
   for (uint32_t p = 0; p < NP; p++) {
+    if (p >= NL) { /* part and volume probes skip their own object, so never sit inside it */
+      st->probe_data[8u * (p * BN_NCELL) + 6u] = 1.0f;
+      continue;
+    }
     uint32_t cnt[17] = {0};
     uint32_t nearc = 0, back = 0;
     for (uint32_t c = 0; c < BN_NCELL; c++) {
@@ -2177,7 +2309,7 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
     uint32_t own = Gs->part_surface & 0xFFFFu;
     const float* xf = in->parts[own].xf;
     f3 P = xf_point(xf, F3(Gs->mu[0], Gs->mu[1], Gs->mu[2]));
-    bn_weights pw = bn_probe_weights(L, st->probe_data, P);
+    bn_weights pw = bn_weights_for(in, &PS, st->probe_data, P, own);
     f3 Lsh[9];
     for (int m = 0; m < 9; m++) Lsh[m] = F3(0.0f, 0.0f, 0.0f);
     for (int q = 0; q < 8; q++) {

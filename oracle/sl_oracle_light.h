@@ -78,6 +78,9 @@ typedef struct orc_probe_layout {
   float levels[16];
   const float* ground; /* dims[0] x dims[1], or NULL (0) */
   float tmax;
+  uint32_t part_probes; /* 1: 8 probes per part after the lattice, gathering for the movable ones */
+  uint32_t n_vols;      /* static probe volumes: (part, nx, ny, nz) each */
+  uint32_t vols[32][4];
 } orc_probe_layout;
 
 typedef struct orc_bounce_in {

@@ -39,7 +39,8 @@ class RenderOptions(C.Structure):
 class ProbeLayout(C.Structure):
     """sl_probe_layout (include/splatlight.h)."""
     _fields_ = [("dims", C.c_uint32 * 3), ("terrain", C.c_uint32), ("lo", C.c_float * 3), ("step", C.c_float * 3),
-                ("levels", C.c_float * 16), ("ground", C.c_void_p), ("tmax", C.c_float)]
+                ("levels", C.c_float * 16), ("ground", C.c_void_p), ("tmax", C.c_float), ("n_vols", C.c_uint32),
+                ("vols", (C.c_uint32 * 4) * 32)]
 
 
 class BatchOptions(C.Structure):

@@ -316,7 +316,7 @@ def environment_sky(env: dict | None):
 def probe_layout(asset: Asset) -> dict:
     """probeLayout (src/lighting.js:220-286) on the asset's header: the room layout for an asset with `room`, else
     the terrain layout over `bounds` (probes.layout may force either); probes.dims / heights_m / terrain_parts as
-    given (the static probe volumes of :289-314 are not part of this pipeline)."""
+    given; the static probe volumes (probes.volumes, else probeVolumes's rule, :289-314)."""
     from . import probes as PR
     h = asset.header
     pr = h.get("probes") or {}
@@ -334,6 +334,9 @@ def probe_layout(asset: Asset) -> dict:
         return PR.room_layout(box, environment=env)
     names = [p.get("name") for p in h["parts"]]
     tp = [names.index(n) for n in pr.get("terrain_parts", []) if n in names]
+    named = None
+    if pr.get("volumes"):
+        named = [(names.index(v["part"]), v["dims"]) for v in pr["volumes"] if v.get("part") in names]
     return PR.terrain_layout(asset.gaussians, asset.parts, box, dims=tuple(pr.get("dims", (16, 16, 5))[:2]),
                              heights=tuple(pr.get("heights_m", (0.3, 1.0, 3.0, 8.0, 20.0))), terrain_parts=tp,
-                             environment=env)
+                             environment=env, volumes=named)

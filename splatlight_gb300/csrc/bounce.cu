@@ -117,15 +117,74 @@ __device__ __forceinline__ uint32_t cell_of(f3 w) {
 __device__ __forceinline__ float ground_at(const BounceParams& B, const float* ground, uint32_t i, uint32_t j) {
   return ground ? ground[i * B.dims[1] + j] : 0.0f;
 }
-__device__ __forceinline__ f3 probe_pos(const BounceParams& B, const float* ground, uint32_t p) {
+__device__ __forceinline__ f3 lattice_pos(const BounceParams& B, const float* ground, uint32_t p) {
   const uint32_t i = p / (B.dims[1] * B.dims[2]), j = (p / B.dims[2]) % B.dims[1], k = p % B.dims[2];
   return F3(B.lo[0] + B.step[0] * (float)i, B.lo[1] + B.step[1] * (float)j, ground_at(B, ground, i, j) + B.levels[k]);
+}
+
+// is_part_probe_part (bounce.wgsl:264-266): a movable part's Gaussians read its own 8 probes
+__device__ __forceinline__ bool part_probe_part(const BounceParams& B, const sl_part* parts, uint32_t q) {
+  return q < B.part_count && (parts[q].flags & 1u) == 0u && parts[q].root != kNone;
+}
+__device__ __forceinline__ bool has_vol(const BounceParams& B, uint32_t q) { return q < 32u && B.vol_dims[q][0] > 0u; }
+__device__ __forceinline__ uint32_t vol_of_probe(const BounceParams& B, uint32_t r) {
+  for (uint32_t q = 0; q < B.part_count && q < 32u; q++) {
+    const uint32_t n = B.vol_dims[q][0] * B.vol_dims[q][1] * B.vol_dims[q][2];
+    if (n > 0u && r >= B.vol_first[q] && r < B.vol_first[q] + n) return q;
+  }
+  return kNone;
+}
+// part_probe_frame (bounce.wgsl:256-262): the part root's centre and 0.95 of its axis spreads, at most half its bound
+__device__ __forceinline__ void part_frame(const sl_node* __restrict__ tnodes, const sl_part* parts, uint32_t q, f3& c,
+                                           f3& h) {
+  const sl_node* nd = &tnodes[parts[q].root];
+  const f3 a = F3(nd->cinv_diag[0], nd->cinv_diag[1], nd->cinv_diag[2]);
+  const f3 o = F3(nd->cinv_off[0], nd->cinv_off[1], nd->cinv_off[2]);
+  const float det = a.x * (a.y * a.z - o.z * o.z) - o.x * (o.x * a.z - o.z * o.y) + o.y * (o.x * o.z - a.y * o.y);
+  const f3 var = div3(F3(a.y * a.z - o.z * o.z, a.x * a.z - o.y * o.y, a.x * a.y - o.x * o.x), fmaxf(det, 1e-30f));
+  const float hb = 0.5f * parts[q].bound[3];
+  c = F3(nd->mean[0], nd->mean[1], nd->mean[2]);
+  h = F3(fminf(0.95f * sqrtf(fmaxf(var.x, 0.0f)), hb), fminf(0.95f * sqrtf(fmaxf(var.y, 0.0f)), hb),
+         fminf(0.95f * sqrtf(fmaxf(var.z, 0.0f)), hb));
+}
+// vol_frame (bounce.wgsl:69-73): the part frame widened to about the part's extent
+__device__ __forceinline__ void vol_frame(const sl_node* __restrict__ tnodes, const sl_part* parts, uint32_t q, f3& c,
+                                          f3& h) {
+  f3 h0;
+  part_frame(tnodes, parts, q, c, h0);
+  const float R = parts[q].bound[3];
+  h = F3(fminf(1.6f * h0.x, R), fminf(1.6f * h0.y, R), fminf(1.6f * h0.z, R));
+}
+// probe_pos (bounce.wgsl:217-244): the lattice, each part's 2x2x2 cube, the volumes' grids
+__device__ __forceinline__ f3 probe_pos(const BounceParams& B, const float* ground, const sl_node* __restrict__ tnodes,
+                                        const sl_part* parts, uint32_t p) {
+  if (p >= B.NL + 8u * B.part_count) {
+    const uint32_t r = p - B.NL, q = vol_of_probe(B, r);
+    if (q == kNone) return F3(0.0f, 0.0f, 0.0f);
+    const uint32_t* d = B.vol_dims[q];
+    const uint32_t l = r - B.vol_first[q];
+    const f3 ijk = F3((float)(l / (d[1] * d[2])), (float)((l / d[2]) % d[1]), (float)(l % d[2]));
+    f3 c, h;
+    vol_frame(tnodes, parts, q, c, h);
+    const f3 den = F3(fmaxf((float)d[0] - 1.0f, 1.0f), fmaxf((float)d[1] - 1.0f, 1.0f), fmaxf((float)d[2] - 1.0f, 1.0f));
+    const f3 t = mul3v(mul3(h, 2.0f), ijk);
+    return xf_point(parts[q].xf, add3(sub3(c, h), F3(t.x / den.x, t.y / den.y, t.z / den.z)));
+  }
+  if (p >= B.NL) {
+    const uint32_t q = (p - B.NL) / 8u, k = (p - B.NL) % 8u;
+    const f3 sgn = F3((float)(k >> 2u) * 2.0f - 1.0f, (float)((k >> 1u) & 1u) * 2.0f - 1.0f,
+                      (float)(k & 1u) * 2.0f - 1.0f);
+    f3 c, h;
+    part_frame(tnodes, parts, q, c, h);
+    return xf_point(parts[q].xf, add3(c, mul3v(sgn, h)));
+  }
+  return lattice_pos(B, ground, p);
 }
 
 // probe_cheb (bounce.wgsl:759-768): DDGI Chebyshev visibility of P from probe p (pow(x, 3) as x x x)
 __device__ __forceinline__ float probe_cheb(const BounceParams& B, const float* ground, const float4* pd, uint32_t p,
                                             f3 P) {
-  const f3 v = sub3(P, probe_pos(B, ground, p));
+  const f3 v = sub3(P, lattice_pos(B, ground, p));
   const float dist = len3(v);
   const float4 mm = pd[2u * (p * kCells + cell_of(div3(v, fmaxf(dist, 1e-9f)))) + 1u];
   const float var = fmaxf(mm.y - mm.x * mm.x, 1e-4f);
@@ -180,7 +239,7 @@ __device__ __forceinline__ Weights probe_weights(const BounceParams& B, const fl
       if (ii < 0 || jj < 0 || kk < 0 || ii >= (int)dm[0] || jj >= (int)dm[1] || kk >= (int)dm[2]) continue;
       const uint32_t p = ((uint32_t)ii * dm[1] + (uint32_t)jj) * dm[2] + (uint32_t)kk;
       if (pd[2u * (p * kCells) + 1u].z <= 0.0f) continue;
-      const float d = fmaxf(len3(sub3(P, probe_pos(B, ground, p))), 0.05f);
+      const float d = fmaxf(len3(sub3(P, lattice_pos(B, ground, p))), 0.05f);
       const float w = fmaxf(probe_cheb(B, ground, pd, p, P), 1e-3f) / (d * d);
       if (w <= out.w[7]) continue;
       uint32_t at = 7u;
@@ -202,6 +261,56 @@ __device__ __forceinline__ Weights probe_weights(const BounceParams& B, const fl
 #pragma unroll
   for (int c = 0; c < 8; c++) out.w[c] /= fmaxf(wsum, 1e-12f);
   return out;
+}
+
+__device__ __forceinline__ float sel(uint32_t o, float f) { return o ? f : 1.0f - f; }
+
+// probe_weights (bounce.wgsl:813-885): a movable part's Gaussians trilinear over its own 8 probes, a static volume's
+// over its grid (neither with the Chebyshev test), the rest over the lattice
+__device__ __forceinline__ Weights weights_for(const BounceParams& B, const float* ground, const float4* pd,
+                                               const sl_node* __restrict__ tnodes, const sl_part* parts, f3 P,
+                                               uint32_t own) {
+  if (part_probe_part(B, parts, own)) {
+    f3 c, h;
+    part_frame(tnodes, parts, own, c, h);
+    const float* xf = parts[own].xf;
+    const f3 lp = xf_dir_inv(xf, sub3(P, F3(xf[3], xf[7], xf[11])));
+    const f3 num = add3(sub3(lp, c), h);
+    const f3 f = F3(clampf(num.x / fmaxf(2.0f * h.x, 1e-6f), 0.0f, 1.0f),
+                    clampf(num.y / fmaxf(2.0f * h.y, 1e-6f), 0.0f, 1.0f),
+                    clampf(num.z / fmaxf(2.0f * h.z, 1e-6f), 0.0f, 1.0f));
+    Weights out;
+#pragma unroll
+    for (uint32_t k = 0; k < 8u; k++) {
+      out.pid[k] = B.NL + own * 8u + k;
+      out.w[k] = sel(k >> 2u, f.x) * sel((k >> 1u) & 1u, f.y) * sel(k & 1u, f.z);
+    }
+    return out;
+  }
+  if (has_vol(B, own)) {
+    f3 c, h;
+    vol_frame(tnodes, parts, own, c, h);
+    const float* xf = parts[own].xf;
+    const f3 lp = xf_dir_inv(xf, sub3(P, F3(xf[3], xf[7], xf[11])));
+    const uint32_t* d = B.vol_dims[own];
+    const f3 num = add3(sub3(lp, c), h);
+    const f3 fq = F3(clampf(num.x / fmaxf(2.0f * h.x, 1e-6f), 0.0f, 1.0f) * ((float)d[0] - 1.0f),
+                     clampf(num.y / fmaxf(2.0f * h.y, 1e-6f), 0.0f, 1.0f) * ((float)d[1] - 1.0f),
+                     clampf(num.z / fmaxf(2.0f * h.z, 1e-6f), 0.0f, 1.0f) * ((float)d[2] - 1.0f));
+    uint32_t fi[3] = {(uint32_t)floorf(fq.x), (uint32_t)floorf(fq.y), (uint32_t)floorf(fq.z)};
+#pragma unroll
+    for (int a = 0; a < 3; a++) fi[a] = fi[a] < d[a] - 2u ? fi[a] : d[a] - 2u;
+    const f3 fr = F3(fq.x - (float)fi[0], fq.y - (float)fi[1], fq.z - (float)fi[2]);
+    Weights out;
+#pragma unroll
+    for (uint32_t k = 0; k < 8u; k++) {
+      const uint32_t ox = k >> 2u, oy = (k >> 1u) & 1u, oz = k & 1u;
+      out.pid[k] = B.NL + B.vol_first[own] + ((fi[0] + ox) * d[1] + (fi[1] + oy)) * d[2] + (fi[2] + oz);
+      out.w[k] = sel(ox, fr.x) * sel(oy, fr.y) * sel(oz, fr.z);
+    }
+    return out;
+  }
+  return probe_weights(B, ground, pd, P);
 }
 
 __device__ __forceinline__ uint32_t mat_index(const sl_gaussian& G, uint32_t mat_count) {
@@ -358,10 +467,20 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(const __grid_constant_
   const uint32_t id = blockIdx.x * kThreads + threadIdx.x;
   if (id >= B.NP * kCells) return;
   const uint32_t p = id / kCells, c = id % kCells;
-  const f3 o = probe_pos(B, ground, p);
+  // a part probe skips its own part (a static part's stay idle); a volume's probes skip their object
+  uint32_t skip = kNone;
+  if (p >= B.NL && p < B.NL + 8u * B.part_count) {
+    skip = (p - B.NL) / 8u;
+    if (!part_probe_part(B, parts, skip)) return;
+  } else if (p >= B.NL) {
+    skip = vol_of_probe(B, p - B.NL);
+    if (skip == kNone) return;
+  }
+  const f3 o = probe_pos(B, ground, tnodes, parts, p);
   const f3 w = cell_dir(tab, c);
+  const float brad = p < B.NL ? B.brad : 0.0f;   // probes off the lattice cut around themselves
   f3 cen = o;
-  if (!B.terrain) {
+  if (!B.terrain && p < B.NL) {
     const uint32_t dz = B.dims[2];
     const float bx = (float)((p / (B.dims[1] * dz)) / 2u), by = (float)(((p / dz) % B.dims[1]) / 2u),
                 bz = (float)((p % dz) / 2u);
@@ -376,7 +495,7 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(const __grid_constant_
   for (uint32_t q = 0; q < B.part_count; q++) {
     const float* xf = parts[q].xf;
     const uint32_t root = parts[q].root;
-    if (root == kNone) continue;
+    if (root == kNone || q == skip) continue;
     const f3 Po = xf_dir_inv(xf, sub3(o, F3(xf[3], xf[7], xf[11])));
     const f3 wr = xf_dir_inv(xf, w);
     const f3 cr = xf_dir_inv(xf, sub3(cen, F3(xf[3], xf[7], xf[11])));
@@ -393,7 +512,7 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(const __grid_constant_
       if (dot3(e, e) > mr.w * mr.w) continue;
       const GNode nd = load_gnode(&tnodes[ni]);
       bool use_node = ni < B.G;
-      if (!use_node) use_node = len3(sub3(cr, nd.mean)) - B.brad > kProbeTheta * nd.smax;
+      if (!use_node) use_node = len3(sub3(cr, nd.mean)) - brad > kProbeTheta * nd.smax;
       if (use_node) {
         const float tau = nd.kappa * sqrtf(fmaxf(dot3(wr, sym_mul(nd.sn_d, nd.sn_o, wr)), 0.0f)) *
                           seg_geom(nd, Po, wr, 0.0f, t1);
@@ -468,6 +587,10 @@ __global__ void __launch_bounds__(kThreads) valid_kernel(const __grid_constant__
                                                          const sl_part* __restrict__ parts, float4* __restrict__ pd) {
   const uint32_t p = blockIdx.x * kThreads + threadIdx.x;
   if (p >= B.NP) return;
+  if (p >= B.NL) {  // part and volume probes skip their own object, so never sit inside it
+    pd[2u * (p * kCells) + 1u].z = 1.0f;
+    return;
+  }
   uint32_t cnt[17];
 #pragma unroll
   for (int i = 0; i < 17; i++) cnt[i] = 0u;
@@ -517,6 +640,7 @@ __global__ void __launch_bounds__(kThreads) bounce_kernel(const __grid_constant_
                                                           const sl_vgrid* __restrict__ vgrid,
                                                           const sl_part* __restrict__ parts,
                                                           const sl_material* __restrict__ mats,
+                                                          const sl_node* __restrict__ tnodes,
                                                           const float* __restrict__ ground,
                                                           const float4* __restrict__ pd,
                                                           const float4* __restrict__ probe_sh,
@@ -531,7 +655,7 @@ __global__ void __launch_bounds__(kThreads) bounce_kernel(const __grid_constant_
   const uint32_t own = G.part_surface & 0xFFFFu;
   const float* xf = parts[own].xf;
   const f3 P = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
-  const Weights pw = probe_weights(B, ground, pd, P);
+  const Weights pw = weights_for(B, ground, pd, tnodes, parts, P, own);
   f3 Lsh[9];
 #pragma unroll
   for (int m = 0; m < 9; m++) Lsh[m] = F3(0.0f, 0.0f, 0.0f);
@@ -614,7 +738,8 @@ cudaError_t launch_bounce_frame(const BounceParams& B, const ShadeParams& SH, co
     valid_kernel<<<blocks(B.NP), kThreads, 0, s>>>(B, D.parts, D.probe_data);
     psh2_kernel<<<blocks(B.NP), kThreads, 0, s>>>(B, D.tab, D.probe_data, D.probe_sh);
   }
-  bounce_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.mats, D.ground, D.probe_data,
+  bounce_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.mats, D.tnodes, D.ground,
+                                                 D.probe_data,
                                                  D.probe_sh, D.xfer, D.lo_b);
   return cudaGetLastError();
 }

@@ -929,8 +929,9 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
     for (uint32_t q = 0; q < P; q++)
       if (r->parts[q].root != 0xFFFFFFFFu && r->parts[q].root >= l->n_tree)
         return fail(SL_ERR_INVALID_ARG, "a part's tree root lies outside the tree set by sl_lighting_set_tree");
+    if (P != l->BP.part_count)
+      return fail(SL_ERR_INVALID_ARG, "the part count changed since sl_lighting_set_probes: set the probes again");
     BounceParams B = l->BP;
-    B.part_count = P;
     B.alpha = l->bn_first ? 1.0f : l->bn_blend;
     B.frame = l->bn_frame;
     B.force = l->bn_first ? 1u : 0u;
@@ -1016,13 +1017,32 @@ int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* lay, uint32_t 
   for (uint32_t k = 0; k + 1 < dz; k++)
     if (!(lay->levels[k + 1] > lay->levels[k])) return fail(SL_ERR_INVALID_ARG, "probe levels must ascend");
   if (!(blend > 0.0f && blend <= 1.0f)) return fail(SL_ERR_INVALID_ARG, "blend must be in (0, 1]");
+  if (lay->n_vols > 32) return fail(SL_ERR_INVALID_ARG, "at most 32 probe volumes");
   cudaSetDevice(l->device);
-  const uint32_t G = l->count, N = l->n_tree, NP = dx * dy * dz;
+  const uint32_t G = l->count, N = l->n_tree, NL = dx * dy * dz, P = l->r->part_count;
   BounceParams& B = l->BP;
   B = BounceParams{};
+  // the probes after the lattice: 8 per part, then the volumes' grids (lighting.js:739-740, 797-799)
+  uint32_t off = 8u * P;
+  for (uint32_t v = 0; v < lay->n_vols; v++) {
+    const uint32_t q = lay->vols[v][0], nx = lay->vols[v][1], ny = lay->vols[v][2], nz = lay->vols[v][3];
+    if (q >= 32 || q >= P) return fail(SL_ERR_INVALID_ARG, "a probe volume names a part outside 0-31 or the scene");
+    if (l->r->parts[q].root >= N) return fail(SL_ERR_INVALID_ARG, "a probe volume's part has no tree root");
+    if (nx < 2 || ny < 2 || nz < 2 || nx > 64 || ny > 64 || nz > 64)
+      return fail(SL_ERR_INVALID_ARG, "probe volume grids take 2-64 probes per axis");
+    if (B.vol_dims[q][0]) return fail(SL_ERR_INVALID_ARG, "two probe volumes on one part");
+    B.vol_first[q] = off;
+    B.vol_dims[q][0] = nx;
+    B.vol_dims[q][1] = ny;
+    B.vol_dims[q][2] = nz;
+    off += nx * ny * nz;
+  }
+  const uint32_t NP = NL + off;
   B.G = G;
   B.N = N;
   B.NP = NP;
+  B.NL = NL;
+  B.part_count = P;
   B.mat_count = l->material_count;
   B.dims[0] = dx;
   B.dims[1] = dy;

@@ -17,7 +17,8 @@ constexpr uint32_t kTabFloats = 512 + 42 + 126;
 
 // bounce.wgsl ProbeParams (the fields this path reads) + the frame's inputs
 struct BounceParams {
-  uint32_t G, N, NP, part_count, mat_count;
+  uint32_t G, N, NP, NL, part_count, mat_count;  // NP: every probe; NL: the lattice's (then 8 per part, volumes)
+  uint32_t vol_first[32], vol_dims[32][3];       // per part: its static volume's first probe after the lattice, grid
   uint32_t dims[3], terrain;
   float lo[3], step[3], levels[16];
   float tmax, brad, alpha;

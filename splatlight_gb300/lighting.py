@@ -96,8 +96,13 @@ class Lighting:
         self._ground = np.ascontiguousarray(layout["ground"], np.float32) if layout.get("ground") is not None else None
         lay.ground = self._ground.ctypes.data if self._ground is not None else None
         lay.tmax = float(layout["tmax"])
+        vols = list(layout.get("vols", []))[:32]
+        lay.n_vols = len(vols)
+        for i, v in enumerate(vols):
+            lay.vols[i][:] = [int(x) for x in v]
         N.check(self._lib.sl_lighting_set_probes(self._h, C.byref(lay), int(max_depth), C.c_float(blend)))
-        self.probe_count = int(np.prod(layout["dims"]))
+        self.probe_count = int(np.prod(layout["dims"])) + 8 * self.renderer.part_count + \
+            sum(int(v[1]) * int(v[2]) * int(v[3]) for v in vols)
 
     def set_sky(self, sh_rgb) -> None:
         """The probes' sky: up to 16 real SH coefficients (bands 0-3), rgb; None or empty = no sky."""

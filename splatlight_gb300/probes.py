@@ -27,16 +27,17 @@ def room_layout(box, environment: bool = False) -> dict:
     step = [2 * h / (n - 1) for h in half]
     levels = [lo[2] + k * step[2] for k in range(n)]
     return {"terrain": False, "dims": [n, n, n], "lo": lo, "step": step, "levels": levels, "ground": None,
-            "tmax": _tmax(box, environment)}
+            "tmax": _tmax(box, environment), "vols": []}
 
 
 def terrain_layout(gaussians: np.ndarray, parts: np.ndarray, box, dims=(16, 16, 5),
-                   heights=(0.3, 1.0, 3.0, 8.0, 20.0), terrain_parts=None, environment: bool = True) -> dict:
+                   heights=(0.3, 1.0, 3.0, 8.0, 20.0), terrain_parts=None, environment: bool = True,
+                   volumes=None) -> dict:
     """The terrain layout (lighting.js:234-286): dims[0] x dims[1] columns over box's x, y, each with one probe per
     height above the terrain under it -- the highest Gaussian centre of the terrain parts in the column's cell, empty
     cells taking their filled neighbours' mean ring by ring, else the box floor.  The terrain parts are the named
     ones, else the static part (flags bit 0) with the widest x-y footprint of its Gaussian centres (sampled every
-    max(1, n >> 12))."""
+    max(1, n >> 12)).  volumes: the asset's named (part, dims) volumes, else probe_volumes picks them."""
     dims = [int(dims[0]), int(dims[1]), len(heights)]
     if dims[0] * dims[1] > 1024 or dims[2] > 16:
         raise ValueError("probe terrain layout: at most 1024 columns and 16 levels")
@@ -84,7 +85,27 @@ def terrain_layout(gaussians: np.ndarray, parts: np.ndarray, box, dims=(16, 16, 
                     ground[i * dims[1] + j] = s / c
     ground[np.isinf(ground)] = box[2][0]
     return {"terrain": True, "dims": dims, "lo": lo, "step": [step[0], step[1], 0.0], "levels": list(heights),
-            "ground": ground.astype(np.float32), "tmax": _tmax(box, environment)}
+            "ground": ground.astype(np.float32), "tmax": _tmax(box, environment),
+            "vols": probe_volumes(parts, box, tp, volumes)}
+
+
+def probe_volumes(parts: np.ndarray, box, terrain_parts, named=None) -> list:
+    """probeVolumes (lighting.js:289-314): the named (part, dims) volumes, else every static part but the terrain
+    whose bounding radius is 1 m to a quarter of the scene's half-diagonal (a tree, a rock, a house; not the ground or
+    a carpet of grass), a grid of about 1.2 m spacing, 2-6 per axis.  Parts 0-31 only."""
+    if named is not None:
+        return [(int(q), *[int(v) for v in d]) for q, d in named if q < 32]
+    half = 0.5 * math.hypot(*[b - a for a, b in box])
+    out = []
+    for q, p in enumerate(parts):
+        if q >= 32 or q in terrain_parts or (int(p["flags"]) & 1) == 0:
+            continue
+        R = float(p["bound"][3])
+        if R < 1.0 or R > 0.25 * half:
+            continue
+        n = max(2, min(6, math.floor(R / 1.2 + 0.5)))   # Math.round
+        out.append((q, n, n, n))
+    return out
 
 
 def for_scene(scene) -> dict:

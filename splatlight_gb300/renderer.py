@@ -27,6 +27,7 @@ class SplatRenderer:
                                              max_emitters, C.byref(h)))
         self._h = h
         self.count = len(self._g)
+        self.part_count = len(self._p)
         self.last_stats = N.RenderStats()
         self._bound = None
 
