@@ -466,7 +466,7 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(const __grid_constant_
                                                           float4* __restrict__ pd) {
   const uint32_t id = blockIdx.x * kThreads + threadIdx.x;
   if (id >= B.NP * kCells) return;
-  const uint32_t p = id / kCells, c = id % kCells;
+  const uint32_t p = id / kCells, c = id % kCells;  // one probe per block; a warp takes two elevation rows of cells
   // a part probe skips its own part (a static part's stay idle); a volume's probes skip their object
   uint32_t skip = kNone;
   if (p >= B.NL && p < B.NL + 8u * B.part_count) {
@@ -491,7 +491,14 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(const __grid_constant_
   float ht[kHitMax], hv[kHitMax];
   uint32_t hn[kHitMax];
   uint32_t k = 0;
-  uint32_t stack[kStack];
+  // The warp's 32 rays belong to one probe, so whether a node is used whole or opened (the cut about the probe's
+  // centre) is the same for all of them: the warp walks one depth-first stack, each entry carrying the lanes whose
+  // rays met its parent, and a lane acts only on the entries in its mask.  Restricted to one lane this is exactly that
+  // ray's own depth-first walk (the same nodes in the same order), so its hits, and everything after, are unchanged.
+  __shared__ uint32_t s_node[kThreads / 32][kStack], s_mask[kThreads / 32][kStack];
+  const uint32_t lane = threadIdx.x & 31u, wi = threadIdx.x >> 5;
+  uint32_t* stn = s_node[wi];
+  uint32_t* stm = s_mask[wi];
   for (uint32_t q = 0; q < B.part_count; q++) {
     const float* xf = parts[q].xf;
     const uint32_t root = parts[q].root;
@@ -499,54 +506,76 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(const __grid_constant_
     const f3 Po = xf_dir_inv(xf, sub3(o, F3(xf[3], xf[7], xf[11])));
     const f3 wr = xf_dir_inv(xf, w);
     const f3 cr = xf_dir_inv(xf, sub3(cen, F3(xf[3], xf[7], xf[11])));
-    stack[0] = root;
+    if (lane == 0) {
+      stn[0] = root;
+      stm[0] = 0xffffffffu;
+    }
+    __syncwarp();
     uint32_t sp = 1;
-    while (sp > 0u) {
+    // a tree visits each node once; the bound (warp-uniform) only keeps a malformed, cyclic tree from spinning
+    for (uint32_t guard = 0; sp > 0u && guard < 4u * B.N + 64u; guard++) {
       sp--;
-      const uint32_t ni = stack[sp];
-      // the bound test first, on one 16-byte load (mean, radius); the rest of the node only when the ray meets it
-      const float4 mr = __ldg(reinterpret_cast<const float4*>(&tnodes[ni]));
-      const f3 d = sub3(F3(mr.x, mr.y, mr.z), Po);
-      const float tt = clampf(dot3(d, wr), 0.0f, t1);
-      const f3 e = sub3(d, mul3(wr, tt));
-      if (dot3(e, e) > mr.w * mr.w) continue;
+      const uint32_t ni = stn[sp], mask = stm[sp];
+      __syncwarp();  // every lane has read the entry before a push may overwrite it
+      // the bound test on one 16-byte load (mean, radius), by the lanes whose rays met the parent
+      bool hit = false;
+      f3 d = F3(0.0f, 0.0f, 0.0f);
+      if ((mask >> lane) & 1u) {
+        const float4 mr = __ldg(reinterpret_cast<const float4*>(&tnodes[ni]));
+        d = sub3(F3(mr.x, mr.y, mr.z), Po);
+        const float tt = clampf(dot3(d, wr), 0.0f, t1);
+        const f3 e = sub3(d, mul3(wr, tt));
+        hit = !(dot3(e, e) > mr.w * mr.w);
+      }
+      const uint32_t hits = __ballot_sync(0xffffffffu, hit);
+      if (hits == 0u) continue;
       const GNode nd = load_gnode(&tnodes[ni]);
       bool use_node = ni < B.G;
       if (!use_node) use_node = len3(sub3(cr, nd.mean)) - brad > kProbeTheta * nd.smax;
       if (use_node) {
-        const float tau = nd.kappa * sqrtf(fmaxf(dot3(wr, sym_mul(nd.sn_d, nd.sn_o, wr)), 0.0f)) *
-                          seg_geom(nd, Po, wr, 0.0f, t1);
-        if (tau > 1e-6f) {
-          const f3 cw = sym_mul(nd.cinv_d, nd.cinv_o, wr);
-          const float den = dot3(cw, wr);
-          const float tp = fabsf(den) > 1e-30f ? clampf(dot3(cw, d) / den, 0.0f, t1) : t1;
-          uint32_t at = k < kHitMax - 1u ? k : kHitMax - 1u;
-          const uint32_t l = kHitMax - 1u;
-          if (k == kHitMax && tp >= ht[l]) {
-            ht[l] = fmaxf(ht[l], tp);
-            hv[l] = fminf(hv[l] + tau, 64.0f);
-            continue;
+        if (hit) {
+          const float tau = nd.kappa * sqrtf(fmaxf(dot3(wr, sym_mul(nd.sn_d, nd.sn_o, wr)), 0.0f)) *
+                            seg_geom(nd, Po, wr, 0.0f, t1);
+          if (tau > 1e-6f) {
+            const f3 cw = sym_mul(nd.cinv_d, nd.cinv_o, wr);
+            const float den = dot3(cw, wr);
+            const float tp = fabsf(den) > 1e-30f ? clampf(dot3(cw, d) / den, 0.0f, t1) : t1;
+            uint32_t at = k < kHitMax - 1u ? k : kHitMax - 1u;
+            const uint32_t l = kHitMax - 1u;
+            if (k == kHitMax && tp >= ht[l]) {
+              ht[l] = fmaxf(ht[l], tp);
+              hv[l] = fminf(hv[l] + tau, 64.0f);
+            } else {
+              const bool full = k == kHitMax;
+              const float sv = full ? hv[l] : 0.0f, stv = full ? ht[l] : 0.0f;
+              while (at > 0u && ht[at - 1u] > tp) {
+                ht[at] = ht[at - 1u];
+                hv[at] = hv[at - 1u];
+                hn[at] = hn[at - 1u];
+                at--;
+              }
+              ht[at] = tp;
+              hv[at] = tau;
+              hn[at] = ni;
+              if (full) {
+                ht[l] = fmaxf(ht[l], stv);
+                hv[l] = fminf(hv[l] + sv, 64.0f);
+              }
+              k = k + 1u < kHitMax ? k + 1u : kHitMax;
+            }
           }
-          const bool full = k == kHitMax;
-          const float sv = full ? hv[l] : 0.0f, stv = full ? ht[l] : 0.0f;
-          while (at > 0u && ht[at - 1u] > tp) {
-            ht[at] = ht[at - 1u];
-            hv[at] = hv[at - 1u];
-            hn[at] = hn[at - 1u];
-            at--;
-          }
-          ht[at] = tp;
-          hv[at] = tau;
-          hn[at] = ni;
-          if (full) {
-            ht[l] = fmaxf(ht[l], stv);
-            hv[l] = fminf(hv[l] + sv, 64.0f);
-          }
-          k = k + 1u < kHitMax ? k + 1u : kHitMax;
         }
       } else {
-        for (uint32_t j = nd.child_lo; j < nd.child_hi; j++)
-          if (sp < kStack) stack[sp++] = kids[j];
+        for (uint32_t j = nd.child_lo; j < nd.child_hi; j++) {
+          if (sp < kStack) {
+            if (lane == 0) {
+              stn[sp] = kids[j];
+              stm[sp] = hits;
+            }
+            sp++;
+          }
+        }
+        __syncwarp();
       }
     }
   }
