@@ -681,7 +681,7 @@ def stage_rooflines(st, ms, peak_hbm, fp32_peak, peak_kind):
             "depth_sort": (52.0 * vis, "GB/s", peak_hbm, "hbm"),
             "bin": (56.0 * vis + 48.0 * ent, "GB/s", peak_hbm, "hbm"),
             "coverage": (12.0 * float(st.fragments), "TFLOP/s", fp32_peak, "fp32 issue"),
-            "shade": (336.0 * float(st.shaded), "GB/s", peak_hbm, "hbm"),
+            "shade": (336.0 * float(st.shaded), "GB/s", peak_hbm, "instruction issue"),
             "composite": (20.0 * float(st.fragments), "TFLOP/s", fp32_peak, "fp32 issue")}
     out = {}
     for k, (w, unit, peak, bound) in work.items():
@@ -691,6 +691,10 @@ def stage_rooflines(st, ms, peak_hbm, fp32_peak, peak_kind):
                   "peak": round(peak, 1), "frac": round(ach / peak, 4) if peak else None,
                   "peak_kind": peak_kind if unit == "GB/s" else "nominal FP32 issue rate at the sampled max SM clock",
                   "algorithmic_per_launch": w}
+        if bound == "instruction issue":
+            # the shading pass's cost is its per-light arithmetic (the footprint integrals, the SGGX and ASG lobes:
+            # issue-bound under ncu); its bytes are reported against HBM only for the survey's 336 B per Gaussian
+            out[k]["frac_of"] = "HBM (not the kernel's bound)"
     return out
 
 

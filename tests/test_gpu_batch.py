@@ -347,3 +347,29 @@ def test_bad_arguments(cuda):
             with pytest.raises(SplatlightError):
                 B.set_tile(16, 8)
             assert np.isfinite(B.render([v])[0]).all()
+
+
+def test_full_size_lit_batch(cuda):
+    """Config 2 at full size on its two largest scenes: the 1,048,576- and 2,097,152-Gaussian hill scenes lit (emitter
+    light map, sun maps), two 1920x1080 views of each from different cameras in one batch; every view's permutation,
+    ranges and lists equal the per-view path's, its image within 1e-3, with the per-view shading pass re-run at that
+    view's eye."""
+    s1 = scene.hill(1048576, seed=1)
+    s2 = scene.hill(2097152, seed=1)
+    eyes = {0: [s1.eye, camera.orbit_eye((0.0, 0.0, 1.5), 9.0, 1.2, 0.35)],
+            1: [s2.eye, camera.orbit_eye((0.0, 0.0, 1.5), 7.0, 3.9, 0.55)]}
+    with SplatRenderer(s1.gaussians, s1.parts) as r1, SplatRenderer(s2.gaussians, s2.parts) as r2:
+        L1 = for_scene(r1, s1)
+        L2 = for_scene(r2, s2)
+        L1.update(s1.eye, camera_forward(s1))
+        L2.update(s2.eye, camera_forward(s2))
+        ss, rr, LL = [s1, s2], [r1, r2], [L1, L2]
+        views = [View(k, _frame(ss[k], 1920, 1080, VIEW_LIT, eye=e, target=ss[k].target), e)
+                 for k in (0, 1) for e in eyes[k]]
+        with BatchRenderer(rr, LL, max_views=len(views)) as B:
+            _render(B, views)
+            for k, v in enumerate(views):
+                LL[v.scene].shade(v.eye)
+                _assert_view(B, k, v, rr[v.scene], (16, 16), exact=False)
+        L1.close()
+        L2.close()
