@@ -364,7 +364,8 @@ def run_sort(args, stream, flush, n=1 << 26):
     """The stable radix sort alone on n random keys: 16-bit (2 passes, sl_sort_keys16) and 24-bit segmented-style
     32-bit keys (3 passes, sl_sort_keys32), device time per call (digit histograms + passes + scratch clears), against
     the library sort (torch.sort, stable: CUB's radix sort) on the same keys.  Bandwidth uses the algorithmic bytes
-    per element 4 + 16 P (P passes; a key+value read and write per pass plus one key read for the histograms)."""
+    per element 4 + 16 P (P passes; a key+value read and write per pass plus one key read for the histograms).  The
+    library bars: CUB's DeviceRadixSort over the keys' own bits, and torch.sort over all 32 bits."""
     import ctypes as C
 
     import torch
@@ -407,10 +408,41 @@ def run_sort(args, stream, flush, n=1 << 26):
         with torch.cuda.stream(stream):
             torch.sort(k24, stable=True)
 
+    # CUB's DeviceRadixSort::SortPairs over the keys' own bits (end_bit 16 / 24), values = indices, as ours
+    from splatlight_gb300 import build as B
+    cub = C.CDLL(str(B.build_library_bar()))
+    for fn_name in ("cub_sort_pairs16", "cub_sort_pairs32"):
+        getattr(cub, fn_name).restype = C.c_int
+        getattr(cub, fn_name).argtypes = [C.c_void_p] * 4 + [C.c_uint32, C.c_int, C.c_void_p,
+                                                             C.POINTER(C.c_size_t), C.c_void_p]
+    idx = torch.arange(n, dtype=torch.int32, device="cuda")
+    k16o = torch.empty_like(k16h)
+    k24o = torch.empty_like(k24)
+    vo = torch.empty_like(idx)
+    tb = C.c_size_t(0)
+    cub.cub_sort_pairs16(None, None, None, None, n, 16, None, C.byref(tb), None)
+    tb24 = C.c_size_t(0)
+    cub.cub_sort_pairs32(None, None, None, None, n, 24, None, C.byref(tb24), None)
+    temp = torch.empty(max(tb.value, tb24.value) + 256, dtype=torch.uint8, device="cuda")
+
+    def cub16():
+        t = C.c_size_t(tb.value)
+        rc = cub.cub_sort_pairs16(k16h.data_ptr(), k16o.data_ptr(), idx.data_ptr(), vo.data_ptr(), n, 16,
+                                  temp.data_ptr(), C.byref(t), C.c_void_p(sc))
+        assert rc == 0, rc
+
+    def cub24():
+        t = C.c_size_t(tb24.value)
+        rc = cub.cub_sort_pairs32(k24.data_ptr(), k24o.data_ptr(), idx.data_ptr(), vo.data_ptr(), n, 24,
+                                  temp.data_ptr(), C.byref(t), C.c_void_p(sc))
+        assert rc == 0, rc
+
     res = {"n": n, "peak_gbs": hbm, "peak_kind": peak_kind,
-           "library_note": "torch.sort(stable) on the same values as int32 keys (no bit-range control: all 32 bits)"}
-    for name, fn, passes in (("ours_16bit", ours16, 2), ("ours_24bit", ours24, 3), ("library_16bit", lib16, 2),
-                             ("library_24bit", lib24, 3)):
+           "library_note": "cub_*: CUB DeviceRadixSort::SortPairs (the toolkit's onesweep) over bits [0, 16) / "
+                           "[0, 24), values = indices; torch_*: torch.sort(stable) on the same values as int32 keys "
+                           "(all 32 bits)"}
+    for name, fn, passes in (("ours_16bit", ours16, 2), ("ours_24bit", ours24, 3), ("cub_16bit", cub16, 2),
+                             ("cub_24bit", cub24, 3), ("torch_16bit", lib16, 2), ("torch_24bit", lib24, 3)):
         for _ in range(3):
             fn()
         ms = timed(fn, 5)

@@ -1,4 +1,5 @@
-"""Builds libsplatlight.so (every CUDA kernel and the C ABI) in-tree for sm_103a with nvcc.
+"""Builds libsplatlight.so (every CUDA kernel and the C ABI) in-tree for sm_103a with nvcc, and the sort leg's
+library bar (library_bar/libcub_sort.so: CUB's radix sort, for comparison only).
 
 Each translation unit compiles in parallel to an object under splatlight_gb300/_build/, then one shared library is
 linked next to this file.  project.cu, lighting.cu, tiles.cu, batch.cu and lod.cu are compiled with --fmad=false:
@@ -62,6 +63,24 @@ def needs_build() -> bool:
     t = LIB.stat().st_mtime
     deps = list(CSRC.glob("*")) + list((ROOT / "include").glob("*.h"))
     return any(p.stat().st_mtime > t for p in deps)
+
+
+BAR_SRC = PKG / "library_bar" / "cub_sort.cu"
+BAR_LIB = PKG / "library_bar" / "libcub_sort.so"
+
+
+def build_library_bar(force: bool = False) -> Path:
+    """The sort leg's library bar (CUB's DeviceRadixSort, a comparison baseline the pipeline never calls)."""
+    if not force and BAR_LIB.exists() and BAR_LIB.stat().st_mtime >= BAR_SRC.stat().st_mtime:
+        return BAR_LIB
+    tmp = BAR_LIB.with_suffix(".so.tmp")
+    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden", "-shared",
+           str(BAR_SRC), "-o", str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {BAR_SRC.name}:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, BAR_LIB)
+    return BAR_LIB
 
 
 def build(force: bool = False, jobs: int | None = None) -> Path:
