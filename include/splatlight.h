@@ -305,9 +305,12 @@ typedef struct sl_probe_layout {
  * movable parts gather, skipping their own part, and serve that part's Gaussians), then the static volumes' grids
  * (serving their part's Gaussians).  blend: the history weight of each gather after the first (1: taken as is, the
  * reference's default; 0.5: ?probeblend=ema).  Needs sl_lighting_set_tree and the renderer's parts (their count is
- * fixed from here on).  Not built: bounce_dirs (near-mirror materials, flake lobe below 0.1 rad, take no bounce),
+ * fixed from here on).  emitters_dark (the reference's emitBounceFix, on by default there): the Gaussians of the
+ * emitters' own part (sl_lighting_set_emitters' skip_part) send nothing into the probes -- their light reaches the
+ * scene as direct light -- though they still occlude.  Not built: bounce_dirs (near-mirror materials, flake lobe below 0.1 rad, take no bounce),
  * near-field visibility and reflection (off by default in the reference). */
-SL_API int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* layout, uint32_t max_depth, float blend);
+SL_API int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* layout, uint32_t max_depth, float blend,
+                                  int emitters_dark);
 /* The environment's sky for the probes (src/environment.js:116-124; bounce.wgsl sky_radiance :148-160): n_coef (<= 16)
  * real SH coefficients, rgb, bands 0-3, seen by probe rays that leave the scene.  0 coefficients: no sky. */
 SL_API int sl_lighting_set_sky(sl_lighting* l, const float* sh_rgb, uint32_t n_coef);

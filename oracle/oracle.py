@@ -484,7 +484,7 @@ class BounceIn(C.Structure):
                 ("normal", C.c_float * 3), ("lamp_T", C.c_void_p), ("env_T", C.c_void_p), ("lights", C.c_void_p),
                 ("n_lights", C.c_uint32), ("sky_sh", C.c_void_p), ("lay", ProbeLayoutC), ("max_depth", C.c_uint32),
                 ("eye", C.c_float * 3), ("alpha", C.c_float), ("frame", C.c_uint32), ("force", C.c_uint32),
-                ("moved_mask", C.c_uint32)]
+                ("moved_mask", C.c_uint32), ("dark_part", C.c_uint32)]
 
 
 class BounceState(C.Structure):
@@ -516,7 +516,8 @@ class Bounce:
     lamp_T, env_T, nodes) of oracle.lighting on the scene (the leaves' iso_norm and the maps' transmittance);
     layout: a probes.* layout dict; sky_sh: (16, 3) or None."""
 
-    def __init__(self, scene, tree, lit, layout, sky_sh=None, max_depth: int = 0, blend: float = 1.0):
+    def __init__(self, scene, tree, lit, layout, sky_sh=None, max_depth: int = 0, blend: float = 1.0,
+                 emitters_dark: bool = True):
         self.scene = scene
         G = scene.count
         tn = np.ascontiguousarray(tree[0]).copy()
@@ -528,6 +529,7 @@ class Bounce:
             max_depth = int(tn["depth"][G:].max()) + 1 if len(tn) > G else 1
         self.max_depth = max_depth
         self.blend = blend
+        self.dark_part = int(getattr(scene, "emit_skip_part", 0xFFFFFFFF)) if emitters_dark else 0xFFFFFFFF
         self.lamp_T = np.ascontiguousarray(lit[1], np.float32)
         self.env_T = np.ascontiguousarray(lit[2], np.float32)
         rec = np.ascontiguousarray(scene.emitters).view(np.float32).reshape(-1, 16).copy()
@@ -600,6 +602,7 @@ class Bounce:
         B.frame = self.frame
         B.force = 1 if self.first else 0
         B.moved_mask = moved_mask
+        B.dark_part = self.dark_part
         st = BounceState(**{k: v.ctypes.data for k, v in self.state.items()})
         rc = L.orc_bounce_frame(C.byref(B), C.byref(st), threads)
         if rc != 0:

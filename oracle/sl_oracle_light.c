@@ -2067,8 +2067,10 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
     const sl_node* nd = &in->nodes[g];
     const float* xf = in->parts[Gs->part_surface & 0xFFFFu].xf;
     float s3 = Gs->scale[0] * Gs->scale[1] * Gs->scale[2];
-    f3 Lr = add3(F3(st->lo_dir[4 * g], st->lo_dir[4 * g + 1], st->lo_dir[4 * g + 2]),
-                 F3(st->lo_b[12 * g + 4], st->lo_b[12 * g + 5], st->lo_b[12 * g + 6]));
+    int dark = (Gs->part_surface & 0xFFFFu) == in->dark_part; /* emitBounceFix (bounce.wgsl:1177-1187) */
+    f3 Lr = dark ? F3(0.0f, 0.0f, 0.0f)
+                 : add3(F3(st->lo_dir[4 * g], st->lo_dir[4 * g + 1], st->lo_dir[4 * g + 2]),
+                        F3(st->lo_b[12 * g + 4], st->lo_b[12 * g + 5], st->lo_b[12 * g + 6]));
     for (int k = 0; k < 14; k++) {
       f3 wo = xf_dir_inv(xf, F3(d14[3 * k], d14[3 * k + 1], d14[3 * k + 2]));
       float w = footprint(nd, s3 * s3, wo) * vgrid_lookup(&in->vgrid[g], wo);

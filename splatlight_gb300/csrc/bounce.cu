@@ -381,7 +381,10 @@ __global__ void __launch_bounds__(kThreads) leaf_kernel(const __grid_constant__ 
   const float* xf = parts[G.part_surface & 0xFFFFu].xf;
   const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
   const float4 ld = lo_dir[g], lb = lo_b[3u * g + 1u];
-  const f3 L = add3(F3(ld.x, ld.y, ld.z), F3(lb.x, lb.y, lb.z));
+  // the emitters' own part sends nothing into the probes (PP.refl.w, emitBounceFix: their light reaches the scene as
+  // direct light; the weights stay, so they still occlude)
+  const bool dark = (G.part_surface & 0xFFFFu) == B.dark_part;
+  const f3 L = dark ? F3(0.0f, 0.0f, 0.0f) : add3(F3(ld.x, ld.y, ld.z), F3(lb.x, lb.y, lb.z));
   const sl_vgrid& vg = vgrid[g];
   for (int k = 0; k < 14; k++) {
     const f3 wo = xf_dir_inv(xf, ld3(tab + kTabD14 + 3 * k));

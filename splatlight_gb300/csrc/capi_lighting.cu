@@ -937,6 +937,7 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
     B.force = l->bn_first ? 1u : 0u;
     B.moved_mask = moved_mask;
     B.has_sky = l->has_sky ? 1u : 0u;
+    B.dark_part = l->bn_emit_dark ? l->skip_part : 0xFFFFFFFFu;
     memcpy(B.sky, l->sky, sizeof(B.sky));
     for (int k = 0; k < 3; k++) B.eye[k] = eye[k];
     ShadeParams SHd;
@@ -1005,7 +1006,8 @@ int sl_renderer_bind_lighting(sl_renderer* r, sl_lighting* l) {
   return SL_OK;
 }
 
-int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* lay, uint32_t max_depth, float blend) {
+int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* lay, uint32_t max_depth, float blend,
+                           int emitters_dark) {
   if (!l || !lay) return fail(SL_ERR_INVALID_ARG, "null argument");
   if (l->n_tree < l->count || l->tree_depth.size() != l->n_tree)
     return fail(SL_ERR_INVALID_ARG, "the probe gather walks the scene's tree: sl_lighting_set_tree first");
@@ -1094,6 +1096,7 @@ int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* lay, uint32_t 
     SL_CHECK_CUDA(cudaMemset(z.b->ptr, 0, z.bytes), "bounce buffers");
   }
   l->bn_blend = blend;
+  l->bn_emit_dark = emitters_dark != 0;
   l->bn_first = true;
   l->bn_frame = 0;
   l->bounce_on = true;

@@ -23,6 +23,7 @@ struct BounceParams {
   float lo[3], step[3], levels[16];
   float tmax, brad, alpha;
   uint32_t frame, force, moved_mask, has_sky;
+  uint32_t dark_part;  // the part whose Gaussians send nothing into the probes (0xFFFFFFFF: none)
   float eye[3];
   float sky[48];  // 16 SH coefficients (bands 0-3), rgb
 };

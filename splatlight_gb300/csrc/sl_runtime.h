@@ -140,7 +140,7 @@ struct sl_lighting {
   std::vector<uint32_t> tree_depth, tree_part;
   // probe bounce (bounce.cu; lighting.js initBounce / encodeBounce): the layout and frame state in BP, the internal
   // nodes by depth for node_up, the sky SH
-  bool bounce_on = false, bn_first = true;
+  bool bounce_on = false, bn_first = true, bn_emit_dark = true;
   uint32_t bn_frame = 0;
   float bn_blend = 1.0f;
   sl::BounceParams BP{};

@@ -83,9 +83,10 @@ class Lighting:
                                                len(k)))
         self.tree_count = len(nd)
 
-    def set_probes(self, layout: dict, max_depth: int = 0, blend: float = 1.0) -> None:
+    def set_probes(self, layout: dict, max_depth: int = 0, blend: float = 1.0, emitters_dark: bool = True) -> None:
         """The probe bounce over a lattice (probes.room_layout / probes.terrain_layout); needs set_tree.  From the
-        next update on, each update runs one bounce frame and the renderer adds gain x lo_b to the lit colour."""
+        next update on, each update runs one bounce frame and the renderer adds gain x lo_b to the lit colour.
+        emitters_dark: the emitters' own part sends nothing into the probes (the reference's emitBounceFix)."""
         lay = N.ProbeLayout()
         lay.dims[:] = [int(v) for v in layout["dims"]]
         lay.terrain = 1 if layout["terrain"] else 0
@@ -100,7 +101,8 @@ class Lighting:
         lay.n_vols = len(vols)
         for i, v in enumerate(vols):
             lay.vols[i][:] = [int(x) for x in v]
-        N.check(self._lib.sl_lighting_set_probes(self._h, C.byref(lay), int(max_depth), C.c_float(blend)))
+        N.check(self._lib.sl_lighting_set_probes(self._h, C.byref(lay), int(max_depth), C.c_float(blend),
+                                                 1 if emitters_dark else 0))
         self.probe_count = int(np.prod(layout["dims"])) + 8 * self.renderer.part_count + \
             sum(int(v[1]) * int(v[2]) * int(v[3]) for v in vols)
 
