@@ -46,7 +46,9 @@ def _close(name, a, b, rtol=RTOL, atol=ATOL, frac=0.0, scaled=False):
     assert n <= frac * a.size, f"{name}: {n} of {a.size} differ (max abs {worst:.3e})"
 
 
-def _run(s, tree, layout, frames=FRAMES, gain=1.0):
+def _run(s, tree, layout, frames=FRAMES, gain=1.0, moves=None):
+    """frames bounce frames on GPU and restatement side by side; moves: {frame: (parts, moved_mask)} written before
+    that frame's update (the maps re-splat; both sides take the GPU's transmittance of that frame)."""
     import torch
     from oracle import oracle as O
     r = SplatRenderer(s.gaussians, s.parts)
@@ -57,12 +59,20 @@ def _run(s, tree, layout, frames=FRAMES, gain=1.0):
     fwd = camera_forward(s)
     b = None
     for f in range(frames):
-        L.update(s.eye, fwd)
+        mask = 0
+        if moves and f in moves:
+            parts, mask = moves[f]
+            r.write_parts(parts)
+        L.update(s.eye, fwd, moved_mask=mask)
         torch.cuda.synchronize()
+        col, lamp_t, env_t, nodes = L.read()
         if b is None:
-            col, lamp_t, env_t, nodes = L.read()
             b = O.Bounce(s, tree, (col, lamp_t, env_t, nodes), layout, sky_sh=s.sky_sh)
-        ost = b.step(s.eye, threads=16)
+        if moves and f in moves:
+            b.scene = dataclasses.replace(b.scene, parts=moves[f][0])
+        b.lamp_T = np.ascontiguousarray(lamp_t, np.float32)
+        b.env_T = np.ascontiguousarray(env_t, np.float32)
+        ost = b.step(s.eye, moved_mask=mask, threads=16)
         gst = L.read_bounce()
         pd, opd = gst["probe_data"], ost["probe_data"]
         # discrete fields exactly: first-hit part (.w of the colour record), near / backface flags, validity
@@ -111,6 +121,25 @@ def test_bounce_cornell_asset():
     s = A.asset_scene(A.load_asset(p), width=256, height=256)
     s, tree = S.with_tree(s)
     _run(s, tree, s.probes, frames=4)
+
+
+def test_bounce_moving_part():
+    """The Cornell room's short box (a movable part, with its 8 riding probes) moves between frames: the transfer of
+    the Gaussians near it refreshes, its probes follow it, the light maps re-splat; then it rests again."""
+    p = ASSETS / "cornell_sdf_room_plain_bin"
+    if not (p / "asset.json").exists():
+        pytest.skip("reference assets not copied (tests/golden/copy_assets.py)")
+    from splatlight_gb300 import asset as A
+    s = A.asset_scene(A.load_asset(p), width=256, height=256)
+    s, tree = S.with_tree(s)
+    q = next(i for i in range(len(s.parts)) if (int(s.parts["flags"][i]) & 1) == 0)   # the first movable part
+    moved = s.parts.copy()
+    moved["xf_prev"][q] = moved["xf"][q]
+    moved["xf"][q][3] += 0.08
+    moved["xf"][q][7] += 0.05
+    rest = moved.copy()
+    rest["xf_prev"][q] = rest["xf"][q]
+    _run(s, tree, s.probes, frames=4, moves={1: (moved, 1 << q), 2: (rest, 0)})
 
 
 def test_bounce_hill_lite_asset():
