@@ -2,7 +2,8 @@
 // 1066-1082; environment.wgsl:311-359, 353-359), for the Gaussians g % 4 == frame % 4 (stage 2: a quarter a frame):
 // shade_emitters toward the 14 fixed directions DIRS14 (the light cut, M39 transfer, ASG off), each direction's colour
 // alb acc_k T iso_norm weighted by footprint x V toward it, then the distant lights' catch alb sum_k I_k T_k V A
-// iso_norm for non-emissive Gaussians.  A shiny Gaussian evaluates its specular lobe 14 times per light, so this
+// iso_norm for non-emissive Gaussians.  The quarter is taken in the shading pass's Morton order, so a warp's Gaussians
+// share their light cuts.  A shiny Gaussian evaluates its specular lobe 14 times per light, so this
 // translation unit is compiled for speed (fused multiply-add, approximate division and square root, hardware
 // transcendentals), as the shading pass is: its output is continuous in its inputs and checked to a tolerance; the
 // per-light parts of the lobe (the SGGX projected area along the light, the lobe's scale) are taken once per light.
@@ -39,9 +40,11 @@ __global__ void __launch_bounds__(kThreads, 4) direct_kernel(const __grid_consta
                                                              const float* __restrict__ tree,
                                                              const float* __restrict__ lamp_T,
                                                              const float4* __restrict__ env_T,
+                                                             const uint32_t* __restrict__ quarter, uint32_t count,
                                                              float4* __restrict__ lo_dir) {
-  const uint32_t g = (blockIdx.x * kThreads + threadIdx.x) * 4u + B.frame % 4u;
-  if (g >= B.G) return;
+  const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= count) return;
+  const uint32_t g = quarter[i];
   const sl_gaussian& G = gs[g];
   const Leaf nd = load_leaf(&nodes[g]);
   uint32_t mi = G.flags & 0xFFFFu;
@@ -157,10 +160,11 @@ __global__ void __launch_bounds__(kThreads, 4) direct_kernel(const __grid_consta
 }  // namespace
 
 cudaError_t launch_bounce_direct(const BounceParams& B, const ShadeParams& SH, const BounceBuffers& D, cudaStream_t s) {
-  const uint64_t quarter = (B.G + 3u) / 4u;
-  if (quarter == 0) return cudaSuccess;
-  direct_kernel<<<(uint32_t)((quarter + kThreads - 1) / kThreads), kThreads, 0, s>>>(
-      B, SH, D.gs, D.nodes, D.vgrid, D.parts, D.mats, D.tree, D.lamp_T, D.env_T, D.lo_dir);
+  const uint32_t q = B.frame % 4u, count = D.quarter_off[q + 1] - D.quarter_off[q];
+  if (count == 0) return cudaSuccess;
+  direct_kernel<<<(count + kThreads - 1) / kThreads, kThreads, 0, s>>>(B, SH, D.gs, D.nodes, D.vgrid, D.parts, D.mats,
+                                                                      D.tree, D.lamp_T, D.env_T,
+                                                                      D.quarters + D.quarter_off[q], count, D.lo_dir);
   return cudaGetLastError();
 }
 

@@ -534,7 +534,7 @@ int sl_lighting_destroy(sl_lighting* l) {
                        &l->lm_acc, &l->lm_mip, &l->sm_acc, &l->sm_mip, &l->sm_layers, &l->sm_dirty, &l->order,
                        &l->g_blur, &l->n_blur, &l->tree_nodes, &l->node_parent, &l->kids, &l->bn_tab,
                        &l->bn_ground, &l->bn_up, &l->probe_data, &l->probe_sh, &l->xfer, &l->lo_dir, &l->lo_b,
-                       &l->node_acc, &l->node_sh};
+                       &l->node_acc, &l->node_sh, &l->bn_quarters};
   for (sl::DevBuf* b : all) b->release();
   delete l;
   return SL_OK;
@@ -956,6 +956,8 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
     D.tab = l->bn_tab.as<float>();
     D.ground = l->bn_ground.as<float>();
     D.up_list = l->bn_up.as<uint32_t>();
+    D.quarters = l->bn_quarters.as<uint32_t>();
+    for (int q = 0; q < 5; q++) D.quarter_off[q] = l->bn_quarter_off[q];
     D.xfer = l->xfer.as<float4>();
     D.lo_dir = l->lo_dir.as<float4>();
     D.lo_b = l->lo_b.as<float4>();
@@ -1074,6 +1076,21 @@ int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* lay, uint32_t 
     l->bn_level_off[d] = (uint32_t)up.size();
     l->bn_level_cnt[d] = (uint32_t)by[d].size();
     up.insert(up.end(), by[d].begin(), by[d].end());
+  }
+  // direct_dirs_emit's quarters (g % 4 == frame % 4), each in the shading pass's Morton order so a warp's Gaussians
+  // share their light cuts
+  {
+    std::vector<uint32_t> order(G), q4;
+    q4.reserve(G);
+    SL_CHECK_CUDA(cudaMemcpy(order.data(), l->order.ptr, 4ull * G, cudaMemcpyDeviceToHost), "shading order");
+    for (uint32_t q = 0; q < 4; q++) {
+      l->bn_quarter_off[q] = (uint32_t)q4.size();
+      for (uint32_t g : order)
+        if (g % 4u == q) q4.push_back(g);
+    }
+    l->bn_quarter_off[4] = (uint32_t)q4.size();
+    SL_CHECK_CUDA(l->bn_quarters.ensure(4ull * G + 16), "quarters");
+    if (G) SL_CHECK_CUDA(cudaMemcpy(l->bn_quarters.ptr, q4.data(), 4ull * G, cudaMemcpyHostToDevice), "quarters");
   }
   float tab[kTabFloats];
   iso_dirs(tab + kTabCells);

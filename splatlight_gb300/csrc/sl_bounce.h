@@ -42,6 +42,8 @@ struct BounceBuffers {
   const float* tab;
   const float* ground;    // dims[0] x dims[1] ground heights, or null
   const uint32_t* up_list;  // internal nodes grouped by depth
+  const uint32_t* quarters; // the Gaussians g with g % 4 == q, for q = 0..3 in turn, each in the shading (Morton) order
+  uint32_t quarter_off[5];  // quarter q is quarters[quarter_off[q] .. quarter_off[q + 1])
   float4 *xfer, *lo_dir, *lo_b, *node_acc, *probe_data, *probe_sh;
   uint32_t* node_sh;
 };
