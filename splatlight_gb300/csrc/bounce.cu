@@ -327,7 +327,8 @@ __global__ void __launch_bounds__(kThreads) xfer_kernel(const __grid_constant__ 
                                                         const sl_node* __restrict__ nodes,
                                                         const sl_vgrid* __restrict__ vgrid,
                                                         const sl_part* __restrict__ parts,
-                                                        const float* __restrict__ tab, float4* __restrict__ xfer) {
+                                                        const float* __restrict__ tab, float4* __restrict__ xfer,
+                                                        float* __restrict__ leaf_w) {
   const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
   if (g >= B.G) return;
   const sl_gaussian& G = gs[g];
@@ -363,32 +364,29 @@ __global__ void __launch_bounds__(kThreads) xfer_kernel(const __grid_constant__ 
   xfer[3u * g] = make_float4(t[0], t[1], t[2], t[3]);
   xfer[3u * g + 1u] = make_float4(t[4], t[5], t[6], t[7]);
   xfer[3u * g + 2u] = make_float4(t[8], 0.0f, 0.0f, 0.0f);
+  // node_leaf's weights toward D14, footprint x V: like the transfer they change only when the part turns
+  for (int k = 0; k < 14; k++) {
+    const f3 wo = xf_dir_inv(xf, ld3(tab + kTabD14 + 3 * k));
+    leaf_w[14u * g + (uint32_t)k] = footprint(nd, s3 * s3, wo) * vgrid_lookup(vg, wo);
+  }
 }
 
 // node_leaf: per leaf and direction (L w, w), L its light toward the probes plus last frame's bounce
 __global__ void __launch_bounds__(kThreads) leaf_kernel(const __grid_constant__ BounceParams B,
                                                         const sl_gaussian* __restrict__ gs,
-                                                        const sl_node* __restrict__ nodes,
-                                                        const sl_vgrid* __restrict__ vgrid,
-                                                        const sl_part* __restrict__ parts,
-                                                        const float* __restrict__ tab,
+                                                        const float* __restrict__ leaf_w,
                                                         const float4* __restrict__ lo_dir,
                                                         const float4* __restrict__ lo_b, float4* __restrict__ acc) {
   const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
   if (g >= B.G) return;
   const sl_gaussian& G = gs[g];
-  const Leaf nd = load_leaf(&nodes[g]);
-  const float* xf = parts[G.part_surface & 0xFFFFu].xf;
-  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
   const float4 ld = lo_dir[g], lb = lo_b[3u * g + 1u];
   // the emitters' own part sends nothing into the probes (PP.refl.w, emitBounceFix: their light reaches the scene as
   // direct light; the weights stay, so they still occlude)
   const bool dark = (G.part_surface & 0xFFFFu) == B.dark_part;
   const f3 L = dark ? F3(0.0f, 0.0f, 0.0f) : add3(F3(ld.x, ld.y, ld.z), F3(lb.x, lb.y, lb.z));
-  const sl_vgrid& vg = vgrid[g];
   for (int k = 0; k < 14; k++) {
-    const f3 wo = xf_dir_inv(xf, ld3(tab + kTabD14 + 3 * k));
-    const float w = footprint(nd, s3 * s3, wo) * vgrid_lookup(vg, wo);
+    const float w = leaf_w[14u * g + (uint32_t)k];
     acc[14u * g + (uint32_t)k] = make_float4(L.x * w, L.y * w, L.z * w, w);
   }
 }
@@ -752,11 +750,11 @@ cudaError_t launch_bounce_frame(const BounceParams& B, const ShadeParams& SH, co
   if (B.G == 0) return cudaSuccess;
   // iso_xfer only where something may have changed a transfer: a forced refresh or a part that moved (lighting.js
   // :1036-1039 skips the dispatch otherwise)
-  if (B.force || B.moved_mask) xfer_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.tab, D.xfer);
+  if (B.force || B.moved_mask)
+    xfer_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.tab, D.xfer, D.leaf_w);
   cudaError_t e = launch_bounce_direct(B, SH, D, s);
   if (e != cudaSuccess) return e;
-  leaf_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.tab, D.lo_dir, D.lo_b,
-                                               D.node_acc);
+  leaf_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.leaf_w, D.lo_dir, D.lo_b, D.node_acc);
   for (int d = (int)level_cnt.size() - 1; d >= 1; d--) {
     const uint32_t n = level_cnt[(size_t)d];
     if (n == 0) continue;

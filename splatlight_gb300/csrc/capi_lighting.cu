@@ -534,7 +534,7 @@ int sl_lighting_destroy(sl_lighting* l) {
                        &l->lm_acc, &l->lm_mip, &l->sm_acc, &l->sm_mip, &l->sm_layers, &l->sm_dirty, &l->order,
                        &l->g_blur, &l->n_blur, &l->tree_nodes, &l->node_parent, &l->kids, &l->bn_tab,
                        &l->bn_ground, &l->bn_up, &l->probe_data, &l->probe_sh, &l->xfer, &l->lo_dir, &l->lo_b,
-                       &l->node_acc, &l->node_sh, &l->bn_quarters};
+                       &l->node_acc, &l->node_sh, &l->bn_quarters, &l->bn_leaf_w};
   for (sl::DevBuf* b : all) b->release();
   delete l;
   return SL_OK;
@@ -957,6 +957,7 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
     D.ground = l->bn_ground.as<float>();
     D.up_list = l->bn_up.as<uint32_t>();
     D.quarters = l->bn_quarters.as<uint32_t>();
+    D.leaf_w = l->bn_leaf_w.as<float>();
     for (int q = 0; q < 5; q++) D.quarter_off[q] = l->bn_quarter_off[q];
     D.xfer = l->xfer.as<float4>();
     D.lo_dir = l->lo_dir.as<float4>();
@@ -1107,7 +1108,8 @@ int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* lay, uint32_t 
     sl::DevBuf* b;
     size_t bytes;
   } bufs[] = {{&l->probe_data, 32ull * NP * 128}, {&l->probe_sh, 144ull * NP}, {&l->xfer, 48ull * G},
-              {&l->lo_dir, 16ull * G}, {&l->lo_b, 48ull * G}, {&l->node_acc, 224ull * N}, {&l->node_sh, 56ull * N}};
+              {&l->lo_dir, 16ull * G}, {&l->lo_b, 48ull * G}, {&l->node_acc, 224ull * N}, {&l->node_sh, 56ull * N},
+              {&l->bn_leaf_w, 56ull * G}};
   for (const Sz& z : bufs) {
     SL_CHECK_CUDA(z.b->ensure(z.bytes), "bounce buffers");
     SL_CHECK_CUDA(cudaMemset(z.b->ptr, 0, z.bytes), "bounce buffers");

@@ -147,7 +147,8 @@ struct sl_lighting {
   std::vector<uint32_t> bn_level_off, bn_level_cnt;
   float sky[48] = {};
   bool has_sky = false;
-  sl::DevBuf bn_tab, bn_ground, bn_up, probe_data, probe_sh, xfer, lo_dir, lo_b, node_acc, node_sh, bn_quarters;
+  sl::DevBuf bn_tab, bn_ground, bn_up, probe_data, probe_sh, xfer, lo_dir, lo_b, node_acc, node_sh, bn_quarters,
+      bn_leaf_w;
   uint32_t bn_quarter_off[5] = {};
 };
 
