@@ -304,11 +304,12 @@ typedef struct sl_probe_layout {
  * (palette[3].x).  After the lattice come 8 probes per part (part_probe_frame's cube, riding with the part; those of
  * movable parts gather, skipping their own part, and serve that part's Gaussians), then the static volumes' grids
  * (serving their part's Gaussians).  blend: the history weight of each gather after the first (1: taken as is, the
- * reference's default; 0.5: ?probeblend=ema).  Needs sl_lighting_set_tree and the renderer's parts (their count is
- * fixed from here on).  emitters_dark (the reference's emitBounceFix, on by default there): the Gaussians of the
- * emitters' own part (sl_lighting_set_emitters' skip_part) send nothing into the probes -- their light reaches the
- * scene as direct light -- though they still occlude.  Not built: bounce_dirs (near-mirror materials, flake lobe below 0.1 rad, take no bounce),
- * near-field visibility and reflection (off by default in the reference). */
+ * reference's default; 0.5: ?probeblend=ema; -1: ?probeblend=fir, the gather and the two before it tapered 0.5, 0.3,
+ * 0.2).  Needs sl_lighting_set_tree and the renderer's parts (their count is fixed from here on).  emitters_dark (the
+ * reference's emitBounceFix, on by default there): the Gaussians of the emitters' own part (sl_lighting_set_emitters'
+ * skip_part) send nothing into the probes -- their light reaches the scene as direct light -- though they still
+ * occlude.  Not built: bounce_dirs (near-mirror materials, flake lobe below 0.1 rad, take no bounce), near-field
+ * visibility and reflection (off by default in the reference). */
 SL_API int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* layout, uint32_t max_depth, float blend,
                                   int emitters_dark);
 /* The environment's sky for the probes (src/environment.js:116-124; bounce.wgsl sky_radiance :148-160): n_coef (<= 16)

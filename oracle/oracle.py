@@ -488,7 +488,8 @@ class BounceIn(C.Structure):
 
 
 class BounceState(C.Structure):
-    _fields_ = [(n, C.c_void_p) for n in ("probe_data", "probe_sh", "xfer", "lo_dir", "lo_b", "node_acc", "node_sh")]
+    _fields_ = [(n, C.c_void_p) for n in ("probe_data", "probe_sh", "xfer", "lo_dir", "lo_b", "node_acc", "node_sh",
+                                          "probe_hist")]
 
 
 def bounce_tables():
@@ -554,7 +555,7 @@ class Bounce:
         self.state = {"probe_data": np.zeros((NP, 128, 8), np.float32), "probe_sh": np.zeros((NP, 9, 4), np.float32),
                       "xfer": np.zeros((G, 12), np.float32), "lo_dir": np.zeros((G, 4), np.float32),
                       "lo_b": np.zeros((G, 3, 4), np.float32), "node_acc": np.zeros((N, 14, 4), np.float32),
-                      "node_sh": np.zeros((N, 14), np.uint32)}
+                      "node_sh": np.zeros((N, 14), np.uint32), "probe_hist": np.zeros((NP, 128, 16), np.float32)}
         self.frame = 0
         self.first = True
 

@@ -2246,6 +2246,20 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
     float a = in->alpha;
     float* r0 = st->probe_data + 8u * id;
     float* r1 = r0 + 4;
+    float* h = st->probe_hist + 16u * id; /* g1a, g1b, g2a, g2b */
+    if (a < 0.0f) { /* FIR_TAPS (bounce.wgsl:1253, :1379-1393) */
+      r0[0] = 0.5f * acc.x + 0.3f * h[0] + 0.2f * h[8];
+      r0[1] = 0.5f * acc.y + 0.3f * h[1] + 0.2f * h[9];
+      r0[2] = 0.5f * acc.z + 0.3f * h[2] + 0.2f * h[10];
+      r0[3] = first_part;
+      r1[0] = 0.5f * m1 + 0.3f * h[3] + 0.2f * h[11];
+      r1[1] = 0.5f * m2 + 0.3f * h[4] + 0.2f * h[12];
+      r1[3] = nearv;
+      for (int q = 0; q < 8; q++) h[8 + q] = h[q];
+      h[0] = acc.x; h[1] = acc.y; h[2] = acc.z; h[3] = m1;
+      h[4] = m2; h[5] = h[6] = h[7] = 0.0f;
+      continue;
+    }
     r0[0] = mixf(r0[0], acc.x, a);
     r0[1] = mixf(r0[1], acc.y, a);
     r0[2] = mixf(r0[2], acc.z, a);
@@ -2253,6 +2267,10 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
     r1[0] = mixf(r1[0], m1, a);
     r1[1] = mixf(r1[1], m2, a);
     r1[3] = nearv;
+    if (a >= 1.0f) {
+      h[0] = h[8] = acc.x; h[1] = h[9] = acc.y; h[2] = h[10] = acc.z; h[3] = h[11] = m1;
+      h[4] = h[12] = m2; h[5] = h[6] = h[7] = h[13] = h[14] = h[15] = 0.0f;
+    }
   }
   /* probe_valid */
   for (uint32_t p = 0; p < NP; p++) {

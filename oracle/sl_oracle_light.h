@@ -121,6 +121,7 @@ typedef struct orc_bounce_state {
   float* lo_b;       /* G x 12 */
   float* node_acc;   /* N x 14 x 4 */
   uint32_t* node_sh; /* N x 14 */
+  float* probe_hist; /* NP x 128 x 16: the last two gathers per ray, (rgb, m1), (m2, 0, 0, 0) each */
 } orc_bounce_state;
 
 

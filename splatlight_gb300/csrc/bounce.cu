@@ -464,7 +464,7 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(const __grid_constant_
                                                           const float* __restrict__ tab,
                                                           const float* __restrict__ ground,
                                                           const uint32_t* __restrict__ node_sh,
-                                                          float4* __restrict__ pd) {
+                                                          float4* __restrict__ pd, float4* __restrict__ hist) {
   const uint32_t id = blockIdx.x * kThreads + threadIdx.x;
   if (id >= B.NP * kCells) return;
   const uint32_t p = id / kCells, c = id % kCells;  // one probe per block; a warp takes two elevation rows of cells
@@ -606,10 +606,29 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(const __grid_constant_
   if (B.has_sky && t1 >= B.tmax * 0.999f) acc = add3(acc, mul3(sky_radiance(B.sky, w), T));
   m1 += T * t1;
   m2 += T * t1 * t1;
+  // the history blend: an EMA of weight alpha (1: the gather as is), or alpha < 0 the tapered blend of this gather and
+  // the two before it (FIR_TAPS 0.5, 0.3, 0.2: ?probeblend=fir); a gather with alpha >= 1 fills both history entries
   const float a = B.alpha;
   const float4 old0 = pd[2u * id], old1 = pd[2u * id + 1u];
+  float4* hp = hist + 4u * id;
+  if (a < 0.0f) {
+    const float4 g1a = hp[0], g1b = hp[1], g2a = hp[2], g2b = hp[3];
+    pd[2u * id] = make_float4(0.5f * acc.x + 0.3f * g1a.x + 0.2f * g2a.x, 0.5f * acc.y + 0.3f * g1a.y + 0.2f * g2a.y,
+                              0.5f * acc.z + 0.3f * g1a.z + 0.2f * g2a.z, first_part);
+    pd[2u * id + 1u] = make_float4(0.5f * m1 + 0.3f * g1a.w + 0.2f * g2a.w, 0.5f * m2 + 0.3f * g1b.x + 0.2f * g2b.x,
+                                   old1.z, nearv);
+    hp[2] = g1a;
+    hp[3] = g1b;
+    hp[0] = make_float4(acc.x, acc.y, acc.z, m1);
+    hp[1] = make_float4(m2, 0.0f, 0.0f, 0.0f);
+    return;
+  }
   pd[2u * id] = make_float4(mixf(old0.x, acc.x, a), mixf(old0.y, acc.y, a), mixf(old0.z, acc.z, a), first_part);
   pd[2u * id + 1u] = make_float4(mixf(old1.x, m1, a), mixf(old1.y, m2, a), old1.z, nearv);
+  if (a >= 1.0f) {
+    hp[0] = hp[2] = make_float4(acc.x, acc.y, acc.z, m1);
+    hp[1] = hp[3] = make_float4(m2, 0.0f, 0.0f, 0.0f);
+  }
 }
 
 // probe_valid: one probe per thread
@@ -764,7 +783,8 @@ cudaError_t launch_bounce_frame(const BounceParams& B, const ShadeParams& SH, co
   sh2_kernel<<<blocks(B.N), kThreads, 0, s>>>(B.N, D.tab, D.node_acc, D.node_sh);
   if (B.NP) {
     gather_kernel<<<blocks((uint64_t)B.NP * kCells), kThreads, 0, s>>>(B, D.tnodes, D.kids, D.vgrid, D.parts, D.tab,
-                                                                       D.ground, D.node_sh, D.probe_data);
+                                                                       D.ground, D.node_sh, D.probe_data,
+                                                                       D.probe_hist);
     valid_kernel<<<blocks(B.NP), kThreads, 0, s>>>(B, D.parts, D.probe_data);
     psh2_kernel<<<blocks(B.NP), kThreads, 0, s>>>(B, D.tab, D.probe_data, D.probe_sh);
   }

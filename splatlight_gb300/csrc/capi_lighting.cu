@@ -534,7 +534,7 @@ int sl_lighting_destroy(sl_lighting* l) {
                        &l->lm_acc, &l->lm_mip, &l->sm_acc, &l->sm_mip, &l->sm_layers, &l->sm_dirty, &l->order,
                        &l->g_blur, &l->n_blur, &l->tree_nodes, &l->node_parent, &l->kids, &l->bn_tab,
                        &l->bn_ground, &l->bn_up, &l->probe_data, &l->probe_sh, &l->xfer, &l->lo_dir, &l->lo_b,
-                       &l->node_acc, &l->node_sh, &l->bn_quarters, &l->bn_leaf_w};
+                       &l->node_acc, &l->node_sh, &l->bn_quarters, &l->bn_leaf_w, &l->probe_hist};
   for (sl::DevBuf* b : all) b->release();
   delete l;
   return SL_OK;
@@ -958,6 +958,7 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
     D.up_list = l->bn_up.as<uint32_t>();
     D.quarters = l->bn_quarters.as<uint32_t>();
     D.leaf_w = l->bn_leaf_w.as<float>();
+    D.probe_hist = l->probe_hist.as<float4>();
     for (int q = 0; q < 5; q++) D.quarter_off[q] = l->bn_quarter_off[q];
     D.xfer = l->xfer.as<float4>();
     D.lo_dir = l->lo_dir.as<float4>();
@@ -1021,7 +1022,8 @@ int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* lay, uint32_t 
     return fail(SL_ERR_INVALID_ARG, "probe layout: positive spacing and ray length");
   for (uint32_t k = 0; k + 1 < dz; k++)
     if (!(lay->levels[k + 1] > lay->levels[k])) return fail(SL_ERR_INVALID_ARG, "probe levels must ascend");
-  if (!(blend > 0.0f && blend <= 1.0f)) return fail(SL_ERR_INVALID_ARG, "blend must be in (0, 1]");
+  if (!((blend > 0.0f && blend <= 1.0f) || blend == -1.0f))
+    return fail(SL_ERR_INVALID_ARG, "blend must be in (0, 1], or -1 (the FIR blend)");
   if (lay->n_vols > 32) return fail(SL_ERR_INVALID_ARG, "at most 32 probe volumes");
   cudaSetDevice(l->device);
   const uint32_t G = l->count, N = l->n_tree, NL = dx * dy * dz, P = l->r->part_count;
@@ -1109,7 +1111,7 @@ int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* lay, uint32_t 
     size_t bytes;
   } bufs[] = {{&l->probe_data, 32ull * NP * 128}, {&l->probe_sh, 144ull * NP}, {&l->xfer, 48ull * G},
               {&l->lo_dir, 16ull * G}, {&l->lo_b, 48ull * G}, {&l->node_acc, 224ull * N}, {&l->node_sh, 56ull * N},
-              {&l->bn_leaf_w, 56ull * G}};
+              {&l->bn_leaf_w, 56ull * G}, {&l->probe_hist, 64ull * NP * 128}};
   for (const Sz& z : bufs) {
     SL_CHECK_CUDA(z.b->ensure(z.bytes), "bounce buffers");
     SL_CHECK_CUDA(cudaMemset(z.b->ptr, 0, z.bytes), "bounce buffers");

@@ -45,6 +45,7 @@ struct BounceBuffers {
   const uint32_t* quarters; // the Gaussians g with g % 4 == q, for q = 0..3 in turn, each in the shading (Morton) order
   uint32_t quarter_off[5];  // quarter q is quarters[quarter_off[q] .. quarter_off[q + 1])
   float4 *xfer, *lo_dir, *lo_b, *node_acc, *probe_data, *probe_sh;
+  float4* probe_hist;  // per ray the last two gathers, (rgb, m1), (m2): the FIR blend's history
   float* leaf_w;  // per Gaussian node_leaf's 14 weights (footprint x V toward D14), refreshed with the transfer
   uint32_t* node_sh;
 };

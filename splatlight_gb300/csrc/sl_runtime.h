@@ -148,7 +148,7 @@ struct sl_lighting {
   float sky[48] = {};
   bool has_sky = false;
   sl::DevBuf bn_tab, bn_ground, bn_up, probe_data, probe_sh, xfer, lo_dir, lo_b, node_acc, node_sh, bn_quarters,
-      bn_leaf_w;
+      bn_leaf_w, probe_hist;
   uint32_t bn_quarter_off[5] = {};
 };
 

@@ -86,7 +86,8 @@ class Lighting:
     def set_probes(self, layout: dict, max_depth: int = 0, blend: float = 1.0, emitters_dark: bool = True) -> None:
         """The probe bounce over a lattice (probes.room_layout / probes.terrain_layout); needs set_tree.  From the
         next update on, each update runs one bounce frame and the renderer adds gain x lo_b to the lit colour.
-        emitters_dark: the emitters' own part sends nothing into the probes (the reference's emitBounceFix)."""
+        emitters_dark: the emitters' own part sends nothing into the probes (the reference's emitBounceFix).
+        blend: each gather's history weight after the first (1 as is; -1 the FIR blend of the last three)."""
         lay = N.ProbeLayout()
         lay.dims[:] = [int(v) for v in layout["dims"]]
         lay.terrain = 1 if layout["terrain"] else 0

@@ -46,7 +46,7 @@ def _close(name, a, b, rtol=RTOL, atol=ATOL, frac=0.0, scaled=False):
     assert n <= frac * a.size, f"{name}: {n} of {a.size} differ (max abs {worst:.3e})"
 
 
-def _run(s, tree, layout, frames=FRAMES, gain=1.0, moves=None):
+def _run(s, tree, layout, frames=FRAMES, gain=1.0, moves=None, blend=1.0):
     """frames bounce frames on GPU and restatement side by side; moves: {frame: (parts, moved_mask)} written before
     that frame's update (the maps re-splat; both sides take the GPU's transmittance of that frame)."""
     import torch
@@ -55,7 +55,7 @@ def _run(s, tree, layout, frames=FRAMES, gain=1.0, moves=None):
     L = for_scene(r, s)
     L.set_tree(*tree)
     L.set_sky(s.sky_sh)
-    L.set_probes(layout)
+    L.set_probes(layout, blend=blend)
     fwd = camera_forward(s)
     b = None
     for f in range(frames):
@@ -67,7 +67,7 @@ def _run(s, tree, layout, frames=FRAMES, gain=1.0, moves=None):
         torch.cuda.synchronize()
         col, lamp_t, env_t, nodes = L.read()
         if b is None:
-            b = O.Bounce(s, tree, (col, lamp_t, env_t, nodes), layout, sky_sh=s.sky_sh)
+            b = O.Bounce(s, tree, (col, lamp_t, env_t, nodes), layout, sky_sh=s.sky_sh, blend=blend)
         if moves and f in moves:
             b.scene = dataclasses.replace(b.scene, parts=moves[f][0])
         b.lamp_T = np.ascontiguousarray(lamp_t, np.float32)
@@ -104,6 +104,16 @@ def test_bounce_hill_terrain_sky():
     _, _, st = _run(s, tree, PR.for_scene(s))
     # the sky reaches the ground through the probes: a positive bounce on most Gaussians
     assert (st["lo_b"][:, 0, :3].sum(axis=1) > 0).mean() > 0.9
+
+
+@pytest.mark.parametrize("blend", [0.5, -1.0])
+def test_bounce_history_blends(blend):
+    """The probes' history blends after the first gather: the EMA (?probeblend=ema, weight 0.5) and the tapered blend
+    of the last three gathers (?probeblend=fir)."""
+    s = _bounce_lit(S.hill(20000, seed=6, width=160, height=120, n_emit=4))
+    s = dataclasses.replace(s, shadow_res=128, sun_res=128)
+    s, tree = S.with_tree(s)
+    _run(s, tree, PR.for_scene(s), frames=4, blend=blend)
 
 
 def test_bounce_cornell_room():
