@@ -308,8 +308,9 @@ typedef struct sl_probe_layout {
  * 0.2).  Needs sl_lighting_set_tree and the renderer's parts (their count is fixed from here on).  emitters_dark (the
  * reference's emitBounceFix, on by default there): the Gaussians of the emitters' own part (sl_lighting_set_emitters'
  * skip_part) send nothing into the probes -- their light reaches the scene as direct light -- though they still
- * occlude.  Not built: bounce_dirs (near-mirror materials, flake lobe below 0.1 rad, take no bounce), near-field
- * visibility and reflection (off by default in the reference). */
+ * occlude.  Near-mirror materials (a flake lobe below 0.1 rad) take bounce_dirs' per-cell path, with the cells near
+ * the eye's mirror direction as lights with a size when ASG highlights are on (sl_lighting_set_options).  Not built:
+ * near-field visibility and reflection (off by default in the reference). */
 SL_API int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* layout, uint32_t max_depth, float blend,
                                   int emitters_dark);
 /* The environment's sky for the probes (src/environment.js:116-124; bounce.wgsl sky_radiance :148-160): n_coef (<= 16)

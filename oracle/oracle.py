@@ -484,7 +484,7 @@ class BounceIn(C.Structure):
                 ("normal", C.c_float * 3), ("lamp_T", C.c_void_p), ("env_T", C.c_void_p), ("lights", C.c_void_p),
                 ("n_lights", C.c_uint32), ("sky_sh", C.c_void_p), ("lay", ProbeLayoutC), ("max_depth", C.c_uint32),
                 ("eye", C.c_float * 3), ("alpha", C.c_float), ("frame", C.c_uint32), ("force", C.c_uint32),
-                ("moved_mask", C.c_uint32), ("dark_part", C.c_uint32)]
+                ("moved_mask", C.c_uint32), ("dark_part", C.c_uint32), ("asg_cells", C.c_uint32)]
 
 
 class BounceState(C.Structure):
@@ -518,7 +518,7 @@ class Bounce:
     layout: a probes.* layout dict; sky_sh: (16, 3) or None."""
 
     def __init__(self, scene, tree, lit, layout, sky_sh=None, max_depth: int = 0, blend: float = 1.0,
-                 emitters_dark: bool = True):
+                 emitters_dark: bool = True, asg: bool = True):
         self.scene = scene
         G = scene.count
         tn = np.ascontiguousarray(tree[0]).copy()
@@ -530,6 +530,7 @@ class Bounce:
             max_depth = int(tn["depth"][G:].max()) + 1 if len(tn) > G else 1
         self.max_depth = max_depth
         self.blend = blend
+        self.asg = asg
         self.dark_part = int(getattr(scene, "emit_skip_part", 0xFFFFFFFF)) if emitters_dark else 0xFFFFFFFF
         self.lamp_T = np.ascontiguousarray(lit[1], np.float32)
         self.env_T = np.ascontiguousarray(lit[2], np.float32)
@@ -604,6 +605,7 @@ class Bounce:
         B.force = 1 if self.first else 0
         B.moved_mask = moved_mask
         B.dark_part = self.dark_part
+        B.asg_cells = 1 if self.asg else 0
         st = BounceState(**{k: v.ctypes.data for k, v in self.state.items()})
         rc = L.orc_bounce_frame(C.byref(B), C.byref(st), threads)
         if rc != 0:

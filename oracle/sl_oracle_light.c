@@ -2003,14 +2003,110 @@ static void bn_direct_one(const orc_bounce_in* in, uint32_t g, float* lo_dir) {
   lo_dir[4u * g + 3] = 0.0f;
 }
 
+/* the cells as lights (cell_asg_phase, bounce.wgsl:180-191): per cell the elevation and azimuth tangents and the
+ * angular variances of a Gaussian CELL_STD of the cell across, float64 then rounded: 8 floats per cell */
+static void bn_cell_asg_table(float* t) {
+  const double CELL_STD = 0.4;
+  for (int c = 0; c < 128; c++) {
+    int i = c / 16, j = c % 16;
+    double el = 0.5 * M_PI - (i + 0.5) * M_PI / 8.0, az = -M_PI + (j + 0.5) * 2.0 * M_PI / 16.0;
+    double s_el = CELL_STD * M_PI / 8.0, s_az = CELL_STD * 2.0 * M_PI / 16.0 * fmax(cos(el), 0.05);
+    float* o = t + 8 * c;
+    o[0] = (float)(-sin(el) * cos(az));
+    o[1] = (float)(-sin(el) * sin(az));
+    o[2] = (float)cos(el);
+    o[3] = (float)(-sin(az));
+    o[4] = (float)cos(az);
+    o[5] = 0.0f;
+    o[6] = (float)(s_el * s_el);
+    o[7] = (float)(s_az * s_az);
+  }
+}
+
+/* bounce_dirs for a near-mirror Gaussian (bounce.wgsl:887-985, the M39 path): the 8 probes' per-cell radiance through
+ * its transfer (V, footprint, solid angle) and the specular lobe toward D14 and the eye (the cells within about three
+ * lobe widths of the eye's mirror direction as lights with a size when asg_cells) into lo_b */
+static void bn_dirs_one(const orc_bounce_in* in, const bn_probes* PS, const float* cells, const float* casg,
+                        const float* d14, orc_bounce_state* st, uint32_t g) {
+  const sl_gaussian* G = &in->gs[g];
+  const sl_node* nd = &in->nodes[g];
+  const sl_material* mat = &in->mats[mat_index(G, in->mat_count)];
+  uint32_t own = G->part_surface & 0xFFFFu;
+  const float* xf = in->parts[own].xf;
+  f3 P = xf_point(xf, F3(G->mu[0], G->mu[1], G->mu[2]));
+  m3f Rq = quat_matrix(G->quat);
+  m3f Dm = m3_diag(F3(mat->flake[0], mat->flake[1], mat->flake[2]));
+  m3f t0 = m3_mul(&Rq, &Dm);
+  m3f RqT = m3_t(&Rq);
+  m3f Sloc = m3_mul(&t0, &RqT);
+  f3 n = Rq.c[0], t1 = Rq.c[1], t2 = Rq.c[2];
+  f3 Sd = F3(Sloc.c[0].x, Sloc.c[1].y, Sloc.c[2].z), So = F3(Sloc.c[1].x, Sloc.c[2].x, Sloc.c[2].y);
+  f3 flake = F3(mat->flake[0], mat->flake[1], mat->flake[2]);
+  float s3 = G->scale[0] * G->scale[1] * G->scale[2];
+  float detC = s3 * s3;
+  float ks = spec_weight(mat);
+  float inorm = iso_norm(nd);
+  bn_weights pw = bn_weights_for(in, PS, st->probe_data, P, own);
+  float lobe_w = sqrtf(fminf(mat->flake[1], mat->flake[2]) / fmaxf(mat->flake[0], 1e-12f));
+  float near_ang = fminf(3.0f * (0.4f * BN_PI / 8.0f + 2.0f * lobe_w), BN_PI);
+  f3 wo[15];
+  for (int k = 0; k < 14; k++) wo[k] = xf_dir_inv(xf, F3(d14[3 * k], d14[3 * k + 1], d14[3 * k + 2]));
+  wo[14] = xf_dir_inv(xf, norm3(sub3(F3(in->eye[0], in->eye[1], in->eye[2]), P)));
+  f3 acc[15];
+  for (int k = 0; k < 15; k++) acc[k] = F3(0.0f, 0.0f, 0.0f);
+  f3 wr_eye = mirror3(wo[14], n);
+  for (uint32_t c = 0; c < BN_NCELL; c++) {
+    f3 L = F3(0.0f, 0.0f, 0.0f);
+    for (int k = 0; k < 8; k++) {
+      if (pw.w[k] > 0.0f) {
+        const float* r0 = st->probe_data + 8u * (pw.pid[k] * BN_NCELL + c);
+        L = add3(L, mul3(F3(r0[0], r0[1], r0[2]), pw.w[k]));
+      }
+    }
+    if (L.x + L.y + L.z <= 0.0f) continue;
+    f3 u = xf_dir_inv(xf, bn_cell_dir(cells, c));
+    float vis = vgrid_lookup(&in->vgrid[g], u) * 1.0f;
+    if (vis <= 0.0f) continue;
+    f3 lin = mul3(L, vis * footprint(nd, detC, u) * cells[4 * c + 3]);
+    f3 ur = mirror3(u, n);
+    float damp = iso_damp(inorm, footprint(nd, detC, ur) * vgrid_lookup(&in->vgrid[g], ur));
+    for (int k = 0; k < 14; k++) acc[k] = add3(acc[k], mul3(lin, iso_lobe_from(ks, phase_specular(Sd, So, u, wo[k]), damp)));
+    float lobe14;
+    if (in->asg_cells && sl_acosf(clampf(dot3(u, wr_eye), -1.0f, 1.0f)) < near_ang) {
+      const float* e = casg + 8 * c;
+      f3 lb0 = xf_dir_inv(xf, F3(e[0], e[1], e[2])), lb1 = xf_dir_inv(xf, F3(e[3], e[4], e[5]));
+      s2m sl = {e[6], 0.0f, e[7]};
+      lobe14 = iso_lobe_from(ks, asg_phase(u, lb0, lb1, sl, n, t1, t2, flake, Sd, So, wo[14]), damp);
+    } else {
+      lobe14 = iso_lobe_from(ks, phase_specular(Sd, So, u, wo[14]), damp);
+    }
+    acc[14] = add3(acc[14], mul3(lin, lobe14));
+  }
+  f3 send = F3(0.0f, 0.0f, 0.0f);
+  float ws = 0.0f;
+  for (int k = 0; k < 14; k++) {
+    float w = footprint(nd, detC, wo[k]) * vgrid_lookup(&in->vgrid[g], wo[k]);
+    send = add3(send, mul3(acc[k], w));
+    ws += w;
+  }
+  send = div3(send, fmaxf(ws, 1e-20f));
+  f3 sc = mul3(F3(G->albedo[0], G->albedo[1], G->albedo[2]), inorm);
+  f3 eyec = mul3v(sc, acc[14]), sendc = mul3v(sc, send);
+  float* lb = st->lo_b + 12u * g;
+  lb[0] = eyec.x; lb[1] = eyec.y; lb[2] = eyec.z; lb[3] = 0.0f;
+  lb[4] = sendc.x; lb[5] = sendc.y; lb[6] = sendc.z; lb[7] = 0.0f;
+  lb[8] = lb[9] = lb[10] = lb[11] = 0.0f;
+}
+
 int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads) {
   const orc_probe_layout* L = &in->lay;
   const uint32_t G = in->count, N = in->n_nodes;
   const bn_probes PS = bn_probe_set(in);
   const uint32_t NP = PS.n_probes, NL = PS.nl;
-  float cells[4 * 128], d14[42], pinv[126];
+  float cells[4 * 128], d14[42], pinv[126], casg[8 * 128];
   orc_iso_dirs(cells);
   orc_bounce_tables(d14, pinv);
+  bn_cell_asg_table(casg);
   (void)nthreads;
 
   /* iso_xfer: where something moved relative to the Gaussian, or forced */
@@ -2325,7 +2421,10 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
     const sl_material* mat = &in->mats[mat_index(Gs, in->mat_count)];
     float ks = spec_weight(mat);
     float lw = sqrtf(fminf(mat->flake[1], mat->flake[2]) / fmaxf(mat->flake[0], 1e-12f));
-    if (ks > 0.0f && !(lw >= BN_GLOSS_SH_MIN)) continue; /* near-mirror: bounce_dirs (not restated) */
+    if (ks > 0.0f && !(lw >= BN_GLOSS_SH_MIN)) { /* near-mirror: bounce_dirs */
+      bn_dirs_one(in, &PS, cells, casg, d14, st, g);
+      continue;
+    }
     uint32_t own = Gs->part_surface & 0xFFFFu;
     const float* xf = in->parts[own].xf;
     f3 P = xf_point(xf, F3(Gs->mu[0], Gs->mu[1], Gs->mu[2]));

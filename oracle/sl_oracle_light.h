@@ -111,6 +111,8 @@ typedef struct orc_bounce_in {
   uint32_t force;      /* iso_xfer refreshes every Gaussian */
   uint32_t moved_mask; /* parts that moved this frame (the reference's Part flags bit 1) */
   uint32_t dark_part;  /* the part whose Gaussians send nothing into the probes (PP.refl.w - 1; NONE: none) */
+  uint32_t asg_cells;  /* U.iso bit 2 (asgSpec): near-mirror Gaussians see the cells near their mirror direction as
+                          lights with an angular size (cell_asg_phase) */
 } orc_bounce_in;
 
 typedef struct orc_bounce_state {

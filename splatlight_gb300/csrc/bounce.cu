@@ -10,12 +10,15 @@
 //             the hits kept depth-sorted (16, the farthest folded into the last), composited front to back with the
 //             nodes' SH2 radiance, the sky SH beyond; depth moments for the Chebyshev test
 //   valid     probe_valid (:1417-1447); psh2: probe_sh2 (:1029-1041)
-//   bounce    bounce_sh (:1044-1095) with gloss_sh (:1102-1125): the 8 surrounding probes (trilinear x valid x
-//             Chebyshev, with the 4x4x4 fallback) dotted with the Gaussian's transfer into lo_b
+//   dirs      bounce_dirs (:887-985) for near-mirror Gaussians (flake lobe below 0.1 rad): the probes' per-cell
+//             radiance through the Gaussian's transfer and specular lobe, the cells near the eye's mirror direction as
+//             lights with a size (cell_asg_phase)
+//   bounce    bounce_sh (:1044-1095) with gloss_sh (:1102-1125) for the others: the 8 surrounding probes (trilinear x
+//             valid x Chebyshev with the 4x4x4 fallback; a movable part's own 8 probes; a static volume's grid) dotted
+//             with the Gaussian's transfer into lo_b
 // The translation unit is compiled with --fmad=false and the deterministic transcendentals of sl_detmath.h, so the
-// CPU restatement reproduces it given the same light toward the probes (whose kernel is compiled for speed).  Every Gaussian reads the lattice (riding part probes and static probe volumes are
-// not built); near-field visibility is off (the reference's default); near-mirror materials (flake lobe below
-// 0.1 rad), which the reference gives to bounce_dirs, keep a zero bounce.
+// CPU restatement reproduces it given the same light toward the probes (whose kernel is compiled for speed).
+// Near-field visibility is off (the reference's default).
 #include <cuda_fp16.h>
 
 #include "light_math.cuh"
@@ -759,6 +762,96 @@ __global__ void __launch_bounds__(kThreads) bounce_kernel(const __grid_constant_
   lo_b[3u * g + 2u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
+// bounce_dirs (bounce.wgsl:887-985, the M39 path), for near-mirror Gaussians (a specular flake lobe narrower than
+// 0.1 rad, which the probes' SH2 cannot hold): the 8 probes' per-cell radiance through the Gaussian's transfer (V,
+// footprint, solid angle) and its specular lobe toward D14 (their footprint x V weighted mean: toward the probes) and
+// toward the eye (cells within about three lobe widths of the eye's mirror direction as lights with a size:
+// cell_asg_phase) into lo_b; the other Gaussians are bounce_sh's
+__global__ void __launch_bounds__(kThreads) dirs_kernel(const __grid_constant__ BounceParams B,
+                                                        const sl_gaussian* __restrict__ gs,
+                                                        const sl_node* __restrict__ nodes,
+                                                        const sl_vgrid* __restrict__ vgrid,
+                                                        const sl_part* __restrict__ parts,
+                                                        const sl_material* __restrict__ mats,
+                                                        const sl_node* __restrict__ tnodes,
+                                                        const float* __restrict__ tab,
+                                                        const float* __restrict__ ground,
+                                                        const float4* __restrict__ pd, float4* __restrict__ lo_b) {
+  const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
+  if (g >= B.G) return;
+  const sl_gaussian& G = gs[g];
+  const sl_material mat = mats[mat_index(G, B.mat_count)];
+  const float ks = spec_weight(mat);
+  const float lw = sqrtf(fminf(mat.flake[1], mat.flake[2]) / fmaxf(mat.flake[0], 1e-12f));
+  if (!(ks > 0.0f && !(lw >= kGlossShMin))) return;
+  const uint32_t own = G.part_surface & 0xFFFFu;
+  const float* xf = parts[own].xf;
+  const f3 P = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  const Leaf nd = load_leaf(&nodes[g]);
+  const m3 Rq = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]);
+  const m3 Sloc = m3m(m3m(Rq, m3diag(F3(mat.flake[0], mat.flake[1], mat.flake[2]))), m3t(Rq));
+  const f3 n = Rq.c[0];
+  const f3 Sd = F3(Sloc.c[0].x, Sloc.c[1].y, Sloc.c[2].z), So = F3(Sloc.c[1].x, Sloc.c[2].x, Sloc.c[2].y);
+  const f3 flake = F3(mat.flake[0], mat.flake[1], mat.flake[2]);
+  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
+  const float detC = s3 * s3;
+  const sl_vgrid& vg = vgrid[g];
+  const Weights pw = weights_for(B, ground, pd, tnodes, parts, P, own);
+  const float near_ang = fminf(3.0f * (0.4f * kPi / 8.0f + 2.0f * lw), kPi);
+  const f3 wo14 = xf_dir_inv(xf, norm3(sub3(ld3(B.eye), P)));
+  const f3 wr_eye = mirror3(wo14, n);
+  const SpecPre sp = spec_prepare(Sd, So);
+  const AsgPre ap = asg_prepare(n, Rq.c[1], Rq.c[2], flake, Sd, So, wo14);
+  f3 acc[15];
+#pragma unroll
+  for (int k = 0; k < 15; k++) acc[k] = F3(0.0f, 0.0f, 0.0f);
+  for (uint32_t c = 0; c < kCells; c++) {
+    f3 L = F3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (pw.w[k] > 0.0f) {
+        const float4 r0 = pd[2u * (pw.pid[k] * kCells + c)];
+        L = add3(L, mul3(F3(r0.x, r0.y, r0.z), pw.w[k]));
+      }
+    if (L.x + L.y + L.z <= 0.0f) continue;
+    const f3 u = xf_dir_inv(xf, cell_dir(tab, c));
+    const float vis = vgrid_lookup(vg, u) * 1.0f;
+    if (vis <= 0.0f) continue;
+    const f3 lin = mul3(L, vis * footprint(nd, detC, u) * cell_omega(tab, c));
+    const f3 ur = mirror3(u, n);
+    const float damp = iso_damp(nd.iso_norm, footprint(nd, detC, ur) * vgrid_lookup(vg, ur));
+#pragma unroll
+    for (int k = 0; k < 14; k++) {
+      const f3 wo = xf_dir_inv(xf, ld3(tab + kTabD14 + 3 * k));
+      acc[k] = add3(acc[k], mul3(lin, iso_lobe_from(ks, phase_specular_p(sp, u, wo), damp)));
+    }
+    float lobe14;
+    if (B.asg_cells && lm_acos(clampf(dot3(u, wr_eye), -1.0f, 1.0f)) < near_ang) {
+      const float* e = tab + kTabCellAsg + 8u * c;
+      const f3 lb0 = xf_dir_inv(xf, ld3(e)), lb1 = xf_dir_inv(xf, ld3(e + 3));
+      lobe14 = iso_lobe_from(ks, asg_phase_p(ap, sp, u, lb0, lb1, s2m{e[6], 0.0f, e[7]}, wo14), damp);
+    } else {
+      lobe14 = iso_lobe_from(ks, phase_specular_p(sp, u, wo14), damp);
+    }
+    acc[14] = add3(acc[14], mul3(lin, lobe14));
+  }
+  f3 send = F3(0.0f, 0.0f, 0.0f);
+  float ws = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 14; k++) {
+    const f3 wo = xf_dir_inv(xf, ld3(tab + kTabD14 + 3 * k));
+    const float w = footprint(nd, detC, wo) * vgrid_lookup(vg, wo);
+    send = add3(send, mul3(acc[k], w));
+    ws += w;
+  }
+  send = div3(send, fmaxf(ws, 1e-20f));
+  const f3 sc = mul3(F3(G.albedo[0], G.albedo[1], G.albedo[2]), nd.iso_norm);
+  const f3 eyec = mul3v(sc, acc[14]), sendc = mul3v(sc, send);
+  lo_b[3u * g] = make_float4(eyec.x, eyec.y, eyec.z, 0.0f);
+  lo_b[3u * g + 1u] = make_float4(sendc.x, sendc.y, sendc.z, 0.0f);
+  lo_b[3u * g + 2u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
 inline uint32_t blocks(uint64_t n) { return (uint32_t)((n + kThreads - 1) / kThreads); }
 
 }  // namespace
@@ -788,6 +881,8 @@ cudaError_t launch_bounce_frame(const BounceParams& B, const ShadeParams& SH, co
     valid_kernel<<<blocks(B.NP), kThreads, 0, s>>>(B, D.parts, D.probe_data);
     psh2_kernel<<<blocks(B.NP), kThreads, 0, s>>>(B, D.tab, D.probe_data, D.probe_sh);
   }
+  dirs_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.mats, D.tnodes, D.tab, D.ground,
+                                               D.probe_data, D.lo_b);
   bounce_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.mats, D.tnodes, D.ground,
                                                  D.probe_data,
                                                  D.probe_sh, D.xfer, D.lo_b);

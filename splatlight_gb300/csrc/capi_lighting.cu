@@ -336,6 +336,24 @@ void bounce_tables(float* d14, float* pinv) {
     }
 }
 
+void cell_asg_table(float* t) {
+  const double kCellStd = 0.4;
+  for (int c = 0; c < 128; c++) {
+    const int i = c / 16, j = c % 16;
+    const double el = 0.5 * M_PI - (i + 0.5) * M_PI / 8.0, az = -M_PI + (j + 0.5) * 2.0 * M_PI / 16.0;
+    const double s_el = kCellStd * M_PI / 8.0, s_az = kCellStd * 2.0 * M_PI / 16.0 * std::max(std::cos(el), 0.05);
+    float* o = t + 8 * c;
+    o[0] = (float)(-std::sin(el) * std::cos(az));
+    o[1] = (float)(-std::sin(el) * std::sin(az));
+    o[2] = (float)std::cos(el);
+    o[3] = (float)(-std::sin(az));
+    o[4] = (float)std::cos(az);
+    o[5] = 0.0f;
+    o[6] = (float)(s_el * s_el);
+    o[7] = (float)(s_az * s_az);
+  }
+}
+
 // Skip links for a stackless walk of the light cut (the GPU shading pass).  The cut is the walk of a 48-entry stack
 // that pushes (lo, hi) and so pops hi first: node order = preorder with the hi subtree before the lo one.  Per node,
 // word 7 = the node that walk reaches once this node's subtree is done (its skip); word 19 = 1 when the stack would
@@ -938,6 +956,7 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
     B.moved_mask = moved_mask;
     B.has_sky = l->has_sky ? 1u : 0u;
     B.dark_part = l->bn_emit_dark ? l->skip_part : 0xFFFFFFFFu;
+    B.asg_cells = l->asg ? 1u : 0u;
     memcpy(B.sky, l->sky, sizeof(B.sky));
     for (int k = 0; k < 3; k++) B.eye[k] = eye[k];
     ShadeParams SHd;
@@ -1098,6 +1117,7 @@ int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* lay, uint32_t 
   float tab[kTabFloats];
   iso_dirs(tab + kTabCells);
   bounce_tables(tab + kTabD14, tab + kTabPinv);
+  cell_asg_table(tab + kTabCellAsg);
   SL_CHECK_CUDA(l->bn_tab.ensure(sizeof(tab)), "bounce table");
   SL_CHECK_CUDA(cudaMemcpy(l->bn_tab.ptr, tab, sizeof(tab), cudaMemcpyHostToDevice), "bounce table");
   SL_CHECK_CUDA(l->bn_up.ensure(4ull * up.size() + 16), "node_up lists");

@@ -9,11 +9,13 @@ struct sl_lighting;
 
 namespace sl {
 
-// the constant table (one device buffer): 128 cells x (direction, solid angle), D14, the 9 x 14 SH2 fit
+// the constant table (one device buffer): 128 cells x (direction, solid angle), D14, the 9 x 14 SH2 fit, and per cell
+// its elevation and azimuth tangents and angular variances as a light (cell_asg_phase)
 constexpr uint32_t kTabCells = 0;
 constexpr uint32_t kTabD14 = 512;
 constexpr uint32_t kTabPinv = 512 + 42;
-constexpr uint32_t kTabFloats = 512 + 42 + 126;
+constexpr uint32_t kTabCellAsg = 512 + 42 + 126;
+constexpr uint32_t kTabFloats = 512 + 42 + 126 + 1024;
 
 // bounce.wgsl ProbeParams (the fields this path reads) + the frame's inputs
 struct BounceParams {
@@ -24,6 +26,7 @@ struct BounceParams {
   float tmax, brad, alpha;
   uint32_t frame, force, moved_mask, has_sky;
   uint32_t dark_part;  // the part whose Gaussians send nothing into the probes (0xFFFFFFFF: none)
+  uint32_t asg_cells;  // near-mirror Gaussians see the cells near their mirror direction as lights with a size
   float eye[3];
   float sky[48];  // 16 SH coefficients (bands 0-3), rgb
 };
@@ -55,6 +58,8 @@ void shade_params(const sl_lighting* l, const float* eye, ShadeParams& SH);
 void iso_dirs(float* d);
 // D14 and the 9 x 14 least-squares SH2 fit on it (lighting.js:188-209), float64 then rounded.
 void bounce_tables(float* d14, float* pinv);
+// cell_asg_phase's per-cell frame (bounce.wgsl:180-191): e_el, e_az, then s_el^2, s_az^2, 8 floats a cell, float64
+void cell_asg_table(float* t);
 
 // direct_dirs_emit + env_dirs for the Gaussians g % 4 == frame % 4 (bounce_direct.cu) into lo_dir
 cudaError_t launch_bounce_direct(const BounceParams& B, const ShadeParams& SH, const BounceBuffers& D, cudaStream_t s);

@@ -4,9 +4,9 @@ gather (colour, depth moments, first-hit part and near flags), validity and SH2,
 The restatement takes the GPU's own lighting state (iso_norm, lamp and sun transmittance), so the bounce alone is
 compared; those inputs have their own parity tests.  The geometry (first-hit parts, near flags, validity, depth
 moments, transfer) is exact or within a few float32 ulps: both sides run the same float32 arithmetic in the same
-order.  The light toward the probes comes from a kernel compiled for speed (as the shading pass), within 1e-4 of the
-restatement; through the half-precision node SH2 (a flip of one half step is 5e-4 of a coefficient) and the frames'
-feedback, the radiance downstream agrees within 2e-3.
+order.  The light toward the probes comes from a kernel compiled for speed (as the shading pass, and to the same
+1e-3); through the half-precision node SH2 (a flip of one half step is 5e-4 of a coefficient) and the frames'
+feedback, the radiance downstream agrees within 2e-3 (of the largest value, where a value is near zero).
 
 Scenes: the hill-like scene (terrain lattice, its sky), the Cornell-like room (room lattice, no sky), and, when the
 assets are copied, the reference's Cornell room (room layout) and hill_lite (terrain layout, its environment's sky),
@@ -81,8 +81,8 @@ def _run(s, tree, layout, frames=FRAMES, gain=1.0, moves=None, blend=1.0):
         assert np.array_equal(pd[:, 0, 6], opd[:, 0, 6]), f"frame {f}: probe validity differs"
         _close(f"frame {f} probe moments", pd[:, :, 4:6], opd[:, :, 4:6])
         _close(f"frame {f} transfer", gst["xfer"], ost["xfer"])
-        _close(f"frame {f} light toward the probes", gst["lo_dir"], ost["lo_dir"], rtol=1e-4 if f == 0 else RAD_RTOL,
-               atol=RAD_ATOL, scaled=f > 0)
+        _close(f"frame {f} light toward the probes", gst["lo_dir"], ost["lo_dir"], rtol=1e-3 if f == 0 else RAD_RTOL,
+               atol=RAD_ATOL, scaled=True)
         _close(f"frame {f} node sums", gst["node_acc"], ost["node_acc"], rtol=RAD_RTOL, atol=RAD_ATOL, scaled=True)
         gh = gst["node_sh"].view(np.float16).astype(np.float64)
         oh = ost["node_sh"].view(np.float16).astype(np.float64)
@@ -114,6 +114,21 @@ def test_bounce_history_blends(blend):
     s = dataclasses.replace(s, shadow_res=128, sun_res=128)
     s, tree = S.with_tree(s)
     _run(s, tree, PR.for_scene(s), frames=4, blend=blend)
+
+
+def test_bounce_near_mirror_materials():
+    """bounce_dirs: a quarter of the hill's materials made near-mirror (roughness 0.05: a flake lobe below 0.1 rad)
+    take the per-cell path -- the probes' per-cell radiance through their transfer and specular lobe, the cells near
+    the eye's mirror direction as lights with a size -- the rest bounce_sh's."""
+    s = _bounce_lit(S.hill(20000, seed=7, width=160, height=120, n_emit=4))
+    m = s.materials.copy()
+    m["flake"][:8] = (1.0, 0.0025, 0.0025)
+    s = dataclasses.replace(s, shadow_res=128, sun_res=128, materials=m)
+    s, tree = S.with_tree(s)
+    mirror = (s.gaussians["flags"] & 0xFFFF) < 8
+    assert 0.1 < mirror.mean() < 0.5
+    _, _, st = _run(s, tree, PR.for_scene(s), frames=3)
+    assert (st["lo_b"][mirror, 0, :3].sum(axis=1) > 0).mean() > 0.5
 
 
 def test_bounce_cornell_room():
