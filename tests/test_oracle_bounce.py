@@ -100,3 +100,15 @@ def test_open_sky_reaches_the_probes(orc):
     col = up[..., :3][open_rays]
     assert np.all(col <= L * (1 + 1e-5))   # the sky times the ray's transmittance (<= 1)
     assert np.allclose(col.max(axis=0), L, rtol=1e-5)
+
+
+def test_probe_volumes_rule():
+    """probeVolumes (lighting.js:289-314): static non-terrain parts with a bounding radius of 1 m to a quarter of the
+    scene's half-diagonal get a grid of about 1.2 m spacing, 2-6 per axis (Math.round); named volumes win."""
+    parts = np.zeros(5, dtype=S.PART)
+    parts["flags"] = [1, 1, 1, 0, 1]
+    parts["bound"][:, 3] = [30.0, 2.9, 0.5, 3.0, 7.8]
+    box = ((-50.0, 50.0), (-50.0, 50.0), (0.0, 10.0))     # half-diagonal 71: the quarter is 17.8 m
+    vols = PR.probe_volumes(parts, box, terrain_parts=[0])
+    assert vols == [(1, 2, 2, 2), (4, 6, 6, 6)]              # 2.9 / 1.2 rounds to 2; 7.8 / 1.2 = 6.5 -> 7, capped at 6
+    assert PR.probe_volumes(parts, box, [0], named=[(2, (3, 4, 5))]) == [(2, 3, 4, 5)]
