@@ -378,10 +378,42 @@ SL_API int sl_lod_read(sl_lod* l, uint32_t* flags, float* node_colour, sl_gaussi
 /* The frame's linear RGBA image (device, W x H x 4 floats, as sl_render writes it) to 8-bit sRGB RGBA (device,
  * W x H x 4 bytes): exposure (frame->exposure), the tone curve frame->tone[0] (0 clamp, 1 AgX, 2 ACES filmic,
  * 3 Reinhard on luminance, 4 Khronos PBR Neutral, 5 Hable filmic), the sRGB transfer function; view mode 2 maps the
- * contributor count through the reference's heat ramp.  The sky background the reference blends where splats leave
- * it showing belongs to its environment sky model (not on this path): those pixels stay black.  Stream-ordered. */
+ * contributor count through the reference's heat ramp.  Bare pixels stay black here; sl_display_env adds the
+ * environment's sky and light discs where the splats leave the sky showing.  Stream-ordered. */
 SL_API int sl_display(const float* image_dev, uint32_t width, uint32_t height, const sl_render_frame* frame,
                       uint8_t* out_dev, void* stream);
+
+/* The environment as the display draws it (src/environment.js write :111-150, shaders/display.wgsl Env / SkyBg
+ * :7-20): the lighting sky's 16 SH coefficients, the distant lights (direction toward the light, angular std,
+ * irradiance, the visible disc's std or 0), and the background sky: up to 81 SH coefficients (bands 0-8; 0 = the
+ * lighting sky), the horizon ring's lobes with their widths (ring_par = 1 / (2 along^2), 1 / (2 across^2)), the ground
+ * below the horizon (ground_blend = sin of the blend half-width) and the glow round the sun (std 0 = none). */
+typedef struct sl_display_sky {
+  uint32_t has_sky;          /* Env.info.y: a lighting sky is present */
+  uint32_t n_lights;         /* up to 4 */
+  float sky_sh[16][3];
+  float light_dir[4][3];
+  float light_std[4];
+  float light_irr[4][3];
+  float disc_std[4];
+  uint32_t bg_count;         /* background coefficients, 0-81 (a square: (l + 1)^2) */
+  uint32_t ring_count;       /* horizon lobes, 0-8 */
+  float bg_sh[81][3];
+  float ring[8][3];
+  float ground[3];
+  float ground_blend;
+  float ring_par[2];
+  float glow[3];
+  float glow_std;
+  float glow_dir[3];
+} sl_display_sky;
+
+/* sl_display with the environment (display.wgsl fs :120-133): in the lit view, where the splats leave the sky showing
+ * (bare = 1 - alpha > 1/1024), the pixel adds bare x (the background sky toward its view direction, the glow, the
+ * horizon ring and the ground, when a sky is present, plus the distant lights' discs), before exposure and the tone
+ * curve.  sky NULL: as sl_display. */
+SL_API int sl_display_env(const float* image_dev, uint32_t width, uint32_t height, const sl_render_frame* frame,
+                          const sl_display_sky* sky, uint8_t* out_dev, void* stream);
 
 /* ---- sort (shaders/radix.wgsl) --------------------------------------------------------------------------------- */
 

@@ -393,6 +393,23 @@ def display(img, exposure: float = 1.0, tone: int = 0, view_mode: int = 3):
     return out
 
 
+def display_env(img, frame, sky):
+    """Display resolve with the environment behind the splats (orc_display_env, FP64): H x W x 4 float -> uint8."""
+    L = lib()
+    fn = L.orc_display_env
+    fn.restype = None
+    fn.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, C.c_uint32, C.c_void_p, C.c_float,
+                   C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_void_p]
+    a = np.ascontiguousarray(img, dtype=np.float32)
+    f = np.asarray(frame).reshape(())
+    view = np.ascontiguousarray(f["view"], np.float32)
+    out = np.empty(a.shape[:-1] + (4,), np.uint8)
+    fn(a.ctypes.data, a.shape[1], a.shape[0], float(f["exposure"]), int(f["tone"][0]), int(f["view_mode"]),
+       view.ctypes.data, float(f["viewport"][0]), float(f["viewport"][1]), float(f["focal"][0]),
+       float(f["focal"][1]), C.byref(sky) if sky is not None else None, out.ctypes.data)
+    return out
+
+
 def lod_records(gaussians, nodes, kids):
     """src/lod.js nodeGaussians restated (sl_oracle_lod.c): the internal nodes' Gaussian records."""
     from splatlight_gb300.structs import GAUSSIAN

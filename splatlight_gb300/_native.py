@@ -43,6 +43,16 @@ class ProbeLayout(C.Structure):
                 ("vols", (C.c_uint32 * 4) * 32)]
 
 
+class DisplaySky(C.Structure):
+    """sl_display_sky (include/splatlight.h)."""
+    _fields_ = [("has_sky", C.c_uint32), ("n_lights", C.c_uint32), ("sky_sh", (C.c_float * 3) * 16),
+                ("light_dir", (C.c_float * 3) * 4), ("light_std", C.c_float * 4), ("light_irr", (C.c_float * 3) * 4),
+                ("disc_std", C.c_float * 4), ("bg_count", C.c_uint32), ("ring_count", C.c_uint32),
+                ("bg_sh", (C.c_float * 3) * 81), ("ring", (C.c_float * 3) * 8), ("ground", C.c_float * 3),
+                ("ground_blend", C.c_float), ("ring_par", C.c_float * 2), ("glow", C.c_float * 3),
+                ("glow_std", C.c_float), ("glow_dir", C.c_float * 3)]
+
+
 class BatchOptions(C.Structure):
     _fields_ = [("max_views", C.c_uint32), ("max_tiles", C.c_uint32), ("max_slots", C.c_uint64),
                 ("max_entries", C.c_uint64), ("tile_w", C.c_uint32), ("tile_h", C.c_uint32),
@@ -125,6 +135,7 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_lighting_read": (_I, [_P, _P, _P, _P, _P]),
     "sl_renderer_bind_lighting": (_I, [_P, _P]),
     "sl_display": (_I, [_P, _U32, _U32, _P, _P, _P]),
+    "sl_display_env": (_I, [_P, _U32, _U32, _P, _P, _P, _P]),
     "sl_lod_create": (_I, [_P, _P, _U32, _P, _U32, C.POINTER(_P)]),
     "sl_lod_destroy": (_I, [_P]),
     "sl_lod_select": (_I, [_P, _P, _U32, _U32, C.c_float, _P]),

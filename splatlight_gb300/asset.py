@@ -301,6 +301,38 @@ def asset_scene(asset: Asset, width: int | None = None, height: int | None = Non
         probes=probe_layout(asset))
 
 
+def display_sky(env: dict | None):
+    """The environment as the display draws it (Environment.write, src/environment.js:111-150, with its start state:
+    sky and light gains 1): an sl_display_sky with the lighting sky, the distant lights with their visible discs'
+    std (display_std_deg), and -- when sky.background_sh_rgb is given -- the background SH, the horizon ring
+    (along_deg 25, across_deg 8 by default) with the ground below it (a 1 degree blend) and the glow round the sun
+    (angular_std_deg 12 by default; toward the first light unless it has its own direction and does not follow the
+    sun).  None without an environment."""
+    from . import display as D
+    if not env:
+        return None
+    lights = environment_lights(env)
+    raw = (env.get("lights") or [])[:4]
+    lights = [tuple(L) + (float(raw[k].get("display_std_deg", 0.0)) * DEG,) for k, L in enumerate(lights)]
+    sk = env.get("sky") or {}
+    bg = None
+    if sk.get("background_sh_rgb"):
+        bg = {"sh": sk["background_sh_rgb"][:81]}
+        hz, ground = sk.get("horizon"), sk.get("ground_rgb")
+        if hz and ground:
+            along = float(hz.get("along_deg", 25)) * DEG
+            across = float(hz.get("across_deg", 8)) * DEG
+            bg.update(ring=hz["rgb"][:8], ring_par=(1.0 / (2.0 * along * along), 1.0 / (2.0 * across * across)),
+                      ground=ground, ground_blend=math.sin(1.0 * DEG))
+        g = sk.get("glow")
+        if g:
+            follow = bool(g.get("follows_sun", True))
+            d = sun_dir(*sun_angles(lights[0][0])) if (follow or not g.get("dir")) and lights else \
+                _normalize(g.get("dir") or [0.0, 0.0, 1.0])
+            bg.update(glow=g["irradiance_rgb"], glow_std=float(g.get("angular_std_deg", 12)) * DEG, glow_dir=d)
+    return D.sky(environment_sky(env), lights, bg)
+
+
 def environment_sky(env: dict | None):
     """The sky the probes see (parseEnvironment's sh, Environment.write with the sky gain at 1,
     src/environment.js:25, 116-124): environment.sky.sh_rgb, up to 16 coefficients, (16, 3) float32; None without
