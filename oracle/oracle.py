@@ -80,6 +80,7 @@ _EXTRA: dict = {
     "orc_composite": (None, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                              C.c_int]),
     "orc_lod_records": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "orc_lod_vgrids": (C.c_int, [C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "orc_lod_select": (None, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                               C.c_uint32, C.c_uint32, C.c_float, C.c_void_p]),
     "orc_lod_colour": (None, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -423,6 +424,18 @@ def lod_records(gaussians, nodes, kids):
     return out[:len(nd) - len(g)]
 
 
+def lod_vgrids(nodes, G, kids, vgrid):
+    """src/lod.js nodeGaussians' node V grids restated (sl_oracle_lod.c): (N - G) records of 128 cells."""
+    from splatlight_gb300.structs import VGRID
+    nd = np.ascontiguousarray(nodes)
+    k = np.ascontiguousarray(kids, dtype=np.uint32)
+    v = np.ascontiguousarray(vgrid)
+    out = np.zeros(max(len(nd) - G, 1), dtype=VGRID)
+    if lib().orc_lod_vgrids(G, nd.ctypes.data, len(nd), k.ctypes.data, v.ctypes.data, out.ctypes.data) != 0:
+        raise RuntimeError("orc_lod_vgrids failed")
+    return out[:len(nd) - G]
+
+
 def lod_select(nodes, G, kids, parts, frame, flags, emit_part=0xFFFFFFFF, size_rule=1, blur_lod=0.0):
     """lod.wgsl lod_select restated: updates ``flags`` (N u32, the previous frame's cut) in place."""
     nd = np.ascontiguousarray(nodes)
@@ -501,12 +514,14 @@ class BounceIn(C.Structure):
                 ("normal", C.c_float * 3), ("lamp_T", C.c_void_p), ("env_T", C.c_void_p), ("lights", C.c_void_p),
                 ("n_lights", C.c_uint32), ("sky_sh", C.c_void_p), ("lay", ProbeLayoutC), ("max_depth", C.c_uint32),
                 ("eye", C.c_float * 3), ("alpha", C.c_float), ("frame", C.c_uint32), ("force", C.c_uint32),
-                ("moved_mask", C.c_uint32), ("dark_part", C.c_uint32), ("asg_cells", C.c_uint32)]
+                ("moved_mask", C.c_uint32), ("dark_part", C.c_uint32), ("asg_cells", C.c_uint32),
+                ("sender_cut", C.c_uint32), ("sc_reselect", C.c_uint32), ("node_gs", C.c_void_p),
+                ("node_vg", C.c_void_p)]
 
 
 class BounceState(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in ("probe_data", "probe_sh", "xfer", "lo_dir", "lo_b", "node_acc", "node_sh",
-                                          "probe_hist")]
+                                          "probe_hist", "sc_flag", "sc_X", "sc_T", "sc_envT")]
 
 
 def bounce_tables():
@@ -532,10 +547,11 @@ class Bounce:
     """The probe bounce restated (sl_oracle_light.c orc_bounce_frame), stateful over frames.  scene: a Scene whose
     parts carry their tree roots; tree = (nodes, kids) (the leaves, then the internal nodes); lit = the (colour,
     lamp_T, env_T, nodes) of oracle.lighting on the scene (the leaves' iso_norm and the maps' transmittance);
-    layout: a probes.* layout dict; sky_sh: (16, 3) or None."""
+    layout: a probes.* layout dict; sky_sh: (16, 3) or None; sender_cut: the reference's default level of detail
+    for the senders (bounce.wgsl sc_select), re-selected on the first frame and whenever a part moved."""
 
     def __init__(self, scene, tree, lit, layout, sky_sh=None, max_depth: int = 0, blend: float = 1.0,
-                 emitters_dark: bool = True, asg: bool = True):
+                 emitters_dark: bool = True, asg: bool = True, sender_cut: bool = False):
         self.scene = scene
         G = scene.count
         tn = np.ascontiguousarray(tree[0]).copy()
@@ -573,7 +589,13 @@ class Bounce:
         self.state = {"probe_data": np.zeros((NP, 128, 8), np.float32), "probe_sh": np.zeros((NP, 9, 4), np.float32),
                       "xfer": np.zeros((G, 12), np.float32), "lo_dir": np.zeros((G, 4), np.float32),
                       "lo_b": np.zeros((G, 3, 4), np.float32), "node_acc": np.zeros((N, 14, 4), np.float32),
-                      "node_sh": np.zeros((N, 14), np.uint32), "probe_hist": np.zeros((NP, 128, 16), np.float32)}
+                      "node_sh": np.zeros((N, 14), np.uint32), "probe_hist": np.zeros((NP, 128, 16), np.float32),
+                      "sc_flag": np.zeros(N, np.uint32), "sc_X": np.zeros((max(N - G, 1), 8, 4), np.float32),
+                      "sc_T": np.zeros(max(N - G, 1), np.float32), "sc_envT": np.zeros((max(N - G, 1), 4), np.float32)}
+        self.sender_cut = sender_cut
+        if sender_cut:
+            self.node_gs = np.ascontiguousarray(lod_records(scene.gaussians, tn, self.kids))
+            self.node_vg = np.ascontiguousarray(lod_vgrids(tn, G, self.kids, scene.vgrid))
         self.frame = 0
         self.first = True
 
@@ -623,6 +645,10 @@ class Bounce:
         B.moved_mask = moved_mask
         B.dark_part = self.dark_part
         B.asg_cells = 1 if self.asg else 0
+        B.sender_cut = 1 if self.sender_cut else 0
+        B.sc_reselect = 1 if (self.first or moved_mask) else 0
+        if self.sender_cut:
+            B.node_gs, B.node_vg = self.node_gs.ctypes.data, self.node_vg.ctypes.data
         st = BounceState(**{k: v.ctypes.data for k, v in self.state.items()})
         rc = L.orc_bounce_frame(C.byref(B), C.byref(st), threads)
         if rc != 0:

@@ -89,6 +89,9 @@ int64_t orc_render_lod(const sl_gaussian* gaussians, uint32_t count, const sl_pa
  * internal node, deepest first; colour: 4 floats per leaf or NULL; lo_b: 12 floats per leaf or NULL). */
 int orc_lod_records(const sl_gaussian* gauss, uint32_t G, const sl_node* nodes, uint32_t N, const uint32_t* kids,
                     sl_gaussian* out);
+/* nodeGaussians' node V grids (src/lod.js): N - G records, the mass-weighted mean of the children's cells */
+int orc_lod_vgrids(uint32_t G, const sl_node* nodes, uint32_t N, const uint32_t* kids, const sl_vgrid* leaf_vg,
+                   sl_vgrid* out);
 void orc_lod_select(const sl_node* nodes, uint32_t N, uint32_t G, const uint32_t* kids, const sl_part* parts,
                     uint32_t part_count, const sl_render_frame* f, uint32_t emit_part, uint32_t size_rule,
                     float blur_lod, uint32_t* flags);

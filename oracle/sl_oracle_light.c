@@ -1554,9 +1554,10 @@ int orc_lighting(const sl_gaussian* gs, uint32_t count, const sl_part* parts, ui
  * call: iso_xfer (bounce.wgsl:993-1026), direct_dirs_emit (emissive.wgsl:1012-1016, 1066-1082) and env_dirs
  * (environment.wgsl:311-359) for a quarter of the Gaussians, node_leaf / node_up / node_sh2 (bounce.wgsl:1166-1236),
  * probe_gather (:1255-1410, no rectangle lamps), probe_valid (:1417-1447), probe_sh2 (:1029-1041), bounce_sh
- * (:1044-1095, with gloss_sh :1102-1125).  Every Gaussian reads the lattice (the probes that ride on movable parts and
- * static probe volumes are not part of this restatement); near-field visibility is off (near_byte = 1, the
- * reference's default).  The WGSL pow(x, 3) of probe_cheb is taken as x x x. */
+ * (:1044-1095, with gloss_sh :1102-1125) and bounce_dirs (:887-985).  The probes: the lattice, 8 riding on each
+ * movable part (part_probe_frame) and the static volumes' grids (vol_frame); near-field visibility is off
+ * (near_byte = 1, the reference's default).  The WGSL pow(x, 3) of probe_cheb is taken as x x x.  The sender cut
+ * (the reference's default) follows below. */
 
 #define BN_NCELL 128u
 #define BN_HIT_MAX 16u
@@ -2098,6 +2099,299 @@ static void bn_dirs_one(const orc_bounce_in* in, const bn_probes* PS, const floa
   lb[8] = lb[9] = lb[10] = lb[11] = 0.0f;
 }
 
+/* ---- the sender cut (bounce.wgsl:1448-1730 sc_select .. node_sh2_sc; emissive.wgsl:1018-1064
+ * direct_dirs_emit_sc / direct_dirs_nodes_sc; environment.wgsl:317-351 env_dirs_sc / env_dirs_nodes_sc; host
+ * src/lighting.js:1057-1095), the reference's default level of detail for the probes' senders.
+ * On a re-selection (the first frame, or one in which a part moved) every node of every part's tree is marked, top
+ * down by depth: BELOW (above the parts, under a cut node or a cut leaf: never read), OPEN (some probe's gather opens
+ * it), NODE (every probe uses it whole) or LEAF (a leaf whose parent is OPEN, or a part's root).  A cut node is lit as
+ * one two-sided Gaussian (its nodeGaussians record and V grid), its shadow T the mean over 8 leaves reached by
+ * mass-weighted random descents; its 14-direction sums come from that light plus the probes' SH2 at its centre through
+ * its own two-face transfer; node_up sums the OPEN nodes only, and the gather reads zero under the cut.
+ * Two choices here where the reference's result depends on the order its atomics hand out slots: the cut is not
+ * capped (the reference stops at 2^18 cut nodes a frame, past which nodes open), and a cut node refreshes its shadow
+ * and direct light in the frames with node % 4 == frame % 4 (the reference: its slot % 4). */
+enum { SC_BELOW = 0u, SC_OPEN = 1u, SC_NODE = 2u, SC_LEAF = 3u };
+#define SC_SAMPLES 8u
+
+/* pcg_hash and to_unit (common.wgsl:98-104) */
+static uint32_t sc_pcg(uint32_t x) {
+  uint32_t s = x * 747796405u + 2891336453u;
+  uint32_t w = ((s >> ((s >> 28u) + 4u)) ^ s) * 277803737u;
+  return (w >> 22u) ^ w;
+}
+static float sc_to_unit(uint32_t x) { return (float)(x >> 8u) * (1.0f / 16777216.0f); }
+/* sc_face (common.wgsl:342-345), SC_FACE_K 1 */
+static float sc_face(float c) { return clampf(c * 1.0f, -1.0f, 1.0f); }
+/* sc_mass (bounce.wgsl): kappa / sqrt(det cinv) */
+static float sc_mass(const sl_node* nd) {
+  return nd->kappa / sqrtf(fmaxf(sym_det(nd_cinv_d(nd), nd_cinv_o(nd)), 1e-30f));
+}
+static float sc_round(float x) { return rintf(x); } /* WGSL round: half to even */
+
+/* sc_probe_dist (bounce.wgsl:1478-1513): the smallest (distance - margin) from world point P to the gather centres of
+ * the probes that see part `own`: the room lattice's nearest 2x2x2 block centre less the block radius, the terrain's
+ * 3 x 3 columns around P, each movable part's 8 probes but own's, each static volume's nearest grid probe */
+static float sc_probe_dist(const orc_bounce_in* in, const bn_probes* PS, f3 P, uint32_t own, float brad) {
+  const orc_probe_layout* L = &in->lay;
+  float best = 1e30f;
+  const float m = 0.0f; /* the gathers of probes that cut around themselves keep no margin (vol_info.y = 0) */
+  if (!L->terrain) {
+    const float Pv[3] = {P.x, P.y, P.z};
+    float b[3];
+    for (int a = 0; a < 3; a++) {
+      float nb = (float)((L->dims[a] + 1u) / 2u);
+      b[a] = clampf(sc_round(((Pv[a] - L->lo[a]) / fmaxf(L->step[a], 1e-6f) - 0.5f) * 0.5f), 0.0f, nb - 1.0f);
+    }
+    f3 cen = F3(L->lo[0] + L->step[0] * (2.0f * b[0] + 0.5f), L->lo[1] + L->step[1] * (2.0f * b[1] + 0.5f),
+                L->lo[2] + L->step[2] * (2.0f * b[2] + 0.5f));
+    best = len3(sub3(P, cen)) - brad;
+  } else {
+    float fx = clampf(sc_round((P.x - L->lo[0]) / fmaxf(L->step[0], 1e-6f)), -1e9f, 1e9f);
+    float fy = clampf(sc_round((P.y - L->lo[1]) / fmaxf(L->step[1], 1e-6f)), -1e9f, 1e9f);
+    int ci = (int)fx, cj = (int)fy;
+    for (int di = -1; di <= 1; di++) {
+      for (int dj = -1; dj <= 1; dj++) {
+        int ii = ci + di, jj = cj + dj;
+        uint32_t i = (uint32_t)(ii < 0 ? 0 : (ii > (int)L->dims[0] - 1 ? (int)L->dims[0] - 1 : ii));
+        uint32_t j = (uint32_t)(jj < 0 ? 0 : (jj > (int)L->dims[1] - 1 ? (int)L->dims[1] - 1 : jj));
+        float x = L->lo[0] + L->step[0] * (float)i, y = L->lo[1] + L->step[1] * (float)j;
+        float gz = bn_ground(L, i, j);
+        for (uint32_t k = 0; k < L->dims[2]; k++) best = fminf(best, len3(sub3(P, F3(x, y, gz + L->levels[k]))) - m);
+      }
+    }
+  }
+  for (uint32_t q = 0; q < in->part_count && q < 32u; q++) {
+    if (q == own) continue;
+    const float* xf = in->parts[q].xf;
+    if (bn_is_part_probe_part(in, q)) {
+      f3 c, h;
+      bn_part_frame(in, q, &c, &h);
+      if (len3(sub3(P, xf_point(xf, c))) - len3(h) - m >= best) continue;
+      for (uint32_t k = 0; k < 8u; k++) best = fminf(best, len3(sub3(P, bn_probe_pos(in, PS, PS->nl + q * 8u + k))) - m);
+    } else if (bn_has_vol(PS, q)) {
+      f3 c, h;
+      bn_vol_frame(in, q, &c, &h);
+      const float d[3] = {(float)PS->vol_dims[q][0], (float)PS->vol_dims[q][1], (float)PS->vol_dims[q][2]};
+      f3 lp = xf_dir_inv(xf, sub3(P, F3(xf[3], xf[7], xf[11])));
+      const float lv[3] = {lp.x, lp.y, lp.z}, cv[3] = {c.x, c.y, c.z}, hv[3] = {h.x, h.y, h.z};
+      float g[3];
+      for (int a = 0; a < 3; a++) {
+        float span = fmaxf(d[a] - 1.0f, 1.0f);
+        float ijk = clampf(sc_round((lv[a] - cv[a] + hv[a]) / fmaxf(2.0f * hv[a], 1e-6f) * span), 0.0f, d[a] - 1.0f);
+        g[a] = cv[a] - hv[a] + 2.0f * hv[a] * ijk / span;
+      }
+      best = fminf(best, len3(sub3(lp, F3(g[0], g[1], g[2]))) - m);
+    }
+  }
+  return best;
+}
+
+/* sc_select (bounce.wgsl:1528-1545) for node n, its parent's mark already set */
+static uint32_t sc_select_one(const orc_bounce_in* in, const bn_probes* PS, const uint32_t* parent,
+                              const uint32_t* flag, uint32_t n, float brad) {
+  const sl_node* nd = &in->nodes[n];
+  uint32_t q = nd->part;
+  if (q >= in->part_count) return SC_BELOW; /* scene nodes above the parts: the gather starts at part roots */
+  if (in->parts[q].root != n && (parent[n] == NONE_U32 || flag[parent[n]] != SC_OPEN)) return SC_BELOW;
+  if (n < in->count) return SC_LEAF;
+  f3 P = xf_point(in->parts[q].xf, F3(nd->mean[0], nd->mean[1], nd->mean[2]));
+  return sc_probe_dist(in, PS, P, q, brad) <= BN_THETA * nd->smax ? SC_OPEN : SC_NODE;
+}
+
+/* sc_xfer (bounce.wgsl:1640-1672): per cut node and face of its short axis the share of the SH2 transfer from its own
+ * V grid and the face's exposure; 6 vec4: face 0 t0-3, t4-7, (t8, S, 0, 0), then face 1 */
+static void sc_xfer_one(const orc_bounce_in* in, const float* cells, uint32_t n, float* X) {
+  const uint32_t r = n - in->count;
+  const sl_gaussian* G = &in->node_gs[r];
+  const sl_node* nd = &in->nodes[n];
+  const float* xf = in->parts[G->part_surface & 0xFFFFu].xf;
+  m3f Rq = quat_matrix(G->quat);
+  f3 nrm = Rq.c[0];
+  float s3 = G->scale[0] * G->scale[1] * G->scale[2];
+  float t[20];
+  for (int i = 0; i < 20; i++) t[i] = 0.0f;
+  float S0 = 0.0f;
+  for (uint32_t cc = 0; cc < BN_NCELL; cc++) {
+    f3 w = bn_cell_dir(cells, cc);
+    f3 u = xf_dir_inv(xf, w);
+    float a = footprint(nd, s3 * s3, u) * cells[4 * cc + 3];
+    S0 += a;
+    float v = vgrid_lookup(&in->node_vg[r], u);
+    if (v <= 0.0f) continue;
+    float h = 0.5f + 0.5f * sc_face(dot3(u, nrm));
+    float y[9];
+    bn_sh2(w, y);
+    for (int i = 0; i < 9; i++) {
+      t[i] += a * v * h * y[i];
+      t[10 + i] += a * v * (1.0f - h) * y[i];
+    }
+    t[9] += a * v * h;
+    t[19] += a * v * (1.0f - h);
+  }
+  float Smin = fmaxf(0.5f * 0.02f * S0, 1e-30f); /* iso_init.wgsl ISO_EPS, per face */
+  for (int f = 0; f < 2; f++) {
+    const float* o = t + 10 * f;
+    float* x = X + 12 * f;
+    x[0] = o[0]; x[1] = o[1]; x[2] = o[2]; x[3] = o[3];
+    x[4] = o[4]; x[5] = o[5]; x[6] = o[6]; x[7] = o[7];
+    x[8] = o[8]; x[9] = fmaxf(o[9], Smin); x[10] = 0.0f; x[11] = 0.0f;
+  }
+}
+
+/* sc_shadow (bounce.wgsl:1566-1625): the mean lamp T and distant-light T over SC_SAMPLES leaves under n, each reached
+ * by a descent that picks a child with probability by mass (a fixed hash per node and sample).  The Gaussians carry
+ * one lamp T each here, so the reference's per-lamp slots reduce to that mean. */
+static void sc_shadow_one(const orc_bounce_in* in, uint32_t n, float* T_out, float* E_out) {
+  const uint32_t G = in->count;
+  float T = 0.0f, E[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  for (uint32_t s = 0; s < SC_SAMPLES; s++) {
+    uint32_t m = n, h = sc_pcg(n * SC_SAMPLES + s);
+    for (uint32_t it = 0; it < 64u && m >= G; it++) {
+      const sl_node* nd = &in->nodes[m];
+      float tot = 0.0f;
+      for (uint32_t j = nd->child_lo; j < nd->child_hi; j++) tot += sc_mass(&in->nodes[in->kids[j]]);
+      float u = sc_to_unit(h) * tot;
+      h = sc_pcg(h);
+      uint32_t pick = in->kids[nd->child_lo];
+      for (uint32_t j = nd->child_lo; j < nd->child_hi; j++) {
+        pick = in->kids[j];
+        u -= sc_mass(&in->nodes[in->kids[j]]);
+        if (u <= 0.0f) break;
+      }
+      m = pick;
+    }
+    /* trees are at most 64 levels deep (checked where the cut is set up), so m is a leaf */
+    T += in->lamp_T[m];
+    for (int c = 0; c < 4; c++) E[c] += in->env_T[4u * m + c];
+  }
+  *T_out = T / (float)SC_SAMPLES;
+  for (int c = 0; c < 4; c++) E_out[c] = E[c] / (float)SC_SAMPLES;
+}
+
+/* direct_dirs_nodes_sc + env_dirs_nodes_sc: the light each face of cut node n catches, before albedo and exposure
+ * (matte: shininess left out of the senders), into X's entries 6 and 7 */
+static void sc_direct_node(const orc_bounce_in* in, uint32_t n, float T, const float* E, float* X) {
+  const uint32_t r = n - in->count;
+  const sl_gaussian* G = &in->node_gs[r];
+  const sl_node* nd = &in->nodes[n];
+  const float* xf = in->parts[G->part_surface & 0xFFFFu].xf;
+  m3f Rq = quat_matrix(G->quat);
+  f3 nrm = Rq.c[0];
+  float s3 = G->scale[0] * G->scale[1] * G->scale[2];
+  float detC = s3 * s3;
+  f3 P = xf_point(xf, F3(G->mu[0], G->mu[1], G->mu[2]));
+  f3 c0 = F3(0.0f, 0.0f, 0.0f), c1 = F3(0.0f, 0.0f, 0.0f);
+  if (in->n_emit) {
+    uint32_t stack[48];
+    uint32_t sp = 1;
+    stack[0] = in->tree_root;
+    while (sp > 0u) {
+      sp--;
+      const float* e = in->tree + 24u * stack[sp];
+      uint32_t child_lo = sl_float_to_bits(e[11]), child_hi = sl_float_to_bits(e[15]);
+      f3 emean = F3(e[0], e[1], e[2]);
+      int use;
+      if (child_lo == NONE_U32 || in->emit_mode == 0u) {
+        use = child_lo == NONE_U32;
+      } else {
+        f3 d = sub3(P, emean);
+        use = dot3(d, d) > in->emit_theta * in->emit_theta * e[3] * e[3];
+      }
+      if (!use) {
+        if (sp + 2u <= 48u) { stack[sp] = child_lo; stack[sp + 1u] = child_hi; sp += 2u; }
+        continue;
+      }
+      f3 d = sub3(emean, P);
+      float d2 = dot3(d, d);
+      if (d2 < 1e-8f) continue;
+      f3 ww = div3(d, sqrtf(d2));
+      f3 wi = xf_dir_inv(xf, ww);
+      float vi = vgrid_lookup(&in->node_vg[r], wi);
+      if (vi <= 1e-7f) continue;
+      f3 mw = mul3(ww, -1.0f);
+      float s = 1.0f;
+      if (in->one_sided) {
+        f3 nn = F3(in->normal[0], in->normal[1], in->normal[2]);
+        float cs = dot3(mw, nn);
+        s = in->edge_soft > 0.0f ? smoothstepf(-in->edge_soft, in->edge_soft, cs) : (cs > 0.0f ? 1.0f : 0.0f);
+      }
+      float mq = sqrtf(fmaxf(dot3(mw, sym_mul(F3(e[4], e[5], e[6]), F3(e[8], e[9], e[10]), mw)), 0.0f));
+      f3 I = mul3(F3(e[12], e[13], e[14]), s * in->emit_scale * mq);
+      f3 light = mul3(I, vi * footprint(nd, detC, wi) / d2 * 1.0f);
+      float h = 0.5f + 0.5f * sc_face(dot3(wi, nrm));
+      c0 = add3(c0, mul3(light, h));
+      c1 = add3(c1, mul3(light, 1.0f - h));
+    }
+  }
+  c0 = mul3(c0, T);
+  c1 = mul3(c1, T);
+  const sl_material* mat = &in->mats[mat_index(G, in->mat_count)];
+  if (in->n_lights && (mat->flags & 1u) == 0u) {
+    for (uint32_t k = 0; k < in->n_lights && k < 4u; k++) {
+      f3 wi = xf_dir_inv(xf, F3(in->lights[k].dir[0], in->lights[k].dir[1], in->lights[k].dir[2]));
+      float v = vgrid_lookup(&in->node_vg[r], wi);
+      if (v <= 1e-7f) continue;
+      f3 c = mul3(F3(in->lights[k].irr[0], in->lights[k].irr[1], in->lights[k].irr[2]),
+                  E[k] * v * footprint(nd, detC, wi));
+      float h = 0.5f + 0.5f * sc_face(dot3(wi, nrm));
+      c0 = add3(c0, mul3(c, h));
+      c1 = add3(c1, mul3(c, 1.0f - h));
+    }
+  }
+  X[24] = c0.x; X[25] = c0.y; X[26] = c0.z; X[27] = 0.0f;
+  X[28] = c1.x; X[29] = c1.y; X[30] = c1.z; X[31] = 0.0f;
+}
+
+/* node_cut (bounce.wgsl:1682-1716): cut node n as one sender, each face's light (its direct light plus the probes'
+ * SH2 at its centre through the face's transfer, over the face's exposure) shown toward each D_k by its share there */
+static void sc_node_cut(const orc_bounce_in* in, const bn_probes* PS, const float* d14, const float* pd,
+                        const float* probe_sh, uint32_t n, const float* X, float* acc) {
+  const uint32_t r = n - in->count;
+  const sl_gaussian* G = &in->node_gs[r];
+  const sl_node* nd = &in->nodes[n];
+  uint32_t own = G->part_surface & 0xFFFFu;
+  const float* xf = in->parts[own].xf;
+  f3 P = xf_point(xf, F3(G->mu[0], G->mu[1], G->mu[2]));
+  m3f Rq = quat_matrix(G->quat);
+  f3 nrm = Rq.c[0];
+  float s3 = G->scale[0] * G->scale[1] * G->scale[2];
+  bn_weights pw = bn_weights_for(in, PS, pd, P, own);
+  f3 Lsh[9];
+  for (int i = 0; i < 9; i++) Lsh[i] = F3(0.0f, 0.0f, 0.0f);
+  for (int k = 0; k < 8; k++) {
+    float w = pw.w[k];
+    if (w <= 0.0f) continue;
+    for (int i = 0; i < 9; i++) {
+      const float* s = probe_sh + 4u * (9u * pw.pid[k] + (uint32_t)i);
+      Lsh[i] = add3(Lsh[i], mul3(F3(s[0], s[1], s[2]), w));
+    }
+  }
+  f3 col[2];
+  f3 alb = F3(G->albedo[0], G->albedo[1], G->albedo[2]);
+  for (int f = 0; f < 2; f++) {
+    const float* x = X + 12 * f;
+    f3 B = mul3(Lsh[0], x[0]);
+    for (int i = 1; i < 9; i++) B = add3(B, mul3(Lsh[i], x[i]));
+    B = F3(fmaxf(B.x, 0.0f), fmaxf(B.y, 0.0f), fmaxf(B.z, 0.0f));
+    f3 Ld = add3(F3(X[24 + 4 * f], X[25 + 4 * f], X[26 + 4 * f]), B);
+    Ld = F3(fmaxf(Ld.x, 0.0f), fmaxf(Ld.y, 0.0f), fmaxf(Ld.z, 0.0f));
+    col[f] = div3(mul3v(alb, Ld), x[9]);
+  }
+  int dark = own == in->dark_part;
+  for (int k = 0; k < 14; k++) {
+    f3 wo = xf_dir_inv(xf, F3(d14[3 * k], d14[3 * k + 1], d14[3 * k + 2]));
+    float w = footprint(nd, s3 * s3, wo) * vgrid_lookup(&in->node_vg[r], wo);
+    float h = 0.5f + 0.5f * sc_face(dot3(wo, nrm));
+    f3 L = dark ? F3(0.0f, 0.0f, 0.0f) : add3(mul3(col[0], h), mul3(col[1], 1.0f - h));
+    float* o = acc + 4u * (14u * n + (uint32_t)k);
+    o[0] = L.x * w;
+    o[1] = L.y * w;
+    o[2] = L.z * w;
+    o[3] = w;
+  }
+}
+
 int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads) {
   const orc_probe_layout* L = &in->lay;
   const uint32_t G = in->count, N = in->n_nodes;
@@ -2147,11 +2441,73 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
     xo[9] = xo[10] = xo[11] = 0.0f;
   }
 
-  /* direct_dirs_emit + env_dirs: a quarter of the Gaussians (g % 4 == frame % 4) */
+  /* the sender cut: re-selected top down by depth when a part moved (or on the first frame), with the cut nodes'
+   * transfer; then the shadow T of the cut nodes that refresh this frame */
+  const int sc = in->sender_cut != 0u;
+  const uint32_t fq = in->frame % 4u;
+  const int resel = sc && in->sc_reselect != 0u;
+  const float sc_brad = L->terrain ? 0.0f : (float)(0.5 * sqrt((double)L->step[0] * L->step[0] +
+                                                               (double)L->step[1] * L->step[1] +
+                                                               (double)L->step[2] * L->step[2]));
+  if (resel) {
+    uint32_t* parent = (uint32_t*)malloc(sizeof(uint32_t) * N);
+    uint32_t* by_depth = (uint32_t*)malloc(sizeof(uint32_t) * N);
+    uint32_t dcount[257] = {0};
+    if (!parent || !by_depth) return -1;
+    for (uint32_t n = 0; n < N; n++) parent[n] = NONE_U32;
+    for (uint32_t n = G; n < N; n++)
+      for (uint32_t j = in->nodes[n].child_lo; j < in->nodes[n].child_hi; j++) parent[in->kids[j]] = n;
+    for (uint32_t n = 0; n < N; n++) dcount[(in->nodes[n].depth < 255u ? in->nodes[n].depth : 255u) + 1u]++;
+    for (int d = 1; d < 257; d++) dcount[d] += dcount[d - 1];
+    uint32_t fill[256];
+    for (int d = 0; d < 256; d++) fill[d] = dcount[d];
+    for (uint32_t n = 0; n < N; n++) by_depth[fill[in->nodes[n].depth < 255u ? in->nodes[n].depth : 255u]++] = n;
+    for (int d = 0; d < 256; d++) {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 256)
+#endif
+      for (int64_t t = dcount[d]; t < (int64_t)dcount[d + 1]; t++) {
+        uint32_t n = by_depth[t];
+        st->sc_flag[n] = sc_select_one(in, &PS, parent, st->sc_flag, n, sc_brad);
+      }
+    }
+    free(parent);
+    free(by_depth);
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
 #endif
-  for (int64_t gi = in->frame % 4u; gi < (int64_t)G; gi += 4) bn_direct_one(in, (uint32_t)gi, st->lo_dir);
+    for (int64_t ni = G; ni < (int64_t)N; ni++)
+      if (st->sc_flag[ni] == SC_NODE) sc_xfer_one(in, cells, (uint32_t)ni, st->sc_X + 32u * (uint32_t)(ni - G));
+  }
+  if (sc) {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+#endif
+    for (int64_t ni = G; ni < (int64_t)N; ni++) {
+      uint32_t n = (uint32_t)ni;
+      if (st->sc_flag[n] != SC_NODE || !(resel || n % 4u == fq)) continue;
+      sc_shadow_one(in, n, st->sc_T + (n - G), st->sc_envT + 4u * (n - G));
+    }
+  }
+
+  /* direct_dirs_emit + env_dirs: a quarter of the Gaussians (g % 4 == frame % 4); with the sender cut only the cut's
+   * leaves among them (direct_dirs_emit_sc, env_dirs_sc), then the cut nodes that refresh this frame
+   * (direct_dirs_nodes_sc, env_dirs_nodes_sc) */
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+#endif
+  for (int64_t gi = in->frame % 4u; gi < (int64_t)G; gi += 4)
+    if (!sc || st->sc_flag[gi] == SC_LEAF) bn_direct_one(in, (uint32_t)gi, st->lo_dir);
+  if (sc) {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+#endif
+    for (int64_t ni = G; ni < (int64_t)N; ni++) {
+      uint32_t n = (uint32_t)ni;
+      if (st->sc_flag[n] != SC_NODE || !(resel || n % 4u == fq)) continue;
+      sc_direct_node(in, n, st->sc_T[n - G], st->sc_envT + 4u * (n - G), st->sc_X + 32u * (n - G));
+    }
+  }
 
   /* node_leaf */
 #ifdef _OPENMP
@@ -2159,6 +2515,7 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
 #endif
   for (int64_t gi = 0; gi < (int64_t)G; gi++) {
     uint32_t g = (uint32_t)gi;
+    if (sc && st->sc_flag[g] != SC_LEAF) continue; /* node_leaf_list: the cut's leaves */
     const sl_gaussian* Gs = &in->gs[g];
     const sl_node* nd = &in->nodes[g];
     const float* xf = in->parts[Gs->part_surface & 0xFFFFu].xf;
@@ -2177,7 +2534,17 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
       o[3] = w;
     }
   }
-  /* node_up: depths max_depth - 1 .. 1, children summed in kids order */
+  /* node_cut: the cut nodes as senders, from the probes of the frame before */
+  if (sc) {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+#endif
+    for (int64_t ni = G; ni < (int64_t)N; ni++)
+      if (st->sc_flag[ni] == SC_NODE)
+        sc_node_cut(in, &PS, d14, st->probe_data, st->probe_sh, (uint32_t)ni, st->sc_X + 32u * (uint32_t)(ni - G),
+                    st->node_acc);
+  }
+  /* node_up: depths max_depth - 1 .. 1, children summed in kids order (with the sender cut the open nodes only) */
   for (int d = (int)in->max_depth - 1; d >= 1; d--) {
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nthreads) schedule(static, 256)
@@ -2185,6 +2552,7 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
     for (int64_t ii = G; ii < (int64_t)N; ii++) {
       const sl_node* nd = &in->nodes[ii];
       if (nd->depth != (uint32_t)d || nd->part == NONE_U32) continue;
+      if (sc && st->sc_flag[ii] != SC_OPEN) continue;
       for (int k = 0; k < 14; k++) {
         float s[4] = {0, 0, 0, 0};
         for (uint32_t j = nd->child_lo; j < nd->child_hi; j++) {
@@ -2201,6 +2569,10 @@ int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads
 #pragma omp parallel for num_threads(nthreads) schedule(static, 256)
 #endif
   for (int64_t ii = 0; ii < (int64_t)N; ii++) {
+    if (sc && st->sc_flag[ii] == SC_BELOW) { /* under the cut: the gather reads zero (the reference's null slot) */
+      for (int j = 0; j < 14; j++) st->node_sh[14u * (uint32_t)ii + (uint32_t)j] = 0u;
+      continue;
+    }
     f3 Lk[14];
     for (int k = 0; k < 14; k++) {
       const float* a = st->node_acc + 4u * (14u * (uint32_t)ii + (uint32_t)k);

@@ -113,6 +113,11 @@ typedef struct orc_bounce_in {
   uint32_t dark_part;  /* the part whose Gaussians send nothing into the probes (PP.refl.w - 1; NONE: none) */
   uint32_t asg_cells;  /* U.iso bit 2 (asgSpec): near-mirror Gaussians see the cells near their mirror direction as
                           lights with an angular size (cell_asg_phase) */
+  uint32_t sender_cut;  /* the sender cut (bounce.wgsl sc_select; the reference's default): only the senders some probe
+                           resolves are lit, the rest of each part's tree as the nodes every probe uses whole */
+  uint32_t sc_reselect; /* re-select the cut this frame (the first frame, or a part moved) */
+  const sl_gaussian* node_gs; /* the internal nodes as Gaussians (orc_lod_records), N - G */
+  const sl_vgrid* node_vg;    /* their V grids (orc_lod_vgrids), N - G */
 } orc_bounce_in;
 
 typedef struct orc_bounce_state {
@@ -124,12 +129,18 @@ typedef struct orc_bounce_state {
   float* node_acc;   /* N x 14 x 4 */
   uint32_t* node_sh; /* N x 14 */
   float* probe_hist; /* NP x 128 x 16: the last two gathers per ray, (rgb, m1), (m2, 0, 0, 0) each */
+  /* the sender cut's state (unused without it) */
+  uint32_t* sc_flag; /* N: BELOW 0, OPEN 1, NODE 2, LEAF 3 */
+  float* sc_X;       /* (N - G) x 32: per cut node the two faces' transfer and exposure (24), their direct light (8) */
+  float* sc_T;       /* N - G: a cut node's lamp T */
+  float* sc_envT;    /* (N - G) x 4: its distant lights' T */
 } orc_bounce_state;
 
 
-/* One frame of the probe bounce (the reference's encodeBounce with ?sendercut=0): iso_xfer, direct_dirs_emit +
- * env_dirs for the Gaussians g % 4 == frame % 4, node_leaf, node_up, node_sh2, probe_gather, probe_valid, probe_sh2,
- * bounce_sh.  The state persists between frames (zero it before the first). */
+/* One frame of the probe bounce (the reference's encodeBounce): iso_xfer, direct_dirs_emit + env_dirs for the
+ * Gaussians g % 4 == frame % 4, node_leaf, node_up, node_sh2, probe_gather, probe_valid, probe_sh2, bounce_sh; with
+ * the sender cut (in->sender_cut) sc_select, sc_xfer, sc_shadow and the cut nodes' direct light, node_leaf on the cut's
+ * leaves, node_cut, node_up on the open nodes.  The state persists between frames (zero it before the first). */
 int orc_bounce_frame(const orc_bounce_in* in, orc_bounce_state* st, int nthreads);
 /* D14 (14 x 3) and the 9 x 14 least-squares SH2 fit on it, float64 then rounded */
 void orc_bounce_tables(float* d14, float* pinv);

@@ -156,6 +156,53 @@ int orc_lod_records(const sl_gaussian* gauss, uint32_t G, const sl_node* nodes, 
   return 0;
 }
 
+/* nodeGaussians' node V grids (src/lod.js:47-50, 86-88, 99-103): per internal node, deepest first, the mass-weighted
+ * mean of its children's cells, kept as float32 (each addition rounded there), then rounded half up and clamped at 255 */
+int orc_lod_vgrids(uint32_t G, const sl_node* nodes, uint32_t N, const uint32_t* kids, const sl_vgrid* leaf_vg,
+                   sl_vgrid* out) {
+  if (N <= G) return 0;
+  double* mass = (double*)calloc(N, sizeof(double));
+  float* V = (float*)calloc((size_t)(N - G) * 128u, sizeof(float));
+  uint32_t* order = (uint32_t*)malloc(sizeof(uint32_t) * (N - G));
+  if (!mass || !V || !order) return -1;
+  for (uint32_t g = 0; g < G; g++) {
+    double C[3][3];
+    double det = orc_node_cov(&nodes[g], C);
+    mass[g] = (double)nodes[g].kappa / sqrt(det > 1e-30 ? det : 1e-30);
+  }
+  uint32_t max_d = 0, k = 0;
+  for (uint32_t n = G; n < N; n++)
+    if (nodes[n].depth > max_d) max_d = nodes[n].depth;
+  for (int64_t d = max_d; d >= 0; d--)
+    for (uint32_t n = G; n < N; n++)
+      if (nodes[n].depth == (uint32_t)d) order[k++] = n;
+  for (uint32_t t = 0; t < N - G; t++) {
+    uint32_t n = order[t], lo = nodes[n].child_lo, hi = nodes[n].child_hi;
+    double m = 0.0;
+    for (uint32_t j = lo; j < hi; j++) m += mass[kids[j]];
+    mass[n] = m;
+    float* vn = V + (size_t)(n - G) * 128u;
+    for (uint32_t j = lo; j < hi; j++) {
+      uint32_t ch = kids[j];
+      double w = mass[ch] / (m > 1e-30 ? m : 1e-30);
+      const uint8_t* lb = ch < G ? (const uint8_t*)&leaf_vg[ch] : NULL;
+      const float* vc = ch < G ? NULL : V + (size_t)(ch - G) * 128u;
+      for (int q = 0; q < 128; q++) vn[q] = (float)((double)vn[q] + w * (double)(lb ? (float)lb[q] : vc[q]));
+    }
+  }
+  for (uint32_t r = 0; r < N - G; r++) {
+    uint8_t* o = (uint8_t*)&out[r];
+    for (int q = 0; q < 128; q++) {
+      double v = floor((double)V[(size_t)r * 128u + q] + 0.5);
+      o[q] = (uint8_t)(v > 255.0 ? 255.0 : (v < 0.0 ? 0.0 : v));
+    }
+  }
+  free(mass);
+  free(V);
+  free(order);
+  return 0;
+}
+
 enum { ORC_NONE = 0, ORC_OPEN = 1, ORC_DRAW = 2, ORC_CAND = 3, ORC_UNDER = 4 };
 
 /* lod.wgsl lod_select (:169-225), one depth after the other from the roots down */

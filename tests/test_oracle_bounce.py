@@ -112,3 +112,110 @@ def test_probe_volumes_rule():
     vols = PR.probe_volumes(parts, box, terrain_parts=[0])
     assert vols == [(1, 2, 2, 2), (4, 6, 6, 6)]              # 2.9 / 1.2 rounds to 2; 7.8 / 1.2 = 6.5 -> 7, capped at 6
     assert PR.probe_volumes(parts, box, [0], named=[(2, (3, 4, 5))]) == [(2, 3, 4, 5)]
+
+
+# ---- the sender cut (bounce.wgsl sc_select .. node_cut; the reference's default level of detail for the senders)
+
+def _node_vgrids_numpy(nodes, G, kids, vgrid):
+    """src/lod.js nodeGaussians' V grids in numpy: masses in float64, each cell kept as float32, half up, <= 255."""
+    N = len(nodes)
+    a = nodes["cinv_diag"].astype(np.float64)
+    o = nodes["cinv_off"].astype(np.float64)
+    det = (a[:, 0] * (a[:, 1] * a[:, 2] - o[:, 2] * o[:, 2]) - o[:, 0] * (o[:, 0] * a[:, 2] - o[:, 2] * o[:, 1])
+           + o[:, 1] * (o[:, 0] * o[:, 2] - a[:, 1] * o[:, 1]))
+    mass = np.zeros(N)
+    mass[:G] = nodes["kappa"][:G].astype(np.float64) / np.sqrt(np.maximum(det[:G], 1e-30))
+    V = np.zeros((N, 128), np.float32)
+    V[:G] = np.ascontiguousarray(vgrid).view(np.uint8).reshape(G, 128)
+    order = sorted(range(G, N), key=lambda n: -int(nodes["depth"][n]))   # stable: index order within a depth
+    for n in order:
+        ch = kids[nodes["child_lo"][n]:nodes["child_hi"][n]]
+        m = 0.0
+        for c in ch:
+            m += mass[c]
+        mass[n] = m
+        for c in ch:
+            V[n] = (V[n].astype(np.float64) + (mass[c] / max(m, 1e-30)) * V[c].astype(np.float64)).astype(np.float32)
+    return np.minimum(255.0, np.floor(V[G:].astype(np.float64) + 0.5)).astype(np.uint8)
+
+
+def test_node_vgrids_match_numpy(orc):
+    s, tree = S.with_tree(S.subset(S.cornell(), 1500))
+    nodes, kids = tree
+    got = orc.lod_vgrids(nodes, s.count, kids, s.vgrid).view(np.uint8).reshape(-1, 128)
+    ref = _node_vgrids_numpy(nodes, s.count, kids, s.vgrid)
+    assert got.shape == ref.shape and np.array_equal(got, ref)
+    assert got.max() <= 255 and got.astype(np.int64).sum() > 0
+
+
+def _cut_scene(name):
+    if name == "hill":
+        s = S.hill(6000, seed=4, width=64, height=64, n_emit=4)
+    else:
+        s = S.subset(S.cornell(), 8000)
+    s = dataclasses.replace(s, shadow_res=64, sun_res=64)
+    return S.with_tree(s)
+
+
+@pytest.mark.parametrize("name", ["hill", "cornell"])
+def test_sender_cut_marks(orc, name):
+    """Under an OPEN node every child is marked, under any other mark none is; every lattice probe's gather uses each
+    cut node whole (distance from its gather centre less the block margin above theta smax)."""
+    s, tree = _cut_scene(name)
+    lit = orc.lighting(s, threads=4)
+    lay = PR.for_scene(s)
+    b = orc.Bounce(s, tree, lit, lay, sky_sh=s.sky_sh, sender_cut=True)
+    st = b.step(s.eye, threads=4)
+    fl, tn, kids, G = st["sc_flag"], b.nodes, b.kids, s.count
+    counts = np.bincount(fl, minlength=4)
+    assert counts[2] > 0 and counts[3] > 0 and counts[1] > 0     # cut nodes, cut leaves, open nodes
+    assert (fl[:G] != 2).all() and (fl[G:] != 3).all()           # leaves are never NODE, internal nodes never LEAF
+    for n in range(G, len(tn)):
+        ch = kids[tn["child_lo"][n]:tn["child_hi"][n]]
+        assert ((fl[ch] != 0) if fl[n] == 1 else (fl[ch] == 0)).all()
+    d, lo, step = lay["dims"], np.array(lay["lo"]), np.array(lay["step"])
+    ii, jj, kk = np.meshgrid(np.arange(d[0]), np.arange(d[1]), np.arange(d[2]), indexing="ij")
+    if lay["terrain"]:
+        cen = np.stack([lo[0] + step[0] * ii, lo[1] + step[1] * jj,
+                        lay["ground"].reshape(d[0], d[1])[ii, jj] + np.array(lay["levels"])[kk]], -1)
+        brad = 0.0
+    else:
+        cen = lo + step * (2 * (np.stack([ii, jj, kk], -1) // 2) + 0.5)
+        brad = 0.5 * np.linalg.norm(step)
+    cen = cen.reshape(-1, 3)
+    cut = np.nonzero(fl == 2)[0]
+    dmin = np.array([np.linalg.norm(cen - m, axis=1).min() for m in tn["mean"][cut].astype(np.float64)]) - brad
+    assert (dmin > 4.0 * tn["smax"][cut]).all()
+
+
+def test_sender_cut_with_nothing_to_cut_is_the_exact_path(orc):
+    """With every node too large for any probe to use whole, the cut is every leaf under open nodes and the frame
+    equals the per-leaf path bit for bit."""
+    s, (nodes, kids) = _cut_scene("hill")
+    nodes = nodes.copy()
+    nodes["smax"][s.count:] = 1e9
+    lit = orc.lighting(s, threads=4)
+    lay = PR.for_scene(s)
+    ex = orc.Bounce(s, (nodes, kids), lit, lay, sky_sh=s.sky_sh)
+    sc = orc.Bounce(s, (nodes, kids), lit, lay, sky_sh=s.sky_sh, sender_cut=True)
+    for f in range(3):
+        a, b = ex.step(s.eye, threads=4), sc.step(s.eye, threads=4)
+    assert np.bincount(b["sc_flag"], minlength=4)[2] == 0
+    for k in ("probe_data", "probe_sh", "lo_dir", "lo_b", "node_sh"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("name", ["hill", "cornell"])
+def test_sender_cut_is_close_to_the_exact_path(orc, name):
+    """The cut approximates what the leaves send: after a few frames the bounce toward the eye is within 3% of the
+    per-leaf path in the mean and 10% of its largest value anywhere."""
+    s, tree = _cut_scene(name)
+    lit = orc.lighting(s, threads=4)
+    lay = PR.for_scene(s)
+    ex = orc.Bounce(s, tree, lit, lay, sky_sh=s.sky_sh)
+    sc = orc.Bounce(s, tree, lit, lay, sky_sh=s.sky_sh, sender_cut=True)
+    for f in range(4):
+        a, b = ex.step(s.eye, threads=4)["lo_b"][:, 0, :3].copy(), sc.step(s.eye, threads=4)["lo_b"][:, 0, :3]
+    assert a.mean() > 0
+    assert (np.abs(b.mean(0) - a.mean(0)) <= 0.03 * a.mean(0)).all()
+    assert np.abs(b - a).max() <= 0.1 * a.max()
