@@ -294,7 +294,8 @@ typedef struct sl_probe_layout {
   uint32_t vols[32][4]; /* (part 0-31, nx, ny, nz): a grid over the part's rest-frame box serving its Gaussians */
 } sl_probe_layout;
 
-/* Lighting.initBounce (src/lighting.js:723-816) without the sender cut (?sendercut=0): after each update's shading the
+/* Lighting.initBounce (src/lighting.js:723-816), with every leaf a sender (?sendercut=0; the reference's default sender
+ * cut is sl_lighting_set_sender_cut): after each update's shading the
  * probe bounce runs one frame (encodeBounce :1018-1103; runtime/wgsl/bounce.wgsl, M39 stage 2): the Gaussians'
  * transfer SH2 (iso_xfer, on the first frame and near parts that moved), their light toward the probes for a quarter
  * of them (direct_dirs_emit + env_dirs), the tree's sums of it and their SH2 (node_leaf, node_up over depths
@@ -316,10 +317,25 @@ SL_API int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* layout,
 /* The environment's sky for the probes (src/environment.js:116-124; bounce.wgsl sky_radiance :148-160): n_coef (<= 16)
  * real SH coefficients, rgb, bands 0-3, seen by probe rays that leave the scene.  0 coefficients: no sky. */
 SL_API int sl_lighting_set_sky(sl_lighting* l, const float* sh_rgb, uint32_t n_coef);
+/* The sender cut (src/lighting.js senderCut, :411-412, 1057-1095; runtime/wgsl/bounce.wgsl sc_select .. node_sh2_sc
+ * :1448-1730; the reference's default): on (1), only the senders some probe's gather can resolve are lit.  Each frame
+ * in which a part moved (and the first) marks every node of the parts' trees top down: BELOW (never read), OPEN (some
+ * probe opens it), NODE (every probe uses it whole) or LEAF (a leaf under an open node).  The cut's leaves send as
+ * before (a quarter of them a frame); each cut node is lit as one two-sided Gaussian (nodeGaussians' record and V
+ * grid, src/lod.js:44-107; the shadow T of 8 leaves reached by mass-weighted descents, sc_shadow), its light plus the
+ * probes' SH2 at its centre through its two faces' transfer (sc_xfer, node_cut); node_up sums the open nodes only.
+ * A cut node refreshes its shadow and direct light in the frames node % 4 == frame % 4 (every cut node in a frame
+ * that re-selected), and the cut is not capped (the reference opens nodes past 2^18 a frame, in the order its atomics
+ * hand out slots).  Needs sl_lighting_set_probes, a tree at most 64 levels deep whose internal nodes all have
+ * children, and the renderer bound; off (0) returns to every leaf.  Setting the tree again turns it off. */
+SL_API int sl_lighting_set_sender_cut(sl_lighting* l, uint32_t on);
 /* Debug read-back of the bounce (synchronous; bytes from the start): what = 0 lo_b (3 float4 per Gaussian: toward
  * the eye, toward the probes, lanes), 1 lo_dir (float4 per Gaussian), 2 the transfer (3 float4 per Gaussian), 3 the
  * probes' SH2 (9 float4 per probe), 4 probe_data (2 float4 per probe and cell), 5 node_sh (14 words per node),
- * 6 node_acc (14 float4 per node). */
+ * 6 node_acc (14 float4 per node); with the sender cut on: 7 the marks (one word per node: 0 below, 1 open, 2 node,
+ * 3 leaf), 8 the cut nodes' transfer and direct light (8 float4 per internal node: each face's transfer t0-3, t4-7,
+ * (t8, exposure), then the faces' direct light), 9 their lamp T (float per internal node), 10 their distant-light T
+ * (float4 per internal node); entries of nodes off the cut hold what an earlier cut left. */
 SL_API int sl_lighting_read_bounce(sl_lighting* l, uint32_t what, void* dst, size_t bytes);
 
 /* encode(encoder, eye, timers, changed, still) (src/lighting.js:1258-1274) + Environment.encodeDirect

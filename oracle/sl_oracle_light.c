@@ -2249,6 +2249,7 @@ static void sc_shadow_one(const orc_bounce_in* in, uint32_t n, float* T_out, flo
     uint32_t m = n, h = sc_pcg(n * SC_SAMPLES + s);
     for (uint32_t it = 0; it < 64u && m >= G; it++) {
       const sl_node* nd = &in->nodes[m];
+      if (nd->child_hi <= nd->child_lo) break; /* no children to descend into: the sample counts T = 1 */
       float tot = 0.0f;
       for (uint32_t j = nd->child_lo; j < nd->child_hi; j++) tot += sc_mass(&in->nodes[in->kids[j]]);
       float u = sc_to_unit(h) * tot;
@@ -2262,8 +2263,8 @@ static void sc_shadow_one(const orc_bounce_in* in, uint32_t n, float* T_out, flo
       m = pick;
     }
     /* trees are at most 64 levels deep (checked where the cut is set up), so m is a leaf */
-    T += in->lamp_T[m];
-    for (int c = 0; c < 4; c++) E[c] += in->env_T[4u * m + c];
+    T += m < G ? in->lamp_T[m] : 1.0f;
+    for (int c = 0; c < 4; c++) E[c] += m < G ? in->env_T[4u * m + c] : 1.0f;
   }
   *T_out = T / (float)SC_SAMPLES;
   for (int c = 0; c < 4; c++) E_out[c] = E[c] / (float)SC_SAMPLES;

@@ -130,6 +130,7 @@ PROTOTYPES: dict[str, tuple] = {
     "sl_lighting_set_probes": (_I, [_P, _P, _U32, C.c_float, C.c_int]),
     "sl_lighting_set_sky": (_I, [_P, _P, _U32]),
     "sl_lighting_read_bounce": (_I, [_P, _U32, _P, C.c_size_t]),
+    "sl_lighting_set_sender_cut": (_I, [_P, _U32]),
     "sl_lighting_update": (_I, [_P, _P, _P, _U32, _P]),
     "sl_lighting_shade": (_I, [_P, _P, _P]),
     "sl_lighting_read": (_I, [_P, _P, _P, _P, _P]),

@@ -1,5 +1,5 @@
-// Probe bounce (runtime/wgsl/bounce.wgsl, the M39 stage-2 loop; host src/lighting.js:723-816, 1018-1103), the
-// reference's path without the sender cut (?sendercut=0): one frame per sl_lighting_update, in its dispatch order
+// Probe bounce (runtime/wgsl/bounce.wgsl, the M39 stage-2 loop; host src/lighting.js:723-816, 1018-1103): one frame
+// per sl_lighting_update, in its dispatch order
 //   xfer      iso_xfer (bounce.wgsl:993-1026): per Gaussian near something that moved (or on a forced refresh) the
 //             SH2 of its transfer iso_norm A(w) V(w) over the 128 world cells
 //   direct    direct_dirs_emit + env_dirs (bounce_direct.cu): a quarter of the Gaussians per frame, the light each
@@ -16,6 +16,9 @@
 //   bounce    bounce_sh (:1044-1095) with gloss_sh (:1102-1125) for the others: the 8 surrounding probes (trilinear x
 //             valid x Chebyshev with the 4x4x4 fallback; a movable part's own 8 probes; a static volume's grid) dotted
 //             with the Gaussian's transfer into lo_b
+// With the sender cut (sc_select .. node_sh2_sc, :1448-1730) the frame adds: on a re-selection sc_select per depth
+// (top down) and sc_xfer for the cut nodes; sc_shadow; the cut's leaves and nodes' direct light (bounce_direct.cu);
+// node_leaf on the cut's leaves; node_cut; node_up on the open nodes; node_sh2 zero under the cut.
 // The translation unit is compiled with --fmad=false and the deterministic transcendentals of sl_detmath.h, so the
 // CPU restatement reproduces it given the same light toward the probes (whose kernel is compiled for speed).
 // Near-field visibility is off (the reference's default).
@@ -379,9 +382,11 @@ __global__ void __launch_bounds__(kThreads) leaf_kernel(const __grid_constant__ 
                                                         const sl_gaussian* __restrict__ gs,
                                                         const float* __restrict__ leaf_w,
                                                         const float4* __restrict__ lo_dir,
-                                                        const float4* __restrict__ lo_b, float4* __restrict__ acc) {
+                                                        const float4* __restrict__ lo_b,
+                                                        const uint32_t* __restrict__ flag, float4* __restrict__ acc) {
   const uint32_t g = blockIdx.x * kThreads + threadIdx.x;
   if (g >= B.G) return;
+  if (flag && flag[g] != kScLeaf) return;  // node_leaf_list: with the sender cut, the cut's leaves only
   const sl_gaussian& G = gs[g];
   const float4 ld = lo_dir[g], lb = lo_b[3u * g + 1u];
   // the emitters' own part sends nothing into the probes (PP.refl.w, emitBounceFix: their light reaches the scene as
@@ -398,10 +403,11 @@ __global__ void __launch_bounds__(kThreads) leaf_kernel(const __grid_constant__ 
 __global__ void __launch_bounds__(kThreads) up_kernel(const sl_node* __restrict__ nodes,
                                                       const uint32_t* __restrict__ kids,
                                                       const uint32_t* __restrict__ list, uint32_t count,
-                                                      float4* __restrict__ acc) {
+                                                      const uint32_t* __restrict__ flag, float4* __restrict__ acc) {
   const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
   if (t >= count * 14u) return;
   const uint32_t i = list[t / 14u], k = t % 14u;
+  if (flag && flag[i] != kScOpen) return;  // node_up_sc: the open nodes only
   const uint32_t lo = nodes[i].child_lo, hi = nodes[i].child_hi;
   float4 s = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   for (uint32_t j = lo; j < hi; j++) {
@@ -416,9 +422,16 @@ __global__ void __launch_bounds__(kThreads) up_kernel(const sl_node* __restrict_
 
 // node_sh2: the 14-direction means fitted to SH2 (pinv), 27 halves in 14 words
 __global__ void __launch_bounds__(kThreads) sh2_kernel(uint32_t N, const float* __restrict__ tab,
-                                                       const float4* __restrict__ acc, uint32_t* __restrict__ node_sh) {
+                                                       const float4* __restrict__ acc,
+                                                       const uint32_t* __restrict__ flag,
+                                                       uint32_t* __restrict__ node_sh) {
   const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
   if (i >= N) return;
+  if (flag && flag[i] == kScBelow) {  // under the sender cut: the gather reads zero (the reference's null slot)
+#pragma unroll
+    for (int j = 0; j < 14; j++) node_sh[14u * i + (uint32_t)j] = 0u;
+    return;
+  }
   f3 L[14];
 #pragma unroll
   for (int k = 0; k < 14; k++) {
@@ -852,28 +865,314 @@ __global__ void __launch_bounds__(kThreads) dirs_kernel(const __grid_constant__ 
   lo_b[3u * g + 2u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
+// ---- the sender cut (bounce.wgsl:1448-1730) ------------------------------------------------------------------------
+
+// pcg_hash and to_unit (common.wgsl:98-104); sc_face (common.wgsl:342-345, SC_FACE_K 1)
+__device__ __forceinline__ uint32_t pcg_hash(uint32_t x) {
+  const uint32_t s = x * 747796405u + 2891336453u;
+  const uint32_t w = ((s >> ((s >> 28u) + 4u)) ^ s) * 277803737u;
+  return (w >> 22u) ^ w;
+}
+__device__ __forceinline__ float to_unit(uint32_t x) { return (float)(x >> 8u) * (1.0f / 16777216.0f); }
+__device__ __forceinline__ float sc_face(float c) { return clampf(c * 1.0f, -1.0f, 1.0f); }
+__device__ __forceinline__ float sc_mass(const sl_node* __restrict__ n) {
+  return n->kappa / sqrtf(fmaxf(sym_det(F3(n->cinv_diag[0], n->cinv_diag[1], n->cinv_diag[2]),
+                                        F3(n->cinv_off[0], n->cinv_off[1], n->cinv_off[2])),
+                                1e-30f));
+}
+// a cut node refreshes its shadow and direct light when the cut was re-selected, else a quarter of them a frame
+__device__ __forceinline__ bool sc_now(const BounceParams& B, uint32_t n) {
+  return B.sc_reselect != 0u || n % 4u == B.frame % 4u;
+}
+
+// sc_probe_dist (bounce.wgsl:1478-1513): the smallest (distance - margin) from world point P to the gather centres of
+// the probes that see part `own` (the room's nearest 2x2x2 block centre less the block radius; the terrain's 3 x 3
+// columns around P; each movable part's 8 probes but own's; each static volume's nearest grid probe).  The gathers
+// of probes that cut around themselves keep no margin (vol_info.y 0).  WGSL round is half to even: rintf.
+__device__ float sc_probe_dist(const BounceParams& B, const float* __restrict__ ground,
+                               const sl_node* __restrict__ tnodes, const sl_part* __restrict__ parts, f3 P,
+                               uint32_t own) {
+  float best = 1e30f;
+  if (!B.terrain) {
+    const float Pv[3] = {P.x, P.y, P.z};
+    float b[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const float nb = (float)((B.dims[a] + 1u) / 2u);
+      b[a] = clampf(rintf(((Pv[a] - B.lo[a]) / fmaxf(B.step[a], 1e-6f) - 0.5f) * 0.5f), 0.0f, nb - 1.0f);
+    }
+    const f3 cen = F3(B.lo[0] + B.step[0] * (2.0f * b[0] + 0.5f), B.lo[1] + B.step[1] * (2.0f * b[1] + 0.5f),
+                      B.lo[2] + B.step[2] * (2.0f * b[2] + 0.5f));
+    best = len3(sub3(P, cen)) - B.brad;
+  } else {
+    const int ci = (int)clampf(rintf((P.x - B.lo[0]) / fmaxf(B.step[0], 1e-6f)), -1e9f, 1e9f);
+    const int cj = (int)clampf(rintf((P.y - B.lo[1]) / fmaxf(B.step[1], 1e-6f)), -1e9f, 1e9f);
+    for (int di = -1; di <= 1; di++) {
+      for (int dj = -1; dj <= 1; dj++) {
+        const int ii = min(max(ci + di, 0), (int)B.dims[0] - 1), jj = min(max(cj + dj, 0), (int)B.dims[1] - 1);
+        const uint32_t i = (uint32_t)ii, j = (uint32_t)jj;
+        const float x = B.lo[0] + B.step[0] * (float)i, y = B.lo[1] + B.step[1] * (float)j;
+        const float gz = ground_at(B, ground, i, j);
+        for (uint32_t k = 0; k < B.dims[2]; k++) best = fminf(best, len3(sub3(P, F3(x, y, gz + B.levels[k]))));
+      }
+    }
+  }
+  for (uint32_t q = 0; q < B.part_count && q < 32u; q++) {
+    if (q == own) continue;
+    const float* xf = parts[q].xf;
+    if (part_probe_part(B, parts, q)) {
+      f3 c, h;
+      part_frame(tnodes, parts, q, c, h);
+      if (len3(sub3(P, xf_point(xf, c))) - len3(h) >= best) continue;
+      for (uint32_t k = 0; k < 8u; k++)
+        best = fminf(best, len3(sub3(P, probe_pos(B, ground, tnodes, parts, B.NL + q * 8u + k))));
+    } else if (has_vol(B, q)) {
+      f3 c, h;
+      vol_frame(tnodes, parts, q, c, h);
+      const f3 lp = xf_dir_inv(xf, sub3(P, F3(xf[3], xf[7], xf[11])));
+      const float lv[3] = {lp.x, lp.y, lp.z}, cv[3] = {c.x, c.y, c.z}, hv[3] = {h.x, h.y, h.z};
+      float g[3];
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        const float d = (float)B.vol_dims[q][a];
+        const float span = fmaxf(d - 1.0f, 1.0f);
+        const float ijk = clampf(rintf((lv[a] - cv[a] + hv[a]) / fmaxf(2.0f * hv[a], 1e-6f) * span), 0.0f, d - 1.0f);
+        g[a] = cv[a] - hv[a] + 2.0f * hv[a] * ijk / span;
+      }
+      best = fminf(best, len3(sub3(lp, F3(g[0], g[1], g[2]))));
+    }
+  }
+  return best;
+}
+
+// sc_select (bounce.wgsl:1528-1545) over one depth, the depth above already marked; the cut nodes join sc_list
+__global__ void __launch_bounds__(kThreads) sc_select_kernel(const __grid_constant__ BounceParams B,
+                                                             const sl_node* __restrict__ tnodes,
+                                                             const sl_part* __restrict__ parts,
+                                                             const float* __restrict__ ground,
+                                                             const uint32_t* __restrict__ parent,
+                                                             const uint32_t* __restrict__ level, uint32_t count,
+                                                             uint32_t* __restrict__ flag, uint32_t* __restrict__ list) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= count) return;
+  const uint32_t n = level[t];
+  const sl_node& nd = tnodes[n];
+  const uint32_t q = nd.part;
+  uint32_t m;
+  if (q >= B.part_count) {
+    m = kScBelow;  // scene nodes above the parts: the gather starts at part roots
+  } else if (parts[q].root != n && (parent[n] == kNone || flag[parent[n]] != kScOpen)) {
+    m = kScBelow;
+  } else if (n < B.G) {
+    m = kScLeaf;
+  } else {
+    const f3 P = xf_point(parts[q].xf, F3(nd.mean[0], nd.mean[1], nd.mean[2]));
+    m = sc_probe_dist(B, ground, tnodes, parts, P, q) <= kProbeTheta * nd.smax ? kScOpen : kScNode;
+  }
+  flag[n] = m;
+  if (m == kScNode) list[1u + atomicAdd(&list[0], 1u)] = n;
+}
+
+// sc_xfer (bounce.wgsl:1640-1672): per cut node and face of its short axis, the SH2 transfer from its own V grid and
+// the face's exposure (at least 1% of the whole): 6 vec4, face 0 t0-3, t4-7, (t8, S), then face 1
+__global__ void __launch_bounds__(kThreads) sc_xfer_kernel(const __grid_constant__ BounceParams B,
+                                                           const uint32_t* __restrict__ list,
+                                                           const sl_node* __restrict__ tnodes,
+                                                           const sl_gaussian* __restrict__ sc_gs,
+                                                           const sl_vgrid* __restrict__ sc_vg,
+                                                           const sl_part* __restrict__ parts,
+                                                           const float* __restrict__ tab, float4* __restrict__ X) {
+  const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= list[0]) return;
+  const uint32_t n = list[1u + i], r = n - B.G;
+  const sl_gaussian& G = sc_gs[r];
+  const Leaf nd = load_leaf(&tnodes[n]);
+  const float* xf = parts[G.part_surface & 0xFFFFu].xf;
+  const f3 nrm = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]).c[0];
+  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
+  const sl_vgrid& vg = sc_vg[r];
+  float t[20];
+#pragma unroll
+  for (int m = 0; m < 20; m++) t[m] = 0.0f;
+  float S0 = 0.0f;
+  for (uint32_t c = 0; c < kCells; c++) {
+    const f3 w = cell_dir(tab, c);
+    const f3 u = xf_dir_inv(xf, w);
+    const float a = footprint(nd, s3 * s3, u) * cell_omega(tab, c);
+    S0 += a;
+    const float v = vgrid_lookup(vg, u);
+    if (v <= 0.0f) continue;
+    const float h = 0.5f + 0.5f * sc_face(dot3(u, nrm));
+    float y[9];
+    sh2_basis(w, y);
+#pragma unroll
+    for (int m = 0; m < 9; m++) {
+      t[m] += a * v * h * y[m];
+      t[10 + m] += a * v * (1.0f - h) * y[m];
+    }
+    t[9] += a * v * h;
+    t[19] += a * v * (1.0f - h);
+  }
+  const float Smin = fmaxf(0.5f * 0.02f * S0, 1e-30f);  // iso_init.wgsl ISO_EPS, per face
+#pragma unroll
+  for (int f = 0; f < 2; f++) {
+    const float* o = t + 10 * f;
+    X[8u * r + 3u * (uint32_t)f] = make_float4(o[0], o[1], o[2], o[3]);
+    X[8u * r + 3u * (uint32_t)f + 1u] = make_float4(o[4], o[5], o[6], o[7]);
+    X[8u * r + 3u * (uint32_t)f + 2u] = make_float4(o[8], fmaxf(o[9], Smin), 0.0f, 0.0f);
+  }
+}
+
+// sc_shadow (bounce.wgsl:1566-1625): the mean lamp T and distant-light T of 8 leaves under the cut node, each reached
+// by a descent that picks a child with probability by mass (a fixed hash per node and sample).  A Gaussian carries
+// one lamp T here, so the reference's per-lamp slots reduce to that mean.
+__global__ void __launch_bounds__(kThreads) sc_shadow_kernel(const __grid_constant__ BounceParams B,
+                                                             const uint32_t* __restrict__ list,
+                                                             const sl_node* __restrict__ tnodes,
+                                                             const uint32_t* __restrict__ kids,
+                                                             const float* __restrict__ lamp_T,
+                                                             const float4* __restrict__ env_T,
+                                                             float* __restrict__ sc_T, float4* __restrict__ sc_E) {
+  const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= list[0]) return;
+  const uint32_t n = list[1u + i];
+  if (!sc_now(B, n)) return;
+  float T = 0.0f;
+  float4 E = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  for (uint32_t s = 0; s < 8u; s++) {
+    uint32_t m = n, h = pcg_hash(n * 8u + s);
+    for (uint32_t it = 0; it < 64u && m >= B.G; it++) {
+      const uint32_t lo = tnodes[m].child_lo, hi = tnodes[m].child_hi;
+      if (hi <= lo) break;  // no children to descend into: the sample counts T = 1
+      float tot = 0.0f;
+      for (uint32_t j = lo; j < hi; j++) tot += sc_mass(&tnodes[kids[j]]);
+      float u = to_unit(h) * tot;
+      h = pcg_hash(h);
+      uint32_t pick = kids[lo];
+      for (uint32_t j = lo; j < hi; j++) {
+        pick = kids[j];
+        u -= sc_mass(&tnodes[kids[j]]);
+        if (u <= 0.0f) break;
+      }
+      m = pick;
+    }
+    // the tree is at most 64 levels deep (sl_lighting_set_sender_cut), so m is a leaf
+    const float4 e = m < B.G ? env_T[m] : make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    T += m < B.G ? lamp_T[m] : 1.0f;
+    E.x += e.x;
+    E.y += e.y;
+    E.z += e.z;
+    E.w += e.w;
+  }
+  const uint32_t r = n - B.G;
+  sc_T[r] = T / 8.0f;
+  sc_E[r] = make_float4(E.x / 8.0f, E.y / 8.0f, E.z / 8.0f, E.w / 8.0f);
+}
+
+// node_cut (bounce.wgsl:1682-1716): a cut node as one sender, each face's light (its direct light plus the probes'
+// SH2 at its centre through the face's transfer, over the face's exposure) shown toward each D_k by its share there
+__global__ void __launch_bounds__(kThreads) node_cut_kernel(const __grid_constant__ BounceParams B,
+                                                            const uint32_t* __restrict__ list,
+                                                            const sl_node* __restrict__ tnodes,
+                                                            const sl_gaussian* __restrict__ sc_gs,
+                                                            const sl_vgrid* __restrict__ sc_vg,
+                                                            const sl_part* __restrict__ parts,
+                                                            const float* __restrict__ tab,
+                                                            const float* __restrict__ ground,
+                                                            const float4* __restrict__ pd,
+                                                            const float4* __restrict__ probe_sh,
+                                                            const float4* __restrict__ X, float4* __restrict__ acc) {
+  const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= list[0]) return;
+  const uint32_t n = list[1u + i], r = n - B.G;
+  const sl_gaussian& G = sc_gs[r];
+  const Leaf nd = load_leaf(&tnodes[n]);
+  const uint32_t own = G.part_surface & 0xFFFFu;
+  const float* xf = parts[own].xf;
+  const f3 P = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  const f3 nrm = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]).c[0];
+  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
+  const Weights pw = weights_for(B, ground, pd, tnodes, parts, P, own);
+  f3 Lsh[9];
+#pragma unroll
+  for (int m = 0; m < 9; m++) Lsh[m] = F3(0.0f, 0.0f, 0.0f);
+  for (int k = 0; k < 8; k++) {
+    const float w = pw.w[k];
+    if (w <= 0.0f) continue;
+#pragma unroll
+    for (int m = 0; m < 9; m++) {
+      const float4 c = probe_sh[9u * pw.pid[k] + (uint32_t)m];
+      Lsh[m] = add3(Lsh[m], mul3(F3(c.x, c.y, c.z), w));
+    }
+  }
+  const f3 alb = F3(G.albedo[0], G.albedo[1], G.albedo[2]);
+  f3 col[2];
+#pragma unroll
+  for (int f = 0; f < 2; f++) {
+    const float4 a = X[8u * r + 3u * (uint32_t)f], b = X[8u * r + 3u * (uint32_t)f + 1u],
+                 c = X[8u * r + 3u * (uint32_t)f + 2u], d = X[8u * r + 6u + (uint32_t)f];
+    const float x[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
+    f3 Bv = mul3(Lsh[0], x[0]);
+#pragma unroll
+    for (int m = 1; m < 9; m++) Bv = add3(Bv, mul3(Lsh[m], x[m]));
+    col[f] = div3(mul3v(alb, max0(add3(F3(d.x, d.y, d.z), max0(Bv)))), c.y);
+  }
+  const bool dark = own == B.dark_part;
+  const sl_vgrid& vg = sc_vg[r];
+  for (int k = 0; k < 14; k++) {
+    const f3 wo = xf_dir_inv(xf, ld3(tab + kTabD14 + 3 * k));
+    const float w = footprint(nd, s3 * s3, wo) * vgrid_lookup(vg, wo);
+    const float h = 0.5f + 0.5f * sc_face(dot3(wo, nrm));
+    const f3 L = dark ? F3(0.0f, 0.0f, 0.0f) : add3(mul3(col[0], h), mul3(col[1], 1.0f - h));
+    acc[14u * n + (uint32_t)k] = make_float4(L.x * w, L.y * w, L.z * w, w);
+  }
+}
+
 inline uint32_t blocks(uint64_t n) { return (uint32_t)((n + kThreads - 1) / kThreads); }
 
 }  // namespace
 
 cudaError_t launch_bounce_frame(const BounceParams& B, const ShadeParams& SH, const BounceBuffers& D,
                                 const std::vector<uint32_t>& level_off, const std::vector<uint32_t>& level_cnt,
+                                const std::vector<uint32_t>& sc_off, const std::vector<uint32_t>& sc_cnt,
                                 cudaStream_t s) {
   if (B.G == 0) return cudaSuccess;
   // iso_xfer only where something may have changed a transfer: a forced refresh or a part that moved (lighting.js
   // :1036-1039 skips the dispatch otherwise)
   if (B.force || B.moved_mask)
     xfer_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.nodes, D.vgrid, D.parts, D.tab, D.xfer, D.leaf_w);
+  // the sender cut: selected again top down when a part moved (or on its first frame), with the cut nodes'
+  // transfer; then the shadow T of the cut nodes that refresh this frame.  Its kernels run over every internal node's
+  // slot and stop past the cut's count.
+  const bool sc = B.sender_cut != 0u;
+  const uint32_t I = B.N - B.G;
+  const uint32_t* flag = sc ? D.sc_flag : nullptr;
+  if (sc && B.sc_reselect) {
+    cudaMemsetAsync(D.sc_list, 0, 4, s);
+    for (size_t d = 0; d < sc_cnt.size(); d++) {
+      if (sc_cnt[d] == 0) continue;
+      sc_select_kernel<<<blocks(sc_cnt[d]), kThreads, 0, s>>>(B, D.tnodes, D.parts, D.ground, D.parent,
+                                                              D.sc_level + sc_off[d], sc_cnt[d], D.sc_flag, D.sc_list);
+    }
+    if (I) sc_xfer_kernel<<<blocks(I), kThreads, 0, s>>>(B, D.sc_list, D.tnodes, D.sc_gs, D.sc_vg, D.parts, D.tab,
+                                                          D.sc_X);
+  }
+  if (sc && I)
+    sc_shadow_kernel<<<blocks(I), kThreads, 0, s>>>(B, D.sc_list, D.tnodes, D.kids, D.lamp_T, D.env_T, D.sc_T,
+                                                    D.sc_E);
   cudaError_t e = launch_bounce_direct(B, SH, D, s);
   if (e != cudaSuccess) return e;
-  leaf_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.leaf_w, D.lo_dir, D.lo_b, D.node_acc);
+  leaf_kernel<<<blocks(B.G), kThreads, 0, s>>>(B, D.gs, D.leaf_w, D.lo_dir, D.lo_b, flag, D.node_acc);
+  if (sc && I)
+    node_cut_kernel<<<blocks(I), kThreads, 0, s>>>(B, D.sc_list, D.tnodes, D.sc_gs, D.sc_vg, D.parts, D.tab,
+                                                   D.ground, D.probe_data, D.probe_sh, D.sc_X, D.node_acc);
   for (int d = (int)level_cnt.size() - 1; d >= 1; d--) {
     const uint32_t n = level_cnt[(size_t)d];
     if (n == 0) continue;
-    up_kernel<<<blocks(14ull * n), kThreads, 0, s>>>(D.tnodes, D.kids, D.up_list + level_off[(size_t)d], n,
+    up_kernel<<<blocks(14ull * n), kThreads, 0, s>>>(D.tnodes, D.kids, D.up_list + level_off[(size_t)d], n, flag,
                                                      D.node_acc);
   }
-  sh2_kernel<<<blocks(B.N), kThreads, 0, s>>>(B.N, D.tab, D.node_acc, D.node_sh);
+  sh2_kernel<<<blocks(B.N), kThreads, 0, s>>>(B.N, D.tab, D.node_acc, flag, D.node_sh);
   if (B.NP) {
     gather_kernel<<<blocks((uint64_t)B.NP * kCells), kThreads, 0, s>>>(B, D.tnodes, D.kids, D.vgrid, D.parts, D.tab,
                                                                        D.ground, D.node_sh, D.probe_data,

@@ -41,10 +41,12 @@ __global__ void __launch_bounds__(kThreads, 4) direct_kernel(const __grid_consta
                                                              const float* __restrict__ lamp_T,
                                                              const float4* __restrict__ env_T,
                                                              const uint32_t* __restrict__ quarter, uint32_t count,
+                                                             const uint32_t* __restrict__ flag,
                                                              float4* __restrict__ lo_dir) {
   const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
   if (i >= count) return;
   const uint32_t g = quarter[i];
+  if (flag && flag[g] != kScLeaf) return;  // direct_dirs_emit_sc / env_dirs_sc: the sender cut's leaves only
   const sl_gaussian& G = gs[g];
   const Leaf nd = load_leaf(&nodes[g]);
   uint32_t mi = G.flags & 0xFFFFu;
@@ -157,14 +159,112 @@ __global__ void __launch_bounds__(kThreads, 4) direct_kernel(const __grid_consta
   lo_dir[g] = make_float4(c.x, c.y, c.z, 0.0f);
 }
 
+// direct_dirs_nodes_sc + env_dirs_nodes_sc (emissive.wgsl:1032-1064, environment.wgsl:329-351): the light each face of
+// a cut node (its short axis' two sides) catches, before albedo and exposure, from the emitters' light cut (matte:
+// shininess left out of the senders) times its sampled lamp T, then the distant lights' catch with its sampled T
+__global__ void __launch_bounds__(kThreads, 4) direct_nodes_kernel(const __grid_constant__ BounceParams B,
+                                                                   const __grid_constant__ ShadeParams SH,
+                                                                   const uint32_t* __restrict__ list,
+                                                                   const sl_node* __restrict__ tnodes,
+                                                                   const sl_gaussian* __restrict__ sc_gs,
+                                                                   const sl_vgrid* __restrict__ sc_vg,
+                                                                   const sl_part* __restrict__ parts,
+                                                                   const sl_material* __restrict__ mats,
+                                                                   const float* __restrict__ tree,
+                                                                   const float* __restrict__ sc_T,
+                                                                   const float4* __restrict__ sc_E,
+                                                                   float4* __restrict__ X) {
+  const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= list[0]) return;
+  const uint32_t n = list[1u + i];
+  if (!(B.sc_reselect != 0u || n % 4u == B.frame % 4u)) return;
+  const uint32_t r = n - B.G;
+  const sl_gaussian& G = sc_gs[r];
+  const Leaf nd = load_leaf(&tnodes[n]);
+  const float* xf = parts[G.part_surface & 0xFFFFu].xf;
+  const f3 nrm = quat_matrix(G.quat[0], G.quat[1], G.quat[2], G.quat[3]).c[0];
+  const float s3 = G.scale[0] * G.scale[1] * G.scale[2];
+  const float detC = s3 * s3;
+  const f3 P = xf_point(xf, F3(G.mu[0], G.mu[1], G.mu[2]));
+  const sl_vgrid& vg = sc_vg[r];
+  f3 c0 = F3(0.0f, 0.0f, 0.0f), c1 = F3(0.0f, 0.0f, 0.0f);
+  if (SH.n_emit) {
+    uint32_t node = SH.root;
+    for (uint32_t guard = 0; node != kNone && guard < (1u << 16); guard++) {
+      const float* e = tree + 24u * node;
+      const uint32_t child_lo = __float_as_uint(e[11]), child_hi = __float_as_uint(e[15]);
+      const uint32_t skip = __float_as_uint(e[7]);
+      const f3 emean = F3(e[0], e[1], e[2]);
+      bool use;
+      if (child_lo == kNone || SH.mode == 0u) {
+        use = child_lo == kNone;
+      } else {
+        const f3 d = sub3(P, emean);
+        use = dot3(d, d) > SH.theta * SH.theta * e[3] * e[3];
+      }
+      if (!use) {
+        node = (child_lo != kNone && __float_as_uint(e[19]) == 0u) ? child_hi : skip;
+        continue;
+      }
+      node = skip;
+      const f3 d = sub3(emean, P);
+      const float d2 = dot3(d, d);
+      if (d2 < 1e-8f) continue;
+      const f3 ww = div3(d, sqrtf(d2));
+      const f3 wi = xf_dir_inv(xf, ww);
+      const float vi = vgrid_lookup(vg, wi);
+      if (vi <= 1e-7f) continue;
+      const f3 mw = mul3(ww, -1.0f);
+      float s = 1.0f;
+      if (SH.one_sided) {
+        const float cs = dot3(mw, ld3(SH.normal));
+        s = SH.edge_soft > 0.0f ? smoothstepf(-SH.edge_soft, SH.edge_soft, cs) : (cs > 0.0f ? 1.0f : 0.0f);
+      }
+      const float mq = sqrtf(fmaxf(dot3(mw, sym_mul(F3(e[4], e[5], e[6]), F3(e[8], e[9], e[10]), mw)), 0.0f));
+      const f3 I = mul3(F3(e[12], e[13], e[14]), s * SH.scale * mq);
+      const f3 light = mul3(I, vi * footprint(nd, detC, wi) / d2);
+      const float h = 0.5f + 0.5f * clampf(dot3(wi, nrm), -1.0f, 1.0f);
+      c0 = add3(c0, mul3(light, h));
+      c1 = add3(c1, mul3(light, 1.0f - h));
+    }
+  }
+  const float T = sc_T[r];
+  c0 = mul3(c0, T);
+  c1 = mul3(c1, T);
+  uint32_t mi = G.flags & 0xFFFFu;
+  const uint32_t mtop = (SH.material_count > 1u ? SH.material_count : 1u) - 1u;
+  mi = mi < mtop ? mi : mtop;
+  if (SH.n_lights && (mats[mi].flags & 1u) == 0u) {
+    const float4 et = sc_E[r];
+    const float Tk[4] = {et.x, et.y, et.z, et.w};
+    for (uint32_t k = 0; k < SH.n_lights && k < 4u; k++) {
+      const f3 wi = xf_dir_inv(xf, ld3(SH.lights[k].dir));
+      const float v = vgrid_lookup(vg, wi);
+      if (v <= 1e-7f) continue;
+      const f3 c = mul3(ld3(SH.lights[k].irr), Tk[k] * v * footprint(nd, detC, wi));
+      const float h = 0.5f + 0.5f * clampf(dot3(wi, nrm), -1.0f, 1.0f);
+      c0 = add3(c0, mul3(c, h));
+      c1 = add3(c1, mul3(c, 1.0f - h));
+    }
+  }
+  X[8u * r + 6u] = make_float4(c0.x, c0.y, c0.z, 0.0f);
+  X[8u * r + 7u] = make_float4(c1.x, c1.y, c1.z, 0.0f);
+}
+
 }  // namespace
 
 cudaError_t launch_bounce_direct(const BounceParams& B, const ShadeParams& SH, const BounceBuffers& D, cudaStream_t s) {
   const uint32_t q = B.frame % 4u, count = D.quarter_off[q + 1] - D.quarter_off[q];
-  if (count == 0) return cudaSuccess;
-  direct_kernel<<<(count + kThreads - 1) / kThreads, kThreads, 0, s>>>(B, SH, D.gs, D.nodes, D.vgrid, D.parts, D.mats,
-                                                                      D.tree, D.lamp_T, D.env_T,
-                                                                      D.quarters + D.quarter_off[q], count, D.lo_dir);
+  const bool sc = B.sender_cut != 0u;
+  if (count)
+    direct_kernel<<<(count + kThreads - 1) / kThreads, kThreads, 0, s>>>(
+        B, SH, D.gs, D.nodes, D.vgrid, D.parts, D.mats, D.tree, D.lamp_T, D.env_T, D.quarters + D.quarter_off[q],
+        count, sc ? D.sc_flag : nullptr, D.lo_dir);
+  const uint32_t I = B.N - B.G;
+  if (sc && I)
+    direct_nodes_kernel<<<(I + kThreads - 1) / kThreads, kThreads, 0, s>>>(B, SH, D.sc_list, D.tnodes, D.sc_gs,
+                                                                          D.sc_vg, D.parts, D.mats, D.tree, D.sc_T,
+                                                                          D.sc_E, D.sc_X);
   return cudaGetLastError();
 }
 

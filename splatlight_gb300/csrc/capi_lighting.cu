@@ -552,7 +552,8 @@ int sl_lighting_destroy(sl_lighting* l) {
                        &l->lm_acc, &l->lm_mip, &l->sm_acc, &l->sm_mip, &l->sm_layers, &l->sm_dirty, &l->order,
                        &l->g_blur, &l->n_blur, &l->tree_nodes, &l->node_parent, &l->kids, &l->bn_tab,
                        &l->bn_ground, &l->bn_up, &l->probe_data, &l->probe_sh, &l->xfer, &l->lo_dir, &l->lo_b,
-                       &l->node_acc, &l->node_sh, &l->bn_quarters, &l->bn_leaf_w, &l->probe_hist};
+                       &l->node_acc, &l->node_sh, &l->bn_quarters, &l->bn_leaf_w, &l->probe_hist,
+                       &l->sc_level, &l->sc_gs, &l->sc_vg, &l->sc_flag, &l->sc_X, &l->sc_T, &l->sc_E, &l->sc_list};
   for (sl::DevBuf* b : all) b->release();
   delete l;
   return SL_OK;
@@ -680,7 +681,9 @@ int sl_lighting_set_tree(sl_lighting* l, const sl_node* nodes, uint32_t n_nodes,
     l->tree_part[i] = nodes[i].part;
   }
   l->n_tree = n_nodes;
+  l->n_kids = n_kids;
   l->bounce_on = false;  // the probes are laid over a tree: set them again
+  l->bn_sc = false;      // so is the sender cut's node data
   l->blur_init = false;
   l->lm_dirty = true;
   l->sm_dirty_all = true;
@@ -943,7 +946,7 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
                              l->tree.as<float>(), l->lamp_T.as<float>(), l->env_T.as<float4>(), l->order.as<uint32_t>(),
                              l->colour.as<float4>(), G, s),
                 "shade");
-  if (l->bounce_on) {  // the probe bounce after the shading (lighting.js encodeBounce, ?sendercut=0)
+  if (l->bounce_on) {  // the probe bounce after the shading (lighting.js encodeBounce)
     for (uint32_t q = 0; q < P; q++)
       if (r->parts[q].root != 0xFFFFFFFFu && r->parts[q].root >= l->n_tree)
         return fail(SL_ERR_INVALID_ARG, "a part's tree root lies outside the tree set by sl_lighting_set_tree");
@@ -957,6 +960,8 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
     B.has_sky = l->has_sky ? 1u : 0u;
     B.dark_part = l->bn_emit_dark ? l->skip_part : 0xFFFFFFFFu;
     B.asg_cells = l->asg ? 1u : 0u;
+    B.sender_cut = l->bn_sc ? 1u : 0u;
+    B.sc_reselect = l->bn_sc && (l->bn_sc_stale || moved_mask != 0u) ? 1u : 0u;
     memcpy(B.sky, l->sky, sizeof(B.sky));
     for (int k = 0; k < 3; k++) B.eye[k] = eye[k];
     ShadeParams SHd;
@@ -986,8 +991,22 @@ int sl_lighting_update(sl_lighting* l, const float* eye, const float* forward, u
     D.probe_data = l->probe_data.as<float4>();
     D.probe_sh = l->probe_sh.as<float4>();
     D.node_sh = l->node_sh.as<uint32_t>();
-    SL_CHECK_CUDA(launch_bounce_frame(B, SHd, D, l->bn_level_off, l->bn_level_cnt, s), "probe bounce");
+    if (l->bn_sc) {
+      D.sc_level = l->sc_level.as<uint32_t>();
+      D.parent = l->node_parent.as<uint32_t>();
+      D.sc_gs = l->sc_gs.as<sl_gaussian>();
+      D.sc_vg = l->sc_vg.as<sl_vgrid>();
+      D.sc_flag = l->sc_flag.as<uint32_t>();
+      D.sc_X = l->sc_X.as<float4>();
+      D.sc_T = l->sc_T.as<float>();
+      D.sc_E = l->sc_E.as<float4>();
+      D.sc_list = l->sc_list.as<uint32_t>();
+    }
+    SL_CHECK_CUDA(launch_bounce_frame(B, SHd, D, l->bn_level_off, l->bn_level_cnt, l->sc_level_off, l->sc_level_cnt,
+                                      s),
+                  "probe bounce");
     l->bn_first = false;
+    if (B.sc_reselect) l->bn_sc_stale = false;
     l->bn_frame++;
   }
   return SL_OK;
@@ -1139,6 +1158,7 @@ int sl_lighting_set_probes(sl_lighting* l, const sl_probe_layout* lay, uint32_t 
   l->bn_blend = blend;
   l->bn_emit_dark = emitters_dark != 0;
   l->bn_first = true;
+  l->bn_sc_stale = true;  // the cut is selected over the new probes
   l->bn_frame = 0;
   l->bounce_on = true;
   if (l->r && l->r->lighting == l) l->r->lo_b = l->lo_b.as<float4>();
@@ -1155,13 +1175,85 @@ int sl_lighting_set_sky(sl_lighting* l, const float* sh_rgb, uint32_t n_coef) {
   return SL_OK;
 }
 
+int sl_lighting_set_sender_cut(sl_lighting* l, uint32_t on) {
+  if (!l) return fail(SL_ERR_INVALID_ARG, "null argument");
+  if (!on) {
+    l->bn_sc = false;
+    return SL_OK;
+  }
+  if (!l->bounce_on) return fail(SL_ERR_INVALID_ARG, "the sender cut selects over the probes: sl_lighting_set_probes first");
+  if (!l->r) return fail(SL_ERR_INVALID_ARG, "the sender cut needs the renderer bound (its Gaussians)");
+  cudaSetDevice(l->device);
+  const uint32_t G = l->count, N = l->n_tree;
+  std::vector<sl_node> nodes(N);
+  std::vector<uint32_t> kids(l->n_kids);
+  std::vector<sl_gaussian> gs(G);
+  std::vector<sl_vgrid> vg(G);
+  SL_CHECK_CUDA(cudaDeviceSynchronize(), "sync");
+  SL_CHECK_CUDA(cudaMemcpy(nodes.data(), l->tree_nodes.ptr, sizeof(sl_node) * (size_t)N, cudaMemcpyDeviceToHost), "tree");
+  if (l->n_kids)
+    SL_CHECK_CUDA(cudaMemcpy(kids.data(), l->kids.ptr, 4ull * l->n_kids, cudaMemcpyDeviceToHost), "kids");
+  SL_CHECK_CUDA(cudaMemcpy(gs.data(), l->r->gaussians.ptr, sizeof(sl_gaussian) * (size_t)G, cudaMemcpyDeviceToHost),
+                "gaussians");
+  SL_CHECK_CUDA(cudaMemcpy(vg.data(), l->vgrid.ptr, sizeof(sl_vgrid) * (size_t)G, cudaMemcpyDeviceToHost), "vgrid");
+  // sc_shadow's descents take at most 64 steps, and each picks among a node's children
+  uint32_t maxd = 0;
+  for (uint32_t n = 0; n < N; n++) {
+    maxd = std::max(maxd, nodes[n].depth);
+    if (n >= G && nodes[n].part != 0xFFFFFFFFu && nodes[n].child_hi <= nodes[n].child_lo)
+      return fail(SL_ERR_INVALID_ARG, "the sender cut needs every internal node of a part to have children");
+  }
+  if (maxd > 64u) return fail(SL_ERR_INVALID_ARG, "the sender cut's shadow descents reach 64 levels: tree too deep");
+  std::vector<sl_gaussian> recs;
+  std::vector<sl_vgrid> nvg;
+  int rc = sl::node_records(gs.data(), G, nodes.data(), N, kids.data(), l->n_kids, recs, vg.data(), &nvg);
+  if (rc != SL_OK) return rc;
+  // sc_select's levels: every node by depth, index order within a depth
+  std::vector<std::vector<uint32_t>> by(maxd + 1);
+  for (uint32_t n = 0; n < N; n++) by[nodes[n].depth].push_back(n);
+  std::vector<uint32_t> level;
+  level.reserve(N);
+  l->sc_level_off.assign(maxd + 1, 0);
+  l->sc_level_cnt.assign(maxd + 1, 0);
+  for (uint32_t d = 0; d <= maxd; d++) {
+    l->sc_level_off[d] = (uint32_t)level.size();
+    l->sc_level_cnt[d] = (uint32_t)by[d].size();
+    level.insert(level.end(), by[d].begin(), by[d].end());
+  }
+  const size_t I = N - G;
+  SL_CHECK_CUDA(l->sc_level.ensure(4ull * N + 16), "sender cut");
+  SL_CHECK_CUDA(l->sc_gs.ensure(sizeof(sl_gaussian) * I + 16), "sender cut");
+  SL_CHECK_CUDA(l->sc_vg.ensure(sizeof(sl_vgrid) * I + 16), "sender cut");
+  SL_CHECK_CUDA(l->sc_flag.ensure(4ull * N + 16), "sender cut");
+  SL_CHECK_CUDA(l->sc_X.ensure(128ull * I + 16), "sender cut");
+  SL_CHECK_CUDA(l->sc_T.ensure(4ull * I + 16), "sender cut");
+  SL_CHECK_CUDA(l->sc_E.ensure(16ull * I + 16), "sender cut");
+  SL_CHECK_CUDA(l->sc_list.ensure(4ull * I + 16), "sender cut");
+  if (N) SL_CHECK_CUDA(cudaMemcpy(l->sc_level.ptr, level.data(), 4ull * N, cudaMemcpyHostToDevice), "sender cut");
+  if (I) {
+    SL_CHECK_CUDA(cudaMemcpy(l->sc_gs.ptr, recs.data(), sizeof(sl_gaussian) * I, cudaMemcpyHostToDevice), "sender cut");
+    SL_CHECK_CUDA(cudaMemcpy(l->sc_vg.ptr, nvg.data(), sizeof(sl_vgrid) * I, cudaMemcpyHostToDevice), "sender cut");
+  }
+  SL_CHECK_CUDA(cudaMemset(l->sc_flag.ptr, 0, 4ull * N + 16), "sender cut");
+  SL_CHECK_CUDA(cudaMemset(l->sc_X.ptr, 0, 128ull * I + 16), "sender cut");
+  SL_CHECK_CUDA(cudaMemset(l->sc_T.ptr, 0, 4ull * I + 16), "sender cut");
+  SL_CHECK_CUDA(cudaMemset(l->sc_E.ptr, 0, 16ull * I + 16), "sender cut");
+  SL_CHECK_CUDA(cudaMemset(l->sc_list.ptr, 0, 4ull * I + 16), "sender cut");
+  l->bn_sc = true;
+  l->bn_sc_stale = true;
+  return SL_OK;
+}
+
 int sl_lighting_read_bounce(sl_lighting* l, uint32_t what, void* dst, size_t bytes) {
   if (!l || !dst) return fail(SL_ERR_INVALID_ARG, "null argument");
   if (!l->bounce_on) return fail(SL_ERR_INVALID_ARG, "no probes set");
-  const size_t G = l->count, N = l->n_tree, NP = l->BP.NP;
-  const sl::DevBuf* src[] = {&l->lo_b, &l->lo_dir, &l->xfer, &l->probe_sh, &l->probe_data, &l->node_sh, &l->node_acc};
-  const size_t size[] = {48 * G, 16 * G, 48 * G, 144 * NP, 32 * NP * 128, 56 * N, 224 * N};
-  if (what >= 7) return fail(SL_ERR_INVALID_ARG, "unknown bounce buffer");
+  const size_t G = l->count, N = l->n_tree, NP = l->BP.NP, I = N - G;
+  const sl::DevBuf* src[] = {&l->lo_b, &l->lo_dir, &l->xfer, &l->probe_sh, &l->probe_data, &l->node_sh,
+                             &l->node_acc, &l->sc_flag, &l->sc_X, &l->sc_T, &l->sc_E};
+  const size_t size[] = {48 * G, 16 * G, 48 * G, 144 * NP, 32 * NP * 128, 56 * N, 224 * N, 4 * N, 128 * I, 4 * I,
+                         16 * I};
+  if (what >= 11) return fail(SL_ERR_INVALID_ARG, "unknown bounce buffer");
+  if (what >= 7 && !l->bn_sc) return fail(SL_ERR_INVALID_ARG, "the sender cut is off");
   if (bytes > size[what]) return fail(SL_ERR_INVALID_ARG, "read past the bounce buffer");
   cudaSetDevice(l->device);
   SL_CHECK_CUDA(cudaDeviceSynchronize(), "sync");

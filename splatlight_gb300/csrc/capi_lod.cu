@@ -112,9 +112,16 @@ void node_cov(const sl_node& nd, M3d C, double* det_out) {
   *det_out = det;
 }
 
-// nodeGaussians (src/lod.js:44-107): internal nodes G..N-1 as Gaussian records, children before parents.
+}  // namespace
+
+// nodeGaussians (src/lod.js:44-107): internal nodes G..N-1 as Gaussian records, children before parents; with vg
+// their V grids too (lod.js:47-50, 86-88, 99-103): per cell the mass-weighted mean of the children's, kept as float32
+// (each addition rounded there), then rounded half up and clamped at 255.
 int node_records(const sl_gaussian* gauss, uint32_t G, const sl_node* nodes, uint32_t N, const uint32_t* kids,
-                 uint32_t n_kids, std::vector<sl_gaussian>& out) {
+                 uint32_t n_kids, std::vector<sl_gaussian>& out, const sl_vgrid* leaf_vg,
+                 std::vector<sl_vgrid>* vg) {
+  std::vector<float> V;
+  if (vg) V.assign((size_t)(N - G) * 128u, 0.0f);
   std::vector<double> mass(N), alb(3 * (size_t)N);
   std::vector<uint32_t> mat(N, 0);
   for (uint32_t g = 0; g < G; g++) {
@@ -141,6 +148,16 @@ int node_records(const sl_gaussian* gauss, uint32_t G, const sl_node* nodes, uin
     }
     mass[n] = m;
     for (int j = 0; j < 3; j++) alb[3 * (size_t)n + j] = c[j] / std::max(m, 1e-30);
+    if (vg) {
+      float* vn = V.data() + (size_t)(n - G) * 128u;
+      for (uint32_t k = lo; k < hi; k++) {
+        const uint32_t ch = kids[k];
+        const double w = mass[ch] / std::max(m, 1e-30);
+        const uint8_t* lb = ch < G ? reinterpret_cast<const uint8_t*>(&leaf_vg[ch]) : nullptr;
+        const float* vc = ch < G ? nullptr : V.data() + (size_t)(ch - G) * 128u;
+        for (int q = 0; q < 128; q++) vn[q] = (float)((double)vn[q] + w * (double)(lb ? (float)lb[q] : vc[q]));
+      }
+    }
     mat[n] = hi > lo ? mat[kids[lo]] : 0u;
     M3d C;
     double det_unused;
@@ -163,10 +180,16 @@ int node_records(const sl_gaussian* gauss, uint32_t G, const sl_node* nodes, uin
     for (int j = 0; j < 3; j++) o.albedo[j] = (float)alb[3 * (size_t)n + j];
     o.flags = mat[n];
   }
+  if (vg) {
+    vg->assign(N - G, sl_vgrid{});
+    for (size_t r = 0; r < (size_t)(N - G); r++) {
+      uint8_t* o = reinterpret_cast<uint8_t*>(&(*vg)[r]);
+      for (int q = 0; q < 128; q++) o[q] = (uint8_t)std::min(255.0, std::floor((double)V[r * 128u + q] + 0.5));
+    }
+  }
   return SL_OK;
 }
 
-}  // namespace
 }  // namespace sl
 
 using namespace sl;

@@ -29,7 +29,12 @@ struct BounceParams {
   uint32_t asg_cells;  // near-mirror Gaussians see the cells near their mirror direction as lights with a size
   float eye[3];
   float sky[48];  // 16 SH coefficients (bands 0-3), rgb
+  uint32_t sender_cut;   // the sender cut (bounce.wgsl sc_select .. node_sh2_sc) instead of every leaf
+  uint32_t sc_reselect;  // the cut is selected again this frame (the first frame, or a part moved)
 };
+
+// a node's mark under the sender cut (bounce.wgsl:1463-1466)
+constexpr uint32_t kScBelow = 0, kScOpen = 1, kScNode = 2, kScLeaf = 3;
 
 struct BounceBuffers {
   const sl_gaussian* gs;
@@ -51,6 +56,18 @@ struct BounceBuffers {
   float4* probe_hist;  // per ray the last two gathers, (rgb, m1), (m2): the FIR blend's history
   float* leaf_w;  // per Gaussian node_leaf's 14 weights (footprint x V toward D14), refreshed with the transfer
   uint32_t* node_sh;
+  // the sender cut: every node by depth, parents, the internal nodes as Gaussians and their V grids (N - G each),
+  // per node its mark, per internal node 8 vec4 (two faces' transfer and exposure, their direct light), the lamp T
+  // and distant-light T, the cut nodes' list with its count at sc_list[0] (nodes from sc_list[1])
+  const uint32_t* sc_level;
+  const uint32_t* parent;
+  const sl_gaussian* sc_gs;
+  const sl_vgrid* sc_vg;
+  uint32_t* sc_flag;
+  float4* sc_X;
+  float* sc_T;
+  float4* sc_E;
+  uint32_t* sc_list;
 };
 
 // The shading pass's parameters for an eye (capi_lighting.cu); iso_init's 128 cells, float64 then rounded.
@@ -61,13 +78,16 @@ void bounce_tables(float* d14, float* pinv);
 // cell_asg_phase's per-cell frame (bounce.wgsl:180-191): e_el, e_az, then s_el^2, s_az^2, 8 floats a cell, float64
 void cell_asg_table(float* t);
 
-// direct_dirs_emit + env_dirs for the Gaussians g % 4 == frame % 4 (bounce_direct.cu) into lo_dir
+// direct_dirs_emit + env_dirs for the Gaussians g % 4 == frame % 4 (bounce_direct.cu) into lo_dir; with the sender
+// cut only the cut's leaves among them, then direct_dirs_nodes_sc + env_dirs_nodes_sc for the cut nodes that refresh
+// this frame into sc_X
 cudaError_t launch_bounce_direct(const BounceParams& B, const ShadeParams& SH, const BounceBuffers& D, cudaStream_t s);
 
 // One frame of the bounce: level_off / level_cnt give each depth's internal nodes in up_list (depths 1 ..
-// max_depth - 1 are summed, deepest first).
+// max_depth - 1 are summed, deepest first); sc_off / sc_cnt every node of each depth in sc_level (the sender cut).
 cudaError_t launch_bounce_frame(const BounceParams& B, const ShadeParams& SH, const BounceBuffers& D,
                                 const std::vector<uint32_t>& level_off, const std::vector<uint32_t>& level_cnt,
+                                const std::vector<uint32_t>& sc_off, const std::vector<uint32_t>& sc_cnt,
                                 cudaStream_t s);
 
 }  // namespace sl

@@ -135,7 +135,7 @@ struct sl_lighting {
   sl::DevBuf g_blur, n_blur;
   // the scene's tree for the motion-blur cut and the probe gather (leaves then internal nodes), every node's parent,
   // the children lists, and per node its depth and part (host)
-  uint32_t n_tree = 0;
+  uint32_t n_tree = 0, n_kids = 0;
   sl::DevBuf tree_nodes, node_parent, kids;
   std::vector<uint32_t> tree_depth, tree_part;
   // probe bounce (bounce.cu; lighting.js initBounce / encodeBounce): the layout and frame state in BP, the internal
@@ -150,9 +150,20 @@ struct sl_lighting {
   sl::DevBuf bn_tab, bn_ground, bn_up, probe_data, probe_sh, xfer, lo_dir, lo_b, node_acc, node_sh, bn_quarters,
       bn_leaf_w, probe_hist;
   uint32_t bn_quarter_off[5] = {};
+  // the sender cut (bounce.wgsl sc_select): on/off, re-select on the next frame; every node by depth (sc_level);
+  // the internal nodes as Gaussians and their V grids; per node its mark; per internal node the cut's transfer and
+  // direct light, shadow T and distant-light T; the cut nodes' list and count
+  bool bn_sc = false, bn_sc_stale = true;
+  std::vector<uint32_t> sc_level_off, sc_level_cnt;
+  sl::DevBuf sc_level, sc_gs, sc_vg, sc_flag, sc_X, sc_T, sc_E, sc_list;
 };
 
 namespace sl {
 // ShadeParams of a lighting object seen from `eye` (capi_lighting.cu)
 void shade_params(const sl_lighting* l, const float* eye, ShadeParams& SH);
+// nodeGaussians (capi_lod.cu; src/lod.js:44-107): the internal nodes G..N-1 as Gaussian records, and (vg non-null)
+// their V grids, the mass-weighted mean of their children's cells
+int node_records(const sl_gaussian* gauss, uint32_t G, const sl_node* nodes, uint32_t N, const uint32_t* kids,
+                 uint32_t n_kids, std::vector<sl_gaussian>& out, const sl_vgrid* leaf_vg = nullptr,
+                 std::vector<sl_vgrid>* vg = nullptr);
 }  // namespace sl

@@ -82,6 +82,7 @@ class Lighting:
         N.check(self._lib.sl_lighting_set_tree(self._h, nd.ctypes.data, len(nd), k.ctypes.data if len(k) else None,
                                                len(k)))
         self.tree_count = len(nd)
+        self.sender_cut = False   # a new tree turns the sender cut off
 
     def set_probes(self, layout: dict, max_depth: int = 0, blend: float = 1.0, emitters_dark: bool = True) -> None:
         """The probe bounce over a lattice (probes.room_layout / probes.terrain_layout); needs set_tree.  From the
@@ -107,6 +108,13 @@ class Lighting:
         self.probe_count = int(np.prod(layout["dims"])) + 8 * self.renderer.part_count + \
             sum(int(v[1]) * int(v[2]) * int(v[3]) for v in vols)
 
+    def set_sender_cut(self, on: bool = True) -> None:
+        """The sender cut (the reference's default level of detail for the probes' senders, bounce.wgsl sc_select):
+        only the senders some probe resolves are lit, the rest of each part's tree as the nodes every probe uses whole.
+        Needs set_probes; selected again on the next update and whenever a part moved."""
+        N.check(self._lib.sl_lighting_set_sender_cut(self._h, 1 if on else 0))
+        self.sender_cut = bool(on)
+
     def set_sky(self, sh_rgb) -> None:
         """The probes' sky: up to 16 real SH coefficients (bands 0-3), rgb; None or empty = no sky."""
         sh = np.ascontiguousarray(np.zeros((0, 3)) if sh_rgb is None else sh_rgb, np.float32).reshape(-1, 3)
@@ -114,11 +122,15 @@ class Lighting:
 
     def read_bounce(self):
         """The bounce state as a dict of host arrays: lo_b (G, 3, 4), lo_dir (G, 4), xfer (G, 12), probe_sh (NP, 9, 4),
-        probe_data (NP, 128, 8), node_sh (N, 14) and node_acc (N, 14, 4)."""
+        probe_data (NP, 128, 8), node_sh (N, 14) and node_acc (N, 14, 4); with the sender cut also sc_flag (N,),
+        sc_X (N - G, 8, 4), sc_T (N - G,) and sc_envT (N - G, 4)."""
         G, NP, Nn = self.count, self.probe_count, self.tree_count
         shapes = [("lo_b", (G, 3, 4), np.float32), ("lo_dir", (G, 4), np.float32), ("xfer", (G, 12), np.float32),
                   ("probe_sh", (NP, 9, 4), np.float32), ("probe_data", (NP, 128, 8), np.float32),
                   ("node_sh", (Nn, 14), np.uint32), ("node_acc", (Nn, 14, 4), np.float32)]
+        if getattr(self, "sender_cut", False):
+            shapes += [("sc_flag", (Nn,), np.uint32), ("sc_X", (Nn - G, 8, 4), np.float32),
+                       ("sc_T", (Nn - G,), np.float32), ("sc_envT", (Nn - G, 4), np.float32)]
         out = {}
         for k, (name, shape, dt) in enumerate(shapes):
             a = np.empty(shape, dt)

@@ -46,9 +46,11 @@ def _close(name, a, b, rtol=RTOL, atol=ATOL, frac=0.0, scaled=False):
     assert n <= frac * a.size, f"{name}: {n} of {a.size} differ (max abs {worst:.3e})"
 
 
-def _run(s, tree, layout, frames=FRAMES, gain=1.0, moves=None, blend=1.0):
+def _run(s, tree, layout, frames=FRAMES, gain=1.0, moves=None, blend=1.0, sender_cut=False):
     """frames bounce frames on GPU and restatement side by side; moves: {frame: (parts, moved_mask)} written before
-    that frame's update (the maps re-splat; both sides take the GPU's transmittance of that frame)."""
+    that frame's update (the maps re-splat; both sides take the GPU's transmittance of that frame).  sender_cut: the
+    reference's default senders; its marks are exact, the cut nodes' transfer within RTOL, their shadow T exact up to
+    float32 sums, their direct light (a kernel compiled for speed) within 1e-3."""
     import torch
     from oracle import oracle as O
     r = SplatRenderer(s.gaussians, s.parts)
@@ -56,6 +58,8 @@ def _run(s, tree, layout, frames=FRAMES, gain=1.0, moves=None, blend=1.0):
     L.set_tree(*tree)
     L.set_sky(s.sky_sh)
     L.set_probes(layout, blend=blend)
+    if sender_cut:
+        L.set_sender_cut(True)
     fwd = camera_forward(s)
     b = None
     for f in range(frames):
@@ -67,13 +71,23 @@ def _run(s, tree, layout, frames=FRAMES, gain=1.0, moves=None, blend=1.0):
         torch.cuda.synchronize()
         col, lamp_t, env_t, nodes = L.read()
         if b is None:
-            b = O.Bounce(s, tree, (col, lamp_t, env_t, nodes), layout, sky_sh=s.sky_sh, blend=blend)
+            b = O.Bounce(s, tree, (col, lamp_t, env_t, nodes), layout, sky_sh=s.sky_sh, blend=blend,
+                         sender_cut=sender_cut)
         if moves and f in moves:
             b.scene = dataclasses.replace(b.scene, parts=moves[f][0])
         b.lamp_T = np.ascontiguousarray(lamp_t, np.float32)
         b.env_T = np.ascontiguousarray(env_t, np.float32)
         ost = b.step(s.eye, moved_mask=mask, threads=16)
         gst = L.read_bounce()
+        if sender_cut:
+            assert np.array_equal(gst["sc_flag"], ost["sc_flag"]), f"frame {f}: sender-cut marks differ"
+            cut = gst["sc_flag"][s.count:] == 2
+            assert cut.any()
+            _close(f"frame {f} cut transfer", gst["sc_X"][cut, :6], ost["sc_X"][cut, :6])
+            _close(f"frame {f} cut shadow T", gst["sc_T"][cut], ost["sc_T"][cut])
+            _close(f"frame {f} cut distant T", gst["sc_envT"][cut], ost["sc_envT"][cut])
+            _close(f"frame {f} cut direct light", gst["sc_X"][cut, 6:], ost["sc_X"][cut, 6:], rtol=1e-3,
+                   atol=RAD_ATOL, scaled=True)
         pd, opd = gst["probe_data"], ost["probe_data"]
         # discrete fields exactly: first-hit part (.w of the colour record), near / backface flags, validity
         assert np.array_equal(pd[:, :, 3], opd[:, :, 3]), f"frame {f}: first-hit parts differ"
@@ -202,3 +216,54 @@ def test_bounce_in_the_lit_frame():
                            view_mode=VIEW_LIT, n_emit=s.n_drawn_emitters, bounce_gain=0.0)
     img0 = r.render(f0)
     assert img.sum() > img0.sum()   # the bounce brightens the frame
+
+
+# ---- the sender cut (the reference's default senders: bounce.wgsl sc_select .. node_sh2_sc)
+
+def test_sender_cut_hill_terrain_sky():
+    """The hill's terrain lattice with its sky: the cut's marks, its nodes' transfer, sampled shadow and direct light,
+    and everything downstream against the restatement over 5 frames (the cut nodes refresh a quarter a frame)."""
+    s = _bounce_lit(S.hill(40000, seed=3, width=320, height=240, n_emit=8))
+    s = dataclasses.replace(s, shadow_res=256, sun_res=256)
+    s, tree = S.with_tree(s)
+    _, L, st = _run(s, tree, PR.for_scene(s), sender_cut=True)
+    fl = st["sc_flag"]
+    assert (fl[s.count:] == 2).sum() > 0 and (fl[:s.count] == 3).sum() > 0
+    assert (st["lo_b"][:, 0, :3].sum(axis=1) > 0).mean() > 0.9
+
+
+def test_sender_cut_cornell_room():
+    s = _bounce_lit(S.cornell(20000, seed=2, width=256, height=256, n_emit=4))
+    s = dataclasses.replace(s, shadow_res=256)
+    s, tree = S.with_tree(s)
+    _run(s, tree, PR.for_scene(s), frames=4, sender_cut=True)
+
+
+def test_sender_cut_moving_part():
+    """The reference's Cornell room with the cut: the short box moves (the cut is selected again around its riding
+    probes), then rests."""
+    p = ASSETS / "cornell_sdf_room_plain_bin"
+    if not (p / "asset.json").exists():
+        pytest.skip("reference assets not copied (tests/golden/copy_assets.py)")
+    from splatlight_gb300 import asset as A
+    s = A.asset_scene(A.load_asset(p), width=256, height=256)
+    s, tree = S.with_tree(s)
+    q = next(i for i in range(len(s.parts)) if (int(s.parts["flags"][i]) & 1) == 0)
+    moved = s.parts.copy()
+    moved["xf_prev"][q] = moved["xf"][q]
+    moved["xf"][q][3] += 0.08
+    moved["xf"][q][7] += 0.05
+    rest = moved.copy()
+    rest["xf_prev"][q] = rest["xf"][q]
+    _run(s, tree, s.probes, frames=4, moves={1: (moved, 1 << q), 2: (rest, 0)}, sender_cut=True)
+
+
+def test_sender_cut_hill_lite_asset():
+    p = ASSETS / "hill_lite_bin"
+    if not (p / "asset.json").exists():
+        pytest.skip("reference assets not copied (tests/golden/copy_assets.py)")
+    from splatlight_gb300 import asset as A
+    s = A.asset_scene(A.load_asset(p), width=256, height=256)
+    s, tree = S.with_tree(s)
+    _run(s, tree, s.probes, frames=3, sender_cut=True)
+
