@@ -600,6 +600,23 @@ def run_bounce(args, stream, flush):
     ms_frame_b = timed(lambda: (L.update(s.eye, fwd, stream=sc), r.render(fb, out=out, stream=sc)), steps)
     ms_frame_0 = timed(lambda: (L.shade(s.eye, stream=sc), r.render(f0, out=out, stream=sc)), steps)
     st = L.read_bounce()
+    # the sender cut (the reference's default senders): a frame that selects the cut again (as after a part moved),
+    # then the steady frames between, where a quarter of the cut refreshes
+    t0 = time.perf_counter()
+    L.set_sender_cut(True)
+    t_sc = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    ms_sc_select = timed(lambda: L.update(s.eye, fwd, stream=sc), 1) - ms_shade   # the first frame selects
+    for _ in range(8):
+        L.update(s.eye, fwd, stream=sc)
+    torch.cuda.synchronize()
+    ms_sc = timed(lambda: L.update(s.eye, fwd, stream=sc), steps) - ms_shade
+    sst = L.read_bounce()
+    fl = sst["sc_flag"]
+    res_sc = {"bounce_ms": round(ms_sc, 4), "reselect_frame_ms": round(ms_sc_select, 4),
+              "cut_nodes": int((fl[s.count:] == 2).sum()), "cut_leaves": int((fl[:s.count] == 3).sum()),
+              "open_nodes": int((fl[s.count:] == 1).sum()), "setup_s": round(t_sc, 2),
+              "mean_bounce_rgb": [round(float(v), 5) for v in sst["lo_b"][:, 0, :3].mean(axis=0)]}
     res = {"workload": f"hill-like 1,048,576 Gaussians (seed 1), its {len(tree[0]) - s.count:,}-node moment-matched "
                        f"tree, terrain lattice {lay['dims'][0]}x{lay['dims'][1]}x{lay['dims'][2]} probes x 128 cells "
                        "(ray length {:.1f} m), the scene's sky SH; bounce frame = direct light toward the probes for a "
@@ -612,7 +629,7 @@ def run_bounce(args, stream, flush):
            "probes": L.probe_count, "lattice_probes": int(np.prod(lay["dims"])),
            "valid_probes": int((st["probe_data"][:, 0, 6] > 0).sum()),
            "mean_bounce_rgb": [round(float(v), 5) for v in st["lo_b"][:, 0, :3].mean(axis=0)],
-           "tree_build_s": round(t_tree, 2)}
+           "tree_build_s": round(t_tree, 2), "sender_cut": res_sc}
     L.close()
     r.close()
     return res
