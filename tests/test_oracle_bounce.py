@@ -219,3 +219,22 @@ def test_sender_cut_is_close_to_the_exact_path(orc, name):
     assert a.mean() > 0
     assert (np.abs(b.mean(0) - a.mean(0)) <= 0.03 * a.mean(0)).all()
     assert np.abs(b - a).max() <= 0.1 * a.max()
+
+
+@pytest.mark.parametrize("name", ["cornell_sdf_room_plain_bin", "hill_lite_bin"])
+def test_sender_cut_on_the_reference_assets(orc, name):
+    """With the reference's own baked trees and V grids the cut sends what the leaves send: once the probes have
+    settled (8 frames) the mean bounce toward the eye is within 2% of the per-leaf path, per channel."""
+    p = ROOT / "tests" / "golden" / "assets" / name
+    if not (p / "asset.json").exists():
+        pytest.skip("reference assets not copied (tests/golden/copy_assets.py)")
+    from splatlight_gb300 import asset as A
+    s = A.asset_scene(A.load_asset(p), width=64, height=64)
+    s, tree = S.with_tree(s)
+    lit = orc.lighting(s, threads=8)
+    ex = orc.Bounce(s, tree, lit, s.probes, sky_sh=s.sky_sh)
+    sc = orc.Bounce(s, tree, lit, s.probes, sky_sh=s.sky_sh, sender_cut=True)
+    for f in range(8):
+        a, b = ex.step(s.eye, threads=8)["lo_b"][:, 0, :3].copy(), sc.step(s.eye, threads=8)["lo_b"][:, 0, :3]
+    assert (np.bincount(sc.state["sc_flag"], minlength=4)[2:] > 0).all()
+    assert (np.abs(b.mean(0) - a.mean(0)) <= 0.02 * a.mean(0)).all()
