@@ -476,16 +476,6 @@ static tnode t_leaf(tbuild* B, uint32_t i) {
   return nd;
 }
 
-static const float* g_sort_rec;
-static int g_sort_ax;
-static int cmp_pos(const void* a, const void* b) {
-  uint32_t p = *(const uint32_t*)a, q = *(const uint32_t*)b;
-  double d = (double)g_sort_rec[16u * p + g_sort_ax] - (double)g_sort_rec[16u * q + g_sort_ax];
-  if (d < 0) return -1;
-  if (d > 0) return 1;
-  return p < q ? -1 : (p > q ? 1 : 0);  /* stable: ties keep index order (JS sort is stable) */
-}
-
 static uint32_t t_build(tbuild* B, uint32_t* idx, uint32_t n) {
   if (n == 1) {
     tnode l = t_leaf(B, idx[0]);
@@ -502,10 +492,7 @@ static uint32_t t_build(tbuild* B, uint32_t* idx, uint32_t n) {
   int ax = 0;
   for (int k = 0; k < 3; k++)
     if (hi[k] - lo[k] > hi[ax] - lo[ax]) ax = k;
-  /* the JS sort compares positions; ties are stable in the order of idx, which is ascending index order here */
-  g_sort_rec = B->rec;
-  g_sort_ax = ax;
-  /* idx arrives in index order at every level only at the root; keep the incoming order for ties instead */
+  /* the JS sort compares positions and is stable: ties keep the incoming order of idx */
   uint32_t* tmp = (uint32_t*)malloc(sizeof(uint32_t) * n * 2);
   for (uint32_t a = 0; a < n; a++) { tmp[2 * a] = idx[a]; tmp[2 * a + 1] = a; }
   /* insertion sort by (position, incoming rank): stable and deterministic (n <= a few thousand emitters) */
