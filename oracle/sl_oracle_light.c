@@ -2086,8 +2086,8 @@ static void bn_dirs_one(const orc_bounce_in* in, const bn_probes* PS, const floa
   lb[8] = lb[9] = lb[10] = lb[11] = 0.0f;
 }
 
-/* ---- the sender cut (bounce.wgsl:1448-1730 sc_select .. node_sh2_sc; emissive.wgsl:1018-1064
- * direct_dirs_emit_sc / direct_dirs_nodes_sc; environment.wgsl:317-351 env_dirs_sc / env_dirs_nodes_sc; host
+/* ---- the sender cut (bounce.wgsl:1448-1730 sc_select .. node_sh2_sc; emissive.wgsl:1018-1065
+ * direct_dirs_emit_sc / direct_dirs_nodes_sc; environment.wgsl:317-352 env_dirs_sc / env_dirs_nodes_sc; host
  * src/lighting.js:1057-1095), the reference's default level of detail for the probes' senders.
  * On a re-selection (the first frame, or one in which a part moved) every node of every part's tree is marked, top
  * down by depth: BELOW (above the parts, under a cut node or a cut leaf: never read), OPEN (some probe's gather opens
@@ -2116,7 +2116,7 @@ static float sc_mass(const sl_node* nd) {
 }
 static float sc_round(float x) { return rintf(x); } /* WGSL round: half to even */
 
-/* sc_probe_dist (bounce.wgsl:1478-1513): the smallest (distance - margin) from world point P to the gather centres of
+/* sc_probe_dist (bounce.wgsl:1478-1516): the smallest (distance - margin) from world point P to the gather centres of
  * the probes that see part `own`: the room lattice's nearest 2x2x2 block centre less the block radius, the terrain's
  * 3 x 3 columns around P, each movable part's 8 probes but own's, each static volume's nearest grid probe */
 static float sc_probe_dist(const orc_bounce_in* in, const bn_probes* PS, f3 P, uint32_t own, float brad) {
@@ -2174,7 +2174,7 @@ static float sc_probe_dist(const orc_bounce_in* in, const bn_probes* PS, f3 P, u
   return best;
 }
 
-/* sc_select (bounce.wgsl:1528-1545) for node n, its parent's mark already set */
+/* sc_select (bounce.wgsl:1529-1548) for node n, its parent's mark already set */
 static uint32_t sc_select_one(const orc_bounce_in* in, const bn_probes* PS, const uint32_t* parent,
                               const uint32_t* flag, uint32_t n, float brad) {
   const sl_node* nd = &in->nodes[n];
@@ -2186,7 +2186,7 @@ static uint32_t sc_select_one(const orc_bounce_in* in, const bn_probes* PS, cons
   return sc_probe_dist(in, PS, P, q, brad) <= BN_THETA * nd->smax ? SC_OPEN : SC_NODE;
 }
 
-/* sc_xfer (bounce.wgsl:1640-1672): per cut node and face of its short axis the share of the SH2 transfer from its own
+/* sc_xfer (bounce.wgsl:1631-1667): per cut node and face of its short axis the share of the SH2 transfer from its own
  * V grid and the face's exposure; 6 vec4: face 0 t0-3, t4-7, (t8, S, 0, 0), then face 1 */
 static void sc_xfer_one(const orc_bounce_in* in, const float* cells, uint32_t n, float* X) {
   const uint32_t r = n - in->count;
@@ -2226,7 +2226,7 @@ static void sc_xfer_one(const orc_bounce_in* in, const float* cells, uint32_t n,
   }
 }
 
-/* sc_shadow (bounce.wgsl:1566-1625): the mean lamp T and distant-light T over SC_SAMPLES leaves under n, each reached
+/* sc_shadow (bounce.wgsl:1566-1624): the mean lamp T and distant-light T over SC_SAMPLES leaves under n, each reached
  * by a descent that picks a child with probability by mass (a fixed hash per node and sample).  The Gaussians carry
  * one lamp T each here, so the reference's per-lamp slots reduce to that mean. */
 static void sc_shadow_one(const orc_bounce_in* in, uint32_t n, float* T_out, float* E_out) {
@@ -2331,7 +2331,7 @@ static void sc_direct_node(const orc_bounce_in* in, uint32_t n, float T, const f
   X[28] = c1.x; X[29] = c1.y; X[30] = c1.z; X[31] = 0.0f;
 }
 
-/* node_cut (bounce.wgsl:1682-1716): cut node n as one sender, each face's light (its direct light plus the probes'
+/* node_cut (bounce.wgsl:1669-1712): cut node n as one sender, each face's light (its direct light plus the probes'
  * SH2 at its centre through the face's transfer, over the face's exposure) shown toward each D_k by its share there */
 static void sc_node_cut(const orc_bounce_in* in, const bn_probes* PS, const float* d14, const float* pd,
                         const float* probe_sh, uint32_t n, const float* X, float* acc) {

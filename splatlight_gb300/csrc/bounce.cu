@@ -885,7 +885,7 @@ __device__ __forceinline__ bool sc_now(const BounceParams& B, uint32_t n) {
   return B.sc_reselect != 0u || n % 4u == B.frame % 4u;
 }
 
-// sc_probe_dist (bounce.wgsl:1478-1513): the smallest (distance - margin) from world point P to the gather centres of
+// sc_probe_dist (bounce.wgsl:1478-1516): the smallest (distance - margin) from world point P to the gather centres of
 // the probes that see part `own` (the room's nearest 2x2x2 block centre less the block radius; the terrain's 3 x 3
 // columns around P; each movable part's 8 probes but own's; each static volume's nearest grid probe).  The gathers
 // of probes that cut around themselves keep no margin (vol_info.y 0).  WGSL round is half to even: rintf.
@@ -945,7 +945,7 @@ __device__ float sc_probe_dist(const BounceParams& B, const float* __restrict__ 
   return best;
 }
 
-// sc_select (bounce.wgsl:1528-1545) over one depth, the depth above already marked; the cut nodes join sc_list
+// sc_select (bounce.wgsl:1529-1548) over one depth, the depth above already marked; the cut nodes join sc_list
 __global__ void __launch_bounds__(kThreads) sc_select_kernel(const __grid_constant__ BounceParams B,
                                                              const sl_node* __restrict__ tnodes,
                                                              const sl_part* __restrict__ parts,
@@ -973,7 +973,7 @@ __global__ void __launch_bounds__(kThreads) sc_select_kernel(const __grid_consta
   if (m == kScNode) list[1u + atomicAdd(&list[0], 1u)] = n;
 }
 
-// sc_xfer (bounce.wgsl:1640-1672): per cut node and face of its short axis, the SH2 transfer from its own V grid and
+// sc_xfer (bounce.wgsl:1631-1667): per cut node and face of its short axis, the SH2 transfer from its own V grid and
 // the face's exposure (at least 1% of the whole): 6 vec4, face 0 t0-3, t4-7, (t8, S), then face 1
 __global__ void __launch_bounds__(kThreads) sc_xfer_kernel(const __grid_constant__ BounceParams B,
                                                            const uint32_t* __restrict__ list,
@@ -1023,7 +1023,7 @@ __global__ void __launch_bounds__(kThreads) sc_xfer_kernel(const __grid_constant
   }
 }
 
-// sc_shadow (bounce.wgsl:1566-1625): the mean lamp T and distant-light T of 8 leaves under the cut node, each reached
+// sc_shadow (bounce.wgsl:1566-1624): the mean lamp T and distant-light T of 8 leaves under the cut node, each reached
 // by a descent that picks a child with probability by mass (a fixed hash per node and sample).  A Gaussian carries
 // one lamp T here, so the reference's per-lamp slots reduce to that mean.
 __global__ void __launch_bounds__(kThreads) sc_shadow_kernel(const __grid_constant__ BounceParams B,
@@ -1069,7 +1069,7 @@ __global__ void __launch_bounds__(kThreads) sc_shadow_kernel(const __grid_consta
   sc_E[r] = make_float4(E.x / 8.0f, E.y / 8.0f, E.z / 8.0f, E.w / 8.0f);
 }
 
-// node_cut (bounce.wgsl:1682-1716): a cut node as one sender, each face's light (its direct light plus the probes'
+// node_cut (bounce.wgsl:1669-1712): a cut node as one sender, each face's light (its direct light plus the probes'
 // SH2 at its centre through the face's transfer, over the face's exposure) shown toward each D_k by its share there
 __global__ void __launch_bounds__(kThreads) node_cut_kernel(const __grid_constant__ BounceParams B,
                                                             const uint32_t* __restrict__ list,

@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(kThreads, 4) direct_kernel(const __grid_consta
   lo_dir[g] = make_float4(c.x, c.y, c.z, 0.0f);
 }
 
-// direct_dirs_nodes_sc + env_dirs_nodes_sc (emissive.wgsl:1032-1064, environment.wgsl:329-351): the light each face of
+// direct_dirs_nodes_sc + env_dirs_nodes_sc (emissive.wgsl:1030-1065, environment.wgsl:329-352): the light each face of
 // a cut node (its short axis' two sides) catches, before albedo and exposure, from the emitters' light cut (matte:
 // shininess left out of the senders) times its sampled lamp T, then the distant lights' catch with its sampled T
 __global__ void __launch_bounds__(kThreads, 4) direct_nodes_kernel(const __grid_constant__ BounceParams B,
