@@ -130,3 +130,32 @@ def test_missing_asset_folder(A, tmp_path):
     with pytest.raises(A.AssetError) as e:
         A.load_asset(tmp_path / "nothing_here")
     assert "Could not load" in str(e.value)
+
+
+def test_probe_layouts_from_the_headers(A):
+    """probeLayout (src/lighting.js:220-286) on the shipped headers: the Cornell room's 8^3 lattice inset 0.125 m from
+    its `room` walls (no environment: rays of 6 m); hill_lite's 16 x 16 x 5 terrain lattice over its `bounds` (cell
+    centres, the default heights, rays across the whole scene for its environment), its ground inside the bounds, and
+    the one static volume probeVolumes picks (its tree part, 4 per axis); hill_lite's sky SH for the probes."""
+    a = A.load_asset(_need(NAMES[0]))
+    lay = A.probe_layout(a)
+    room = a.header["room"]
+    box = [(float(room[k][0]), float(room[k][1])) for k in "xyz"]
+    half = [(b - c) / 2 - 0.125 for c, b in box]
+    assert not lay["terrain"] and lay["dims"] == [8, 8, 8] and lay["tmax"] == 6.0 and lay["vols"] == []
+    assert np.allclose(lay["lo"], [(c + b) / 2 - h for (c, b), h in zip(box, half)])
+    assert np.allclose(lay["step"], [2 * h / 7 for h in half])
+    assert A.environment_sky(a.header.get("environment")) is None
+    a = A.load_asset(_need(NAMES[1]))
+    lay = A.probe_layout(a)
+    lo, hi = (np.asarray(a.header["bounds"][k], np.float64) for k in ("lo", "hi"))
+    step = (hi - lo)[:2] / 16
+    assert lay["terrain"] and lay["dims"] == [16, 16, 5] and list(lay["levels"]) == [0.3, 1.0, 3.0, 8.0, 20.0]
+    assert np.allclose(lay["step"][:2], step) and np.allclose(lay["lo"][:2], lo[:2] + step / 2)
+    assert np.isclose(lay["tmax"], max(6.0, float(np.linalg.norm(hi - lo))))
+    g = np.asarray(lay["ground"])
+    assert g.shape == (256,) and np.isfinite(g).all() and (g >= lo[2] - 1e-4).all() and (g <= hi[2] + 1e-4).all()
+    assert [tuple(v) for v in lay["vols"]] == [(2, 4, 4, 4)]
+    sky = A.environment_sky(a.header["environment"])
+    assert sky.shape == (16, 3)
+    assert np.allclose(sky, np.asarray(a.header["environment"]["sky"]["sh_rgb"][:16], np.float64))
