@@ -1,6 +1,9 @@
 """The probe bounce's CPU side: the restatement's tables and half rounding, the probe layouts (src/lighting.js
-probeLayout), and properties of the restated bounce that hold whatever the scene (no light and no sky: no bounce;
-an open sky: the upward probe rays carry the sky's radiance times their transmittance)."""
+probeLayout), properties of the restated bounce that hold whatever the scene (no light and no sky: no bounce;
+an open sky: the upward probe rays carry the sky's radiance times their transmittance; the same bits on any thread
+count), and the sender cut's (its marks down the tree and against every lattice probe's gather rule, the node V
+grids, the per-leaf path when nothing can be cut, and how close it sends to every leaf, on the reference's assets
+too)."""
 import dataclasses
 import math
 import sys
